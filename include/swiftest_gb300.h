@@ -1,0 +1,139 @@
+/*
+ * swiftest_gb300.h -- C ABI of the GB300 (sm_103a) implementation of Swiftest's
+ * integrator hot path: pair-gravity kick, Danby Kepler drift, close-encounter
+ * checks, and the WHM / HELIO / SyMBA step loops that call them.
+ *
+ * Every entry point returns an int status (SWG_OK == 0, negative on error),
+ * never aborts, never throws across the ABI.  Arrays follow the reference's
+ * Fortran layout: positions and velocities are (3,n) column-major doubles
+ * (x, y, z of one body contiguous); encounter indices are 1-based int32;
+ * logical masks are int32 0/1 (gfortran's 4-byte default logical).
+ *
+ * Pointer arguments live in the memory space named by the `mem` argument:
+ * SWG_MEM_HOST (copied to and from the GPU inside the call, which then
+ * synchronizes) or SWG_MEM_DEVICE (device pointers; the call is ordered on
+ * the context's stream and only synchronizes where a count must be returned).
+ */
+#ifndef SWIFTEST_GB300_H
+#define SWIFTEST_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SWG_OK 0
+#define SWG_ERR_ARG (-1)       /* invalid argument */
+#define SWG_ERR_CUDA (-2)      /* CUDA runtime error (message in swg_last_error) */
+#define SWG_ERR_CAPACITY (-3)  /* output list too small; *nenc holds the required size */
+#define SWG_ERR_NOMEM (-4)     /* device allocation failed */
+#define SWG_ERR_DRIFT (-5)     /* Danby drift failed for a massive body in WHM (reference aborts) */
+#define SWG_ERR_RECURSION (-6) /* SyMBA recursion step fell below machine epsilon */
+#define SWG_ERR_STATE (-7)     /* call out of order (e.g. step before initialize) */
+
+#define SWG_MEM_HOST 0
+#define SWG_MEM_DEVICE 1
+
+/* arithmetic of the pair kick */
+#define SWG_FP64 0  /* FP64, reference operation order: bit-identical to the serial reference loop */
+#define SWG_MIXED 1 /* FP64 positions split into float hi/lo, FP32 r^-3, float-float partial sums, FP64 total */
+
+/* encounter-check modes (reference: param%lencounter_sas_plpl / _pltp) */
+#define SWG_ENC_TRIANGULAR 0
+#define SWG_ENC_SORTSWEEP 1
+
+typedef struct swg_ctx swg_ctx;
+
+/* Context: one per host thread; owns a CUDA stream and a grow-only device arena. */
+int swg_create(swg_ctx **ctx, int device);
+int swg_destroy(swg_ctx *ctx);
+int swg_synchronize(swg_ctx *ctx);
+const char *swg_last_error(const swg_ctx *ctx);
+/* number of kernels this context has launched since creation */
+int64_t swg_launch_count(const swg_ctx *ctx);
+
+/* ---- pair-gravity kick ------------------------------------------------------
+ * Replaces swiftest_kick_getacch_int_all_tri_rad_pl / _tri_norad_pl
+ * (src/swiftest/swiftest_kick.f90:165-371; interface swiftest_module.f90:940-991).
+ * acc is inout and accumulates like the reference.  radius == NULL selects the
+ * norad variant.  nplm < npl selects the GMTINY (semi-interacting) loop shape. */
+int swg_kick_getacch_int_all_tri_pl(swg_ctx *ctx, int32_t npl, int32_t nplm, const double *r, const double *Gmass,
+                                    const double *radius, double *acc, int precision, int mem);
+
+/* Replaces swiftest_kick_getacch_int_all_flat_rad_pl / _flat_norad_pl
+ * (swiftest_kick.f90:69-162).  k_plpl is the (2,nplpl) 1-based pair list; pass
+ * NULL for the canonical list built by swiftest_util_flatten_eucl_plpl
+ * (swiftest_util.f90:1090-1131) restricted to rows i <= nplm, which the GPU
+ * derives from tile coordinates instead of reading. */
+int swg_kick_getacch_int_all_flat_pl(swg_ctx *ctx, int32_t npl, int32_t nplm, int64_t nplpl, const int32_t *k_plpl,
+                                     const double *r, const double *Gmass, const double *radius, double *acc,
+                                     int precision, int mem);
+
+/* Replaces swiftest_kick_getacch_int_all_tp (swiftest_kick.f90:374-415). */
+int swg_kick_getacch_int_all_tp(swg_ctx *ctx, int32_t ntp, int32_t npl, const double *rtp, const double *rpl,
+                                const double *GMpl, const int32_t *lmask, double *acc, int precision, int mem);
+
+/* ---- Danby drift ---------------------------------------------------------------
+ * Replaces swiftest_drift_all (src/swiftest/swiftest_drift.f90:60-108; interface
+ * swiftest_module.f90:513-522) including drift_one/_dan/_kepmd/_kepu*.
+ * iflag gets the reference's per-body status (0 ok, 1 kepmd/Newton, 2 Laguerre). */
+int swg_drift_all(swg_ctx *ctx, const double *mu, double *x, double *v, int32_t n, int32_t lgr, double inv_c2,
+                  double dt, const int32_t *lmask, int32_t *iflag, int mem);
+
+/* ---- encounter checks -----------------------------------------------------------
+ * Replace encounter_check_all_plpl / _plplm / _pltp (src/encounter/encounter_check.f90:14-140).
+ * Caller-capacity protocol (Fortran allocatable outputs cannot cross the ABI):
+ * on return *nenc is the number of encounters; if it exceeds cap the call
+ * returns SWG_ERR_CAPACITY and the caller retries with a larger buffer.
+ * Output order is (index1, index2) ascending; lvdotr is int32 0/1. */
+int swg_encounter_check_all_plpl(swg_ctx *ctx, int mode, int32_t npl, const double *r, const double *v,
+                                 const double *renc, double dt, int64_t cap, int64_t *nenc, int32_t *index1,
+                                 int32_t *index2, int32_t *lvdotr, int mem);
+int swg_encounter_check_all_plplm(swg_ctx *ctx, int mode, int32_t nplm, int32_t nplt, const double *rplm,
+                                  const double *vplm, const double *rplt, const double *vplt, const double *rencm,
+                                  const double *renct, double dt, int64_t cap, int64_t *nenc, int32_t *index1,
+                                  int32_t *index2, int32_t *lvdotr, int mem);
+int swg_encounter_check_all_pltp(swg_ctx *ctx, int mode, int32_t npl, int32_t ntp, const double *rpl,
+                                 const double *vpl, const double *rtp, const double *vtp, const double *renc,
+                                 double dt, int64_t cap, int64_t *nenc, int32_t *index1, int32_t *index2,
+                                 int32_t *lvdotr, int mem);
+
+/* ---- device-resident n-body system and step loops ---------------------------------
+ * Mirrors swiftest_nbody_system with whm_step_system (src/whm/whm_step.f90:14-104),
+ * helio_step_system (src/helio/helio_step.f90:14-119) and symba_step_system
+ * (src/symba/symba_step.f90:14-331).  State stays in HBM between steps. */
+#define SWG_WHM 0
+#define SWG_HELIO 1
+#define SWG_SYMBA 2
+typedef struct swg_system swg_system;
+int swg_system_create(swg_ctx *ctx, int integrator, int32_t npl, int32_t ntp, swg_system **sys);
+int swg_system_destroy(swg_system *sys);
+int swg_system_set_cb(swg_system *sys, double GMcb, double Rcb);
+/* host arrays; massive bodies sorted as the reference's initialize does
+ * (HELIO/SyMBA: by mass descending; WHM: by heliocentric distance) */
+int swg_system_set_pl(swg_system *sys, const double *rh, const double *vh, const double *Gmass, const double *radius,
+                      const double *rhill);
+int swg_system_set_tp(swg_system *sys, const double *rh, const double *vh);
+/* loop_mode 0 triangular / 1 flat; encounter modes; rhscale (reference: 6.5);
+ * lclose; gmtiny (<= 0 off); precision of the pair kick */
+int swg_system_set_param(swg_system *sys, double dt, int loop_mode, int enc_plpl, int enc_pltp, double rhscale,
+                         int lclose, double gmtiny, int precision);
+int swg_system_initialize(swg_system *sys);
+int swg_system_step(swg_system *sys, int32_t nsteps);
+int swg_system_get_pl(swg_system *sys, double *rh, double *vh, int32_t *status);
+int swg_system_get_tp(swg_system *sys, double *rh, double *vh, int32_t *status);
+/* out[9]: te, ke, pe, be, Lx, Ly, Lz, GMtot (swiftest_util.f90:1172-1401, whose central-body
+ * potential uses the body's barycentric distance), then te_helio: the same total with the
+ * central-body potential at the heliocentric distance. */
+int swg_system_energy(swg_system *sys, double *out);
+/* out: steps with encounters, max recursion depth, sum plpl enc, sum pltp enc, collisions */
+int swg_system_stats(swg_system *sys, int64_t *out);
+/* level-0 encounter lists of the last step */
+int swg_system_plpl_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
+int swg_system_pltp_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

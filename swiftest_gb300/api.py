@@ -1,0 +1,263 @@
+"""Python host layer over the C ABI: numpy in, numpy out.
+
+Names and argument meanings follow the reference's Fortran procedures
+(src/swiftest/swiftest_module.f90:505-539, 924-1010; src/encounter/encounter_module.f90).
+Arrays use the reference layout: positions/velocities of shape (n, 3) in C
+order, which is the same memory as Fortran's (3, n); encounter indices are
+1-based; masks are int32 0/1.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One CUDA stream plus a grow-only device arena (``swg_ctx``)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = C.c_void_p()
+        rc = self.lib.swg_create(C.byref(h), device)
+        if rc != L.SWG_OK:
+            raise L.SwiftestGB300Error("swg_create", rc, "no usable CUDA device")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.swg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, fn: str, rc: int):
+        if rc != L.SWG_OK:
+            msg = self.lib.swg_last_error(self.h)
+            raise L.SwiftestGB300Error(fn, rc, msg.decode() if msg else "")
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.swg_launch_count(self.h))
+
+    def synchronize(self):
+        self.check("swg_synchronize", self.lib.swg_synchronize(self.h))
+
+    # ---- kick -------------------------------------------------------------
+    def kick_getacch_int_all_tri_pl(self, r, Gmass, radius=None, acc=None, nplm=None, precision=L.SWG_FP64):
+        r = _f64(r, (-1, 3))
+        npl = r.shape[0]
+        acc = np.zeros((npl, 3)) if acc is None else _f64(acc, (npl, 3)).copy()
+        nplm = npl if nplm is None else int(nplm)
+        g = _f64(Gmass)
+        rad = None if radius is None else _f64(radius)
+        rc = self.lib.swg_kick_getacch_int_all_tri_pl(self.h, npl, nplm, _ptr(r), _ptr(g), _ptr(rad), _ptr(acc),
+                                                      precision, L.SWG_MEM_HOST)
+        self.check("swg_kick_getacch_int_all_tri_pl", rc)
+        return acc
+
+    def kick_getacch_int_all_flat_pl(self, r, Gmass, radius=None, acc=None, k_plpl=None, nplm=None,
+                                     precision=L.SWG_FP64):
+        r = _f64(r, (-1, 3))
+        npl = r.shape[0]
+        nplm = npl if nplm is None else int(nplm)
+        acc = np.zeros((npl, 3)) if acc is None else _f64(acc, (npl, 3)).copy()
+        g = _f64(Gmass)
+        rad = None if radius is None else _f64(radius)
+        if k_plpl is None:
+            nplpl = nplm * npl - nplm * (nplm + 1) // 2
+            kp = None
+        else:
+            kp = _i32(k_plpl).reshape(-1, 2)
+            nplpl = kp.shape[0]
+        rc = self.lib.swg_kick_getacch_int_all_flat_pl(self.h, npl, nplm, nplpl, _ptr(kp), _ptr(r), _ptr(g),
+                                                       _ptr(rad), _ptr(acc), precision, L.SWG_MEM_HOST)
+        self.check("swg_kick_getacch_int_all_flat_pl", rc)
+        return acc
+
+    def kick_getacch_int_all_tp(self, rtp, rpl, GMpl, lmask=None, acc=None, precision=L.SWG_FP64):
+        rtp = _f64(rtp, (-1, 3))
+        rpl = _f64(rpl, (-1, 3))
+        ntp, npl = rtp.shape[0], rpl.shape[0]
+        acc = np.zeros((ntp, 3)) if acc is None else _f64(acc, (ntp, 3)).copy()
+        m = np.ones(ntp, np.int32) if lmask is None else _i32(lmask)
+        g = _f64(GMpl)
+        rc = self.lib.swg_kick_getacch_int_all_tp(self.h, ntp, npl, _ptr(rtp), _ptr(rpl), _ptr(g), _ptr(m),
+                                                  _ptr(acc), precision, L.SWG_MEM_HOST)
+        self.check("swg_kick_getacch_int_all_tp", rc)
+        return acc
+
+    # ---- drift ------------------------------------------------------------
+    def drift_all(self, mu, x, v, dt, lmask=None, lgr=False, inv_c2=0.0):
+        x = _f64(x, (-1, 3)).copy()
+        v = _f64(v, (-1, 3)).copy()
+        n = x.shape[0]
+        mu = np.full(n, float(mu)) if np.isscalar(mu) else _f64(mu)
+        m = np.ones(n, np.int32) if lmask is None else _i32(lmask)
+        iflag = np.zeros(n, np.int32)
+        rc = self.lib.swg_drift_all(self.h, _ptr(mu), _ptr(x), _ptr(v), n, int(bool(lgr)), float(inv_c2), float(dt),
+                                    _ptr(m), _ptr(iflag), L.SWG_MEM_HOST)
+        self.check("swg_drift_all", rc)
+        return x, v, iflag
+
+    # ---- encounters -------------------------------------------------------
+    def _enc(self, fn, args, cap):
+        n = C.c_int64(0)
+        while True:
+            i1 = np.zeros(max(cap, 1), np.int32)
+            i2 = np.zeros(max(cap, 1), np.int32)
+            lv = np.zeros(max(cap, 1), np.int32)
+            rc = getattr(self.lib, fn)(self.h, *args, cap, C.byref(n), _ptr(i1), _ptr(i2), _ptr(lv), L.SWG_MEM_HOST)
+            if rc == L.SWG_ERR_CAPACITY:
+                cap = int(n.value)
+                continue
+            self.check(fn, rc)
+            k = int(n.value)
+            return i1[:k].copy(), i2[:k].copy(), lv[:k].astype(bool)
+
+    def encounter_check_all_plpl(self, r, v, renc, dt, mode=L.SWG_ENC_TRIANGULAR, cap=1024):
+        r = _f64(r, (-1, 3))
+        v = _f64(v, (-1, 3))
+        renc = _f64(renc)
+        return self._enc("swg_encounter_check_all_plpl",
+                         [mode, r.shape[0], _ptr(r), _ptr(v), _ptr(renc), float(dt)], cap)
+
+    def encounter_check_all_plplm(self, rplm, vplm, rplt, vplt, rencm, renct, dt, mode=L.SWG_ENC_TRIANGULAR,
+                                  cap=1024):
+        rplm, vplm = _f64(rplm, (-1, 3)), _f64(vplm, (-1, 3))
+        rplt, vplt = _f64(rplt, (-1, 3)), _f64(vplt, (-1, 3))
+        rencm, renct = _f64(rencm), _f64(renct)
+        return self._enc("swg_encounter_check_all_plplm",
+                         [mode, rplm.shape[0], rplt.shape[0], _ptr(rplm), _ptr(vplm), _ptr(rplt), _ptr(vplt),
+                          _ptr(rencm), _ptr(renct), float(dt)], cap)
+
+    def encounter_check_all_pltp(self, rpl, vpl, rtp, vtp, renc, dt, mode=L.SWG_ENC_TRIANGULAR, cap=1024):
+        rpl, vpl = _f64(rpl, (-1, 3)), _f64(vpl, (-1, 3))
+        rtp, vtp = _f64(rtp, (-1, 3)), _f64(vtp, (-1, 3))
+        renc = _f64(renc)
+        return self._enc("swg_encounter_check_all_pltp",
+                         [mode, rpl.shape[0], rtp.shape[0], _ptr(rpl), _ptr(vpl), _ptr(rtp), _ptr(vtp), _ptr(renc),
+                          float(dt)], cap)
+
+
+INTEGRATORS = {"WHM": L.SWG_WHM, "HELIO": L.SWG_HELIO, "SYMBA": L.SWG_SYMBA}
+
+
+class NBodySystem:
+    """Device-resident n-body system stepped by the WHM / HELIO / SyMBA loops.
+
+    Mirrors ``swiftest_nbody_system`` + ``step`` (src/swiftest/swiftest_driver.f90:130-180).
+    Massive bodies must already be ordered as the reference's initialise does
+    (HELIO/SyMBA: Gmass descending; WHM: heliocentric distance ascending), which
+    ``initial_conditions.sort_for_integrator`` provides.
+    """
+
+    def __init__(self, ctx: Context, integrator: str, cb, pl, tp=None, dt=0.01, loop_mode="TRIANGULAR",
+                 encounter_check_plpl="TRIANGULAR", encounter_check_pltp="TRIANGULAR", rhscale=6.5, lclose=True,
+                 gmtiny=0.0, precision="FP64"):
+        self.ctx = ctx
+        lib = ctx.lib
+        self.integrator = integrator.upper()
+        npl = len(pl["Gmass"])
+        ntp = 0 if tp is None else len(tp["rh"])
+        h = C.c_void_p()
+        ctx.check("swg_system_create", lib.swg_system_create(ctx.h, INTEGRATORS[self.integrator], npl, ntp,
+                                                             C.byref(h)))
+        self.h = h
+        self.npl, self.ntp = npl, ntp
+        ctx.check("swg_system_set_cb", lib.swg_system_set_cb(h, float(cb["Gmass"]), float(cb["radius"])))
+        self._keep = []
+        if npl:
+            arrs = [_f64(pl["rh"], (npl, 3)), _f64(pl["vh"], (npl, 3)), _f64(pl["Gmass"]), _f64(pl["radius"]),
+                    _f64(pl["rhill"])]
+            ctx.check("swg_system_set_pl", lib.swg_system_set_pl(h, *[_ptr(a) for a in arrs]))
+        if ntp:
+            arrs = [_f64(tp["rh"], (ntp, 3)), _f64(tp["vh"], (ntp, 3))]
+            ctx.check("swg_system_set_tp", lib.swg_system_set_tp(h, *[_ptr(a) for a in arrs]))
+        enc = {"TRIANGULAR": L.SWG_ENC_TRIANGULAR, "SORTSWEEP": L.SWG_ENC_SORTSWEEP}
+        loop = {"TRIANGULAR": 0, "FLAT": 1}[loop_mode.upper()]
+        prec = {"FP64": L.SWG_FP64, "MIXED": L.SWG_MIXED}[precision.upper()]
+        ctx.check("swg_system_set_param", lib.swg_system_set_param(
+            h, float(dt), loop, enc[encounter_check_plpl.upper()], enc[encounter_check_pltp.upper()], float(rhscale),
+            int(bool(lclose)), float(gmtiny), prec))
+        ctx.check("swg_system_initialize", lib.swg_system_initialize(h))
+
+    def step(self, nsteps: int = 1):
+        self.ctx.check("swg_system_step", self.ctx.lib.swg_system_step(self.h, int(nsteps)))
+
+    def get_pl(self):
+        rh = np.zeros((self.npl, 3))
+        vh = np.zeros((self.npl, 3))
+        st = np.zeros(self.npl, np.int32)
+        self.ctx.check("swg_system_get_pl", self.ctx.lib.swg_system_get_pl(self.h, _ptr(rh), _ptr(vh), _ptr(st)))
+        return rh, vh, st
+
+    def get_tp(self):
+        rh = np.zeros((self.ntp, 3))
+        vh = np.zeros((self.ntp, 3))
+        st = np.zeros(self.ntp, np.int32)
+        self.ctx.check("swg_system_get_tp", self.ctx.lib.swg_system_get_tp(self.h, _ptr(rh), _ptr(vh), _ptr(st)))
+        return rh, vh, st
+
+    def energy(self):
+        out = np.zeros(9)
+        self.ctx.check("swg_system_energy", self.ctx.lib.swg_system_energy(self.h, _ptr(out)))
+        return {"te": out[0], "ke": out[1], "pe": out[2], "be": out[3], "L": out[4:7].copy(), "GMtot": out[7],
+                "te_helio": out[8]}
+
+    def stats(self):
+        out = np.zeros(5, np.int64)
+        self.ctx.check("swg_system_stats", self.ctx.lib.swg_system_stats(self.h, _ptr(out)))
+        return {"steps_with_encounters": int(out[0]), "max_recursion": int(out[1]), "plpl_encounters": int(out[2]),
+                "pltp_encounters": int(out[3]), "collisions": int(out[4])}
+
+    def _list(self, fn):
+        n = C.c_int64(0)
+        cap = 1024
+        while True:
+            i1 = np.zeros(cap, np.int32)
+            i2 = np.zeros(cap, np.int32)
+            rc = getattr(self.ctx.lib, fn)(self.h, cap, C.byref(n), _ptr(i1), _ptr(i2))
+            if rc == L.SWG_ERR_CAPACITY:
+                cap = int(n.value)
+                continue
+            self.ctx.check(fn, rc)
+            return i1[:n.value].copy(), i2[:n.value].copy()
+
+    def plpl_list(self):
+        return self._list("swg_system_plpl_list")
+
+    def pltp_list(self):
+        return self._list("swg_system_pltp_list")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.swg_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

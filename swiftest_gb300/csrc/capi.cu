@@ -1,0 +1,288 @@
+// capi.cu -- context management and the kernel-level C ABI entry points.
+//
+// Each entry point mirrors one Fortran procedure of the reference (cited in
+// include/swiftest_gb300.h).  With SWG_MEM_HOST the arrays are staged through
+// the context's grow-only device slots; with SWG_MEM_DEVICE the caller's
+// device pointers are used directly.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "swg_internal.cuh"
+
+namespace swg {
+
+int cuda_status(swg_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return SWG_OK;
+    if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return SWG_ERR_CUDA;
+}
+
+int launch_status(swg_ctx *c, const char *what) { return cuda_status(c, cudaGetLastError(), what); }
+
+int ensure(swg_ctx *c, DevBuf &buf, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (buf.ptr && buf.bytes >= bytes) return SWG_OK;
+    if (buf.ptr) {
+        cudaFree(buf.ptr);
+        buf.ptr = nullptr;
+        buf.bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&buf.ptr, bytes);
+    if (e != cudaSuccess) {
+        buf.ptr = nullptr;
+        if (c) c->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return SWG_ERR_NOMEM;
+    }
+    buf.bytes = bytes;
+    return SWG_OK;
+}
+
+int ensure_slot(swg_ctx *c, int slot, size_t bytes, void **out) {
+    SWG_TRY(ensure(c, c->slot[slot], bytes));
+    *out = c->slot[slot].ptr;
+    return SWG_OK;
+}
+
+}  // namespace swg
+
+using namespace swg;
+
+namespace {
+
+// Stage an input array: host -> slot, or pass the device pointer through.
+template <typename T>
+int stage_in(swg_ctx *c, int mem, int slot, const T *p, size_t n, T **d) {
+    if (!p) {
+        *d = nullptr;
+        return SWG_OK;
+    }
+    if (mem == SWG_MEM_DEVICE) {
+        *d = const_cast<T *>(p);
+        return SWG_OK;
+    }
+    void *q;
+    SWG_TRY(ensure_slot(c, slot, sizeof(T) * (n ? n : 1), &q));
+    if (n) SWG_TRY(cuda_status(c, cudaMemcpyAsync(q, p, sizeof(T) * n, cudaMemcpyHostToDevice, c->stream), "H2D"));
+    *d = (T *)q;
+    return SWG_OK;
+}
+template <typename T>
+int stage_out(swg_ctx *c, int mem, T *p, const T *d, size_t n) {
+    if (mem == SWG_MEM_DEVICE || !p || n == 0) return SWG_OK;
+    return cuda_status(c, cudaMemcpyAsync(p, d, sizeof(T) * n, cudaMemcpyDeviceToHost, c->stream), "D2H");
+}
+int finish(swg_ctx *c, int mem) {
+    if (mem == SWG_MEM_DEVICE) return launch_status(c, "launch");
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "sync");
+}
+bool bad_mem(int mem) { return mem != SWG_MEM_HOST && mem != SWG_MEM_DEVICE; }
+bool bad_prec(int p) { return p != SWG_FP64 && p != SWG_MIXED; }
+
+}  // namespace
+
+extern "C" {
+
+int swg_create(swg_ctx **ctx, int device) {
+    if (!ctx) return SWG_ERR_ARG;
+    *ctx = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return SWG_ERR_CUDA;
+    if (device < 0 || device >= ndev) return SWG_ERR_ARG;
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return SWG_ERR_CUDA;
+    swg_ctx *c = new swg_ctx();
+    c->device = device;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return SWG_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    *ctx = c;
+    return SWG_OK;
+}
+
+int swg_destroy(swg_ctx *c) {
+    if (!c) return SWG_OK;
+    cudaStreamSynchronize(c->stream);
+    for (auto &b : c->slot)
+        if (b.ptr) cudaFree(b.ptr);
+    DevBuf *eb[] = {&c->enc.raw, &c->enc.sort, &c->enc.counters};
+    for (DevBuf *b : eb)
+        if (b->ptr) cudaFree(b->ptr);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SWG_OK;
+}
+
+int swg_synchronize(swg_ctx *c) {
+    if (!c) return SWG_ERR_ARG;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+const char *swg_last_error(const swg_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+int64_t swg_launch_count(const swg_ctx *c) { return c ? c->launches : 0; }
+
+int swg_kick_getacch_int_all_tri_pl(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const double *Gmass,
+                                    const double *radius, double *acc, int precision, int mem) {
+    if (!c || npl < 0 || nplm < 0 || nplm > npl || bad_mem(mem) || bad_prec(precision)) return SWG_ERR_ARG;
+    if (npl == 0) return SWG_OK;
+    if (!r || !Gmass || !acc) return SWG_ERR_ARG;
+    double *dr, *dg, *dR, *da;
+    SWG_TRY(stage_in(c, mem, 0, r, 3 * (size_t)npl, &dr));
+    SWG_TRY(stage_in(c, mem, 1, Gmass, (size_t)npl, &dg));
+    SWG_TRY(stage_in(c, mem, 2, radius, (size_t)npl, &dR));
+    SWG_TRY(stage_in(c, mem, 3, (const double *)acc, 3 * (size_t)npl, &da));
+    if (precision == SWG_MIXED) {
+        const int nch = kick_mixed_chunks(c, npl, npl);
+        SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, nch)));
+        SWG_TRY(kick_mixed_launch(c, false, npl, npl, nplm, dr, dr, dg, dR, nullptr, da, 0, nch, c->slot[10].ptr));
+    } else {
+        const int mode = (npl - nplm) > nplm ? KICK_SPLIT : KICK_DIRECT;
+        SWG_TRY(kick_plpl_fp64(c, npl, nplm, dr, dg, dR, da, mode, 0));
+    }
+    SWG_TRY(stage_out(c, mem, acc, da, 3 * (size_t)npl));
+    return finish(c, mem);
+}
+
+int swg_kick_getacch_int_all_flat_pl(swg_ctx *c, int32_t npl, int32_t nplm, int64_t nplpl, const int32_t *k_plpl,
+                                     const double *r, const double *Gmass, const double *radius, double *acc,
+                                     int precision, int mem) {
+    if (!c || npl < 0 || nplm < 0 || nplm > npl || nplpl < 0 || bad_mem(mem) || bad_prec(precision))
+        return SWG_ERR_ARG;
+    if (npl == 0) return SWG_OK;
+    if (!r || !Gmass || !acc) return SWG_ERR_ARG;
+    double *dr, *dg, *dR, *da;
+    SWG_TRY(stage_in(c, mem, 0, r, 3 * (size_t)npl, &dr));
+    SWG_TRY(stage_in(c, mem, 1, Gmass, (size_t)npl, &dg));
+    SWG_TRY(stage_in(c, mem, 2, radius, (size_t)npl, &dR));
+    SWG_TRY(stage_in(c, mem, 3, (const double *)acc, 3 * (size_t)npl, &da));
+    if (!k_plpl) {
+        if (nplpl != nplplm_count(npl, nplm)) {
+            c->err = "nplpl does not match the canonical pair count for (npl, nplm)";
+            return SWG_ERR_ARG;
+        }
+        if (precision == SWG_MIXED) {
+            const int nch = kick_mixed_chunks(c, npl, npl);
+            SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, nch)));
+            SWG_TRY(kick_mixed_launch(c, false, npl, npl, nplm, dr, dr, dg, dR, nullptr, da, 0, nch, c->slot[10].ptr));
+        } else {
+            SWG_TRY(kick_plpl_fp64(c, npl, nplm, dr, dg, dR, da, KICK_SPLIT, 0));
+        }
+    } else {
+        int32_t *dk;
+        SWG_TRY(stage_in(c, mem, 4, k_plpl, 2 * (size_t)nplpl, &dk));
+        void *scr;
+        SWG_TRY(ensure_slot(c, 11, sizeof(double) * 6 * (size_t)npl, &scr));
+        SWG_TRY(kick_pairs(c, npl, nplpl, dk, nullptr, nullptr, dr, dg, dR, da, 1.0, (double *)scr));
+    }
+    SWG_TRY(stage_out(c, mem, acc, da, 3 * (size_t)npl));
+    return finish(c, mem);
+}
+
+int swg_kick_getacch_int_all_tp(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const double *rpl,
+                                const double *GMpl, const int32_t *lmask, double *acc, int precision, int mem) {
+    if (!c || ntp < 0 || npl < 0 || bad_mem(mem) || bad_prec(precision)) return SWG_ERR_ARG;
+    if (ntp == 0 || npl == 0) return SWG_OK;
+    if (!rtp || !rpl || !GMpl || !lmask || !acc) return SWG_ERR_ARG;
+    double *drt, *drp, *dg, *da;
+    int32_t *dm;
+    SWG_TRY(stage_in(c, mem, 0, rtp, 3 * (size_t)ntp, &drt));
+    SWG_TRY(stage_in(c, mem, 1, rpl, 3 * (size_t)npl, &drp));
+    SWG_TRY(stage_in(c, mem, 2, GMpl, (size_t)npl, &dg));
+    SWG_TRY(stage_in(c, mem, 4, lmask, (size_t)ntp, &dm));
+    SWG_TRY(stage_in(c, mem, 3, (const double *)acc, 3 * (size_t)ntp, &da));
+    if (precision == SWG_MIXED) {
+        const int nch = kick_mixed_chunks(c, ntp, npl);
+        SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(ntp, nch)));
+        SWG_TRY(kick_mixed_launch(c, true, ntp, npl, 0, drt, drp, dg, nullptr, dm, da, 0, nch, c->slot[10].ptr));
+    } else {
+        SWG_TRY(kick_tp_fp64(c, ntp, npl, drt, drp, dg, dm, da, 0));
+    }
+    SWG_TRY(stage_out(c, mem, acc, da, 3 * (size_t)ntp));
+    return finish(c, mem);
+}
+
+int swg_drift_all(swg_ctx *c, const double *mu, double *x, double *v, int32_t n, int32_t lgr, double inv_c2,
+                  double dt, const int32_t *lmask, int32_t *iflag, int mem) {
+    if (!c || n < 0 || bad_mem(mem)) return SWG_ERR_ARG;
+    if (n == 0) return SWG_OK;
+    if (!mu || !x || !v || !lmask || !iflag) return SWG_ERR_ARG;
+    double *dmu, *dx, *dv;
+    int32_t *dm, *df;
+    SWG_TRY(stage_in(c, mem, 0, mu, (size_t)n, &dmu));
+    SWG_TRY(stage_in(c, mem, 1, (const double *)x, 3 * (size_t)n, &dx));
+    SWG_TRY(stage_in(c, mem, 2, (const double *)v, 3 * (size_t)n, &dv));
+    SWG_TRY(stage_in(c, mem, 4, lmask, (size_t)n, &dm));
+    SWG_TRY(stage_in(c, mem, 5, (const int32_t *)iflag, (size_t)n, &df));
+    SWG_TRY(drift_all(c, dmu, 0.0, dx, dv, n, lgr, inv_c2, dt, dm, df));
+    SWG_TRY(stage_out(c, mem, x, dx, 3 * (size_t)n));
+    SWG_TRY(stage_out(c, mem, v, dv, 3 * (size_t)n));
+    SWG_TRY(stage_out(c, mem, iflag, df, (size_t)n));
+    return finish(c, mem);
+}
+
+}  // extern "C"
+
+namespace {
+int enc_common(swg_ctx *c, int kind, int mode, int32_t n1, const double *r1, const double *v1, const double *renc1,
+               int32_t n2, const double *r2, const double *v2, const double *renc2, double dt, int64_t cap,
+               int64_t *nenc, int32_t *index1, int32_t *index2, int32_t *lvdotr, int mem) {
+    if (!c || !nenc || n1 < 0 || n2 < 0 || cap < 0 || bad_mem(mem)) return SWG_ERR_ARG;
+    if (mode != SWG_ENC_TRIANGULAR && mode != SWG_ENC_SORTSWEEP) return SWG_ERR_ARG;
+    *nenc = 0;
+    if (n1 == 0 || (kind != 0 && n2 == 0 && kind == 2)) return SWG_OK;
+    double *d1r, *d1v, *d1c, *d2r = nullptr, *d2v = nullptr, *d2c = nullptr;
+    SWG_TRY(stage_in(c, mem, 0, r1, 3 * (size_t)n1, &d1r));
+    SWG_TRY(stage_in(c, mem, 1, v1, 3 * (size_t)n1, &d1v));
+    SWG_TRY(stage_in(c, mem, 2, renc1, (size_t)n1, &d1c));
+    if (kind != 0 && n2 > 0) {
+        SWG_TRY(stage_in(c, mem, 3, r2, 3 * (size_t)n2, &d2r));
+        SWG_TRY(stage_in(c, mem, 4, v2, 3 * (size_t)n2, &d2v));
+        SWG_TRY(stage_in(c, mem, 5, renc2, (size_t)n2, &d2c));
+    }
+    int64_t n = 0;
+    int32_t *i1, *i2, *lv;
+    SWG_TRY(encounter_check_kind(c, c->enc, kind, mode, n1, d1r, d1v, d1c, n2, d2r, d2v, d2c, dt, &n, &i1, &i2, &lv));
+    *nenc = n;
+    if (n > cap) return SWG_ERR_CAPACITY;
+    if (n == 0) return SWG_OK;
+    if (!index1 || !index2 || !lvdotr) return SWG_ERR_ARG;
+    const cudaMemcpyKind kd = mem == SWG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(index1, i1, 4 * n, kd, c->stream), "enc out"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(index2, i2, 4 * n, kd, c->stream), "enc out"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(lvdotr, lv, 4 * n, kd, c->stream), "enc out"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "enc sync");
+}
+}  // namespace
+
+extern "C" {
+
+int swg_encounter_check_all_plpl(swg_ctx *c, int mode, int32_t npl, const double *r, const double *v,
+                                 const double *renc, double dt, int64_t cap, int64_t *nenc, int32_t *index1,
+                                 int32_t *index2, int32_t *lvdotr, int mem) {
+    return enc_common(c, 0, mode, npl, r, v, renc, 0, nullptr, nullptr, nullptr, dt, cap, nenc, index1, index2,
+                      lvdotr, mem);
+}
+
+int swg_encounter_check_all_plplm(swg_ctx *c, int mode, int32_t nplm, int32_t nplt, const double *rplm,
+                                  const double *vplm, const double *rplt, const double *vplt, const double *rencm,
+                                  const double *renct, double dt, int64_t cap, int64_t *nenc, int32_t *index1,
+                                  int32_t *index2, int32_t *lvdotr, int mem) {
+    return enc_common(c, 1, mode, nplm, rplm, vplm, rencm, nplt, rplt, vplt, renct, dt, cap, nenc, index1, index2,
+                      lvdotr, mem);
+}
+
+int swg_encounter_check_all_pltp(swg_ctx *c, int mode, int32_t npl, int32_t ntp, const double *rpl,
+                                 const double *vpl, const double *rtp, const double *vtp, const double *renc,
+                                 double dt, int64_t cap, int64_t *nenc, int32_t *index1, int32_t *index2,
+                                 int32_t *lvdotr, int mem) {
+    return enc_common(c, 2, mode, npl, rpl, vpl, renc, ntp, rtp, vtp, nullptr, dt, cap, nenc, index1, index2,
+                      lvdotr, mem);
+}
+
+}  // extern "C"

@@ -1,0 +1,559 @@
+// encounter.cu -- close-encounter checks for sm_103a.
+//
+// Restates encounter_check_all_plpl / _plplm / _pltp (src/encounter/encounter_check.f90:14-140)
+// in both of the reference's modes:
+//   * TRIANGULAR (:384-570): every pair is tested with encounter_check_one (:573-621).
+//   * SORTSWEEP  (:143-326, :763-988): 1-D radial bounding boxes |r| +- 1.1 renc,
+//     sorted; each body whose box holds >= 2 foreign extents strictly inside
+//     (the reference's loverlap test) tests the bodies whose extents lie inside.
+//
+// The encounter decision is made in FP64 with the reference's expression order
+// (this file is compiled with -fmad=false), so lists are bit-identical to the
+// reference loop.  In TRIANGULAR mode a conservative FP32 prefilter first
+// rejects pairs whose closest approach over [0, dt] provably exceeds the
+// encounter radius:  min_t |x + v t| >= |x| - |v| dt.  The FP32 estimate of
+// |x| - |v| dt is lowered by a relative 2e-6 plus absolute terms covering the
+// hi/lo position split and the float rounding of velocities, and the radius is
+// raised by 1e-5 relative plus 4e-15 |x|^2/R, which bounds the FP64 rounding of
+// r^2 - (v.r)^2/v^2.  Only pairs the FP64 test could accept reach it, so the
+// prefilter changes speed, never the list.
+//
+// Output: pairs are appended with an atomic counter (up to cap), then sorted by
+// (index1, index2) with a bitonic sort (single CTA in shared memory when the
+// padded length fits, else global compare-exchange passes).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "swg_internal.cuh"
+
+namespace swg {
+
+constexpr int ET = 128;  // partner tile / block size
+
+// encounter_check_one (:573-621), FP64, reference expression order
+__device__ __forceinline__ void d_encounter_one(double xr, double yr, double zr, double vxr, double vyr, double vzr,
+                                                double renc, double dt, int &lenc, int &lvdotr) {
+    const double r2 = xr * xr + yr * yr + zr * zr;
+    const double r2crit = renc * renc;
+    double vdotr, r2min;
+    if (r2 > r2crit) {
+        vdotr = vxr * xr + vyr * yr + vzr * zr;
+        if (vdotr > 0.0) {
+            r2min = r2;
+        } else {
+            const double v2 = vxr * vxr + vyr * vyr + vzr * vzr;
+            if (v2 <= VSMALL) {
+                r2min = r2;
+            } else {
+                const double tmin = -vdotr / v2;
+                if (tmin < dt)
+                    r2min = r2 - vdotr * vdotr / v2;
+                else
+                    r2min = r2 + 2.0 * vdotr * dt + v2 * (dt * dt);
+            }
+        }
+    } else {
+        vdotr = -1.0;
+        r2min = r2;
+    }
+    lvdotr = (vdotr < 0.0);
+    lenc = lvdotr && (r2min <= r2crit);
+}
+
+struct BodyF {
+    float4 a;  // x_hi, y_hi, z_hi, renc
+    float4 b;  // x_lo, y_lo, z_lo, |r|
+    float4 v;  // vx, vy, vz, |v|
+};
+
+__device__ __forceinline__ BodyF load_body(const double *r, const double *v, const double *renc, int i) {
+    BodyF o;
+    const double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+    const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+    o.a = make_float4(xh, yh, zh, renc ? __double2float_rn(renc[i]) : 0.f);
+    o.b = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
+                      __double2float_rn(z - (double)zh), sqrtf(xh * xh + yh * yh + zh * zh));
+    const float vx = __double2float_rn(v[3 * i]), vy = __double2float_rn(v[3 * i + 1]),
+                vz = __double2float_rn(v[3 * i + 2]);
+    o.v = make_float4(vx, vy, vz, sqrtf(vx * vx + vy * vy + vz * vz));
+    return o;
+}
+
+// true when the pair certainly fails encounter_check_one (see file header)
+__device__ __forceinline__ bool prefilter_reject(const BodyF &p, const BodyF &q, float dtf) {
+    const float dx = (p.a.x - q.a.x) + (p.b.x - q.b.x);
+    const float dy = (p.a.y - q.a.y) + (p.b.y - q.b.y);
+    const float dz = (p.a.z - q.a.z) + (p.b.z - q.b.z);
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float dvx = p.v.x - q.v.x, dvy = p.v.y - q.v.y, dvz = p.v.z - q.v.z;
+    const float vmag = sqrtf(dvx * dvx + dvy * dvy + dvz * dvz);
+    const float R = p.a.w + q.a.w;
+    const float xlo = sqrtf(r2) * (1.0f - 2e-6f) - 1e-13f * (p.b.w + q.b.w);
+    const float vhi = vmag * (1.0f + 2e-6f) + 2e-7f * (p.v.w + q.v.w);
+    const float dlo = xlo - vhi * dtf;
+    const float rhi = R * (1.0f + 1e-5f) + 4e-15f * (r2 / R);
+    return dlo > rhi;  // NaN/inf comparisons are false: such pairs go to the FP64 test
+}
+
+// Receivers: list-2 bodies j (one thread each).  Partners: list-1 bodies i,
+// i < j when `upper` (pl-pl), all i otherwise.  Pair written as (i+1, j+1+shift2).
+__global__ void __launch_bounds__(ET) k_encounter_tri(int n1, const double *__restrict__ r1,
+                                                      const double *__restrict__ v1,
+                                                      const double *__restrict__ renc1, int n2,
+                                                      const double *__restrict__ r2, const double *__restrict__ v2,
+                                                      const double *__restrict__ renc2, int upper, int shift2,
+                                                      double dt, long long cap, int32_t *__restrict__ o1,
+                                                      int32_t *__restrict__ o2, int32_t *__restrict__ olv,
+                                                      unsigned long long *__restrict__ count) {
+    __shared__ float4 sa[ET], sb[ET], sv[ET];
+    const int j = blockIdx.x * ET + threadIdx.x;
+    const bool active = j < n2;
+    BodyF q;
+    if (active) q = load_body(r2, v2, renc2, j);
+    const float dtf = __double2float_ru(dt) * (1.0f + 1e-6f);
+    const int iend_blk = upper ? min(n1, (int)(blockIdx.x * ET + ET)) : n1;
+    const int iend = upper ? j : n1;
+    for (int i0 = 0; i0 < iend_blk; i0 += ET) {
+        const int il = i0 + threadIdx.x;
+        if (il < n1) {
+            BodyF p = load_body(r1, v1, renc1, il);
+            sa[threadIdx.x] = p.a;
+            sb[threadIdx.x] = p.b;
+            sv[threadIdx.x] = p.v;
+        }
+        __syncthreads();
+        if (active) {
+            const int nt = min(ET, iend - i0);
+            for (int ii = 0; ii < nt; ii++) {
+                BodyF p;
+                p.a = sa[ii];
+                p.b = sb[ii];
+                p.v = sv[ii];
+                if (prefilter_reject(p, q, dtf)) continue;
+                const int i = i0 + ii;
+                const double xr = r2[3 * j + 0] - r1[3 * i + 0];
+                const double yr = r2[3 * j + 1] - r1[3 * i + 1];
+                const double zr = r2[3 * j + 2] - r1[3 * i + 2];
+                const double vxr = v2[3 * j + 0] - v1[3 * i + 0];
+                const double vyr = v2[3 * j + 1] - v1[3 * i + 1];
+                const double vzr = v2[3 * j + 2] - v1[3 * i + 2];
+                const double renc12 = renc1[i] + (renc2 ? renc2[j] : 0.0);
+                int lenc, lv;
+                d_encounter_one(xr, yr, zr, vxr, vyr, vzr, renc12, dt, lenc, lv);
+                if (lenc) {
+                    const unsigned long long k = atomicAdd(count, 1ull);
+                    if ((long long)k < cap) {
+                        o1[k] = i + 1;
+                        o2[k] = j + 1 + shift2;
+                        olv[k] = lv;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ sorting
+// Generic (key, val) sort, ascending by (key, val).  Padding uses all-ones.
+constexpr int SORT_SMEM_N = 4096;  // elements sorted in one CTA (48 KB)
+
+__device__ __forceinline__ bool kv_greater(uint64_t ka, uint32_t va, uint64_t kb, uint32_t vb) {
+    return ka > kb || (ka == kb && va > vb);
+}
+
+__global__ void k_bitonic_shared(uint64_t *keys, uint32_t *vals, int64_t n_pad, int kmax_global) {
+    // Sorts each SORT_SMEM_N segment completely (kmax_global == 0) or finishes the
+    // merge stages j < SORT_SMEM_N of a global stage k (kmax_global == k).
+    __shared__ uint64_t sk[SORT_SMEM_N];
+    __shared__ uint32_t sv[SORT_SMEM_N];
+    const int64_t base = (int64_t)blockIdx.x * SORT_SMEM_N;
+    const int len = (int)((n_pad - base) < (int64_t)SORT_SMEM_N ? (n_pad - base) : (int64_t)SORT_SMEM_N);
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        sk[t] = keys[base + t];
+        sv[t] = vals[base + t];
+    }
+    __syncthreads();
+    if (kmax_global == 0) {
+        for (int k = 2; k <= len; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int t = threadIdx.x; t < len; t += blockDim.x) {
+                    const int p = t ^ jj;
+                    if (p > t) {
+                        const int64_t gt = base + t;
+                        const bool up = ((gt & k) == 0);
+                        const bool sw = up ? kv_greater(sk[t], sv[t], sk[p], sv[p]) : kv_greater(sk[p], sv[p], sk[t], sv[t]);
+                        if (sw) {
+                            uint64_t tk = sk[t];
+                            sk[t] = sk[p];
+                            sk[p] = tk;
+                            uint32_t tv = sv[t];
+                            sv[t] = sv[p];
+                            sv[p] = tv;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+    } else {
+        const int64_t k = kmax_global;
+        for (int jj = SORT_SMEM_N >> 1; jj > 0; jj >>= 1) {
+            for (int t = threadIdx.x; t < len; t += blockDim.x) {
+                const int p = t ^ jj;
+                if (p > t) {
+                    const int64_t gt = base + t;
+                    const bool up = ((gt & k) == 0);
+                    const bool sw = up ? kv_greater(sk[t], sv[t], sk[p], sv[p]) : kv_greater(sk[p], sv[p], sk[t], sv[t]);
+                    if (sw) {
+                        uint64_t tk = sk[t];
+                        sk[t] = sk[p];
+                        sk[p] = tk;
+                        uint32_t tv = sv[t];
+                        sv[t] = sv[p];
+                        sv[p] = tv;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        keys[base + t] = sk[t];
+        vals[base + t] = sv[t];
+    }
+}
+
+__global__ void k_bitonic_global(uint64_t *keys, uint32_t *vals, int64_t n_pad, int64_t k, int64_t jj) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n_pad) return;
+    const int64_t p = t ^ jj;
+    if (p <= t) return;
+    const bool up = ((t & k) == 0);
+    const uint64_t kt = keys[t], kp = keys[p];
+    const uint32_t vt = vals[t], vp = vals[p];
+    const bool sw = up ? kv_greater(kt, vt, kp, vp) : kv_greater(kp, vp, kt, vt);
+    if (sw) {
+        keys[t] = kp;
+        keys[p] = kt;
+        vals[t] = vp;
+        vals[p] = vt;
+    }
+}
+
+__global__ void k_fill_pad(uint64_t *keys, uint32_t *vals, int64_t n, int64_t n_pad) {
+    const int64_t t = n + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < n_pad) {
+        keys[t] = ~0ull;
+        vals[t] = ~0u;
+    }
+}
+
+int64_t sort_padded_len(int64_t n) {
+    int64_t p = 1;
+    while (p < n) p <<= 1;
+    return p < 2 ? 2 : p;
+}
+
+// keys/vals must have room for sort_padded_len(n) elements.
+int sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals) {
+    if (n <= 1) return SWG_OK;
+    const int64_t n_pad = sort_padded_len(n);
+    if (n_pad > n) {
+        k_fill_pad<<<(int)((n_pad - n + 255) / 256), 256, 0, c->stream>>>(keys, vals, n, n_pad);
+        c->launches++;
+    }
+    const int64_t nseg = (n_pad + SORT_SMEM_N - 1) / SORT_SMEM_N;
+    k_bitonic_shared<<<(int)nseg, 512, 0, c->stream>>>(keys, vals, n_pad, 0);
+    c->launches++;
+    for (int64_t k = 2 * (int64_t)SORT_SMEM_N; k <= n_pad; k <<= 1) {
+        for (int64_t jj = k >> 1; jj >= SORT_SMEM_N; jj >>= 1) {
+            k_bitonic_global<<<(int)((n_pad + 255) / 256), 256, 0, c->stream>>>(keys, vals, n_pad, k, jj);
+            c->launches++;
+        }
+        k_bitonic_shared<<<(int)nseg, 512, 0, c->stream>>>(keys, vals, n_pad, (int)k);
+        c->launches++;
+    }
+    return launch_status(c, "sort_kv");
+}
+
+// pack (i1,i2,lv) into key=(i1<<32|i2), val=lv ; and back
+__global__ void k_pack_pairs(int64_t n, const int32_t *i1, const int32_t *i2, const int32_t *lv, uint64_t *keys,
+                             uint32_t *vals) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    keys[t] = ((uint64_t)(uint32_t)i1[t] << 32) | (uint64_t)(uint32_t)i2[t];
+    vals[t] = (uint32_t)lv[t];
+}
+// unpack, dropping repeated (i1,i2) keys (they carry the same lvdotr); the
+// surviving count goes to *nout.  Single pass with a block-wide prefix via atomics
+// is not order-preserving, so compaction uses a flag + scan in one block.
+__global__ void k_unpack_unique(int64_t n, const uint64_t *keys, const uint32_t *vals, int32_t *i1, int32_t *i2,
+                                int32_t *lv, unsigned long long *nout) {
+    // one block; sequential chunks with block scan
+    __shared__ int64_t s_base;
+    __shared__ int s_scan[1024];
+    if (threadIdx.x == 0) s_base = 0;
+    __syncthreads();
+    for (int64_t c0 = 0; c0 < n; c0 += blockDim.x) {
+        const int64_t t = c0 + threadIdx.x;
+        int keep = 0;
+        if (t < n) keep = (t == 0) || (keys[t] != keys[t - 1]);
+        s_scan[threadIdx.x] = keep;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            int add = (threadIdx.x >= (unsigned)off) ? s_scan[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_scan[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (keep) {
+            const int64_t o = s_base + s_scan[threadIdx.x] - 1;
+            i1[o] = (int32_t)(keys[t] >> 32);
+            i2[o] = (int32_t)(keys[t] & 0xffffffffull);
+            lv[o] = (int32_t)vals[t];
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_base += s_scan[threadIdx.x];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *nout = (unsigned long long)s_base;
+}
+
+// scratch: 12 bytes per padded element
+size_t sort_pairs_scratch_bytes(int64_t n) { return (size_t)sort_padded_len(n) * 12 + 256; }
+
+int sort_pairs_unique(swg_ctx *c, int64_t n, int32_t *i1, int32_t *i2, int32_t *lv, void *scratch,
+                      unsigned long long *d_nout) {
+    if (n <= 0) return SWG_OK;
+    const int64_t n_pad = sort_padded_len(n);
+    uint64_t *keys = (uint64_t *)scratch;
+    uint32_t *vals = (uint32_t *)(keys + n_pad);
+    k_pack_pairs<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(n, i1, i2, lv, keys, vals);
+    c->launches++;
+    SWG_TRY(sort_kv(c, n, keys, vals));
+    k_unpack_unique<<<1, 1024, 0, c->stream>>>(n, keys, vals, i1, i2, lv, d_nout);
+    c->launches++;
+    return launch_status(c, "sort_pairs_unique");
+}
+
+// ------------------------------------------------------------------ sort & sweep
+// orderable bit pattern of a double (ascending numeric order)
+__device__ __forceinline__ uint64_t d2key(double x) {
+    uint64_t u = (uint64_t)__double_as_longlong(x);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// gfortran NORM2 (scaled sum of squares), as used for |r| in the sweep extents
+__device__ __forceinline__ double d_norm2e(double a, double b, double c) {
+    double scale = 0.0, ssq = 1.0;
+    const double v[3] = {a, b, c};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (v[k] != 0.0) {
+            const double absx = fabs(v[k]);
+            if (scale < absx) {
+                const double q = scale / absx;
+                ssq = 1.0 + ssq * q * q;
+                scale = absx;
+            } else {
+                const double q = absx / scale;
+                ssq = ssq + q * q;
+            }
+        }
+    }
+    return scale * sqrt(ssq);
+}
+
+// extents: body b (0..ntot-1) -> keys[b] = rmin, keys[ntot+b] = rmax, vals = extent index
+__global__ void k_sas_extents(int n1, const double *r1, const double *renc1, int n2, const double *r2,
+                              const double *renc2, uint64_t *keys, uint32_t *vals) {
+    const int ntot = n1 + n2;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= ntot) return;
+    const double *r = b < n1 ? &r1[3 * b] : &r2[3 * (b - n1)];
+    const double rc = b < n1 ? renc1[b] : (renc2 ? renc2[b - n1] : 0.0);
+    const double rmag = d_norm2e(r[0], r[1], r[2]);
+    keys[b] = d2key(rmag - RSWEEP_FACTOR * rc);
+    vals[b] = (uint32_t)b;
+    keys[ntot + b] = d2key(rmag + RSWEEP_FACTOR * rc);
+    vals[ntot + b] = (uint32_t)(ntot + b);
+}
+
+__global__ void k_sas_positions(int ntot, const uint32_t *vals, int32_t *ibeg, int32_t *iend) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 2 * ntot) return;
+    const uint32_t e = vals[k];
+    if (e < (uint32_t)ntot)
+        ibeg[e] = k + 1;
+    else
+        iend[e - ntot] = k + 1;
+}
+
+// sweep: body b with loverlap tests the bodies whose extents are strictly inside its box
+__global__ void k_sas_sweep(int n1, const double *r1, const double *v1, const double *renc1, int n2,
+                            const double *r2, const double *v2, const double *renc2, int single, int shift2, double dt,
+                            const uint32_t *vals, const int32_t *ibeg, const int32_t *iend, long long cap,
+                            int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count) {
+    const int ntot = n1 + n2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntot) return;
+    if (!((ibeg[i] + 1) < (iend[i] - 1))) return;
+    const bool il1 = i < n1;
+    const double *ri = il1 ? &r1[3 * i] : &r2[3 * (i - n1)];
+    const double *vi = il1 ? &v1[3 * i] : &v2[3 * (i - n1)];
+    const double renci = il1 ? renc1[i] : (renc2 ? renc2[i - n1] : 0.0);
+    for (int p = ibeg[i] + 1; p <= iend[i] - 1; p++) {
+        int b = (int)vals[p - 1];
+        if (b >= ntot) b -= ntot;
+        const bool bl1 = b < n1;
+        if (!single && bl1 == il1) continue;
+        const double *rb = bl1 ? &r1[3 * b] : &r2[3 * (b - n1)];
+        const double *vb = bl1 ? &v1[3 * b] : &v2[3 * (b - n1)];
+        const double rencb = bl1 ? renc1[b] : (renc2 ? renc2[b - n1] : 0.0);
+        int lenc, lv;
+        d_encounter_one(rb[0] - ri[0], rb[1] - ri[1], rb[2] - ri[2], vb[0] - vi[0], vb[1] - vi[1], vb[2] - vi[2],
+                        renci + rencb, dt, lenc, lv);
+        if (!lenc) continue;
+        int a, cidx;
+        if (single) {
+            a = min(i, b) + 1;
+            cidx = max(i, b) + 1;
+        } else if (il1) {
+            a = i + 1;
+            cidx = b - n1 + 1 + shift2;
+        } else {
+            a = b + 1;
+            cidx = i - n1 + 1 + shift2;
+        }
+        const unsigned long long k = atomicAdd(count, 1ull);
+        if ((long long)k < cap) {
+            o1[k] = a;
+            o2[k] = cidx;
+            olv[k] = lv;
+        }
+    }
+}
+
+size_t sas_scratch_bytes(int ntot) {
+    return (size_t)sort_padded_len(2 * (int64_t)ntot) * 12 + (size_t)ntot * 8 + 512;
+}
+
+// Runs one encounter check; pairs land unsorted in (o1,o2,olv) (first cap of
+// them) and the total in *count (device).  Caller sorts/dedups afterwards.
+int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const double *v1, const double *renc1, int n2,
+                     const double *r2, const double *v2, const double *renc2, int upper, int shift2, double dt,
+                     long long cap, int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
+                     void *sas_scratch) {
+    if (mode == SWG_ENC_SORTSWEEP) {
+        // single list when upper (pl-pl), double list otherwise
+        const int single = upper ? 1 : 0;
+        const int nb1 = n1, nb2 = single ? 0 : n2;
+        const int ntot = nb1 + nb2;
+        if (ntot <= 0) return SWG_OK;
+        const int64_t n_pad = sort_padded_len(2 * (int64_t)ntot);
+        uint64_t *keys = (uint64_t *)sas_scratch;
+        uint32_t *vals = (uint32_t *)(keys + n_pad);
+        int32_t *ibeg = (int32_t *)(vals + n_pad);
+        int32_t *iend = ibeg + ntot;
+        k_sas_extents<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, renc1, nb2, r2, renc2, keys, vals);
+        c->launches++;
+        SWG_TRY(sort_kv(c, 2 * (int64_t)ntot, keys, vals));
+        k_sas_positions<<<(2 * ntot + 255) / 256, 256, 0, c->stream>>>(ntot, vals, ibeg, iend);
+        c->launches++;
+        k_sas_sweep<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, v1, renc1, nb2, r2, v2, renc2, single,
+                                                               shift2, dt, vals, ibeg, iend, cap, o1, o2, olv,
+                                                               count);
+        c->launches++;
+        return launch_status(c, "encounter_sas");
+    }
+    if (n1 <= 0 || n2 <= 0) return SWG_OK;
+    k_encounter_tri<<<(n2 + ET - 1) / ET, ET, 0, c->stream>>>(n1, r1, v1, renc1, n2, r2, v2, renc2, upper, shift2, dt,
+                                                              cap, o1, o2, olv, count);
+    c->launches++;
+    return launch_status(c, "encounter_tri");
+}
+
+// shift index2 by `shift` for entries [from, to)
+__global__ void k_shift_i2(long long from, long long to, int32_t *i2, int shift) {
+    const long long t = from + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < to) i2[t] += shift;
+}
+
+int shift_index2(swg_ctx *c, long long from, long long to, int32_t *i2, int shift) {
+    if (to <= from || shift == 0) return SWG_OK;
+    k_shift_i2<<<(int)((to - from + 255) / 256), 256, 0, c->stream>>>(from, to, i2, shift);
+    c->launches++;
+    return launch_status(c, "shift_i2");
+}
+
+}  // namespace swg
+
+namespace swg {
+
+int encounter_check_kind(swg_ctx *c, EncWork &w, int kind, int mode, int32_t n1, const double *r1,
+                         const double *v1, const double *renc1, int32_t n2, const double *r2, const double *v2,
+                         const double *renc2, double dt, int64_t *n_out, int32_t **o1, int32_t **o2,
+                         int32_t **olv) {
+    *n_out = 0;
+    SWG_TRY(ensure(c, w.counters, 2 * sizeof(unsigned long long)));
+    unsigned long long *d_count = (unsigned long long *)w.counters.ptr;
+    if (w.rawcap < 1024) {
+        w.rawcap = 1024;
+        SWG_TRY(ensure(c, w.raw, (size_t)w.rawcap * 3 * sizeof(int32_t)));
+    }
+    const int ntot = (kind == 0 ? n1 : n1 + n2);
+    if (mode == SWG_ENC_SORTSWEEP) SWG_TRY(ensure(c, w.sort, sas_scratch_bytes(ntot)));
+    unsigned long long h_count = 0;
+    for (int attempt = 0; attempt < 8; attempt++) {
+        int32_t *i1 = (int32_t *)w.raw.ptr, *i2 = i1 + w.rawcap, *lv = i2 + w.rawcap;
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), c->stream), "memset"));
+        if (kind == 0) {
+            SWG_TRY(encounter_launch(c, mode, n1, r1, v1, renc1, n1, r1, v1, renc1, 1, 0, dt, w.rawcap, i1, i2, lv,
+                                     d_count, w.sort.ptr));
+        } else if (kind == 1) {
+            SWG_TRY(encounter_launch(c, mode, n1, r1, v1, renc1, n1, r1, v1, renc1, 1, 0, dt, w.rawcap, i1, i2, lv,
+                                     d_count, w.sort.ptr));
+            if (n2 > 0)
+                SWG_TRY(encounter_launch(c, mode, n1, r1, v1, renc1, n2, r2, v2, renc2, 0, n1, dt, w.rawcap, i1, i2,
+                                         lv, d_count, w.sort.ptr));
+        } else {
+            SWG_TRY(encounter_launch(c, mode, n1, r1, v1, renc1, n2, r2, v2, nullptr, 0, 0, dt, w.rawcap, i1, i2, lv,
+                                     d_count, w.sort.ptr));
+        }
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(&h_count, d_count, sizeof(h_count), cudaMemcpyDeviceToHost, c->stream),
+                            "count"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
+        if ((int64_t)h_count <= w.rawcap) break;
+        // grow the raw buffers and redo the check
+        w.rawcap = (int64_t)h_count + h_count / 2 + 1024;
+        DevBuf fresh;
+        SWG_TRY(ensure(c, fresh, (size_t)w.rawcap * 3 * sizeof(int32_t)));
+        cudaFree(w.raw.ptr);
+        w.raw = fresh;
+    }
+    int32_t *i1 = (int32_t *)w.raw.ptr, *i2 = i1 + w.rawcap, *lv = i2 + w.rawcap;
+    *o1 = i1;
+    *o2 = i2;
+    *olv = lv;
+    if (h_count == 0) return SWG_OK;
+    const bool need_unique = (mode == SWG_ENC_SORTSWEEP);
+    (void)need_unique;
+    // sort by (index1, index2) and drop repeats (sweep duplicates); the sort scratch
+    // is separate from the sweep scratch only in size, the sweep is finished.
+    const size_t need = sort_pairs_scratch_bytes((int64_t)h_count);
+    if (mode == SWG_ENC_SORTSWEEP) {
+        if (w.sort.bytes < need) SWG_TRY(ensure(c, w.sort, need));
+    } else {
+        SWG_TRY(ensure(c, w.sort, need));
+    }
+    SWG_TRY(sort_pairs_unique(c, (int64_t)h_count, i1, i2, lv, w.sort.ptr, d_count + 1));
+    unsigned long long h_unique = 0;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(&h_unique, d_count + 1, sizeof(h_unique), cudaMemcpyDeviceToHost, c->stream),
+                        "count"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
+    *n_out = (int64_t)h_unique;
+    return SWG_OK;
+}
+
+}  // namespace swg

@@ -1,0 +1,500 @@
+// kick.cu -- pair-gravity kick kernels for sm_103a.
+//
+// Restates swiftest_kick_getacch_int_all_* (src/swiftest/swiftest_kick.f90:69-470).
+//
+// Layout: positions are the reference's (3,n) FP64 arrays.  Each thread owns one
+// receiving body and walks the partners in ascending index order through
+// shared-memory tiles, so every per-body sum has the same operands in the same
+// order as the reference's serial loop:
+//   * KICK_DIRECT  -- the triangular loop without GMTINY bodies
+//                     (swiftest_kick.f90:221-264): acc_i += Gm_j/(r^2 sqrt r^2) * dx
+//   * KICK_SPLIT   -- the symmetric loops (flat :69-162, triangular with GMTINY
+//                     bodies :183-219): ahi_i = sum_{j>i} Gm_j irij3 dx,
+//                     ahj_i = sum_{j<i} Gm_j irij3 dx, acc = (acc + ahi) + ahj.
+// The FP64 path is therefore bit-identical to the reference loop evaluated
+// serially with no FMA contraction (this file is compiled with -fmad=false).
+//
+// The mixed path (SWG_MIXED) splits each FP64 coordinate into a float hi/lo
+// pair, forms displacements as (xj_hi - xi_hi) + (xj_lo - xi_lo) in FP32, takes
+// r^-3 from rsqrtf refined by one Newton step, accumulates 64-partner FP32
+// partials into float-float (TwoSum) accumulators, and adds the total to the
+// FP64 acceleration.  Partner ranges are split over blocks to fill all SMs;
+// the last block of each body tile folds the partials in a fixed order, so
+// results are deterministic.
+#include <cuda_runtime.h>
+
+#include "swg_internal.cuh"
+
+namespace swg {
+
+constexpr int KT = 128;       // bodies per block and partners per shared tile (FP64)
+constexpr int MT = 64;        // partners per FP32 partial (mixed)
+constexpr int MBLOCK = 128;   // threads per block (mixed)
+
+// ------------------------------------------------------------------ FP64 exact
+template <bool RAD, int MODE>
+__global__ void __launch_bounds__(KT) k_kick_plpl_fp64(int npl, int nplm, const double *__restrict__ r,
+                                                      const double *__restrict__ Gm,
+                                                      const double *__restrict__ R, double *__restrict__ acc,
+                                                      int acc_is_zero) {
+    __shared__ double sx[KT], sy[KT], sz[KT], sg[KT], sr[KT];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < npl;
+    double xi = 0, yi = 0, zi = 0, Ri = 0;
+    if (active) {
+        xi = r[3 * i + 0];
+        yi = r[3 * i + 1];
+        zi = r[3 * i + 2];
+        if (RAD) Ri = R[i];
+    }
+    double ax = 0, ay = 0, az = 0;  // DIRECT: running acc ; SPLIT: ahi
+    double bx = 0, by = 0, bz = 0;  // SPLIT: ahj
+    if (MODE == KICK_DIRECT && active && !acc_is_zero) {
+        ax = acc[3 * i + 0];
+        ay = acc[3 * i + 1];
+        az = acc[3 * i + 2];
+    }
+    // partner range: DIRECT i<nplm: all j != i; i>=nplm: j<nplm.
+    // SPLIT: j>i (ahi, only when i<nplm) and j<min(i,nplm) (ahj).
+    const int jend = (i < nplm) ? npl : nplm;
+    // the block walks tiles up to the largest jend of its threads
+    const int blk_jend = (blockIdx.x * blockDim.x < (unsigned)nplm) ? npl : nplm;
+    for (int j0 = 0; j0 < blk_jend; j0 += KT) {
+        const int jl = j0 + threadIdx.x;
+        if (jl < npl) {
+            sx[threadIdx.x] = r[3 * jl + 0];
+            sy[threadIdx.x] = r[3 * jl + 1];
+            sz[threadIdx.x] = r[3 * jl + 2];
+            sg[threadIdx.x] = Gm[jl];
+            if (RAD) sr[threadIdx.x] = R[jl];
+        }
+        __syncthreads();
+        if (active) {
+            const int nt = min(KT, jend - j0);
+            for (int jj = 0; jj < nt; jj++) {
+                const int j = j0 + jj;
+                if (j == i) continue;
+                const double rx = sx[jj] - xi;
+                const double ry = sy[jj] - yi;
+                const double rz = sz[jj] - zi;
+                const double rji2 = rx * rx + ry * ry + rz * rz;
+                if (RAD) {
+                    const double rs = Ri + sr[jj];
+                    if (!(rji2 > rs * rs)) continue;
+                }
+                if (MODE == KICK_DIRECT) {
+                    const double fac = sg[jj] / (rji2 * sqrt(rji2));
+                    ax = ax + fac * rx;
+                    ay = ay + fac * ry;
+                    az = az + fac * rz;
+                } else {
+                    const double irij3 = 1.0 / (rji2 * sqrt(rji2));
+                    const double fac = sg[jj] * irij3;
+                    if (j > i) {
+                        ax = ax + fac * rx;
+                        ay = ay + fac * ry;
+                        az = az + fac * rz;
+                    } else {
+                        bx = bx + fac * rx;
+                        by = by + fac * ry;
+                        bz = bz + fac * rz;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    if (MODE == KICK_DIRECT) {
+        acc[3 * i + 0] = ax;
+        acc[3 * i + 1] = ay;
+        acc[3 * i + 2] = az;
+    } else {
+        double a0 = acc_is_zero ? 0.0 : acc[3 * i + 0];
+        double a1 = acc_is_zero ? 0.0 : acc[3 * i + 1];
+        double a2 = acc_is_zero ? 0.0 : acc[3 * i + 2];
+        acc[3 * i + 0] = a0 + ax + bx;
+        acc[3 * i + 1] = a1 + ay + by;
+        acc[3 * i + 2] = a2 + az + bz;
+    }
+}
+
+// pl -> tp, swiftest_kick_getacch_int_all_tp (:374-415): acc -= Gm_j/(r^2 sqrt r^2) (r_tp - r_j)
+__global__ void __launch_bounds__(KT) k_kick_tp_fp64(int ntp, int npl, const double *__restrict__ rtp,
+                                                    const double *__restrict__ rpl, const double *__restrict__ Gm,
+                                                    const int32_t *__restrict__ lmask, double *__restrict__ acc,
+                                                    int acc_is_zero) {
+    __shared__ double sx[KT], sy[KT], sz[KT], sg[KT];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < ntp && lmask[i] != 0;
+    double xi = 0, yi = 0, zi = 0, ax = 0, ay = 0, az = 0;
+    if (active) {
+        xi = rtp[3 * i + 0];
+        yi = rtp[3 * i + 1];
+        zi = rtp[3 * i + 2];
+        if (!acc_is_zero) {
+            ax = acc[3 * i + 0];
+            ay = acc[3 * i + 1];
+            az = acc[3 * i + 2];
+        }
+    }
+    for (int j0 = 0; j0 < npl; j0 += KT) {
+        const int jl = j0 + threadIdx.x;
+        if (jl < npl) {
+            sx[threadIdx.x] = rpl[3 * jl + 0];
+            sy[threadIdx.x] = rpl[3 * jl + 1];
+            sz[threadIdx.x] = rpl[3 * jl + 2];
+            sg[threadIdx.x] = Gm[jl];
+        }
+        __syncthreads();
+        if (active) {
+            const int nt = min(KT, npl - j0);
+            for (int jj = 0; jj < nt; jj++) {
+                const double rx = xi - sx[jj];
+                const double ry = yi - sy[jj];
+                const double rz = zi - sz[jj];
+                const double rji2 = rx * rx + ry * ry + rz * rz;
+                const double fac = sg[jj] / (rji2 * sqrt(rji2));
+                ax = ax - fac * rx;
+                ay = ay - fac * ry;
+                az = az - fac * rz;
+            }
+        }
+        __syncthreads();
+    }
+    if (active) {
+        acc[3 * i + 0] = ax;
+        acc[3 * i + 1] = ay;
+        acc[3 * i + 2] = az;
+    } else if (i < ntp && acc_is_zero) {
+        acc[3 * i + 0] = 0.0;
+        acc[3 * i + 1] = 0.0;
+        acc[3 * i + 2] = 0.0;
+    }
+}
+
+// ------------------------------------------------------------------ mixed
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF &a, float p) {
+    // TwoSum (Knuth): exact error of hi + p, folded into lo.
+    const float s = a.hi + p;
+    const float bp = s - a.hi;
+    const float err = (a.hi - (s - bp)) + (p - bp);
+    a.hi = s;
+    a.lo = a.lo + err;
+}
+
+__device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
+
+// Receivers i in [blockIdx.x*MBLOCK, ...), partners j in chunk blockIdx.y of
+// length chunk.  TP: receivers are test particles (partners all pl, sign -),
+// else pl-pl with the (i<nplm || j<nplm) interaction rule and optional radius guard.
+template <bool TP, bool RAD>
+__global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int nplm, const double *__restrict__ rrecv,
+                                                      const double *__restrict__ rpart,
+                                                      const double *__restrict__ Gm, const double *__restrict__ R,
+                                                      const int32_t *__restrict__ lmask, double *__restrict__ acc,
+                                                      int acc_is_zero, int chunk, float *__restrict__ partial,
+                                                      unsigned *__restrict__ counters) {
+    __shared__ float4 sA[MT];  // x_hi, y_hi, z_hi, Gm
+    __shared__ float4 sB[MT];  // x_lo, y_lo, z_lo, R
+    __shared__ bool s_last;
+    const int i = blockIdx.x * MBLOCK + threadIdx.x;
+    const bool inrange = i < nrecv;
+    const bool active = inrange && (!TP || lmask[i] != 0);
+    float xh = 0, yh = 0, zh = 0, xl = 0, yl = 0, zl = 0, Ri = 0;
+    if (inrange) {
+        split_hi_lo(rrecv[3 * i + 0], xh, xl);
+        split_hi_lo(rrecv[3 * i + 1], yh, yl);
+        split_hi_lo(rrecv[3 * i + 2], zh, zl);
+        if (RAD) Ri = __double2float_rn(R[i]);
+    }
+    FF ax = {0.f, 0.f}, ay = {0.f, 0.f}, az = {0.f, 0.f};
+    const int jbeg = blockIdx.y * chunk;
+    const int jstop = min(npart, jbeg + chunk);
+    for (int j0 = jbeg; j0 < jstop; j0 += MT) {
+        for (int t = threadIdx.x; t < MT; t += MBLOCK) {
+            const int jl = j0 + t;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (jl < jstop) {
+                split_hi_lo(rpart[3 * jl + 0], a.x, b.x);
+                split_hi_lo(rpart[3 * jl + 1], a.y, b.y);
+                split_hi_lo(rpart[3 * jl + 2], a.z, b.z);
+                a.w = __double2float_rn(Gm[jl]);
+                b.w = RAD ? __double2float_rn(R[jl]) : 0.f;
+            }
+            sA[t] = a;
+            sB[t] = b;
+        }
+        __syncthreads();
+        const int nt = min(MT, jstop - j0);
+        float px = 0.f, py = 0.f, pz = 0.f;
+#pragma unroll 4
+        for (int jj = 0; jj < nt; jj++) {
+            const float4 a = sA[jj];
+            const float4 b = sB[jj];
+            const float dx = (a.x - xh) + (b.x - xl);
+            const float dy = (a.y - yh) + (b.y - yl);
+            const float dz = (a.z - zh) + (b.z - zl);
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            float y = rsqrtf(r2);
+            y = y * fmaf(-0.5f * r2, y * y, 1.5f);
+            float fac = a.w * (y * y * y);
+            bool ok;
+            if (TP) {
+                ok = true;
+            } else {
+                const int j = j0 + jj;
+                ok = (j != i) && (i < nplm || j < nplm);
+                if (RAD) {
+                    const float rs = Ri + b.w;
+                    ok = ok && (r2 > rs * rs);
+                }
+            }
+            fac = ok ? fac : 0.f;
+            px = fmaf(fac, dx, px);
+            py = fmaf(fac, dy, py);
+            pz = fmaf(fac, dz, pz);
+        }
+        ff_add(ax, px);
+        ff_add(ay, py);
+        ff_add(az, pz);
+        __syncthreads();
+    }
+    const int nchunk = gridDim.y;
+    if (nchunk == 1) {
+        if (active) {
+            // pl-pl: acc_i += sum Gm_j (r_j - r_i)/r^3 ; tp: acc_tp -= sum Gm_j (r_tp - r_j)/r^3,
+            // i.e. the same partner-minus-self sum added to acc.
+            double *a = &acc[3 * i];
+            const double sx = (double)ax.hi + (double)ax.lo, sy = (double)ay.hi + (double)ay.lo,
+                         sz = (double)az.hi + (double)az.lo;
+            a[0] = (acc_is_zero ? 0.0 : a[0]) + sx;
+            a[1] = (acc_is_zero ? 0.0 : a[1]) + sy;
+            a[2] = (acc_is_zero ? 0.0 : a[2]) + sz;
+        } else if (inrange && acc_is_zero) {
+            acc[3 * i + 0] = acc[3 * i + 1] = acc[3 * i + 2] = 0.0;
+        }
+        return;
+    }
+    // Multi-chunk: publish partials, last block of this receiver tile folds them.
+    if (inrange) {
+        float *p = &partial[((size_t)blockIdx.y * nrecv + i) * 6];
+        p[0] = ax.hi;
+        p[1] = ax.lo;
+        p[2] = ay.hi;
+        p[3] = ay.lo;
+        p[4] = az.hi;
+        p[5] = az.lo;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(&counters[blockIdx.x], 1u);
+        s_last = (prev == (unsigned)nchunk - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (active) {
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int cidx = 0; cidx < nchunk; cidx++) {
+            const volatile float *p = &partial[((size_t)cidx * nrecv + i) * 6];
+            sx += (double)p[0] + (double)p[1];
+            sy += (double)p[2] + (double)p[3];
+            sz += (double)p[4] + (double)p[5];
+        }
+        double *a = &acc[3 * i];
+        a[0] = (acc_is_zero ? 0.0 : a[0]) + sx;
+        a[1] = (acc_is_zero ? 0.0 : a[1]) + sy;
+        a[2] = (acc_is_zero ? 0.0 : a[2]) + sz;
+    } else if (inrange && acc_is_zero) {
+        acc[3 * i + 0] = acc[3 * i + 1] = acc[3 * i + 2] = 0.0;
+    }
+    if (threadIdx.x == 0) counters[blockIdx.x] = 0u;  // re-arm for the next launch
+}
+
+// ------------------------------------------------------------------ pair lists
+// Serial pass over an explicit pair list, restating the flat loop
+// (swiftest_kick.f90:69-115) in list order: ahi/ahj accumulate per body.
+template <bool RAD>
+__global__ void k_kick_pairs_serial(int64_t npairs, const int32_t *__restrict__ k, const int32_t *__restrict__ i1,
+                                    const int32_t *__restrict__ i2, const double *__restrict__ r,
+                                    const double *__restrict__ Gm, const double *__restrict__ R, double *ahi,
+                                    double *ahj) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int64_t q = 0; q < npairs; q++) {
+        const int i = (k ? k[2 * q] : i1[q]) - 1;
+        const int j = (k ? k[2 * q + 1] : i2[q]) - 1;
+        const double rx = r[3 * j + 0] - r[3 * i + 0];
+        const double ry = r[3 * j + 1] - r[3 * i + 1];
+        const double rz = r[3 * j + 2] - r[3 * i + 2];
+        const double rji2 = rx * rx + ry * ry + rz * rz;
+        if (RAD) {
+            const double rs = R[i] + R[j];
+            if (!(rji2 > rs * rs)) continue;
+        }
+        const double irij3 = 1.0 / (rji2 * sqrt(rji2));
+        const double faci = Gm[i] * irij3;
+        const double facj = Gm[j] * irij3;
+        ahi[3 * i + 0] = ahi[3 * i + 0] + facj * rx;
+        ahi[3 * i + 1] = ahi[3 * i + 1] + facj * ry;
+        ahi[3 * i + 2] = ahi[3 * i + 2] + facj * rz;
+        ahj[3 * j + 0] = ahj[3 * j + 0] - faci * rx;
+        ahj[3 * j + 1] = ahj[3 * j + 1] - faci * ry;
+        ahj[3 * j + 2] = ahj[3 * j + 2] - faci * rz;
+    }
+}
+
+// Parallel variant for long lists: atomic accumulation (order not fixed).
+template <bool RAD>
+__global__ void k_kick_pairs_atomic(int64_t npairs, const int32_t *__restrict__ k, const int32_t *__restrict__ i1,
+                                    const int32_t *__restrict__ i2, const double *__restrict__ r,
+                                    const double *__restrict__ Gm, const double *__restrict__ R, double *ahi,
+                                    double *ahj) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < npairs; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (k ? k[2 * q] : i1[q]) - 1;
+        const int j = (k ? k[2 * q + 1] : i2[q]) - 1;
+        const double rx = r[3 * j + 0] - r[3 * i + 0];
+        const double ry = r[3 * j + 1] - r[3 * i + 1];
+        const double rz = r[3 * j + 2] - r[3 * i + 2];
+        const double rji2 = rx * rx + ry * ry + rz * rz;
+        if (RAD) {
+            const double rs = R[i] + R[j];
+            if (!(rji2 > rs * rs)) continue;
+        }
+        const double irij3 = 1.0 / (rji2 * sqrt(rji2));
+        const double faci = Gm[i] * irij3;
+        const double facj = Gm[j] * irij3;
+        atomicAdd(&ahi[3 * i + 0], facj * rx);
+        atomicAdd(&ahi[3 * i + 1], facj * ry);
+        atomicAdd(&ahi[3 * i + 2], facj * rz);
+        atomicAdd(&ahj[3 * j + 0], -(faci * rx));
+        atomicAdd(&ahj[3 * j + 1], -(faci * ry));
+        atomicAdd(&ahj[3 * j + 2], -(faci * rz));
+    }
+}
+
+// sign > 0: acc = (acc + ahi) + ahj     (flat kernel semantics)
+// sign < 0: acc = acc - ((0 + ahi) + ahj) (symba_kick_getacch_pl, symba_kick.f90:61-70)
+__global__ void k_apply_pairs(int npl, const double *__restrict__ ahi, const double *__restrict__ ahj, double *acc,
+                              double sign) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * npl) return;
+    if (sign > 0)
+        acc[t] = acc[t] + ahi[t] + ahj[t];
+    else
+        acc[t] = acc[t] - (ahi[t] + ahj[t]);
+}
+
+// ------------------------------------------------------------------ launchers
+static inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+size_t kick_mixed_scratch_bytes(int nrecv, int nchunk) {
+    return KICK_COUNTERS * sizeof(unsigned) + (size_t)nchunk * nrecv * 6 * sizeof(float) + 256;
+}
+
+int ensure_kick_scratch(swg_ctx *c, DevBuf &buf, size_t bytes) {
+    if (buf.ptr && buf.bytes >= bytes) return SWG_OK;
+    void *old = buf.ptr;
+    buf.ptr = nullptr;
+    buf.bytes = 0;
+    if (old) cudaFree(old);
+    SWG_TRY(ensure(c, buf, bytes));
+    return cuda_status(c, cudaMemsetAsync(buf.ptr, 0, KICK_COUNTERS * sizeof(unsigned), c->stream), "memset");
+}
+
+// Chooses the partner split so that the grid covers ~2 blocks per SM.
+int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart) {
+    const int bx = div_up(nrecv, MBLOCK);
+    const int target = 2 * (c->num_sms > 0 ? c->num_sms : 152);
+    int nchunk = div_up(target, bx);
+    const int maxchunk = div_up(npart, MT);  // at least one tile per chunk
+    if (nchunk > maxchunk) nchunk = maxchunk;
+    if (nchunk < 1) nchunk = 1;
+    return nchunk;
+}
+
+int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const double *rrecv, const double *rpart,
+                      const double *Gm, const double *R, const int32_t *lmask, double *acc, int acc_is_zero,
+                      int nchunk, void *scratch) {
+    if (nrecv <= 0) return SWG_OK;
+    const int bx = div_up(nrecv, MBLOCK);
+    int chunk = div_up(npart, nchunk);
+    chunk = div_up(chunk, MT) * MT;
+    nchunk = npart > 0 ? div_up(npart, chunk) : 1;
+    if (bx > (int)KICK_COUNTERS) return SWG_ERR_ARG;
+    unsigned *counters = (unsigned *)scratch;
+    float *partial = (float *)((char *)scratch + KICK_COUNTERS * sizeof(unsigned));
+    dim3 grid(bx, nchunk);
+    if (tp)
+        k_kick_mixed<true, false><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, 0, rrecv, rpart, Gm, nullptr, lmask,
+                                                                  acc, acc_is_zero, chunk, partial, counters);
+    else if (R)
+        k_kick_mixed<false, true><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, nplm, rrecv, rpart, Gm, R, nullptr,
+                                                                  acc, acc_is_zero, chunk, partial, counters);
+    else
+        k_kick_mixed<false, false><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, nplm, rrecv, rpart, Gm, nullptr,
+                                                                   nullptr, acc, acc_is_zero, chunk, partial,
+                                                                   counters);
+    c->launches++;
+    return launch_status(c, "kick_mixed");
+}
+
+int kick_plpl_fp64(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const double *Gm, const double *R,
+                   double *acc, int mode, int acc_is_zero) {
+    if (npl <= 0) return SWG_OK;
+    const int grid = div_up(npl, KT);
+    if (mode == KICK_DIRECT) {
+        if (R)
+            k_kick_plpl_fp64<true, KICK_DIRECT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
+        else
+            k_kick_plpl_fp64<false, KICK_DIRECT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
+    } else {
+        if (R)
+            k_kick_plpl_fp64<true, KICK_SPLIT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
+        else
+            k_kick_plpl_fp64<false, KICK_SPLIT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
+    }
+    c->launches++;
+    return launch_status(c, "kick_plpl_fp64");
+}
+
+int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const double *rpl, const double *Gm,
+                 const int32_t *lmask, double *acc, int acc_is_zero) {
+    if (ntp <= 0) return SWG_OK;
+    k_kick_tp_fp64<<<div_up(ntp, KT), KT, 0, c->stream>>>(ntp, npl, rtp, rpl, Gm, lmask, acc, acc_is_zero);
+    c->launches++;
+    return launch_status(c, "kick_tp_fp64");
+}
+
+int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,
+               const double *r, const double *Gm, const double *R, double *acc, double sign, double *ahi_ahj) {
+    if (npairs <= 0 || npl <= 0) return SWG_OK;
+    double *ahi = ahi_ahj, *ahj = ahi_ahj + 3 * (size_t)npl;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(ahi_ahj, 0, sizeof(double) * 6 * (size_t)npl, c->stream), "memset"));
+    if (npairs <= 65536) {
+        if (R)
+            k_kick_pairs_serial<true><<<1, 32, 0, c->stream>>>(npairs, k, i1, i2, r, Gm, R, ahi, ahj);
+        else
+            k_kick_pairs_serial<false><<<1, 32, 0, c->stream>>>(npairs, k, i1, i2, r, Gm, R, ahi, ahj);
+    } else {
+        const int grid = (int)std::min<int64_t>((npairs + 255) / 256, 4 * 152);
+        if (R)
+            k_kick_pairs_atomic<true><<<grid, 256, 0, c->stream>>>(npairs, k, i1, i2, r, Gm, R, ahi, ahj);
+        else
+            k_kick_pairs_atomic<false><<<grid, 256, 0, c->stream>>>(npairs, k, i1, i2, r, Gm, R, ahi, ahj);
+    }
+    c->launches++;
+    SWG_TRY(launch_status(c, "kick_pairs"));
+    k_apply_pairs<<<div_up(3 * (int64_t)npl, 256), 256, 0, c->stream>>>(npl, ahi, ahj, acc, sign);
+    c->launches++;
+    return launch_status(c, "apply_pairs");
+}
+
+}  // namespace swg

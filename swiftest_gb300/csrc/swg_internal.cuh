@@ -1,0 +1,128 @@
+// swg_internal.cuh -- shared declarations of the swiftest_gb300 CUDA library.
+//
+// All translation units are compiled with -fmad=false so that FP64 expressions
+// keep the reference's rounding (no contraction into fused multiply-adds);
+// kernels that want FMA (the mixed-precision kick) call fmaf() explicitly.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/swiftest_gb300.h"
+
+namespace swg {
+
+// Reference status codes, src/globals/globals_module.f90:86-101.
+constexpr int ST_ACTIVE = 0;
+constexpr int ST_INACTIVE = 1;
+constexpr int ST_DISCARDED_DRIFTERR = -7;
+
+// Reference constants, src/globals/globals_module.f90:33-38.
+constexpr double TWOPI = 6.283185307179586476925286766559005768394;
+constexpr double PIBY2 = 1.570796326794896619231321691639751442099;
+constexpr double PI3BY2 = 4.712388980384689857693965074919254326296;
+constexpr double THIRD = 0.333333333333333333333333333333333333333;
+constexpr double SIXTH = 0.166666666666666666666666666666666666667;
+constexpr double VSMALL = 1.4916681462400413e-154;  // sqrt(tiny(1.0_DP))
+constexpr double RSWEEP_FACTOR = 1.1;                // encounter_module.f90:21
+constexpr double RSHELL = 0.48075;                   // symba_module.f90:23
+constexpr int NTENC = 3;                             // symba_module.f90:21
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// Encounter workspace: raw pair buffers, sort scratch and counters, grown on demand.
+struct EncWork {
+    DevBuf raw;      // i1, i2, lv raw (3 * rawcap int32)
+    int64_t rawcap = 0;
+    DevBuf sort;     // sort / sweep scratch
+    DevBuf counters; // 2 x unsigned long long
+};
+
+}  // namespace swg
+
+struct swg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    int num_sms = 0;
+    // scratch arena slots used by the flat C entry points (host-memory staging
+    // and kernel scratch); each slot is grow-only.
+    swg::DevBuf slot[24];
+    swg::EncWork enc;
+};
+
+namespace swg {
+
+// Ensure buf holds at least `bytes` (grow-only); returns SWG_OK or SWG_ERR_NOMEM.
+int ensure(swg_ctx *c, DevBuf &buf, size_t bytes);
+// Records a CUDA error into the context; returns SWG_ERR_CUDA if e != success.
+int cuda_status(swg_ctx *c, cudaError_t e, const char *what);
+// Checks the last launch error.
+int launch_status(swg_ctx *c, const char *what);
+int ensure_slot(swg_ctx *c, int slot, size_t bytes, void **out);
+// Mixed-kick scratch: a fixed block of zeroed "last block" counters followed by
+// the partial sums; (re)allocation zeroes the counters.
+constexpr size_t KICK_COUNTERS = 65536;
+int ensure_kick_scratch(swg_ctx *c, DevBuf &buf, size_t bytes);
+
+// ---------------------------------------------------------------- kernels API
+// All pointers are device pointers; work is ordered on c->stream.
+
+// kick.cu -- pair kick
+enum KickMode { KICK_DIRECT = 0, KICK_SPLIT = 1 };
+int kick_plpl_fp64(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const double *Gm, const double *R,
+                   double *acc, int mode, int acc_is_zero);
+int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const double *rpl, const double *Gm,
+                 const int32_t *lmask, double *acc, int acc_is_zero);
+size_t kick_mixed_scratch_bytes(int nrecv, int nchunk);
+int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart);
+int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const double *rrecv, const double *rpart,
+                      const double *Gm, const double *R, const int32_t *lmask, double *acc, int acc_is_zero,
+                      int nchunk, void *scratch);
+// explicit 1-based pair list (k_plpl(2,n) or separate i1/i2); ahi_ahj: 6*npl doubles of scratch
+// sign > 0: acc = (acc + ahi) + ahj ; sign < 0: acc = acc - (ahi + ahj)
+int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,
+               const double *r, const double *Gm, const double *R, double *acc, double sign, double *ahi_ahj);
+
+// drift.cu -- Danby drift
+int drift_all(swg_ctx *c, const double *mu, double mu_scalar, double *x, double *v, int32_t n, int32_t lgr,
+              double inv_c2, double dt, const int32_t *lmask, int32_t *iflag);
+int drift_masked(swg_ctx *c, double mu, double *x, double *v, int32_t n, const int32_t *levelg, int irec, double dt,
+                 int32_t *status, int32_t *nfail);
+
+// encounter.cu -- encounter checks and sorting
+int64_t sort_padded_len(int64_t n);
+size_t sort_pairs_scratch_bytes(int64_t n);
+int sort_pairs_unique(swg_ctx *c, int64_t n, int32_t *i1, int32_t *i2, int32_t *lv, void *scratch,
+                      unsigned long long *d_nout);
+size_t sas_scratch_bytes(int ntot);
+int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const double *v1, const double *renc1, int n2,
+                     const double *r2, const double *v2, const double *renc2, int upper, int shift2, double dt,
+                     long long cap, int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
+                     void *sas_scratch);
+
+// Full check of one kind (0 plpl, 1 plplm, 2 pltp): sorted unique pairs in the
+// workspace's raw buffers; *n_out gets the count (host).  Synchronizes.
+int encounter_check_kind(swg_ctx *c, EncWork &w, int kind, int mode, int32_t n1, const double *r1,
+                         const double *v1, const double *renc1, int32_t n2, const double *r2, const double *v2,
+                         const double *renc2, double dt, int64_t *n_out, int32_t **i1, int32_t **i2, int32_t **lv);
+
+// Scalar-broadcast helpers
+__host__ __device__ inline int64_t nplplm_count(int64_t npl, int64_t nplm) {
+    return nplm * npl - nplm * (nplm + 1) / 2;
+}
+
+}  // namespace swg
+
+#define SWG_TRY(expr)                 \
+    do {                              \
+        int _rc = (expr);             \
+        if (_rc != SWG_OK) return _rc; \
+    } while (0)

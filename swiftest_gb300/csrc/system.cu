@@ -1,0 +1,1462 @@
+// system.cu -- device-resident n-body system and the WHM / HELIO / SyMBA step loops.
+//
+// Host C++ here plays the role of the reference's type-bound procedures
+// (whm_step.f90, helio_step.f90, symba_step.f90): it orders kernels on the
+// context's stream and keeps every array in HBM between steps.  The host only
+// waits where the reference makes a data-dependent decision: after the level-0
+// encounter check (interp vs plain HELIO step) and, inside the SyMBA
+// recursion, on the "any deeper encounter" flag of each sub-step.
+//
+// O(N) serial sums of the reference (the Sun's barycentric momentum in
+// helio_drift_linear_pl, vh2vb / vb2vh, WHM Jacobi prefix sums) run in one
+// thread in the reference's index order when the kick precision is FP64, so the
+// FP64 path reproduces the serial reference loop bit for bit; in the mixed path
+// they use a fixed-order block reduction.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "swg_internal.cuh"
+
+using namespace swg;
+
+// device-side central-body record (doubles)
+enum { CB_VB = 0, CB_RB = 3, CB_PTBEG = 6, CB_PTEND = 9, CB_N = 12 };
+
+struct swg_system {
+    swg_ctx *c = nullptr;
+    int integrator = SWG_HELIO;
+    int32_t npl = 0, ntp = 0, nplm = 0;
+    double GMcb = 0, Rcb = 0;
+    double dt = 0, rhscale = 6.5, gmtiny = 0;
+    int loop_mode = 0, enc_plpl = 0, enc_pltp = 0, lclose = 0, precision = SWG_FP64;
+    int lfirst_pl = 1, lfirst_tp = 1, lfirstkick = 1, irec = -1, initialized = 0;
+    double t = 0;
+    // massive bodies
+    double *rh = nullptr, *vh = nullptr, *vb = nullptr, *ah = nullptr, *rbeg = nullptr, *rend = nullptr;
+    double *Gmass = nullptr, *radius = nullptr, *rhill = nullptr;
+    double *xj = nullptr, *vj = nullptr, *eta = nullptr, *muj = nullptr, *ir3h = nullptr, *ir3j = nullptr;
+    int32_t *status = nullptr, *lmask = nullptr, *levelg = nullptr, *levelm = nullptr, *nplenc = nullptr,
+            *ntpenc = nullptr, *iflag = nullptr;
+    // test particles
+    double *trh = nullptr, *tvh = nullptr, *tvb = nullptr, *tah = nullptr;
+    int32_t *tstatus = nullptr, *tlmask = nullptr, *tlevelg = nullptr, *tlevelm = nullptr, *tnplenc = nullptr,
+            *tiflag = nullptr;
+    double *dcb = nullptr;  // CB_N doubles
+    // encounter lists (SyMBA): i1, i2, lvdotr, status, level
+    int32_t *plpl_l = nullptr, *pltp_l = nullptr;  // 5 * cap int32 each
+    int64_t plpl_n = 0, pltp_n = 0, plpl_cap = 0, pltp_cap = 0;
+    EncWork enc;
+    // scratch
+    DevBuf kick_scratch, pair_scratch, flags, red;
+    int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail
+    int64_t stats[5] = {0, 0, 0, 0, 0};
+};
+
+namespace {
+
+inline int grid_for(int64_t n, int bs) { return (int)std::max<int64_t>(1, (n + bs - 1) / bs); }
+
+template <typename T>
+int dalloc(swg_ctx *c, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        c->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return SWG_ERR_NOMEM;
+    }
+    cudaMemsetAsync(*p, 0, n * sizeof(T), c->stream);
+    return SWG_OK;
+}
+
+// ---------------------------------------------------------------- small kernels
+// helio_drift_linear_pl (helio_drift.f90:129-163): pt = sum(Gm*vb, mask)/GMcb ; rh += pt*dt
+__global__ void k_lindrift_pl(int npl, const double *__restrict__ Gm, const double *__restrict__ vb,
+                              const int32_t *__restrict__ lmask, double GMcb, double *rh, double dt, double *dcb,
+                              int slot, int exact) {
+    __shared__ double s_pt[3];
+    __shared__ double s_red[3][256];
+    if (exact) {
+        if (threadIdx.x == 0) {
+            double px = 0.0, py = 0.0, pz = 0.0;
+            for (int i = 0; i < npl; i++) {
+                if (!lmask[i]) continue;
+                px = px + Gm[i] * vb[3 * i + 0];
+                py = py + Gm[i] * vb[3 * i + 1];
+                pz = pz + Gm[i] * vb[3 * i + 2];
+            }
+            s_pt[0] = px / GMcb;
+            s_pt[1] = py / GMcb;
+            s_pt[2] = pz / GMcb;
+        }
+    } else {
+        double px = 0.0, py = 0.0, pz = 0.0;
+        for (int i = threadIdx.x; i < npl; i += blockDim.x) {
+            if (!lmask[i]) continue;
+            px += Gm[i] * vb[3 * i + 0];
+            py += Gm[i] * vb[3 * i + 1];
+            pz += Gm[i] * vb[3 * i + 2];
+        }
+        s_red[0][threadIdx.x] = px;
+        s_red[1][threadIdx.x] = py;
+        s_red[2][threadIdx.x] = pz;
+        __syncthreads();
+        for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+            if (threadIdx.x < (unsigned)off)
+                for (int d = 0; d < 3; d++) s_red[d][threadIdx.x] += s_red[d][threadIdx.x + off];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0)
+            for (int d = 0; d < 3; d++) s_pt[d] = s_red[d][0] / GMcb;
+    }
+    __syncthreads();
+    const double ptx = s_pt[0], pty = s_pt[1], ptz = s_pt[2];
+    for (int i = threadIdx.x; i < npl; i += blockDim.x) {
+        if (!lmask[i]) continue;
+        rh[3 * i + 0] = rh[3 * i + 0] + ptx * dt;
+        rh[3 * i + 1] = rh[3 * i + 1] + pty * dt;
+        rh[3 * i + 2] = rh[3 * i + 2] + ptz * dt;
+    }
+    if (threadIdx.x == 0) {
+        dcb[slot + 0] = ptx;
+        dcb[slot + 1] = pty;
+        dcb[slot + 2] = ptz;
+    }
+}
+
+// swiftest_util_coord_vh2vb_pl (swiftest_util.f90:424-456)
+__global__ void k_vh2vb_pl(int npl, const double *__restrict__ Gm, const double *__restrict__ vh, double *vb,
+                           double GMcb, double *dcb) {
+    __shared__ double s_cb[3];
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int i = 0; i < npl; i++) sum = sum + Gm[i];
+        const double Gmtot = GMcb + sum;
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int i = 0; i < npl; i++) {
+            cx = cx - Gm[i] * vh[3 * i + 0];
+            cy = cy - Gm[i] * vh[3 * i + 1];
+            cz = cz - Gm[i] * vh[3 * i + 2];
+        }
+        s_cb[0] = cx / Gmtot;
+        s_cb[1] = cy / Gmtot;
+        s_cb[2] = cz / Gmtot;
+        dcb[CB_VB + 0] = s_cb[0];
+        dcb[CB_VB + 1] = s_cb[1];
+        dcb[CB_VB + 2] = s_cb[2];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npl; i += blockDim.x)
+        for (int d = 0; d < 3; d++) vb[3 * i + d] = vh[3 * i + d] + s_cb[d];
+}
+
+// swiftest_util_coord_vb2vh_pl (swiftest_util.f90:363-392), reverse-order sum
+__global__ void k_vb2vh_pl(int npl, const double *__restrict__ Gm, const double *__restrict__ vb,
+                           const int32_t *__restrict__ status, double *vh, double GMcb, double *dcb) {
+    __shared__ double s_cb[3];
+    if (threadIdx.x == 0) {
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int i = npl - 1; i >= 0; i--) {
+            if (status[i] == ST_INACTIVE) continue;
+            cx = cx - Gm[i] * vb[3 * i + 0] / GMcb;
+            cy = cy - Gm[i] * vb[3 * i + 1] / GMcb;
+            cz = cz - Gm[i] * vb[3 * i + 2] / GMcb;
+        }
+        s_cb[0] = cx;
+        s_cb[1] = cy;
+        s_cb[2] = cz;
+        dcb[CB_VB + 0] = cx;
+        dcb[CB_VB + 1] = cy;
+        dcb[CB_VB + 2] = cz;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npl; i += blockDim.x)
+        for (int d = 0; d < 3; d++) vh[3 * i + d] = vb[3 * i + d] - s_cb[d];
+}
+
+// test particles: mode 0 vh2vb(vbcb=-pt) ; 1 vb2vh(vbcb=-pt) ; 2 lindrift rh += pt*dt ;
+// 3 lindrift then vb2vh (end of step) ; 4 vh2vb then lindrift (start of step) ;
+// 5 heliocentric to barycentric velocity with the central body's vb (initialisation)
+__global__ void k_tp_misc(int ntp, const int32_t *__restrict__ tlmask, double *trh, double *tvh, double *tvb,
+                          const double *__restrict__ dcb, int slot, double dt, int mode) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntp || !tlmask[i]) return;
+    for (int d = 0; d < 3; d++) {
+        const double pt = dcb[slot + d];
+        const double vbcb = -pt;
+        if (mode == 0 || mode == 4) tvb[3 * i + d] = tvh[3 * i + d] + vbcb;
+        if (mode == 2 || mode == 3 || mode == 4) trh[3 * i + d] = trh[3 * i + d] + pt * dt;
+        if (mode == 1 || mode == 3) tvh[3 * i + d] = tvb[3 * i + d] - vbcb;
+        if (mode == 5) tvb[3 * i + d] = tvh[3 * i + d] + dcb[slot + d];
+    }
+}
+
+// v += a*dt (masked) ; optionally rcopy = r (set_beg_end)
+__global__ void k_kick_update(int n, double *v, const double *__restrict__ a, const int32_t *__restrict__ lmask,
+                              double dt, const double *__restrict__ r, double *rcopy) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (rcopy)
+        for (int d = 0; d < 3; d++) rcopy[3 * i + d] = r[3 * i + d];
+    if (!lmask[i]) return;
+    for (int d = 0; d < 3; d++) v[3 * i + d] = v[3 * i + d] + a[3 * i + d] * dt;
+}
+
+// symba_kick_getacch_tp add-back loop (symba_kick.f90:104-118), list order
+__global__ void k_pltp_addback(int64_t n, const int32_t *__restrict__ i1, const int32_t *__restrict__ i2,
+                               const int32_t *__restrict__ tlmask, const double *__restrict__ trh,
+                               const double *__restrict__ rp, const double *__restrict__ Gm, double *tah) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int64_t k = 0; k < n; k++) {
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        if (!tlmask[j]) continue;
+        const double dx = trh[3 * j + 0] - rp[3 * i + 0];
+        const double dy = trh[3 * j + 1] - rp[3 * i + 1];
+        const double dz = trh[3 * j + 2] - rp[3 * i + 2];
+        const double rjj = dx * dx + dy * dy + dz * dz;
+        const double fac = Gm[i] / (rjj * sqrt(rjj));
+        tah[3 * j + 0] = tah[3 * j + 0] + fac * dx;
+        tah[3 * j + 1] = tah[3 * j + 1] + fac * dy;
+        tah[3 * j + 2] = tah[3 * j + 2] + fac * dz;
+    }
+}
+
+// symba_step_reset_system (symba_step.f90:265-331) + set_renc(0)
+__global__ void k_symba_reset(int npl, int ntp, int32_t *levelg, int32_t *levelm, int32_t *nplenc, int32_t *ntpenc,
+                              int32_t *lmask, int32_t *tlevelg, int32_t *tlevelm, int32_t *tnplenc,
+                              int32_t *tlmask) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < npl) {
+        levelg[i] = -1;
+        levelm[i] = -1;
+        nplenc[i] = 0;
+        ntpenc[i] = 0;
+        lmask[i] = 1;
+    }
+    if (i < ntp) {
+        tlevelg[i] = -1;
+        tlevelm[i] = -1;
+        tnplenc[i] = 0;
+        tlmask[i] = 1;
+    }
+}
+
+// symba_util_set_renc (symba_util.f90:245-267)
+__device__ __forceinline__ double d_renc(double rhill, double rhscale, int scale) {
+    double rshell_irec = 1.0;
+    for (int k = 1; k <= scale; k++) rshell_irec = rshell_irec * RSHELL;
+    return rhill * rhscale * rshell_irec;
+}
+__global__ void k_set_renc(int npl, const double *rhill, double rhscale, int scale, double *renc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < npl) renc[i] = d_renc(rhill[i], rhscale, scale);
+}
+
+// level-0 bookkeeping of symba_encounter_check_pl / _tp (symba_encounter_check.f90:53-83, 267-290)
+__global__ void k_level0_mark(int64_t n, int32_t *l, int64_t cap, int tp, int32_t *levelg, int32_t *levelm,
+                              int32_t *cnt1, int32_t *tlevelg, int32_t *tlevelm, int32_t *cnt2) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int32_t *i1 = l, *i2 = l + cap, *st = l + 3 * cap, *lev = l + 4 * cap;
+    const int i = i1[k] - 1, j = i2[k] - 1;
+    st[k] = ST_ACTIVE;
+    lev[k] = 0;
+    levelg[i] = 0;
+    levelm[i] = 0;
+    if (!tp) {
+        levelg[j] = 0;
+        levelm[j] = 0;
+        atomicAdd(&cnt1[i], 1);
+        atomicAdd(&cnt1[j], 1);
+    } else {
+        tlevelg[j] = 0;
+        tlevelm[j] = 0;
+        atomicAdd(&cnt1[i], 1);
+        atomicAdd(&cnt2[j], 1);
+    }
+}
+
+// encounter_check_one (encounter_check.f90:573-621)
+__device__ __forceinline__ void d_enc_one(double xr, double yr, double zr, double vxr, double vyr, double vzr,
+                                          double renc, double dt, int &lenc, int &lvdotr) {
+    const double r2 = xr * xr + yr * yr + zr * zr;
+    const double r2crit = renc * renc;
+    double vdotr, r2min;
+    if (r2 > r2crit) {
+        vdotr = vxr * xr + vyr * yr + vzr * zr;
+        if (vdotr > 0.0) {
+            r2min = r2;
+        } else {
+            const double v2 = vxr * vxr + vyr * vyr + vzr * vzr;
+            if (v2 <= VSMALL) {
+                r2min = r2;
+            } else {
+                const double tmin = -vdotr / v2;
+                if (tmin < dt)
+                    r2min = r2 - vdotr * vdotr / v2;
+                else
+                    r2min = r2 + 2.0 * vdotr * dt + v2 * (dt * dt);
+            }
+        }
+    } else {
+        vdotr = -1.0;
+        r2min = r2;
+    }
+    lvdotr = (vdotr < 0.0);
+    lenc = lvdotr && (r2min <= r2crit);
+}
+
+// symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), one block.
+// flag[0] |= any encounter at level irec.
+__global__ void k_list_check(int64_t npp, int32_t *pp, int64_t ppcap, int64_t npt, int32_t *pt, int64_t ptcap,
+                             const double *__restrict__ rh, const double *__restrict__ vb,
+                             const double *__restrict__ trh, const double *__restrict__ tvb,
+                             const double *__restrict__ rhill, const double *__restrict__ radius, double rhscale,
+                             int irec, double dt, int32_t *levelg, int32_t *levelm, int32_t *tlevelg,
+                             int32_t *tlevelm, int32_t *flag, uint8_t *lenc_scratch) {
+    __shared__ int s_any;
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    // phase 1: tests (reads positions only)
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        const bool isp = k < npp;
+        const int64_t q = isp ? k : k - npp;
+        int32_t *l = isp ? pp : pt;
+        const int64_t cap = isp ? ppcap : ptcap;
+        int32_t *i1 = l, *i2 = l + cap, *lv = l + 2 * cap, *st = l + 3 * cap, *lev = l + 4 * cap;
+        uint8_t le_out = 0;
+        if (st[q] == ST_ACTIVE && lev[q] == irec - 1) {
+            const int i = i1[q] - 1, j = i2[q] - 1;
+            double xr[3], vr[3];
+            const double *rj = isp ? &rh[3 * j] : &trh[3 * j];
+            const double *vj = isp ? &vb[3 * j] : &tvb[3 * j];
+            for (int d = 0; d < 3; d++) {
+                xr[d] = rj[d] - rh[3 * i + d];
+                vr[d] = vj[d] - vb[3 * i + d];
+            }
+            const double renci = d_renc(rhill[i], rhscale, irec);
+            const double rcrit = isp ? renci + d_renc(rhill[j], rhscale, irec) : renci;
+            int le, lvd;
+            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            lv[q] = lvd;
+            if (le) {
+                const double rs = isp ? radius[i] + radius[j] : radius[i];
+                const double rlim2 = isp ? rs * rs : radius[i] * radius[i];
+                const double rji2 = xr[0] * xr[0] + xr[1] * xr[1] + xr[2] * xr[2];
+                le = rji2 > rlim2;
+            }
+            le_out = (uint8_t)le;
+        }
+        lenc_scratch[k] = le_out;
+    }
+    __syncthreads();
+    // phase 2: levels
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        if (!lenc_scratch[k]) continue;
+        s_any = 1;
+        const bool isp = k < npp;
+        const int64_t q = isp ? k : k - npp;
+        int32_t *l = isp ? pp : pt;
+        const int64_t cap = isp ? ppcap : ptcap;
+        const int i = l[q] - 1, j = l[cap + q] - 1;
+        levelg[i] = irec;
+        atomicMax(&levelm[i], irec);
+        if (isp) {
+            levelg[j] = irec;
+            atomicMax(&levelm[j], irec);
+        } else {
+            tlevelg[j] = irec;
+            atomicMax(&tlevelm[j], irec);
+        }
+        l[4 * cap + q] = irec;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) flag[0] = s_any;
+}
+
+// powi: square-and-multiply (gfortran's real**integer)
+__device__ __forceinline__ double d_powi(double x, int m) {
+    unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
+    double y = (n % 2) ? x : 1.0;
+    while (n >>= 1) {
+        x = x * x;
+        if (n % 2) y = y * x;
+    }
+    return m < 0 ? 1.0 / y : y;
+}
+
+// symba_kick_list_plpl (symba_kick.f90:126-232), serial in list order (one thread)
+__device__ void d_kick_list_plpl(int64_t nenc, int32_t *l, int64_t cap, int npl, const int32_t *status,
+                                 int32_t *lmask, const int32_t *levelg, const double *rh, double *vb, double *ah,
+                                 const double *Gm, const double *rhill, double rhscale, double dt, int irec, int sgn,
+                                 uint8_t *good) {
+    if (nenc == 0 || npl == 0) return;
+    for (int i = 0; i < npl; i++) lmask[i] = status[i] != ST_INACTIVE;
+    const int32_t *i1 = l, *i2 = l + cap, *st = l + 3 * cap;
+    const int irm1 = irec - 1;
+    const int irecl = sgn < 0 ? irec - 1 : irec;
+    int64_t ngood = 0;
+    for (int64_t k = 0; k < nenc; k++) {
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        good[k] = (st[k] == ST_ACTIVE) && (levelg[i] >= irm1) && (levelg[j] >= irm1);
+        ngood += good[k];
+    }
+    if (ngood == 0) return;
+    for (int64_t k = 0; k < nenc; k++) {
+        if (!good[k]) continue;
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * j + d] = 0.0;
+    }
+    const double rs2 = rhscale * rhscale;
+    const double rshell_pow = d_powi(RSHELL, 2 * irecl);
+    for (int64_t k = 0; k < nenc; k++) {
+        if (!good[k]) continue;
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        const double rhs = rhill[i] + rhill[j];
+        const double ri = ((rhs * rhs) * rs2) * rshell_pow;
+        const double rim1 = ri * (RSHELL * RSHELL);
+        double dx[3];
+        for (int d = 0; d < 3; d++) dx[d] = rh[3 * j + d] - rh[3 * i + d];
+        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        double fac;
+        if (r2 < rim1) {
+            good[k] = 0;
+            continue;
+        }
+        if (r2 < ri) {
+            const double ris = sqrt(ri);
+            const double r = sqrt(r2);
+            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
+            fac = pow(r2, -1.5) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+        } else {
+            const double ir3 = 1.0 / (r2 * sqrt(r2));
+            fac = ir3;
+        }
+        const double faci = fac * Gm[i];
+        const double facj = fac * Gm[j];
+        for (int d = 0; d < 3; d++) {
+            ah[3 * i + d] = ah[3 * i + d] + facj * dx[d];
+            ah[3 * j + d] = ah[3 * j + d] - faci * dx[d];
+        }
+    }
+    for (int64_t k = 0; k < nenc; k++) {
+        if (!good[k]) continue;
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        for (int d = 0; d < 3; d++) {
+            vb[3 * i + d] = vb[3 * i + d] + (double)sgn * dt * ah[3 * i + d];
+            vb[3 * j + d] = vb[3 * j + d] + (double)sgn * dt * ah[3 * j + d];
+        }
+        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * j + d] = 0.0;
+    }
+}
+
+// symba_kick_list_pltp (symba_kick.f90:235-340), serial in list order (one thread)
+__device__ void d_kick_list_pltp(int64_t nenc, int32_t *l, int64_t cap, int npl, int ntp, const int32_t *status,
+                                 int32_t *lmask, const int32_t *tstatus, int32_t *tlmask, const int32_t *levelg,
+                                 const int32_t *tlevelg, const double *rh, const double *trh, double *tvb,
+                                 double *tah, const double *Gm, const double *rhill, double rhscale, double dt,
+                                 int irec, int sgn, uint8_t *good) {
+    if (nenc == 0 || npl == 0 || ntp == 0) return;
+    for (int i = 0; i < npl; i++) lmask[i] = status[i] != ST_INACTIVE;
+    for (int i = 0; i < ntp; i++) tlmask[i] = tstatus[i] != ST_INACTIVE;
+    const int32_t *i1 = l, *i2 = l + cap, *st = l + 3 * cap;
+    const int irm1 = irec - 1;
+    const int irecl = sgn < 0 ? irec - 1 : irec;
+    int64_t ngood = 0;
+    for (int64_t k = 0; k < nenc; k++) {
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        good[k] = (st[k] == ST_ACTIVE) && (levelg[i] >= irm1) && (tlevelg[j] >= irm1);
+        ngood += good[k];
+    }
+    if (ngood == 0) return;
+    for (int64_t k = 0; k < nenc; k++) {
+        if (!good[k]) continue;
+        const int j = i2[k] - 1;
+        for (int d = 0; d < 3; d++) tah[3 * j + d] = 0.0;
+    }
+    const double rs2 = rhscale * rhscale;
+    const double rshell_pow = d_powi(RSHELL, 2 * irecl);
+    for (int64_t k = 0; k < nenc; k++) {
+        if (!good[k]) continue;
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        const double ri = ((rhill[i] * rhill[i]) * rs2) * rshell_pow;
+        const double rim1 = ri * (RSHELL * RSHELL);
+        double dx[3];
+        for (int d = 0; d < 3; d++) dx[d] = trh[3 * j + d] - rh[3 * i + d];
+        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        double fac;
+        if (r2 < rim1) {
+            good[k] = 0;
+            continue;
+        }
+        if (r2 < ri) {
+            const double ris = sqrt(ri);
+            const double r = sqrt(r2);
+            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
+            fac = pow(r2, -1.5) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+        } else {
+            const double ir3 = 1.0 / (r2 * sqrt(r2));
+            fac = ir3;
+        }
+        const double faci = fac * Gm[i];
+        for (int d = 0; d < 3; d++) tah[3 * j + d] = tah[3 * j + d] - faci * dx[d];
+    }
+    for (int64_t k = 0; k < nenc; k++) {
+        if (!good[k]) continue;
+        const int j = i2[k] - 1;
+        for (int d = 0; d < 3; d++) {
+            tvb[3 * j + d] = tvb[3 * j + d] + (double)sgn * dt * tah[3 * j + d];
+            tah[3 * j + d] = 0.0;
+        }
+    }
+}
+
+struct KickListArgs {
+    int64_t npp, ppcap, npt, ptcap;
+    int32_t *pp, *pt;
+    int npl, ntp;
+    const int32_t *status, *tstatus, *levelg, *tlevelg;
+    int32_t *lmask, *tlmask;
+    const double *rh, *trh, *Gm, *rhill;
+    double *vb, *ah, *tvb, *tah;
+    double rhscale, dt;
+    int irec, both;
+    uint8_t *good_pp, *good_pt;
+};
+
+// one kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237):
+// warp 0 does the pl-pl list, warp 1 the pl-tp list (disjoint data)
+__global__ void k_kick_lists(KickListArgs a) {
+    if (threadIdx.x == 0) {
+        d_kick_list_plpl(a.npp, a.pp, a.ppcap, a.npl, a.status, a.lmask, a.levelg, a.rh, a.vb, a.ah, a.Gm, a.rhill,
+                         a.rhscale, a.dt, a.irec, 1, a.good_pp);
+        if (a.both)
+            d_kick_list_plpl(a.npp, a.pp, a.ppcap, a.npl, a.status, a.lmask, a.levelg, a.rh, a.vb, a.ah, a.Gm,
+                             a.rhill, a.rhscale, a.dt, a.irec, -1, a.good_pp);
+    } else if (threadIdx.x == 32) {
+        d_kick_list_pltp(a.npt, a.pt, a.ptcap, a.npl, a.ntp, a.status, a.lmask, a.tstatus, a.tlmask, a.levelg,
+                         a.tlevelg, a.rh, a.trh, a.tvb, a.tah, a.Gm, a.rhill, a.rhscale, a.dt, a.irec, 1, a.good_pt);
+        if (a.both)
+            d_kick_list_pltp(a.npt, a.pt, a.ptcap, a.npl, a.ntp, a.status, a.lmask, a.tstatus, a.tlmask, a.levelg,
+                             a.tlevelg, a.rh, a.trh, a.tvb, a.tah, a.Gm, a.rhill, a.rhscale, a.dt, a.irec, -1,
+                             a.good_pt);
+    }
+}
+
+// symba_step_set_recur_levels_system (symba_step.f90:118-160)
+__global__ void k_set_recur_levels(int npl, int ntp, int64_t npp, int64_t ppcap, int64_t npt, int64_t ptcap,
+                                   int32_t *levelg, int32_t *tlevelg, int32_t *pp, int32_t *pt, int ireci) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int irecp = ireci + 1;
+    if (k < npl && levelg[k] == irecp) levelg[k] = ireci;
+    if (k < ntp && tlevelg[k] == irecp) tlevelg[k] = ireci;
+    if (k < npp && pp[4 * ppcap + k] == irecp) pp[4 * ppcap + k] = ireci;
+    if (k < npt && pt[4 * ptcap + k] == irecp) pt[4 * ptcap + k] = ireci;
+}
+
+// SyMBA drift of both populations (symba_drift_pl/_tp, symba_drift.f90:14-61)
+__global__ void k_noop() {}
+
+// ---- WHM serial coordinate kernels (whm_coord.f90:14-124) and accelerations (whm_kick.f90:125-215)
+__global__ void k_whm_h2j(int n, const double *Gm, const double *eta, const double *rh, const double *vh, double *xj,
+                          double *vj) {
+    if (threadIdx.x != 0) return;
+    for (int d = 0; d < 3; d++) {
+        xj[d] = rh[d];
+        vj[d] = vh[d];
+    }
+    double sx[3] = {0, 0, 0}, sv[3] = {0, 0, 0};
+    for (int i = 1; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            sx[d] = sx[d] + Gm[i - 1] * rh[3 * (i - 1) + d];
+            sv[d] = sv[d] + Gm[i - 1] * vh[3 * (i - 1) + d];
+            const double cap = sx[d] / eta[i - 1];
+            const double capv = sv[d] / eta[i - 1];
+            xj[3 * i + d] = rh[3 * i + d] - cap;
+            vj[3 * i + d] = vh[3 * i + d] - capv;
+        }
+}
+__global__ void k_whm_j2h(int n, const double *Gm, const double *eta, const double *xj, const double *vj, double *rh,
+                          double *vh) {
+    if (threadIdx.x != 0) return;
+    for (int d = 0; d < 3; d++) {
+        rh[d] = xj[d];
+        vh[d] = vj[d];
+    }
+    double sx[3] = {0, 0, 0}, sv[3] = {0, 0, 0};
+    for (int i = 1; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            sx[d] = sx[d] + Gm[i - 1] * xj[3 * (i - 1) + d] / eta[i - 1];
+            sv[d] = sv[d] + Gm[i - 1] * vj[3 * (i - 1) + d] / eta[i - 1];
+            rh[3 * i + d] = xj[3 * i + d] + sx[d];
+            vh[3 * i + d] = vj[3 * i + d] + sv[d];
+        }
+}
+__global__ void k_whm_vh2vj(int n, const double *Gm, const double *eta, const double *vh, double *vj) {
+    if (threadIdx.x != 0) return;
+    for (int d = 0; d < 3; d++) vj[d] = vh[d];
+    double sv[3] = {0, 0, 0};
+    for (int i = 1; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            sv[d] = sv[d] + Gm[i - 1] * vh[3 * (i - 1) + d];
+            const double capv = sv[d] / eta[i - 1];
+            vj[3 * i + d] = vh[3 * i + d] - capv;
+        }
+}
+// whm_kick_getacch_ah0 (:125-149)
+__device__ void d_whm_ah0(const double *mu, const double *rhp, int n, double *ah0) {
+    ah0[0] = ah0[1] = ah0[2] = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double r2 = rhp[3 * i] * rhp[3 * i] + rhp[3 * i + 1] * rhp[3 * i + 1] + rhp[3 * i + 2] * rhp[3 * i + 2];
+        const double ir3h = 1.0 / (r2 * sqrt(r2));
+        const double fac = mu[i] * ir3h;
+        for (int d = 0; d < 3; d++) ah0[d] = ah0[d] - fac * rhp[3 * i + d];
+    }
+}
+// whm_kick_getacch_pl up to accel_int: ir3h/ir3j, ah0, ah1, ah2 (one block; serial parts in thread 0)
+__global__ void k_whm_accel_pl(int n, const double *Gm, double GMcb, const double *rh, const double *xj,
+                               const int32_t *lmask, double *ir3h, double *ir3j, double *ah) {
+    __shared__ double s_ah0[3];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double r2 = rh[3 * i] * rh[3 * i] + rh[3 * i + 1] * rh[3 * i + 1] + rh[3 * i + 2] * rh[3 * i + 2];
+        double ir = 1.0 / sqrt(r2);
+        ir3h[i] = ir / r2;
+        r2 = xj[3 * i] * xj[3 * i] + xj[3 * i + 1] * xj[3 * i + 1] + xj[3 * i + 2] * xj[3 * i + 2];
+        ir = 1.0 / sqrt(r2);
+        ir3j[i] = ir / r2;
+    }
+    if (threadIdx.x == 0) d_whm_ah0(Gm + 1, rh + 3, n - 1, s_ah0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * i + d] + s_ah0[d];
+        if (i >= 1 && lmask[i])
+            for (int d = 0; d < 3; d++) {
+                const double ah1j = xj[3 * i + d] * ir3j[i];
+                const double ah1h = rh[3 * i + d] * ir3h[i];
+                ah[3 * i + d] = ah[3 * i + d] + GMcb * (ah1j - ah1h);
+            }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ah2[3] = {0, 0, 0}, ah2o[3] = {0, 0, 0};
+        double etaj = GMcb;
+        for (int i = 1; i < n; i++) {
+            if (!lmask[i]) continue;
+            etaj = etaj + Gm[i - 1];
+            const double fac = Gm[i] * GMcb * ir3j[i] / etaj;
+            for (int d = 0; d < 3; d++) {
+                ah2[d] = ah2o[d] + fac * xj[3 * i + d];
+                ah[3 * i + d] = ah[3 * i + d] + ah2[d];
+                ah2o[d] = ah2[d];
+            }
+        }
+    }
+}
+// whm_kick_getacch_tp ah0 part (:70-122): tah += ah0(rp) for masked tp ; zero first when requested
+__global__ void k_whm_tp_ah0(int ntp, int npl, const double *Gm, const double *rp, const int32_t *tlmask, double *tah,
+                             int zero) {
+    __shared__ double s_ah0[3];
+    if (threadIdx.x == 0) d_whm_ah0(Gm, rp, npl, s_ah0);
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntp; i += gridDim.x * blockDim.x) {
+        if (!tlmask[i]) continue;
+        for (int d = 0; d < 3; d++) tah[3 * i + d] = (zero ? 0.0 : tah[3 * i + d]) + s_ah0[d];
+    }
+}
+__global__ void k_any_nonzero(int n, const int32_t *v, int32_t *flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && v[i] != 0) atomicOr(flag, 1);
+}
+__global__ void k_whm_drift_status(int n, const int32_t *iflag, int32_t *status, int32_t *lmask) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && iflag[i] != 0) {
+        status[i] = ST_DISCARDED_DRIFTERR;
+        lmask[i] = 0;
+    }
+}
+
+// ---- energy / momentum (swiftest_util.f90:1172-1401), masses as G*m
+__device__ __forceinline__ double d_norm2s(double a, double b, double c) {
+    double scale = 0.0, ssq = 1.0;
+    const double v[3] = {a, b, c};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (v[k] != 0.0) {
+            const double absx = fabs(v[k]);
+            if (scale < absx) {
+                const double q = scale / absx;
+                ssq = 1.0 + ssq * q * q;
+                scale = absx;
+            } else {
+                const double q = absx / scale;
+                ssq = ssq + q * q;
+            }
+        }
+    }
+    return scale * sqrt(ssq);
+}
+__global__ void k_energy_rows(int n, const double *rb, const double *Gm, const int32_t *status, double *rows) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double row = 0.0;
+    if (status[i] != ST_INACTIVE) {
+        for (int j = i + 1; j < n; j++) {
+            if (status[j] == ST_INACTIVE) continue;
+            row = row + (-(Gm[i] * Gm[j]) / d_norm2s(rb[3 * i] - rb[3 * j], rb[3 * i + 1] - rb[3 * j + 1],
+                                                    rb[3 * i + 2] - rb[3 * j + 2]));
+        }
+    }
+    rows[i] = row;
+}
+__global__ void k_energy_final(int n, int whm, const double *rh, const double *vh, const double *vbin,
+                               const double *Gm, const double *radius, const int32_t *status, double GMcb, double Rcb,
+                               int lclose, const double *rows, double *rb, double *out) {
+    if (threadIdx.x != 0) return;
+    double cbvb[3];
+    if (whm) {
+        double sum = 0.0;
+        for (int i = 0; i < n; i++) sum = sum + Gm[i];
+        const double Gmtot = GMcb + sum;
+        double c3[3] = {0, 0, 0};
+        for (int i = 0; i < n; i++)
+            for (int d = 0; d < 3; d++) c3[d] = c3[d] - Gm[i] * vh[3 * i + d];
+        for (int d = 0; d < 3; d++) cbvb[d] = c3[d] / Gmtot;
+    } else {
+        double c3[3] = {0, 0, 0};
+        for (int i = n - 1; i >= 0; i--) {
+            if (status[i] == ST_INACTIVE) continue;
+            for (int d = 0; d < 3; d++) c3[d] = c3[d] - Gm[i] * vbin[3 * i + d] / GMcb;
+        }
+        for (int d = 0; d < 3; d++) cbvb[d] = c3[d];
+    }
+    double Gmtot = GMcb, xt[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++) {
+        if (status[i] == ST_INACTIVE) continue;
+        Gmtot = Gmtot + Gm[i];
+        for (int d = 0; d < 3; d++) xt[d] = xt[d] + Gm[i] * rh[3 * i + d];
+    }
+    double cbrb[3];
+    for (int d = 0; d < 3; d++) cbrb[d] = -xt[d] / Gmtot;
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) rb[3 * i + d] = rh[3 * i + d] + cbrb[d];
+    const double mcb = GMcb;
+    const double kecb = mcb * (cbvb[0] * cbvb[0] + cbvb[1] * cbvb[1] + cbvb[2] * cbvb[2]);
+    double L[3] = {mcb * (cbrb[1] * cbvb[2] - cbrb[2] * cbvb[1]), mcb * (cbrb[2] * cbvb[0] - cbrb[0] * cbvb[2]),
+                   mcb * (cbrb[0] * cbvb[1] - cbrb[1] * cbvb[0])};
+    double kesum = 0.0, Lp[3] = {0, 0, 0}, pecb = 0.0, pecb_h = 0.0, be = 0.0, gsum = 0.0;
+    for (int i = 0; i < n; i++) {
+        if (status[i] == ST_INACTIVE) continue;
+        double v[3];
+        for (int d = 0; d < 3; d++) v[d] = whm ? vh[3 * i + d] + cbvb[d] : vbin[3 * i + d];
+        const double *r = &rb[3 * i];
+        const double m = Gm[i];
+        Lp[0] = Lp[0] + m * (r[1] * v[2] - r[2] * v[1]);
+        Lp[1] = Lp[1] + m * (r[2] * v[0] - r[0] * v[2]);
+        Lp[2] = Lp[2] + m * (r[0] * v[1] - r[1] * v[0]);
+        kesum = kesum + m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        pecb = pecb + (-GMcb * m / d_norm2s(r[0], r[1], r[2]));
+        pecb_h = pecb_h + (-GMcb * m / d_norm2s(rh[3 * i], rh[3 * i + 1], rh[3 * i + 2]));
+        if (lclose) be = be + (-3.0 * m * m / (5.0 * radius[i]));
+        gsum = gsum + m;
+    }
+    double pe = 0.0;
+    for (int i = 0; i < n; i++) pe = pe + rows[i];
+    const double pe_pairs = pe;
+    pe = pe + pecb;
+    const double ke = 0.5 * (kecb + kesum);
+    out[0] = ke + pe + be;
+    out[1] = ke;
+    out[2] = pe;
+    out[3] = be;
+    out[4] = L[0] + Lp[0];
+    out[5] = L[1] + Lp[1];
+    out[6] = L[2] + Lp[2];
+    out[7] = GMcb + gsum;
+    out[8] = ke + (pe_pairs + pecb_h) + be;
+}
+
+}  // namespace
+
+// ======================================================================== host side
+namespace {
+
+int L(swg_ctx *c, const char *what) {
+    c->launches++;
+    return launch_status(c, what);
+}
+
+bool exact(const swg_system *s) { return s->precision == SWG_FP64; }
+
+int pair_scratch(swg_system *s, double **p) {
+    SWG_TRY(ensure(s->c, s->pair_scratch, sizeof(double) * 6 * (size_t)std::max(1, s->npl)));
+    *p = (double *)s->pair_scratch.ptr;
+    return SWG_OK;
+}
+
+// pl-pl interaction accelerations (swiftest_kick.f90:12-43 / symba_kick.f90:14-33), acc starts at zero
+int accel_int_pl(swg_system *s, int acc_is_zero) {
+    swg_ctx *c = s->c;
+    const bool symba = s->integrator == SWG_SYMBA;
+    const double *rad = (symba || s->lclose) ? s->radius : nullptr;
+    const int32_t nplm = symba ? s->nplm : s->npl;
+    if (s->precision == SWG_MIXED) {
+        const int nch = kick_mixed_chunks(c, s->npl, s->npl);
+        SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->npl, nch)));
+        return kick_mixed_launch(c, false, s->npl, s->npl, nplm, s->rh, s->rh, s->Gmass, rad, nullptr, s->ah,
+                                 acc_is_zero, nch, s->kick_scratch.ptr);
+    }
+    // flat, or triangular with GMTINY bodies dominating -> symmetric (split) sums
+    const int mode = (s->loop_mode == 1 || (s->npl - nplm) > nplm) ? KICK_SPLIT : KICK_DIRECT;
+    return kick_plpl_fp64(c, s->npl, nplm, s->rh, s->Gmass, rad, s->ah, mode, acc_is_zero);
+}
+
+// helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76)
+int kick_vb_pl(swg_system *s, double dt, int lbeg) {
+    swg_ctx *c = s->c;
+    if (s->npl == 0) return SWG_OK;
+    SWG_TRY(accel_int_pl(s, 1));
+    if (s->integrator == SWG_SYMBA && s->plpl_n > 0) {
+        double *scr;
+        SWG_TRY(pair_scratch(s, &scr));
+        SWG_TRY(kick_pairs(c, s->npl, s->plpl_n, nullptr, s->plpl_l, s->plpl_l + s->plpl_cap, s->rh, s->Gmass,
+                           s->radius, s->ah, -1.0, scr));
+    }
+    k_kick_update<<<grid_for(s->npl, 128), 128, 0, c->stream>>>(s->npl, s->vb, s->ah, s->lmask, dt, s->rh,
+                                                                 lbeg ? s->rbeg : s->rend);
+    return L(c, "kick_update_pl");
+}
+
+// helio_kick_vb_tp (helio_kick.f90:135-169) with symba_kick_getacch_tp (symba_kick.f90:79-123)
+int kick_vb_tp(swg_system *s, double dt, int lbeg) {
+    swg_ctx *c = s->c;
+    if (s->ntp == 0) return SWG_OK;
+    const double *rp = lbeg ? s->rbeg : s->rend;
+    if (s->npl > 0) {
+        if (s->precision == SWG_MIXED) {
+            const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
+            SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, nch)));
+            SWG_TRY(kick_mixed_launch(c, true, s->ntp, s->npl, 0, s->trh, rp, s->Gmass, nullptr, s->tlmask, s->tah,
+                                      1, nch, s->kick_scratch.ptr));
+        } else {
+            SWG_TRY(kick_tp_fp64(c, s->ntp, s->npl, s->trh, rp, s->Gmass, s->tlmask, s->tah, 1));
+        }
+    } else {
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(s->tah, 0, sizeof(double) * 3 * s->ntp, c->stream), "memset"));
+    }
+    if (s->integrator == SWG_SYMBA && s->pltp_n > 0) {
+        k_pltp_addback<<<1, 32, 0, c->stream>>>(s->pltp_n, s->pltp_l, s->pltp_l + s->pltp_cap, s->tlmask, s->trh,
+                                                rp, s->Gmass, s->tah);
+        SWG_TRY(L(c, "pltp_addback"));
+    }
+    k_kick_update<<<grid_for(s->ntp, 128), 128, 0, c->stream>>>(s->ntp, s->tvb, s->tah, s->tlmask, dt, nullptr,
+                                                                 nullptr);
+    return L(c, "kick_update_tp");
+}
+
+int lindrift_pl(swg_system *s, double dt, int lbeg) {
+    if (s->npl == 0) return SWG_OK;
+    k_lindrift_pl<<<1, 256, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->lmask, s->GMcb, s->rh, dt, s->dcb,
+                                               lbeg ? CB_PTBEG : CB_PTEND, exact(s));
+    return L(s->c, "lindrift_pl");
+}
+int tp_misc(swg_system *s, int slot, double dt, int mode) {
+    if (s->ntp == 0) return SWG_OK;
+    k_tp_misc<<<grid_for(s->ntp, 256), 256, 0, s->c->stream>>>(s->ntp, s->tlmask, s->trh, s->tvh, s->tvb, s->dcb,
+                                                                slot, dt, mode);
+    return L(s->c, "tp_misc");
+}
+int vh2vb_pl(swg_system *s) {
+    if (s->npl == 0) return SWG_OK;
+    k_vh2vb_pl<<<1, 256, 0, s->c->stream>>>(s->npl, s->Gmass, s->vh, s->vb, s->GMcb, s->dcb);
+    return L(s->c, "vh2vb_pl");
+}
+int vb2vh_pl(swg_system *s) {
+    if (s->npl == 0) return SWG_OK;
+    k_vb2vh_pl<<<1, 256, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->status, s->vh, s->GMcb, s->dcb);
+    return L(s->c, "vb2vh_pl");
+}
+// drift with the SyMBA level mask (levelg == irec) or the plain status mask
+int drift_pl(swg_system *s, double dt) {
+    if (s->npl == 0) return SWG_OK;
+    const int32_t *lev = s->integrator == SWG_SYMBA ? s->levelg : nullptr;
+    return drift_masked(s->c, s->GMcb, s->rh, s->vb, s->npl, lev, s->irec, dt, s->status, nullptr);
+}
+int drift_tp(swg_system *s, double dt) {
+    if (s->ntp == 0) return SWG_OK;
+    const int32_t *lev = s->integrator == SWG_SYMBA ? s->tlevelg : nullptr;
+    double *v = s->integrator == SWG_WHM ? s->tvh : s->tvb;
+    return drift_masked(s->c, s->GMcb, s->trh, v, s->ntp, lev, s->irec, dt, s->tstatus, nullptr);
+}
+
+// helio_step_pl / _tp (helio_step.f90:37-119) via whm_step_system (whm_step.f90:14-35)
+int helio_step(swg_system *s, double dt) {
+    const double dth = 0.5 * dt;
+    s->lfirst_tp = s->lfirst_pl;
+    if (s->npl > 0) {
+        if (s->lfirst_pl) {
+            SWG_TRY(vh2vb_pl(s));
+            s->lfirst_pl = 0;
+        }
+        SWG_TRY(lindrift_pl(s, dth, 1));
+        SWG_TRY(kick_vb_pl(s, dth, 1));
+        SWG_TRY(drift_pl(s, dt));
+        SWG_TRY(kick_vb_pl(s, dth, 0));
+        SWG_TRY(lindrift_pl(s, dth, 0));
+        SWG_TRY(vb2vh_pl(s));
+    }
+    if (s->ntp > 0) {
+        if (s->lfirst_tp) {
+            SWG_TRY(tp_misc(s, CB_PTBEG, dth, 4));
+            s->lfirst_tp = 0;
+        } else {
+            SWG_TRY(tp_misc(s, CB_PTBEG, dth, 2));
+        }
+        SWG_TRY(kick_vb_tp(s, dth, 1));
+        SWG_TRY(drift_tp(s, dt));
+        SWG_TRY(kick_vb_tp(s, dth, 0));
+        SWG_TRY(tp_misc(s, CB_PTEND, dth, 3));
+    }
+    return SWG_OK;
+}
+
+// ---- WHM (whm_step.f90:14-104)
+int whm_accel_pl(swg_system *s) {
+    swg_ctx *c = s->c;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(s->ah, 0, sizeof(double) * 3 * s->npl, c->stream), "memset"));
+    k_whm_accel_pl<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->GMcb, s->rh, s->xj, s->lmask, s->ir3h, s->ir3j,
+                                             s->ah);
+    SWG_TRY(L(c, "whm_accel_pl"));
+    return accel_int_pl(s, 0);
+}
+int whm_kick_vh_pl(swg_system *s, double dt, int lbeg) {
+    swg_ctx *c = s->c;
+    if (lbeg) {
+        if (s->lfirst_pl) {
+            k_whm_h2j<<<1, 32, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->rh, s->vh, s->xj, s->vj);
+            SWG_TRY(L(c, "whm_h2j"));
+            SWG_TRY(whm_accel_pl(s));
+            s->lfirst_pl = 0;
+        }
+        k_kick_update<<<grid_for(s->npl, 128), 128, 0, c->stream>>>(s->npl, s->vh, s->ah, s->lmask, dt, s->rh,
+                                                                     s->rbeg);
+    } else {
+        SWG_TRY(whm_accel_pl(s));
+        k_kick_update<<<grid_for(s->npl, 128), 128, 0, c->stream>>>(s->npl, s->vh, s->ah, s->lmask, dt, s->rh,
+                                                                     s->rend);
+    }
+    return L(c, "kick_update_whm");
+}
+int whm_accel_tp(swg_system *s, int lbeg, int zero) {
+    swg_ctx *c = s->c;
+    const double *rp = lbeg ? s->rbeg : s->rend;
+    k_whm_tp_ah0<<<grid_for(s->ntp, 256), 256, 0, c->stream>>>(s->ntp, s->npl, s->Gmass, rp, s->tlmask, s->tah, zero);
+    SWG_TRY(L(c, "whm_tp_ah0"));
+    if (s->precision == SWG_MIXED) {
+        const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
+        SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, nch)));
+        return kick_mixed_launch(c, true, s->ntp, s->npl, 0, s->trh, rp, s->Gmass, nullptr, s->tlmask, s->tah, 0,
+                                 nch, s->kick_scratch.ptr);
+    }
+    return kick_tp_fp64(c, s->ntp, s->npl, s->trh, rp, s->Gmass, s->tlmask, s->tah, 0);
+}
+int whm_kick_vh_tp(swg_system *s, double dt, int lbeg) {
+    swg_ctx *c = s->c;
+    if (s->lfirst_tp) {
+        SWG_TRY(whm_accel_tp(s, 1, 1));
+        s->lfirst_tp = 0;
+    }
+    if (!lbeg) SWG_TRY(whm_accel_tp(s, 0, 1));
+    k_kick_update<<<grid_for(s->ntp, 128), 128, 0, c->stream>>>(s->ntp, s->tvh, s->tah, s->tlmask, dt, nullptr,
+                                                                 nullptr);
+    return L(c, "kick_update_whm_tp");
+}
+int whm_step(swg_system *s, double dt) {
+    swg_ctx *c = s->c;
+    const double dth = 0.5 * dt;
+    s->lfirst_tp = s->lfirst_pl;
+    if (s->npl > 0) {
+        SWG_TRY(whm_kick_vh_pl(s, dth, 1));
+        k_whm_vh2vj<<<1, 32, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->vh, s->vj);
+        SWG_TRY(L(c, "whm_vh2vj"));
+        SWG_TRY(drift_all(c, s->muj, 0.0, s->xj, s->vj, s->npl, 0, 0.0, dt, s->lmask, s->iflag));
+        int32_t *dflag = (int32_t *)s->flags.ptr;
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(dflag + 1, 0, sizeof(int32_t), c->stream), "memset"));
+        k_any_nonzero<<<grid_for(s->npl, 256), 256, 0, c->stream>>>(s->npl, s->iflag, dflag + 1);
+        SWG_TRY(L(c, "any_nonzero"));
+        k_whm_drift_status<<<grid_for(s->npl, 256), 256, 0, c->stream>>>(s->npl, s->iflag, s->status, s->lmask);
+        SWG_TRY(L(c, "whm_drift_status"));
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->h_flags + 1, dflag + 1, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                               c->stream),
+                            "flag"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
+        if (s->h_flags[1] != 0) {
+            c->err = "Danby drift failed for a massive body (WHM stops the run)";
+            return SWG_ERR_DRIFT;
+        }
+        k_whm_j2h<<<1, 32, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->xj, s->vj, s->rh, s->vh);
+        SWG_TRY(L(c, "whm_j2h"));
+        SWG_TRY(whm_kick_vh_pl(s, dth, 0));
+    }
+    if (s->ntp > 0) {
+        SWG_TRY(whm_kick_vh_tp(s, dth, 1));
+        SWG_TRY(drift_tp(s, dt));
+        SWG_TRY(whm_kick_vh_tp(s, dth, 0));
+    }
+    return SWG_OK;
+}
+
+// ---- SyMBA
+int ensure_list(swg_system *s, int32_t **l, int64_t *cap, int64_t need) {
+    if (need <= *cap) return SWG_OK;
+    const int64_t ncap = std::max<int64_t>(need + need / 2, 256);
+    int32_t *fresh = nullptr;
+    SWG_TRY(dalloc(s->c, &fresh, (size_t)5 * ncap));
+    if (*l) cudaFree(*l);
+    *l = fresh;
+    *cap = ncap;
+    return SWG_OK;
+}
+
+// level-0 checks: symba_encounter_check_pl / _tp (symba_encounter_check.f90:14-87, 238-296)
+int symba_level0(swg_system *s, double dt, int *lany) {
+    swg_ctx *c = s->c;
+    *lany = 0;
+    s->plpl_n = s->pltp_n = 0;
+    // renc at level 0 is computed inside the checks from rhill
+    double *renc = (double *)s->red.ptr;
+    k_set_renc<<<grid_for(s->npl, 128), 128, 0, c->stream>>>(s->npl, s->rhill, s->rhscale, 0, renc);
+    SWG_TRY(L(c, "set_renc"));
+    if (s->npl > 0) {
+        int64_t n = 0;
+        int32_t *i1, *i2, *lv;
+        const int32_t nplt = s->npl - s->nplm;
+        if (nplt == 0)
+            SWG_TRY(encounter_check_kind(c, s->enc, 0, s->enc_plpl, s->npl, s->rh, s->vb, renc, 0, nullptr, nullptr,
+                                         nullptr, dt, &n, &i1, &i2, &lv));
+        else
+            SWG_TRY(encounter_check_kind(c, s->enc, 1, s->enc_plpl, s->nplm, s->rh, s->vb, renc, nplt,
+                                         s->rh + 3 * s->nplm, s->vb + 3 * s->nplm, renc + s->nplm, dt, &n, &i1, &i2,
+                                         &lv));
+        SWG_TRY(ensure_list(s, &s->plpl_l, &s->plpl_cap, n));
+        if (n > 0) {
+            for (int f = 0; f < 3; f++) {
+                const int32_t *src = f == 0 ? i1 : (f == 1 ? i2 : lv);
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->plpl_l + f * s->plpl_cap, src, sizeof(int32_t) * n,
+                                                       cudaMemcpyDeviceToDevice, c->stream),
+                                    "copy list"));
+            }
+            k_level0_mark<<<grid_for(n, 128), 128, 0, c->stream>>>(n, s->plpl_l, s->plpl_cap, 0, s->levelg, s->levelm,
+                                                                   s->nplenc, nullptr, nullptr, nullptr);
+            SWG_TRY(L(c, "level0_mark_pl"));
+        }
+        s->plpl_n = n;
+    }
+    if (s->ntp > 0 && s->npl > 0) {
+        int64_t n = 0;
+        int32_t *i1, *i2, *lv;
+        SWG_TRY(encounter_check_kind(c, s->enc, 2, s->enc_pltp, s->npl, s->rh, s->vb, renc, s->ntp, s->trh, s->tvb,
+                                     nullptr, dt, &n, &i1, &i2, &lv));
+        SWG_TRY(ensure_list(s, &s->pltp_l, &s->pltp_cap, n));
+        if (n > 0) {
+            for (int f = 0; f < 3; f++) {
+                const int32_t *src = f == 0 ? i1 : (f == 1 ? i2 : lv);
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->pltp_l + f * s->pltp_cap, src, sizeof(int32_t) * n,
+                                                       cudaMemcpyDeviceToDevice, c->stream),
+                                    "copy list"));
+            }
+            k_level0_mark<<<grid_for(n, 128), 128, 0, c->stream>>>(n, s->pltp_l, s->pltp_cap, 1, s->levelg, s->levelm,
+                                                                   s->ntpenc, s->tlevelg, s->tlevelm, s->tnplenc);
+            SWG_TRY(L(c, "level0_mark_tp"));
+        }
+        s->pltp_n = n;
+    }
+    s->stats[2] += s->plpl_n;
+    s->stats[3] += s->pltp_n;
+    *lany = (s->plpl_n + s->pltp_n) > 0;
+    return SWG_OK;
+}
+
+int kick_lists(swg_system *s, double dt, int irec, int both) {
+    swg_ctx *c = s->c;
+    if (s->plpl_n == 0 && s->pltp_n == 0) return SWG_OK;
+    KickListArgs a;
+    a.npp = s->plpl_n;
+    a.ppcap = s->plpl_cap;
+    a.npt = s->pltp_n;
+    a.ptcap = s->pltp_cap;
+    a.pp = s->plpl_l;
+    a.pt = s->pltp_l;
+    a.npl = s->npl;
+    a.ntp = s->ntp;
+    a.status = s->status;
+    a.tstatus = s->tstatus;
+    a.levelg = s->levelg;
+    a.tlevelg = s->tlevelg;
+    a.lmask = s->lmask;
+    a.tlmask = s->tlmask;
+    a.rh = s->rh;
+    a.trh = s->trh;
+    a.Gm = s->Gmass;
+    a.rhill = s->rhill;
+    a.vb = s->vb;
+    a.ah = s->ah;
+    a.tvb = s->tvb;
+    a.tah = s->tah;
+    a.rhscale = s->rhscale;
+    a.dt = dt;
+    a.irec = irec;
+    a.both = both;
+    uint8_t *good = (uint8_t *)s->enc.sort.ptr;  // list-sized byte scratch (sort buffer is idle here)
+    a.good_pp = good;
+    a.good_pt = good + s->plpl_n;
+    k_kick_lists<<<1, 64, 0, c->stream>>>(a);
+    return L(c, "kick_lists");
+}
+
+// symba_step_recur_system (symba_step.f90:163-262)
+int symba_recur(swg_system *s, int ireci) {
+    swg_ctx *c = s->c;
+    s->irec = ireci;
+    double p3 = 1.0;
+    for (int k = 0; k < ireci; k++) p3 *= 3.0;
+    const double dtl = s->dt / p3;
+    const double dth = 0.5 * dtl;
+    if (dtl / s->dt < 2.220446049250313e-16) {
+        c->err = "SyMBA local time step too small";
+        return SWG_ERR_RECURSION;
+    }
+    const int irecp = ireci + 1;
+    if (irecp > s->stats[1]) s->stats[1] = irecp;
+    const int nloops = ireci == 0 ? 1 : NTENC;
+    int32_t *dflag = (int32_t *)s->flags.ptr;
+    for (int j = 1; j <= nloops; j++) {
+        k_list_check<<<1, 256, 0, c->stream>>>(s->plpl_n, s->plpl_l, s->plpl_cap, s->pltp_n, s->pltp_l, s->pltp_cap,
+                                               s->rh, s->vb, s->trh, s->tvb, s->rhill, s->radius, s->rhscale, irecp,
+                                               dtl, s->levelg, s->levelm, s->tlevelg, s->tlevelm, dflag,
+                                               (uint8_t *)s->enc.sort.ptr + s->plpl_n + s->pltp_n);
+        SWG_TRY(L(c, "list_check"));
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->h_flags, dflag, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream),
+                            "flag"));
+        SWG_TRY(kick_lists(s, dth, irecp, ireci != 0));
+        SWG_TRY(drift_pl(s, dtl));
+        SWG_TRY(drift_tp(s, dtl));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
+        const int lencounter = s->h_flags[0];
+        if (lencounter) SWG_TRY(symba_recur(s, irecp));
+        s->irec = ireci;
+        SWG_TRY(kick_lists(s, dth, irecp, ireci != 0));
+        const int64_t nmax = std::max<int64_t>(std::max<int64_t>(s->npl, s->ntp), std::max(s->plpl_n, s->pltp_n));
+        k_set_recur_levels<<<grid_for(nmax, 256), 256, 0, c->stream>>>(s->npl, s->ntp, s->plpl_n, s->plpl_cap,
+                                                                        s->pltp_n, s->pltp_cap, s->levelg, s->tlevelg,
+                                                                        s->plpl_l, s->pltp_l, ireci);
+        SWG_TRY(L(c, "set_recur_levels"));
+        s->irec = ireci;
+    }
+    return SWG_OK;
+}
+
+// symba_step_interp_system (symba_step.f90:55-115)
+int symba_interp(swg_system *s, double dt) {
+    const double dth = 0.5 * dt;
+    s->irec = -1;
+    if (s->lfirst_pl) SWG_TRY(vh2vb_pl(s));
+    SWG_TRY(lindrift_pl(s, dth, 1));
+    SWG_TRY(kick_vb_pl(s, dth, 1));
+    SWG_TRY(drift_pl(s, dt));
+    if (s->ntp > 0) {
+        SWG_TRY(tp_misc(s, CB_PTBEG, dth, s->lfirst_tp ? 4 : 2));
+        SWG_TRY(kick_vb_tp(s, dth, 1));
+        SWG_TRY(drift_tp(s, dt));
+    }
+    SWG_TRY(symba_recur(s, 0));
+    s->irec = -1;
+    SWG_TRY(kick_vb_pl(s, dth, 0));
+    SWG_TRY(lindrift_pl(s, dth, 0));
+    SWG_TRY(vb2vh_pl(s));
+    if (s->ntp > 0) {
+        SWG_TRY(kick_vb_tp(s, dth, 0));
+        SWG_TRY(tp_misc(s, CB_PTEND, dth, 3));
+    }
+    return SWG_OK;
+}
+
+// symba_step_system (symba_step.f90:14-52); both level-0 checks are evaluated
+int symba_step(swg_system *s, double dt) {
+    swg_ctx *c = s->c;
+    const int nmax = std::max(s->npl, s->ntp);
+    k_symba_reset<<<grid_for(nmax, 256), 256, 0, c->stream>>>(s->npl, s->ntp, s->levelg, s->levelm, s->nplenc,
+                                                               s->ntpenc, s->lmask, s->tlevelg, s->tlevelm,
+                                                               s->tnplenc, s->tlmask);
+    SWG_TRY(L(c, "symba_reset"));
+    s->lfirst_tp = s->lfirstkick;
+    s->lfirst_pl = s->lfirstkick;
+    int lany = 0;
+    SWG_TRY(symba_level0(s, dt, &lany));
+    if (lany) {
+        s->stats[0]++;
+        // list-sized byte scratch for kick/check flags lives in the sort buffer
+        SWG_TRY(ensure(c, s->enc.sort, (size_t)2 * (s->plpl_n + s->pltp_n) + 64));
+        SWG_TRY(symba_interp(s, dt));
+    } else {
+        s->irec = -1;
+        SWG_TRY(helio_step(s, dt));
+    }
+    s->lfirstkick = s->lfirst_pl;
+    return SWG_OK;
+}
+
+}  // namespace
+
+// ======================================================================== C ABI
+extern "C" {
+
+int swg_system_create(swg_ctx *c, int integrator, int32_t npl, int32_t ntp, swg_system **out) {
+    if (!c || !out || npl < 0 || ntp < 0 || integrator < SWG_WHM || integrator > SWG_SYMBA) return SWG_ERR_ARG;
+    swg_system *s = new swg_system();
+    s->c = c;
+    s->integrator = integrator;
+    s->npl = npl;
+    s->ntp = ntp;
+    s->nplm = npl;
+    const size_t n = std::max(npl, 1), m = std::max(ntp, 1);
+    int rc = SWG_OK;
+    double **pd[] = {&s->rh, &s->vh, &s->vb, &s->ah, &s->rbeg, &s->rend, &s->xj, &s->vj};
+    for (auto p : pd)
+        if (rc == SWG_OK) rc = dalloc(c, p, 3 * n);
+    double **pn[] = {&s->Gmass, &s->radius, &s->rhill, &s->eta, &s->muj, &s->ir3h, &s->ir3j};
+    for (auto p : pn)
+        if (rc == SWG_OK) rc = dalloc(c, p, n);
+    int32_t **pi[] = {&s->status, &s->lmask, &s->levelg, &s->levelm, &s->nplenc, &s->ntpenc, &s->iflag};
+    for (auto p : pi)
+        if (rc == SWG_OK) rc = dalloc(c, p, n);
+    double **td[] = {&s->trh, &s->tvh, &s->tvb, &s->tah};
+    for (auto p : td)
+        if (rc == SWG_OK) rc = dalloc(c, p, 3 * m);
+    int32_t **ti[] = {&s->tstatus, &s->tlmask, &s->tlevelg, &s->tlevelm, &s->tnplenc, &s->tiflag};
+    for (auto p : ti)
+        if (rc == SWG_OK) rc = dalloc(c, p, m);
+    if (rc == SWG_OK) rc = dalloc(c, &s->dcb, CB_N);
+    if (rc == SWG_OK) rc = ensure(c, s->flags, 64);
+    if (rc == SWG_OK) rc = ensure(c, s->red, sizeof(double) * (4 * n + 64));
+    if (rc == SWG_OK) {
+        cudaError_t e = cudaMallocHost((void **)&s->h_flags, 64);
+        if (e != cudaSuccess) rc = cuda_status(c, e, "cudaMallocHost");
+    }
+    if (rc != SWG_OK) {
+        swg_system_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "create");
+}
+
+int swg_system_destroy(swg_system *s) {
+    if (!s) return SWG_OK;
+    swg_ctx *c = s->c;
+    if (c) cudaStreamSynchronize(c->stream);
+    void *ptrs[] = {s->rh, s->vh, s->vb, s->ah, s->rbeg, s->rend, s->xj, s->vj, s->Gmass, s->radius, s->rhill,
+                    s->eta, s->muj, s->ir3h, s->ir3j, s->status, s->lmask, s->levelg, s->levelm, s->nplenc,
+                    s->ntpenc, s->iflag, s->trh, s->tvh, s->tvb, s->tah, s->tstatus, s->tlmask, s->tlevelg,
+                    s->tlevelm, s->tnplenc, s->tiflag, s->dcb, s->plpl_l, s->pltp_l, s->enc.raw.ptr,
+                    s->enc.sort.ptr, s->enc.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
+                    s->red.ptr};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (s->h_flags) cudaFreeHost(s->h_flags);
+    delete s;
+    return SWG_OK;
+}
+
+int swg_system_set_cb(swg_system *s, double GMcb, double Rcb) {
+    if (!s || !(GMcb > 0.0)) return SWG_ERR_ARG;
+    s->GMcb = GMcb;
+    s->Rcb = Rcb;
+    return SWG_OK;
+}
+
+int swg_system_set_pl(swg_system *s, const double *rh, const double *vh, const double *Gmass, const double *radius,
+                      const double *rhill) {
+    if (!s) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const size_t n = s->npl;
+    if (n == 0) return SWG_OK;
+    if (!rh || !vh || !Gmass || !radius || !rhill) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->rh, rh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->vh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->Gmass, Gmass, 8 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->radius, radius, 8 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->rhill, rhill, 8 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    s->initialized = 0;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "set_pl");
+}
+
+int swg_system_set_tp(swg_system *s, const double *rh, const double *vh) {
+    if (!s) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const size_t n = s->ntp;
+    if (n == 0) return SWG_OK;
+    if (!rh || !vh) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->trh, rh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_tp"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->tvh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_tp"));
+    s->initialized = 0;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "set_tp");
+}
+
+int swg_system_set_param(swg_system *s, double dt, int loop_mode, int enc_plpl, int enc_pltp, double rhscale,
+                         int lclose, double gmtiny, int precision) {
+    if (!s || !(dt > 0.0) || (loop_mode != 0 && loop_mode != 1) || (precision != SWG_FP64 && precision != SWG_MIXED))
+        return SWG_ERR_ARG;
+    if ((enc_plpl != SWG_ENC_TRIANGULAR && enc_plpl != SWG_ENC_SORTSWEEP) ||
+        (enc_pltp != SWG_ENC_TRIANGULAR && enc_pltp != SWG_ENC_SORTSWEEP) || !(rhscale > 0.0))
+        return SWG_ERR_ARG;
+    s->dt = dt;
+    s->loop_mode = loop_mode;
+    s->enc_plpl = enc_plpl;
+    s->enc_pltp = enc_pltp;
+    s->rhscale = rhscale;
+    s->lclose = lclose;
+    s->gmtiny = gmtiny;
+    s->precision = precision;
+    return SWG_OK;
+}
+
+// Initialisation as helio_util_setup_initialize_system (helio_util.f90:14-43) /
+// whm_util_set_mu_eta_pl (whm_util.f90:175-198); bodies arrive pre-sorted.
+int swg_system_initialize(swg_system *s) {
+    if (!s || !(s->GMcb > 0.0) || !(s->dt > 0.0)) return SWG_ERR_STATE;
+    swg_ctx *c = s->c;
+    const int n = s->npl;
+    std::vector<int32_t> ones(std::max(n, s->ntp), 1), zeros(std::max(n, s->ntp), 0);
+    if (n > 0) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->status, zeros.data(), 4 * n, cudaMemcpyHostToDevice, c->stream), "init"));
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->lmask, ones.data(), 4 * n, cudaMemcpyHostToDevice, c->stream), "init"));
+    }
+    if (s->ntp > 0) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->tstatus, zeros.data(), 4 * s->ntp, cudaMemcpyHostToDevice, c->stream), "init"));
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->tlmask, ones.data(), 4 * s->ntp, cudaMemcpyHostToDevice, c->stream), "init"));
+    }
+    std::vector<double> Gm(n);
+    if (n > 0)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(Gm.data(), s->Gmass, 8 * n, cudaMemcpyDeviceToHost, c->stream), "init"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "init"));
+    s->nplm = n;
+    if (s->gmtiny > 0.0) {
+        int m = 0;
+        for (int i = 0; i < n; i++) m += !(Gm[i] < s->gmtiny);
+        s->nplm = m;
+    }
+    if (s->integrator == SWG_WHM) {
+        std::vector<double> eta(n), muj(n);
+        if (n > 0) {
+            eta[0] = s->GMcb + Gm[0];
+            muj[0] = eta[0];
+            for (int i = 1; i < n; i++) {
+                eta[i] = eta[i - 1] + Gm[i];
+                muj[i] = s->GMcb * eta[i] / eta[i - 1];
+            }
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->eta, eta.data(), 8 * n, cudaMemcpyHostToDevice, c->stream), "init"));
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->muj, muj.data(), 8 * n, cudaMemcpyHostToDevice, c->stream), "init"));
+        }
+    } else {
+        SWG_TRY(vh2vb_pl(s));
+        if (s->ntp > 0) {
+            // tp h2b: vb = vh + cb%vb
+            SWG_TRY(tp_misc(s, CB_VB, 0.0, 5));
+        }
+    }
+    s->lfirst_pl = s->lfirst_tp = s->lfirstkick = 1;
+    s->irec = -1;
+    s->t = 0.0;
+    s->initialized = 1;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "init");
+}
+
+int swg_system_step(swg_system *s, int32_t nsteps) {
+    if (!s || !s->initialized) return SWG_ERR_STATE;
+    for (int32_t k = 0; k < nsteps; k++) {
+        int rc;
+        if (s->integrator == SWG_WHM)
+            rc = whm_step(s, s->dt);
+        else if (s->integrator == SWG_HELIO)
+            rc = helio_step(s, s->dt);
+        else
+            rc = symba_step(s, s->dt);
+        if (rc != SWG_OK) return rc;
+        s->t += s->dt;
+    }
+    return SWG_OK;
+}
+
+int swg_system_get_pl(swg_system *s, double *rh, double *vh, int32_t *status) {
+    if (!s) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const size_t n = s->npl;
+    if (n == 0) return SWG_OK;
+    if (rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(rh, s->rh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_pl"));
+    if (vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(vh, s->vh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_pl"));
+    if (status)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(status, s->status, 4 * n, cudaMemcpyDeviceToHost, c->stream), "get_pl"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "get_pl");
+}
+
+int swg_system_get_tp(swg_system *s, double *rh, double *vh, int32_t *status) {
+    if (!s) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const size_t n = s->ntp;
+    if (n == 0) return SWG_OK;
+    if (rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(rh, s->trh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_tp"));
+    if (vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(vh, s->tvh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_tp"));
+    if (status)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(status, s->tstatus, 4 * n, cudaMemcpyDeviceToHost, c->stream), "get_tp"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "get_tp");
+}
+
+int swg_system_energy(swg_system *s, double *out) {
+    if (!s || !out) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const int n = s->npl;
+    double *rows = (double *)s->red.ptr;
+    double *rb = rows + std::max(n, 1);
+    double *dout = rb + 3 * std::max(n, 1);
+    // barycentric positions first (energy rows need rb): the final kernel computes rb,
+    // so run it twice: once for rb, then rows, then again for the totals.
+    k_energy_final<<<1, 32, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
+                                            s->status, s->GMcb, s->Rcb, s->lclose, rows, rb, dout);
+    SWG_TRY(L(c, "energy_rb"));
+    k_energy_rows<<<grid_for(n, 128), 128, 0, c->stream>>>(n, rb, s->Gmass, s->status, rows);
+    SWG_TRY(L(c, "energy_rows"));
+    k_energy_final<<<1, 32, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
+                                            s->status, s->GMcb, s->Rcb, s->lclose, rows, rb, dout);
+    SWG_TRY(L(c, "energy_final"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(out, dout, 9 * 8, cudaMemcpyDeviceToHost, c->stream), "energy"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "energy");
+}
+
+int swg_system_stats(swg_system *s, int64_t *out) {
+    if (!s || !out) return SWG_ERR_ARG;
+    std::memcpy(out, s->stats, sizeof(s->stats));
+    return SWG_OK;
+}
+
+static int copy_list(swg_system *s, int32_t *l, int64_t lcap, int64_t n, int64_t cap, int64_t *nout, int32_t *i1,
+                     int32_t *i2) {
+    *nout = n;
+    if (n > cap) return SWG_ERR_CAPACITY;
+    if (n == 0) return SWG_OK;
+    swg_ctx *c = s->c;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(i1, l, 4 * n, cudaMemcpyDeviceToHost, c->stream), "list"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(i2, l + lcap, 4 * n, cudaMemcpyDeviceToHost, c->stream), "list"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "list");
+}
+int swg_system_plpl_list(swg_system *s, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2) {
+    if (!s || !n) return SWG_ERR_ARG;
+    return copy_list(s, s->plpl_l, s->plpl_cap, s->plpl_n, cap, n, i1, i2);
+}
+int swg_system_pltp_list(swg_system *s, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2) {
+    if (!s || !n) return SWG_ERR_ARG;
+    return copy_list(s, s->pltp_l, s->pltp_cap, s->pltp_n, cap, n, i1, i2);
+}
+
+}  // extern "C"

@@ -1,0 +1,213 @@
+"""Known-answer tests that pin the CPU oracle (the reference ships no kernel-level golden vectors).
+
+* drift: analytic two-body Kepler propagation, reversibility, conservation
+* kick: closed-form two/three-body accelerations, Newton's third law, loop-shape equivalence
+* encounter: hand-built geometries, brute-force pair lists, the sort-and-sweep loverlap quirk
+* step loops: WHM with one planet is exact Kepler; the reference's conservation-slope
+  thresholds (tests/test_swiftest.py:119-121 of the reference) on its 8-planet example
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from swiftest_gb300 import initial_conditions as IC
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+# ---------------------------------------------------------------- drift
+def test_drift_matches_analytic_kepler():
+    rng = np.random.default_rng(0)
+    n = 200
+    a = rng.uniform(0.3, 5.0, n)
+    e = rng.uniform(0.0, 0.7, n)
+    inc, O_, w, M = (rng.uniform(0, np.pi, n), rng.uniform(0, 2 * np.pi, n), rng.uniform(0, 2 * np.pi, n),
+                     rng.uniform(0, 2 * np.pi, n))
+    mu = IC.GMCB
+    r0, v0 = IC.el2xv(mu, a, e, inc, O_, w, M)
+    for dt in (0.001, 0.05, 0.9):
+        nmean = np.sqrt(mu / a ** 3)
+        r1, v1 = IC.el2xv(mu, a, e, inc, O_, w, M + nmean * dt)
+        x, v, fl = O.drift_all(mu, r0, v0, dt)
+        assert np.all(fl == 0)
+        assert np.max(np.linalg.norm(x - r1, axis=1) / a) < 1e-10
+        assert np.max(np.linalg.norm(v - v1, axis=1) / np.linalg.norm(v1, axis=1)) < 1e-10
+
+
+def test_drift_hyperbolic_reversible_and_conservative():
+    rng = np.random.default_rng(1)
+    x0 = rng.normal(size=(50, 3))
+    v0 = rng.normal(size=(50, 3)) * 12.0  # well above escape speed
+    mu = IC.GMCB
+    x1, v1, f1 = O.drift_all(mu, x0, v0, 0.3)
+    x2, v2, f2 = O.drift_all(mu, x1, v1, -0.3)
+    assert np.all(f1 == 0) and np.all(f2 == 0)
+    assert np.max(np.abs(x2 - x0)) < 1e-10 and np.max(np.abs(v2 - v0)) < 1e-9
+    E0 = 0.5 * (v0 ** 2).sum(1) - mu / np.linalg.norm(x0, axis=1)
+    E1 = 0.5 * (v1 ** 2).sum(1) - mu / np.linalg.norm(x1, axis=1)
+    assert np.max(np.abs(E1 - E0) / np.abs(E0)) < 1e-12
+    h0, h1 = np.cross(x0, v0), np.cross(x1, v1)
+    assert np.max(np.linalg.norm(h1 - h0, axis=1) / np.linalg.norm(h0, axis=1)) < 1e-12
+
+
+def test_drift_mask_and_circular_quarter_orbit():
+    mu = IC.GMCB
+    x = np.array([[1.0, 0, 0], [2.0, 0, 0]])
+    v = np.array([[0, np.sqrt(mu), 0], [0, 1.0, 0]])
+    x1, v1, fl = O.drift_all(mu, x, v, 0.25, lmask=np.array([1, 0], np.int32))
+    assert np.allclose(x1[0], [0, 1, 0], atol=1e-12) and np.allclose(v1[0], [-np.sqrt(mu), 0, 0], atol=1e-11)
+    assert np.array_equal(x1[1], x[1]) and np.array_equal(v1[1], v[1])
+
+
+# ---------------------------------------------------------------- kick
+def test_kick_two_and_three_body_closed_form():
+    r = np.array([[1.0, 0, 0], [1.5, 0.2, -0.1], [0.3, -0.7, 0.05]])
+    Gm = np.array([1e-3, 2e-4, 5e-5])
+    acc = O.kick_tri_pl(r, Gm)
+    ref = np.zeros_like(r)
+    for i in range(3):
+        for j in range(3):
+            if i != j:
+                d = r[j] - r[i]
+                ref[i] += Gm[j] * d / np.linalg.norm(d) ** 3
+    assert np.allclose(acc, ref, rtol=1e-14, atol=0)
+    at = O.kick_tp(np.array([[0.0, 1.0, 0.0]]), r, Gm)
+    rt = -sum(Gm[j] * (np.array([0.0, 1.0, 0.0]) - r[j]) / np.linalg.norm(np.array([0.0, 1.0, 0.0]) - r[j]) ** 3
+              for j in range(3))
+    assert np.allclose(at[0], rt, rtol=1e-14)
+
+
+def test_kick_newton_third_law_and_loop_shapes():
+    cb, pl, _ = IC.make_system(seed=2, npl=300, ntp=0)
+    a_tri = O.kick_tri_pl(pl["rh"], pl["Gmass"])
+    a_flat = O.kick_flat_pl(pl["rh"], pl["Gmass"])
+    assert np.allclose(a_tri, a_flat, rtol=1e-12, atol=1e-300)
+    p = (pl["Gmass"][:, None] * a_flat).sum(0)
+    assert np.all(np.abs(p) < 1e-14 * (pl["Gmass"][:, None] * np.abs(a_flat)).sum(0))
+
+
+def test_kick_gmtiny_excludes_tiny_tiny_pairs():
+    r = np.array([[1.0, 0, 0], [0, 1.0, 0], [0, 0, 1.0]])
+    Gm = np.array([1e-3, 1e-9, 1e-9])
+    a = O.kick_tri_pl(r, Gm, nplm=1)  # bodies 2 and 3 are semi-interacting
+    d12 = r[0] - r[1]
+    assert np.allclose(a[1], Gm[0] * d12 / np.linalg.norm(d12) ** 3, rtol=1e-14)
+    af = O.kick_flat_pl(r, Gm, nplm=1)
+    assert np.allclose(a, af, rtol=1e-13)
+
+
+def test_kick_radius_guard():
+    r = np.array([[1.0, 0, 0], [1.0 + 1e-5, 0, 0], [2.0, 0, 0]])
+    Gm = np.array([1e-6, 1e-6, 1e-6])
+    R = np.array([1e-5, 1e-5, 1e-5])  # bodies 1 and 2 overlap
+    a = O.kick_tri_pl(r, Gm, R)
+    assert np.allclose(a[0], Gm[2] * (r[2] - r[0]) / np.linalg.norm(r[2] - r[0]) ** 3, rtol=1e-14)
+
+
+def test_flatten_index_formula():
+    k = O.flatten(6)
+    # swiftest_util_flatten_eucl_ij_to_k (swiftest_util.f90:1031-1055)
+    for kk, (i, j) in enumerate(k, start=1):
+        assert (i - 1) * 6 - i * (i - 1) // 2 + (j - i) == kk
+    assert len(O.flatten(6, 2)) == 2 * 6 - 2 * 3 // 2
+
+
+# ---------------------------------------------------------------- encounters
+def test_encounter_one_geometries():
+    R, dt = 1e-2, 0.1
+    # inside the radius: always an encounter
+    assert O.encounter_one([5e-3, 0, 0], [1.0, 0, 0], R, dt) == (True, True)
+    # receding
+    assert O.encounter_one([0.1, 0, 0], [1.0, 0, 0], R, dt) == (False, False)
+    # approaching, closest approach (offset 5e-3) reached within dt
+    assert O.encounter_one([0.05, 5e-3, 0], [-1.0, 0, 0], R, dt) == (True, True)
+    # approaching, closest approach after dt, still outside at dt
+    assert O.encounter_one([0.5, 0, 0], [-1.0, 0, 0], R, dt) == (False, True)
+    # approaching, closest approach after dt, inside at dt
+    assert O.encounter_one([0.105, 0, 0], [-1.0, 0, 0], R, dt) == (True, True)
+
+
+def _brute(r, v, renc, dt):
+    out = []
+    for i in range(len(r)):
+        for j in range(i + 1, len(r)):
+            le, lv = O.encounter_one(r[j] - r[i], v[j] - v[i], renc[i] + renc[j], dt)
+            if le:
+                out.append((i + 1, j + 1, lv))
+    return out
+
+
+def test_encounter_triangular_matches_brute_force():
+    rng = np.random.default_rng(3)
+    r = rng.normal(size=(120, 3)) * 0.03
+    v = rng.normal(size=(120, 3))
+    renc = rng.uniform(1e-3, 6e-3, 120)
+    i1, i2, lv = O.encounter_plpl(r, v, renc, 0.01)
+    assert list(zip(i1, i2, lv)) == _brute(r, v, renc, 0.01)
+    assert len(i1) > 0
+
+
+def test_sortsweep_loverlap_quirk():
+    # Two bodies whose radial boxes overlap only partially: no body has two foreign
+    # extents strictly inside its box, so the sweep (like the reference's) misses the
+    # pair that the triangular check finds.
+    r = np.array([[1.0, 0, 0], [1.0015, 0, 0]])
+    v = np.zeros((2, 3))
+    renc = np.array([1e-3, 1e-3])
+    tri = O.encounter_plpl(r, v, renc, 0.01, mode=0)
+    sas = O.encounter_plpl(r, v, renc, 0.01, mode=1)
+    assert list(tri[0]) == [1] and len(sas[0]) == 0
+    # a third body inside the first box makes the first body sweep its neighbours
+    r3 = np.vstack([r, [[0.0, 1.0, 0.0]]])  # radially inside box 1, spatially far
+    sas3 = O.encounter_plpl(r3, np.zeros((3, 3)), np.array([1e-3, 1e-3, 1e-4]), 0.01, mode=1)
+    assert (1, 2) in list(zip(sas3[0], sas3[1]))
+
+
+def test_sortsweep_subset_of_triangular():
+    rng = np.random.default_rng(4)
+    r = rng.normal(size=(400, 3)) * 0.05 + [1, 0, 0]
+    v = rng.normal(size=(400, 3)) * 0.01
+    renc = rng.uniform(1e-3, 5e-3, 400)
+    tri = set(zip(*O.encounter_plpl(r, v, renc, 0.01, mode=0)[:2]))
+    sas = set(zip(*O.encounter_plpl(r, v, renc, 0.01, mode=1)[:2]))
+    assert sas <= tri and len(sas) > 0.5 * len(tri)
+
+
+# ---------------------------------------------------------------- step loops
+def test_whm_single_planet_is_exact_kepler():
+    mu_cb = IC.GMCB
+    Gm = 1e-3 * mu_cb
+    pl = {"rh": np.array([[1.0, 0.0, 0.0]]), "vh": np.array([[0.0, np.sqrt(mu_cb + Gm) * 1.05, 0.0]]),
+          "Gmass": np.array([Gm]), "radius": np.array([1e-4]), "rhill": np.array([0.07])}
+    cb = {"Gmass": mu_cb, "radius": IC.RCB}
+    s = O.OracleSystem("WHM", cb, pl, None, dt=0.01)
+    s.step(100)
+    rh, vh, _ = s.get_pl()
+    x, v, _ = O.drift_all(mu_cb + Gm, pl["rh"], pl["vh"], 1.0)
+    assert np.allclose(rh, x, rtol=0, atol=1e-12) and np.allclose(vh, v, rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("integ", ["WHM", "HELIO", "SYMBA"])
+def test_solar_system_conservation_slopes(integ):
+    d = np.load(GOLDEN / "solar8.npz")
+    cb = {"Gmass": float(d["GMcb"]), "radius": float(d["Rcb"])}
+    pl = {k: d[k] for k in ("rh", "vh", "Gmass", "radius", "rhill")}
+    pl = IC.sort_for_integrator(pl, integ)
+    s = O.OracleSystem(integ, cb, pl, None, dt=float(d["dt"]))
+    e0 = s.energy()
+    ts, dE, dL = [], [], []
+    for k in range(1, 41):
+        s.step(913)  # 40 samples over 100 yr at dt = 1 day
+        e = s.energy()
+        ts.append(k * 913 / 365.25)
+        # te_helio: the reference's total energy (swiftest_util.f90:1172-1291) with the
+        # central-body potential at the heliocentric distance; the reference formula
+        # itself divides by the barycentric distance (:1316), which swings at the 3e-4
+        # level with Jupiter's orbit and has no meaningful slope.
+        dE.append((e["te_helio"] - e0["te_helio"]) / abs(e0["te_helio"]))
+        dL.append(np.linalg.norm(e["L"] - e0["L"]) / np.linalg.norm(e0["L"]))
+    # reference thresholds: |d(dE/E)/dt| < 1e-8 /yr, |d(dL/L)/dt| < 1e-10 /yr
+    assert abs(np.polyfit(ts, dE, 1)[0]) < 1e-8
+    assert abs(np.polyfit(ts, dL, 1)[0]) < 1e-10
