@@ -133,6 +133,28 @@ int swg_system_stats(swg_system *sys, int64_t *out);
 int swg_system_plpl_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
 int swg_system_pltp_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
 
+/* Upload / download the integrator state (positions and heliocentric velocities of
+ * massive bodies and test particles) of an initialized system without resetting its
+ * step flags: the per-step exchange a host-side caller that owns the arrays performs.
+ * NULL pointers are skipped.  get_state_async is ordered on the stream; call
+ * swg_synchronize before reading the host arrays. */
+int swg_system_set_state(swg_system *sys, const double *rh, const double *vh, const double *trh, const double *tvh);
+int swg_system_get_state_async(swg_system *sys, double *rh, double *vh, double *trh, double *tvh);
+
+/* ---- measurement helpers (no counterpart in the reference) ------------------------
+ * Per-kernel-class CUDA-event profile of the step loop: classes 0 pl-pl kick,
+ * 1 pl-tp kick, 2 drift, 3 level-0 encounter checks, 4 SyMBA recursion lists.
+ * out[2k] = launches recorded, out[2k+1] = summed milliseconds. */
+int swg_system_profile(swg_system *sys, int enable);
+int swg_system_profile_read(swg_system *sys, double *out);
+/* write `bytes` of a context-owned buffer on the context stream (evicts L2) */
+int swg_flush_l2(swg_ctx *ctx, int64_t bytes);
+/* CUDA events on the context stream: 16 slots */
+int swg_event_record(swg_ctx *ctx, int slot);
+int swg_event_elapsed(swg_ctx *ctx, int a, int b, double *ms);
+/* FMA-chain throughput probe: kind 0 FP32 (FFMA), 1 FP64 (DFMA); TFLOP/s */
+int swg_probe_peak(swg_ctx *ctx, int kind, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

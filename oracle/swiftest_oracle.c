@@ -16,6 +16,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* src/globals/globals_module.f90:33-38,86-101,133-135 */
 static const double TWOPI = 6.283185307179586476925286766559005768394;
@@ -53,6 +56,25 @@ static double powi(double x, int m) {
         if (n % 2) y = y * x;
     }
     return m < 0 ? 1.0 / y : y;
+}
+
+/* x**(-1.5) for the SyMBA shell kick (symba_kick.f90:204,307, where the reference
+ * calls libm pow).  sqrt(x) and x*sqrt(x) are carried as double-double pairs with
+ * Dekker's error-free transformations (residuals from fma), then one Newton step on
+ * the reciprocal: within half an ulp of the exact value except in rare near-tie
+ * cases, and the same bits on every IEEE machine with fma (the GPU side runs the
+ * identical sequence), unlike libm pow whose last bit varies between libraries. */
+static double pow_m1p5(double x) {
+    if (!(x > 0.0) || isinf(x)) return pow(x, -1.5);
+    double s = sqrt(x);
+    double rs = fma(-s, s, x);
+    double ds = rs / (2.0 * s);
+    double p = x * s;
+    double ep = fma(x, s, -p);
+    double ql = ep + x * ds;
+    double y0 = 1.0 / p;
+    double err = fma(-y0, p, 1.0) - y0 * ql;
+    return fma(y0, err, y0);
 }
 
 /* gfortran NORM2: scaled sum of squares (LAPACK dnrm2 style). */
@@ -121,6 +143,8 @@ void orc_kick_getacch_int_all_tri_pl(int32_t npl, int32_t nplm, const double *r,
         free(ahi);
         free(ahj);
     } else {
+        /* rows are independent: the reference's OpenMP row loop, each row summed in j order */
+#pragma omp parallel for schedule(static)
         for (int32_t i = 0; i < nplm; i++) {
             for (int32_t j = 0; j < npl; j++) {
                 if (j == i) continue;
@@ -617,21 +641,42 @@ static int pl_export(const pairlist *p, int64_t cap, int64_t *nenc, int32_t *ind
 static void tri_rect(int32_t n1, const double *r1, const double *v1, const double *renc1, int32_t n2,
                      const double *r2, const double *v2, const double *renc2, double dt, int upper, int32_t shift2,
                      pairlist *out) {
-    for (int32_t i = 0; i < n1; i++) {
-        int32_t j0 = upper ? i + 1 : 0;
-        for (int32_t j = j0; j < n2; j++) {
-            double xr = r2[3 * j + 0] - r1[3 * i + 0];
-            double yr = r2[3 * j + 1] - r1[3 * i + 1];
-            double zr = r2[3 * j + 2] - r1[3 * i + 2];
-            double vxr = v2[3 * j + 0] - v1[3 * i + 0];
-            double vyr = v2[3 * j + 1] - v1[3 * i + 1];
-            double vzr = v2[3 * j + 2] - v1[3 * i + 2];
-            double renc12 = renc1[i] + (renc2 ? renc2[j] : 0.0);
-            int32_t lenc, lv;
-            orc_encounter_check_one(xr, yr, zr, vxr, vyr, vzr, renc12, dt, &lenc, &lv);
-            if (lenc) pl_push(out, i + 1, j + 1 + shift2, lv);
+    /* rows are split into contiguous per-thread blocks (static schedule, like the
+     * reference's OpenMP loop); concatenating the blocks in thread order keeps
+     * the list in row order */
+    int nthr = 1;
+#ifdef _OPENMP
+    nthr = omp_get_max_threads();
+#endif
+    pairlist *part = calloc((size_t)nthr, sizeof(pairlist));
+#pragma omp parallel num_threads(nthr)
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+#pragma omp for schedule(static)
+        for (int32_t i = 0; i < n1; i++) {
+            int32_t j0 = upper ? i + 1 : 0;
+            for (int32_t j = j0; j < n2; j++) {
+                double xr = r2[3 * j + 0] - r1[3 * i + 0];
+                double yr = r2[3 * j + 1] - r1[3 * i + 1];
+                double zr = r2[3 * j + 2] - r1[3 * i + 2];
+                double vxr = v2[3 * j + 0] - v1[3 * i + 0];
+                double vyr = v2[3 * j + 1] - v1[3 * i + 1];
+                double vzr = v2[3 * j + 2] - v1[3 * i + 2];
+                double renc12 = renc1[i] + (renc2 ? renc2[j] : 0.0);
+                int32_t lenc, lv;
+                orc_encounter_check_one(xr, yr, zr, vxr, vyr, vzr, renc12, dt, &lenc, &lv);
+                if (lenc) pl_push(&part[t], i + 1, j + 1 + shift2, lv);
+            }
         }
     }
+    for (int t = 0; t < nthr; t++) {
+        for (int64_t k = 0; k < part[t].n; k++) pl_push(out, part[t].i1[k], part[t].i2[k], part[t].lv[k]);
+        pl_free(&part[t]);
+    }
+    free(part);
 }
 
 /* Sort of (index1,index2,lvdotr) triples by (index1, index2).  The pair keys
@@ -1560,7 +1605,7 @@ static void symba_kick_list_plpl(orc_system *s, double dt, int irec, int sgn) {
                 double ris = sqrt(ri);
                 double r = sqrt(r2);
                 double rr = (ris - r) / (ris * (1.0 - RSHELL));
-                fac = pow(r2, -1.5) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+                fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
             } else {
                 double ir3 = 1.0 / (r2 * sqrt(r2));
                 fac = ir3;
@@ -1626,7 +1671,7 @@ static void symba_kick_list_pltp(orc_system *s, double dt, int irec, int sgn) {
                 double ris = sqrt(ri);
                 double r = sqrt(r2);
                 double rr = (ris - r) / (ris * (1.0 - RSHELL));
-                fac = pow(r2, -1.5) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+                fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
             } else {
                 double ir3 = 1.0 / (r2 * sqrt(r2));
                 fac = ir3;

@@ -65,6 +65,14 @@ SIGNATURES = {
     "swg_system_stats": (_INT, [_P, _P]),
     "swg_system_plpl_list": (_INT, [_P, _I64, C.POINTER(_I64), _P, _P]),
     "swg_system_pltp_list": (_INT, [_P, _I64, C.POINTER(_I64), _P, _P]),
+    "swg_system_set_state": (_INT, [_P, _P, _P, _P, _P]),
+    "swg_system_get_state_async": (_INT, [_P, _P, _P, _P, _P]),
+    "swg_system_profile": (_INT, [_P, _INT]),
+    "swg_system_profile_read": (_INT, [_P, _P]),
+    "swg_flush_l2": (_INT, [_P, _I64]),
+    "swg_event_record": (_INT, [_P, _INT]),
+    "swg_event_elapsed": (_INT, [_P, _INT, _INT, C.POINTER(_D)]),
+    "swg_probe_peak": (_INT, [_P, _INT, C.POINTER(_D)]),
 }
 
 _lib = None

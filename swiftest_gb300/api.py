@@ -64,6 +64,23 @@ class Context:
     def synchronize(self):
         self.check("swg_synchronize", self.lib.swg_synchronize(self.h))
 
+    # ---- measurement helpers ---------------------------------------------
+    def flush_l2(self, nbytes: int = 512 << 20):
+        self.check("swg_flush_l2", self.lib.swg_flush_l2(self.h, int(nbytes)))
+
+    def event_record(self, slot: int):
+        self.check("swg_event_record", self.lib.swg_event_record(self.h, int(slot)))
+
+    def event_elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        self.check("swg_event_elapsed", self.lib.swg_event_elapsed(self.h, int(a), int(b), C.byref(ms)))
+        return float(ms.value)
+
+    def probe_peak_tflops(self, kind: str = "fp32") -> float:
+        t = C.c_double()
+        self.check("swg_probe_peak", self.lib.swg_probe_peak(self.h, 0 if kind == "fp32" else 1, C.byref(t)))
+        return float(t.value)
+
     # ---- kick -------------------------------------------------------------
     def kick_getacch_int_all_tri_pl(self, r, Gmass, radius=None, acc=None, nplm=None, precision=L.SWG_FP64):
         r = _f64(r, (-1, 3))
@@ -205,6 +222,26 @@ class NBodySystem:
 
     def step(self, nsteps: int = 1):
         self.ctx.check("swg_system_step", self.ctx.lib.swg_system_step(self.h, int(nsteps)))
+
+    def set_state(self, rh=None, vh=None, trh=None, tvh=None):
+        """Upload positions / heliocentric velocities (host arrays) without resetting step flags."""
+        self.ctx.check("swg_system_set_state", self.ctx.lib.swg_system_set_state(
+            self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
+
+    def get_state_async(self, rh=None, vh=None, trh=None, tvh=None):
+        self.ctx.check("swg_system_get_state_async", self.ctx.lib.swg_system_get_state_async(
+            self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
+
+    PROFILE_CLASSES = ("kick_pl", "kick_tp", "drift", "encounter_level0", "symba_recursion")
+
+    def profile(self, enable: bool = True):
+        self.ctx.check("swg_system_profile", self.ctx.lib.swg_system_profile(self.h, int(bool(enable))))
+
+    def profile_read(self):
+        out = np.zeros(10)
+        self.ctx.check("swg_system_profile_read", self.ctx.lib.swg_system_profile_read(self.h, _ptr(out)))
+        return {k: {"launches": int(out[2 * i]), "ms": float(out[2 * i + 1])}
+                for i, k in enumerate(self.PROFILE_CLASSES)}
 
     def get_pl(self):
         rh = np.zeros((self.npl, 3))

@@ -6,6 +6,7 @@
 // device pointers are used directly.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -113,6 +114,8 @@ int swg_destroy(swg_ctx *c) {
     DevBuf *eb[] = {&c->enc.raw, &c->enc.sort, &c->enc.counters};
     for (DevBuf *b : eb)
         if (b->ptr) cudaFree(b->ptr);
+    for (void *e : c->events)
+        if (e) cudaEventDestroy((cudaEvent_t)e);
     cudaStreamDestroy(c->stream);
     delete c;
     return SWG_OK;
@@ -283,6 +286,95 @@ int swg_encounter_check_all_pltp(swg_ctx *c, int mode, int32_t npl, int32_t ntp,
                                  int32_t *lvdotr, int mem) {
     return enc_common(c, 2, mode, npl, rpl, vpl, renc, ntp, rtp, vtp, nullptr, dt, cap, nenc, index1, index2,
                       lvdotr, mem);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- measurement helpers
+namespace {
+__global__ void k_probe_ffma(float *out, int iters, float seed) {
+    float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f, a4 = a0 + 4.f, a5 = a0 + 5.f,
+          a6 = a0 + 6.f, a7 = a0 + 7.f;
+    const float m = 0.9999999f, b = 1e-7f;
+    for (int k = 0; k < iters; k++) {
+        a0 = fmaf(a0, m, b);
+        a1 = fmaf(a1, m, b);
+        a2 = fmaf(a2, m, b);
+        a3 = fmaf(a3, m, b);
+        a4 = fmaf(a4, m, b);
+        a5 = fmaf(a5, m, b);
+        a6 = fmaf(a6, m, b);
+        a7 = fmaf(a7, m, b);
+    }
+    const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 12345.678f) out[0] = s;  // keeps the chain live
+}
+__global__ void k_probe_dfma(double *out, int iters, double seed) {
+    double a0 = seed + threadIdx.x, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;
+    const double m = 0.9999999, b = 1e-7;
+    for (int k = 0; k < iters; k++) {
+        a0 = fma(a0, m, b);
+        a1 = fma(a1, m, b);
+        a2 = fma(a2, m, b);
+        a3 = fma(a3, m, b);
+    }
+    const double s = a0 + a1 + a2 + a3;
+    if (s == 12345.678) out[0] = s;
+}
+}  // namespace
+
+extern "C" {
+
+int swg_flush_l2(swg_ctx *c, int64_t bytes) {
+    if (!c || bytes <= 0) return SWG_ERR_ARG;
+    void *p;
+    SWG_TRY(ensure_slot(c, 20, (size_t)bytes, &p));
+    return cuda_status(c, cudaMemsetAsync(p, (int)(c->launches & 0xff), (size_t)bytes, c->stream), "flush");
+}
+
+int swg_event_record(swg_ctx *c, int slot) {
+    if (!c || slot < 0 || slot >= 16) return SWG_ERR_ARG;
+    if (!c->events[slot]) SWG_TRY(cuda_status(c, cudaEventCreate((cudaEvent_t *)&c->events[slot]), "event"));
+    return cuda_status(c, cudaEventRecord((cudaEvent_t)c->events[slot], c->stream), "event");
+}
+
+int swg_event_elapsed(swg_ctx *c, int a, int b, double *ms) {
+    if (!c || !ms || a < 0 || b < 0 || a >= 16 || b >= 16 || !c->events[a] || !c->events[b]) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaEventSynchronize((cudaEvent_t)c->events[b]), "event"));
+    float f = 0.f;
+    SWG_TRY(cuda_status(c, cudaEventElapsedTime(&f, (cudaEvent_t)c->events[a], (cudaEvent_t)c->events[b]), "event"));
+    *ms = f;
+    return SWG_OK;
+}
+
+int swg_probe_peak(swg_ctx *c, int kind, double *tflops) {
+    if (!c || !tflops || (kind != 0 && kind != 1)) return SWG_ERR_ARG;
+    void *p;
+    SWG_TRY(ensure_slot(c, 21, 64, &p));
+    const int blocks = (c->num_sms > 0 ? c->num_sms : 152) * 8, threads = 256;
+    const int iters = kind == 0 ? 1 << 16 : 1 << 11;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 0.0;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(e0, c->stream);
+        if (kind == 0)
+            k_probe_ffma<<<blocks, threads, 0, c->stream>>>((float *)p, iters, 1.0f);
+        else
+            k_probe_dfma<<<blocks, threads, 0, c->stream>>>((double *)p, iters, 1.0);
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * iters * (kind == 0 ? 8 : 4) * (double)blocks * threads;
+        if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->launches += 4;
+    *tflops = best;
+    return launch_status(c, "probe");
 }
 
 }  // extern "C"

@@ -56,6 +56,7 @@ struct swg_ctx {
     // and kernel scratch); each slot is grow-only.
     swg::DevBuf slot[24];
     swg::EncWork enc;
+    void *events[16] = {nullptr};  // measurement events (cudaEvent_t), created on first use
 };
 
 namespace swg {

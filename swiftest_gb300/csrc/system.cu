@@ -53,7 +53,40 @@ struct swg_system {
     DevBuf kick_scratch, pair_scratch, flags, red;
     int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail
     int64_t stats[5] = {0, 0, 0, 0, 0};
+    // optional CUDA-event profile per kernel class (see PROF_* below)
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_pool;
+    std::vector<int> prof_cls;  // class of record k (events 2k, 2k+1)
+    size_t prof_n = 0;
 };
+
+// kernel classes of the step profile
+enum { PROF_KICK_PL = 0, PROF_KICK_TP = 1, PROF_DRIFT = 2, PROF_ENC0 = 3, PROF_RECUR = 4, PROF_NCLS = 5 };
+
+namespace {
+int prof_begin(swg_system *s, int cls) {
+    if (!s->prof_on) return -1;
+    const size_t k = s->prof_n++;
+    while (s->prof_pool.size() < 2 * s->prof_n) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return -1;
+        s->prof_pool.push_back(e);
+    }
+    if (s->prof_cls.size() < s->prof_n) s->prof_cls.resize(s->prof_n);
+    s->prof_cls[k] = cls;
+    cudaEventRecord(s->prof_pool[2 * k], s->c->stream);
+    return (int)k;
+}
+void prof_end(swg_system *s, int k) {
+    if (k >= 0) cudaEventRecord(s->prof_pool[2 * k + 1], s->c->stream);
+}
+struct ProfScope {
+    swg_system *s;
+    int k;
+    ProfScope(swg_system *s_, int cls) : s(s_), k(prof_begin(s_, cls)) {}
+    ~ProfScope() { prof_end(s, k); }
+};
+}  // namespace
 
 namespace {
 
@@ -376,6 +409,23 @@ __global__ void k_list_check(int64_t npp, int32_t *pp, int64_t ppcap, int64_t np
     if (threadIdx.x == 0) flag[0] = s_any;
 }
 
+// x**(-1.5) of the shell kick (symba_kick.f90:204,307): sqrt(x) and x*sqrt(x) as
+// double-double pairs (Dekker's error-free transformations with fma residuals),
+// then one Newton step on the reciprocal.  Within half an ulp except in rare
+// near-tie cases, and the same bits as the host evaluation of the same sequence.
+__device__ __forceinline__ double pow_m1p5(double x) {
+    if (!(x > 0.0) || isinf(x)) return pow(x, -1.5);
+    const double s = sqrt(x);
+    const double rs = fma(-s, s, x);
+    const double ds = rs / (2.0 * s);
+    const double p = x * s;
+    const double ep = fma(x, s, -p);
+    const double ql = ep + x * ds;
+    const double y0 = 1.0 / p;
+    const double err = fma(-y0, p, 1.0) - y0 * ql;
+    return fma(y0, err, y0);
+}
+
 // powi: square-and-multiply (gfortran's real**integer)
 __device__ __forceinline__ double d_powi(double x, int m) {
     unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
@@ -429,7 +479,7 @@ __device__ void d_kick_list_plpl(int64_t nenc, int32_t *l, int64_t cap, int npl,
             const double ris = sqrt(ri);
             const double r = sqrt(r2);
             const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            fac = pow(r2, -1.5) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         } else {
             const double ir3 = 1.0 / (r2 * sqrt(r2));
             fac = ir3;
@@ -495,7 +545,7 @@ __device__ void d_kick_list_pltp(int64_t nenc, int32_t *l, int64_t cap, int npl,
             const double ris = sqrt(ri);
             const double r = sqrt(r2);
             const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            fac = pow(r2, -1.5) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         } else {
             const double ir3 = 1.0 / (r2 * sqrt(r2));
             fac = ir3;
@@ -816,7 +866,10 @@ int accel_int_pl(swg_system *s, int acc_is_zero) {
 int kick_vb_pl(swg_system *s, double dt, int lbeg) {
     swg_ctx *c = s->c;
     if (s->npl == 0) return SWG_OK;
-    SWG_TRY(accel_int_pl(s, 1));
+    {
+        ProfScope ps(s, PROF_KICK_PL);
+        SWG_TRY(accel_int_pl(s, 1));
+    }
     if (s->integrator == SWG_SYMBA && s->plpl_n > 0) {
         double *scr;
         SWG_TRY(pair_scratch(s, &scr));
@@ -834,6 +887,7 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
     if (s->ntp == 0) return SWG_OK;
     const double *rp = lbeg ? s->rbeg : s->rend;
     if (s->npl > 0) {
+        ProfScope ps(s, PROF_KICK_TP);
         if (s->precision == SWG_MIXED) {
             const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
             SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, nch)));
@@ -881,12 +935,14 @@ int vb2vh_pl(swg_system *s) {
 int drift_pl(swg_system *s, double dt) {
     if (s->npl == 0) return SWG_OK;
     const int32_t *lev = s->integrator == SWG_SYMBA ? s->levelg : nullptr;
+    ProfScope ps(s, PROF_DRIFT);
     return drift_masked(s->c, s->GMcb, s->rh, s->vb, s->npl, lev, s->irec, dt, s->status, nullptr);
 }
 int drift_tp(swg_system *s, double dt) {
     if (s->ntp == 0) return SWG_OK;
     const int32_t *lev = s->integrator == SWG_SYMBA ? s->tlevelg : nullptr;
     double *v = s->integrator == SWG_WHM ? s->tvh : s->tvb;
+    ProfScope ps(s, PROF_DRIFT);
     return drift_masked(s->c, s->GMcb, s->trh, v, s->ntp, lev, s->irec, dt, s->tstatus, nullptr);
 }
 
@@ -1132,6 +1188,7 @@ int symba_recur(swg_system *s, int ireci) {
     const int nloops = ireci == 0 ? 1 : NTENC;
     int32_t *dflag = (int32_t *)s->flags.ptr;
     for (int j = 1; j <= nloops; j++) {
+        ProfScope ps1(s, PROF_RECUR);
         k_list_check<<<1, 256, 0, c->stream>>>(s->plpl_n, s->plpl_l, s->plpl_cap, s->pltp_n, s->pltp_l, s->pltp_cap,
                                                s->rh, s->vb, s->trh, s->tvb, s->rhill, s->radius, s->rhscale, irecp,
                                                dtl, s->levelg, s->levelm, s->tlevelg, s->tlevelm, dflag,
@@ -1140,12 +1197,15 @@ int symba_recur(swg_system *s, int ireci) {
         SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->h_flags, dflag, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream),
                             "flag"));
         SWG_TRY(kick_lists(s, dth, irecp, ireci != 0));
+        prof_end(s, ps1.k);
+        ps1.k = -1;
         SWG_TRY(drift_pl(s, dtl));
         SWG_TRY(drift_tp(s, dtl));
         SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
         const int lencounter = s->h_flags[0];
         if (lencounter) SWG_TRY(symba_recur(s, irecp));
         s->irec = ireci;
+        ProfScope ps2(s, PROF_RECUR);
         SWG_TRY(kick_lists(s, dth, irecp, ireci != 0));
         const int64_t nmax = std::max<int64_t>(std::max<int64_t>(s->npl, s->ntp), std::max(s->plpl_n, s->pltp_n));
         k_set_recur_levels<<<grid_for(nmax, 256), 256, 0, c->stream>>>(s->npl, s->ntp, s->plpl_n, s->plpl_cap,
@@ -1193,7 +1253,10 @@ int symba_step(swg_system *s, double dt) {
     s->lfirst_tp = s->lfirstkick;
     s->lfirst_pl = s->lfirstkick;
     int lany = 0;
-    SWG_TRY(symba_level0(s, dt, &lany));
+    {
+        ProfScope ps(s, PROF_ENC0);
+        SWG_TRY(symba_level0(s, dt, &lany));
+    }
     if (lany) {
         s->stats[0]++;
         // list-sized byte scratch for kick/check flags lives in the sort buffer
@@ -1265,6 +1328,7 @@ int swg_system_destroy(swg_system *s) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);
+    for (cudaEvent_t e : s->prof_pool) cudaEventDestroy(e);
     delete s;
     return SWG_OK;
 }
@@ -1457,6 +1521,49 @@ int swg_system_plpl_list(swg_system *s, int64_t cap, int64_t *n, int32_t *i1, in
 int swg_system_pltp_list(swg_system *s, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2) {
     if (!s || !n) return SWG_ERR_ARG;
     return copy_list(s, s->pltp_l, s->pltp_cap, s->pltp_n, cap, n, i1, i2);
+}
+
+int swg_system_set_state(swg_system *s, const double *rh, const double *vh, const double *trh, const double *tvh) {
+    if (!s || !s->initialized) return SWG_ERR_STATE;
+    swg_ctx *c = s->c;
+    const size_t n = s->npl, m = s->ntp;
+    if (n && rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->rh, rh, 24 * n, cudaMemcpyHostToDevice, c->stream), "state"));
+    if (n && vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->vh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "state"));
+    if (m && trh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->trh, trh, 24 * m, cudaMemcpyHostToDevice, c->stream), "state"));
+    if (m && tvh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->tvh, tvh, 24 * m, cudaMemcpyHostToDevice, c->stream), "state"));
+    return SWG_OK;
+}
+
+int swg_system_get_state_async(swg_system *s, double *rh, double *vh, double *trh, double *tvh) {
+    if (!s) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const size_t n = s->npl, m = s->ntp;
+    if (n && rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(rh, s->rh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "state"));
+    if (n && vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(vh, s->vh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "state"));
+    if (m && trh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(trh, s->trh, 24 * m, cudaMemcpyDeviceToHost, c->stream), "state"));
+    if (m && tvh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(tvh, s->tvh, 24 * m, cudaMemcpyDeviceToHost, c->stream), "state"));
+    return SWG_OK;
+}
+
+int swg_system_profile(swg_system *s, int enable) {
+    if (!s) return SWG_ERR_ARG;
+    s->prof_on = enable != 0;
+    s->prof_n = 0;
+    return SWG_OK;
+}
+
+int swg_system_profile_read(swg_system *s, double *out) {
+    if (!s || !out) return SWG_ERR_ARG;
+    for (int k = 0; k < 2 * PROF_NCLS; k++) out[k] = 0.0;
+    SWG_TRY(cuda_status(s->c, cudaStreamSynchronize(s->c->stream), "profile"));
+    for (size_t k = 0; k < s->prof_n; k++) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->prof_pool[2 * k], s->prof_pool[2 * k + 1]) != cudaSuccess) continue;
+        out[2 * s->prof_cls[k]] += 1.0;
+        out[2 * s->prof_cls[k] + 1] += ms;
+    }
+    s->prof_n = 0;
+    return SWG_OK;
 }
 
 }  // extern "C"
