@@ -27,151 +27,8 @@
 
 namespace swg {
 
-constexpr int KT = 128;       // bodies per block and partners per shared tile (FP64)
 constexpr int MT = 64;        // partners per FP32 partial (mixed)
 constexpr int MBLOCK = 128;   // threads per block (mixed)
-
-// ------------------------------------------------------------------ FP64 exact
-template <bool RAD, int MODE>
-__global__ void __launch_bounds__(KT) k_kick_plpl_fp64(int npl, int nplm, const double *__restrict__ r,
-                                                      const double *__restrict__ Gm,
-                                                      const double *__restrict__ R, double *__restrict__ acc,
-                                                      int acc_is_zero) {
-    __shared__ double sx[KT], sy[KT], sz[KT], sg[KT], sr[KT];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < npl;
-    double xi = 0, yi = 0, zi = 0, Ri = 0;
-    if (active) {
-        xi = r[3 * i + 0];
-        yi = r[3 * i + 1];
-        zi = r[3 * i + 2];
-        if (RAD) Ri = R[i];
-    }
-    double ax = 0, ay = 0, az = 0;  // DIRECT: running acc ; SPLIT: ahi
-    double bx = 0, by = 0, bz = 0;  // SPLIT: ahj
-    if (MODE == KICK_DIRECT && active && !acc_is_zero) {
-        ax = acc[3 * i + 0];
-        ay = acc[3 * i + 1];
-        az = acc[3 * i + 2];
-    }
-    // partner range: DIRECT i<nplm: all j != i; i>=nplm: j<nplm.
-    // SPLIT: j>i (ahi, only when i<nplm) and j<min(i,nplm) (ahj).
-    const int jend = (i < nplm) ? npl : nplm;
-    // the block walks tiles up to the largest jend of its threads
-    const int blk_jend = (blockIdx.x * blockDim.x < (unsigned)nplm) ? npl : nplm;
-    for (int j0 = 0; j0 < blk_jend; j0 += KT) {
-        const int jl = j0 + threadIdx.x;
-        if (jl < npl) {
-            sx[threadIdx.x] = r[3 * jl + 0];
-            sy[threadIdx.x] = r[3 * jl + 1];
-            sz[threadIdx.x] = r[3 * jl + 2];
-            sg[threadIdx.x] = Gm[jl];
-            if (RAD) sr[threadIdx.x] = R[jl];
-        }
-        __syncthreads();
-        if (active) {
-            const int nt = min(KT, jend - j0);
-            for (int jj = 0; jj < nt; jj++) {
-                const int j = j0 + jj;
-                if (j == i) continue;
-                const double rx = sx[jj] - xi;
-                const double ry = sy[jj] - yi;
-                const double rz = sz[jj] - zi;
-                const double rji2 = rx * rx + ry * ry + rz * rz;
-                if (RAD) {
-                    const double rs = Ri + sr[jj];
-                    if (!(rji2 > rs * rs)) continue;
-                }
-                if (MODE == KICK_DIRECT) {
-                    const double fac = sg[jj] / (rji2 * sqrt(rji2));
-                    ax = ax + fac * rx;
-                    ay = ay + fac * ry;
-                    az = az + fac * rz;
-                } else {
-                    const double irij3 = 1.0 / (rji2 * sqrt(rji2));
-                    const double fac = sg[jj] * irij3;
-                    if (j > i) {
-                        ax = ax + fac * rx;
-                        ay = ay + fac * ry;
-                        az = az + fac * rz;
-                    } else {
-                        bx = bx + fac * rx;
-                        by = by + fac * ry;
-                        bz = bz + fac * rz;
-                    }
-                }
-            }
-        }
-        __syncthreads();
-    }
-    if (!active) return;
-    if (MODE == KICK_DIRECT) {
-        acc[3 * i + 0] = ax;
-        acc[3 * i + 1] = ay;
-        acc[3 * i + 2] = az;
-    } else {
-        double a0 = acc_is_zero ? 0.0 : acc[3 * i + 0];
-        double a1 = acc_is_zero ? 0.0 : acc[3 * i + 1];
-        double a2 = acc_is_zero ? 0.0 : acc[3 * i + 2];
-        acc[3 * i + 0] = a0 + ax + bx;
-        acc[3 * i + 1] = a1 + ay + by;
-        acc[3 * i + 2] = a2 + az + bz;
-    }
-}
-
-// pl -> tp, swiftest_kick_getacch_int_all_tp (:374-415): acc -= Gm_j/(r^2 sqrt r^2) (r_tp - r_j)
-__global__ void __launch_bounds__(KT) k_kick_tp_fp64(int ntp, int npl, const double *__restrict__ rtp,
-                                                    const double *__restrict__ rpl, const double *__restrict__ Gm,
-                                                    const int32_t *__restrict__ lmask, double *__restrict__ acc,
-                                                    int acc_is_zero) {
-    __shared__ double sx[KT], sy[KT], sz[KT], sg[KT];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < ntp && lmask[i] != 0;
-    double xi = 0, yi = 0, zi = 0, ax = 0, ay = 0, az = 0;
-    if (active) {
-        xi = rtp[3 * i + 0];
-        yi = rtp[3 * i + 1];
-        zi = rtp[3 * i + 2];
-        if (!acc_is_zero) {
-            ax = acc[3 * i + 0];
-            ay = acc[3 * i + 1];
-            az = acc[3 * i + 2];
-        }
-    }
-    for (int j0 = 0; j0 < npl; j0 += KT) {
-        const int jl = j0 + threadIdx.x;
-        if (jl < npl) {
-            sx[threadIdx.x] = rpl[3 * jl + 0];
-            sy[threadIdx.x] = rpl[3 * jl + 1];
-            sz[threadIdx.x] = rpl[3 * jl + 2];
-            sg[threadIdx.x] = Gm[jl];
-        }
-        __syncthreads();
-        if (active) {
-            const int nt = min(KT, npl - j0);
-            for (int jj = 0; jj < nt; jj++) {
-                const double rx = xi - sx[jj];
-                const double ry = yi - sy[jj];
-                const double rz = zi - sz[jj];
-                const double rji2 = rx * rx + ry * ry + rz * rz;
-                const double fac = sg[jj] / (rji2 * sqrt(rji2));
-                ax = ax - fac * rx;
-                ay = ay - fac * ry;
-                az = az - fac * rz;
-            }
-        }
-        __syncthreads();
-    }
-    if (active) {
-        acc[3 * i + 0] = ax;
-        acc[3 * i + 1] = ay;
-        acc[3 * i + 2] = az;
-    } else if (i < ntp && acc_is_zero) {
-        acc[3 * i + 0] = 0.0;
-        acc[3 * i + 1] = 0.0;
-        acc[3 * i + 2] = 0.0;
-    }
-}
 
 // ------------------------------------------------------------------ mixed
 struct FF {
@@ -444,33 +301,6 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
                                                                    counters);
     c->launches++;
     return launch_status(c, "kick_mixed");
-}
-
-int kick_plpl_fp64(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const double *Gm, const double *R,
-                   double *acc, int mode, int acc_is_zero) {
-    if (npl <= 0) return SWG_OK;
-    const int grid = div_up(npl, KT);
-    if (mode == KICK_DIRECT) {
-        if (R)
-            k_kick_plpl_fp64<true, KICK_DIRECT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
-        else
-            k_kick_plpl_fp64<false, KICK_DIRECT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
-    } else {
-        if (R)
-            k_kick_plpl_fp64<true, KICK_SPLIT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
-        else
-            k_kick_plpl_fp64<false, KICK_SPLIT><<<grid, KT, 0, c->stream>>>(npl, nplm, r, Gm, R, acc, acc_is_zero);
-    }
-    c->launches++;
-    return launch_status(c, "kick_plpl_fp64");
-}
-
-int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const double *rpl, const double *Gm,
-                 const int32_t *lmask, double *acc, int acc_is_zero) {
-    if (ntp <= 0) return SWG_OK;
-    k_kick_tp_fp64<<<div_up(ntp, KT), KT, 0, c->stream>>>(ntp, npl, rtp, rpl, Gm, lmask, acc, acc_is_zero);
-    c->launches++;
-    return launch_status(c, "kick_tp_fp64");
 }
 
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <vector>
 
+#include "drift_impl.cuh"
 #include "swg_internal.cuh"
 
 using namespace swg;
@@ -48,10 +49,12 @@ struct swg_system {
     // encounter lists (SyMBA): i1, i2, lvdotr, status, level
     int32_t *plpl_l = nullptr, *pltp_l = nullptr;  // 5 * cap int32 each
     int64_t plpl_n = 0, pltp_n = 0, plpl_cap = 0, pltp_cap = 0;
-    EncWork enc;
+    EncWork enc, enc2;
     // scratch
     DevBuf kick_scratch, pair_scratch, flags, red;
-    int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail
+    int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail, [2] recursion status, [3] deepest level
+    int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr;
+    DevBuf rec_scratch;
     int64_t stats[5] = {0, 0, 0, 0, 0};
     // optional CUDA-event profile per kernel class (see PROF_* below)
     bool prof_on = false;
@@ -105,47 +108,91 @@ int dalloc(swg_ctx *c, T **p, size_t n) {
 }
 
 // ---------------------------------------------------------------- small kernels
-// helio_drift_linear_pl (helio_drift.f90:129-163): pt = sum(Gm*vb, mask)/GMcb ; rh += pt*dt
-__global__ void k_lindrift_pl(int npl, const double *__restrict__ Gm, const double *__restrict__ vb,
-                              const int32_t *__restrict__ lmask, double GMcb, double *rh, double dt, double *dcb,
-                              int slot, int exact) {
-    __shared__ double s_pt[3];
-    __shared__ double s_red[3][256];
-    if (exact) {
-        if (threadIdx.x == 0) {
-            double px = 0.0, py = 0.0, pz = 0.0;
-            for (int i = 0; i < npl; i++) {
-                if (!lmask[i]) continue;
-                px = px + Gm[i] * vb[3 * i + 0];
-                py = py + Gm[i] * vb[3 * i + 1];
-                pz = pz + Gm[i] * vb[3 * i + 2];
+// Ordered sums of the reference's O(N) serial loops.  The terms are formed by the
+// whole block into shared memory, chunk by chunk; thread 0 then adds them one at a
+// time in the reference's index order (exact == 1), which reproduces its rounding.
+// With exact == 0 the block reduces each chunk as a tree (fixed order, faster).
+constexpr int RB = 1024;  // threads of the reduction kernels
+
+struct Sum3 {
+    double x, y, z;
+};
+
+// Sum over i of sign*term(i) for i = 0..n-1 (reverse: n-1..0); term components are
+// written by term_fn into the chunk arrays (with a 0/1 mask).
+template <class TermFn>
+__device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, double sign) {
+    __shared__ double cx[RB], cy[RB], cz[RB];
+    __shared__ unsigned char cm[RB];
+    __shared__ double rx[RB / 32], ry[RB / 32], rz[RB / 32];
+    __shared__ Sum3 acc;
+    if (threadIdx.x == 0) acc = {0.0, 0.0, 0.0};
+    __syncthreads();
+    for (int c0 = 0; c0 < n; c0 += RB) {
+        const int k = threadIdx.x;
+        const int idx = reverse ? n - 1 - (c0 + k) : c0 + k;
+        double tx = 0, ty = 0, tz = 0;
+        unsigned char m = 0;
+        if (c0 + k < n) m = term_fn(idx, tx, ty, tz);
+        const int cnt = min(RB, n - c0);
+        if (exact) {
+            cx[k] = tx;
+            cy[k] = ty;
+            cz[k] = tz;
+            cm[k] = m;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double ax = acc.x, ay = acc.y, az = acc.z;
+                for (int q = 0; q < cnt; q++) {
+                    if (!cm[q]) continue;
+                    ax = ax + sign * cx[q];
+                    ay = ay + sign * cy[q];
+                    az = az + sign * cz[q];
+                }
+                acc = {ax, ay, az};
             }
-            s_pt[0] = px / GMcb;
-            s_pt[1] = py / GMcb;
-            s_pt[2] = pz / GMcb;
-        }
-    } else {
-        double px = 0.0, py = 0.0, pz = 0.0;
-        for (int i = threadIdx.x; i < npl; i += blockDim.x) {
-            if (!lmask[i]) continue;
-            px += Gm[i] * vb[3 * i + 0];
-            py += Gm[i] * vb[3 * i + 1];
-            pz += Gm[i] * vb[3 * i + 2];
-        }
-        s_red[0][threadIdx.x] = px;
-        s_red[1][threadIdx.x] = py;
-        s_red[2][threadIdx.x] = pz;
-        __syncthreads();
-        for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-            if (threadIdx.x < (unsigned)off)
-                for (int d = 0; d < 3; d++) s_red[d][threadIdx.x] += s_red[d][threadIdx.x + off];
+            __syncthreads();
+        } else {
+            if (!m) tx = ty = tz = 0.0;
+            for (int off = 16; off > 0; off >>= 1) {
+                tx += __shfl_down_sync(0xffffffffu, tx, off);
+                ty += __shfl_down_sync(0xffffffffu, ty, off);
+                tz += __shfl_down_sync(0xffffffffu, tz, off);
+            }
+            if ((k & 31) == 0) {
+                rx[k >> 5] = tx;
+                ry[k >> 5] = ty;
+                rz[k >> 5] = tz;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double ax = 0, ay = 0, az = 0;
+                for (int w = 0; w < RB / 32; w++) {
+                    ax += rx[w];
+                    ay += ry[w];
+                    az += rz[w];
+                }
+                acc = {acc.x + sign * ax, acc.y + sign * ay, acc.z + sign * az};
+            }
             __syncthreads();
         }
-        if (threadIdx.x == 0)
-            for (int d = 0; d < 3; d++) s_pt[d] = s_red[d][0] / GMcb;
     }
-    __syncthreads();
-    const double ptx = s_pt[0], pty = s_pt[1], ptz = s_pt[2];
+    return acc;
+}
+
+// helio_drift_linear_pl (helio_drift.f90:129-163): pt = sum(Gm*vb, mask)/GMcb ; rh += pt*dt
+__global__ void __launch_bounds__(RB) k_lindrift_pl(int npl, const double *__restrict__ Gm,
+                                                    const double *__restrict__ vb, const int32_t *__restrict__ lmask,
+                                                    double GMcb, double *rh, double dt, double *dcb, int slot,
+                                                    int exact) {
+    auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = Gm[i] * vb[3 * i + 0];
+        y = Gm[i] * vb[3 * i + 1];
+        z = Gm[i] * vb[3 * i + 2];
+        return lmask[i] != 0;
+    };
+    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, 1.0);
+    const double ptx = s.x / GMcb, pty = s.y / GMcb, ptz = s.z / GMcb;
     for (int i = threadIdx.x; i < npl; i += blockDim.x) {
         if (!lmask[i]) continue;
         rh[3 * i + 0] = rh[3 * i + 0] + ptx * dt;
@@ -160,53 +207,57 @@ __global__ void k_lindrift_pl(int npl, const double *__restrict__ Gm, const doub
 }
 
 // swiftest_util_coord_vh2vb_pl (swiftest_util.f90:424-456)
-__global__ void k_vh2vb_pl(int npl, const double *__restrict__ Gm, const double *__restrict__ vh, double *vb,
-                           double GMcb, double *dcb) {
-    __shared__ double s_cb[3];
+__global__ void __launch_bounds__(RB) k_vh2vb_pl(int npl, const double *__restrict__ Gm,
+                                                 const double *__restrict__ vh, double *vb, double GMcb, double *dcb,
+                                                 int exact) {
+    auto gm = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = Gm[i];
+        y = z = 0.0;
+        return 1;
+    };
+    const Sum3 g = ordered_sum3(npl, false, exact != 0, gm, 1.0);
+    const double Gmtot = GMcb + g.x;
+    auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = Gm[i] * vh[3 * i + 0];
+        y = Gm[i] * vh[3 * i + 1];
+        z = Gm[i] * vh[3 * i + 2];
+        return 1;
+    };
+    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, -1.0);
+    const double cx = s.x / Gmtot, cy = s.y / Gmtot, cz = s.z / Gmtot;
     if (threadIdx.x == 0) {
-        double sum = 0.0;
-        for (int i = 0; i < npl; i++) sum = sum + Gm[i];
-        const double Gmtot = GMcb + sum;
-        double cx = 0.0, cy = 0.0, cz = 0.0;
-        for (int i = 0; i < npl; i++) {
-            cx = cx - Gm[i] * vh[3 * i + 0];
-            cy = cy - Gm[i] * vh[3 * i + 1];
-            cz = cz - Gm[i] * vh[3 * i + 2];
-        }
-        s_cb[0] = cx / Gmtot;
-        s_cb[1] = cy / Gmtot;
-        s_cb[2] = cz / Gmtot;
-        dcb[CB_VB + 0] = s_cb[0];
-        dcb[CB_VB + 1] = s_cb[1];
-        dcb[CB_VB + 2] = s_cb[2];
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < npl; i += blockDim.x)
-        for (int d = 0; d < 3; d++) vb[3 * i + d] = vh[3 * i + d] + s_cb[d];
-}
-
-// swiftest_util_coord_vb2vh_pl (swiftest_util.f90:363-392), reverse-order sum
-__global__ void k_vb2vh_pl(int npl, const double *__restrict__ Gm, const double *__restrict__ vb,
-                           const int32_t *__restrict__ status, double *vh, double GMcb, double *dcb) {
-    __shared__ double s_cb[3];
-    if (threadIdx.x == 0) {
-        double cx = 0.0, cy = 0.0, cz = 0.0;
-        for (int i = npl - 1; i >= 0; i--) {
-            if (status[i] == ST_INACTIVE) continue;
-            cx = cx - Gm[i] * vb[3 * i + 0] / GMcb;
-            cy = cy - Gm[i] * vb[3 * i + 1] / GMcb;
-            cz = cz - Gm[i] * vb[3 * i + 2] / GMcb;
-        }
-        s_cb[0] = cx;
-        s_cb[1] = cy;
-        s_cb[2] = cz;
         dcb[CB_VB + 0] = cx;
         dcb[CB_VB + 1] = cy;
         dcb[CB_VB + 2] = cz;
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < npl; i += blockDim.x)
-        for (int d = 0; d < 3; d++) vh[3 * i + d] = vb[3 * i + d] - s_cb[d];
+    for (int i = threadIdx.x; i < npl; i += blockDim.x) {
+        vb[3 * i + 0] = vh[3 * i + 0] + cx;
+        vb[3 * i + 1] = vh[3 * i + 1] + cy;
+        vb[3 * i + 2] = vh[3 * i + 2] + cz;
+    }
+}
+
+// swiftest_util_coord_vb2vh_pl (swiftest_util.f90:363-392), reverse-order sum
+__global__ void __launch_bounds__(RB) k_vb2vh_pl(int npl, const double *__restrict__ Gm,
+                                                 const double *__restrict__ vb, const int32_t *__restrict__ status,
+                                                 double *vh, double GMcb, double *dcb, int exact) {
+    auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = Gm[i] * vb[3 * i + 0] / GMcb;
+        y = Gm[i] * vb[3 * i + 1] / GMcb;
+        z = Gm[i] * vb[3 * i + 2] / GMcb;
+        return status[i] != ST_INACTIVE;
+    };
+    const Sum3 s = ordered_sum3(npl, true, exact != 0, term, -1.0);
+    if (threadIdx.x == 0) {
+        dcb[CB_VB + 0] = s.x;
+        dcb[CB_VB + 1] = s.y;
+        dcb[CB_VB + 2] = s.z;
+    }
+    for (int i = threadIdx.x; i < npl; i += blockDim.x) {
+        vh[3 * i + 0] = vb[3 * i + 0] - s.x;
+        vh[3 * i + 1] = vb[3 * i + 1] - s.y;
+        vh[3 * i + 2] = vb[3 * i + 2] - s.z;
+    }
 }
 
 // test particles: mode 0 vh2vb(vbcb=-pt) ; 1 vb2vh(vbcb=-pt) ; 2 lindrift rh += pt*dt ;
@@ -311,6 +362,83 @@ __global__ void k_level0_mark(int64_t n, int32_t *l, int64_t cap, int tp, int32_
     }
 }
 
+// Sort a short raw pair list by (index1, index2), drop repeated pairs, and write it as a
+// SyMBA encounter list with status ACTIVE, level 0 and the level-0 body marks of
+// symba_encounter_check_pl / _tp (symba_encounter_check.f90:53-83, 267-290).  One block.
+constexpr int FIN_N = 4096;
+__global__ void __launch_bounds__(1024) k_list_finalize(int n, const int32_t *__restrict__ ri1,
+                                                        const int32_t *__restrict__ ri2,
+                                                        const int32_t *__restrict__ rlv, int32_t *l, int64_t cap,
+                                                        int tp, int32_t *levelg, int32_t *levelm, int32_t *cnt1,
+                                                        int32_t *tlevelg, int32_t *tlevelm, int32_t *cnt2,
+                                                        unsigned long long *nout) {
+    __shared__ unsigned long long key[FIN_N];
+    __shared__ int s_part[1024];
+    int npad = 1;
+    while (npad < n) npad <<= 1;
+    for (int t = threadIdx.x; t < npad; t += blockDim.x)
+        key[t] = t < n ? (((unsigned long long)(uint32_t)ri1[t] << 33) | ((unsigned long long)(uint32_t)ri2[t] << 1) |
+                          (unsigned long long)(rlv[t] != 0))
+                       : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= npad; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+                const int p = t ^ jj;
+                if (p > t) {
+                    const bool up = (t & k) == 0;
+                    const unsigned long long a = key[t], b = key[p];
+                    if (up ? a > b : a < b) {
+                        key[t] = b;
+                        key[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // each thread owns 4 consecutive entries; keep the first of each (index1, index2)
+    const int base = 4 * threadIdx.x;
+    int keep[4], cntk = 0;
+    for (int q = 0; q < 4; q++) {
+        const int t = base + q;
+        keep[q] = t < n && (t == 0 || (key[t] >> 1) != (key[t - 1] >> 1));
+        cntk += keep[q];
+    }
+    s_part[threadIdx.x] = cntk;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int v = threadIdx.x >= (unsigned)off ? s_part[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int o = s_part[threadIdx.x] - cntk;
+    for (int q = 0; q < 4; q++) {
+        if (!keep[q]) continue;
+        const unsigned long long kk = key[base + q];
+        const int i1 = (int)(kk >> 33), i2 = (int)((kk >> 1) & 0xffffffffull), lv = (int)(kk & 1ull);
+        l[o] = i1;
+        l[cap + o] = i2;
+        l[2 * cap + o] = lv;
+        l[3 * cap + o] = ST_ACTIVE;
+        l[4 * cap + o] = 0;
+        levelg[i1 - 1] = 0;
+        levelm[i1 - 1] = 0;
+        atomicAdd(&cnt1[i1 - 1], 1);
+        if (!tp) {
+            levelg[i2 - 1] = 0;
+            levelm[i2 - 1] = 0;
+            atomicAdd(&cnt1[i2 - 1], 1);
+        } else {
+            tlevelg[i2 - 1] = 0;
+            tlevelm[i2 - 1] = 0;
+            atomicAdd(&cnt2[i2 - 1], 1);
+        }
+        o++;
+    }
+    if (threadIdx.x == 1023) *nout = (unsigned long long)s_part[1023];
+}
+
 // encounter_check_one (encounter_check.f90:573-621)
 __device__ __forceinline__ void d_enc_one(double xr, double yr, double zr, double vxr, double vyr, double vzr,
                                           double renc, double dt, int &lenc, int &lvdotr) {
@@ -341,74 +469,6 @@ __device__ __forceinline__ void d_enc_one(double xr, double yr, double zr, doubl
     lenc = lvdotr && (r2min <= r2crit);
 }
 
-// symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), one block.
-// flag[0] |= any encounter at level irec.
-__global__ void k_list_check(int64_t npp, int32_t *pp, int64_t ppcap, int64_t npt, int32_t *pt, int64_t ptcap,
-                             const double *__restrict__ rh, const double *__restrict__ vb,
-                             const double *__restrict__ trh, const double *__restrict__ tvb,
-                             const double *__restrict__ rhill, const double *__restrict__ radius, double rhscale,
-                             int irec, double dt, int32_t *levelg, int32_t *levelm, int32_t *tlevelg,
-                             int32_t *tlevelm, int32_t *flag, uint8_t *lenc_scratch) {
-    __shared__ int s_any;
-    if (threadIdx.x == 0) s_any = 0;
-    __syncthreads();
-    // phase 1: tests (reads positions only)
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
-        const bool isp = k < npp;
-        const int64_t q = isp ? k : k - npp;
-        int32_t *l = isp ? pp : pt;
-        const int64_t cap = isp ? ppcap : ptcap;
-        int32_t *i1 = l, *i2 = l + cap, *lv = l + 2 * cap, *st = l + 3 * cap, *lev = l + 4 * cap;
-        uint8_t le_out = 0;
-        if (st[q] == ST_ACTIVE && lev[q] == irec - 1) {
-            const int i = i1[q] - 1, j = i2[q] - 1;
-            double xr[3], vr[3];
-            const double *rj = isp ? &rh[3 * j] : &trh[3 * j];
-            const double *vj = isp ? &vb[3 * j] : &tvb[3 * j];
-            for (int d = 0; d < 3; d++) {
-                xr[d] = rj[d] - rh[3 * i + d];
-                vr[d] = vj[d] - vb[3 * i + d];
-            }
-            const double renci = d_renc(rhill[i], rhscale, irec);
-            const double rcrit = isp ? renci + d_renc(rhill[j], rhscale, irec) : renci;
-            int le, lvd;
-            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
-            lv[q] = lvd;
-            if (le) {
-                const double rs = isp ? radius[i] + radius[j] : radius[i];
-                const double rlim2 = isp ? rs * rs : radius[i] * radius[i];
-                const double rji2 = xr[0] * xr[0] + xr[1] * xr[1] + xr[2] * xr[2];
-                le = rji2 > rlim2;
-            }
-            le_out = (uint8_t)le;
-        }
-        lenc_scratch[k] = le_out;
-    }
-    __syncthreads();
-    // phase 2: levels
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
-        if (!lenc_scratch[k]) continue;
-        s_any = 1;
-        const bool isp = k < npp;
-        const int64_t q = isp ? k : k - npp;
-        int32_t *l = isp ? pp : pt;
-        const int64_t cap = isp ? ppcap : ptcap;
-        const int i = l[q] - 1, j = l[cap + q] - 1;
-        levelg[i] = irec;
-        atomicMax(&levelm[i], irec);
-        if (isp) {
-            levelg[j] = irec;
-            atomicMax(&levelm[j], irec);
-        } else {
-            tlevelg[j] = irec;
-            atomicMax(&tlevelm[j], irec);
-        }
-        l[4 * cap + q] = irec;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) flag[0] = s_any;
-}
-
 // x**(-1.5) of the shell kick (symba_kick.f90:204,307): sqrt(x) and x*sqrt(x) as
 // double-double pairs (Dekker's error-free transformations with fma residuals),
 // then one Newton step on the reciprocal.  Within half an ulp except in rare
@@ -437,34 +497,110 @@ __device__ __forceinline__ double d_powi(double x, int m) {
     return m < 0 ? 1.0 / y : y;
 }
 
-// symba_kick_list_plpl (symba_kick.f90:126-232), serial in list order (one thread)
-__device__ void d_kick_list_plpl(int64_t nenc, int32_t *l, int64_t cap, int npl, const int32_t *status,
-                                 int32_t *lmask, const int32_t *levelg, const double *rh, double *vb, double *ah,
-                                 const double *Gm, const double *rhill, double rhscale, double dt, int irec, int sgn,
-                                 uint8_t *good) {
-    if (nenc == 0 || npl == 0) return;
-    for (int i = 0; i < npl; i++) lmask[i] = status[i] != ST_INACTIVE;
-    const int32_t *i1 = l, *i2 = l + cap, *st = l + 3 * cap;
+// Encounter lists live in one int32 allocation per kind: [i1 | i2 | lvdotr | status | level],
+// each `cap` long.
+struct RecArgs {
+    int npl, ntp;
+    int64_t npp, ppcap, npt, ptcap;
+    int32_t *pp, *pt;
+    double *rh, *vb, *ah, *trh, *tvb, *tah;
+    const double *Gm, *rhill, *radius;
+    int32_t *status, *tstatus, *levelg, *levelm, *tlevelg, *tlevelm;
+    double GMcb, rhscale, dt;
+    uint8_t *lenc, *good;           // list-sized byte scratch
+    int32_t *bpl, *btp;             // compact sets of bodies that appear in the lists
+    int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
+    int32_t *out;                   // [0] status, [1] deepest level reached
+};
+
+// symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), whole block.
+__device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any) {
+    const int64_t npp = a.npp, npt = a.npt;
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        const bool isp = k < npp;
+        const int64_t q = isp ? k : k - npp;
+        int32_t *l = isp ? a.pp : a.pt;
+        const int64_t cap = isp ? a.ppcap : a.ptcap;
+        int32_t *i1 = l, *i2 = l + cap, *lv = l + 2 * cap, *st = l + 3 * cap, *lev = l + 4 * cap;
+        uint8_t le_out = 0;
+        if (st[q] == ST_ACTIVE && lev[q] == irec - 1) {
+            const int i = i1[q] - 1, j = i2[q] - 1;
+            double xr[3], vr[3];
+            const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
+            const double *vj = isp ? &a.vb[3 * j] : &a.tvb[3 * j];
+            for (int d = 0; d < 3; d++) {
+                xr[d] = rj[d] - a.rh[3 * i + d];
+                vr[d] = vj[d] - a.vb[3 * i + d];
+            }
+            const double renci = d_renc(a.rhill[i], a.rhscale, irec);
+            const double rcrit = isp ? renci + d_renc(a.rhill[j], a.rhscale, irec) : renci;
+            int le, lvd;
+            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            lv[q] = lvd;
+            if (le) {
+                const double rs = isp ? a.radius[i] + a.radius[j] : a.radius[i];
+                const double rlim2 = isp ? rs * rs : a.radius[i] * a.radius[i];
+                const double rji2 = xr[0] * xr[0] + xr[1] * xr[1] + xr[2] * xr[2];
+                le = rji2 > rlim2;
+            }
+            le_out = (uint8_t)le;
+        }
+        a.lenc[k] = le_out;
+    }
+    __syncthreads();
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        if (!a.lenc[k]) continue;
+        *s_any = 1;
+        const bool isp = k < npp;
+        const int64_t q = isp ? k : k - npp;
+        int32_t *l = isp ? a.pp : a.pt;
+        const int64_t cap = isp ? a.ppcap : a.ptcap;
+        const int i = l[q] - 1, j = l[cap + q] - 1;
+        a.levelg[i] = irec;
+        atomicMax(&a.levelm[i], irec);
+        if (isp) {
+            a.levelg[j] = irec;
+            atomicMax(&a.levelm[j], irec);
+        } else {
+            a.tlevelg[j] = irec;
+            atomicMax(&a.tlevelm[j], irec);
+        }
+        l[4 * cap + q] = irec;
+    }
+    __syncthreads();
+}
+
+// symba_kick_list_plpl (symba_kick.f90:126-232), serial in list order (one thread).
+// The reference's lmask refresh at entry is kept by the step loop instead
+// (lmask == status /= INACTIVE at every point the recursion can reach).
+__device__ void d_kick_list_plpl(const RecArgs &a, double dt, int irec, int sgn) {
+    const int64_t nenc = a.npp;
+    if (nenc == 0 || a.npl == 0) return;
+    const int64_t cap = a.ppcap;
+    const int32_t *i1 = a.pp, *i2 = a.pp + cap, *st = a.pp + 3 * cap;
+    uint8_t *good = a.good;
     const int irm1 = irec - 1;
     const int irecl = sgn < 0 ? irec - 1 : irec;
     int64_t ngood = 0;
     for (int64_t k = 0; k < nenc; k++) {
         const int i = i1[k] - 1, j = i2[k] - 1;
-        good[k] = (st[k] == ST_ACTIVE) && (levelg[i] >= irm1) && (levelg[j] >= irm1);
+        good[k] = (st[k] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.levelg[j] >= irm1);
         ngood += good[k];
     }
     if (ngood == 0) return;
+    double *ah = a.ah, *vb = a.vb;
+    const double *rh = a.rh;
     for (int64_t k = 0; k < nenc; k++) {
         if (!good[k]) continue;
         const int i = i1[k] - 1, j = i2[k] - 1;
         for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * j + d] = 0.0;
     }
-    const double rs2 = rhscale * rhscale;
+    const double rs2 = a.rhscale * a.rhscale;
     const double rshell_pow = d_powi(RSHELL, 2 * irecl);
     for (int64_t k = 0; k < nenc; k++) {
         if (!good[k]) continue;
         const int i = i1[k] - 1, j = i2[k] - 1;
-        const double rhs = rhill[i] + rhill[j];
+        const double rhs = a.rhill[i] + a.rhill[j];
         const double ri = ((rhs * rhs) * rs2) * rshell_pow;
         const double rim1 = ri * (RSHELL * RSHELL);
         double dx[3];
@@ -484,8 +620,8 @@ __device__ void d_kick_list_plpl(int64_t nenc, int32_t *l, int64_t cap, int npl,
             const double ir3 = 1.0 / (r2 * sqrt(r2));
             fac = ir3;
         }
-        const double faci = fac * Gm[i];
-        const double facj = fac * Gm[j];
+        const double faci = fac * a.Gm[i];
+        const double facj = fac * a.Gm[j];
         for (int d = 0; d < 3; d++) {
             ah[3 * i + d] = ah[3 * i + d] + facj * dx[d];
             ah[3 * j + d] = ah[3 * j + d] - faci * dx[d];
@@ -503,38 +639,36 @@ __device__ void d_kick_list_plpl(int64_t nenc, int32_t *l, int64_t cap, int npl,
 }
 
 // symba_kick_list_pltp (symba_kick.f90:235-340), serial in list order (one thread)
-__device__ void d_kick_list_pltp(int64_t nenc, int32_t *l, int64_t cap, int npl, int ntp, const int32_t *status,
-                                 int32_t *lmask, const int32_t *tstatus, int32_t *tlmask, const int32_t *levelg,
-                                 const int32_t *tlevelg, const double *rh, const double *trh, double *tvb,
-                                 double *tah, const double *Gm, const double *rhill, double rhscale, double dt,
-                                 int irec, int sgn, uint8_t *good) {
-    if (nenc == 0 || npl == 0 || ntp == 0) return;
-    for (int i = 0; i < npl; i++) lmask[i] = status[i] != ST_INACTIVE;
-    for (int i = 0; i < ntp; i++) tlmask[i] = tstatus[i] != ST_INACTIVE;
-    const int32_t *i1 = l, *i2 = l + cap, *st = l + 3 * cap;
+__device__ void d_kick_list_pltp(const RecArgs &a, double dt, int irec, int sgn) {
+    const int64_t nenc = a.npt;
+    if (nenc == 0 || a.npl == 0 || a.ntp == 0) return;
+    const int64_t cap = a.ptcap;
+    const int32_t *i1 = a.pt, *i2 = a.pt + cap, *st = a.pt + 3 * cap;
+    uint8_t *good = a.good + a.npp;
     const int irm1 = irec - 1;
     const int irecl = sgn < 0 ? irec - 1 : irec;
     int64_t ngood = 0;
     for (int64_t k = 0; k < nenc; k++) {
         const int i = i1[k] - 1, j = i2[k] - 1;
-        good[k] = (st[k] == ST_ACTIVE) && (levelg[i] >= irm1) && (tlevelg[j] >= irm1);
+        good[k] = (st[k] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
         ngood += good[k];
     }
     if (ngood == 0) return;
+    double *tah = a.tah, *tvb = a.tvb;
     for (int64_t k = 0; k < nenc; k++) {
         if (!good[k]) continue;
         const int j = i2[k] - 1;
         for (int d = 0; d < 3; d++) tah[3 * j + d] = 0.0;
     }
-    const double rs2 = rhscale * rhscale;
+    const double rs2 = a.rhscale * a.rhscale;
     const double rshell_pow = d_powi(RSHELL, 2 * irecl);
     for (int64_t k = 0; k < nenc; k++) {
         if (!good[k]) continue;
         const int i = i1[k] - 1, j = i2[k] - 1;
-        const double ri = ((rhill[i] * rhill[i]) * rs2) * rshell_pow;
+        const double ri = ((a.rhill[i] * a.rhill[i]) * rs2) * rshell_pow;
         const double rim1 = ri * (RSHELL * RSHELL);
         double dx[3];
-        for (int d = 0; d < 3; d++) dx[d] = trh[3 * j + d] - rh[3 * i + d];
+        for (int d = 0; d < 3; d++) dx[d] = a.trh[3 * j + d] - a.rh[3 * i + d];
         const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
         double fac;
         if (r2 < rim1) {
@@ -550,7 +684,7 @@ __device__ void d_kick_list_pltp(int64_t nenc, int32_t *l, int64_t cap, int npl,
             const double ir3 = 1.0 / (r2 * sqrt(r2));
             fac = ir3;
         }
-        const double faci = fac * Gm[i];
+        const double faci = fac * a.Gm[i];
         for (int d = 0; d < 3; d++) tah[3 * j + d] = tah[3 * j + d] - faci * dx[d];
     }
     for (int64_t k = 0; k < nenc; k++) {
@@ -563,51 +697,151 @@ __device__ void d_kick_list_pltp(int64_t nenc, int32_t *l, int64_t cap, int npl,
     }
 }
 
-struct KickListArgs {
-    int64_t npp, ppcap, npt, ptcap;
-    int32_t *pp, *pt;
-    int npl, ntp;
-    const int32_t *status, *tstatus, *levelg, *tlevelg;
-    int32_t *lmask, *tlmask;
-    const double *rh, *trh, *Gm, *rhill;
-    double *vb, *ah, *tvb, *tah;
-    double rhscale, dt;
-    int irec, both;
-    uint8_t *good_pp, *good_pt;
-};
-
-// one kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237):
-// warp 0 does the pl-pl list, warp 1 the pl-tp list (disjoint data)
-__global__ void k_kick_lists(KickListArgs a) {
+// One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): thread 0
+// kicks the pl-pl list, thread 32 the pl-tp list (disjoint data), then the block syncs.
+__device__ void blk_kick_lists(const RecArgs &a, double dt, int irecp, bool both) {
     if (threadIdx.x == 0) {
-        d_kick_list_plpl(a.npp, a.pp, a.ppcap, a.npl, a.status, a.lmask, a.levelg, a.rh, a.vb, a.ah, a.Gm, a.rhill,
-                         a.rhscale, a.dt, a.irec, 1, a.good_pp);
-        if (a.both)
-            d_kick_list_plpl(a.npp, a.pp, a.ppcap, a.npl, a.status, a.lmask, a.levelg, a.rh, a.vb, a.ah, a.Gm,
-                             a.rhill, a.rhscale, a.dt, a.irec, -1, a.good_pp);
+        d_kick_list_plpl(a, dt, irecp, 1);
+        if (both) d_kick_list_plpl(a, dt, irecp, -1);
     } else if (threadIdx.x == 32) {
-        d_kick_list_pltp(a.npt, a.pt, a.ptcap, a.npl, a.ntp, a.status, a.lmask, a.tstatus, a.tlmask, a.levelg,
-                         a.tlevelg, a.rh, a.trh, a.tvb, a.tah, a.Gm, a.rhill, a.rhscale, a.dt, a.irec, 1, a.good_pt);
-        if (a.both)
-            d_kick_list_pltp(a.npt, a.pt, a.ptcap, a.npl, a.ntp, a.status, a.lmask, a.tstatus, a.tlmask, a.levelg,
-                             a.tlevelg, a.rh, a.trh, a.tvb, a.tah, a.Gm, a.rhill, a.rhscale, a.dt, a.irec, -1,
-                             a.good_pt);
+        d_kick_list_pltp(a, dt, irecp, 1);
+        if (both) d_kick_list_pltp(a, dt, irecp, -1);
     }
+    __syncthreads();
+}
+
+// symba_drift_pl / _tp at level irec (symba_drift.f90:14-61) over the bodies that
+// appear in the lists (every other body has levelg == -1 inside the recursion).
+__device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec, double dt) {
+    for (int b = threadIdx.x; b < nbpl + nbtp; b += blockDim.x) {
+        const bool isp = b < nbpl;
+        const int i = isp ? a.bpl[b] : a.btp[b - nbpl];
+        const int32_t *lev = isp ? a.levelg : a.tlevelg;
+        int32_t *st = isp ? a.status : a.tstatus;
+        if (lev[i] != irec || st[i] == ST_INACTIVE) continue;
+        double *x = isp ? &a.rh[3 * i] : &a.trh[3 * i];
+        double *v = isp ? &a.vb[3 * i] : &a.tvb[3 * i];
+        double rx = x[0], ry = x[1], rz = x[2], vx = v[0], vy = v[1], vz = v[2];
+        const int fl = d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
+        x[0] = rx;
+        x[1] = ry;
+        x[2] = rz;
+        v[0] = vx;
+        v[1] = vy;
+        v[2] = vz;
+        if (fl != 0) st[i] = ST_DISCARDED_DRIFTERR;
+    }
+    __syncthreads();
 }
 
 // symba_step_set_recur_levels_system (symba_step.f90:118-160)
-__global__ void k_set_recur_levels(int npl, int ntp, int64_t npp, int64_t ppcap, int64_t npt, int64_t ptcap,
-                                   int32_t *levelg, int32_t *tlevelg, int32_t *pp, int32_t *pt, int ireci) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ void blk_set_recur_levels(const RecArgs &a, int nbpl, int nbtp, int ireci) {
     const int irecp = ireci + 1;
-    if (k < npl && levelg[k] == irecp) levelg[k] = ireci;
-    if (k < ntp && tlevelg[k] == irecp) tlevelg[k] = ireci;
-    if (k < npp && pp[4 * ppcap + k] == irecp) pp[4 * ppcap + k] = ireci;
-    if (k < npt && pt[4 * ptcap + k] == irecp) pt[4 * ptcap + k] = ireci;
+    for (int b = threadIdx.x; b < nbpl + nbtp; b += blockDim.x) {
+        int32_t *lev = b < nbpl ? &a.levelg[a.bpl[b]] : &a.tlevelg[a.btp[b - nbpl]];
+        if (*lev == irecp) *lev = ireci;
+    }
+    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x) {
+        int32_t *lev = k < a.npp ? &a.pp[4 * a.ppcap + k] : &a.pt[4 * a.ptcap + (k - a.npp)];
+        if (*lev == irecp) *lev = ireci;
+    }
+    __syncthreads();
 }
 
-// SyMBA drift of both populations (symba_drift_pl/_tp, symba_drift.f90:14-61)
-__global__ void k_noop() {}
+constexpr int MAXLEV = 48;
+constexpr int RECT = 256;  // threads of the recursion kernel
+
+// symba_step_recur_system (symba_step.f90:163-262) for the whole recursion tree of one
+// step, started at level 0, in a single block: the reference's recursive calls become
+// an explicit stack of (loop counter, phase) per level, and every per-level operation
+// is a block-wide device function separated by barriers.
+__global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
+    __shared__ int s_nbpl, s_nbtp, s_any;
+    __shared__ int s_j[MAXLEV], s_phase[MAXLEV];
+    if (threadIdx.x == 0) {
+        s_nbpl = s_nbtp = 0;
+        a.out[0] = 0;
+    }
+    __syncthreads();
+    // compact sets of bodies named in the lists
+    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x) {
+        const bool isp = k < a.npp;
+        const int64_t q = isp ? k : k - a.npp;
+        const int32_t *l = isp ? a.pp : a.pt;
+        const int64_t cap = isp ? a.ppcap : a.ptcap;
+        const int i = l[q] - 1, j = l[cap + q] - 1;
+        if (atomicExch(&a.mark_pl[i], 1) == 0) a.bpl[atomicAdd(&s_nbpl, 1)] = i;
+        if (isp) {
+            if (atomicExch(&a.mark_pl[j], 1) == 0) a.bpl[atomicAdd(&s_nbpl, 1)] = j;
+        } else {
+            if (atomicExch(&a.mark_tp[j], 1) == 0) a.btp[atomicAdd(&s_nbtp, 1)] = j;
+        }
+    }
+    __syncthreads();
+    const int nbpl = s_nbpl, nbtp = s_nbtp;
+    int ireci = 0;
+    if (threadIdx.x == 0) {
+        s_j[0] = 1;
+        s_phase[0] = 0;
+    }
+    __syncthreads();
+    int deepest = 0;
+    for (;;) {
+        double p3 = 1.0;
+        for (int k = 0; k < ireci; k++) p3 *= 3.0;
+        const double dtl = a.dt / p3;
+        const double dth = 0.5 * dtl;
+        const int irecp = ireci + 1;
+        const int nloops = ireci == 0 ? 1 : NTENC;
+        if (s_phase[ireci] == 0) {
+            if (s_j[ireci] > nloops) {
+                if (ireci == 0) break;
+                __syncthreads();
+                ireci--;
+                if (threadIdx.x == 0) s_phase[ireci] = 1;
+                __syncthreads();
+                continue;
+            }
+            if (dtl / a.dt < 2.220446049250313e-16) {
+                if (threadIdx.x == 0) a.out[0] = SWG_ERR_RECURSION;
+                break;
+            }
+            if (irecp > deepest) deepest = irecp;
+            if (threadIdx.x == 0) s_any = 0;
+            __syncthreads();
+            blk_list_check(a, irecp, dtl, &s_any);
+            blk_kick_lists(a, dth, irecp, ireci != 0);
+            blk_drift(a, nbpl, nbtp, ireci, dtl);
+            const int any = s_any;
+            __syncthreads();
+            if (any) {
+                if (ireci + 1 >= MAXLEV) {
+                    if (threadIdx.x == 0) a.out[0] = SWG_ERR_RECURSION;
+                    break;
+                }
+                ireci++;
+                if (threadIdx.x == 0) {
+                    s_j[ireci] = 1;
+                    s_phase[ireci] = 0;
+                }
+                __syncthreads();
+                continue;
+            }
+        }
+        // after the deeper levels (or none) for loop j of level ireci
+        blk_kick_lists(a, dth, irecp, ireci != 0);
+        blk_set_recur_levels(a, nbpl, nbtp, ireci);
+        if (threadIdx.x == 0) {
+            s_j[ireci]++;
+            s_phase[ireci] = 0;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbpl; b += blockDim.x) a.mark_pl[a.bpl[b]] = 0;
+    for (int b = threadIdx.x; b < nbtp; b += blockDim.x) a.mark_tp[a.btp[b]] = 0;
+    if (threadIdx.x == 0) atomicMax(&a.out[1], deepest);
+}
 
 // ---- WHM serial coordinate kernels (whm_coord.f90:14-124) and accelerations (whm_kick.f90:125-215)
 __global__ void k_whm_h2j(int n, const double *Gm, const double *eta, const double *rh, const double *vh, double *xj,
@@ -911,7 +1145,7 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
 
 int lindrift_pl(swg_system *s, double dt, int lbeg) {
     if (s->npl == 0) return SWG_OK;
-    k_lindrift_pl<<<1, 256, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->lmask, s->GMcb, s->rh, dt, s->dcb,
+    k_lindrift_pl<<<1, RB, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->lmask, s->GMcb, s->rh, dt, s->dcb,
                                                lbeg ? CB_PTBEG : CB_PTEND, exact(s));
     return L(s->c, "lindrift_pl");
 }
@@ -923,12 +1157,12 @@ int tp_misc(swg_system *s, int slot, double dt, int mode) {
 }
 int vh2vb_pl(swg_system *s) {
     if (s->npl == 0) return SWG_OK;
-    k_vh2vb_pl<<<1, 256, 0, s->c->stream>>>(s->npl, s->Gmass, s->vh, s->vb, s->GMcb, s->dcb);
+    k_vh2vb_pl<<<1, RB, 0, s->c->stream>>>(s->npl, s->Gmass, s->vh, s->vb, s->GMcb, s->dcb, exact(s));
     return L(s->c, "vh2vb_pl");
 }
 int vb2vh_pl(swg_system *s) {
     if (s->npl == 0) return SWG_OK;
-    k_vb2vh_pl<<<1, 256, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->status, s->vh, s->GMcb, s->dcb);
+    k_vb2vh_pl<<<1, RB, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->status, s->vh, s->GMcb, s->dcb, exact(s));
     return L(s->c, "vb2vh_pl");
 }
 // drift with the SyMBA level mask (levelg == irec) or the plain status mask
@@ -1076,57 +1310,119 @@ int ensure_list(swg_system *s, int32_t **l, int64_t *cap, int64_t need) {
 }
 
 // level-0 checks: symba_encounter_check_pl / _tp (symba_encounter_check.f90:14-87, 238-296)
+// Level-0 checks of symba_encounter_check_pl / _tp (symba_encounter_check.f90:14-87,
+// 238-296).  Both checks are launched before one host synchronization reads the two
+// counts; short lists are sorted, de-duplicated and turned into SyMBA encounter
+// lists (status, level, level-0 marks) by one single-block kernel each.
 int symba_level0(swg_system *s, double dt, int *lany) {
     swg_ctx *c = s->c;
     *lany = 0;
     s->plpl_n = s->pltp_n = 0;
-    // renc at level 0 is computed inside the checks from rhill
     double *renc = (double *)s->red.ptr;
     k_set_renc<<<grid_for(s->npl, 128), 128, 0, c->stream>>>(s->npl, s->rhill, s->rhscale, 0, renc);
     SWG_TRY(L(c, "set_renc"));
-    if (s->npl > 0) {
-        int64_t n = 0;
-        int32_t *i1, *i2, *lv;
-        const int32_t nplt = s->npl - s->nplm;
-        if (nplt == 0)
-            SWG_TRY(encounter_check_kind(c, s->enc, 0, s->enc_plpl, s->npl, s->rh, s->vb, renc, 0, nullptr, nullptr,
-                                         nullptr, dt, &n, &i1, &i2, &lv));
-        else
-            SWG_TRY(encounter_check_kind(c, s->enc, 1, s->enc_plpl, s->nplm, s->rh, s->vb, renc, nplt,
-                                         s->rh + 3 * s->nplm, s->vb + 3 * s->nplm, renc + s->nplm, dt, &n, &i1, &i2,
-                                         &lv));
-        SWG_TRY(ensure_list(s, &s->plpl_l, &s->plpl_cap, n));
-        if (n > 0) {
-            for (int f = 0; f < 3; f++) {
-                const int32_t *src = f == 0 ? i1 : (f == 1 ? i2 : lv);
-                SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->plpl_l + f * s->plpl_cap, src, sizeof(int32_t) * n,
-                                                       cudaMemcpyDeviceToDevice, c->stream),
-                                    "copy list"));
-            }
-            k_level0_mark<<<grid_for(n, 128), 128, 0, c->stream>>>(n, s->plpl_l, s->plpl_cap, 0, s->levelg, s->levelm,
-                                                                   s->nplenc, nullptr, nullptr, nullptr);
-            SWG_TRY(L(c, "level0_mark_pl"));
+    const int32_t nplt = s->npl - s->nplm;
+    const bool do_pp = s->npl > 0, do_pt = s->ntp > 0 && s->npl > 0;
+    EncWork *w[2] = {&s->enc, &s->enc2};
+    for (int k = 0; k < 2; k++) {
+        SWG_TRY(ensure(c, w[k]->counters, 2 * sizeof(unsigned long long)));
+        if (w[k]->rawcap < 1024) {
+            w[k]->rawcap = 1024;
+            SWG_TRY(ensure(c, w[k]->raw, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
         }
-        s->plpl_n = n;
     }
-    if (s->ntp > 0 && s->npl > 0) {
-        int64_t n = 0;
-        int32_t *i1, *i2, *lv;
-        SWG_TRY(encounter_check_kind(c, s->enc, 2, s->enc_pltp, s->npl, s->rh, s->vb, renc, s->ntp, s->trh, s->tvb,
-                                     nullptr, dt, &n, &i1, &i2, &lv));
-        SWG_TRY(ensure_list(s, &s->pltp_l, &s->pltp_cap, n));
-        if (n > 0) {
+    if (s->enc_plpl == SWG_ENC_SORTSWEEP) SWG_TRY(ensure(c, s->enc.sort, sas_scratch_bytes(s->npl)));
+    if (s->enc_pltp == SWG_ENC_SORTSWEEP) SWG_TRY(ensure(c, s->enc2.sort, sas_scratch_bytes(s->npl + s->ntp)));
+    unsigned long long *h = (unsigned long long *)(s->h_flags + 8);
+    auto launch = [&](int kind) -> int {
+        EncWork &e = *w[kind];
+        int32_t *i1 = (int32_t *)e.raw.ptr, *i2 = i1 + e.rawcap, *lv = i2 + e.rawcap;
+        unsigned long long *cnt = (unsigned long long *)e.counters.ptr;
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
+        if (kind == 0) {
+            if (nplt == 0) {
+                SWG_TRY(encounter_launch(c, s->enc_plpl, s->npl, s->rh, s->vb, renc, s->npl, s->rh, s->vb, renc, 1, 0,
+                                         dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
+            } else {
+                SWG_TRY(encounter_launch(c, s->enc_plpl, s->nplm, s->rh, s->vb, renc, s->nplm, s->rh, s->vb, renc, 1,
+                                         0, dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
+                SWG_TRY(encounter_launch(c, s->enc_plpl, s->nplm, s->rh, s->vb, renc, nplt, s->rh + 3 * s->nplm,
+                                         s->vb + 3 * s->nplm, renc + s->nplm, 0, s->nplm, dt, e.rawcap, i1, i2, lv,
+                                         cnt, e.sort.ptr));
+            }
+        } else {
+            SWG_TRY(encounter_launch(c, s->enc_pltp, s->npl, s->rh, s->vb, renc, s->ntp, s->trh, s->tvb, nullptr, 0, 0,
+                                     dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
+        }
+        return cuda_status(c, cudaMemcpyAsync(&h[kind], cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                              c->stream),
+                           "count");
+    };
+    h[0] = h[1] = 0;
+    if (do_pp) SWG_TRY(launch(0));
+    if (do_pt) SWG_TRY(launch(1));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
+    for (int k = 0; k < 2; k++) {  // capacity overflow: grow the raw buffers and redo that check
+        if ((int64_t)h[k] <= w[k]->rawcap) continue;
+        w[k]->rawcap = (int64_t)h[k] + (int64_t)h[k] / 2 + 1024;
+        DevBuf fresh;
+        SWG_TRY(ensure(c, fresh, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
+        cudaFree(w[k]->raw.ptr);
+        w[k]->raw = fresh;
+        SWG_TRY(launch(k));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
+    }
+    bool need_count_sync = false;
+    for (int k = 0; k < 2; k++) {
+        const int64_t n = (int64_t)h[k];
+        if (n == 0) continue;
+        EncWork &e = *w[k];
+        int32_t **list = k == 0 ? &s->plpl_l : &s->pltp_l;
+        int64_t *cap = k == 0 ? &s->plpl_cap : &s->pltp_cap;
+        SWG_TRY(ensure_list(s, list, cap, n));
+        int32_t *i1 = (int32_t *)e.raw.ptr, *i2 = i1 + e.rawcap, *lv = i2 + e.rawcap;
+        unsigned long long *cnt = (unsigned long long *)e.counters.ptr;
+        if (n <= FIN_N) {
+            k_list_finalize<<<1, 1024, 0, c->stream>>>((int)n, i1, i2, lv, *list, *cap, k, s->levelg, s->levelm,
+                                                       k == 0 ? s->nplenc : s->ntpenc, s->tlevelg, s->tlevelm,
+                                                       s->tnplenc, cnt + 1);
+            SWG_TRY(L(c, "list_finalize"));
+        } else {
+            SWG_TRY(ensure(c, e.sort, sort_pairs_scratch_bytes(n)));
+            SWG_TRY(sort_pairs_unique(c, n, i1, i2, lv, e.sort.ptr, cnt + 1));
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(&h[2 + k], cnt + 1, sizeof(unsigned long long),
+                                                   cudaMemcpyDeviceToHost, c->stream),
+                                "count"));
+            SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
+            const int64_t m = (int64_t)h[2 + k];
             for (int f = 0; f < 3; f++) {
                 const int32_t *src = f == 0 ? i1 : (f == 1 ? i2 : lv);
-                SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->pltp_l + f * s->pltp_cap, src, sizeof(int32_t) * n,
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(*list + f * *cap, src, sizeof(int32_t) * m,
                                                        cudaMemcpyDeviceToDevice, c->stream),
                                     "copy list"));
             }
-            k_level0_mark<<<grid_for(n, 128), 128, 0, c->stream>>>(n, s->pltp_l, s->pltp_cap, 1, s->levelg, s->levelm,
-                                                                   s->ntpenc, s->tlevelg, s->tlevelm, s->tnplenc);
-            SWG_TRY(L(c, "level0_mark_tp"));
+            k_level0_mark<<<grid_for(m, 128), 128, 0, c->stream>>>(m, *list, *cap, k, s->levelg, s->levelm,
+                                                                   k == 0 ? s->nplenc : s->ntpenc, s->tlevelg,
+                                                                   s->tlevelm, s->tnplenc);
+            SWG_TRY(L(c, "level0_mark"));
+            (k == 0 ? s->plpl_n : s->pltp_n) = m;
+            continue;
         }
-        s->pltp_n = n;
+        const int mode = k == 0 ? s->enc_plpl : s->enc_pltp;
+        if (mode == SWG_ENC_SORTSWEEP) {
+            // the sweep can report a pair twice; the exact count is known after de-duplication
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(&h[2 + k], cnt + 1, sizeof(unsigned long long),
+                                                   cudaMemcpyDeviceToHost, c->stream),
+                                "count"));
+            need_count_sync = true;
+        } else {
+            (k == 0 ? s->plpl_n : s->pltp_n) = n;  // triangular lists hold no repeats
+        }
+    }
+    if (need_count_sync) {
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
+        if (s->enc_plpl == SWG_ENC_SORTSWEEP && h[0] > 0 && h[0] <= FIN_N) s->plpl_n = (int64_t)h[2];
+        if (s->enc_pltp == SWG_ENC_SORTSWEEP && h[1] > 0 && h[1] <= FIN_N) s->pltp_n = (int64_t)h[3];
     }
     s->stats[2] += s->plpl_n;
     s->stats[3] += s->pltp_n;
@@ -1134,87 +1430,55 @@ int symba_level0(swg_system *s, double dt, int *lany) {
     return SWG_OK;
 }
 
-int kick_lists(swg_system *s, double dt, int irec, int both) {
+// Launch the whole SyMBA recursion of one step (symba_step_recur_system from level 0)
+// as one single-block kernel; no host round trip until the next step's checks.
+int symba_recursion(swg_system *s, double dt) {
     swg_ctx *c = s->c;
-    if (s->plpl_n == 0 && s->pltp_n == 0) return SWG_OK;
-    KickListArgs a;
+    const int64_t n = s->plpl_n + s->pltp_n;
+    SWG_TRY(ensure(c, s->rec_scratch, (size_t)(2 * n + 64) + sizeof(int32_t) * (size_t)(3 * n + 64)));
+    RecArgs a;
+    a.npl = s->npl;
+    a.ntp = s->ntp;
     a.npp = s->plpl_n;
     a.ppcap = s->plpl_cap;
     a.npt = s->pltp_n;
     a.ptcap = s->pltp_cap;
     a.pp = s->plpl_l;
     a.pt = s->pltp_l;
-    a.npl = s->npl;
-    a.ntp = s->ntp;
+    a.rh = s->rh;
+    a.vb = s->vb;
+    a.ah = s->ah;
+    a.trh = s->trh;
+    a.tvb = s->tvb;
+    a.tah = s->tah;
+    a.Gm = s->Gmass;
+    a.rhill = s->rhill;
+    a.radius = s->radius;
     a.status = s->status;
     a.tstatus = s->tstatus;
     a.levelg = s->levelg;
+    a.levelm = s->levelm;
     a.tlevelg = s->tlevelg;
-    a.lmask = s->lmask;
-    a.tlmask = s->tlmask;
-    a.rh = s->rh;
-    a.trh = s->trh;
-    a.Gm = s->Gmass;
-    a.rhill = s->rhill;
-    a.vb = s->vb;
-    a.ah = s->ah;
-    a.tvb = s->tvb;
-    a.tah = s->tah;
+    a.tlevelm = s->tlevelm;
+    a.GMcb = s->GMcb;
     a.rhscale = s->rhscale;
     a.dt = dt;
-    a.irec = irec;
-    a.both = both;
-    uint8_t *good = (uint8_t *)s->enc.sort.ptr;  // list-sized byte scratch (sort buffer is idle here)
-    a.good_pp = good;
-    a.good_pt = good + s->plpl_n;
-    k_kick_lists<<<1, 64, 0, c->stream>>>(a);
-    return L(c, "kick_lists");
-}
-
-// symba_step_recur_system (symba_step.f90:163-262)
-int symba_recur(swg_system *s, int ireci) {
-    swg_ctx *c = s->c;
-    s->irec = ireci;
-    double p3 = 1.0;
-    for (int k = 0; k < ireci; k++) p3 *= 3.0;
-    const double dtl = s->dt / p3;
-    const double dth = 0.5 * dtl;
-    if (dtl / s->dt < 2.220446049250313e-16) {
-        c->err = "SyMBA local time step too small";
-        return SWG_ERR_RECURSION;
-    }
-    const int irecp = ireci + 1;
-    if (irecp > s->stats[1]) s->stats[1] = irecp;
-    const int nloops = ireci == 0 ? 1 : NTENC;
-    int32_t *dflag = (int32_t *)s->flags.ptr;
-    for (int j = 1; j <= nloops; j++) {
-        ProfScope ps1(s, PROF_RECUR);
-        k_list_check<<<1, 256, 0, c->stream>>>(s->plpl_n, s->plpl_l, s->plpl_cap, s->pltp_n, s->pltp_l, s->pltp_cap,
-                                               s->rh, s->vb, s->trh, s->tvb, s->rhill, s->radius, s->rhscale, irecp,
-                                               dtl, s->levelg, s->levelm, s->tlevelg, s->tlevelm, dflag,
-                                               (uint8_t *)s->enc.sort.ptr + s->plpl_n + s->pltp_n);
-        SWG_TRY(L(c, "list_check"));
-        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->h_flags, dflag, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream),
-                            "flag"));
-        SWG_TRY(kick_lists(s, dth, irecp, ireci != 0));
-        prof_end(s, ps1.k);
-        ps1.k = -1;
-        SWG_TRY(drift_pl(s, dtl));
-        SWG_TRY(drift_tp(s, dtl));
-        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
-        const int lencounter = s->h_flags[0];
-        if (lencounter) SWG_TRY(symba_recur(s, irecp));
-        s->irec = ireci;
-        ProfScope ps2(s, PROF_RECUR);
-        SWG_TRY(kick_lists(s, dth, irecp, ireci != 0));
-        const int64_t nmax = std::max<int64_t>(std::max<int64_t>(s->npl, s->ntp), std::max(s->plpl_n, s->pltp_n));
-        k_set_recur_levels<<<grid_for(nmax, 256), 256, 0, c->stream>>>(s->npl, s->ntp, s->plpl_n, s->plpl_cap,
-                                                                        s->pltp_n, s->pltp_cap, s->levelg, s->tlevelg,
-                                                                        s->plpl_l, s->pltp_l, ireci);
-        SWG_TRY(L(c, "set_recur_levels"));
-        s->irec = ireci;
-    }
-    return SWG_OK;
+    int32_t *ibuf = (int32_t *)s->rec_scratch.ptr;
+    a.bpl = ibuf;                 // up to 2*npp + npt bodies
+    a.btp = ibuf + 2 * n + 32;    // up to npt bodies
+    uint8_t *bbuf = (uint8_t *)(ibuf + 3 * n + 64);
+    a.lenc = bbuf;
+    a.good = bbuf + n + 32;
+    a.mark_pl = s->mark_pl;
+    a.mark_tp = s->mark_tp;
+    a.out = s->rec_out;
+    ProfScope ps(s, PROF_RECUR);
+    k_symba_recursion<<<1, RECT, 0, c->stream>>>(a);
+    SWG_TRY(L(c, "symba_recursion"));
+    // status word read back at the next host synchronization
+    return cuda_status(c, cudaMemcpyAsync(s->h_flags + 2, s->rec_out, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                          c->stream),
+                       "recursion status");
 }
 
 // symba_step_interp_system (symba_step.f90:55-115)
@@ -1230,7 +1494,7 @@ int symba_interp(swg_system *s, double dt) {
         SWG_TRY(kick_vb_tp(s, dth, 1));
         SWG_TRY(drift_tp(s, dt));
     }
-    SWG_TRY(symba_recur(s, 0));
+    SWG_TRY(symba_recursion(s, dt));
     s->irec = -1;
     SWG_TRY(kick_vb_pl(s, dth, 0));
     SWG_TRY(lindrift_pl(s, dth, 0));
@@ -1259,8 +1523,6 @@ int symba_step(swg_system *s, double dt) {
     }
     if (lany) {
         s->stats[0]++;
-        // list-sized byte scratch for kick/check flags lives in the sort buffer
-        SWG_TRY(ensure(c, s->enc.sort, (size_t)2 * (s->plpl_n + s->pltp_n) + 64));
         SWG_TRY(symba_interp(s, dt));
     } else {
         s->irec = -1;
@@ -1301,6 +1563,9 @@ int swg_system_create(swg_ctx *c, int integrator, int32_t npl, int32_t ntp, swg_
     for (auto p : ti)
         if (rc == SWG_OK) rc = dalloc(c, p, m);
     if (rc == SWG_OK) rc = dalloc(c, &s->dcb, CB_N);
+    if (rc == SWG_OK) rc = dalloc(c, &s->mark_pl, n);
+    if (rc == SWG_OK) rc = dalloc(c, &s->mark_tp, m);
+    if (rc == SWG_OK) rc = dalloc(c, &s->rec_out, 4);
     if (rc == SWG_OK) rc = ensure(c, s->flags, 64);
     if (rc == SWG_OK) rc = ensure(c, s->red, sizeof(double) * (4 * n + 64));
     if (rc == SWG_OK) {
@@ -1323,8 +1588,8 @@ int swg_system_destroy(swg_system *s) {
                     s->eta, s->muj, s->ir3h, s->ir3j, s->status, s->lmask, s->levelg, s->levelm, s->nplenc,
                     s->ntpenc, s->iflag, s->trh, s->tvh, s->tvb, s->tah, s->tstatus, s->tlmask, s->tlevelg,
                     s->tlevelm, s->tnplenc, s->tiflag, s->dcb, s->plpl_l, s->pltp_l, s->enc.raw.ptr,
-                    s->enc.sort.ptr, s->enc.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
-                    s->red.ptr};
+                    s->enc.sort.ptr, s->enc.counters.ptr, s->enc2.raw.ptr, s->enc2.sort.ptr, s->enc2.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
+                    s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_scratch.ptr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);
@@ -1439,6 +1704,7 @@ int swg_system_initialize(swg_system *s) {
 
 int swg_system_step(swg_system *s, int32_t nsteps) {
     if (!s || !s->initialized) return SWG_ERR_STATE;
+    s->h_flags[2] = 0;
     for (int32_t k = 0; k < nsteps; k++) {
         int rc;
         if (s->integrator == SWG_WHM)
@@ -1448,7 +1714,18 @@ int swg_system_step(swg_system *s, int32_t nsteps) {
         else
             rc = symba_step(s, s->dt);
         if (rc != SWG_OK) return rc;
+        if (s->h_flags[2] != 0) {  // recursion status of an earlier step, seen at a sync point
+            s->c->err = "SyMBA local time step too small";
+            return s->h_flags[2];
+        }
         s->t += s->dt;
+    }
+    if (s->integrator == SWG_SYMBA) {
+        SWG_TRY(cuda_status(s->c, cudaStreamSynchronize(s->c->stream), "step"));
+        if (s->h_flags[2] != 0) {
+            s->c->err = "SyMBA local time step too small";
+            return s->h_flags[2];
+        }
     }
     return SWG_OK;
 }
@@ -1500,6 +1777,11 @@ int swg_system_energy(swg_system *s, double *out) {
 
 int swg_system_stats(swg_system *s, int64_t *out) {
     if (!s || !out) return SWG_ERR_ARG;
+    if (s->integrator == SWG_SYMBA) {
+        int32_t dev[4];
+        SWG_TRY(cuda_status(s->c, cudaMemcpy(dev, s->rec_out, sizeof(dev), cudaMemcpyDeviceToHost), "stats"));
+        s->stats[1] = dev[1];
+    }
     std::memcpy(out, s->stats, sizeof(s->stats));
     return SWG_OK;
 }
