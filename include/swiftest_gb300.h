@@ -70,6 +70,18 @@ int swg_kick_getacch_int_all_flat_pl(swg_ctx *ctx, int32_t npl, int32_t nplm, in
                                      const double *r, const double *Gmass, const double *radius, double *acc,
                                      int precision, int mem);
 
+/* Same computation as swg_kick_getacch_int_all_tri_pl with SWG_MIXED, for callers that
+ * must not allocate device memory (an integrator recorded into a CUDA graph, or an
+ * application that owns every allocation in a fixed pool): it calls no cudaMalloc or
+ * cudaFree and takes device pointers and a cudaStream_t.  It has no counterpart in
+ * the reference.  Its scratch is one 4 MiB device array per GPU, held until exit and
+ * shared by all calls: calls that overlap on the GPU race; npl above
+ * SWG_NOALLOC_MAX_NPL is rejected with SWG_ERR_ARG.  The first call on a device
+ * resolves the array's address; make it before any stream capture. */
+#define SWG_NOALLOC_MAX_NPL 1048576
+int swg_kick_getacch_int_all_tri_pl_noalloc(int32_t npl, int32_t nplm, const double *r, const double *Gmass,
+                                            const double *radius, double *acc, void *stream);
+
 /* Replaces swiftest_kick_getacch_int_all_tp (swiftest_kick.f90:374-415). */
 int swg_kick_getacch_int_all_tp(swg_ctx *ctx, int32_t ntp, int32_t npl, const double *rtp, const double *rpl,
                                 const double *GMpl, const int32_t *lmask, double *acc, int precision, int mem);

@@ -45,6 +45,7 @@ SIGNATURES = {
     "swg_kick_getacch_int_all_tri_pl": (_INT, [_P, _I32, _I32, _P, _P, _P, _P, _INT, _INT]),
     "swg_kick_getacch_int_all_flat_pl": (_INT, [_P, _I32, _I32, _I64, _P, _P, _P, _P, _P, _INT, _INT]),
     "swg_kick_getacch_int_all_tp": (_INT, [_P, _I32, _I32, _P, _P, _P, _P, _P, _INT, _INT]),
+    "swg_kick_getacch_int_all_tri_pl_noalloc": (_INT, [_I32, _I32, _P, _P, _P, _P, _P]),
     "swg_drift_all": (_INT, [_P, _P, _P, _P, _I32, _I32, _D, _D, _P, _P, _INT]),
     "swg_encounter_check_all_plpl": (_INT, [_P, _INT, _I32, _P, _P, _P, _D, _I64, C.POINTER(_I64), _P, _P, _P, _INT]),
     "swg_encounter_check_all_plplm": (_INT, [_P, _INT, _I32, _I32, _P, _P, _P, _P, _P, _P, _D, _I64,

@@ -303,6 +303,48 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
     return launch_status(c, "kick_mixed");
 }
 
+// Mixed pl-pl kick on a caller's stream with caller-provided scratch (counters first,
+// then partials); used by the entry point that allocates nothing (kick_noalloc.cu).
+// Same chunking and kernel as kick_mixed_launch.
+cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, int num_sms, int npl, int nplm, const double *r,
+                                      const double *Gm, const double *R, double *acc, void *scratch,
+                                      size_t counter_bytes) {
+    if (npl <= 0) return cudaSuccess;
+    const int bx = div_up(npl, MBLOCK);
+    const int target = 2 * (num_sms > 0 ? num_sms : 152);
+    int nchunk = div_up(target, bx);
+    const int maxchunk = div_up(npl, MT);
+    if (nchunk > maxchunk) nchunk = maxchunk;
+    if (nchunk < 1) nchunk = 1;
+    int chunk = div_up(npl, nchunk);
+    chunk = div_up(chunk, MT) * MT;
+    nchunk = div_up(npl, chunk);
+    unsigned *counters = (unsigned *)scratch;
+    float *partial = (float *)((char *)scratch + counter_bytes);
+    dim3 grid(bx, nchunk);
+    if (R)
+        k_kick_mixed<false, true><<<grid, MBLOCK, 0, stream>>>(npl, npl, nplm, r, r, Gm, R, nullptr, acc, 0, chunk,
+                                                               partial, counters);
+    else
+        k_kick_mixed<false, false><<<grid, MBLOCK, 0, stream>>>(npl, npl, nplm, r, r, Gm, nullptr, nullptr, acc, 0,
+                                                                chunk, partial, counters);
+    return cudaGetLastError();
+}
+
+// largest partial-sum footprint (nchunk * npl entries) the launcher above can request
+int64_t kick_mixed_plpl_partials_max(int num_sms, int npl) {
+    const int bx = div_up(npl, MBLOCK);
+    const int target = 2 * (num_sms > 0 ? num_sms : 152);
+    int nchunk = div_up(target, bx);
+    const int maxchunk = div_up(npl, MT);
+    if (nchunk > maxchunk) nchunk = maxchunk;
+    if (nchunk < 1) nchunk = 1;
+    int chunk = div_up(npl, nchunk);
+    chunk = div_up(chunk, MT) * MT;
+    nchunk = div_up(npl, chunk);
+    return nchunk > 1 ? (int64_t)nchunk * npl : 0;
+}
+
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,
                const double *r, const double *Gm, const double *R, double *acc, double sign, double *ahi_ahj) {
     if (npairs <= 0 || npl <= 0) return SWG_OK;

@@ -87,6 +87,10 @@ int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart);
 int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const double *rrecv, const double *rpart,
                       const double *Gm, const double *R, const int32_t *lmask, double *acc, int acc_is_zero,
                       int nchunk, void *scratch);
+cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, int num_sms, int npl, int nplm, const double *r,
+                                      const double *Gm, const double *R, double *acc, void *scratch,
+                                      size_t counter_bytes);
+int64_t kick_mixed_plpl_partials_max(int num_sms, int npl);
 // explicit 1-based pair list (k_plpl(2,n) or separate i1/i2); ahi_ahj: 6*npl doubles of scratch
 // sign > 0: acc = (acc + ahi) + ahj ; sign < 0: acc = acc - (ahi + ahj)
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,
