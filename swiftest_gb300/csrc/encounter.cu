@@ -95,35 +95,53 @@ __device__ __forceinline__ bool prefilter_reject(const BodyF &p, const BodyF &q,
     return dlo > rhi;  // NaN/inf comparisons are false: such pairs go to the FP64 test
 }
 
-// Receivers: list-2 bodies j (one thread each).  Partners: list-1 bodies i,
-// i < j when `upper` (pl-pl), all i otherwise.  Pair written as (i+1, j+1+shift2).
-__global__ void __launch_bounds__(ET) k_encounter_tri(int n1, const double *__restrict__ r1,
-                                                      const double *__restrict__ v1,
-                                                      const double *__restrict__ renc1, int n2,
-                                                      const double *__restrict__ r2, const double *__restrict__ v2,
-                                                      const double *__restrict__ renc2, int upper, int shift2,
-                                                      double dt, long long cap, int32_t *__restrict__ o1,
-                                                      int32_t *__restrict__ o2, int32_t *__restrict__ olv,
-                                                      unsigned long long *__restrict__ count) {
-    __shared__ float4 sa[ET], sb[ET], sv[ET];
+// Float copies of the bodies for the prefilter, written once per check.
+__global__ void k_encounter_prep(int n, const double *__restrict__ r, const double *__restrict__ v,
+                                 const double *__restrict__ renc, float4 *A, float4 *B, float4 *V) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const BodyF o = load_body(r, v, renc, i);
+    A[i] = o.a;
+    B[i] = o.b;
+    V[i] = o.v;
+}
+
+constexpr int EP = 64;  // partners per shared-memory tile
+
+// Receivers: list-2 bodies j (one thread each, blockIdx.x tiles of ET).  Partners:
+// list-1 bodies i in chunk blockIdx.y (i < j when `upper`, i.e. pl-pl).  Pair written
+// as (i+1, j+1+shift2); the list is sorted afterwards, so the chunking is invisible.
+__global__ void __launch_bounds__(ET) k_encounter_tri(
+    int n1, const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
+    const double *__restrict__ r1, const double *__restrict__ v1, const double *__restrict__ renc1, int n2,
+    const float4 *__restrict__ A2, const float4 *__restrict__ B2, const float4 *__restrict__ V2,
+    const double *__restrict__ r2, const double *__restrict__ v2, const double *__restrict__ renc2, int upper,
+    int shift2, double dt, int chunk, long long cap, int32_t *__restrict__ o1, int32_t *__restrict__ o2,
+    int32_t *__restrict__ olv, unsigned long long *__restrict__ count) {
+    __shared__ float4 sa[EP], sb[EP], sv[EP];
     const int j = blockIdx.x * ET + threadIdx.x;
     const bool active = j < n2;
+    const int ibeg = blockIdx.y * chunk;
+    int iend = min(n1, ibeg + chunk);
+    if (upper) iend = min(iend, (int)(blockIdx.x * ET + ET));
+    if (ibeg >= iend) return;  // whole block outside the upper triangle
     BodyF q;
-    if (active) q = load_body(r2, v2, renc2, j);
+    if (active) {
+        q.a = A2[j];
+        q.b = B2[j];
+        q.v = V2[j];
+    }
+    const int own_end = upper ? min(iend, j) : iend;
     const float dtf = __double2float_ru(dt) * (1.0f + 1e-6f);
-    const int iend_blk = upper ? min(n1, (int)(blockIdx.x * ET + ET)) : n1;
-    const int iend = upper ? j : n1;
-    for (int i0 = 0; i0 < iend_blk; i0 += ET) {
-        const int il = i0 + threadIdx.x;
-        if (il < n1) {
-            BodyF p = load_body(r1, v1, renc1, il);
-            sa[threadIdx.x] = p.a;
-            sb[threadIdx.x] = p.b;
-            sv[threadIdx.x] = p.v;
+    for (int i0 = ibeg; i0 < iend; i0 += EP) {
+        if (threadIdx.x < EP && i0 + threadIdx.x < iend) {
+            sa[threadIdx.x] = A1[i0 + threadIdx.x];
+            sb[threadIdx.x] = B1[i0 + threadIdx.x];
+            sv[threadIdx.x] = V1[i0 + threadIdx.x];
         }
         __syncthreads();
         if (active) {
-            const int nt = min(ET, iend - i0);
+            const int nt = min(EP, own_end - i0);
             for (int ii = 0; ii < nt; ii++) {
                 BodyF p;
                 p.a = sa[ii];
@@ -468,10 +486,38 @@ int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const doubl
         return launch_status(c, "encounter_sas");
     }
     if (n1 <= 0 || n2 <= 0) return SWG_OK;
-    k_encounter_tri<<<(n2 + ET - 1) / ET, ET, 0, c->stream>>>(n1, r1, v1, renc1, n2, r2, v2, renc2, upper, shift2, dt,
-                                                              cap, o1, o2, olv, count);
+    // float copies for the prefilter: list 1 then (unless it is the same list) list 2
+    float4 *A1 = (float4 *)sas_scratch, *B1 = A1 + n1, *V1 = B1 + n1;
+    float4 *A2 = A1, *B2 = B1, *V2 = V1;
+    k_encounter_prep<<<(n1 + 255) / 256, 256, 0, c->stream>>>(n1, r1, v1, renc1, A1, B1, V1);
+    c->launches++;
+    const bool same = upper && r2 == r1;
+    if (!same) {
+        A2 = V1 + n1;
+        B2 = A2 + n2;
+        V2 = B2 + n2;
+        k_encounter_prep<<<(n2 + 255) / 256, 256, 0, c->stream>>>(n2, r2, v2, renc2, A2, B2, V2);
+        c->launches++;
+    }
+    const int bx = (n2 + ET - 1) / ET;
+    const int target = 4 * (c->num_sms > 0 ? c->num_sms : 152);
+    int nchunk = (target + bx - 1) / bx;
+    const int maxchunk = (n1 + EP - 1) / EP;
+    if (nchunk > maxchunk) nchunk = maxchunk;
+    if (nchunk < 1) nchunk = 1;
+    int chunk = (n1 + nchunk - 1) / nchunk;
+    chunk = (chunk + EP - 1) / EP * EP;
+    nchunk = (n1 + chunk - 1) / chunk;
+    k_encounter_tri<<<dim3(bx, nchunk), ET, 0, c->stream>>>(n1, A1, B1, V1, r1, v1, renc1, n2, A2, B2, V2, r2, v2,
+                                                            renc2, upper, shift2, dt, chunk, cap, o1, o2, olv, count);
     c->launches++;
     return launch_status(c, "encounter_tri");
+}
+
+// scratch of one encounter_launch call (mode, list sizes)
+size_t encounter_scratch_bytes(int mode, int n1, int n2) {
+    if (mode == SWG_ENC_SORTSWEEP) return sas_scratch_bytes(n1 + n2);
+    return (size_t)3 * sizeof(float4) * (size_t)(n1 + n2) + 256;
 }
 
 // shift index2 by `shift` for entries [from, to)
@@ -503,7 +549,8 @@ int encounter_check_kind(swg_ctx *c, EncWork &w, int kind, int mode, int32_t n1,
         SWG_TRY(ensure(c, w.raw, (size_t)w.rawcap * 3 * sizeof(int32_t)));
     }
     const int ntot = (kind == 0 ? n1 : n1 + n2);
-    if (mode == SWG_ENC_SORTSWEEP) SWG_TRY(ensure(c, w.sort, sas_scratch_bytes(ntot)));
+    SWG_TRY(ensure(c, w.sort, encounter_scratch_bytes(mode, n1, kind == 0 ? n1 : n2)));
+    (void)ntot;
     unsigned long long h_count = 0;
     for (int attempt = 0; attempt < 8; attempt++) {
         int32_t *i1 = (int32_t *)w.raw.ptr, *i2 = i1 + w.rawcap, *lv = i2 + w.rawcap;

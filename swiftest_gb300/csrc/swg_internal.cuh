@@ -108,6 +108,8 @@ size_t sort_pairs_scratch_bytes(int64_t n);
 int sort_pairs_unique(swg_ctx *c, int64_t n, int32_t *i1, int32_t *i2, int32_t *lv, void *scratch,
                       unsigned long long *d_nout);
 size_t sas_scratch_bytes(int ntot);
+// scratch one encounter_launch call needs (the `sas_scratch` argument, either mode)
+size_t encounter_scratch_bytes(int mode, int n1, int n2);
 int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const double *v1, const double *renc1, int n2,
                      const double *r2, const double *v2, const double *renc2, int upper, int shift2, double dt,
                      long long cap, int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,

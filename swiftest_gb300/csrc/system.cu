@@ -120,12 +120,20 @@ struct Sum3 {
 
 // Sum over i of sign*term(i) for i = 0..n-1 (reverse: n-1..0); term components are
 // written by term_fn into the chunk arrays (with a 0/1 mask).
+// shared-memory workspace of ordered_sum3 (one per kernel)
+struct SumScratch {
+    double cx[RB], cy[RB], cz[RB];
+    double rx[RB / 32], ry[RB / 32], rz[RB / 32];
+    unsigned char cm[RB];
+    Sum3 acc;
+};
+
 template <class TermFn>
-__device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, double sign) {
-    __shared__ double cx[RB], cy[RB], cz[RB];
-    __shared__ unsigned char cm[RB];
-    __shared__ double rx[RB / 32], ry[RB / 32], rz[RB / 32];
-    __shared__ Sum3 acc;
+__device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, double sign, SumScratch &sh) {
+    double *cx = sh.cx, *cy = sh.cy, *cz = sh.cz, *rx = sh.rx, *ry = sh.ry, *rz = sh.rz;
+    unsigned char *cm = sh.cm;
+    Sum3 &acc = sh.acc;
+    __syncthreads();  // a previous sum's result may still be being read
     if (threadIdx.x == 0) acc = {0.0, 0.0, 0.0};
     __syncthreads();
     for (int c0 = 0; c0 < n; c0 += RB) {
@@ -191,7 +199,8 @@ __global__ void __launch_bounds__(RB) k_lindrift_pl(int npl, const double *__res
         z = Gm[i] * vb[3 * i + 2];
         return lmask[i] != 0;
     };
-    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, 1.0);
+    __shared__ SumScratch sh;
+    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, 1.0, sh);
     const double ptx = s.x / GMcb, pty = s.y / GMcb, ptz = s.z / GMcb;
     for (int i = threadIdx.x; i < npl; i += blockDim.x) {
         if (!lmask[i]) continue;
@@ -215,7 +224,8 @@ __global__ void __launch_bounds__(RB) k_vh2vb_pl(int npl, const double *__restri
         y = z = 0.0;
         return 1;
     };
-    const Sum3 g = ordered_sum3(npl, false, exact != 0, gm, 1.0);
+    __shared__ SumScratch sh;
+    const Sum3 g = ordered_sum3(npl, false, exact != 0, gm, 1.0, sh);
     const double Gmtot = GMcb + g.x;
     auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
         x = Gm[i] * vh[3 * i + 0];
@@ -223,7 +233,7 @@ __global__ void __launch_bounds__(RB) k_vh2vb_pl(int npl, const double *__restri
         z = Gm[i] * vh[3 * i + 2];
         return 1;
     };
-    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, -1.0);
+    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, -1.0, sh);
     const double cx = s.x / Gmtot, cy = s.y / Gmtot, cz = s.z / Gmtot;
     if (threadIdx.x == 0) {
         dcb[CB_VB + 0] = cx;
@@ -247,7 +257,8 @@ __global__ void __launch_bounds__(RB) k_vb2vh_pl(int npl, const double *__restri
         z = Gm[i] * vb[3 * i + 2] / GMcb;
         return status[i] != ST_INACTIVE;
     };
-    const Sum3 s = ordered_sum3(npl, true, exact != 0, term, -1.0);
+    __shared__ SumScratch sh;
+    const Sum3 s = ordered_sum3(npl, true, exact != 0, term, -1.0, sh);
     if (threadIdx.x == 0) {
         dcb[CB_VB + 0] = s.x;
         dcb[CB_VB + 1] = s.y;
@@ -508,6 +519,7 @@ struct RecArgs {
     int32_t *status, *tstatus, *levelg, *levelm, *tlevelg, *tlevelm;
     double GMcb, rhscale, dt;
     uint8_t *lenc, *good;           // list-sized byte scratch
+    double *terms;                  // 6 doubles per list entry
     int32_t *bpl, *btp;             // compact sets of bodies that appear in the lists
     int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
     int32_t *out;                   // [0] status, [1] deepest level reached
@@ -570,144 +582,136 @@ __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any
     __syncthreads();
 }
 
-// symba_kick_list_plpl (symba_kick.f90:126-232), serial in list order (one thread).
-// The reference's lmask refresh at entry is kept by the step loop instead
-// (lmask == status /= INACTIVE at every point the recursion can reach).
-__device__ void d_kick_list_plpl(const RecArgs &a, double dt, int irec, int sgn) {
-    const int64_t nenc = a.npp;
-    if (nenc == 0 || a.npl == 0) return;
-    const int64_t cap = a.ppcap;
-    const int32_t *i1 = a.pp, *i2 = a.pp + cap, *st = a.pp + 3 * cap;
-    uint8_t *good = a.good;
+// symba_kick_list_plpl / _pltp (symba_kick.f90:126-340) for one sign, whole block.
+// The per-pair factors (sqrt, divide, the shell polynomial) depend only on positions,
+// so every pair is evaluated in parallel into `terms`; thread 0 (pl-pl) and thread 32
+// (pl-tp) then apply the additions in list order, exactly as the reference's serial
+// loops do, which keeps the rounding of bodies that sit in several pairs.  The
+// reference's lmask refresh at entry is kept by the step loop instead (lmask ==
+// status /= INACTIVE wherever the recursion runs).
+__device__ void blk_kick_lists_sgn(const RecArgs &a, double dt, int irec, int sgn) {
+    const int64_t npp = a.npp, npt = a.npt;
+    if (npp + npt == 0) return;
     const int irm1 = irec - 1;
     const int irecl = sgn < 0 ? irec - 1 : irec;
-    int64_t ngood = 0;
-    for (int64_t k = 0; k < nenc; k++) {
-        const int i = i1[k] - 1, j = i2[k] - 1;
-        good[k] = (st[k] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.levelg[j] >= irm1);
-        ngood += good[k];
-    }
-    if (ngood == 0) return;
-    double *ah = a.ah, *vb = a.vb;
-    const double *rh = a.rh;
-    for (int64_t k = 0; k < nenc; k++) {
-        if (!good[k]) continue;
-        const int i = i1[k] - 1, j = i2[k] - 1;
-        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * j + d] = 0.0;
-    }
     const double rs2 = a.rhscale * a.rhscale;
     const double rshell_pow = d_powi(RSHELL, 2 * irecl);
-    for (int64_t k = 0; k < nenc; k++) {
-        if (!good[k]) continue;
-        const int i = i1[k] - 1, j = i2[k] - 1;
-        const double rhs = a.rhill[i] + a.rhill[j];
-        const double ri = ((rhs * rhs) * rs2) * rshell_pow;
-        const double rim1 = ri * (RSHELL * RSHELL);
-        double dx[3];
-        for (int d = 0; d < 3; d++) dx[d] = rh[3 * j + d] - rh[3 * i + d];
-        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-        double fac;
-        if (r2 < rim1) {
-            good[k] = 0;
-            continue;
-        }
-        if (r2 < ri) {
-            const double ris = sqrt(ri);
-            const double r = sqrt(r2);
-            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+    const int32_t *pi1 = a.pp, *pi2 = a.pp + a.ppcap, *pst = a.pp + 3 * a.ppcap;
+    const int32_t *ti1 = a.pt, *ti2 = a.pt + a.ptcap, *tst = a.pt + 3 * a.ptcap;
+    const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
+    // good flags
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        if (k < npp) {
+            const int i = pi1[k] - 1, j = pi2[k] - 1;
+            a.good[k] = do_pp && (pst[k] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.levelg[j] >= irm1);
         } else {
-            const double ir3 = 1.0 / (r2 * sqrt(r2));
-            fac = ir3;
+            const int64_t q = k - npp;
+            const int i = ti1[q] - 1, j = ti2[q] - 1;
+            a.good[k] = do_pt && (tst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
         }
-        const double faci = fac * a.Gm[i];
-        const double facj = fac * a.Gm[j];
-        for (int d = 0; d < 3; d++) {
-            ah[3 * i + d] = ah[3 * i + d] + facj * dx[d];
-            ah[3 * j + d] = ah[3 * j + d] - faci * dx[d];
-        }
-    }
-    for (int64_t k = 0; k < nenc; k++) {
-        if (!good[k]) continue;
-        const int i = i1[k] - 1, j = i2[k] - 1;
-        for (int d = 0; d < 3; d++) {
-            vb[3 * i + d] = vb[3 * i + d] + (double)sgn * dt * ah[3 * i + d];
-            vb[3 * j + d] = vb[3 * j + d] + (double)sgn * dt * ah[3 * j + d];
-        }
-        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * j + d] = 0.0;
-    }
-}
-
-// symba_kick_list_pltp (symba_kick.f90:235-340), serial in list order (one thread)
-__device__ void d_kick_list_pltp(const RecArgs &a, double dt, int irec, int sgn) {
-    const int64_t nenc = a.npt;
-    if (nenc == 0 || a.npl == 0 || a.ntp == 0) return;
-    const int64_t cap = a.ptcap;
-    const int32_t *i1 = a.pt, *i2 = a.pt + cap, *st = a.pt + 3 * cap;
-    uint8_t *good = a.good + a.npp;
-    const int irm1 = irec - 1;
-    const int irecl = sgn < 0 ? irec - 1 : irec;
-    int64_t ngood = 0;
-    for (int64_t k = 0; k < nenc; k++) {
-        const int i = i1[k] - 1, j = i2[k] - 1;
-        good[k] = (st[k] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
-        ngood += good[k];
-    }
-    if (ngood == 0) return;
-    double *tah = a.tah, *tvb = a.tvb;
-    for (int64_t k = 0; k < nenc; k++) {
-        if (!good[k]) continue;
-        const int j = i2[k] - 1;
-        for (int d = 0; d < 3; d++) tah[3 * j + d] = 0.0;
-    }
-    const double rs2 = a.rhscale * a.rhscale;
-    const double rshell_pow = d_powi(RSHELL, 2 * irecl);
-    for (int64_t k = 0; k < nenc; k++) {
-        if (!good[k]) continue;
-        const int i = i1[k] - 1, j = i2[k] - 1;
-        const double ri = ((a.rhill[i] * a.rhill[i]) * rs2) * rshell_pow;
-        const double rim1 = ri * (RSHELL * RSHELL);
-        double dx[3];
-        for (int d = 0; d < 3; d++) dx[d] = a.trh[3 * j + d] - a.rh[3 * i + d];
-        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-        double fac;
-        if (r2 < rim1) {
-            good[k] = 0;
-            continue;
-        }
-        if (r2 < ri) {
-            const double ris = sqrt(ri);
-            const double r = sqrt(r2);
-            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
-        } else {
-            const double ir3 = 1.0 / (r2 * sqrt(r2));
-            fac = ir3;
-        }
-        const double faci = fac * a.Gm[i];
-        for (int d = 0; d < 3; d++) tah[3 * j + d] = tah[3 * j + d] - faci * dx[d];
-    }
-    for (int64_t k = 0; k < nenc; k++) {
-        if (!good[k]) continue;
-        const int j = i2[k] - 1;
-        for (int d = 0; d < 3; d++) {
-            tvb[3 * j + d] = tvb[3 * j + d] + (double)sgn * dt * tah[3 * j + d];
-            tah[3 * j + d] = 0.0;
-        }
-    }
-}
-
-// One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): thread 0
-// kicks the pl-pl list, thread 32 the pl-tp list (disjoint data), then the block syncs.
-__device__ void blk_kick_lists(const RecArgs &a, double dt, int irecp, bool both) {
-    if (threadIdx.x == 0) {
-        d_kick_list_plpl(a, dt, irecp, 1);
-        if (both) d_kick_list_plpl(a, dt, irecp, -1);
-    } else if (threadIdx.x == 32) {
-        d_kick_list_pltp(a, dt, irecp, 1);
-        if (both) d_kick_list_pltp(a, dt, irecp, -1);
     }
     __syncthreads();
+    // zero the accelerations of the bodies in good pairs
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        if (!a.good[k]) continue;
+        if (k < npp) {
+            const int i = pi1[k] - 1, j = pi2[k] - 1;
+            for (int d = 0; d < 3; d++) a.ah[3 * i + d] = a.ah[3 * j + d] = 0.0;
+        } else {
+            const int j = ti2[k - npp] - 1;
+            for (int d = 0; d < 3; d++) a.tah[3 * j + d] = 0.0;
+        }
+    }
+    __syncthreads();
+    // per-pair terms
+    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+        if (!a.good[k]) continue;
+        const bool isp = k < npp;
+        const int64_t q = isp ? k : k - npp;
+        const int i = (isp ? pi1 : ti1)[q] - 1, j = (isp ? pi2 : ti2)[q] - 1;
+        double ri;
+        if (isp) {
+            const double rhs = a.rhill[i] + a.rhill[j];
+            ri = ((rhs * rhs) * rs2) * rshell_pow;
+        } else {
+            ri = ((a.rhill[i] * a.rhill[i]) * rs2) * rshell_pow;
+        }
+        const double rim1 = ri * (RSHELL * RSHELL);
+        const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
+        double dx[3];
+        for (int d = 0; d < 3; d++) dx[d] = rj[d] - a.rh[3 * i + d];
+        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        if (r2 < rim1) {
+            a.good[k] = 0;
+            continue;
+        }
+        double fac;
+        if (r2 < ri) {
+            const double ris = sqrt(ri);
+            const double r = sqrt(r2);
+            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
+            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+        } else {
+            const double ir3 = 1.0 / (r2 * sqrt(r2));
+            fac = ir3;
+        }
+        double *t = &a.terms[6 * k];
+        const double faci = fac * a.Gm[i];
+        if (isp) {
+            const double facj = fac * a.Gm[j];
+            for (int d = 0; d < 3; d++) {
+                t[d] = facj * dx[d];
+                t[3 + d] = faci * dx[d];
+            }
+        } else {
+            for (int d = 0; d < 3; d++) t[d] = faci * dx[d];
+        }
+    }
+    __syncthreads();
+    // ordered accumulation and velocity kick
+    if (threadIdx.x == 0) {
+        for (int64_t k = 0; k < npp; k++) {
+            if (!a.good[k]) continue;
+            const int i = pi1[k] - 1, j = pi2[k] - 1;
+            const double *t = &a.terms[6 * k];
+            for (int d = 0; d < 3; d++) {
+                a.ah[3 * i + d] = a.ah[3 * i + d] + t[d];
+                a.ah[3 * j + d] = a.ah[3 * j + d] - t[3 + d];
+            }
+        }
+        for (int64_t k = 0; k < npp; k++) {
+            if (!a.good[k]) continue;
+            const int i = pi1[k] - 1, j = pi2[k] - 1;
+            for (int d = 0; d < 3; d++) {
+                a.vb[3 * i + d] = a.vb[3 * i + d] + (double)sgn * dt * a.ah[3 * i + d];
+                a.vb[3 * j + d] = a.vb[3 * j + d] + (double)sgn * dt * a.ah[3 * j + d];
+            }
+            for (int d = 0; d < 3; d++) a.ah[3 * i + d] = a.ah[3 * j + d] = 0.0;
+        }
+    } else if (threadIdx.x == 32) {
+        for (int64_t q = 0; q < npt; q++) {
+            if (!a.good[npp + q]) continue;
+            const int j = ti2[q] - 1;
+            const double *t = &a.terms[6 * (npp + q)];
+            for (int d = 0; d < 3; d++) a.tah[3 * j + d] = a.tah[3 * j + d] - t[d];
+        }
+        for (int64_t q = 0; q < npt; q++) {
+            if (!a.good[npp + q]) continue;
+            const int j = ti2[q] - 1;
+            for (int d = 0; d < 3; d++) {
+                a.tvb[3 * j + d] = a.tvb[3 * j + d] + (double)sgn * dt * a.tah[3 * j + d];
+                a.tah[3 * j + d] = 0.0;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): the
+// +1 kicks of both lists, then (below level 0) the -1 kicks.
+__device__ void blk_kick_lists(const RecArgs &a, double dt, int irecp, bool both) {
+    blk_kick_lists_sgn(a, dt, irecp, 1);
+    if (both) blk_kick_lists_sgn(a, dt, irecp, -1);
 }
 
 // symba_drift_pl / _tp at level irec (symba_drift.f90:14-61) over the bodies that
@@ -994,71 +998,103 @@ __global__ void k_energy_rows(int n, const double *rb, const double *Gm, const i
     }
     rows[i] = row;
 }
-__global__ void k_energy_final(int n, int whm, const double *rh, const double *vh, const double *vbin,
-                               const double *Gm, const double *radius, const int32_t *status, double GMcb, double Rcb,
-                               int lclose, const double *rows, double *rb, double *out) {
-    if (threadIdx.x != 0) return;
+__global__ void __launch_bounds__(RB) k_energy_final(int n, int whm, const double *rh, const double *vh,
+                                                     const double *vbin, const double *Gm, const double *radius,
+                                                     const int32_t *status, double GMcb, double Rcb, int lclose,
+                                                     const double *rows, double *rb, double *out) {
+    __shared__ SumScratch sh;
     double cbvb[3];
     if (whm) {
-        double sum = 0.0;
-        for (int i = 0; i < n; i++) sum = sum + Gm[i];
-        const double Gmtot = GMcb + sum;
-        double c3[3] = {0, 0, 0};
-        for (int i = 0; i < n; i++)
-            for (int d = 0; d < 3; d++) c3[d] = c3[d] - Gm[i] * vh[3 * i + d];
-        for (int d = 0; d < 3; d++) cbvb[d] = c3[d] / Gmtot;
+        auto gm = [&](int i, double &x, double &y, double &z) -> unsigned char {
+            x = Gm[i];
+            y = z = 0.0;
+            return 1;
+        };
+        const double Gmtot = GMcb + ordered_sum3(n, false, false, gm, 1.0, sh).x;
+        auto t = [&](int i, double &x, double &y, double &z) -> unsigned char {
+            x = Gm[i] * vh[3 * i];
+            y = Gm[i] * vh[3 * i + 1];
+            z = Gm[i] * vh[3 * i + 2];
+            return 1;
+        };
+        const Sum3 c3 = ordered_sum3(n, false, false, t, -1.0, sh);
+        cbvb[0] = c3.x / Gmtot;
+        cbvb[1] = c3.y / Gmtot;
+        cbvb[2] = c3.z / Gmtot;
     } else {
-        double c3[3] = {0, 0, 0};
-        for (int i = n - 1; i >= 0; i--) {
-            if (status[i] == ST_INACTIVE) continue;
-            for (int d = 0; d < 3; d++) c3[d] = c3[d] - Gm[i] * vbin[3 * i + d] / GMcb;
-        }
-        for (int d = 0; d < 3; d++) cbvb[d] = c3[d];
+        auto t = [&](int i, double &x, double &y, double &z) -> unsigned char {
+            x = Gm[i] * vbin[3 * i] / GMcb;
+            y = Gm[i] * vbin[3 * i + 1] / GMcb;
+            z = Gm[i] * vbin[3 * i + 2] / GMcb;
+            return status[i] != ST_INACTIVE;
+        };
+        const Sum3 c3 = ordered_sum3(n, true, false, t, -1.0, sh);
+        cbvb[0] = c3.x;
+        cbvb[1] = c3.y;
+        cbvb[2] = c3.z;
     }
-    double Gmtot = GMcb, xt[3] = {0, 0, 0};
-    for (int i = 0; i < n; i++) {
-        if (status[i] == ST_INACTIVE) continue;
-        Gmtot = Gmtot + Gm[i];
-        for (int d = 0; d < 3; d++) xt[d] = xt[d] + Gm[i] * rh[3 * i + d];
-    }
-    double cbrb[3];
-    for (int d = 0; d < 3; d++) cbrb[d] = -xt[d] / Gmtot;
-    for (int i = 0; i < n; i++)
+    auto gact = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = Gm[i];
+        y = z = 0.0;
+        return status[i] != ST_INACTIVE;
+    };
+    const double gsum = ordered_sum3(n, false, false, gact, 1.0, sh).x;
+    const double Gmtot = GMcb + gsum;
+    auto xt = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = Gm[i] * rh[3 * i];
+        y = Gm[i] * rh[3 * i + 1];
+        z = Gm[i] * rh[3 * i + 2];
+        return status[i] != ST_INACTIVE;
+    };
+    const Sum3 x3 = ordered_sum3(n, false, false, xt, 1.0, sh);
+    const double cbrb[3] = {-x3.x / Gmtot, -x3.y / Gmtot, -x3.z / Gmtot};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
         for (int d = 0; d < 3; d++) rb[3 * i + d] = rh[3 * i + d] + cbrb[d];
-    const double mcb = GMcb;
-    const double kecb = mcb * (cbvb[0] * cbvb[0] + cbvb[1] * cbvb[1] + cbvb[2] * cbvb[2]);
-    double L[3] = {mcb * (cbrb[1] * cbvb[2] - cbrb[2] * cbvb[1]), mcb * (cbrb[2] * cbvb[0] - cbrb[0] * cbvb[2]),
-                   mcb * (cbrb[0] * cbvb[1] - cbrb[1] * cbvb[0])};
-    double kesum = 0.0, Lp[3] = {0, 0, 0}, pecb = 0.0, pecb_h = 0.0, be = 0.0, gsum = 0.0;
-    for (int i = 0; i < n; i++) {
-        if (status[i] == ST_INACTIVE) continue;
-        double v[3];
-        for (int d = 0; d < 3; d++) v[d] = whm ? vh[3 * i + d] + cbvb[d] : vbin[3 * i + d];
+    __syncthreads();
+    auto vel = [&](int i, int d) { return whm ? vh[3 * i + d] + cbvb[d] : vbin[3 * i + d]; };
+    auto Lt = [&](int i, double &x, double &y, double &z) -> unsigned char {
         const double *r = &rb[3 * i];
-        const double m = Gm[i];
-        Lp[0] = Lp[0] + m * (r[1] * v[2] - r[2] * v[1]);
-        Lp[1] = Lp[1] + m * (r[2] * v[0] - r[0] * v[2]);
-        Lp[2] = Lp[2] + m * (r[0] * v[1] - r[1] * v[0]);
-        kesum = kesum + m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-        pecb = pecb + (-GMcb * m / d_norm2s(r[0], r[1], r[2]));
-        pecb_h = pecb_h + (-GMcb * m / d_norm2s(rh[3 * i], rh[3 * i + 1], rh[3 * i + 2]));
-        if (lclose) be = be + (-3.0 * m * m / (5.0 * radius[i]));
-        gsum = gsum + m;
+        const double v0 = vel(i, 0), v1 = vel(i, 1), v2 = vel(i, 2);
+        x = Gm[i] * (r[1] * v2 - r[2] * v1);
+        y = Gm[i] * (r[2] * v0 - r[0] * v2);
+        z = Gm[i] * (r[0] * v1 - r[1] * v0);
+        return status[i] != ST_INACTIVE;
+    };
+    const Sum3 Lp = ordered_sum3(n, false, false, Lt, 1.0, sh);
+    auto kt = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        const double v0 = vel(i, 0), v1 = vel(i, 1), v2 = vel(i, 2);
+        x = Gm[i] * (v0 * v0 + v1 * v1 + v2 * v2);
+        y = -GMcb * Gm[i] / d_norm2s(rb[3 * i], rb[3 * i + 1], rb[3 * i + 2]);
+        z = -GMcb * Gm[i] / d_norm2s(rh[3 * i], rh[3 * i + 1], rh[3 * i + 2]);
+        return status[i] != ST_INACTIVE;
+    };
+    const Sum3 kp = ordered_sum3(n, false, false, kt, 1.0, sh);
+    auto bt = [&](int i, double &x, double &y, double &z) -> unsigned char {
+        x = lclose ? -3.0 * Gm[i] * Gm[i] / (5.0 * radius[i]) : 0.0;
+        y = rows[i];
+        z = 0.0;
+        return 1;
+    };
+    const Sum3 bp = ordered_sum3(n, false, false, bt, 1.0, sh);
+    if (threadIdx.x == 0) {
+        const double mcb = GMcb;
+        const double kecb = mcb * (cbvb[0] * cbvb[0] + cbvb[1] * cbvb[1] + cbvb[2] * cbvb[2]);
+        const double L[3] = {mcb * (cbrb[1] * cbvb[2] - cbrb[2] * cbvb[1]), mcb * (cbrb[2] * cbvb[0] - cbrb[0] * cbvb[2]),
+                             mcb * (cbrb[0] * cbvb[1] - cbrb[1] * cbvb[0])};
+        const double pe_pairs = bp.y;
+        const double pe = pe_pairs + kp.y;
+        const double be = bp.x;
+        const double ke = 0.5 * (kecb + kp.x);
+        out[0] = ke + pe + be;
+        out[1] = ke;
+        out[2] = pe;
+        out[3] = be;
+        out[4] = L[0] + Lp.x;
+        out[5] = L[1] + Lp.y;
+        out[6] = L[2] + Lp.z;
+        out[7] = GMcb + gsum;
+        out[8] = ke + (pe_pairs + kp.z) + be;
     }
-    double pe = 0.0;
-    for (int i = 0; i < n; i++) pe = pe + rows[i];
-    const double pe_pairs = pe;
-    pe = pe + pecb;
-    const double ke = 0.5 * (kecb + kesum);
-    out[0] = ke + pe + be;
-    out[1] = ke;
-    out[2] = pe;
-    out[3] = be;
-    out[4] = L[0] + Lp[0];
-    out[5] = L[1] + Lp[1];
-    out[6] = L[2] + Lp[2];
-    out[7] = GMcb + gsum;
-    out[8] = ke + (pe_pairs + pecb_h) + be;
 }
 
 }  // namespace
@@ -1331,8 +1367,8 @@ int symba_level0(swg_system *s, double dt, int *lany) {
             SWG_TRY(ensure(c, w[k]->raw, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
         }
     }
-    if (s->enc_plpl == SWG_ENC_SORTSWEEP) SWG_TRY(ensure(c, s->enc.sort, sas_scratch_bytes(s->npl)));
-    if (s->enc_pltp == SWG_ENC_SORTSWEEP) SWG_TRY(ensure(c, s->enc2.sort, sas_scratch_bytes(s->npl + s->ntp)));
+    SWG_TRY(ensure(c, s->enc.sort, encounter_scratch_bytes(s->enc_plpl, s->npl, s->npl)));
+    SWG_TRY(ensure(c, s->enc2.sort, encounter_scratch_bytes(s->enc_pltp, s->npl, s->ntp)));
     unsigned long long *h = (unsigned long long *)(s->h_flags + 8);
     auto launch = [&](int kind) -> int {
         EncWork &e = *w[kind];
@@ -1435,7 +1471,8 @@ int symba_level0(swg_system *s, double dt, int *lany) {
 int symba_recursion(swg_system *s, double dt) {
     swg_ctx *c = s->c;
     const int64_t n = s->plpl_n + s->pltp_n;
-    SWG_TRY(ensure(c, s->rec_scratch, (size_t)(2 * n + 64) + sizeof(int32_t) * (size_t)(3 * n + 64)));
+    SWG_TRY(ensure(c, s->rec_scratch, sizeof(double) * (size_t)(6 * n + 8) + (size_t)(2 * n + 64) +
+                                          sizeof(int32_t) * (size_t)(3 * n + 64)));
     RecArgs a;
     a.npl = s->npl;
     a.ntp = s->ntp;
@@ -1463,7 +1500,8 @@ int symba_recursion(swg_system *s, double dt) {
     a.GMcb = s->GMcb;
     a.rhscale = s->rhscale;
     a.dt = dt;
-    int32_t *ibuf = (int32_t *)s->rec_scratch.ptr;
+    a.terms = (double *)s->rec_scratch.ptr;
+    int32_t *ibuf = (int32_t *)(a.terms + 6 * n + 8);
     a.bpl = ibuf;                 // up to 2*npp + npt bodies
     a.btp = ibuf + 2 * n + 32;    // up to npt bodies
     uint8_t *bbuf = (uint8_t *)(ibuf + 3 * n + 64);
@@ -1763,12 +1801,12 @@ int swg_system_energy(swg_system *s, double *out) {
     double *dout = rb + 3 * std::max(n, 1);
     // barycentric positions first (energy rows need rb): the final kernel computes rb,
     // so run it twice: once for rb, then rows, then again for the totals.
-    k_energy_final<<<1, 32, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
+    k_energy_final<<<1, RB, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
                                             s->status, s->GMcb, s->Rcb, s->lclose, rows, rb, dout);
     SWG_TRY(L(c, "energy_rb"));
     k_energy_rows<<<grid_for(n, 128), 128, 0, c->stream>>>(n, rb, s->Gmass, s->status, rows);
     SWG_TRY(L(c, "energy_rows"));
-    k_energy_final<<<1, 32, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
+    k_energy_final<<<1, RB, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
                                             s->status, s->GMcb, s->Rcb, s->lclose, rows, rb, dout);
     SWG_TRY(L(c, "energy_final"));
     SWG_TRY(cuda_status(c, cudaMemcpyAsync(out, dout, 9 * 8, cudaMemcpyDeviceToHost, c->stream), "energy"));
