@@ -1,0 +1,65 @@
+"""Run one hot-path kernel on a C1-shaped workload, for profilers (ncu) and quick timing.
+
+    python -m swiftest_gb300.profile_cases <case> [--npl N] [--ntp M] [--reps R]
+
+cases: kick_tp_mixed, kick_pl_mixed, kick_tp_fp64, kick_pl_fp64, drift, encounter_pltp,
+encounter_plpl, symba_mixed, symba_fp64.  Inputs are the seeded C1 disk (AU, Msun, yr).
+Prints the average wall time per call (host buffers, so it includes the copies).
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("case")
+    p.add_argument("--npl", type=int, default=2000)
+    p.add_argument("--ntp", type=int, default=10000)
+    p.add_argument("--reps", type=int, default=3)
+    a = p.parse_args(argv)
+    from swiftest_gb300 import SWG_FP64, SWG_MIXED
+    from swiftest_gb300 import build as B
+    from swiftest_gb300 import initial_conditions as IC
+    from swiftest_gb300.api import Context, NBodySystem
+    B.build()
+    cb, pl, tp = IC.make_system(seed=0, npl=a.npl, ntp=a.ntp, amin=0.3, amax=3.0)
+    pl = IC.sort_for_integrator(pl, "SYMBA")
+    ctx = Context(0)
+    renc = pl["rhill"]
+    cases = {
+        "kick_tp_mixed": lambda: ctx.kick_getacch_int_all_tp(tp["rh"], pl["rh"], pl["Gmass"], precision=SWG_MIXED),
+        "kick_pl_mixed": lambda: ctx.kick_getacch_int_all_tri_pl(pl["rh"], pl["Gmass"], pl["radius"],
+                                                                 precision=SWG_MIXED),
+        "kick_tp_fp64": lambda: ctx.kick_getacch_int_all_tp(tp["rh"], pl["rh"], pl["Gmass"], precision=SWG_FP64),
+        "kick_pl_fp64": lambda: ctx.kick_getacch_int_all_tri_pl(pl["rh"], pl["Gmass"], pl["radius"],
+                                                                precision=SWG_FP64),
+        "drift": lambda: ctx.drift_all(IC.GMCB, tp["rh"], tp["vh"], 0.005),
+        "encounter_pltp": lambda: ctx.encounter_check_all_pltp(pl["rh"], pl["vh"], tp["rh"], tp["vh"], renc, 0.005),
+        "encounter_plpl": lambda: ctx.encounter_check_all_plpl(pl["rh"], pl["vh"], renc, 0.005),
+    }
+    if a.case.startswith("symba"):
+        prec = "MIXED" if a.case.endswith("mixed") else "FP64"
+        s = NBodySystem(ctx, "SYMBA", cb, pl, tp, dt=0.005, rhscale=1.0, precision=prec)
+        run = lambda: s.step(1)  # noqa: E731
+    else:
+        run = cases[a.case]
+    run()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        run()
+    ctx.synchronize()
+    print(f"{a.case}: {1e3 * (time.perf_counter() - t0) / a.reps:.3f} ms per call (host buffers)")
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
