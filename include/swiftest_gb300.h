@@ -139,7 +139,8 @@ int swg_system_get_tp(swg_system *sys, double *rh, double *vh, int32_t *status);
  * potential uses the body's barycentric distance), then te_helio: the same total with the
  * central-body potential at the heliocentric distance. */
 int swg_system_energy(swg_system *sys, double *out);
-/* out: steps with encounters, max recursion depth, sum plpl enc, sum pltp enc, collisions */
+/* out[6]: steps with encounters, max recursion depth, sum plpl enc, sum pltp enc, collisions,
+ * recursion sub-steps executed */
 int swg_system_stats(swg_system *sys, int64_t *out);
 /* level-0 encounter lists of the last step */
 int swg_system_plpl_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);

@@ -247,10 +247,11 @@ class OracleSystem:
                 "te_helio": out[8]}
 
     def stats(self):
-        out = np.zeros(5, np.int64)
+        out = np.zeros(6, np.int64)
         self.lib.orc_system_stats(self.h, _p(out))
         return {"steps_with_encounters": int(out[0]), "max_recursion": int(out[1]), "plpl_encounters": int(out[2]),
-                "pltp_encounters": int(out[3]), "collisions": int(out[4])}
+                "pltp_encounters": int(out[3]), "collisions": int(out[4]),
+                "recursion_substeps": int(out[5])}
 
     def plpl_list(self):
         n = self.lib.orc_system_plpl_list(self.h, 0, None, None)

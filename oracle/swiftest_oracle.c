@@ -906,7 +906,7 @@ struct orc_system {
     int irec;
     double t;
     enclist plpl, pltp;
-    int64_t stats[5];
+    int64_t stats[6];
     int64_t last_plpl_n, last_pltp_n;
     int32_t *last_plpl, *last_pltp;
 };
@@ -1713,6 +1713,7 @@ static int symba_recur(orc_system *s, int ireci) {
     if (dtl / s->dt < 2.220446049250313e-16) return -6; /* local time step too small */
     int irecp = ireci + 1;
     if (irecp > s->stats[1]) s->stats[1] = irecp;
+    s->stats[5] += nloops;
     int nloops = ireci == 0 ? 1 : NTENC;
     for (int j = 1; j <= nloops; j++) {
         int a = symba_list_check_plpl(s, dtl, irecp);

@@ -87,7 +87,8 @@ void orc_system_get_tp(const orc_system *s, double *rh, double *vh, int32_t *sta
 int32_t orc_system_npl(const orc_system *s);
 /* energy: te (total), L(3), ke_orbit, pe ; uses the reference's formulas */
 void orc_system_energy(orc_system *s, double *out /* te, ke, pe, be, Lx, Ly, Lz, GMtot, te_helio */);
-/* step-level counters: [n_steps_with_encounters, max_recursion_level, total_plpl_enc, total_pltp_enc, ncollisions] */
+/* step-level counters: [n_steps_with_encounters, max_recursion_level, total_plpl_enc, total_pltp_enc, ncollisions,
+ * recursion sub-steps] */
 void orc_system_stats(const orc_system *s, int64_t *out);
 /* last level-0 encounter lists */
 int64_t orc_system_plpl_list(const orc_system *s, int64_t cap, int32_t *i1, int32_t *i2);

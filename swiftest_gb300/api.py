@@ -9,6 +9,7 @@ order, which is the same memory as Fortran's (3, n); encounter indices are
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -40,8 +41,12 @@ class Context:
         if rc != L.SWG_OK:
             raise L.SwiftestGB300Error("swg_create", rc, "no usable CUDA device")
         self.h = h
+        self._systems = weakref.WeakSet()
 
     def close(self):
+        # the C context destroys the systems still attached to it; mark them closed
+        for s in list(getattr(self, "_systems", ())):
+            s.h = None
         if getattr(self, "h", None):
             self.lib.swg_destroy(self.h)
             self.h = None
@@ -202,6 +207,7 @@ class NBodySystem:
         ctx.check("swg_system_create", lib.swg_system_create(ctx.h, INTEGRATORS[self.integrator], npl, ntp,
                                                              C.byref(h)))
         self.h = h
+        ctx._systems.add(self)
         self.npl, self.ntp = npl, ntp
         ctx.check("swg_system_set_cb", lib.swg_system_set_cb(h, float(cb["Gmass"]), float(cb["radius"])))
         self._keep = []
@@ -264,10 +270,11 @@ class NBodySystem:
                 "te_helio": out[8]}
 
     def stats(self):
-        out = np.zeros(5, np.int64)
+        out = np.zeros(6, np.int64)
         self.ctx.check("swg_system_stats", self.ctx.lib.swg_system_stats(self.h, _ptr(out)))
         return {"steps_with_encounters": int(out[0]), "max_recursion": int(out[1]), "plpl_encounters": int(out[2]),
-                "pltp_encounters": int(out[3]), "collisions": int(out[4])}
+                "pltp_encounters": int(out[3]), "collisions": int(out[4]),
+                "recursion_substeps": int(out[5])}
 
     def _list(self, fn):
         n = C.c_int64(0)
@@ -289,9 +296,9 @@ class NBodySystem:
         return self._list("swg_system_pltp_list")
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
             self.ctx.lib.swg_system_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -108,6 +108,8 @@ int swg_create(swg_ctx **ctx, int device) {
 
 int swg_destroy(swg_ctx *c) {
     if (!c) return SWG_OK;
+    // systems still alive belong to this context: release them first
+    while (!c->systems.empty()) swg_system_destroy((swg_system *)c->systems.back());
     cudaStreamSynchronize(c->stream);
     for (auto &b : c->slot)
         if (b.ptr) cudaFree(b.ptr);

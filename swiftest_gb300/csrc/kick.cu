@@ -266,10 +266,11 @@ int ensure_kick_scratch(swg_ctx *c, DevBuf &buf, size_t bytes) {
     return cuda_status(c, cudaMemsetAsync(buf.ptr, 0, KICK_COUNTERS * sizeof(unsigned), c->stream), "memset");
 }
 
-// Chooses the partner split so that the grid covers ~2 blocks per SM.
+// Chooses the partner split so that the grid covers ~8 blocks (32 warps) per SM: the
+// pair loop is latency-bound (rsqrt and dependent FMAs), so occupancy hides it.
 int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart) {
     const int bx = div_up(nrecv, MBLOCK);
-    const int target = 2 * (c->num_sms > 0 ? c->num_sms : 152);
+    const int target = 8 * (c->num_sms > 0 ? c->num_sms : 152);
     int nchunk = div_up(target, bx);
     const int maxchunk = div_up(npart, MT);  // at least one tile per chunk
     if (nchunk > maxchunk) nchunk = maxchunk;

@@ -57,6 +57,7 @@ struct swg_ctx {
     swg::DevBuf slot[24];
     swg::EncWork enc;
     void *events[16] = {nullptr};  // measurement events (cudaEvent_t), created on first use
+    std::vector<void *> systems;   // live swg_system objects, destroyed with the context
 };
 
 namespace swg {

@@ -55,7 +55,7 @@ struct swg_system {
     int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail, [2] recursion status, [3] deepest level
     int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr;
     DevBuf rec_scratch;
-    int64_t stats[5] = {0, 0, 0, 0, 0};
+    int64_t stats[6] = {0, 0, 0, 0, 0, 0};
     // optional CUDA-event profile per kernel class (see PROF_* below)
     bool prof_on = false;
     std::vector<cudaEvent_t> prof_pool;
@@ -789,7 +789,7 @@ __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
         s_phase[0] = 0;
     }
     __syncthreads();
-    int deepest = 0;
+    int deepest = 0, substeps = 0;
     for (;;) {
         double p3 = 1.0;
         for (int k = 0; k < ireci; k++) p3 *= 3.0;
@@ -811,6 +811,7 @@ __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
                 break;
             }
             if (irecp > deepest) deepest = irecp;
+            substeps++;
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
             blk_list_check(a, irecp, dtl, &s_any);
@@ -844,7 +845,10 @@ __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
     __syncthreads();
     for (int b = threadIdx.x; b < nbpl; b += blockDim.x) a.mark_pl[a.bpl[b]] = 0;
     for (int b = threadIdx.x; b < nbtp; b += blockDim.x) a.mark_tp[a.btp[b]] = 0;
-    if (threadIdx.x == 0) atomicMax(&a.out[1], deepest);
+    if (threadIdx.x == 0) {
+        atomicMax(&a.out[1], deepest);
+        atomicAdd(&a.out[2], substeps);
+    }
 }
 
 // ---- WHM serial coordinate kernels (whm_coord.f90:14-124) and accelerations (whm_kick.f90:125-215)
@@ -1579,6 +1583,7 @@ int swg_system_create(swg_ctx *c, int integrator, int32_t npl, int32_t ntp, swg_
     if (!c || !out || npl < 0 || ntp < 0 || integrator < SWG_WHM || integrator > SWG_SYMBA) return SWG_ERR_ARG;
     swg_system *s = new swg_system();
     s->c = c;
+    c->systems.push_back(s);
     s->integrator = integrator;
     s->npl = npl;
     s->ntp = ntp;
@@ -1621,7 +1626,11 @@ int swg_system_create(swg_ctx *c, int integrator, int32_t npl, int32_t ntp, swg_
 int swg_system_destroy(swg_system *s) {
     if (!s) return SWG_OK;
     swg_ctx *c = s->c;
-    if (c) cudaStreamSynchronize(c->stream);
+    if (c) {
+        cudaStreamSynchronize(c->stream);
+        auto it = std::find(c->systems.begin(), c->systems.end(), (void *)s);
+        if (it != c->systems.end()) c->systems.erase(it);
+    }
     void *ptrs[] = {s->rh, s->vh, s->vb, s->ah, s->rbeg, s->rend, s->xj, s->vj, s->Gmass, s->radius, s->rhill,
                     s->eta, s->muj, s->ir3h, s->ir3j, s->status, s->lmask, s->levelg, s->levelm, s->nplenc,
                     s->ntpenc, s->iflag, s->trh, s->tvh, s->tvb, s->tah, s->tstatus, s->tlmask, s->tlevelg,
@@ -1819,6 +1828,7 @@ int swg_system_stats(swg_system *s, int64_t *out) {
         int32_t dev[4];
         SWG_TRY(cuda_status(s->c, cudaMemcpy(dev, s->rec_out, sizeof(dev), cudaMemcpyDeviceToHost), "stats"));
         s->stats[1] = dev[1];
+        s->stats[5] = dev[2];
     }
     std::memcpy(out, s->stats, sizeof(s->stats));
     return SWG_OK;

@@ -96,3 +96,16 @@ def test_symba_mixed_conservation(ctx):
     dLm = np.linalg.norm(em["L"] - e0["L"]) / np.linalg.norm(e0["L"])
     assert dEm < max(2 * dEf, 1e-9), (dEm, dEf)
     assert dLm < 1e-9
+
+
+def test_context_close_releases_systems():
+    # a system still open when its context closes is released by the context; closing it
+    # afterwards is a no-op (no use of the freed context)
+    from swiftest_gb300.api import Context
+    c = Context(0)
+    cb, pl, tp = _setup("SYMBA", 5, 50, 50)
+    s = NBodySystem(c, "SYMBA", cb, pl, tp, dt=0.005, rhscale=3.0)
+    s.step(2)
+    c.close()
+    s.close()
+    assert s.h is None
