@@ -1713,8 +1713,8 @@ static int symba_recur(orc_system *s, int ireci) {
     if (dtl / s->dt < 2.220446049250313e-16) return -6; /* local time step too small */
     int irecp = ireci + 1;
     if (irecp > s->stats[1]) s->stats[1] = irecp;
-    s->stats[5] += nloops;
     int nloops = ireci == 0 ? 1 : NTENC;
+    s->stats[5] += nloops;
     for (int j = 1; j <= nloops; j++) {
         int a = symba_list_check_plpl(s, dtl, irecp);
         int b = symba_list_check_pltp(s, dtl, irecp);
