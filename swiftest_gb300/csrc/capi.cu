@@ -144,7 +144,7 @@ int swg_kick_getacch_int_all_tri_pl(swg_ctx *c, int32_t npl, int32_t nplm, const
     SWG_TRY(stage_in(c, mem, 3, (const double *)acc, 3 * (size_t)npl, &da));
     if (precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, npl, npl);
-        SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, nch)));
+        SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, npl, nch)));
         SWG_TRY(kick_mixed_launch(c, false, npl, npl, nplm, dr, dr, dg, dR, nullptr, da, 0, nch, c->slot[10].ptr));
     } else {
         const int mode = (npl - nplm) > nplm ? KICK_SPLIT : KICK_DIRECT;
@@ -173,7 +173,7 @@ int swg_kick_getacch_int_all_flat_pl(swg_ctx *c, int32_t npl, int32_t nplm, int6
         }
         if (precision == SWG_MIXED) {
             const int nch = kick_mixed_chunks(c, npl, npl);
-            SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, nch)));
+            SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, npl, nch)));
             SWG_TRY(kick_mixed_launch(c, false, npl, npl, nplm, dr, dr, dg, dR, nullptr, da, 0, nch, c->slot[10].ptr));
         } else {
             SWG_TRY(kick_plpl_fp64(c, npl, nplm, dr, dg, dR, da, KICK_SPLIT, 0));
@@ -203,7 +203,7 @@ int swg_kick_getacch_int_all_tp(swg_ctx *c, int32_t ntp, int32_t npl, const doub
     SWG_TRY(stage_in(c, mem, 3, (const double *)acc, 3 * (size_t)ntp, &da));
     if (precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, ntp, npl);
-        SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(ntp, nch)));
+        SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(ntp, npl, nch)));
         SWG_TRY(kick_mixed_launch(c, true, ntp, npl, 0, drt, drp, dg, nullptr, dm, da, 0, nch, c->slot[10].ptr));
     } else {
         SWG_TRY(kick_tp_fp64(c, ntp, npl, drt, drp, dg, dm, da, 0));

@@ -10,12 +10,9 @@
 // The encounter decision is made in FP64 with the reference's expression order
 // (this file is compiled with -fmad=false), so lists are bit-identical to the
 // reference loop.  In TRIANGULAR mode a conservative FP32 prefilter first
-// rejects pairs whose closest approach over [0, dt] provably exceeds the
-// encounter radius:  min_t |x + v t| >= |x| - |v| dt.  The FP32 estimate of
-// |x| - |v| dt is lowered by a relative 2e-6 plus absolute terms covering the
-// hi/lo position split and the float rounding of velocities, and the radius is
-// raised by 1e-5 relative plus 4e-15 |x|^2/R, which bounds the FP64 rounding of
-// r^2 - (v.r)^2/v^2.  Only pairs the FP64 test could accept reach it, so the
+// rejects pairs whose closest approach over the step provably exceeds the
+// encounter radius (min_t |x + v t| >= |x| - |v| |dt|; see prefilter_reject for
+// the margins).  Only pairs the FP64 test could accept reach it, so the
 // prefilter changes speed, never the list.
 //
 // Output: pairs are appended with an atomic counter (up to cap), then sorted by
@@ -79,20 +76,25 @@ __device__ __forceinline__ BodyF load_body(const double *r, const double *v, con
     return o;
 }
 
-// true when the pair certainly fails encounter_check_one (see file header)
+// True when the pair certainly fails encounter_check_one.  The FP64 test accepts a
+// pair only if its computed r2min <= R^2, and that computed value is at least
+// D^2 - 6.7e-16 r^2 with D >= |x| - |v| |dt| (the closest approach of the linear
+// motion over the step).  So |x| (1 - 2.6e-8) > R + |v| |dt| guarantees rejection.
+// It is evaluated without square roots or divisions: |v| is bounded by the L1 norm
+// of the float velocity difference, and the comparison is made on squares,
+//     r^2 (1 - 4e-6) > (R (1 + 1e-5) + V |dt| + e_x)^2,
+// where the relative margins cover float rounding of r^2, R and |x| (< 1e-6) and
+// e_x, V's extra term cover the hi/lo position split and the float rounding of the
+// velocities.  NaN or inf inputs make the comparison false: such pairs go to the FP64 test.
 __device__ __forceinline__ bool prefilter_reject(const BodyF &p, const BodyF &q, float dtf) {
     const float dx = (p.a.x - q.a.x) + (p.b.x - q.b.x);
     const float dy = (p.a.y - q.a.y) + (p.b.y - q.b.y);
     const float dz = (p.a.z - q.a.z) + (p.b.z - q.b.z);
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    const float dvx = p.v.x - q.v.x, dvy = p.v.y - q.v.y, dvz = p.v.z - q.v.z;
-    const float vmag = sqrtf(dvx * dvx + dvy * dvy + dvz * dvz);
-    const float R = p.a.w + q.a.w;
-    const float xlo = sqrtf(r2) * (1.0f - 2e-6f) - 1e-13f * (p.b.w + q.b.w);
-    const float vhi = vmag * (1.0f + 2e-6f) + 2e-7f * (p.v.w + q.v.w);
-    const float dlo = xlo - vhi * dtf;
-    const float rhi = R * (1.0f + 1e-5f) + 4e-15f * (r2 / R);
-    return dlo > rhi;  // NaN/inf comparisons are false: such pairs go to the FP64 test
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float vl1 = fabsf(p.v.x - q.v.x) + fabsf(p.v.y - q.v.y) + fabsf(p.v.z - q.v.z);
+    const float vhi = fmaf(vl1, 1.0f + 2e-6f, 2e-7f * (p.v.w + q.v.w));
+    const float reff = fmaf(p.a.w + q.a.w, 1.0f + 1e-5f, fmaf(vhi, dtf, 1e-13f * (p.b.w + q.b.w)));
+    return r2 * (1.0f - 4e-6f) > reff * reff;
 }
 
 // Float copies of the bodies for the prefilter, written once per check.
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(ET) k_encounter_tri(
         q.v = V2[j];
     }
     const int own_end = upper ? min(iend, j) : iend;
-    const float dtf = __double2float_ru(dt) * (1.0f + 1e-6f);
+    const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);  // |dt| bounds either direction of time
     for (int i0 = ibeg; i0 < iend; i0 += EP) {
         if (threadIdx.x < EP && i0 + threadIdx.x < iend) {
             sa[threadIdx.x] = A1[i0 + threadIdx.x];

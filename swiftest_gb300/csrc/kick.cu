@@ -57,7 +57,9 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
                                                       const double *__restrict__ Gm, const double *__restrict__ R,
                                                       const int32_t *__restrict__ lmask, double *__restrict__ acc,
                                                       int acc_is_zero, int chunk, float *__restrict__ partial,
-                                                      unsigned *__restrict__ counters) {
+                                                      unsigned *__restrict__ counters,
+                                                      const float4 *__restrict__ pA, const float4 *__restrict__ pB) {
+    // pA/pB (optional): partners already split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R)
     __shared__ float4 sA[MT];  // x_hi, y_hi, z_hi, Gm
     __shared__ float4 sB[MT];  // x_lo, y_lo, z_lo, R
     __shared__ bool s_last;
@@ -78,7 +80,10 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
         for (int t = threadIdx.x; t < MT; t += MBLOCK) {
             const int jl = j0 + t;
             float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (jl < jstop) {
+            if (jl < jstop && pA) {
+                a = pA[jl];
+                b = pB[jl];
+            } else if (jl < jstop) {
                 split_hi_lo(rpart[3 * jl + 0], a.x, b.x);
                 split_hi_lo(rpart[3 * jl + 1], a.y, b.y);
                 split_hi_lo(rpart[3 * jl + 2], a.z, b.z);
@@ -176,6 +181,23 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
     if (threadIdx.x == 0) counters[blockIdx.x] = 0u;  // re-arm for the next launch
 }
 
+// Partners split once per kick into float hi/lo pairs (the conversion runs on the
+// FP64 pipe, which is narrow on GB300; doing it here instead of in every block
+// keeps the pair kernel on the FP32 pipe).
+__global__ void k_kick_split(int n, const double *__restrict__ r, const double *__restrict__ Gm,
+                             const double *__restrict__ R, float4 *A, float4 *B) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float4 a, b;
+    split_hi_lo(r[3 * j + 0], a.x, b.x);
+    split_hi_lo(r[3 * j + 1], a.y, b.y);
+    split_hi_lo(r[3 * j + 2], a.z, b.z);
+    a.w = __double2float_rn(Gm[j]);
+    b.w = R ? __double2float_rn(R[j]) : 0.f;
+    A[j] = a;
+    B[j] = b;
+}
+
 // ------------------------------------------------------------------ pair lists
 // Serial pass over an explicit pair list, restating the flat loop
 // (swiftest_kick.f90:69-115) in list order: ahi/ahj accumulate per body.
@@ -252,8 +274,9 @@ __global__ void k_apply_pairs(int npl, const double *__restrict__ ahi, const dou
 // ------------------------------------------------------------------ launchers
 static inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
-size_t kick_mixed_scratch_bytes(int nrecv, int nchunk) {
-    return KICK_COUNTERS * sizeof(unsigned) + (size_t)nchunk * nrecv * 6 * sizeof(float) + 256;
+size_t kick_mixed_scratch_bytes(int nrecv, int npart, int nchunk) {
+    return KICK_COUNTERS * sizeof(unsigned) + (size_t)nchunk * nrecv * 6 * sizeof(float) +
+           (size_t)2 * sizeof(float4) * (size_t)npart + 512;
 }
 
 int ensure_kick_scratch(swg_ctx *c, DevBuf &buf, size_t bytes) {
@@ -289,17 +312,23 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
     if (bx > (int)KICK_COUNTERS) return SWG_ERR_ARG;
     unsigned *counters = (unsigned *)scratch;
     float *partial = (float *)((char *)scratch + KICK_COUNTERS * sizeof(unsigned));
+    const size_t poff = ((KICK_COUNTERS * sizeof(unsigned) + (size_t)nchunk * nrecv * 6 * sizeof(float)) + 255) & ~size_t(255);
+    float4 *pA = (float4 *)((char *)scratch + poff), *pB = pA + npart;
+    if (npart > 0) {
+        k_kick_split<<<div_up(npart, 256), 256, 0, c->stream>>>(npart, rpart, Gm, tp ? nullptr : R, pA, pB);
+        c->launches++;
+    }
     dim3 grid(bx, nchunk);
     if (tp)
         k_kick_mixed<true, false><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, 0, rrecv, rpart, Gm, nullptr, lmask,
-                                                                  acc, acc_is_zero, chunk, partial, counters);
+                                                                  acc, acc_is_zero, chunk, partial, counters, pA, pB);
     else if (R)
         k_kick_mixed<false, true><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, nplm, rrecv, rpart, Gm, R, nullptr,
-                                                                  acc, acc_is_zero, chunk, partial, counters);
+                                                                  acc, acc_is_zero, chunk, partial, counters, pA, pB);
     else
         k_kick_mixed<false, false><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, nplm, rrecv, rpart, Gm, nullptr,
                                                                    nullptr, acc, acc_is_zero, chunk, partial,
-                                                                   counters);
+                                                                   counters, pA, pB);
     c->launches++;
     return launch_status(c, "kick_mixed");
 }
@@ -325,10 +354,10 @@ cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, int num_sms, int npl,
     dim3 grid(bx, nchunk);
     if (R)
         k_kick_mixed<false, true><<<grid, MBLOCK, 0, stream>>>(npl, npl, nplm, r, r, Gm, R, nullptr, acc, 0, chunk,
-                                                               partial, counters);
+                                                               partial, counters, nullptr, nullptr);
     else
         k_kick_mixed<false, false><<<grid, MBLOCK, 0, stream>>>(npl, npl, nplm, r, r, Gm, nullptr, nullptr, acc, 0,
-                                                                chunk, partial, counters);
+                                                                chunk, partial, counters, nullptr, nullptr);
     return cudaGetLastError();
 }
 

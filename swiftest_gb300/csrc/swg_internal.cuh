@@ -83,7 +83,7 @@ int kick_plpl_fp64(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const
                    double *acc, int mode, int acc_is_zero);
 int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const double *rpl, const double *Gm,
                  const int32_t *lmask, double *acc, int acc_is_zero);
-size_t kick_mixed_scratch_bytes(int nrecv, int nchunk);
+size_t kick_mixed_scratch_bytes(int nrecv, int npart, int nchunk);
 int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart);
 int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const double *rrecv, const double *rpart,
                       const double *Gm, const double *R, const int32_t *lmask, double *acc, int acc_is_zero,

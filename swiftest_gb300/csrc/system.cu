@@ -525,10 +525,17 @@ struct RecArgs {
     int32_t *out;                   // [0] status, [1] deepest level reached
 };
 
+// Item index of this thread in the recursion kernel's block loops: consecutive items go
+// to different warps, hence to different SM sub-partitions.  The few pairs and bodies
+// of an encounter each run a long serial FP64 chain, and GB300's narrow FP64 pipe
+// takes about as long for a warp instruction with one active lane as with 32, so
+// spreading them over the four sub-partitions' pipes is what runs them concurrently.
+__device__ __forceinline__ int spread_tid() { return (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+
 // symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), whole block.
 __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any) {
     const int64_t npp = a.npp, npt = a.npt;
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
         const bool isp = k < npp;
         const int64_t q = isp ? k : k - npp;
         int32_t *l = isp ? a.pp : a.pt;
@@ -560,7 +567,7 @@ __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any
         a.lenc[k] = le_out;
     }
     __syncthreads();
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
+    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
         if (!a.lenc[k]) continue;
         *s_any = 1;
         const bool isp = k < npp;
@@ -584,12 +591,16 @@ __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any
 
 // symba_kick_list_plpl / _pltp (symba_kick.f90:126-340) for one sign, whole block.
 // The per-pair factors (sqrt, divide, the shell polynomial) depend only on positions,
-// so every pair is evaluated in parallel into `terms`; thread 0 (pl-pl) and thread 32
-// (pl-tp) then apply the additions in list order, exactly as the reference's serial
-// loops do, which keeps the rounding of bodies that sit in several pairs.  The
+// so every pair is evaluated in parallel into `terms`.  The additions are then made
+// by one thread per body, which walks the list in order and adds only its own terms:
+// each body receives exactly the reference's additions in the reference's order,
+// while GB300's narrow FP64 pipe sees one instruction stream for all bodies instead
+// of one serial stream per pair.  A body that sits in several pairs gets its velocity
+// kicked once with its full acceleration, as in the reference (its later pairs add
+// zero).  good[k]: 0 not kicked, 1 kicked, 2 zeroed then skipped (r^2 < rim1).  The
 // reference's lmask refresh at entry is kept by the step loop instead (lmask ==
 // status /= INACTIVE wherever the recursion runs).
-__device__ void blk_kick_lists_sgn(const RecArgs &a, double dt, int irec, int sgn) {
+__device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, double dt, int irec, int sgn) {
     const int64_t npp = a.npp, npt = a.npt;
     if (npp + npt == 0) return;
     const int irm1 = irec - 1;
@@ -599,36 +610,20 @@ __device__ void blk_kick_lists_sgn(const RecArgs &a, double dt, int irec, int sg
     const int32_t *pi1 = a.pp, *pi2 = a.pp + a.ppcap, *pst = a.pp + 3 * a.ppcap;
     const int32_t *ti1 = a.pt, *ti2 = a.pt + a.ptcap, *tst = a.pt + 3 * a.ptcap;
     const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
-    // good flags
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
-        if (k < npp) {
-            const int i = pi1[k] - 1, j = pi2[k] - 1;
-            a.good[k] = do_pp && (pst[k] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.levelg[j] >= irm1);
-        } else {
-            const int64_t q = k - npp;
-            const int i = ti1[q] - 1, j = ti2[q] - 1;
-            a.good[k] = do_pt && (tst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
-        }
-    }
-    __syncthreads();
-    // zero the accelerations of the bodies in good pairs
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
-        if (!a.good[k]) continue;
-        if (k < npp) {
-            const int i = pi1[k] - 1, j = pi2[k] - 1;
-            for (int d = 0; d < 3; d++) a.ah[3 * i + d] = a.ah[3 * j + d] = 0.0;
-        } else {
-            const int j = ti2[k - npp] - 1;
-            for (int d = 0; d < 3; d++) a.tah[3 * j + d] = 0.0;
-        }
-    }
-    __syncthreads();
-    // per-pair terms
-    for (int64_t k = threadIdx.x; k < npp + npt; k += blockDim.x) {
-        if (!a.good[k]) continue;
+    // good flags and per-pair terms
+    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
         const bool isp = k < npp;
         const int64_t q = isp ? k : k - npp;
         const int i = (isp ? pi1 : ti1)[q] - 1, j = (isp ? pi2 : ti2)[q] - 1;
+        bool g;
+        if (isp)
+            g = do_pp && (pst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.levelg[j] >= irm1);
+        else
+            g = do_pt && (tst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
+        if (!g) {
+            a.good[k] = 0;
+            continue;
+        }
         double ri;
         if (isp) {
             const double rhs = a.rhill[i] + a.rhill[j];
@@ -642,9 +637,10 @@ __device__ void blk_kick_lists_sgn(const RecArgs &a, double dt, int irec, int sg
         for (int d = 0; d < 3; d++) dx[d] = rj[d] - a.rh[3 * i + d];
         const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
         if (r2 < rim1) {
-            a.good[k] = 0;
+            a.good[k] = 2;
             continue;
         }
+        a.good[k] = 1;
         double fac;
         if (r2 < ri) {
             const double ris = sqrt(ri);
@@ -668,39 +664,61 @@ __device__ void blk_kick_lists_sgn(const RecArgs &a, double dt, int irec, int sg
         }
     }
     __syncthreads();
-    // ordered accumulation and velocity kick
-    if (threadIdx.x == 0) {
-        for (int64_t k = 0; k < npp; k++) {
-            if (!a.good[k]) continue;
-            const int i = pi1[k] - 1, j = pi2[k] - 1;
-            const double *t = &a.terms[6 * k];
-            for (int d = 0; d < 3; d++) {
-                a.ah[3 * i + d] = a.ah[3 * i + d] + t[d];
-                a.ah[3 * j + d] = a.ah[3 * j + d] - t[3 + d];
+    // ordered per-body accumulation and the velocity kick
+    const double sdt = (double)sgn * dt;
+    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
+        const bool isp = b < nbpl;
+        const int body = isp ? a.bpl[b] : a.btp[b - nbpl];
+        bool zeroed = false, kicked = false;
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        if (isp) {
+            for (int64_t k = 0; k < npp; k++) {
+                const int i = pi1[k] - 1, j = pi2[k] - 1;
+                if (i != body && j != body) continue;
+                const uint8_t g = a.good[k];
+                if (g == 0) continue;
+                zeroed = true;
+                if (g != 1) continue;
+                kicked = true;
+                const double *t = &a.terms[6 * k];
+                if (i == body) {
+                    ax = ax + t[0];
+                    ay = ay + t[1];
+                    az = az + t[2];
+                } else {
+                    ax = ax - t[3];
+                    ay = ay - t[4];
+                    az = az - t[5];
+                }
             }
-        }
-        for (int64_t k = 0; k < npp; k++) {
-            if (!a.good[k]) continue;
-            const int i = pi1[k] - 1, j = pi2[k] - 1;
-            for (int d = 0; d < 3; d++) {
-                a.vb[3 * i + d] = a.vb[3 * i + d] + (double)sgn * dt * a.ah[3 * i + d];
-                a.vb[3 * j + d] = a.vb[3 * j + d] + (double)sgn * dt * a.ah[3 * j + d];
+            if (zeroed) {
+                if (kicked) {
+                    a.vb[3 * body + 0] = a.vb[3 * body + 0] + sdt * ax;
+                    a.vb[3 * body + 1] = a.vb[3 * body + 1] + sdt * ay;
+                    a.vb[3 * body + 2] = a.vb[3 * body + 2] + sdt * az;
+                }
+                a.ah[3 * body + 0] = a.ah[3 * body + 1] = a.ah[3 * body + 2] = 0.0;
             }
-            for (int d = 0; d < 3; d++) a.ah[3 * i + d] = a.ah[3 * j + d] = 0.0;
-        }
-    } else if (threadIdx.x == 32) {
-        for (int64_t q = 0; q < npt; q++) {
-            if (!a.good[npp + q]) continue;
-            const int j = ti2[q] - 1;
-            const double *t = &a.terms[6 * (npp + q)];
-            for (int d = 0; d < 3; d++) a.tah[3 * j + d] = a.tah[3 * j + d] - t[d];
-        }
-        for (int64_t q = 0; q < npt; q++) {
-            if (!a.good[npp + q]) continue;
-            const int j = ti2[q] - 1;
-            for (int d = 0; d < 3; d++) {
-                a.tvb[3 * j + d] = a.tvb[3 * j + d] + (double)sgn * dt * a.tah[3 * j + d];
-                a.tah[3 * j + d] = 0.0;
+        } else {
+            for (int64_t q = 0; q < npt; q++) {
+                if (ti2[q] - 1 != body) continue;
+                const uint8_t g = a.good[npp + q];
+                if (g == 0) continue;
+                zeroed = true;
+                if (g != 1) continue;
+                kicked = true;
+                const double *t = &a.terms[6 * (npp + q)];
+                ax = ax - t[0];
+                ay = ay - t[1];
+                az = az - t[2];
+            }
+            if (zeroed) {
+                if (kicked) {
+                    a.tvb[3 * body + 0] = a.tvb[3 * body + 0] + sdt * ax;
+                    a.tvb[3 * body + 1] = a.tvb[3 * body + 1] + sdt * ay;
+                    a.tvb[3 * body + 2] = a.tvb[3 * body + 2] + sdt * az;
+                }
+                a.tah[3 * body + 0] = a.tah[3 * body + 1] = a.tah[3 * body + 2] = 0.0;
             }
         }
     }
@@ -709,15 +727,15 @@ __device__ void blk_kick_lists_sgn(const RecArgs &a, double dt, int irec, int sg
 
 // One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): the
 // +1 kicks of both lists, then (below level 0) the -1 kicks.
-__device__ void blk_kick_lists(const RecArgs &a, double dt, int irecp, bool both) {
-    blk_kick_lists_sgn(a, dt, irecp, 1);
-    if (both) blk_kick_lists_sgn(a, dt, irecp, -1);
+__device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, double dt, int irecp, bool both) {
+    blk_kick_lists_sgn(a, nbpl, nbtp, dt, irecp, 1);
+    if (both) blk_kick_lists_sgn(a, nbpl, nbtp, dt, irecp, -1);
 }
 
 // symba_drift_pl / _tp at level irec (symba_drift.f90:14-61) over the bodies that
 // appear in the lists (every other body has levelg == -1 inside the recursion).
 __device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec, double dt) {
-    for (int b = threadIdx.x; b < nbpl + nbtp; b += blockDim.x) {
+    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
         const bool isp = b < nbpl;
         const int i = isp ? a.bpl[b] : a.btp[b - nbpl];
         const int32_t *lev = isp ? a.levelg : a.tlevelg;
@@ -741,7 +759,7 @@ __device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec, double
 // symba_step_set_recur_levels_system (symba_step.f90:118-160)
 __device__ void blk_set_recur_levels(const RecArgs &a, int nbpl, int nbtp, int ireci) {
     const int irecp = ireci + 1;
-    for (int b = threadIdx.x; b < nbpl + nbtp; b += blockDim.x) {
+    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
         int32_t *lev = b < nbpl ? &a.levelg[a.bpl[b]] : &a.tlevelg[a.btp[b - nbpl]];
         if (*lev == irecp) *lev = ireci;
     }
@@ -815,7 +833,7 @@ __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
             blk_list_check(a, irecp, dtl, &s_any);
-            blk_kick_lists(a, dth, irecp, ireci != 0);
+            blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
             blk_drift(a, nbpl, nbtp, ireci, dtl);
             const int any = s_any;
             __syncthreads();
@@ -834,7 +852,7 @@ __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
             }
         }
         // after the deeper levels (or none) for loop j of level ireci
-        blk_kick_lists(a, dth, irecp, ireci != 0);
+        blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
         blk_set_recur_levels(a, nbpl, nbtp, ireci);
         if (threadIdx.x == 0) {
             s_j[ireci]++;
@@ -1127,7 +1145,7 @@ int accel_int_pl(swg_system *s, int acc_is_zero) {
     const int32_t nplm = symba ? s->nplm : s->npl;
     if (s->precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, s->npl, s->npl);
-        SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->npl, nch)));
+        SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->npl, s->npl, nch)));
         return kick_mixed_launch(c, false, s->npl, s->npl, nplm, s->rh, s->rh, s->Gmass, rad, nullptr, s->ah,
                                  acc_is_zero, nch, s->kick_scratch.ptr);
     }
@@ -1164,7 +1182,7 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
         ProfScope ps(s, PROF_KICK_TP);
         if (s->precision == SWG_MIXED) {
             const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
-            SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, nch)));
+            SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, s->npl, nch)));
             SWG_TRY(kick_mixed_launch(c, true, s->ntp, s->npl, 0, s->trh, rp, s->Gmass, nullptr, s->tlmask, s->tah,
                                       1, nch, s->kick_scratch.ptr));
         } else {
@@ -1285,7 +1303,7 @@ int whm_accel_tp(swg_system *s, int lbeg, int zero) {
     SWG_TRY(L(c, "whm_tp_ah0"));
     if (s->precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
-        SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, nch)));
+        SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, s->npl, nch)));
         return kick_mixed_launch(c, true, s->ntp, s->npl, 0, s->trh, rp, s->Gmass, nullptr, s->tlmask, s->tah, 0,
                                  nch, s->kick_scratch.ptr);
     }
