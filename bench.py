@@ -1,21 +1,28 @@
 #!/usr/bin/env python
-"""Benchmark: SyMBA body-steps/s on one GB300 for the C1 disk (2000 massive bodies
-+ 10 000 test particles, 1-Hill-radius encounter radius, dt = 0.005 yr).
+"""Benchmark: SyMBA body-steps/s on one GB300, mixed precision + batched vs the FP64 GPU path.
 
-A step is one symba_step_system call on the device-resident system.  The
-headline ``value`` is the mixed-precision path (FP32 pair kicks with float-float
-sums; FP64 drift, encounter tests and recursion); the FP64 path runs the same
-steps from the same initial conditions and is reported beside it together with
-both paths' |dE/E| and |dL/L| (matched-accuracy comparison).
+Workload (default ``--workload c4``): the batched planetesimal-disk ensemble, 256
+independent SyMBA systems with N_pl log-uniform in [500, 5000] (547,900 massive bodies in
+total for seed 0), masses log-uniform in [1e-11, 1e-7] Msun, a in [0.5, 2] AU, e and i
+Rayleigh(0.02), dt = 0.002 yr, 1-Hill-radius encounter radius (RHSCALE = 1), TRIANGULAR
+level-0 checks, recursive encounter kicks in FP64.  A step advances every system by one
+symba_step_system.  ``--workload c1`` runs the single-system C1 disk (2000 pl + 10 000 tp)
+instead.
 
-Timing: W untimed warm-up steps, then K steps, each preceded by an untimed
-512 MB memset that evicts L2 (the C1 working set, ~3 MB, would otherwise sit in
-L2), each bracketed by CUDA events on the library's stream.  Under torchrun the
-ranks run independent replicas (SyMBA does not shard across GPUs here) with a
-barrier and the max time over ranks.
+``value``: body-steps/s of the mixed-precision batched path (FP32 pair kicks with
+float-float sums; FP64 drift, encounter decisions, recursion) with the state resident in
+HBM.  The FP64 path (same kernels' FP64 variants, bit-identical to the reference loop
+order) runs the same warm-up and timed steps from the same initial conditions; both
+paths' |dE/E| and |dL/L| over those steps are reported (matched-accuracy comparison).
 
-``--impl reference`` times the CPU restatement of the reference (the oracle,
-OpenMP) on the same workload on rank 0.
+Timing: W untimed warm-up steps, then K steps, each preceded by an untimed 512 MB memset
+that evicts L2 (the C4 state, ~60 MB, would otherwise sit in the 129 MB L2), each bracketed
+by CUDA events on the library's stream.  Under torchrun the ranks run independent replicas
+(weak scaling; an ensemble shards by system with no exchange) with a barrier and the max
+time over ranks.
+
+``--impl reference`` times the CPU restatement of the reference (the oracle, OpenMP) on a
+bounded sample of the same workload on rank 0.
 """
 from __future__ import annotations
 
@@ -43,10 +50,10 @@ def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=30)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--npl", type=int, default=2000)
-    p.add_argument("--ntp", type=int, default=10000)
+    p.add_argument("--workload", default="c4", choices=["c4", "c1"])
+    p.add_argument("--nsys", type=int, default=None, help="first NSYS systems of the C4 ensemble")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     return p.parse_args()
 
@@ -63,23 +70,98 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
-def workload(args):
-    from swiftest_gb300 import initial_conditions as IC
-    cfg = dict(IC.CONFIGS["C1"])
-    cfg["npl"], cfg["ntp"] = args.npl, args.ntp
-    cb, pl, tp = IC.make_system(seed=cfg["seed"], npl=cfg["npl"], ntp=cfg["ntp"], mmin=cfg["mmin"], mmax=cfg["mmax"],
-                                amin=cfg["amin"], amax=cfg["amax"], sig_e=cfg["sig_e"], sig_i=cfg["sig_i"])
-    pl = IC.sort_for_integrator(pl, "SYMBA")
-    return cfg, cb, pl, tp
+# ---------------------------------------------------------------- workloads
+class C4:
+    """The batched SyMBA ensemble (CSR-packed systems stepped together)."""
+
+    def __init__(self, args):
+        from swiftest_gb300 import initial_conditions as IC
+        self.E = IC.make_ensemble("C4", nsys=args.nsys)
+        self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
+        self.pairs_per_step = 2 * float(sum(int(n) * (int(n) - 1) for n in self.E["npl"]))
+
+    def make(self, ctx, precision):
+        from swiftest_gb300.api import Ensemble
+        return Ensemble(ctx, self.E, precision=precision)
+
+    def state_arrays(self):
+        E = self.E
+        return [(int(E["npl"].sum()), 3), (int(E["npl"].sum()), 3), (int(E["ntp"].sum()), 3), (int(E["ntp"].sum()), 3)]
+
+    def config(self, precision):
+        n = self.E["npl"]
+        return {"workload": f"C4 batched SyMBA ensemble: {len(n)} planetesimal disks, N_pl log-uniform in "
+                            f"[500, 5000] ({int(n.sum())} pl total, 0 tp), m in [1e-11, 1e-7] Msun, a in [0.5, 2] AU, "
+                            "e,i Rayleigh(0.02), dt=0.002 yr, RHSCALE=1.0 (1 Hill radius), TRIANGULAR level-0 checks",
+                "nsys": len(n), "npl_total": int(n.sum()), "ntp_total": int(self.E["ntp"].sum()),
+                "npl_min": int(n.min()), "npl_max": int(n.max()), "dt": self.E["dt"], "rhscale": self.E["rhscale"],
+                "seed": 0, "precision": precision, "l2": "flushed before every timed step (512 MB memset, untimed)"}
+
+    def oracle_sample(self, budget_s, steps_per_system=1):
+        """Oracle steps over systems 0, 1, ... until the time budget is used."""
+        from oracle import oracle as O
+        from swiftest_gb300 import initial_conditions as IC
+        cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
+        bs, t_all, nsys = 0, 0.0, 0
+        for pl, tp in self.E["systems"]:
+            s = O.OracleSystem("SYMBA", cb, pl, None, dt=self.E["dt"], rhscale=self.E["rhscale"], lclose=True)
+            t0 = time.perf_counter()
+            s.step(steps_per_system)
+            t_all += time.perf_counter() - t0
+            bs += len(pl["Gmass"]) * steps_per_system
+            nsys += 1
+            if t_all > budget_s:
+                break
+        return bs, t_all, f"{steps_per_system} SyMBA step(s) of each of the first {nsys} C4 systems ({bs} body-steps)"
 
 
-def config_block(cfg, precision):
-    return {"workload": f"C1 SyMBA disk: {cfg['npl']} pl + {cfg['ntp']} tp, a in [{cfg['amin']}, {cfg['amax']}] AU, "
-                        f"RHSCALE={cfg['rhscale']} (1 Hill radius), dt={cfg['dt']} yr, TRIANGULAR encounter checks",
-            "npl": cfg["npl"], "ntp": cfg["ntp"], "dt": cfg["dt"], "rhscale": cfg["rhscale"], "seed": cfg["seed"],
-            "precision": precision, "l2": "flushed before every timed step (512 MB memset, untimed)"}
+class C1:
+    """The single-system C1 disk."""
+
+    def __init__(self, args):
+        from swiftest_gb300 import initial_conditions as IC
+        cfg = dict(IC.CONFIGS["C1"])
+        cb, pl, tp = IC.make_system(seed=cfg["seed"], npl=cfg["npl"], ntp=cfg["ntp"], mmin=cfg["mmin"],
+                                    mmax=cfg["mmax"], amin=cfg["amin"], amax=cfg["amax"], sig_e=cfg["sig_e"],
+                                    sig_i=cfg["sig_i"])
+        self.cfg, self.cb, self.pl, self.tp = cfg, cb, IC.sort_for_integrator(pl, "SYMBA"), tp
+        self.nbodies = cfg["npl"] + cfg["ntp"]
+        npl, ntp = cfg["npl"], cfg["ntp"]
+        self.pairs_per_step = 2.0 * (npl * (npl - 1) + npl * ntp)
+
+    def make(self, ctx, precision):
+        from swiftest_gb300.api import NBodySystem
+        c = self.cfg
+        return NBodySystem(ctx, "SYMBA", self.cb, self.pl, self.tp, dt=c["dt"], rhscale=c["rhscale"], lclose=True,
+                           precision=precision)
+
+    def state_arrays(self):
+        n, m = self.cfg["npl"], self.cfg["ntp"]
+        return [(n, 3), (n, 3), (m, 3), (m, 3)]
+
+    def config(self, precision):
+        c = self.cfg
+        return {"workload": f"C1 SyMBA disk: {c['npl']} pl + {c['ntp']} tp, a in [{c['amin']}, {c['amax']}] AU, "
+                            f"RHSCALE={c['rhscale']} (1 Hill radius), dt={c['dt']} yr, TRIANGULAR encounter checks",
+                "npl": c["npl"], "ntp": c["ntp"], "dt": c["dt"], "rhscale": c["rhscale"], "seed": c["seed"],
+                "precision": precision, "l2": "flushed before every timed step (512 MB memset, untimed)"}
+
+    def oracle_sample(self, budget_s):
+        from oracle import oracle as O
+        c = self.cfg
+        s = O.OracleSystem("SYMBA", self.cb, self.pl, self.tp, dt=c["dt"], rhscale=c["rhscale"], lclose=True)
+        s.step(1)
+        n, t0 = 0, time.perf_counter()
+        while True:
+            s.step(1)
+            n += 1
+            el = time.perf_counter() - t0
+            if el > budget_s or n >= 200:
+                break
+        return self.nbodies * n, el, f"{n} SyMBA steps of the C1 system ({self.nbodies} bodies) after 1 warm-up step"
 
 
+# ---------------------------------------------------------------- measurement
 class ClockSampler:
     """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
 
@@ -133,16 +215,33 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
 def rel_energy(e0, e1):
-    dE = abs(e1["te_helio"] - e0["te_helio"]) / abs(e0["te_helio"])
-    dE_ref = abs(e1["te"] - e0["te"]) / abs(e0["te"])
-    dL = float(np.linalg.norm(e1["L"] - e0["L"]) / np.linalg.norm(e0["L"]))
-    return dE, dE_ref, dL
+    """|dE/E| (heliocentric central-body potential and the reference's formula) and |dL/L|,
+    as arrays over systems (one entry for a single system)."""
+    def arr(x):
+        return np.atleast_1d(np.asarray(x, dtype=np.float64))
+    dE = np.abs(arr(e1["te_helio"]) - arr(e0["te_helio"])) / np.abs(arr(e0["te_helio"]))
+    dEr = np.abs(arr(e1["te"]) - arr(e0["te"])) / np.abs(arr(e0["te"]))
+    L0, L1 = np.atleast_2d(e0["L"]), np.atleast_2d(e1["L"])
+    dL = np.linalg.norm(L1 - L0, axis=1) / np.linalg.norm(L0, axis=1)
+    return dE, dEr, dL
 
 
-def run_path(ctx, cfg, cb, pl, tp, precision, steps, warmup, profile=False, clocks=None):
-    from swiftest_gb300.api import NBodySystem
-    s = NBodySystem(ctx, "SYMBA", cb, pl, tp, dt=cfg["dt"], rhscale=cfg["rhscale"], lclose=True, precision=precision)
+def err_summary(dE, dEr, dL):
+    return {"dE_E_max": float(dE.max()), "dE_E_median": float(np.median(dE)), "dE_E_ref_formula_max": float(dEr.max()),
+            "dL_L_max": float(dL.max())}
+
+
+def run_path(ctx, wl, precision, steps, warmup, profile=False, clocks=None):
+    s = wl.make(ctx, precision)
     e0 = s.energy()
     s.step(warmup)
     ctx.synchronize()
@@ -150,8 +249,7 @@ def run_path(ctx, cfg, cb, pl, tp, precision, steps, warmup, profile=False, cloc
     if profile:
         s.profile(True)
     total_ms = 0.0
-    cm = clocks if clocks is not None else _Null()
-    with cm:
+    with clocks if clocks is not None else _Null():
         for _ in range(steps):
             ctx.flush_l2()
             ctx.event_record(0)
@@ -168,23 +266,13 @@ def run_path(ctx, cfg, cb, pl, tp, precision, steps, warmup, profile=False, cloc
     return total_ms, launches, prof, rel_energy(e0, e1), stats
 
 
-class _Null:
-    def __enter__(self):
-        return self
-
-    def __exit__(self, *a):
-        return False
-
-
-def run_e2e(ctx, cfg, cb, pl, tp, precision, steps):
-    """Same metric through the C ABI with host buffers: every step uploads the
-    state (pinned host arrays -> device), steps once, and reads the state back."""
+def run_e2e(ctx, wl, precision, steps):
+    """The same metric through the public API with host buffers: every step uploads the
+    state (pinned host arrays -> device), steps once and reads the state back."""
     import torch
-    from swiftest_gb300.api import NBodySystem
-    s = NBodySystem(ctx, "SYMBA", cb, pl, tp, dt=cfg["dt"], rhscale=cfg["rhscale"], lclose=True, precision=precision)
+    s = wl.make(ctx, precision)
     s.step(2)
-    npl, ntp = s.npl, s.ntp
-    pinned = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for n in (npl, npl, ntp, ntp)]
+    pinned = [torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for shape in wl.state_arrays()]
     s.get_state_async(*pinned)
     ctx.synchronize()
     total_ms = 0.0
@@ -201,51 +289,42 @@ def run_e2e(ctx, cfg, cb, pl, tp, precision, steps):
     return total_ms, nbytes
 
 
-def cpu_baseline(cfg, cb, pl, tp, budget_s):
-    """The oracle (C restatement of the reference's OpenMP path) on this host: steps of
-    the same C1 system until the time budget is used."""
-    from oracle import oracle as O
+def cpu_baseline(wl, budget_s):
+    """The oracle (C restatement of the reference's OpenMP path) on this host, on a bounded
+    sample of the same workload."""
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    s = O.OracleSystem("SYMBA", cb, pl, tp, dt=cfg["dt"], rhscale=cfg["rhscale"], lclose=True)
-    s.step(1)
-    n, t0 = 0, time.perf_counter()
-    while True:
-        s.step(1)
-        n += 1
-        el = time.perf_counter() - t0
-        if el > budget_s or n >= 200:
-            break
-    nb = cfg["npl"] + cfg["ntp"]
-    return {"value": nb * n / el, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)),
-            "kind": "port",
-            "sample": f"{n} SyMBA steps of the same C1 system ({nb} bodies) after 1 warm-up step, "
-                      f"{el:.1f} s wall, C restatement of the reference loops with OpenMP"}
+    from oracle import oracle as O
+    O.build()
+    bs, el, sample = wl.oracle_sample(budget_s)
+    return {"value": bs / el, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)), "kind": "port",
+            "sample": f"{sample}, {el:.1f} s, C restatement of the reference loops with OpenMP"}
 
 
 def reference_arm(args, world, rank):
     if rank != 0:
         return 0
-    cfg, cb, pl, tp = workload(args)
-    from oracle import oracle as O
-    O.build()
+    wl = C4(args) if args.workload == "c4" else C1(args)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    s = O.OracleSystem("SYMBA", cb, pl, tp, dt=cfg["dt"], rhscale=cfg["rhscale"], lclose=True)
-    s.step(max(args.warmup, 1))
-    t0 = time.perf_counter()
-    s.step(args.steps)
-    el = time.perf_counter() - t0
-    nb = cfg["npl"] + cfg["ntp"]
-    v = nb * args.steps / el
+    from oracle import oracle as O
+    O.build()
+    budget = max(2.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        wl.oracle_sample(budget / 4)
+    bs_tot, el_tot, sample = 0, 0.0, ""
+    for _ in range(args.steps):
+        bs, el, sample = wl.oracle_sample(budget)
+        bs_tot += bs
+        el_tot += el
+    v = bs_tot / el_tot
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded C1 disk)",
-            "config": config_block(cfg, "FP64 CPU"),
+            "warmup": args.warmup, "ms_per_step": 1e3 * el_tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng)",
+            "config": wl.config("FP64 CPU"),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-                             "sample": f"{args.steps} timed SyMBA steps of the full C1 system after {args.warmup} "
-                                       "warm-up steps (C restatement of the reference's OpenMP loops; the Fortran "
-                                       "reference cannot be compiled on this image)"},
+                             "sample": f"each step: {sample} (C restatement of the reference's OpenMP loops; the "
+                                       "Fortran reference cannot be compiled on this image)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -269,65 +348,59 @@ def main():
     from swiftest_gb300 import build as B
     B.build()
     from swiftest_gb300.api import Context
-    cfg, cb, pl, tp = workload(args)
+    wl = C4(args) if args.workload == "c4" else C1(args)
     ctx = Context(local)
-    nb = cfg["npl"] + cfg["ntp"]
     clocks = ClockSampler(local)
     if td:
         td.barrier()
-    ms_mixed, launches, prof, (dE_m, dEr_m, dL_m), st_m = run_path(ctx, cfg, cb, pl, tp, "MIXED", args.steps,
-                                                                    args.warmup, profile=True, clocks=clocks)
-    ms_fp64, _, prof64, (dE_f, dEr_f, dL_f), st_f = run_path(ctx, cfg, cb, pl, tp, "FP64", args.steps, args.warmup,
-                                                             profile=True)
+    ms_mixed, launches, prof, err_m, st_m = run_path(ctx, wl, "MIXED", args.steps, args.warmup, profile=True,
+                                                     clocks=clocks)
+    ms_fp64, _, prof64, err_f, st_f = run_path(ctx, wl, "FP64", args.steps, args.warmup, profile=True)
     if td:
         import torch
         t = torch.tensor([ms_mixed, ms_fp64], dtype=torch.float64)
         td.all_reduce(t, op=td.ReduceOp.MAX)
         ms_mixed, ms_fp64 = float(t[0]), float(t[1])
-    e2e_ms, e2e_bytes = run_e2e(ctx, cfg, cb, pl, tp, "MIXED", args.steps)
+    e2e_ms, e2e_bytes = run_e2e(ctx, wl, "MIXED", args.steps)
+    nb = wl.nbodies
     value = world * nb * args.steps / (ms_mixed * 1e-3)
     fp64_value = world * nb * args.steps / (ms_fp64 * 1e-3)
 
-    # roofline of the dominant kernel class (mixed path), from the live CUDA-event profile
-    npl, ntp = cfg["npl"], cfg["ntp"]
-    flops_per_launch = {"kick_pl": FLOPS_PER_INTERACTION * npl * (npl - 1),
-                        "kick_tp": FLOPS_PER_INTERACTION * npl * ntp}
-    dom = max(prof, key=lambda k: prof[k]["ms"])
-    roof = None
+    # roofline of the pair kick (mixed path), from the live CUDA-event profile on the library's stream
     peak32 = ctx.probe_peak_tflops("fp32")
     peak64 = ctx.probe_peak_tflops("fp64")
     traffic = load_traffic()
-    kick_cls = max(("kick_pl", "kick_tp"), key=lambda k: prof[k]["ms"])
-    if prof[kick_cls]["launches"]:
-        avg_ms = prof[kick_cls]["ms"] / prof[kick_cls]["launches"]
-        ach = flops_per_launch[kick_cls] / (avg_ms * 1e-3) / 1e12
-        roof = {"kernel": f"{kick_cls} (mixed FP32 pair kick)", "bound": "fp32", "achieved": ach, "peak": peak32,
-                "unit": "TFLOP/s", "frac": ach / peak32 if peak32 else None,
-                "peak_source": "FP32 FFMA-chain probe measured by bench.py on this GPU (MEASURED_PEAKS.json "
-                               "has no FP32 figure)",
-                "algorithmic_flops_per_launch": flops_per_launch[kick_cls], "avg_launch_ms": avg_ms,
-                "traffic": traffic.get(kick_cls)}
+    roof = None
+    kick = prof["kick_pl"]
+    if kick["launches"]:
+        avg_ms = kick["ms"] / kick["launches"]
+        flops = FLOPS_PER_INTERACTION * wl.pairs_per_step / 2  # one pl-pl evaluation
+        ach = flops / (avg_ms * 1e-3) / 1e12
+        roof = {"kernel": "kick_pl (mixed FP32 pair kick, batched persistent launch)", "bound": "fp32",
+                "achieved": ach, "peak": peak32, "unit": "TFLOP/s", "frac": ach / peak32 if peak32 else None,
+                "peak_source": "FP32 FFMA-chain probe measured by bench.py on this GPU (MEASURED_PEAKS.json has no "
+                               "FP32 figure)",
+                "algorithmic_flops_per_launch": flops, "avg_launch_ms": avg_ms,
+                "traffic": traffic.get(f"kick_pl_{args.workload}")}
     kernel_profile = {k: {"launches": v["launches"], "ms_total": round(v["ms"], 4),
                           "share": round(v["ms"] / ms_mixed, 4)} for k, v in prof.items()}
-    cpu = cpu_baseline(cfg, cb, pl, tp, args.cpu_seconds) if rank == 0 else None
-    csum = clocks.summary()
-    pairs_per_step = 2 * (npl * (npl - 1) + npl * ntp)
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    cpu = cpu_baseline(wl, args.cpu_seconds) if rank == 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_mixed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 (f32 pair kicks)", "data": "synthetic (seeded C1 disk, numpy default_rng)",
-        "config": config_block(cfg, "mixed"),
-        "fp64_path": {"value": fp64_value, "ms_per_step": ms_fp64 / args.steps, "dE_E": dE_f, "dE_E_ref_formula": dEr_f,
-                      "dL_L": dL_f, "stats": st_f,
+        "dtype": "f64 (f32 pair kicks)", "data": "synthetic (seeded, numpy default_rng)",
+        "config": wl.config("mixed"),
+        "fp64_path": {"value": fp64_value, "ms_per_step": ms_fp64 / args.steps, **err_summary(*err_f), "stats": st_f,
                       "kernel_profile": {k: {"launches": v["launches"], "ms_total": round(v["ms"], 4)}
                                          for k, v in prof64.items()}},
-        "mixed_path": {"dE_E": dE_m, "dE_E_ref_formula": dEr_m, "dL_L": dL_m, "stats": st_m},
+        "mixed_path": {**err_summary(*err_m), "stats": st_m},
         "speedup_mixed_vs_fp64": value / fp64_value,
-        "pair_interactions_per_s": pairs_per_step * args.steps / (ms_mixed * 1e-3),
+        "pair_interactions_per_s": world * wl.pairs_per_step * args.steps / (ms_mixed * 1e-3),
         "kernel_profile": kernel_profile, "dominant_kernel_class": dom,
         "roofline": roof, "fp64_peak_probe_tflops": peak64,
         "cpu_baseline": cpu,
-        "clocks": csum,
+        "clocks": clocks.summary(),
         "e2e": {"value": world * nb * args.steps / (e2e_ms * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": e2e_bytes // 2, "d2h_bytes_per_step": e2e_bytes // 2},
         "gpu_launches": int(launches),

@@ -154,6 +154,42 @@ int swg_system_pltp_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, 
 int swg_system_set_state(swg_system *sys, const double *rh, const double *vh, const double *trh, const double *tvh);
 int swg_system_get_state_async(swg_system *sys, double *rh, double *vh, double *trh, double *tvh);
 
+/* ---- batched ensembles of independent systems -------------------------------------
+ * No single counterpart in the reference, which integrates one system per run: an
+ * ensemble is many runs of helio_step_system / symba_step_system (helio_step.f90:14-119,
+ * symba_step.f90:14-331) advanced together, each system taking exactly the steps it
+ * would take alone (bit-identical in SWG_FP64).  Systems are packed CSR-style: arrays
+ * of massive bodies are the concatenation of every system's (3, npl[s]) block in system
+ * order (test particles likewise with ntp[s]), each block sorted as the reference's
+ * initialize leaves it (by mass, descending).  All systems share dt; GMTINY is not
+ * supported.  integrator: SWG_HELIO or SWG_SYMBA (TRIANGULAR level-0 checks). */
+typedef struct swg_ensemble swg_ensemble;
+int swg_ensemble_create(swg_ctx *ctx, int integrator, int32_t nsys, const int32_t *npl, const int32_t *ntp,
+                        swg_ensemble **ens);
+int swg_ensemble_destroy(swg_ensemble *ens);
+/* per-system central body: GMcb[nsys], Rcb[nsys] (Rcb may be NULL) */
+int swg_ensemble_set_cb(swg_ensemble *ens, const double *GMcb, const double *Rcb);
+int swg_ensemble_set_pl(swg_ensemble *ens, const double *rh, const double *vh, const double *Gmass,
+                        const double *radius, const double *rhill);
+int swg_ensemble_set_tp(swg_ensemble *ens, const double *rh, const double *vh);
+int swg_ensemble_set_param(swg_ensemble *ens, double dt, double rhscale, int lclose, int precision);
+int swg_ensemble_initialize(swg_ensemble *ens);
+int swg_ensemble_step(swg_ensemble *ens, int32_t nsteps);
+int swg_ensemble_get_pl(swg_ensemble *ens, double *rh, double *vh, int32_t *status);
+int swg_ensemble_get_tp(swg_ensemble *ens, double *rh, double *vh, int32_t *status);
+/* out[9*nsys]: per system the nine values of swg_system_energy */
+int swg_ensemble_energy(swg_ensemble *ens, double *out);
+/* out[6] over all systems: system-steps with encounters, max recursion depth, sum plpl
+ * enc, sum pltp enc, collisions, recursion sub-steps */
+int swg_ensemble_stats(swg_ensemble *ens, int64_t *out);
+/* level-0 pl-pl list of system sys from the last step, indices local to the system */
+int swg_ensemble_plpl_list(swg_ensemble *ens, int32_t sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
+int swg_ensemble_set_state(swg_ensemble *ens, const double *rh, const double *vh, const double *trh,
+                           const double *tvh);
+int swg_ensemble_get_state_async(swg_ensemble *ens, double *rh, double *vh, double *trh, double *tvh);
+int swg_ensemble_profile(swg_ensemble *ens, int enable);
+int swg_ensemble_profile_read(swg_ensemble *ens, double *out);
+
 /* ---- measurement helpers (no counterpart in the reference) ------------------------
  * Per-kernel-class CUDA-event profile of the step loop: classes 0 pl-pl kick,
  * 1 pl-tp kick, 2 drift, 3 level-0 encounter checks, 4 SyMBA recursion lists.

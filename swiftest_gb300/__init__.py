@@ -9,12 +9,12 @@ from ._lib import (SWG_ENC_SORTSWEEP, SWG_ENC_TRIANGULAR, SWG_FP64, SWG_HELIO, S
                    SwiftestGB300Error)
 
 __all__ = ["_lib", "SWG_FP64", "SWG_MIXED", "SWG_ENC_TRIANGULAR", "SWG_ENC_SORTSWEEP", "SWG_WHM", "SWG_HELIO",
-           "SWG_SYMBA", "SwiftestGB300Error", "Context", "NBodySystem"]
+           "SWG_SYMBA", "SwiftestGB300Error", "Context", "NBodySystem", "Ensemble"]
 
 
 def __getattr__(name):
     # the compute classes load the shared library on first use (no fallback)
-    if name in ("Context", "NBodySystem"):
+    if name in ("Context", "NBodySystem", "Ensemble"):
         from . import api
         return getattr(api, name)
     raise AttributeError(name)

@@ -61,7 +61,7 @@ SIGNATURES = {
     "swg_system_initialize": (_INT, [_P]),
     "swg_system_step": (_INT, [_P, _I32]),
     "swg_system_get_pl": (_INT, [_P, _P, _P, _P]),
-    "swg_system_get_tp": (_INT, [_P, _P, _P]),
+    "swg_system_get_tp": (_INT, [_P, _P, _P, _P]),
     "swg_system_energy": (_INT, [_P, _P]),
     "swg_system_stats": (_INT, [_P, _P]),
     "swg_system_plpl_list": (_INT, [_P, _I64, C.POINTER(_I64), _P, _P]),
@@ -70,6 +70,23 @@ SIGNATURES = {
     "swg_system_get_state_async": (_INT, [_P, _P, _P, _P, _P]),
     "swg_system_profile": (_INT, [_P, _INT]),
     "swg_system_profile_read": (_INT, [_P, _P]),
+    "swg_ensemble_create": (_INT, [_P, _INT, _I32, _P, _P, C.POINTER(_P)]),
+    "swg_ensemble_destroy": (_INT, [_P]),
+    "swg_ensemble_set_cb": (_INT, [_P, _P, _P]),
+    "swg_ensemble_set_pl": (_INT, [_P, _P, _P, _P, _P, _P]),
+    "swg_ensemble_set_tp": (_INT, [_P, _P, _P]),
+    "swg_ensemble_set_param": (_INT, [_P, _D, _D, _INT, _INT]),
+    "swg_ensemble_initialize": (_INT, [_P]),
+    "swg_ensemble_step": (_INT, [_P, _I32]),
+    "swg_ensemble_get_pl": (_INT, [_P, _P, _P, _P]),
+    "swg_ensemble_get_tp": (_INT, [_P, _P, _P, _P]),
+    "swg_ensemble_energy": (_INT, [_P, _P]),
+    "swg_ensemble_stats": (_INT, [_P, _P]),
+    "swg_ensemble_plpl_list": (_INT, [_P, _I32, _I64, C.POINTER(_I64), _P, _P]),
+    "swg_ensemble_set_state": (_INT, [_P, _P, _P, _P, _P]),
+    "swg_ensemble_get_state_async": (_INT, [_P, _P, _P, _P, _P]),
+    "swg_ensemble_profile": (_INT, [_P, _INT]),
+    "swg_ensemble_profile_read": (_INT, [_P, _P]),
     "swg_flush_l2": (_INT, [_P, _I64]),
     "swg_event_record": (_INT, [_P, _INT]),
     "swg_event_elapsed": (_INT, [_P, _INT, _INT, C.POINTER(_D)]),

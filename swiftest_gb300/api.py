@@ -44,7 +44,7 @@ class Context:
         self._systems = weakref.WeakSet()
 
     def close(self):
-        # the C context destroys the systems still attached to it; mark them closed
+        # the C context destroys the systems and ensembles still attached to it; mark them closed
         for s in list(getattr(self, "_systems", ())):
             s.h = None
         if getattr(self, "h", None):
@@ -298,6 +298,120 @@ class NBodySystem:
     def close(self):
         if getattr(self, "h", None) and getattr(self.ctx, "h", None):
             self.ctx.lib.swg_system_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """Many independent systems stepped together (``swg_ensemble``), CSR-packed.
+
+    ``ens`` is the dict of ``initial_conditions.make_ensemble``: per-system ``npl``,
+    ``ntp``, ``GMcb``, ``Rcb`` and the concatenated, per-system sorted body arrays.
+    Each system takes exactly the steps of ``NBodySystem`` with the same integrator
+    (bit-identical with precision="FP64").
+    """
+
+    PROFILE_CLASSES = NBodySystem.PROFILE_CLASSES
+
+    def __init__(self, ctx: Context, ens: dict, dt=None, rhscale=None, lclose=True, precision="FP64"):
+        self.ctx = ctx
+        lib = ctx.lib
+        self.integrator = ens["integrator"].upper()
+        self.npl = _i32(ens["npl"])
+        self.ntp = _i32(ens["ntp"])
+        self.nsys = len(self.npl)
+        self.NPL, self.NTP = int(self.npl.sum()), int(self.ntp.sum())
+        self.poff = np.concatenate([[0], np.cumsum(self.npl)]).astype(np.int64)
+        self.toff = np.concatenate([[0], np.cumsum(self.ntp)]).astype(np.int64)
+        h = C.c_void_p()
+        ctx.check("swg_ensemble_create", lib.swg_ensemble_create(ctx.h, INTEGRATORS[self.integrator], self.nsys,
+                                                                 _ptr(self.npl), _ptr(self.ntp), C.byref(h)))
+        self.h = h
+        ctx._systems.add(self)
+        ctx.check("swg_ensemble_set_cb", lib.swg_ensemble_set_cb(h, _ptr(_f64(ens["GMcb"])), _ptr(_f64(ens["Rcb"]))))
+        pl, tp = ens["pl"], ens["tp"]
+        if self.NPL:
+            arrs = [_f64(pl["rh"], (self.NPL, 3)), _f64(pl["vh"], (self.NPL, 3)), _f64(pl["Gmass"]),
+                    _f64(pl["radius"]), _f64(pl["rhill"])]
+            ctx.check("swg_ensemble_set_pl", lib.swg_ensemble_set_pl(h, *[_ptr(a) for a in arrs]))
+        if self.NTP:
+            arrs = [_f64(tp["rh"], (self.NTP, 3)), _f64(tp["vh"], (self.NTP, 3))]
+            ctx.check("swg_ensemble_set_tp", lib.swg_ensemble_set_tp(h, *[_ptr(a) for a in arrs]))
+        prec = {"FP64": L.SWG_FP64, "MIXED": L.SWG_MIXED}[precision.upper()]
+        ctx.check("swg_ensemble_set_param", lib.swg_ensemble_set_param(
+            h, float(ens["dt"] if dt is None else dt), float(ens["rhscale"] if rhscale is None else rhscale),
+            int(bool(lclose)), prec))
+        ctx.check("swg_ensemble_initialize", lib.swg_ensemble_initialize(h))
+
+    def step(self, nsteps: int = 1):
+        self.ctx.check("swg_ensemble_step", self.ctx.lib.swg_ensemble_step(self.h, int(nsteps)))
+
+    def set_state(self, rh=None, vh=None, trh=None, tvh=None):
+        self.ctx.check("swg_ensemble_set_state", self.ctx.lib.swg_ensemble_set_state(
+            self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
+
+    def get_state_async(self, rh=None, vh=None, trh=None, tvh=None):
+        self.ctx.check("swg_ensemble_get_state_async", self.ctx.lib.swg_ensemble_get_state_async(
+            self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
+
+    def get_pl(self):
+        rh = np.zeros((self.NPL, 3))
+        vh = np.zeros((self.NPL, 3))
+        st = np.zeros(self.NPL, np.int32)
+        self.ctx.check("swg_ensemble_get_pl", self.ctx.lib.swg_ensemble_get_pl(self.h, _ptr(rh), _ptr(vh), _ptr(st)))
+        return rh, vh, st
+
+    def get_tp(self):
+        rh = np.zeros((self.NTP, 3))
+        vh = np.zeros((self.NTP, 3))
+        st = np.zeros(self.NTP, np.int32)
+        self.ctx.check("swg_ensemble_get_tp", self.ctx.lib.swg_ensemble_get_tp(self.h, _ptr(rh), _ptr(vh), _ptr(st)))
+        return rh, vh, st
+
+    def energy(self):
+        """Per-system energy / momentum: dict of arrays (length nsys)."""
+        out = np.zeros((self.nsys, 9))
+        self.ctx.check("swg_ensemble_energy", self.ctx.lib.swg_ensemble_energy(self.h, _ptr(out)))
+        return {"te": out[:, 0].copy(), "ke": out[:, 1].copy(), "pe": out[:, 2].copy(), "be": out[:, 3].copy(),
+                "L": out[:, 4:7].copy(), "GMtot": out[:, 7].copy(), "te_helio": out[:, 8].copy()}
+
+    def stats(self):
+        out = np.zeros(6, np.int64)
+        self.ctx.check("swg_ensemble_stats", self.ctx.lib.swg_ensemble_stats(self.h, _ptr(out)))
+        return {"system_steps_with_encounters": int(out[0]), "max_recursion": int(out[1]),
+                "plpl_encounters": int(out[2]), "pltp_encounters": int(out[3]), "collisions": int(out[4]),
+                "recursion_substeps": int(out[5])}
+
+    def plpl_list(self, sys: int):
+        n = C.c_int64(0)
+        cap = 256
+        while True:
+            i1 = np.zeros(cap, np.int32)
+            i2 = np.zeros(cap, np.int32)
+            rc = self.ctx.lib.swg_ensemble_plpl_list(self.h, int(sys), cap, C.byref(n), _ptr(i1), _ptr(i2))
+            if rc == L.SWG_ERR_CAPACITY:
+                cap = int(n.value)
+                continue
+            self.ctx.check("swg_ensemble_plpl_list", rc)
+            return i1[:n.value].copy(), i2[:n.value].copy()
+
+    def profile(self, enable: bool = True):
+        self.ctx.check("swg_ensemble_profile", self.ctx.lib.swg_ensemble_profile(self.h, int(bool(enable))))
+
+    def profile_read(self):
+        out = np.zeros(10)
+        self.ctx.check("swg_ensemble_profile_read", self.ctx.lib.swg_ensemble_profile_read(self.h, _ptr(out)))
+        return {k: {"launches": int(out[2 * i]), "ms": float(out[2 * i + 1])}
+                for i, k in enumerate(self.PROFILE_CLASSES)}
+
+    def close(self):
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
+            self.ctx.lib.swg_ensemble_destroy(self.h)
         self.h = None
 
     def __del__(self):

@@ -110,6 +110,7 @@ int swg_destroy(swg_ctx *c) {
     if (!c) return SWG_OK;
     // systems still alive belong to this context: release them first
     while (!c->systems.empty()) swg_system_destroy((swg_system *)c->systems.back());
+    while (!c->ensembles.empty()) swg_ensemble_destroy((swg_ensemble *)c->ensembles.back());
     cudaStreamSynchronize(c->stream);
     for (auto &b : c->slot)
         if (b.ptr) cudaFree(b.ptr);

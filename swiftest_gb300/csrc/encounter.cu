@@ -110,22 +110,22 @@ __global__ void k_encounter_prep(int n, const double *__restrict__ r, const doub
 
 constexpr int EP = 64;  // partners per shared-memory tile
 
-// Receivers: list-2 bodies j (one thread each, blockIdx.x tiles of ET).  Partners:
-// list-1 bodies i in chunk blockIdx.y (i < j when `upper`, i.e. pl-pl).  Pair written
-// as (i+1, j+1+shift2); the list is sorted afterwards, so the chunking is invisible.
-__global__ void __launch_bounds__(ET) k_encounter_tri(
+// Receivers: list-2 bodies j in [j0, j0 + ET) (one thread each).  Partners: list-1 bodies
+// i in [ibeg, iend) (i < j when `upper`, i.e. pl-pl).  A pair is written as
+// (i + 1 + base1, j + 1 + base2); lists are sorted afterwards, so the tiling is invisible.
+// Whole block; returns at once (block-uniformly) when the range is empty.
+__device__ __forceinline__ void enc_tri_tile(
     int n1, const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
     const double *__restrict__ r1, const double *__restrict__ v1, const double *__restrict__ renc1, int n2,
     const float4 *__restrict__ A2, const float4 *__restrict__ B2, const float4 *__restrict__ V2,
-    const double *__restrict__ r2, const double *__restrict__ v2, const double *__restrict__ renc2, int upper,
-    int shift2, double dt, int chunk, long long cap, int32_t *__restrict__ o1, int32_t *__restrict__ o2,
-    int32_t *__restrict__ olv, unsigned long long *__restrict__ count) {
+    const double *__restrict__ r2, const double *__restrict__ v2, const double *__restrict__ renc2, int upper, int j0,
+    int ibeg, int iend, int base1, int base2, double dt, long long cap, int32_t *__restrict__ o1,
+    int32_t *__restrict__ o2, int32_t *__restrict__ olv, unsigned long long *__restrict__ count) {
     __shared__ float4 sa[EP], sb[EP], sv[EP];
-    const int j = blockIdx.x * ET + threadIdx.x;
+    const int j = j0 + threadIdx.x;
     const bool active = j < n2;
-    const int ibeg = blockIdx.y * chunk;
-    int iend = min(n1, ibeg + chunk);
-    if (upper) iend = min(iend, (int)(blockIdx.x * ET + ET));
+    iend = min(n1, iend);
+    if (upper) iend = min(iend, j0 + ET);
     if (ibeg >= iend) return;  // whole block outside the upper triangle
     BodyF q;
     if (active) {
@@ -163,8 +163,8 @@ __global__ void __launch_bounds__(ET) k_encounter_tri(
                 if (lenc) {
                     const unsigned long long k = atomicAdd(count, 1ull);
                     if ((long long)k < cap) {
-                        o1[k] = i + 1;
-                        o2[k] = j + 1 + shift2;
+                        o1[k] = i + 1 + base1;
+                        o2[k] = j + 1 + base2;
                         olv[k] = lv;
                     }
                 }
@@ -172,6 +172,40 @@ __global__ void __launch_bounds__(ET) k_encounter_tri(
         }
         __syncthreads();
     }
+}
+
+// One system: receivers tile blockIdx.x, partner chunk blockIdx.y.
+__global__ void __launch_bounds__(ET) k_encounter_tri(
+    int n1, const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
+    const double *__restrict__ r1, const double *__restrict__ v1, const double *__restrict__ renc1, int n2,
+    const float4 *__restrict__ A2, const float4 *__restrict__ B2, const float4 *__restrict__ V2,
+    const double *__restrict__ r2, const double *__restrict__ v2, const double *__restrict__ renc2, int upper,
+    int shift2, double dt, int chunk, long long cap, int32_t *__restrict__ o1, int32_t *__restrict__ o2,
+    int32_t *__restrict__ olv, unsigned long long *__restrict__ count) {
+    const int ibeg = blockIdx.y * chunk;
+    enc_tri_tile(n1, A1, B1, V1, r1, v1, renc1, n2, A2, B2, V2, r2, v2, renc2, upper, blockIdx.x * ET, ibeg,
+                 ibeg + chunk, 0, shift2, dt, cap, o1, o2, olv, count);
+}
+
+// Batched (ensemble) check: block b takes item b = (system s, first receiver j0) of a
+// table sorted by cost.  List 1 is system s's pl ([off1[s], off1[s] + n1[s]) in the
+// float/double arrays), list 2 its pl again (upper, pl-pl) or its tp (off2, n2).  Pairs
+// are written with global 1-based indices, so the sorted list groups by system.
+__global__ void __launch_bounds__(ET) k_encounter_tri_batched(
+    const int4 *__restrict__ items, const int32_t *__restrict__ off1, const int32_t *__restrict__ n1s,
+    const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
+    const double *__restrict__ r1, const double *__restrict__ v1, const double *__restrict__ renc1,
+    const int32_t *__restrict__ off2, const int32_t *__restrict__ n2s, const float4 *__restrict__ A2,
+    const float4 *__restrict__ B2, const float4 *__restrict__ V2, const double *__restrict__ r2,
+    const double *__restrict__ v2, const double *__restrict__ renc2, int upper, double dt, long long cap,
+    int32_t *__restrict__ o1, int32_t *__restrict__ o2, int32_t *__restrict__ olv,
+    unsigned long long *__restrict__ count) {
+    const int4 w = items[blockIdx.x];
+    const int s = w.x;
+    const int a = off1[s], b = off2[s];
+    enc_tri_tile(n1s[s], A1 + a, B1 + a, V1 + a, r1 + 3 * (size_t)a, v1 + 3 * (size_t)a, renc1 + a, n2s[s], A2 + b,
+                 B2 + b, V2 + b, r2 + 3 * (size_t)b, v2 + 3 * (size_t)b, renc2 ? renc2 + b : nullptr, upper, w.y, 0,
+                 n1s[s], a, b, dt, cap, o1, o2, olv, count);
 }
 
 // ------------------------------------------------------------------ sorting
@@ -514,6 +548,30 @@ int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const doubl
                                                             renc2, upper, shift2, dt, chunk, cap, o1, o2, olv, count);
     c->launches++;
     return launch_status(c, "encounter_tri");
+}
+
+// Float copies (A, B, V) of n bodies for the prefilter of the batched check.
+int encounter_prep_launch(swg_ctx *c, int64_t n, const double *r, const double *v, const double *renc, float4 *A,
+                          float4 *B, float4 *V) {
+    if (n <= 0) return SWG_OK;
+    k_encounter_prep<<<(int)((n + 255) / 256), 256, 0, c->stream>>>((int)n, r, v, renc, A, B, V);
+    c->launches++;
+    return launch_status(c, "encounter_prep");
+}
+
+// Batched TRIANGULAR check over an item table (see k_encounter_tri_batched); F1/F2 are
+// the prepared float copies (3 arrays of float4 each, A|B|V) of list 1 and list 2.
+int encounter_tri_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *off1, const int32_t *n1,
+                          const float4 *F1, int64_t nf1, const double *r1, const double *v1, const double *renc1,
+                          const int32_t *off2, const int32_t *n2, const float4 *F2, int64_t nf2, const double *r2,
+                          const double *v2, const double *renc2, int upper, double dt, long long cap, int32_t *o1,
+                          int32_t *o2, int32_t *olv, unsigned long long *count) {
+    if (nitems <= 0) return SWG_OK;
+    k_encounter_tri_batched<<<nitems, ET, 0, c->stream>>>(items, off1, n1, F1, F1 + nf1, F1 + 2 * nf1, r1, v1, renc1,
+                                                          off2, n2, F2, F2 + nf2, F2 + 2 * nf2, r2, v2, renc2, upper,
+                                                          dt, cap, o1, o2, olv, count);
+    c->launches++;
+    return launch_status(c, "encounter_tri_batched");
 }
 
 // scratch of one encounter_launch call (mode, list sizes)

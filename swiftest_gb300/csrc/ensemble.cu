@@ -1,0 +1,1020 @@
+// ensemble.cu -- batched ensembles of independent systems (HELIO and SyMBA).
+//
+// Many independent planetary systems of uneven size are packed CSR-style and step
+// together: every kernel of a step covers all systems at once, so one launch
+// sequence advances the whole ensemble.  The decomposition per kernel kind:
+//   * per-body work (kick update, linear drift of tp, Danby drift, resets): flat
+//     over all bodies, the body's system found through psys / tsys;
+//   * the reference's O(N) ordered sums (vh2vb, vb2vh, linear drift momentum, the
+//     energy totals) and the SyMBA recursion: one block per system;
+//   * the pair kernels (kick, level-0 encounter check): a table of receiver tiles of
+//     every system sorted by cost, largest first (kick.cu, kick_fp64.cu, encounter.cu),
+//     the mixed kick as one persistent launch pulling tiles from a device queue;
+//   * encounter-list kernels that the reference runs serially per system (pair
+//     subtraction from the kick, the tp add-back): one thread per system.
+// Each system takes exactly the steps of the single-system path (system.cu, which
+// restates whm_step.f90 / helio_step.f90 / symba_step.f90), so in FP64 mode every
+// system's trajectory is bit-identical to stepping it alone.
+//
+// HBM layout: system s owns massive bodies [poff[s], poff[s] + npl[s]) of the (3, NPL)
+// FP64 arrays rh, vh, vb, ah, ... and test particles [toff[s], toff[s] + ntp[s]) of the
+// (3, NTP) arrays; per-system scalars (GMcb, the central-body record dcb, first-step
+// flags, encounter-list segments) are small device arrays indexed by s.  Encounter
+// lists of all systems share one pool per kind with global 1-based body indices,
+// sorted by (index1, index2), so system s's pairs form one contiguous segment.
+// The systems share dt; GMTINY is not supported (every body fully interacting).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "drift_impl.cuh"
+#include "swg_internal.cuh"
+#include "symba_dev.cuh"
+
+using namespace swg;
+using namespace swg::sdev;
+
+static_assert(KICK_MIXED_TILE == 128 && KICK_FP64_TILE == 8 && ENC_TILE == 128, "tile sizes of the batched kernels");
+
+struct swg_ensemble {
+    swg_ctx *c = nullptr;
+    int integrator = SWG_SYMBA;
+    int32_t nsys = 0;
+    int64_t NPL = 0, NTP = 0;
+    std::vector<int32_t> h_npl, h_ntp, h_poff, h_toff;
+    std::vector<double> h_GMcb, h_Rcb;
+    double dt = 0, rhscale = 6.5, t = 0;
+    int lclose = 0, precision = SWG_FP64, initialized = 0, cb_set = 0;
+    // per system (device)
+    int32_t *npl = nullptr, *ntp = nullptr, *poff = nullptr, *toff = nullptr;
+    double *GMcb = nullptr, *dcb = nullptr;  // dcb: CB_N doubles per system
+    int32_t *lfirst = nullptr, *lany = nullptr, *seg_pp = nullptr, *seg_pt = nullptr, *enc_steps = nullptr;
+    // massive bodies
+    int32_t *psys = nullptr;
+    double *rh = nullptr, *vh = nullptr, *vb = nullptr, *ah = nullptr, *rbeg = nullptr, *rend = nullptr;
+    double *Gmass = nullptr, *radius = nullptr, *rhill = nullptr, *renc = nullptr;
+    int32_t *status = nullptr, *lmask = nullptr, *levelg = nullptr, *levelm = nullptr, *nplenc = nullptr,
+            *ntpenc = nullptr, *mark_pl = nullptr, *pmark = nullptr;
+    double *ahi = nullptr, *ahj = nullptr;
+    // test particles
+    int32_t *tsys = nullptr;
+    double *trh = nullptr, *tvh = nullptr, *tvb = nullptr, *tah = nullptr;
+    int32_t *tstatus = nullptr, *tlmask = nullptr, *tlevelg = nullptr, *tlevelm = nullptr, *tnplenc = nullptr,
+            *mark_tp = nullptr;
+    // float copies: split partners of the mixed kick (A|B), prefilter copies (A|B|V)
+    float4 *kA = nullptr, *kB = nullptr, *eP = nullptr, *eT = nullptr;
+    // item tables of the batched pair kernels
+    int4 *it_mpl = nullptr, *it_mtp = nullptr, *it_fpl = nullptr, *it_ftp = nullptr, *it_epp = nullptr,
+         *it_ept = nullptr;
+    int n_mpl = 0, n_mtp = 0, n_fpl = 0, n_ftp = 0, n_epp = 0, n_ept = 0;
+    unsigned *head = nullptr;
+    // encounter lists: [i1 | i2 | lvdotr | status | level] * cap, global 1-based indices
+    int32_t *pp_l = nullptr, *pt_l = nullptr;
+    int64_t pp_n = 0, pt_n = 0, pp_cap = 0, pt_cap = 0;
+    EncWork enc_pp, enc_pt;
+    int32_t *rec_out = nullptr;  // [0] status, [1] deepest level, [2] sub-steps
+    DevBuf rec_scratch, rows;
+    double *eout = nullptr;      // 9 per system
+    int32_t *h_flags = nullptr;  // pinned: [2] recursion status; +8: two unsigned long long counts
+    int64_t stats[6] = {0, 0, 0, 0, 0, 0};
+    StepProfile prof;
+};
+
+namespace {
+
+inline int grid_for(int64_t n, int bs) { return (int)std::max<int64_t>(1, (n + bs - 1) / bs); }
+
+int L(swg_ctx *c, const char *what) {
+    c->launches++;
+    return launch_status(c, what);
+}
+
+template <typename T>
+int dalloc(swg_ctx *c, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        c->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return SWG_ERR_NOMEM;
+    }
+    return cuda_status(c, cudaMemsetAsync(*p, 0, n * sizeof(T), c->stream), "memset");
+}
+
+template <typename T>
+int upload(swg_ctx *c, T *dst, const std::vector<T> &src) {
+    if (src.empty()) return SWG_OK;
+    return cuda_status(c, cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, c->stream),
+                       "upload");
+}
+
+// ---------------------------------------------------------------- kernels
+// one block per system: swiftest_util_coord_vh2vb_pl (only systems whose first-step
+// flag is set when lfirst != nullptr), helio_drift_linear_pl, swiftest_util_coord_vb2vh_pl
+__global__ void __launch_bounds__(RB) k_ens_vh2vb(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+                                                  const int32_t *__restrict__ lfirst, const double *__restrict__ Gm,
+                                                  const double *__restrict__ vh, double *vb,
+                                                  const double *__restrict__ GMcb, double *dcb, int exact) {
+    const int s = blockIdx.x;
+    if (npl[s] == 0 || (lfirst && !lfirst[s])) return;
+    __shared__ SumScratch sh;
+    const size_t o = poff[s];
+    blk_vh2vb_pl(npl[s], Gm + o, vh + 3 * o, vb + 3 * o, GMcb[s], dcb + CB_N * s, exact, sh);
+}
+__global__ void __launch_bounds__(RB) k_ens_lindrift(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+                                                     const double *__restrict__ Gm, const double *__restrict__ vb,
+                                                     const int32_t *__restrict__ lmask, const double *__restrict__ GMcb,
+                                                     double *rh, double dt, double *dcb, int slot, int exact) {
+    const int s = blockIdx.x;
+    if (npl[s] == 0) return;
+    __shared__ SumScratch sh;
+    const size_t o = poff[s];
+    blk_lindrift_pl(npl[s], Gm + o, vb + 3 * o, lmask + o, GMcb[s], rh + 3 * o, dt, dcb + CB_N * s, slot, exact, sh);
+}
+__global__ void __launch_bounds__(RB) k_ens_vb2vh(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+                                                  const double *__restrict__ Gm, const double *__restrict__ vb,
+                                                  const int32_t *__restrict__ status, double *vh,
+                                                  const double *__restrict__ GMcb, double *dcb, int exact) {
+    const int s = blockIdx.x;
+    if (npl[s] == 0) return;
+    __shared__ SumScratch sh;
+    const size_t o = poff[s];
+    blk_vb2vh_pl(npl[s], Gm + o, vb + 3 * o, status + o, vh + 3 * o, GMcb[s], dcb + CB_N * s, exact, sh);
+}
+
+// Test-particle coordinate updates with their own system's central-body record (modes
+// as k_tp_misc of system.cu: 2 linear drift, 3 linear drift then vb2vh, 4 vh2vb then
+// linear drift, 5 vb = vh + the central body's vb).  mode_first >= 0 replaces mode
+// for systems still in their first step.
+__global__ void k_ens_tp_misc(int64_t ntp, const int32_t *__restrict__ tsys, const int32_t *__restrict__ tlmask,
+                              double *trh, double *tvh, double *tvb, const double *__restrict__ dcb, int slot,
+                              double dt, int mode, int mode_first, const int32_t *__restrict__ lfirst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= ntp || !tlmask[i]) return;
+    const int s = tsys[i];
+    const int m = (mode_first >= 0 && lfirst[s]) ? mode_first : mode;
+    const double *cb = dcb + CB_N * s;
+    for (int d = 0; d < 3; d++) {
+        const double pt = cb[slot + d];
+        const double vbcb = -pt;
+        if (m == 4) tvb[3 * i + d] = tvh[3 * i + d] + vbcb;
+        if (m == 2 || m == 3 || m == 4) trh[3 * i + d] = trh[3 * i + d] + pt * dt;
+        if (m == 3) tvh[3 * i + d] = tvb[3 * i + d] - vbcb;
+        if (m == 5) tvb[3 * i + d] = tvh[3 * i + d] + cb[slot + d];
+    }
+}
+
+// Segment (first entry, count) of each system in an encounter-list pool sorted by index1
+// (global 1-based pl index): binary searches for the system's pl range, so a system
+// without pairs still gets the position where its pairs would start (the recursion
+// places its scratch by these positions).
+__device__ __forceinline__ int64_t lower_bound_i32(const int32_t *__restrict__ a, int64_t n, int32_t v) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a[mid] < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+__global__ void k_ens_segments(int nsys, int64_t n, const int32_t *__restrict__ i1, const int32_t *__restrict__ poff,
+                               int32_t *seg) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    const int64_t b = lower_bound_i32(i1, n, poff[s] + 1), e = lower_bound_i32(i1, n, poff[s + 1] + 1);
+    seg[2 * s] = (int32_t)b;
+    seg[2 * s + 1] = (int32_t)(e - b);
+}
+
+// symba_kick_getacch_pl's subtraction of the encountering pairs (symba_kick.f90:61-70)
+// through the flat pair loop (swiftest_kick.f90:69-115), one thread per system walking
+// its list segment in order: ahi/ahj of the listed bodies, then acc -= ahi + ahj once
+// per body (unlisted bodies would subtract zero).
+__global__ void k_ens_kick_pairs(int nsys, const int32_t *__restrict__ seg, const int32_t *__restrict__ l,
+                                 int64_t cap, const double *__restrict__ r, const double *__restrict__ Gm,
+                                 const double *__restrict__ R, double *ahi, double *ahj, int32_t *mark, double *acc) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys || seg[2 * s + 1] == 0) return;
+    const int n = seg[2 * s + 1];
+    const int32_t *i1 = l + seg[2 * s], *i2 = i1 + cap;
+    for (int q = 0; q < n; q++)
+        for (int d = 0; d < 3; d++) {
+            ahi[3 * (i1[q] - 1) + d] = ahj[3 * (i1[q] - 1) + d] = 0.0;
+            ahi[3 * (i2[q] - 1) + d] = ahj[3 * (i2[q] - 1) + d] = 0.0;
+        }
+    for (int q = 0; q < n; q++) {
+        const int i = i1[q] - 1, j = i2[q] - 1;
+        const double rx = r[3 * j + 0] - r[3 * i + 0];
+        const double ry = r[3 * j + 1] - r[3 * i + 1];
+        const double rz = r[3 * j + 2] - r[3 * i + 2];
+        const double rji2 = rx * rx + ry * ry + rz * rz;
+        const double rs = R[i] + R[j];
+        if (!(rji2 > rs * rs)) continue;
+        const double irij3 = 1.0 / (rji2 * sqrt(rji2));
+        const double faci = Gm[i] * irij3;
+        const double facj = Gm[j] * irij3;
+        ahi[3 * i + 0] = ahi[3 * i + 0] + facj * rx;
+        ahi[3 * i + 1] = ahi[3 * i + 1] + facj * ry;
+        ahi[3 * i + 2] = ahi[3 * i + 2] + facj * rz;
+        ahj[3 * j + 0] = ahj[3 * j + 0] - faci * rx;
+        ahj[3 * j + 1] = ahj[3 * j + 1] - faci * ry;
+        ahj[3 * j + 2] = ahj[3 * j + 2] - faci * rz;
+    }
+    for (int q = 0; q < n; q++) {
+        const int b2[2] = {i1[q] - 1, i2[q] - 1};
+        for (int e = 0; e < 2; e++) {
+            const int b = b2[e];
+            if (mark[b]) continue;
+            mark[b] = 1;
+            for (int d = 0; d < 3; d++) acc[3 * b + d] = acc[3 * b + d] - (ahi[3 * b + d] + ahj[3 * b + d]);
+        }
+    }
+    for (int q = 0; q < n; q++) mark[i1[q] - 1] = mark[i2[q] - 1] = 0;
+}
+
+// symba_kick_getacch_tp add-back loop (symba_kick.f90:104-118), one thread per system
+__global__ void k_ens_pltp_addback(int nsys, const int32_t *__restrict__ seg, const int32_t *__restrict__ l,
+                                   int64_t cap, const int32_t *__restrict__ tlmask, const double *__restrict__ trh,
+                                   const double *__restrict__ rp, const double *__restrict__ Gm, double *tah) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys || seg[2 * s + 1] == 0) return;
+    const int n = seg[2 * s + 1];
+    const int32_t *i1 = l + seg[2 * s], *i2 = i1 + cap;
+    for (int k = 0; k < n; k++) {
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        if (!tlmask[j]) continue;
+        const double dx = trh[3 * j + 0] - rp[3 * i + 0];
+        const double dy = trh[3 * j + 1] - rp[3 * i + 1];
+        const double dz = trh[3 * j + 2] - rp[3 * i + 2];
+        const double rjj = dx * dx + dy * dy + dz * dz;
+        const double fac = Gm[i] / (rjj * sqrt(rjj));
+        tah[3 * j + 0] = tah[3 * j + 0] + fac * dx;
+        tah[3 * j + 1] = tah[3 * j + 1] + fac * dy;
+        tah[3 * j + 2] = tah[3 * j + 2] + fac * dz;
+    }
+}
+
+// End of step: a system that took the plain HELIO step clears its first-step flag
+// (helio_step.f90), one that interpolated keeps it (symba_step_interp_system never
+// clears lfirst); count the steps with encounters.  lany == nullptr: HELIO ensemble.
+__global__ void k_ens_finish(int nsys, const int32_t *__restrict__ lany, int32_t *lfirst, int32_t *enc_steps) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    const int any = lany ? lany[s] : 0;
+    if (!any) lfirst[s] = 0;
+    enc_steps[s] += any;
+}
+__global__ void k_ens_lany(int nsys, const int32_t *__restrict__ seg_pp, const int32_t *__restrict__ seg_pt,
+                           int32_t *lany) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsys) lany[s] = (seg_pp[2 * s + 1] + seg_pt[2 * s + 1]) > 0;
+}
+
+// The SyMBA recursion of every system with encounters this step, one block each
+// (blk_symba_recursion on the system's list segments; body arrays are global).
+struct EnsRecArgs {
+    RecArgs base;  // global arrays, list pools and scratch bases
+    const int32_t *seg_pp, *seg_pt, *npl, *ntp;
+    const double *GMcb;
+};
+__global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e) {
+    const int s = blockIdx.x;
+    const int64_t k0 = e.seg_pp[2 * s], npp = e.seg_pp[2 * s + 1];
+    const int64_t t0 = e.seg_pt[2 * s], npt = e.seg_pt[2 * s + 1];
+    if (npp + npt == 0) return;
+    RecArgs a = e.base;
+    a.npl = e.npl[s];
+    a.ntp = e.ntp[s];
+    a.npp = npp;
+    a.npt = npt;
+    a.pp = e.base.pp + k0;
+    a.pt = e.base.pt + t0;
+    a.GMcb = e.GMcb[s];
+    const int64_t q = k0 + t0;  // entries of the systems before s
+    a.terms = e.base.terms + 6 * q;
+    a.lenc = e.base.lenc + q;
+    a.good = e.base.good + q;
+    a.bpl = e.base.bpl + 2 * k0 + t0;
+    a.btp = e.base.btp + t0;
+    blk_symba_recursion(a);
+}
+
+// energy / momentum per system: totals (one block each) and potential rows (flat)
+__global__ void __launch_bounds__(RB) k_ens_energy_final(const int32_t *__restrict__ poff,
+                                                         const int32_t *__restrict__ npl, const double *rh,
+                                                         const double *vh, const double *vb, const double *Gm,
+                                                         const double *radius, const int32_t *status,
+                                                         const double *__restrict__ GMcb, int lclose,
+                                                         const double *rows, double *rb, double *out) {
+    const int s = blockIdx.x;
+    __shared__ SumScratch sh;
+    const size_t o = poff[s];
+    blk_energy_final(npl[s], 0, rh + 3 * o, vh + 3 * o, vb + 3 * o, Gm + o, radius + o, status + o, GMcb[s], lclose,
+                     rows + o, rb + 3 * o, out + 9 * s, sh);
+}
+__global__ void k_ens_energy_rows(int64_t n, const int32_t *__restrict__ psys, const int32_t *__restrict__ poff,
+                                  const int32_t *__restrict__ npl, const double *rb, const double *Gm,
+                                  const int32_t *status, double *rows) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = psys[i];
+    const size_t o = poff[s];
+    rows[i] = d_energy_row((int)(i - o), npl[s], rb + 3 * o, Gm + o, status + o);
+}
+
+// ---------------------------------------------------------------- host side
+bool exact(const swg_ensemble *e) { return e->precision == SWG_FP64; }
+
+// Tiles of every system, sorted by cost (largest first; ties keep system order).
+// recv(s) receivers per system in tiles of `tile`; cost(s, r0, nr) orders them.
+template <class Recv, class Cost>
+std::vector<int4> make_items(int nsys, int tile, Recv recv, Cost cost) {
+    std::vector<int4> it;
+    std::vector<double> w;
+    for (int s = 0; s < nsys; s++) {
+        const int n = recv(s);
+        for (int r0 = 0; r0 < n; r0 += tile) {
+            const int nr = std::min(tile, n - r0);
+            it.push_back(make_int4(s, r0, nr, 0));
+            w.push_back(cost(s, r0, nr));
+        }
+    }
+    std::vector<size_t> ord(it.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return w[a] > w[b]; });
+    std::vector<int4> out(it.size());
+    for (size_t k = 0; k < ord.size(); k++) out[k] = it[ord[k]];
+    return out;
+}
+
+int put_items(swg_ensemble *e, int4 **dst, int *n, const std::vector<int4> &items) {
+    if (*dst) cudaFree(*dst);
+    *dst = nullptr;
+    *n = (int)items.size();
+    SWG_TRY(dalloc(e->c, dst, items.size()));
+    return upload(e->c, *dst, items);
+}
+
+int build_items(swg_ensemble *e) {
+    const int S = e->nsys;
+    auto npl = [&](int s) { return e->h_npl[s]; };
+    auto ntp = [&](int s) { return e->h_ntp[s]; };
+    auto tp_recv = [&](int s) { return e->h_ntp[s]; };
+    auto plcost = [&](int s, int, int nr) { return (double)nr * e->h_npl[s]; };
+    SWG_TRY(put_items(e, &e->it_mpl, &e->n_mpl, make_items(S, KICK_MIXED_TILE, npl, plcost)));
+    SWG_TRY(put_items(e, &e->it_mtp, &e->n_mtp, make_items(S, KICK_MIXED_TILE, tp_recv, plcost)));
+    SWG_TRY(put_items(e, &e->it_fpl, &e->n_fpl, make_items(S, KICK_FP64_TILE, npl, plcost)));
+    SWG_TRY(put_items(e, &e->it_ftp, &e->n_ftp, make_items(S, KICK_FP64_TILE, ntp, plcost)));
+    // pl-pl check: tile j0 tests partners i < j, i.e. up to j0 + nr
+    auto tri = [&](int, int r0, int nr) { return (double)nr * (r0 + nr); };
+    SWG_TRY(put_items(e, &e->it_epp, &e->n_epp, make_items(S, ENC_TILE, npl, tri)));
+    auto tp_with_pl = [&](int s) { return e->h_npl[s] > 0 ? e->h_ntp[s] : 0; };
+    SWG_TRY(put_items(e, &e->it_ept, &e->n_ept, make_items(S, ENC_TILE, tp_with_pl, plcost)));
+    return SWG_OK;
+}
+
+int ensure_pool(swg_ensemble *e, int32_t **l, int64_t *cap, int64_t need) {
+    if (need <= *cap) return SWG_OK;
+    const int64_t ncap = std::max<int64_t>(need + need / 2, 1024);
+    int32_t *fresh = nullptr;
+    SWG_TRY(dalloc(e->c, &fresh, (size_t)5 * ncap));
+    if (*l) cudaFree(*l);
+    *l = fresh;
+    *cap = ncap;
+    return SWG_OK;
+}
+
+// pl-pl accelerations of all systems into ah (helio_kick_getacch_int_pl / symba_kick_getacch_int_pl)
+int accel_int_pl(swg_ensemble *e) {
+    swg_ctx *c = e->c;
+    const bool rad = e->integrator == SWG_SYMBA || e->lclose;
+    const double *R = rad ? e->radius : nullptr;
+    if (e->precision == SWG_MIXED) {
+        SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB));
+        return kick_mixed_batched(c, false, rad, e->n_mpl, e->it_mpl, e->poff, e->poff, e->npl, e->rh, R, e->kA,
+                                  e->kB, nullptr, e->ah, 1, e->head);
+    }
+    return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah, 1);
+}
+
+// helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76)
+int kick_vb_pl(swg_ensemble *e, double dt, int lbeg) {
+    swg_ctx *c = e->c;
+    if (e->NPL == 0) return SWG_OK;
+    {
+        ProfScope ps(e->prof, c->stream, PROF_KICK_PL);
+        SWG_TRY(accel_int_pl(e));
+    }
+    if (e->integrator == SWG_SYMBA && e->pp_n > 0) {
+        k_ens_kick_pairs<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pp, e->pp_l, e->pp_cap, e->rh,
+                                                                      e->Gmass, e->radius, e->ahi, e->ahj, e->pmark,
+                                                                      e->ah);
+        SWG_TRY(L(c, "ens_kick_pairs"));
+    }
+    k_kick_update<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->vb, e->ah, e->lmask, dt, e->rh,
+                                                                 lbeg ? e->rbeg : e->rend);
+    return L(c, "kick_update_pl");
+}
+
+// helio_kick_vb_tp (helio_kick.f90:135-169) with symba_kick_getacch_tp (symba_kick.f90:79-123).
+// The mixed path reuses the partner split of the pl kick just before it: the pl
+// positions it was taken from are exactly rbeg / rend.
+int kick_vb_tp(swg_ensemble *e, double dt, int lbeg) {
+    swg_ctx *c = e->c;
+    if (e->NTP == 0) return SWG_OK;
+    const double *rp = lbeg ? e->rbeg : e->rend;
+    {
+        ProfScope ps(e->prof, c->stream, PROF_KICK_TP);
+        if (e->precision == SWG_MIXED) {
+            SWG_TRY(kick_mixed_batched(c, true, false, e->n_mtp, e->it_mtp, e->toff, e->poff, e->npl, e->trh, nullptr,
+                                       e->kA, e->kB, e->tlmask, e->tah, 1, e->head));
+        } else {
+            SWG_TRY(kick_tp_fp64_batched(c, e->n_ftp, e->it_ftp, e->toff, e->ntp, e->poff, e->npl, e->trh, rp,
+                                         e->Gmass, e->tlmask, e->tah, 1));
+        }
+    }
+    if (e->integrator == SWG_SYMBA && e->pt_n > 0) {
+        k_ens_pltp_addback<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pt, e->pt_l, e->pt_cap,
+                                                                        e->tlmask, e->trh, rp, e->Gmass, e->tah);
+        SWG_TRY(L(c, "ens_pltp_addback"));
+    }
+    k_kick_update<<<grid_for(e->NTP, 128), 128, 0, c->stream>>>((int)e->NTP, e->tvb, e->tah, e->tlmask, dt, nullptr,
+                                                                 nullptr);
+    return L(c, "kick_update_tp");
+}
+
+int lindrift_pl(swg_ensemble *e, double dt, int slot) {
+    if (e->NPL == 0) return SWG_OK;
+    k_ens_lindrift<<<e->nsys, RB, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->lmask, e->GMcb, e->rh, dt,
+                                                     e->dcb, slot, exact(e));
+    return L(e->c, "ens_lindrift");
+}
+int tp_misc(swg_ensemble *e, int slot, double dt, int mode, int mode_first) {
+    if (e->NTP == 0) return SWG_OK;
+    k_ens_tp_misc<<<grid_for(e->NTP, 256), 256, 0, e->c->stream>>>(e->NTP, e->tsys, e->tlmask, e->trh, e->tvh, e->tvb,
+                                                                    e->dcb, slot, dt, mode, mode_first, e->lfirst);
+    return L(e->c, "ens_tp_misc");
+}
+int vh2vb_pl(swg_ensemble *e, bool first_only) {
+    if (e->NPL == 0) return SWG_OK;
+    k_ens_vh2vb<<<e->nsys, RB, 0, e->c->stream>>>(e->poff, e->npl, first_only ? e->lfirst : nullptr, e->Gmass, e->vh,
+                                                  e->vb, e->GMcb, e->dcb, exact(e));
+    return L(e->c, "ens_vh2vb");
+}
+int vb2vh_pl(swg_ensemble *e) {
+    if (e->NPL == 0) return SWG_OK;
+    k_ens_vb2vh<<<e->nsys, RB, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->status, e->vh, e->GMcb, e->dcb,
+                                                  exact(e));
+    return L(e->c, "ens_vb2vh");
+}
+// Danby drift of every body at level -1 (SyMBA: bodies outside encounters) with its
+// own system's GMcb; HELIO drifts every active body.
+int drift_bodies(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    ProfScope ps(e->prof, c->stream, PROF_DRIFT);
+    const bool symba = e->integrator == SWG_SYMBA;
+    if (e->NPL > 0)
+        SWG_TRY(drift_masked(c, 0.0, e->rh, e->vb, (int32_t)e->NPL, symba ? e->levelg : nullptr, -1, dt, e->status,
+                             nullptr, e->GMcb, e->psys));
+    if (e->NTP > 0)
+        SWG_TRY(drift_masked(c, 0.0, e->trh, e->tvb, (int32_t)e->NTP, symba ? e->tlevelg : nullptr, -1, dt,
+                             e->tstatus, nullptr, e->GMcb, e->tsys));
+    return SWG_OK;
+}
+
+// Level-0 checks of every system (symba_encounter_check_pl / _tp,
+// symba_encounter_check.f90:14-87, 238-296), TRIANGULAR: both batched checks, one host
+// synchronization for the two counts, then the sorted lists with their level-0 marks
+// and each system's segment.
+int symba_level0(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    e->pp_n = e->pt_n = 0;
+    k_set_renc<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->rhill, e->rhscale, 0, e->renc);
+    SWG_TRY(L(c, "set_renc"));
+    EncWork *w[2] = {&e->enc_pp, &e->enc_pt};
+    for (int k = 0; k < 2; k++) {
+        SWG_TRY(ensure(c, w[k]->counters, 2 * sizeof(unsigned long long)));
+        if (w[k]->rawcap < 4096) {
+            w[k]->rawcap = 4096;
+            SWG_TRY(ensure(c, w[k]->raw, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
+        }
+    }
+    SWG_TRY(encounter_prep_launch(c, e->NPL, e->rh, e->vb, e->renc, e->eP, e->eP + e->NPL, e->eP + 2 * e->NPL));
+    if (e->n_ept > 0)
+        SWG_TRY(encounter_prep_launch(c, e->NTP, e->trh, e->tvb, nullptr, e->eT, e->eT + e->NTP, e->eT + 2 * e->NTP));
+    unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
+    auto launch = [&](int kind) -> int {
+        EncWork &x = *w[kind];
+        int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
+        unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
+        if (kind == 0)
+            SWG_TRY(encounter_tri_batched(c, e->n_epp, e->it_epp, e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc,
+                                          e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc, 1, dt, x.rawcap, i1,
+                                          i2, lv, cnt));
+        else
+            SWG_TRY(encounter_tri_batched(c, e->n_ept, e->it_ept, e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc,
+                                          e->toff, e->ntp, e->eT, e->NTP, e->trh, e->tvb, nullptr, 0, dt, x.rawcap, i1,
+                                          i2, lv, cnt));
+        return cuda_status(c, cudaMemcpyAsync(&h[kind], cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                              c->stream),
+                           "count");
+    };
+    h[0] = h[1] = 0;
+    const bool do_pt = e->n_ept > 0;
+    SWG_TRY(launch(0));
+    if (do_pt) SWG_TRY(launch(1));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
+    for (int k = 0; k < 2; k++) {  // capacity overflow: grow the raw buffers and redo that check
+        if ((int64_t)h[k] <= w[k]->rawcap) continue;
+        w[k]->rawcap = (int64_t)h[k] + (int64_t)h[k] / 2 + 4096;
+        DevBuf fresh;
+        SWG_TRY(ensure(c, fresh, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
+        cudaFree(w[k]->raw.ptr);
+        w[k]->raw = fresh;
+        SWG_TRY(launch(k));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
+    }
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->seg_pp, 0, sizeof(int32_t) * 2 * e->nsys, c->stream), "memset"));
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->seg_pt, 0, sizeof(int32_t) * 2 * e->nsys, c->stream), "memset"));
+    for (int k = 0; k < 2; k++) {
+        const int64_t n = (int64_t)h[k];  // triangular lists hold no repeated pairs
+        if (n == 0) continue;
+        EncWork &x = *w[k];
+        int32_t **list = k == 0 ? &e->pp_l : &e->pt_l;
+        int64_t *cap = k == 0 ? &e->pp_cap : &e->pt_cap;
+        SWG_TRY(ensure_pool(e, list, cap, n));
+        int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
+        unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
+        if (n <= 4096) {
+            k_list_finalize<<<1, 1024, 0, c->stream>>>((int)n, i1, i2, lv, *list, *cap, k, e->levelg, e->levelm,
+                                                       k == 0 ? e->nplenc : e->ntpenc, e->tlevelg, e->tlevelm,
+                                                       e->tnplenc, cnt + 1);
+            SWG_TRY(L(c, "list_finalize"));
+        } else {
+            SWG_TRY(ensure(c, x.sort, sort_pairs_scratch_bytes(n)));
+            SWG_TRY(sort_pairs_unique(c, n, i1, i2, lv, x.sort.ptr, cnt + 1));
+            for (int f = 0; f < 3; f++) {
+                const int32_t *src = f == 0 ? i1 : (f == 1 ? i2 : lv);
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(*list + f * *cap, src, sizeof(int32_t) * n,
+                                                       cudaMemcpyDeviceToDevice, c->stream),
+                                    "copy list"));
+            }
+            k_level0_mark<<<grid_for(n, 128), 128, 0, c->stream>>>(n, *list, *cap, k, e->levelg, e->levelm,
+                                                                   k == 0 ? e->nplenc : e->ntpenc, e->tlevelg,
+                                                                   e->tlevelm, e->tnplenc);
+            SWG_TRY(L(c, "level0_mark"));
+        }
+        k_ens_segments<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, n, *list, e->poff,
+                                                                       k == 0 ? e->seg_pp : e->seg_pt);
+        SWG_TRY(L(c, "ens_segments"));
+        (k == 0 ? e->pp_n : e->pt_n) = n;
+    }
+    k_ens_lany<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, e->seg_pp, e->seg_pt, e->lany);
+    SWG_TRY(L(c, "ens_lany"));
+    e->stats[2] += e->pp_n;
+    e->stats[3] += e->pt_n;
+    return SWG_OK;
+}
+
+int symba_recursion(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    const int64_t n = e->pp_n + e->pt_n;
+    SWG_TRY(ensure(c, e->rec_scratch, sizeof(double) * (size_t)(6 * n + 8) + (size_t)(2 * n + 64) +
+                                          sizeof(int32_t) * (size_t)(3 * n + 64)));
+    EnsRecArgs x;
+    RecArgs &a = x.base;
+    a.npl = 0;
+    a.ntp = 0;
+    a.npp = a.npt = 0;
+    a.ppcap = e->pp_cap;
+    a.ptcap = e->pt_cap;
+    a.pp = e->pp_l;
+    a.pt = e->pt_l;
+    a.rh = e->rh;
+    a.vb = e->vb;
+    a.ah = e->ah;
+    a.trh = e->trh;
+    a.tvb = e->tvb;
+    a.tah = e->tah;
+    a.Gm = e->Gmass;
+    a.rhill = e->rhill;
+    a.radius = e->radius;
+    a.status = e->status;
+    a.tstatus = e->tstatus;
+    a.levelg = e->levelg;
+    a.levelm = e->levelm;
+    a.tlevelg = e->tlevelg;
+    a.tlevelm = e->tlevelm;
+    a.GMcb = 0.0;
+    a.rhscale = e->rhscale;
+    a.dt = dt;
+    a.terms = (double *)e->rec_scratch.ptr;
+    int32_t *ibuf = (int32_t *)(a.terms + 6 * n + 8);
+    a.bpl = ibuf;               // 2 * npp + npt per system
+    a.btp = ibuf + 2 * n + 32;  // npt per system
+    uint8_t *bbuf = (uint8_t *)(ibuf + 3 * n + 64);
+    a.lenc = bbuf;
+    a.good = bbuf + n + 32;
+    a.mark_pl = e->mark_pl;
+    a.mark_tp = e->mark_tp;
+    a.out = e->rec_out;
+    x.seg_pp = e->seg_pp;
+    x.seg_pt = e->seg_pt;
+    x.npl = e->npl;
+    x.ntp = e->ntp;
+    x.GMcb = e->GMcb;
+    ProfScope ps(e->prof, c->stream, PROF_RECUR);
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_out, 0, sizeof(int32_t), c->stream), "memset"));
+    k_ens_symba_recursion<<<e->nsys, RECT, 0, c->stream>>>(x);
+    SWG_TRY(L(c, "ens_symba_recursion"));
+    return cuda_status(c, cudaMemcpyAsync(e->h_flags + 2, e->rec_out, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                          c->stream),
+                       "recursion status");
+}
+
+// One step of every system: symba_step_system (symba_step.f90:14-52) or
+// helio_step_system (helio_step.f90:14-119).  A SyMBA system without encounters takes
+// the HELIO step; the kernel sequence below is the same for both cases (empty lists
+// make the pair subtraction, the add-back and the recursion no-ops, and every body sits
+// at level -1), so all systems advance in one sequence.  Order as in
+// symba_step_interp_system: pl and tp first halves, recursion, second halves.
+int ens_step(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    const bool symba = e->integrator == SWG_SYMBA;
+    const double dth = 0.5 * dt;
+    if (symba) {
+        const int64_t nmax = std::max(e->NPL, e->NTP);
+        k_symba_reset<<<grid_for(nmax, 256), 256, 0, c->stream>>>((int)e->NPL, (int)e->NTP, e->levelg, e->levelm,
+                                                                   e->nplenc, e->ntpenc, e->lmask, e->tlevelg,
+                                                                   e->tlevelm, e->tnplenc, e->tlmask);
+        SWG_TRY(L(c, "symba_reset"));
+        ProfScope ps(e->prof, c->stream, PROF_ENC0);
+        SWG_TRY(symba_level0(e, dt));
+    }
+    SWG_TRY(vh2vb_pl(e, true));
+    SWG_TRY(lindrift_pl(e, dth, CB_PTBEG));
+    SWG_TRY(kick_vb_pl(e, dth, 1));
+    SWG_TRY(tp_misc(e, CB_PTBEG, dth, 2, 4));
+    SWG_TRY(kick_vb_tp(e, dth, 1));
+    SWG_TRY(drift_bodies(e, dt));
+    if (symba && e->pp_n + e->pt_n > 0) SWG_TRY(symba_recursion(e, dt));
+    SWG_TRY(kick_vb_pl(e, dth, 0));
+    SWG_TRY(lindrift_pl(e, dth, CB_PTEND));
+    SWG_TRY(vb2vh_pl(e));
+    SWG_TRY(kick_vb_tp(e, dth, 0));
+    SWG_TRY(tp_misc(e, CB_PTEND, dth, 3, -1));
+    k_ens_finish<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, symba ? e->lany : nullptr, e->lfirst,
+                                                                 e->enc_steps);
+    return L(c, "ens_finish");
+}
+
+}  // namespace
+
+// ======================================================================== C ABI
+extern "C" {
+
+int swg_ensemble_destroy(swg_ensemble *e);
+
+int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t *npl, const int32_t *ntp,
+                        swg_ensemble **out) {
+    if (!c || !out || nsys <= 0 || !npl || (integrator != SWG_HELIO && integrator != SWG_SYMBA)) return SWG_ERR_ARG;
+    int64_t NPL = 0, NTP = 0;
+    for (int s = 0; s < nsys; s++) {
+        const int32_t m = ntp ? ntp[s] : 0;
+        if (npl[s] < 0 || m < 0) return SWG_ERR_ARG;
+        NPL += npl[s];
+        NTP += m;
+    }
+    if (NPL >= (int64_t)1 << 31 || NTP >= (int64_t)1 << 31) return SWG_ERR_ARG;
+    swg_ensemble *e = new swg_ensemble();
+    e->c = c;
+    c->ensembles.push_back(e);
+    e->integrator = integrator;
+    e->nsys = nsys;
+    e->NPL = NPL;
+    e->NTP = NTP;
+    e->h_npl.assign(npl, npl + nsys);
+    e->h_ntp.assign(nsys, 0);
+    if (ntp) e->h_ntp.assign(ntp, ntp + nsys);
+    e->h_poff.assign(nsys + 1, 0);
+    e->h_toff.assign(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) {
+        e->h_poff[s + 1] = e->h_poff[s] + e->h_npl[s];
+        e->h_toff[s + 1] = e->h_toff[s] + e->h_ntp[s];
+    }
+    std::vector<int32_t> psys(NPL), tsys(NTP);
+    for (int s = 0; s < nsys; s++) {
+        std::fill(psys.begin() + e->h_poff[s], psys.begin() + e->h_poff[s + 1], s);
+        std::fill(tsys.begin() + e->h_toff[s], tsys.begin() + e->h_toff[s + 1], s);
+    }
+    const size_t n = std::max<int64_t>(NPL, 1), m = std::max<int64_t>(NTP, 1), S = nsys;
+    int rc = SWG_OK;
+    int32_t **ps[] = {&e->npl, &e->ntp, &e->poff, &e->toff, &e->lfirst, &e->lany, &e->enc_steps};
+    for (auto p : ps)
+        if (rc == SWG_OK) rc = dalloc(c, p, S + 1);
+    if (rc == SWG_OK) rc = dalloc(c, &e->seg_pp, 2 * S);
+    if (rc == SWG_OK) rc = dalloc(c, &e->seg_pt, 2 * S);
+    if (rc == SWG_OK) rc = dalloc(c, &e->GMcb, S);
+    if (rc == SWG_OK) rc = dalloc(c, &e->dcb, CB_N * S);
+    if (rc == SWG_OK) rc = dalloc(c, &e->eout, 9 * S);
+    double **pd[] = {&e->rh, &e->vh, &e->vb, &e->ah, &e->rbeg, &e->rend, &e->ahi, &e->ahj};
+    for (auto p : pd)
+        if (rc == SWG_OK) rc = dalloc(c, p, 3 * n);
+    double **pn[] = {&e->Gmass, &e->radius, &e->rhill, &e->renc};
+    for (auto p : pn)
+        if (rc == SWG_OK) rc = dalloc(c, p, n);
+    int32_t **pi[] = {&e->psys, &e->status, &e->lmask, &e->levelg, &e->levelm, &e->nplenc, &e->ntpenc, &e->mark_pl,
+                      &e->pmark};
+    for (auto p : pi)
+        if (rc == SWG_OK) rc = dalloc(c, p, n);
+    double **td[] = {&e->trh, &e->tvh, &e->tvb, &e->tah};
+    for (auto p : td)
+        if (rc == SWG_OK) rc = dalloc(c, p, 3 * m);
+    int32_t **ti[] = {&e->tsys, &e->tstatus, &e->tlmask, &e->tlevelg, &e->tlevelm, &e->tnplenc, &e->mark_tp};
+    for (auto p : ti)
+        if (rc == SWG_OK) rc = dalloc(c, p, m);
+    if (rc == SWG_OK) rc = dalloc(c, &e->kA, 2 * n);
+    if (rc == SWG_OK) e->kB = e->kA + n;
+    if (rc == SWG_OK) rc = dalloc(c, &e->eP, 3 * n);
+    if (rc == SWG_OK) rc = dalloc(c, &e->eT, 3 * m);
+    if (rc == SWG_OK) rc = dalloc(c, &e->head, 4);
+    if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
+    if (rc == SWG_OK) rc = ensure(c, e->rows, sizeof(double) * 4 * n);
+    if (rc == SWG_OK) {
+        cudaError_t err = cudaMallocHost((void **)&e->h_flags, 64);
+        if (err != cudaSuccess) rc = cuda_status(c, err, "cudaMallocHost");
+    }
+    if (rc == SWG_OK) rc = upload(c, e->npl, e->h_npl);
+    if (rc == SWG_OK) rc = upload(c, e->ntp, e->h_ntp);
+    if (rc == SWG_OK) rc = upload(c, e->poff, e->h_poff);
+    if (rc == SWG_OK) rc = upload(c, e->toff, e->h_toff);
+    if (rc == SWG_OK) rc = upload(c, e->psys, psys);
+    if (rc == SWG_OK) rc = upload(c, e->tsys, tsys);
+    if (rc == SWG_OK) rc = build_items(e);
+    if (rc == SWG_OK) rc = cuda_status(c, cudaStreamSynchronize(c->stream), "create");
+    if (rc != SWG_OK) {
+        swg_ensemble_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return SWG_OK;
+}
+
+int swg_ensemble_destroy(swg_ensemble *e) {
+    if (!e) return SWG_OK;
+    swg_ctx *c = e->c;
+    if (c) {
+        cudaStreamSynchronize(c->stream);
+        auto it = std::find(c->ensembles.begin(), c->ensembles.end(), (void *)e);
+        if (it != c->ensembles.end()) c->ensembles.erase(it);
+    }
+    void *ptrs[] = {e->npl, e->ntp, e->poff, e->toff, e->GMcb, e->dcb, e->lfirst, e->lany, e->seg_pp, e->seg_pt,
+                    e->enc_steps, e->psys, e->rh, e->vh, e->vb, e->ah, e->rbeg, e->rend, e->Gmass, e->radius,
+                    e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
+                    e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
+                    e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->it_mpl, e->it_mtp,
+                    e->it_fpl, e->it_ftp, e->it_epp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
+                    e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_scratch.ptr, e->rows.ptr, e->eout};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (e->h_flags) cudaFreeHost(e->h_flags);
+    e->prof.release();
+    delete e;
+    return SWG_OK;
+}
+
+int swg_ensemble_set_cb(swg_ensemble *e, const double *GMcb, const double *Rcb) {
+    if (!e || !GMcb) return SWG_ERR_ARG;
+    for (int s = 0; s < e->nsys; s++)
+        if (!(GMcb[s] > 0.0)) return SWG_ERR_ARG;
+    e->h_GMcb.assign(GMcb, GMcb + e->nsys);
+    e->h_Rcb.assign(e->nsys, 0.0);
+    if (Rcb) e->h_Rcb.assign(Rcb, Rcb + e->nsys);
+    e->cb_set = 1;
+    SWG_TRY(upload(e->c, e->GMcb, e->h_GMcb));
+    return cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "set_cb");
+}
+
+int swg_ensemble_set_pl(swg_ensemble *e, const double *rh, const double *vh, const double *Gmass,
+                        const double *radius, const double *rhill) {
+    if (!e) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const size_t n = e->NPL;
+    if (n == 0) return SWG_OK;
+    if (!rh || !vh || !Gmass || !radius || !rhill) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->rh, rh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->vh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->Gmass, Gmass, 8 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->radius, radius, 8 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->rhill, rhill, 8 * n, cudaMemcpyHostToDevice, c->stream), "set_pl"));
+    e->initialized = 0;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "set_pl");
+}
+
+int swg_ensemble_set_tp(swg_ensemble *e, const double *rh, const double *vh) {
+    if (!e) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const size_t n = e->NTP;
+    if (n == 0) return SWG_OK;
+    if (!rh || !vh) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->trh, rh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_tp"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->tvh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_tp"));
+    e->initialized = 0;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "set_tp");
+}
+
+int swg_ensemble_set_param(swg_ensemble *e, double dt, double rhscale, int lclose, int precision) {
+    if (!e || !(dt > 0.0) || !(rhscale > 0.0) || (precision != SWG_FP64 && precision != SWG_MIXED))
+        return SWG_ERR_ARG;
+    e->dt = dt;
+    e->rhscale = rhscale;
+    e->lclose = lclose != 0;
+    e->precision = precision;
+    return SWG_OK;
+}
+
+// helio_util_setup_initialize_system (helio_util.f90:14-43) for every system; bodies
+// arrive sorted as the reference's initialize leaves them (by mass, descending)
+int swg_ensemble_initialize(swg_ensemble *e) {
+    if (!e || !e->cb_set || !(e->dt > 0.0)) return SWG_ERR_STATE;
+    swg_ctx *c = e->c;
+    std::vector<int32_t> ones(std::max(e->NPL, e->NTP), 1), first(e->nsys, 1);
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->status, 0, 4 * std::max<int64_t>(e->NPL, 1), c->stream), "init"));
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->tstatus, 0, 4 * std::max<int64_t>(e->NTP, 1), c->stream), "init"));
+    if (e->NPL > 0)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->lmask, ones.data(), 4 * e->NPL, cudaMemcpyHostToDevice, c->stream),
+                            "init"));
+    if (e->NTP > 0)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->tlmask, ones.data(), 4 * e->NTP, cudaMemcpyHostToDevice, c->stream),
+                            "init"));
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->dcb, 0, sizeof(double) * CB_N * e->nsys, c->stream), "init"));
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->enc_steps, 0, sizeof(int32_t) * e->nsys, c->stream), "init"));
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_out, 0, sizeof(int32_t) * 4, c->stream), "init"));
+    SWG_TRY(upload(c, e->lfirst, first));
+    SWG_TRY(vh2vb_pl(e, false));
+    SWG_TRY(tp_misc(e, CB_VB, 0.0, 5, -1));  // tp vb = vh + the central body's vb
+    e->t = 0.0;
+    std::memset(e->stats, 0, sizeof(e->stats));
+    e->initialized = 1;
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "init");
+}
+
+int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
+    if (!e || !e->initialized) return SWG_ERR_STATE;
+    e->h_flags[2] = 0;
+    for (int32_t k = 0; k < nsteps; k++) {
+        SWG_TRY(ens_step(e, e->dt));
+        if (e->h_flags[2] != 0) {  // recursion status of an earlier step, seen at a sync point
+            e->c->err = "SyMBA local time step too small";
+            return e->h_flags[2];
+        }
+        e->t += e->dt;
+    }
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "step"));
+    if (e->h_flags[2] != 0) {
+        e->c->err = "SyMBA local time step too small";
+        return e->h_flags[2];
+    }
+    return SWG_OK;
+}
+
+int swg_ensemble_get_pl(swg_ensemble *e, double *rh, double *vh, int32_t *status) {
+    if (!e) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const size_t n = e->NPL;
+    if (n == 0) return SWG_OK;
+    if (rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(rh, e->rh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_pl"));
+    if (vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(vh, e->vh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_pl"));
+    if (status)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(status, e->status, 4 * n, cudaMemcpyDeviceToHost, c->stream), "get_pl"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "get_pl");
+}
+
+int swg_ensemble_get_tp(swg_ensemble *e, double *rh, double *vh, int32_t *status) {
+    if (!e) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const size_t n = e->NTP;
+    if (n == 0) return SWG_OK;
+    if (rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(rh, e->trh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_tp"));
+    if (vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(vh, e->tvh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "get_tp"));
+    if (status)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(status, e->tstatus, 4 * n, cudaMemcpyDeviceToHost, c->stream), "get_tp"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "get_tp");
+}
+
+int swg_ensemble_energy(swg_ensemble *e, double *out) {
+    if (!e || !out) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const int64_t n = std::max<int64_t>(e->NPL, 1);
+    double *rows = (double *)e->rows.ptr, *rb = rows + n;
+    // the totals kernel also writes rb, which the rows need: totals, rows, totals
+    k_ens_energy_final<<<e->nsys, RB, 0, c->stream>>>(e->poff, e->npl, e->rh, e->vh, e->vb, e->Gmass, e->radius,
+                                                      e->status, e->GMcb, e->lclose, rows, rb, e->eout);
+    SWG_TRY(L(c, "ens_energy_rb"));
+    if (e->NPL > 0) {
+        k_ens_energy_rows<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>(e->NPL, e->psys, e->poff, e->npl, rb,
+                                                                         e->Gmass, e->status, rows);
+        SWG_TRY(L(c, "ens_energy_rows"));
+    }
+    k_ens_energy_final<<<e->nsys, RB, 0, c->stream>>>(e->poff, e->npl, e->rh, e->vh, e->vb, e->Gmass, e->radius,
+                                                      e->status, e->GMcb, e->lclose, rows, rb, e->eout);
+    SWG_TRY(L(c, "ens_energy_final"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(out, e->eout, sizeof(double) * 9 * e->nsys, cudaMemcpyDeviceToHost,
+                                           c->stream),
+                        "energy"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "energy");
+}
+
+int swg_ensemble_stats(swg_ensemble *e, int64_t *out) {
+    if (!e || !out) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    std::vector<int32_t> steps(e->nsys);
+    int32_t dev[4];
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(steps.data(), e->enc_steps, 4 * e->nsys, cudaMemcpyDeviceToHost, c->stream),
+                        "stats"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(dev, e->rec_out, sizeof(dev), cudaMemcpyDeviceToHost, c->stream), "stats"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "stats"));
+    int64_t tot = 0;
+    for (int32_t v : steps) tot += v;
+    e->stats[0] = tot;
+    e->stats[1] = dev[1];
+    e->stats[5] = dev[2];
+    std::memcpy(out, e->stats, sizeof(e->stats));
+    return SWG_OK;
+}
+
+// Level-0 encounter list of system `sys` from the last step, local 1-based indices.
+int swg_ensemble_plpl_list(swg_ensemble *e, int32_t sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2) {
+    if (!e || !n || sys < 0 || sys >= e->nsys) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    int32_t seg[2] = {0, 0};
+    *n = 0;
+    if (e->pp_n > 0) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(seg, e->seg_pp + 2 * sys, sizeof(seg), cudaMemcpyDeviceToHost, c->stream),
+                            "list"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "list"));
+    }
+    *n = seg[1];
+    if (seg[1] > cap) return SWG_ERR_CAPACITY;
+    if (seg[1] == 0) return SWG_OK;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(i1, e->pp_l + seg[0], 4 * (size_t)seg[1], cudaMemcpyDeviceToHost, c->stream),
+                        "list"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(i2, e->pp_l + e->pp_cap + seg[0], 4 * (size_t)seg[1],
+                                           cudaMemcpyDeviceToHost, c->stream),
+                        "list"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "list"));
+    const int32_t o = e->h_poff[sys];
+    for (int32_t k = 0; k < seg[1]; k++) {
+        i1[k] -= o;
+        i2[k] -= o;
+    }
+    return SWG_OK;
+}
+
+int swg_ensemble_set_state(swg_ensemble *e, const double *rh, const double *vh, const double *trh, const double *tvh) {
+    if (!e || !e->initialized) return SWG_ERR_STATE;
+    swg_ctx *c = e->c;
+    const size_t n = e->NPL, m = e->NTP;
+    if (n && rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->rh, rh, 24 * n, cudaMemcpyHostToDevice, c->stream), "state"));
+    if (n && vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->vh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "state"));
+    if (m && trh)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->trh, trh, 24 * m, cudaMemcpyHostToDevice, c->stream), "state"));
+    if (m && tvh)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->tvh, tvh, 24 * m, cudaMemcpyHostToDevice, c->stream), "state"));
+    return SWG_OK;
+}
+
+int swg_ensemble_get_state_async(swg_ensemble *e, double *rh, double *vh, double *trh, double *tvh) {
+    if (!e) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const size_t n = e->NPL, m = e->NTP;
+    if (n && rh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(rh, e->rh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "state"));
+    if (n && vh) SWG_TRY(cuda_status(c, cudaMemcpyAsync(vh, e->vh, 24 * n, cudaMemcpyDeviceToHost, c->stream), "state"));
+    if (m && trh)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(trh, e->trh, 24 * m, cudaMemcpyDeviceToHost, c->stream), "state"));
+    if (m && tvh)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(tvh, e->tvh, 24 * m, cudaMemcpyDeviceToHost, c->stream), "state"));
+    return SWG_OK;
+}
+
+int swg_ensemble_profile(swg_ensemble *e, int enable) {
+    if (!e) return SWG_ERR_ARG;
+    e->prof.on = enable != 0;
+    e->prof.n = 0;
+    return SWG_OK;
+}
+
+int swg_ensemble_profile_read(swg_ensemble *e, double *out) {
+    if (!e || !out) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "profile"));
+    e->prof.read(out, PROF_NCLS);
+    return SWG_OK;
+}
+
+}  // extern "C"

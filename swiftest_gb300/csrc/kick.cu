@@ -23,6 +23,8 @@
 // results are deterministic.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "swg_internal.cuh"
 
 namespace swg {
@@ -48,36 +50,37 @@ __device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) {
     lo = __double2float_rn(x - (double)hi);
 }
 
-// Receivers i in [blockIdx.x*MBLOCK, ...), partners j in chunk blockIdx.y of
-// length chunk.  TP: receivers are test particles (partners all pl, sign -),
-// else pl-pl with the (i<nplm || j<nplm) interaction rule and optional radius guard.
-template <bool TP, bool RAD>
-__global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int nplm, const double *__restrict__ rrecv,
-                                                      const double *__restrict__ rpart,
-                                                      const double *__restrict__ Gm, const double *__restrict__ R,
-                                                      const int32_t *__restrict__ lmask, double *__restrict__ acc,
-                                                      int acc_is_zero, int chunk, float *__restrict__ partial,
-                                                      unsigned *__restrict__ counters,
-                                                      const float4 *__restrict__ pA, const float4 *__restrict__ pB) {
-    // pA/pB (optional): partners already split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R)
-    __shared__ float4 sA[MT];  // x_hi, y_hi, z_hi, Gm
-    __shared__ float4 sB[MT];  // x_lo, y_lo, z_lo, R
-    __shared__ bool s_last;
-    const int i = blockIdx.x * MBLOCK + threadIdx.x;
-    const bool inrange = i < nrecv;
-    const bool active = inrange && (!TP || lmask[i] != 0);
-    float xh = 0, yh = 0, zh = 0, xl = 0, yl = 0, zl = 0, Ri = 0;
-    if (inrange) {
-        split_hi_lo(rrecv[3 * i + 0], xh, xl);
-        split_hi_lo(rrecv[3 * i + 1], yh, yl);
-        split_hi_lo(rrecv[3 * i + 2], zh, zl);
-        if (RAD) Ri = __double2float_rn(R[i]);
-    }
-    FF ax = {0.f, 0.f}, ay = {0.f, 0.f}, az = {0.f, 0.f};
-    const int jbeg = blockIdx.y * chunk;
-    const int jstop = min(npart, jbeg + chunk);
+// One receiving body of the mixed kick: its coordinates split into float hi/lo.
+struct MixedRecv {
+    float xh, yh, zh, xl, yl, zl, R;
+};
+
+template <bool RAD>
+__device__ __forceinline__ MixedRecv mixed_recv(const double *__restrict__ r, const double *__restrict__ R, int i) {
+    MixedRecv q;
+    split_hi_lo(r[3 * i + 0], q.xh, q.xl);
+    split_hi_lo(r[3 * i + 1], q.yh, q.yl);
+    split_hi_lo(r[3 * i + 2], q.zh, q.zl);
+    q.R = RAD ? __double2float_rn(R[i]) : 0.f;
+    return q;
+}
+
+// Sweep of partners [jbeg, jstop) (indices into the partner arrays) for this thread's
+// receiver, whole block: 64-partner FP32 partials folded into float-float (ax, ay, az).
+// pA/pB hold the partners already split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R);
+// without them each tile converts rpart/Gm/R itself.
+// Pair rule (pl-pl; TP has none): the reference skips j == i and, with GMTINY bodies,
+// pairs of two bodies both at index >= nplm (GMT); with RAD it also skips pairs closer
+// than the sum of the radii, which covers j == i (r^2 == 0 exactly), so the index test
+// is only made without RAD.  `self` is the receiver's index in the partner arrays.
+template <bool TP, bool RAD, bool GMT>
+__device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, int self, int nplm, bool self_m, const MixedRecv &q,
+                                            const double *__restrict__ rpart, const double *__restrict__ Gm,
+                                            const double *__restrict__ R, const float4 *__restrict__ pA,
+                                            const float4 *__restrict__ pB, float4 *sA, float4 *sB, FF &ax, FF &ay,
+                                            FF &az) {
     for (int j0 = jbeg; j0 < jstop; j0 += MT) {
-        for (int t = threadIdx.x; t < MT; t += MBLOCK) {
+        for (int t = threadIdx.x; t < MT; t += blockDim.x) {
             const int jl = j0 + t;
             float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
             if (jl < jstop && pA) {
@@ -100,25 +103,25 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
         for (int jj = 0; jj < nt; jj++) {
             const float4 a = sA[jj];
             const float4 b = sB[jj];
-            const float dx = (a.x - xh) + (b.x - xl);
-            const float dy = (a.y - yh) + (b.y - yl);
-            const float dz = (a.z - zh) + (b.z - zl);
+            const float dx = (a.x - q.xh) + (b.x - q.xl);
+            const float dy = (a.y - q.yh) + (b.y - q.yl);
+            const float dz = (a.z - q.zh) + (b.z - q.zl);
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             float y = rsqrtf(r2);
             y = y * fmaf(-0.5f * r2, y * y, 1.5f);
             float fac = a.w * (y * y * y);
-            bool ok;
-            if (TP) {
-                ok = true;
-            } else {
+            if (!TP) {
                 const int j = j0 + jj;
-                ok = (j != i) && (i < nplm || j < nplm);
+                bool ok = true;
+                if (GMT) ok = self_m || j < nplm;
                 if (RAD) {
-                    const float rs = Ri + b.w;
+                    const float rs = q.R + b.w;
                     ok = ok && (r2 > rs * rs);
+                } else {
+                    ok = ok && (j != self);
                 }
+                fac = ok ? fac : 0.f;
             }
-            fac = ok ? fac : 0.f;
             px = fmaf(fac, dx, px);
             py = fmaf(fac, dy, py);
             pz = fmaf(fac, dz, pz);
@@ -128,20 +131,47 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
         ff_add(az, pz);
         __syncthreads();
     }
+}
+
+// acc (+)= the float-float totals.  pl-pl: acc_i += sum Gm_j (r_j - r_i)/r^3; tp:
+// acc_tp -= sum Gm_j (r_tp - r_j)/r^3, i.e. the same partner-minus-self sum added to acc.
+__device__ __forceinline__ void mixed_store(double *a, const FF &ax, const FF &ay, const FF &az, int acc_is_zero) {
+    const double sx = (double)ax.hi + (double)ax.lo, sy = (double)ay.hi + (double)ay.lo,
+                 sz = (double)az.hi + (double)az.lo;
+    a[0] = (acc_is_zero ? 0.0 : a[0]) + sx;
+    a[1] = (acc_is_zero ? 0.0 : a[1]) + sy;
+    a[2] = (acc_is_zero ? 0.0 : a[2]) + sz;
+}
+
+// Receivers i in [blockIdx.x*MBLOCK, ...), partners j in chunk blockIdx.y of
+// length chunk.  TP: receivers are test particles (partners all pl, sign -),
+// else pl-pl with the (i<nplm || j<nplm) interaction rule and optional radius guard.
+template <bool TP, bool RAD, bool GMT>
+__global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int nplm, const double *__restrict__ rrecv,
+                                                      const double *__restrict__ rpart,
+                                                      const double *__restrict__ Gm, const double *__restrict__ R,
+                                                      const int32_t *__restrict__ lmask, double *__restrict__ acc,
+                                                      int acc_is_zero, int chunk, float *__restrict__ partial,
+                                                      unsigned *__restrict__ counters,
+                                                      const float4 *__restrict__ pA, const float4 *__restrict__ pB) {
+    __shared__ float4 sA[MT];  // x_hi, y_hi, z_hi, Gm
+    __shared__ float4 sB[MT];  // x_lo, y_lo, z_lo, R
+    __shared__ bool s_last;
+    const int i = blockIdx.x * MBLOCK + threadIdx.x;
+    const bool inrange = i < nrecv;
+    const bool active = inrange && (!TP || lmask[i] != 0);
+    MixedRecv q = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (inrange) q = mixed_recv<RAD>(rrecv, R, i);
+    FF ax = {0.f, 0.f}, ay = {0.f, 0.f}, az = {0.f, 0.f};
+    const int jbeg = blockIdx.y * chunk;
+    const int jstop = min(npart, jbeg + chunk);
+    mixed_sweep<TP, RAD, GMT>(jbeg, jstop, i, nplm, i < nplm, q, rpart, Gm, R, pA, pB, sA, sB, ax, ay, az);
     const int nchunk = gridDim.y;
     if (nchunk == 1) {
-        if (active) {
-            // pl-pl: acc_i += sum Gm_j (r_j - r_i)/r^3 ; tp: acc_tp -= sum Gm_j (r_tp - r_j)/r^3,
-            // i.e. the same partner-minus-self sum added to acc.
-            double *a = &acc[3 * i];
-            const double sx = (double)ax.hi + (double)ax.lo, sy = (double)ay.hi + (double)ay.lo,
-                         sz = (double)az.hi + (double)az.lo;
-            a[0] = (acc_is_zero ? 0.0 : a[0]) + sx;
-            a[1] = (acc_is_zero ? 0.0 : a[1]) + sy;
-            a[2] = (acc_is_zero ? 0.0 : a[2]) + sz;
-        } else if (inrange && acc_is_zero) {
+        if (active)
+            mixed_store(&acc[3 * i], ax, ay, az, acc_is_zero);
+        else if (inrange && acc_is_zero)
             acc[3 * i + 0] = acc[3 * i + 1] = acc[3 * i + 2] = 0.0;
-        }
         return;
     }
     // Multi-chunk: publish partials, last block of this receiver tile folds them.
@@ -179,6 +209,51 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
         acc[3 * i + 0] = acc[3 * i + 1] = acc[3 * i + 2] = 0.0;
     }
     if (threadIdx.x == 0) counters[blockIdx.x] = 0u;  // re-arm for the next launch
+}
+
+// Batched (ensemble) mixed kick: a persistent grid pulls receiver tiles of CSR-packed
+// systems from a work queue (items sorted by cost, largest first, so the tail is made
+// of small tiles).  Item: system s, receivers [r0, r0 + nr) of that system.  Receivers
+// sit at roff[s] + i in rrecv/acc/lmask, partners at poff[s] + j (j < npart[s]) in the
+// pre-split pA/pB.  pl-pl (!TP): rrecv is the pl array, roff == poff, and the receiver
+// is skipped as its own partner through the radius rule (RAD) or the index test.
+template <bool TP, bool RAD>
+__global__ void __launch_bounds__(MBLOCK) k_kick_mixed_batched(int nitems, const int4 *__restrict__ items,
+                                                              const int32_t *__restrict__ roff,
+                                                              const int32_t *__restrict__ poff,
+                                                              const int32_t *__restrict__ npart,
+                                                              const double *__restrict__ rrecv,
+                                                              const double *__restrict__ R,
+                                                              const float4 *__restrict__ pA,
+                                                              const float4 *__restrict__ pB,
+                                                              const int32_t *__restrict__ lmask,
+                                                              double *__restrict__ acc, int acc_is_zero,
+                                                              unsigned *__restrict__ head) {
+    __shared__ float4 sA[MT];
+    __shared__ float4 sB[MT];
+    __shared__ int s_item;
+    for (;;) {
+        __syncthreads();  // every thread has read the previous s_item
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(head, 1u);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) break;
+        const int4 w = items[it];  // (system, r0, nr, unused)
+        const int s = w.x;
+        const bool inrange = (int)threadIdx.x < w.z;
+        const int gi = roff[s] + w.y + threadIdx.x;
+        const bool active = inrange && (!TP || lmask[gi] != 0);
+        MixedRecv q = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (inrange) q = mixed_recv<RAD>(rrecv, R, gi);
+        FF ax = {0.f, 0.f}, ay = {0.f, 0.f}, az = {0.f, 0.f};
+        const int p0 = poff[s];
+        mixed_sweep<TP, RAD, false>(p0, p0 + npart[s], gi, 0, true, q, nullptr, nullptr, nullptr, pA, pB, sA, sB, ax,
+                                    ay, az);
+        if (active)
+            mixed_store(&acc[3 * gi], ax, ay, az, acc_is_zero);
+        else if (inrange && acc_is_zero)
+            acc[3 * gi + 0] = acc[3 * gi + 1] = acc[3 * gi + 2] = 0.0;
+    }
 }
 
 // Partners split once per kick into float hi/lo pairs (the conversion runs on the
@@ -274,6 +349,25 @@ __global__ void k_apply_pairs(int npl, const double *__restrict__ ahi, const dou
 // ------------------------------------------------------------------ launchers
 static inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// pl-pl variants of k_kick_mixed: radius guard or not, GMTINY rule or not
+static void launch_mixed_plpl(dim3 grid, cudaStream_t st, int npl, int nplm, const double *r, const double *Gm,
+                              const double *R, double *acc, int acc_is_zero, int chunk, float *partial,
+                              unsigned *counters, const float4 *pA, const float4 *pB) {
+    const bool gmt = nplm < npl;
+    if (R && gmt)
+        k_kick_mixed<false, true, true><<<grid, MBLOCK, 0, st>>>(npl, npl, nplm, r, r, Gm, R, nullptr, acc,
+                                                                 acc_is_zero, chunk, partial, counters, pA, pB);
+    else if (R)
+        k_kick_mixed<false, true, false><<<grid, MBLOCK, 0, st>>>(npl, npl, nplm, r, r, Gm, R, nullptr, acc,
+                                                                  acc_is_zero, chunk, partial, counters, pA, pB);
+    else if (gmt)
+        k_kick_mixed<false, false, true><<<grid, MBLOCK, 0, st>>>(npl, npl, nplm, r, r, Gm, nullptr, nullptr, acc,
+                                                                  acc_is_zero, chunk, partial, counters, pA, pB);
+    else
+        k_kick_mixed<false, false, false><<<grid, MBLOCK, 0, st>>>(npl, npl, nplm, r, r, Gm, nullptr, nullptr, acc,
+                                                                   acc_is_zero, chunk, partial, counters, pA, pB);
+}
+
 size_t kick_mixed_scratch_bytes(int nrecv, int npart, int nchunk) {
     return KICK_COUNTERS * sizeof(unsigned) + (size_t)nchunk * nrecv * 6 * sizeof(float) +
            (size_t)2 * sizeof(float4) * (size_t)npart + 512;
@@ -320,15 +414,11 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
     }
     dim3 grid(bx, nchunk);
     if (tp)
-        k_kick_mixed<true, false><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, 0, rrecv, rpart, Gm, nullptr, lmask,
-                                                                  acc, acc_is_zero, chunk, partial, counters, pA, pB);
-    else if (R)
-        k_kick_mixed<false, true><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, nplm, rrecv, rpart, Gm, R, nullptr,
-                                                                  acc, acc_is_zero, chunk, partial, counters, pA, pB);
+        k_kick_mixed<true, false, false><<<grid, MBLOCK, 0, c->stream>>>(
+            nrecv, npart, 0, rrecv, rpart, Gm, nullptr, lmask, acc, acc_is_zero, chunk, partial, counters, pA, pB);
     else
-        k_kick_mixed<false, false><<<grid, MBLOCK, 0, c->stream>>>(nrecv, npart, nplm, rrecv, rpart, Gm, nullptr,
-                                                                   nullptr, acc, acc_is_zero, chunk, partial,
-                                                                   counters, pA, pB);
+        launch_mixed_plpl(grid, c->stream, nrecv, nplm, rrecv, Gm, R, acc, acc_is_zero, chunk, partial, counters, pA,
+                          pB);
     c->launches++;
     return launch_status(c, "kick_mixed");
 }
@@ -352,12 +442,7 @@ cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, int num_sms, int npl,
     unsigned *counters = (unsigned *)scratch;
     float *partial = (float *)((char *)scratch + counter_bytes);
     dim3 grid(bx, nchunk);
-    if (R)
-        k_kick_mixed<false, true><<<grid, MBLOCK, 0, stream>>>(npl, npl, nplm, r, r, Gm, R, nullptr, acc, 0, chunk,
-                                                               partial, counters, nullptr, nullptr);
-    else
-        k_kick_mixed<false, false><<<grid, MBLOCK, 0, stream>>>(npl, npl, nplm, r, r, Gm, nullptr, nullptr, acc, 0,
-                                                                chunk, partial, counters, nullptr, nullptr);
+    launch_mixed_plpl(grid, stream, npl, nplm, r, Gm, R, acc, 0, chunk, partial, counters, nullptr, nullptr);
     return cudaGetLastError();
 }
 
@@ -373,6 +458,53 @@ int64_t kick_mixed_plpl_partials_max(int num_sms, int npl) {
     chunk = div_up(chunk, MT) * MT;
     nchunk = div_up(npl, chunk);
     return nchunk > 1 ? (int64_t)nchunk * npl : 0;
+}
+
+// Split n partner bodies into float hi/lo tiles (A = x_hi, y_hi, z_hi, Gm; B = x_lo, y_lo, z_lo, R).
+int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
+                      float4 *B) {
+    if (n <= 0) return SWG_OK;
+    k_kick_split<<<div_up(n, 256), 256, 0, c->stream>>>((int)n, r, Gm, R, A, B);
+    c->launches++;
+    return launch_status(c, "kick_split");
+}
+
+// Persistent batched mixed kick over a work queue of receiver tiles (see
+// k_kick_mixed_batched); pA/pB must hold the split partners.  The queue head is reset
+// on the stream before the launch; the grid is one wave of resident blocks.
+int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *items, const int32_t *roff,
+                       const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
+                       const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
+                       unsigned *head) {
+    if (nitems <= 0) return SWG_OK;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
+    static int occ[3] = {0, 0, 0};  // resident blocks per SM of each variant, queried once
+    const int v = tp ? 0 : (rad ? 1 : 2);
+    if (occ[v] == 0) {
+        int nb = 0;
+        cudaError_t e = tp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_batched<true, false>,
+                                                                           MBLOCK, 0)
+                           : rad ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                       &nb, k_kick_mixed_batched<false, true>, MBLOCK, 0)
+                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                       &nb, k_kick_mixed_batched<false, false>, MBLOCK, 0);
+        SWG_TRY(cuda_status(c, e, "occupancy"));
+        occ[v] = nb > 0 ? nb : 1;
+    }
+    const int grid = std::min(nitems, occ[v] * (c->num_sms > 0 ? c->num_sms : 152));
+    if (tp)
+        k_kick_mixed_batched<true, false><<<grid, MBLOCK, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
+                                                                          nullptr, pA, pB, lmask, acc, acc_is_zero,
+                                                                          head);
+    else if (rad)
+        k_kick_mixed_batched<false, true><<<grid, MBLOCK, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R,
+                                                                          pA, pB, nullptr, acc, acc_is_zero, head);
+    else
+        k_kick_mixed_batched<false, false><<<grid, MBLOCK, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
+                                                                           nullptr, pA, pB, nullptr, acc,
+                                                                           acc_is_zero, head);
+    c->launches++;
+    return launch_status(c, "kick_mixed_batched");
 }
 
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,

@@ -23,19 +23,19 @@
 namespace swg {
 
 constexpr int FT = 256;  // threads per block
+constexpr int FP64_RT = 8;  // receivers per block (FT / FP64_RT partners per round)
 
+// Receivers [i0, i0 + RT) of one system against all its partners, whole block.
 template <bool RAD, int MODE, int RT>
-__global__ void __launch_bounds__(FT) k_kick_plpl_fp64(int npl, int nplm, const double *__restrict__ r,
-                                                      const double *__restrict__ Gm,
-                                                      const double *__restrict__ R, double *__restrict__ acc,
-                                                      int acc_is_zero) {
+__device__ __forceinline__ void fp64_plpl_group(int npl, int nplm, const double *__restrict__ r,
+                                                const double *__restrict__ Gm, const double *__restrict__ R,
+                                                double *__restrict__ acc, int acc_is_zero, int i0) {
     constexpr int PT = FT / RT;
     __shared__ double sx[PT], sy[PT], sz[PT], sg[PT], sr[PT];
     __shared__ double tx[RT][PT + 1], ty[RT][PT + 1], tz[RT][PT + 1];
     __shared__ unsigned char tf[RT][PT];
     const int t = threadIdx.x;
     const int rr = t / PT, pp = t % PT;
-    const int i0 = blockIdx.x * RT;
     const int i = i0 + rr;  // receiver of this thread's terms
     double xi = 0, yi = 0, zi = 0, Ri = 0;
     if (i < npl) {
@@ -132,16 +132,15 @@ __global__ void __launch_bounds__(FT) k_kick_plpl_fp64(int npl, int nplm, const 
 
 // pl -> tp (swiftest_kick.f90:374-415): acc -= Gm_j/(r^2 sqrt r^2) * (r_tp - r_j), masked
 template <int RT>
-__global__ void __launch_bounds__(FT) k_kick_tp_fp64(int ntp, int npl, const double *__restrict__ rtp,
-                                                    const double *__restrict__ rpl, const double *__restrict__ Gm,
-                                                    const int32_t *__restrict__ lmask, double *__restrict__ acc,
-                                                    int acc_is_zero) {
+__device__ __forceinline__ void fp64_tp_group(int ntp, int npl, const double *__restrict__ rtp,
+                                              const double *__restrict__ rpl, const double *__restrict__ Gm,
+                                              const int32_t *__restrict__ lmask, double *__restrict__ acc,
+                                              int acc_is_zero, int i0) {
     constexpr int PT = FT / RT;
     __shared__ double sx[PT], sy[PT], sz[PT], sg[PT];
     __shared__ double tx[RT][PT + 1], ty[RT][PT + 1], tz[RT][PT + 1];
     const int t = threadIdx.x;
     const int rr = t / PT, pp = t % PT;
-    const int i0 = blockIdx.x * RT;
     const int i = i0 + rr;
     const bool iact = i < ntp && lmask[i] != 0;
     double xi = 0, yi = 0, zi = 0;
@@ -203,6 +202,55 @@ __global__ void __launch_bounds__(FT) k_kick_tp_fp64(int ntp, int npl, const dou
     }
 }
 
+template <bool RAD, int MODE, int RT>
+__global__ void __launch_bounds__(FT) k_kick_plpl_fp64(int npl, int nplm, const double *__restrict__ r,
+                                                      const double *__restrict__ Gm, const double *__restrict__ R,
+                                                      double *__restrict__ acc, int acc_is_zero) {
+    fp64_plpl_group<RAD, MODE, RT>(npl, nplm, r, Gm, R, acc, acc_is_zero, blockIdx.x * RT);
+}
+
+template <int RT>
+__global__ void __launch_bounds__(FT) k_kick_tp_fp64(int ntp, int npl, const double *__restrict__ rtp,
+                                                    const double *__restrict__ rpl, const double *__restrict__ Gm,
+                                                    const int32_t *__restrict__ lmask, double *__restrict__ acc,
+                                                    int acc_is_zero) {
+    fp64_tp_group<RT>(ntp, npl, rtp, rpl, Gm, lmask, acc, acc_is_zero, blockIdx.x * RT);
+}
+
+// Batched (ensemble) forms: block b takes item b = (system s, first receiver r0) of a
+// table sorted by cost; system s's pl occupy [poff[s], poff[s] + npl[s]) and its tp
+// [toff[s], toff[s] + ntp[s]).  Every system is fully interacting (KICK_DIRECT).
+template <bool RAD, int RT>
+__global__ void __launch_bounds__(FT) k_kick_plpl_fp64_batched(const int4 *__restrict__ items,
+                                                              const int32_t *__restrict__ poff,
+                                                              const int32_t *__restrict__ npl,
+                                                              const double *__restrict__ r,
+                                                              const double *__restrict__ Gm,
+                                                              const double *__restrict__ R, double *__restrict__ acc,
+                                                              int acc_is_zero) {
+    const int4 w = items[blockIdx.x];
+    const int o = poff[w.x], n = npl[w.x];
+    fp64_plpl_group<RAD, KICK_DIRECT, RT>(n, n, r + 3 * (size_t)o, Gm + o, RAD ? R + o : nullptr, acc + 3 * (size_t)o,
+                                          acc_is_zero, w.y);
+}
+
+template <int RT>
+__global__ void __launch_bounds__(FT) k_kick_tp_fp64_batched(const int4 *__restrict__ items,
+                                                            const int32_t *__restrict__ toff,
+                                                            const int32_t *__restrict__ ntp,
+                                                            const int32_t *__restrict__ poff,
+                                                            const int32_t *__restrict__ npl,
+                                                            const double *__restrict__ rtp,
+                                                            const double *__restrict__ rpl,
+                                                            const double *__restrict__ Gm,
+                                                            const int32_t *__restrict__ lmask,
+                                                            double *__restrict__ acc, int acc_is_zero) {
+    const int4 w = items[blockIdx.x];
+    const int ot = toff[w.x], op = poff[w.x];
+    fp64_tp_group<RT>(ntp[w.x], npl[w.x], rtp + 3 * (size_t)ot, rpl + 3 * (size_t)op, Gm + op, lmask + ot,
+                      acc + 3 * (size_t)ot, acc_is_zero, w.y);
+}
+
 static inline int div_up_i(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 int kick_plpl_fp64(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const double *Gm, const double *R,
@@ -232,6 +280,30 @@ int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const 
     k_kick_tp_fp64<RT><<<div_up_i(ntp, RT), FT, 0, c->stream>>>(ntp, npl, rtp, rpl, Gm, lmask, acc, acc_is_zero);
     c->launches++;
     return launch_status(c, "kick_tp_fp64");
+}
+
+int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
+                           const int32_t *npl, const double *r, const double *Gm, const double *R, double *acc,
+                           int acc_is_zero) {
+    if (nitems <= 0) return SWG_OK;
+    if (rad)
+        k_kick_plpl_fp64_batched<true, FP64_RT><<<nitems, FT, 0, c->stream>>>(items, poff, npl, r, Gm, R, acc,
+                                                                              acc_is_zero);
+    else
+        k_kick_plpl_fp64_batched<false, FP64_RT><<<nitems, FT, 0, c->stream>>>(items, poff, npl, r, Gm, nullptr, acc,
+                                                                               acc_is_zero);
+    c->launches++;
+    return launch_status(c, "kick_plpl_fp64_batched");
+}
+
+int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
+                         const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
+                         const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero) {
+    if (nitems <= 0) return SWG_OK;
+    k_kick_tp_fp64_batched<FP64_RT><<<nitems, FT, 0, c->stream>>>(items, toff, ntp, poff, npl, rtp, rpl, Gm, lmask,
+                                                                  acc, acc_is_zero);
+    c->launches++;
+    return launch_status(c, "kick_tp_fp64_batched");
 }
 
 }  // namespace swg

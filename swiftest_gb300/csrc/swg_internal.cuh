@@ -44,6 +44,57 @@ struct EncWork {
     DevBuf counters; // 2 x unsigned long long
 };
 
+// CUDA-event profile of a step loop by kernel class: begin() records the start event of
+// a record on the stream and returns its index (-1 when off), end() its stop event;
+// read() sums launches and milliseconds per class after a synchronization.
+struct StepProfile {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;  // events 2k, 2k+1 of record k
+    std::vector<int> cls;           // class of record k
+    size_t n = 0;
+    int begin(cudaStream_t st, int c) {
+        if (!on) return -1;
+        const size_t k = n++;
+        while (pool.size() < 2 * n) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            pool.push_back(e);
+        }
+        if (cls.size() < n) cls.resize(n);
+        cls[k] = c;
+        cudaEventRecord(pool[2 * k], st);
+        return (int)k;
+    }
+    void end(cudaStream_t st, int k) {
+        if (k >= 0) cudaEventRecord(pool[2 * k + 1], st);
+    }
+    // out[2c] += launches, out[2c + 1] += ms for classes c < ncls; clears the records
+    void read(double *out, int ncls) {
+        for (int k = 0; k < 2 * ncls; k++) out[k] = 0.0;
+        for (size_t k = 0; k < n; k++) {
+            float ms = 0.f;
+            if (cls[k] >= ncls || cudaEventElapsedTime(&ms, pool[2 * k], pool[2 * k + 1]) != cudaSuccess) continue;
+            out[2 * cls[k]] += 1.0;
+            out[2 * cls[k] + 1] += ms;
+        }
+        n = 0;
+    }
+    void release() {
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+        pool.clear();
+    }
+};
+// RAII record of one kernel class
+struct ProfScope {
+    StepProfile &p;
+    cudaStream_t st;
+    int k;
+    ProfScope(StepProfile &p_, cudaStream_t st_, int c) : p(p_), st(st_), k(p_.begin(st_, c)) {}
+    ~ProfScope() { p.end(st, k); }
+};
+// kernel classes of the step profiles
+enum { PROF_KICK_PL = 0, PROF_KICK_TP = 1, PROF_DRIFT = 2, PROF_ENC0 = 3, PROF_RECUR = 4, PROF_NCLS = 5 };
+
 }  // namespace swg
 
 struct swg_ctx {
@@ -58,6 +109,7 @@ struct swg_ctx {
     swg::EncWork enc;
     void *events[16] = {nullptr};  // measurement events (cudaEvent_t), created on first use
     std::vector<void *> systems;   // live swg_system objects, destroyed with the context
+    std::vector<void *> ensembles; // live swg_ensemble objects, destroyed with the context
 };
 
 namespace swg {
@@ -97,11 +149,31 @@ int64_t kick_mixed_plpl_partials_max(int num_sms, int npl);
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,
                const double *r, const double *Gm, const double *R, double *acc, double sign, double *ahi_ahj);
 
+// Batched (ensemble) pair kernels.  Items are int4 (system, first receiver, receivers,
+// unused) sorted by cost, largest first; per-system offsets and counts are device arrays.
+int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
+                      float4 *B);
+int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *items, const int32_t *roff,
+                       const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
+                       const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
+                       unsigned *head);
+int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
+                           const int32_t *npl, const double *r, const double *Gm, const double *R, double *acc,
+                           int acc_is_zero);
+int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
+                         const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
+                         const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
+// receivers per item of the batched kernels
+constexpr int KICK_MIXED_TILE = 128;
+constexpr int KICK_FP64_TILE = 8;
+constexpr int ENC_TILE = 128;
+
 // drift.cu -- Danby drift
 int drift_all(swg_ctx *c, const double *mu, double mu_scalar, double *x, double *v, int32_t n, int32_t lgr,
               double inv_c2, double dt, const int32_t *lmask, int32_t *iflag);
+// mu_sys/sys (optional): body i uses mu_sys[sys[i]] instead of mu (CSR-packed ensembles)
 int drift_masked(swg_ctx *c, double mu, double *x, double *v, int32_t n, const int32_t *levelg, int irec, double dt,
-                 int32_t *status, int32_t *nfail);
+                 int32_t *status, int32_t *nfail, const double *mu_sys = nullptr, const int32_t *sys = nullptr);
 
 // encounter.cu -- encounter checks and sorting
 int64_t sort_padded_len(int64_t n);
@@ -115,6 +187,14 @@ int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const doubl
                      const double *r2, const double *v2, const double *renc2, int upper, int shift2, double dt,
                      long long cap, int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
                      void *sas_scratch);
+
+int encounter_prep_launch(swg_ctx *c, int64_t n, const double *r, const double *v, const double *renc, float4 *A,
+                          float4 *B, float4 *V);
+int encounter_tri_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *off1, const int32_t *n1,
+                          const float4 *F1, int64_t nf1, const double *r1, const double *v1, const double *renc1,
+                          const int32_t *off2, const int32_t *n2, const float4 *F2, int64_t nf2, const double *r2,
+                          const double *v2, const double *renc2, int upper, double dt, long long cap, int32_t *o1,
+                          int32_t *o2, int32_t *olv, unsigned long long *count);
 
 // Full check of one kind (0 plpl, 1 plplm, 2 pltp): sorted unique pairs in the
 // workspace's raw buffers; *n_out gets the count (host).  Synchronizes.

@@ -20,11 +20,11 @@
 
 #include "drift_impl.cuh"
 #include "swg_internal.cuh"
+#include "symba_dev.cuh"
 
 using namespace swg;
+using namespace swg::sdev;
 
-// device-side central-body record (doubles)
-enum { CB_VB = 0, CB_RB = 3, CB_PTBEG = 6, CB_PTEND = 9, CB_N = 12 };
 
 struct swg_system {
     swg_ctx *c = nullptr;
@@ -56,40 +56,8 @@ struct swg_system {
     int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr;
     DevBuf rec_scratch;
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
-    // optional CUDA-event profile per kernel class (see PROF_* below)
-    bool prof_on = false;
-    std::vector<cudaEvent_t> prof_pool;
-    std::vector<int> prof_cls;  // class of record k (events 2k, 2k+1)
-    size_t prof_n = 0;
+    StepProfile prof;  // optional CUDA-event profile per kernel class (PROF_*)
 };
-
-// kernel classes of the step profile
-enum { PROF_KICK_PL = 0, PROF_KICK_TP = 1, PROF_DRIFT = 2, PROF_ENC0 = 3, PROF_RECUR = 4, PROF_NCLS = 5 };
-
-namespace {
-int prof_begin(swg_system *s, int cls) {
-    if (!s->prof_on) return -1;
-    const size_t k = s->prof_n++;
-    while (s->prof_pool.size() < 2 * s->prof_n) {
-        cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return -1;
-        s->prof_pool.push_back(e);
-    }
-    if (s->prof_cls.size() < s->prof_n) s->prof_cls.resize(s->prof_n);
-    s->prof_cls[k] = cls;
-    cudaEventRecord(s->prof_pool[2 * k], s->c->stream);
-    return (int)k;
-}
-void prof_end(swg_system *s, int k) {
-    if (k >= 0) cudaEventRecord(s->prof_pool[2 * k + 1], s->c->stream);
-}
-struct ProfScope {
-    swg_system *s;
-    int k;
-    ProfScope(swg_system *s_, int cls) : s(s_), k(prof_begin(s_, cls)) {}
-    ~ProfScope() { prof_end(s, k); }
-};
-}  // namespace
 
 namespace {
 
@@ -107,168 +75,26 @@ int dalloc(swg_ctx *c, T **p, size_t n) {
     return SWG_OK;
 }
 
-// ---------------------------------------------------------------- small kernels
-// Ordered sums of the reference's O(N) serial loops.  The terms are formed by the
-// whole block into shared memory, chunk by chunk; thread 0 then adds them one at a
-// time in the reference's index order (exact == 1), which reproduces its rounding.
-// With exact == 0 the block reduces each chunk as a tree (fixed order, faster).
-constexpr int RB = 1024;  // threads of the reduction kernels
 
-struct Sum3 {
-    double x, y, z;
-};
-
-// Sum over i of sign*term(i) for i = 0..n-1 (reverse: n-1..0); term components are
-// written by term_fn into the chunk arrays (with a 0/1 mask).
-// shared-memory workspace of ordered_sum3 (one per kernel)
-struct SumScratch {
-    double cx[RB], cy[RB], cz[RB];
-    double rx[RB / 32], ry[RB / 32], rz[RB / 32];
-    unsigned char cm[RB];
-    Sum3 acc;
-};
-
-template <class TermFn>
-__device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, double sign, SumScratch &sh) {
-    double *cx = sh.cx, *cy = sh.cy, *cz = sh.cz, *rx = sh.rx, *ry = sh.ry, *rz = sh.rz;
-    unsigned char *cm = sh.cm;
-    Sum3 &acc = sh.acc;
-    __syncthreads();  // a previous sum's result may still be being read
-    if (threadIdx.x == 0) acc = {0.0, 0.0, 0.0};
-    __syncthreads();
-    for (int c0 = 0; c0 < n; c0 += RB) {
-        const int k = threadIdx.x;
-        const int idx = reverse ? n - 1 - (c0 + k) : c0 + k;
-        double tx = 0, ty = 0, tz = 0;
-        unsigned char m = 0;
-        if (c0 + k < n) m = term_fn(idx, tx, ty, tz);
-        const int cnt = min(RB, n - c0);
-        if (exact) {
-            cx[k] = tx;
-            cy[k] = ty;
-            cz[k] = tz;
-            cm[k] = m;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double ax = acc.x, ay = acc.y, az = acc.z;
-                for (int q = 0; q < cnt; q++) {
-                    if (!cm[q]) continue;
-                    ax = ax + sign * cx[q];
-                    ay = ay + sign * cy[q];
-                    az = az + sign * cz[q];
-                }
-                acc = {ax, ay, az};
-            }
-            __syncthreads();
-        } else {
-            if (!m) tx = ty = tz = 0.0;
-            for (int off = 16; off > 0; off >>= 1) {
-                tx += __shfl_down_sync(0xffffffffu, tx, off);
-                ty += __shfl_down_sync(0xffffffffu, ty, off);
-                tz += __shfl_down_sync(0xffffffffu, tz, off);
-            }
-            if ((k & 31) == 0) {
-                rx[k >> 5] = tx;
-                ry[k >> 5] = ty;
-                rz[k >> 5] = tz;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double ax = 0, ay = 0, az = 0;
-                for (int w = 0; w < RB / 32; w++) {
-                    ax += rx[w];
-                    ay += ry[w];
-                    az += rz[w];
-                }
-                acc = {acc.x + sign * ax, acc.y + sign * ay, acc.z + sign * az};
-            }
-            __syncthreads();
-        }
-    }
-    return acc;
-}
-
-// helio_drift_linear_pl (helio_drift.f90:129-163): pt = sum(Gm*vb, mask)/GMcb ; rh += pt*dt
+// One-block kernels over a single system's arrays (block-wide bodies in symba_dev.cuh).
 __global__ void __launch_bounds__(RB) k_lindrift_pl(int npl, const double *__restrict__ Gm,
                                                     const double *__restrict__ vb, const int32_t *__restrict__ lmask,
                                                     double GMcb, double *rh, double dt, double *dcb, int slot,
                                                     int exact) {
-    auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i] * vb[3 * i + 0];
-        y = Gm[i] * vb[3 * i + 1];
-        z = Gm[i] * vb[3 * i + 2];
-        return lmask[i] != 0;
-    };
     __shared__ SumScratch sh;
-    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, 1.0, sh);
-    const double ptx = s.x / GMcb, pty = s.y / GMcb, ptz = s.z / GMcb;
-    for (int i = threadIdx.x; i < npl; i += blockDim.x) {
-        if (!lmask[i]) continue;
-        rh[3 * i + 0] = rh[3 * i + 0] + ptx * dt;
-        rh[3 * i + 1] = rh[3 * i + 1] + pty * dt;
-        rh[3 * i + 2] = rh[3 * i + 2] + ptz * dt;
-    }
-    if (threadIdx.x == 0) {
-        dcb[slot + 0] = ptx;
-        dcb[slot + 1] = pty;
-        dcb[slot + 2] = ptz;
-    }
+    blk_lindrift_pl(npl, Gm, vb, lmask, GMcb, rh, dt, dcb, slot, exact, sh);
 }
-
-// swiftest_util_coord_vh2vb_pl (swiftest_util.f90:424-456)
 __global__ void __launch_bounds__(RB) k_vh2vb_pl(int npl, const double *__restrict__ Gm,
                                                  const double *__restrict__ vh, double *vb, double GMcb, double *dcb,
                                                  int exact) {
-    auto gm = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i];
-        y = z = 0.0;
-        return 1;
-    };
     __shared__ SumScratch sh;
-    const Sum3 g = ordered_sum3(npl, false, exact != 0, gm, 1.0, sh);
-    const double Gmtot = GMcb + g.x;
-    auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i] * vh[3 * i + 0];
-        y = Gm[i] * vh[3 * i + 1];
-        z = Gm[i] * vh[3 * i + 2];
-        return 1;
-    };
-    const Sum3 s = ordered_sum3(npl, false, exact != 0, term, -1.0, sh);
-    const double cx = s.x / Gmtot, cy = s.y / Gmtot, cz = s.z / Gmtot;
-    if (threadIdx.x == 0) {
-        dcb[CB_VB + 0] = cx;
-        dcb[CB_VB + 1] = cy;
-        dcb[CB_VB + 2] = cz;
-    }
-    for (int i = threadIdx.x; i < npl; i += blockDim.x) {
-        vb[3 * i + 0] = vh[3 * i + 0] + cx;
-        vb[3 * i + 1] = vh[3 * i + 1] + cy;
-        vb[3 * i + 2] = vh[3 * i + 2] + cz;
-    }
+    blk_vh2vb_pl(npl, Gm, vh, vb, GMcb, dcb, exact, sh);
 }
-
-// swiftest_util_coord_vb2vh_pl (swiftest_util.f90:363-392), reverse-order sum
 __global__ void __launch_bounds__(RB) k_vb2vh_pl(int npl, const double *__restrict__ Gm,
                                                  const double *__restrict__ vb, const int32_t *__restrict__ status,
                                                  double *vh, double GMcb, double *dcb, int exact) {
-    auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i] * vb[3 * i + 0] / GMcb;
-        y = Gm[i] * vb[3 * i + 1] / GMcb;
-        z = Gm[i] * vb[3 * i + 2] / GMcb;
-        return status[i] != ST_INACTIVE;
-    };
     __shared__ SumScratch sh;
-    const Sum3 s = ordered_sum3(npl, true, exact != 0, term, -1.0, sh);
-    if (threadIdx.x == 0) {
-        dcb[CB_VB + 0] = s.x;
-        dcb[CB_VB + 1] = s.y;
-        dcb[CB_VB + 2] = s.z;
-    }
-    for (int i = threadIdx.x; i < npl; i += blockDim.x) {
-        vh[3 * i + 0] = vb[3 * i + 0] - s.x;
-        vh[3 * i + 1] = vb[3 * i + 1] - s.y;
-        vh[3 * i + 2] = vb[3 * i + 2] - s.z;
-    }
+    blk_vb2vh_pl(npl, Gm, vb, status, vh, GMcb, dcb, exact, sh);
 }
 
 // test particles: mode 0 vh2vb(vbcb=-pt) ; 1 vb2vh(vbcb=-pt) ; 2 lindrift rh += pt*dt ;
@@ -288,16 +114,6 @@ __global__ void k_tp_misc(int ntp, const int32_t *__restrict__ tlmask, double *t
     }
 }
 
-// v += a*dt (masked) ; optionally rcopy = r (set_beg_end)
-__global__ void k_kick_update(int n, double *v, const double *__restrict__ a, const int32_t *__restrict__ lmask,
-                              double dt, const double *__restrict__ r, double *rcopy) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (rcopy)
-        for (int d = 0; d < 3; d++) rcopy[3 * i + d] = r[3 * i + d];
-    if (!lmask[i]) return;
-    for (int d = 0; d < 3; d++) v[3 * i + d] = v[3 * i + d] + a[3 * i + d] * dt;
-}
 
 // symba_kick_getacch_tp add-back loop (symba_kick.f90:104-118), list order
 __global__ void k_pltp_addback(int64_t n, const int32_t *__restrict__ i1, const int32_t *__restrict__ i2,
@@ -318,555 +134,25 @@ __global__ void k_pltp_addback(int64_t n, const int32_t *__restrict__ i1, const 
     }
 }
 
-// symba_step_reset_system (symba_step.f90:265-331) + set_renc(0)
-__global__ void k_symba_reset(int npl, int ntp, int32_t *levelg, int32_t *levelm, int32_t *nplenc, int32_t *ntpenc,
-                              int32_t *lmask, int32_t *tlevelg, int32_t *tlevelm, int32_t *tnplenc,
-                              int32_t *tlmask) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < npl) {
-        levelg[i] = -1;
-        levelm[i] = -1;
-        nplenc[i] = 0;
-        ntpenc[i] = 0;
-        lmask[i] = 1;
-    }
-    if (i < ntp) {
-        tlevelg[i] = -1;
-        tlevelm[i] = -1;
-        tnplenc[i] = 0;
-        tlmask[i] = 1;
-    }
-}
 
-// symba_util_set_renc (symba_util.f90:245-267)
-__device__ __forceinline__ double d_renc(double rhill, double rhscale, int scale) {
-    double rshell_irec = 1.0;
-    for (int k = 1; k <= scale; k++) rshell_irec = rshell_irec * RSHELL;
-    return rhill * rhscale * rshell_irec;
-}
-__global__ void k_set_renc(int npl, const double *rhill, double rhscale, int scale, double *renc) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < npl) renc[i] = d_renc(rhill[i], rhscale, scale);
-}
 
-// level-0 bookkeeping of symba_encounter_check_pl / _tp (symba_encounter_check.f90:53-83, 267-290)
-__global__ void k_level0_mark(int64_t n, int32_t *l, int64_t cap, int tp, int32_t *levelg, int32_t *levelm,
-                              int32_t *cnt1, int32_t *tlevelg, int32_t *tlevelm, int32_t *cnt2) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int32_t *i1 = l, *i2 = l + cap, *st = l + 3 * cap, *lev = l + 4 * cap;
-    const int i = i1[k] - 1, j = i2[k] - 1;
-    st[k] = ST_ACTIVE;
-    lev[k] = 0;
-    levelg[i] = 0;
-    levelm[i] = 0;
-    if (!tp) {
-        levelg[j] = 0;
-        levelm[j] = 0;
-        atomicAdd(&cnt1[i], 1);
-        atomicAdd(&cnt1[j], 1);
-    } else {
-        tlevelg[j] = 0;
-        tlevelm[j] = 0;
-        atomicAdd(&cnt1[i], 1);
-        atomicAdd(&cnt2[j], 1);
-    }
-}
-
-// Sort a short raw pair list by (index1, index2), drop repeated pairs, and write it as a
-// SyMBA encounter list with status ACTIVE, level 0 and the level-0 body marks of
-// symba_encounter_check_pl / _tp (symba_encounter_check.f90:53-83, 267-290).  One block.
-constexpr int FIN_N = 4096;
-__global__ void __launch_bounds__(1024) k_list_finalize(int n, const int32_t *__restrict__ ri1,
-                                                        const int32_t *__restrict__ ri2,
-                                                        const int32_t *__restrict__ rlv, int32_t *l, int64_t cap,
-                                                        int tp, int32_t *levelg, int32_t *levelm, int32_t *cnt1,
-                                                        int32_t *tlevelg, int32_t *tlevelm, int32_t *cnt2,
-                                                        unsigned long long *nout) {
-    __shared__ unsigned long long key[FIN_N];
-    __shared__ int s_part[1024];
-    int npad = 1;
-    while (npad < n) npad <<= 1;
-    for (int t = threadIdx.x; t < npad; t += blockDim.x)
-        key[t] = t < n ? (((unsigned long long)(uint32_t)ri1[t] << 33) | ((unsigned long long)(uint32_t)ri2[t] << 1) |
-                          (unsigned long long)(rlv[t] != 0))
-                       : ~0ull;
-    __syncthreads();
-    for (int k = 2; k <= npad; k <<= 1)
-        for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int t = threadIdx.x; t < npad; t += blockDim.x) {
-                const int p = t ^ jj;
-                if (p > t) {
-                    const bool up = (t & k) == 0;
-                    const unsigned long long a = key[t], b = key[p];
-                    if (up ? a > b : a < b) {
-                        key[t] = b;
-                        key[p] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    // each thread owns 4 consecutive entries; keep the first of each (index1, index2)
-    const int base = 4 * threadIdx.x;
-    int keep[4], cntk = 0;
-    for (int q = 0; q < 4; q++) {
-        const int t = base + q;
-        keep[q] = t < n && (t == 0 || (key[t] >> 1) != (key[t - 1] >> 1));
-        cntk += keep[q];
-    }
-    s_part[threadIdx.x] = cntk;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int v = threadIdx.x >= (unsigned)off ? s_part[threadIdx.x - off] : 0;
-        __syncthreads();
-        s_part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    int o = s_part[threadIdx.x] - cntk;
-    for (int q = 0; q < 4; q++) {
-        if (!keep[q]) continue;
-        const unsigned long long kk = key[base + q];
-        const int i1 = (int)(kk >> 33), i2 = (int)((kk >> 1) & 0xffffffffull), lv = (int)(kk & 1ull);
-        l[o] = i1;
-        l[cap + o] = i2;
-        l[2 * cap + o] = lv;
-        l[3 * cap + o] = ST_ACTIVE;
-        l[4 * cap + o] = 0;
-        levelg[i1 - 1] = 0;
-        levelm[i1 - 1] = 0;
-        atomicAdd(&cnt1[i1 - 1], 1);
-        if (!tp) {
-            levelg[i2 - 1] = 0;
-            levelm[i2 - 1] = 0;
-            atomicAdd(&cnt1[i2 - 1], 1);
-        } else {
-            tlevelg[i2 - 1] = 0;
-            tlevelm[i2 - 1] = 0;
-            atomicAdd(&cnt2[i2 - 1], 1);
-        }
-        o++;
-    }
-    if (threadIdx.x == 1023) *nout = (unsigned long long)s_part[1023];
-}
-
-// encounter_check_one (encounter_check.f90:573-621)
-__device__ __forceinline__ void d_enc_one(double xr, double yr, double zr, double vxr, double vyr, double vzr,
-                                          double renc, double dt, int &lenc, int &lvdotr) {
-    const double r2 = xr * xr + yr * yr + zr * zr;
-    const double r2crit = renc * renc;
-    double vdotr, r2min;
-    if (r2 > r2crit) {
-        vdotr = vxr * xr + vyr * yr + vzr * zr;
-        if (vdotr > 0.0) {
-            r2min = r2;
-        } else {
-            const double v2 = vxr * vxr + vyr * vyr + vzr * vzr;
-            if (v2 <= VSMALL) {
-                r2min = r2;
-            } else {
-                const double tmin = -vdotr / v2;
-                if (tmin < dt)
-                    r2min = r2 - vdotr * vdotr / v2;
-                else
-                    r2min = r2 + 2.0 * vdotr * dt + v2 * (dt * dt);
-            }
-        }
-    } else {
-        vdotr = -1.0;
-        r2min = r2;
-    }
-    lvdotr = (vdotr < 0.0);
-    lenc = lvdotr && (r2min <= r2crit);
-}
-
-// x**(-1.5) of the shell kick (symba_kick.f90:204,307): sqrt(x) and x*sqrt(x) as
-// double-double pairs (Dekker's error-free transformations with fma residuals),
-// then one Newton step on the reciprocal.  Within half an ulp except in rare
-// near-tie cases, and the same bits as the host evaluation of the same sequence.
-__device__ __forceinline__ double pow_m1p5(double x) {
-    if (!(x > 0.0) || isinf(x)) return pow(x, -1.5);
-    const double s = sqrt(x);
-    const double rs = fma(-s, s, x);
-    const double ds = rs / (2.0 * s);
-    const double p = x * s;
-    const double ep = fma(x, s, -p);
-    const double ql = ep + x * ds;
-    const double y0 = 1.0 / p;
-    const double err = fma(-y0, p, 1.0) - y0 * ql;
-    return fma(y0, err, y0);
-}
-
-// powi: square-and-multiply (gfortran's real**integer)
-__device__ __forceinline__ double d_powi(double x, int m) {
-    unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
-    double y = (n % 2) ? x : 1.0;
-    while (n >>= 1) {
-        x = x * x;
-        if (n % 2) y = y * x;
-    }
-    return m < 0 ? 1.0 / y : y;
-}
-
-// Encounter lists live in one int32 allocation per kind: [i1 | i2 | lvdotr | status | level],
-// each `cap` long.
-struct RecArgs {
-    int npl, ntp;
-    int64_t npp, ppcap, npt, ptcap;
-    int32_t *pp, *pt;
-    double *rh, *vb, *ah, *trh, *tvb, *tah;
-    const double *Gm, *rhill, *radius;
-    int32_t *status, *tstatus, *levelg, *levelm, *tlevelg, *tlevelm;
-    double GMcb, rhscale, dt;
-    uint8_t *lenc, *good;           // list-sized byte scratch
-    double *terms;                  // 6 doubles per list entry
-    int32_t *bpl, *btp;             // compact sets of bodies that appear in the lists
-    int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
-    int32_t *out;                   // [0] status, [1] deepest level reached
-};
-
-// Item index of this thread in the recursion kernel's block loops: consecutive items go
-// to different warps, hence to different SM sub-partitions.  The few pairs and bodies
-// of an encounter each run a long serial FP64 chain, and GB300's narrow FP64 pipe
-// takes about as long for a warp instruction with one active lane as with 32, so
-// spreading them over the four sub-partitions' pipes is what runs them concurrently.
-__device__ __forceinline__ int spread_tid() { return (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5); }
-
-// symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), whole block.
-__device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any) {
-    const int64_t npp = a.npp, npt = a.npt;
-    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
-        const bool isp = k < npp;
-        const int64_t q = isp ? k : k - npp;
-        int32_t *l = isp ? a.pp : a.pt;
-        const int64_t cap = isp ? a.ppcap : a.ptcap;
-        int32_t *i1 = l, *i2 = l + cap, *lv = l + 2 * cap, *st = l + 3 * cap, *lev = l + 4 * cap;
-        uint8_t le_out = 0;
-        if (st[q] == ST_ACTIVE && lev[q] == irec - 1) {
-            const int i = i1[q] - 1, j = i2[q] - 1;
-            double xr[3], vr[3];
-            const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
-            const double *vj = isp ? &a.vb[3 * j] : &a.tvb[3 * j];
-            for (int d = 0; d < 3; d++) {
-                xr[d] = rj[d] - a.rh[3 * i + d];
-                vr[d] = vj[d] - a.vb[3 * i + d];
-            }
-            const double renci = d_renc(a.rhill[i], a.rhscale, irec);
-            const double rcrit = isp ? renci + d_renc(a.rhill[j], a.rhscale, irec) : renci;
-            int le, lvd;
-            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
-            lv[q] = lvd;
-            if (le) {
-                const double rs = isp ? a.radius[i] + a.radius[j] : a.radius[i];
-                const double rlim2 = isp ? rs * rs : a.radius[i] * a.radius[i];
-                const double rji2 = xr[0] * xr[0] + xr[1] * xr[1] + xr[2] * xr[2];
-                le = rji2 > rlim2;
-            }
-            le_out = (uint8_t)le;
-        }
-        a.lenc[k] = le_out;
-    }
-    __syncthreads();
-    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
-        if (!a.lenc[k]) continue;
-        *s_any = 1;
-        const bool isp = k < npp;
-        const int64_t q = isp ? k : k - npp;
-        int32_t *l = isp ? a.pp : a.pt;
-        const int64_t cap = isp ? a.ppcap : a.ptcap;
-        const int i = l[q] - 1, j = l[cap + q] - 1;
-        a.levelg[i] = irec;
-        atomicMax(&a.levelm[i], irec);
-        if (isp) {
-            a.levelg[j] = irec;
-            atomicMax(&a.levelm[j], irec);
-        } else {
-            a.tlevelg[j] = irec;
-            atomicMax(&a.tlevelm[j], irec);
-        }
-        l[4 * cap + q] = irec;
-    }
-    __syncthreads();
-}
-
-// symba_kick_list_plpl / _pltp (symba_kick.f90:126-340) for one sign, whole block.
-// The per-pair factors (sqrt, divide, the shell polynomial) depend only on positions,
-// so every pair is evaluated in parallel into `terms`.  The additions are then made
-// by one thread per body, which walks the list in order and adds only its own terms:
-// each body receives exactly the reference's additions in the reference's order,
-// while GB300's narrow FP64 pipe sees one instruction stream for all bodies instead
-// of one serial stream per pair.  A body that sits in several pairs gets its velocity
-// kicked once with its full acceleration, as in the reference (its later pairs add
-// zero).  good[k]: 0 not kicked, 1 kicked, 2 zeroed then skipped (r^2 < rim1).  The
-// reference's lmask refresh at entry is kept by the step loop instead (lmask ==
-// status /= INACTIVE wherever the recursion runs).
-__device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, double dt, int irec, int sgn) {
-    const int64_t npp = a.npp, npt = a.npt;
-    if (npp + npt == 0) return;
-    const int irm1 = irec - 1;
-    const int irecl = sgn < 0 ? irec - 1 : irec;
-    const double rs2 = a.rhscale * a.rhscale;
-    const double rshell_pow = d_powi(RSHELL, 2 * irecl);
-    const int32_t *pi1 = a.pp, *pi2 = a.pp + a.ppcap, *pst = a.pp + 3 * a.ppcap;
-    const int32_t *ti1 = a.pt, *ti2 = a.pt + a.ptcap, *tst = a.pt + 3 * a.ptcap;
-    const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
-    // good flags and per-pair terms
-    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
-        const bool isp = k < npp;
-        const int64_t q = isp ? k : k - npp;
-        const int i = (isp ? pi1 : ti1)[q] - 1, j = (isp ? pi2 : ti2)[q] - 1;
-        bool g;
-        if (isp)
-            g = do_pp && (pst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.levelg[j] >= irm1);
-        else
-            g = do_pt && (tst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
-        if (!g) {
-            a.good[k] = 0;
-            continue;
-        }
-        double ri;
-        if (isp) {
-            const double rhs = a.rhill[i] + a.rhill[j];
-            ri = ((rhs * rhs) * rs2) * rshell_pow;
-        } else {
-            ri = ((a.rhill[i] * a.rhill[i]) * rs2) * rshell_pow;
-        }
-        const double rim1 = ri * (RSHELL * RSHELL);
-        const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
-        double dx[3];
-        for (int d = 0; d < 3; d++) dx[d] = rj[d] - a.rh[3 * i + d];
-        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-        if (r2 < rim1) {
-            a.good[k] = 2;
-            continue;
-        }
-        a.good[k] = 1;
-        double fac;
-        if (r2 < ri) {
-            const double ris = sqrt(ri);
-            const double r = sqrt(r2);
-            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
-        } else {
-            const double ir3 = 1.0 / (r2 * sqrt(r2));
-            fac = ir3;
-        }
-        double *t = &a.terms[6 * k];
-        const double faci = fac * a.Gm[i];
-        if (isp) {
-            const double facj = fac * a.Gm[j];
-            for (int d = 0; d < 3; d++) {
-                t[d] = facj * dx[d];
-                t[3 + d] = faci * dx[d];
-            }
-        } else {
-            for (int d = 0; d < 3; d++) t[d] = faci * dx[d];
-        }
-    }
-    __syncthreads();
-    // ordered per-body accumulation and the velocity kick
-    const double sdt = (double)sgn * dt;
-    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
-        const bool isp = b < nbpl;
-        const int body = isp ? a.bpl[b] : a.btp[b - nbpl];
-        bool zeroed = false, kicked = false;
-        double ax = 0.0, ay = 0.0, az = 0.0;
-        if (isp) {
-            for (int64_t k = 0; k < npp; k++) {
-                const int i = pi1[k] - 1, j = pi2[k] - 1;
-                if (i != body && j != body) continue;
-                const uint8_t g = a.good[k];
-                if (g == 0) continue;
-                zeroed = true;
-                if (g != 1) continue;
-                kicked = true;
-                const double *t = &a.terms[6 * k];
-                if (i == body) {
-                    ax = ax + t[0];
-                    ay = ay + t[1];
-                    az = az + t[2];
-                } else {
-                    ax = ax - t[3];
-                    ay = ay - t[4];
-                    az = az - t[5];
-                }
-            }
-            if (zeroed) {
-                if (kicked) {
-                    a.vb[3 * body + 0] = a.vb[3 * body + 0] + sdt * ax;
-                    a.vb[3 * body + 1] = a.vb[3 * body + 1] + sdt * ay;
-                    a.vb[3 * body + 2] = a.vb[3 * body + 2] + sdt * az;
-                }
-                a.ah[3 * body + 0] = a.ah[3 * body + 1] = a.ah[3 * body + 2] = 0.0;
-            }
-        } else {
-            for (int64_t q = 0; q < npt; q++) {
-                if (ti2[q] - 1 != body) continue;
-                const uint8_t g = a.good[npp + q];
-                if (g == 0) continue;
-                zeroed = true;
-                if (g != 1) continue;
-                kicked = true;
-                const double *t = &a.terms[6 * (npp + q)];
-                ax = ax - t[0];
-                ay = ay - t[1];
-                az = az - t[2];
-            }
-            if (zeroed) {
-                if (kicked) {
-                    a.tvb[3 * body + 0] = a.tvb[3 * body + 0] + sdt * ax;
-                    a.tvb[3 * body + 1] = a.tvb[3 * body + 1] + sdt * ay;
-                    a.tvb[3 * body + 2] = a.tvb[3 * body + 2] + sdt * az;
-                }
-                a.tah[3 * body + 0] = a.tah[3 * body + 1] = a.tah[3 * body + 2] = 0.0;
-            }
-        }
-    }
-    __syncthreads();
-}
-
-// One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): the
-// +1 kicks of both lists, then (below level 0) the -1 kicks.
-__device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, double dt, int irecp, bool both) {
-    blk_kick_lists_sgn(a, nbpl, nbtp, dt, irecp, 1);
-    if (both) blk_kick_lists_sgn(a, nbpl, nbtp, dt, irecp, -1);
-}
-
-// symba_drift_pl / _tp at level irec (symba_drift.f90:14-61) over the bodies that
-// appear in the lists (every other body has levelg == -1 inside the recursion).
-__device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec, double dt) {
-    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
-        const bool isp = b < nbpl;
-        const int i = isp ? a.bpl[b] : a.btp[b - nbpl];
-        const int32_t *lev = isp ? a.levelg : a.tlevelg;
-        int32_t *st = isp ? a.status : a.tstatus;
-        if (lev[i] != irec || st[i] == ST_INACTIVE) continue;
-        double *x = isp ? &a.rh[3 * i] : &a.trh[3 * i];
-        double *v = isp ? &a.vb[3 * i] : &a.tvb[3 * i];
-        double rx = x[0], ry = x[1], rz = x[2], vx = v[0], vy = v[1], vz = v[2];
-        const int fl = d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
-        x[0] = rx;
-        x[1] = ry;
-        x[2] = rz;
-        v[0] = vx;
-        v[1] = vy;
-        v[2] = vz;
-        if (fl != 0) st[i] = ST_DISCARDED_DRIFTERR;
-    }
-    __syncthreads();
-}
-
-// symba_step_set_recur_levels_system (symba_step.f90:118-160)
-__device__ void blk_set_recur_levels(const RecArgs &a, int nbpl, int nbtp, int ireci) {
-    const int irecp = ireci + 1;
-    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
-        int32_t *lev = b < nbpl ? &a.levelg[a.bpl[b]] : &a.tlevelg[a.btp[b - nbpl]];
-        if (*lev == irecp) *lev = ireci;
-    }
-    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x) {
-        int32_t *lev = k < a.npp ? &a.pp[4 * a.ppcap + k] : &a.pt[4 * a.ptcap + (k - a.npp)];
-        if (*lev == irecp) *lev = ireci;
-    }
-    __syncthreads();
-}
-
-constexpr int MAXLEV = 48;
-constexpr int RECT = 256;  // threads of the recursion kernel
-
-// symba_step_recur_system (symba_step.f90:163-262) for the whole recursion tree of one
-// step, started at level 0, in a single block: the reference's recursive calls become
-// an explicit stack of (loop counter, phase) per level, and every per-level operation
-// is a block-wide device function separated by barriers.
+// The whole SyMBA recursion of one step, one block (blk_symba_recursion).
 __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
-    __shared__ int s_nbpl, s_nbtp, s_any;
-    __shared__ int s_j[MAXLEV], s_phase[MAXLEV];
-    if (threadIdx.x == 0) {
-        s_nbpl = s_nbtp = 0;
-        a.out[0] = 0;
-    }
-    __syncthreads();
-    // compact sets of bodies named in the lists
-    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x) {
-        const bool isp = k < a.npp;
-        const int64_t q = isp ? k : k - a.npp;
-        const int32_t *l = isp ? a.pp : a.pt;
-        const int64_t cap = isp ? a.ppcap : a.ptcap;
-        const int i = l[q] - 1, j = l[cap + q] - 1;
-        if (atomicExch(&a.mark_pl[i], 1) == 0) a.bpl[atomicAdd(&s_nbpl, 1)] = i;
-        if (isp) {
-            if (atomicExch(&a.mark_pl[j], 1) == 0) a.bpl[atomicAdd(&s_nbpl, 1)] = j;
-        } else {
-            if (atomicExch(&a.mark_tp[j], 1) == 0) a.btp[atomicAdd(&s_nbtp, 1)] = j;
-        }
-    }
-    __syncthreads();
-    const int nbpl = s_nbpl, nbtp = s_nbtp;
-    int ireci = 0;
-    if (threadIdx.x == 0) {
-        s_j[0] = 1;
-        s_phase[0] = 0;
-    }
-    __syncthreads();
-    int deepest = 0, substeps = 0;
-    for (;;) {
-        double p3 = 1.0;
-        for (int k = 0; k < ireci; k++) p3 *= 3.0;
-        const double dtl = a.dt / p3;
-        const double dth = 0.5 * dtl;
-        const int irecp = ireci + 1;
-        const int nloops = ireci == 0 ? 1 : NTENC;
-        if (s_phase[ireci] == 0) {
-            if (s_j[ireci] > nloops) {
-                if (ireci == 0) break;
-                __syncthreads();
-                ireci--;
-                if (threadIdx.x == 0) s_phase[ireci] = 1;
-                __syncthreads();
-                continue;
-            }
-            if (dtl / a.dt < 2.220446049250313e-16) {
-                if (threadIdx.x == 0) a.out[0] = SWG_ERR_RECURSION;
-                break;
-            }
-            if (irecp > deepest) deepest = irecp;
-            substeps++;
-            if (threadIdx.x == 0) s_any = 0;
-            __syncthreads();
-            blk_list_check(a, irecp, dtl, &s_any);
-            blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
-            blk_drift(a, nbpl, nbtp, ireci, dtl);
-            const int any = s_any;
-            __syncthreads();
-            if (any) {
-                if (ireci + 1 >= MAXLEV) {
-                    if (threadIdx.x == 0) a.out[0] = SWG_ERR_RECURSION;
-                    break;
-                }
-                ireci++;
-                if (threadIdx.x == 0) {
-                    s_j[ireci] = 1;
-                    s_phase[ireci] = 0;
-                }
-                __syncthreads();
-                continue;
-            }
-        }
-        // after the deeper levels (or none) for loop j of level ireci
-        blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
-        blk_set_recur_levels(a, nbpl, nbtp, ireci);
-        if (threadIdx.x == 0) {
-            s_j[ireci]++;
-            s_phase[ireci] = 0;
-        }
-        __syncthreads();
-    }
-    __syncthreads();
-    for (int b = threadIdx.x; b < nbpl; b += blockDim.x) a.mark_pl[a.bpl[b]] = 0;
-    for (int b = threadIdx.x; b < nbtp; b += blockDim.x) a.mark_tp[a.btp[b]] = 0;
-    if (threadIdx.x == 0) {
-        atomicMax(&a.out[1], deepest);
-        atomicAdd(&a.out[2], substeps);
-    }
+    if (threadIdx.x == 0) a.out[0] = 0;
+    blk_symba_recursion(a);
+}
+
+// energy diagnostic: potential rows (one thread per row) and the one-block totals
+__global__ void k_energy_rows(int n, const double *rb, const double *Gm, const int32_t *status, double *rows) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rows[i] = d_energy_row(i, n, rb, Gm, status);
+}
+__global__ void __launch_bounds__(RB) k_energy_final(int n, int whm, const double *rh, const double *vh,
+                                                     const double *vbin, const double *Gm, const double *radius,
+                                                     const int32_t *status, double GMcb, int lclose,
+                                                     const double *rows, double *rb, double *out) {
+    __shared__ SumScratch sh;
+    blk_energy_final(n, whm, rh, vh, vbin, Gm, radius, status, GMcb, lclose, rows, rb, out, sh);
 }
 
 // ---- WHM serial coordinate kernels (whm_coord.f90:14-124) and accelerations (whm_kick.f90:125-215)
@@ -987,137 +273,6 @@ __global__ void k_whm_drift_status(int n, const int32_t *iflag, int32_t *status,
     }
 }
 
-// ---- energy / momentum (swiftest_util.f90:1172-1401), masses as G*m
-__device__ __forceinline__ double d_norm2s(double a, double b, double c) {
-    double scale = 0.0, ssq = 1.0;
-    const double v[3] = {a, b, c};
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        if (v[k] != 0.0) {
-            const double absx = fabs(v[k]);
-            if (scale < absx) {
-                const double q = scale / absx;
-                ssq = 1.0 + ssq * q * q;
-                scale = absx;
-            } else {
-                const double q = absx / scale;
-                ssq = ssq + q * q;
-            }
-        }
-    }
-    return scale * sqrt(ssq);
-}
-__global__ void k_energy_rows(int n, const double *rb, const double *Gm, const int32_t *status, double *rows) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double row = 0.0;
-    if (status[i] != ST_INACTIVE) {
-        for (int j = i + 1; j < n; j++) {
-            if (status[j] == ST_INACTIVE) continue;
-            row = row + (-(Gm[i] * Gm[j]) / d_norm2s(rb[3 * i] - rb[3 * j], rb[3 * i + 1] - rb[3 * j + 1],
-                                                    rb[3 * i + 2] - rb[3 * j + 2]));
-        }
-    }
-    rows[i] = row;
-}
-__global__ void __launch_bounds__(RB) k_energy_final(int n, int whm, const double *rh, const double *vh,
-                                                     const double *vbin, const double *Gm, const double *radius,
-                                                     const int32_t *status, double GMcb, double Rcb, int lclose,
-                                                     const double *rows, double *rb, double *out) {
-    __shared__ SumScratch sh;
-    double cbvb[3];
-    if (whm) {
-        auto gm = [&](int i, double &x, double &y, double &z) -> unsigned char {
-            x = Gm[i];
-            y = z = 0.0;
-            return 1;
-        };
-        const double Gmtot = GMcb + ordered_sum3(n, false, false, gm, 1.0, sh).x;
-        auto t = [&](int i, double &x, double &y, double &z) -> unsigned char {
-            x = Gm[i] * vh[3 * i];
-            y = Gm[i] * vh[3 * i + 1];
-            z = Gm[i] * vh[3 * i + 2];
-            return 1;
-        };
-        const Sum3 c3 = ordered_sum3(n, false, false, t, -1.0, sh);
-        cbvb[0] = c3.x / Gmtot;
-        cbvb[1] = c3.y / Gmtot;
-        cbvb[2] = c3.z / Gmtot;
-    } else {
-        auto t = [&](int i, double &x, double &y, double &z) -> unsigned char {
-            x = Gm[i] * vbin[3 * i] / GMcb;
-            y = Gm[i] * vbin[3 * i + 1] / GMcb;
-            z = Gm[i] * vbin[3 * i + 2] / GMcb;
-            return status[i] != ST_INACTIVE;
-        };
-        const Sum3 c3 = ordered_sum3(n, true, false, t, -1.0, sh);
-        cbvb[0] = c3.x;
-        cbvb[1] = c3.y;
-        cbvb[2] = c3.z;
-    }
-    auto gact = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i];
-        y = z = 0.0;
-        return status[i] != ST_INACTIVE;
-    };
-    const double gsum = ordered_sum3(n, false, false, gact, 1.0, sh).x;
-    const double Gmtot = GMcb + gsum;
-    auto xt = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i] * rh[3 * i];
-        y = Gm[i] * rh[3 * i + 1];
-        z = Gm[i] * rh[3 * i + 2];
-        return status[i] != ST_INACTIVE;
-    };
-    const Sum3 x3 = ordered_sum3(n, false, false, xt, 1.0, sh);
-    const double cbrb[3] = {-x3.x / Gmtot, -x3.y / Gmtot, -x3.z / Gmtot};
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        for (int d = 0; d < 3; d++) rb[3 * i + d] = rh[3 * i + d] + cbrb[d];
-    __syncthreads();
-    auto vel = [&](int i, int d) { return whm ? vh[3 * i + d] + cbvb[d] : vbin[3 * i + d]; };
-    auto Lt = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        const double *r = &rb[3 * i];
-        const double v0 = vel(i, 0), v1 = vel(i, 1), v2 = vel(i, 2);
-        x = Gm[i] * (r[1] * v2 - r[2] * v1);
-        y = Gm[i] * (r[2] * v0 - r[0] * v2);
-        z = Gm[i] * (r[0] * v1 - r[1] * v0);
-        return status[i] != ST_INACTIVE;
-    };
-    const Sum3 Lp = ordered_sum3(n, false, false, Lt, 1.0, sh);
-    auto kt = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        const double v0 = vel(i, 0), v1 = vel(i, 1), v2 = vel(i, 2);
-        x = Gm[i] * (v0 * v0 + v1 * v1 + v2 * v2);
-        y = -GMcb * Gm[i] / d_norm2s(rb[3 * i], rb[3 * i + 1], rb[3 * i + 2]);
-        z = -GMcb * Gm[i] / d_norm2s(rh[3 * i], rh[3 * i + 1], rh[3 * i + 2]);
-        return status[i] != ST_INACTIVE;
-    };
-    const Sum3 kp = ordered_sum3(n, false, false, kt, 1.0, sh);
-    auto bt = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = lclose ? -3.0 * Gm[i] * Gm[i] / (5.0 * radius[i]) : 0.0;
-        y = rows[i];
-        z = 0.0;
-        return 1;
-    };
-    const Sum3 bp = ordered_sum3(n, false, false, bt, 1.0, sh);
-    if (threadIdx.x == 0) {
-        const double mcb = GMcb;
-        const double kecb = mcb * (cbvb[0] * cbvb[0] + cbvb[1] * cbvb[1] + cbvb[2] * cbvb[2]);
-        const double L[3] = {mcb * (cbrb[1] * cbvb[2] - cbrb[2] * cbvb[1]), mcb * (cbrb[2] * cbvb[0] - cbrb[0] * cbvb[2]),
-                             mcb * (cbrb[0] * cbvb[1] - cbrb[1] * cbvb[0])};
-        const double pe_pairs = bp.y;
-        const double pe = pe_pairs + kp.y;
-        const double be = bp.x;
-        const double ke = 0.5 * (kecb + kp.x);
-        out[0] = ke + pe + be;
-        out[1] = ke;
-        out[2] = pe;
-        out[3] = be;
-        out[4] = L[0] + Lp.x;
-        out[5] = L[1] + Lp.y;
-        out[6] = L[2] + Lp.z;
-        out[7] = GMcb + gsum;
-        out[8] = ke + (pe_pairs + kp.z) + be;
-    }
-}
 
 }  // namespace
 
@@ -1159,7 +314,7 @@ int kick_vb_pl(swg_system *s, double dt, int lbeg) {
     swg_ctx *c = s->c;
     if (s->npl == 0) return SWG_OK;
     {
-        ProfScope ps(s, PROF_KICK_PL);
+        ProfScope ps(s->prof, s->c->stream, PROF_KICK_PL);
         SWG_TRY(accel_int_pl(s, 1));
     }
     if (s->integrator == SWG_SYMBA && s->plpl_n > 0) {
@@ -1179,7 +334,7 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
     if (s->ntp == 0) return SWG_OK;
     const double *rp = lbeg ? s->rbeg : s->rend;
     if (s->npl > 0) {
-        ProfScope ps(s, PROF_KICK_TP);
+        ProfScope ps(s->prof, s->c->stream, PROF_KICK_TP);
         if (s->precision == SWG_MIXED) {
             const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
             SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, s->npl, nch)));
@@ -1227,14 +382,14 @@ int vb2vh_pl(swg_system *s) {
 int drift_pl(swg_system *s, double dt) {
     if (s->npl == 0) return SWG_OK;
     const int32_t *lev = s->integrator == SWG_SYMBA ? s->levelg : nullptr;
-    ProfScope ps(s, PROF_DRIFT);
+    ProfScope ps(s->prof, s->c->stream, PROF_DRIFT);
     return drift_masked(s->c, s->GMcb, s->rh, s->vb, s->npl, lev, s->irec, dt, s->status, nullptr);
 }
 int drift_tp(swg_system *s, double dt) {
     if (s->ntp == 0) return SWG_OK;
     const int32_t *lev = s->integrator == SWG_SYMBA ? s->tlevelg : nullptr;
     double *v = s->integrator == SWG_WHM ? s->tvh : s->tvb;
-    ProfScope ps(s, PROF_DRIFT);
+    ProfScope ps(s->prof, s->c->stream, PROF_DRIFT);
     return drift_masked(s->c, s->GMcb, s->trh, v, s->ntp, lev, s->irec, dt, s->tstatus, nullptr);
 }
 
@@ -1532,7 +687,7 @@ int symba_recursion(swg_system *s, double dt) {
     a.mark_pl = s->mark_pl;
     a.mark_tp = s->mark_tp;
     a.out = s->rec_out;
-    ProfScope ps(s, PROF_RECUR);
+    ProfScope ps(s->prof, s->c->stream, PROF_RECUR);
     k_symba_recursion<<<1, RECT, 0, c->stream>>>(a);
     SWG_TRY(L(c, "symba_recursion"));
     // status word read back at the next host synchronization
@@ -1578,7 +733,7 @@ int symba_step(swg_system *s, double dt) {
     s->lfirst_pl = s->lfirstkick;
     int lany = 0;
     {
-        ProfScope ps(s, PROF_ENC0);
+        ProfScope ps(s->prof, s->c->stream, PROF_ENC0);
         SWG_TRY(symba_level0(s, dt, &lany));
     }
     if (lany) {
@@ -1658,7 +813,7 @@ int swg_system_destroy(swg_system *s) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);
-    for (cudaEvent_t e : s->prof_pool) cudaEventDestroy(e);
+    s->prof.release();
     delete s;
     return SWG_OK;
 }
@@ -1829,12 +984,12 @@ int swg_system_energy(swg_system *s, double *out) {
     // barycentric positions first (energy rows need rb): the final kernel computes rb,
     // so run it twice: once for rb, then rows, then again for the totals.
     k_energy_final<<<1, RB, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
-                                            s->status, s->GMcb, s->Rcb, s->lclose, rows, rb, dout);
+                                            s->status, s->GMcb, s->lclose, rows, rb, dout);
     SWG_TRY(L(c, "energy_rb"));
     k_energy_rows<<<grid_for(n, 128), 128, 0, c->stream>>>(n, rb, s->Gmass, s->status, rows);
     SWG_TRY(L(c, "energy_rows"));
     k_energy_final<<<1, RB, 0, c->stream>>>(n, s->integrator == SWG_WHM, s->rh, s->vh, s->vb, s->Gmass, s->radius,
-                                            s->status, s->GMcb, s->Rcb, s->lclose, rows, rb, dout);
+                                            s->status, s->GMcb, s->lclose, rows, rb, dout);
     SWG_TRY(L(c, "energy_final"));
     SWG_TRY(cuda_status(c, cudaMemcpyAsync(out, dout, 9 * 8, cudaMemcpyDeviceToHost, c->stream), "energy"));
     return cuda_status(c, cudaStreamSynchronize(c->stream), "energy");
@@ -1844,7 +999,9 @@ int swg_system_stats(swg_system *s, int64_t *out) {
     if (!s || !out) return SWG_ERR_ARG;
     if (s->integrator == SWG_SYMBA) {
         int32_t dev[4];
-        SWG_TRY(cuda_status(s->c, cudaMemcpy(dev, s->rec_out, sizeof(dev), cudaMemcpyDeviceToHost), "stats"));
+        SWG_TRY(cuda_status(s->c, cudaMemcpyAsync(dev, s->rec_out, sizeof(dev), cudaMemcpyDeviceToHost, s->c->stream),
+                            "stats"));
+        SWG_TRY(cuda_status(s->c, cudaStreamSynchronize(s->c->stream), "stats"));
         s->stats[1] = dev[1];
         s->stats[5] = dev[2];
     }
@@ -1895,22 +1052,15 @@ int swg_system_get_state_async(swg_system *s, double *rh, double *vh, double *tr
 
 int swg_system_profile(swg_system *s, int enable) {
     if (!s) return SWG_ERR_ARG;
-    s->prof_on = enable != 0;
-    s->prof_n = 0;
+    s->prof.on = enable != 0;
+    s->prof.n = 0;
     return SWG_OK;
 }
 
 int swg_system_profile_read(swg_system *s, double *out) {
     if (!s || !out) return SWG_ERR_ARG;
-    for (int k = 0; k < 2 * PROF_NCLS; k++) out[k] = 0.0;
     SWG_TRY(cuda_status(s->c, cudaStreamSynchronize(s->c->stream), "profile"));
-    for (size_t k = 0; k < s->prof_n; k++) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, s->prof_pool[2 * k], s->prof_pool[2 * k + 1]) != cudaSuccess) continue;
-        out[2 * s->prof_cls[k]] += 1.0;
-        out[2 * s->prof_cls[k] + 1] += ms;
-    }
-    s->prof_n = 0;
+    s->prof.read(out, PROF_NCLS);
     return SWG_OK;
 }
 

@@ -115,3 +115,48 @@ CONFIGS = {
     "C1": dict(integrator="SYMBA", seed=0, npl=2000, ntp=10000, mmin=1e-10, mmax=1e-6, amin=0.3, amax=3.0,
                sig_e=0.01, sig_i=0.005, dt=0.005, nsteps=10000, rhscale=1.0),
 }
+
+# Ensemble configurations: system sizes are log-uniform, drawn from default_rng(seed);
+# system s is then generated by make_system(seed=s, ...) and sorted for its integrator.
+ENSEMBLES = {
+    # batched HELIO ensemble: 512 systems, N_pl in [10, 2000], N_tp = 5 N_pl, C0 distributions
+    "C3": dict(integrator="HELIO", nsys=512, nmin=10, nmax=2000, tp_per_pl=5, mmin=1e-10, mmax=1e-6, amin=0.5,
+               amax=5.0, sig_e=0.01, sig_i=0.005, dt=0.01, rhscale=6.5),
+    # batched SyMBA planetesimal disks: 256 systems, N_pl in [500, 5000], no tp
+    "C4": dict(integrator="SYMBA", nsys=256, nmin=500, nmax=5000, tp_per_pl=0, mmin=1e-11, mmax=1e-7, amin=0.5,
+               amax=2.0, sig_e=0.02, sig_i=0.02, dt=0.002, rhscale=1.0),
+}
+
+
+def ensemble_sizes(nsys, nmin, nmax, seed=0):
+    """Per-system massive-body counts, log-uniform in [nmin, nmax]."""
+    rng = np.random.default_rng(seed)
+    return np.rint(np.exp(rng.uniform(np.log(nmin), np.log(nmax), nsys))).astype(np.int32)
+
+
+def make_ensemble(name="C4", nsys=None, seed=0, scale=1.0, **over):
+    """CSR-packed ensemble of independent systems.
+
+    Returns a dict: ``integrator``, ``dt``, ``rhscale``, per-system ``npl``/``ntp``
+    (int32) and ``GMcb``/``Rcb``, and the concatenated body arrays ``pl`` (rh, vh,
+    Gmass, radius, rhill) and ``tp`` (rh, vh), each system's block sorted for the
+    integrator.  ``nsys`` takes the first systems of the configuration; ``scale``
+    multiplies every system size (for small test ensembles)."""
+    cfg = dict(ENSEMBLES[name])
+    cfg.update(over)
+    n_all = ensemble_sizes(cfg["nsys"], cfg["nmin"], cfg["nmax"], seed)
+    nsys = cfg["nsys"] if nsys is None else int(nsys)
+    npl = np.maximum(np.rint(n_all[:nsys] * scale).astype(np.int32), 2 if cfg["integrator"] == "SYMBA" else 1)
+    ntp = (npl * cfg["tp_per_pl"]).astype(np.int32)
+    pls, tps = [], []
+    for s in range(nsys):
+        _, pl, tp = make_system(seed=s, npl=int(npl[s]), ntp=int(ntp[s]), mmin=cfg["mmin"], mmax=cfg["mmax"],
+                                amin=cfg["amin"], amax=cfg["amax"], sig_e=cfg["sig_e"], sig_i=cfg["sig_i"])
+        pls.append(sort_for_integrator(pl, cfg["integrator"]))
+        tps.append(tp)
+    keys = ("rh", "vh", "Gmass", "radius", "rhill")
+    pl = {k: np.concatenate([p[k] for p in pls]) for k in keys}
+    tp = {k: (np.concatenate([t[k] for t in tps]) if ntp.sum() else np.zeros((0, 3))) for k in ("rh", "vh")}
+    return {"name": name, "integrator": cfg["integrator"], "dt": cfg["dt"], "rhscale": cfg["rhscale"],
+            "npl": npl, "ntp": ntp, "GMcb": np.full(nsys, GMCB), "Rcb": np.full(nsys, RCB), "pl": pl, "tp": tp,
+            "systems": [(pls[s], tps[s]) for s in range(nsys)]}

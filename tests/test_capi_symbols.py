@@ -50,3 +50,22 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
             _lib.load(tmp_path / "absent.so")
         finally:
             _lib._lib = None
+
+
+def _prototypes():
+    """name -> number of parameters, from the header's prototypes."""
+    protos = {}
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b(swg_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+            args = m.group(2).strip()
+            protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return protos
+
+
+def test_python_binding_argument_counts():
+    from swiftest_gb300 import _lib
+    protos = _prototypes()
+    assert protos
+    wrong = {n: (k, len(_lib.SIGNATURES[n][1])) for n, k in protos.items() if len(_lib.SIGNATURES[n][1]) != k}
+    assert not wrong, wrong

@@ -1,0 +1,123 @@
+"""GPU parity of the batched ensemble (CSR-packed systems stepped together) against the oracle.
+
+Every system of an ensemble must take exactly the steps it would take alone, so in
+FP64 mode each system's state after the run is compared bit for bit with the oracle
+stepping that system by itself (the stated 1e-9 relative tolerance is asserted too),
+together with its level-0 encounter list and the summed SyMBA statistics.  The mixed
+path is checked for energy and angular-momentum conservation against the FP64 path.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from swiftest_gb300 import initial_conditions as IC
+from swiftest_gb300.api import Ensemble
+
+pytestmark = pytest.mark.gpu
+
+
+def _compact(name, nsys, scale, tp_per_pl):
+    # compact disks (0.8-1.2 AU, heavier bodies) so that SyMBA systems meet encounters
+    return IC.make_ensemble(name, nsys=nsys, scale=scale, tp_per_pl=tp_per_pl, amin=0.8, amax=1.2, mmin=1e-9,
+                            mmax=1e-6)
+
+
+def _oracles(E, **kw):
+    cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
+    return [O.OracleSystem(E["integrator"], cb, pl, tp if len(tp["rh"]) else None, **kw) for pl, tp in E["systems"]]
+
+
+def _check_states(ens, refs, tol=1e-9):
+    rh, vh, st = ens.get_pl()
+    trh, tvh, tst = ens.get_tp()
+    exact = True
+    for s, ref in enumerate(refs):
+        a, b = ens.poff[s], ens.poff[s + 1]
+        r_rh, r_vh, r_st = ref.get_pl()
+        assert np.array_equal(st[a:b], r_st)
+        pairs = [(rh[a:b], r_rh), (vh[a:b], r_vh)]
+        if ens.ntp[s]:
+            a, b = ens.toff[s], ens.toff[s + 1]
+            o_rh, o_vh, o_st = ref.get_tp()
+            assert np.array_equal(tst[a:b], o_st)
+            pairs += [(trh[a:b], o_rh), (tvh[a:b], o_vh)]
+        for x, y in pairs:
+            rel = np.linalg.norm(x - y, axis=1) / np.linalg.norm(y, axis=1)
+            assert rel.max() <= tol, (s, rel.max())
+            exact = exact and np.array_equal(x, y)
+    return exact
+
+
+def test_symba_ensemble_fp64_bitexact(ctx):
+    E = _compact("C4", nsys=7, scale=0.04, tp_per_pl=2)
+    kw = dict(dt=0.005, rhscale=3.0)
+    ens = Ensemble(ctx, E, precision="FP64", **kw)
+    refs = _oracles(E, **kw)
+    for _ in range(4):
+        ens.step(25)
+        for ref in refs:
+            ref.step(25)
+        for s, ref in enumerate(refs):
+            gi = ens.plpl_list(s)
+            ri = ref.plpl_list()
+            assert all(np.array_equal(a, b) for a, b in zip(gi, ri)), s
+    assert _check_states(ens, refs)
+    st = ens.stats()
+    rs = [r.stats() for r in refs]
+    assert st["system_steps_with_encounters"] == sum(r["steps_with_encounters"] for r in rs)
+    assert st["plpl_encounters"] == sum(r["plpl_encounters"] for r in rs)
+    assert st["pltp_encounters"] == sum(r["pltp_encounters"] for r in rs)
+    assert st["max_recursion"] == max(r["max_recursion"] for r in rs)
+    assert st["recursion_substeps"] == sum(r["recursion_substeps"] for r in rs)
+    assert st["system_steps_with_encounters"] > 0 and st["max_recursion"] >= 1
+    eg = ens.energy()
+    for s, ref in enumerate(refs):
+        er = ref.energy()
+        assert abs(eg["te"][s] - er["te"]) <= 1e-12 * abs(er["te"])
+
+
+def test_helio_ensemble_fp64_bitexact(ctx):
+    E = IC.make_ensemble("C3", nsys=9, scale=0.08)
+    kw = dict(dt=0.01)
+    ens = Ensemble(ctx, E, precision="FP64", **kw)
+    refs = _oracles(E, rhscale=6.5, **kw)
+    ens.step(150)
+    for ref in refs:
+        ref.step(150)
+    assert _check_states(ens, refs)
+
+
+def test_symba_ensemble_uneven_sizes(ctx):
+    # systems of very different sizes (2 .. 300 bodies, tp-free and tp-carrying) in one ensemble
+    parts = [IC.make_system(seed=s, npl=n, ntp=t, amin=0.8, amax=1.2, mmin=1e-9, mmax=1e-6)
+             for s, (n, t) in enumerate([(2, 0), (300, 0), (17, 40), (129, 1), (64, 0)])]
+    systems = [(IC.sort_for_integrator(pl, "SYMBA"), tp) for _, pl, tp in parts]
+    E = {"integrator": "SYMBA", "dt": 0.005, "rhscale": 3.0,
+         "npl": np.array([len(p["Gmass"]) for p, _ in systems], np.int32),
+         "ntp": np.array([len(t["rh"]) for _, t in systems], np.int32),
+         "GMcb": np.full(len(systems), IC.GMCB), "Rcb": np.full(len(systems), IC.RCB),
+         "pl": {k: np.concatenate([p[k] for p, _ in systems]) for k in ("rh", "vh", "Gmass", "radius", "rhill")},
+         "tp": {k: np.concatenate([t[k] for _, t in systems]) for k in ("rh", "vh")}, "systems": systems}
+    ens = Ensemble(ctx, E, precision="FP64")
+    refs = _oracles(E, dt=0.005, rhscale=3.0)
+    ens.step(60)
+    for ref in refs:
+        ref.step(60)
+    assert _check_states(ens, refs)
+
+
+def test_symba_ensemble_mixed_conservation(ctx):
+    E = _compact("C4", nsys=5, scale=0.06, tp_per_pl=0)
+    kw = dict(dt=0.005, rhscale=2.0)
+    f = Ensemble(ctx, E, precision="FP64", **kw)
+    m = Ensemble(ctx, E, precision="MIXED", **kw)
+    e0 = f.energy()
+    f.step(300)
+    m.step(300)
+    ef, em = f.energy(), m.energy()
+    dEf = np.abs(ef["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
+    dEm = np.abs(em["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
+    dLm = np.linalg.norm(em["L"] - e0["L"], axis=1) / np.linalg.norm(e0["L"], axis=1)
+    assert np.all(dEm < np.maximum(2 * dEf, 1e-9)), (dEm, dEf)
+    assert np.all(dLm < 1e-9)
+    assert f.stats()["plpl_encounters"] > 0
