@@ -3,7 +3,8 @@
     python -m swiftest_gb300.profile_cases <case> [--npl N] [--ntp M] [--reps R]
 
 cases: kick_tp_mixed, kick_pl_mixed, kick_tp_fp64, kick_pl_fp64, drift, encounter_pltp,
-encounter_plpl, symba_mixed, symba_fp64.  Inputs are the seeded C1 disk (AU, Msun, yr).
+encounter_plpl, symba_mixed, symba_fp64 (inputs: the seeded C1 disk, AU, Msun, yr), and
+ens_mixed, ens_fp64 (steps of the C4 batched SyMBA ensemble, first --nsys systems).
 Prints the average wall time per call (host buffers, so it includes the copies).
 """
 from __future__ import annotations
@@ -24,6 +25,7 @@ def main(argv=None):
     p.add_argument("--npl", type=int, default=2000)
     p.add_argument("--ntp", type=int, default=10000)
     p.add_argument("--reps", type=int, default=3)
+    p.add_argument("--nsys", type=int, default=None)
     a = p.parse_args(argv)
     from swiftest_gb300 import SWG_FP64, SWG_MIXED
     from swiftest_gb300 import build as B
@@ -45,7 +47,12 @@ def main(argv=None):
         "encounter_pltp": lambda: ctx.encounter_check_all_pltp(pl["rh"], pl["vh"], tp["rh"], tp["vh"], renc, 0.005),
         "encounter_plpl": lambda: ctx.encounter_check_all_plpl(pl["rh"], pl["vh"], renc, 0.005),
     }
-    if a.case.startswith("symba"):
+    if a.case.startswith("ens"):
+        from swiftest_gb300.api import Ensemble
+        E = IC.make_ensemble("C4", nsys=a.nsys)
+        ens = Ensemble(ctx, E, precision="MIXED" if a.case.endswith("mixed") else "FP64")
+        run = lambda: ens.step(1)  # noqa: E731
+    elif a.case.startswith("symba"):
         prec = "MIXED" if a.case.endswith("mixed") else "FP64"
         s = NBodySystem(ctx, "SYMBA", cb, pl, tp, dt=0.005, rhscale=1.0, precision=prec)
         run = lambda: s.step(1)  # noqa: E731
