@@ -1,0 +1,255 @@
+// encounter_sorted.cu -- batched TRIANGULAR pl-pl check over radius-sorted tiles.
+//
+// The reference's triangular check (src/encounter/encounter_check.f90:436-475) tests every
+// pair i < j with encounter_check_one (:573-621).  Here, per system, the bodies are ordered
+// by heliocentric distance (one shared-memory sort per system) and cut into tiles of 64;
+// a pair of tiles is skipped when no pair in it can pass the FP64 test, and every other
+// pair goes through the same FP32 prefilter and FP64 decision as the unsorted kernel, on
+// the bodies' original indices and in the reference's orientation (i < j).  The list is
+// sorted by (index1, index2) afterwards, so it is the triangular check's list exactly; the
+// order only decides how much is skipped.
+//
+// Why a tile pair can be skipped.  encounter_check_one accepts (i, j) only if its computed
+// r2min <= (renc_i + renc_j)^2, where r2min is the minimum over t in [0, dt] of
+// |x_rel + v_rel t|^2 up to a rounding of 6.7e-16 r^2 (see prefilter_reject), i.e. only if
+// D <= R (1 + 1e-15) + 2.6e-8 r with D = min_t |x_rel(t)|.  By the reverse triangle
+// inequality D >= min_t | |x_j + v_j t| - |x_i + v_i t| |, and for |t| <= |dt|
+//     |x|^2 - 2 |x.v| |dt|  <=  |x + v t|^2  <=  |x|^2 + 2 |x.v| |dt| + |v|^2 dt^2,
+// so each body's distance from the central body stays in an interval [lo, hi] over the
+// step.  If the intervals of two tiles are separated by a gap larger than the largest
+// renc_i + renc_j (plus margins for float rounding of the bounds and the 2.6e-8 r term,
+// r <= hi_i + hi_j), no pair across them is accepted.  NaN positions make every
+// comparison false, so such tiles are never skipped.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "encounter_dev.cuh"
+#include "swg_internal.cuh"
+
+namespace swg {
+
+constexpr int SB = 64;                   // bodies per bound tile
+constexpr int SQ = 128;                  // receivers per block (two bound tiles)
+constexpr int SORT_MAX = 16384;          // largest system ordered in shared memory
+static_assert(SQ == ENC_SORTED_TILE && SB == ENC_BOUND_TILE, "tile sizes of the sorted check");
+
+// Per system (one block): order the bodies by |r| (ties by index).  perm[poff + p] is the
+// global index of the body at sorted position p.  Systems above SORT_MAX keep their order.
+__global__ void __launch_bounds__(1024) k_radial_sort(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+                                                      const double *__restrict__ r, int32_t *__restrict__ perm) {
+    extern __shared__ unsigned char smem[];
+    const int s = blockIdx.x;
+    const int n = npl[s], o = poff[s];
+    if (n > SORT_MAX) {
+        for (int t = threadIdx.x; t < n; t += blockDim.x) perm[o + t] = o + t;
+        return;
+    }
+    int npad = 1;
+    while (npad < n) npad <<= 1;
+    float *key = (float *)smem;
+    int32_t *idx = (int32_t *)(key + npad);
+    for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+        float k = __int_as_float(0x7f800000);  // +inf pads the tail
+        if (t < n) {
+            const double *x = &r[3 * (size_t)(o + t)];
+            k = (float)sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        }
+        key[t] = k;
+        idx[t] = t;
+    }
+    __syncthreads();
+    for (int k = 2; k <= npad; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+                const int p = t ^ jj;
+                if (p > t) {
+                    const bool up = (t & k) == 0;
+                    const float ka = key[t], kb = key[p];
+                    const int ia = idx[t], ib = idx[p];
+                    // (key, index) order; a NaN key compares as not-greater, which keeps
+                    // the network a permutation
+                    const bool gt = ka > kb || (ka == kb && ia > ib);
+                    const bool lt = kb > ka || (ka == kb && ib > ia);
+                    if (up ? gt : lt) {
+                        key[t] = kb;
+                        key[p] = ka;
+                        idx[t] = ib;
+                        idx[p] = ia;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int t = threadIdx.x; t < n; t += blockDim.x) perm[o + t] = o + idx[t];
+}
+
+// One block of SB threads per bound tile (sys, first sorted position): the prefilter's
+// float copies in sorted order and the tile's bounds (min lo, max hi, max renc), rounded
+// outward.
+__global__ void __launch_bounds__(SB) k_sorted_prep(const int2 *__restrict__ tiles, const int32_t *__restrict__ poff,
+                                                    const int32_t *__restrict__ npl, const int32_t *__restrict__ perm,
+                                                    const double *__restrict__ r, const double *__restrict__ v,
+                                                    const double *__restrict__ renc, double adt, float4 *A, float4 *B,
+                                                    float4 *V, float4 *bounds) {
+    __shared__ float s_lo[SB / 32], s_hi[SB / 32], s_R[SB / 32];
+    const int2 tl = tiles[blockIdx.x];
+    const int p = poff[tl.x] + tl.y + threadIdx.x;
+    const bool in = tl.y + (int)threadIdx.x < npl[tl.x];
+    float lo = __int_as_float(0x7f800000), hi = -__int_as_float(0x7f800000), Rm = 0.f;
+    if (in) {
+        const int g = perm[p];
+        const BodyF o = load_body(r, v, renc, g);
+        A[p] = o.a;
+        B[p] = o.b;
+        V[p] = o.v;
+        const double *x = &r[3 * (size_t)g], *u = &v[3 * (size_t)g];
+        const double x2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+        const double xv = fabs(x[0] * u[0] + x[1] * u[1] + x[2] * u[2]);
+        const double v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+        const double h2 = x2 + 2.0 * xv * adt + v2 * adt * adt;
+        const double l2 = fmax(x2 - 2.0 * xv * adt, 0.0);
+        lo = __double2float_rd(sqrt(l2) * (1.0 - 1e-12));
+        hi = __double2float_ru(sqrt(h2) * (1.0 + 1e-12));
+        Rm = __double2float_ru(renc[g]);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        lo = fminf(lo, __shfl_down_sync(0xffffffffu, lo, off));
+        hi = fmaxf(hi, __shfl_down_sync(0xffffffffu, hi, off));
+        Rm = fmaxf(Rm, __shfl_down_sync(0xffffffffu, Rm, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_lo[threadIdx.x >> 5] = lo;
+        s_hi[threadIdx.x >> 5] = hi;
+        s_R[threadIdx.x >> 5] = Rm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < SB / 32; w++) {
+            lo = fminf(lo, s_lo[w]);
+            hi = fmaxf(hi, s_hi[w]);
+            Rm = fmaxf(Rm, s_R[w]);
+        }
+        bounds[blockIdx.x] = make_float4(lo, hi, Rm, 0.f);
+    }
+}
+
+// True when no pair across tiles P and Q can pass the FP64 test (see the file comment).
+__device__ __forceinline__ bool tiles_apart(float4 P, float4 Q) {
+    const float gap = fmaxf(__fsub_rd(P.x, Q.y), __fsub_rd(Q.x, P.y));
+    const float reach = __fmaf_ru(__fadd_ru(P.z, Q.z), 1.0f + 1e-5f, 1e-7f * __fadd_ru(P.y, Q.y));
+    return gap > reach;
+}
+
+// Item (system, first receiver in sorted order q0, receivers nr): receivers are sorted
+// positions [q0, q0 + nr), partners sorted positions p < q; tbase[s] is the system's first
+// bound tile.
+__global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict__ items, const int32_t *__restrict__ poff,
+                                                         const int32_t *__restrict__ tbase,
+                                                         const int32_t *__restrict__ perm, const float4 *__restrict__ A,
+                                                         const float4 *__restrict__ B, const float4 *__restrict__ V,
+                                                         const float4 *__restrict__ bounds, const double *__restrict__ r,
+                                                         const double *__restrict__ v, const double *__restrict__ renc,
+                                                         double dt, long long cap, int32_t *__restrict__ o1,
+                                                         int32_t *__restrict__ o2, int32_t *__restrict__ olv,
+                                                         unsigned long long *__restrict__ count) {
+    __shared__ float4 sa[SB], sb[SB], sv[SB];
+    __shared__ int32_t sg[SB];
+    const int4 w = items[blockIdx.x];
+    const int s = w.x, q0 = w.y, nr = w.z;
+    const int o = poff[s];
+    const int qt = tbase[s] + q0 / SB;  // first bound tile of the receivers
+    float4 Q = bounds[qt];
+    if (nr > SB) {
+        const float4 Q2 = bounds[qt + 1];
+        Q = make_float4(fminf(Q.x, Q2.x), fmaxf(Q.y, Q2.y), fmaxf(Q.z, Q2.z), 0.f);
+    }
+    const int q = q0 + threadIdx.x;  // sorted position within the system
+    const bool active = (int)threadIdx.x < nr;
+    BodyF me;
+    int gq = 0;
+    if (active) {
+        me.a = A[o + q];
+        me.b = B[o + q];
+        me.v = V[o + q];
+        gq = perm[o + q];
+    }
+    const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);
+    const int pend = q0 + nr;  // partners p < q <= q0 + nr - 1
+    for (int p0 = 0; p0 < pend; p0 += SB) {
+        if (tiles_apart(bounds[tbase[s] + p0 / SB], Q)) continue;  // block-uniform
+        if (threadIdx.x < SB && p0 + (int)threadIdx.x < pend) {
+            const int pp = o + p0 + threadIdx.x;
+            sa[threadIdx.x] = A[pp];
+            sb[threadIdx.x] = B[pp];
+            sv[threadIdx.x] = V[pp];
+            sg[threadIdx.x] = perm[pp];
+        }
+        __syncthreads();
+        if (active) {
+            const int nt = min(SB, q - p0);  // partners p < q of this tile
+            for (int ii = 0; ii < nt; ii++) {
+                BodyF other;
+                other.a = sa[ii];
+                other.b = sb[ii];
+                other.v = sv[ii];
+                if (prefilter_reject(other, me, dtf)) continue;
+                const int gp = sg[ii];
+                const int i = min(gp, gq), j = max(gp, gq);  // the reference's orientation, i < j
+                const double xr = r[3 * (size_t)j + 0] - r[3 * (size_t)i + 0];
+                const double yr = r[3 * (size_t)j + 1] - r[3 * (size_t)i + 1];
+                const double zr = r[3 * (size_t)j + 2] - r[3 * (size_t)i + 2];
+                const double vxr = v[3 * (size_t)j + 0] - v[3 * (size_t)i + 0];
+                const double vyr = v[3 * (size_t)j + 1] - v[3 * (size_t)i + 1];
+                const double vzr = v[3 * (size_t)j + 2] - v[3 * (size_t)i + 2];
+                int lenc, lv;
+                d_encounter_one(xr, yr, zr, vxr, vyr, vzr, renc[i] + renc[j], dt, lenc, lv);
+                if (lenc) {
+                    const unsigned long long k = atomicAdd(count, 1ull);
+                    if ((long long)k < cap) {
+                        o1[k] = i + 1;
+                        o2[k] = j + 1;
+                        olv[k] = lv;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Dynamic shared memory of k_radial_sort for systems of up to nmax bodies.
+static size_t radial_sort_smem(int nmax) {
+    int npad = 1;
+    while (npad < std::min(nmax, SORT_MAX)) npad <<= 1;
+    return (size_t)8 * npad;
+}
+
+int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t *poff, const int32_t *npl,
+                                  const double *r, const double *v, const double *renc, double dt, int32_t *perm,
+                                  float4 *F, int64_t NPL, int ntiles, const int2 *tiles, const int32_t *tbase,
+                                  float4 *bounds, int nitems, const int4 *items, long long cap, int32_t *o1,
+                                  int32_t *o2, int32_t *olv, unsigned long long *count) {
+    if (nitems <= 0 || ntiles <= 0) return SWG_OK;
+    const size_t smem = radial_sort_smem(nmax);
+    static size_t smem_set = 0;
+    if (smem > 48 * 1024 && smem > smem_set) {
+        SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)smem),
+                            "radial sort smem"));
+        smem_set = smem;
+    }
+    k_radial_sort<<<nsys, 1024, smem, c->stream>>>(poff, npl, r, perm);
+    c->launches++;
+    SWG_TRY(launch_status(c, "radial_sort"));
+    k_sorted_prep<<<ntiles, SB, 0, c->stream>>>(tiles, poff, npl, perm, r, v, renc, fabs(dt), F, F + NPL, F + 2 * NPL,
+                                                bounds);
+    c->launches++;
+    SWG_TRY(launch_status(c, "sorted_prep"));
+    k_encounter_sorted<<<nitems, SQ, 0, c->stream>>>(items, poff, tbase, perm, F, F + NPL, F + 2 * NPL, bounds, r, v,
+                                                     renc, dt, cap, o1, o2, olv, count);
+    c->launches++;
+    return launch_status(c, "encounter_sorted");
+}
+
+}  // namespace swg

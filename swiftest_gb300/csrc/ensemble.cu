@@ -64,12 +64,19 @@ struct swg_ensemble {
     double *trh = nullptr, *tvh = nullptr, *tvb = nullptr, *tah = nullptr;
     int32_t *tstatus = nullptr, *tlmask = nullptr, *tlevelg = nullptr, *tlevelm = nullptr, *tnplenc = nullptr,
             *mark_tp = nullptr;
-    // float copies: split partners of the mixed kick (A|B), prefilter copies (A|B|V)
-    float4 *kA = nullptr, *kB = nullptr, *eP = nullptr, *eT = nullptr;
+    // float copies: split partners of the mixed kick (A|B), prefilter copies (A|B|V) in body
+    // order (pl-tp check) and in radius order (pl-pl check)
+    float4 *kA = nullptr, *kB = nullptr, *eP = nullptr, *eT = nullptr, *eS = nullptr;
+    // radius-sorted pl-pl check: order, bound tiles (system, first sorted position), the
+    // systems' first tiles, bounds, receiver items
+    int32_t *perm = nullptr, *tbase = nullptr;
+    int2 *tiles = nullptr;
+    float4 *bounds = nullptr;
+    int4 *it_esp = nullptr;
+    int ntiles = 0, n_esp = 0, nmax = 0;
     // item tables of the batched pair kernels
-    int4 *it_mpl = nullptr, *it_mtp = nullptr, *it_fpl = nullptr, *it_ftp = nullptr, *it_epp = nullptr,
-         *it_ept = nullptr;
-    int n_mpl = 0, n_mtp = 0, n_fpl = 0, n_ftp = 0, n_epp = 0, n_ept = 0;
+    int4 *it_mpl = nullptr, *it_mtp = nullptr, *it_fpl = nullptr, *it_ftp = nullptr, *it_ept = nullptr;
+    int n_mpl = 0, n_mtp = 0, n_fpl = 0, n_ftp = 0, n_ept = 0;
     unsigned *head = nullptr;
     // encounter lists: [i1 | i2 | lvdotr | status | level] * cap, global 1-based indices
     int32_t *pp_l = nullptr, *pt_l = nullptr;
@@ -369,11 +376,25 @@ int build_items(swg_ensemble *e) {
     SWG_TRY(put_items(e, &e->it_mtp, &e->n_mtp, make_items(S, KICK_MIXED_TILE, tp_recv, plcost)));
     SWG_TRY(put_items(e, &e->it_fpl, &e->n_fpl, make_items(S, KICK_FP64_TILE, npl, plcost)));
     SWG_TRY(put_items(e, &e->it_ftp, &e->n_ftp, make_items(S, KICK_FP64_TILE, ntp, plcost)));
-    // pl-pl check: tile j0 tests partners i < j, i.e. up to j0 + nr
-    auto tri = [&](int, int r0, int nr) { return (double)nr * (r0 + nr); };
-    SWG_TRY(put_items(e, &e->it_epp, &e->n_epp, make_items(S, ENC_TILE, npl, tri)));
     auto tp_with_pl = [&](int s) { return e->h_npl[s] > 0 ? e->h_ntp[s] : 0; };
     SWG_TRY(put_items(e, &e->it_ept, &e->n_ept, make_items(S, ENC_TILE, tp_with_pl, plcost)));
+    // radius-sorted pl-pl check: receiver tiles in system order (their cost depends on
+    // the geometry), bound tiles of every system
+    SWG_TRY(put_items(e, &e->it_esp, &e->n_esp, make_items(S, ENC_SORTED_TILE, npl, [](int, int, int) { return 0.0; })));
+    std::vector<int2> tiles;
+    std::vector<int32_t> tbase(S + 1, 0);
+    for (int s = 0; s < S; s++) {
+        tbase[s] = (int32_t)tiles.size();
+        for (int p0 = 0; p0 < e->h_npl[s]; p0 += ENC_BOUND_TILE) tiles.push_back(make_int2(s, p0));
+        e->nmax = std::max(e->nmax, (int)e->h_npl[s]);
+    }
+    tbase[S] = (int32_t)tiles.size();
+    e->ntiles = (int)tiles.size();
+    SWG_TRY(dalloc(e->c, &e->tiles, tiles.size()));
+    SWG_TRY(upload(e->c, e->tiles, tiles));
+    SWG_TRY(dalloc(e->c, &e->tbase, tbase.size()));
+    SWG_TRY(upload(e->c, e->tbase, tbase));
+    SWG_TRY(dalloc(e->c, &e->bounds, tiles.size()));
     return SWG_OK;
 }
 
@@ -503,9 +524,10 @@ int symba_level0(swg_ensemble *e, double dt) {
             SWG_TRY(ensure(c, w[k]->raw, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
         }
     }
-    SWG_TRY(encounter_prep_launch(c, e->NPL, e->rh, e->vb, e->renc, e->eP, e->eP + e->NPL, e->eP + 2 * e->NPL));
-    if (e->n_ept > 0)
+    if (e->n_ept > 0) {  // body-order copies for the pl-tp check
+        SWG_TRY(encounter_prep_launch(c, e->NPL, e->rh, e->vb, e->renc, e->eP, e->eP + e->NPL, e->eP + 2 * e->NPL));
         SWG_TRY(encounter_prep_launch(c, e->NTP, e->trh, e->tvb, nullptr, e->eT, e->eT + e->NTP, e->eT + 2 * e->NTP));
+    }
     unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
     auto launch = [&](int kind) -> int {
         EncWork &x = *w[kind];
@@ -513,9 +535,9 @@ int symba_level0(swg_ensemble *e, double dt) {
         unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
         SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
         if (kind == 0)
-            SWG_TRY(encounter_tri_batched(c, e->n_epp, e->it_epp, e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc,
-                                          e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc, 1, dt, x.rawcap, i1,
-                                          i2, lv, cnt));
+            SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->rh, e->vb, e->renc, dt,
+                                                  e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase, e->bounds,
+                                                  e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
         else
             SWG_TRY(encounter_tri_batched(c, e->n_ept, e->it_ept, e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc,
                                           e->toff, e->ntp, e->eT, e->NTP, e->trh, e->tvb, nullptr, 0, dt, x.rawcap, i1,
@@ -742,6 +764,8 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) e->kB = e->kA + n;
     if (rc == SWG_OK) rc = dalloc(c, &e->eP, 3 * n);
     if (rc == SWG_OK) rc = dalloc(c, &e->eT, 3 * m);
+    if (rc == SWG_OK) rc = dalloc(c, &e->eS, 3 * n);
+    if (rc == SWG_OK) rc = dalloc(c, &e->perm, n);
     if (rc == SWG_OK) rc = dalloc(c, &e->head, 4);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
     if (rc == SWG_OK) rc = ensure(c, e->rows, sizeof(double) * 4 * n);
@@ -777,8 +801,9 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->enc_steps, e->psys, e->rh, e->vh, e->vb, e->ah, e->rbeg, e->rend, e->Gmass, e->radius,
                     e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
                     e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
-                    e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->it_mpl, e->it_mtp,
-                    e->it_fpl, e->it_ftp, e->it_epp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
+                    e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->eS, e->perm, e->tbase,
+                    e->tiles, e->bounds, e->it_esp, e->it_mpl, e->it_mtp,
+                    e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
                     e->enc_pt.counters.ptr, e->rec_out, e->rec_scratch.ptr, e->rows.ptr, e->eout};
     for (void *p : ptrs)

@@ -167,6 +167,8 @@ int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_
 constexpr int KICK_MIXED_TILE = 128;
 constexpr int KICK_FP64_TILE = 8;
 constexpr int ENC_TILE = 128;
+constexpr int ENC_SORTED_TILE = 128;  // receivers per item of the radius-sorted pl-pl check
+constexpr int ENC_BOUND_TILE = 64;    // bodies per bound tile of the radius-sorted check
 
 // drift.cu -- Danby drift
 int drift_all(swg_ctx *c, const double *mu, double mu_scalar, double *x, double *v, int32_t n, int32_t lgr,
@@ -195,6 +197,17 @@ int encounter_tri_batched(swg_ctx *c, int nitems, const int4 *items, const int32
                           const int32_t *off2, const int32_t *n2, const float4 *F2, int64_t nf2, const double *r2,
                           const double *v2, const double *renc2, int upper, double dt, long long cap, int32_t *o1,
                           int32_t *o2, int32_t *olv, unsigned long long *count);
+
+// Batched TRIANGULAR pl-pl check over radius-sorted tiles (encounter_sorted.cu): per
+// system sort by |r| into perm, float copies F (3 * NPL float4, sorted order) and bound
+// tiles (tiles[k] = (system, first sorted position), tbase[s] = system's first tile),
+// then one block per item (system, first sorted receiver, receivers).  nmax: largest
+// system.  Pairs are written with global 1-based indices, index1 < index2.
+int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t *poff, const int32_t *npl,
+                                  const double *r, const double *v, const double *renc, double dt, int32_t *perm,
+                                  float4 *F, int64_t NPL, int ntiles, const int2 *tiles, const int32_t *tbase,
+                                  float4 *bounds, int nitems, const int4 *items, long long cap, int32_t *o1,
+                                  int32_t *o2, int32_t *olv, unsigned long long *count);
 
 // Full check of one kind (0 plpl, 1 plplm, 2 pltp): sorted unique pairs in the
 // workspace's raw buffers; *n_out gets the count (host).  Synchronizes.
