@@ -88,6 +88,10 @@ struct swg_ensemble {
     int32_t *h_flags = nullptr;  // pinned: [2] recursion status; +8: two unsigned long long counts
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
     StepProfile prof;
+    // side stream for the closing kick of systems without encounters (overlaps the recursion)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    unsigned *head2 = nullptr;
 };
 
 namespace {
@@ -409,26 +413,39 @@ int ensure_pool(swg_ensemble *e, int32_t **l, int64_t *cap, int64_t need) {
     return SWG_OK;
 }
 
-// pl-pl accelerations of all systems into ah (helio_kick_getacch_int_pl / symba_kick_getacch_int_pl)
-int accel_int_pl(swg_ensemble *e) {
+// pl-pl accelerations into ah (helio_kick_getacch_int_pl / symba_kick_getacch_int_pl) of all
+// systems, or (flag != nullptr) of the systems whose flag equals phase, on c->stream.
+int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr, int phase = 0) {
     swg_ctx *c = e->c;
     const bool rad = e->integrator == SWG_SYMBA || e->lclose;
     const double *R = rad ? e->radius : nullptr;
     if (e->precision == SWG_MIXED) {
-        SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB));
+        SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB, flag ? e->psys : nullptr, flag, phase));
         return kick_mixed_batched(c, false, rad, e->n_mpl, e->it_mpl, e->poff, e->poff, e->npl, e->rh, R, e->kA,
-                                  e->kB, nullptr, e->ah, 1, e->head);
+                                  e->kB, nullptr, e->ah, 1, head, flag, phase);
     }
-    return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah, 1);
+    return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah, 1, flag,
+                                  phase);
 }
 
-// helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76)
-int kick_vb_pl(swg_ensemble *e, double dt, int lbeg) {
+// Runs f with the context's stream temporarily replaced (single host thread).
+template <class F>
+int on_stream(swg_ctx *c, cudaStream_t st, F f) {
+    const cudaStream_t saved = c->stream;
+    c->stream = st;
+    const int rc = f();
+    c->stream = saved;
+    return rc;
+}
+
+// helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76).
+// have_acc: the accelerations are already in ah (see ens_step).
+int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false) {
     swg_ctx *c = e->c;
     if (e->NPL == 0) return SWG_OK;
-    {
+    if (!have_acc) {
         ProfScope ps(e->prof, c->stream, PROF_KICK_PL);
-        SWG_TRY(accel_int_pl(e));
+        SWG_TRY(accel_int_pl(e, e->head));
     }
     if (e->integrator == SWG_SYMBA && e->pp_n > 0) {
         k_ens_kick_pairs<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pp, e->pp_l, e->pp_cap, e->rh,
@@ -684,8 +701,25 @@ int ens_step(swg_ensemble *e, double dt) {
     SWG_TRY(tp_misc(e, CB_PTBEG, dth, 2, 4));
     SWG_TRY(kick_vb_tp(e, dth, 1));
     SWG_TRY(drift_bodies(e, dt));
-    if (symba && e->pp_n + e->pt_n > 0) SWG_TRY(symba_recursion(e, dt));
-    SWG_TRY(kick_vb_pl(e, dth, 0));
+    const bool rec = symba && e->pp_n + e->pt_n > 0;
+    if (rec && !e->prof.on && e->NPL > 0) {
+        // The closing accelerations of systems without encounters do not depend on the
+        // recursion: compute them on the side stream while the recursion of the other
+        // systems runs (recursion launched first, so its blocks are resident), then those
+        // of the recursing systems.  Each system's arithmetic is unchanged.
+        swg_ctx *c = e->c;
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
+        SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
+        SWG_TRY(symba_recursion(e, dt));
+        SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
+        SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
+        SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+        SWG_TRY(kick_vb_pl(e, dth, 0, true));
+    } else {
+        if (rec) SWG_TRY(symba_recursion(e, dt));
+        SWG_TRY(kick_vb_pl(e, dth, 0));
+    }
     SWG_TRY(lindrift_pl(e, dth, CB_PTEND));
     SWG_TRY(vb2vh_pl(e));
     SWG_TRY(kick_vb_tp(e, dth, 0));
@@ -767,6 +801,10 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->eS, 3 * n);
     if (rc == SWG_OK) rc = dalloc(c, &e->perm, n);
     if (rc == SWG_OK) rc = dalloc(c, &e->head, 4);
+    if (rc == SWG_OK) rc = dalloc(c, &e->head2, 4);
+    if (rc == SWG_OK) rc = cuda_status(c, cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking), "side stream");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming), "event");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
     if (rc == SWG_OK) rc = ensure(c, e->rows, sizeof(double) * 4 * n);
     if (rc == SWG_OK) {
@@ -802,13 +840,17 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
                     e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
                     e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->eS, e->perm, e->tbase,
-                    e->tiles, e->bounds, e->it_esp, e->it_mpl, e->it_mtp,
+                    e->tiles, e->bounds, e->it_esp, e->head2, e->it_mpl, e->it_mtp,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
                     e->enc_pt.counters.ptr, e->rec_out, e->rec_scratch.ptr, e->rows.ptr, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
+    if (e->side) cudaStreamSynchronize(e->side);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
+    if (e->side) cudaStreamDestroy(e->side);
     e->prof.release();
     delete e;
     return SWG_OK;

@@ -30,7 +30,7 @@
 namespace swg {
 
 constexpr int MT = 64;        // partners per FP32 partial (mixed)
-constexpr int MBLOCK = 128;   // threads per block (mixed)
+constexpr int MBLOCK = 128;   // threads per block (mixed, one system)
 
 // ------------------------------------------------------------------ mixed
 struct FF {
@@ -65,20 +65,31 @@ __device__ __forceinline__ MixedRecv mixed_recv(const double *__restrict__ r, co
     return q;
 }
 
-// Sweep of partners [jbeg, jstop) (indices into the partner arrays) for this thread's
-// receiver, whole block: 64-partner FP32 partials folded into float-float (ax, ay, az).
+// r^-3 in FP32: rsqrtf's estimate y0 refined by one Newton step applied to the cube.
+// With e = 1 - r2 y0^2 the Newton iterate is y1 = y0 (1 + e/2), and
+// y1^3 = y0^3 (1 + 3e/2) + O(e^2) = y0^3 (2.5 - 1.5 r2 y0^2); e ~ 1e-7, so the dropped
+// terms are ~1e-14 relative.
+__device__ __forceinline__ float rinv3(float r2) {
+    const float y = rsqrtf(r2);
+    const float t = y * y;
+    return (t * y) * fmaf(-1.5f, r2 * t, 2.5f);
+}
+
+// Sweep of partners [jbeg, jstop) (indices into the partner arrays) for this thread's RPT
+// receivers, whole block: 64-partner FP32 partials folded into float-float (ax, ay, az).
 // pA/pB hold the partners already split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R);
 // without them each tile converts rpart/Gm/R itself.
 // Pair rule (pl-pl; TP has none): the reference skips j == i and, with GMTINY bodies,
 // pairs of two bodies both at index >= nplm (GMT); with RAD it also skips pairs closer
 // than the sum of the radii, which covers j == i (r^2 == 0 exactly), so the index test
-// is only made without RAD.  `self` is the receiver's index in the partner arrays.
-template <bool TP, bool RAD, bool GMT>
-__device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, int self, int nplm, bool self_m, const MixedRecv &q,
+// is only made without RAD.  self[k] is receiver k's index in the partner arrays.
+template <bool TP, bool RAD, bool GMT, int RPT>
+__device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&self)[RPT], int nplm,
+                                            const bool (&self_m)[RPT], const MixedRecv (&q)[RPT],
                                             const double *__restrict__ rpart, const double *__restrict__ Gm,
                                             const double *__restrict__ R, const float4 *__restrict__ pA,
-                                            const float4 *__restrict__ pB, float4 *sA, float4 *sB, FF &ax, FF &ay,
-                                            FF &az) {
+                                            const float4 *__restrict__ pB, float4 *sA, float4 *sB, FF (&ax)[RPT],
+                                            FF (&ay)[RPT], FF (&az)[RPT]) {
     for (int j0 = jbeg; j0 < jstop; j0 += MT) {
         for (int t = threadIdx.x; t < MT; t += blockDim.x) {
             const int jl = j0 + t;
@@ -98,37 +109,43 @@ __device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, int self, int n
         }
         __syncthreads();
         const int nt = min(MT, jstop - j0);
-        float px = 0.f, py = 0.f, pz = 0.f;
+        float px[RPT], py[RPT], pz[RPT];
+#pragma unroll
+        for (int k = 0; k < RPT; k++) px[k] = py[k] = pz[k] = 0.f;
 #pragma unroll 4
         for (int jj = 0; jj < nt; jj++) {
             const float4 a = sA[jj];
             const float4 b = sB[jj];
-            const float dx = (a.x - q.xh) + (b.x - q.xl);
-            const float dy = (a.y - q.yh) + (b.y - q.yl);
-            const float dz = (a.z - q.zh) + (b.z - q.zl);
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            float y = rsqrtf(r2);
-            y = y * fmaf(-0.5f * r2, y * y, 1.5f);
-            float fac = a.w * (y * y * y);
-            if (!TP) {
-                const int j = j0 + jj;
-                bool ok = true;
-                if (GMT) ok = self_m || j < nplm;
-                if (RAD) {
-                    const float rs = q.R + b.w;
-                    ok = ok && (r2 > rs * rs);
-                } else {
-                    ok = ok && (j != self);
+#pragma unroll
+            for (int k = 0; k < RPT; k++) {
+                const float dx = (a.x - q[k].xh) + (b.x - q[k].xl);
+                const float dy = (a.y - q[k].yh) + (b.y - q[k].yl);
+                const float dz = (a.z - q[k].zh) + (b.z - q[k].zl);
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                float fac = a.w * rinv3(r2);
+                if (!TP) {
+                    const int j = j0 + jj;
+                    bool ok = true;
+                    if (GMT) ok = self_m[k] || j < nplm;
+                    if (RAD) {
+                        const float rs = q[k].R + b.w;
+                        ok = ok && (r2 > rs * rs);
+                    } else {
+                        ok = ok && (j != self[k]);
+                    }
+                    fac = ok ? fac : 0.f;
                 }
-                fac = ok ? fac : 0.f;
+                px[k] = fmaf(fac, dx, px[k]);
+                py[k] = fmaf(fac, dy, py[k]);
+                pz[k] = fmaf(fac, dz, pz[k]);
             }
-            px = fmaf(fac, dx, px);
-            py = fmaf(fac, dy, py);
-            pz = fmaf(fac, dz, pz);
         }
-        ff_add(ax, px);
-        ff_add(ay, py);
-        ff_add(az, pz);
+#pragma unroll
+        for (int k = 0; k < RPT; k++) {
+            ff_add(ax[k], px[k]);
+            ff_add(ay[k], py[k]);
+            ff_add(az[k], pz[k]);
+        }
         __syncthreads();
     }
 }
@@ -160,12 +177,15 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
     const int i = blockIdx.x * MBLOCK + threadIdx.x;
     const bool inrange = i < nrecv;
     const bool active = inrange && (!TP || lmask[i] != 0);
-    MixedRecv q = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (inrange) q = mixed_recv<RAD>(rrecv, R, i);
-    FF ax = {0.f, 0.f}, ay = {0.f, 0.f}, az = {0.f, 0.f};
+    MixedRecv q[1] = {{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}};
+    if (inrange) q[0] = mixed_recv<RAD>(rrecv, R, i);
+    FF axa[1] = {{0.f, 0.f}}, aya[1] = {{0.f, 0.f}}, aza[1] = {{0.f, 0.f}};
     const int jbeg = blockIdx.y * chunk;
     const int jstop = min(npart, jbeg + chunk);
-    mixed_sweep<TP, RAD, GMT>(jbeg, jstop, i, nplm, i < nplm, q, rpart, Gm, R, pA, pB, sA, sB, ax, ay, az);
+    const int self[1] = {i};
+    const bool self_m[1] = {i < nplm};
+    mixed_sweep<TP, RAD, GMT, 1>(jbeg, jstop, self, nplm, self_m, q, rpart, Gm, R, pA, pB, sA, sB, axa, aya, aza);
+    const FF ax = axa[0], ay = aya[0], az = aza[0];
     const int nchunk = gridDim.y;
     if (nchunk == 1) {
         if (active)
@@ -213,22 +233,29 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
 
 // Batched (ensemble) mixed kick: a persistent grid pulls receiver tiles of CSR-packed
 // systems from a work queue (items sorted by cost, largest first, so the tail is made
-// of small tiles).  Item: system s, receivers [r0, r0 + nr) of that system.  Receivers
-// sit at roff[s] + i in rrecv/acc/lmask, partners at poff[s] + j (j < npart[s]) in the
-// pre-split pA/pB.  pl-pl (!TP): rrecv is the pl array, roff == poff, and the receiver
-// is skipped as its own partner through the radius rule (RAD) or the index test.
+// of small tiles).  With sys_flag, only systems whose flag equals `phase` are kicked (the
+// ensemble kicks systems without encounters while the recursion of the others runs).  Item: system s, receivers [r0, r0 + nr) of that system, nr <= 128:
+// MB_THREADS threads own MB_RPT receivers each (r0 + t and r0 + t + MB_THREADS), which
+// halves the shared-memory reads per pair.  Receivers sit at roff[s] + i in
+// rrecv/acc/lmask, partners at poff[s] + j (j < npart[s]) in the pre-split pA/pB.  pl-pl
+// (!TP): rrecv is the pl array, roff == poff, and the receiver is skipped as its own
+// partner through the radius rule (RAD) or the index test.
+constexpr int MB_THREADS = 64;
+constexpr int MB_RPT = 2;
+static_assert(MB_THREADS * MB_RPT == KICK_MIXED_TILE && MB_THREADS >= MT, "batched mixed kick tiling");
 template <bool TP, bool RAD>
-__global__ void __launch_bounds__(MBLOCK) k_kick_mixed_batched(int nitems, const int4 *__restrict__ items,
-                                                              const int32_t *__restrict__ roff,
-                                                              const int32_t *__restrict__ poff,
-                                                              const int32_t *__restrict__ npart,
-                                                              const double *__restrict__ rrecv,
-                                                              const double *__restrict__ R,
-                                                              const float4 *__restrict__ pA,
-                                                              const float4 *__restrict__ pB,
-                                                              const int32_t *__restrict__ lmask,
-                                                              double *__restrict__ acc, int acc_is_zero,
-                                                              unsigned *__restrict__ head) {
+__global__ void __launch_bounds__(MB_THREADS) k_kick_mixed_batched(int nitems, const int4 *__restrict__ items,
+                                                                  const int32_t *__restrict__ roff,
+                                                                  const int32_t *__restrict__ poff,
+                                                                  const int32_t *__restrict__ npart,
+                                                                  const double *__restrict__ rrecv,
+                                                                  const double *__restrict__ R,
+                                                                  const float4 *__restrict__ pA,
+                                                                  const float4 *__restrict__ pB,
+                                                                  const int32_t *__restrict__ lmask,
+                                                                  double *__restrict__ acc, int acc_is_zero,
+                                                                  unsigned *__restrict__ head,
+                                                                  const int32_t *__restrict__ sys_flag, int phase) {
     __shared__ float4 sA[MT];
     __shared__ float4 sB[MT];
     __shared__ int s_item;
@@ -240,29 +267,45 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed_batched(int nitems, const
         if (it >= nitems) break;
         const int4 w = items[it];  // (system, r0, nr, unused)
         const int s = w.x;
-        const bool inrange = (int)threadIdx.x < w.z;
-        const int gi = roff[s] + w.y + threadIdx.x;
-        const bool active = inrange && (!TP || lmask[gi] != 0);
-        MixedRecv q = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (inrange) q = mixed_recv<RAD>(rrecv, R, gi);
-        FF ax = {0.f, 0.f}, ay = {0.f, 0.f}, az = {0.f, 0.f};
+        if (sys_flag && sys_flag[s] != phase) continue;  // another launch's system (block-uniform)
+        MixedRecv q[MB_RPT];
+        FF ax[MB_RPT], ay[MB_RPT], az[MB_RPT];
+        int gi[MB_RPT];
+        bool inr[MB_RPT], sm[MB_RPT];
+#pragma unroll
+        for (int k = 0; k < MB_RPT; k++) {
+            const int l = threadIdx.x + k * MB_THREADS;
+            inr[k] = l < w.z;
+            gi[k] = roff[s] + w.y + l;
+            sm[k] = true;
+            q[k] = MixedRecv{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (inr[k]) q[k] = mixed_recv<RAD>(rrecv, R, gi[k]);
+            ax[k] = ay[k] = az[k] = FF{0.f, 0.f};
+        }
         const int p0 = poff[s];
-        mixed_sweep<TP, RAD, false>(p0, p0 + npart[s], gi, 0, true, q, nullptr, nullptr, nullptr, pA, pB, sA, sB, ax,
-                                    ay, az);
-        if (active)
-            mixed_store(&acc[3 * gi], ax, ay, az, acc_is_zero);
-        else if (inrange && acc_is_zero)
-            acc[3 * gi + 0] = acc[3 * gi + 1] = acc[3 * gi + 2] = 0.0;
+        mixed_sweep<TP, RAD, false, MB_RPT>(p0, p0 + npart[s], gi, 0, sm, q, nullptr, nullptr, nullptr, pA, pB, sA,
+                                            sB, ax, ay, az);
+#pragma unroll
+        for (int k = 0; k < MB_RPT; k++) {
+            if (!inr[k]) continue;
+            if (!TP || lmask[gi[k]] != 0)
+                mixed_store(&acc[3 * gi[k]], ax[k], ay[k], az[k], acc_is_zero);
+            else if (acc_is_zero)
+                acc[3 * gi[k] + 0] = acc[3 * gi[k] + 1] = acc[3 * gi[k] + 2] = 0.0;
+        }
     }
 }
 
 // Partners split once per kick into float hi/lo pairs (the conversion runs on the
 // FP64 pipe, which is narrow on GB300; doing it here instead of in every block
 // keeps the pair kernel on the FP32 pipe).
+// sysid/flag (optional): split only bodies whose system's flag equals phase.
 __global__ void k_kick_split(int n, const double *__restrict__ r, const double *__restrict__ Gm,
-                             const double *__restrict__ R, float4 *A, float4 *B) {
+                             const double *__restrict__ R, float4 *A, float4 *B, const int32_t *__restrict__ sysid,
+                             const int32_t *__restrict__ flag, int phase) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
+    if (sysid && flag[sysid[j]] != phase) return;
     float4 a, b;
     split_hi_lo(r[3 * j + 0], a.x, b.x);
     split_hi_lo(r[3 * j + 1], a.y, b.y);
@@ -409,7 +452,8 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
     const size_t poff = ((KICK_COUNTERS * sizeof(unsigned) + (size_t)nchunk * nrecv * 6 * sizeof(float)) + 255) & ~size_t(255);
     float4 *pA = (float4 *)((char *)scratch + poff), *pB = pA + npart;
     if (npart > 0) {
-        k_kick_split<<<div_up(npart, 256), 256, 0, c->stream>>>(npart, rpart, Gm, tp ? nullptr : R, pA, pB);
+        k_kick_split<<<div_up(npart, 256), 256, 0, c->stream>>>(npart, rpart, Gm, tp ? nullptr : R, pA, pB, nullptr,
+                                                                 nullptr, 0);
         c->launches++;
     }
     dim3 grid(bx, nchunk);
@@ -462,9 +506,9 @@ int64_t kick_mixed_plpl_partials_max(int num_sms, int npl) {
 
 // Split n partner bodies into float hi/lo tiles (A = x_hi, y_hi, z_hi, Gm; B = x_lo, y_lo, z_lo, R).
 int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
-                      float4 *B) {
+                      float4 *B, const int32_t *sysid, const int32_t *flag, int phase) {
     if (n <= 0) return SWG_OK;
-    k_kick_split<<<div_up(n, 256), 256, 0, c->stream>>>((int)n, r, Gm, R, A, B);
+    k_kick_split<<<div_up(n, 256), 256, 0, c->stream>>>((int)n, r, Gm, R, A, B, sysid, flag, phase);
     c->launches++;
     return launch_status(c, "kick_split");
 }
@@ -475,7 +519,7 @@ int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, 
 int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *items, const int32_t *roff,
                        const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
                        const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
-                       unsigned *head) {
+                       unsigned *head, const int32_t *sys_flag, int phase) {
     if (nitems <= 0) return SWG_OK;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
     static int occ[3] = {0, 0, 0};  // resident blocks per SM of each variant, queried once
@@ -483,26 +527,27 @@ int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *it
     if (occ[v] == 0) {
         int nb = 0;
         cudaError_t e = tp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_batched<true, false>,
-                                                                           MBLOCK, 0)
+                                                                           MB_THREADS, 0)
                            : rad ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                                       &nb, k_kick_mixed_batched<false, true>, MBLOCK, 0)
+                                       &nb, k_kick_mixed_batched<false, true>, MB_THREADS, 0)
                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                                       &nb, k_kick_mixed_batched<false, false>, MBLOCK, 0);
+                                       &nb, k_kick_mixed_batched<false, false>, MB_THREADS, 0);
         SWG_TRY(cuda_status(c, e, "occupancy"));
         occ[v] = nb > 0 ? nb : 1;
     }
     const int grid = std::min(nitems, occ[v] * (c->num_sms > 0 ? c->num_sms : 152));
     if (tp)
-        k_kick_mixed_batched<true, false><<<grid, MBLOCK, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
+        k_kick_mixed_batched<true, false><<<grid, MB_THREADS, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
                                                                           nullptr, pA, pB, lmask, acc, acc_is_zero,
-                                                                          head);
+                                                                          head, sys_flag, phase);
     else if (rad)
-        k_kick_mixed_batched<false, true><<<grid, MBLOCK, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R,
-                                                                          pA, pB, nullptr, acc, acc_is_zero, head);
+        k_kick_mixed_batched<false, true><<<grid, MB_THREADS, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R,
+                                                                          pA, pB, nullptr, acc, acc_is_zero, head,
+                                                                          sys_flag, phase);
     else
-        k_kick_mixed_batched<false, false><<<grid, MBLOCK, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
+        k_kick_mixed_batched<false, false><<<grid, MB_THREADS, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
                                                                            nullptr, pA, pB, nullptr, acc,
-                                                                           acc_is_zero, head);
+                                                                           acc_is_zero, head, sys_flag, phase);
     c->launches++;
     return launch_status(c, "kick_mixed_batched");
 }

@@ -151,15 +151,16 @@ int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const 
 
 // Batched (ensemble) pair kernels.  Items are int4 (system, first receiver, receivers,
 // unused) sorted by cost, largest first; per-system offsets and counts are device arrays.
+// sys_flag/phase (optional, pl-pl): only systems s with sys_flag[s] == phase are processed.
 int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
-                      float4 *B);
+                      float4 *B, const int32_t *sysid = nullptr, const int32_t *sys_flag = nullptr, int phase = 0);
 int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *items, const int32_t *roff,
                        const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
                        const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
-                       unsigned *head);
+                       unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
 int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const double *r, const double *Gm, const double *R, double *acc,
-                           int acc_is_zero);
+                           int acc_is_zero, const int32_t *sys_flag = nullptr, int phase = 0);
 int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
                          const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
                          const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
