@@ -9,6 +9,10 @@
 // sorted by (index1, index2) afterwards, so it is the triangular check's list exactly; the
 // order only decides how much is skipped.
 //
+// The order only has to be roughly radial, so it is refreshed every few steps (bodies move
+// ~1e-4 of the disk width per step); the bounds are recomputed from the current state at
+// every check.
+//
 // Why a tile pair can be skipped.  encounter_check_one accepts (i, j) only if its computed
 // r2min <= (renc_i + renc_j)^2, where r2min is the minimum over t in [0, dt] of
 // |x_rel + v_rel t|^2 up to a rounding of 6.7e-16 r^2 (see prefilter_reject), i.e. only if
@@ -90,7 +94,7 @@ __global__ void __launch_bounds__(1024) k_radial_sort(const int32_t *__restrict_
 __global__ void __launch_bounds__(SB) k_sorted_prep(const int2 *__restrict__ tiles, const int32_t *__restrict__ poff,
                                                     const int32_t *__restrict__ npl, const int32_t *__restrict__ perm,
                                                     const double *__restrict__ r, const double *__restrict__ v,
-                                                    const double *__restrict__ renc, double adt, float4 *A, float4 *B,
+                                                    const double *__restrict__ renc, float adt, float4 *A, float4 *B,
                                                     float4 *V, float4 *bounds) {
     __shared__ float s_lo[SB / 32], s_hi[SB / 32], s_R[SB / 32];
     const int2 tl = tiles[blockIdx.x];
@@ -103,15 +107,18 @@ __global__ void __launch_bounds__(SB) k_sorted_prep(const int2 *__restrict__ til
         A[p] = o.a;
         B[p] = o.b;
         V[p] = o.v;
-        const double *x = &r[3 * (size_t)g], *u = &v[3 * (size_t)g];
-        const double x2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
-        const double xv = fabs(x[0] * u[0] + x[1] * u[1] + x[2] * u[2]);
-        const double v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-        const double h2 = x2 + 2.0 * xv * adt + v2 * adt * adt;
-        const double l2 = fmax(x2 - 2.0 * xv * adt, 0.0);
-        lo = __double2float_rd(sqrt(l2) * (1.0 - 1e-12));
-        hi = __double2float_ru(sqrt(h2) * (1.0 + 1e-12));
-        Rm = __double2float_ru(renc[g]);
+        // The interval in FP32 from the float copies.  The hi parts and the rounded
+        // velocity are within 6e-8 (relative) of the FP64 values, and the float sums
+        // below add < 5e-7 relative to |x|^2, |v|^2 and, for x.v (which may cancel),
+        // < 5e-7 |x| |v| absolute; the margins (1e-5 of each term, plus 1e-5 |x||v| on
+        // x.v) bound the true interval from outside.
+        const float x2 = fmaf(o.a.z, o.a.z, fmaf(o.a.y, o.a.y, o.a.x * o.a.x));
+        const float v2 = fmaf(o.v.z, o.v.z, fmaf(o.v.y, o.v.y, o.v.x * o.v.x));
+        const float xv = fabsf(fmaf(o.a.z, o.v.z, fmaf(o.a.y, o.v.y, o.a.x * o.v.x))) + 1e-5f * sqrtf(x2 * v2);
+        const float T = adt;
+        lo = sqrtf(fmaxf(x2 * (1.0f - 1e-5f) - 2.0f * xv * T * (1.0f + 1e-5f), 0.0f)) * (1.0f - 1e-5f);
+        hi = sqrtf((x2 + 2.0f * xv * T + v2 * T * T) * (1.0f + 1e-5f)) * (1.0f + 1e-5f);
+        Rm = o.a.w * (1.0f + 1e-5f);
     }
     for (int off = 16; off > 0; off >>= 1) {
         lo = fminf(lo, __shfl_down_sync(0xffffffffu, lo, off));
@@ -137,7 +144,7 @@ __global__ void __launch_bounds__(SB) k_sorted_prep(const int2 *__restrict__ til
 // True when no pair across tiles P and Q can pass the FP64 test (see the file comment).
 __device__ __forceinline__ bool tiles_apart(float4 P, float4 Q) {
     const float gap = fmaxf(__fsub_rd(P.x, Q.y), __fsub_rd(Q.x, P.y));
-    const float reach = __fmaf_ru(__fadd_ru(P.z, Q.z), 1.0f + 1e-5f, 1e-7f * __fadd_ru(P.y, Q.y));
+    const float reach = __fmaf_ru(__fadd_ru(P.z, Q.z), 1.0f + 1e-5f, 1e-6f * __fadd_ru(P.y, Q.y));
     return gap > reach;
 }
 
@@ -226,23 +233,26 @@ static size_t radial_sort_smem(int nmax) {
 }
 
 int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t *poff, const int32_t *npl,
-                                  const double *r, const double *v, const double *renc, double dt, int32_t *perm,
-                                  float4 *F, int64_t NPL, int ntiles, const int2 *tiles, const int32_t *tbase,
-                                  float4 *bounds, int nitems, const int4 *items, long long cap, int32_t *o1,
-                                  int32_t *o2, int32_t *olv, unsigned long long *count) {
+                                  const double *r, const double *v, const double *renc, double dt, bool resort,
+                                  int32_t *perm, float4 *F, int64_t NPL, int ntiles, const int2 *tiles,
+                                  const int32_t *tbase, float4 *bounds, int nitems, const int4 *items, long long cap,
+                                  int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count) {
     if (nitems <= 0 || ntiles <= 0) return SWG_OK;
-    const size_t smem = radial_sort_smem(nmax);
-    static size_t smem_set = 0;
-    if (smem > 48 * 1024 && smem > smem_set) {
-        SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    (int)smem),
-                            "radial sort smem"));
-        smem_set = smem;
+    if (resort) {
+        const size_t smem = radial_sort_smem(nmax);
+        static size_t smem_set = 0;
+        if (smem > 48 * 1024 && smem > smem_set) {
+            SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        (int)smem),
+                                "radial sort smem"));
+            smem_set = smem;
+        }
+        k_radial_sort<<<nsys, 1024, smem, c->stream>>>(poff, npl, r, perm);
+        c->launches++;
+        SWG_TRY(launch_status(c, "radial_sort"));
     }
-    k_radial_sort<<<nsys, 1024, smem, c->stream>>>(poff, npl, r, perm);
-    c->launches++;
-    SWG_TRY(launch_status(c, "radial_sort"));
-    k_sorted_prep<<<ntiles, SB, 0, c->stream>>>(tiles, poff, npl, perm, r, v, renc, fabs(dt), F, F + NPL, F + 2 * NPL,
+    const float adt = (float)fabs(dt) * (1.0f + 1e-6f);  // |dt| rounded to float, then up
+    k_sorted_prep<<<ntiles, SB, 0, c->stream>>>(tiles, poff, npl, perm, r, v, renc, adt, F, F + NPL, F + 2 * NPL,
                                                 bounds);
     c->launches++;
     SWG_TRY(launch_status(c, "sorted_prep"));

@@ -92,7 +92,11 @@ struct swg_ensemble {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned *head2 = nullptr;
+    int64_t nchecks = 0;  // level-0 checks so far (the radial order is refreshed every RESORT_EVERY)
 };
+
+// level-0 checks between refreshes of the radial order of the pl-pl check
+constexpr int RESORT_EVERY = 8;
 
 namespace {
 
@@ -546,6 +550,7 @@ int symba_level0(swg_ensemble *e, double dt) {
         SWG_TRY(encounter_prep_launch(c, e->NTP, e->trh, e->tvb, nullptr, e->eT, e->eT + e->NTP, e->eT + 2 * e->NTP));
     }
     unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
+    const bool resort = e->nchecks++ % RESORT_EVERY == 0;
     auto launch = [&](int kind) -> int {
         EncWork &x = *w[kind];
         int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
@@ -553,8 +558,8 @@ int symba_level0(swg_ensemble *e, double dt) {
         SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
         if (kind == 0)
             SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->rh, e->vb, e->renc, dt,
-                                                  e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase, e->bounds,
-                                                  e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
+                                                  resort, e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase,
+                                                  e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
         else
             SWG_TRY(encounter_tri_batched(c, e->n_ept, e->it_ept, e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc,
                                           e->toff, e->ntp, e->eT, e->NTP, e->trh, e->tvb, nullptr, 0, dt, x.rawcap, i1,
@@ -927,6 +932,7 @@ int swg_ensemble_initialize(swg_ensemble *e) {
     SWG_TRY(vh2vb_pl(e, false));
     SWG_TRY(tp_misc(e, CB_VB, 0.0, 5, -1));  // tp vb = vh + the central body's vb
     e->t = 0.0;
+    e->nchecks = 0;
     std::memset(e->stats, 0, sizeof(e->stats));
     e->initialized = 1;
     return cuda_status(c, cudaStreamSynchronize(c->stream), "init");

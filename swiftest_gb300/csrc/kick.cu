@@ -16,7 +16,7 @@
 //
 // The mixed path (SWG_MIXED) splits each FP64 coordinate into a float hi/lo
 // pair, forms displacements as (xj_hi - xi_hi) + (xj_lo - xi_lo) in FP32, takes
-// r^-3 from rsqrtf refined by one Newton step, accumulates 64-partner FP32
+// r^-3 from the hardware rsqrt estimate refined by one Newton step, accumulates 64-partner FP32
 // partials into float-float (TwoSum) accumulators, and adds the total to the
 // FP64 acceleration.  Partner ranges are split over blocks to fill all SMs;
 // the last block of each body tile folds the partials in a fixed order, so
@@ -65,12 +65,21 @@ __device__ __forceinline__ MixedRecv mixed_recv(const double *__restrict__ r, co
     return q;
 }
 
-// r^-3 in FP32: rsqrtf's estimate y0 refined by one Newton step applied to the cube.
+// Hardware reciprocal square root estimate (one MUFU instruction, subnormals flushed):
+// r^2 of two distinct bodies is never subnormal, and a zero r^2 (a body paired with
+// itself) gives +inf, which the pair rule replaces by a zero factor.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// r^-3 in FP32: the hardware estimate y0 refined by one Newton step applied to the cube.
 // With e = 1 - r2 y0^2 the Newton iterate is y1 = y0 (1 + e/2), and
 // y1^3 = y0^3 (1 + 3e/2) + O(e^2) = y0^3 (2.5 - 1.5 r2 y0^2); e ~ 1e-7, so the dropped
 // terms are ~1e-14 relative.
 __device__ __forceinline__ float rinv3(float r2) {
-    const float y = rsqrtf(r2);
+    const float y = rsqrt_approx(r2);
     const float t = y * y;
     return (t * y) * fmaf(-1.5f, r2 * t, 2.5f);
 }
@@ -112,7 +121,7 @@ __device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&sel
         float px[RPT], py[RPT], pz[RPT];
 #pragma unroll
         for (int k = 0; k < RPT; k++) px[k] = py[k] = pz[k] = 0.f;
-#pragma unroll 4
+#pragma unroll 8
         for (int jj = 0; jj < nt; jj++) {
             const float4 a = sA[jj];
             const float4 b = sB[jj];

@@ -204,11 +204,13 @@ int encounter_tri_batched(swg_ctx *c, int nitems, const int4 *items, const int32
 // tiles (tiles[k] = (system, first sorted position), tbase[s] = system's first tile),
 // then one block per item (system, first sorted receiver, receivers).  nmax: largest
 // system.  Pairs are written with global 1-based indices, index1 < index2.
+// resort: refresh the radial order (perm is kept between calls; any permutation gives the
+// same list, the order only decides how many tile pairs are skipped).
 int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t *poff, const int32_t *npl,
-                                  const double *r, const double *v, const double *renc, double dt, int32_t *perm,
-                                  float4 *F, int64_t NPL, int ntiles, const int2 *tiles, const int32_t *tbase,
-                                  float4 *bounds, int nitems, const int4 *items, long long cap, int32_t *o1,
-                                  int32_t *o2, int32_t *olv, unsigned long long *count);
+                                  const double *r, const double *v, const double *renc, double dt, bool resort,
+                                  int32_t *perm, float4 *F, int64_t NPL, int ntiles, const int2 *tiles,
+                                  const int32_t *tbase, float4 *bounds, int nitems, const int4 *items, long long cap,
+                                  int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count);
 
 // Full check of one kind (0 plpl, 1 plplm, 2 pltp): sorted unique pairs in the
 // workspace's raw buffers; *n_out gets the count (host).  Synchronizes.

@@ -121,3 +121,23 @@ def test_symba_ensemble_mixed_conservation(ctx):
     assert np.all(dEm < np.maximum(2 * dEf, 1e-9)), (dEm, dEf)
     assert np.all(dLm < 1e-9)
     assert f.stats()["plpl_encounters"] > 0
+
+
+def test_symba_ensemble_lists_many_tiles(ctx):
+    # systems of 150-1500 bodies (many 64-body tiles, radius-sorted culling active), lists
+    # checked against the oracle's all-pairs check at every step across a re-sort boundary
+    E = IC.make_ensemble("C4", nsys=4, scale=0.3)
+    kw = dict(dt=0.002, rhscale=4.0)
+    ens = Ensemble(ctx, E, precision="FP64", **kw)
+    refs = _oracles(E, **kw)
+    total = 0
+    for _ in range(12):
+        ens.step(1)
+        for s, ref in enumerate(refs):
+            ref.step(1)
+            gi = ens.plpl_list(s)
+            ri = ref.plpl_list()
+            assert all(np.array_equal(a, b) for a, b in zip(gi, ri)), s
+            total += len(ri[0])
+    assert total > 0
+    assert _check_states(ens, refs)
