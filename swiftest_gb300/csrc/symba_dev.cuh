@@ -21,18 +21,20 @@ namespace sdev {
 enum { CB_VB = 0, CB_RB = 3, CB_PTBEG = 6, CB_PTEND = 9, CB_N = 12 };
 
 // ---------------------------------------------------------------- small kernels
-// Ordered sums of the reference's O(N) serial loops.  The terms are formed by the
-// whole block into shared memory, chunk by chunk; thread 0 then adds them one at a
-// time in the reference's index order (exact == 1), which reproduces its rounding.
-// With exact == 0 the block reduces each chunk as a tree (fixed order, faster).
+// Ordered sums of the reference's O(N) serial loops.  exact == 1: the terms are formed
+// by the whole block into shared memory, chunk by chunk, and thread 0 adds them one at
+// a time in the reference's index order, which reproduces its rounding.  exact == 0:
+// thread t adds its own terms t, t + RB, t + 2 RB, ... in registers, then the block
+// combines the RB partial sums as a tree (warp shuffles, then one warp over the warp
+// sums): a fixed order, so results are deterministic, with no serial chain.
 constexpr int RB = 1024;  // threads of the reduction kernels
 
 struct Sum3 {
     double x, y, z;
 };
 
-// Sum over i of sign*term(i) for i = 0..n-1 (reverse: n-1..0); term components are
-// written by term_fn into the chunk arrays (with a 0/1 mask).
+// Sum over i of sign*term(i) for i = 0..n-1 (reverse: n-1..0); term_fn(i, x, y, z)
+// writes the components and returns the 0/1 mask.
 // shared-memory workspace of ordered_sum3 (one per kernel)
 struct SumScratch {
     double cx[RB], cy[RB], cz[RB];
@@ -41,22 +43,30 @@ struct SumScratch {
     Sum3 acc;
 };
 
+__device__ __forceinline__ void warp_sum3(double &x, double &y, double &z) {
+    for (int off = 16; off > 0; off >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, off);
+        y += __shfl_down_sync(0xffffffffu, y, off);
+        z += __shfl_down_sync(0xffffffffu, z, off);
+    }
+}
+
 template <class TermFn>
 __device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, double sign, SumScratch &sh) {
     double *cx = sh.cx, *cy = sh.cy, *cz = sh.cz, *rx = sh.rx, *ry = sh.ry, *rz = sh.rz;
     unsigned char *cm = sh.cm;
     Sum3 &acc = sh.acc;
     __syncthreads();  // a previous sum's result may still be being read
-    if (threadIdx.x == 0) acc = {0.0, 0.0, 0.0};
-    __syncthreads();
-    for (int c0 = 0; c0 < n; c0 += RB) {
-        const int k = threadIdx.x;
-        const int idx = reverse ? n - 1 - (c0 + k) : c0 + k;
-        double tx = 0, ty = 0, tz = 0;
-        unsigned char m = 0;
-        if (c0 + k < n) m = term_fn(idx, tx, ty, tz);
-        const int cnt = min(RB, n - c0);
-        if (exact) {
+    if (exact) {
+        if (threadIdx.x == 0) acc = {0.0, 0.0, 0.0};
+        __syncthreads();
+        for (int c0 = 0; c0 < n; c0 += RB) {
+            const int k = threadIdx.x;
+            const int idx = reverse ? n - 1 - (c0 + k) : c0 + k;
+            double tx = 0, ty = 0, tz = 0;
+            unsigned char m = 0;
+            if (c0 + k < n) m = term_fn(idx, tx, ty, tz);
+            const int cnt = min(RB, n - c0);
             cx[k] = tx;
             cy[k] = ty;
             cz[k] = tz;
@@ -73,33 +83,35 @@ __device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, do
                 acc = {ax, ay, az};
             }
             __syncthreads();
-        } else {
-            if (!m) tx = ty = tz = 0.0;
-            for (int off = 16; off > 0; off >>= 1) {
-                tx += __shfl_down_sync(0xffffffffu, tx, off);
-                ty += __shfl_down_sync(0xffffffffu, ty, off);
-                tz += __shfl_down_sync(0xffffffffu, tz, off);
-            }
-            if ((k & 31) == 0) {
-                rx[k >> 5] = tx;
-                ry[k >> 5] = ty;
-                rz[k >> 5] = tz;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double ax = 0, ay = 0, az = 0;
-                for (int w = 0; w < RB / 32; w++) {
-                    ax += rx[w];
-                    ay += ry[w];
-                    az += rz[w];
-                }
-                acc = {acc.x + sign * ax, acc.y + sign * ay, acc.z + sign * az};
-            }
-            __syncthreads();
+        }
+        return acc;
+    }
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int q = threadIdx.x; q < n; q += RB) {
+        double tx, ty, tz;
+        if (term_fn(reverse ? n - 1 - q : q, tx, ty, tz)) {
+            ax += tx;
+            ay += ty;
+            az += tz;
         }
     }
+    warp_sum3(ax, ay, az);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        rx[w] = ax;
+        ry[w] = ay;
+        rz[w] = az;
+    }
+    __syncthreads();
+    if (w == 0) {
+        double x = rx[threadIdx.x], y = ry[threadIdx.x], z = rz[threadIdx.x];  // RB / 32 == 32 warp sums
+        warp_sum3(x, y, z);
+        if (threadIdx.x == 0) acc = {sign * x, sign * y, sign * z};
+    }
+    __syncthreads();
     return acc;
 }
+static_assert(RB / 32 == 32, "ordered_sum3 combines the warp sums in one warp");
 
 // helio_drift_linear_pl (helio_drift.f90:129-163): pt = sum(Gm*vb, mask)/GMcb ; rh += pt*dt
 static __device__ void blk_lindrift_pl(int npl, const double *__restrict__ Gm,
@@ -158,14 +170,23 @@ static __device__ void blk_vh2vb_pl(int npl, const double *__restrict__ Gm,
     }
 }
 
-// swiftest_util_coord_vb2vh_pl (swiftest_util.f90:363-392), reverse-order sum
+// swiftest_util_coord_vb2vh_pl (swiftest_util.f90:363-392), reverse-order sum.  The
+// reference divides every term by GMcb; the non-exact path multiplies by the reciprocal
+// instead (an FP64 divide is ~20 instructions on the narrow FP64 pipe).
 static __device__ void blk_vb2vh_pl(int npl, const double *__restrict__ Gm,
                                                  const double *__restrict__ vb, const int32_t *__restrict__ status,
                                                  double *vh, double GMcb, double *dcb, int exact, SumScratch &sh) {
+    const double inv = 1.0 / GMcb;
     auto term = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = Gm[i] * vb[3 * i + 0] / GMcb;
-        y = Gm[i] * vb[3 * i + 1] / GMcb;
-        z = Gm[i] * vb[3 * i + 2] / GMcb;
+        if (exact) {
+            x = Gm[i] * vb[3 * i + 0] / GMcb;
+            y = Gm[i] * vb[3 * i + 1] / GMcb;
+            z = Gm[i] * vb[3 * i + 2] / GMcb;
+        } else {
+            x = Gm[i] * vb[3 * i + 0] * inv;
+            y = Gm[i] * vb[3 * i + 1] * inv;
+            z = Gm[i] * vb[3 * i + 2] * inv;
+        }
         return status[i] != ST_INACTIVE;
     };
     const Sum3 s = ordered_sum3(npl, true, exact != 0, term, -1.0, sh);
