@@ -29,6 +29,7 @@ static const double SIXTH = 0.166666666666666666666666666666666666667;
 #define ST_ACTIVE 0
 #define ST_INACTIVE 1
 #define ST_DISCARDED_DRIFTERR (-7)
+#define ST_COLLIDED (-14)
 /* sqrt(tiny(1.0_DP)) */
 #define VSMALL 1.4916681462400413e-154
 
@@ -1404,13 +1405,15 @@ static void symba_reset(orc_system *s) {
         s->nplenc[i] = s->ntpenc[i] = 0;
         s->levelg[i] = s->levelm[i] = -1;
         s->lencounter[i] = 0;
-        s->lmask[i] = 1;
+        /* the reference sets lmask = .true. because merged bodies have left its arrays;
+         * here they stay in place with status INACTIVE */
+        s->lmask[i] = s->status[i] != ST_INACTIVE;
     }
     symba_set_renc(s, 0);
     for (int32_t i = 0; i < s->ntp; i++) {
         s->tnplenc[i] = 0;
         s->tlevelg[i] = s->tlevelm[i] = -1;
-        s->tlmask[i] = 1;
+        s->tlmask[i] = s->tstatus[i] != ST_INACTIVE;
     }
     s->lfirst_tp = s->lfirstkick;
     s->lfirst_pl = s->lfirstkick;
@@ -1692,6 +1695,182 @@ static void symba_kick_list_pltp(orc_system *s, double dt, int irec, int sgn) {
 }
 
 /* symba_step_set_recur_levels_system (symba_step.f90:118-160) */
+/* swiftest_orbel_xv2aeq (src/swiftest/swiftest_orbel.f90:700-764) */
+static void xv2aeq(double mu, double rx, double ry, double rz, double vx, double vy, double vz, double *a,
+                   double *e, double *q) {
+    const double TINYV = 4.0e-15; /* swiftest_orbel.f90:11 */
+    *a = 0.0;
+    *e = 0.0;
+    *q = 0.0;
+    double r = sqrt(rx * rx + ry * ry + rz * rz);
+    double v2 = vx * vx + vy * vy + vz * vz;
+    double hx = ry * vz - rz * vy, hy = rz * vx - rx * vz, hz = rx * vy - ry * vx;
+    double h2 = hx * hx + hy * hy + hz * hz;
+    if (h2 < 2.2250738585072014e-308) return; /* tiny(1.0_DP) */
+    double energy = 0.5 * v2 - mu / r;
+    int type; /* -1 ellipse, 0 parabola, 1 hyperbola */
+    double fac = 0.0;
+    if (fabs(energy * r / mu) < sqrt(TINYV)) {
+        type = 0;
+    } else {
+        *a = -0.5 * mu / energy;
+        if (*a < 0.0) {
+            fac = -h2 / (mu * *a);
+            type = fac > TINYV ? 1 : 0;
+        } else {
+            type = -1;
+        }
+    }
+    if (type == -1) {
+        fac = 1.0 - h2 / (mu * *a);
+        if (fac > TINYV) *e = sqrt(fac);
+        *q = *a * (1.0 - *e);
+    } else if (type == 0) {
+        *a = 0.5 * h2 / mu;
+        *e = 1.0;
+        *q = *a;
+    } else {
+        *e = sqrt(1.0 + fac);
+        *q = *a * (1.0 - *e);
+    }
+}
+
+/* collision_check_one (src/collision/collision_check.f90:16-57) */
+static int collision_check_one(double xr, double yr, double zr, double vxr, double vyr, double vzr, double Gmtot,
+                               double rlim, double dt, int lvdotr) {
+    double r2 = xr * xr + yr * yr + zr * zr;
+    double rlim2 = rlim * rlim;
+    if (r2 <= rlim2) return 1;
+    double vdotr = xr * vxr + yr * vyr + zr * vzr;
+    if (lvdotr && vdotr > 0.0) {
+        double tcr2 = r2 / (vxr * vxr + vyr * vyr + vzr * vzr);
+        double dt2 = dt * dt;
+        if (tcr2 <= dt2) {
+            double a, e, q;
+            xv2aeq(Gmtot, xr, yr, zr, vxr, vyr, vzr, &a, &e, &q);
+            return q < rlim;
+        }
+    }
+    return 0;
+}
+
+/* collision_check_plpl / _pltp (src/collision/collision_check.f90:60-271): ACTIVE pairs
+ * whose pl (pl-pl: index1) or tp (pl-tp: index2) is at level >= irec; a colliding pair's
+ * status becomes COLLIDED.  Returns whether any pair collided. */
+static int symba_collision_check(orc_system *s, int irec, double dt) {
+    int any = 0;
+    for (int64_t k = 0; k < s->plpl.n; k++) {
+        if (s->plpl.status[k] != ST_ACTIVE) continue;
+        int32_t i = s->plpl.i1[k] - 1, j = s->plpl.i2[k] - 1;
+        if (s->levelg[i] < irec) continue;
+        double x[3], v[3];
+        for (int d = 0; d < 3; d++) {
+            x[d] = s->rh[3 * i + d] - s->rh[3 * j + d];
+            v[d] = s->vb[3 * i + d] - s->vb[3 * j + d];
+        }
+        if (collision_check_one(x[0], x[1], x[2], v[0], v[1], v[2], s->Gmass[i] + s->Gmass[j],
+                                s->radius[i] + s->radius[j], dt, s->plpl.lvdotr[k] != 0)) {
+            s->plpl.status[k] = ST_COLLIDED;
+            any = 1;
+        }
+    }
+    for (int64_t k = 0; k < s->pltp.n; k++) {
+        if (s->pltp.status[k] != ST_ACTIVE) continue;
+        int32_t i = s->pltp.i1[k] - 1, j = s->pltp.i2[k] - 1;
+        if (s->tlevelg[j] < irec) continue;
+        double x[3], v[3];
+        for (int d = 0; d < 3; d++) {
+            x[d] = s->rh[3 * i + d] - s->trh[3 * j + d];
+            v[d] = s->vb[3 * i + d] - s->tvb[3 * j + d];
+        }
+        if (collision_check_one(x[0], x[1], x[2], v[0], v[1], v[2], s->Gmass[i], s->radius[i], dt,
+                                s->pltp.lvdotr[k] != 0)) {
+            s->pltp.status[k] = ST_COLLIDED;
+            any = 1;
+        }
+    }
+    return any;
+}
+
+/* Resolution of the COLLIDED pairs by perfect merging (collision_resolve_plpl / _pltp,
+ * collision_resolve.f90:521-695, with collision_generate_merge, collision_generate.f90:158-260):
+ * a pl-tp collision discards the tp; a pl-pl pair becomes one body in the slot of the more
+ * massive one, with the summed G*m, the radius of the summed volume, the centre-of-mass
+ * position and velocity, and the Hill radius of its new orbit (swiftest_util_set_rhill,
+ * swiftest_util.f90:2260-2280).  Removed bodies stay in their slots with status INACTIVE,
+ * zero G*m, radius, Hill radius and velocity, parked at a distant position of their own
+ * (the reference removes them from its arrays); list entries naming a removed body are
+ * redirected to the merged body and self-pairs made INACTIVE.  Not restated: the torque
+ * that removes the residual angular momentum, the collision energy bookkeeping, cascades
+ * and the re-sort by mass. */
+static void park(double *r, double *v, int64_t k) {
+    r[0] = 1.0e6 + (double)k;
+    r[1] = r[2] = 0.0;
+    v[0] = v[1] = v[2] = 0.0;
+}
+static void symba_resolve_collisions(orc_system *s) {
+    for (int64_t k = 0; k < s->pltp.n; k++) {
+        if (s->pltp.status[k] != ST_COLLIDED) continue;
+        int32_t j = s->pltp.i2[k] - 1;
+        if (s->tstatus[j] == ST_INACTIVE) continue;
+        s->tstatus[j] = ST_INACTIVE;
+        s->tlmask[j] = 0;
+        park(&s->trh[3 * j], &s->tvb[3 * j], (int64_t)s->npl + j);
+        s->stats[4]++;
+    }
+    int have_cbvb = 0;
+    double cbvb[3] = {0.0, 0.0, 0.0};
+    for (int64_t k = 0; k < s->plpl.n; k++) {
+        if (s->plpl.status[k] != ST_COLLIDED) continue;
+        int32_t i = s->plpl.i1[k] - 1, j = s->plpl.i2[k] - 1;
+        if (i == j || s->status[i] == ST_INACTIVE || s->status[j] == ST_INACTIVE) continue;
+        if (!have_cbvb) { /* swiftest_util_coord_vb2vh_pl's sum, before the merges */
+            for (int32_t b = s->npl - 1; b >= 0; b--) {
+                if (s->status[b] == ST_INACTIVE) continue;
+                for (int d = 0; d < 3; d++) cbvb[d] = cbvb[d] - s->Gmass[b] * s->vb[3 * b + d] / s->GMcb;
+            }
+            have_cbvb = 1;
+        }
+        int32_t keep = s->Gmass[j] > s->Gmass[i] ? j : i, gone = keep == i ? j : i;
+        double Gi = s->Gmass[i], Gj = s->Gmass[j], Gtot = Gi + Gj;
+        double rnew[3], vnew[3], vh[3];
+        for (int d = 0; d < 3; d++) {
+            rnew[d] = (Gi * s->rh[3 * i + d] + Gj * s->rh[3 * j + d]) / Gtot;
+            vnew[d] = (Gi * s->vb[3 * i + d] + Gj * s->vb[3 * j + d]) / Gtot;
+            vh[d] = vnew[d] - cbvb[d];
+        }
+        double PI = 3.141592653589793238462643383279502884197;
+        double volume = 4.0 / 3.0 * PI *
+                        (s->radius[i] * s->radius[i] * s->radius[i] + s->radius[j] * s->radius[j] * s->radius[j]);
+        double Rnew = pow(3.0 * volume / (4.0 * PI), THIRD);
+        double a, e, q;
+        xv2aeq(s->GMcb + Gtot, rnew[0], rnew[1], rnew[2], vh[0], vh[1], vh[2], &a, &e, &q);
+        double scale = pow(Gtot / s->GMcb / 3.0, THIRD);
+        double rhill = a > 0.0 ? a * scale : sqrt(rnew[0] * rnew[0] + rnew[1] * rnew[1] + rnew[2] * rnew[2]) * scale;
+        for (int d = 0; d < 3; d++) {
+            s->rh[3 * keep + d] = rnew[d];
+            s->vb[3 * keep + d] = vnew[d];
+        }
+        s->Gmass[keep] = Gtot;
+        s->radius[keep] = Rnew;
+        s->rhill[keep] = rhill;
+        s->Gmass[gone] = 0.0;
+        s->radius[gone] = 0.0;
+        s->rhill[gone] = 0.0;
+        s->status[gone] = ST_INACTIVE;
+        s->lmask[gone] = 0;
+        park(&s->rh[3 * gone], &s->vb[3 * gone], gone);
+        for (int64_t m = 0; m < s->plpl.n; m++) {
+            if (s->plpl.i1[m] == gone + 1) s->plpl.i1[m] = keep + 1;
+            if (s->plpl.i2[m] == gone + 1) s->plpl.i2[m] = keep + 1;
+            if (s->plpl.i1[m] == s->plpl.i2[m]) s->plpl.status[m] = ST_INACTIVE;
+        }
+        for (int64_t m = 0; m < s->pltp.n; m++)
+            if (s->pltp.i1[m] == gone + 1) s->pltp.i1[m] = keep + 1;
+        s->stats[4]++;
+    }
+}
+
 static void symba_set_recur_levels(orc_system *s, int ireci) {
     int irecp = ireci + 1;
     for (int32_t i = 0; i < s->npl; i++)
@@ -1738,6 +1917,7 @@ static int symba_recur(orc_system *s, int ireci) {
             symba_kick_list_plpl(s, dth, irecp, -1);
             symba_kick_list_pltp(s, dth, irecp, -1);
         }
+        if (s->lclose && symba_collision_check(s, ireci, dtl)) symba_resolve_collisions(s);
         symba_set_recur_levels(s, ireci);
     }
     return 0;

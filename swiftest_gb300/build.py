@@ -2,8 +2,10 @@
 
 Each ``csrc/*.cu`` translation unit is compiled in parallel by nvcc for
 ``sm_103a`` only, with ``-fmad=false`` so FP64 expressions keep the reference's
-rounding (kernels that want fused multiply-adds call ``fmaf`` explicitly), and
-the objects are linked into one shared library exporting the C ABI declared in
+rounding (kernels that want fused multiply-adds call ``fmaf`` explicitly) and the
+host compiler's ``-ffp-contract=off`` for the same reason on the host side (the
+collision resolution runs there, and aarch64 hosts have FMA), and the objects are
+linked into one shared library exporting the C ABI declared in
 ``include/swiftest_gb300.h``.
 """
 from __future__ import annotations
@@ -22,7 +24,7 @@ LIB = PKG / "libswiftest_gb300.so"
 BUILD = ROOT / "_build" / "swiftest_gb300"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2",
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
 

@@ -39,6 +39,14 @@ using namespace swg::sdev;
 
 static_assert(KICK_MIXED_TILE == 128 && KICK_FP64_TILE == 8 && ENC_TILE == 128, "tile sizes of the batched kernels");
 
+// Arguments of the ensemble recursion kernel: the shared base plus per-system tables.
+struct EnsRecArgs {
+    RecArgs base;  // global arrays, list pools and scratch bases
+    const int32_t *seg_pp, *seg_pt, *npl, *ntp;
+    const double *GMcb;
+    int32_t *resume, *pend;  // REC_STATE ints and one pause flag per system
+};
+
 struct swg_ensemble {
     swg_ctx *c = nullptr;
     int integrator = SWG_SYMBA;
@@ -83,9 +91,12 @@ struct swg_ensemble {
     int64_t pp_n = 0, pt_n = 0, pp_cap = 0, pt_cap = 0;
     EncWork enc_pp, enc_pt;
     int32_t *rec_out = nullptr;  // [0] status, [1] deepest level, [2] sub-steps
+    int32_t *rec_resume = nullptr, *rec_pend = nullptr;  // per system: paused recursion stack, pause flag
     DevBuf rec_scratch, rows;
     double *eout = nullptr;      // 9 per system
     int32_t *h_flags = nullptr;  // pinned: [2] recursion status; +8: two unsigned long long counts
+    std::vector<int32_t> h_pend;  // per-system pause flags read after a recursion launch
+    EnsRecArgs rec_args;          // arguments of the step's recursion launch (reused to resume)
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
     StepProfile prof;
     // side stream for the closing kick of systems without encounters (overlaps the recursion)
@@ -291,16 +302,12 @@ __global__ void k_ens_lany(int nsys, const int32_t *__restrict__ seg_pp, const i
 
 // The SyMBA recursion of every system with encounters this step, one block each
 // (blk_symba_recursion on the system's list segments; body arrays are global).
-struct EnsRecArgs {
-    RecArgs base;  // global arrays, list pools and scratch bases
-    const int32_t *seg_pp, *seg_pt, *npl, *ntp;
-    const double *GMcb;
-};
-__global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e) {
+__global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e, int resume_only) {
     const int s = blockIdx.x;
     const int64_t k0 = e.seg_pp[2 * s], npp = e.seg_pp[2 * s + 1];
     const int64_t t0 = e.seg_pt[2 * s], npt = e.seg_pt[2 * s + 1];
     if (npp + npt == 0) return;
+    if (resume_only && e.resume[(size_t)REC_STATE * s] == 0) return;  // finished before the pause
     RecArgs a = e.base;
     a.npl = e.npl[s];
     a.ntp = e.ntp[s];
@@ -315,6 +322,8 @@ __global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e) {
     a.good = e.base.good + q;
     a.bpl = e.base.bpl + 2 * k0 + t0;
     a.btp = e.base.btp + t0;
+    a.resume = e.resume + (size_t)REC_STATE * s;
+    a.pend = e.pend + s;
     blk_symba_recursion(a);
 }
 
@@ -625,7 +634,95 @@ int symba_level0(swg_ensemble *e, double dt) {
     return SWG_OK;
 }
 
-int symba_recursion(swg_ensemble *e, double dt) {
+// Collisions found by system s's paused recursion: host copies of the system's slices and
+// list segments (indices made local), perfect merging, and the modified arrays written back.
+int resolve_collisions(swg_ensemble *e, int s) {
+    swg_ctx *c = e->c;
+    const int32_t p0 = e->h_poff[s], npl = e->h_npl[s], t0 = e->h_toff[s], ntp = e->h_ntp[s];
+    int32_t seg[4];
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(seg, e->seg_pp + 2 * s, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                           c->stream),
+                        "collision"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(seg + 2, e->seg_pt + 2 * s, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                           c->stream),
+                        "collision"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "collision"));
+    const int64_t npp = seg[1], npt = seg[3];
+    const size_t n = std::max(npl, 1), m = std::max(ntp, 1);
+    std::vector<double> rh(3 * n), vb(3 * n), Gm(n), R(n), rhill(n), trh(3 * m), tvb(3 * m);
+    std::vector<int32_t> st(n), lm(n), tst(m), tlm(m);
+    std::vector<int32_t> pp(3 * std::max<int64_t>(npp, 1)), pt(3 * std::max<int64_t>(npt, 1));
+    struct Copy {
+        void *h;
+        void *d;
+        size_t bytes;
+    };
+    const size_t P = p0, T = t0;
+    std::vector<Copy> xs = {{rh.data(), e->rh + 3 * P, 24 * (size_t)npl},    {vb.data(), e->vb + 3 * P, 24 * (size_t)npl},
+                            {Gm.data(), e->Gmass + P, 8 * (size_t)npl},      {R.data(), e->radius + P, 8 * (size_t)npl},
+                            {rhill.data(), e->rhill + P, 8 * (size_t)npl},   {st.data(), e->status + P, 4 * (size_t)npl},
+                            {lm.data(), e->lmask + P, 4 * (size_t)npl},      {trh.data(), e->trh + 3 * T, 24 * (size_t)ntp},
+                            {tvb.data(), e->tvb + 3 * T, 24 * (size_t)ntp},  {tst.data(), e->tstatus + T, 4 * (size_t)ntp},
+                            {tlm.data(), e->tlmask + T, 4 * (size_t)ntp}};
+    for (int f = 0; f < 3; f++) {  // i1, i2, status of each list segment
+        const int field = f == 2 ? 3 : f;
+        if (npp) xs.push_back({pp.data() + f * npp, e->pp_l + field * e->pp_cap + seg[0], 4 * (size_t)npp});
+        if (npt) xs.push_back({pt.data() + f * npt, e->pt_l + field * e->pt_cap + seg[2], 4 * (size_t)npt});
+    }
+    for (const Copy &x : xs)
+        if (x.bytes)
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.h, x.d, x.bytes, cudaMemcpyDeviceToHost, c->stream), "collision"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "collision"));
+    // global 1-based indices -> local
+    for (int64_t k = 0; k < npp; k++) {
+        pp[k] -= p0;
+        pp[npp + k] -= p0;
+    }
+    for (int64_t k = 0; k < npt; k++) {
+        pt[k] -= p0;
+        pt[npt + k] -= t0;
+    }
+    CollisionSystem cs;
+    cs.npl = npl;
+    cs.ntp = ntp;
+    cs.GMcb = e->h_GMcb[s];
+    cs.rh = rh.data();
+    cs.vb = vb.data();
+    cs.Gm = Gm.data();
+    cs.R = R.data();
+    cs.rhill = rhill.data();
+    cs.status = st.data();
+    cs.lmask = lm.data();
+    cs.trh = trh.data();
+    cs.tvb = tvb.data();
+    cs.tstatus = tst.data();
+    cs.tlmask = tlm.data();
+    cs.npp = npp;
+    cs.npt = npt;
+    cs.pp_i1 = pp.data();
+    cs.pp_i2 = pp.data() + npp;
+    cs.pp_st = pp.data() + 2 * npp;
+    cs.pt_i1 = pt.data();
+    cs.pt_i2 = pt.data() + npt;
+    cs.pt_st = pt.data() + 2 * npt;
+    e->stats[4] += resolve_collisions_host(cs);
+    for (int64_t k = 0; k < npp; k++) {
+        pp[k] += p0;
+        pp[npp + k] += p0;
+    }
+    for (int64_t k = 0; k < npt; k++) {
+        pt[k] += p0;
+        pt[npt + k] += t0;
+    }
+    for (const Copy &x : xs)
+        if (x.bytes)
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.d, x.h, x.bytes, cudaMemcpyHostToDevice, c->stream), "collision"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "collision");
+}
+
+// Launch the SyMBA recursion of every system with encounters (one block each).  Paused
+// systems are resumed by recursion_finish.
+int recursion_launch(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     const int64_t n = e->pp_n + e->pt_n;
     SWG_TRY(ensure(c, e->rec_scratch, sizeof(double) * (size_t)(6 * n + 8) + (size_t)(2 * n + 64) +
@@ -667,19 +764,48 @@ int symba_recursion(swg_ensemble *e, double dt) {
     a.mark_pl = e->mark_pl;
     a.mark_tp = e->mark_tp;
     a.out = e->rec_out;
+    a.lclose = e->lclose;
     x.seg_pp = e->seg_pp;
     x.seg_pt = e->seg_pt;
     x.npl = e->npl;
     x.ntp = e->ntp;
     x.GMcb = e->GMcb;
-    ProfScope ps(e->prof, c->stream, PROF_RECUR);
+    x.resume = e->rec_resume;
+    x.pend = e->rec_pend;
+    e->rec_args = x;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_out, 0, sizeof(int32_t), c->stream), "memset"));
-    k_ens_symba_recursion<<<e->nsys, RECT, 0, c->stream>>>(x);
-    SWG_TRY(L(c, "ens_symba_recursion"));
+    if (e->lclose)
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_pend, 0, sizeof(int32_t) * e->nsys, c->stream), "memset"));
+    k_ens_symba_recursion<<<e->nsys, RECT, 0, c->stream>>>(x, 0);
+    return L(c, "ens_symba_recursion");
+}
+
+// With collision checks on (lclose), wait for the recursion, resolve the collisions of the
+// systems whose recursion paused on the host and resume those systems, until none pauses.
+int recursion_finish(swg_ensemble *e) {
+    swg_ctx *c = e->c;
+    while (e->lclose) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->h_pend.data(), e->rec_pend, sizeof(int32_t) * e->nsys,
+                                               cudaMemcpyDeviceToHost, c->stream),
+                            "pending"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "recursion"));
+        bool any = false;
+        for (int s = 0; s < e->nsys; s++)
+            if (e->h_pend[s]) {
+                any = true;
+                SWG_TRY(resolve_collisions(e, s));
+            }
+        if (!any) break;
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_pend, 0, sizeof(int32_t) * e->nsys, c->stream), "memset"));
+        k_ens_symba_recursion<<<e->nsys, RECT, 0, c->stream>>>(e->rec_args, 1);
+        SWG_TRY(L(c, "ens_symba_recursion"));
+    }
     return cuda_status(c, cudaMemcpyAsync(e->h_flags + 2, e->rec_out, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                           c->stream),
                        "recursion status");
 }
+
+
 
 // One step of every system: symba_step_system (symba_step.f90:14-52) or
 // helio_step_system (helio_step.f90:14-119).  A SyMBA system without encounters takes
@@ -695,7 +821,8 @@ int ens_step(swg_ensemble *e, double dt) {
         const int64_t nmax = std::max(e->NPL, e->NTP);
         k_symba_reset<<<grid_for(nmax, 256), 256, 0, c->stream>>>((int)e->NPL, (int)e->NTP, e->levelg, e->levelm,
                                                                    e->nplenc, e->ntpenc, e->lmask, e->tlevelg,
-                                                                   e->tlevelm, e->tnplenc, e->tlmask);
+                                                                   e->tlevelm, e->tnplenc, e->tlmask, e->status,
+                                                                   e->tstatus);
         SWG_TRY(L(c, "symba_reset"));
         ProfScope ps(e->prof, c->stream, PROF_ENC0);
         SWG_TRY(symba_level0(e, dt));
@@ -715,14 +842,19 @@ int ens_step(swg_ensemble *e, double dt) {
         swg_ctx *c = e->c;
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
-        SWG_TRY(symba_recursion(e, dt));
+        SWG_TRY(recursion_launch(e, dt));
         SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
+        SWG_TRY(recursion_finish(e));
         SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
         SWG_TRY(kick_vb_pl(e, dth, 0, true));
     } else {
-        if (rec) SWG_TRY(symba_recursion(e, dt));
+        if (rec) {
+            ProfScope ps(e->prof, c->stream, PROF_RECUR);
+            SWG_TRY(recursion_launch(e, dt));
+            SWG_TRY(recursion_finish(e));
+        }
         SWG_TRY(kick_vb_pl(e, dth, 0));
     }
     SWG_TRY(lindrift_pl(e, dth, CB_PTEND));
@@ -811,6 +943,9 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
+    if (rc == SWG_OK) rc = dalloc(c, &e->rec_resume, (size_t)REC_STATE * S);
+    if (rc == SWG_OK) rc = dalloc(c, &e->rec_pend, S);
+    e->h_pend.assign(S, 0);
     if (rc == SWG_OK) rc = ensure(c, e->rows, sizeof(double) * 4 * n);
     if (rc == SWG_OK) {
         cudaError_t err = cudaMallocHost((void **)&e->h_flags, 64);
@@ -848,7 +983,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->it_mpl, e->it_mtp,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_scratch.ptr, e->rows.ptr, e->eout};
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->rec_scratch.ptr, e->rows.ptr, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);

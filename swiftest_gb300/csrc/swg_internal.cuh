@@ -18,6 +18,7 @@ namespace swg {
 constexpr int ST_ACTIVE = 0;
 constexpr int ST_INACTIVE = 1;
 constexpr int ST_DISCARDED_DRIFTERR = -7;
+constexpr int ST_COLLIDED = -14;
 
 // Reference constants, src/globals/globals_module.f90:33-38.
 constexpr double TWOPI = 6.283185307179586476925286766559005768394;
@@ -217,6 +218,22 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
 int encounter_check_kind(swg_ctx *c, EncWork &w, int kind, int mode, int32_t n1, const double *r1,
                          const double *v1, const double *renc1, int32_t n2, const double *r2, const double *v2,
                          const double *renc2, double dt, int64_t *n_out, int32_t **i1, int32_t **i2, int32_t **lv);
+
+// collision.cu -- host-side resolution of detected collisions (perfect merging) for one
+// system, on host copies of its arrays (local indices; lists hold 1-based local indices).
+// Returns the number of collisions resolved.
+struct CollisionSystem {
+    int32_t npl = 0, ntp = 0;
+    double GMcb = 0.0;
+    double *rh = nullptr, *vb = nullptr, *Gm = nullptr, *R = nullptr, *rhill = nullptr;
+    int32_t *status = nullptr, *lmask = nullptr;
+    double *trh = nullptr, *tvb = nullptr;
+    int32_t *tstatus = nullptr, *tlmask = nullptr;
+    int64_t npp = 0, npt = 0;
+    int32_t *pp_i1 = nullptr, *pp_i2 = nullptr, *pp_st = nullptr;
+    int32_t *pt_i1 = nullptr, *pt_i2 = nullptr, *pt_st = nullptr;
+};
+int64_t resolve_collisions_host(CollisionSystem &c);
 
 // Scalar-broadcast helpers
 __host__ __device__ inline int64_t nplplm_count(int64_t npl, int64_t nplm) {

@@ -383,7 +383,15 @@ struct RecArgs {
     int32_t *bpl, *btp;             // compact sets of bodies that appear in the lists
     int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
     int32_t *out;                   // [0] status, [1] deepest level reached
+    int lclose;                     // check for collisions at every level (param%lclose)
+    int32_t *resume;                // REC_STATE ints: saved recursion stack of a paused step
+    int32_t *pend;                  // set to 1 when the recursion pauses for a collision
 };
+
+// Saved stack of a recursion paused for a collision: [0] 1 when paused, [1] level,
+// [2, 2 + MAXLEV) loop counters, [2 + MAXLEV, 2 + 2 MAXLEV) phases.
+constexpr int MAXLEV = 48;
+constexpr int REC_STATE = 2 + 2 * MAXLEV;
 
 // Item index of this thread in the recursion kernel's block loops: consecutive items go
 // to different warps, hence to different SM sub-partitions.  The few pairs and bodies
@@ -630,7 +638,94 @@ static __device__ void blk_set_recur_levels(const RecArgs &a, int nbpl, int nbtp
     __syncthreads();
 }
 
-constexpr int MAXLEV = 48;
+// swiftest_orbel_xv2aeq (src/swiftest/swiftest_orbel.f90:700-764): semimajor axis,
+// eccentricity and pericentre distance of the relative two-body orbit.
+__device__ __forceinline__ void d_xv2aeq(double mu, double rx, double ry, double rz, double vx, double vy, double vz,
+                                         double &a, double &e, double &q) {
+    const double TINYV = 4.0e-15;  // swiftest_orbel.f90:11
+    a = 0.0;
+    e = 0.0;
+    q = 0.0;
+    const double r = sqrt(rx * rx + ry * ry + rz * rz);
+    const double v2 = vx * vx + vy * vy + vz * vz;
+    const double hx = ry * vz - rz * vy, hy = rz * vx - rx * vz, hz = rx * vy - ry * vx;
+    const double h2 = hx * hx + hy * hy + hz * hz;
+    if (h2 < 2.2250738585072014e-308) return;  // tiny(1.0_DP)
+    const double energy = 0.5 * v2 - mu / r;
+    int type;  // -1 ellipse, 0 parabola, 1 hyperbola
+    double fac = 0.0;
+    if (fabs(energy * r / mu) < sqrt(TINYV)) {
+        type = 0;
+    } else {
+        a = -0.5 * mu / energy;
+        if (a < 0.0) {
+            fac = -h2 / (mu * a);
+            type = fac > TINYV ? 1 : 0;
+        } else {
+            type = -1;
+        }
+    }
+    if (type == -1) {
+        fac = 1.0 - h2 / (mu * a);
+        if (fac > TINYV) e = sqrt(fac);
+        q = a * (1.0 - e);
+    } else if (type == 0) {
+        a = 0.5 * h2 / mu;
+        e = 1.0;
+        q = a;
+    } else {
+        e = sqrt(1.0 + fac);
+        q = a * (1.0 - e);
+    }
+}
+
+// collision_check_one (src/collision/collision_check.f90:16-57)
+__device__ __forceinline__ bool d_collision_one(double xr, double yr, double zr, double vxr, double vyr, double vzr,
+                                                double Gmtot, double rlim, double dt, bool lvdotr) {
+    const double r2 = xr * xr + yr * yr + zr * zr;
+    const double rlim2 = rlim * rlim;
+    if (r2 <= rlim2) return true;
+    const double vdotr = xr * vxr + yr * vyr + zr * vzr;
+    if (lvdotr && vdotr > 0.0) {
+        const double tcr2 = r2 / (vxr * vxr + vyr * vyr + vzr * vzr);
+        const double dt2 = dt * dt;
+        if (tcr2 <= dt2) {
+            double a, e, q;
+            d_xv2aeq(Gmtot, xr, yr, zr, vxr, vyr, vzr, a, e, q);
+            return q < rlim;
+        }
+    }
+    return false;
+}
+
+// collision_check_plpl / _pltp (src/collision/collision_check.f90:60-271) for the pairs of
+// one system at recursion level irec: ACTIVE pairs whose pl (pl-pl: index1) or tp (pl-tp:
+// index2) sits at level >= irec are tested; a colliding pair's status becomes COLLIDED
+// and *s_coll is set.  The host resolves the collisions (merge, tp discard).
+static __device__ void blk_collision_check(const RecArgs &a, int irec, double dt, int *s_coll) {
+    for (int64_t k = spread_tid(); k < a.npp + a.npt; k += blockDim.x) {
+        const bool isp = k < a.npp;
+        const int64_t q = isp ? k : k - a.npp;
+        int32_t *l = isp ? a.pp : a.pt;
+        const int64_t cap = isp ? a.ppcap : a.ptcap;
+        int32_t *st = l + 3 * cap;
+        if (st[q] != ST_ACTIVE) continue;
+        const int i = l[q] - 1, j = l[cap + q] - 1;
+        if ((isp ? a.levelg[i] : a.tlevelg[j]) < irec) continue;
+        const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
+        const double *vj = isp ? &a.vb[3 * j] : &a.tvb[3 * j];
+        const double xr = a.rh[3 * i] - rj[0], yr = a.rh[3 * i + 1] - rj[1], zr = a.rh[3 * i + 2] - rj[2];
+        const double vxr = a.vb[3 * i] - vj[0], vyr = a.vb[3 * i + 1] - vj[1], vzr = a.vb[3 * i + 2] - vj[2];
+        const double Gmtot = isp ? a.Gm[i] + a.Gm[j] : a.Gm[i];
+        const double rlim = isp ? a.radius[i] + a.radius[j] : a.radius[i];
+        if (d_collision_one(xr, yr, zr, vxr, vyr, vzr, Gmtot, rlim, dt, l[2 * cap + q] != 0)) {
+            st[q] = ST_COLLIDED;
+            *s_coll = 1;
+        }
+    }
+    __syncthreads();
+}
+
 constexpr int RECT = 256;  // threads of the recursion kernel
 
 // symba_step_recur_system (symba_step.f90:163-262) for the whole recursion tree of one
@@ -662,12 +757,20 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
     __syncthreads();
     const int nbpl = s_nbpl, nbtp = s_nbtp;
     int ireci = 0;
-    if (threadIdx.x == 0) {
+    const bool resumed = a.resume && a.resume[0] == 1;
+    if (resumed) {  // continue a step paused after a collision check
+        ireci = a.resume[1];
+        for (int k = threadIdx.x; k <= ireci; k += blockDim.x) {
+            s_j[k] = a.resume[2 + k];
+            s_phase[k] = a.resume[2 + MAXLEV + k];
+        }
+    } else if (threadIdx.x == 0) {
         s_j[0] = 1;
         s_phase[0] = 0;
     }
     __syncthreads();
     int deepest = 0, substeps = 0;
+    bool paused = false;
     for (;;) {
         double p3 = 1.0;
         for (int k = 0; k < ireci; k++) p3 *= 3.0;
@@ -675,6 +778,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
         const double dth = 0.5 * dtl;
         const int irecp = ireci + 1;
         const int nloops = ireci == 0 ? 1 : NTENC;
+        if (s_phase[ireci] == 2) goto after_collision;  // resumed: collisions of this loop resolved
         if (s_phase[ireci] == 0) {
             if (s_j[ireci] > nloops) {
                 if (ireci == 0) break;
@@ -713,6 +817,26 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
         }
         // after the deeper levels (or none) for loop j of level ireci
         blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
+        if (a.lclose) {
+            if (threadIdx.x == 0) s_any = 0;
+            __syncthreads();
+            blk_collision_check(a, ireci, dtl, &s_any);
+            if (s_any) {  // pause: the host resolves the collisions, then resumes here
+                if (threadIdx.x == 0) {
+                    s_phase[ireci] = 2;
+                    a.resume[0] = 1;
+                    a.resume[1] = ireci;
+                    for (int k = 0; k <= ireci; k++) {
+                        a.resume[2 + k] = s_j[k];
+                        a.resume[2 + MAXLEV + k] = s_phase[k];
+                    }
+                    *a.pend = 1;
+                }
+                paused = true;
+                break;
+            }
+        }
+    after_collision:
         blk_set_recur_levels(a, nbpl, nbtp, ireci);
         if (threadIdx.x == 0) {
             s_j[ireci]++;
@@ -721,6 +845,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
         __syncthreads();
     }
     __syncthreads();
+    if (!paused && resumed && threadIdx.x == 0) a.resume[0] = 0;
     for (int b = threadIdx.x; b < nbpl; b += blockDim.x) a.mark_pl[a.bpl[b]] = 0;
     for (int b = threadIdx.x; b < nbtp; b += blockDim.x) a.mark_tp[a.btp[b]] = 0;
     if (threadIdx.x == 0) {
@@ -876,23 +1001,26 @@ static __global__ void k_kick_update(int n, double *v, const double *__restrict_
     for (int d = 0; d < 3; d++) v[3 * i + d] = v[3 * i + d] + a[3 * i + d] * dt;
 }
 
-// symba_step_reset_system (symba_step.f90:265-331) + set_renc(0)
+// symba_step_reset_system (symba_step.f90:265-331) + set_renc(0).  The reference sets
+// lmask = .true. because removed bodies have left the arrays; here they stay in place with
+// status INACTIVE, so lmask is status /= INACTIVE.
 static __global__ void k_symba_reset(int npl, int ntp, int32_t *levelg, int32_t *levelm, int32_t *nplenc, int32_t *ntpenc,
                               int32_t *lmask, int32_t *tlevelg, int32_t *tlevelm, int32_t *tnplenc,
-                              int32_t *tlmask) {
+                              int32_t *tlmask, const int32_t *__restrict__ status,
+                              const int32_t *__restrict__ tstatus) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < npl) {
         levelg[i] = -1;
         levelm[i] = -1;
         nplenc[i] = 0;
         ntpenc[i] = 0;
-        lmask[i] = 1;
+        lmask[i] = status[i] != ST_INACTIVE;  // bodies removed by a collision stay masked
     }
     if (i < ntp) {
         tlevelg[i] = -1;
         tlevelm[i] = -1;
         tnplenc[i] = 0;
-        tlmask[i] = 1;
+        tlmask[i] = tstatus[i] != ST_INACTIVE;
     }
 }
 

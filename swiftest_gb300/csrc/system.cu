@@ -52,8 +52,9 @@ struct swg_system {
     EncWork enc, enc2;
     // scratch
     DevBuf kick_scratch, pair_scratch, flags, red;
-    int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail, [2] recursion status, [3] deepest level
-    int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr;
+    int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail, [2] recursion status, [3] deepest level,
+                                 // [4] collision pending
+    int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr, *rec_resume = nullptr;
     DevBuf rec_scratch;
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
     StepProfile prof;  // optional CUDA-event profile per kernel class (PROF_*)
@@ -643,6 +644,69 @@ int symba_level0(swg_system *s, double dt, int *lany) {
     return SWG_OK;
 }
 
+// Collisions found by a paused recursion: host copies of the system, perfect merging
+// (resolve_collisions_host), and the modified arrays written back.
+int resolve_collisions(swg_system *s) {
+    swg_ctx *c = s->c;
+    const size_t n = std::max(s->npl, 1), m = std::max(s->ntp, 1);
+    std::vector<double> rh(3 * n), vb(3 * n), Gm(n), R(n), rhill(n), trh(3 * m), tvb(3 * m);
+    std::vector<int32_t> st(n), lm(n), tst(m), tlm(m);
+    const int64_t npp = s->plpl_n, npt = s->pltp_n;
+    std::vector<int32_t> pp(3 * std::max<int64_t>(npp, 1)), pt(3 * std::max<int64_t>(npt, 1));
+    struct Copy {
+        void *h;
+        void *d;
+        size_t bytes;
+    };
+    std::vector<Copy> pl_arrays = {{rh.data(), s->rh, 24 * (size_t)s->npl},   {vb.data(), s->vb, 24 * (size_t)s->npl},
+                                   {Gm.data(), s->Gmass, 8 * (size_t)s->npl}, {R.data(), s->radius, 8 * (size_t)s->npl},
+                                   {rhill.data(), s->rhill, 8 * (size_t)s->npl},
+                                   {st.data(), s->status, 4 * (size_t)s->npl}, {lm.data(), s->lmask, 4 * (size_t)s->npl},
+                                   {trh.data(), s->trh, 24 * (size_t)s->ntp}, {tvb.data(), s->tvb, 24 * (size_t)s->ntp},
+                                   {tst.data(), s->tstatus, 4 * (size_t)s->ntp},
+                                   {tlm.data(), s->tlmask, 4 * (size_t)s->ntp}};
+    std::vector<Copy> lists;
+    for (int f = 0; f < 3; f++) {  // i1, i2, status of each list
+        const int field = f == 2 ? 3 : f;
+        if (npp) lists.push_back({pp.data() + f * npp, s->plpl_l + field * s->plpl_cap, 4 * (size_t)npp});
+        if (npt) lists.push_back({pt.data() + f * npt, s->pltp_l + field * s->pltp_cap, 4 * (size_t)npt});
+    }
+    for (auto *v : {&pl_arrays, &lists})
+        for (const Copy &x : *v)
+            if (x.bytes)
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.h, x.d, x.bytes, cudaMemcpyDeviceToHost, c->stream), "collision"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "collision"));
+    CollisionSystem cs;
+    cs.npl = s->npl;
+    cs.ntp = s->ntp;
+    cs.GMcb = s->GMcb;
+    cs.rh = rh.data();
+    cs.vb = vb.data();
+    cs.Gm = Gm.data();
+    cs.R = R.data();
+    cs.rhill = rhill.data();
+    cs.status = st.data();
+    cs.lmask = lm.data();
+    cs.trh = trh.data();
+    cs.tvb = tvb.data();
+    cs.tstatus = tst.data();
+    cs.tlmask = tlm.data();
+    cs.npp = npp;
+    cs.npt = npt;
+    cs.pp_i1 = pp.data();
+    cs.pp_i2 = pp.data() + npp;
+    cs.pp_st = pp.data() + 2 * npp;
+    cs.pt_i1 = pt.data();
+    cs.pt_i2 = pt.data() + npt;
+    cs.pt_st = pt.data() + 2 * npt;
+    s->stats[4] += resolve_collisions_host(cs);
+    for (auto *v : {&pl_arrays, &lists})
+        for (const Copy &x : *v)
+            if (x.bytes)
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.d, x.h, x.bytes, cudaMemcpyHostToDevice, c->stream), "collision"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "collision");
+}
+
 // Launch the whole SyMBA recursion of one step (symba_step_recur_system from level 0)
 // as one single-block kernel; no host round trip until the next step's checks.
 int symba_recursion(swg_system *s, double dt) {
@@ -687,9 +751,24 @@ int symba_recursion(swg_system *s, double dt) {
     a.mark_pl = s->mark_pl;
     a.mark_tp = s->mark_tp;
     a.out = s->rec_out;
+    a.lclose = s->lclose;
+    a.resume = s->rec_resume;
+    a.pend = s->rec_out + 3;
     ProfScope ps(s->prof, s->c->stream, PROF_RECUR);
-    k_symba_recursion<<<1, RECT, 0, c->stream>>>(a);
-    SWG_TRY(L(c, "symba_recursion"));
+    for (;;) {
+        if (s->lclose)
+            SWG_TRY(cuda_status(c, cudaMemsetAsync(a.pend, 0, sizeof(int32_t), c->stream), "memset"));
+        k_symba_recursion<<<1, RECT, 0, c->stream>>>(a);
+        SWG_TRY(L(c, "symba_recursion"));
+        if (!s->lclose) break;
+        // a collision pauses the recursion: resolve it on the host, then resume
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->h_flags + 4, a.pend, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                               c->stream),
+                            "pending"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "recursion"));
+        if (s->h_flags[4] == 0) break;
+        SWG_TRY(resolve_collisions(s));
+    }
     // status word read back at the next host synchronization
     return cuda_status(c, cudaMemcpyAsync(s->h_flags + 2, s->rec_out, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                           c->stream),
@@ -727,7 +806,7 @@ int symba_step(swg_system *s, double dt) {
     const int nmax = std::max(s->npl, s->ntp);
     k_symba_reset<<<grid_for(nmax, 256), 256, 0, c->stream>>>(s->npl, s->ntp, s->levelg, s->levelm, s->nplenc,
                                                                s->ntpenc, s->lmask, s->tlevelg, s->tlevelm,
-                                                               s->tnplenc, s->tlmask);
+                                                               s->tnplenc, s->tlmask, s->status, s->tstatus);
     SWG_TRY(L(c, "symba_reset"));
     s->lfirst_tp = s->lfirstkick;
     s->lfirst_pl = s->lfirstkick;
@@ -782,6 +861,7 @@ int swg_system_create(swg_ctx *c, int integrator, int32_t npl, int32_t ntp, swg_
     if (rc == SWG_OK) rc = dalloc(c, &s->mark_pl, n);
     if (rc == SWG_OK) rc = dalloc(c, &s->mark_tp, m);
     if (rc == SWG_OK) rc = dalloc(c, &s->rec_out, 4);
+    if (rc == SWG_OK) rc = dalloc(c, &s->rec_resume, REC_STATE);
     if (rc == SWG_OK) rc = ensure(c, s->flags, 64);
     if (rc == SWG_OK) rc = ensure(c, s->red, sizeof(double) * (4 * n + 64));
     if (rc == SWG_OK) {
@@ -809,7 +889,7 @@ int swg_system_destroy(swg_system *s) {
                     s->ntpenc, s->iflag, s->trh, s->tvh, s->tvb, s->tah, s->tstatus, s->tlmask, s->tlevelg,
                     s->tlevelm, s->tnplenc, s->tiflag, s->dcb, s->plpl_l, s->pltp_l, s->enc.raw.ptr,
                     s->enc.sort.ptr, s->enc.counters.ptr, s->enc2.raw.ptr, s->enc2.sort.ptr, s->enc2.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
-                    s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_scratch.ptr};
+                    s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_resume, s->rec_scratch.ptr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);

@@ -211,3 +211,25 @@ def test_solar_system_conservation_slopes(integ):
     # reference thresholds: |d(dE/E)/dt| < 1e-8 /yr, |d(dL/L)/dt| < 1e-10 /yr
     assert abs(np.polyfit(ts, dE, 1)[0]) < 1e-8
     assert abs(np.polyfit(ts, dL, 1)[0]) < 1e-10
+
+
+def test_oracle_collisions_merge_conserves_mass():
+    # inflated radii: pl-pl merges and pl-tp discards within a short run
+    cb, pl, tp = IC.make_system(seed=7, npl=150, ntp=300, amin=0.8, amax=1.2, mmin=1e-9, mmax=1e-6)
+    pl = IC.sort_for_integrator(pl, "SYMBA")
+    pl["radius"] = pl["radius"] * 300.0
+    ref = O.OracleSystem("SYMBA", cb, pl, tp, dt=0.005, rhscale=3.0)
+    e0 = ref.energy()
+    ref.step(100)
+    st = ref.stats()
+    rh, vh, s = ref.get_pl()
+    trh, tvh, ts = ref.get_tp()
+    assert st["collisions"] > 0
+    e1 = ref.energy()
+    assert abs(e1["GMtot"] - e0["GMtot"]) <= 1e-13 * e0["GMtot"]
+    gone = s == 1
+    assert gone.any() and np.all(np.abs(vh[gone]).max(axis=1) < 1e3)
+    # without collision checks (lclose off) nothing merges
+    ref2 = O.OracleSystem("SYMBA", cb, pl, tp, dt=0.005, rhscale=3.0, lclose=False)
+    ref2.step(100)
+    assert ref2.stats()["collisions"] == 0
