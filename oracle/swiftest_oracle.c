@@ -2040,6 +2040,48 @@ int orc_system_initialize(orc_system *s) {
     return 0;
 }
 
+/* swiftest_discard_pl_close (src/swiftest/swiftest_discard.f90:293-336) */
+static int discard_pl_close(const double *dx, const double *dv, double dt, double r2crit) {
+    double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+    if (r2 <= r2crit) return 1;
+    double vdotr = dx[0] * dv[0] + dx[1] * dv[1] + dx[2] * dv[2];
+    if (vdotr > 0.0) return 0;
+    double v2 = dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2];
+    double tmin = -vdotr / v2;
+    double r2min;
+    if (tmin < dt)
+        r2min = r2 - vdotr * vdotr / v2;
+    else
+        r2min = r2 + 2.0 * vdotr * dt + v2 * (dt * dt);
+    r2min = r2min < r2 ? r2min : r2;
+    return r2min <= r2crit;
+}
+
+/* swiftest_discard_pl_tp (src/swiftest/swiftest_discard.f90:244-290), the driver's discard
+ * step after each step when param%lclose: an ACTIVE tp that comes within a pl's radius
+ * leaves the system (the reference spills it out of its arrays; here it stays in its slot
+ * with status INACTIVE, masked, parked with no velocity at 1e6 AU + (npl + its index)). */
+static void discard_pl_tp(orc_system *s) {
+    for (int32_t i = 0; i < s->ntp; i++) {
+        if (s->tstatus[i] != ST_ACTIVE) continue;
+        for (int32_t j = 0; j < s->npl; j++) {
+            double dx[3], dv[3];
+            for (int d = 0; d < 3; d++) {
+                dx[d] = s->trh[3 * i + d] - s->rh[3 * j + d];
+                dv[d] = s->tvh[3 * i + d] - s->vh[3 * j + d];
+            }
+            if (!discard_pl_close(dx, dv, s->dt, s->radius[j] * s->radius[j])) continue;
+            s->tstatus[i] = ST_INACTIVE;
+            s->tlmask[i] = 0;
+            s->trh[3 * i] = 1.0e6 + (double)((int64_t)s->npl + i);
+            s->trh[3 * i + 1] = s->trh[3 * i + 2] = 0.0;
+            for (int d = 0; d < 3; d++) s->tvh[3 * i + d] = s->tvb[3 * i + d] = 0.0;
+            s->stats[4]++;
+            break;
+        }
+    }
+}
+
 int orc_system_step(orc_system *s, int32_t nsteps) {
     for (int32_t n = 0; n < nsteps; n++) {
         int rc = 0;
@@ -2050,6 +2092,7 @@ int orc_system_step(orc_system *s, int32_t nsteps) {
         } else
             rc = symba_step(s, s->dt);
         if (rc) return rc;
+        if (s->lclose && s->npl > 0 && s->ntp > 0) discard_pl_tp(s);
         s->t += s->dt;
     }
     return 0;

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "encounter_dev.cuh"
 #include "swg_internal.cuh"
 
@@ -41,20 +43,45 @@ __global__ void k_encounter_prep(int n, const double *__restrict__ r, const doub
 
 constexpr int EP = 64;  // partners per shared-memory tile
 
+// swiftest_discard_pl_close (src/swiftest/swiftest_discard.f90:293-336): does the relative
+// linear motion (dx, dv) come within sqrt(r2crit) during the step dt?
+__device__ __forceinline__ bool d_discard_close(double dx, double dy, double dz, double dvx, double dvy, double dvz,
+                                                double dt, double r2crit) {
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 <= r2crit) return true;
+    const double vdotr = dx * dvx + dy * dvy + dz * dvz;
+    if (vdotr > 0.0) return false;
+    const double v2 = dvx * dvx + dvy * dvy + dvz * dvz;
+    const double tmin = -vdotr / v2;
+    double r2min;
+    if (tmin < dt)
+        r2min = r2 - vdotr * vdotr / v2;
+    else
+        r2min = r2 + 2.0 * vdotr * dt + v2 * (dt * dt);
+    r2min = r2min < r2 ? r2min : r2;
+    return r2min <= r2crit;
+}
+
 // Receivers: list-2 bodies j in [j0, j0 + ET) (one thread each).  Partners: list-1 bodies
 // i in [ibeg, iend) (i < j when `upper`, i.e. pl-pl).  A pair is written as
 // (i + 1 + base1, j + 1 + base2); lists are sorted afterwards, so the tiling is invisible.
+// DISCARD: the close-approach scan of swiftest_discard_pl_tp instead (list 1 = pl with
+// renc1 = their radii, list 2 = the tp with status st2): the FP64 test is
+// swiftest_discard_pl_close with r2crit = radius^2, and a hit sets o2[base2 + j] = 1.  The
+// prefilter bound holds for it too (same closest-approach expression).
 // Whole block; returns at once (block-uniformly) when the range is empty.
+template <bool DISCARD>
 __device__ __forceinline__ void enc_tri_tile(
     int n1, const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
     const double *__restrict__ r1, const double *__restrict__ v1, const double *__restrict__ renc1, int n2,
     const float4 *__restrict__ A2, const float4 *__restrict__ B2, const float4 *__restrict__ V2,
     const double *__restrict__ r2, const double *__restrict__ v2, const double *__restrict__ renc2, int upper, int j0,
     int ibeg, int iend, int base1, int base2, double dt, long long cap, int32_t *__restrict__ o1,
-    int32_t *__restrict__ o2, int32_t *__restrict__ olv, unsigned long long *__restrict__ count) {
+    int32_t *__restrict__ o2, int32_t *__restrict__ olv, unsigned long long *__restrict__ count,
+    const int32_t *__restrict__ st2 = nullptr) {
     __shared__ float4 sa[EP], sb[EP], sv[EP];
     const int j = j0 + threadIdx.x;
-    const bool active = j < n2;
+    const bool active = j < n2 && (!DISCARD || st2[j] == ST_ACTIVE);
     iend = min(n1, iend);
     if (upper) iend = min(iend, j0 + ET);
     if (ibeg >= iend) return;  // whole block outside the upper triangle
@@ -88,6 +115,10 @@ __device__ __forceinline__ void enc_tri_tile(
                 const double vxr = v2[3 * j + 0] - v1[3 * i + 0];
                 const double vyr = v2[3 * j + 1] - v1[3 * i + 1];
                 const double vzr = v2[3 * j + 2] - v1[3 * i + 2];
+                if (DISCARD) {
+                    if (d_discard_close(xr, yr, zr, vxr, vyr, vzr, dt, renc1[i] * renc1[i])) o2[base2 + j] = 1;
+                    continue;
+                }
                 const double renc12 = renc1[i] + (renc2 ? renc2[j] : 0.0);
                 int lenc, lv;
                 d_encounter_one(xr, yr, zr, vxr, vyr, vzr, renc12, dt, lenc, lv);
@@ -106,22 +137,24 @@ __device__ __forceinline__ void enc_tri_tile(
 }
 
 // One system: receivers tile blockIdx.x, partner chunk blockIdx.y.
+template <bool DISCARD>
 __global__ void __launch_bounds__(ET) k_encounter_tri(
     int n1, const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
     const double *__restrict__ r1, const double *__restrict__ v1, const double *__restrict__ renc1, int n2,
     const float4 *__restrict__ A2, const float4 *__restrict__ B2, const float4 *__restrict__ V2,
     const double *__restrict__ r2, const double *__restrict__ v2, const double *__restrict__ renc2, int upper,
     int shift2, double dt, int chunk, long long cap, int32_t *__restrict__ o1, int32_t *__restrict__ o2,
-    int32_t *__restrict__ olv, unsigned long long *__restrict__ count) {
+    int32_t *__restrict__ olv, unsigned long long *__restrict__ count, const int32_t *__restrict__ st2) {
     const int ibeg = blockIdx.y * chunk;
-    enc_tri_tile(n1, A1, B1, V1, r1, v1, renc1, n2, A2, B2, V2, r2, v2, renc2, upper, blockIdx.x * ET, ibeg,
-                 ibeg + chunk, 0, shift2, dt, cap, o1, o2, olv, count);
+    enc_tri_tile<DISCARD>(n1, A1, B1, V1, r1, v1, renc1, n2, A2, B2, V2, r2, v2, renc2, upper, blockIdx.x * ET, ibeg,
+                          ibeg + chunk, 0, shift2, dt, cap, o1, o2, olv, count, st2);
 }
 
 // Batched (ensemble) check: block b takes item b = (system s, first receiver j0) of a
 // table sorted by cost.  List 1 is system s's pl ([off1[s], off1[s] + n1[s]) in the
 // float/double arrays), list 2 its pl again (upper, pl-pl) or its tp (off2, n2).  Pairs
 // are written with global 1-based indices, so the sorted list groups by system.
+template <bool DISCARD>
 __global__ void __launch_bounds__(ET) k_encounter_tri_batched(
     const int4 *__restrict__ items, const int32_t *__restrict__ off1, const int32_t *__restrict__ n1s,
     const float4 *__restrict__ A1, const float4 *__restrict__ B1, const float4 *__restrict__ V1,
@@ -130,13 +163,14 @@ __global__ void __launch_bounds__(ET) k_encounter_tri_batched(
     const float4 *__restrict__ B2, const float4 *__restrict__ V2, const double *__restrict__ r2,
     const double *__restrict__ v2, const double *__restrict__ renc2, int upper, double dt, long long cap,
     int32_t *__restrict__ o1, int32_t *__restrict__ o2, int32_t *__restrict__ olv,
-    unsigned long long *__restrict__ count) {
+    unsigned long long *__restrict__ count, const int32_t *__restrict__ st2) {
     const int4 w = items[blockIdx.x];
     const int s = w.x;
     const int a = off1[s], b = off2[s];
-    enc_tri_tile(n1s[s], A1 + a, B1 + a, V1 + a, r1 + 3 * (size_t)a, v1 + 3 * (size_t)a, renc1 + a, n2s[s], A2 + b,
-                 B2 + b, V2 + b, r2 + 3 * (size_t)b, v2 + 3 * (size_t)b, renc2 ? renc2 + b : nullptr, upper, w.y, 0,
-                 n1s[s], a, b, dt, cap, o1, o2, olv, count);
+    enc_tri_tile<DISCARD>(n1s[s], A1 + a, B1 + a, V1 + a, r1 + 3 * (size_t)a, v1 + 3 * (size_t)a, renc1 + a,
+                          n2s[s], A2 + b, B2 + b, V2 + b, r2 + 3 * (size_t)b, v2 + 3 * (size_t)b,
+                          renc2 ? renc2 + b : nullptr, upper, w.y, 0, n1s[s], a, b, dt, cap, o1, o2, olv, count,
+                          st2 ? st2 + b : nullptr);
 }
 
 // ------------------------------------------------------------------ sorting
@@ -475,8 +509,9 @@ int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const doubl
     int chunk = (n1 + nchunk - 1) / nchunk;
     chunk = (chunk + EP - 1) / EP * EP;
     nchunk = (n1 + chunk - 1) / chunk;
-    k_encounter_tri<<<dim3(bx, nchunk), ET, 0, c->stream>>>(n1, A1, B1, V1, r1, v1, renc1, n2, A2, B2, V2, r2, v2,
-                                                            renc2, upper, shift2, dt, chunk, cap, o1, o2, olv, count);
+    k_encounter_tri<false><<<dim3(bx, nchunk), ET, 0, c->stream>>>(n1, A1, B1, V1, r1, v1, renc1, n2, A2, B2, V2, r2,
+                                                                   v2, renc2, upper, shift2, dt, chunk, cap, o1, o2, olv,
+                                                                   count, nullptr);
     c->launches++;
     return launch_status(c, "encounter_tri");
 }
@@ -498,11 +533,54 @@ int encounter_tri_batched(swg_ctx *c, int nitems, const int4 *items, const int32
                           const double *v2, const double *renc2, int upper, double dt, long long cap, int32_t *o1,
                           int32_t *o2, int32_t *olv, unsigned long long *count) {
     if (nitems <= 0) return SWG_OK;
-    k_encounter_tri_batched<<<nitems, ET, 0, c->stream>>>(items, off1, n1, F1, F1 + nf1, F1 + 2 * nf1, r1, v1, renc1,
-                                                          off2, n2, F2, F2 + nf2, F2 + 2 * nf2, r2, v2, renc2, upper,
-                                                          dt, cap, o1, o2, olv, count);
+    k_encounter_tri_batched<false><<<nitems, ET, 0, c->stream>>>(items, off1, n1, F1, F1 + nf1, F1 + 2 * nf1, r1, v1,
+                                                                 renc1, off2, n2, F2, F2 + nf2, F2 + 2 * nf2, r2, v2,
+                                                                 renc2, upper, dt, cap, o1, o2, olv, count, nullptr);
     c->launches++;
     return launch_status(c, "encounter_tri_batched");
+}
+
+// Close-approach discard scan (swiftest_discard_pl_tp, src/swiftest/swiftest_discard.f90:244-290)
+// of the ACTIVE test particles of one system against its massive bodies: heliocentric
+// positions and velocities, r2crit = radius^2; flag[j] = 1 for every tp that comes too
+// close to some pl (flag zeroed by the caller).  F: scratch for the float copies,
+// 3 * (npl + ntp) float4.
+int discard_pl_tp_launch(swg_ctx *c, int32_t npl, const double *rpl, const double *vpl, const double *radius,
+                         int32_t ntp, const double *rtp, const double *vtp, const int32_t *tstatus, double dt,
+                         float4 *F, int32_t *flag) {
+    if (npl <= 0 || ntp <= 0) return SWG_OK;
+    float4 *A1 = F, *B1 = A1 + npl, *V1 = B1 + npl, *A2 = V1 + npl, *B2 = A2 + ntp, *V2 = B2 + ntp;
+    k_encounter_prep<<<(npl + 255) / 256, 256, 0, c->stream>>>(npl, rpl, vpl, radius, A1, B1, V1);
+    k_encounter_prep<<<(ntp + 255) / 256, 256, 0, c->stream>>>(ntp, rtp, vtp, nullptr, A2, B2, V2);
+    c->launches += 2;
+    const int bx = (ntp + ET - 1) / ET;
+    const int target = 4 * (c->num_sms > 0 ? c->num_sms : 152);
+    int nchunk = std::max(1, std::min((target + bx - 1) / bx, (npl + EP - 1) / EP));
+    int chunk = (npl + nchunk - 1) / nchunk;
+    chunk = (chunk + EP - 1) / EP * EP;
+    nchunk = (npl + chunk - 1) / chunk;
+    k_encounter_tri<true><<<dim3(bx, nchunk), ET, 0, c->stream>>>(npl, A1, B1, V1, rpl, vpl, radius, ntp, A2, B2, V2,
+                                                                  rtp, vtp, nullptr, 0, 0, dt, chunk, 0, nullptr,
+                                                                  flag, nullptr, nullptr, tstatus);
+    c->launches++;
+    return launch_status(c, "discard_pl_tp");
+}
+
+// The same scan for every system of an ensemble over its pl-tp item table; F1/F2: the
+// float copies (A|B|V) of all pl (nf1 = NPL) and tp (nf2 = NTP), prepared here.
+int discard_pl_tp_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
+                          int64_t NPL, const double *rpl, const double *vpl, const double *radius,
+                          const int32_t *toff, const int32_t *ntp, int64_t NTP, const double *rtp, const double *vtp,
+                          const int32_t *tstatus, double dt, float4 *F1, float4 *F2, int32_t *flag) {
+    if (nitems <= 0) return SWG_OK;
+    SWG_TRY(encounter_prep_launch(c, NPL, rpl, vpl, radius, F1, F1 + NPL, F1 + 2 * NPL));
+    SWG_TRY(encounter_prep_launch(c, NTP, rtp, vtp, nullptr, F2, F2 + NTP, F2 + 2 * NTP));
+    k_encounter_tri_batched<true><<<nitems, ET, 0, c->stream>>>(items, poff, npl, F1, F1 + NPL, F1 + 2 * NPL, rpl, vpl,
+                                                                radius, toff, ntp, F2, F2 + NTP, F2 + 2 * NTP, rtp,
+                                                                vtp, nullptr, 0, dt, 0, nullptr, flag, nullptr,
+                                                                nullptr, tstatus);
+    c->launches++;
+    return launch_status(c, "discard_pl_tp_batched");
 }
 
 // scratch of one encounter_launch call (mode, list sizes)

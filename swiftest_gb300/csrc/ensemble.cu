@@ -92,6 +92,8 @@ struct swg_ensemble {
     EncWork enc_pp, enc_pt;
     int32_t *rec_out = nullptr;  // [0] status, [1] deepest level, [2] sub-steps
     int32_t *rec_resume = nullptr, *rec_pend = nullptr;  // per system: paused recursion stack, pause flag
+    int32_t *tflag = nullptr;                // tp flagged by the close-approach scan
+    unsigned long long *ndiscard = nullptr;  // tp removed by the scan
     DevBuf rec_scratch, rows;
     double *eout = nullptr;      // 9 per system
     int32_t *h_flags = nullptr;  // pinned: [2] recursion status; +8: two unsigned long long counts
@@ -866,6 +868,19 @@ int ens_step(swg_ensemble *e, double dt) {
     return L(c, "ens_finish");
 }
 
+// swiftest_discard_pl_tp of every system (src/swiftest/swiftest_discard.f90:244-290), after
+// each step when close encounters are checked, on the pl-tp items of the encounter check.
+int discard_step(swg_ensemble *e) {
+    if (!e->lclose || e->n_ept == 0) return SWG_OK;
+    swg_ctx *c = e->c;
+    SWG_TRY(discard_pl_tp_batched(c, e->n_ept, e->it_ept, e->poff, e->npl, e->NPL, e->rh, e->vh, e->radius, e->toff,
+                                  e->ntp, e->NTP, e->trh, e->tvh, e->tstatus, e->dt, e->eP, e->eT, e->tflag));
+    k_apply_discard<<<grid_for(e->NTP, 256), 256, 0, c->stream>>>(e->NTP, e->tflag, e->tstatus, e->tlmask, e->trh,
+                                                                   e->tvh, e->tvb, 0, e->tsys, e->toff, e->npl,
+                                                                   e->ndiscard);
+    return L(c, "apply_discard");
+}
+
 }  // namespace
 
 // ======================================================================== C ABI
@@ -945,6 +960,8 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_resume, (size_t)REC_STATE * S);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_pend, S);
+    if (rc == SWG_OK) rc = dalloc(c, &e->tflag, m);
+    if (rc == SWG_OK) rc = dalloc(c, &e->ndiscard, 1);
     e->h_pend.assign(S, 0);
     if (rc == SWG_OK) rc = ensure(c, e->rows, sizeof(double) * 4 * n);
     if (rc == SWG_OK) {
@@ -983,7 +1000,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->it_mpl, e->it_mtp,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->rec_scratch.ptr, e->rows.ptr, e->eout};
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
@@ -1078,6 +1095,7 @@ int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
     e->h_flags[2] = 0;
     for (int32_t k = 0; k < nsteps; k++) {
         SWG_TRY(ens_step(e, e->dt));
+        SWG_TRY(discard_step(e));
         if (e->h_flags[2] != 0) {  // recursion status of an earlier step, seen at a sync point
             e->c->err = "SyMBA local time step too small";
             return e->h_flags[2];
@@ -1150,10 +1168,14 @@ int swg_ensemble_stats(swg_ensemble *e, int64_t *out) {
     SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "stats"));
     int64_t tot = 0;
     for (int32_t v : steps) tot += v;
+    unsigned long long nd = 0;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(&nd, e->ndiscard, sizeof(nd), cudaMemcpyDeviceToHost, c->stream), "stats"));
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "stats"));
     e->stats[0] = tot;
     e->stats[1] = dev[1];
     e->stats[5] = dev[2];
     std::memcpy(out, e->stats, sizeof(e->stats));
+    out[4] += (int64_t)nd;
     return SWG_OK;
 }
 

@@ -200,6 +200,16 @@ int encounter_tri_batched(swg_ctx *c, int nitems, const int4 *items, const int32
                           const double *v2, const double *renc2, int upper, double dt, long long cap, int32_t *o1,
                           int32_t *o2, int32_t *olv, unsigned long long *count);
 
+// swiftest_discard_pl_tp close-approach scans (encounter.cu): flag[j] = 1 (flag zeroed by
+// the caller) for each ACTIVE tp that comes within a pl's radius during the step.
+int discard_pl_tp_launch(swg_ctx *c, int32_t npl, const double *rpl, const double *vpl, const double *radius,
+                         int32_t ntp, const double *rtp, const double *vtp, const int32_t *tstatus, double dt,
+                         float4 *F, int32_t *flag);
+int discard_pl_tp_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
+                          int64_t NPL, const double *rpl, const double *vpl, const double *radius,
+                          const int32_t *toff, const int32_t *ntp, int64_t NTP, const double *rtp, const double *vtp,
+                          const int32_t *tstatus, double dt, float4 *F1, float4 *F2, int32_t *flag);
+
 // Batched TRIANGULAR pl-pl check over radius-sorted tiles (encounter_sorted.cu): per
 // system sort by |r| into perm, float copies F (3 * NPL float4, sorted order) and bound
 // tiles (tiles[k] = (system, first sorted position), tbase[s] = system's first tile),

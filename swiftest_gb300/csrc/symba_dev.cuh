@@ -1030,5 +1030,29 @@ static __global__ void k_set_renc(int npl, const double *rhill, double rhscale, 
     if (i < npl) renc[i] = d_renc(rhill[i], rhscale, scale);
 }
 
+// Test particles flagged by the close-approach scan (swiftest_discard_pl_tp) leave the
+// system: status INACTIVE, masked, parked with no velocity at 1e6 AU + (npl + local index)
+// (the reference spills them out of its arrays).  tsys/toff/npls (optional) give each
+// test particle's system in a CSR-packed ensemble; otherwise one system of npl bodies.
+static __global__ void k_apply_discard(int64_t ntp, int32_t *flag, int32_t *tstatus, int32_t *tlmask, double *trh,
+                                       double *tvh, double *tvb, int npl, const int32_t *__restrict__ tsys,
+                                       const int32_t *__restrict__ toff, const int32_t *__restrict__ npls,
+                                       unsigned long long *count) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= ntp || !flag[j]) return;
+    flag[j] = 0;
+    int64_t slot = npl + j;
+    if (tsys) {
+        const int s = tsys[j];
+        slot = npls[s] + (j - toff[s]);
+    }
+    tstatus[j] = ST_INACTIVE;
+    tlmask[j] = 0;
+    trh[3 * j] = 1.0e6 + (double)slot;
+    trh[3 * j + 1] = trh[3 * j + 2] = 0.0;
+    for (int d = 0; d < 3; d++) tvh[3 * j + d] = tvb[3 * j + d] = 0.0;
+    atomicAdd(count, 1ull);
+}
+
 }  // namespace sdev
 }  // namespace swg

@@ -56,6 +56,9 @@ struct swg_system {
                                  // [4] collision pending
     int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr, *rec_resume = nullptr;
     DevBuf rec_scratch;
+    DevBuf discard_scratch;                 // float copies of the close-approach scan
+    int32_t *tflag = nullptr;               // tp flagged by the scan
+    unsigned long long *ndiscard = nullptr; // tp removed by the scan
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
     StepProfile prof;  // optional CUDA-event profile per kernel class (PROF_*)
 };
@@ -800,6 +803,20 @@ int symba_interp(swg_system *s, double dt) {
     return SWG_OK;
 }
 
+// swiftest_discard_pl_tp (src/swiftest/swiftest_discard.f90:244-290), run after each step
+// when close encounters are checked (param%lclose), as the driver's discard step does.
+int discard_step(swg_system *s) {
+    if (!s->lclose || s->npl == 0 || s->ntp == 0) return SWG_OK;
+    swg_ctx *c = s->c;
+    SWG_TRY(ensure(c, s->discard_scratch, sizeof(float4) * 3 * ((size_t)s->npl + s->ntp) + 256));
+    SWG_TRY(discard_pl_tp_launch(c, s->npl, s->rh, s->vh, s->radius, s->ntp, s->trh, s->tvh, s->tstatus, s->dt,
+                                 (float4 *)s->discard_scratch.ptr, s->tflag));
+    k_apply_discard<<<grid_for(s->ntp, 256), 256, 0, c->stream>>>(s->ntp, s->tflag, s->tstatus, s->tlmask, s->trh,
+                                                                  s->tvh, s->tvb, s->npl, nullptr, nullptr, nullptr,
+                                                                  s->ndiscard);
+    return L(c, "apply_discard");
+}
+
 // symba_step_system (symba_step.f90:14-52); both level-0 checks are evaluated
 int symba_step(swg_system *s, double dt) {
     swg_ctx *c = s->c;
@@ -862,6 +879,8 @@ int swg_system_create(swg_ctx *c, int integrator, int32_t npl, int32_t ntp, swg_
     if (rc == SWG_OK) rc = dalloc(c, &s->mark_tp, m);
     if (rc == SWG_OK) rc = dalloc(c, &s->rec_out, 4);
     if (rc == SWG_OK) rc = dalloc(c, &s->rec_resume, REC_STATE);
+    if (rc == SWG_OK) rc = dalloc(c, &s->tflag, m);
+    if (rc == SWG_OK) rc = dalloc(c, &s->ndiscard, 1);
     if (rc == SWG_OK) rc = ensure(c, s->flags, 64);
     if (rc == SWG_OK) rc = ensure(c, s->red, sizeof(double) * (4 * n + 64));
     if (rc == SWG_OK) {
@@ -889,7 +908,8 @@ int swg_system_destroy(swg_system *s) {
                     s->ntpenc, s->iflag, s->trh, s->tvh, s->tvb, s->tah, s->tstatus, s->tlmask, s->tlevelg,
                     s->tlevelm, s->tnplenc, s->tiflag, s->dcb, s->plpl_l, s->pltp_l, s->enc.raw.ptr,
                     s->enc.sort.ptr, s->enc.counters.ptr, s->enc2.raw.ptr, s->enc2.sort.ptr, s->enc2.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
-                    s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_resume, s->rec_scratch.ptr};
+                    s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_resume, s->rec_scratch.ptr,
+                    s->discard_scratch.ptr, s->tflag, s->ndiscard};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);
@@ -1014,6 +1034,7 @@ int swg_system_step(swg_system *s, int32_t nsteps) {
         else
             rc = symba_step(s, s->dt);
         if (rc != SWG_OK) return rc;
+        SWG_TRY(discard_step(s));
         if (s->h_flags[2] != 0) {  // recursion status of an earlier step, seen at a sync point
             s->c->err = "SyMBA local time step too small";
             return s->h_flags[2];
@@ -1085,7 +1106,12 @@ int swg_system_stats(swg_system *s, int64_t *out) {
         s->stats[1] = dev[1];
         s->stats[5] = dev[2];
     }
+    unsigned long long nd = 0;
+    SWG_TRY(cuda_status(s->c, cudaMemcpyAsync(&nd, s->ndiscard, sizeof(nd), cudaMemcpyDeviceToHost, s->c->stream),
+                        "stats"));
+    SWG_TRY(cuda_status(s->c, cudaStreamSynchronize(s->c->stream), "stats"));
     std::memcpy(out, s->stats, sizeof(s->stats));
+    out[4] += (int64_t)nd;
     return SWG_OK;
 }
 

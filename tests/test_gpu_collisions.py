@@ -72,3 +72,45 @@ def test_ensemble_collisions_bitexact(ctx):
         assert np.array_equal(trh[a:b], orh) and np.array_equal(tvh[a:b], ovh) and np.array_equal(tst[a:b], ost)
         ncoll += r.stats()["collisions"]
     assert ncoll > 0 and ens.stats()["collisions"] == ncoll
+
+
+def _helio_crowded(seed, npl=60, ntp=600, inflate=1000.0):
+    cb, pl, tp = IC.make_system(seed=seed, npl=npl, ntp=ntp, amin=0.8, amax=1.2, mmin=1e-9, mmax=1e-6)
+    pl = IC.sort_for_integrator(pl, "HELIO")
+    pl["radius"] = pl["radius"] * inflate
+    return cb, pl, tp
+
+
+def test_helio_discard_bitexact(ctx):
+    # swiftest_discard_pl_tp after every step: test particles that pass within a (inflated)
+    # planet radius leave the system, identically on the GPU and in the oracle
+    cb, pl, tp = _helio_crowded(11)
+    gpu = NBodySystem(ctx, "HELIO", cb, pl, tp, dt=0.005)
+    ref = O.OracleSystem("HELIO", cb, pl, tp, dt=0.005)
+    gpu.step(200)
+    ref.step(200)
+    for a, b in zip(gpu.get_pl() + gpu.get_tp(), ref.get_pl() + ref.get_tp()):
+        assert np.array_equal(a, b)
+    assert gpu.stats()["collisions"] == ref.stats()["collisions"] > 10
+
+
+def test_helio_ensemble_discard_bitexact(ctx):
+    systems = [_helio_crowded(seed, npl=40, ntp=300)[1:] for seed in (11, 12)]
+    E = {"integrator": "HELIO", "dt": 0.005, "rhscale": 6.5,
+         "npl": np.array([len(p["Gmass"]) for p, _ in systems], np.int32),
+         "ntp": np.array([len(t["rh"]) for _, t in systems], np.int32),
+         "GMcb": np.full(2, IC.GMCB), "Rcb": np.full(2, IC.RCB),
+         "pl": {k: np.concatenate([p[k] for p, _ in systems]) for k in ("rh", "vh", "Gmass", "radius", "rhill")},
+         "tp": {k: np.concatenate([t[k] for _, t in systems]) for k in ("rh", "vh")}, "systems": systems}
+    ens = Ensemble(ctx, E, precision="FP64")
+    cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
+    refs = [O.OracleSystem("HELIO", cb, pl, tp, dt=0.005) for pl, tp in systems]
+    ens.step(200)
+    for r in refs:
+        r.step(200)
+    trh, tvh, tst = ens.get_tp()
+    for s, r in enumerate(refs):
+        a, b = ens.toff[s], ens.toff[s + 1]
+        orh, ovh, ost = r.get_tp()
+        assert np.array_equal(trh[a:b], orh) and np.array_equal(tvh[a:b], ovh) and np.array_equal(tst[a:b], ost)
+    assert ens.stats()["collisions"] == sum(r.stats()["collisions"] for r in refs) > 0
