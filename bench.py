@@ -7,7 +7,7 @@ total for seed 0), masses log-uniform in [1e-11, 1e-7] Msun, a in [0.5, 2] AU, e
 Rayleigh(0.02), dt = 0.002 yr, 1-Hill-radius encounter radius (RHSCALE = 1), TRIANGULAR
 level-0 checks, recursive encounter kicks in FP64.  A step advances every system by one
 symba_step_system.  ``--workload c1`` runs the single-system C1 disk (2000 pl + 10 000 tp)
-instead.
+instead, ``--workload c3`` the batched HELIO ensemble (512 systems with test particles).
 
 ``value``: body-steps/s of the mixed-precision batched path (FP32 pair kicks with
 float-float sums; FP64 drift, encounter decisions, recursion) with the state resident in
@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c4", choices=["c4", "c1"])
+    p.add_argument("--workload", default="c4", choices=["c4", "c3", "c1"])
     p.add_argument("--nsys", type=int, default=None, help="first NSYS systems of the C4 ensemble")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     return p.parse_args()
@@ -80,7 +80,8 @@ class C4:
         from swiftest_gb300 import initial_conditions as IC
         self.E = IC.make_ensemble("C4", nsys=args.nsys)
         self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
-        self.pairs_per_step = 2 * float(sum(int(n) * (int(n) - 1) for n in self.E["npl"]))
+        self.plpl_pairs = float(sum(int(n) * (int(n) - 1) for n in self.E["npl"]))  # per kick evaluation
+        self.pairs_per_step = 2 * self.plpl_pairs
 
     def make(self, ctx, precision):
         from swiftest_gb300.api import Ensemble
@@ -117,6 +118,42 @@ class C4:
         return bs, t_all, f"{steps_per_system} SyMBA step(s) of each of the first {nsys} C4 systems ({bs} body-steps)"
 
 
+class C3(C4):
+    """The batched HELIO ensemble: 512 systems, N_pl log-uniform in [10, 2000], N_tp = 5 N_pl."""
+
+    def __init__(self, args):
+        from swiftest_gb300 import initial_conditions as IC
+        self.E = IC.make_ensemble("C3", nsys=args.nsys)
+        self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
+        n = [int(x) for x in self.E["npl"]]
+        self.plpl_pairs = float(sum(k * (k - 1) for k in n))
+        self.pairs_per_step = 2 * float(sum(k * (k - 1) + 5 * k * k for k in n))
+
+    def config(self, precision):
+        n, m = self.E["npl"], self.E["ntp"]
+        return {"workload": f"C3 batched HELIO ensemble: {len(n)} systems, N_pl log-uniform in [10, 2000] "
+                            f"({int(n.sum())} pl, {int(m.sum())} tp = 5 N_pl), m in [1e-10, 1e-6] Msun, a in [0.5, 5] AU, "
+                            "e Rayleigh(0.01), i Rayleigh(0.005), dt=0.01 yr, close-approach discards on",
+                "nsys": len(n), "npl_total": int(n.sum()), "ntp_total": int(m.sum()), "dt": self.E["dt"], "seed": 0,
+                "precision": precision, "l2": "flushed before every timed step (512 MB memset, untimed)"}
+
+    def oracle_sample(self, budget_s, steps_per_system=1):
+        from oracle import oracle as O
+        from swiftest_gb300 import initial_conditions as IC
+        cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
+        bs, t_all, nsys = 0, 0.0, 0
+        for pl, tp in self.E["systems"]:
+            s = O.OracleSystem("HELIO", cb, pl, tp, dt=self.E["dt"], lclose=True)
+            t0 = time.perf_counter()
+            s.step(steps_per_system)
+            t_all += time.perf_counter() - t0
+            bs += (len(pl["Gmass"]) + len(tp["rh"])) * steps_per_system
+            nsys += 1
+            if t_all > budget_s:
+                break
+        return bs, t_all, f"{steps_per_system} HELIO step(s) of each of the first {nsys} C3 systems ({bs} body-steps)"
+
+
 class C1:
     """The single-system C1 disk."""
 
@@ -129,6 +166,7 @@ class C1:
         self.cfg, self.cb, self.pl, self.tp = cfg, cb, IC.sort_for_integrator(pl, "SYMBA"), tp
         self.nbodies = cfg["npl"] + cfg["ntp"]
         npl, ntp = cfg["npl"], cfg["ntp"]
+        self.plpl_pairs = float(npl * (npl - 1))
         self.pairs_per_step = 2.0 * (npl * (npl - 1) + npl * ntp)
 
     def make(self, ctx, precision):
@@ -315,7 +353,7 @@ def cpu_baseline(wl, budget_s):
 def reference_arm(args, world, rank):
     if rank != 0:
         return 0
-    wl = C4(args) if args.workload == "c4" else C1(args)
+    wl = {"c4": C4, "c3": C3, "c1": C1}[args.workload](args)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     from oracle import oracle as O
@@ -359,7 +397,7 @@ def main():
     from swiftest_gb300 import build as B
     B.build()
     from swiftest_gb300.api import Context
-    wl = C4(args) if args.workload == "c4" else C1(args)
+    wl = {"c4": C4, "c3": C3, "c1": C1}[args.workload](args)
     ctx = Context(local)
     clocks = ClockSampler(local)
     if td:
@@ -386,7 +424,7 @@ def main():
     kick = prof["kick_pl"]
     if kick["launches"]:
         avg_ms = kick["ms"] / kick["launches"]
-        flops = FLOPS_PER_INTERACTION * wl.pairs_per_step / 2  # one pl-pl evaluation
+        flops = FLOPS_PER_INTERACTION * wl.plpl_pairs  # one pl-pl evaluation
         ach = flops / (avg_ms * 1e-3) / 1e12
         roof = {"kernel": "kick_pl (mixed FP32 pair kick, batched persistent launch)", "bound": "fp32",
                 "achieved": ach, "peak": peak32, "unit": "TFLOP/s", "frac": ach / peak32 if peak32 else None,

@@ -139,8 +139,9 @@ int swg_system_get_tp(swg_system *sys, double *rh, double *vh, int32_t *status);
  * potential uses the body's barycentric distance), then te_helio: the same total with the
  * central-body potential at the heliocentric distance. */
 int swg_system_energy(swg_system *sys, double *out);
-/* out[6]: steps with encounters, max recursion depth, sum plpl enc, sum pltp enc, collisions,
- * recursion sub-steps executed */
+/* out[6]: steps with encounters, max recursion depth, sum plpl enc, sum pltp enc, collisions
+ * resolved plus test particles removed by the close-approach discard scan, recursion
+ * sub-steps executed */
 int swg_system_stats(swg_system *sys, int64_t *out);
 /* level-0 encounter lists of the last step */
 int swg_system_plpl_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
@@ -187,6 +188,10 @@ int swg_ensemble_plpl_list(swg_ensemble *ens, int32_t sys, int64_t cap, int64_t 
 int swg_ensemble_set_state(swg_ensemble *ens, const double *rh, const double *vh, const double *trh,
                            const double *tvh);
 int swg_ensemble_get_state_async(swg_ensemble *ens, double *rh, double *vh, double *trh, double *tvh);
+/* HELIO ensembles replay each step as a CUDA graph captured after the first step (default
+ * on; results are identical either way).  SyMBA steps always run eagerly: each takes one
+ * host decision (the encounter-list sizes). */
+int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
 int swg_ensemble_profile(swg_ensemble *ens, int enable);
 int swg_ensemble_profile_read(swg_ensemble *ens, double *out);
 

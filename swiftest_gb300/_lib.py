@@ -85,6 +85,7 @@ SIGNATURES = {
     "swg_ensemble_plpl_list": (_INT, [_P, _I32, _I64, C.POINTER(_I64), _P, _P]),
     "swg_ensemble_set_state": (_INT, [_P, _P, _P, _P, _P]),
     "swg_ensemble_get_state_async": (_INT, [_P, _P, _P, _P, _P]),
+    "swg_ensemble_use_graphs": (_INT, [_P, _INT]),
     "swg_ensemble_profile": (_INT, [_P, _INT]),
     "swg_ensemble_profile_read": (_INT, [_P, _P]),
     "swg_flush_l2": (_INT, [_P, _I64]),

@@ -400,6 +400,9 @@ class Ensemble:
             self.ctx.check("swg_ensemble_plpl_list", rc)
             return i1[:n.value].copy(), i2[:n.value].copy()
 
+    def use_graphs(self, enable: bool = True):
+        self.ctx.check("swg_ensemble_use_graphs", self.ctx.lib.swg_ensemble_use_graphs(self.h, int(bool(enable))))
+
     def profile(self, enable: bool = True):
         self.ctx.check("swg_ensemble_profile", self.ctx.lib.swg_ensemble_profile(self.h, int(bool(enable))))
 

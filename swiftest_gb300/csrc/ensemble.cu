@@ -106,6 +106,10 @@ struct swg_ensemble {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned *head2 = nullptr;
     int64_t nchecks = 0;  // level-0 checks so far (the radial order is refreshed every RESORT_EVERY)
+    // CUDA graph of one HELIO step (+ discard scan): captured after one eager step, replayed
+    bool use_graph = true;
+    int64_t eager_steps = 0, graph_launches = 0;
+    cudaGraphExec_t graph = nullptr;
 };
 
 // level-0 checks between refreshes of the radial order of the pl-pl check
@@ -1005,6 +1009,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
     if (e->side) cudaStreamSynchronize(e->side);
+    if (e->graph) cudaGraphExecDestroy(e->graph);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->side) cudaStreamDestroy(e->side);
@@ -1056,6 +1061,9 @@ int swg_ensemble_set_tp(swg_ensemble *e, const double *rh, const double *vh) {
 int swg_ensemble_set_param(swg_ensemble *e, double dt, double rhscale, int lclose, int precision) {
     if (!e || !(dt > 0.0) || !(rhscale > 0.0) || (precision != SWG_FP64 && precision != SWG_MIXED))
         return SWG_ERR_ARG;
+    if (e->graph) cudaGraphExecDestroy(e->graph);  // a captured step holds the old parameters
+    e->graph = nullptr;
+    e->eager_steps = 0;
     e->dt = dt;
     e->rhscale = rhscale;
     e->lclose = lclose != 0;
@@ -1085,6 +1093,9 @@ int swg_ensemble_initialize(swg_ensemble *e) {
     SWG_TRY(tp_misc(e, CB_VB, 0.0, 5, -1));  // tp vb = vh + the central body's vb
     e->t = 0.0;
     e->nchecks = 0;
+    e->eager_steps = 0;
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
     std::memset(e->stats, 0, sizeof(e->stats));
     e->initialized = 1;
     return cuda_status(c, cudaStreamSynchronize(c->stream), "init");
@@ -1092,10 +1103,37 @@ int swg_ensemble_initialize(swg_ensemble *e) {
 
 int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
     if (!e || !e->initialized) return SWG_ERR_STATE;
+    swg_ctx *c = e->c;
     e->h_flags[2] = 0;
+    // A HELIO step takes no host decision (first-step flags live on the device), so after
+    // one eager step (which also makes every lazy allocation and query) the step and its
+    // discard scan are captured once as a CUDA graph and replayed.  SyMBA steps read the
+    // encounter-list sizes on the host and run eagerly.
+    const bool graphable = e->integrator == SWG_HELIO && e->use_graph && !e->prof.on;
     for (int32_t k = 0; k < nsteps; k++) {
-        SWG_TRY(ens_step(e, e->dt));
-        SWG_TRY(discard_step(e));
+        if (graphable && e->eager_steps > 0) {
+            if (!e->graph) {
+                cudaGraph_t g = nullptr;
+                const int64_t l0 = c->launches;
+                SWG_TRY(cuda_status(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture"));
+                int rc = ens_step(e, e->dt);
+                if (rc == SWG_OK) rc = discard_step(e);
+                const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+                SWG_TRY(rc);
+                SWG_TRY(cuda_status(c, ce, "capture"));
+                e->graph_launches = c->launches - l0;
+                c->launches = l0;
+                const cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+                cudaGraphDestroy(g);
+                SWG_TRY(cuda_status(c, ie, "graph instantiate"));
+            }
+            SWG_TRY(cuda_status(c, cudaGraphLaunch(e->graph, c->stream), "graph launch"));
+            c->launches += e->graph_launches;
+        } else {
+            SWG_TRY(ens_step(e, e->dt));
+            SWG_TRY(discard_step(e));
+            e->eager_steps++;
+        }
         if (e->h_flags[2] != 0) {  // recursion status of an earlier step, seen at a sync point
             e->c->err = "SyMBA local time step too small";
             return e->h_flags[2];
@@ -1230,6 +1268,12 @@ int swg_ensemble_get_state_async(swg_ensemble *e, double *rh, double *vh, double
         SWG_TRY(cuda_status(c, cudaMemcpyAsync(trh, e->trh, 24 * m, cudaMemcpyDeviceToHost, c->stream), "state"));
     if (m && tvh)
         SWG_TRY(cuda_status(c, cudaMemcpyAsync(tvh, e->tvh, 24 * m, cudaMemcpyDeviceToHost, c->stream), "state"));
+    return SWG_OK;
+}
+
+int swg_ensemble_use_graphs(swg_ensemble *e, int enable) {
+    if (!e) return SWG_ERR_ARG;
+    e->use_graph = enable != 0;
     return SWG_OK;
 }
 

@@ -141,3 +141,17 @@ def test_symba_ensemble_lists_many_tiles(ctx):
             total += len(ri[0])
     assert total > 0
     assert _check_states(ens, refs)
+
+
+def test_helio_ensemble_graph_replay_matches_eager(ctx):
+    # HELIO steps replayed from a captured CUDA graph give the same bits as eager steps
+    E = IC.make_ensemble("C3", nsys=6, scale=0.1)
+    out = []
+    for graphs in (True, False):
+        ens = Ensemble(ctx, E, precision="MIXED", dt=0.01)
+        ens.use_graphs(graphs)
+        ens.step(40)
+        out.append(ens.get_pl() + ens.get_tp())
+        ens.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
