@@ -192,6 +192,16 @@ int swg_ensemble_get_state_async(swg_ensemble *ens, double *rh, double *vh, doub
  * on; results are identical either way).  SyMBA steps always run eagerly: each takes one
  * host decision (the encounter-list sizes). */
 int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
+/* Tile shape of the batched mixed-precision kick (no counterpart in the reference).
+ * Every shape gives bit-identical accelerations; by default (variant -1) each kick kind
+ * takes the fastest shape for its GPU and mean system size, timed on the ensemble's own
+ * data at its first kick and cached in $SWG_TUNE_CACHE, else
+ * $HOME/.cache/swiftest_gb300/kick_tune.txt.  0 .. SWG_KICK_NVARIANT-1 forces a shape.
+ * kick_variant reads the shape in use for kind 0 (pl-pl) or 1 (pl-tp), -1 before the
+ * first mixed kick of that kind. */
+#define SWG_KICK_NVARIANT 5
+int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
+int swg_ensemble_kick_variant(swg_ensemble *ens, int kind, int *variant);
 int swg_ensemble_profile(swg_ensemble *ens, int enable);
 int swg_ensemble_profile_read(swg_ensemble *ens, double *out);
 

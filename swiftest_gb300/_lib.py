@@ -23,6 +23,7 @@ SWG_MEM_HOST = 0
 SWG_MEM_DEVICE = 1
 SWG_FP64 = 0
 SWG_MIXED = 1
+SWG_KICK_NVARIANT = 5
 SWG_ENC_TRIANGULAR = 0
 SWG_ENC_SORTSWEEP = 1
 SWG_WHM = 0
@@ -86,6 +87,8 @@ SIGNATURES = {
     "swg_ensemble_set_state": (_INT, [_P, _P, _P, _P, _P]),
     "swg_ensemble_get_state_async": (_INT, [_P, _P, _P, _P, _P]),
     "swg_ensemble_use_graphs": (_INT, [_P, _INT]),
+    "swg_ensemble_set_kick_variant": (_INT, [_P, _INT]),
+    "swg_ensemble_kick_variant": (_INT, [_P, _INT, C.POINTER(_INT)]),
     "swg_ensemble_profile": (_INT, [_P, _INT]),
     "swg_ensemble_profile_read": (_INT, [_P, _P]),
     "swg_flush_l2": (_INT, [_P, _I64]),

@@ -403,6 +403,19 @@ class Ensemble:
     def use_graphs(self, enable: bool = True):
         self.ctx.check("swg_ensemble_use_graphs", self.ctx.lib.swg_ensemble_use_graphs(self.h, int(bool(enable))))
 
+    def set_kick_variant(self, variant: int = -1):
+        """Force the mixed kick's tile shape (0 .. SWG_KICK_NVARIANT-1) or autotune it (-1)."""
+        self.ctx.check("swg_ensemble_set_kick_variant", self.ctx.lib.swg_ensemble_set_kick_variant(self.h, int(variant)))
+
+    def kick_variant(self):
+        """Tile shapes in use by the mixed pl-pl and pl-tp kicks (-1: not chosen yet)."""
+        out = []
+        for kind in (0, 1):
+            v = C.c_int(-1)
+            self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, kind, C.byref(v)))
+            out.append(int(v.value))
+        return {"pl": out[0], "tp": out[1]}
+
     def profile(self, enable: bool = True):
         self.ctx.check("swg_ensemble_profile", self.ctx.lib.swg_ensemble_profile(self.h, int(bool(enable))))
 

@@ -37,7 +37,7 @@
 using namespace swg;
 using namespace swg::sdev;
 
-static_assert(KICK_MIXED_TILE == 128 && KICK_FP64_TILE == 8 && ENC_TILE == 128, "tile sizes of the batched kernels");
+static_assert(KICK_FP64_TILE == 8 && ENC_TILE == 128, "tile sizes of the batched kernels");
 
 // Arguments of the ensemble recursion kernel: the shared base plus per-system tables.
 struct EnsRecArgs {
@@ -83,8 +83,13 @@ struct swg_ensemble {
     int4 *it_esp = nullptr;
     int ntiles = 0, n_esp = 0, nmax = 0;
     // item tables of the batched pair kernels
-    int4 *it_mpl = nullptr, *it_mtp = nullptr, *it_fpl = nullptr, *it_ftp = nullptr, *it_ept = nullptr;
-    int n_mpl = 0, n_mtp = 0, n_fpl = 0, n_ftp = 0, n_ept = 0;
+    int4 *it_fpl = nullptr, *it_ftp = nullptr, *it_ept = nullptr;
+    int n_fpl = 0, n_ftp = 0, n_ept = 0;
+    // mixed kick of kind k (0 pl-pl, 1 pl-tp): tile-shape variant (-1 until chosen by the
+    // autotuner at the first such kick) and its items; force_variant >= 0 overrides the tuner
+    int kv[2] = {-1, -1}, n_kit[2] = {0, 0};
+    int4 *kit[2] = {nullptr, nullptr};
+    int force_variant = -1;
     unsigned *head = nullptr;
     // encounter lists: [i1 | i2 | lvdotr | status | level] * cap, global 1-based indices
     int32_t *pp_l = nullptr, *pt_l = nullptr;
@@ -393,10 +398,7 @@ int build_items(swg_ensemble *e) {
     const int S = e->nsys;
     auto npl = [&](int s) { return e->h_npl[s]; };
     auto ntp = [&](int s) { return e->h_ntp[s]; };
-    auto tp_recv = [&](int s) { return e->h_ntp[s]; };
     auto plcost = [&](int s, int, int nr) { return (double)nr * e->h_npl[s]; };
-    SWG_TRY(put_items(e, &e->it_mpl, &e->n_mpl, make_items(S, KICK_MIXED_TILE, npl, plcost)));
-    SWG_TRY(put_items(e, &e->it_mtp, &e->n_mtp, make_items(S, KICK_MIXED_TILE, tp_recv, plcost)));
     SWG_TRY(put_items(e, &e->it_fpl, &e->n_fpl, make_items(S, KICK_FP64_TILE, npl, plcost)));
     SWG_TRY(put_items(e, &e->it_ftp, &e->n_ftp, make_items(S, KICK_FP64_TILE, ntp, plcost)));
     auto tp_with_pl = [&](int s) { return e->h_npl[s] > 0 ? e->h_ntp[s] : 0; };
@@ -432,6 +434,114 @@ int ensure_pool(swg_ensemble *e, int32_t **l, int64_t *cap, int64_t need) {
     return SWG_OK;
 }
 
+// ------------------------------------------------ mixed kick: tile shape chosen by timing
+// Receiver tiles of the mixed kick of kind k (0 pl-pl, 1 pl-tp) for tiles of `tile`.
+std::vector<int4> kick_items(const swg_ensemble *e, int k, int tile) {
+    auto recv = [&](int s) { return k == 0 ? e->h_npl[s] : e->h_ntp[s]; };
+    auto cost = [&](int s, int, int nr) { return (double)nr * e->h_npl[s]; };
+    return make_items(e->nsys, tile, recv, cost);
+}
+
+// Size bucket of the tuning key: floor(log2) of the mean receivers per system.
+int size_bucket(const swg_ensemble *e, int k) {
+    int b = 0;
+    for (double m = (double)(k == 0 ? e->NPL : e->NTP) / std::max(1, e->nsys); m >= 2.0; m *= 0.5) b++;
+    return b;
+}
+
+// One mixed kick of kind k with the given shape and items into acc (overwritten); the
+// partners must be split into kA/kB.
+int mixed_kick(swg_ensemble *e, int k, int variant, const int4 *items, int nitems, double *acc, bool rad,
+               unsigned *head, const int32_t *flag, int phase) {
+    if (k == 0)
+        return kick_mixed_batched(e->c, variant, false, rad, nitems, items, e->poff, e->poff, e->npl, e->rh,
+                                  rad ? e->radius : nullptr, e->kA, e->kB, nullptr, acc, 1, head, flag, phase);
+    return kick_mixed_batched(e->c, variant, true, false, nitems, items, e->toff, e->poff, e->npl, e->trh, nullptr,
+                              e->kA, e->kB, e->tlmask, acc, 1, head);
+}
+
+// Scratch of the timing runs, released on every exit path.
+struct TuneScratch {
+    double *acc = nullptr;
+    int4 *items = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    ~TuneScratch() {
+        if (acc) cudaFree(acc);
+        if (items) cudaFree(items);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
+// Times every tile shape of the mixed kick of kind k on this ensemble's current data (one
+// warm-up and three timed launches each, into scratch accelerations) and returns the
+// fastest.  All shapes give identical results, so only the time differs.
+int time_kick_variants(swg_ensemble *e, int k, bool rad, unsigned *head, const int32_t *flag, int phase, int *best) {
+    swg_ctx *c = e->c;
+    TuneScratch t;
+    SWG_TRY(dalloc(c, &t.acc, 3 * (size_t)(k == 0 ? e->NPL : e->NTP)));
+    for (cudaEvent_t &x : t.ev) SWG_TRY(cuda_status(c, cudaEventCreate(&x), "event"));
+    float best_ms = 0.f;
+    *best = 0;
+    for (int v = 0; v < KICK_NVARIANT; v++) {
+        const std::vector<int4> items = kick_items(e, k, kick_variant_tile(v));
+        if (t.items) cudaFree(t.items);
+        t.items = nullptr;
+        SWG_TRY(dalloc(c, &t.items, items.size()));
+        SWG_TRY(upload(c, t.items, items));
+        const int n = (int)items.size();
+        SWG_TRY(mixed_kick(e, k, v, t.items, n, t.acc, rad, head, flag, phase));
+        SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[0], c->stream), "event"));
+        for (int rep = 0; rep < 3; rep++) SWG_TRY(mixed_kick(e, k, v, t.items, n, t.acc, rad, head, flag, phase));
+        SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[1], c->stream), "event"));
+        SWG_TRY(cuda_status(c, cudaEventSynchronize(t.ev[1]), "event"));
+        float ms = 0.f;
+        SWG_TRY(cuda_status(c, cudaEventElapsedTime(&ms, t.ev[0], t.ev[1]), "event"));
+        if (v == 0 || ms < best_ms) {
+            best_ms = ms;
+            *best = v;
+        }
+    }
+    return SWG_OK;
+}
+
+// Makes sure the mixed kick of kind k has a tile shape and items: the forced shape, else
+// the cached choice for (GPU, kind, size bucket), else the fastest one timed here (and
+// cached).  Runs eagerly at the first such kick; a CUDA graph capture never meets an
+// unchosen kind (graphs are captured after an eager step, and every change of shape or
+// kind drops the graph).
+int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int32_t *flag, int phase) {
+    if (e->kv[k] >= 0) return SWG_OK;
+    swg_ctx *c = e->c;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    SWG_TRY(cuda_status(c, cudaStreamIsCapturing(c->stream, &cap), "capture status"));
+    if (cap != cudaStreamCaptureStatusNone) {
+        c->err = "mixed kick shape not chosen before graph capture";
+        return SWG_ERR_STATE;
+    }
+    int v = e->force_variant;
+    if (v < 0) {
+        const std::string key =
+            tune_key(c->device, k == 0 ? (rad ? "kick_pl_rad" : "kick_pl") : "kick_tp", size_bucket(e, k));
+        v = tune_lookup(key);
+        if (v < 0) {
+            SWG_TRY(time_kick_variants(e, k, rad, head, flag, phase, &v));
+            tune_store(key, v);
+        }
+    }
+    SWG_TRY(put_items(e, &e->kit[k], &e->n_kit[k], kick_items(e, k, kick_variant_tile(v))));
+    e->kv[k] = v;
+    return SWG_OK;
+}
+
+// Forget the chosen shapes (and the graph holding their items).
+void reset_kick_plans(swg_ensemble *e) {
+    for (int k = 0; k < 2; k++) e->kv[k] = -1;
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+    e->eager_steps = 0;
+}
+
 // pl-pl accelerations into ah (helio_kick_getacch_int_pl / symba_kick_getacch_int_pl) of all
 // systems, or (flag != nullptr) of the systems whose flag equals phase, on c->stream.
 int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr, int phase = 0) {
@@ -440,8 +550,8 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
     const double *R = rad ? e->radius : nullptr;
     if (e->precision == SWG_MIXED) {
         SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB, flag ? e->psys : nullptr, flag, phase));
-        return kick_mixed_batched(c, false, rad, e->n_mpl, e->it_mpl, e->poff, e->poff, e->npl, e->rh, R, e->kA,
-                                  e->kB, nullptr, e->ah, 1, head, flag, phase);
+        SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
+        return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase);
     }
     return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah, 1, flag,
                                   phase);
@@ -487,8 +597,8 @@ int kick_vb_tp(swg_ensemble *e, double dt, int lbeg) {
     {
         ProfScope ps(e->prof, c->stream, PROF_KICK_TP);
         if (e->precision == SWG_MIXED) {
-            SWG_TRY(kick_mixed_batched(c, true, false, e->n_mtp, e->it_mtp, e->toff, e->poff, e->npl, e->trh, nullptr,
-                                       e->kA, e->kB, e->tlmask, e->tah, 1, e->head));
+            SWG_TRY(ensure_kick_plan(e, 1, false, e->head, nullptr, 0));
+            SWG_TRY(mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, e->head, nullptr, 0));
         } else {
             SWG_TRY(kick_tp_fp64_batched(c, e->n_ftp, e->it_ftp, e->toff, e->ntp, e->poff, e->npl, e->trh, rp,
                                          e->Gmass, e->tlmask, e->tah, 1));
@@ -1001,7 +1111,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
                     e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
                     e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->eS, e->perm, e->tbase,
-                    e->tiles, e->bounds, e->it_esp, e->head2, e->it_mpl, e->it_mtp,
+                    e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1],
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
                     e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->eout};
@@ -1061,9 +1171,7 @@ int swg_ensemble_set_tp(swg_ensemble *e, const double *rh, const double *vh) {
 int swg_ensemble_set_param(swg_ensemble *e, double dt, double rhscale, int lclose, int precision) {
     if (!e || !(dt > 0.0) || !(rhscale > 0.0) || (precision != SWG_FP64 && precision != SWG_MIXED))
         return SWG_ERR_ARG;
-    if (e->graph) cudaGraphExecDestroy(e->graph);  // a captured step holds the old parameters
-    e->graph = nullptr;
-    e->eager_steps = 0;
+    reset_kick_plans(e);  // a captured step holds the old parameters; the kick kind may change
     e->dt = dt;
     e->rhscale = rhscale;
     e->lclose = lclose != 0;
@@ -1274,6 +1382,20 @@ int swg_ensemble_get_state_async(swg_ensemble *e, double *rh, double *vh, double
 int swg_ensemble_use_graphs(swg_ensemble *e, int enable) {
     if (!e) return SWG_ERR_ARG;
     e->use_graph = enable != 0;
+    return SWG_OK;
+}
+
+int swg_ensemble_set_kick_variant(swg_ensemble *e, int variant) {
+    if (!e || variant < -1 || variant >= KICK_NVARIANT) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick variant"));
+    e->force_variant = variant;
+    reset_kick_plans(e);
+    return SWG_OK;
+}
+
+int swg_ensemble_kick_variant(swg_ensemble *e, int kind, int *variant) {
+    if (!e || !variant || kind < 0 || kind > 1) return SWG_ERR_ARG;
+    *variant = e->kv[kind];
     return SWG_OK;
 }
 

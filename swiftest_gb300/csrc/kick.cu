@@ -243,28 +243,25 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
 // Batched (ensemble) mixed kick: a persistent grid pulls receiver tiles of CSR-packed
 // systems from a work queue (items sorted by cost, largest first, so the tail is made
 // of small tiles).  With sys_flag, only systems whose flag equals `phase` are kicked (the
-// ensemble kicks systems without encounters while the recursion of the others runs).  Item: system s, receivers [r0, r0 + nr) of that system, nr <= 128:
-// MB_THREADS threads own MB_RPT receivers each (r0 + t and r0 + t + MB_THREADS), which
-// halves the shared-memory reads per pair.  Receivers sit at roff[s] + i in
-// rrecv/acc/lmask, partners at poff[s] + j (j < npart[s]) in the pre-split pA/pB.  pl-pl
-// (!TP): rrecv is the pl array, roff == poff, and the receiver is skipped as its own
-// partner through the radius rule (RAD) or the index test.
-constexpr int MB_THREADS = 64;
-constexpr int MB_RPT = 2;
-static_assert(MB_THREADS * MB_RPT == KICK_MIXED_TILE && MB_THREADS >= MT, "batched mixed kick tiling");
-template <bool TP, bool RAD>
-__global__ void __launch_bounds__(MB_THREADS) k_kick_mixed_batched(int nitems, const int4 *__restrict__ items,
-                                                                  const int32_t *__restrict__ roff,
-                                                                  const int32_t *__restrict__ poff,
-                                                                  const int32_t *__restrict__ npart,
-                                                                  const double *__restrict__ rrecv,
-                                                                  const double *__restrict__ R,
-                                                                  const float4 *__restrict__ pA,
-                                                                  const float4 *__restrict__ pB,
-                                                                  const int32_t *__restrict__ lmask,
-                                                                  double *__restrict__ acc, int acc_is_zero,
-                                                                  unsigned *__restrict__ head,
-                                                                  const int32_t *__restrict__ sys_flag, int phase) {
+// ensemble kicks systems without encounters while the recursion of the others runs).
+// Item: system s, receivers [r0, r0 + nr) of that system, nr <= T * RPT: T threads own
+// RPT receivers each (r0 + t, r0 + t + T, ...), sharing each shared-memory partner read.
+// Receivers sit at roff[s] + i in rrecv/acc/lmask, partners at poff[s] + j (j < npart[s])
+// in the pre-split pA/pB.  pl-pl (!TP): rrecv is the pl array, roff == poff, and the
+// receiver is skipped as its own partner through the radius rule (RAD) or the index test.
+// Every (T, RPT) variant adds each receiver's terms in the same order (64-partner tiles in
+// partner order), so the variants give identical bits; the autotuner picks among them.
+template <bool TP, bool RAD, int T, int RPT>
+__global__ void __launch_bounds__(T) k_kick_mixed_batched(int nitems, const int4 *__restrict__ items,
+                                                         const int32_t *__restrict__ roff,
+                                                         const int32_t *__restrict__ poff,
+                                                         const int32_t *__restrict__ npart,
+                                                         const double *__restrict__ rrecv,
+                                                         const double *__restrict__ R,
+                                                         const float4 *__restrict__ pA, const float4 *__restrict__ pB,
+                                                         const int32_t *__restrict__ lmask, double *__restrict__ acc,
+                                                         int acc_is_zero, unsigned *__restrict__ head,
+                                                         const int32_t *__restrict__ sys_flag, int phase) {
     __shared__ float4 sA[MT];
     __shared__ float4 sB[MT];
     __shared__ int s_item;
@@ -277,13 +274,13 @@ __global__ void __launch_bounds__(MB_THREADS) k_kick_mixed_batched(int nitems, c
         const int4 w = items[it];  // (system, r0, nr, unused)
         const int s = w.x;
         if (sys_flag && sys_flag[s] != phase) continue;  // another launch's system (block-uniform)
-        MixedRecv q[MB_RPT];
-        FF ax[MB_RPT], ay[MB_RPT], az[MB_RPT];
-        int gi[MB_RPT];
-        bool inr[MB_RPT], sm[MB_RPT];
+        MixedRecv q[RPT];
+        FF ax[RPT], ay[RPT], az[RPT];
+        int gi[RPT];
+        bool inr[RPT], sm[RPT];
 #pragma unroll
-        for (int k = 0; k < MB_RPT; k++) {
-            const int l = threadIdx.x + k * MB_THREADS;
+        for (int k = 0; k < RPT; k++) {
+            const int l = threadIdx.x + k * T;
             inr[k] = l < w.z;
             gi[k] = roff[s] + w.y + l;
             sm[k] = true;
@@ -292,10 +289,10 @@ __global__ void __launch_bounds__(MB_THREADS) k_kick_mixed_batched(int nitems, c
             ax[k] = ay[k] = az[k] = FF{0.f, 0.f};
         }
         const int p0 = poff[s];
-        mixed_sweep<TP, RAD, false, MB_RPT>(p0, p0 + npart[s], gi, 0, sm, q, nullptr, nullptr, nullptr, pA, pB, sA,
-                                            sB, ax, ay, az);
+        mixed_sweep<TP, RAD, false, RPT>(p0, p0 + npart[s], gi, 0, sm, q, nullptr, nullptr, nullptr, pA, pB, sA, sB,
+                                         ax, ay, az);
 #pragma unroll
-        for (int k = 0; k < MB_RPT; k++) {
+        for (int k = 0; k < RPT; k++) {
             if (!inr[k]) continue;
             if (!TP || lmask[gi[k]] != 0)
                 mixed_store(&acc[3 * gi[k]], ax[k], ay[k], az[k], acc_is_zero);
@@ -522,43 +519,72 @@ int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, 
     return launch_status(c, "kick_split");
 }
 
-// Persistent batched mixed kick over a work queue of receiver tiles (see
-// k_kick_mixed_batched); pA/pB must hold the split partners.  The queue head is reset
-// on the stream before the launch; the grid is one wave of resident blocks.
-int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *items, const int32_t *roff,
-                       const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
-                       const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
-                       unsigned *head, const int32_t *sys_flag, int phase) {
-    if (nitems <= 0) return SWG_OK;
-    SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
-    static int occ[3] = {0, 0, 0};  // resident blocks per SM of each variant, queried once
-    const int v = tp ? 0 : (rad ? 1 : 2);
-    if (occ[v] == 0) {
+// Tile shapes of the batched mixed kick: (threads per block, receivers per thread).
+struct KickShape {
+    int threads, rpt;
+};
+static constexpr KickShape KICK_SHAPES[KICK_NVARIANT] = {{64, 2}, {128, 1}, {128, 2}, {32, 4}, {64, 4}};
+
+int kick_variant_tile(int variant) { return KICK_SHAPES[variant].threads * KICK_SHAPES[variant].rpt; }
+
+template <bool TP, bool RAD, int T, int RPT>
+static int launch_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *roff, const int32_t *poff,
+                          const int32_t *npart, const double *rrecv, const double *R, const float4 *pA,
+                          const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero, unsigned *head,
+                          const int32_t *sys_flag, int phase) {
+    static int occ = 0;  // resident blocks per SM of this variant, queried once
+    if (occ == 0) {
         int nb = 0;
-        cudaError_t e = tp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_batched<true, false>,
-                                                                           MB_THREADS, 0)
-                           : rad ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                                       &nb, k_kick_mixed_batched<false, true>, MB_THREADS, 0)
-                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                                       &nb, k_kick_mixed_batched<false, false>, MB_THREADS, 0);
-        SWG_TRY(cuda_status(c, e, "occupancy"));
-        occ[v] = nb > 0 ? nb : 1;
+        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_batched<TP, RAD, T, RPT>,
+                                                                             T, 0),
+                            "occupancy"));
+        occ = nb > 0 ? nb : 1;
     }
-    const int grid = std::min(nitems, occ[v] * (c->num_sms > 0 ? c->num_sms : 152));
-    if (tp)
-        k_kick_mixed_batched<true, false><<<grid, MB_THREADS, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
-                                                                          nullptr, pA, pB, lmask, acc, acc_is_zero,
-                                                                          head, sys_flag, phase);
-    else if (rad)
-        k_kick_mixed_batched<false, true><<<grid, MB_THREADS, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R,
-                                                                          pA, pB, nullptr, acc, acc_is_zero, head,
-                                                                          sys_flag, phase);
-    else
-        k_kick_mixed_batched<false, false><<<grid, MB_THREADS, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv,
-                                                                           nullptr, pA, pB, nullptr, acc,
-                                                                           acc_is_zero, head, sys_flag, phase);
+    const int grid = std::min(nitems, occ * (c->num_sms > 0 ? c->num_sms : 152));
+    k_kick_mixed_batched<TP, RAD, T, RPT><<<grid, T, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R, pA,
+                                                                      pB, lmask, acc, acc_is_zero, head, sys_flag,
+                                                                      phase);
     c->launches++;
     return launch_status(c, "kick_mixed_batched");
+}
+
+template <bool TP, bool RAD>
+static int launch_variant(swg_ctx *c, int variant, int nitems, const int4 *items, const int32_t *roff,
+                          const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
+                          const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
+                          unsigned *head, const int32_t *sys_flag, int phase) {
+#define SWG_KV(T, P)                                                                                                  \
+    return launch_batched<TP, RAD, T, P>(c, nitems, items, roff, poff, npart, rrecv, R, pA, pB, lmask, acc,           \
+                                         acc_is_zero, head, sys_flag, phase)
+    switch (variant) {
+        case 0: SWG_KV(64, 2);
+        case 1: SWG_KV(128, 1);
+        case 2: SWG_KV(128, 2);
+        case 3: SWG_KV(32, 4);
+        default: SWG_KV(64, 4);
+    }
+#undef SWG_KV
+}
+
+// Persistent batched mixed kick over a work queue of receiver tiles (see
+// k_kick_mixed_batched); pA/pB must hold the split partners and the items must be tiles of
+// kick_variant_tile(variant) receivers.  The queue head is reset on the stream before the
+// launch; the grid is one wave of resident blocks.
+int kick_mixed_batched(swg_ctx *c, int variant, bool tp, bool rad, int nitems, const int4 *items,
+                       const int32_t *roff, const int32_t *poff, const int32_t *npart, const double *rrecv,
+                       const double *R, const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc,
+                       int acc_is_zero, unsigned *head, const int32_t *sys_flag, int phase) {
+    if (nitems <= 0) return SWG_OK;
+    if (variant < 0 || variant >= KICK_NVARIANT) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
+    if (tp)
+        return launch_variant<true, false>(c, variant, nitems, items, roff, poff, npart, rrecv, nullptr, pA, pB, lmask,
+                                           acc, acc_is_zero, head, sys_flag, phase);
+    if (rad)
+        return launch_variant<false, true>(c, variant, nitems, items, roff, poff, npart, rrecv, R, pA, pB, nullptr,
+                                           acc, acc_is_zero, head, sys_flag, phase);
+    return launch_variant<false, false>(c, variant, nitems, items, roff, poff, npart, rrecv, nullptr, pA, pB, nullptr,
+                                        acc, acc_is_zero, head, sys_flag, phase);
 }
 
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,

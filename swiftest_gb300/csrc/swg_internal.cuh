@@ -155,18 +155,26 @@ int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const 
 // sys_flag/phase (optional, pl-pl): only systems s with sys_flag[s] == phase are processed.
 int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
                       float4 *B, const int32_t *sysid = nullptr, const int32_t *sys_flag = nullptr, int phase = 0);
-int kick_mixed_batched(swg_ctx *c, bool tp, bool rad, int nitems, const int4 *items, const int32_t *roff,
-                       const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
-                       const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
-                       unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
+// variant: tile shape of the batched mixed kick (0 .. KICK_NVARIANT-1; identical results),
+// whose items are tiles of kick_variant_tile(variant) receivers.
+constexpr int KICK_NVARIANT = SWG_KICK_NVARIANT;
+int kick_variant_tile(int variant);
+int kick_mixed_batched(swg_ctx *c, int variant, bool tp, bool rad, int nitems, const int4 *items,
+                       const int32_t *roff, const int32_t *poff, const int32_t *npart, const double *rrecv,
+                       const double *R, const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc,
+                       int acc_is_zero, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
 int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const double *r, const double *Gm, const double *R, double *acc,
                            int acc_is_zero, const int32_t *sys_flag = nullptr, int phase = 0);
 int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
                          const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
                          const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
+// autotune.cu -- cache of tuned kernel shapes: key of (device, kind, size bucket); the cached
+// variant or -1; store (kept for the process and appended to the cache file)
+std::string tune_key(int device, const char *kind, int bucket);
+int tune_lookup(const std::string &key);
+void tune_store(const std::string &key, int variant);
 // receivers per item of the batched kernels
-constexpr int KICK_MIXED_TILE = 128;
 constexpr int KICK_FP64_TILE = 8;
 constexpr int ENC_TILE = 128;
 constexpr int ENC_SORTED_TILE = 128;  // receivers per item of the radius-sorted pl-pl check

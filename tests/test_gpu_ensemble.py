@@ -155,3 +155,26 @@ def test_helio_ensemble_graph_replay_matches_eager(ctx):
         ens.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+def test_mixed_kick_shapes_identical(ctx):
+    # every tile shape of the batched mixed kick gives the same bits (pl-pl with the
+    # radius guard and pl-tp, systems of uneven sizes spanning several tiles); the
+    # autotuned choice is one of them
+    E = IC.make_ensemble("C4", nsys=5, scale=0.15, tp_per_pl=1)
+    out = []
+    for v in list(range(5)) + [-1]:
+        ens = Ensemble(ctx, E, precision="MIXED", dt=0.005, rhscale=3.0)
+        ens.set_kick_variant(v)
+        assert ens.kick_variant() == {"pl": -1, "tp": -1}
+        ens.step(20)
+        kv = ens.kick_variant()
+        if v >= 0:
+            assert kv == {"pl": v, "tp": v}
+        else:
+            assert 0 <= kv["pl"] < 5 and 0 <= kv["tp"] < 5
+        out.append(ens.get_pl() + ens.get_tp())
+        ens.close()
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            assert np.array_equal(a, b)
