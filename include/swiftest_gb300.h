@@ -192,15 +192,23 @@ int swg_ensemble_get_state_async(swg_ensemble *ens, double *rh, double *vh, doub
  * on; results are identical either way).  SyMBA steps always run eagerly: each takes one
  * host decision (the encounter-list sizes). */
 int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
-/* Tile shape of the batched mixed-precision kick (no counterpart in the reference).
- * Every shape gives bit-identical accelerations; by default (variant -1) each kick kind
- * takes the fastest shape for its GPU and mean system size, timed on the ensemble's own
- * data at its first kick and cached in $SWG_TUNE_CACHE, else
- * $HOME/.cache/swiftest_gb300/kick_tune.txt.  0 .. SWG_KICK_NVARIANT-1 forces a shape.
- * kick_variant reads the shape in use for kind 0 (pl-pl) or 1 (pl-tp), -1 before the
- * first mixed kick of that kind. */
+/* Kernel of the batched mixed-precision kick (no counterpart in the reference).  By
+ * default (variant -1) the pl-pl kick evaluates each pair once for both bodies
+ * (SWG_KICK_SYMMETRIC) and the pl-tp kick takes the fastest of SWG_KICK_NVARIANT tile
+ * shapes of the receiver-broadcast kernel for its GPU and mean system size, timed on the
+ * ensemble's own data at its first kick and cached in $SWG_TUNE_CACHE, else
+ * $HOME/.cache/swiftest_gb300/kick_tune.txt.  Every broadcast shape gives bit-identical
+ * accelerations; the symmetric kernel adds the same terms in another order.  Variants
+ * 0 .. SWG_KICK_NVARIANT-1 force that broadcast shape on both kinds.  kick_variant reads
+ * the kernel in use for kind 0 (pl-pl) or 1 (pl-tp), -1 before the first mixed kick of
+ * that kind. */
 #define SWG_KICK_NVARIANT 5
+#define SWG_KICK_SYMMETRIC 5
 int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
+/* swiftest_kick_getacch_int_all_tri_pl (swiftest_kick.f90:183-264) of every system from its
+ * current positions, in the ensemble's precision and pair rule (radius guard for SyMBA or
+ * with close-encounter checks): acc[3*NPL] on the host, zero-based sums over all pairs. */
+int swg_ensemble_getacch_int_pl(swg_ensemble *ens, double *acc);
 int swg_ensemble_kick_variant(swg_ensemble *ens, int kind, int *variant);
 int swg_ensemble_profile(swg_ensemble *ens, int enable);
 int swg_ensemble_profile_read(swg_ensemble *ens, double *out);

@@ -24,6 +24,7 @@ SWG_MEM_DEVICE = 1
 SWG_FP64 = 0
 SWG_MIXED = 1
 SWG_KICK_NVARIANT = 5
+SWG_KICK_SYMMETRIC = 5
 SWG_ENC_TRIANGULAR = 0
 SWG_ENC_SORTSWEEP = 1
 SWG_WHM = 0
@@ -89,6 +90,7 @@ SIGNATURES = {
     "swg_ensemble_use_graphs": (_INT, [_P, _INT]),
     "swg_ensemble_set_kick_variant": (_INT, [_P, _INT]),
     "swg_ensemble_kick_variant": (_INT, [_P, _INT, C.POINTER(_INT)]),
+    "swg_ensemble_getacch_int_pl": (_INT, [_P, _P]),
     "swg_ensemble_profile": (_INT, [_P, _INT]),
     "swg_ensemble_profile_read": (_INT, [_P, _P]),
     "swg_flush_l2": (_INT, [_P, _I64]),

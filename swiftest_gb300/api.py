@@ -404,11 +404,19 @@ class Ensemble:
         self.ctx.check("swg_ensemble_use_graphs", self.ctx.lib.swg_ensemble_use_graphs(self.h, int(bool(enable))))
 
     def set_kick_variant(self, variant: int = -1):
-        """Force the mixed kick's tile shape (0 .. SWG_KICK_NVARIANT-1) or autotune it (-1)."""
+        """Force a broadcast tile shape (0 .. SWG_KICK_NVARIANT-1) on both mixed kicks, or
+        use the default (-1): symmetric pl-pl kernel, autotuned pl-tp shape."""
         self.ctx.check("swg_ensemble_set_kick_variant", self.ctx.lib.swg_ensemble_set_kick_variant(self.h, int(variant)))
 
+    def getacch_int_pl(self):
+        """Pair accelerations of every system's massive bodies from the current positions."""
+        out = np.zeros((int(self.poff[-1]), 3))
+        self.ctx.check("swg_ensemble_getacch_int_pl", self.ctx.lib.swg_ensemble_getacch_int_pl(self.h, _ptr(out)))
+        return out
+
     def kick_variant(self):
-        """Tile shapes in use by the mixed pl-pl and pl-tp kicks (-1: not chosen yet)."""
+        """Kernels in use by the mixed pl-pl and pl-tp kicks: a broadcast tile shape,
+        SWG_KICK_SYMMETRIC, or -1 before the first mixed kick of that kind."""
         out = []
         for kind in (0, 1):
             v = C.c_int(-1)

@@ -90,6 +90,11 @@ struct swg_ensemble {
     int kv[2] = {-1, -1}, n_kit[2] = {0, 0};
     int4 *kit[2] = {nullptr, nullptr};
     int force_variant = -1;
+    // symmetric pl-pl mixed kick (the default): tile-pair items, each system's first slot, slot sums
+    int4 *it_sym = nullptr;
+    int n_sym = 0;
+    int32_t *sym_base = nullptr;
+    float *sym_part = nullptr;
     unsigned *head = nullptr;
     // encounter lists: [i1 | i2 | lvdotr | status | level] * cap, global 1-based indices
     int32_t *pp_l = nullptr, *pt_l = nullptr;
@@ -520,6 +525,19 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
         return SWG_ERR_STATE;
     }
     int v = e->force_variant;
+    if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel (built once)
+        if (!e->it_sym) {
+            std::vector<int4> items;
+            std::vector<int32_t> base;
+            const int64_t nslot = kick_sym_items(e->nsys, e->h_npl.data(), items, base);
+            SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
+            SWG_TRY(dalloc(c, &e->sym_base, base.size()));
+            SWG_TRY(upload(c, e->sym_base, base));
+            SWG_TRY(dalloc(c, &e->sym_part, (size_t)nslot * 12 * KICK_SYM_TILE));
+        }
+        e->kv[0] = KICK_SYMMETRIC;
+        return SWG_OK;
+    }
     if (v < 0) {
         const std::string key =
             tune_key(c->device, k == 0 ? (rad ? "kick_pl_rad" : "kick_pl") : "kick_tp", size_bucket(e, k));
@@ -551,6 +569,12 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
     if (e->precision == SWG_MIXED) {
         SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB, flag ? e->psys : nullptr, flag, phase));
         SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
+        if (e->kv[0] == KICK_SYMMETRIC) {
+            SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->kA, e->kB, e->sym_part,
+                                           head, flag, phase));
+            return kick_mixed_sym_reduce(c, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part, e->ah, 1, flag,
+                                         phase);
+        }
         return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase);
     }
     return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah, 1, flag,
@@ -1111,7 +1135,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
                     e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
                     e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->eS, e->perm, e->tbase,
-                    e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1],
+                    e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
                     e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->eout};
@@ -1383,6 +1407,16 @@ int swg_ensemble_use_graphs(swg_ensemble *e, int enable) {
     if (!e) return SWG_ERR_ARG;
     e->use_graph = enable != 0;
     return SWG_OK;
+}
+
+int swg_ensemble_getacch_int_pl(swg_ensemble *e, double *acc) {
+    if (!e || !acc) return SWG_ERR_ARG;
+    if (e->NPL == 0) return SWG_OK;
+    swg_ctx *c = e->c;
+    SWG_TRY(accel_int_pl(e, e->head));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(acc, e->ah, sizeof(double) * 3 * e->NPL, cudaMemcpyDeviceToHost, c->stream),
+                        "getacch"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "getacch");
 }
 
 int swg_ensemble_set_kick_variant(swg_ensemble *e, int variant) {

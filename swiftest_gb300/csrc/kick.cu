@@ -25,64 +25,12 @@
 
 #include <algorithm>
 
+#include "kick_mixed.cuh"
 #include "swg_internal.cuh"
 
 namespace swg {
 
-constexpr int MT = 64;        // partners per FP32 partial (mixed)
 constexpr int MBLOCK = 128;   // threads per block (mixed, one system)
-
-// ------------------------------------------------------------------ mixed
-struct FF {
-    float hi, lo;
-};
-__device__ __forceinline__ void ff_add(FF &a, float p) {
-    // TwoSum (Knuth): exact error of hi + p, folded into lo.
-    const float s = a.hi + p;
-    const float bp = s - a.hi;
-    const float err = (a.hi - (s - bp)) + (p - bp);
-    a.hi = s;
-    a.lo = a.lo + err;
-}
-
-__device__ __forceinline__ void split_hi_lo(double x, float &hi, float &lo) {
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(x - (double)hi);
-}
-
-// One receiving body of the mixed kick: its coordinates split into float hi/lo.
-struct MixedRecv {
-    float xh, yh, zh, xl, yl, zl, R;
-};
-
-template <bool RAD>
-__device__ __forceinline__ MixedRecv mixed_recv(const double *__restrict__ r, const double *__restrict__ R, int i) {
-    MixedRecv q;
-    split_hi_lo(r[3 * i + 0], q.xh, q.xl);
-    split_hi_lo(r[3 * i + 1], q.yh, q.yl);
-    split_hi_lo(r[3 * i + 2], q.zh, q.zl);
-    q.R = RAD ? __double2float_rn(R[i]) : 0.f;
-    return q;
-}
-
-// Hardware reciprocal square root estimate (one MUFU instruction, subnormals flushed):
-// r^2 of two distinct bodies is never subnormal, and a zero r^2 (a body paired with
-// itself) gives +inf, which the pair rule replaces by a zero factor.
-__device__ __forceinline__ float rsqrt_approx(float x) {
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// r^-3 in FP32: the hardware estimate y0 refined by one Newton step applied to the cube.
-// With e = 1 - r2 y0^2 the Newton iterate is y1 = y0 (1 + e/2), and
-// y1^3 = y0^3 (1 + 3e/2) + O(e^2) = y0^3 (2.5 - 1.5 r2 y0^2); e ~ 1e-7, so the dropped
-// terms are ~1e-14 relative.
-__device__ __forceinline__ float rinv3(float r2) {
-    const float y = rsqrt_approx(r2);
-    const float t = y * y;
-    return (t * y) * fmaf(-1.5f, r2 * t, 2.5f);
-}
 
 // Sweep of partners [jbeg, jstop) (indices into the partner arrays) for this thread's RPT
 // receivers, whole block: 64-partner FP32 partials folded into float-float (ax, ay, az).
@@ -91,15 +39,24 @@ __device__ __forceinline__ float rinv3(float r2) {
 // Pair rule (pl-pl; TP has none): the reference skips j == i and, with GMTINY bodies,
 // pairs of two bodies both at index >= nplm (GMT); with RAD it also skips pairs closer
 // than the sum of the radii, which covers j == i (r^2 == 0 exactly), so the index test
-// is only made without RAD.  self[k] is receiver k's index in the partner arrays.
+// is only made without RAD.  self[k] is receiver k's index in the partner arrays; every
+// receiver of the block lies in [slo, shi).
+// The rule is applied pair by pair only on tiles that can need it: tiles holding one of
+// the block's own receivers (the self pairs) and, with GMT, every tile.  On the others
+// the pairs are taken unguarded and, with RAD, a receiver whose closest partner in the
+// tile lies within its radius plus the tile's largest radius recomputes that tile with
+// the rule.  A pair the rule keeps gets the same operations either way, so the partials
+// are the same bits as with the rule applied everywhere.
 template <bool TP, bool RAD, bool GMT, int RPT>
-__device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&self)[RPT], int nplm,
+__device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&self)[RPT], int slo, int shi, int nplm,
                                             const bool (&self_m)[RPT], const MixedRecv (&q)[RPT],
                                             const double *__restrict__ rpart, const double *__restrict__ Gm,
                                             const double *__restrict__ R, const float4 *__restrict__ pA,
                                             const float4 *__restrict__ pB, float4 *sA, float4 *sB, FF (&ax)[RPT],
                                             FF (&ay)[RPT], FF (&az)[RPT]) {
+    __shared__ unsigned sRmax[2];  // largest partner radius of the tile, per loading warp (float bits)
     for (int j0 = jbeg; j0 < jstop; j0 += MT) {
+        float rmax = 0.f;
         for (int t = threadIdx.x; t < MT; t += blockDim.x) {
             const int jl = j0 + t;
             float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -115,38 +72,38 @@ __device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&sel
             }
             sA[t] = a;
             sB[t] = b;
+            rmax = fmaxf(rmax, b.w);
+        }
+        if (!TP && RAD && threadIdx.x < MT) {  // whole warps: blockDim.x is a multiple of 32
+            const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(rmax));  // radii are >= 0
+            if ((threadIdx.x & 31) == 0) {
+                sRmax[threadIdx.x >> 5] = m;
+                if (blockDim.x == 32) sRmax[1] = 0u;
+            }
         }
         __syncthreads();
         const int nt = min(MT, jstop - j0);
-        float px[RPT], py[RPT], pz[RPT];
+        float px[RPT], py[RPT], pz[RPT], mn[RPT];
+        const bool guard = !TP && (GMT || (j0 < shi && j0 + nt > slo));  // block-uniform
+        if (guard) {
+            mixed_tile<TP, RAD, GMT, true, RPT>(j0, nt, self, nplm, self_m, q, sA, sB, px, py, pz, mn);
+        } else {
 #pragma unroll
-        for (int k = 0; k < RPT; k++) px[k] = py[k] = pz[k] = 0.f;
-#pragma unroll 8
-        for (int jj = 0; jj < nt; jj++) {
-            const float4 a = sA[jj];
-            const float4 b = sB[jj];
+            for (int k = 0; k < RPT; k++) mn[k] = 3.0e38f;
+            mixed_tile<TP, RAD, GMT, false, RPT>(j0, nt, self, nplm, self_m, q, sA, sB, px, py, pz, mn);
+            if (!TP && RAD) {
+                const float rt = fmaxf(__uint_as_float(sRmax[0]), __uint_as_float(sRmax[1]));
 #pragma unroll
-            for (int k = 0; k < RPT; k++) {
-                const float dx = (a.x - q[k].xh) + (b.x - q[k].xl);
-                const float dy = (a.y - q[k].yh) + (b.y - q[k].yl);
-                const float dz = (a.z - q[k].zh) + (b.z - q[k].zl);
-                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                float fac = a.w * rinv3(r2);
-                if (!TP) {
-                    const int j = j0 + jj;
-                    bool ok = true;
-                    if (GMT) ok = self_m[k] || j < nplm;
-                    if (RAD) {
-                        const float rs = q[k].R + b.w;
-                        ok = ok && (r2 > rs * rs);
-                    } else {
-                        ok = ok && (j != self[k]);
+                for (int k = 0; k < RPT; k++) {
+                    const float rs = q[k].R + rt;
+                    if (mn[k] <= rs * rs) {  // rare: a pair of this tile may lie within the radii
+                        float gx[RPT], gy[RPT], gz[RPT], gm[RPT];
+                        mixed_tile<TP, RAD, GMT, true, RPT>(j0, nt, self, nplm, self_m, q, sA, sB, gx, gy, gz, gm);
+                        px[k] = gx[k];
+                        py[k] = gy[k];
+                        pz[k] = gz[k];
                     }
-                    fac = ok ? fac : 0.f;
                 }
-                px[k] = fmaf(fac, dx, px[k]);
-                py[k] = fmaf(fac, dy, py[k]);
-                pz[k] = fmaf(fac, dz, pz[k]);
             }
         }
 #pragma unroll
@@ -193,7 +150,9 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
     const int jstop = min(npart, jbeg + chunk);
     const int self[1] = {i};
     const bool self_m[1] = {i < nplm};
-    mixed_sweep<TP, RAD, GMT, 1>(jbeg, jstop, self, nplm, self_m, q, rpart, Gm, R, pA, pB, sA, sB, axa, aya, aza);
+    const int slo = blockIdx.x * MBLOCK;
+    mixed_sweep<TP, RAD, GMT, 1>(jbeg, jstop, self, slo, slo + MBLOCK, nplm, self_m, q, rpart, Gm, R, pA, pB, sA, sB,
+                                 axa, aya, aza);
     const FF ax = axa[0], ay = aya[0], az = aza[0];
     const int nchunk = gridDim.y;
     if (nchunk == 1) {
@@ -289,7 +248,9 @@ __global__ void __launch_bounds__(T) k_kick_mixed_batched(int nitems, const int4
             ax[k] = ay[k] = az[k] = FF{0.f, 0.f};
         }
         const int p0 = poff[s];
-        mixed_sweep<TP, RAD, false, RPT>(p0, p0 + npart[s], gi, 0, sm, q, nullptr, nullptr, nullptr, pA, pB, sA, sB,
+        const int slo = roff[s] + w.y;  // receivers in partner indexing (pl-pl: roff == poff)
+        mixed_sweep<TP, RAD, false, RPT>(p0, p0 + npart[s], gi, slo, slo + w.z, 0, sm, q, nullptr, nullptr, nullptr, pA,
+                                         pB, sA, sB,
                                          ax, ay, az);
 #pragma unroll
         for (int k = 0; k < RPT; k++) {

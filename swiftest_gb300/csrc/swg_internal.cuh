@@ -158,6 +158,7 @@ int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, 
 // variant: tile shape of the batched mixed kick (0 .. KICK_NVARIANT-1; identical results),
 // whose items are tiles of kick_variant_tile(variant) receivers.
 constexpr int KICK_NVARIANT = SWG_KICK_NVARIANT;
+constexpr int KICK_SYMMETRIC = SWG_KICK_SYMMETRIC;  // the symmetric pl-pl kernel (kick_sym.cu)
 int kick_variant_tile(int variant);
 int kick_mixed_batched(swg_ctx *c, int variant, bool tp, bool rad, int nitems, const int4 *items,
                        const int32_t *roff, const int32_t *poff, const int32_t *npart, const double *rrecv,
@@ -169,6 +170,18 @@ int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, 
 int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
                          const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
                          const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
+// kick_sym.cu -- symmetric mixed pl-pl kick (each pair once, applied to both bodies) over
+// tile pairs of KICK_SYM_TILE bodies.  kick_sym_items builds the items (system, I, J, slot)
+// sorted by cost and each system's first slot; returns the number of slots.  part holds
+// 12 * KICK_SYM_TILE floats per slot; kick_mixed_sym_reduce writes acc (+)= the sums.
+constexpr int KICK_SYM_TILE = 128;
+int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase);
+int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
+                           const int32_t *npl, const float4 *pA, const float4 *pB, float *part, unsigned *head,
+                           const int32_t *sys_flag = nullptr, int phase = 0);
+int kick_mixed_sym_reduce(swg_ctx *c, int64_t n, const int32_t *psys, const int32_t *poff, const int32_t *npl,
+                          const int32_t *sbase, const float *part, double *acc, int acc_is_zero,
+                          const int32_t *sys_flag = nullptr, int phase = 0);
 // autotune.cu -- cache of tuned kernel shapes: key of (device, kind, size bucket); the cached
 // variant or -1; store (kept for the process and appended to the cache file)
 std::string tune_key(int device, const char *kind, int bucket);

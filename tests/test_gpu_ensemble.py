@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from swiftest_gb300 import _lib as L
 from swiftest_gb300 import initial_conditions as IC
 from swiftest_gb300.api import Ensemble
 
@@ -158,9 +159,9 @@ def test_helio_ensemble_graph_replay_matches_eager(ctx):
 
 
 def test_mixed_kick_shapes_identical(ctx):
-    # every tile shape of the batched mixed kick gives the same bits (pl-pl with the
-    # radius guard and pl-tp, systems of uneven sizes spanning several tiles); the
-    # autotuned choice is one of them
+    # every broadcast tile shape of the batched mixed kick gives the same bits (pl-pl with
+    # the radius guard and pl-tp, systems of uneven sizes spanning several tiles); the
+    # default runs the symmetric pl-pl kernel and an autotuned pl-tp shape
     E = IC.make_ensemble("C4", nsys=5, scale=0.15, tp_per_pl=1)
     out = []
     for v in list(range(5)) + [-1]:
@@ -172,9 +173,53 @@ def test_mixed_kick_shapes_identical(ctx):
         if v >= 0:
             assert kv == {"pl": v, "tp": v}
         else:
-            assert 0 <= kv["pl"] < 5 and 0 <= kv["tp"] < 5
+            assert kv["pl"] == L.SWG_KICK_SYMMETRIC and 0 <= kv["tp"] < 5
         out.append(ens.get_pl() + ens.get_tp())
         ens.close()
-    for other in out[1:]:
+    for other in out[1:5]:
         for a, b in zip(out[0], other):
             assert np.array_equal(a, b)
+    for a, b in zip(out[0][:2], out[5][:2]):  # pl rh, vh: the same sums in another order
+        rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(a, axis=1)
+        assert rel.max() < 1e-9, rel.max()
+
+
+def _pack(E, systems):
+    # the ensemble dict of E with its systems replaced
+    E = dict(E)
+    E["systems"] = systems
+    E["npl"] = np.array([len(pl["Gmass"]) for pl, _ in systems], np.int32)
+    E["ntp"] = np.array([len(tp["rh"]) for _, tp in systems], np.int32)
+    E["pl"] = {k: np.concatenate([pl[k] for pl, _ in systems]) for k in ("rh", "vh", "Gmass", "radius", "rhill")}
+    E["tp"] = {k: np.concatenate([tp[k] for _, tp in systems]) for k in ("rh", "vh")}
+    return E
+
+
+@pytest.mark.parametrize("integrator,lclose", [("SYMBA", True), ("HELIO", False)])
+def test_ensemble_getacch_mixed_tolerance(ctx, integrator, lclose):
+    # pair accelerations of every system (symmetric and broadcast kernels) against the oracle's
+    # FP64 triangular kick; systems of 2 to ~700 bodies, tiles partly filled, an overlapping pair
+    E = IC.make_ensemble("C4", nsys=6, scale=0.3)
+    E["integrator"] = integrator
+    sysl = [({k: v.copy() for k, v in pl.items()}, tp) for pl, tp in E["systems"]]
+    pl1 = sysl[1][0]  # 279 bodies: pairs within the radii inside a tile and across tiles
+    for i, j in [(3, 7), (20, 270), (150, 100)]:
+        pl1["rh"][j] = pl1["rh"][i] + 1e-6 * np.array([0.6, -0.48, 0.64])
+        pl1["radius"][[i, j]] = 1e-5
+    sysl[2] = ({k: v[:2].copy() for k, v in sysl[2][0].items()}, sysl[2][1])
+    E = _pack(E, sysl)
+    rad = integrator == "SYMBA" or lclose
+    want = [O.kick_tri_pl(pl["rh"], pl["Gmass"], pl["radius"] if rad else None) for pl, _ in sysl]
+    for v in (-1, 1):
+        ens = Ensemble(ctx, E, precision="MIXED", dt=0.005, lclose=lclose)
+        ens.set_kick_variant(v)
+        g = ens.getacch_int_pl()
+        for s, r in enumerate(want):
+            a, b = ens.poff[s], ens.poff[s + 1]
+            e = np.linalg.norm(g[a:b] - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
+            # FP32 pair terms with float-float partial sums: 2e-5 max, 1e-6 RMS per body
+            assert e.max() < 2e-5, (v, s, e.max())
+            assert np.sqrt(np.mean(e ** 2)) < 1e-6, (v, s)
+        g2 = ens.getacch_int_pl()
+        assert np.array_equal(g, g2)  # deterministic
+        ens.close()

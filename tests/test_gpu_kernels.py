@@ -87,6 +87,30 @@ def test_kick_mixed_tp_tolerance(ctx, ntp, npl):
     assert np.sqrt(np.mean(e ** 2)) < 1e-6
 
 
+@pytest.mark.parametrize("guard", ["radius", "index"])
+def test_kick_mixed_close_and_overlapping_pairs(ctx, guard):
+    # bodies placed next to others in distant tiles: pairs within the sum of the radii are
+    # dropped by the radius rule, a close pair just outside it is kept and dominates
+    cb, pl, _ = _sys(12, 1000, 0)
+    rh, R = pl["rh"].copy(), pl["radius"].copy()
+    u = np.array([0.6, -0.48, 0.64])
+    for i, j, sep in [(5, 700, 1e-6), (300, 950, 1e-6), (513, 2, 3e-6), (140, 260, 1e-4)]:
+        rh[j] = rh[i] + sep * u
+        R[i] = R[j] = 1e-5
+    Rk = R if guard == "radius" else None
+    g = ctx.kick_getacch_int_all_tri_pl(rh, pl["Gmass"], Rk, precision=SWG_MIXED)
+    r = O.kick_tri_pl(rh, pl["Gmass"], Rk)
+    e = _relerr(g, r)
+    assert np.all(np.isfinite(g))
+    if guard == "radius":
+        assert e.max() < 2e-5, e.max()
+    else:  # without the radius rule the 1e-6 pairs are kept: FP32 r^-3 of a 1e-6 separation
+        keep = np.ones(len(e), bool)
+        keep[[5, 700, 300, 950, 513, 2]] = False
+        assert e[keep].max() < 2e-5, e[keep].max()
+        assert e[~keep].max() < 1e-3, e[~keep].max()
+
+
 def test_kick_mixed_deterministic(ctx):
     cb, pl, tp = _sys(10, 3000, 0)
     a = ctx.kick_getacch_int_all_tri_pl(pl["rh"], pl["Gmass"], pl["radius"], precision=SWG_MIXED)
