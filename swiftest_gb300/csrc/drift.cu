@@ -72,6 +72,8 @@ __global__ void __launch_bounds__(128) k_drift_all(const double *__restrict__ mu
 // levelg == irec (levelg == nullptr: every body with status /= INACTIVE);
 // failures set status = DISCARDED_DRIFTERR and are counted in *nfail.
 // mu_sys/sys (optional): the body's own system's central-body mu (CSR-packed ensembles).
+// FAST: the fast FP64 form of the solver (mixed-precision path, see drift_impl.cuh).
+template <bool FAST>
 __global__ void __launch_bounds__(128) k_drift_masked(double mu, double *x, double *v, int n,
                                                       const int32_t *__restrict__ levelg, int irec, double dt,
                                                       int32_t *__restrict__ status, int32_t *nfail,
@@ -84,7 +86,7 @@ __global__ void __launch_bounds__(128) k_drift_masked(double mu, double *x, doub
     double rx = x[3 * i], ry = x[3 * i + 1], rz = x[3 * i + 2];
     double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
     const double m = mu_sys ? mu_sys[sys[i]] : mu;
-    const int fl = d_drift_one(m, rx, ry, rz, vx, vy, vz, dt);
+    const int fl = FAST ? d_drift_one_fast(m, rx, ry, rz, vx, vy, vz, dt) : d_drift_one(m, rx, ry, rz, vx, vy, vz, dt);
     x[3 * i] = rx;
     x[3 * i + 1] = ry;
     x[3 * i + 2] = rz;
@@ -106,10 +108,14 @@ int drift_all(swg_ctx *c, const double *mu, double mu_scalar, double *x, double 
 }
 
 int drift_masked(swg_ctx *c, double mu, double *x, double *v, int32_t n, const int32_t *levelg, int irec, double dt,
-                 int32_t *status, int32_t *nfail, const double *mu_sys, const int32_t *sys) {
+                 int32_t *status, int32_t *nfail, const double *mu_sys, const int32_t *sys, bool fast) {
     if (n <= 0) return SWG_OK;
-    k_drift_masked<<<(n + 127) / 128, 128, 0, c->stream>>>(mu, x, v, n, levelg, irec, dt, status, nfail, mu_sys,
-                                                           sys);
+    if (fast)
+        k_drift_masked<true><<<(n + 127) / 128, 128, 0, c->stream>>>(mu, x, v, n, levelg, irec, dt, status, nfail,
+                                                                     mu_sys, sys);
+    else
+        k_drift_masked<false><<<(n + 127) / 128, 128, 0, c->stream>>>(mu, x, v, n, levelg, irec, dt, status, nfail,
+                                                                      mu_sys, sys);
     c->launches++;
     return launch_status(c, "drift_masked");
 }

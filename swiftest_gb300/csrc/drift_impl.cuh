@@ -282,4 +282,104 @@ __device__ inline int d_drift_one(double mu, double &rx, double &ry, double &rz,
     return iflag;
 }
 
+// ------------------------------------------------------------------ fast FP64 form
+// The same Danby drift, still entirely in FP64, for the mixed-precision path: where the
+// reference divides by the same quantity several times (r0, mu, alpha, en, fp) the fast
+// form takes one reciprocal (or reciprocal square root) and multiplies, contracts
+// products into FMAs, and folds the constant divisors.  On GB300 each FP64 divide or
+// square root is a multi-instruction sequence on the narrow FP64 pipe, so this roughly
+// halves the drift's FP64 work.  Results agree with the reference form to a few units
+// in the last place; the universal-variable branch (large steps or eccentric orbits) is
+// the reference form unchanged.
+__device__ inline void d_kepmd_fast(double dm, double es, double ec, double &x, double &s, double &c) {
+    const double a0 = 39916800.0, a1 = 6652800.0, a2 = 332640.0, a3 = 7920.0, a4 = 110.0;
+    const double inv_a0 = 1.0 / 39916800.0;
+    const double fac1 = 1.0 / (1.0 - ec);
+    const double q = fac1 * dm;
+    const double fac2 = fma(es * es, fac1, -ec * THIRD);
+    double xx = q * (1.0 - 0.5 * fac1 * q * fma(-q, fac2, es));
+    double y = xx * xx;
+    double ss = xx * fma(-y, fma(-y, fma(-y, fma(-y, a4 - y, a3), a2), a1), a0) * inv_a0;
+    double cc = sqrt(fma(-ss, ss, 1.0));
+    const double f = fma(es, 1.0 - cc, fma(-ec, ss, xx)) - dm;
+    const double fp = fma(es, ss, fma(-ec, cc, 1.0));
+    const double fpp = fma(ec, ss, es * cc);
+    const double fppp = fma(ec, cc, -es * ss);
+    double dx = -(f / fp);
+    dx = -(f / fma(dx * fpp, 0.5, fp));
+    dx = -(f / fma(dx * dx * fppp, SIXTH, fma(dx * fpp, 0.5, fp)));
+    xx = xx + dx;
+    y = xx * xx;
+    ss = xx * fma(-y, fma(-y, fma(-y, fma(-y, a4 - y, a3), a2), a1), a0) * inv_a0;
+    cc = sqrt(fma(-ss, ss, 1.0));
+    x = xx;
+    s = ss;
+    c = cc;
+}
+
+__device__ inline void d_drift_dan_fast(double mu, double &rx0, double &ry0, double &rz0, double &vx0, double &vy0,
+                                        double &vz0, double dt0, int &iflag) {
+    iflag = 0;
+    const double r2 = fma(rz0, rz0, fma(ry0, ry0, rx0 * rx0));
+    const double inv_r0 = rsqrt(r2);
+    const double v0s = fma(vz0, vz0, fma(vy0, vy0, vx0 * vx0));
+    const double u = fma(rz0, vz0, fma(ry0, vy0, rx0 * vx0));
+    const double alpha = fma(2.0 * mu, inv_r0, -v0s);
+    if (alpha > 0.0) {
+        const double inv_mu = 1.0 / mu;
+        const double rsa = rsqrt(alpha);
+        const double a = mu * rsa * rsa;                 // mu / alpha
+        const double ia = alpha * inv_mu;                // 1 / a
+        const double en = alpha * (alpha * rsa) * inv_mu;  // sqrt(mu / a^3)
+        const double inv_en = mu * (rsa * rsa * rsa);
+        const double ec = fma(-(r2 * inv_r0), ia, 1.0);
+        const double es = u * inv_en * ia * ia;
+        const double esq = fma(ec, ec, es * es);
+        const double den = dt0 * en;
+        const double dm = fma(-(double)(int)(den * (1.0 / TWOPI)), TWOPI, den);
+        if ((esq < E2MAX) && (dm * dm < DM2MAX) && (esq * (dm * dm) < E2DM2MAX)) {
+            const double dt = dm * inv_en;
+            double xkep, s, c;
+            d_kepmd_fast(dm, es, ec, xkep, s, c);
+            const double fchk = fma(es, 1.0 - c, fma(-ec, s, xkep)) - dm;
+            if (fchk * fchk > DANBYB * DANBYB) {
+                iflag = 1;
+                return;
+            }
+            const double fp = fma(es, s, fma(-ec, c, 1.0));
+            const double inv_fp = 1.0 / fp;
+            const double ar = a * inv_r0;
+            const double f = fma(ar, c - 1.0, 1.0);
+            const double g = fma(s - xkep, inv_en, dt);
+            const double fdot = -(ar * inv_fp * en * s);
+            const double gdot = fma(c - 1.0, inv_fp, 1.0);
+            const double rx = fma(rx0, f, vx0 * g), ry = fma(ry0, f, vy0 * g), rz = fma(rz0, f, vz0 * g);
+            const double vx = fma(rx0, fdot, vx0 * gdot), vy = fma(ry0, fdot, vy0 * gdot),
+                         vz = fma(rz0, fdot, vz0 * gdot);
+            rx0 = rx;
+            ry0 = ry;
+            rz0 = rz;
+            vx0 = vx;
+            vy0 = vy;
+            vz0 = vz;
+            return;
+        }
+    }
+    d_drift_dan(mu, rx0, ry0, rz0, vx0, vy0, vz0, dt0, iflag);  // universal variables: the reference form
+}
+
+__device__ inline int d_drift_one_fast(double mu, double &rx, double &ry, double &rz, double &vx, double &vy,
+                                       double &vz, double dt) {
+    int iflag;
+    d_drift_dan_fast(mu, rx, ry, rz, vx, vy, vz, dt, iflag);
+    if (iflag != 0) {
+        const double dttmp = 0.1 * dt;
+        for (int i = 1; i <= 10; i++) {
+            d_drift_dan_fast(mu, rx, ry, rz, vx, vy, vz, dttmp, iflag);
+            if (iflag != 0) break;
+        }
+    }
+    return iflag;
+}
+
 }  // namespace swg

@@ -94,7 +94,7 @@ struct swg_ensemble {
     int4 *it_sym = nullptr;
     int n_sym = 0;
     int32_t *sym_base = nullptr;
-    float *sym_part = nullptr;
+    float *sym_part = nullptr, *sym_ppart = nullptr;  // receiver slots, then pair slots (one allocation)
     unsigned *head = nullptr;
     // encounter lists: [i1 | i2 | lvdotr | status | level] * cap, global 1-based indices
     int32_t *pp_l = nullptr, *pt_l = nullptr;
@@ -105,6 +105,7 @@ struct swg_ensemble {
     int32_t *tflag = nullptr;                // tp flagged by the close-approach scan
     unsigned long long *ndiscard = nullptr;  // tp removed by the scan
     DevBuf rec_scratch, rows;
+    DevBuf pair_terms;  // pl-pl pool: six pair terms and a kept flag per entry
     double *eout = nullptr;      // 9 per system
     int32_t *h_flags = nullptr;  // pinned: [2] recursion status; +8: two unsigned long long counts
     std::vector<int32_t> h_pend;  // per-system pause flags read after a recursion launch
@@ -153,9 +154,13 @@ int upload(swg_ctx *c, T *dst, const std::vector<T> &src) {
 }
 
 // ---------------------------------------------------------------- kernels
+// threads per system of the per-system sums: a system has a few thousand bodies at most
+// and several systems share an SM, so small blocks keep the reduction trees short
+constexpr int ENS_SUM_T = 256;
+
 // one block per system: swiftest_util_coord_vh2vb_pl (only systems whose first-step
 // flag is set when lfirst != nullptr), helio_drift_linear_pl, swiftest_util_coord_vb2vh_pl
-__global__ void __launch_bounds__(RB) k_ens_vh2vb(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+__global__ void __launch_bounds__(ENS_SUM_T) k_ens_vh2vb(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
                                                   const int32_t *__restrict__ lfirst, const double *__restrict__ Gm,
                                                   const double *__restrict__ vh, double *vb,
                                                   const double *__restrict__ GMcb, double *dcb, int exact) {
@@ -165,7 +170,7 @@ __global__ void __launch_bounds__(RB) k_ens_vh2vb(const int32_t *__restrict__ po
     const size_t o = poff[s];
     blk_vh2vb_pl(npl[s], Gm + o, vh + 3 * o, vb + 3 * o, GMcb[s], dcb + CB_N * s, exact, sh);
 }
-__global__ void __launch_bounds__(RB) k_ens_lindrift(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+__global__ void __launch_bounds__(ENS_SUM_T) k_ens_lindrift(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
                                                      const double *__restrict__ Gm, const double *__restrict__ vb,
                                                      const int32_t *__restrict__ lmask, const double *__restrict__ GMcb,
                                                      double *rh, double dt, double *dcb, int slot, int exact) {
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(RB) k_ens_lindrift(const int32_t *__restrict__
     const size_t o = poff[s];
     blk_lindrift_pl(npl[s], Gm + o, vb + 3 * o, lmask + o, GMcb[s], rh + 3 * o, dt, dcb + CB_N * s, slot, exact, sh);
 }
-__global__ void __launch_bounds__(RB) k_ens_vb2vh(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+__global__ void __launch_bounds__(ENS_SUM_T) k_ens_vb2vh(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
                                                   const double *__restrict__ Gm, const double *__restrict__ vb,
                                                   const int32_t *__restrict__ status, double *vh,
                                                   const double *__restrict__ GMcb, double *dcb, int exact) {
@@ -236,35 +241,65 @@ __global__ void k_ens_segments(int nsys, int64_t n, const int32_t *__restrict__ 
 // through the flat pair loop (swiftest_kick.f90:69-115), one thread per system walking
 // its list segment in order: ahi/ahj of the listed bodies, then acc -= ahi + ahj once
 // per body (unlisted bodies would subtract zero).
+// Terms of symba_kick_getacch_pl's pair subtraction for every entry of the pl-pl pool, one
+// thread each: t = (Gm_j irij3 dx, Gm_i irij3 dx), ok = the pair passes the radius rule.
+// The square root and divide of each pair run here in parallel; k_ens_kick_pairs adds the
+// terms in list order.
+__global__ void k_ens_pair_terms(int64_t n, const int32_t *__restrict__ l, int64_t cap, const double *__restrict__ r,
+                                 const double *__restrict__ Gm, const double *__restrict__ R, double *t,
+                                 uint8_t *ok) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int i = l[q] - 1, j = l[cap + q] - 1;
+    const double rx = r[3 * j + 0] - r[3 * i + 0];
+    const double ry = r[3 * j + 1] - r[3 * i + 1];
+    const double rz = r[3 * j + 2] - r[3 * i + 2];
+    const double rji2 = rx * rx + ry * ry + rz * rz;
+    const double rs = R[i] + R[j];
+    if (!(rji2 > rs * rs)) {
+        ok[q] = 0;
+        return;
+    }
+    const double irij3 = 1.0 / (rji2 * sqrt(rji2));
+    const double faci = Gm[i] * irij3;
+    const double facj = Gm[j] * irij3;
+    double *o = t + 6 * q;
+    o[0] = facj * rx;
+    o[1] = facj * ry;
+    o[2] = facj * rz;
+    o[3] = faci * rx;
+    o[4] = faci * ry;
+    o[5] = faci * rz;
+    ok[q] = 1;
+}
+
+// symba_kick_getacch_pl (symba_kick.f90:36-76) pair subtraction of every system: the
+// pair terms accumulated into ahi/ahj in list order (swiftest_kick_getacch_int_all_flat
+// order), then acc -= ahi + ahj once per body.  One thread per system.
 __global__ void k_ens_kick_pairs(int nsys, const int32_t *__restrict__ seg, const int32_t *__restrict__ l,
-                                 int64_t cap, const double *__restrict__ r, const double *__restrict__ Gm,
-                                 const double *__restrict__ R, double *ahi, double *ahj, int32_t *mark, double *acc) {
+                                 int64_t cap, const double *__restrict__ t, const uint8_t *__restrict__ ok,
+                                 double *ahi, double *ahj, int32_t *mark, double *acc) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nsys || seg[2 * s + 1] == 0) return;
     const int n = seg[2 * s + 1];
     const int32_t *i1 = l + seg[2 * s], *i2 = i1 + cap;
+    const double *ts = t + 6 * (int64_t)seg[2 * s];
+    const uint8_t *oks = ok + seg[2 * s];
     for (int q = 0; q < n; q++)
         for (int d = 0; d < 3; d++) {
             ahi[3 * (i1[q] - 1) + d] = ahj[3 * (i1[q] - 1) + d] = 0.0;
             ahi[3 * (i2[q] - 1) + d] = ahj[3 * (i2[q] - 1) + d] = 0.0;
         }
     for (int q = 0; q < n; q++) {
+        if (!oks[q]) continue;
         const int i = i1[q] - 1, j = i2[q] - 1;
-        const double rx = r[3 * j + 0] - r[3 * i + 0];
-        const double ry = r[3 * j + 1] - r[3 * i + 1];
-        const double rz = r[3 * j + 2] - r[3 * i + 2];
-        const double rji2 = rx * rx + ry * ry + rz * rz;
-        const double rs = R[i] + R[j];
-        if (!(rji2 > rs * rs)) continue;
-        const double irij3 = 1.0 / (rji2 * sqrt(rji2));
-        const double faci = Gm[i] * irij3;
-        const double facj = Gm[j] * irij3;
-        ahi[3 * i + 0] = ahi[3 * i + 0] + facj * rx;
-        ahi[3 * i + 1] = ahi[3 * i + 1] + facj * ry;
-        ahi[3 * i + 2] = ahi[3 * i + 2] + facj * rz;
-        ahj[3 * j + 0] = ahj[3 * j + 0] - faci * rx;
-        ahj[3 * j + 1] = ahj[3 * j + 1] - faci * ry;
-        ahj[3 * j + 2] = ahj[3 * j + 2] - faci * rz;
+        const double *o = ts + 6 * q;
+        ahi[3 * i + 0] = ahi[3 * i + 0] + o[0];
+        ahi[3 * i + 1] = ahi[3 * i + 1] + o[1];
+        ahi[3 * i + 2] = ahi[3 * i + 2] + o[2];
+        ahj[3 * j + 0] = ahj[3 * j + 0] - o[3];
+        ahj[3 * j + 1] = ahj[3 * j + 1] - o[4];
+        ahj[3 * j + 2] = ahj[3 * j + 2] - o[5];
     }
     for (int q = 0; q < n; q++) {
         const int b2[2] = {i1[q] - 1, i2[q] - 1};
@@ -529,11 +564,13 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
         if (!e->it_sym) {
             std::vector<int4> items;
             std::vector<int32_t> base;
-            const int64_t nslot = kick_sym_items(e->nsys, e->h_npl.data(), items, base);
+            int64_t npair = 0;
+            const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), items, base, &npair);
             SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
             SWG_TRY(dalloc(c, &e->sym_base, base.size()));
             SWG_TRY(upload(c, e->sym_base, base));
-            SWG_TRY(dalloc(c, &e->sym_part, (size_t)nslot * 12 * KICK_SYM_TILE));
+            SWG_TRY(dalloc(c, &e->sym_part, (size_t)(6 * nrecv + 3 * npair) * KICK_SYM_TILE));
+            e->sym_ppart = e->sym_part + (size_t)nrecv * 6 * KICK_SYM_TILE;
         }
         e->kv[0] = KICK_SYMMETRIC;
         return SWG_OK;
@@ -570,10 +607,10 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB, flag ? e->psys : nullptr, flag, phase));
         SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
         if (e->kv[0] == KICK_SYMMETRIC) {
-            SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->kA, e->kB, e->sym_part,
-                                           head, flag, phase));
-            return kick_mixed_sym_reduce(c, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part, e->ah, 1, flag,
-                                         phase);
+            SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
+                                           e->sym_part, e->sym_ppart, head, flag, phase));
+            return kick_mixed_sym_reduce(c, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part, e->sym_ppart,
+                                         e->ah, 1, flag, phase);
         }
         return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase);
     }
@@ -601,9 +638,14 @@ int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false) {
         SWG_TRY(accel_int_pl(e, e->head));
     }
     if (e->integrator == SWG_SYMBA && e->pp_n > 0) {
-        k_ens_kick_pairs<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pp, e->pp_l, e->pp_cap, e->rh,
-                                                                      e->Gmass, e->radius, e->ahi, e->ahj, e->pmark,
-                                                                      e->ah);
+        SWG_TRY(ensure(c, e->pair_terms, (size_t)e->pp_n * (6 * sizeof(double) + 1)));
+        double *t = (double *)e->pair_terms.ptr;
+        uint8_t *ok = (uint8_t *)(t + 6 * e->pp_n);
+        k_ens_pair_terms<<<grid_for(e->pp_n, 128), 128, 0, c->stream>>>(e->pp_n, e->pp_l, e->pp_cap, e->rh, e->Gmass,
+                                                                        e->radius, t, ok);
+        SWG_TRY(L(c, "ens_pair_terms"));
+        k_ens_kick_pairs<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pp, e->pp_l, e->pp_cap, t, ok,
+                                                                      e->ahi, e->ahj, e->pmark, e->ah);
         SWG_TRY(L(c, "ens_kick_pairs"));
     }
     k_kick_update<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->vb, e->ah, e->lmask, dt, e->rh,
@@ -640,7 +682,7 @@ int kick_vb_tp(swg_ensemble *e, double dt, int lbeg) {
 
 int lindrift_pl(swg_ensemble *e, double dt, int slot) {
     if (e->NPL == 0) return SWG_OK;
-    k_ens_lindrift<<<e->nsys, RB, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->lmask, e->GMcb, e->rh, dt,
+    k_ens_lindrift<<<e->nsys, ENS_SUM_T, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->lmask, e->GMcb, e->rh, dt,
                                                      e->dcb, slot, exact(e));
     return L(e->c, "ens_lindrift");
 }
@@ -652,13 +694,13 @@ int tp_misc(swg_ensemble *e, int slot, double dt, int mode, int mode_first) {
 }
 int vh2vb_pl(swg_ensemble *e, bool first_only) {
     if (e->NPL == 0) return SWG_OK;
-    k_ens_vh2vb<<<e->nsys, RB, 0, e->c->stream>>>(e->poff, e->npl, first_only ? e->lfirst : nullptr, e->Gmass, e->vh,
+    k_ens_vh2vb<<<e->nsys, ENS_SUM_T, 0, e->c->stream>>>(e->poff, e->npl, first_only ? e->lfirst : nullptr, e->Gmass, e->vh,
                                                   e->vb, e->GMcb, e->dcb, exact(e));
     return L(e->c, "ens_vh2vb");
 }
 int vb2vh_pl(swg_ensemble *e) {
     if (e->NPL == 0) return SWG_OK;
-    k_ens_vb2vh<<<e->nsys, RB, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->status, e->vh, e->GMcb, e->dcb,
+    k_ens_vb2vh<<<e->nsys, ENS_SUM_T, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->status, e->vh, e->GMcb, e->dcb,
                                                   exact(e));
     return L(e->c, "ens_vb2vh");
 }
@@ -670,10 +712,10 @@ int drift_bodies(swg_ensemble *e, double dt) {
     const bool symba = e->integrator == SWG_SYMBA;
     if (e->NPL > 0)
         SWG_TRY(drift_masked(c, 0.0, e->rh, e->vb, (int32_t)e->NPL, symba ? e->levelg : nullptr, -1, dt, e->status,
-                             nullptr, e->GMcb, e->psys));
+                             nullptr, e->GMcb, e->psys, !exact(e)));
     if (e->NTP > 0)
         SWG_TRY(drift_masked(c, 0.0, e->trh, e->tvb, (int32_t)e->NTP, symba ? e->tlevelg : nullptr, -1, dt,
-                             e->tstatus, nullptr, e->GMcb, e->tsys));
+                             e->tstatus, nullptr, e->GMcb, e->tsys, !exact(e)));
     return SWG_OK;
 }
 
@@ -1138,7 +1180,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->eout};
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);

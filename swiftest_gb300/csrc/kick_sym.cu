@@ -8,27 +8,30 @@
 // instructions per interaction against the broadcast kernels that evaluate each pair
 // once per receiving body.
 //
-// Work: every system's bodies form tiles of KICK_SYM_TILE; an item is a pair of tiles (I, J),
-// I <= J, of one system, pulled from a work queue by a persistent grid.
-//   * I < J: the block's two warps hold 64 receivers of tile I each (two per lane); tile
-//     J is staged in shared memory as four 32-partner sub-tiles, each stored twice in a
-//     row so that lane t reads partner (t + s) mod 32 at step s without wrapping.  At
-//     every step each lane evaluates its receivers against that partner, adds to its own
-//     receiver partials, and subtracts from an accumulator of that partner which the warp
-//     rotates one lane down after the step (three shuffles), so after 32 steps every
-//     partner accumulator holds the sum over the warp's 64 receivers and is back on the
-//     lane of its partner.  Tiles I < J hold no self pairs; with radii, pairs that the
-//     radius rule could drop are found per sub-tile (the smallest r^2 a receiver met
-//     against its radius plus the sub-tile's largest) and that sub-tile is recomputed with
-//     the rule applied pair by pair, so every kept pair gets the same operations.
-//   * I == J: each receiver sums over the whole tile with the pair rule applied pair by
-//     pair (as the broadcast kernel does).
-// Receiver-side sums (32-partner FP32 partials folded into float-float) and partner-side
-// sums (64-receiver FP32 partials per warp, folded across the warps into float-float) go
-// to per-item slots; a second kernel adds, for every body, its slots in a fixed order
-// (tiles below its own as partner side, then its own and above as receiver side) in
-// float-float, converted to FP64 once.
-// No atomics touch the sums, so results are deterministic.
+// Work: every system's bodies form tiles of KICK_SYM_TILE = 128 (four 32-body sub-tiles).
+// An item is a strip of one row of the upper triangle of tile pairs: tile I against tiles
+// J0 .. J0 + nJ - 1 of one system; a persistent grid of one-warp blocks pulls items from a
+// work queue.  Lane t holds the four receivers 32k + t of tile I (k = 0..3) in registers.
+// Tile J is staged in shared memory with each 32-partner sub-tile stored twice in a row,
+// so that lane t reads partner (t + s) mod 32 at step s without wrapping.
+//   * I < J, for each sub-tile u of J: at every step s each lane evaluates its receivers
+//     against partner (t + s) mod 32, adds to its receiver partials, and subtracts from an
+//     accumulator of that partner which the warp rotates one lane down after the step
+//     (three shuffles): after 32 steps every partner accumulator holds the sum over the
+//     128 receivers and is back on the lane of its partner.
+//   * I == J: sub-tile u against receivers k < u as above (so each pair is evaluated once);
+//     the partner accumulators of sub-tile u then belong to receiver u of the same lane.
+//     Receiver u against its own sub-tile is evaluated one-sided with the pair rule
+//     applied pair by pair (self pairs).
+// Tiles and sub-tiles other than the diagonal ones hold no self pairs; with radii, pairs
+// that the radius rule could drop are found per sub-tile (the smallest r^2 a receiver met
+// against its radius plus the sub-tile's largest radius) and that sub-tile is recomputed
+// with the rule applied pair by pair, so every kept pair gets the same operations.
+// Receiver sums (32-partner FP32 partials folded into float-float) go to one receiver slot
+// per item; partner sums of each off-diagonal tile pair (FP32 sums over 128 receivers) to
+// the system's pair slot of (I, J).  A second kernel adds, for every body, its pair slots
+// (tiles below its own) and then its receiver slots, in float-float, converted to FP64
+// once.  No atomics touch the sums, so results are deterministic.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,25 +43,26 @@ namespace swg {
 
 namespace {
 
-constexpr int SW = 2;                  // warps per block
-constexpr int SR = 2;                  // receivers per lane
-constexpr int TS = KICK_SYM_TILE;      // bodies per tile
-constexpr int NSUB = TS / 32;          // 32-partner sub-tiles per tile
-static_assert(TS == SW * 32 * SR && TS % 32 == 0, "tile of the symmetric kick");
-constexpr float PAD_POS = 3.0e6f;      // position of the padding beyond a system's last body
+constexpr int TS = KICK_SYM_TILE;  // bodies per tile
+constexpr int SR = TS / 32;        // receivers per lane = 32-body sub-tiles per tile
+constexpr int STRIP = 4;           // tiles J per item (one row strip of the upper triangle)
+constexpr float PAD_POS = 3.0e6f;  // position of the padding beyond a system's last body
+constexpr unsigned FULL = 0xffffffffu;
 
-// slot of tile pair (I, J), I <= J, among a system's nt tiles (row-major upper triangle)
-__host__ __device__ __forceinline__ int tri_slot(int I, int J, int nt) { return I * nt - I * (I - 1) / 2 + (J - I); }
+// pair slot of tiles (I, J), I < J, among a system's nt tiles (row-major strict upper triangle)
+__host__ __device__ __forceinline__ int pair_slot(int I, int J, int nt) {
+    return I * (nt - 1) - I * (I - 1) / 2 + (J - I - 1);
+}
 
-// 32 steps of one sub-tile for this lane's receivers (see the file comment).  A/B point
-// at the lane's first partner of the doubled sub-tile; src is the lane above.
+// 32 steps of one sub-tile for receivers k < NK of this lane (see the file comment).  A/B
+// point at the lane's first partner of the doubled sub-tile; src is the lane above.
 // GUARD: the radius rule pair by pair (RAD only); else, with RAD, mn keeps the smallest r^2.
-template <bool RAD, bool GUARD>
+template <bool RAD, bool GUARD, int NK>
 __device__ __forceinline__ void sym_subtile(const float4 *A, const float4 *B, const MixedRecv (&q)[SR],
                                             const float (&gm)[SR], int src, float (&px)[SR], float (&py)[SR],
                                             float (&pz)[SR], float &qx, float &qy, float &qz, float (&mn)[SR]) {
 #pragma unroll
-    for (int k = 0; k < SR; k++) {
+    for (int k = 0; k < NK; k++) {
         px[k] = py[k] = pz[k] = 0.f;
         mn[k] = 3.0e38f;
     }
@@ -68,7 +72,7 @@ __device__ __forceinline__ void sym_subtile(const float4 *A, const float4 *B, co
         const float4 a = A[s];
         const float4 b = B[s];
 #pragma unroll
-        for (int k = 0; k < SR; k++) {
+        for (int k = 0; k < NK; k++) {
             const float dx = (a.x - q[k].xh) + (b.x - q[k].xl);
             const float dy = (a.y - q[k].yh) + (b.y - q[k].yl);
             const float dz = (a.z - q[k].zh) + (b.z - q[k].zl);
@@ -87,114 +91,144 @@ __device__ __forceinline__ void sym_subtile(const float4 *A, const float4 *B, co
             qy = fmaf(-fj, dy, qy);
             qz = fmaf(-fj, dz, qz);
         }
-        qx = __shfl_sync(0xffffffffu, qx, src);
-        qy = __shfl_sync(0xffffffffu, qy, src);
-        qz = __shfl_sync(0xffffffffu, qz, src);
+        qx = __shfl_sync(FULL, qx, src);
+        qy = __shfl_sync(FULL, qy, src);
+        qz = __shfl_sync(FULL, qz, src);
     }
 }
 
-// Item: (system, tile I, tile J, slot).  pA/pB: every body split into (x_hi, y_hi, z_hi, Gm),
-// (x_lo, y_lo, z_lo, R); part: per slot [side 0 receivers | side 1 partners] x
-// [x_hi, x_lo, y_hi, y_lo, z_hi, z_lo] x TS floats.
+// sym_subtile without the rule, then (RAD) recomputed with it when some receiver k < NK
+// may meet a partner within the radii.
+template <bool RAD, int NK>
+__device__ __forceinline__ void sym_subtile_ruled(const float4 *A, const float4 *B, const MixedRecv (&q)[SR],
+                                                  const float (&gm)[SR], const bool (&ok)[SR], int src,
+                                                  float (&px)[SR], float (&py)[SR], float (&pz)[SR], float &qx,
+                                                  float &qy, float &qz) {
+    float mn[SR];
+    sym_subtile<RAD, false, NK>(A, B, q, gm, src, px, py, pz, qx, qy, qz, mn);
+    if (RAD) {
+        const float rt = __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(B[0].w)));  // radii are >= 0
+        bool need = false;
+#pragma unroll
+        for (int k = 0; k < NK; k++) {
+            const float rs = q[k].R + rt;
+            need = need || (ok[k] && mn[k] <= rs * rs);
+        }
+        if (__any_sync(FULL, need))  // rare: a pair may lie within the radii
+            sym_subtile<RAD, true, NK>(A, B, q, gm, src, px, py, pz, qx, qy, qz, mn);
+    }
+}
+
+__device__ __forceinline__ void ff_add3(FF &x, FF &y, FF &z, float a, float b, float c) {
+    ff_add(x, a);
+    ff_add(y, b);
+    ff_add(z, c);
+}
+
+// Sub-tile U of a diagonal tile (I == J): receivers k < U against it with the rotation,
+// whose partner sums belong to receiver U of this lane, and receiver U against it
+// one-sided with the pair rule.
+template <bool RAD, int U>
+__device__ __forceinline__ void diag_subtile(const float4 *sA, const float4 *sB, const MixedRecv (&q)[SR],
+                                             const float (&gm)[SR], const bool (&ok)[SR], const int (&self)[SR],
+                                             int j0, int lane, FF (&ax)[SR], FF (&ay)[SR], FF (&az)[SR]) {
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    if (U > 0) {
+        float px[SR], py[SR], pz[SR];
+        sym_subtile_ruled<RAD, U>(sA + U * 64 + lane, sB + U * 64 + lane, q, gm, ok, (lane + 1) & 31, px, py, pz, qx,
+                                  qy, qz);
+#pragma unroll
+        for (int k = 0; k < U; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
+    }
+    const MixedRecv qu[1] = {q[U]};
+    const int su[1] = {self[U]};
+    const bool mu[1] = {true};
+    float sx[1], sy[1], sz[1], smn[1];
+    mixed_tile<false, RAD, false, true, 1>(j0 + U * 32, 32, su, 0, mu, qu, sA + U * 64, sB + U * 64, sx, sy, sz, smn);
+    ff_add3(ax[U], ay[U], az[U], sx[0], sy[0], sz[0]);
+    if (U > 0) ff_add3(ax[U], ay[U], az[U], qx, qy, qz);
+}
+
+// Item: (system, tile I, first tile J0 | tiles nJ << 24, receiver slot).  pA/pB: every
+// body split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R).  A receiver slot is
+// [x_hi, x_lo, y_hi, y_lo, z_hi, z_lo] x TS floats, a pair slot [x, y, z] x TS floats.
 template <bool RAD>
-__global__ void __launch_bounds__(SW * 32) k_kick_mixed_sym(int nitems, const int4 *__restrict__ items,
-                                                           const int32_t *__restrict__ poff,
-                                                           const int32_t *__restrict__ npl,
-                                                           const float4 *__restrict__ pA,
-                                                           const float4 *__restrict__ pB, float *__restrict__ part,
-                                                           unsigned *__restrict__ head,
-                                                           const int32_t *__restrict__ sys_flag, int phase) {
-    __shared__ float4 sA[NSUB * 64];  // sub-tile u at [64u, 64u + 64): its 32 partners twice
-    __shared__ float4 sB[NSUB * 64];
-    __shared__ float sQ[SW][3][TS];   // partner-side partials of each warp
-    __shared__ int s_item;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *__restrict__ items,
+                                                      const int32_t *__restrict__ poff,
+                                                      const int32_t *__restrict__ npl,
+                                                      const int32_t *__restrict__ sbase,
+                                                      const float4 *__restrict__ pA, const float4 *__restrict__ pB,
+                                                      float *__restrict__ rpart, float *__restrict__ ppart,
+                                                      unsigned *__restrict__ head,
+                                                      const int32_t *__restrict__ sys_flag, int phase) {
+    __shared__ float4 sA[SR * 64];  // sub-tile u at [64u, 64u + 64): its 32 partners twice
+    __shared__ float4 sB[SR * 64];
+    const int lane = threadIdx.x;
     const float4 pad_a = make_float4(PAD_POS, PAD_POS, PAD_POS, 0.f), zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (;;) {
-        __syncthreads();  // every thread is done with the previous item's shared data
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(head, 1u);
-        __syncthreads();
-        const int it = s_item;
-        if (it >= nitems) break;
+        unsigned it = 0;
+        if (lane == 0) it = atomicAdd(head, 1u);
+        it = __shfl_sync(FULL, it, 0);
+        if (it >= (unsigned)nitems) break;
         const int4 w = items[it];
-        const int s = w.x, I = w.y, J = w.z;
-        if (sys_flag && sys_flag[s] != phase) continue;  // block-uniform
-        const int p0 = poff[s], n = npl[s];
-        for (int t = threadIdx.x; t < TS; t += SW * 32) {
-            const int j = J * TS + t;
-            const float4 a = j < n ? pA[p0 + j] : pad_a;
-            const float4 b = j < n ? pB[p0 + j] : zero;
-            const int o = (t >> 5) * 64 + (t & 31);
-            sA[o] = a;
-            sA[o + 32] = a;
-            sB[o] = b;
-            sB[o + 32] = b;
-        }
+        const int s = w.x, I = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
+        if (sys_flag && sys_flag[s] != phase) continue;  // warp-uniform
+        const int p0 = poff[s], n = npl[s], nt = (n + TS - 1) / TS;
         MixedRecv q[SR];
         float gm[SR];
         bool ok[SR];
         int self[SR];
-        bool self_m[SR];
 #pragma unroll
         for (int k = 0; k < SR; k++) {
-            const int i = I * TS + warp * 32 * SR + k * 32 + lane;
+            const int i = I * TS + k * 32 + lane;
             ok[k] = i < n;
             self[k] = i;
-            self_m[k] = true;
             const float4 a = ok[k] ? pA[p0 + i] : pad_a;
             const float4 b = ok[k] ? pB[p0 + i] : zero;
             q[k] = MixedRecv{a.x, a.y, a.z, b.x, b.y, b.z, b.w};
             gm[k] = a.w;
         }
-        __syncthreads();
         FF ax[SR], ay[SR], az[SR];
 #pragma unroll
         for (int k = 0; k < SR; k++) ax[k] = ay[k] = az[k] = FF{0.f, 0.f};
-        float px[SR], py[SR], pz[SR], mn[SR];
-        if (I == J) {
-            for (int u = 0; u < NSUB; u++) {
-                mixed_tile<false, RAD, false, true, SR>(J * TS + u * 32, 32, self, 0, self_m, q, sA + u * 64,
-                                                        sB + u * 64, px, py, pz, mn);
+        for (int jj = 0; jj < nJ; jj++) {
+            const int J = J0 + jj;
+            __syncwarp();  // the previous tile's shared data is consumed
 #pragma unroll
-                for (int k = 0; k < SR; k++) {
-                    ff_add(ax[k], px[k]);
-                    ff_add(ay[k], py[k]);
-                    ff_add(az[k], pz[k]);
-                }
+            for (int u = 0; u < SR; u++) {
+                const int j = J * TS + u * 32 + lane;
+                const float4 a = j < n ? pA[p0 + j] : pad_a;
+                const float4 b = j < n ? pB[p0 + j] : zero;
+                sA[u * 64 + lane] = a;
+                sA[u * 64 + 32 + lane] = a;
+                sB[u * 64 + lane] = b;
+                sB[u * 64 + 32 + lane] = b;
             }
-        } else {
-            const int src = (lane + 1) & 31;
-            for (int u = 0; u < NSUB; u++) {
-                const float4 *A = sA + u * 64 + lane;
-                const float4 *B = sB + u * 64 + lane;
-                float qx, qy, qz;
-                sym_subtile<RAD, false>(A, B, q, gm, src, px, py, pz, qx, qy, qz, mn);
-                if (RAD) {
-                    const float rt = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(B[0].w)));
-                    bool need = false;
+            __syncwarp();
+            if (I == J) {
+                static_assert(SR == 4, "diagonal sub-tiles");
+                diag_subtile<RAD, 0>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
+                diag_subtile<RAD, 1>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
+                diag_subtile<RAD, 2>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
+                diag_subtile<RAD, 3>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
+                continue;
+            }
+            float *o1 = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, J, nt)) * 3 * TS;
+            for (int u = 0; u < SR; u++) {
+                float px[SR], py[SR], pz[SR], qx, qy, qz;
+                sym_subtile_ruled<RAD, SR>(sA + u * 64 + lane, sB + u * 64 + lane, q, gm, ok, (lane + 1) & 31, px, py,
+                                           pz, qx, qy, qz);
 #pragma unroll
-                    for (int k = 0; k < SR; k++) {
-                        const float rs = q[k].R + rt;
-                        need = need || (ok[k] && mn[k] <= rs * rs);
-                    }
-                    if (__any_sync(0xffffffffu, need))  // rare: a pair may lie within the radii
-                        sym_subtile<RAD, true>(A, B, q, gm, src, px, py, pz, qx, qy, qz, mn);
-                }
-#pragma unroll
-                for (int k = 0; k < SR; k++) {
-                    ff_add(ax[k], px[k]);
-                    ff_add(ay[k], py[k]);
-                    ff_add(az[k], pz[k]);
-                }
-                sQ[warp][0][u * 32 + lane] = qx;
-                sQ[warp][1][u * 32 + lane] = qy;
-                sQ[warp][2][u * 32 + lane] = qz;
+                for (int k = 0; k < SR; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
+                o1[0 * TS + u * 32 + lane] = qx;
+                o1[1 * TS + u * 32 + lane] = qy;
+                o1[2 * TS + u * 32 + lane] = qz;
             }
         }
-        float *o0 = part + (size_t)w.w * 12 * TS;
+        float *o0 = rpart + (size_t)w.w * 6 * TS;
 #pragma unroll
         for (int k = 0; k < SR; k++) {
-            const int il = warp * 32 * SR + k * 32 + lane;
+            const int il = k * 32 + lane;
             o0[0 * TS + il] = ax[k].hi;
             o0[1 * TS + il] = ax[k].lo;
             o0[2 * TS + il] = ay[k].hi;
@@ -202,35 +236,18 @@ __global__ void __launch_bounds__(SW * 32) k_kick_mixed_sym(int nitems, const in
             o0[4 * TS + il] = az[k].hi;
             o0[5 * TS + il] = az[k].lo;
         }
-        if (I != J) {
-            __syncthreads();
-            float *o1 = o0 + 6 * TS;
-            for (int t = threadIdx.x; t < TS; t += SW * 32) {
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    FF f{0.f, 0.f};
-#pragma unroll
-                    for (int v = 0; v < SW; v++) ff_add(f, sQ[v][c][t]);
-                    o1[(2 * c) * TS + t] = f.hi;
-                    o1[(2 * c + 1) * TS + t] = f.lo;
-                }
-            }
-        }
     }
 }
 
-// Per body: acc (+)= its slots in a fixed order.  The slots' float-float values are added
-// in float-float (hi parts by TwoSum, lo parts plainly) and converted to FP64 once: FP64
-// arithmetic per slot would run on the narrow FP64 pipe and bound this kernel.
-__device__ __forceinline__ void ff_acc(FF &a, float &lo, const float *o, int l) {
-    ff_add(a, o[l]);
-    lo += o[KICK_SYM_TILE + l];
-}
-
+// Per body: acc (+)= its slots in a fixed order (pair slots of the tiles below its own,
+// then the receiver slots of its own row).  The slots' values are added in float-float
+// (hi parts by TwoSum, lo parts plainly) and converted to FP64 once: FP64 arithmetic per
+// slot would run on the narrow FP64 pipe and bound this kernel.
 __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, const int32_t *__restrict__ poff,
                                   const int32_t *__restrict__ npl, const int32_t *__restrict__ sbase,
-                                  const float *__restrict__ part, double *__restrict__ acc, int acc_is_zero,
-                                  const int32_t *__restrict__ sys_flag, int phase) {
+                                  const float *__restrict__ rpart, const float *__restrict__ ppart,
+                                  double *__restrict__ acc, int acc_is_zero, const int32_t *__restrict__ sys_flag,
+                                  int phase) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= n) return;
     const int s = psys[b];
@@ -239,17 +256,18 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
     const int nt = (npl[s] + TS - 1) / TS, K = i / TS, l = i % TS;
     FF fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
     float lx = 0.f, ly = 0.f, lz = 0.f;
+    int row = 0;  // first receiver slot of row K
     for (int I = 0; I < K; I++) {
-        const float *o = part + ((size_t)(sbase[s] + tri_slot(I, K, nt)) * 12 + 6) * TS;
-        ff_acc(fx, lx, o, l);
-        ff_acc(fy, ly, o + 2 * TS, l);
-        ff_acc(fz, lz, o + 4 * TS, l);
+        const float *o = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, K, nt)) * 3 * TS;
+        ff_add3(fx, fy, fz, o[l], o[TS + l], o[2 * TS + l]);
+        row += (nt - I + STRIP - 1) / STRIP;
     }
-    for (int J = K; J < nt; J++) {
-        const float *o = part + (size_t)(sbase[s] + tri_slot(K, J, nt)) * 12 * TS;
-        ff_acc(fx, lx, o, l);
-        ff_acc(fy, ly, o + 2 * TS, l);
-        ff_acc(fz, lz, o + 4 * TS, l);
+    for (int m = 0; m < (nt - K + STRIP - 1) / STRIP; m++) {
+        const float *o = rpart + (size_t)(sbase[2 * s] + row + m) * 6 * TS;
+        ff_add3(fx, fy, fz, o[l], o[2 * TS + l], o[4 * TS + l]);
+        lx += o[TS + l];
+        ly += o[3 * TS + l];
+        lz += o[5 * TS + l];
     }
     const double sx = (double)fx.hi + ((double)fx.lo + (double)lx);
     const double sy = (double)fy.hi + ((double)fy.lo + (double)ly);
@@ -262,20 +280,26 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
 
 }  // namespace
 
-int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase) {
+int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase,
+                       int64_t *npair_slots) {
     items.clear();
-    sbase.assign(nsys, 0);
+    sbase.assign(2 * (size_t)nsys, 0);
     std::vector<int64_t> cost;
-    int64_t nslot = 0;
+    int64_t nrs = 0, nps = 0;
     for (int s = 0; s < nsys; s++) {
         const int nt = (npl[s] + TS - 1) / TS;
-        sbase[s] = (int32_t)nslot;
+        sbase[2 * s] = (int32_t)nrs;
+        sbase[2 * s + 1] = (int32_t)nps;
+        auto rows = [&](int T) { return (int64_t)std::min(TS, npl[s] - T * TS); };
         for (int I = 0; I < nt; I++)
-            for (int J = I; J < nt; J++) {
-                items.push_back(make_int4(s, I, J, (int)(nslot + tri_slot(I, J, nt))));
-                cost.push_back((int64_t)std::min(TS, npl[s] - I * TS) * std::min(TS, npl[s] - J * TS));
+            for (int J0 = I; J0 < nt; J0 += STRIP) {
+                const int nJ = std::min(STRIP, nt - J0);
+                items.push_back(make_int4(s, I, J0 | (nJ << 24), (int)nrs++));
+                int64_t c = 0;
+                for (int J = J0; J < J0 + nJ; J++) c += rows(I) * rows(J);
+                cost.push_back(c);
             }
-        nslot += (int64_t)nt * (nt + 1) / 2;
+        nps += (int64_t)nt * (nt - 1) / 2;
     }
     std::vector<size_t> ord(items.size());
     for (size_t k = 0; k < ord.size(); k++) ord[k] = k;
@@ -283,40 +307,41 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &item
     std::vector<int4> sorted(items.size());
     for (size_t k = 0; k < ord.size(); k++) sorted[k] = items[ord[k]];
     items.swap(sorted);
-    return nslot;
+    *npair_slots = nps;
+    return nrs;
 }
 
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
-                           const int32_t *npl, const float4 *pA, const float4 *pB, float *part, unsigned *head,
-                           const int32_t *sys_flag, int phase) {
+                           const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
+                           float *ppart, unsigned *head, const int32_t *sys_flag, int phase) {
     if (nitems <= 0) return SWG_OK;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
     static int occ[2] = {0, 0};  // resident blocks per SM, queried once per variant
     int &o = occ[rad ? 1 : 0];
     if (o == 0) {
         int nb = 0;
-        SWG_TRY(cuda_status(c, rad ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<true>, SW * 32, 0)
-                                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<false>, SW * 32, 0),
+        SWG_TRY(cuda_status(c, rad ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<true>, 32, 0)
+                                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<false>, 32, 0),
                             "occupancy"));
         o = nb > 0 ? nb : 1;
     }
     const int grid = std::min(nitems, o * (c->num_sms > 0 ? c->num_sms : 152));
     if (rad)
-        k_kick_mixed_sym<true><<<grid, SW * 32, 0, c->stream>>>(nitems, items, poff, npl, pA, pB, part, head, sys_flag,
-                                                               phase);
+        k_kick_mixed_sym<true><<<grid, 32, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
+                                                               head, sys_flag, phase);
     else
-        k_kick_mixed_sym<false><<<grid, SW * 32, 0, c->stream>>>(nitems, items, poff, npl, pA, pB, part, head, sys_flag,
-                                                                phase);
+        k_kick_mixed_sym<false><<<grid, 32, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
+                                                                head, sys_flag, phase);
     c->launches++;
     return launch_status(c, "kick_mixed_sym");
 }
 
 int kick_mixed_sym_reduce(swg_ctx *c, int64_t n, const int32_t *psys, const int32_t *poff, const int32_t *npl,
-                          const int32_t *sbase, const float *part, double *acc, int acc_is_zero,
+                          const int32_t *sbase, const float *rpart, const float *ppart, double *acc, int acc_is_zero,
                           const int32_t *sys_flag, int phase) {
     if (n <= 0) return SWG_OK;
-    k_kick_sym_reduce<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(n, psys, poff, npl, sbase, part, acc, acc_is_zero,
-                                                                      sys_flag, phase);
+    k_kick_sym_reduce<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(n, psys, poff, npl, sbase, rpart, ppart, acc,
+                                                                      acc_is_zero, sys_flag, phase);
     c->launches++;
     return launch_status(c, "kick_sym_reduce");
 }

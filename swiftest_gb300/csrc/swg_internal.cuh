@@ -171,16 +171,19 @@ int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_
                          const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
                          const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
 // kick_sym.cu -- symmetric mixed pl-pl kick (each pair once, applied to both bodies) over
-// tile pairs of KICK_SYM_TILE bodies.  kick_sym_items builds the items (system, I, J, slot)
-// sorted by cost and each system's first slot; returns the number of slots.  part holds
-// 12 * KICK_SYM_TILE floats per slot; kick_mixed_sym_reduce writes acc (+)= the sums.
+// tile pairs of KICK_SYM_TILE bodies.  kick_sym_items builds the items (row strips of tile
+// pairs, sorted by cost) and per system its first receiver slot and first pair slot
+// (sbase[2s], sbase[2s+1]); returns the number of receiver slots, *npair_slots the number of
+// pair slots.  A receiver slot holds 6 * KICK_SYM_TILE floats, a pair slot 3 * KICK_SYM_TILE;
+// kick_mixed_sym_reduce writes acc (+)= the sums.
 constexpr int KICK_SYM_TILE = 128;
-int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase);
+int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase,
+                       int64_t *npair_slots);
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
-                           const int32_t *npl, const float4 *pA, const float4 *pB, float *part, unsigned *head,
-                           const int32_t *sys_flag = nullptr, int phase = 0);
+                           const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
+                           float *ppart, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
 int kick_mixed_sym_reduce(swg_ctx *c, int64_t n, const int32_t *psys, const int32_t *poff, const int32_t *npl,
-                          const int32_t *sbase, const float *part, double *acc, int acc_is_zero,
+                          const int32_t *sbase, const float *rpart, const float *ppart, double *acc, int acc_is_zero,
                           const int32_t *sys_flag = nullptr, int phase = 0);
 // autotune.cu -- cache of tuned kernel shapes: key of (device, kind, size bucket); the cached
 // variant or -1; store (kept for the process and appended to the cache file)
@@ -196,9 +199,11 @@ constexpr int ENC_BOUND_TILE = 64;    // bodies per bound tile of the radius-sor
 // drift.cu -- Danby drift
 int drift_all(swg_ctx *c, const double *mu, double mu_scalar, double *x, double *v, int32_t n, int32_t lgr,
               double inv_c2, double dt, const int32_t *lmask, int32_t *iflag);
-// mu_sys/sys (optional): body i uses mu_sys[sys[i]] instead of mu (CSR-packed ensembles)
+// mu_sys/sys (optional): body i uses mu_sys[sys[i]] instead of mu (CSR-packed ensembles);
+// fast: the fast FP64 form of the solver (mixed-precision path)
 int drift_masked(swg_ctx *c, double mu, double *x, double *v, int32_t n, const int32_t *levelg, int irec, double dt,
-                 int32_t *status, int32_t *nfail, const double *mu_sys = nullptr, const int32_t *sys = nullptr);
+                 int32_t *status, int32_t *nfail, const double *mu_sys = nullptr, const int32_t *sys = nullptr,
+                 bool fast = false);
 
 // encounter.cu -- encounter checks and sorting
 int64_t sort_padded_len(int64_t n);

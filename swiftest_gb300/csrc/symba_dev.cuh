@@ -25,9 +25,10 @@ enum { CB_VB = 0, CB_RB = 3, CB_PTBEG = 6, CB_PTEND = 9, CB_N = 12 };
 // by the whole block into shared memory, chunk by chunk, and thread 0 adds them one at
 // a time in the reference's index order, which reproduces its rounding.  exact == 0:
 // thread t adds its own terms t, t + RB, t + 2 RB, ... in registers, then the block
-// combines the RB partial sums as a tree (warp shuffles, then one warp over the warp
-// sums): a fixed order, so results are deterministic, with no serial chain.
-constexpr int RB = 1024;  // threads of the reduction kernels
+// combines the partial sums as a tree (warp shuffles, then one warp over the warp
+// sums): a fixed order, so results are deterministic, with no serial chain.  The block
+// may have any multiple of 32 threads up to RB.
+constexpr int RB = 1024;  // most threads of the reduction kernels
 
 struct Sum3 {
     double x, y, z;
@@ -60,13 +61,14 @@ __device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, do
     if (exact) {
         if (threadIdx.x == 0) acc = {0.0, 0.0, 0.0};
         __syncthreads();
-        for (int c0 = 0; c0 < n; c0 += RB) {
+        const int nb = blockDim.x;
+        for (int c0 = 0; c0 < n; c0 += nb) {
             const int k = threadIdx.x;
             const int idx = reverse ? n - 1 - (c0 + k) : c0 + k;
             double tx = 0, ty = 0, tz = 0;
             unsigned char m = 0;
             if (c0 + k < n) m = term_fn(idx, tx, ty, tz);
-            const int cnt = min(RB, n - c0);
+            const int cnt = min(nb, n - c0);
             cx[k] = tx;
             cy[k] = ty;
             cz[k] = tz;
@@ -87,7 +89,7 @@ __device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, do
         return acc;
     }
     double ax = 0.0, ay = 0.0, az = 0.0;
-    for (int q = threadIdx.x; q < n; q += RB) {
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
         double tx, ty, tz;
         if (term_fn(reverse ? n - 1 - q : q, tx, ty, tz)) {
             ax += tx;
@@ -104,7 +106,8 @@ __device__ Sum3 ordered_sum3(int n, bool reverse, bool exact, TermFn term_fn, do
     }
     __syncthreads();
     if (w == 0) {
-        double x = rx[threadIdx.x], y = ry[threadIdx.x], z = rz[threadIdx.x];  // RB / 32 == 32 warp sums
+        const bool have = threadIdx.x < (blockDim.x >> 5);  // one warp sum per warp of the block
+        double x = have ? rx[threadIdx.x] : 0.0, y = have ? ry[threadIdx.x] : 0.0, z = have ? rz[threadIdx.x] : 0.0;
         warp_sum3(x, y, z);
         if (threadIdx.x == 0) acc = {sign * x, sign * y, sign * z};
     }
@@ -128,9 +131,15 @@ static __device__ void blk_lindrift_pl(int npl, const double *__restrict__ Gm,
     const double ptx = s.x / GMcb, pty = s.y / GMcb, ptz = s.z / GMcb;
     for (int i = threadIdx.x; i < npl; i += blockDim.x) {
         if (!lmask[i]) continue;
-        rh[3 * i + 0] = rh[3 * i + 0] + ptx * dt;
-        rh[3 * i + 1] = rh[3 * i + 1] + pty * dt;
-        rh[3 * i + 2] = rh[3 * i + 2] + ptz * dt;
+        if (exact) {
+            rh[3 * i + 0] = rh[3 * i + 0] + ptx * dt;
+            rh[3 * i + 1] = rh[3 * i + 1] + pty * dt;
+            rh[3 * i + 2] = rh[3 * i + 2] + ptz * dt;
+        } else {  // one rounding per coordinate (the FP64 pipe is narrow)
+            rh[3 * i + 0] = fma(ptx, dt, rh[3 * i + 0]);
+            rh[3 * i + 1] = fma(pty, dt, rh[3 * i + 1]);
+            rh[3 * i + 2] = fma(ptz, dt, rh[3 * i + 2]);
+        }
     }
     if (threadIdx.x == 0) {
         dcb[slot + 0] = ptx;
@@ -183,9 +192,10 @@ static __device__ void blk_vb2vh_pl(int npl, const double *__restrict__ Gm,
             y = Gm[i] * vb[3 * i + 1] / GMcb;
             z = Gm[i] * vb[3 * i + 2] / GMcb;
         } else {
-            x = Gm[i] * vb[3 * i + 0] * inv;
-            y = Gm[i] * vb[3 * i + 1] * inv;
-            z = Gm[i] * vb[3 * i + 2] * inv;
+            const double g = Gm[i] * inv;
+            x = g * vb[3 * i + 0];
+            y = g * vb[3 * i + 1];
+            z = g * vb[3 * i + 2];
         }
         return status[i] != ST_INACTIVE;
     };
@@ -962,10 +972,11 @@ static __device__ void blk_energy_final(int n, int whm, const double *rh, const 
     };
     const Sum3 kp = ordered_sum3(n, false, false, kt, 1.0, sh);
     auto bt = [&](int i, double &x, double &y, double &z) -> unsigned char {
-        x = lclose ? -3.0 * Gm[i] * Gm[i] / (5.0 * radius[i]) : 0.0;
+        const bool act = status[i] != ST_INACTIVE;  // a removed body has no radius: no binding term
+        x = lclose && act ? -3.0 * Gm[i] * Gm[i] / (5.0 * radius[i]) : 0.0;
         y = rows[i];
         z = 0.0;
-        return 1;
+        return act;
     };
     const Sum3 bp = ordered_sum3(n, false, false, bt, 1.0, sh);
     if (threadIdx.x == 0) {

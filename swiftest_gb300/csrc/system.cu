@@ -387,14 +387,16 @@ int drift_pl(swg_system *s, double dt) {
     if (s->npl == 0) return SWG_OK;
     const int32_t *lev = s->integrator == SWG_SYMBA ? s->levelg : nullptr;
     ProfScope ps(s->prof, s->c->stream, PROF_DRIFT);
-    return drift_masked(s->c, s->GMcb, s->rh, s->vb, s->npl, lev, s->irec, dt, s->status, nullptr);
+    return drift_masked(s->c, s->GMcb, s->rh, s->vb, s->npl, lev, s->irec, dt, s->status, nullptr, nullptr, nullptr,
+                        !exact(s));
 }
 int drift_tp(swg_system *s, double dt) {
     if (s->ntp == 0) return SWG_OK;
     const int32_t *lev = s->integrator == SWG_SYMBA ? s->tlevelg : nullptr;
     double *v = s->integrator == SWG_WHM ? s->tvh : s->tvb;
     ProfScope ps(s->prof, s->c->stream, PROF_DRIFT);
-    return drift_masked(s->c, s->GMcb, s->trh, v, s->ntp, lev, s->irec, dt, s->tstatus, nullptr);
+    return drift_masked(s->c, s->GMcb, s->trh, v, s->ntp, lev, s->irec, dt, s->tstatus, nullptr, nullptr, nullptr,
+                        !exact(s));
 }
 
 // helio_step_pl / _tp (helio_step.f90:37-119) via whm_step_system (whm_step.f90:14-35)

@@ -41,6 +41,10 @@ def test_symba_collisions_bitexact(ctx):
     # mass is conserved by merging
     e0, e1 = NBodySystem(ctx, "SYMBA", cb, pl, tp, **kw).energy(), gpu.energy()
     assert abs(e1["GMtot"] - e0["GMtot"]) <= 1e-13 * e0["GMtot"]
+    # removed bodies (no mass, no radius) take no part in the energy
+    er = ref.energy()
+    for k in ("te", "ke", "pe", "be"):
+        assert np.isfinite(e1[k]) and abs(e1[k] - er[k]) <= 1e-12 * abs(er[k]), k
 
 
 def test_ensemble_collisions_bitexact(ctx):
@@ -72,6 +76,10 @@ def test_ensemble_collisions_bitexact(ctx):
         assert np.array_equal(trh[a:b], orh) and np.array_equal(tvh[a:b], ovh) and np.array_equal(tst[a:b], ost)
         ncoll += r.stats()["collisions"]
     assert ncoll > 0 and ens.stats()["collisions"] == ncoll
+    eg = ens.energy()
+    for s, r in enumerate(refs):
+        er = r.energy()
+        assert np.isfinite(eg["te"][s]) and abs(eg["te"][s] - er["te"]) <= 1e-12 * abs(er["te"]), s
 
 
 def _helio_crowded(seed, npl=60, ntp=600, inflate=1000.0):

@@ -223,3 +223,28 @@ def test_ensemble_getacch_mixed_tolerance(ctx, integrator, lclose):
         g2 = ens.getacch_int_pl()
         assert np.array_equal(g, g2)  # deterministic
         ens.close()
+
+
+def test_mixed_drift_matches_fp64_drift(ctx):
+    # massless bodies feel no pair forces and move the central body not at all, so the
+    # mixed and FP64 ensembles differ only in the drift: the fast FP64 solver form of the
+    # mixed path against the reference form, over circular, eccentric and hyperbolic orbits
+    E = IC.make_ensemble("C3", nsys=4, scale=0.1)
+    sysl = []
+    for s, (pl, tp) in enumerate(E["systems"]):
+        pl = {k: v.copy() for k, v in pl.items()}
+        pl["Gmass"][:] = 0.0
+        pl["rhill"][:] = 0.0
+        f = np.linspace(0.3, 1.5, len(pl["Gmass"]))  # speed factors: e up to ~0.9, hyperbolic above sqrt(2)
+        pl["vh"] = pl["vh"] * f[:, None]
+        sysl.append((pl, tp))
+    E = _pack(E, sysl)
+    out = []
+    for prec in ("FP64", "MIXED"):
+        ens = Ensemble(ctx, E, precision=prec, dt=0.01, lclose=False)
+        ens.step(100)
+        out.append(ens.get_pl() + ens.get_tp())
+        ens.close()
+    for a, b in zip(out[0][:2] + out[0][3:5], out[1][:2] + out[1][3:5]):
+        rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(a, axis=1)
+        assert rel.max() < 1e-12, rel.max()
