@@ -106,6 +106,12 @@ struct swg_ensemble {
     unsigned long long *ndiscard = nullptr;  // tp removed by the scan
     DevBuf rec_scratch, rows;
     DevBuf pair_terms;  // pl-pl pool: six pair terms and a kept flag per entry
+    // chunks of the mixed path's per-system sums: (system, first body, bodies, chunk index in
+    // its system), each system's (first chunk, chunks), four partial sums per chunk
+    int4 *chunks = nullptr;
+    int2 *sys_chunks = nullptr;
+    double *chunk_part = nullptr;
+    int nchunks = 0;
     double *eout = nullptr;      // 9 per system
     int32_t *h_flags = nullptr;  // pinned: [2] recursion status; +8: two unsigned long long counts
     std::vector<int32_t> h_pend;  // per-system pause flags read after a recursion launch
@@ -189,6 +195,122 @@ __global__ void __launch_bounds__(ENS_SUM_T) k_ens_vb2vh(const int32_t *__restri
     __shared__ SumScratch sh;
     const size_t o = poff[s];
     blk_vb2vh_pl(npl[s], Gm + o, vb + 3 * o, status + o, vh + 3 * o, GMcb[s], dcb + CB_N * s, exact, sh);
+}
+
+// ---- per-system sums of the mixed path over 256-body chunks of every system
+// The block-per-system kernels above leave the largest systems on one SM each, and these
+// sums are FP64 work on GB300's narrow FP64 pipe; the mixed path instead forms partial sums
+// over chunks of CHUNK bodies of every system (grid over all chunks), then each chunk adds
+// its system's partials in chunk order and applies the result to its own bodies.  The
+// order is fixed, so results are deterministic.
+constexpr int CHUNK = 256, CHUNK_T = 64;  // bodies per chunk, threads per chunk block
+enum { SUM_VH2VB = 0, SUM_LIN = 1, SUM_VB2VH = 2 };
+
+// chunk: (system, first body, bodies, unused); out: 4 doubles per chunk (sum of weights
+// for SUM_VH2VB, then the three momentum components)
+template <int MODE>
+__global__ void __launch_bounds__(CHUNK_T) k_chunk_sums(int nchunks, const int4 *__restrict__ chunks,
+                                                       const int32_t *__restrict__ lfirst,
+                                                       const double *__restrict__ Gm, const double *__restrict__ v,
+                                                       const int32_t *__restrict__ mask, double *__restrict__ out) {
+    const int c = blockIdx.x;
+    const int4 ch = chunks[c];
+    if (MODE == SUM_VH2VB && lfirst && !lfirst[ch.x]) return;
+    double w = 0.0, x = 0.0, y = 0.0, z = 0.0;
+    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
+        const int i = ch.y + k;
+        bool on = true;
+        if (MODE == SUM_LIN) on = mask[i] != 0;
+        if (MODE == SUM_VB2VH) on = mask[i] != ST_INACTIVE;
+        if (!on) continue;
+        const double g = Gm[i];
+        w += g;
+        x = fma(g, v[3 * i + 0], x);
+        y = fma(g, v[3 * i + 1], y);
+        z = fma(g, v[3 * i + 2], z);
+    }
+    __shared__ double sh[CHUNK_T / 32][4];
+    for (int off = 16; off > 0; off >>= 1) {
+        if (MODE == SUM_VH2VB) w += __shfl_down_sync(0xffffffffu, w, off);
+        x += __shfl_down_sync(0xffffffffu, x, off);
+        y += __shfl_down_sync(0xffffffffu, y, off);
+        z += __shfl_down_sync(0xffffffffu, z, off);
+    }
+    const int wp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        sh[wp][0] = w;
+        sh[wp][1] = x;
+        sh[wp][2] = y;
+        sh[wp][3] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int q = 0; q < CHUNK_T / 32; q++) t += sh[q][threadIdx.x];
+        out[4 * c + threadIdx.x] = t;
+    }
+}
+
+// The system's chunk partials added in chunk order, then applied to this chunk's bodies:
+// SUM_VH2VB: vb = vh + c, c = -sum(Gm vh) / (GMcb + sum Gm) (swiftest_util_coord_vh2vb_pl);
+// SUM_LIN: pt = sum(Gm vb) / GMcb, rh += pt dt (helio_drift_linear_pl);
+// SUM_VB2VH: c = -sum(Gm vb) / GMcb, vh = vb - c (swiftest_util_coord_vb2vh_pl).
+// The system's first chunk records the result in the central-body record.
+template <int MODE>
+__global__ void __launch_bounds__(CHUNK_T) k_chunk_apply(const int4 *__restrict__ chunks,
+                                                        const int2 *__restrict__ sys_chunks,
+                                                        const int32_t *__restrict__ lfirst,
+                                                        const double *__restrict__ part,
+                                                        const double *__restrict__ GMcb,
+                                                        const int32_t *__restrict__ lmask, const double *vin,
+                                                        double *vout, double *rh, double dt, double *dcb, int slot) {
+    const int c = blockIdx.x;
+    const int4 ch = chunks[c];
+    const int s = ch.x;
+    if (MODE == SUM_VH2VB && lfirst && !lfirst[s]) return;
+    __shared__ double tot[4];
+    if (threadIdx.x < 4) {
+        const int2 r = sys_chunks[s];
+        double t = 0.0;
+        for (int q = r.x; q < r.x + r.y; q++) t += part[4 * q + threadIdx.x];
+        tot[threadIdx.x] = t;
+    }
+    __syncthreads();
+    double cx, cy, cz;
+    if (MODE == SUM_VH2VB) {
+        const double f = -1.0 / (GMcb[s] + tot[0]);
+        cx = tot[1] * f;
+        cy = tot[2] * f;
+        cz = tot[3] * f;
+    } else {
+        const double f = (MODE == SUM_LIN ? 1.0 : -1.0) / GMcb[s];
+        cx = tot[1] * f;
+        cy = tot[2] * f;
+        cz = tot[3] * f;
+    }
+    if (ch.w == 0 && threadIdx.x == 0) {
+        double *d = dcb + CB_N * s + (MODE == SUM_LIN ? slot : CB_VB);
+        d[0] = cx;
+        d[1] = cy;
+        d[2] = cz;
+    }
+    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
+        const int i = ch.y + k;
+        if (MODE == SUM_VH2VB) {
+            vout[3 * i + 0] = vin[3 * i + 0] + cx;
+            vout[3 * i + 1] = vin[3 * i + 1] + cy;
+            vout[3 * i + 2] = vin[3 * i + 2] + cz;
+        } else if (MODE == SUM_LIN) {
+            if (!lmask[i]) continue;
+            rh[3 * i + 0] = fma(cx, dt, rh[3 * i + 0]);
+            rh[3 * i + 1] = fma(cy, dt, rh[3 * i + 1]);
+            rh[3 * i + 2] = fma(cz, dt, rh[3 * i + 2]);
+        } else {
+            vout[3 * i + 0] = vin[3 * i + 0] - cx;
+            vout[3 * i + 1] = vin[3 * i + 1] - cy;
+            vout[3 * i + 2] = vin[3 * i + 2] - cz;
+        }
+    }
 }
 
 // Test-particle coordinate updates with their own system's central-body record (modes
@@ -460,7 +582,20 @@ int build_items(swg_ensemble *e) {
     SWG_TRY(dalloc(e->c, &e->tbase, tbase.size()));
     SWG_TRY(upload(e->c, e->tbase, tbase));
     SWG_TRY(dalloc(e->c, &e->bounds, tiles.size()));
-    return SWG_OK;
+    std::vector<int4> chunks;
+    std::vector<int2> sys_chunks(S);
+    for (int s = 0; s < S; s++) {
+        sys_chunks[s] = make_int2((int)chunks.size(), 0);
+        for (int b0 = 0, k = 0; b0 < e->h_npl[s]; b0 += CHUNK, k++)
+            chunks.push_back(make_int4(s, e->h_poff[s] + b0, std::min(CHUNK, e->h_npl[s] - b0), k));
+        sys_chunks[s].y = (int)chunks.size() - sys_chunks[s].x;
+    }
+    e->nchunks = (int)chunks.size();
+    SWG_TRY(dalloc(e->c, &e->chunks, chunks.size()));
+    SWG_TRY(upload(e->c, e->chunks, chunks));
+    SWG_TRY(dalloc(e->c, &e->sys_chunks, sys_chunks.size()));
+    SWG_TRY(upload(e->c, e->sys_chunks, sys_chunks));
+    return dalloc(e->c, &e->chunk_part, 4 * chunks.size());
 }
 
 int ensure_pool(swg_ensemble *e, int32_t **l, int64_t *cap, int64_t need) {
@@ -680,8 +815,23 @@ int kick_vb_tp(swg_ensemble *e, double dt, int lbeg) {
     return L(c, "kick_update_tp");
 }
 
+// Mixed path: one per-system sum over chunks (partials, then apply).
+template <int MODE>
+int chunk_sum(swg_ensemble *e, const int32_t *lfirst, const double *vsum, const int32_t *mask, const double *vin,
+              double *vout, double dt, int slot) {
+    swg_ctx *c = e->c;
+    if (e->nchunks == 0) return SWG_OK;
+    k_chunk_sums<MODE><<<e->nchunks, CHUNK_T, 0, c->stream>>>(e->nchunks, e->chunks, lfirst, e->Gmass, vsum, mask,
+                                                              e->chunk_part);
+    SWG_TRY(L(c, "chunk_sums"));
+    k_chunk_apply<MODE><<<e->nchunks, CHUNK_T, 0, c->stream>>>(e->chunks, e->sys_chunks, lfirst, e->chunk_part,
+                                                               e->GMcb, e->lmask, vin, vout, e->rh, dt, e->dcb, slot);
+    return L(c, "chunk_apply");
+}
+
 int lindrift_pl(swg_ensemble *e, double dt, int slot) {
     if (e->NPL == 0) return SWG_OK;
+    if (!exact(e)) return chunk_sum<SUM_LIN>(e, nullptr, e->vb, e->lmask, nullptr, nullptr, dt, slot);
     k_ens_lindrift<<<e->nsys, ENS_SUM_T, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->lmask, e->GMcb, e->rh, dt,
                                                      e->dcb, slot, exact(e));
     return L(e->c, "ens_lindrift");
@@ -694,12 +844,15 @@ int tp_misc(swg_ensemble *e, int slot, double dt, int mode, int mode_first) {
 }
 int vh2vb_pl(swg_ensemble *e, bool first_only) {
     if (e->NPL == 0) return SWG_OK;
+    if (!exact(e))
+        return chunk_sum<SUM_VH2VB>(e, first_only ? e->lfirst : nullptr, e->vh, nullptr, e->vh, e->vb, 0.0, 0);
     k_ens_vh2vb<<<e->nsys, ENS_SUM_T, 0, e->c->stream>>>(e->poff, e->npl, first_only ? e->lfirst : nullptr, e->Gmass, e->vh,
                                                   e->vb, e->GMcb, e->dcb, exact(e));
     return L(e->c, "ens_vh2vb");
 }
 int vb2vh_pl(swg_ensemble *e) {
     if (e->NPL == 0) return SWG_OK;
+    if (!exact(e)) return chunk_sum<SUM_VB2VH>(e, nullptr, e->vb, e->status, e->vb, e->vh, 0.0, 0);
     k_ens_vb2vh<<<e->nsys, ENS_SUM_T, 0, e->c->stream>>>(e->poff, e->npl, e->Gmass, e->vb, e->status, e->vh, e->GMcb, e->dcb,
                                                   exact(e));
     return L(e->c, "ens_vb2vh");
@@ -1180,7 +1333,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->eout};
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
