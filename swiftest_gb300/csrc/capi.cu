@@ -112,6 +112,7 @@ int swg_destroy(swg_ctx *c) {
     while (!c->systems.empty()) swg_system_destroy((swg_system *)c->systems.back());
     while (!c->ensembles.empty()) swg_ensemble_destroy((swg_ensemble *)c->ensembles.back());
     cudaStreamSynchronize(c->stream);
+    kick_sym_single_free(c);
     for (auto &b : c->slot)
         if (b.ptr) cudaFree(b.ptr);
     DevBuf *eb[] = {&c->enc.raw, &c->enc.sort, &c->enc.counters};
@@ -143,7 +144,9 @@ int swg_kick_getacch_int_all_tri_pl(swg_ctx *c, int32_t npl, int32_t nplm, const
     SWG_TRY(stage_in(c, mem, 1, Gmass, (size_t)npl, &dg));
     SWG_TRY(stage_in(c, mem, 2, radius, (size_t)npl, &dR));
     SWG_TRY(stage_in(c, mem, 3, (const double *)acc, 3 * (size_t)npl, &da));
-    if (precision == SWG_MIXED) {
+    if (precision == SWG_MIXED && nplm == npl && kick_sym_single_ok(npl, c->num_sms)) {
+        SWG_TRY(kick_mixed_sym_single(c, npl, dr, dg, dR, da, 0));
+    } else if (precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, npl, npl);
         SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, npl, nch)));
         SWG_TRY(kick_mixed_launch(c, false, npl, npl, nplm, dr, dr, dg, dR, nullptr, da, 0, nch, c->slot[10].ptr));
@@ -172,7 +175,9 @@ int swg_kick_getacch_int_all_flat_pl(swg_ctx *c, int32_t npl, int32_t nplm, int6
             c->err = "nplpl does not match the canonical pair count for (npl, nplm)";
             return SWG_ERR_ARG;
         }
-        if (precision == SWG_MIXED) {
+        if (precision == SWG_MIXED && nplm == npl && kick_sym_single_ok(npl, c->num_sms)) {
+            SWG_TRY(kick_mixed_sym_single(c, npl, dr, dg, dR, da, 0));
+        } else if (precision == SWG_MIXED) {
             const int nch = kick_mixed_chunks(c, npl, npl);
             SWG_TRY(ensure_kick_scratch(c, c->slot[10], kick_mixed_scratch_bytes(npl, npl, nch)));
             SWG_TRY(kick_mixed_launch(c, false, npl, npl, nplm, dr, dr, dg, dR, nullptr, da, 0, nch, c->slot[10].ptr));

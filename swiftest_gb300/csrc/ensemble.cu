@@ -92,7 +92,7 @@ struct swg_ensemble {
     int force_variant = -1;
     // symmetric pl-pl mixed kick (the default): tile-pair items, each system's first slot, slot sums
     int4 *it_sym = nullptr;
-    int n_sym = 0;
+    int n_sym = 0, sym_strip = 1;
     int32_t *sym_base = nullptr;
     float *sym_part = nullptr, *sym_ppart = nullptr;  // receiver slots, then pair slots (one allocation)
     unsigned *head = nullptr;
@@ -700,7 +700,8 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
             std::vector<int4> items;
             std::vector<int32_t> base;
             int64_t npair = 0;
-            const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), items, base, &npair);
+            e->sym_strip = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms);
+            const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), e->sym_strip, items, base, &npair);
             SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
             SWG_TRY(dalloc(c, &e->sym_base, base.size()));
             SWG_TRY(upload(c, e->sym_base, base));
@@ -744,8 +745,8 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         if (e->kv[0] == KICK_SYMMETRIC) {
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
                                            e->sym_part, e->sym_ppart, head, flag, phase));
-            return kick_mixed_sym_reduce(c, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part, e->sym_ppart,
-                                         e->ah, 1, flag, phase);
+            return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
+                                         e->sym_ppart, e->ah, 1, flag, phase);
         }
         return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase);
     }

@@ -35,6 +35,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <string>
+#include <vector>
 
 #include "kick_mixed.cuh"
 #include "swg_internal.cuh"
@@ -45,7 +47,7 @@ namespace {
 
 constexpr int TS = KICK_SYM_TILE;  // bodies per tile
 constexpr int SR = TS / 32;        // receivers per lane = 32-body sub-tiles per tile
-constexpr int STRIP = 4;           // tiles J per item (one row strip of the upper triangle)
+constexpr int MAX_STRIP = 4;       // most tiles J per item (one row strip of the upper triangle)
 constexpr float PAD_POS = 3.0e6f;  // position of the padding beyond a system's last body
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -247,10 +249,10 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
                                   const int32_t *__restrict__ npl, const int32_t *__restrict__ sbase,
                                   const float *__restrict__ rpart, const float *__restrict__ ppart,
                                   double *__restrict__ acc, int acc_is_zero, const int32_t *__restrict__ sys_flag,
-                                  int phase) {
+                                  int phase, int strip) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= n) return;
-    const int s = psys[b];
+    const int s = psys ? psys[b] : 0;
     if (sys_flag && sys_flag[s] != phase) return;
     const int i = (int)(b - poff[s]);
     const int nt = (npl[s] + TS - 1) / TS, K = i / TS, l = i % TS;
@@ -260,9 +262,9 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
     for (int I = 0; I < K; I++) {
         const float *o = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, K, nt)) * 3 * TS;
         ff_add3(fx, fy, fz, o[l], o[TS + l], o[2 * TS + l]);
-        row += (nt - I + STRIP - 1) / STRIP;
+        row += (nt - I + strip - 1) / strip;
     }
-    for (int m = 0; m < (nt - K + STRIP - 1) / STRIP; m++) {
+    for (int m = 0; m < (nt - K + strip - 1) / strip; m++) {
         const float *o = rpart + (size_t)(sbase[2 * s] + row + m) * 6 * TS;
         ff_add3(fx, fy, fz, o[l], o[2 * TS + l], o[4 * TS + l]);
         lx += o[TS + l];
@@ -280,8 +282,24 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
 
 }  // namespace
 
-int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase,
-                       int64_t *npair_slots) {
+int kick_sym_strip(int32_t nsys, const int32_t *npl, int num_sms) {
+    int64_t pairs = 0;
+    for (int s = 0; s < nsys; s++) {
+        const int64_t nt = (npl[s] + TS - 1) / TS;
+        pairs += nt * (nt + 1) / 2;
+    }
+    // strips of MAX_STRIP measured fastest whenever they leave a few items per SM; shorter
+    // strips only when the work would not spread over the SMs otherwise
+    return pairs >= 4 * MAX_STRIP * (int64_t)(num_sms > 0 ? num_sms : 152) ? MAX_STRIP : 1;
+}
+
+bool kick_sym_single_ok(int32_t npl, int num_sms) {
+    const int64_t nt = (npl + TS - 1) / TS;
+    return nt * (nt + 1) / 2 >= 32 * (int64_t)(num_sms > 0 ? num_sms : 152);
+}
+
+int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<int4> &items,
+                       std::vector<int32_t> &sbase, int64_t *npair_slots) {
     items.clear();
     sbase.assign(2 * (size_t)nsys, 0);
     std::vector<int64_t> cost;
@@ -292,8 +310,8 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &item
         sbase[2 * s + 1] = (int32_t)nps;
         auto rows = [&](int T) { return (int64_t)std::min(TS, npl[s] - T * TS); };
         for (int I = 0; I < nt; I++)
-            for (int J0 = I; J0 < nt; J0 += STRIP) {
-                const int nJ = std::min(STRIP, nt - J0);
+            for (int J0 = I; J0 < nt; J0 += strip) {
+                const int nJ = std::min(strip, nt - J0);
                 items.push_back(make_int4(s, I, J0 | (nJ << 24), (int)nrs++));
                 int64_t c = 0;
                 for (int J = J0; J < J0 + nJ; J++) c += rows(I) * rows(J);
@@ -336,14 +354,85 @@ int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, 
     return launch_status(c, "kick_mixed_sym");
 }
 
-int kick_mixed_sym_reduce(swg_ctx *c, int64_t n, const int32_t *psys, const int32_t *poff, const int32_t *npl,
-                          const int32_t *sbase, const float *rpart, const float *ppart, double *acc, int acc_is_zero,
-                          const int32_t *sys_flag, int phase) {
+int kick_mixed_sym_reduce(swg_ctx *c, int strip, int64_t n, const int32_t *psys, const int32_t *poff,
+                          const int32_t *npl, const int32_t *sbase, const float *rpart, const float *ppart,
+                          double *acc, int acc_is_zero, const int32_t *sys_flag, int phase) {
     if (n <= 0) return SWG_OK;
     k_kick_sym_reduce<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(n, psys, poff, npl, sbase, rpart, ppart, acc,
-                                                                      acc_is_zero, sys_flag, phase);
+                                                                      acc_is_zero, sys_flag, phase, strip);
     c->launches++;
     return launch_status(c, "kick_sym_reduce");
+}
+
+// ---- one system (the C ABI kicks and the single-system step loops)
+// Plan of the last system size seen by the context: items, [poff = 0, npl, slot bases],
+// slots, split partners and a queue head.
+struct SymSingle {
+    int32_t npl = -1;
+    int nitems = 0, strip = 1;
+    int4 *items = nullptr;
+    int32_t *meta = nullptr;
+    float *part = nullptr, *ppart = nullptr;
+    float4 *pA = nullptr, *pB = nullptr;
+    unsigned *head = nullptr;
+    void release() {
+        void *ptrs[] = {items, meta, part, pA, pB, head};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        *this = SymSingle();
+    }
+};
+
+void kick_sym_single_free(swg_ctx *c) {
+    if (!c->sym_single) return;
+    SymSingle *p = (SymSingle *)c->sym_single;
+    p->release();
+    delete p;
+    c->sym_single = nullptr;
+}
+
+template <typename T>
+static int sym_alloc(swg_ctx *c, T **p, size_t n) {
+    const cudaError_t e = cudaMalloc((void **)p, (n ? n : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        c->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return SWG_ERR_NOMEM;
+    }
+    return SWG_OK;
+}
+
+int kick_mixed_sym_single(swg_ctx *c, int32_t npl, const double *r, const double *Gm, const double *R, double *acc,
+                          int acc_is_zero) {
+    if (npl <= 0) return SWG_OK;
+    if (!c->sym_single) c->sym_single = new SymSingle();
+    SymSingle &p = *(SymSingle *)c->sym_single;
+    if (p.npl != npl) {
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "sync"));
+        p.release();
+        std::vector<int4> items;
+        std::vector<int32_t> base;
+        int64_t npair = 0;
+        p.strip = kick_sym_strip(1, &npl, c->num_sms);
+        const int64_t nrecv = kick_sym_items(1, &npl, p.strip, items, base, &npair);
+        const int32_t meta[4] = {0, npl, base[0], base[1]};
+        SWG_TRY(sym_alloc(c, &p.items, items.size()));
+        SWG_TRY(sym_alloc(c, &p.meta, 4));
+        SWG_TRY(sym_alloc(c, &p.part, (size_t)(6 * nrecv + 3 * npair) * TS));
+        SWG_TRY(sym_alloc(c, &p.pA, (size_t)npl));
+        SWG_TRY(sym_alloc(c, &p.pB, (size_t)npl));
+        SWG_TRY(sym_alloc(c, &p.head, 1));
+        SWG_TRY(cuda_status(c, cudaMemcpy(p.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice),
+                            "upload"));
+        SWG_TRY(cuda_status(c, cudaMemcpy(p.meta, meta, sizeof(meta), cudaMemcpyHostToDevice), "upload"));
+        p.ppart = p.part + (size_t)6 * nrecv * TS;
+        p.nitems = (int)items.size();
+        p.npl = npl;
+    }
+    SWG_TRY(kick_split_launch(c, npl, r, Gm, R, p.pA, p.pB));
+    SWG_TRY(kick_mixed_sym_batched(c, R != nullptr, p.nitems, p.items, p.meta, p.meta + 1, p.meta + 2, p.pA, p.pB,
+                                   p.part, p.ppart, p.head));
+    return kick_mixed_sym_reduce(c, p.strip, npl, nullptr, p.meta, p.meta + 1, p.meta + 2, p.part, p.ppart, acc,
+                                 acc_is_zero);
 }
 
 }  // namespace swg

@@ -111,6 +111,7 @@ struct swg_ctx {
     void *events[16] = {nullptr};  // measurement events (cudaEvent_t), created on first use
     std::vector<void *> systems;   // live swg_system objects, destroyed with the context
     std::vector<void *> ensembles; // live swg_ensemble objects, destroyed with the context
+    void *sym_single = nullptr;    // cached plan of the one-system symmetric kick (kick_sym.cu)
 };
 
 namespace swg {
@@ -177,14 +178,23 @@ int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_
 // pair slots.  A receiver slot holds 6 * KICK_SYM_TILE floats, a pair slot 3 * KICK_SYM_TILE;
 // kick_mixed_sym_reduce writes acc (+)= the sums.
 constexpr int KICK_SYM_TILE = 128;
-int64_t kick_sym_items(int32_t nsys, const int32_t *npl, std::vector<int4> &items, std::vector<int32_t> &sbase,
-                       int64_t *npair_slots);
+// strip: tiles J per item (4, or 1 when that would leave too few items to fill the GPU)
+int kick_sym_strip(int32_t nsys, const int32_t *npl, int num_sms);
+int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<int4> &items,
+                       std::vector<int32_t> &sbase, int64_t *npair_slots);
+// a single system has enough tile pairs to fill the GPU (else the broadcast kernel is faster)
+bool kick_sym_single_ok(int32_t npl, int num_sms);
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
                            float *ppart, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
-int kick_mixed_sym_reduce(swg_ctx *c, int64_t n, const int32_t *psys, const int32_t *poff, const int32_t *npl,
-                          const int32_t *sbase, const float *rpart, const float *ppart, double *acc, int acc_is_zero,
-                          const int32_t *sys_flag = nullptr, int phase = 0);
+// one system (psys == nullptr below): plan cached in the context for the last npl; acc (+)= the
+// pair accelerations (radius rule with R, else j != i); no GMTINY bodies
+int kick_mixed_sym_single(swg_ctx *c, int32_t npl, const double *r, const double *Gm, const double *R, double *acc,
+                          int acc_is_zero);
+void kick_sym_single_free(swg_ctx *c);
+int kick_mixed_sym_reduce(swg_ctx *c, int strip, int64_t n, const int32_t *psys, const int32_t *poff,
+                          const int32_t *npl, const int32_t *sbase, const float *rpart, const float *ppart,
+                          double *acc, int acc_is_zero, const int32_t *sys_flag = nullptr, int phase = 0);
 // autotune.cu -- cache of tuned kernel shapes: key of (device, kind, size bucket); the cached
 // variant or -1; store (kept for the process and appended to the cache file)
 std::string tune_key(int device, const char *kind, int bucket);

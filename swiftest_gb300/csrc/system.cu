@@ -302,6 +302,8 @@ int accel_int_pl(swg_system *s, int acc_is_zero) {
     const bool symba = s->integrator == SWG_SYMBA;
     const double *rad = (symba || s->lclose) ? s->radius : nullptr;
     const int32_t nplm = symba ? s->nplm : s->npl;
+    if (s->precision == SWG_MIXED && nplm == s->npl && kick_sym_single_ok(s->npl, c->num_sms))
+        return kick_mixed_sym_single(c, s->npl, s->rh, s->Gmass, rad, s->ah, acc_is_zero);
     if (s->precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, s->npl, s->npl);
         SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->npl, s->npl, nch)));

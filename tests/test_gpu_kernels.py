@@ -66,7 +66,7 @@ def _relerr(a, b):
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
 
 
-@pytest.mark.parametrize("npl", [64, 1000, 4096])
+@pytest.mark.parametrize("npl", [64, 1000, 4096, 16384])  # 16384: the symmetric kernel
 def test_kick_mixed_plpl_tolerance(ctx, npl):
     cb, pl, _ = _sys(8, npl, 0)
     g = ctx.kick_getacch_int_all_tri_pl(pl["rh"], pl["Gmass"], pl["radius"], precision=SWG_MIXED)
@@ -87,14 +87,20 @@ def test_kick_mixed_tp_tolerance(ctx, ntp, npl):
     assert np.sqrt(np.mean(e ** 2)) < 1e-6
 
 
+@pytest.mark.parametrize("npl", [1000, 16000])  # broadcast kernel, symmetric kernel
 @pytest.mark.parametrize("guard", ["radius", "index"])
-def test_kick_mixed_close_and_overlapping_pairs(ctx, guard):
-    # bodies placed next to others in distant tiles: pairs within the sum of the radii are
-    # dropped by the radius rule, a close pair just outside it is kept and dominates
-    cb, pl, _ = _sys(12, 1000, 0)
+def test_kick_mixed_close_and_overlapping_pairs(ctx, guard, npl):
+    # bodies placed next to others: pairs within the sum of the radii are dropped by the
+    # radius rule, a close pair just outside it is kept and dominates.  Pairs across tiles,
+    # within one 128-body tile across 32-body sub-tiles (10, 100) and within one sub-tile
+    # (40, 45)
+    cb, pl, _ = _sys(12, npl, 0)
     rh, R = pl["rh"].copy(), pl["radius"].copy()
     u = np.array([0.6, -0.48, 0.64])
-    for i, j, sep in [(5, 700, 1e-6), (300, 950, 1e-6), (513, 2, 3e-6), (140, 260, 1e-4)]:
+    f = npl // 1000
+    pairs = [(5, 700 * f, 1e-6), (300 * f, 950 * f, 1e-6), (513 * f, 2, 3e-6), (140 * f, 260 * f, 1e-4),
+             (10, 100, 2e-6), (40, 45, 2e-6)]
+    for i, j, sep in pairs:
         rh[j] = rh[i] + sep * u
         R[i] = R[j] = 1e-5
     Rk = R if guard == "radius" else None
@@ -106,7 +112,7 @@ def test_kick_mixed_close_and_overlapping_pairs(ctx, guard):
         assert e.max() < 2e-5, e.max()
     else:  # without the radius rule the 1e-6 pairs are kept: FP32 r^-3 of a 1e-6 separation
         keep = np.ones(len(e), bool)
-        keep[[5, 700, 300, 950, 513, 2]] = False
+        keep[[b for i, j, sep in pairs if sep < 1e-5 for b in (i, j)]] = False
         assert e[keep].max() < 2e-5, e[keep].max()
         assert e[~keep].max() < 1e-3, e[~keep].max()
 
