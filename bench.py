@@ -7,7 +7,8 @@ total for seed 0), masses log-uniform in [1e-11, 1e-7] Msun, a in [0.5, 2] AU, e
 Rayleigh(0.02), dt = 0.002 yr, 1-Hill-radius encounter radius (RHSCALE = 1), TRIANGULAR
 level-0 checks, recursive encounter kicks in FP64.  A step advances every system by one
 symba_step_system.  ``--workload c1`` runs the single-system C1 disk (2000 pl + 10 000 tp)
-instead, ``--workload c3`` the batched HELIO ensemble (512 systems with test particles).
+instead, ``--workload c3`` the batched HELIO ensemble (512 systems with test particles),
+``--workload c3w`` the same systems stepped by WHM.
 
 ``value``: body-steps/s of the mixed-precision batched path (FP32 pair kicks with
 float-float sums; FP64 drift, encounter decisions, recursion) with the state resident in
@@ -54,7 +55,7 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="c4", choices=["c4", "c3", "c1"])
+    p.add_argument("--workload", default="c4", choices=["c4", "c3", "c3w", "c1"])
     p.add_argument("--nsys", type=int, default=None, help="first NSYS systems of the C4 ensemble")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     return p.parse_args()
@@ -152,6 +153,39 @@ class C3(C4):
             if t_all > budget_s:
                 break
         return bs, t_all, f"{steps_per_system} HELIO step(s) of each of the first {nsys} C3 systems ({bs} body-steps)"
+
+
+class C3W(C3):
+    """The batched WHM ensemble: the C3 systems stepped by WHM (Jacobi coordinates)."""
+
+    def __init__(self, args):
+        from swiftest_gb300 import initial_conditions as IC
+        self.E = IC.make_ensemble("C3", nsys=args.nsys, integrator="WHM")
+        self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
+        n = [int(x) for x in self.E["npl"]]
+        self.plpl_pairs = float(sum(k * (k - 1) for k in n))
+        self.pairs_per_step = float(sum(k * (k - 1) + 5 * k * k for k in n))  # one evaluation per step
+
+    def config(self, precision):
+        c = super().config(precision)
+        c["workload"] = c["workload"].replace("C3 batched HELIO ensemble", "C3 batched WHM ensemble")
+        return c
+
+    def oracle_sample(self, budget_s, steps_per_system=1):
+        from oracle import oracle as O
+        from swiftest_gb300 import initial_conditions as IC
+        cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
+        bs, t_all, nsys = 0, 0.0, 0
+        for pl, tp in self.E["systems"]:
+            s = O.OracleSystem("WHM", cb, pl, tp, dt=self.E["dt"], lclose=True)
+            t0 = time.perf_counter()
+            s.step(steps_per_system)
+            t_all += time.perf_counter() - t0
+            bs += (len(pl["Gmass"]) + len(tp["rh"])) * steps_per_system
+            nsys += 1
+            if t_all > budget_s:
+                break
+        return bs, t_all, f"{steps_per_system} WHM step(s) of each of the first {nsys} C3 systems ({bs} body-steps)"
 
 
 class C1:
@@ -353,7 +387,7 @@ def cpu_baseline(wl, budget_s):
 def reference_arm(args, world, rank):
     if rank != 0:
         return 0
-    wl = {"c4": C4, "c3": C3, "c1": C1}[args.workload](args)
+    wl = {"c4": C4, "c3": C3, "c3w": C3W, "c1": C1}[args.workload](args)
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     from oracle import oracle as O
@@ -397,7 +431,7 @@ def main():
     from swiftest_gb300 import build as B
     B.build()
     from swiftest_gb300.api import Context
-    wl = {"c4": C4, "c3": C3, "c1": C1}[args.workload](args)
+    wl = {"c4": C4, "c3": C3, "c3w": C3W, "c1": C1}[args.workload](args)
     ctx = Context(local)
     clocks = ClockSampler(local)
     if td:

@@ -157,13 +157,16 @@ int swg_system_get_state_async(swg_system *sys, double *rh, double *vh, double *
 
 /* ---- batched ensembles of independent systems -------------------------------------
  * No single counterpart in the reference, which integrates one system per run: an
- * ensemble is many runs of helio_step_system / symba_step_system (helio_step.f90:14-119,
- * symba_step.f90:14-331) advanced together, each system taking exactly the steps it
- * would take alone (bit-identical in SWG_FP64).  Systems are packed CSR-style: arrays
- * of massive bodies are the concatenation of every system's (3, npl[s]) block in system
- * order (test particles likewise with ntp[s]), each block sorted as the reference's
- * initialize leaves it (by mass, descending).  All systems share dt; GMTINY is not
- * supported.  integrator: SWG_HELIO or SWG_SYMBA (TRIANGULAR level-0 checks). */
+ * ensemble is many runs of whm_step_system / helio_step_system / symba_step_system
+ * (whm_step.f90:14-104, helio_step.f90:14-119, symba_step.f90:14-331) advanced together,
+ * each system taking exactly the steps it would take alone (bit-identical in SWG_FP64).
+ * Systems are packed CSR-style: arrays of massive bodies are the concatenation of every
+ * system's (3, npl[s]) block in system order (test particles likewise with ntp[s]), each
+ * block ordered as the reference's initialize leaves it (HELIO/SyMBA: by mass, descending;
+ * WHM: input order).  All systems share dt; GMTINY is not supported.  integrator: SWG_WHM,
+ * SWG_HELIO or SWG_SYMBA (TRIANGULAR level-0 checks).  A WHM ensemble whose Danby drift
+ * fails for a massive body returns SWG_ERR_DRIFT from the step call (the reference stops
+ * the run). */
 typedef struct swg_ensemble swg_ensemble;
 int swg_ensemble_create(swg_ctx *ctx, int integrator, int32_t nsys, const int32_t *npl, const int32_t *ntp,
                         swg_ensemble **ens);
@@ -188,9 +191,9 @@ int swg_ensemble_plpl_list(swg_ensemble *ens, int32_t sys, int64_t cap, int64_t 
 int swg_ensemble_set_state(swg_ensemble *ens, const double *rh, const double *vh, const double *trh,
                            const double *tvh);
 int swg_ensemble_get_state_async(swg_ensemble *ens, double *rh, double *vh, double *trh, double *tvh);
-/* HELIO ensembles replay each step as a CUDA graph captured after the first step (default
- * on; results are identical either way).  SyMBA steps always run eagerly: each takes one
- * host decision (the encounter-list sizes). */
+/* WHM and HELIO ensembles replay each step as a CUDA graph captured after the first step
+ * (default on; results are identical either way).  SyMBA steps always run eagerly: each
+ * takes one host decision (the encounter-list sizes). */
 int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
 /* Kernel of the batched mixed-precision kick (no counterpart in the reference).  By
  * default (variant -1) the pl-pl kick evaluates each pair once for both bodies

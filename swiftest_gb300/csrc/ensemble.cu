@@ -106,6 +106,12 @@ struct swg_ensemble {
     unsigned long long *ndiscard = nullptr;  // tp removed by the scan
     DevBuf rec_scratch, rows;
     DevBuf pair_terms;  // pl-pl pool: six pair terms and a kept flag per entry
+    // WHM: per-body eta / muj (whm_util_set_mu_eta_pl), Jacobi coordinates, ir3 terms, drift
+    // flags, the per-system ah0 of the tp kick, first-step flag (host: all systems start together)
+    double *eta = nullptr, *muj = nullptr, *xj = nullptr, *vj = nullptr, *ir3h = nullptr, *ir3j = nullptr,
+           *whm_ah0 = nullptr;
+    int32_t *iflag = nullptr, *whm_fail = nullptr;
+    int whm_first = 1;
     // chunks of the mixed path's per-system sums: (system, first body, bodies, chunk index in
     // its system), each system's (first chunk, chunks), four partial sums per chunk
     int4 *chunks = nullptr;
@@ -500,17 +506,69 @@ __global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e, int 
     blk_symba_recursion(a);
 }
 
+// ---- WHM (whm_step.f90, whm_kick.f90, whm_coord.f90) of every system: one block per system
+// for the reference's serial Jacobi sums (one thread, in the reference's order)
+enum { WHM_H2J = 0, WHM_J2H = 1, WHM_VH2VJ = 2 };
+__global__ void k_ens_whm_coord(int mode, const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+                                const double *Gm, const double *eta, double *rh, double *vh, double *xj, double *vj) {
+    const int s = blockIdx.x;
+    if (npl[s] == 0) return;
+    __shared__ WhmScratch sh;
+    const size_t o = poff[s];
+    if (mode == WHM_H2J)
+        blk_whm_h2j(npl[s], Gm + o, eta + o, rh + 3 * o, vh + 3 * o, xj + 3 * o, vj + 3 * o, sh);
+    else if (mode == WHM_J2H)
+        blk_whm_j2h(npl[s], Gm + o, eta + o, xj + 3 * o, vj + 3 * o, rh + 3 * o, vh + 3 * o, sh);
+    else
+        blk_whm_vh2vj(npl[s], Gm + o, eta + o, vh + 3 * o, vj + 3 * o, sh);
+}
+__global__ void k_ens_whm_accel(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl, const double *Gm,
+                                const double *__restrict__ GMcb, const double *rh, const double *xj,
+                                const int32_t *lmask, double *ir3h, double *ir3j, double *ah) {
+    const int s = blockIdx.x;
+    if (npl[s] == 0) return;
+    __shared__ WhmScratch sh;
+    const size_t o = poff[s];
+    blk_whm_accel_pl(npl[s], Gm + o, GMcb[s], rh + 3 * o, xj + 3 * o, lmask + o, ir3h + o, ir3j + o, ah + 3 * o, sh);
+}
+// ah0 of whm_kick_getacch_tp (whm_kick.f90:70-122) per system at the pl positions rp
+__global__ void k_ens_whm_ah0(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl, const double *Gm,
+                              const double *rp, double *ah0) {
+    const int s = blockIdx.x;
+    __shared__ WhmScratch sh;
+    const size_t o = poff[s];
+    blk_whm_ah0(Gm + o, rp + 3 * o, npl[s], ah0 + 3 * s, sh);
+}
+// tah = ah0 of the test particle's system (masked), before the pair kick adds to it
+__global__ void k_ens_whm_tp_ah0(int64_t ntp, const int32_t *__restrict__ tsys, const int32_t *__restrict__ tlmask,
+                                 const double *__restrict__ ah0, double *tah) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= ntp || !tlmask[i]) return;
+    const double *a = ah0 + 3 * tsys[i];
+    for (int d = 0; d < 3; d++) tah[3 * i + d] = 0.0 + a[d];
+}
+// whm_drift_pl's failure handling (whm_drift.f90:14-58): status, mask and a run-wide flag
+__global__ void k_ens_whm_drift_status(int64_t n, const int32_t *__restrict__ iflag, int32_t *status, int32_t *lmask,
+                                       int32_t *fail) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && iflag[i] != 0) {
+        status[i] = ST_DISCARDED_DRIFTERR;
+        lmask[i] = 0;
+        atomicOr(fail, 1);
+    }
+}
+
 // energy / momentum per system: totals (one block each) and potential rows (flat)
 __global__ void __launch_bounds__(RB) k_ens_energy_final(const int32_t *__restrict__ poff,
                                                          const int32_t *__restrict__ npl, const double *rh,
                                                          const double *vh, const double *vb, const double *Gm,
                                                          const double *radius, const int32_t *status,
-                                                         const double *__restrict__ GMcb, int lclose,
+                                                         const double *__restrict__ GMcb, int lclose, int whm,
                                                          const double *rows, double *rb, double *out) {
     const int s = blockIdx.x;
     __shared__ SumScratch sh;
     const size_t o = poff[s];
-    blk_energy_final(npl[s], 0, rh + 3 * o, vh + 3 * o, vb + 3 * o, Gm + o, radius + o, status + o, GMcb[s], lclose,
+    blk_energy_final(npl[s], whm, rh + 3 * o, vh + 3 * o, vb + 3 * o, Gm + o, radius + o, status + o, GMcb[s], lclose,
                      rows + o, rb + 3 * o, out + 9 * s, sh);
 }
 __global__ void k_ens_energy_rows(int64_t n, const int32_t *__restrict__ psys, const int32_t *__restrict__ poff,
@@ -627,12 +685,13 @@ int size_bucket(const swg_ensemble *e, int k) {
 // One mixed kick of kind k with the given shape and items into acc (overwritten); the
 // partners must be split into kA/kB.
 int mixed_kick(swg_ensemble *e, int k, int variant, const int4 *items, int nitems, double *acc, bool rad,
-               unsigned *head, const int32_t *flag, int phase) {
+               unsigned *head, const int32_t *flag, int phase, int acc_is_zero = 1) {
     if (k == 0)
         return kick_mixed_batched(e->c, variant, false, rad, nitems, items, e->poff, e->poff, e->npl, e->rh,
-                                  rad ? e->radius : nullptr, e->kA, e->kB, nullptr, acc, 1, head, flag, phase);
+                                  rad ? e->radius : nullptr, e->kA, e->kB, nullptr, acc, acc_is_zero, head, flag,
+                                  phase);
     return kick_mixed_batched(e->c, variant, true, false, nitems, items, e->toff, e->poff, e->npl, e->trh, nullptr,
-                              e->kA, e->kB, e->tlmask, acc, 1, head);
+                              e->kA, e->kB, e->tlmask, acc, acc_is_zero, head);
 }
 
 // Scratch of the timing runs, released on every exit path.
@@ -735,7 +794,7 @@ void reset_kick_plans(swg_ensemble *e) {
 
 // pl-pl accelerations into ah (helio_kick_getacch_int_pl / symba_kick_getacch_int_pl) of all
 // systems, or (flag != nullptr) of the systems whose flag equals phase, on c->stream.
-int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr, int phase = 0) {
+int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr, int phase = 0, int acc_is_zero = 1) {
     swg_ctx *c = e->c;
     const bool rad = e->integrator == SWG_SYMBA || e->lclose;
     const double *R = rad ? e->radius : nullptr;
@@ -746,12 +805,12 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
                                            e->sym_part, e->sym_ppart, head, flag, phase));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                         e->sym_ppart, e->ah, 1, flag, phase);
+                                         e->sym_ppart, e->ah, acc_is_zero, flag, phase);
         }
-        return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase);
+        return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase, acc_is_zero);
     }
-    return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah, 1, flag,
-                                  phase);
+    return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah,
+                                  acc_is_zero, flag, phase);
 }
 
 // Runs f with the context's stream temporarily replaced (single host thread).
@@ -1202,6 +1261,91 @@ int ens_step(swg_ensemble *e, double dt) {
     return L(c, "ens_finish");
 }
 
+// ---- WHM step of every system (whm_step_system, whm_step.f90:14-104).  The first-step flag
+// is shared (all systems start together), so after the first step every step runs the same
+// launch sequence and is replayed from a CUDA graph.
+// whm_kick_vh_pl (whm_kick.f90:218-262): accelerations (whm_kick_getacch_pl: ah0, ah1, ah2,
+// then the pair kick added on top) and vh += ah dt
+int whm_accel_pl(swg_ensemble *e) {
+    swg_ctx *c = e->c;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(e->ah, 0, sizeof(double) * 3 * e->NPL, c->stream), "memset"));
+    k_ens_whm_accel<<<e->nsys, 256, 0, c->stream>>>(e->poff, e->npl, e->Gmass, e->GMcb, e->rh, e->xj, e->lmask,
+                                                    e->ir3h, e->ir3j, e->ah);
+    SWG_TRY(L(c, "ens_whm_accel"));
+    ProfScope ps(e->prof, c->stream, PROF_KICK_PL);
+    return accel_int_pl(e, e->head, nullptr, 0, 0);
+}
+int whm_coord(swg_ensemble *e, int mode) {
+    k_ens_whm_coord<<<e->nsys, 256, 0, e->c->stream>>>(mode, e->poff, e->npl, e->Gmass, e->eta, e->rh, e->vh, e->xj,
+                                                       e->vj);
+    return L(e->c, "ens_whm_coord");
+}
+int whm_kick_vh_pl(swg_ensemble *e, double dt, int lbeg) {
+    swg_ctx *c = e->c;
+    if (!lbeg || e->whm_first) {
+        if (lbeg) SWG_TRY(whm_coord(e, WHM_H2J));
+        SWG_TRY(whm_accel_pl(e));
+    }
+    k_kick_update<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->vh, e->ah, e->lmask, dt, e->rh,
+                                                                 lbeg ? e->rbeg : e->rend);
+    return L(c, "kick_update_whm");
+}
+// whm_kick_vh_tp (whm_kick.f90:265-318) with whm_kick_getacch_tp (:70-122): tah = ah0 of the
+// system at rp, plus the pl-tp pair kick
+int whm_accel_tp(swg_ensemble *e, int lbeg) {
+    swg_ctx *c = e->c;
+    const double *rp = lbeg ? e->rbeg : e->rend;
+    k_ens_whm_ah0<<<e->nsys, 256, 0, c->stream>>>(e->poff, e->npl, e->Gmass, rp, e->whm_ah0);
+    SWG_TRY(L(c, "ens_whm_ah0"));
+    k_ens_whm_tp_ah0<<<grid_for(e->NTP, 256), 256, 0, c->stream>>>(e->NTP, e->tsys, e->tlmask, e->whm_ah0, e->tah);
+    SWG_TRY(L(c, "ens_whm_tp_ah0"));
+    ProfScope ps(e->prof, c->stream, PROF_KICK_TP);
+    if (e->precision == SWG_MIXED) {
+        // the partner split of the pl kick just before holds rp (rbeg or rend)
+        SWG_TRY(ensure_kick_plan(e, 1, false, e->head, nullptr, 0));
+        return mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, e->head, nullptr, 0, 0);
+    }
+    return kick_tp_fp64_batched(c, e->n_ftp, e->it_ftp, e->toff, e->ntp, e->poff, e->npl, e->trh, rp, e->Gmass,
+                                e->tlmask, e->tah, 0);
+}
+int whm_kick_vh_tp(swg_ensemble *e, double dt, int lbeg, bool first) {
+    swg_ctx *c = e->c;
+    if (first) SWG_TRY(whm_accel_tp(e, 1));
+    if (!lbeg) SWG_TRY(whm_accel_tp(e, 0));
+    k_kick_update<<<grid_for(e->NTP, 128), 128, 0, c->stream>>>((int)e->NTP, e->tvh, e->tah, e->tlmask, dt, nullptr,
+                                                                 nullptr);
+    return L(c, "kick_update_whm_tp");
+}
+int whm_ens_step(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    const double dth = 0.5 * dt;
+    const bool first_tp = e->whm_first != 0;
+    if (e->NPL > 0) {
+        SWG_TRY(whm_kick_vh_pl(e, dth, 1));
+        e->whm_first = 0;
+        SWG_TRY(whm_coord(e, WHM_VH2VJ));
+        {
+            ProfScope ps(e->prof, c->stream, PROF_DRIFT);
+            SWG_TRY(drift_all(c, e->muj, 0.0, e->xj, e->vj, (int32_t)e->NPL, 0, 0.0, dt, e->lmask, e->iflag));
+        }
+        k_ens_whm_drift_status<<<grid_for(e->NPL, 256), 256, 0, c->stream>>>(e->NPL, e->iflag, e->status, e->lmask,
+                                                                             e->whm_fail);
+        SWG_TRY(L(c, "ens_whm_drift_status"));
+        SWG_TRY(whm_coord(e, WHM_J2H));
+        SWG_TRY(whm_kick_vh_pl(e, dth, 0));
+    }
+    if (e->NTP > 0) {
+        SWG_TRY(whm_kick_vh_tp(e, dth, 1, first_tp));
+        {
+            ProfScope ps(e->prof, c->stream, PROF_DRIFT);
+            SWG_TRY(drift_masked(c, 0.0, e->trh, e->tvh, (int32_t)e->NTP, nullptr, -1, dt, e->tstatus, nullptr,
+                                 e->GMcb, e->tsys, !exact(e)));
+        }
+        SWG_TRY(whm_kick_vh_tp(e, dth, 0, false));
+    }
+    return SWG_OK;
+}
+
 // swiftest_discard_pl_tp of every system (src/swiftest/swiftest_discard.f90:244-290), after
 // each step when close encounters are checked, on the pl-tp items of the encounter check.
 int discard_step(swg_ensemble *e) {
@@ -1224,7 +1368,8 @@ int swg_ensemble_destroy(swg_ensemble *e);
 
 int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t *npl, const int32_t *ntp,
                         swg_ensemble **out) {
-    if (!c || !out || nsys <= 0 || !npl || (integrator != SWG_HELIO && integrator != SWG_SYMBA)) return SWG_ERR_ARG;
+    if (!c || !out || nsys <= 0 || !npl || (integrator != SWG_WHM && integrator != SWG_HELIO && integrator != SWG_SYMBA))
+        return SWG_ERR_ARG;
     int64_t NPL = 0, NTP = 0;
     for (int s = 0; s < nsys; s++) {
         const int32_t m = ntp ? ntp[s] : 0;
@@ -1297,6 +1442,16 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->tflag, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->ndiscard, 1);
     e->h_pend.assign(S, 0);
+    if (integrator == SWG_WHM) {
+        double **wd[] = {&e->eta, &e->muj, &e->ir3h, &e->ir3j};
+        for (auto p : wd)
+            if (rc == SWG_OK) rc = dalloc(c, p, n);
+        if (rc == SWG_OK) rc = dalloc(c, &e->xj, 3 * n);
+        if (rc == SWG_OK) rc = dalloc(c, &e->vj, 3 * n);
+        if (rc == SWG_OK) rc = dalloc(c, &e->whm_ah0, 3 * S);
+        if (rc == SWG_OK) rc = dalloc(c, &e->iflag, n);
+        if (rc == SWG_OK) rc = dalloc(c, &e->whm_fail, 1);
+    }
     if (rc == SWG_OK) rc = ensure(c, e->rows, sizeof(double) * 4 * n);
     if (rc == SWG_OK) {
         cudaError_t err = cudaMallocHost((void **)&e->h_flags, 64);
@@ -1334,7 +1489,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eout};
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
@@ -1417,6 +1572,37 @@ int swg_ensemble_initialize(swg_ensemble *e) {
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->enc_steps, 0, sizeof(int32_t) * e->nsys, c->stream), "init"));
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_out, 0, sizeof(int32_t) * 4, c->stream), "init"));
     SWG_TRY(upload(c, e->lfirst, first));
+    if (e->integrator == SWG_WHM) {  // whm_util_set_mu_eta_pl (whm_util.f90:175-198) per system
+        std::vector<double> Gm(e->NPL), eta(e->NPL), muj(e->NPL);
+        if (e->NPL > 0) {
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(Gm.data(), e->Gmass, 8 * e->NPL, cudaMemcpyDeviceToHost, c->stream),
+                                "init"));
+            SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "init"));
+        }
+        for (int s = 0; s < e->nsys; s++) {
+            const int32_t o = e->h_poff[s], n = e->h_npl[s];
+            if (n == 0) continue;
+            eta[o] = e->h_GMcb[s] + Gm[o];
+            muj[o] = eta[o];
+            for (int i = 1; i < n; i++) {
+                eta[o + i] = eta[o + i - 1] + Gm[o + i];
+                muj[o + i] = e->h_GMcb[s] * eta[o + i] / eta[o + i - 1];
+            }
+        }
+        SWG_TRY(upload(c, e->eta, eta));
+        SWG_TRY(upload(c, e->muj, muj));
+        SWG_TRY(cuda_status(c, cudaMemsetAsync(e->whm_fail, 0, sizeof(int32_t), c->stream), "init"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "init"));
+        e->whm_first = 1;
+        e->t = 0.0;
+        e->nchecks = 0;
+        e->eager_steps = 0;
+        if (e->graph) cudaGraphExecDestroy(e->graph);
+        e->graph = nullptr;
+        std::memset(e->stats, 0, sizeof(e->stats));
+        e->initialized = 1;
+        return SWG_OK;
+    }
     SWG_TRY(vh2vb_pl(e, false));
     SWG_TRY(tp_misc(e, CB_VB, 0.0, 5, -1));  // tp vb = vh + the central body's vb
     e->t = 0.0;
@@ -1437,14 +1623,14 @@ int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
     // one eager step (which also makes every lazy allocation and query) the step and its
     // discard scan are captured once as a CUDA graph and replayed.  SyMBA steps read the
     // encounter-list sizes on the host and run eagerly.
-    const bool graphable = e->integrator == SWG_HELIO && e->use_graph && !e->prof.on;
+    const bool graphable = e->integrator != SWG_SYMBA && e->use_graph && !e->prof.on;
     for (int32_t k = 0; k < nsteps; k++) {
         if (graphable && e->eager_steps > 0) {
             if (!e->graph) {
                 cudaGraph_t g = nullptr;
                 const int64_t l0 = c->launches;
                 SWG_TRY(cuda_status(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture"));
-                int rc = ens_step(e, e->dt);
+                int rc = e->integrator == SWG_WHM ? whm_ens_step(e, e->dt) : ens_step(e, e->dt);
                 if (rc == SWG_OK) rc = discard_step(e);
                 const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
                 SWG_TRY(rc);
@@ -1458,7 +1644,7 @@ int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
             SWG_TRY(cuda_status(c, cudaGraphLaunch(e->graph, c->stream), "graph launch"));
             c->launches += e->graph_launches;
         } else {
-            SWG_TRY(ens_step(e, e->dt));
+            SWG_TRY(e->integrator == SWG_WHM ? whm_ens_step(e, e->dt) : ens_step(e, e->dt));
             SWG_TRY(discard_step(e));
             e->eager_steps++;
         }
@@ -1468,10 +1654,18 @@ int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
         }
         e->t += e->dt;
     }
+    if (e->integrator == SWG_WHM && e->NPL > 0)
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->h_flags + 3, e->whm_fail, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                               c->stream),
+                            "flag"));
     SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "step"));
     if (e->h_flags[2] != 0) {
         e->c->err = "SyMBA local time step too small";
         return e->h_flags[2];
+    }
+    if (e->integrator == SWG_WHM && e->NPL > 0 && e->h_flags[3] != 0) {
+        e->c->err = "Danby drift failed for a massive body (WHM stops the run)";
+        return SWG_ERR_DRIFT;
     }
     return SWG_OK;
 }
@@ -1507,7 +1701,8 @@ int swg_ensemble_energy(swg_ensemble *e, double *out) {
     double *rows = (double *)e->rows.ptr, *rb = rows + n;
     // the totals kernel also writes rb, which the rows need: totals, rows, totals
     k_ens_energy_final<<<e->nsys, RB, 0, c->stream>>>(e->poff, e->npl, e->rh, e->vh, e->vb, e->Gmass, e->radius,
-                                                      e->status, e->GMcb, e->lclose, rows, rb, e->eout);
+                                                      e->status, e->GMcb, e->lclose, e->integrator == SWG_WHM, rows, rb,
+                                                      e->eout);
     SWG_TRY(L(c, "ens_energy_rb"));
     if (e->NPL > 0) {
         k_ens_energy_rows<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>(e->NPL, e->psys, e->poff, e->npl, rb,
@@ -1515,7 +1710,8 @@ int swg_ensemble_energy(swg_ensemble *e, double *out) {
         SWG_TRY(L(c, "ens_energy_rows"));
     }
     k_ens_energy_final<<<e->nsys, RB, 0, c->stream>>>(e->poff, e->npl, e->rh, e->vh, e->vb, e->Gmass, e->radius,
-                                                      e->status, e->GMcb, e->lclose, rows, rb, e->eout);
+                                                      e->status, e->GMcb, e->lclose, e->integrator == SWG_WHM, rows, rb,
+                                                      e->eout);
     SWG_TRY(L(c, "ens_energy_final"));
     SWG_TRY(cuda_status(c, cudaMemcpyAsync(out, e->eout, sizeof(double) * 9 * e->nsys, cudaMemcpyDeviceToHost,
                                            c->stream),

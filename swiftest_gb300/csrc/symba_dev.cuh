@@ -1000,6 +1000,211 @@ static __device__ void blk_energy_final(int n, int whm, const double *rh, const 
     }
 }
 
+// ---- WHM (Jacobi coordinates)
+// The reference's Jacobi conversions and the ah0 / ah2 accelerations are running sums over
+// the bodies in index order.  Here the whole block forms the terms (products and quotients)
+// into shared memory, one thread per component adds them in index order (the only serial
+// part: the additions, with the reference's operands and order, so FP64 results stay
+// bit-identical), and the block uses the running sums; bodies go through in chunks of WCH.
+constexpr int WCH = 512;
+struct WhmScratch {
+    double t[6][WCH];      // terms, then (in place) inclusive running sums
+    double run[6];         // running sums carried across chunks
+    double e[WCH];         // ah2: etaj per body
+    unsigned char m[WCH];  // ah2: the body's mask
+};
+
+// t[c][q] <- run[c] + t[c][0] + ... + t[c][q] for c < m (one thread per component)
+static __device__ __forceinline__ void whm_running(WhmScratch &sh, int m, int cnt) {
+    __syncthreads();
+    if (threadIdx.x < m) {
+        const int c = threadIdx.x;
+        double s = sh.run[c];
+        for (int q = 0; q < cnt; q++) {
+            s = s + sh.t[c][q];
+            sh.t[c][q] = s;
+        }
+        sh.run[c] = s;
+    }
+    __syncthreads();
+}
+
+// whm_coord_h2j_pl (whm_coord.f90:14-51)
+static __device__ void blk_whm_h2j(int n, const double *Gm, const double *eta, const double *rh, const double *vh,
+                                   double *xj, double *vj, WhmScratch &sh) {
+    if (n <= 0) return;
+    if (threadIdx.x < 3) {
+        xj[threadIdx.x] = rh[threadIdx.x];
+        vj[threadIdx.x] = vh[threadIdx.x];
+    }
+    if (threadIdx.x < 6) sh.run[threadIdx.x] = 0.0;
+    for (int c0 = 1; c0 < n; c0 += WCH) {
+        const int cnt = min(WCH, n - c0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int k = c0 + q - 1;
+            for (int d = 0; d < 3; d++) {
+                sh.t[d][q] = Gm[k] * rh[3 * k + d];
+                sh.t[3 + d][q] = Gm[k] * vh[3 * k + d];
+            }
+        }
+        whm_running(sh, 6, cnt);
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int i = c0 + q;
+            for (int d = 0; d < 3; d++) {
+                const double cap = sh.t[d][q] / eta[i - 1];
+                const double capv = sh.t[3 + d][q] / eta[i - 1];
+                xj[3 * i + d] = rh[3 * i + d] - cap;
+                vj[3 * i + d] = vh[3 * i + d] - capv;
+            }
+        }
+    }
+}
+// whm_coord_j2h_pl (:54-90)
+static __device__ void blk_whm_j2h(int n, const double *Gm, const double *eta, const double *xj, const double *vj,
+                                   double *rh, double *vh, WhmScratch &sh) {
+    if (n <= 0) return;
+    if (threadIdx.x < 3) {
+        rh[threadIdx.x] = xj[threadIdx.x];
+        vh[threadIdx.x] = vj[threadIdx.x];
+    }
+    if (threadIdx.x < 6) sh.run[threadIdx.x] = 0.0;
+    for (int c0 = 1; c0 < n; c0 += WCH) {
+        const int cnt = min(WCH, n - c0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int k = c0 + q - 1;
+            for (int d = 0; d < 3; d++) {
+                sh.t[d][q] = Gm[k] * xj[3 * k + d] / eta[k];
+                sh.t[3 + d][q] = Gm[k] * vj[3 * k + d] / eta[k];
+            }
+        }
+        whm_running(sh, 6, cnt);
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int i = c0 + q;
+            for (int d = 0; d < 3; d++) {
+                rh[3 * i + d] = xj[3 * i + d] + sh.t[d][q];
+                vh[3 * i + d] = vj[3 * i + d] + sh.t[3 + d][q];
+            }
+        }
+    }
+}
+// whm_coord_vh2vj_pl (:93-124)
+static __device__ void blk_whm_vh2vj(int n, const double *Gm, const double *eta, const double *vh, double *vj,
+                                     WhmScratch &sh) {
+    if (n <= 0) return;
+    if (threadIdx.x < 3) vj[threadIdx.x] = vh[threadIdx.x];
+    if (threadIdx.x < 3) sh.run[threadIdx.x] = 0.0;
+    for (int c0 = 1; c0 < n; c0 += WCH) {
+        const int cnt = min(WCH, n - c0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int k = c0 + q - 1;
+            for (int d = 0; d < 3; d++) sh.t[d][q] = Gm[k] * vh[3 * k + d];
+        }
+        whm_running(sh, 3, cnt);
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int i = c0 + q;
+            for (int d = 0; d < 3; d++) {
+                const double capv = sh.t[d][q] / eta[i - 1];
+                vj[3 * i + d] = vh[3 * i + d] - capv;
+            }
+        }
+    }
+}
+// whm_kick_getacch_ah0 (whm_kick.f90:125-149): ah0 = -sum mu_i rhp_i / |rhp_i|^3 in index
+// order, into out[3] (shared or global), visible to the block on return
+static __device__ void blk_whm_ah0(const double *mu, const double *rhp, int n, double *out, WhmScratch &sh) {
+    if (threadIdx.x < 3) sh.run[threadIdx.x] = 0.0;
+    for (int c0 = 0; c0 < n; c0 += WCH) {
+        const int cnt = min(WCH, n - c0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            const int i = c0 + q;
+            const double r2 =
+                rhp[3 * i] * rhp[3 * i] + rhp[3 * i + 1] * rhp[3 * i + 1] + rhp[3 * i + 2] * rhp[3 * i + 2];
+            const double ir3h = 1.0 / (r2 * sqrt(r2));
+            const double fac = mu[i] * ir3h;
+            for (int d = 0; d < 3; d++) sh.t[d][q] = -(fac * rhp[3 * i + d]);  // a - b == a + (-b)
+        }
+        whm_running(sh, 3, cnt);
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) out[threadIdx.x] = sh.run[threadIdx.x];
+    __syncthreads();
+}
+// whm_kick_getacch_pl (whm_kick.f90:14-67) up to accel_int, with set_ir3j (whm_util.f90:117-140),
+// ah1 (:152-179) and ah2 (:182-215), whole block
+static __device__ void blk_whm_accel_pl(int n, const double *Gm, double GMcb, const double *rh, const double *xj,
+                                        const int32_t *lmask, double *ir3h, double *ir3j, double *ah,
+                                        WhmScratch &sh) {
+    __shared__ double s_ah0[3];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double r2 = rh[3 * i] * rh[3 * i] + rh[3 * i + 1] * rh[3 * i + 1] + rh[3 * i + 2] * rh[3 * i + 2];
+        double ir = 1.0 / sqrt(r2);
+        ir3h[i] = ir / r2;
+        r2 = xj[3 * i] * xj[3 * i] + xj[3 * i + 1] * xj[3 * i + 1] + xj[3 * i + 2] * xj[3 * i + 2];
+        ir = 1.0 / sqrt(r2);
+        ir3j[i] = ir / r2;
+    }
+    blk_whm_ah0(Gm + 1, rh + 3, n - 1, s_ah0, sh);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * i + d] + s_ah0[d];
+        if (i >= 1 && lmask[i])
+            for (int d = 0; d < 3; d++) {
+                const double ah1j = xj[3 * i + d] * ir3j[i];
+                const double ah1h = rh[3 * i + d] * ir3h[i];
+                ah[3 * i + d] = ah[3 * i + d] + GMcb * (ah1j - ah1h);
+            }
+    }
+    // ah2: etaj = GMcb + the masked Gm[i-1] in order; ah2_i = ah2_(previous masked) + fac_i xj_i
+    if (threadIdx.x == 0) sh.run[3] = GMcb;
+    if (threadIdx.x < 3) sh.run[threadIdx.x] = 0.0;
+    for (int c0 = 1; c0 < n; c0 += WCH) {
+        const int cnt = min(WCH, n - c0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {  // stage the masks and Gm[i-1]
+            sh.m[q] = lmask[c0 + q] != 0;
+            sh.e[q] = Gm[c0 + q - 1];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double etaj = sh.run[3];
+            for (int q = 0; q < cnt; q++) {
+                if (!sh.m[q]) continue;
+                etaj = etaj + sh.e[q];
+                sh.e[q] = etaj;
+            }
+            sh.run[3] = etaj;
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            if (!sh.m[q]) continue;
+            const int i = c0 + q;
+            const double fac = Gm[i] * GMcb * ir3j[i] / sh.e[q];
+            for (int d = 0; d < 3; d++) sh.t[d][q] = fac * xj[3 * i + d];
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            const int d = threadIdx.x;
+            double a2 = sh.run[d];
+            for (int q = 0; q < cnt; q++) {
+                if (!sh.m[q]) continue;
+                a2 = a2 + sh.t[d][q];
+                sh.t[d][q] = a2;
+            }
+            sh.run[d] = a2;
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            if (!sh.m[q]) continue;
+            const int i = c0 + q;
+            for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * i + d] + sh.t[d][q];
+        }
+    }
+    __syncthreads();
+}
+
 // ---- flat per-body kernels of the step loops
 // v += a*dt (masked) ; optionally rcopy = r (set_beg_end)
 static __global__ void k_kick_update(int n, double *v, const double *__restrict__ a, const int32_t *__restrict__ lmask,

@@ -159,107 +159,32 @@ __global__ void __launch_bounds__(RB) k_energy_final(int n, int whm, const doubl
     blk_energy_final(n, whm, rh, vh, vbin, Gm, radius, status, GMcb, lclose, rows, rb, out, sh);
 }
 
-// ---- WHM serial coordinate kernels (whm_coord.f90:14-124) and accelerations (whm_kick.f90:125-215)
+// ---- WHM coordinate kernels and accelerations (block device code in symba_dev.cuh)
 __global__ void k_whm_h2j(int n, const double *Gm, const double *eta, const double *rh, const double *vh, double *xj,
                           double *vj) {
-    if (threadIdx.x != 0) return;
-    for (int d = 0; d < 3; d++) {
-        xj[d] = rh[d];
-        vj[d] = vh[d];
-    }
-    double sx[3] = {0, 0, 0}, sv[3] = {0, 0, 0};
-    for (int i = 1; i < n; i++)
-        for (int d = 0; d < 3; d++) {
-            sx[d] = sx[d] + Gm[i - 1] * rh[3 * (i - 1) + d];
-            sv[d] = sv[d] + Gm[i - 1] * vh[3 * (i - 1) + d];
-            const double cap = sx[d] / eta[i - 1];
-            const double capv = sv[d] / eta[i - 1];
-            xj[3 * i + d] = rh[3 * i + d] - cap;
-            vj[3 * i + d] = vh[3 * i + d] - capv;
-        }
+    __shared__ WhmScratch sh;
+    blk_whm_h2j(n, Gm, eta, rh, vh, xj, vj, sh);
 }
 __global__ void k_whm_j2h(int n, const double *Gm, const double *eta, const double *xj, const double *vj, double *rh,
                           double *vh) {
-    if (threadIdx.x != 0) return;
-    for (int d = 0; d < 3; d++) {
-        rh[d] = xj[d];
-        vh[d] = vj[d];
-    }
-    double sx[3] = {0, 0, 0}, sv[3] = {0, 0, 0};
-    for (int i = 1; i < n; i++)
-        for (int d = 0; d < 3; d++) {
-            sx[d] = sx[d] + Gm[i - 1] * xj[3 * (i - 1) + d] / eta[i - 1];
-            sv[d] = sv[d] + Gm[i - 1] * vj[3 * (i - 1) + d] / eta[i - 1];
-            rh[3 * i + d] = xj[3 * i + d] + sx[d];
-            vh[3 * i + d] = vj[3 * i + d] + sv[d];
-        }
+    __shared__ WhmScratch sh;
+    blk_whm_j2h(n, Gm, eta, xj, vj, rh, vh, sh);
 }
 __global__ void k_whm_vh2vj(int n, const double *Gm, const double *eta, const double *vh, double *vj) {
-    if (threadIdx.x != 0) return;
-    for (int d = 0; d < 3; d++) vj[d] = vh[d];
-    double sv[3] = {0, 0, 0};
-    for (int i = 1; i < n; i++)
-        for (int d = 0; d < 3; d++) {
-            sv[d] = sv[d] + Gm[i - 1] * vh[3 * (i - 1) + d];
-            const double capv = sv[d] / eta[i - 1];
-            vj[3 * i + d] = vh[3 * i + d] - capv;
-        }
+    __shared__ WhmScratch sh;
+    blk_whm_vh2vj(n, Gm, eta, vh, vj, sh);
 }
-// whm_kick_getacch_ah0 (:125-149)
-__device__ void d_whm_ah0(const double *mu, const double *rhp, int n, double *ah0) {
-    ah0[0] = ah0[1] = ah0[2] = 0.0;
-    for (int i = 0; i < n; i++) {
-        const double r2 = rhp[3 * i] * rhp[3 * i] + rhp[3 * i + 1] * rhp[3 * i + 1] + rhp[3 * i + 2] * rhp[3 * i + 2];
-        const double ir3h = 1.0 / (r2 * sqrt(r2));
-        const double fac = mu[i] * ir3h;
-        for (int d = 0; d < 3; d++) ah0[d] = ah0[d] - fac * rhp[3 * i + d];
-    }
-}
-// whm_kick_getacch_pl up to accel_int: ir3h/ir3j, ah0, ah1, ah2 (one block; serial parts in thread 0)
 __global__ void k_whm_accel_pl(int n, const double *Gm, double GMcb, const double *rh, const double *xj,
                                const int32_t *lmask, double *ir3h, double *ir3j, double *ah) {
-    __shared__ double s_ah0[3];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double r2 = rh[3 * i] * rh[3 * i] + rh[3 * i + 1] * rh[3 * i + 1] + rh[3 * i + 2] * rh[3 * i + 2];
-        double ir = 1.0 / sqrt(r2);
-        ir3h[i] = ir / r2;
-        r2 = xj[3 * i] * xj[3 * i] + xj[3 * i + 1] * xj[3 * i + 1] + xj[3 * i + 2] * xj[3 * i + 2];
-        ir = 1.0 / sqrt(r2);
-        ir3j[i] = ir / r2;
-    }
-    if (threadIdx.x == 0) d_whm_ah0(Gm + 1, rh + 3, n - 1, s_ah0);
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * i + d] + s_ah0[d];
-        if (i >= 1 && lmask[i])
-            for (int d = 0; d < 3; d++) {
-                const double ah1j = xj[3 * i + d] * ir3j[i];
-                const double ah1h = rh[3 * i + d] * ir3h[i];
-                ah[3 * i + d] = ah[3 * i + d] + GMcb * (ah1j - ah1h);
-            }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double ah2[3] = {0, 0, 0}, ah2o[3] = {0, 0, 0};
-        double etaj = GMcb;
-        for (int i = 1; i < n; i++) {
-            if (!lmask[i]) continue;
-            etaj = etaj + Gm[i - 1];
-            const double fac = Gm[i] * GMcb * ir3j[i] / etaj;
-            for (int d = 0; d < 3; d++) {
-                ah2[d] = ah2o[d] + fac * xj[3 * i + d];
-                ah[3 * i + d] = ah[3 * i + d] + ah2[d];
-                ah2o[d] = ah2[d];
-            }
-        }
-    }
+    __shared__ WhmScratch sh;
+    blk_whm_accel_pl(n, Gm, GMcb, rh, xj, lmask, ir3h, ir3j, ah, sh);
 }
 // whm_kick_getacch_tp ah0 part (:70-122): tah += ah0(rp) for masked tp ; zero first when requested
 __global__ void k_whm_tp_ah0(int ntp, int npl, const double *Gm, const double *rp, const int32_t *tlmask, double *tah,
                              int zero) {
+    __shared__ WhmScratch sh;
     __shared__ double s_ah0[3];
-    if (threadIdx.x == 0) d_whm_ah0(Gm, rp, npl, s_ah0);
-    __syncthreads();
+    blk_whm_ah0(Gm, rp, npl, s_ah0, sh);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntp; i += gridDim.x * blockDim.x) {
         if (!tlmask[i]) continue;
         for (int d = 0; d < 3; d++) tah[3 * i + d] = (zero ? 0.0 : tah[3 * i + d]) + s_ah0[d];
@@ -445,7 +370,7 @@ int whm_kick_vh_pl(swg_system *s, double dt, int lbeg) {
     swg_ctx *c = s->c;
     if (lbeg) {
         if (s->lfirst_pl) {
-            k_whm_h2j<<<1, 32, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->rh, s->vh, s->xj, s->vj);
+            k_whm_h2j<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->rh, s->vh, s->xj, s->vj);
             SWG_TRY(L(c, "whm_h2j"));
             SWG_TRY(whm_accel_pl(s));
             s->lfirst_pl = 0;
@@ -489,7 +414,7 @@ int whm_step(swg_system *s, double dt) {
     s->lfirst_tp = s->lfirst_pl;
     if (s->npl > 0) {
         SWG_TRY(whm_kick_vh_pl(s, dth, 1));
-        k_whm_vh2vj<<<1, 32, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->vh, s->vj);
+        k_whm_vh2vj<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->vh, s->vj);
         SWG_TRY(L(c, "whm_vh2vj"));
         SWG_TRY(drift_all(c, s->muj, 0.0, s->xj, s->vj, s->npl, 0, 0.0, dt, s->lmask, s->iflag));
         int32_t *dflag = (int32_t *)s->flags.ptr;
@@ -506,7 +431,7 @@ int whm_step(swg_system *s, double dt) {
             c->err = "Danby drift failed for a massive body (WHM stops the run)";
             return SWG_ERR_DRIFT;
         }
-        k_whm_j2h<<<1, 32, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->xj, s->vj, s->rh, s->vh);
+        k_whm_j2h<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->xj, s->vj, s->rh, s->vh);
         SWG_TRY(L(c, "whm_j2h"));
         SWG_TRY(whm_kick_vh_pl(s, dth, 0));
     }

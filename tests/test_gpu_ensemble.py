@@ -88,6 +88,41 @@ def test_helio_ensemble_fp64_bitexact(ctx):
     assert _check_states(ens, refs)
 
 
+def test_whm_ensemble_fp64_bitexact(ctx):
+    # batched WHM (Jacobi coordinates per system, serial sums in the reference's order)
+    E = IC.make_ensemble("C3", nsys=9, scale=0.08, integrator="WHM")
+    kw = dict(dt=0.01)
+    ens = Ensemble(ctx, E, precision="FP64", **kw)
+    refs = _oracles(E, **kw)
+    ens.step(150)
+    for ref in refs:
+        ref.step(150)
+    assert _check_states(ens, refs)
+    eg = ens.energy()
+    for s, ref in enumerate(refs):
+        er = ref.energy()
+        assert abs(eg["te"][s] - er["te"]) <= 1e-12 * abs(er["te"])
+
+
+def test_whm_ensemble_mixed(ctx):
+    # mixed WHM: graph replay gives the eager bits; energy error within 2x of the FP64 path's
+    E = IC.make_ensemble("C3", nsys=6, scale=0.1, integrator="WHM")
+    out, dE = [], {}
+    for prec, graphs in (("MIXED", True), ("MIXED", False), ("FP64", True)):
+        ens = Ensemble(ctx, E, precision=prec, dt=0.01)
+        ens.use_graphs(graphs)
+        e0 = ens.energy()
+        ens.step(300)
+        e1 = ens.energy()
+        dE[(prec, graphs)] = np.abs((e1["te"] - e0["te"]) / e0["te"])
+        out.append(ens.get_pl() + ens.get_tp())
+        ens.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    assert np.all(dE[("MIXED", True)] < np.maximum(2 * dE[("FP64", True)], 1e-10)), (dE[("MIXED", True)],
+                                                                                    dE[("FP64", True)])
+
+
 def test_symba_ensemble_uneven_sizes(ctx):
     # systems of very different sizes (2 .. 300 bodies, tp-free and tp-carrying) in one ensemble
     parts = [IC.make_system(seed=s, npl=n, ntp=t, amin=0.8, amax=1.2, mmin=1e-9, mmax=1e-6)
