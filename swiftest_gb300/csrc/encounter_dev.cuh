@@ -39,6 +39,25 @@ __device__ __forceinline__ void d_encounter_one(double xr, double yr, double zr,
     lenc = lvdotr && (r2min <= r2crit);
 }
 
+// swiftest_discard_pl_close (src/swiftest/swiftest_discard.f90:293-336): does the relative
+// linear motion (dx, dv) come within sqrt(r2crit) during the step dt?
+__device__ __forceinline__ bool d_discard_close(double dx, double dy, double dz, double dvx, double dvy, double dvz,
+                                                double dt, double r2crit) {
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 <= r2crit) return true;
+    const double vdotr = dx * dvx + dy * dvy + dz * dvz;
+    if (vdotr > 0.0) return false;
+    const double v2 = dvx * dvx + dvy * dvy + dvz * dvz;
+    const double tmin = -vdotr / v2;
+    double r2min;
+    if (tmin < dt)
+        r2min = r2 - vdotr * vdotr / v2;
+    else
+        r2min = r2 + 2.0 * vdotr * dt + v2 * (dt * dt);
+    r2min = r2min < r2 ? r2min : r2;
+    return r2min <= r2crit;
+}
+
 struct BodyF {
     float4 a;  // x_hi, y_hi, z_hi, renc
     float4 b;  // x_lo, y_lo, z_lo, |r|

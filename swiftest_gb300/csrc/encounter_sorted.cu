@@ -225,11 +225,141 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
     }
 }
 
+// pl-tp over radius-sorted tiles: the level-0 pl-tp check (encounter_check_all_pltp,
+// TRIANGULAR, encounter_check.f90:525-570, tp renc = 0) or, DISCARD, the close-approach scan
+// of swiftest_discard_pl_tp (swiftest_discard.f90:244-290: flag[tp] = 1 when an ACTIVE tp
+// comes within a pl's radius, renc = radius).  Item (system, first tp in sorted order q0,
+// tp count nr): the tp receivers against every pl tile of the system that is not apart
+// from them (the bound argument of the file comment holds for both tests: same closest-
+// approach expression).  Pairs are written with global 1-based indices (pl, tp).
+template <bool DISCARD>
+__global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ items, const int32_t *__restrict__ poff,
+                                                    const int32_t *__restrict__ npl, const int32_t *__restrict__ ptbase,
+                                                    const int32_t *__restrict__ pperm, const float4 *__restrict__ PA,
+                                                    const float4 *__restrict__ PB, const float4 *__restrict__ PV,
+                                                    const float4 *__restrict__ pbounds, const double *__restrict__ rp,
+                                                    const double *__restrict__ vp, const double *__restrict__ rencp,
+                                                    const int32_t *__restrict__ toff,
+                                                    const int32_t *__restrict__ ttbase,
+                                                    const int32_t *__restrict__ tperm, const float4 *__restrict__ TA,
+                                                    const float4 *__restrict__ TB, const float4 *__restrict__ TV,
+                                                    const float4 *__restrict__ tbounds, const double *__restrict__ rt,
+                                                    const double *__restrict__ vt,
+                                                    const int32_t *__restrict__ tstatus, double dt, long long cap,
+                                                    int32_t *__restrict__ o1, int32_t *__restrict__ o2,
+                                                    int32_t *__restrict__ olv, unsigned long long *__restrict__ count,
+                                                    int32_t *__restrict__ flag) {
+    __shared__ float4 sa[SB], sb[SB], sv[SB];
+    __shared__ int32_t sg[SB];
+    const int4 w = items[blockIdx.x];
+    const int s = w.x, q0 = w.y, nr = w.z;
+    const int po = poff[s], n1 = npl[s], to = toff[s];
+    const int qt = ttbase[s] + q0 / SB;
+    float4 Q = tbounds[qt];
+    if (nr > SB) {
+        const float4 Q2 = tbounds[qt + 1];
+        Q = make_float4(fminf(Q.x, Q2.x), fmaxf(Q.y, Q2.y), fmaxf(Q.z, Q2.z), 0.f);
+    }
+    bool active = (int)threadIdx.x < nr;
+    BodyF me;
+    int gq = 0;
+    if (active) {
+        me.a = TA[to + q0 + threadIdx.x];
+        me.b = TB[to + q0 + threadIdx.x];
+        me.v = TV[to + q0 + threadIdx.x];
+        gq = tperm[to + q0 + threadIdx.x];
+        if (DISCARD) active = tstatus[gq] == ST_ACTIVE;
+    }
+    const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);
+    for (int p0 = 0; p0 < n1; p0 += SB) {
+        if (tiles_apart(pbounds[ptbase[s] + p0 / SB], Q)) continue;  // block-uniform
+        if (threadIdx.x < SB && p0 + (int)threadIdx.x < n1) {
+            const int pp = po + p0 + threadIdx.x;
+            sa[threadIdx.x] = PA[pp];
+            sb[threadIdx.x] = PB[pp];
+            sv[threadIdx.x] = PV[pp];
+            sg[threadIdx.x] = pperm[pp];
+        }
+        __syncthreads();
+        if (active) {
+            const int nt = min(SB, n1 - p0);
+            for (int ii = 0; ii < nt; ii++) {
+                BodyF other;
+                other.a = sa[ii];
+                other.b = sb[ii];
+                other.v = sv[ii];
+                if (prefilter_reject(other, me, dtf)) continue;
+                const int i = sg[ii];  // pl (global index)
+                const double xr = rt[3 * (size_t)gq + 0] - rp[3 * (size_t)i + 0];
+                const double yr = rt[3 * (size_t)gq + 1] - rp[3 * (size_t)i + 1];
+                const double zr = rt[3 * (size_t)gq + 2] - rp[3 * (size_t)i + 2];
+                const double vxr = vt[3 * (size_t)gq + 0] - vp[3 * (size_t)i + 0];
+                const double vyr = vt[3 * (size_t)gq + 1] - vp[3 * (size_t)i + 1];
+                const double vzr = vt[3 * (size_t)gq + 2] - vp[3 * (size_t)i + 2];
+                if (DISCARD) {
+                    if (d_discard_close(xr, yr, zr, vxr, vyr, vzr, dt, rencp[i] * rencp[i])) flag[gq] = 1;
+                    continue;
+                }
+                int lenc, lv;
+                d_encounter_one(xr, yr, zr, vxr, vyr, vzr, rencp[i] + 0.0, dt, lenc, lv);
+                if (lenc) {
+                    const unsigned long long k = atomicAdd(count, 1ull);
+                    if ((long long)k < cap) {
+                        o1[k] = i + 1;
+                        o2[k] = gq + 1;
+                        olv[k] = lv;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Dynamic shared memory of k_radial_sort for systems of up to nmax bodies.
 static size_t radial_sort_smem(int nmax) {
     int npad = 1;
     while (npad < std::min(nmax, SORT_MAX)) npad <<= 1;
     return (size_t)8 * npad;
+}
+
+int sorted_set_prep(swg_ctx *c, const SortedSet &x, int nsys, bool resort, double dt) {
+    if (x.ntiles <= 0) return SWG_OK;
+    if (resort) {
+        const size_t smem = radial_sort_smem(x.nmax);
+        static size_t smem_set = 0;
+        if (smem > 48 * 1024 && smem > smem_set) {
+            SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        (int)smem),
+                                "radial sort smem"));
+            smem_set = smem;
+        }
+        k_radial_sort<<<nsys, 1024, smem, c->stream>>>(x.off, x.n, x.r, x.perm);
+        c->launches++;
+        SWG_TRY(launch_status(c, "radial_sort"));
+    }
+    const float adt = (float)fabs(dt) * (1.0f + 1e-6f);
+    k_sorted_prep<<<x.ntiles, SB, 0, c->stream>>>(x.tiles, x.off, x.n, x.perm, x.r, x.v, x.renc, adt, x.F, x.F + x.N,
+                                                  x.F + 2 * x.N, x.bounds);
+    c->launches++;
+    return launch_status(c, "sorted_prep");
+}
+
+int pltp_sorted_batched(swg_ctx *c, bool discard, const SortedSet &pl, const SortedSet &tp, const int32_t *tstatus,
+                        int nitems, const int4 *items, double dt, long long cap, int32_t *o1, int32_t *o2,
+                        int32_t *olv, unsigned long long *count, int32_t *flag) {
+    if (nitems <= 0 || pl.ntiles <= 0) return SWG_OK;
+#define SWG_PLTP_ARGS                                                                                                 \
+    items, pl.off, pl.n, pl.tbase, pl.perm, pl.F, pl.F + pl.N, pl.F + 2 * pl.N, pl.bounds, pl.r, pl.v, pl.renc,      \
+        tp.off, tp.tbase, tp.perm, tp.F, tp.F + tp.N, tp.F + 2 * tp.N, tp.bounds, tp.r, tp.v, tstatus, dt, cap, o1, o2, \
+        olv, count, flag
+    if (discard)
+        k_pltp_sorted<true><<<nitems, SQ, 0, c->stream>>>(SWG_PLTP_ARGS);
+    else
+        k_pltp_sorted<false><<<nitems, SQ, 0, c->stream>>>(SWG_PLTP_ARGS);
+#undef SWG_PLTP_ARGS
+    c->launches++;
+    return launch_status(c, discard ? "discard_pltp_sorted" : "encounter_pltp_sorted");
 }
 
 int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t *poff, const int32_t *npl,

@@ -72,9 +72,9 @@ struct swg_ensemble {
     double *trh = nullptr, *tvh = nullptr, *tvb = nullptr, *tah = nullptr;
     int32_t *tstatus = nullptr, *tlmask = nullptr, *tlevelg = nullptr, *tlevelm = nullptr, *tnplenc = nullptr,
             *mark_tp = nullptr;
-    // float copies: split partners of the mixed kick (A|B), prefilter copies (A|B|V) in body
-    // order (pl-tp check) and in radius order (pl-pl check)
-    float4 *kA = nullptr, *kB = nullptr, *eP = nullptr, *eT = nullptr, *eS = nullptr;
+    // float copies: split partners of the mixed kick (A|B), prefilter copies (A|B|V) of the
+    // tp and the pl, both in radius order
+    float4 *kA = nullptr, *kB = nullptr, *eT = nullptr, *eS = nullptr;
     // radius-sorted pl-pl check: order, bound tiles (system, first sorted position), the
     // systems' first tiles, bounds, receiver items
     int32_t *perm = nullptr, *tbase = nullptr;
@@ -82,9 +82,18 @@ struct swg_ensemble {
     float4 *bounds = nullptr;
     int4 *it_esp = nullptr;
     int ntiles = 0, n_esp = 0, nmax = 0;
+    // radius-sorted pl-tp checks (level 0 and the discard scan): the tp order, tp bound tiles,
+    // the systems' first tp tiles, bounds, tp receiver items; eT holds the tp float copies in
+    // sorted order
+    int32_t *tperm = nullptr, *ttbase = nullptr;
+    int2 *ttiles = nullptr;
+    float4 *tbounds = nullptr;
+    int4 *it_tsp = nullptr;
+    int nttiles = 0, n_tsp = 0, ntmax = 0;
+    int64_t ndisc = 0;  // discard scans so far (HELIO/WHM refresh the orders every RESORT_EVERY)
     // item tables of the batched pair kernels
-    int4 *it_fpl = nullptr, *it_ftp = nullptr, *it_ept = nullptr;
-    int n_fpl = 0, n_ftp = 0, n_ept = 0;
+    int4 *it_fpl = nullptr, *it_ftp = nullptr;
+    int n_fpl = 0, n_ftp = 0;
     // mixed kick of kind k (0 pl-pl, 1 pl-tp): tile-shape variant (-1 until chosen by the
     // autotuner at the first such kick) and its items; force_variant >= 0 overrides the tuner
     int kv[2] = {-1, -1}, n_kit[2] = {0, 0};
@@ -622,7 +631,23 @@ int build_items(swg_ensemble *e) {
     SWG_TRY(put_items(e, &e->it_fpl, &e->n_fpl, make_items(S, KICK_FP64_TILE, npl, plcost)));
     SWG_TRY(put_items(e, &e->it_ftp, &e->n_ftp, make_items(S, KICK_FP64_TILE, ntp, plcost)));
     auto tp_with_pl = [&](int s) { return e->h_npl[s] > 0 ? e->h_ntp[s] : 0; };
-    SWG_TRY(put_items(e, &e->it_ept, &e->n_ept, make_items(S, ENC_TILE, tp_with_pl, plcost)));
+    SWG_TRY(put_items(e, &e->it_tsp, &e->n_tsp, make_items(S, ENC_SORTED_TILE, tp_with_pl, plcost)));
+    {  // tp bound tiles of the sorted pl-tp checks
+        std::vector<int2> tt;
+        std::vector<int32_t> tb(S + 1, 0);
+        for (int s = 0; s < S; s++) {
+            tb[s] = (int32_t)tt.size();
+            for (int p0 = 0; p0 < e->h_ntp[s]; p0 += ENC_BOUND_TILE) tt.push_back(make_int2(s, p0));
+            e->ntmax = std::max(e->ntmax, (int)e->h_ntp[s]);
+        }
+        tb[S] = (int32_t)tt.size();
+        e->nttiles = (int)tt.size();
+        SWG_TRY(dalloc(e->c, &e->ttiles, tt.size()));
+        SWG_TRY(upload(e->c, e->ttiles, tt));
+        SWG_TRY(dalloc(e->c, &e->ttbase, tb.size()));
+        SWG_TRY(upload(e->c, e->ttbase, tb));
+        SWG_TRY(dalloc(e->c, &e->tbounds, tt.size()));
+    }
     // radius-sorted pl-pl check: receiver tiles in system order (their cost depends on
     // the geometry), bound tiles of every system
     SWG_TRY(put_items(e, &e->it_esp, &e->n_esp, make_items(S, ENC_SORTED_TILE, npl, [](int, int, int) { return 0.0; })));
@@ -936,6 +961,42 @@ int drift_bodies(swg_ensemble *e, double dt) {
 // symba_encounter_check.f90:14-87, 238-296), TRIANGULAR: both batched checks, one host
 // synchronization for the two counts, then the sorted lists with their level-0 marks
 // and each system's segment.
+// The pl and tp sets of the radius-sorted checks (renc: the pl encounter radii, or the
+// radii for the discard scan); v: the velocities the check uses.
+SortedSet pl_set(swg_ensemble *e, const double *v, const double *renc) {
+    SortedSet x;
+    x.off = e->poff;
+    x.n = e->npl;
+    x.r = e->rh;
+    x.v = v;
+    x.renc = renc;
+    x.perm = e->perm;
+    x.F = e->eS;
+    x.N = e->NPL;
+    x.ntiles = e->ntiles;
+    x.tiles = e->tiles;
+    x.tbase = e->tbase;
+    x.bounds = e->bounds;
+    x.nmax = e->nmax;
+    return x;
+}
+SortedSet tp_set(swg_ensemble *e, const double *v) {
+    SortedSet x;
+    x.off = e->toff;
+    x.n = e->ntp;
+    x.r = e->trh;
+    x.v = v;
+    x.perm = e->tperm;
+    x.F = e->eT;
+    x.N = e->NTP;
+    x.ntiles = e->nttiles;
+    x.tiles = e->ttiles;
+    x.tbase = e->ttbase;
+    x.bounds = e->tbounds;
+    x.nmax = e->ntmax;
+    return x;
+}
+
 int symba_level0(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     e->pp_n = e->pt_n = 0;
@@ -949,10 +1010,6 @@ int symba_level0(swg_ensemble *e, double dt) {
             SWG_TRY(ensure(c, w[k]->raw, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
         }
     }
-    if (e->n_ept > 0) {  // body-order copies for the pl-tp check
-        SWG_TRY(encounter_prep_launch(c, e->NPL, e->rh, e->vb, e->renc, e->eP, e->eP + e->NPL, e->eP + 2 * e->NPL));
-        SWG_TRY(encounter_prep_launch(c, e->NTP, e->trh, e->tvb, nullptr, e->eT, e->eT + e->NTP, e->eT + 2 * e->NTP));
-    }
     unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
     const bool resort = e->nchecks++ % RESORT_EVERY == 0;
     auto launch = [&](int kind) -> int {
@@ -964,16 +1021,16 @@ int symba_level0(swg_ensemble *e, double dt) {
             SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->rh, e->vb, e->renc, dt,
                                                   resort, e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase,
                                                   e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
-        else
-            SWG_TRY(encounter_tri_batched(c, e->n_ept, e->it_ept, e->poff, e->npl, e->eP, e->NPL, e->rh, e->vb, e->renc,
-                                          e->toff, e->ntp, e->eT, e->NTP, e->trh, e->tvb, nullptr, 0, dt, x.rawcap, i1,
-                                          i2, lv, cnt));
+        else  // the pl set was prepared (renc, this step's state) by the pl-pl check just before
+            SWG_TRY(pltp_sorted_batched(c, false, pl_set(e, e->vb, e->renc), tp_set(e, e->tvb), nullptr, e->n_tsp,
+                                        e->it_tsp, dt, x.rawcap, i1, i2, lv, cnt, nullptr));
         return cuda_status(c, cudaMemcpyAsync(&h[kind], cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                               c->stream),
                            "count");
     };
     h[0] = h[1] = 0;
-    const bool do_pt = e->n_ept > 0;
+    const bool do_pt = e->n_tsp > 0;
+    if (do_pt) SWG_TRY(sorted_set_prep(c, tp_set(e, e->tvb), e->nsys, resort, dt));
     SWG_TRY(launch(0));
     if (do_pt) SWG_TRY(launch(1));
     SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
@@ -1349,10 +1406,15 @@ int whm_ens_step(swg_ensemble *e, double dt) {
 // swiftest_discard_pl_tp of every system (src/swiftest/swiftest_discard.f90:244-290), after
 // each step when close encounters are checked, on the pl-tp items of the encounter check.
 int discard_step(swg_ensemble *e) {
-    if (!e->lclose || e->n_ept == 0) return SWG_OK;
+    if (!e->lclose || e->n_tsp == 0) return SWG_OK;
     swg_ctx *c = e->c;
-    SWG_TRY(discard_pl_tp_batched(c, e->n_ept, e->it_ept, e->poff, e->npl, e->NPL, e->rh, e->vh, e->radius, e->toff,
-                                  e->ntp, e->NTP, e->trh, e->tvh, e->tstatus, e->dt, e->eP, e->eT, e->tflag));
+    // SyMBA refreshes the orders in its level-0 checks; HELIO and WHM here
+    const bool resort = e->integrator != SWG_SYMBA && e->ndisc++ % RESORT_EVERY == 0;
+    const SortedSet pl = pl_set(e, e->vh, e->radius), tp = tp_set(e, e->tvh);
+    SWG_TRY(sorted_set_prep(c, pl, e->nsys, resort, e->dt));
+    SWG_TRY(sorted_set_prep(c, tp, e->nsys, resort, e->dt));
+    SWG_TRY(pltp_sorted_batched(c, true, pl, tp, e->tstatus, e->n_tsp, e->it_tsp, e->dt, 0, nullptr, nullptr, nullptr,
+                                nullptr, e->tflag));
     k_apply_discard<<<grid_for(e->NTP, 256), 256, 0, c->stream>>>(e->NTP, e->tflag, e->tstatus, e->tlmask, e->trh,
                                                                    e->tvh, e->tvb, 0, e->tsys, e->toff, e->npl,
                                                                    e->ndiscard);
@@ -1427,7 +1489,7 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
         if (rc == SWG_OK) rc = dalloc(c, p, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->kA, 2 * n);
     if (rc == SWG_OK) e->kB = e->kA + n;
-    if (rc == SWG_OK) rc = dalloc(c, &e->eP, 3 * n);
+    if (rc == SWG_OK) rc = dalloc(c, &e->tperm, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->eT, 3 * m);
     if (rc == SWG_OK) rc = dalloc(c, &e->eS, 3 * n);
     if (rc == SWG_OK) rc = dalloc(c, &e->perm, n);
@@ -1485,9 +1547,9 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->enc_steps, e->psys, e->rh, e->vh, e->vb, e->ah, e->rbeg, e->rend, e->Gmass, e->radius,
                     e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
                     e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
-                    e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eP, e->eT, e->eS, e->perm, e->tbase,
+                    e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eT, e->eS, e->perm, e->tbase, e->tperm, e->ttbase, e->ttiles, e->tbounds, e->it_tsp,
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
-                    e->it_fpl, e->it_ftp, e->it_ept, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
+                    e->it_fpl, e->it_ftp, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
                     e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->eout};
     for (void *p : ptrs)

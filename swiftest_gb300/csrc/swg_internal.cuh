@@ -259,6 +259,33 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
                                   const int32_t *tbase, float4 *bounds, int nitems, const int4 *items, long long cap,
                                   int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count);
 
+// One set of bodies (pl or tp) of CSR-packed systems ordered by |r| per system, for the
+// radius-sorted checks: offsets and counts, positions, velocities, encounter radii (nullptr:
+// zero), the order perm, float copies F (3 * N float4, sorted order), bound tiles
+// (ENC_BOUND_TILE bodies: tiles[k] = (system, first sorted position), tbase[s] = the
+// system's first tile) and their bounds; nmax = the largest system.
+struct SortedSet {
+    const int32_t *off = nullptr, *n = nullptr;
+    const double *r = nullptr, *v = nullptr, *renc = nullptr;
+    int32_t *perm = nullptr;
+    float4 *F = nullptr;
+    int64_t N = 0;
+    int ntiles = 0;
+    const int2 *tiles = nullptr;
+    const int32_t *tbase = nullptr;
+    float4 *bounds = nullptr;
+    int nmax = 0;
+};
+// resort: refresh the order; then the float copies and bounds from the current state
+int sorted_set_prep(swg_ctx *c, const SortedSet &x, int nsys, bool resort, double dt);
+// pl-tp over radius-sorted tiles (both sets prepared at the current state): the level-0
+// pl-tp check (pairs (pl, tp), global 1-based, into o1/o2/olv/count) or, discard, the
+// close-approach scan of swiftest_discard_pl_tp (flag[tp] = 1; tp renc = pl radius).
+// Items: (system, first tp in sorted order, tp count <= ENC_SORTED_TILE).
+int pltp_sorted_batched(swg_ctx *c, bool discard, const SortedSet &pl, const SortedSet &tp, const int32_t *tstatus,
+                        int nitems, const int4 *items, double dt, long long cap, int32_t *o1, int32_t *o2,
+                        int32_t *olv, unsigned long long *count, int32_t *flag);
+
 // Full check of one kind (0 plpl, 1 plplm, 2 pltp): sorted unique pairs in the
 // workspace's raw buffers; *n_out gets the count (host).  Synchronizes.
 int encounter_check_kind(swg_ctx *c, EncWork &w, int kind, int mode, int32_t n1, const double *r1,
