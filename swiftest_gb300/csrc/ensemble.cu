@@ -91,6 +91,10 @@ struct swg_ensemble {
     int4 *it_tsp = nullptr;
     int nttiles = 0, n_tsp = 0, ntmax = 0;
     int64_t ndisc = 0;  // discard scans so far (HELIO/WHM refresh the orders every RESORT_EVERY)
+    // level-0 checks: the state they read (the bodies' arrays, or the copy of them in snap,
+    // which lets the checks run on the side stream while the first kick runs)
+    const double *l0_r = nullptr, *l0_v = nullptr, *l0_tr = nullptr, *l0_tv = nullptr;
+    double *snap = nullptr;  // SyMBA: rh | vb | trh | tvb at the start of the step
     // item tables of the batched pair kernels
     int4 *it_fpl = nullptr, *it_ftp = nullptr;
     int n_fpl = 0, n_ftp = 0;
@@ -957,17 +961,13 @@ int drift_bodies(swg_ensemble *e, double dt) {
     return SWG_OK;
 }
 
-// Level-0 checks of every system (symba_encounter_check_pl / _tp,
-// symba_encounter_check.f90:14-87, 238-296), TRIANGULAR: both batched checks, one host
-// synchronization for the two counts, then the sorted lists with their level-0 marks
-// and each system's segment.
 // The pl and tp sets of the radius-sorted checks (renc: the pl encounter radii, or the
 // radii for the discard scan); v: the velocities the check uses.
-SortedSet pl_set(swg_ensemble *e, const double *v, const double *renc) {
+SortedSet pl_set(swg_ensemble *e, const double *r, const double *v, const double *renc) {
     SortedSet x;
     x.off = e->poff;
     x.n = e->npl;
-    x.r = e->rh;
+    x.r = r;
     x.v = v;
     x.renc = renc;
     x.perm = e->perm;
@@ -980,11 +980,11 @@ SortedSet pl_set(swg_ensemble *e, const double *v, const double *renc) {
     x.nmax = e->nmax;
     return x;
 }
-SortedSet tp_set(swg_ensemble *e, const double *v) {
+SortedSet tp_set(swg_ensemble *e, const double *r, const double *v) {
     SortedSet x;
     x.off = e->toff;
     x.n = e->ntp;
-    x.r = e->trh;
+    x.r = r;
     x.v = v;
     x.perm = e->tperm;
     x.F = e->eT;
@@ -997,9 +997,41 @@ SortedSet tp_set(swg_ensemble *e, const double *v) {
     return x;
 }
 
-int symba_level0(swg_ensemble *e, double dt) {
+// One level-0 check (kind 0 pl-pl, 1 pl-tp) of every system into the raw buffer, counted,
+// the count copied to the host.  resort: refresh the radial orders (pl-pl check).
+int level0_check(swg_ensemble *e, int kind, double dt, bool resort) {
+    swg_ctx *c = e->c;
+    EncWork &x = kind == 0 ? e->enc_pp : e->enc_pt;
+    unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
+    int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
+    unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
+    if (kind == 0)
+        SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->l0_r, e->l0_v, e->renc, dt,
+                                              resort, e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase,
+                                              e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
+    else  // the pl set was prepared (renc, this state) by the pl-pl check just before
+        SWG_TRY(pltp_sorted_batched(c, false, pl_set(e, e->l0_r, e->l0_v, e->renc), tp_set(e, e->l0_tr, e->l0_tv),
+                                    nullptr, e->n_tsp, e->it_tsp, dt, x.rawcap, i1, i2, lv, cnt, nullptr));
+    return cuda_status(c, cudaMemcpyAsync(&h[kind], cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                          c->stream),
+                       "count");
+}
+
+// Level-0 checks of every system (symba_encounter_check_pl / _tp,
+// symba_encounter_check.f90:14-87, 238-296), TRIANGULAR, in two halves: level0_launch
+// queues the checks on c->stream, reading the positions and velocities r, v (pl) and
+// tr, tv (tp) -- the state at the start of the step, or a copy of it -- and the pair
+// counts' copies to the host; level0_finish waits for the counts (one host
+// synchronisation of c->stream), redoes a check whose raw buffer overflowed, and sorts the
+// lists into the pools with the level marks and per-system segments.
+int level0_launch(swg_ensemble *e, double dt, const double *r, const double *v, const double *tr, const double *tv) {
     swg_ctx *c = e->c;
     e->pp_n = e->pt_n = 0;
+    e->l0_r = r;
+    e->l0_v = v;
+    e->l0_tr = tr;
+    e->l0_tv = tv;
     k_set_renc<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->rhill, e->rhscale, 0, e->renc);
     SWG_TRY(L(c, "set_renc"));
     EncWork *w[2] = {&e->enc_pp, &e->enc_pt};
@@ -1012,27 +1044,17 @@ int symba_level0(swg_ensemble *e, double dt) {
     }
     unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
     const bool resort = e->nchecks++ % RESORT_EVERY == 0;
-    auto launch = [&](int kind) -> int {
-        EncWork &x = *w[kind];
-        int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
-        unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
-        SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
-        if (kind == 0)
-            SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->rh, e->vb, e->renc, dt,
-                                                  resort, e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase,
-                                                  e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
-        else  // the pl set was prepared (renc, this step's state) by the pl-pl check just before
-            SWG_TRY(pltp_sorted_batched(c, false, pl_set(e, e->vb, e->renc), tp_set(e, e->tvb), nullptr, e->n_tsp,
-                                        e->it_tsp, dt, x.rawcap, i1, i2, lv, cnt, nullptr));
-        return cuda_status(c, cudaMemcpyAsync(&h[kind], cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                              c->stream),
-                           "count");
-    };
     h[0] = h[1] = 0;
-    const bool do_pt = e->n_tsp > 0;
-    if (do_pt) SWG_TRY(sorted_set_prep(c, tp_set(e, e->tvb), e->nsys, resort, dt));
-    SWG_TRY(launch(0));
-    if (do_pt) SWG_TRY(launch(1));
+    if (e->n_tsp > 0) SWG_TRY(sorted_set_prep(c, tp_set(e, tr, tv), e->nsys, resort, dt));
+    SWG_TRY(level0_check(e, 0, dt, resort));
+    if (e->n_tsp > 0) SWG_TRY(level0_check(e, 1, dt, resort));
+    return SWG_OK;
+}
+
+int level0_finish(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    EncWork *w[2] = {&e->enc_pp, &e->enc_pt};
+    unsigned long long *h = (unsigned long long *)(e->h_flags + 8);
     SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
     for (int k = 0; k < 2; k++) {  // capacity overflow: grow the raw buffers and redo that check
         if ((int64_t)h[k] <= w[k]->rawcap) continue;
@@ -1041,7 +1063,7 @@ int symba_level0(swg_ensemble *e, double dt) {
         SWG_TRY(ensure(c, fresh, (size_t)w[k]->rawcap * 3 * sizeof(int32_t)));
         cudaFree(w[k]->raw.ptr);
         w[k]->raw = fresh;
-        SWG_TRY(launch(k));
+        SWG_TRY(level0_check(e, k, dt, false));  // the sets are still prepared from this state
         SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
     }
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->seg_pp, 0, sizeof(int32_t) * 2 * e->nsys, c->stream), "memset"));
@@ -1269,6 +1291,7 @@ int ens_step(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     const bool symba = e->integrator == SWG_SYMBA;
     const double dth = 0.5 * dt;
+    bool have_acc = false;
     if (symba) {
         const int64_t nmax = std::max(e->NPL, e->NTP);
         k_symba_reset<<<grid_for(nmax, 256), 256, 0, c->stream>>>((int)e->NPL, (int)e->NTP, e->levelg, e->levelm,
@@ -1276,12 +1299,42 @@ int ens_step(swg_ensemble *e, double dt) {
                                                                    e->tlevelm, e->tnplenc, e->tlmask, e->status,
                                                                    e->tstatus);
         SWG_TRY(L(c, "symba_reset"));
-        ProfScope ps(e->prof, c->stream, PROF_ENC0);
-        SWG_TRY(symba_level0(e, dt));
+        if (!e->prof.on && e->NPL > 0) {
+            // The level-0 checks read a copy of the start-of-step state on the side stream
+            // while this stream runs the per-system sums and the first pair accelerations,
+            // which do not depend on the lists; the lists are joined before the pair
+            // subtraction.  Same arithmetic as the sequential order.
+            const size_t n = e->NPL, m = e->NTP;
+            double *sr = e->snap, *sv = sr + 3 * n, *st = sv + 3 * n, *stv = st + 3 * m;
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(sr, e->rh, 24 * n, cudaMemcpyDeviceToDevice, c->stream), "snap"));
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(sv, e->vb, 24 * n, cudaMemcpyDeviceToDevice, c->stream), "snap"));
+            if (m) {
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(st, e->trh, 24 * m, cudaMemcpyDeviceToDevice, c->stream),
+                                    "snap"));
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(stv, e->tvb, 24 * m, cudaMemcpyDeviceToDevice, c->stream),
+                                    "snap"));
+            }
+            SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
+            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
+            SWG_TRY(on_stream(c, e->side, [&] { return level0_launch(e, dt, sr, sv, st, stv); }));
+            SWG_TRY(vh2vb_pl(e, true));
+            SWG_TRY(lindrift_pl(e, dth, CB_PTBEG));
+            SWG_TRY(accel_int_pl(e, e->head));
+            SWG_TRY(on_stream(c, e->side, [&] { return level0_finish(e, dt); }));
+            SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
+            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+            have_acc = true;
+        } else {
+            ProfScope ps(e->prof, c->stream, PROF_ENC0);
+            SWG_TRY(level0_launch(e, dt, e->rh, e->vb, e->trh, e->tvb));
+            SWG_TRY(level0_finish(e, dt));
+        }
     }
-    SWG_TRY(vh2vb_pl(e, true));
-    SWG_TRY(lindrift_pl(e, dth, CB_PTBEG));
-    SWG_TRY(kick_vb_pl(e, dth, 1));
+    if (!have_acc) {
+        SWG_TRY(vh2vb_pl(e, true));
+        SWG_TRY(lindrift_pl(e, dth, CB_PTBEG));
+    }
+    SWG_TRY(kick_vb_pl(e, dth, 1, have_acc));
     SWG_TRY(tp_misc(e, CB_PTBEG, dth, 2, 4));
     SWG_TRY(kick_vb_tp(e, dth, 1));
     SWG_TRY(drift_bodies(e, dt));
@@ -1410,7 +1463,7 @@ int discard_step(swg_ensemble *e) {
     swg_ctx *c = e->c;
     // SyMBA refreshes the orders in its level-0 checks; HELIO and WHM here
     const bool resort = e->integrator != SWG_SYMBA && e->ndisc++ % RESORT_EVERY == 0;
-    const SortedSet pl = pl_set(e, e->vh, e->radius), tp = tp_set(e, e->tvh);
+    const SortedSet pl = pl_set(e, e->rh, e->vh, e->radius), tp = tp_set(e, e->trh, e->tvh);
     SWG_TRY(sorted_set_prep(c, pl, e->nsys, resort, e->dt));
     SWG_TRY(sorted_set_prep(c, tp, e->nsys, resort, e->dt));
     SWG_TRY(pltp_sorted_batched(c, true, pl, tp, e->tstatus, e->n_tsp, e->it_tsp, e->dt, 0, nullptr, nullptr, nullptr,
@@ -1504,6 +1557,7 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->tflag, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->ndiscard, 1);
     e->h_pend.assign(S, 0);
+    if (integrator == SWG_SYMBA && rc == SWG_OK) rc = dalloc(c, &e->snap, 6 * n + 6 * m);
     if (integrator == SWG_WHM) {
         double **wd[] = {&e->eta, &e->muj, &e->ir3h, &e->ir3j};
         for (auto p : wd)
@@ -1551,7 +1605,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->eout};
+                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
