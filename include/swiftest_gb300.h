@@ -155,6 +155,18 @@ int swg_system_pltp_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, 
 int swg_system_set_state(swg_system *sys, const double *rh, const double *vh, const double *trh, const double *tvh);
 int swg_system_get_state_async(swg_system *sys, double *rh, double *vh, double *trh, double *tvh);
 
+/* ---- orbital elements <-> Cartesian state (swiftest_orbel_el2xv_vec / _xv2el_vec,
+ * swiftest_orbel.f90:14-42, 876-910, with swiftest_orbel_el2xv :45-144 and swiftest_orbel_xv2el
+ * :913-1072).  Body i uses mu[i] (GMcb + Gm for massive bodies, GMcb for test particles, as
+ * set_mu does); angles in radians; rh, vh are (3, n).  xv2el also returns the longitude of
+ * pericentre, mean longitude, true, eccentric and hyperbolic anomalies; any output pointer may
+ * be NULL.  FP64; the transcendental functions are CUDA's (last-bit differences from libm). */
+int swg_orbel_el2xv(swg_ctx *ctx, int32_t n, const double *mu, const double *a, const double *e, const double *inc,
+                    const double *capom, const double *omega, const double *capm, double *rh, double *vh, int mem);
+int swg_orbel_xv2el(swg_ctx *ctx, int32_t n, const double *mu, const double *rh, const double *vh, double *a,
+                    double *e, double *inc, double *capom, double *omega, double *capm, double *varpi, double *lam,
+                    double *f, double *cape, double *capf, int mem);
+
 /* ---- batched ensembles of independent systems -------------------------------------
  * No single counterpart in the reference, which integrates one system per run: an
  * ensemble is many runs of whm_step_system / helio_step_system / symba_step_system

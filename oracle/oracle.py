@@ -47,6 +47,8 @@ _SIG = {
     "orc_kick_getacch_int_all_flat_pl": (None, [_I32, _I64, _P, _P, _P, _P, _P]),
     "orc_kick_getacch_int_all_tp": (None, [_I32, _I32, _P, _P, _P, _P, _P]),
     "orc_util_flatten_eucl_plpl": (_I64, [_I32, _I32, _P]),
+    "orc_el2xv": (None, [_I32, _P, _P, _P, _P]),
+    "orc_xv2el": (None, [_I32, _P, _P, _P, _P]),
     "orc_drift_all": (None, [_P, _P, _P, _I32, _I32, _D, _D, _P, _P]),
     "orc_drift_all_count": (_I64, [_P, _P, _P, _I32, _D, _P, _P]),
     "orc_encounter_check_one": (None, [_D, _D, _D, _D, _D, _D, _D, _D, _P, _P]),
@@ -135,6 +137,33 @@ def kick_tp(rtp, rpl, GMpl, lmask=None, acc=None):
     acc = np.zeros((ntp, 3)) if acc is None else _f(acc, (ntp, 3)).copy()
     lib.orc_kick_getacch_int_all_tp(ntp, rpl.shape[0], _p(rtp), _p(rpl), _p(_f(GMpl)), _p(m), _p(acc))
     return acc
+
+
+ELEMENTS = ("a", "e", "inc", "capom", "omega", "capm", "varpi", "lam", "f", "cape", "capf")
+
+
+def el2xv(mu, a, e, inc, capom, omega, capm):
+    """swiftest_orbel_el2xv of every body: (rh, vh), each (n, 3)."""
+    lib = load()
+    a = np.ascontiguousarray(a, np.float64)
+    n = len(a)
+    mu = np.full(n, float(mu)) if np.isscalar(mu) else np.ascontiguousarray(mu, np.float64)
+    el = np.ascontiguousarray(np.stack([a, e, inc, capom, omega, capm]), np.float64)
+    rh, vh = np.zeros((n, 3)), np.zeros((n, 3))
+    lib.orc_el2xv(n, _p(mu), _p(el), _p(rh), _p(vh))
+    return rh, vh
+
+
+def xv2el(mu, rh, vh):
+    """swiftest_orbel_xv2el of every body: dict of the eleven element arrays."""
+    lib = load()
+    rh = np.ascontiguousarray(rh, np.float64).reshape(-1, 3)
+    vh = np.ascontiguousarray(vh, np.float64).reshape(-1, 3)
+    n = len(rh)
+    mu = np.full(n, float(mu)) if np.isscalar(mu) else np.ascontiguousarray(mu, np.float64)
+    out = np.zeros((11, n))
+    lib.orc_xv2el(n, _p(mu), _p(rh), _p(vh), _p(out))
+    return {k: out[i].copy() for i, k in enumerate(ELEMENTS)}
 
 
 def drift_all(mu, x, v, dt, lmask=None, lgr=False, inv_c2=0.0):

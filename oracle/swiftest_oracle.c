@@ -565,6 +565,352 @@ int64_t orc_drift_all_count(const double *mu, double *x, double *v, int32_t n, d
 }
 
 /* =====================================================================
+ * Orbital elements: src/swiftest/swiftest_orbel.f90
+ * ===================================================================== */
+
+#define ORB_TINY 4.0e-15 /* swiftest_orbel.f90:11 */
+#define ORB_PI 3.141592653589793238462643383279502884197
+enum { ORB_ELLIPSE = -1, ORB_PARABOLA = 0, ORB_HYPERBOLA = 1 };
+
+/* swiftest_orbel_schget, :199-207 */
+static void orbel_schget(double angle, double *shx, double *chx) {
+    *shx = sinh(angle);
+    *chx = sqrt(1.0 + (*shx) * (*shx));
+}
+
+/* swiftest_orbel_flon, :199-265 (line numbers of the function body in the module) */
+static double orbel_flon(double e, double icapn) {
+    const double a11 = 156.0, a9 = 17160.0, a7 = 1235520.0, a5 = 51891840.0, a3 = 1037836800.0;
+    const double b11 = 11 * a11, b9 = 9 * a9, b7 = 7 * a7, b5 = 5 * a5, b3 = 3 * a3;
+    int iflag = 0;
+    double capn = icapn;
+    if (icapn < 0.0) {
+        iflag = 1;
+        capn = -icapn;
+    }
+    double a1 = 6227020800.0 * (1.0 - 1.0 / e);
+    double a0 = -(6227020800.0 * capn / e);
+    double b1 = a1;
+    double a = 6 * (e - 1.0) / e;
+    double b = -(6 * capn / e);
+    double sq = sqrt(0.25 * (b * b) + (a * a * a) / 27.0);
+    double biga = pow(-(0.5 * b) + sq, 1.0 / 3.0);
+    double bigb = -pow(0.5 * b + sq, 1.0 / 3.0);
+    double x = biga + bigb;
+    double flon = x;
+    if (capn >= ORB_TINY) {
+        for (int i = 1; i <= 10; i++) {
+            double x2 = x * x;
+            double f = a0 + x * (a1 + x2 * (a3 + x2 * (a5 + x2 * (a7 + x2 * (a9 + x2 * (a11 + x2))))));
+            double fp = b1 + x2 * (b3 + x2 * (b5 + x2 * (b7 + x2 * (b9 + x2 * (b11 + 13 * x2)))));
+            double dx = -f / fp;
+            flon = x + dx;
+            if (fabs(dx) <= ORB_TINY) break;
+            x = flon;
+        }
+    }
+    if (iflag == 1) flon = -flon;
+    return flon;
+}
+
+/* swiftest_orbel_fget */
+static double orbel_fget(double e, double capn) {
+    double x;
+    if (capn < 0.0)
+        x = -log(-(2 * capn / e) + 1.8);
+    else
+        x = log(2 * capn / e + 1.8);
+    double fget = x;
+    for (int i = 1; i <= 10; i++) {
+        double shx, chx;
+        orbel_schget(x, &shx, &chx);
+        double esh = e * shx, ech = e * chx;
+        double f = esh - x - capn;
+        double fp = ech - 1.0;
+        double fpp = esh, fppp = ech;
+        double dx = -f / fp;
+        dx = -f / (fp + dx * fpp / 2.0);
+        dx = -f / (fp + dx * fpp / 2.0 + (dx * dx) * fppp / 6.0);
+        fget = x + dx;
+        if (fabs(dx) <= ORB_TINY) return fget;
+        x = fget;
+    }
+    return fget;
+}
+
+/* swiftest_orbel_zget */
+static double orbel_zget(double iq) {
+    double q = iq < 0.0 ? -iq : iq, z;
+    if (q < 1.0e-3) {
+        z = q * (1.0 - ((q * q) / 3.0) * (1.0 - q * q));
+    } else {
+        double x = 0.5 * (3 * q + sqrt(9 * (q * q) + 4.0));
+        double tmp = pow(x, 1.0 / 3.0);
+        z = tmp - 1.0 / tmp;
+    }
+    return iq < 0.0 ? -z : z;
+}
+
+/* swiftest_orbel_esolmd */
+static double orbel_esolmd(double e, double m) {
+    double sm, cm, sx, cx;
+    orbel_scget(m, &sm, &cm);
+    double x = m + e * sm * (1.0 + e * (cm + e * (1.0 - 1.5 * (sm * sm))));
+    orbel_scget(x, &sx, &cx);
+    double es = e * sx, ec = e * cx;
+    double f = x - es - m, fp = 1.0 - ec, fpp = es, fppp = ec;
+    double dx = -f / fp;
+    dx = -f / (fp + dx * fpp / 2.0);
+    dx = -f / (fp + dx * fpp / 2.0 + (dx * dx) * fppp / 6.0);
+    return x + dx;
+}
+
+/* swiftest_orbel_ehie */
+static double orbel_ehie(double e, double im) {
+    int iflag = 0;
+    int32_t nper = (int32_t)(im / TWOPI);
+    double m = im - nper * TWOPI;
+    if (m < 0.0) m = m + TWOPI;
+    if (m > ORB_PI) {
+        m = TWOPI - m;
+        iflag = 1;
+    }
+    double x = pow(6 * m, 1.0 / 3.0) - m;
+    for (int niter = 1; niter <= 3; niter++) {
+        double sa, ca;
+        orbel_scget(x + m, &sa, &ca);
+        double esa = e * sa, eca = e * ca;
+        double f = x - esa, fp = 1.0 - eca;
+        double dx = -f / fp;
+        dx = -f / (fp + 0.5 * dx * esa);
+        dx = -f / (fp + 0.5 * dx * (esa + eca * dx / 3.0));
+        x = x + dx;
+    }
+    double r = m + x;
+    if (iflag == 1) r = TWOPI - r;
+    return r;
+}
+
+/* swiftest_orbel_eget: two corrections; the first uses dx*2 where the second uses dx**2 */
+static double orbel_eget(double e, double m) {
+    double sm, cm, sx, cx;
+    orbel_scget(m, &sm, &cm);
+    double x = m + e * sm * (1.0 + e * (cm + e * (1.0 - 1.5 * sm * sm)));
+    orbel_scget(x, &sx, &cx);
+    double es = e * sx, ec = e * cx;
+    double f = x - es - m, fp = 1.0 - ec, fpp = es, fppp = ec;
+    double dx = -f / fp;
+    dx = -f / (fp + dx * fpp / 2.0);
+    dx = -f / (fp + dx * fpp / 2.0 + dx * 2 * fppp / 6.0);
+    x = x + dx;
+    orbel_scget(x, &sx, &cx);
+    es = e * sx;
+    ec = e * cx;
+    f = x - es - m;
+    fp = 1.0 - ec;
+    fpp = es;
+    fppp = ec;
+    dx = -f / fp;
+    dx = -f / (fp + dx * fpp / 2.0);
+    dx = -f / (fp + dx * fpp / 2.0 + (dx * dx) * fppp / 6.0);
+    return x + dx;
+}
+
+static double orbel_ehybrid(double e, double m) {
+    if (e < 0.18) return orbel_esolmd(e, m);
+    if (e <= 0.8) return orbel_eget(e, m);
+    return orbel_ehie(e, m);
+}
+
+static double orbel_fhybrid(double e, double n) {
+    double abn = n < 0.0 ? -n : n;
+    if (abn < 0.636 * e - 0.6) return orbel_flon(e, n);
+    return orbel_fget(e, n);
+}
+
+/* swiftest_orbel_el2xv, :45-144 */
+static void orbel_el2xv(double mu, double a, double ie, double inc, double capom, double omega, double capm,
+                        double *r, double *v) {
+    int type;
+    double e = ie;
+    if (ie < 0.0) {
+        e = 0.0;
+        type = ORB_ELLIPSE;
+    } else if (fabs(e - 1.0) < ORB_TINY) {
+        type = ORB_PARABOLA;
+    } else if (e > 1.0) {
+        type = ORB_HYPERBOLA;
+    } else {
+        type = ORB_ELLIPSE;
+    }
+    double sip, cip, so, co, si, ci;
+    orbel_scget(omega, &sip, &cip);
+    orbel_scget(capom, &so, &co);
+    orbel_scget(inc, &si, &ci);
+    double d11 = cip * co - sip * so * ci, d12 = cip * so + sip * co * ci, d13 = sip * si;
+    double d21 = -(sip * co) - cip * so * ci, d22 = -(sip * so) + cip * co * ci, d23 = cip * si;
+    double xfac1 = 0.0, xfac2 = 0.0, vfac1 = 0.0, vfac2 = 0.0;
+    if (type == ORB_ELLIPSE) {
+        double cape = orbel_ehybrid(e, capm), scap, ccap;
+        orbel_scget(cape, &scap, &ccap);
+        double sqe = sqrt(1.0 - e * e), sqgma = sqrt(mu * a);
+        xfac1 = a * (ccap - e);
+        xfac2 = a * sqe * scap;
+        double ri = 1.0 / (a * (1.0 - e * ccap));
+        vfac1 = -ri * sqgma * scap;
+        vfac2 = ri * sqgma * sqe * ccap;
+    }
+    if (type == ORB_HYPERBOLA) {
+        double capf = orbel_fhybrid(e, capm), shcap, chcap;
+        orbel_schget(capf, &shcap, &chcap);
+        double sqe = sqrt(e * e - 1.0), sqgma = sqrt(mu * a);
+        xfac1 = a * (e - chcap);
+        xfac2 = a * sqe * shcap;
+        double ri = 1.0 / (a * (e * chcap - 1.0));
+        vfac1 = -ri * sqgma * shcap;
+        vfac2 = ri * sqgma * sqe * chcap;
+    }
+    if (type == ORB_PARABOLA) {
+        double zpara = orbel_zget(capm), sqgma = sqrt(2 * mu * a);
+        xfac1 = a * (1.0 - zpara * zpara);
+        xfac2 = 2 * a * zpara;
+        double ri = 1.0 / (a * (1.0 + zpara * zpara));
+        vfac1 = -ri * sqgma * zpara;
+        vfac2 = ri * sqgma;
+    }
+    r[0] = d11 * xfac1 + d21 * xfac2;
+    r[1] = d12 * xfac1 + d22 * xfac2;
+    r[2] = d13 * xfac1 + d23 * xfac2;
+    v[0] = d11 * vfac1 + d21 * vfac2;
+    v[1] = d12 * vfac1 + d22 * vfac2;
+    v[2] = d13 * vfac1 + d23 * vfac2;
+}
+
+/* swiftest_orbel_xv2el, :913-1072; out[11] = a, e, inc, capom, omega, capm, varpi, lam, f, cape, capf */
+static void orbel_xv2el(double mu, const double *rv, const double *vv, double *out) {
+    double rx = rv[0], ry = rv[1], rz = rv[2], vx = vv[0], vy = vv[1], vz = vv[2];
+    double a = 0, e = 0, inc = 0, capom = 0, omega = 0, capm = 0, varpi = 0, lam = 0, f = 0, cape = 0, capf = 0;
+    double hx = ry * vz - rz * vy, hy = rz * vx - rx * vz, hz = rx * vy - ry * vx;
+    double h2 = hx * hx + hy * hy + hz * hz;
+    double h = sqrt(h2);
+    if (hz > h) {
+        hz = h;
+        hx = 0.0;
+        hy = 0.0;
+    }
+    if (!(h2 <= 10 * 2.2250738585072014e-308)) {
+        h = sqrt(h2);
+        double r = sqrt(rx * rx + ry * ry + rz * rz);
+        double v2 = vx * vx + vy * vy + vz * vz;
+        double rdotv = rx * vx + ry * vy + rz * vz;
+        double energy = 0.5 * v2 - mu / r;
+        double fac = hz / h, u, w = 0.0;
+        int type;
+        if (fac < -1.0)
+            inc = ORB_PI;
+        else if (fac < 1.0)
+            inc = acos(fac);
+        fac = sqrt(hx * hx + hy * hy) / h;
+        if (fac * fac < ORB_TINY) {
+            u = atan2(ry, rx);
+            if (hz < 0.0) u = -u;
+        } else {
+            capom = atan2(hx, -hy);
+            u = atan2(rz / sin(inc), rx * cos(capom) + ry * sin(capom));
+        }
+        if (capom < 0.0) capom = capom + TWOPI;
+        if (u < 0.0) u = u + TWOPI;
+        if (fabs(energy * r / mu) < sqrt(ORB_TINY)) {
+            type = ORB_PARABOLA;
+        } else {
+            a = -0.5 * mu / energy;
+            if (a < 0.0) {
+                fac = -h2 / (mu * a);
+                type = fac > ORB_TINY ? ORB_HYPERBOLA : ORB_PARABOLA;
+            } else {
+                type = ORB_ELLIPSE;
+            }
+        }
+        if (type == ORB_ELLIPSE) {
+            fac = 1.0 - h2 / (mu * a);
+            if (fac > ORB_TINY) {
+                e = sqrt(fac);
+                cape = 0.0;
+                double face = (a - r) / (a * e);
+                if (face < -1.0)
+                    cape = ORB_PI;
+                else if (face < 1.0)
+                    cape = acos(face);
+                if (rdotv < 0.0) cape = TWOPI - cape;
+                fac = 1.0 - e * cos(cape);
+                double cw = (cos(cape) - e) / fac;
+                double sw = sqrt(1.0 - e * e) * sin(cape) / fac;
+                w = atan2(sw, cw);
+                if (w < 0.0) w = w + TWOPI;
+            } else {
+                cape = u;
+                w = u;
+            }
+            capm = cape - e * sin(cape);
+        } else if (type == ORB_PARABOLA) {
+            a = 0.5 * h2 / mu;
+            e = 1.0;
+            w = 0.0;
+            fac = 2 * a / r - 1.0;
+            if (fac < -1.0)
+                w = ORB_PI;
+            else if (fac < 1.0)
+                w = acos(fac);
+            if (rdotv < 0.0) w = TWOPI - w;
+            double tmpf = tan(0.5 * w);
+            capm = tmpf * (1.0 + tmpf * tmpf / 3.0);
+        } else {
+            e = sqrt(1.0 + fac);
+            double tmpf = fmax((a - r) / (a * e), 1.0);
+            capf = log(tmpf + sqrt(tmpf * tmpf - 1.0));
+            if (rdotv < 0.0) capf = -capf;
+            fac = e * cosh(capf) - 1.0;
+            double cw = (e - cosh(capf)) / fac;
+            double sw = sqrt(e * e - 1.0) * sinh(capf) / fac;
+            w = atan2(sw, cw);
+            if (w < 0.0) w = w + TWOPI;
+            capm = e * sinh(capf) - capf;
+        }
+        omega = u - w;
+        if (omega < 0.0) omega = omega + TWOPI;
+        varpi = fmod(omega + capom, TWOPI);
+        lam = fmod(capm + varpi, TWOPI);
+        if (e > ORB_TINY) {
+            double cf = 1.0 / e * (a * (1.0 - e * e) / r - 1.0);
+            double hr = h / r;
+            double rdot = copysign(sqrt(fmax(v2 - hr * hr, 0.0)), rdotv);
+            double sf = a * (1.0 - e * e) / (h * e) * rdot;
+            f = atan2(sf, cf);
+            if (f < 0.0) f = f + TWOPI;
+        } else {
+            f = u;
+        }
+    }
+    double o[11] = {a, e, inc, capom, omega, capm, varpi, lam, f, cape, capf};
+    memcpy(out, o, sizeof(o));
+}
+
+/* swiftest_orbel_el2xv_vec / swiftest_orbel_xv2el_vec, :14-42, 876-910: body i with mu[i];
+ * el2xv reads el[k * n + i] (a, e, inc, capom, omega, capm), xv2el writes out[k * n + i] */
+void orc_el2xv(int32_t n, const double *mu, const double *el, double *rh, double *vh) {
+    for (int32_t i = 0; i < n; i++)
+        orbel_el2xv(mu[i], el[i], el[n + i], el[2 * n + i], el[3 * n + i], el[4 * n + i], el[5 * n + i], &rh[3 * i],
+                    &vh[3 * i]);
+}
+void orc_xv2el(int32_t n, const double *mu, const double *rh, const double *vh, double *out) {
+    for (int32_t i = 0; i < n; i++) {
+        double o[11];
+        orbel_xv2el(mu[i], &rh[3 * i], &vh[3 * i], o);
+        for (int k = 0; k < 11; k++) out[(size_t)k * n + i] = o[k];
+    }
+}
+
+/* =====================================================================
  * Encounter checks: src/encounter/encounter_check.f90
  * ===================================================================== */
 

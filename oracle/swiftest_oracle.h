@@ -38,6 +38,10 @@ void orc_kick_getacch_int_all_tp(int32_t ntp, int32_t npl, const double *rtp, co
 int64_t orc_util_flatten_eucl_plpl(int32_t npl, int32_t nplm, int32_t *k_plpl /* NULL => count only */);
 
 /* ---- drift: src/swiftest/swiftest_drift.f90 --------------------------- */
+/* swiftest_orbel_el2xv_vec / _xv2el_vec: el[k*n+i] = (a, e, inc, capom, omega, capm)_k of body i;
+ * out[k*n+i] = (a, e, inc, capom, omega, capm, varpi, lam, f, cape, capf)_k */
+void orc_el2xv(int32_t n, const double *mu, const double *el, double *rh, double *vh);
+void orc_xv2el(int32_t n, const double *mu, const double *rh, const double *vh, double *out);
 void orc_drift_all(const double *mu, double *x, double *v, int32_t n, int32_t lgr, double inv_c2, double dt,
                    const int32_t *lmask, int32_t *iflag);
 void orc_drift_one(double mu, double *rx, double *ry, double *rz, double *vx, double *vy, double *vz, double dt,

@@ -48,6 +48,8 @@ SIGNATURES = {
     "swg_kick_getacch_int_all_flat_pl": (_INT, [_P, _I32, _I32, _I64, _P, _P, _P, _P, _P, _INT, _INT]),
     "swg_kick_getacch_int_all_tp": (_INT, [_P, _I32, _I32, _P, _P, _P, _P, _P, _INT, _INT]),
     "swg_kick_getacch_int_all_tri_pl_noalloc": (_INT, [_I32, _I32, _P, _P, _P, _P, _P]),
+    "swg_orbel_el2xv": (_INT, [_P, _I32] + [_P] * 9 + [_INT]),
+    "swg_orbel_xv2el": (_INT, [_P, _I32] + [_P] * 14 + [_INT]),
     "swg_drift_all": (_INT, [_P, _P, _P, _P, _I32, _I32, _D, _D, _P, _P, _INT]),
     "swg_encounter_check_all_plpl": (_INT, [_P, _INT, _I32, _P, _P, _P, _D, _I64, C.POINTER(_I64), _P, _P, _P, _INT]),
     "swg_encounter_check_all_plplm": (_INT, [_P, _INT, _I32, _I32, _P, _P, _P, _P, _P, _P, _D, _I64,

@@ -143,6 +143,33 @@ class Context:
         self.check("swg_drift_all", rc)
         return x, v, iflag
 
+    # ---- orbital elements ----------------------------------------------------
+    ELEMENTS = ("a", "e", "inc", "capom", "omega", "capm", "varpi", "lam", "f", "cape", "capf")
+
+    def el2xv(self, mu, a, e, inc, capom, omega, capm):
+        """Heliocentric positions and velocities (n, 3) from orbital elements (radians)."""
+        a = _f64(a)
+        n = a.shape[0]
+        mu = np.full(n, float(mu)) if np.isscalar(mu) else _f64(mu)
+        els = [_f64(x) for x in (e, inc, capom, omega, capm)]
+        rh, vh = np.zeros((n, 3)), np.zeros((n, 3))
+        rc = self.lib.swg_orbel_el2xv(self.h, n, _ptr(mu), _ptr(a), *[_ptr(x) for x in els], _ptr(rh), _ptr(vh),
+                                      L.SWG_MEM_HOST)
+        self.check("swg_orbel_el2xv", rc)
+        return rh, vh
+
+    def xv2el(self, mu, rh, vh):
+        """Orbital elements of (n, 3) positions and velocities: dict of the eleven arrays."""
+        rh = _f64(rh, (-1, 3))
+        vh = _f64(vh, (-1, 3))
+        n = rh.shape[0]
+        mu = np.full(n, float(mu)) if np.isscalar(mu) else _f64(mu)
+        out = {k: np.zeros(n) for k in self.ELEMENTS}
+        rc = self.lib.swg_orbel_xv2el(self.h, n, _ptr(mu), _ptr(rh), _ptr(vh), *[_ptr(out[k]) for k in self.ELEMENTS],
+                                      L.SWG_MEM_HOST)
+        self.check("swg_orbel_xv2el", rc)
+        return out
+
     # ---- encounters -------------------------------------------------------
     def _enc(self, fn, args, cap):
         n = C.c_int64(0)

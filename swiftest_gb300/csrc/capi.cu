@@ -218,6 +218,50 @@ int swg_kick_getacch_int_all_tp(swg_ctx *c, int32_t ntp, int32_t npl, const doub
     return finish(c, mem);
 }
 
+int swg_orbel_el2xv(swg_ctx *c, int32_t n, const double *mu, const double *a, const double *e, const double *inc,
+                    const double *capom, const double *omega, const double *capm, double *rh, double *vh, int mem) {
+    if (!c || n < 0 || bad_mem(mem)) return SWG_ERR_ARG;
+    if (n == 0) return SWG_OK;
+    if (!mu || !a || !e || !inc || !capom || !omega || !capm || !rh || !vh) return SWG_ERR_ARG;
+    const double *in[7] = {mu, a, e, inc, capom, omega, capm};
+    double *d[7], *dr = rh, *dv = vh;
+    for (int k = 0; k < 7; k++) SWG_TRY(stage_in(c, mem, k, in[k], (size_t)n, &d[k]));
+    if (mem == SWG_MEM_HOST) {  // outputs only: device room, no copy in
+        void *q;
+        SWG_TRY(ensure_slot(c, 7, 24 * (size_t)n, &q));
+        dr = (double *)q;
+        SWG_TRY(ensure_slot(c, 8, 24 * (size_t)n, &q));
+        dv = (double *)q;
+    }
+    SWG_TRY(orbel_el2xv_launch(c, n, d[0], d[1], d[2], d[3], d[4], d[5], d[6], dr, dv));
+    SWG_TRY(stage_out(c, mem, rh, dr, 3 * (size_t)n));
+    SWG_TRY(stage_out(c, mem, vh, dv, 3 * (size_t)n));
+    return finish(c, mem);
+}
+
+int swg_orbel_xv2el(swg_ctx *c, int32_t n, const double *mu, const double *rh, const double *vh, double *a,
+                    double *e, double *inc, double *capom, double *omega, double *capm, double *varpi, double *lam,
+                    double *f, double *cape, double *capf, int mem) {
+    if (!c || n < 0 || bad_mem(mem)) return SWG_ERR_ARG;
+    if (n == 0) return SWG_OK;
+    if (!mu || !rh || !vh) return SWG_ERR_ARG;
+    double *dmu, *dr, *dv;
+    SWG_TRY(stage_in(c, mem, 0, mu, (size_t)n, &dmu));
+    SWG_TRY(stage_in(c, mem, 1, rh, 3 * (size_t)n, &dr));
+    SWG_TRY(stage_in(c, mem, 2, vh, 3 * (size_t)n, &dv));
+    double *out[11] = {a, e, inc, capom, omega, capm, varpi, lam, f, cape, capf};
+    double *dout[11];
+    void *q;  // one scratch slot: the 11 output pointers (device array), then host-mode outputs
+    SWG_TRY(ensure_slot(c, 22, sizeof(dout) + (mem == SWG_MEM_HOST ? 11 * 8 * (size_t)n : 0), &q));
+    double *room = (double *)((char *)q + sizeof(dout));
+    for (int k = 0; k < 11; k++) dout[k] = out[k] && mem == SWG_MEM_HOST ? room + (size_t)k * n : out[k];
+    void *tab = q;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(tab, dout, sizeof(dout), cudaMemcpyHostToDevice, c->stream), "H2D"));
+    SWG_TRY(orbel_xv2el_launch(c, n, dmu, dr, dv, (double *const *)tab));
+    for (int k = 0; k < 11; k++) SWG_TRY(stage_out(c, mem, out[k], dout[k], (size_t)n));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "sync");  // the pointer table is a stack array
+}
+
 int swg_drift_all(swg_ctx *c, const double *mu, double *x, double *v, int32_t n, int32_t lgr, double inv_c2,
                   double dt, const int32_t *lmask, int32_t *iflag, int mem) {
     if (!c || n < 0 || bad_mem(mem)) return SWG_ERR_ARG;

@@ -105,7 +105,8 @@ struct swg_ctx {
     int64_t launches = 0;
     int num_sms = 0;
     // scratch arena slots used by the flat C entry points (host-memory staging
-    // and kernel scratch); each slot is grow-only.
+    // and kernel scratch); each slot is grow-only.  Slot 10 holds the mixed kick's zeroed
+    // block counters (ensure_kick_scratch) and must hold nothing else.
     swg::DevBuf slot[24];
     swg::EncWork enc;
     void *events[16] = {nullptr};  // measurement events (cudaEvent_t), created on first use
@@ -171,6 +172,15 @@ int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, 
 int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
                          const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
                          const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
+// orbel.cu -- orbital elements <-> Cartesian (swiftest_orbel_el2xv / _xv2el), device arrays;
+// out_dev: a device array of 11 device pointers (a, e, inc, capom, omega, capm, varpi, lam, f,
+// cape, capf), null entries skipped
+int orbel_el2xv_launch(swg_ctx *c, int32_t n, const double *mu, const double *a, const double *e,
+                       const double *inc, const double *capom, const double *omega, const double *capm, double *rh,
+                       double *vh);
+int orbel_xv2el_launch(swg_ctx *c, int32_t n, const double *mu, const double *rh, const double *vh,
+                       double *const *out_dev);
+
 // kick_sym.cu -- symmetric mixed pl-pl kick (each pair once, applied to both bodies) over
 // tile pairs of KICK_SYM_TILE bodies.  kick_sym_items builds the items (row strips of tile
 // pairs, sorted by cost) and per system its first receiver slot and first pair slot

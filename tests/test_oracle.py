@@ -1,6 +1,8 @@
 """Known-answer tests that pin the CPU oracle (the reference ships no kernel-level golden vectors).
 
 * drift: analytic two-body Kepler propagation, reversibility, conservation
+* orbital elements: vis-viva and angular momentum of el2xv states, xv2el(el2xv) round trips
+  over every Kepler-solver branch (esolmd, eget, ehie; flon, fget)
 * kick: closed-form two/three-body accelerations, Newton's third law, loop-shape equivalence
 * encounter: hand-built geometries, brute-force pair lists, the sort-and-sweep loverlap quirk
 * step loops: WHM with one planet is exact Kepler; the reference's conservation-slope
@@ -15,6 +17,53 @@ from oracle import oracle as O
 from swiftest_gb300 import initial_conditions as IC
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+# ---------------------------------------------------------------- orbital elements
+def _elements(seed, n, emin, emax):
+    rng = np.random.default_rng(seed)
+    return dict(a=rng.uniform(0.3, 30.0, n), e=rng.uniform(emin, emax, n), inc=rng.uniform(0.0, np.pi, n),
+                capom=rng.uniform(0.0, 2 * np.pi, n), omega=rng.uniform(0.0, 2 * np.pi, n),
+                capm=rng.uniform(-3.0, 3.0, n))
+
+
+@pytest.mark.parametrize("emin,emax", [(0.0, 0.18), (0.18, 0.8), (0.8, 0.99), (1.01, 1.5), (1.5, 8.0)])
+def test_orbel_el2xv_physics_and_round_trip(emin, emax):
+    mu = IC.GMCB
+    el = _elements(int(emin * 100), 400, emin, emax)
+    if emin > 1.0:
+        el["capm"] = np.random.default_rng(7).uniform(-20.0, 20.0, 400)  # hyperbolic mean anomaly
+    rh, vh = O.el2xv(mu, el["a"], el["e"], el["inc"], el["capom"], el["omega"], el["capm"])
+    r = np.linalg.norm(rh, axis=1)
+    v2 = np.sum(vh * vh, axis=1)
+    a_signed = np.where(el["e"] > 1.0, -el["a"], el["a"])  # el2xv takes |a| for hyperbolae
+    np.testing.assert_allclose(v2, mu * (2.0 / r - 1.0 / a_signed), rtol=1e-11)  # vis-viva
+    h = np.linalg.norm(np.cross(rh, vh), axis=1)
+    np.testing.assert_allclose(h, np.sqrt(mu * el["a"] * np.abs(1.0 - el["e"] ** 2)), rtol=1e-11)
+    back = O.xv2el(mu, rh, vh)
+    np.testing.assert_allclose(back["a"], a_signed, rtol=1e-10)
+    np.testing.assert_allclose(back["e"], el["e"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(back["inc"], el["inc"], atol=1e-10)
+    ang = lambda x, y: np.abs(np.angle(np.exp(1j * (x - y))))  # noqa: E731
+    keep = (el["inc"] > 1e-3) & (el["inc"] < np.pi - 1e-3)  # node defined
+    assert ang(back["capom"], el["capom"])[keep].max() < 1e-9
+    assert ang(back["omega"] + back["capom"], el["omega"] + el["capom"]).max() < 1e-8
+    if emax <= 1.0:
+        assert ang(back["capm"], el["capm"]).max() < 1e-8
+    else:
+        np.testing.assert_allclose(back["capm"], el["capm"], rtol=1e-9, atol=1e-9)
+
+
+def test_orbel_circular_and_planar_conventions():
+    mu = IC.GMCB
+    rh, vh = O.el2xv(mu, np.array([1.0]), np.array([0.0]), np.array([0.0]), np.array([0.0]), np.array([0.0]),
+                     np.array([0.3]))
+    np.testing.assert_allclose(rh[0], [np.cos(0.3), np.sin(0.3), 0.0], atol=1e-15)
+    np.testing.assert_allclose(vh[0], np.sqrt(mu) * np.array([-np.sin(0.3), np.cos(0.3), 0.0]), rtol=1e-14,
+                               atol=1e-14)
+    el = O.xv2el(mu, rh, vh)
+    assert el["e"][0] == 0.0 and el["inc"][0] == 0.0 and el["capom"][0] == 0.0  # the reference's conventions
+    assert abs(el["capm"][0] - 0.3) < 1e-12 and abs(el["f"][0] - 0.3) < 1e-12
 
 
 # ---------------------------------------------------------------- drift
