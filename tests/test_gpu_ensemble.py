@@ -283,3 +283,41 @@ def test_mixed_drift_matches_fp64_drift(ctx):
     for a, b in zip(out[0][:2] + out[0][3:5], out[1][:2] + out[1][3:5]):
         rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(a, axis=1)
         assert rel.max() < 1e-12, rel.max()
+
+
+@pytest.mark.parametrize("integrator", ["HELIO", "WHM"])
+def test_ensemble_ragged_and_empty_systems(ctx, integrator):
+    # systems with no massive body (test particles around the central body only), one massive
+    # body, no test particles, and ordinary ones, in one ensemble; FP64 against the oracle,
+    # mixed runs to completion with finite states
+    sizes = [(0, 5), (1, 0), (3, 2), (40, 0), (25, 30)]
+    systems = []
+    for s, (n, t) in enumerate(sizes):
+        _, pl, tp = IC.make_system(seed=20 + s, npl=max(n, 1), ntp=t)
+        pl = {k: v[:n].copy() for k, v in IC.sort_for_integrator(pl, integrator).items()}
+        systems.append((pl, tp))
+    E = _pack({"integrator": integrator, "dt": 0.01, "rhscale": 6.5, "GMcb": np.full(len(sizes), IC.GMCB),
+               "Rcb": np.full(len(sizes), IC.RCB)}, systems)
+    ens = Ensemble(ctx, E, precision="FP64", dt=0.01)
+    refs = [O.OracleSystem(integrator, {"Gmass": IC.GMCB, "radius": IC.RCB}, pl, tp if len(tp["rh"]) else None,
+                           dt=0.01) for pl, tp in systems]
+    ens.step(50)
+    for r in refs:
+        r.step(50)
+    rh, vh, st = ens.get_pl()
+    trh, tvh, tst = ens.get_tp()
+    for s, r in enumerate(refs):
+        a, b = ens.poff[s], ens.poff[s + 1]
+        if b > a:
+            o_rh, o_vh, _ = r.get_pl()
+            assert np.array_equal(rh[a:b], o_rh) and np.array_equal(vh[a:b], o_vh), s
+        a, b = ens.toff[s], ens.toff[s + 1]
+        if b > a:
+            o_rh, o_vh, _ = r.get_tp()
+            assert np.array_equal(trh[a:b], o_rh) and np.array_equal(tvh[a:b], o_vh), s
+    ens.close()
+    m = Ensemble(ctx, E, precision="MIXED", dt=0.01)
+    m.step(50)
+    out = m.get_pl() + m.get_tp()
+    assert all(np.all(np.isfinite(x)) for x in out)
+    m.close()
