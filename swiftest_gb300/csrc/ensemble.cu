@@ -1239,6 +1239,7 @@ int recursion_launch(swg_ensemble *e, double dt) {
     a.mark_tp = e->mark_tp;
     a.out = e->rec_out;
     a.lclose = e->lclose;
+    a.fast = !exact(e);
     x.seg_pp = e->seg_pp;
     x.seg_pt = e->seg_pt;
     x.npl = e->npl;

@@ -394,6 +394,7 @@ struct RecArgs {
     int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
     int32_t *out;                   // [0] status, [1] deepest level reached
     int lclose;                     // check for collisions at every level (param%lclose)
+    int fast;                       // mixed path: fast FP64 forms of the drift and of r^-1.5
     int32_t *resume;                // REC_STATE ints: saved recursion stack of a paused step
     int32_t *pend;                  // set to 1 when the recursion pauses for a collision
 };
@@ -524,7 +525,9 @@ static __device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, 
             const double ris = sqrt(ri);
             const double r = sqrt(r2);
             const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            fac = pow_m1p5(r2) * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+            // FP64 path: the correctly rounded r^-1.5 shared with the oracle; mixed path: 1/(r^2 r)
+            const double p = a.fast ? 1.0 / (r2 * r) : pow_m1p5(r2);
+            fac = p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         } else {
             const double ir3 = 1.0 / (r2 * sqrt(r2));
             fac = ir3;
@@ -622,7 +625,8 @@ static __device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec,
         double *x = isp ? &a.rh[3 * i] : &a.trh[3 * i];
         double *v = isp ? &a.vb[3 * i] : &a.tvb[3 * i];
         double rx = x[0], ry = x[1], rz = x[2], vx = v[0], vy = v[1], vz = v[2];
-        const int fl = d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
+        const int fl = a.fast ? d_drift_one_fast(a.GMcb, rx, ry, rz, vx, vy, vz, dt)
+                              : d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
         x[0] = rx;
         x[1] = ry;
         x[2] = rz;

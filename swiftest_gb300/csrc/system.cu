@@ -684,6 +684,7 @@ int symba_recursion(swg_system *s, double dt) {
     a.mark_tp = s->mark_tp;
     a.out = s->rec_out;
     a.lclose = s->lclose;
+    a.fast = !exact(s);
     a.resume = s->rec_resume;
     a.pend = s->rec_out + 3;
     ProfScope ps(s->prof, s->c->stream, PROF_RECUR);
