@@ -514,6 +514,8 @@ __global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e, int 
     a.good = e.base.good + q;
     a.bpl = e.base.bpl + 2 * k0 + t0;
     a.btp = e.base.btp + t0;
+    a.adj_end = e.base.adj_end + 2 * (k0 + t0);  // bpl and btp slots
+    a.adj = e.base.adj + 2 * k0 + t0;
     a.resume = e.resume + (size_t)REC_STATE * s;
     a.pend = e.pend + s;
     blk_symba_recursion(a);
@@ -1200,7 +1202,7 @@ int recursion_launch(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     const int64_t n = e->pp_n + e->pt_n;
     SWG_TRY(ensure(c, e->rec_scratch, sizeof(double) * (size_t)(6 * n + 8) + (size_t)(2 * n + 64) +
-                                          sizeof(int32_t) * (size_t)(3 * n + 64)));
+                                          sizeof(int32_t) * (size_t)(7 * n + 128)));
     EnsRecArgs x;
     RecArgs &a = x.base;
     a.npl = 0;
@@ -1232,7 +1234,9 @@ int recursion_launch(swg_ensemble *e, double dt) {
     int32_t *ibuf = (int32_t *)(a.terms + 6 * n + 8);
     a.bpl = ibuf;               // 2 * npp + npt per system
     a.btp = ibuf + 2 * n + 32;  // npt per system
-    uint8_t *bbuf = (uint8_t *)(ibuf + 3 * n + 64);
+    a.adj_end = ibuf + 3 * n + 64;  // one per listed body: 2 * (npp + npt) per system
+    a.adj = ibuf + 5 * n + 96;      // two per pl-pl entry, one per pl-tp entry
+    uint8_t *bbuf = (uint8_t *)(ibuf + 7 * n + 128);
     a.lenc = bbuf;
     a.good = bbuf + n + 32;
     a.mark_pl = e->mark_pl;

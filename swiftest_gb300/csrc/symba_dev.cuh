@@ -391,6 +391,7 @@ struct RecArgs {
     uint8_t *lenc, *good;           // list-sized byte scratch
     double *terms;                  // 6 doubles per list entry
     int32_t *bpl, *btp;             // compact sets of bodies that appear in the lists
+    int32_t *adj_end, *adj;         // per-body list entries (CSR: end offsets, entry indices)
     int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
     int32_t *out;                   // [0] status, [1] deepest level reached
     int lclose;                     // check for collisions at every level (param%lclose)
@@ -471,7 +472,8 @@ static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int
 // symba_kick_list_plpl / _pltp (symba_kick.f90:126-340) for one sign, whole block.
 // The per-pair factors (sqrt, divide, the shell polynomial) depend only on positions,
 // so every pair is evaluated in parallel into `terms`.  The additions are then made
-// by one thread per body, which walks the list in order and adds only its own terms:
+// by one thread per body, which walks its own entries (the adjacency built at entry to the
+// recursion, in increasing list order) and adds their terms:
 // each body receives exactly the reference's additions in the reference's order,
 // while GB300's narrow FP64 pipe sees one instruction stream for all bodies instead
 // of one serial stream per pair.  A body that sits in several pairs gets its velocity
@@ -552,10 +554,11 @@ static __device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, 
         const int body = isp ? a.bpl[b] : a.btp[b - nbpl];
         bool zeroed = false, kicked = false;
         double ax = 0.0, ay = 0.0, az = 0.0;
+        const int e0 = b == 0 ? 0 : a.adj_end[b - 1], e1 = a.adj_end[b];
         if (isp) {
-            for (int64_t k = 0; k < npp; k++) {
-                const int i = pi1[k] - 1, j = pi2[k] - 1;
-                if (i != body && j != body) continue;
+            for (int e = e0; e < e1; e++) {
+                const int k = a.adj[e];
+                const int i = pi1[k] - 1;
                 const uint8_t g = a.good[k];
                 if (g == 0) continue;
                 zeroed = true;
@@ -581,14 +584,14 @@ static __device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, 
                 a.ah[3 * body + 0] = a.ah[3 * body + 1] = a.ah[3 * body + 2] = 0.0;
             }
         } else {
-            for (int64_t q = 0; q < npt; q++) {
-                if (ti2[q] - 1 != body) continue;
-                const uint8_t g = a.good[npp + q];
+            for (int e = e0; e < e1; e++) {
+                const int k = a.adj[e];
+                const uint8_t g = a.good[k];
                 if (g == 0) continue;
                 zeroed = true;
                 if (g != 1) continue;
                 kicked = true;
-                const double *t = &a.terms[6 * (npp + q)];
+                const double *t = &a.terms[6 * k];
                 ax = ax - t[0];
                 ay = ay - t[1];
                 az = az - t[2];
@@ -742,6 +745,91 @@ static __device__ void blk_collision_check(const RecArgs &a, int irec, double dt
 
 constexpr int RECT = 256;  // threads of the recursion kernel
 
+// In-place exclusive prefix sum of v[0, n) by the whole block (blockDim a multiple of 32,
+// at most 1024 threads).
+static __device__ void blk_exclusive_scan(int32_t *v, int n) {
+    __shared__ int32_t s_w[32], s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int own = i < n ? v[i] : 0;
+        int x = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int t = lane < nw ? s_w[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            if (lane < nw) s_w[lane] = t;
+        }
+        __syncthreads();
+        const int carry = s_carry;
+        if (i < n) v[i] = x - own + (w > 0 ? s_w[w - 1] : 0) + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = carry + s_w[nw - 1];
+        __syncthreads();
+    }
+}
+
+// Per-body adjacency of the encounter lists, built once per recursion launch: body slot b
+// (bpl slots first, then btp) owns entries adj[adj_end[b-1], adj_end[b]) (from 0 for b = 0),
+// the pl-pl entries naming a bpl body or the pl-tp entries naming a btp body, as combined
+// list indices (pl-tp entry q is npp + q) in increasing order.  The kick's per-body walk
+// then visits only the body's own entries, in the order the reference adds them.  On
+// return mark_pl / mark_tp hold slot + 1 of each listed body (cleared at kernel exit).
+static __device__ void blk_build_adjacency(const RecArgs &a, int nbpl, int nbtp) {
+    const int nb = nbpl + nbtp;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        if (b < nbpl) a.mark_pl[a.bpl[b]] = b + 1;
+        else a.mark_tp[a.btp[b - nbpl]] = b + 1;
+        a.adj_end[b] = 0;
+    }
+    __syncthreads();
+    // entry counts per slot
+    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x) {
+        if (k < a.npp) {
+            atomicAdd(&a.adj_end[a.mark_pl[a.pp[k] - 1] - 1], 1);
+            atomicAdd(&a.adj_end[a.mark_pl[a.pp[a.ppcap + k] - 1] - 1], 1);
+        } else {
+            atomicAdd(&a.adj_end[a.mark_tp[a.pt[a.ptcap + (k - a.npp)] - 1] - 1], 1);
+        }
+    }
+    __syncthreads();
+    blk_exclusive_scan(a.adj_end, nb);
+    // fill: each append advances the slot's start offset, which ends at the slot's end
+    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x) {
+        if (k < a.npp) {
+            a.adj[atomicAdd(&a.adj_end[a.mark_pl[a.pp[k] - 1] - 1], 1)] = (int32_t)k;
+            a.adj[atomicAdd(&a.adj_end[a.mark_pl[a.pp[a.ppcap + k] - 1] - 1], 1)] = (int32_t)k;
+        } else {
+            a.adj[atomicAdd(&a.adj_end[a.mark_tp[a.pt[a.ptcap + (k - a.npp)] - 1] - 1], 1)] = (int32_t)k;
+        }
+    }
+    __syncthreads();
+    // the atomics fill in any order: sort each slot's entries (few per body)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const int e0 = b == 0 ? 0 : a.adj_end[b - 1], e1 = a.adj_end[b];
+        for (int e = e0 + 1; e < e1; e++) {
+            const int32_t v = a.adj[e];
+            int f = e - 1;
+            while (f >= e0 && a.adj[f] > v) {
+                a.adj[f + 1] = a.adj[f];
+                f--;
+            }
+            a.adj[f + 1] = v;
+        }
+    }
+    __syncthreads();
+}
+
 // symba_step_recur_system (symba_step.f90:163-262) for the whole recursion tree of one
 // step, started at level 0, in a single block: the reference's recursive calls become
 // an explicit stack of (loop counter, phase) per level, and every per-level operation
@@ -770,6 +858,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
     }
     __syncthreads();
     const int nbpl = s_nbpl, nbtp = s_nbtp;
+    blk_build_adjacency(a, nbpl, nbtp);
     int ireci = 0;
     const bool resumed = a.resume && a.resume[0] == 1;
     if (resumed) {  // continue a step paused after a collision check
