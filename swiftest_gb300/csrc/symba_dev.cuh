@@ -405,12 +405,19 @@ struct RecArgs {
 constexpr int MAXLEV = 48;
 constexpr int REC_STATE = 2 + 2 * MAXLEV;
 
-// Item index of this thread in the recursion kernel's block loops: consecutive items go
-// to different warps, hence to different SM sub-partitions.  The few pairs and bodies
-// of an encounter each run a long serial FP64 chain, and GB300's narrow FP64 pipe
-// takes about as long for a warp instruction with one active lane as with 32, so
-// spreading them over the four sub-partitions' pipes is what runs them concurrently.
-__device__ __forceinline__ int spread_tid() { return (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+// Item index of this thread in the recursion kernel's block loops (blockDim a multiple
+// of 128): items k, k+1, k+2, k+3 go to warps 0-3, one per SM sub-partition, then to the
+// next lane, and items from 128 on to warps 4-7.  On GB300 a warp issues an FP64
+// instruction at most every ~64 cycles, with one active lane or 32, and an SM at most
+// one every ~19 cycles over all its warps (measured with FMA chains); the recursion's
+// few pairs and bodies each run a long FP64 chain, so the fewest warps that still keep
+// every sub-partition busy (four) run them fastest.  Spreading them over eight warps
+// doubles the SM's FP64 issue load; packing them into one or two warps makes each warp
+// carry the divergent paths (iteration counts, branch kinds) of many chains.
+__device__ __forceinline__ int spread_tid() {
+    const int w = threadIdx.x >> 5;
+    return (w >> 2) * 128 + (threadIdx.x & 31) * 4 + (w & 3);
+}
 
 // symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), whole block.
 static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any) {
