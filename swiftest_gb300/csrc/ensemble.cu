@@ -522,37 +522,39 @@ __global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e, int 
 }
 
 // ---- WHM (whm_step.f90, whm_kick.f90, whm_coord.f90) of every system: one block per system
-// for the reference's serial Jacobi sums (one thread, in the reference's order)
+// for the Jacobi running sums (FP64 path: one thread, in the reference's order)
 enum { WHM_H2J = 0, WHM_J2H = 1, WHM_VH2VJ = 2 };
 __global__ void k_ens_whm_coord(int mode, const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
-                                const double *Gm, const double *eta, double *rh, double *vh, double *xj, double *vj) {
+                                const double *Gm, const double *eta, double *rh, double *vh, double *xj, double *vj,
+                                int exact) {
     const int s = blockIdx.x;
     if (npl[s] == 0) return;
     __shared__ WhmScratch sh;
     const size_t o = poff[s];
     if (mode == WHM_H2J)
-        blk_whm_h2j(npl[s], Gm + o, eta + o, rh + 3 * o, vh + 3 * o, xj + 3 * o, vj + 3 * o, sh);
+        blk_whm_h2j(npl[s], Gm + o, eta + o, rh + 3 * o, vh + 3 * o, xj + 3 * o, vj + 3 * o, sh, exact);
     else if (mode == WHM_J2H)
-        blk_whm_j2h(npl[s], Gm + o, eta + o, xj + 3 * o, vj + 3 * o, rh + 3 * o, vh + 3 * o, sh);
+        blk_whm_j2h(npl[s], Gm + o, eta + o, xj + 3 * o, vj + 3 * o, rh + 3 * o, vh + 3 * o, sh, exact);
     else
-        blk_whm_vh2vj(npl[s], Gm + o, eta + o, vh + 3 * o, vj + 3 * o, sh);
+        blk_whm_vh2vj(npl[s], Gm + o, eta + o, vh + 3 * o, vj + 3 * o, sh, exact);
 }
 __global__ void k_ens_whm_accel(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl, const double *Gm,
                                 const double *__restrict__ GMcb, const double *rh, const double *xj,
-                                const int32_t *lmask, double *ir3h, double *ir3j, double *ah) {
+                                const int32_t *lmask, double *ir3h, double *ir3j, double *ah, int exact) {
     const int s = blockIdx.x;
     if (npl[s] == 0) return;
     __shared__ WhmScratch sh;
     const size_t o = poff[s];
-    blk_whm_accel_pl(npl[s], Gm + o, GMcb[s], rh + 3 * o, xj + 3 * o, lmask + o, ir3h + o, ir3j + o, ah + 3 * o, sh);
+    blk_whm_accel_pl(npl[s], Gm + o, GMcb[s], rh + 3 * o, xj + 3 * o, lmask + o, ir3h + o, ir3j + o, ah + 3 * o, sh,
+                     exact);
 }
 // ah0 of whm_kick_getacch_tp (whm_kick.f90:70-122) per system at the pl positions rp
 __global__ void k_ens_whm_ah0(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl, const double *Gm,
-                              const double *rp, double *ah0) {
+                              const double *rp, double *ah0, int exact) {
     const int s = blockIdx.x;
     __shared__ WhmScratch sh;
     const size_t o = poff[s];
-    blk_whm_ah0(Gm + o, rp + 3 * o, npl[s], ah0 + 3 * s, sh);
+    blk_whm_ah0(Gm + o, rp + 3 * o, npl[s], ah0 + 3 * s, sh, exact);
 }
 // tah = ah0 of the test particle's system (masked), before the pair kick adds to it
 __global__ void k_ens_whm_tp_ah0(int64_t ntp, const int32_t *__restrict__ tsys, const int32_t *__restrict__ tlmask,
@@ -1385,14 +1387,14 @@ int whm_accel_pl(swg_ensemble *e) {
     swg_ctx *c = e->c;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->ah, 0, sizeof(double) * 3 * e->NPL, c->stream), "memset"));
     k_ens_whm_accel<<<e->nsys, 256, 0, c->stream>>>(e->poff, e->npl, e->Gmass, e->GMcb, e->rh, e->xj, e->lmask,
-                                                    e->ir3h, e->ir3j, e->ah);
+                                                    e->ir3h, e->ir3j, e->ah, exact(e));
     SWG_TRY(L(c, "ens_whm_accel"));
     ProfScope ps(e->prof, c->stream, PROF_KICK_PL);
     return accel_int_pl(e, e->head, nullptr, 0, 0);
 }
 int whm_coord(swg_ensemble *e, int mode) {
     k_ens_whm_coord<<<e->nsys, 256, 0, e->c->stream>>>(mode, e->poff, e->npl, e->Gmass, e->eta, e->rh, e->vh, e->xj,
-                                                       e->vj);
+                                                       e->vj, exact(e));
     return L(e->c, "ens_whm_coord");
 }
 int whm_kick_vh_pl(swg_ensemble *e, double dt, int lbeg) {
@@ -1410,7 +1412,7 @@ int whm_kick_vh_pl(swg_ensemble *e, double dt, int lbeg) {
 int whm_accel_tp(swg_ensemble *e, int lbeg) {
     swg_ctx *c = e->c;
     const double *rp = lbeg ? e->rbeg : e->rend;
-    k_ens_whm_ah0<<<e->nsys, 256, 0, c->stream>>>(e->poff, e->npl, e->Gmass, rp, e->whm_ah0);
+    k_ens_whm_ah0<<<e->nsys, 256, 0, c->stream>>>(e->poff, e->npl, e->Gmass, rp, e->whm_ah0, exact(e));
     SWG_TRY(L(c, "ens_whm_ah0"));
     k_ens_whm_tp_ah0<<<grid_for(e->NTP, 256), 256, 0, c->stream>>>(e->NTP, e->tsys, e->tlmask, e->whm_ah0, e->tah);
     SWG_TRY(L(c, "ens_whm_tp_ah0"));

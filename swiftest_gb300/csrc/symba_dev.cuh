@@ -1103,9 +1103,10 @@ static __device__ void blk_energy_final(int n, int whm, const double *rh, const 
 // ---- WHM (Jacobi coordinates)
 // The reference's Jacobi conversions and the ah0 / ah2 accelerations are running sums over
 // the bodies in index order.  Here the whole block forms the terms (products and quotients)
-// into shared memory, one thread per component adds them in index order (the only serial
-// part: the additions, with the reference's operands and order, so FP64 results stay
-// bit-identical), and the block uses the running sums; bodies go through in chunks of WCH.
+// into shared memory, the running sums are taken (exact: one thread per component adds
+// them in index order with the reference's operands, so FP64 results stay bit-identical;
+// mixed path: a segmented warp scan per component), and the block uses them; bodies go
+// through in chunks of WCH.
 constexpr int WCH = 512;
 struct WhmScratch {
     double t[6][WCH];      // terms, then (in place) inclusive running sums
@@ -1114,24 +1115,58 @@ struct WhmScratch {
     unsigned char m[WCH];  // ah2: the body's mask
 };
 
-// t[c][q] <- run[c] + t[c][0] + ... + t[c][q] for c < m (one thread per component)
-static __device__ __forceinline__ void whm_running(WhmScratch &sh, int m, int cnt) {
+// v[q] <- run + v[0] + ... + v[q] for q < cnt, and run <- the last value, by one whole warp
+// (mixed path): lane l sums its segment of ceil(cnt / 32) terms, the warp scans the
+// segment sums, and each lane re-adds its segment from its prefix.  ~2 cnt / 32 + 6 FP64
+// issues on the warp instead of cnt serial additions (a warp issues an FP64 instruction
+// at most every ~64 cycles on GB300); the rounding differs from the serial order.
+static __device__ __forceinline__ void warp_seg_scan(double *v, int cnt, double &run) {
+    const int lane = threadIdx.x & 31;
+    const int seg = (cnt + 31) >> 5, q0 = min(cnt, lane * seg), q1 = min(cnt, q0 + seg);
+    double own = 0.0;
+    for (int q = q0; q < q1; q++) own += v[q];
+    double incl = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    const double base = run;
+    double acc = lane == 0 ? base : base + excl;
+    for (int q = q0; q < q1; q++) {
+        acc += v[q];
+        v[q] = acc;
+    }
+    const double total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    if (lane == 0) run = base + total;
+}
+
+// t[c][q] <- run[c] + t[c][0] + ... + t[c][q] for c < m.  exact: one thread per component
+// adds in index order (the reference's operands and order); otherwise one warp per
+// component runs warp_seg_scan (blockDim >= 32 m).
+static __device__ __forceinline__ void whm_running(WhmScratch &sh, int m, int cnt, bool exact) {
     __syncthreads();
-    if (threadIdx.x < m) {
-        const int c = threadIdx.x;
-        double s = sh.run[c];
-        for (int q = 0; q < cnt; q++) {
-            s = s + sh.t[c][q];
-            sh.t[c][q] = s;
+    if (exact) {
+        if (threadIdx.x < m) {
+            const int c = threadIdx.x;
+            double s = sh.run[c];
+            for (int q = 0; q < cnt; q++) {
+                s = s + sh.t[c][q];
+                sh.t[c][q] = s;
+            }
+            sh.run[c] = s;
         }
-        sh.run[c] = s;
+    } else if ((int)(threadIdx.x >> 5) < m) {
+        const int c = threadIdx.x >> 5;
+        warp_seg_scan(sh.t[c], cnt, sh.run[c]);
     }
     __syncthreads();
 }
 
 // whm_coord_h2j_pl (whm_coord.f90:14-51)
 static __device__ void blk_whm_h2j(int n, const double *Gm, const double *eta, const double *rh, const double *vh,
-                                   double *xj, double *vj, WhmScratch &sh) {
+                                   double *xj, double *vj, WhmScratch &sh, bool exact) {
     if (n <= 0) return;
     if (threadIdx.x < 3) {
         xj[threadIdx.x] = rh[threadIdx.x];
@@ -1148,7 +1183,7 @@ static __device__ void blk_whm_h2j(int n, const double *Gm, const double *eta, c
                 sh.t[3 + d][q] = Gm[k] * vh[3 * k + d];
             }
         }
-        whm_running(sh, 6, cnt);
+        whm_running(sh, 6, cnt, exact);
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
             const int i = c0 + q;
             for (int d = 0; d < 3; d++) {
@@ -1162,7 +1197,7 @@ static __device__ void blk_whm_h2j(int n, const double *Gm, const double *eta, c
 }
 // whm_coord_j2h_pl (:54-90)
 static __device__ void blk_whm_j2h(int n, const double *Gm, const double *eta, const double *xj, const double *vj,
-                                   double *rh, double *vh, WhmScratch &sh) {
+                                   double *rh, double *vh, WhmScratch &sh, bool exact) {
     if (n <= 0) return;
     if (threadIdx.x < 3) {
         rh[threadIdx.x] = xj[threadIdx.x];
@@ -1179,7 +1214,7 @@ static __device__ void blk_whm_j2h(int n, const double *Gm, const double *eta, c
                 sh.t[3 + d][q] = Gm[k] * vj[3 * k + d] / eta[k];
             }
         }
-        whm_running(sh, 6, cnt);
+        whm_running(sh, 6, cnt, exact);
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
             const int i = c0 + q;
             for (int d = 0; d < 3; d++) {
@@ -1191,7 +1226,7 @@ static __device__ void blk_whm_j2h(int n, const double *Gm, const double *eta, c
 }
 // whm_coord_vh2vj_pl (:93-124)
 static __device__ void blk_whm_vh2vj(int n, const double *Gm, const double *eta, const double *vh, double *vj,
-                                     WhmScratch &sh) {
+                                     WhmScratch &sh, bool exact) {
     if (n <= 0) return;
     if (threadIdx.x < 3) vj[threadIdx.x] = vh[threadIdx.x];
     if (threadIdx.x < 3) sh.run[threadIdx.x] = 0.0;
@@ -1202,7 +1237,7 @@ static __device__ void blk_whm_vh2vj(int n, const double *Gm, const double *eta,
             const int k = c0 + q - 1;
             for (int d = 0; d < 3; d++) sh.t[d][q] = Gm[k] * vh[3 * k + d];
         }
-        whm_running(sh, 3, cnt);
+        whm_running(sh, 3, cnt, exact);
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
             const int i = c0 + q;
             for (int d = 0; d < 3; d++) {
@@ -1214,7 +1249,8 @@ static __device__ void blk_whm_vh2vj(int n, const double *Gm, const double *eta,
 }
 // whm_kick_getacch_ah0 (whm_kick.f90:125-149): ah0 = -sum mu_i rhp_i / |rhp_i|^3 in index
 // order, into out[3] (shared or global), visible to the block on return
-static __device__ void blk_whm_ah0(const double *mu, const double *rhp, int n, double *out, WhmScratch &sh) {
+static __device__ void blk_whm_ah0(const double *mu, const double *rhp, int n, double *out, WhmScratch &sh,
+                                   bool exact) {
     if (threadIdx.x < 3) sh.run[threadIdx.x] = 0.0;
     for (int c0 = 0; c0 < n; c0 += WCH) {
         const int cnt = min(WCH, n - c0);
@@ -1227,7 +1263,7 @@ static __device__ void blk_whm_ah0(const double *mu, const double *rhp, int n, d
             const double fac = mu[i] * ir3h;
             for (int d = 0; d < 3; d++) sh.t[d][q] = -(fac * rhp[3 * i + d]);  // a - b == a + (-b)
         }
-        whm_running(sh, 3, cnt);
+        whm_running(sh, 3, cnt, exact);
     }
     __syncthreads();
     if (threadIdx.x < 3) out[threadIdx.x] = sh.run[threadIdx.x];
@@ -1237,7 +1273,7 @@ static __device__ void blk_whm_ah0(const double *mu, const double *rhp, int n, d
 // ah1 (:152-179) and ah2 (:182-215), whole block
 static __device__ void blk_whm_accel_pl(int n, const double *Gm, double GMcb, const double *rh, const double *xj,
                                         const int32_t *lmask, double *ir3h, double *ir3j, double *ah,
-                                        WhmScratch &sh) {
+                                        WhmScratch &sh, bool exact) {
     __shared__ double s_ah0[3];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double r2 = rh[3 * i] * rh[3 * i] + rh[3 * i + 1] * rh[3 * i + 1] + rh[3 * i + 2] * rh[3 * i + 2];
@@ -1247,7 +1283,7 @@ static __device__ void blk_whm_accel_pl(int n, const double *Gm, double GMcb, co
         ir = 1.0 / sqrt(r2);
         ir3j[i] = ir / r2;
     }
-    blk_whm_ah0(Gm + 1, rh + 3, n - 1, s_ah0, sh);
+    blk_whm_ah0(Gm + 1, rh + 3, n - 1, s_ah0, sh, exact);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         for (int d = 0; d < 3; d++) ah[3 * i + d] = ah[3 * i + d] + s_ah0[d];
         if (i >= 1 && lmask[i])
@@ -1268,32 +1304,47 @@ static __device__ void blk_whm_accel_pl(int n, const double *Gm, double GMcb, co
             sh.e[q] = Gm[c0 + q - 1];
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double etaj = sh.run[3];
-            for (int q = 0; q < cnt; q++) {
-                if (!sh.m[q]) continue;
-                etaj = etaj + sh.e[q];
-                sh.e[q] = etaj;
+        if (exact) {
+            if (threadIdx.x == 0) {
+                double etaj = sh.run[3];
+                for (int q = 0; q < cnt; q++) {
+                    if (!sh.m[q]) continue;
+                    etaj = etaj + sh.e[q];
+                    sh.e[q] = etaj;
+                }
+                sh.run[3] = etaj;
             }
-            sh.run[3] = etaj;
+        } else {  // unmasked bodies add zero; their running values are not used
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x)
+                if (!sh.m[q]) sh.e[q] = 0.0;
+            __syncthreads();
+            if (threadIdx.x < 32) warp_seg_scan(sh.e, cnt, sh.run[3]);
         }
         __syncthreads();
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
-            if (!sh.m[q]) continue;
+            if (!sh.m[q]) {
+                for (int d = 0; d < 3; d++) sh.t[d][q] = 0.0;
+                continue;
+            }
             const int i = c0 + q;
             const double fac = Gm[i] * GMcb * ir3j[i] / sh.e[q];
             for (int d = 0; d < 3; d++) sh.t[d][q] = fac * xj[3 * i + d];
         }
         __syncthreads();
-        if (threadIdx.x < 3) {
-            const int d = threadIdx.x;
-            double a2 = sh.run[d];
-            for (int q = 0; q < cnt; q++) {
-                if (!sh.m[q]) continue;
-                a2 = a2 + sh.t[d][q];
-                sh.t[d][q] = a2;
+        if (exact) {
+            if (threadIdx.x < 3) {
+                const int d = threadIdx.x;
+                double a2 = sh.run[d];
+                for (int q = 0; q < cnt; q++) {
+                    if (!sh.m[q]) continue;
+                    a2 = a2 + sh.t[d][q];
+                    sh.t[d][q] = a2;
+                }
+                sh.run[d] = a2;
             }
-            sh.run[d] = a2;
+        } else if (threadIdx.x < 96) {
+            const int d = threadIdx.x >> 5;
+            warp_seg_scan(sh.t[d], cnt, sh.run[d]);
         }
         __syncthreads();
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {

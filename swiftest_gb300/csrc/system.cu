@@ -161,30 +161,30 @@ __global__ void __launch_bounds__(RB) k_energy_final(int n, int whm, const doubl
 
 // ---- WHM coordinate kernels and accelerations (block device code in symba_dev.cuh)
 __global__ void k_whm_h2j(int n, const double *Gm, const double *eta, const double *rh, const double *vh, double *xj,
-                          double *vj) {
+                          double *vj, int exact) {
     __shared__ WhmScratch sh;
-    blk_whm_h2j(n, Gm, eta, rh, vh, xj, vj, sh);
+    blk_whm_h2j(n, Gm, eta, rh, vh, xj, vj, sh, exact);
 }
 __global__ void k_whm_j2h(int n, const double *Gm, const double *eta, const double *xj, const double *vj, double *rh,
-                          double *vh) {
+                          double *vh, int exact) {
     __shared__ WhmScratch sh;
-    blk_whm_j2h(n, Gm, eta, xj, vj, rh, vh, sh);
+    blk_whm_j2h(n, Gm, eta, xj, vj, rh, vh, sh, exact);
 }
-__global__ void k_whm_vh2vj(int n, const double *Gm, const double *eta, const double *vh, double *vj) {
+__global__ void k_whm_vh2vj(int n, const double *Gm, const double *eta, const double *vh, double *vj, int exact) {
     __shared__ WhmScratch sh;
-    blk_whm_vh2vj(n, Gm, eta, vh, vj, sh);
+    blk_whm_vh2vj(n, Gm, eta, vh, vj, sh, exact);
 }
 __global__ void k_whm_accel_pl(int n, const double *Gm, double GMcb, const double *rh, const double *xj,
-                               const int32_t *lmask, double *ir3h, double *ir3j, double *ah) {
+                               const int32_t *lmask, double *ir3h, double *ir3j, double *ah, int exact) {
     __shared__ WhmScratch sh;
-    blk_whm_accel_pl(n, Gm, GMcb, rh, xj, lmask, ir3h, ir3j, ah, sh);
+    blk_whm_accel_pl(n, Gm, GMcb, rh, xj, lmask, ir3h, ir3j, ah, sh, exact);
 }
 // whm_kick_getacch_tp ah0 part (:70-122): tah += ah0(rp) for masked tp ; zero first when requested
 __global__ void k_whm_tp_ah0(int ntp, int npl, const double *Gm, const double *rp, const int32_t *tlmask, double *tah,
-                             int zero) {
+                             int zero, int exact) {
     __shared__ WhmScratch sh;
     __shared__ double s_ah0[3];
-    blk_whm_ah0(Gm, rp, npl, s_ah0, sh);
+    blk_whm_ah0(Gm, rp, npl, s_ah0, sh, exact);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntp; i += gridDim.x * blockDim.x) {
         if (!tlmask[i]) continue;
         for (int d = 0; d < 3; d++) tah[3 * i + d] = (zero ? 0.0 : tah[3 * i + d]) + s_ah0[d];
@@ -362,7 +362,7 @@ int whm_accel_pl(swg_system *s) {
     swg_ctx *c = s->c;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(s->ah, 0, sizeof(double) * 3 * s->npl, c->stream), "memset"));
     k_whm_accel_pl<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->GMcb, s->rh, s->xj, s->lmask, s->ir3h, s->ir3j,
-                                             s->ah);
+                                             s->ah, exact(s));
     SWG_TRY(L(c, "whm_accel_pl"));
     return accel_int_pl(s, 0);
 }
@@ -370,7 +370,7 @@ int whm_kick_vh_pl(swg_system *s, double dt, int lbeg) {
     swg_ctx *c = s->c;
     if (lbeg) {
         if (s->lfirst_pl) {
-            k_whm_h2j<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->rh, s->vh, s->xj, s->vj);
+            k_whm_h2j<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->rh, s->vh, s->xj, s->vj, exact(s));
             SWG_TRY(L(c, "whm_h2j"));
             SWG_TRY(whm_accel_pl(s));
             s->lfirst_pl = 0;
@@ -387,7 +387,8 @@ int whm_kick_vh_pl(swg_system *s, double dt, int lbeg) {
 int whm_accel_tp(swg_system *s, int lbeg, int zero) {
     swg_ctx *c = s->c;
     const double *rp = lbeg ? s->rbeg : s->rend;
-    k_whm_tp_ah0<<<grid_for(s->ntp, 256), 256, 0, c->stream>>>(s->ntp, s->npl, s->Gmass, rp, s->tlmask, s->tah, zero);
+    k_whm_tp_ah0<<<grid_for(s->ntp, 256), 256, 0, c->stream>>>(s->ntp, s->npl, s->Gmass, rp, s->tlmask, s->tah, zero,
+                                                                     exact(s));
     SWG_TRY(L(c, "whm_tp_ah0"));
     if (s->precision == SWG_MIXED) {
         const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
@@ -414,7 +415,7 @@ int whm_step(swg_system *s, double dt) {
     s->lfirst_tp = s->lfirst_pl;
     if (s->npl > 0) {
         SWG_TRY(whm_kick_vh_pl(s, dth, 1));
-        k_whm_vh2vj<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->vh, s->vj);
+        k_whm_vh2vj<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->vh, s->vj, exact(s));
         SWG_TRY(L(c, "whm_vh2vj"));
         SWG_TRY(drift_all(c, s->muj, 0.0, s->xj, s->vj, s->npl, 0, 0.0, dt, s->lmask, s->iflag));
         int32_t *dflag = (int32_t *)s->flags.ptr;
@@ -431,7 +432,7 @@ int whm_step(swg_system *s, double dt) {
             c->err = "Danby drift failed for a massive body (WHM stops the run)";
             return SWG_ERR_DRIFT;
         }
-        k_whm_j2h<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->xj, s->vj, s->rh, s->vh);
+        k_whm_j2h<<<1, 256, 0, c->stream>>>(s->npl, s->Gmass, s->eta, s->xj, s->vj, s->rh, s->vh, exact(s));
         SWG_TRY(L(c, "whm_j2h"));
         SWG_TRY(whm_kick_vh_pl(s, dth, 0));
     }
