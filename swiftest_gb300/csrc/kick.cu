@@ -57,9 +57,10 @@ __device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&sel
     __shared__ unsigned sRmax[2];  // largest partner radius of the tile, per loading warp (float bits)
     for (int j0 = jbeg; j0 < jstop; j0 += MT) {
         float rmax = 0.f;
-        for (int t = threadIdx.x; t < MT; t += blockDim.x) {
-            const int jl = j0 + t;
-            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
+        // partner jl split into (x_hi, y_hi, z_hi, Gm) and (x_lo, y_lo, z_lo, R); zero past jstop
+        auto load = [&](int jl, float4 &a, float4 &b) {
+            a = make_float4(0.f, 0.f, 0.f, 0.f);
+            b = make_float4(0.f, 0.f, 0.f, 0.f);
             if (jl < jstop && pA) {
                 a = pA[jl];
                 b = pB[jl];
@@ -70,9 +71,22 @@ __device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&sel
                 a.w = __double2float_rn(Gm[jl]);
                 b.w = RAD ? __double2float_rn(R[jl]) : 0.f;
             }
-            sA[t] = a;
-            sB[t] = b;
-            rmax = fmaxf(rmax, b.w);
+        };
+        if (TP) {  // paired layout of mixed_tile_tp2
+            for (int p = threadIdx.x; p < MT / 2; p += blockDim.x) {
+                float4 a0, b0, a1, b1;
+                load(j0 + 2 * p, a0, b0);
+                load(j0 + 2 * p + 1, a1, b1);
+                stage_pair(sA, sB, p, a0, b0, a1, b1);
+            }
+        } else {
+            for (int t = threadIdx.x; t < MT; t += blockDim.x) {
+                float4 a, b;
+                load(j0 + t, a, b);
+                sA[t] = a;
+                sB[t] = b;
+                rmax = fmaxf(rmax, b.w);
+            }
         }
         if (!TP && RAD && threadIdx.x < MT) {  // whole warps: blockDim.x is a multiple of 32
             const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(rmax));  // radii are >= 0
@@ -85,7 +99,9 @@ __device__ __forceinline__ void mixed_sweep(int jbeg, int jstop, const int (&sel
         const int nt = min(MT, jstop - j0);
         float px[RPT], py[RPT], pz[RPT], mn[RPT];
         const bool guard = !TP && (GMT || (j0 < shi && j0 + nt > slo));  // block-uniform
-        if (guard) {
+        if (TP) {
+            mixed_tile_tp2<RPT>(nt, q, sA, sB, px, py, pz);
+        } else if (guard) {
             mixed_tile<TP, RAD, GMT, true, RPT>(j0, nt, self, nplm, self_m, q, sA, sB, px, py, pz, mn);
         } else {
 #pragma unroll

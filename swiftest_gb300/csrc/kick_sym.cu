@@ -56,60 +56,152 @@ __host__ __device__ __forceinline__ int pair_slot(int I, int J, int nt) {
     return I * (nt - 1) - I * (I - 1) / 2 + (J - I - 1);
 }
 
-// 32 steps of one sub-tile for receivers k < NK of this lane (see the file comment).  A/B
-// point at the lane's first partner of the doubled sub-tile; src is the lane above.
-// GUARD: the radius rule pair by pair (RAD only); else, with RAD, mn keeps the smallest r^2.
+// Shared layout of a staged 32-partner sub-tile: entry e (0 <= e < 48) holds partners
+// a = e mod 32 and b = (e + 16) mod 32 side by side in four 16-byte words,
+//   P[0][e] = (xh_a, xh_b, yh_a, yh_b)   P[1][e] = (zh_a, zh_b, Gm_a, Gm_b)
+//   P[2][e] = (xl_a, xl_b, yl_a, yl_b)   P[3][e] = (zl_a, zl_b, R_a, R_b)
+// so that each 64-bit half-word is the same quantity of the two partners, ready for the
+// packed FP32 (f32x2) instructions.  Lane t reads entry t + s at step s (s < 16) without
+// wrapping, i.e. partners t + s and t + s + 16 (mod 32): every partner once in 16 steps.
+constexpr int PE = 48;  // entries per staged sub-tile
+struct SubTile {
+    ulonglong2 w[4][PE];
+};
+
+// Stage the sub-tile whose partner for this lane is (a, b) = (hi, Gm), (lo, R): lane t
+// writes entry t and, for t < 16, entry t + 32 (the same two partners t, t + 16).
+__device__ __forceinline__ void stage_subtile(SubTile &P, const float4 &a, const float4 &b, int lane) {
+    const float4 xa = make_float4(__shfl_xor_sync(FULL, a.x, 16), __shfl_xor_sync(FULL, a.y, 16),
+                                  __shfl_xor_sync(FULL, a.z, 16), __shfl_xor_sync(FULL, a.w, 16));
+    const float4 xb = make_float4(__shfl_xor_sync(FULL, b.x, 16), __shfl_xor_sync(FULL, b.y, 16),
+                                  __shfl_xor_sync(FULL, b.z, 16), __shfl_xor_sync(FULL, b.w, 16));
+    // entry t = (partner t, partner (t + 16) mod 32), and (t + 16) mod 32 == t ^ 16
+    const float4 lo_a = a, hi_a = xa, lo_b = b, hi_b = xb;
+    const ulonglong2 w0 = make_ulonglong2(f2_pack(lo_a.x, hi_a.x), f2_pack(lo_a.y, hi_a.y));
+    const ulonglong2 w1 = make_ulonglong2(f2_pack(lo_a.z, hi_a.z), f2_pack(lo_a.w, hi_a.w));
+    const ulonglong2 w2 = make_ulonglong2(f2_pack(lo_b.x, hi_b.x), f2_pack(lo_b.y, hi_b.y));
+    const ulonglong2 w3 = make_ulonglong2(f2_pack(lo_b.z, hi_b.z), f2_pack(lo_b.w, hi_b.w));
+    P.w[0][lane] = w0;
+    P.w[1][lane] = w1;
+    P.w[2][lane] = w2;
+    P.w[3][lane] = w3;
+    if (lane < 16) {
+        P.w[0][lane + 32] = w0;
+        P.w[1][lane + 32] = w1;
+        P.w[2][lane + 32] = w2;
+        P.w[3][lane + 32] = w3;
+    }
+}
+
+// A receiver of this lane in packed form: each coordinate (and the mass) in both halves.
+struct Recv2 {
+    f32x2 xh, yh, zh, xl, yl, zl, gm;
+    float R;
+};
+
+// The pair rule on both halves: zero fi and fj of a pair within the radii (RAD) or, with
+// jself >= 0, of the self pair (partner index jself within the sub-tile).
+template <bool RAD>
+__device__ __forceinline__ void rule2(f32x2 r2, f32x2 Rp, float Rk, int ja, int jb, int jself, f32x2 &fi, f32x2 &fj) {
+    float r2a, r2b, fia, fib, fja, fjb;
+    f2_unpack(r2, r2a, r2b);
+    f2_unpack(fi, fia, fib);
+    f2_unpack(fj, fja, fjb);
+    bool oka, okb;
+    if (RAD) {
+        float Ra, Rb;
+        f2_unpack(Rp, Ra, Rb);
+        const float rsa = Rk + Ra, rsb = Rk + Rb;
+        oka = r2a > rsa * rsa;
+        okb = r2b > rsb * rsb;
+    } else {
+        oka = ja != jself;
+        okb = jb != jself;
+    }
+    fi = f2_pack(oka ? fia : 0.f, okb ? fib : 0.f);
+    fj = f2_pack(oka ? fja : 0.f, okb ? fjb : 0.f);
+}
+
+// 16 steps of one sub-tile for receivers k < NK of this lane (see the file comment): at
+// step s the lane evaluates its receivers against its entry's two partners with the
+// packed instructions, adds to packed receiver partials, and adds Gm_k r^-3 d to a packed
+// accumulator of the two partners, which the warp rotates one lane down after the step.
+// After 16 steps lane t holds partners (t + 16, t); the halves of each partner are joined
+// across lanes t and t ^ 16.  Outputs: receiver partials px.. and minus the partner sums
+// in qx.. (for this lane's partner t).  P points at the lane's first entry.
+// GUARD: the pair rule pair by pair (RAD only); else, with RAD, mn keeps the smallest r^2.
 template <bool RAD, bool GUARD, int NK>
-__device__ __forceinline__ void sym_subtile(const float4 *A, const float4 *B, const MixedRecv (&q)[SR],
-                                            const float (&gm)[SR], int src, float (&px)[SR], float (&py)[SR],
-                                            float (&pz)[SR], float &qx, float &qy, float &qz, float (&mn)[SR]) {
+__device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Recv2 (&q)[SR], int src, float (&px)[SR],
+                                            float (&py)[SR], float (&pz)[SR], float &qx, float &qy, float &qz,
+                                            float (&mn)[SR]) {
+    f32x2 ax[NK], ay[NK], az[NK];
 #pragma unroll
     for (int k = 0; k < NK; k++) {
-        px[k] = py[k] = pz[k] = 0.f;
+        ax[k] = ay[k] = az[k] = 0ull;
         mn[k] = 3.0e38f;
     }
-    qx = qy = qz = 0.f;
-#pragma unroll 8
-    for (int s = 0; s < 32; s++) {
-        const float4 a = A[s];
-        const float4 b = B[s];
+    f32x2 bx = 0ull, by = 0ull, bz = 0ull;
+    const f32x2 c15 = f2_pack(-1.5f, -1.5f), c25 = f2_pack(2.5f, 2.5f);
+    const ulonglong2 *W0 = S.w[0] + lane, *W1 = S.w[1] + lane, *W2 = S.w[2] + lane, *W3 = S.w[3] + lane;
+#pragma unroll 4
+    for (int s = 0; s < 16; s++) {
+        const ulonglong2 h = W0[s], hz = W1[s], l = W2[s], lz = W3[s];
 #pragma unroll
         for (int k = 0; k < NK; k++) {
-            const float dx = (a.x - q[k].xh) + (b.x - q[k].xl);
-            const float dy = (a.y - q[k].yh) + (b.y - q[k].yl);
-            const float dz = (a.z - q[k].zh) + (b.z - q[k].zl);
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const float r3 = rinv3(r2);
-            float fi = a.w * r3, fj = gm[k] * r3;
-            if (RAD && GUARD) {
-                const float rs = q[k].R + b.w;
-                if (!(r2 > rs * rs)) fi = fj = 0.f;
-            }
-            if (RAD && !GUARD) mn[k] = fminf(mn[k], r2);
-            px[k] = fmaf(fi, dx, px[k]);
-            py[k] = fmaf(fi, dy, py[k]);
-            pz[k] = fmaf(fi, dz, pz[k]);
-            qx = fmaf(-fj, dx, qx);
-            qy = fmaf(-fj, dy, qy);
-            qz = fmaf(-fj, dz, qz);
+            const f32x2 dx = f2_add(f2_sub(h.x, q[k].xh), f2_sub(l.x, q[k].xl));
+            const f32x2 dy = f2_add(f2_sub(h.y, q[k].yh), f2_sub(l.y, q[k].yl));
+            const f32x2 dz = f2_add(f2_sub(hz.x, q[k].zh), f2_sub(lz.x, q[k].zl));
+            const f32x2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+            float r2a, r2b;
+            f2_unpack(r2, r2a, r2b);
+            const f32x2 y = f2_pack(rsqrt_approx(r2a), rsqrt_approx(r2b));
+            const f32x2 t = f2_mul(y, y);
+            const f32x2 r3 = f2_mul(f2_mul(t, y), f2_fma(c15, f2_mul(r2, t), c25));
+            f32x2 fi = f2_mul(hz.y, r3), fj = f2_mul(q[k].gm, r3);
+            if (RAD && GUARD) rule2<true>(r2, lz.y, q[k].R, 0, 0, -1, fi, fj);
+            if (RAD && !GUARD) mn[k] = fminf(mn[k], fminf(r2a, r2b));
+            ax[k] = f2_fma(fi, dx, ax[k]);
+            ay[k] = f2_fma(fi, dy, ay[k]);
+            az[k] = f2_fma(fi, dz, az[k]);
+            bx = f2_fma(fj, dx, bx);
+            by = f2_fma(fj, dy, by);
+            bz = f2_fma(fj, dz, bz);
         }
-        qx = __shfl_sync(FULL, qx, src);
-        qy = __shfl_sync(FULL, qy, src);
-        qz = __shfl_sync(FULL, qz, src);
+        bx = __shfl_sync(FULL, bx, src);
+        by = __shfl_sync(FULL, by, src);
+        bz = __shfl_sync(FULL, bz, src);
     }
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+        float e, o;
+        f2_unpack(ax[k], e, o);
+        px[k] = e + o;
+        f2_unpack(ay[k], e, o);
+        py[k] = e + o;
+        f2_unpack(az[k], e, o);
+        pz[k] = e + o;
+    }
+    float lo, hi;
+    f2_unpack(bx, lo, hi);
+    qx = -(hi + __shfl_xor_sync(FULL, lo, 16));
+    f2_unpack(by, lo, hi);
+    qy = -(hi + __shfl_xor_sync(FULL, lo, 16));
+    f2_unpack(bz, lo, hi);
+    qz = -(hi + __shfl_xor_sync(FULL, lo, 16));
 }
 
 // sym_subtile without the rule, then (RAD) recomputed with it when some receiver k < NK
 // may meet a partner within the radii.
 template <bool RAD, int NK>
-__device__ __forceinline__ void sym_subtile_ruled(const float4 *A, const float4 *B, const MixedRecv (&q)[SR],
-                                                  const float (&gm)[SR], const bool (&ok)[SR], int src,
-                                                  float (&px)[SR], float (&py)[SR], float (&pz)[SR], float &qx,
-                                                  float &qy, float &qz) {
+__device__ __forceinline__ void sym_subtile_ruled(const SubTile &S, int lane, const Recv2 (&q)[SR],
+                                                  const bool (&ok)[SR], int src, float (&px)[SR], float (&py)[SR],
+                                                  float (&pz)[SR], float &qx, float &qy, float &qz) {
     float mn[SR];
-    sym_subtile<RAD, false, NK>(A, B, q, gm, src, px, py, pz, qx, qy, qz, mn);
+    sym_subtile<RAD, false, NK>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
     if (RAD) {
-        const float rt = __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(B[0].w)));  // radii are >= 0
+        float Ra, Rb;
+        f2_unpack(S.w[3][lane].y, Ra, Rb);  // the lane's entry: partners lane and lane ^ 16
+        const float rt = __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(fmaxf(Ra, Rb))));  // radii >= 0
         bool need = false;
 #pragma unroll
         for (int k = 0; k < NK; k++) {
@@ -117,7 +209,7 @@ __device__ __forceinline__ void sym_subtile_ruled(const float4 *A, const float4 
             need = need || (ok[k] && mn[k] <= rs * rs);
         }
         if (__any_sync(FULL, need))  // rare: a pair may lie within the radii
-            sym_subtile<RAD, true, NK>(A, B, q, gm, src, px, py, pz, qx, qy, qz, mn);
+            sym_subtile<RAD, true, NK>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
     }
 }
 
@@ -127,27 +219,58 @@ __device__ __forceinline__ void ff_add3(FF &x, FF &y, FF &z, float a, float b, f
     ff_add(z, c);
 }
 
+// Receiver k of this lane (body 32 k + lane of the diagonal tile) against its own
+// sub-tile, one-sided with the pair rule applied pair by pair (the self pair, and with RAD
+// the radius rule): partners lane + s and lane + s + 16 at step s.
+template <bool RAD>
+__device__ __forceinline__ void own_subtile(const SubTile &S, int lane, const Recv2 &q, float &sx, float &sy,
+                                            float &sz) {
+    f32x2 ax = 0ull, ay = 0ull, az = 0ull;
+    const f32x2 c15 = f2_pack(-1.5f, -1.5f), c25 = f2_pack(2.5f, 2.5f);
+    const ulonglong2 *W0 = S.w[0] + lane, *W1 = S.w[1] + lane, *W2 = S.w[2] + lane, *W3 = S.w[3] + lane;
+#pragma unroll 4
+    for (int s = 0; s < 16; s++) {
+        const ulonglong2 h = W0[s], hz = W1[s], l = W2[s], lz = W3[s];
+        const f32x2 dx = f2_add(f2_sub(h.x, q.xh), f2_sub(l.x, q.xl));
+        const f32x2 dy = f2_add(f2_sub(h.y, q.yh), f2_sub(l.y, q.yl));
+        const f32x2 dz = f2_add(f2_sub(hz.x, q.zh), f2_sub(lz.x, q.zl));
+        const f32x2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+        float r2a, r2b;
+        f2_unpack(r2, r2a, r2b);
+        const f32x2 y = f2_pack(rsqrt_approx(r2a), rsqrt_approx(r2b));
+        const f32x2 t = f2_mul(y, y);
+        const f32x2 r3 = f2_mul(f2_mul(t, y), f2_fma(c15, f2_mul(r2, t), c25));
+        f32x2 fi = f2_mul(hz.y, r3), fj = 0ull;
+        rule2<RAD>(r2, lz.y, q.R, (lane + s) & 31, (lane + s + 16) & 31, lane, fi, fj);
+        ax = f2_fma(fi, dx, ax);
+        ay = f2_fma(fi, dy, ay);
+        az = f2_fma(fi, dz, az);
+    }
+    float e, o;
+    f2_unpack(ax, e, o);
+    sx = e + o;
+    f2_unpack(ay, e, o);
+    sy = e + o;
+    f2_unpack(az, e, o);
+    sz = e + o;
+}
+
 // Sub-tile U of a diagonal tile (I == J): receivers k < U against it with the rotation,
 // whose partner sums belong to receiver U of this lane, and receiver U against it
 // one-sided with the pair rule.
 template <bool RAD, int U>
-__device__ __forceinline__ void diag_subtile(const float4 *sA, const float4 *sB, const MixedRecv (&q)[SR],
-                                             const float (&gm)[SR], const bool (&ok)[SR], const int (&self)[SR],
-                                             int j0, int lane, FF (&ax)[SR], FF (&ay)[SR], FF (&az)[SR]) {
+__device__ __forceinline__ void diag_subtile(const SubTile (&sP)[SR], const Recv2 (&q)[SR], const bool (&ok)[SR],
+                                             int lane, FF (&ax)[SR], FF (&ay)[SR], FF (&az)[SR]) {
     float qx = 0.f, qy = 0.f, qz = 0.f;
-    if (U > 0) {
+    if constexpr (U > 0) {
         float px[SR], py[SR], pz[SR];
-        sym_subtile_ruled<RAD, U>(sA + U * 64 + lane, sB + U * 64 + lane, q, gm, ok, (lane + 1) & 31, px, py, pz, qx,
-                                  qy, qz);
+        sym_subtile_ruled<RAD, U>(sP[U], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
 #pragma unroll
         for (int k = 0; k < U; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
     }
-    const MixedRecv qu[1] = {q[U]};
-    const int su[1] = {self[U]};
-    const bool mu[1] = {true};
-    float sx[1], sy[1], sz[1], smn[1];
-    mixed_tile<false, RAD, false, true, 1>(j0 + U * 32, 32, su, 0, mu, qu, sA + U * 64, sB + U * 64, sx, sy, sz, smn);
-    ff_add3(ax[U], ay[U], az[U], sx[0], sy[0], sz[0]);
+    float sx, sy, sz;
+    own_subtile<RAD>(sP[U], lane, q[U], sx, sy, sz);
+    ff_add3(ax[U], ay[U], az[U], sx, sy, sz);
     if (U > 0) ff_add3(ax[U], ay[U], az[U], qx, qy, qz);
 }
 
@@ -163,8 +286,7 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
                                                       float *__restrict__ rpart, float *__restrict__ ppart,
                                                       unsigned *__restrict__ head,
                                                       const int32_t *__restrict__ sys_flag, int phase) {
-    __shared__ float4 sA[SR * 64];  // sub-tile u at [64u, 64u + 64): its 32 partners twice
-    __shared__ float4 sB[SR * 64];
+    __shared__ SubTile sP[SR];
     const int lane = threadIdx.x;
     const float4 pad_a = make_float4(PAD_POS, PAD_POS, PAD_POS, 0.f), zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (;;) {
@@ -176,19 +298,16 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
         const int s = w.x, I = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
         if (sys_flag && sys_flag[s] != phase) continue;  // warp-uniform
         const int p0 = poff[s], n = npl[s], nt = (n + TS - 1) / TS;
-        MixedRecv q[SR];
-        float gm[SR];
+        Recv2 q[SR];
         bool ok[SR];
-        int self[SR];
 #pragma unroll
         for (int k = 0; k < SR; k++) {
             const int i = I * TS + k * 32 + lane;
             ok[k] = i < n;
-            self[k] = i;
             const float4 a = ok[k] ? pA[p0 + i] : pad_a;
             const float4 b = ok[k] ? pB[p0 + i] : zero;
-            q[k] = MixedRecv{a.x, a.y, a.z, b.x, b.y, b.z, b.w};
-            gm[k] = a.w;
+            q[k] = Recv2{f2_pack(a.x, a.x), f2_pack(a.y, a.y), f2_pack(a.z, a.z), f2_pack(b.x, b.x),
+                         f2_pack(b.y, b.y), f2_pack(b.z, b.z), f2_pack(a.w, a.w), b.w};
         }
         FF ax[SR], ay[SR], az[SR];
 #pragma unroll
@@ -201,25 +320,21 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
                 const int j = J * TS + u * 32 + lane;
                 const float4 a = j < n ? pA[p0 + j] : pad_a;
                 const float4 b = j < n ? pB[p0 + j] : zero;
-                sA[u * 64 + lane] = a;
-                sA[u * 64 + 32 + lane] = a;
-                sB[u * 64 + lane] = b;
-                sB[u * 64 + 32 + lane] = b;
+                stage_subtile(sP[u], a, b, lane);
             }
             __syncwarp();
             if (I == J) {
                 static_assert(SR == 4, "diagonal sub-tiles");
-                diag_subtile<RAD, 0>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
-                diag_subtile<RAD, 1>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
-                diag_subtile<RAD, 2>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
-                diag_subtile<RAD, 3>(sA, sB, q, gm, ok, self, J * TS, lane, ax, ay, az);
+                diag_subtile<RAD, 0>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 1>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 2>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 3>(sP, q, ok, lane, ax, ay, az);
                 continue;
             }
             float *o1 = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, J, nt)) * 3 * TS;
             for (int u = 0; u < SR; u++) {
                 float px[SR], py[SR], pz[SR], qx, qy, qz;
-                sym_subtile_ruled<RAD, SR>(sA + u * 64 + lane, sB + u * 64 + lane, q, gm, ok, (lane + 1) & 31, px, py,
-                                           pz, qx, qy, qz);
+                sym_subtile_ruled<RAD, SR>(sP[u], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
 #pragma unroll
                 for (int k = 0; k < SR; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
                 o1[0 * TS + u * 32 + lane] = qx;

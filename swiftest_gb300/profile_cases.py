@@ -4,7 +4,8 @@
 
 cases: kick_tp_mixed, kick_pl_mixed, kick_tp_fp64, kick_pl_fp64, drift, encounter_pltp,
 encounter_plpl, symba_mixed, symba_fp64 (inputs: the seeded C1 disk, AU, Msun, yr), and
-ens_mixed, ens_fp64 (steps of the C4 batched SyMBA ensemble, first --nsys systems).
+ens_mixed, ens_fp64 (steps of a batched ensemble, first --nsys systems: --ensemble C4, the
+SyMBA disks, or C3 / C3W, the HELIO / WHM systems with 5 tp per pl).
 Prints the average wall time per call (host buffers, so it includes the copies).
 """
 from __future__ import annotations
@@ -26,6 +27,7 @@ def main(argv=None):
     p.add_argument("--ntp", type=int, default=10000)
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--nsys", type=int, default=None)
+    p.add_argument("--ensemble", default="C4", choices=["C4", "C3", "C3W"])
     a = p.parse_args(argv)
     from swiftest_gb300 import SWG_FP64, SWG_MIXED
     from swiftest_gb300 import build as B
@@ -49,7 +51,10 @@ def main(argv=None):
     }
     if a.case.startswith("ens"):
         from swiftest_gb300.api import Ensemble
-        E = IC.make_ensemble("C4", nsys=a.nsys)
+        if a.ensemble == "C3W":
+            E = IC.make_ensemble("C3", nsys=a.nsys, integrator="WHM")
+        else:
+            E = IC.make_ensemble(a.ensemble, nsys=a.nsys)
         ens = Ensemble(ctx, E, precision="MIXED" if a.case.endswith("mixed") else "FP64")
         run = lambda: ens.step(1)  # noqa: E731
     elif a.case.startswith("symba"):
