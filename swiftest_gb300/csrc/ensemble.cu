@@ -139,7 +139,8 @@ struct swg_ensemble {
     StepProfile prof;
     // side stream for the closing kick of systems without encounters (overlaps the recursion)
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_drift = nullptr;
+    bool drift_pending = false;   // the level-0 drift runs on the side stream (ev_drift)
     unsigned *head2 = nullptr;
     int64_t nchecks = 0;  // level-0 checks so far (the radial order is refreshed every RESORT_EVERY)
     // CUDA graph of one HELIO step (+ discard scan): captured after one eager step, replayed
@@ -1265,6 +1266,12 @@ int recursion_launch(swg_ensemble *e, double dt) {
 // systems whose recursion paused on the host and resume those systems, until none pauses.
 int recursion_finish(swg_ensemble *e) {
     swg_ctx *c = e->c;
+    if (e->lclose && e->drift_pending) {
+        // collision resolution copies whole system slices: the level-0 drift on the side
+        // stream must be done first
+        SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_drift, 0), "drift"));
+        e->drift_pending = false;
+    }
     while (e->lclose) {
         SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->h_pend.data(), e->rec_pend, sizeof(int32_t) * e->nsys,
                                                cudaMemcpyDeviceToHost, c->stream),
@@ -1344,24 +1351,33 @@ int ens_step(swg_ensemble *e, double dt) {
     SWG_TRY(kick_vb_pl(e, dth, 1, have_acc));
     SWG_TRY(tp_misc(e, CB_PTBEG, dth, 2, 4));
     SWG_TRY(kick_vb_tp(e, dth, 1));
-    SWG_TRY(drift_bodies(e, dt));
     const bool rec = symba && e->pp_n + e->pt_n > 0;
     if (rec && !e->prof.on && e->NPL > 0) {
-        // The closing accelerations of systems without encounters do not depend on the
-        // recursion: compute them on the side stream while the recursion of the other
-        // systems runs (recursion launched first, so its blocks are resident), then those
-        // of the recursing systems.  Each system's arithmetic is unchanged.
+        // The level-0 drift moves only the bodies outside the lists (levelg == -1) and the
+        // recursion only the bodies in them, and the closing accelerations of systems
+        // without encounters do not depend on the recursion: the side stream drifts and
+        // then computes those accelerations while the recursion runs (launched first, so
+        // its blocks are resident); the recursing systems' accelerations follow both.
+        // Each system's arithmetic is unchanged.
         swg_ctx *c = e->c;
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
         SWG_TRY(recursion_launch(e, dt));
+        SWG_TRY(on_stream(c, e->side, [&] { return drift_bodies(e, dt); }));
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_drift, e->side), "drift"));
+        e->drift_pending = true;
         SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
         SWG_TRY(recursion_finish(e));
+        if (e->drift_pending) {
+            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_drift, 0), "drift"));
+            e->drift_pending = false;
+        }
         SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
         SWG_TRY(kick_vb_pl(e, dth, 0, true));
     } else {
+        SWG_TRY(drift_bodies(e, dt));
         if (rec) {
             ProfScope ps(e->prof, c->stream, PROF_RECUR);
             SWG_TRY(recursion_launch(e, dt));
@@ -1558,6 +1574,7 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = cuda_status(c, cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking), "side stream");
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming), "event");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_drift, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_resume, (size_t)REC_STATE * S);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_pend, S);
@@ -1620,6 +1637,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
+    if (e->ev_drift) cudaEventDestroy(e->ev_drift);
     if (e->side) cudaStreamDestroy(e->side);
     e->prof.release();
     delete e;
