@@ -75,6 +75,10 @@ struct swg_ensemble {
     // float copies: split partners of the mixed kick (A|B), prefilter copies (A|B|V) of the
     // tp and the pl, both in radius order
     float4 *kA = nullptr, *kB = nullptr, *eT = nullptr, *eS = nullptr;
+    // second split of the HELIO step's closing kick (kA2/kB2, used when kend is set), so the
+    // tp kick at the step's start can still read kA/kB on the side stream
+    float4 *kA2 = nullptr, *kB2 = nullptr;
+    bool kend = false;
     // radius-sorted pl-pl check: order, bound tiles (system, first sorted position), the
     // systems' first tiles, bounds, receiver items
     int32_t *perm = nullptr, *tbase = nullptr;
@@ -720,12 +724,12 @@ int size_bucket(const swg_ensemble *e, int k) {
 // partners must be split into kA/kB.
 int mixed_kick(swg_ensemble *e, int k, int variant, const int4 *items, int nitems, double *acc, bool rad,
                unsigned *head, const int32_t *flag, int phase, int acc_is_zero = 1) {
+    const float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
     if (k == 0)
         return kick_mixed_batched(e->c, variant, false, rad, nitems, items, e->poff, e->poff, e->npl, e->rh,
-                                  rad ? e->radius : nullptr, e->kA, e->kB, nullptr, acc, acc_is_zero, head, flag,
-                                  phase);
+                                  rad ? e->radius : nullptr, pa, pb, nullptr, acc, acc_is_zero, head, flag, phase);
     return kick_mixed_batched(e->c, variant, true, false, nitems, items, e->toff, e->poff, e->npl, e->trh, nullptr,
-                              e->kA, e->kB, e->tlmask, acc, acc_is_zero, head);
+                              pa, pb, e->tlmask, acc, acc_is_zero, head);
 }
 
 // Scratch of the timing runs, released on every exit path.
@@ -833,10 +837,11 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
     const bool rad = e->integrator == SWG_SYMBA || e->lclose;
     const double *R = rad ? e->radius : nullptr;
     if (e->precision == SWG_MIXED) {
-        SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, e->kA, e->kB, flag ? e->psys : nullptr, flag, phase));
+        float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
+        SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, pa, pb, flag ? e->psys : nullptr, flag, phase));
         SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
         if (e->kv[0] == KICK_SYMMETRIC) {
-            SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
+            SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
                                            e->sym_part, e->sym_ppart, head, flag, phase));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
                                          e->sym_ppart, e->ah, acc_is_zero, flag, phase);
@@ -885,15 +890,17 @@ int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false) {
 // helio_kick_vb_tp (helio_kick.f90:135-169) with symba_kick_getacch_tp (symba_kick.f90:79-123).
 // The mixed path reuses the partner split of the pl kick just before it: the pl
 // positions it was taken from are exactly rbeg / rend.
-int kick_vb_tp(swg_ensemble *e, double dt, int lbeg) {
+// head: the work-queue counter (a stream of its own when the tp kick runs beside the pl work).
+int kick_vb_tp(swg_ensemble *e, double dt, int lbeg, unsigned *head = nullptr) {
     swg_ctx *c = e->c;
     if (e->NTP == 0) return SWG_OK;
     const double *rp = lbeg ? e->rbeg : e->rend;
+    if (!head) head = e->head;
     {
         ProfScope ps(e->prof, c->stream, PROF_KICK_TP);
         if (e->precision == SWG_MIXED) {
-            SWG_TRY(ensure_kick_plan(e, 1, false, e->head, nullptr, 0));
-            SWG_TRY(mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, e->head, nullptr, 0));
+            SWG_TRY(ensure_kick_plan(e, 1, false, head, nullptr, 0));
+            SWG_TRY(mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, head, nullptr, 0));
         } else {
             SWG_TRY(kick_tp_fp64_batched(c, e->n_ftp, e->it_ftp, e->toff, e->ntp, e->poff, e->npl, e->trh, rp,
                                          e->Gmass, e->tlmask, e->tah, 1));
@@ -953,14 +960,14 @@ int vb2vh_pl(swg_ensemble *e) {
 }
 // Danby drift of every body at level -1 (SyMBA: bodies outside encounters) with its
 // own system's GMcb; HELIO drifts every active body.
-int drift_bodies(swg_ensemble *e, double dt) {
+int drift_bodies(swg_ensemble *e, double dt, bool pl = true, bool tp = true) {
     swg_ctx *c = e->c;
     ProfScope ps(e->prof, c->stream, PROF_DRIFT);
     const bool symba = e->integrator == SWG_SYMBA;
-    if (e->NPL > 0)
+    if (pl && e->NPL > 0)
         SWG_TRY(drift_masked(c, 0.0, e->rh, e->vb, (int32_t)e->NPL, symba ? e->levelg : nullptr, -1, dt, e->status,
                              nullptr, e->GMcb, e->psys, !exact(e)));
-    if (e->NTP > 0)
+    if (tp && e->NTP > 0)
         SWG_TRY(drift_masked(c, 0.0, e->trh, e->tvb, (int32_t)e->NTP, symba ? e->tlevelg : nullptr, -1, dt,
                              e->tstatus, nullptr, e->GMcb, e->tsys, !exact(e)));
     return SWG_OK;
@@ -1295,6 +1302,43 @@ int recursion_finish(swg_ensemble *e) {
 
 
 
+// The rest of a HELIO step (helio_step_system, helio_step.f90:14-119) after the opening
+// pl sums, with the test particles on the side stream: their half-steps need the pl only
+// through the start positions (rbeg and the first partner split) and, for the closing kick,
+// the end positions (rend, the second split kA2/kB2) and the closing central-body drift
+// slot, so the tp kick, drift and kick (FP32, FP64, FP32) run beside the pl drift, closing
+// kick and sums.  Each body's arithmetic and order are those of the sequential step.
+int helio_step_split(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    const double dth = 0.5 * dt;
+    unsigned *head_tp = e->head + 1;
+    SWG_TRY(kick_vb_pl(e, dth, 1));
+    SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
+    SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
+    SWG_TRY(on_stream(c, e->side, [&] {
+        SWG_TRY(tp_misc(e, CB_PTBEG, dth, 2, 4));
+        SWG_TRY(kick_vb_tp(e, dth, 1, head_tp));
+        return drift_bodies(e, dt, false, true);
+    }));
+    SWG_TRY(drift_bodies(e, dt, true, false));
+    e->kend = true;
+    int rc = kick_vb_pl(e, dth, 0);
+    if (rc == SWG_OK) rc = lindrift_pl(e, dth, CB_PTEND);
+    if (rc == SWG_OK) rc = vb2vh_pl(e);
+    if (rc == SWG_OK) rc = cuda_status(c, cudaEventRecord(e->ev_drift, c->stream), "pl done");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_drift, 0), "pl done");
+    if (rc == SWG_OK) rc = on_stream(c, e->side, [&] {
+        SWG_TRY(kick_vb_tp(e, dth, 0, head_tp));
+        return tp_misc(e, CB_PTEND, dth, 3, -1);
+    });
+    e->kend = false;
+    SWG_TRY(rc);
+    SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
+    SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+    k_ens_finish<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, nullptr, e->lfirst, e->enc_steps);
+    return L(c, "ens_finish");
+}
+
 // One step of every system: symba_step_system (symba_step.f90:14-52) or
 // helio_step_system (helio_step.f90:14-119).  A SyMBA system without encounters takes
 // the HELIO step; the kernel sequence below is the same for both cases (empty lists
@@ -1348,6 +1392,7 @@ int ens_step(swg_ensemble *e, double dt) {
         SWG_TRY(vh2vb_pl(e, true));
         SWG_TRY(lindrift_pl(e, dth, CB_PTBEG));
     }
+    if (!symba && !e->prof.on && e->NPL > 0 && e->NTP > 0) return helio_step_split(e, dt);
     SWG_TRY(kick_vb_pl(e, dth, 1, have_acc));
     SWG_TRY(tp_misc(e, CB_PTBEG, dth, 2, 4));
     SWG_TRY(kick_vb_tp(e, dth, 1));
@@ -1563,8 +1608,12 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     int32_t **ti[] = {&e->tsys, &e->tstatus, &e->tlmask, &e->tlevelg, &e->tlevelm, &e->tnplenc, &e->mark_tp};
     for (auto p : ti)
         if (rc == SWG_OK) rc = dalloc(c, p, m);
-    if (rc == SWG_OK) rc = dalloc(c, &e->kA, 2 * n);
-    if (rc == SWG_OK) e->kB = e->kA + n;
+    if (rc == SWG_OK) rc = dalloc(c, &e->kA, 4 * n);
+    if (rc == SWG_OK) {
+        e->kB = e->kA + n;
+        e->kA2 = e->kA + 2 * n;
+        e->kB2 = e->kA + 3 * n;
+    }
     if (rc == SWG_OK) rc = dalloc(c, &e->tperm, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->eT, 3 * m);
     if (rc == SWG_OK) rc = dalloc(c, &e->eS, 3 * n);
