@@ -143,6 +143,12 @@ struct swg_ensemble {
     StepProfile prof;
     // side stream for the closing kick of systems without encounters (overlaps the recursion)
     cudaStream_t side = nullptr;
+    // HELIO mixed step: the test particles in two groups of systems (tgroup 0/1; group 1's
+    // bodies from tsplit on), each on its own stream (side, side2)
+    cudaStream_t side2 = nullptr;
+    cudaEvent_t ev_g0 = nullptr, ev_join2 = nullptr;
+    int32_t *tgroup = nullptr;
+    int64_t tsplit = 0;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_drift = nullptr;
     bool drift_pending = false;   // the level-0 drift runs on the side stream (ev_drift)
     unsigned *head2 = nullptr;
@@ -729,7 +735,7 @@ int mixed_kick(swg_ensemble *e, int k, int variant, const int4 *items, int nitem
         return kick_mixed_batched(e->c, variant, false, rad, nitems, items, e->poff, e->poff, e->npl, e->rh,
                                   rad ? e->radius : nullptr, pa, pb, nullptr, acc, acc_is_zero, head, flag, phase);
     return kick_mixed_batched(e->c, variant, true, false, nitems, items, e->toff, e->poff, e->npl, e->trh, nullptr,
-                              pa, pb, e->tlmask, acc, acc_is_zero, head);
+                              pa, pb, e->tlmask, acc, acc_is_zero, head, flag, phase);
 }
 
 // Scratch of the timing runs, released on every exit path.
@@ -1308,10 +1314,86 @@ int recursion_finish(swg_ensemble *e) {
 // the end positions (rend, the second split kA2/kB2) and the closing central-body drift
 // slot, so the tp kick, drift and kick (FP32, FP64, FP32) run beside the pl drift, closing
 // kick and sums.  Each body's arithmetic and order are those of the sequential step.
+// Test particles [t0, t1) of one group: the half-step pieces of helio_step_tp on the
+// context's current stream (tp_misc, the mixed pl-tp kick of the group's systems with its
+// velocity update, and the Danby drift).
+int tp_misc_range(swg_ensemble *e, int64_t t0, int64_t t1, int slot, double dt, int mode, int mode_first) {
+    if (t1 <= t0) return SWG_OK;
+    k_ens_tp_misc<<<grid_for(t1 - t0, 256), 256, 0, e->c->stream>>>(t1 - t0, e->tsys + t0, e->tlmask + t0,
+                                                                     e->trh + 3 * t0, e->tvh + 3 * t0, e->tvb + 3 * t0,
+                                                                     e->dcb, slot, dt, mode, mode_first, e->lfirst);
+    return L(e->c, "ens_tp_misc");
+}
+int kick_tp_group(swg_ensemble *e, double dt, int group, int64_t t0, int64_t t1, unsigned *head) {
+    swg_ctx *c = e->c;
+    SWG_TRY(ensure_kick_plan(e, 1, false, head, nullptr, 0));
+    SWG_TRY(mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, head, e->tgroup, group));
+    if (t1 <= t0) return SWG_OK;
+    k_kick_update<<<grid_for(t1 - t0, 128), 128, 0, c->stream>>>((int)(t1 - t0), e->tvb + 3 * t0, e->tah + 3 * t0,
+                                                                  e->tlmask + t0, dt, nullptr, nullptr);
+    return L(c, "kick_update_tp");
+}
+int drift_tp_range(swg_ensemble *e, int64_t t0, int64_t t1, double dt) {
+    if (t1 <= t0) return SWG_OK;
+    return drift_masked(e->c, 0.0, e->trh + 3 * t0, e->tvb + 3 * t0, (int32_t)(t1 - t0), nullptr, -1, dt,
+                        e->tstatus + t0, nullptr, e->GMcb, e->tsys + t0, !exact(e));
+}
+
+// Mixed path of helio_step_split with the test particles in two groups of systems: group
+// 1's opening kick runs while group 0 drifts, and group 1 drifts while group 0 takes its
+// closing kick, so the FP64 drift overlaps the FP32 kick.
+int helio_step_groups(swg_ensemble *e, double dt) {
+    swg_ctx *c = e->c;
+    const double dth = 0.5 * dt;
+    const int64_t T = e->tsplit, M = e->NTP;
+    unsigned *h0 = e->head + 1, *h1 = e->head + 2;
+    SWG_TRY(kick_vb_pl(e, dth, 1));
+    SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
+    SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
+    SWG_TRY(on_stream(c, e->side, [&] {
+        SWG_TRY(tp_misc_range(e, 0, T, CB_PTBEG, dth, 2, 4));
+        SWG_TRY(kick_tp_group(e, dth, 0, 0, T, h0));
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_g0, c->stream), "group 0"));
+        return drift_tp_range(e, 0, T, dt);
+    }));
+    SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side2, e->ev_g0, 0), "group 0"));
+    SWG_TRY(on_stream(c, e->side2, [&] {
+        SWG_TRY(tp_misc_range(e, T, M, CB_PTBEG, dth, 2, 4));
+        SWG_TRY(kick_tp_group(e, dth, 1, T, M, h1));
+        return drift_tp_range(e, T, M, dt);
+    }));
+    SWG_TRY(drift_bodies(e, dt, true, false));
+    e->kend = true;
+    int rc = kick_vb_pl(e, dth, 0);
+    if (rc == SWG_OK) rc = lindrift_pl(e, dth, CB_PTEND);
+    if (rc == SWG_OK) rc = vb2vh_pl(e);
+    if (rc == SWG_OK) rc = cuda_status(c, cudaEventRecord(e->ev_drift, c->stream), "pl done");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_drift, 0), "pl done");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaStreamWaitEvent(e->side2, e->ev_drift, 0), "pl done");
+    if (rc == SWG_OK) rc = on_stream(c, e->side, [&] {
+        SWG_TRY(kick_tp_group(e, dth, 0, 0, T, h0));
+        SWG_TRY(tp_misc_range(e, 0, T, CB_PTEND, dth, 3, -1));
+        return cuda_status(c, cudaEventRecord(e->ev_join, c->stream), "join");
+    });
+    if (rc == SWG_OK) rc = on_stream(c, e->side2, [&] {
+        SWG_TRY(kick_tp_group(e, dth, 1, T, M, h1));
+        SWG_TRY(tp_misc_range(e, T, M, CB_PTEND, dth, 3, -1));
+        return cuda_status(c, cudaEventRecord(e->ev_join2, c->stream), "join");
+    });
+    e->kend = false;
+    SWG_TRY(rc);
+    SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+    SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join2, 0), "join"));
+    k_ens_finish<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, nullptr, e->lfirst, e->enc_steps);
+    return L(c, "ens_finish");
+}
+
 int helio_step_split(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     const double dth = 0.5 * dt;
     unsigned *head_tp = e->head + 1;
+    if (e->precision == SWG_MIXED && e->tgroup && e->tsplit > 0 && e->tsplit < e->NTP)
+        return helio_step_groups(e, dt);
     SWG_TRY(kick_vb_pl(e, dth, 1));
     SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
     SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
@@ -1470,9 +1552,10 @@ int whm_kick_vh_pl(swg_ensemble *e, double dt, int lbeg) {
 }
 // whm_kick_vh_tp (whm_kick.f90:265-318) with whm_kick_getacch_tp (:70-122): tah = ah0 of the
 // system at rp, plus the pl-tp pair kick
-int whm_accel_tp(swg_ensemble *e, int lbeg) {
+int whm_accel_tp(swg_ensemble *e, int lbeg, unsigned *head = nullptr) {
     swg_ctx *c = e->c;
     const double *rp = lbeg ? e->rbeg : e->rend;
+    if (!head) head = e->head;
     k_ens_whm_ah0<<<e->nsys, 256, 0, c->stream>>>(e->poff, e->npl, e->Gmass, rp, e->whm_ah0, exact(e));
     SWG_TRY(L(c, "ens_whm_ah0"));
     k_ens_whm_tp_ah0<<<grid_for(e->NTP, 256), 256, 0, c->stream>>>(e->NTP, e->tsys, e->tlmask, e->whm_ah0, e->tah);
@@ -1480,16 +1563,16 @@ int whm_accel_tp(swg_ensemble *e, int lbeg) {
     ProfScope ps(e->prof, c->stream, PROF_KICK_TP);
     if (e->precision == SWG_MIXED) {
         // the partner split of the pl kick just before holds rp (rbeg or rend)
-        SWG_TRY(ensure_kick_plan(e, 1, false, e->head, nullptr, 0));
-        return mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, e->head, nullptr, 0, 0);
+        SWG_TRY(ensure_kick_plan(e, 1, false, head, nullptr, 0));
+        return mixed_kick(e, 1, e->kv[1], e->kit[1], e->n_kit[1], e->tah, false, head, nullptr, 0, 0);
     }
     return kick_tp_fp64_batched(c, e->n_ftp, e->it_ftp, e->toff, e->ntp, e->poff, e->npl, e->trh, rp, e->Gmass,
                                 e->tlmask, e->tah, 0);
 }
-int whm_kick_vh_tp(swg_ensemble *e, double dt, int lbeg, bool first) {
+int whm_kick_vh_tp(swg_ensemble *e, double dt, int lbeg, bool first, unsigned *head = nullptr) {
     swg_ctx *c = e->c;
-    if (first) SWG_TRY(whm_accel_tp(e, 1));
-    if (!lbeg) SWG_TRY(whm_accel_tp(e, 0));
+    if (first) SWG_TRY(whm_accel_tp(e, 1, head));
+    if (!lbeg) SWG_TRY(whm_accel_tp(e, 0, head));
     k_kick_update<<<grid_for(e->NTP, 128), 128, 0, c->stream>>>((int)e->NTP, e->tvh, e->tah, e->tlmask, dt, nullptr,
                                                                  nullptr);
     return L(c, "kick_update_whm_tp");
@@ -1498,6 +1581,21 @@ int whm_ens_step(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     const double dth = 0.5 * dt;
     const bool first_tp = e->whm_first != 0;
+    // After the first step the test particles' opening kick reuses the accelerations of the
+    // previous closing kick and their drift needs nothing of the pl: both run on the side
+    // stream beside the pl half-steps; the closing accelerations (at the pl end positions
+    // and their partner split) wait for the pl.  Each body's arithmetic is unchanged.
+    const bool split = !first_tp && !e->prof.on && e->NPL > 0 && e->NTP > 0;
+    unsigned *head_tp = e->head + 1;
+    if (split) {
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
+        SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
+        SWG_TRY(on_stream(c, e->side, [&] {
+            SWG_TRY(whm_kick_vh_tp(e, dth, 1, false, head_tp));
+            return drift_masked(c, 0.0, e->trh, e->tvh, (int32_t)e->NTP, nullptr, -1, dt, e->tstatus, nullptr,
+                                e->GMcb, e->tsys, !exact(e));
+        }));
+    }
     if (e->NPL > 0) {
         SWG_TRY(whm_kick_vh_pl(e, dth, 1));
         e->whm_first = 0;
@@ -1511,6 +1609,13 @@ int whm_ens_step(swg_ensemble *e, double dt) {
         SWG_TRY(L(c, "ens_whm_drift_status"));
         SWG_TRY(whm_coord(e, WHM_J2H));
         SWG_TRY(whm_kick_vh_pl(e, dth, 0));
+    }
+    if (split) {
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_drift, c->stream), "pl done"));
+        SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_drift, 0), "pl done"));
+        SWG_TRY(on_stream(c, e->side, [&] { return whm_kick_vh_tp(e, dth, 0, false, head_tp); }));
+        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
+        return cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join");
     }
     if (e->NTP > 0) {
         SWG_TRY(whm_kick_vh_tp(e, dth, 1, first_tp));
@@ -1630,6 +1735,28 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->tflag, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->ndiscard, 1);
     e->h_pend.assign(S, 0);
+    if (rc == SWG_OK && integrator == SWG_HELIO && m > 0 && S > 1) {
+        // two groups of systems with about equal pl-tp kick work (N_tp N_pl), split at a system
+        double total = 0.0, cum = 0.0;
+        for (int s = 0; s < S; s++) total += (double)e->h_ntp[s] * e->h_npl[s];
+        int split = S;
+        for (int s = 0; s < S; s++) {
+            cum += (double)e->h_ntp[s] * e->h_npl[s];
+            if (cum >= 0.5 * total) {
+                split = s + 1;
+                break;
+            }
+        }
+        std::vector<int32_t> g(S);
+        for (int s = 0; s < S; s++) g[s] = s >= split ? 1 : 0;
+        e->tsplit = split < S ? e->h_toff[split] : m;
+        rc = dalloc(c, &e->tgroup, S);
+        if (rc == SWG_OK) rc = upload(c, e->tgroup, g);
+        if (rc == SWG_OK)
+            rc = cuda_status(c, cudaStreamCreateWithFlags(&e->side2, cudaStreamNonBlocking), "side stream");
+        if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_g0, cudaEventDisableTiming), "event");
+        if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_join2, cudaEventDisableTiming), "event");
+    }
     if (integrator == SWG_SYMBA && rc == SWG_OK) rc = dalloc(c, &e->snap, 6 * n + 6 * m);
     if (integrator == SWG_WHM) {
         double **wd[] = {&e->eta, &e->muj, &e->ir3h, &e->ir3j};
@@ -1688,6 +1815,10 @@ int swg_ensemble_destroy(swg_ensemble *e) {
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->ev_drift) cudaEventDestroy(e->ev_drift);
     if (e->side) cudaStreamDestroy(e->side);
+    if (e->side2) cudaStreamDestroy(e->side2);
+    if (e->ev_g0) cudaEventDestroy(e->ev_g0);
+    if (e->ev_join2) cudaEventDestroy(e->ev_join2);
+    if (e->tgroup) cudaFree(e->tgroup);
     e->prof.release();
     delete e;
     return SWG_OK;
