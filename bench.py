@@ -47,12 +47,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = "SyMBA body-steps/s on 1 GB300: mixed+batched vs FP64 GPU at matched |ΔE/E|"
 UNIT = "body-steps/s"
 FLOPS_PER_INTERACTION = 20.0  # GPU Gems 3 ch. 31 convention (sqrt and divide count 1)
+FP64_STEPS = 20  # timed steps of the FP64 comparison arm (at most --steps)
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="c4", choices=["c4", "c3", "c3w", "c1"])
@@ -247,16 +248,21 @@ class ClockSampler:
         self.index = index
         self.rows = []
         self.proc = None
+        self.i0 = self.i1 = 0
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()  # the timed region starts once sampling runs
+            while not self.rows and time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self.i0 = len(self.rows)
         return self
 
     def _read(self):
@@ -264,6 +270,7 @@ class ClockSampler:
             self.rows.append([x.strip() for x in line.split(",")])
 
     def __exit__(self, *a):
+        self.i1 = len(self.rows)
         if self.proc:
             self.proc.terminate()
             try:
@@ -276,7 +283,8 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        rows = self.rows[self.i0:self.i1] or self.rows[max(0, self.i0 - 1):self.i0 + 1]  # in the timed region
+        for r in rows:
             try:
                 sm.append(float(r[1]))
                 smax.append(float(r[2]))
@@ -286,7 +294,7 @@ class ClockSampler:
                 if len(r) > 5 + k and "Active" in r[5 + k] and "Not" not in r[5 + k]:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_in_timed_region": self.i1 - self.i0}
 
 
 class _Null:
@@ -392,7 +400,7 @@ def reference_arm(args, world, rank):
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     from oracle import oracle as O
     O.build()
-    budget = max(2.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
+    budget = max(0.5, min(6.0, 150.0 / max(1, args.steps + args.warmup)))  # whole run ~2.5 min
     for _ in range(args.warmup):
         wl.oracle_sample(budget / 4)
     bs_tot, el_tot, sample = 0, 0.0, ""
@@ -439,7 +447,8 @@ def main():
     nprof = max(3, min(10, args.steps))
     ms_mixed, launches, (prof, prof_ms), err_m, st_m = run_path(ctx, wl, "MIXED", args.steps, args.warmup, nprof,
                                                                 clocks=clocks)
-    ms_fp64, _, (prof64, _), err_f, st_f = run_path(ctx, wl, "FP64", args.steps, args.warmup, nprof)
+    steps64 = min(args.steps, FP64_STEPS)  # the FP64 comparison arm is ~100x slower per step
+    ms_fp64, _, (prof64, _), err_f, st_f = run_path(ctx, wl, "FP64", steps64, args.warmup, nprof)
     if td:
         import torch
         t = torch.tensor([ms_mixed, ms_fp64], dtype=torch.float64)
@@ -448,7 +457,7 @@ def main():
     e2e_ms, e2e_bytes = run_e2e(ctx, wl, "MIXED", args.steps)
     nb = wl.nbodies
     value = world * nb * args.steps / (ms_mixed * 1e-3)
-    fp64_value = world * nb * args.steps / (ms_fp64 * 1e-3)
+    fp64_value = world * nb * steps64 / (ms_fp64 * 1e-3)
 
     # roofline of the pair kick (mixed path), from the live CUDA-event profile on the library's stream
     peak32 = ctx.probe_peak_tflops("fp32")
@@ -476,7 +485,8 @@ def main():
         "ms_per_step": ms_mixed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (f32 pair kicks)", "data": "synthetic (seeded, numpy default_rng)",
         "config": wl.config("mixed"),
-        "fp64_path": {"value": fp64_value, "ms_per_step": ms_fp64 / args.steps, **err_summary(*err_f), "stats": st_f,
+        "fp64_path": {"value": fp64_value, "steps": steps64, "ms_per_step": ms_fp64 / steps64, **err_summary(*err_f),
+                      "stats": st_f,
                       "kernel_profile": {k: {"launches": v["launches"], "ms_total": round(v["ms"], 4)}
                                          for k, v in prof64.items()}},
         "mixed_path": {**err_summary(*err_m), "stats": st_m},
