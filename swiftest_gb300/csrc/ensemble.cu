@@ -520,9 +520,10 @@ __global__ void __launch_bounds__(RECT) k_ens_symba_recursion(EnsRecArgs e, int 
     a.pt = e.base.pt + t0;
     a.GMcb = e.GMcb[s];
     const int64_t q = k0 + t0;  // entries of the systems before s
-    a.terms = e.base.terms + 6 * q;
+    a.terms = e.base.terms + 12 * q;
     a.lenc = e.base.lenc + q;
     a.good = e.base.good + q;
+    a.good2 = e.base.good2 + q;
     a.bpl = e.base.bpl + 2 * k0 + t0;
     a.btp = e.base.btp + t0;
     a.adj_end = e.base.adj_end + 2 * (k0 + t0);  // bpl and btp slots
@@ -1217,7 +1218,7 @@ int resolve_collisions(swg_ensemble *e, int s) {
 int recursion_launch(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
     const int64_t n = e->pp_n + e->pt_n;
-    SWG_TRY(ensure(c, e->rec_scratch, sizeof(double) * (size_t)(6 * n + 8) + (size_t)(2 * n + 64) +
+    SWG_TRY(ensure(c, e->rec_scratch, sizeof(double) * (size_t)(12 * n + 8) + (size_t)(3 * n + 96) +
                                           sizeof(int32_t) * (size_t)(7 * n + 128)));
     EnsRecArgs x;
     RecArgs &a = x.base;
@@ -1247,7 +1248,7 @@ int recursion_launch(swg_ensemble *e, double dt) {
     a.rhscale = e->rhscale;
     a.dt = dt;
     a.terms = (double *)e->rec_scratch.ptr;
-    int32_t *ibuf = (int32_t *)(a.terms + 6 * n + 8);
+    int32_t *ibuf = (int32_t *)(a.terms + 12 * n + 8);
     a.bpl = ibuf;               // 2 * npp + npt per system
     a.btp = ibuf + 2 * n + 32;  // npt per system
     a.adj_end = ibuf + 3 * n + 64;  // one per listed body: 2 * (npp + npt) per system
@@ -1255,6 +1256,7 @@ int recursion_launch(swg_ensemble *e, double dt) {
     uint8_t *bbuf = (uint8_t *)(ibuf + 7 * n + 128);
     a.lenc = bbuf;
     a.good = bbuf + n + 32;
+    a.good2 = bbuf + 2 * n + 64;
     a.mark_pl = e->mark_pl;
     a.mark_tp = e->mark_tp;
     a.out = e->rec_out;

@@ -388,8 +388,8 @@ struct RecArgs {
     const double *Gm, *rhill, *radius;
     int32_t *status, *tstatus, *levelg, *levelm, *tlevelg, *tlevelm;
     double GMcb, rhscale, dt;
-    uint8_t *lenc, *good;           // list-sized byte scratch
-    double *terms;                  // 6 doubles per list entry
+    uint8_t *lenc, *good, *good2;   // list-sized byte scratch
+    double *terms;                  // 12 doubles per list entry
     int32_t *bpl, *btp;             // compact sets of bodies that appear in the lists
     int32_t *adj_end, *adj;         // per-body list entries (CSR: end offsets, entry indices)
     int32_t *mark_pl, *mark_tp;     // per-body marks, zero outside this kernel
@@ -476,29 +476,34 @@ static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int
     __syncthreads();
 }
 
-// symba_kick_list_plpl / _pltp (symba_kick.f90:126-340) for one sign, whole block.
-// The per-pair factors (sqrt, divide, the shell polynomial) depend only on positions,
-// so every pair is evaluated in parallel into `terms`.  The additions are then made
-// by one thread per body, which walks its own entries (the adjacency built at entry to the
-// recursion, in increasing list order) and adds their terms:
-// each body receives exactly the reference's additions in the reference's order,
-// while GB300's narrow FP64 pipe sees one instruction stream for all bodies instead
-// of one serial stream per pair.  A body that sits in several pairs gets its velocity
-// kicked once with its full acceleration, as in the reference (its later pairs add
-// zero).  good[k]: 0 not kicked, 1 kicked, 2 zeroed then skipped (r^2 < rim1).  The
-// reference's lmask refresh at entry is kept by the step loop instead (lmask ==
+// One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): the +1
+// kicks of both lists (symba_kick_list_plpl / _pltp, symba_kick.f90:126-340) and, below
+// level 0 (both), the -1 kicks, whole block.  The per-pair factors (sqrt, divide, the
+// shell polynomial) depend only on positions, so every pair is evaluated in parallel into
+// `terms`, for both signs in one pass: the two signs differ only in the shell radius
+// (irecl = irec for +1, irec - 1 for -1), so the displacement, r^2, r, r^-3 and (FP64
+// path) r^-1.5 are formed once with the reference's operations and shared.  The
+// additions are then made by one thread per body, which walks its own entries (the
+// adjacency built at entry to the recursion, in increasing list order) and keeps the two
+// signs' sums apart; the +1 velocity kick is applied before the -1 kick, so each body
+// receives exactly the reference's additions in the reference's order, while GB300's
+// narrow FP64 pipe sees one instruction stream for all bodies instead of one serial
+// stream per pair.  A body that sits in several pairs gets its velocity kicked once per
+// sign with its full acceleration, as in the reference (its later pairs add zero).
+// good[k] (+1) and good2[k] (-1): 0 not kicked, 1 kicked, 2 zeroed then skipped
+// (r^2 < rim1).  terms: 12 doubles per entry, the +1 pair terms then the -1 pair terms.
+// The reference's lmask refresh at entry is kept by the step loop instead (lmask ==
 // status /= INACTIVE wherever the recursion runs).
-static __device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, double dt, int irec, int sgn) {
+static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, double dt, int irec, bool both) {
     const int64_t npp = a.npp, npt = a.npt;
     if (npp + npt == 0) return;
     const int irm1 = irec - 1;
-    const int irecl = sgn < 0 ? irec - 1 : irec;
     const double rs2 = a.rhscale * a.rhscale;
-    const double rshell_pow = d_powi(RSHELL, 2 * irecl);
+    const double shell_p = d_powi(RSHELL, 2 * irec), shell_m = d_powi(RSHELL, 2 * (irec - 1));
     const int32_t *pi1 = a.pp, *pi2 = a.pp + a.ppcap, *pst = a.pp + 3 * a.ppcap;
     const int32_t *ti1 = a.pt, *ti2 = a.pt + a.ptcap, *tst = a.pt + 3 * a.ptcap;
     const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
-    // good flags and per-pair terms
+    // good flags and per-pair terms of both signs
     for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
         const bool isp = k < npp;
         const int64_t q = isp ? k : k - npp;
@@ -510,117 +515,101 @@ static __device__ void blk_kick_lists_sgn(const RecArgs &a, int nbpl, int nbtp, 
             g = do_pt && (tst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
         if (!g) {
             a.good[k] = 0;
+            a.good2[k] = 0;
             continue;
         }
-        double ri;
+        double base;
         if (isp) {
             const double rhs = a.rhill[i] + a.rhill[j];
-            ri = ((rhs * rhs) * rs2) * rshell_pow;
+            base = (rhs * rhs) * rs2;
         } else {
-            ri = ((a.rhill[i] * a.rhill[i]) * rs2) * rshell_pow;
+            base = (a.rhill[i] * a.rhill[i]) * rs2;
         }
-        const double rim1 = ri * (RSHELL * RSHELL);
+        const double ri_p = base * shell_p, ri_m = base * shell_m;
         const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
         double dx[3];
         for (int d = 0; d < 3; d++) dx[d] = rj[d] - a.rh[3 * i + d];
         const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
-        if (r2 < rim1) {
-            a.good[k] = 2;
-            continue;
-        }
-        a.good[k] = 1;
-        double fac;
-        if (r2 < ri) {
+        const bool kp = !(r2 < ri_p * (RSHELL * RSHELL));
+        const bool km = both && !(r2 < ri_m * (RSHELL * RSHELL));
+        a.good[k] = kp ? 1 : 2;
+        a.good2[k] = both ? (km ? 1 : 2) : 0;
+        if (!kp && !km) continue;
+        const double r = sqrt(r2);
+        const bool shp = kp && r2 < ri_p, shm = km && r2 < ri_m;
+        const double ir3 = 1.0 / (r2 * r);
+        // FP64 path: the correctly rounded r^-1.5 shared with the oracle; mixed path: 1/(r^2 r)
+        double p = ir3;
+        if (!a.fast && (shp || shm)) p = pow_m1p5(r2);
+        auto shell = [&](double ri) {
             const double ris = sqrt(ri);
-            const double r = sqrt(r2);
             const double rr = (ris - r) / (ris * (1.0 - RSHELL));
-            // FP64 path: the correctly rounded r^-1.5 shared with the oracle; mixed path: 1/(r^2 r)
-            const double p = a.fast ? 1.0 / (r2 * r) : pow_m1p5(r2);
-            fac = p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
-        } else {
-            const double ir3 = 1.0 / (r2 * sqrt(r2));
-            fac = ir3;
-        }
-        double *t = &a.terms[6 * k];
-        const double faci = fac * a.Gm[i];
-        if (isp) {
-            const double facj = fac * a.Gm[j];
-            for (int d = 0; d < 3; d++) {
-                t[d] = facj * dx[d];
-                t[3 + d] = faci * dx[d];
+            return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+        };
+        double *t = &a.terms[12 * k];
+        for (int sg = 0; sg < 2; sg++) {
+            if (!(sg == 0 ? kp : km)) continue;
+            const bool sh = sg == 0 ? shp : shm;
+            const double fac = sh ? shell(sg == 0 ? ri_p : ri_m) : ir3;
+            double *ts = t + 6 * sg;
+            const double faci = fac * a.Gm[i];
+            if (isp) {
+                const double facj = fac * a.Gm[j];
+                for (int d = 0; d < 3; d++) {
+                    ts[d] = facj * dx[d];
+                    ts[3 + d] = faci * dx[d];
+                }
+            } else {
+                for (int d = 0; d < 3; d++) ts[d] = faci * dx[d];
             }
-        } else {
-            for (int d = 0; d < 3; d++) t[d] = faci * dx[d];
         }
     }
     __syncthreads();
-    // ordered per-body accumulation and the velocity kick
-    const double sdt = (double)sgn * dt;
+    // ordered per-body accumulation and the velocity kicks, +1 then -1
     for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
         const bool isp = b < nbpl;
         const int body = isp ? a.bpl[b] : a.btp[b - nbpl];
-        bool zeroed = false, kicked = false;
-        double ax = 0.0, ay = 0.0, az = 0.0;
+        bool zeroed[2] = {false, false}, kicked[2] = {false, false};
+        double ax[2] = {0.0, 0.0}, ay[2] = {0.0, 0.0}, az[2] = {0.0, 0.0};
         const int e0 = b == 0 ? 0 : a.adj_end[b - 1], e1 = a.adj_end[b];
-        if (isp) {
-            for (int e = e0; e < e1; e++) {
-                const int k = a.adj[e];
-                const int i = pi1[k] - 1;
-                const uint8_t g = a.good[k];
+        for (int e = e0; e < e1; e++) {
+            const int k = a.adj[e];
+            // pl-pl entry: + its first three terms as index1, - the last three as index2;
+            // pl-tp entry (tp side): - its first three terms
+            const int off = (isp && pi1[k] - 1 != body) ? 3 : 0;
+            const bool sub = !isp || off == 3;
+            for (int sg = 0; sg < 2; sg++) {
+                const uint8_t g = sg == 0 ? a.good[k] : a.good2[k];
                 if (g == 0) continue;
-                zeroed = true;
+                zeroed[sg] = true;
                 if (g != 1) continue;
-                kicked = true;
-                const double *t = &a.terms[6 * k];
-                if (i == body) {
-                    ax = ax + t[0];
-                    ay = ay + t[1];
-                    az = az + t[2];
+                kicked[sg] = true;
+                const double *t = &a.terms[12 * k + 6 * sg + off];
+                if (sub) {
+                    ax[sg] = ax[sg] - t[0];
+                    ay[sg] = ay[sg] - t[1];
+                    az[sg] = az[sg] - t[2];
                 } else {
-                    ax = ax - t[3];
-                    ay = ay - t[4];
-                    az = az - t[5];
+                    ax[sg] = ax[sg] + t[0];
+                    ay[sg] = ay[sg] + t[1];
+                    az[sg] = az[sg] + t[2];
                 }
             }
-            if (zeroed) {
-                if (kicked) {
-                    a.vb[3 * body + 0] = a.vb[3 * body + 0] + sdt * ax;
-                    a.vb[3 * body + 1] = a.vb[3 * body + 1] + sdt * ay;
-                    a.vb[3 * body + 2] = a.vb[3 * body + 2] + sdt * az;
-                }
-                a.ah[3 * body + 0] = a.ah[3 * body + 1] = a.ah[3 * body + 2] = 0.0;
+        }
+        double *v = isp ? &a.vb[3 * body] : &a.tvb[3 * body];
+        double *acc = isp ? &a.ah[3 * body] : &a.tah[3 * body];
+        for (int sg = 0; sg < 2; sg++) {
+            if (!zeroed[sg]) continue;
+            const double sdt = sg == 0 ? dt : -dt;
+            if (kicked[sg]) {
+                v[0] = v[0] + sdt * ax[sg];
+                v[1] = v[1] + sdt * ay[sg];
+                v[2] = v[2] + sdt * az[sg];
             }
-        } else {
-            for (int e = e0; e < e1; e++) {
-                const int k = a.adj[e];
-                const uint8_t g = a.good[k];
-                if (g == 0) continue;
-                zeroed = true;
-                if (g != 1) continue;
-                kicked = true;
-                const double *t = &a.terms[6 * k];
-                ax = ax - t[0];
-                ay = ay - t[1];
-                az = az - t[2];
-            }
-            if (zeroed) {
-                if (kicked) {
-                    a.tvb[3 * body + 0] = a.tvb[3 * body + 0] + sdt * ax;
-                    a.tvb[3 * body + 1] = a.tvb[3 * body + 1] + sdt * ay;
-                    a.tvb[3 * body + 2] = a.tvb[3 * body + 2] + sdt * az;
-                }
-                a.tah[3 * body + 0] = a.tah[3 * body + 1] = a.tah[3 * body + 2] = 0.0;
-            }
+            acc[0] = acc[1] = acc[2] = 0.0;
         }
     }
     __syncthreads();
-}
-
-// One kick phase of symba_step_recur_system (symba_step.f90:214-219 / 232-237): the
-// +1 kicks of both lists, then (below level 0) the -1 kicks.
-static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, double dt, int irecp, bool both) {
-    blk_kick_lists_sgn(a, nbpl, nbtp, dt, irecp, 1);
-    if (both) blk_kick_lists_sgn(a, nbpl, nbtp, dt, irecp, -1);
 }
 
 // symba_drift_pl / _tp at level irec (symba_drift.f90:14-61) over the bodies that

@@ -645,7 +645,7 @@ int resolve_collisions(swg_system *s) {
 int symba_recursion(swg_system *s, double dt) {
     swg_ctx *c = s->c;
     const int64_t n = s->plpl_n + s->pltp_n;
-    SWG_TRY(ensure(c, s->rec_scratch, sizeof(double) * (size_t)(6 * n + 8) + (size_t)(2 * n + 64) +
+    SWG_TRY(ensure(c, s->rec_scratch, sizeof(double) * (size_t)(12 * n + 8) + (size_t)(3 * n + 96) +
                                           sizeof(int32_t) * (size_t)(7 * n + 128)));
     RecArgs a;
     a.npl = s->npl;
@@ -675,7 +675,7 @@ int symba_recursion(swg_system *s, double dt) {
     a.rhscale = s->rhscale;
     a.dt = dt;
     a.terms = (double *)s->rec_scratch.ptr;
-    int32_t *ibuf = (int32_t *)(a.terms + 6 * n + 8);
+    int32_t *ibuf = (int32_t *)(a.terms + 12 * n + 8);
     a.bpl = ibuf;                 // up to 2*npp + npt bodies
     a.btp = ibuf + 2 * n + 32;    // up to npt bodies
     a.adj_end = ibuf + 3 * n + 64;  // one per listed body (up to 2 * (npp + npt))
@@ -683,6 +683,7 @@ int symba_recursion(swg_system *s, double dt) {
     uint8_t *bbuf = (uint8_t *)(ibuf + 7 * n + 128);
     a.lenc = bbuf;
     a.good = bbuf + n + 32;
+    a.good2 = bbuf + 2 * n + 64;
     a.mark_pl = s->mark_pl;
     a.mark_tp = s->mark_tp;
     a.out = s->rec_out;
