@@ -149,7 +149,11 @@ struct swg_ensemble {
     cudaEvent_t ev_g0 = nullptr, ev_join2 = nullptr;
     int32_t *tgroup = nullptr;
     int64_t tsplit = 0;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_drift = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_drift = nullptr, ev_split = nullptr;
+    // SyMBA mixed closing kick: bodies in the encounter lists (enc_body) and per item of the
+    // symmetric kick 0 / 1 / 2 = system without encounters / no listed body / a listed body
+    uint8_t *enc_body = nullptr;
+    DevBuf sym_iflag;
     bool drift_pending = false;   // the level-0 drift runs on the side stream (ev_drift)
     unsigned *head2 = nullptr;
     int64_t nchecks = 0;  // level-0 checks so far (the radial order is refreshed every RESORT_EVERY)
@@ -501,6 +505,12 @@ __global__ void k_ens_lany(int nsys, const int32_t *__restrict__ seg_pp, const i
                            int32_t *lany) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < nsys) lany[s] = (seg_pp[2 * s + 1] + seg_pt[2 * s + 1]) > 0;
+}
+
+// enc[i] = 1 for a body in this step's encounter lists (levelg >= 0), else 0
+__global__ void k_mark_enc(int64_t n, const int32_t *__restrict__ levelg, uint8_t *__restrict__ enc) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) enc[i] = levelg[i] >= 0 ? 1 : 0;
 }
 
 // The SyMBA recursion of every system with encounters this step, one block each
@@ -1489,21 +1499,60 @@ int ens_step(swg_ensemble *e, double dt) {
         // its blocks are resident); the recursing systems' accelerations follow both.
         // Each system's arithmetic is unchanged.
         swg_ctx *c = e->c;
+        // Mixed symmetric kick: the closing kick's items that involve no listed body (the
+        // bodies the recursion moves) do not wait for the recursion either; flag them now,
+        // while the levels still say which bodies are listed.
+        const bool by_item = e->precision == SWG_MIXED && e->kv[0] == KICK_SYMMETRIC && e->n_sym > 0 && e->enc_body;
+        if (by_item) {
+            k_mark_enc<<<grid_for(e->NPL, 256), 256, 0, c->stream>>>(e->NPL, e->levelg, e->enc_body);
+            SWG_TRY(L(c, "mark_enc"));
+            SWG_TRY(ensure(c, e->sym_iflag, (size_t)e->n_sym));
+            SWG_TRY(kick_sym_item_flags(c, e->n_sym, e->it_sym, e->poff, e->npl, e->lany, e->enc_body,
+                                        (uint8_t *)e->sym_iflag.ptr));
+        }
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
         SWG_TRY(recursion_launch(e, dt));
         SWG_TRY(on_stream(c, e->side, [&] { return drift_bodies(e, dt); }));
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_drift, e->side), "drift"));
         e->drift_pending = true;
-        SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
+        const uint8_t *iflag = (const uint8_t *)e->sym_iflag.ptr;
+        if (by_item) {
+            // side: the unlisted bodies' partner split, then every item of the systems without
+            // encounters and the unlisted items of the others, and the former's sums
+            SWG_TRY(on_stream(c, e->side, [&] {
+                SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, e->radius, e->kA, e->kB, nullptr, nullptr, 0,
+                                          e->enc_body, 0));
+                SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_split, c->stream), "split"));
+                SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA,
+                                               e->kB, e->sym_part, e->sym_ppart, e->head2, nullptr, 0, iflag, 3u));
+                return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base,
+                                             e->sym_part, e->sym_ppart, e->ah, 1, e->lany, 0);
+            }));
+        } else {
+            SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
+        }
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), "join"));
         SWG_TRY(recursion_finish(e));
         if (e->drift_pending) {
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_drift, 0), "drift"));
             e->drift_pending = false;
         }
-        SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
-        SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+        if (by_item) {
+            // main: the listed bodies' split, the listed items, then every sum of the systems
+            // with encounters once the side's items are in
+            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_split, 0), "split"));
+            SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, e->radius, e->kA, e->kB, nullptr, nullptr, 0,
+                                      e->enc_body, 1));
+            SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
+                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u));
+            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+            SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
+                                          e->sym_ppart, e->ah, 1, e->lany, 1));
+        } else {
+            SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
+            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
+        }
         SWG_TRY(kick_vb_pl(e, dth, 0, true));
     } else {
         SWG_TRY(drift_bodies(e, dt));
@@ -1731,6 +1780,8 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming), "event");
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_drift, cudaEventDisableTiming), "event");
+    if (rc == SWG_OK) rc = cuda_status(c, cudaEventCreateWithFlags(&e->ev_split, cudaEventDisableTiming), "event");
+    if (rc == SWG_OK && integrator == SWG_SYMBA) rc = dalloc(c, &e->enc_body, n);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_out, 4);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_resume, (size_t)REC_STATE * S);
     if (rc == SWG_OK) rc = dalloc(c, &e->rec_pend, S);
@@ -1816,6 +1867,9 @@ int swg_ensemble_destroy(swg_ensemble *e) {
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->ev_drift) cudaEventDestroy(e->ev_drift);
+    if (e->ev_split) cudaEventDestroy(e->ev_split);
+    if (e->enc_body) cudaFree(e->enc_body);
+    if (e->sym_iflag.ptr) cudaFree(e->sym_iflag.ptr);
     if (e->side) cudaStreamDestroy(e->side);
     if (e->side2) cudaStreamDestroy(e->side2);
     if (e->ev_g0) cudaEventDestroy(e->ev_g0);

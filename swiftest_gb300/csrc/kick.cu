@@ -283,12 +283,15 @@ __global__ void __launch_bounds__(T) k_kick_mixed_batched(int nitems, const int4
 // FP64 pipe, which is narrow on GB300; doing it here instead of in every block
 // keeps the pair kernel on the FP32 pipe).
 // sysid/flag (optional): split only bodies whose system's flag equals phase.
+// enc/enc_want (optional): split only bodies with enc[j] == enc_want.
 __global__ void k_kick_split(int n, const double *__restrict__ r, const double *__restrict__ Gm,
                              const double *__restrict__ R, float4 *A, float4 *B, const int32_t *__restrict__ sysid,
-                             const int32_t *__restrict__ flag, int phase) {
+                             const int32_t *__restrict__ flag, int phase, const uint8_t *__restrict__ enc,
+                             int enc_want) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     if (sysid && flag[sysid[j]] != phase) return;
+    if (enc && enc[j] != enc_want) return;
     float4 a, b;
     split_hi_lo(r[3 * j + 0], a.x, b.x);
     split_hi_lo(r[3 * j + 1], a.y, b.y);
@@ -436,7 +439,7 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
     float4 *pA = (float4 *)((char *)scratch + poff), *pB = pA + npart;
     if (npart > 0) {
         k_kick_split<<<div_up(npart, 256), 256, 0, c->stream>>>(npart, rpart, Gm, tp ? nullptr : R, pA, pB, nullptr,
-                                                                 nullptr, 0);
+                                                                 nullptr, 0, nullptr, 0);
         c->launches++;
     }
     dim3 grid(bx, nchunk);
@@ -489,9 +492,10 @@ int64_t kick_mixed_plpl_partials_max(int num_sms, int npl) {
 
 // Split n partner bodies into float hi/lo tiles (A = x_hi, y_hi, z_hi, Gm; B = x_lo, y_lo, z_lo, R).
 int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
-                      float4 *B, const int32_t *sysid, const int32_t *flag, int phase) {
+                      float4 *B, const int32_t *sysid, const int32_t *flag, int phase, const uint8_t *enc,
+                      int enc_want) {
     if (n <= 0) return SWG_OK;
-    k_kick_split<<<div_up(n, 256), 256, 0, c->stream>>>((int)n, r, Gm, R, A, B, sysid, flag, phase);
+    k_kick_split<<<div_up(n, 256), 256, 0, c->stream>>>((int)n, r, Gm, R, A, B, sysid, flag, phase, enc, enc_want);
     c->launches++;
     return launch_status(c, "kick_split");
 }

@@ -285,7 +285,8 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
                                                       const float4 *__restrict__ pA, const float4 *__restrict__ pB,
                                                       float *__restrict__ rpart, float *__restrict__ ppart,
                                                       unsigned *__restrict__ head,
-                                                      const int32_t *__restrict__ sys_flag, int phase) {
+                                                      const int32_t *__restrict__ sys_flag, int phase,
+                                                      const uint8_t *__restrict__ iflag, unsigned accept) {
     __shared__ SubTile sP[SR];
     const int lane = threadIdx.x;
     const float4 pad_a = make_float4(PAD_POS, PAD_POS, PAD_POS, 0.f), zero = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -297,6 +298,7 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
         const int4 w = items[it];
         const int s = w.x, I = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
         if (sys_flag && sys_flag[s] != phase) continue;  // warp-uniform
+        if (iflag && !((accept >> iflag[it]) & 1u)) continue;
         const int p0 = poff[s], n = npl[s], nt = (n + TS - 1) / TS;
         Recv2 q[SR];
         bool ok[SR];
@@ -356,6 +358,33 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
     }
 }
 
+// One warp per item: 0 for a system without encounters, else 2 when tile I or one of the
+// strip's tiles J holds a body marked in enc, else 1 (see kick_sym_item_flags).
+__global__ void k_kick_sym_item_flags(int nitems, const int4 *__restrict__ items, const int32_t *__restrict__ poff,
+                                      const int32_t *__restrict__ npl, const int32_t *__restrict__ sys_enc,
+                                      const uint8_t *__restrict__ enc, uint8_t *__restrict__ iflag) {
+    const int it = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (it >= nitems) return;  // whole warps leave together
+    const int4 w = items[it];
+    const int s = w.x, I = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
+    if (!sys_enc[s]) {
+        if (lane == 0) iflag[it] = 0;
+        return;
+    }
+    const int p0 = poff[s], n = npl[s];
+    bool dirty = false;
+    for (int t = -1; t < nJ; t++) {
+        const int T = t < 0 ? I : J0 + t;
+        for (int k = lane; k < TS; k += 32) {
+            const int i = T * TS + k;
+            if (i < n && enc[p0 + i]) dirty = true;
+        }
+    }
+    dirty = __any_sync(FULL, dirty);
+    if (lane == 0) iflag[it] = dirty ? 2 : 1;
+}
+
 // Per body: acc (+)= its slots in a fixed order (pair slots of the tiles below its own,
 // then the receiver slots of its own row).  The slots' values are added in float-float
 // (hi parts by TwoSum, lo parts plainly) and converted to FP64 once: FP64 arithmetic per
@@ -396,6 +425,16 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
 }
 
 }  // namespace
+
+int kick_sym_item_flags(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
+                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag) {
+    if (nitems <= 0) return SWG_OK;
+    const int64_t threads = (int64_t)nitems * 32;
+    k_kick_sym_item_flags<<<(int)((threads + 255) / 256), 256, 0, c->stream>>>(nitems, items, poff, npl, sys_enc,
+                                                                              enc, iflag);
+    c->launches++;
+    return launch_status(c, "kick_sym_item_flags");
+}
 
 int kick_sym_strip(int32_t nsys, const int32_t *npl, int num_sms) {
     int64_t pairs = 0;
@@ -446,7 +485,8 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<
 
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
-                           float *ppart, unsigned *head, const int32_t *sys_flag, int phase) {
+                           float *ppart, unsigned *head, const int32_t *sys_flag, int phase, const uint8_t *iflag,
+                           unsigned accept) {
     if (nitems <= 0) return SWG_OK;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
     static int occ[2] = {0, 0};  // resident blocks per SM, queried once per variant
@@ -461,10 +501,10 @@ int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, 
     const int grid = std::min(nitems, o * (c->num_sms > 0 ? c->num_sms : 152));
     if (rad)
         k_kick_mixed_sym<true><<<grid, 32, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
-                                                               head, sys_flag, phase);
+                                                               head, sys_flag, phase, iflag, accept);
     else
         k_kick_mixed_sym<false><<<grid, 32, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
-                                                                head, sys_flag, phase);
+                                                                head, sys_flag, phase, iflag, accept);
     c->launches++;
     return launch_status(c, "kick_mixed_sym");
 }

@@ -155,8 +155,10 @@ int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const 
 // Batched (ensemble) pair kernels.  Items are int4 (system, first receiver, receivers,
 // unused) sorted by cost, largest first; per-system offsets and counts are device arrays.
 // sys_flag/phase (optional, pl-pl): only systems s with sys_flag[s] == phase are processed.
+// enc/enc_want (optional): split only the bodies j with enc[j] == enc_want.
 int kick_split_launch(swg_ctx *c, int64_t n, const double *r, const double *Gm, const double *R, float4 *A,
-                      float4 *B, const int32_t *sysid = nullptr, const int32_t *sys_flag = nullptr, int phase = 0);
+                      float4 *B, const int32_t *sysid = nullptr, const int32_t *sys_flag = nullptr, int phase = 0,
+                      const uint8_t *enc = nullptr, int enc_want = 0);
 // variant: tile shape of the batched mixed kick (0 .. KICK_NVARIANT-1; identical results),
 // whose items are tiles of kick_variant_tile(variant) receivers.
 constexpr int KICK_NVARIANT = SWG_KICK_NVARIANT;
@@ -194,9 +196,15 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<
                        std::vector<int32_t> &sbase, int64_t *npair_slots);
 // a single system has enough tile pairs to fill the GPU (else the broadcast kernel is faster)
 bool kick_sym_single_ok(int32_t npl, int num_sms);
+// iflag/accept (optional): only items it with bit iflag[it] of accept set are processed.
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
-                           float *ppart, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
+                           float *ppart, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0,
+                           const uint8_t *iflag = nullptr, unsigned accept = 0);
+// iflag[it] of every item: 0 when its system has no encounter (sys_enc[s] == 0), else 2 when
+// one of its tiles holds a body with enc[body] != 0, else 1.
+int kick_sym_item_flags(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
+                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag);
 // one system (psys == nullptr below): plan cached in the context for the last npl; acc (+)= the
 // pair accelerations (radius rule with R, else j != i); no GMTINY bodies
 int kick_mixed_sym_single(swg_ctx *c, int32_t npl, const double *r, const double *Gm, const double *R, double *acc,
