@@ -321,3 +321,28 @@ def test_ensemble_ragged_and_empty_systems(ctx, integrator):
     out = m.get_pl() + m.get_tp()
     assert all(np.all(np.isfinite(x)) for x in out)
     m.close()
+
+
+@pytest.mark.parametrize("integrator", ["SYMBA", "HELIO", "WHM"])
+def test_stream_schedules_match_serial(ctx, integrator):
+    # The overlapped step (side streams: SyMBA level-0 drift and closing-kick items beside
+    # the recursion, HELIO test-particle groups, WHM test-particle drift) gives the same bits
+    # as the serial step that the per-class profile runs.
+    if integrator == "SYMBA":
+        E = _compact("C4", nsys=6, scale=0.25, tp_per_pl=1)
+        kw = dict(dt=0.005, rhscale=3.0)
+    else:
+        E = IC.make_ensemble("C3", nsys=8, scale=0.2, integrator=integrator)
+        kw = dict(dt=0.01)
+    out, stats = [], None
+    for prof in (False, True):
+        ens = Ensemble(ctx, E, precision="MIXED", **kw)
+        ens.profile(prof)
+        ens.step(25)
+        out.append(ens.get_pl() + ens.get_tp())
+        stats = ens.stats()
+        ens.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+    if integrator == "SYMBA":
+        assert stats["plpl_encounters"] > 0
