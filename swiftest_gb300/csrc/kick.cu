@@ -334,6 +334,78 @@ __global__ void k_kick_pairs_serial(int64_t npairs, const int32_t *__restrict__ 
     }
 }
 
+// Short lists (npairs <= PAIRS_SMALL), one block, same bits as k_kick_pairs_serial: thread q
+// evaluates pair q (the FP64 square root and divide of all pairs run at once), then the
+// thread holding the first pair of a body adds that body's terms of every later pair in
+// list order (ahi for index1, ahj for index2), as the serial loop does.
+constexpr int PAIRS_SMALL = 256;
+template <bool RAD>
+__global__ void __launch_bounds__(PAIRS_SMALL) k_kick_pairs_small(int npairs, const int32_t *__restrict__ k,
+                                                                  const int32_t *__restrict__ i1,
+                                                                  const int32_t *__restrict__ i2,
+                                                                  const double *__restrict__ r,
+                                                                  const double *__restrict__ Gm,
+                                                                  const double *__restrict__ R, double *ahi,
+                                                                  double *ahj) {
+    __shared__ double tI[PAIRS_SMALL][3], tJ[PAIRS_SMALL][3];
+    __shared__ int sI[PAIRS_SMALL], sJ[PAIRS_SMALL];
+    __shared__ unsigned char ok[PAIRS_SMALL];
+    const int q = threadIdx.x;
+    if (q < npairs) {
+        const int i = (k ? k[2 * q] : i1[q]) - 1;
+        const int j = (k ? k[2 * q + 1] : i2[q]) - 1;
+        sI[q] = i;
+        sJ[q] = j;
+        const double rx = r[3 * j + 0] - r[3 * i + 0];
+        const double ry = r[3 * j + 1] - r[3 * i + 1];
+        const double rz = r[3 * j + 2] - r[3 * i + 2];
+        const double rji2 = rx * rx + ry * ry + rz * rz;
+        bool keep = true;
+        if (RAD) {
+            const double rs = R[i] + R[j];
+            keep = rji2 > rs * rs;
+        }
+        ok[q] = keep;
+        if (keep) {
+            const double irij3 = 1.0 / (rji2 * sqrt(rji2));
+            const double faci = Gm[i] * irij3;
+            const double facj = Gm[j] * irij3;
+            tI[q][0] = facj * rx;
+            tI[q][1] = facj * ry;
+            tI[q][2] = facj * rz;
+            tJ[q][0] = faci * rx;
+            tJ[q][1] = faci * ry;
+            tJ[q][2] = faci * rz;
+        }
+    }
+    __syncthreads();
+    if (q >= npairs) return;
+    for (int side = 0; side < 2; side++) {
+        const int *s = side == 0 ? sI : sJ;
+        const int b = s[q];
+        bool first = true;
+        for (int p = 0; p < q && first; p++) first = s[p] != b;
+        if (!first) continue;
+        double *a = (side == 0 ? ahi : ahj) + 3 * b;
+        double x = a[0], y = a[1], z = a[2];
+        for (int p = q; p < npairs; p++) {
+            if (s[p] != b || !ok[p]) continue;
+            if (side == 0) {
+                x = x + tI[p][0];
+                y = y + tI[p][1];
+                z = z + tI[p][2];
+            } else {
+                x = x - tJ[p][0];
+                y = y - tJ[p][1];
+                z = z - tJ[p][2];
+            }
+        }
+        a[0] = x;
+        a[1] = y;
+        a[2] = z;
+    }
+}
+
 // Parallel variant for long lists: atomic accumulation (order not fixed).
 template <bool RAD>
 __global__ void k_kick_pairs_atomic(int64_t npairs, const int32_t *__restrict__ k, const int32_t *__restrict__ i1,
@@ -573,7 +645,12 @@ int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const 
     if (npairs <= 0 || npl <= 0) return SWG_OK;
     double *ahi = ahi_ahj, *ahj = ahi_ahj + 3 * (size_t)npl;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(ahi_ahj, 0, sizeof(double) * 6 * (size_t)npl, c->stream), "memset"));
-    if (npairs <= 65536) {
+    if (npairs <= PAIRS_SMALL) {
+        if (R)
+            k_kick_pairs_small<true><<<1, PAIRS_SMALL, 0, c->stream>>>((int)npairs, k, i1, i2, r, Gm, R, ahi, ahj);
+        else
+            k_kick_pairs_small<false><<<1, PAIRS_SMALL, 0, c->stream>>>((int)npairs, k, i1, i2, r, Gm, R, ahi, ahj);
+    } else if (npairs <= 65536) {
         if (R)
             k_kick_pairs_serial<true><<<1, 32, 0, c->stream>>>(npairs, k, i1, i2, r, Gm, R, ahi, ahj);
         else

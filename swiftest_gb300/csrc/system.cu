@@ -140,6 +140,52 @@ __global__ void k_pltp_addback(int64_t n, const int32_t *__restrict__ i1, const 
 
 
 
+// The same add-back for short lists (n <= ADDBACK_SMALL), one block, same bits: thread k
+// evaluates pair k, then the thread holding a test particle's first pair adds that
+// particle's terms in list order.
+constexpr int ADDBACK_SMALL = 256;
+__global__ void __launch_bounds__(ADDBACK_SMALL) k_pltp_addback_small(int n, const int32_t *__restrict__ i1,
+                                                                     const int32_t *__restrict__ i2,
+                                                                     const int32_t *__restrict__ tlmask,
+                                                                     const double *__restrict__ trh,
+                                                                     const double *__restrict__ rp,
+                                                                     const double *__restrict__ Gm, double *tah) {
+    __shared__ double t[ADDBACK_SMALL][3];
+    __shared__ int sj[ADDBACK_SMALL];
+    __shared__ unsigned char ok[ADDBACK_SMALL];
+    const int k = threadIdx.x;
+    if (k < n) {
+        const int i = i1[k] - 1, j = i2[k] - 1;
+        sj[k] = j;
+        ok[k] = tlmask[j] != 0;
+        if (ok[k]) {
+            const double dx = trh[3 * j + 0] - rp[3 * i + 0];
+            const double dy = trh[3 * j + 1] - rp[3 * i + 1];
+            const double dz = trh[3 * j + 2] - rp[3 * i + 2];
+            const double rjj = dx * dx + dy * dy + dz * dz;
+            const double fac = Gm[i] / (rjj * sqrt(rjj));
+            t[k][0] = fac * dx;
+            t[k][1] = fac * dy;
+            t[k][2] = fac * dz;
+        }
+    }
+    __syncthreads();
+    if (k >= n || !ok[k]) return;
+    const int j = sj[k];
+    for (int p = 0; p < k; p++)
+        if (sj[p] == j) return;  // not the particle's first pair
+    double x = tah[3 * j + 0], y = tah[3 * j + 1], z = tah[3 * j + 2];
+    for (int p = k; p < n; p++) {
+        if (sj[p] != j || !ok[p]) continue;
+        x = x + t[p][0];
+        y = y + t[p][1];
+        z = z + t[p][2];
+    }
+    tah[3 * j + 0] = x;
+    tah[3 * j + 1] = y;
+    tah[3 * j + 2] = z;
+}
+
 // The whole SyMBA recursion of one step, one block (blk_symba_recursion).
 __global__ void __launch_bounds__(RECT) k_symba_recursion(RecArgs a) {
     if (threadIdx.x == 0) a.out[0] = 0;
@@ -278,8 +324,13 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
         SWG_TRY(cuda_status(c, cudaMemsetAsync(s->tah, 0, sizeof(double) * 3 * s->ntp, c->stream), "memset"));
     }
     if (s->integrator == SWG_SYMBA && s->pltp_n > 0) {
-        k_pltp_addback<<<1, 32, 0, c->stream>>>(s->pltp_n, s->pltp_l, s->pltp_l + s->pltp_cap, s->tlmask, s->trh,
-                                                rp, s->Gmass, s->tah);
+        if (s->pltp_n <= ADDBACK_SMALL)
+            k_pltp_addback_small<<<1, ADDBACK_SMALL, 0, c->stream>>>((int)s->pltp_n, s->pltp_l,
+                                                                      s->pltp_l + s->pltp_cap, s->tlmask, s->trh, rp,
+                                                                      s->Gmass, s->tah);
+        else
+            k_pltp_addback<<<1, 32, 0, c->stream>>>(s->pltp_n, s->pltp_l, s->pltp_l + s->pltp_cap, s->tlmask,
+                                                    s->trh, rp, s->Gmass, s->tah);
         SWG_TRY(L(c, "pltp_addback"));
     }
     k_kick_update<<<grid_for(s->ntp, 128), 128, 0, c->stream>>>(s->ntp, s->tvb, s->tah, s->tlmask, dt, nullptr,
