@@ -65,8 +65,7 @@ struct swg_ensemble {
     double *rh = nullptr, *vh = nullptr, *vb = nullptr, *ah = nullptr, *rbeg = nullptr, *rend = nullptr;
     double *Gmass = nullptr, *radius = nullptr, *rhill = nullptr, *renc = nullptr;
     int32_t *status = nullptr, *lmask = nullptr, *levelg = nullptr, *levelm = nullptr, *nplenc = nullptr,
-            *ntpenc = nullptr, *mark_pl = nullptr, *pmark = nullptr;
-    double *ahi = nullptr, *ahj = nullptr;
+            *ntpenc = nullptr, *mark_pl = nullptr;
     // test particles
     int32_t *tsys = nullptr;
     double *trh = nullptr, *tvh = nullptr, *tvb = nullptr, *tah = nullptr;
@@ -429,65 +428,81 @@ __global__ void k_ens_pair_terms(int64_t n, const int32_t *__restrict__ l, int64
     ok[q] = 1;
 }
 
-// symba_kick_getacch_pl (symba_kick.f90:36-76) pair subtraction of every system: the
-// pair terms accumulated into ahi/ahj in list order (swiftest_kick_getacch_int_all_flat
-// order), then acc -= ahi + ahj once per body.  One thread per system.
-__global__ void k_ens_kick_pairs(int nsys, const int32_t *__restrict__ seg, const int32_t *__restrict__ l,
-                                 int64_t cap, const double *__restrict__ t, const uint8_t *__restrict__ ok,
-                                 double *ahi, double *ahj, int32_t *mark, double *acc) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+// symba_kick_getacch_pl (symba_kick.f90:36-76) pair subtraction of every system: per body,
+// the pair terms of the pairs naming it as index1 (ahi) and as index2 (ahj) added in list
+// order (swiftest_kick_getacch_int_all_flat order), then acc -= ahi + ahj once per body.
+// One warp per system: a body's sums are formed by the lane that holds its first occurrence
+// in the order (pair 0 index1, pair 0 index2, pair 1 index1, ...).
+__global__ void k_ens_kick_pairs_warp(int nsys, const int32_t *__restrict__ seg, const int32_t *__restrict__ l,
+                                      int64_t cap, const double *__restrict__ t, const uint8_t *__restrict__ ok,
+                                      double *acc) {
+    const int s = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (s >= nsys || seg[2 * s + 1] == 0) return;
     const int n = seg[2 * s + 1];
     const int32_t *i1 = l + seg[2 * s], *i2 = i1 + cap;
     const double *ts = t + 6 * (int64_t)seg[2 * s];
     const uint8_t *oks = ok + seg[2 * s];
-    for (int q = 0; q < n; q++)
-        for (int d = 0; d < 3; d++) {
-            ahi[3 * (i1[q] - 1) + d] = ahj[3 * (i1[q] - 1) + d] = 0.0;
-            ahi[3 * (i2[q] - 1) + d] = ahj[3 * (i2[q] - 1) + d] = 0.0;
+    for (int occ = lane; occ < 2 * n; occ += 32) {
+        const int q = occ >> 1;
+        const int b = ((occ & 1) ? i2[q] : i1[q]) - 1;
+        bool first = true;
+        for (int o = 0; o < occ && first; o++) first = (((o & 1) ? i2[o >> 1] : i1[o >> 1]) - 1) != b;
+        if (!first) continue;
+        double hx = 0.0, hy = 0.0, hz = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+        for (int p = 0; p < n; p++) {
+            if (!oks[p]) continue;
+            const double *o = ts + 6 * p;
+            if (i1[p] - 1 == b) {
+                hx = hx + o[0];
+                hy = hy + o[1];
+                hz = hz + o[2];
+            }
+            if (i2[p] - 1 == b) {
+                jx = jx - o[3];
+                jy = jy - o[4];
+                jz = jz - o[5];
+            }
         }
-    for (int q = 0; q < n; q++) {
-        if (!oks[q]) continue;
-        const int i = i1[q] - 1, j = i2[q] - 1;
-        const double *o = ts + 6 * q;
-        ahi[3 * i + 0] = ahi[3 * i + 0] + o[0];
-        ahi[3 * i + 1] = ahi[3 * i + 1] + o[1];
-        ahi[3 * i + 2] = ahi[3 * i + 2] + o[2];
-        ahj[3 * j + 0] = ahj[3 * j + 0] - o[3];
-        ahj[3 * j + 1] = ahj[3 * j + 1] - o[4];
-        ahj[3 * j + 2] = ahj[3 * j + 2] - o[5];
+        acc[3 * b + 0] = acc[3 * b + 0] - (hx + jx);
+        acc[3 * b + 1] = acc[3 * b + 1] - (hy + jy);
+        acc[3 * b + 2] = acc[3 * b + 2] - (hz + jz);
     }
-    for (int q = 0; q < n; q++) {
-        const int b2[2] = {i1[q] - 1, i2[q] - 1};
-        for (int e = 0; e < 2; e++) {
-            const int b = b2[e];
-            if (mark[b]) continue;
-            mark[b] = 1;
-            for (int d = 0; d < 3; d++) acc[3 * b + d] = acc[3 * b + d] - (ahi[3 * b + d] + ahj[3 * b + d]);
-        }
-    }
-    for (int q = 0; q < n; q++) mark[i1[q] - 1] = mark[i2[q] - 1] = 0;
 }
 
-// symba_kick_getacch_tp add-back loop (symba_kick.f90:104-118), one thread per system
+// symba_kick_getacch_tp add-back loop (symba_kick.f90:104-118) of every system
 __global__ void k_ens_pltp_addback(int nsys, const int32_t *__restrict__ seg, const int32_t *__restrict__ l,
                                    int64_t cap, const int32_t *__restrict__ tlmask, const double *__restrict__ trh,
                                    const double *__restrict__ rp, const double *__restrict__ Gm, double *tah) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per system; each test particle's pairs are added, in list order, by the lane
+    // that holds its first pair (particles in parallel, the reference's order per particle)
+    const int s = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (s >= nsys || seg[2 * s + 1] == 0) return;
     const int n = seg[2 * s + 1];
     const int32_t *i1 = l + seg[2 * s], *i2 = i1 + cap;
-    for (int k = 0; k < n; k++) {
-        const int i = i1[k] - 1, j = i2[k] - 1;
+    for (int k = lane; k < n; k += 32) {
+        const int j = i2[k] - 1;
         if (!tlmask[j]) continue;
-        const double dx = trh[3 * j + 0] - rp[3 * i + 0];
-        const double dy = trh[3 * j + 1] - rp[3 * i + 1];
-        const double dz = trh[3 * j + 2] - rp[3 * i + 2];
-        const double rjj = dx * dx + dy * dy + dz * dz;
-        const double fac = Gm[i] / (rjj * sqrt(rjj));
-        tah[3 * j + 0] = tah[3 * j + 0] + fac * dx;
-        tah[3 * j + 1] = tah[3 * j + 1] + fac * dy;
-        tah[3 * j + 2] = tah[3 * j + 2] + fac * dz;
+        bool first = true;
+        for (int p = 0; p < k && first; p++) first = i2[p] - 1 != j;
+        if (!first) continue;
+        double x = tah[3 * j + 0], y = tah[3 * j + 1], z = tah[3 * j + 2];
+        for (int p = k; p < n; p++) {
+            if (i2[p] - 1 != j) continue;
+            const int i = i1[p] - 1;
+            const double dx = trh[3 * j + 0] - rp[3 * i + 0];
+            const double dy = trh[3 * j + 1] - rp[3 * i + 1];
+            const double dz = trh[3 * j + 2] - rp[3 * i + 2];
+            const double rjj = dx * dx + dy * dy + dz * dz;
+            const double fac = Gm[i] / (rjj * sqrt(rjj));
+            x = x + fac * dx;
+            y = y + fac * dy;
+            z = z + fac * dz;
+        }
+        tah[3 * j + 0] = x;
+        tah[3 * j + 1] = y;
+        tah[3 * j + 2] = z;
     }
 }
 
@@ -895,8 +910,8 @@ int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false) {
         k_ens_pair_terms<<<grid_for(e->pp_n, 128), 128, 0, c->stream>>>(e->pp_n, e->pp_l, e->pp_cap, e->rh, e->Gmass,
                                                                         e->radius, t, ok);
         SWG_TRY(L(c, "ens_pair_terms"));
-        k_ens_kick_pairs<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pp, e->pp_l, e->pp_cap, t, ok,
-                                                                      e->ahi, e->ahj, e->pmark, e->ah);
+        k_ens_kick_pairs_warp<<<grid_for(32 * (int64_t)e->nsys, 128), 128, 0, c->stream>>>(
+            e->nsys, e->seg_pp, e->pp_l, e->pp_cap, t, ok, e->ah);
         SWG_TRY(L(c, "ens_kick_pairs"));
     }
     k_kick_update<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->vb, e->ah, e->lmask, dt, e->rh,
@@ -924,8 +939,8 @@ int kick_vb_tp(swg_ensemble *e, double dt, int lbeg, unsigned *head = nullptr) {
         }
     }
     if (e->integrator == SWG_SYMBA && e->pt_n > 0) {
-        k_ens_pltp_addback<<<grid_for(e->nsys, 64), 64, 0, c->stream>>>(e->nsys, e->seg_pt, e->pt_l, e->pt_cap,
-                                                                        e->tlmask, e->trh, rp, e->Gmass, e->tah);
+        k_ens_pltp_addback<<<grid_for(32 * (int64_t)e->nsys, 128), 128, 0, c->stream>>>(
+            e->nsys, e->seg_pt, e->pt_l, e->pt_cap, e->tlmask, e->trh, rp, e->Gmass, e->tah);
         SWG_TRY(L(c, "ens_pltp_addback"));
     }
     k_kick_update<<<grid_for(e->NTP, 128), 128, 0, c->stream>>>((int)e->NTP, e->tvb, e->tah, e->tlmask, dt, nullptr,
@@ -1748,14 +1763,13 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->GMcb, S);
     if (rc == SWG_OK) rc = dalloc(c, &e->dcb, CB_N * S);
     if (rc == SWG_OK) rc = dalloc(c, &e->eout, 9 * S);
-    double **pd[] = {&e->rh, &e->vh, &e->vb, &e->ah, &e->rbeg, &e->rend, &e->ahi, &e->ahj};
+    double **pd[] = {&e->rh, &e->vh, &e->vb, &e->ah, &e->rbeg, &e->rend};
     for (auto p : pd)
         if (rc == SWG_OK) rc = dalloc(c, p, 3 * n);
     double **pn[] = {&e->Gmass, &e->radius, &e->rhill, &e->renc};
     for (auto p : pn)
         if (rc == SWG_OK) rc = dalloc(c, p, n);
-    int32_t **pi[] = {&e->psys, &e->status, &e->lmask, &e->levelg, &e->levelm, &e->nplenc, &e->ntpenc, &e->mark_pl,
-                      &e->pmark};
+    int32_t **pi[] = {&e->psys, &e->status, &e->lmask, &e->levelg, &e->levelm, &e->nplenc, &e->ntpenc, &e->mark_pl};
     for (auto p : pi)
         if (rc == SWG_OK) rc = dalloc(c, p, n);
     double **td[] = {&e->trh, &e->tvh, &e->tvb, &e->tah};
@@ -1853,7 +1867,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
     void *ptrs[] = {e->npl, e->ntp, e->poff, e->toff, e->GMcb, e->dcb, e->lfirst, e->lany, e->seg_pp, e->seg_pt,
                     e->enc_steps, e->psys, e->rh, e->vh, e->vb, e->ah, e->rbeg, e->rend, e->Gmass, e->radius,
                     e->rhill, e->renc, e->status, e->lmask, e->levelg, e->levelm, e->nplenc, e->ntpenc, e->mark_pl,
-                    e->pmark, e->ahi, e->ahj, e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
+                    e->tsys, e->trh, e->tvh, e->tvb, e->tah, e->tstatus, e->tlmask,
                     e->tlevelg, e->tlevelm, e->tnplenc, e->mark_tp, e->kA, e->eT, e->eS, e->perm, e->tbase, e->tperm, e->ttbase, e->ttiles, e->tbounds, e->it_tsp,
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
