@@ -323,13 +323,17 @@ def test_ensemble_ragged_and_empty_systems(ctx, integrator):
     m.close()
 
 
-@pytest.mark.parametrize("integrator", ["SYMBA", "HELIO", "WHM"])
+@pytest.mark.parametrize("integrator", ["SYMBA", "SYMBA_COLL", "HELIO", "WHM"])
 def test_stream_schedules_match_serial(ctx, integrator):
     # The overlapped step (side streams: SyMBA level-0 drift and closing-kick items beside
     # the recursion, HELIO test-particle groups, WHM test-particle drift) gives the same bits
-    # as the serial step that the per-class profile runs.
-    if integrator == "SYMBA":
+    # as the serial step that the per-class profile runs; SYMBA_COLL inflates the radii so
+    # that the recursion pauses for perfect merges on the host.
+    if integrator.startswith("SYMBA"):
         E = _compact("C4", nsys=6, scale=0.25, tp_per_pl=1)
+        if integrator == "SYMBA_COLL":
+            E["pl"]["radius"] = E["pl"]["radius"] * 300.0
+            E["systems"] = None
         kw = dict(dt=0.005, rhscale=3.0)
     else:
         E = IC.make_ensemble("C3", nsys=8, scale=0.2, integrator=integrator)
@@ -344,5 +348,7 @@ def test_stream_schedules_match_serial(ctx, integrator):
         ens.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
-    if integrator == "SYMBA":
+    if integrator.startswith("SYMBA"):
         assert stats["plpl_encounters"] > 0
+    if integrator == "SYMBA_COLL":
+        assert stats["collisions"] > 0
