@@ -2403,8 +2403,8 @@ static int discard_pl_close(const double *dx, const double *dv, double dt, doubl
     return r2min <= r2crit;
 }
 
-/* swiftest_discard_pl_tp (src/swiftest/swiftest_discard.f90:244-290), the driver's discard
- * step after each step when param%lclose: an ACTIVE tp that comes within a pl's radius
+/* swiftest_discard_pl_tp (src/swiftest/swiftest_discard.f90:244-290), the discard step of the
+ * reference's main loop (swiftest_driver) after each step when param%lclose: an ACTIVE tp that comes within a pl's radius
  * leaves the system (the reference spills it out of its arrays; here it stays in its slot
  * with status INACTIVE, masked, parked with no velocity at 1e6 AU + (npl + its index)). */
 static void discard_pl_tp(orc_system *s) {

@@ -789,7 +789,8 @@ int symba_interp(swg_system *s, double dt) {
 }
 
 // swiftest_discard_pl_tp (src/swiftest/swiftest_discard.f90:244-290), run after each step
-// when close encounters are checked (param%lclose), as the driver's discard step does.
+// when close encounters are checked (param%lclose), as the reference's main loop
+// (swiftest_driver) does after every step.
 int discard_step(swg_system *s) {
     if (!s->lclose || s->npl == 0 || s->ntp == 0) return SWG_OK;
     swg_ctx *c = s->c;
