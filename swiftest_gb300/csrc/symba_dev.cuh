@@ -420,7 +420,8 @@ __device__ __forceinline__ int spread_tid() {
 }
 
 // symba_encounter_check_list_plpl / _pltp (symba_encounter_check.f90:90-235), whole block.
-static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any) {
+// rs_pow[k] = RSHELL^k formed as d_renc forms it (repeated products), k <= MAXLEV.
+static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int *s_any, const double *rs_pow) {
     const int64_t npp = a.npp, npt = a.npt;
     for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
         const bool isp = k < npp;
@@ -438,8 +439,8 @@ static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int
                 xr[d] = rj[d] - a.rh[3 * i + d];
                 vr[d] = vj[d] - a.vb[3 * i + d];
             }
-            const double renci = d_renc(a.rhill[i], a.rhscale, irec);
-            const double rcrit = isp ? renci + d_renc(a.rhill[j], a.rhscale, irec) : renci;
+            const double renci = a.rhill[i] * a.rhscale * rs_pow[irec];  // d_renc(rhill_i, rhscale, irec)
+            const double rcrit = isp ? renci + a.rhill[j] * a.rhscale * rs_pow[irec] : renci;
             int le, lvd;
             d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
             lv[q] = lvd;
@@ -494,12 +495,14 @@ static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int
 // (r^2 < rim1).  terms: 12 doubles per entry, the +1 pair terms then the -1 pair terms.
 // The reference's lmask refresh at entry is kept by the step loop instead (lmask ==
 // status /= INACTIVE wherever the recursion runs).
-static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, double dt, int irec, bool both) {
+// pw[m] = d_powi(RSHELL, m), m <= 2 MAXLEV.
+static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, double dt, int irec, bool both,
+                                      const double *pw) {
     const int64_t npp = a.npp, npt = a.npt;
     if (npp + npt == 0) return;
     const int irm1 = irec - 1;
     const double rs2 = a.rhscale * a.rhscale;
-    const double shell_p = d_powi(RSHELL, 2 * irec), shell_m = d_powi(RSHELL, 2 * (irec - 1));
+    const double shell_p = pw[2 * irec], shell_m = pw[2 * (irec - 1)];
     const int32_t *pi1 = a.pp, *pi2 = a.pp + a.ppcap, *pst = a.pp + 3 * a.ppcap;
     const int32_t *ti1 = a.pt, *ti2 = a.pt + a.ptcap, *tst = a.pt + 3 * a.ptcap;
     const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
@@ -535,15 +538,24 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
         a.good[k] = kp ? 1 : 2;
         a.good2[k] = both ? (km ? 1 : 2) : 0;
         if (!kp && !km) continue;
-        const double r = sqrt(r2);
         const bool shp = kp && r2 < ri_p, shm = km && r2 < ri_m;
-        const double ir3 = 1.0 / (r2 * r);
-        // FP64 path: the correctly rounded r^-1.5 shared with the oracle; mixed path: 1/(r^2 r)
+        // FP64 path: IEEE square root and divide, and the correctly rounded r^-1.5 shared
+        // with the oracle; mixed path: r and r^-3 from one reciprocal square root
+        double r, ir3;
+        if (a.fast) {
+            const double y = rsqrt(r2);
+            r = r2 * y;
+            ir3 = (y * y) * y;
+        } else {
+            r = sqrt(r2);
+            ir3 = 1.0 / (r2 * r);
+        }
         double p = ir3;
         if (!a.fast && (shp || shm)) p = pow_m1p5(r2);
         auto shell = [&](double ri) {
-            const double ris = sqrt(ri);
-            const double rr = (ris - r) / (ris * (1.0 - RSHELL));
+            // rr = (sqrt(ri) - r) / (sqrt(ri) (1 - RSHELL)); mixed path as (1 - r / sqrt(ri)) / (1 - RSHELL)
+            const double rr = a.fast ? (1.0 - r * rsqrt(ri)) * (1.0 / (1.0 - RSHELL))
+                                     : (sqrt(ri) - r) / (sqrt(ri) * (1.0 - RSHELL));
             return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         };
         double *t = &a.terms[12 * k];
@@ -836,6 +848,19 @@ static __device__ void blk_build_adjacency(const RecArgs &a, int nbpl, int nbtp)
 static __device__ void blk_symba_recursion(const RecArgs &a) {
     __shared__ int s_nbpl, s_nbtp, s_any;
     __shared__ int s_j[MAXLEV], s_phase[MAXLEV];
+    // shell-radius powers, formed once per launch with the per-call algorithms (same bits):
+    // s_pw[m] = d_powi(RSHELL, m) (the kick's shell radii), s_rs[k] = RSHELL^k by repeated
+    // products (d_renc, the list check's encounter radii)
+    __shared__ double s_pw[2 * MAXLEV + 2], s_rs[MAXLEV + 1];
+    for (int m = threadIdx.x; m < 2 * MAXLEV + 2; m += blockDim.x) s_pw[m] = d_powi(RSHELL, m);
+    if (threadIdx.x == 0) {
+        double p = 1.0;
+        s_rs[0] = p;
+        for (int k = 1; k <= MAXLEV; k++) {
+            p = p * RSHELL;
+            s_rs[k] = p;
+        }
+    }
     if (threadIdx.x == 0) s_nbpl = s_nbtp = 0;
     __syncthreads();
     // compact sets of bodies named in the lists
@@ -895,8 +920,8 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
             substeps++;
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
-            blk_list_check(a, irecp, dtl, &s_any);
-            blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
+            blk_list_check(a, irecp, dtl, &s_any, s_rs);
+            blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
             blk_drift(a, nbpl, nbtp, ireci, dtl);
             const int any = s_any;
             __syncthreads();
@@ -915,7 +940,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
             }
         }
         // after the deeper levels (or none) for loop j of level ireci
-        blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0);
+        blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
         if (a.lclose) {
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
