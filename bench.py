@@ -47,7 +47,6 @@ sys.path.insert(0, str(ROOT))
 METRIC = "SyMBA body-steps/s on 1 GB300: mixed+batched vs FP64 GPU at matched |ΔE/E|"
 UNIT = "body-steps/s"
 FLOPS_PER_INTERACTION = 20.0  # GPU Gems 3 ch. 31 convention (sqrt and divide count 1)
-FP64_STEPS = 20  # timed steps of the FP64 comparison arm (at most --steps)
 
 
 def parse():
@@ -447,7 +446,7 @@ def main():
     nprof = max(3, min(10, args.steps))
     ms_mixed, launches, (prof, prof_ms), err_m, st_m = run_path(ctx, wl, "MIXED", args.steps, args.warmup, nprof,
                                                                 clocks=clocks)
-    steps64 = min(args.steps, FP64_STEPS)  # the FP64 comparison arm is ~100x slower per step
+    steps64 = args.steps  # same steps as the mixed arm, so the two |dE/E| are over the same run
     ms_fp64, _, (prof64, _), err_f, st_f = run_path(ctx, wl, "FP64", steps64, args.warmup, nprof)
     if td:
         import torch
