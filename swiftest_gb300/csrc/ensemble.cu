@@ -1375,6 +1375,9 @@ int helio_step_groups(swg_ensemble *e, double dt) {
     const int64_t T = e->tsplit, M = e->NTP;
     unsigned *h0 = e->head + 1, *h1 = e->head + 2;
     SWG_TRY(kick_vb_pl(e, dth, 1));
+    // the pl-tp kick's tile shape is timed here, on this stream, before the side streams run
+    // beside it (as in the sequential step, which tunes at the same point)
+    SWG_TRY(ensure_kick_plan(e, 1, false, e->head, nullptr, 0));
     SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
     SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
     SWG_TRY(on_stream(c, e->side, [&] {
@@ -1422,6 +1425,7 @@ int helio_step_split(swg_ensemble *e, double dt) {
     if (e->precision == SWG_MIXED && e->tgroup && e->tsplit > 0 && e->tsplit < e->NTP)
         return helio_step_groups(e, dt);
     SWG_TRY(kick_vb_pl(e, dth, 1));
+    if (e->precision == SWG_MIXED) SWG_TRY(ensure_kick_plan(e, 1, false, e->head, nullptr, 0));  // see above
     SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
     SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
     SWG_TRY(on_stream(c, e->side, [&] {
