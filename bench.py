@@ -62,15 +62,37 @@ def parse():
 
 
 def dist_setup(args):
+    """Ranks of a torchrun launch: one independent replica of the workload per GPU (the
+    ensemble shards by system with no exchange), joined only by a gloo barrier and the max
+    of the timings.  --gpus must equal the launch's WORLD_SIZE."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.gpus != world:
+        raise SystemExit(f"--gpus {args.gpus} but WORLD_SIZE={world}: launch N>1 with "
+                         f"python -m torch.distributed.run --nproc-per-node {args.gpus} bench.py --gpus {args.gpus}")
     pg = None
     if world > 1:
         import torch.distributed as td
         td.init_process_group(backend="gloo")
         pg = td
     return world, rank, local, pg
+
+
+def max_over_ranks(td, values):
+    """The slowest rank's time for each entry of `values` (ms); identity without a group."""
+    if td is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def whole_job_rate(world, units_per_rank, steps, ms):
+    """Units per second of the whole job: every rank processed units_per_rank per step, and
+    the job took the slowest rank's time."""
+    return world * units_per_rank * steps / (ms * 1e-3)
 
 
 # ---------------------------------------------------------------- workloads
@@ -448,15 +470,11 @@ def main():
                                                                 clocks=clocks)
     steps64 = args.steps  # same steps as the mixed arm, so the two |dE/E| are over the same run
     ms_fp64, _, (prof64, _), err_f, st_f = run_path(ctx, wl, "FP64", steps64, args.warmup, nprof)
-    if td:
-        import torch
-        t = torch.tensor([ms_mixed, ms_fp64], dtype=torch.float64)
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        ms_mixed, ms_fp64 = float(t[0]), float(t[1])
     e2e_ms, e2e_bytes = run_e2e(ctx, wl, "MIXED", args.steps)
+    ms_mixed, ms_fp64, e2e_ms = max_over_ranks(td, [ms_mixed, ms_fp64, e2e_ms])
     nb = wl.nbodies
-    value = world * nb * args.steps / (ms_mixed * 1e-3)
-    fp64_value = world * nb * steps64 / (ms_fp64 * 1e-3)
+    value = whole_job_rate(world, nb, args.steps, ms_mixed)
+    fp64_value = whole_job_rate(world, nb, steps64, ms_fp64)
 
     # roofline of the pair kick (mixed path), from the live CUDA-event profile on the library's stream
     peak32 = ctx.probe_peak_tflops("fp32")
@@ -490,12 +508,12 @@ def main():
                                          for k, v in prof64.items()}},
         "mixed_path": {**err_summary(*err_m), "stats": st_m},
         "speedup_mixed_vs_fp64": value / fp64_value,
-        "pair_interactions_per_s": world * wl.pairs_per_step * args.steps / (ms_mixed * 1e-3),
+        "pair_interactions_per_s": whole_job_rate(world, wl.pairs_per_step, args.steps, ms_mixed),
         "kernel_profile": kernel_profile, "dominant_kernel_class": dom,
         "roofline": roof, "fp64_peak_probe_tflops": peak64,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
-        "e2e": {"value": world * nb * args.steps / (e2e_ms * 1e-3), "unit": UNIT,
+        "e2e": {"value": whole_job_rate(world, nb, args.steps, e2e_ms), "unit": UNIT,
                 "h2d_bytes_per_step": e2e_bytes // 2, "d2h_bytes_per_step": e2e_bytes // 2},
         "gpu_launches": int(launches),
     }

@@ -1,6 +1,6 @@
 """Long-run accuracy of the mixed-precision batched path against the FP64 path.
 
-    python -m swiftest_gb300.accuracy [--nsys N] [--steps S] [--every K] [--full-mixed]
+    python benchmarks/accuracy.py [--nsys N] [--steps S] [--every K] [--full-mixed]
 
 Steps the first N systems of the C4 ensemble (256 planetesimal disks, SyMBA, dt = 0.002 yr,
 1-Hill-radius encounter radius) for S steps in both precisions from the same initial

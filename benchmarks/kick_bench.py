@@ -1,6 +1,6 @@
 """Standalone pair-kick benchmark (large single systems) through the C ABI with device pointers.
 
-    python -m swiftest_gb300.kick_bench [--n 16384 65536 131072] [--reps 3]
+    python benchmarks/kick_bench.py [--n 16384 65536 131072] [--reps 3]
 
 For each N: N massive bodies (masses log-uniform in [1e-12, 1e-8] Msun, a in [0.5, 5] AU,
 seed 0) and 4N test particles; one evaluation of

@@ -1,6 +1,6 @@
 """Run one hot-path kernel on a C1-shaped workload, for profilers (ncu) and quick timing.
 
-    python -m swiftest_gb300.profile_cases <case> [--npl N] [--ntp M] [--reps R]
+    python benchmarks/profile_cases.py <case> [--npl N] [--ntp M] [--reps R]
 
 cases: kick_tp_mixed, kick_pl_mixed, kick_tp_fp64, kick_pl_fp64, drift, encounter_pltp,
 encounter_plpl, symba_mixed, symba_fp64 (inputs: the seeded C1 disk, AU, Msun, yr), and

@@ -70,14 +70,22 @@ int swg_kick_getacch_int_all_flat_pl(swg_ctx *ctx, int32_t npl, int32_t nplm, in
                                      const double *r, const double *Gmass, const double *radius, double *acc,
                                      int precision, int mem);
 
-/* Same computation as swg_kick_getacch_int_all_tri_pl with SWG_MIXED, for callers that
- * must not allocate device memory (an integrator recorded into a CUDA graph, or an
- * application that owns every allocation in a fixed pool): it calls no cudaMalloc or
- * cudaFree and takes device pointers and a cudaStream_t.  It has no counterpart in
- * the reference.  Its scratch is one 4 MiB device array per GPU, held until exit and
- * shared by all calls: calls that overlap on the GPU race; npl above
- * SWG_NOALLOC_MAX_NPL is rejected with SWG_ERR_ARG.  The first call on a device
- * resolves the array's address; make it before any stream capture. */
+/* The mixed-precision pl-pl kick of swg_kick_getacch_int_all_tri_pl (SWG_MIXED) for callers
+ * that cannot allocate device memory while they run: an application that owns every
+ * device allocation in a fixed pool sized at start-up, or host code whose step is
+ * recorded into a CUDA graph, where cudaMalloc/cudaFree are not allowed and can
+ * synchronize the device.  It has no counterpart in the reference.  It calls no
+ * cudaMalloc or cudaFree, takes device pointers and a cudaStream_t, and accumulates into
+ * acc like the regular entry point.  It runs the regular entry point's broadcast kernel
+ * on the same grid, so its results are the same bits wherever that entry point takes the
+ * broadcast kernel (nplm < npl, or npl below about 12,000 on GB300); above that the regular
+ * entry point switches to its symmetric kernel and the two agree within the mixed-kick
+ * tolerance (per-body relative error 2e-5), not bit for bit.  Its scratch is one fixed
+ * 16 MiB device array per GPU, held until exit and shared by all calls: it keeps the last
+ * call's contents, the counters are cleared at the start of each call, and calls that
+ * overlap on the GPU race.  npl above SWG_NOALLOC_MAX_NPL is rejected with SWG_ERR_ARG.
+ * The first call on a device resolves the array's address: make it before any stream
+ * capture (a first call on a capturing stream returns SWG_ERR_STATE). */
 #define SWG_NOALLOC_MAX_NPL 1048576
 int swg_kick_getacch_int_all_tri_pl_noalloc(int32_t npl, int32_t nplm, const double *r, const double *Gmass,
                                             const double *radius, double *acc, void *stream);

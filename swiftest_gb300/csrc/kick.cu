@@ -486,15 +486,17 @@ int ensure_kick_scratch(swg_ctx *c, DevBuf &buf, size_t bytes) {
 
 // Chooses the partner split so that the grid covers ~8 blocks (32 warps) per SM: the
 // pair loop is latency-bound (rsqrt and dependent FMAs), so occupancy hides it.
-int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart) {
+int kick_mixed_nchunk(int num_sms, int nrecv, int npart) {
     const int bx = div_up(nrecv, MBLOCK);
-    const int target = 8 * (c->num_sms > 0 ? c->num_sms : 152);
+    const int target = 8 * (num_sms > 0 ? num_sms : 152);
     int nchunk = div_up(target, bx);
     const int maxchunk = div_up(npart, MT);  // at least one tile per chunk
     if (nchunk > maxchunk) nchunk = maxchunk;
     if (nchunk < 1) nchunk = 1;
     return nchunk;
 }
+
+int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart) { return kick_mixed_nchunk(c->num_sms, nrecv, npart); }
 
 int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const double *rrecv, const double *rpart,
                       const double *Gm, const double *R, const int32_t *lmask, double *acc, int acc_is_zero,
@@ -525,41 +527,35 @@ int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const
     return launch_status(c, "kick_mixed");
 }
 
-// Mixed pl-pl kick on a caller's stream with caller-provided scratch (counters first,
-// then partials); used by the entry point that allocates nothing (kick_noalloc.cu).
-// Same chunking and kernel as kick_mixed_launch.
-cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, int num_sms, int npl, int nplm, const double *r,
-                                      const double *Gm, const double *R, double *acc, void *scratch,
-                                      size_t counter_bytes) {
-    if (npl <= 0) return cudaSuccess;
-    const int bx = div_up(npl, MBLOCK);
-    const int target = 2 * (num_sms > 0 ? num_sms : 152);
-    int nchunk = div_up(target, bx);
-    const int maxchunk = div_up(npl, MT);
-    if (nchunk > maxchunk) nchunk = maxchunk;
-    if (nchunk < 1) nchunk = 1;
-    int chunk = div_up(npl, nchunk);
-    chunk = div_up(chunk, MT) * MT;
-    nchunk = div_up(npl, chunk);
-    unsigned *counters = (unsigned *)scratch;
-    float *partial = (float *)((char *)scratch + counter_bytes);
-    dim3 grid(bx, nchunk);
-    launch_mixed_plpl(grid, stream, npl, nplm, r, Gm, R, acc, 0, chunk, partial, counters, nullptr, nullptr);
-    return cudaGetLastError();
+// Grid of the mixed pl-pl kick of one system: bx receiver blocks by nchunk partner chunks
+// of `chunk` partners, exactly as kick_mixed_launch derives it from kick_mixed_chunks.
+// partials = float-float partial-sum entries (6 floats each) the launch writes, 0 when
+// there is one chunk.
+MixedPlplGrid kick_mixed_plpl_grid(int num_sms, int npl) {
+    MixedPlplGrid g{0, 1, 0, 0};
+    if (npl <= 0) return g;
+    g.bx = div_up(npl, MBLOCK);
+    const int nch = kick_mixed_nchunk(num_sms, npl, npl);
+    g.chunk = div_up(div_up(npl, nch), MT) * MT;
+    g.nchunk = div_up(npl, g.chunk);
+    g.partials = g.nchunk > 1 ? (int64_t)g.nchunk * npl : 0;
+    return g;
 }
 
-// largest partial-sum footprint (nchunk * npl entries) the launcher above can request
-int64_t kick_mixed_plpl_partials_max(int num_sms, int npl) {
-    const int bx = div_up(npl, MBLOCK);
-    const int target = 2 * (num_sms > 0 ? num_sms : 152);
-    int nchunk = div_up(target, bx);
-    const int maxchunk = div_up(npl, MT);
-    if (nchunk > maxchunk) nchunk = maxchunk;
-    if (nchunk < 1) nchunk = 1;
-    int chunk = div_up(npl, nchunk);
-    chunk = div_up(chunk, MT) * MT;
-    nchunk = div_up(npl, chunk);
-    return nchunk > 1 ? (int64_t)nchunk * npl : 0;
+// Mixed pl-pl kick on a caller's stream with caller-provided scratch (block counters
+// first, then partials); used by the entry point that allocates nothing
+// (kick_noalloc.cu).  Same grid and kernel as kick_mixed_launch; the partners are split
+// inside each tile instead of by k_kick_split, which gives the same floats, so the
+// accelerations are the same bits.
+cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, const MixedPlplGrid &g, int npl, int nplm,
+                                      const double *r, const double *Gm, const double *R, double *acc, void *scratch,
+                                      size_t counter_bytes) {
+    if (npl <= 0) return cudaSuccess;
+    unsigned *counters = (unsigned *)scratch;
+    float *partial = (float *)((char *)scratch + counter_bytes);
+    dim3 grid(g.bx, g.nchunk);
+    launch_mixed_plpl(grid, stream, npl, nplm, r, Gm, R, acc, 0, g.chunk, partial, counters, nullptr, nullptr);
+    return cudaGetLastError();
 }
 
 // Split n partner bodies into float hi/lo tiles (A = x_hi, y_hi, z_hi, Gm; B = x_lo, y_lo, z_lo, R).

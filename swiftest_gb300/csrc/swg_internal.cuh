@@ -139,14 +139,19 @@ int kick_plpl_fp64(swg_ctx *c, int32_t npl, int32_t nplm, const double *r, const
 int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const double *rpl, const double *Gm,
                  const int32_t *lmask, double *acc, int acc_is_zero);
 size_t kick_mixed_scratch_bytes(int nrecv, int npart, int nchunk);
+int kick_mixed_nchunk(int num_sms, int nrecv, int npart);
 int kick_mixed_chunks(swg_ctx *c, int nrecv, int npart);
 int kick_mixed_launch(swg_ctx *c, bool tp, int nrecv, int npart, int nplm, const double *rrecv, const double *rpart,
                       const double *Gm, const double *R, const int32_t *lmask, double *acc, int acc_is_zero,
                       int nchunk, void *scratch);
-cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, int num_sms, int npl, int nplm, const double *r,
-                                      const double *Gm, const double *R, double *acc, void *scratch,
+struct MixedPlplGrid {
+    int bx, nchunk, chunk;
+    int64_t partials;  // float-float partial entries written (6 floats each), 0 with one chunk
+};
+MixedPlplGrid kick_mixed_plpl_grid(int num_sms, int npl);
+cudaError_t kick_mixed_plpl_on_stream(cudaStream_t stream, const MixedPlplGrid &g, int npl, int nplm,
+                                      const double *r, const double *Gm, const double *R, double *acc, void *scratch,
                                       size_t counter_bytes);
-int64_t kick_mixed_plpl_partials_max(int num_sms, int npl);
 // explicit 1-based pair list (k_plpl(2,n) or separate i1/i2); ahi_ahj: 6*npl doubles of scratch
 // sign > 0: acc = (acc + ahi) + ahj ; sign < 0: acc = acc - (ahi + ahj)
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,

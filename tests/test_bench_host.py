@@ -51,3 +51,47 @@ def test_reference_arm_line():
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "body-steps/s"
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def _rank_worker(rank, world, port, q):
+    import os
+    import torch.distributed as td
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    td.init_process_group("gloo", rank=rank, world_size=world)
+    td.barrier()
+    # rank r took (r + 1) * 10 ms for its mixed steps and 5 ms for its FP64 steps
+    ms = bench.max_over_ranks(td, [10.0 * (rank + 1), 5.0])
+    q.put((rank, ms, bench.whole_job_rate(world, 1000, 4, ms[0])))
+    td.destroy_process_group()
+
+
+def test_replicas_take_the_slowest_rank_gloo():
+    """--gpus N runs N independent replicas (torchrun ranks, gloo): every rank sees the max of
+    the ranks' times, and the whole-job rate counts every rank's units over that time."""
+    import socket
+
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, ms, rate in res:
+        assert ms == [20.0, 5.0]
+        assert rate == 2 * 1000 * 4 / 20e-3
+
+
+def test_gpus_must_match_world_size(monkeypatch):
+    import argparse
+    import pytest
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    with pytest.raises(SystemExit):
+        bench.dist_setup(argparse.Namespace(gpus=2))
+    assert bench.dist_setup(argparse.Namespace(gpus=1))[0] == 1

@@ -69,3 +69,27 @@ def test_python_binding_argument_counts():
     assert protos
     wrong = {n: (k, len(_lib.SIGNATURES[n][1])) for n, k in protos.items() if len(_lib.SIGNATURES[n][1]) != k}
     assert not wrong, wrong
+
+
+def _fortran_interfaces():
+    """bind(C) name -> number of dummy arguments, from fortran/swiftest_gb300_mod.f90."""
+    text = (ROOT / "fortran" / "swiftest_gb300_mod.f90").read_text()
+    text = re.sub(r"!.*", "", text)
+    text = re.sub(r"&\s*\n\s*", " ", text)  # join continuation lines
+    out = {}
+    for m in re.finditer(r"function\s+(\w+)\s*\(([^)]*)\)\s*bind\(C,\s*name=\"(\w+)\"\)", text):
+        args = m.group(2).strip()
+        out[m.group(3)] = 0 if not args else args.count(",") + 1
+    return out
+
+
+def test_fortran_module_matches_header():
+    """The maintainer's iso_c_binding module (not compiled here: no Fortran compiler) names
+    declared entry points only, each with the header's number of arguments."""
+    protos = _prototypes()
+    fort = _fortran_interfaces()
+    assert len(fort) >= 40
+    unknown = sorted(n for n in fort if n not in protos)
+    assert not unknown, unknown
+    wrong = {n: (k, protos[n]) for n, k in fort.items() if protos[n] != k}
+    assert not wrong, wrong
