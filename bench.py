@@ -327,20 +327,27 @@ class _Null:
 
 
 def rel_energy(e0, e1):
-    """|dE/E| (heliocentric central-body potential and the reference's formula) and |dL/L|,
-    as arrays over systems (one entry for a single system)."""
+    """Relative energy and angular-momentum errors between two energy snapshots, as arrays over
+    systems (one entry for a single system), with the reference's collision bookkeeping
+    (swiftest_io.f90:153,181-183): the energy the collision resolutions changed (E_collisions)
+    is taken out of dE, and dL_ref adds the angular momentum booked as escaped (L_escape).
+    dE uses the central-body potential at the heliocentric distance, dE_ref the reference's
+    own formula (barycentric distance)."""
     def arr(x):
         return np.atleast_1d(np.asarray(x, dtype=np.float64))
-    dE = np.abs(arr(e1["te_helio"]) - arr(e0["te_helio"])) / np.abs(arr(e0["te_helio"]))
-    dEr = np.abs(arr(e1["te"]) - arr(e0["te"])) / np.abs(arr(e0["te"]))
+    Ec = arr(e1.get("E_collisions", 0.0)) - arr(e0.get("E_collisions", 0.0))
+    dE = np.abs(arr(e1["te_helio"]) - arr(e0["te_helio"]) - Ec) / np.abs(arr(e0["te_helio"]))
+    dEr = np.abs(arr(e1["te"]) - arr(e0["te"]) - Ec) / np.abs(arr(e0["te"]))
     L0, L1 = np.atleast_2d(e0["L"]), np.atleast_2d(e1["L"])
+    esc = np.atleast_2d(e1.get("L_escape", np.zeros(3))) - np.atleast_2d(e0.get("L_escape", np.zeros(3)))
     dL = np.linalg.norm(L1 - L0, axis=1) / np.linalg.norm(L0, axis=1)
-    return dE, dEr, dL
+    dLr = np.linalg.norm(L1 + esc - L0, axis=1) / np.linalg.norm(L0, axis=1)
+    return dE, dEr, dL, dLr
 
 
-def err_summary(dE, dEr, dL):
+def err_summary(dE, dEr, dL, dLr):
     return {"dE_E_max": float(dE.max()), "dE_E_median": float(np.median(dE)), "dE_E_ref_formula_max": float(dEr.max()),
-            "dL_L_max": float(dL.max())}
+            "dL_L_max": float(dL.max()), "dL_L_ref_formula_max": float(dLr.max())}
 
 
 def run_path(ctx, wl, precision, steps, warmup, prof_steps=0, clocks=None):

@@ -26,9 +26,10 @@ if str(ROOT) not in sys.path:
 
 
 def _errors(e0, e1):
-    dE = np.abs(e1["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
-    dEr = np.abs(e1["te"] - e0["te"]) / np.abs(e0["te"])
-    dL = np.linalg.norm(e1["L"] - e0["L"], axis=1) / np.linalg.norm(e0["L"], axis=1)
+    """|dE/E| (heliocentric central-body potential; and the reference's formula) and |dL/L|
+    per system, with the collision bookkeeping taken out as bench.rel_energy does."""
+    from bench import rel_energy
+    dE, dEr, dL, _ = rel_energy(e0, e1)
     return dE, dEr, dL
 
 

@@ -228,6 +228,12 @@ module swiftest_gb300_mod
          type(c_ptr), value :: sys
          real(c_double), intent(out) :: out(*)
       end function
+      !! out(4): E_collisions, L_escape(3) (G*m units)
+      integer(c_int) function swg_system_collision_terms(sys, out) bind(C, name="swg_system_collision_terms")
+         import :: c_ptr, c_int, c_double
+         type(c_ptr), value :: sys
+         real(c_double), intent(out) :: out(*)
+      end function
       integer(c_int) function swg_system_stats(sys, out) bind(C, name="swg_system_stats")
          import :: c_ptr, c_int, c_int64_t
          type(c_ptr), value :: sys
@@ -318,6 +324,11 @@ module swiftest_gb300_mod
          integer(c_int32_t), intent(out) :: status(*)
       end function
       integer(c_int) function swg_ensemble_energy(ens, out) bind(C, name="swg_ensemble_energy")
+         import :: c_ptr, c_int, c_double
+         type(c_ptr), value :: ens
+         real(c_double), intent(out) :: out(*)
+      end function
+      integer(c_int) function swg_ensemble_collision_terms(ens, out) bind(C, name="swg_ensemble_collision_terms")
          import :: c_ptr, c_int, c_double
          type(c_ptr), value :: ens
          real(c_double), intent(out) :: out(*)

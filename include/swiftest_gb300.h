@@ -147,6 +147,14 @@ int swg_system_get_tp(swg_system *sys, double *rh, double *vh, int32_t *status);
  * potential uses the body's barycentric distance), then te_helio: the same total with the
  * central-body potential at the heliocentric distance. */
 int swg_system_energy(swg_system *sys, double *out);
+/* out[4]: the collision bookkeeping of swiftest_nbody_system (swiftest_module.f90:375-377):
+ * E_collisions, the energy change of the collision resolutions (collision_resolve.f90:634-638),
+ * and L_escape (x, y, z), the impactors' pre-collision orbital angular momentum
+ * (collision_generate.f90:218-220), since initialize.  Masses enter as G*m, so both are G
+ * times the reference's, like every value of swg_system_energy.  The reference's error
+ * terms (swiftest_io.f90:153,181-183) follow: |dE/E| = |te - te0 - E_collisions| / |te0|,
+ * |dL/L| = |L + L_escape - L0| / |L0|. */
+int swg_system_collision_terms(swg_system *sys, double *out);
 /* out[6]: steps with encounters, max recursion depth, sum plpl enc, sum pltp enc, collisions
  * resolved plus test particles removed by the close-approach discard scan, recursion
  * sub-steps executed */
@@ -203,6 +211,8 @@ int swg_ensemble_get_pl(swg_ensemble *ens, double *rh, double *vh, int32_t *stat
 int swg_ensemble_get_tp(swg_ensemble *ens, double *rh, double *vh, int32_t *status);
 /* out[9*nsys]: per system the nine values of swg_system_energy */
 int swg_ensemble_energy(swg_ensemble *ens, double *out);
+/* out[4*nsys]: per system the four values of swg_system_collision_terms */
+int swg_ensemble_collision_terms(swg_ensemble *ens, double *out);
 /* out[6] over all systems: system-steps with encounters, max recursion depth, sum plpl
  * enc, sum pltp enc, collisions, recursion sub-steps */
 int swg_ensemble_stats(swg_ensemble *ens, int64_t *out);

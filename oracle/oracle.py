@@ -69,6 +69,7 @@ _SIG = {
     "orc_system_get_tp": (None, [_P, _P, _P, _P]),
     "orc_system_energy": (None, [_P, _P]),
     "orc_system_stats": (None, [_P, _P]),
+    "orc_system_collision_terms": (None, [_P, _P]),
     "orc_system_plpl_list": (_I64, [_P, _I64, _P, _P]),
     "orc_system_pltp_list": (_I64, [_P, _I64, _P, _P]),
 }
@@ -272,8 +273,10 @@ class OracleSystem:
     def energy(self):
         out = np.zeros(9)
         self.lib.orc_system_energy(self.h, _p(out))
+        ct = np.zeros(4)
+        self.lib.orc_system_collision_terms(self.h, _p(ct))
         return {"te": out[0], "ke": out[1], "pe": out[2], "be": out[3], "L": out[4:7].copy(), "GMtot": out[7],
-                "te_helio": out[8]}
+                "te_helio": out[8], "E_collisions": ct[0], "L_escape": ct[1:4].copy()}
 
     def stats(self):
         out = np.zeros(6, np.int64)

@@ -1252,6 +1252,9 @@ struct orc_system {
     int lfirst_pl, lfirst_tp, lfirstkick;
     int irec;
     double t;
+    /* collision bookkeeping (swiftest_module.f90:375-377, collision_generate.f90:219,
+     * collision_resolve.f90:638), in G*m units */
+    double E_collisions, L_escape[3];
     enclist plpl, pltp;
     int64_t stats[6];
     int64_t last_plpl_n, last_pltp_n;
@@ -2100,10 +2103,11 @@ static int collision_check_one(double xr, double yr, double zr, double vxr, doub
     return 0;
 }
 
-/* collision_check_plpl / _pltp (src/collision/collision_check.f90:60-271): ACTIVE pairs
- * whose pl (pl-pl: index1) or tp (pl-tp: index2) is at level >= irec; a colliding pair's
- * status becomes COLLIDED.  Returns whether any pair collided. */
-static int symba_collision_check(orc_system *s, int irec, double dt) {
+/* collision_check_plpl (src/collision/collision_check.f90:60-160): ACTIVE pairs whose
+ * index1 body sits at level >= irec; a colliding pair's status becomes COLLIDED and both of
+ * its bodies are flagged (the reference sets their status to COLLIDED).  Returns whether
+ * any pair collided. */
+static int collision_check_plpl(orc_system *s, int irec, double dt, unsigned char *coll) {
     int any = 0;
     for (int64_t k = 0; k < s->plpl.n; k++) {
         if (s->plpl.status[k] != ST_ACTIVE) continue;
@@ -2117,9 +2121,17 @@ static int symba_collision_check(orc_system *s, int irec, double dt) {
         if (collision_check_one(x[0], x[1], x[2], v[0], v[1], v[2], s->Gmass[i] + s->Gmass[j],
                                 s->radius[i] + s->radius[j], dt, s->plpl.lvdotr[k] != 0)) {
             s->plpl.status[k] = ST_COLLIDED;
+            if (coll) coll[i] = coll[j] = 1;
             any = 1;
         }
     }
+    return any;
+}
+
+/* collision_check_pltp (src/collision/collision_check.f90:163-271): ACTIVE pairs whose tp
+ * sits at level >= irec. */
+static int collision_check_pltp(orc_system *s, int irec, double dt) {
+    int any = 0;
     for (int64_t k = 0; k < s->pltp.n; k++) {
         if (s->pltp.status[k] != ST_ACTIVE) continue;
         int32_t i = s->pltp.i1[k] - 1, j = s->pltp.i2[k] - 1;
@@ -2138,23 +2150,284 @@ static int symba_collision_check(orc_system *s, int irec, double dt) {
     return any;
 }
 
-/* Resolution of the COLLIDED pairs by perfect merging (collision_resolve_plpl / _pltp,
- * collision_resolve.f90:521-695, with collision_generate_merge, collision_generate.f90:158-260):
- * a pl-tp collision discards the tp; a pl-pl pair becomes one body in the slot of the more
- * massive one, with the summed G*m, the radius of the summed volume, the centre-of-mass
- * position and velocity, and the Hill radius of its new orbit (swiftest_util_set_rhill,
- * swiftest_util.f90:2260-2280).  Removed bodies stay in their slots with status INACTIVE,
- * zero G*m, radius, Hill radius and velocity, parked at a distant position of their own
- * (the reference removes them from its arrays); list entries naming a removed body are
- * redirected to the merged body and self-pairs made INACTIVE.  Not restated: the torque
- * that removes the residual angular momentum, the collision energy bookkeeping, cascades
- * and the re-sort by mass. */
+/* ---- Resolution of the COLLIDED pairs by perfect merging.
+ *
+ * collision_resolve_plpl (src/collision/collision_resolve.f90:521-662) with the MERGE model
+ * (collision_generate_merge, collision_generate.f90:158-260; collision_resolve_mergeaddsub,
+ * collision_resolve.f90:326-518) and the parts of swiftest_util_rearray_pl
+ * (swiftest_util.f90:1638-1808) that change the state, then collision_resolve_pltp
+ * (:665-695).  Energy tracking is on, as in runs that report |dE/E|, and masses are G*m (the
+ * reference's m = G*m/GU with GU = 1), so energies and angular momenta are G times the
+ * reference's and every ratio is unchanged.  Per resolution:
+ *   1. sync: the central body's barycentric velocity (vb2vh, reverse order) and position
+ *      (rh2rb, which also gives every body's rb);
+ *   2. E_before, L_before: the system's energy and angular momentum;
+ *   3. each COLLIDED pair whose two bodies were both flagged by the check, in list order:
+ *      the impactors' centre of mass (rb = rh + cb rb), the angular momentum of each
+ *      impactor about it, L_escape += both (no rotation: the reference books the
+ *      pre-collision orbital angular momentum as escaped), the merged body at the centre of
+ *      mass with the summed G*m and the radius of the summed volume, its velocity torqued by
+ *      the impactors' angular momentum (collision_util_velocity_torque), list entries of the
+ *      removed body redirected to the merged one (a resulting self-pair becomes INACTIVE);
+ *   4. the Hill radius of every body from its current orbit (set_rhill in rearray);
+ *   5. the new system angular momentum: each merged body's velocity is torqued by
+ *      -(L_after - L_before) * m / (sum of the merged masses), then E_collisions +=
+ *      E_after - E_before (E_before stays the value of step 2 through a cascade, as in the
+ *      reference);
+ *   6. the cascade: the pl-pl list is checked again at the same level (newly collided pairs
+ *      flag their bodies); repeat from 3 while any pair collides, at most 1000 times.
+ * The merged body keeps the slot of the more massive impactor (the first on a tie); the
+ * other stays in its slot with status INACTIVE, zero G*m, radius, Hill radius and
+ * velocity, parked at a distant position of its own.  Not restated: the re-sort by mass
+ * and the re-run of the encounter checks inside rearray (whose old and new lists are
+ * matched entry by entry), and the kinship grouping of a body that collides with two
+ * others in one check (the reference merges all three at once; here the first pair merges,
+ * the other pair is set ACTIVE again and merges in the cascade if it still collides).
+ * Returns -1 on a runaway cascade, else the number of merges plus discarded tp. */
 static void park(double *r, double *v, int64_t k) {
     r[0] = 1.0e6 + (double)k;
     r[1] = r[2] = 0.0;
     v[0] = v[1] = v[2] = 0.0;
 }
-static void symba_resolve_collisions(orc_system *s) {
+
+/* operator .unit. (src/operator/operator_unit.f90) */
+static void unit3(const double *a, double *u) {
+    double m = norm2_3(a);
+    for (int d = 0; d < 3; d++) u[d] = m > 2.2250738585072014e-308 ? a[d] / m : 0.0;
+}
+
+/* operator .cross. (src/operator/operator_cross.f90) */
+static void cross3(const double *a, const double *b, double *c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* collision_util_velocity_torque (src/collision/collision_util.f90:1001-1026) */
+static void velocity_torque(const double *dL, double mass, const double *r, double *v) {
+    double dLu[3], ru[3], q[3], c[3];
+    unit3(dL, dLu);
+    unit3(r, ru);
+    double rmag = norm2_3(r), vmag = norm2_3(v);
+    for (int d = 0; d < 3; d++) q[d] = dL[d] / (rmag * mass);
+    double vapply_mag = norm2_3(q);
+    if (vapply_mag / vmag > 2.220446049250313e-16) {
+        cross3(dLu, ru, c);
+        for (int d = 0; d < 3; d++) v[d] = v[d] + vapply_mag * c[d];
+    }
+}
+
+/* swiftest_orbel_xv2el (src/swiftest/swiftest_orbel.f90:913-1072): the semimajor axis */
+static double xv2el_a(double mu, const double *r, const double *v) {
+    const double TINYV = 4.0e-15;
+    double hx = r[1] * v[2] - r[2] * v[1], hy = r[2] * v[0] - r[0] * v[2], hz = r[0] * v[1] - r[1] * v[0];
+    double h2 = hx * hx + hy * hy + hz * hz;
+    if (h2 <= 10.0 * 2.2250738585072014e-308) return 0.0;
+    double rr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double energy = 0.5 * v2 - mu / rr;
+    if (fabs(energy * rr / mu) < sqrt(TINYV)) return 0.5 * h2 / mu; /* parabola */
+    double a = -0.5 * mu / energy;
+    if (a < 0.0 && !(-h2 / (mu * a) > TINYV)) return 0.5 * h2 / mu; /* parabola */
+    return a;
+}
+
+/* swiftest_util_get_energy_and_momentum_system (swiftest_util.f90:1172-1291, triangular
+ * potential :1350-1401) as the resolution calls it: body positions rb, velocities vb, the
+ * central body's rb/vb as the resolution's sync left them, no spin terms. */
+static void resolve_energy(const orc_system *s, const double *rb, const double *cbrb, const double *cbvb,
+                           double *te, double *L) {
+    int32_t n = s->npl;
+    double mcb = s->GMcb;
+    double kecb = mcb * (cbvb[0] * cbvb[0] + cbvb[1] * cbvb[1] + cbvb[2] * cbvb[2]);
+    double Lcb[3] = {mcb * (cbrb[1] * cbvb[2] - cbrb[2] * cbvb[1]), mcb * (cbrb[2] * cbvb[0] - cbrb[0] * cbvb[2]),
+                     mcb * (cbrb[0] * cbvb[1] - cbrb[1] * cbvb[0])};
+    double kesum = 0.0, Lsum[3] = {0.0, 0.0, 0.0};
+    for (int32_t i = 0; i < n; i++) {
+        if (s->status[i] == ST_INACTIVE) continue;
+        const double *r = &rb[3 * i], *v = &s->vb[3 * i];
+        double m = s->Gmass[i];
+        Lsum[0] = Lsum[0] + m * (r[1] * v[2] - r[2] * v[1]);
+        Lsum[1] = Lsum[1] + m * (r[2] * v[0] - r[0] * v[2]);
+        Lsum[2] = Lsum[2] + m * (r[0] * v[1] - r[1] * v[0]);
+        kesum = kesum + m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    }
+    double pe = 0.0;
+    for (int32_t i = 0; i < n; i++) {
+        if (s->status[i] == ST_INACTIVE) continue;
+        double row = 0.0;
+        for (int32_t j = i + 1; j < n; j++) {
+            if (s->status[j] == ST_INACTIVE) continue;
+            double d[3] = {rb[3 * i] - rb[3 * j], rb[3 * i + 1] - rb[3 * j + 1], rb[3 * i + 2] - rb[3 * j + 2]};
+            row = row + (-(s->Gmass[i] * s->Gmass[j]) / norm2_3(d));
+        }
+        pe = pe + row;
+    }
+    double pecb = 0.0, be = 0.0;
+    for (int32_t i = 0; i < n; i++) {
+        if (s->status[i] == ST_INACTIVE) continue;
+        pecb = pecb + (-s->GMcb * s->Gmass[i] / norm2_3(&rb[3 * i]));
+        be = be + (-3.0 * s->Gmass[i] * s->Gmass[i] / (5.0 * s->radius[i]));
+    }
+    pe = pe + pecb;
+    double ke = 0.5 * (kecb + kesum);
+    *te = ke + pe + be;
+    for (int d = 0; d < 3; d++) L[d] = Lcb[d] + Lsum[d];
+}
+
+/* swiftest_util_coord_rh2rb_pl (swiftest_util.f90:488-521) into cbrb and rb */
+static void resolve_rh2rb(const orc_system *s, double *cbrb, double *rb) {
+    double Gmtot = s->GMcb, xtmp[3] = {0.0, 0.0, 0.0};
+    for (int32_t i = 0; i < s->npl; i++) {
+        if (s->status[i] == ST_INACTIVE) continue;
+        Gmtot = Gmtot + s->Gmass[i];
+        for (int d = 0; d < 3; d++) xtmp[d] = xtmp[d] + s->Gmass[i] * s->rh[3 * i + d];
+    }
+    for (int d = 0; d < 3; d++) cbrb[d] = -xtmp[d] / Gmtot;
+    for (int32_t i = 0; i < s->npl; i++) {
+        if (s->status[i] == ST_INACTIVE) continue;
+        for (int d = 0; d < 3; d++) rb[3 * i + d] = s->rh[3 * i + d] + cbrb[d];
+    }
+}
+
+static int64_t resolve_plpl(orc_system *s, int irec, double dtl) {
+    int32_t n = s->npl;
+    int any = 0;
+    for (int64_t k = 0; k < s->plpl.n; k++) any |= s->plpl.status[k] == ST_COLLIDED;
+    if (!any) return 0;
+    unsigned char *coll = calloc((size_t)(n > 0 ? n : 1), 1);
+    double *rb = calloc((size_t)3 * (n > 0 ? n : 1), 8);
+    double *vh = calloc((size_t)3 * (n > 0 ? n : 1), 8);
+    int32_t *newb = malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    for (int64_t k = 0; k < s->plpl.n; k++)
+        if (s->plpl.status[k] == ST_COLLIDED) coll[s->plpl.i1[k] - 1] = coll[s->plpl.i2[k] - 1] = 1;
+    /* 1. sync: vb2vh (swiftest_util.f90:363-395; vh is not refreshed afterwards, the merged
+     * bodies get theirs from b2h) and rh2rb */
+    double cbvb[3] = {0.0, 0.0, 0.0}, cbrb[3];
+    for (int32_t b = n - 1; b >= 0; b--) {
+        if (s->status[b] == ST_INACTIVE) continue;
+        for (int d = 0; d < 3; d++) cbvb[d] = cbvb[d] - s->Gmass[b] * s->vb[3 * b + d] / s->GMcb;
+    }
+    for (int32_t b = 0; b < n; b++)
+        for (int d = 0; d < 3; d++) vh[3 * b + d] = s->vb[3 * b + d] - cbvb[d];
+    resolve_rh2rb(s, cbrb, rb);
+    /* 2. */
+    double E_before, L_before[3];
+    resolve_energy(s, rb, cbrb, cbvb, &E_before, L_before);
+    int64_t nres = 0;
+    for (int loop = 1;; loop++) {
+        /* 3. */
+        int32_t nnew = 0;
+        for (int64_t k = 0; k < s->plpl.n; k++) {
+            if (s->plpl.status[k] != ST_COLLIDED) continue;
+            int32_t i = s->plpl.i1[k] - 1, j = s->plpl.i2[k] - 1;
+            if (!coll[i] || !coll[j]) {
+                /* one impactor already merged in this pass: test the pair again */
+                if (s->status[i] != ST_INACTIVE && s->status[j] != ST_INACTIVE && i != j)
+                    s->plpl.status[k] = ST_ACTIVE;
+                continue;
+            }
+            double m1 = s->Gmass[i], m2 = s->Gmass[j], mtot = m1 + m2;
+            double rb1[3], rb2[3], rbcom[3], vbcom[3], rc1[3], rc2[3], vc1[3], vc2[3];
+            const double *vb1 = &s->vb[3 * i], *vb2 = &s->vb[3 * j];
+            for (int d = 0; d < 3; d++) {
+                rb1[d] = s->rh[3 * i + d] + cbrb[d];
+                rb2[d] = s->rh[3 * j + d] + cbrb[d];
+            }
+            for (int d = 0; d < 3; d++) {
+                rbcom[d] = (m1 * rb1[d] + m2 * rb2[d]) / mtot;
+                vbcom[d] = (m1 * vb1[d] + m2 * vb2[d]) / mtot;
+            }
+            for (int d = 0; d < 3; d++) {
+                rc1[d] = rb1[d] - rbcom[d];
+                rc2[d] = rb2[d] - rbcom[d];
+                vc1[d] = vb1[d] - vbcom[d];
+                vc2[d] = vb2[d] - vbcom[d];
+            }
+            double L1[3] = {m1 * (rc1[1] * vc1[2] - rc1[2] * vc1[1]), m1 * (rc1[2] * vc1[0] - rc1[0] * vc1[2]),
+                            m1 * (rc1[0] * vc1[1] - rc1[1] * vc1[0])};
+            double L2[3] = {m2 * (rc2[1] * vc2[2] - rc2[2] * vc2[1]), m2 * (rc2[2] * vc2[0] - rc2[0] * vc2[2]),
+                            m2 * (rc2[0] * vc2[1] - rc2[1] * vc2[0])};
+            double Lb[3];
+            for (int d = 0; d < 3; d++) {
+                Lb[d] = L1[d] + L2[d];
+                s->L_escape[d] = s->L_escape[d] + L1[d] + L2[d];
+            }
+            double PI = 3.141592653589793238462643383279502884197;
+            double Ri = s->radius[i], Rj = s->radius[j];
+            double volume = 4.0 / 3.0 * PI * (Ri * Ri * Ri + Rj * Rj * Rj);
+            double Rnew = pow(3.0 * volume / (4.0 * PI), THIRD);
+            /* the merged body's velocity, torqued by the residual -(0 - Lb) */
+            double vnew[3] = {vbcom[0], vbcom[1], vbcom[2]};
+            double dL[3] = {-(0.0 - Lb[0]), -(0.0 - Lb[1]), -(0.0 - Lb[2])};
+            velocity_torque(dL, mtot, rbcom, vnew);
+            int32_t keep = m2 > m1 ? j : i, gone = keep == i ? j : i;
+            for (int d = 0; d < 3; d++) {  /* collision_resolve_mergeaddsub: b2h of the new body */
+                rb[3 * keep + d] = rbcom[d];
+                s->rh[3 * keep + d] = rbcom[d] - cbrb[d];
+                s->vb[3 * keep + d] = vnew[d];
+                vh[3 * keep + d] = vnew[d] - cbvb[d];
+            }
+            s->Gmass[keep] = mtot;
+            s->radius[keep] = Rnew;
+            s->Gmass[gone] = 0.0;
+            s->radius[gone] = 0.0;
+            s->rhill[gone] = 0.0;
+            s->status[gone] = ST_INACTIVE;
+            s->lmask[gone] = 0;
+            park(&s->rh[3 * gone], &s->vb[3 * gone], gone);
+            coll[i] = coll[j] = 0;
+            for (int64_t m = 0; m < s->plpl.n; m++) {
+                if (s->plpl.i1[m] == gone + 1) s->plpl.i1[m] = keep + 1;
+                if (s->plpl.i2[m] == gone + 1) s->plpl.i2[m] = keep + 1;
+                if (s->plpl.i1[m] == s->plpl.i2[m]) s->plpl.status[m] = ST_INACTIVE;
+            }
+            for (int64_t m = 0; m < s->pltp.n; m++)
+                if (s->pltp.i1[m] == gone + 1) s->pltp.i1[m] = keep + 1;
+            newb[nnew++] = keep;
+            nres++;
+        }
+        if (nnew == 0) break;
+        double mnew = 0.0;
+        for (int32_t q = 0; q < nnew; q++) mnew = mnew + s->Gmass[newb[q]];
+        /* 4. */
+        if (s->GMcb > 2.2250738585072014e-308) {
+            for (int32_t b = 0; b < n; b++) {
+                if (s->status[b] == ST_INACTIVE) continue;
+                double a = xv2el_a(s->GMcb + s->Gmass[b], &s->rh[3 * b], &vh[3 * b]);
+                double scale = pow(s->Gmass[b] / s->GMcb / 3.0, THIRD);
+                s->rhill[b] = a > 0.0 ? a * scale : norm2_3(&s->rh[3 * b]) * scale;
+            }
+        }
+        /* 5. */
+        double E_after, L_after[3], dL[3];
+        resolve_energy(s, rb, cbrb, cbvb, &E_after, L_after);
+        for (int d = 0; d < 3; d++) dL[d] = L_after[d] - L_before[d];
+        for (int32_t q = 0; q < nnew; q++) {
+            int32_t b = newb[q];
+            double t[3] = {-dL[0] * s->Gmass[b] / mnew, -dL[1] * s->Gmass[b] / mnew, -dL[2] * s->Gmass[b] / mnew};
+            velocity_torque(t, s->Gmass[b], &rb[3 * b], &s->vb[3 * b]);
+        }
+        resolve_energy(s, rb, cbrb, cbvb, &E_after, L_after);
+        s->E_collisions = s->E_collisions + (E_after - E_before);
+        /* 6. */
+        if (!collision_check_plpl(s, irec, dtl, coll)) break;
+        if (loop == 1000) {
+            nres = -1;
+            break;
+        }
+        resolve_rh2rb(s, cbrb, rb);
+    }
+    free(coll);
+    free(rb);
+    free(vh);
+    free(newb);
+    return nres;
+}
+
+/* collision_resolve_pltp (collision_resolve.f90:665-695): the colliding tp is discarded */
+static int64_t resolve_pltp(orc_system *s) {
+    int64_t nres = 0;
     for (int64_t k = 0; k < s->pltp.n; k++) {
         if (s->pltp.status[k] != ST_COLLIDED) continue;
         int32_t j = s->pltp.i2[k] - 1;
@@ -2162,59 +2435,22 @@ static void symba_resolve_collisions(orc_system *s) {
         s->tstatus[j] = ST_INACTIVE;
         s->tlmask[j] = 0;
         park(&s->trh[3 * j], &s->tvb[3 * j], (int64_t)s->npl + j);
-        s->stats[4]++;
+        nres++;
     }
-    int have_cbvb = 0;
-    double cbvb[3] = {0.0, 0.0, 0.0};
-    for (int64_t k = 0; k < s->plpl.n; k++) {
-        if (s->plpl.status[k] != ST_COLLIDED) continue;
-        int32_t i = s->plpl.i1[k] - 1, j = s->plpl.i2[k] - 1;
-        if (i == j || s->status[i] == ST_INACTIVE || s->status[j] == ST_INACTIVE) continue;
-        if (!have_cbvb) { /* swiftest_util_coord_vb2vh_pl's sum, before the merges */
-            for (int32_t b = s->npl - 1; b >= 0; b--) {
-                if (s->status[b] == ST_INACTIVE) continue;
-                for (int d = 0; d < 3; d++) cbvb[d] = cbvb[d] - s->Gmass[b] * s->vb[3 * b + d] / s->GMcb;
-            }
-            have_cbvb = 1;
-        }
-        int32_t keep = s->Gmass[j] > s->Gmass[i] ? j : i, gone = keep == i ? j : i;
-        double Gi = s->Gmass[i], Gj = s->Gmass[j], Gtot = Gi + Gj;
-        double rnew[3], vnew[3], vh[3];
-        for (int d = 0; d < 3; d++) {
-            rnew[d] = (Gi * s->rh[3 * i + d] + Gj * s->rh[3 * j + d]) / Gtot;
-            vnew[d] = (Gi * s->vb[3 * i + d] + Gj * s->vb[3 * j + d]) / Gtot;
-            vh[d] = vnew[d] - cbvb[d];
-        }
-        double PI = 3.141592653589793238462643383279502884197;
-        double volume = 4.0 / 3.0 * PI *
-                        (s->radius[i] * s->radius[i] * s->radius[i] + s->radius[j] * s->radius[j] * s->radius[j]);
-        double Rnew = pow(3.0 * volume / (4.0 * PI), THIRD);
-        double a, e, q;
-        xv2aeq(s->GMcb + Gtot, rnew[0], rnew[1], rnew[2], vh[0], vh[1], vh[2], &a, &e, &q);
-        double scale = pow(Gtot / s->GMcb / 3.0, THIRD);
-        double rhill = a > 0.0 ? a * scale : sqrt(rnew[0] * rnew[0] + rnew[1] * rnew[1] + rnew[2] * rnew[2]) * scale;
-        for (int d = 0; d < 3; d++) {
-            s->rh[3 * keep + d] = rnew[d];
-            s->vb[3 * keep + d] = vnew[d];
-        }
-        s->Gmass[keep] = Gtot;
-        s->radius[keep] = Rnew;
-        s->rhill[keep] = rhill;
-        s->Gmass[gone] = 0.0;
-        s->radius[gone] = 0.0;
-        s->rhill[gone] = 0.0;
-        s->status[gone] = ST_INACTIVE;
-        s->lmask[gone] = 0;
-        park(&s->rh[3 * gone], &s->vb[3 * gone], gone);
-        for (int64_t m = 0; m < s->plpl.n; m++) {
-            if (s->plpl.i1[m] == gone + 1) s->plpl.i1[m] = keep + 1;
-            if (s->plpl.i2[m] == gone + 1) s->plpl.i2[m] = keep + 1;
-            if (s->plpl.i1[m] == s->plpl.i2[m]) s->plpl.status[m] = ST_INACTIVE;
-        }
-        for (int64_t m = 0; m < s->pltp.n; m++)
-            if (s->pltp.i1[m] == gone + 1) s->pltp.i1[m] = keep + 1;
-        s->stats[4]++;
+    return nres;
+}
+
+/* the collision step of symba_step_recur_system (symba_step.f90:242-249) */
+static int symba_collisions(orc_system *s, int irec, double dtl) {
+    int a = collision_check_plpl(s, irec, dtl, NULL);
+    int b = collision_check_pltp(s, irec, dtl);
+    if (a) {
+        int64_t r = resolve_plpl(s, irec, dtl);
+        if (r < 0) return -7;
+        s->stats[4] += r;
     }
+    if (b) s->stats[4] += resolve_pltp(s);
+    return 0;
 }
 
 static void symba_set_recur_levels(orc_system *s, int ireci) {
@@ -2263,7 +2499,10 @@ static int symba_recur(orc_system *s, int ireci) {
             symba_kick_list_plpl(s, dth, irecp, -1);
             symba_kick_list_pltp(s, dth, irecp, -1);
         }
-        if (s->lclose && symba_collision_check(s, ireci, dtl)) symba_resolve_collisions(s);
+        if (s->lclose) {
+            int rc = symba_collisions(s, ireci, dtl);
+            if (rc) return rc;
+        }
         symba_set_recur_levels(s, ireci);
     }
     return 0;
@@ -2455,6 +2694,10 @@ void orc_system_get_tp(const orc_system *s, double *rh, double *vh, int32_t *sta
     if (status) memcpy(status, s->tstatus, sizeof(int32_t) * s->ntp);
 }
 void orc_system_stats(const orc_system *s, int64_t *out) { memcpy(out, s->stats, sizeof(s->stats)); }
+void orc_system_collision_terms(const orc_system *s, double *out) {
+    out[0] = s->E_collisions;
+    for (int d = 0; d < 3; d++) out[1 + d] = s->L_escape[d];
+}
 int64_t orc_system_plpl_list(const orc_system *s, int64_t cap, int32_t *i1, int32_t *i2) {
     for (int64_t k = 0; k < s->last_plpl_n && k < cap; k++) {
         i1[k] = s->last_plpl[2 * k];

@@ -94,6 +94,8 @@ void orc_system_energy(orc_system *s, double *out /* te, ke, pe, be, Lx, Ly, Lz,
 /* step-level counters: [n_steps_with_encounters, max_recursion_level, total_plpl_enc, total_pltp_enc, ncollisions,
  * recursion sub-steps] */
 void orc_system_stats(const orc_system *s, int64_t *out);
+/* out[4]: E_collisions, L_escape (x, y, z) booked by the collision resolution (G*m units) */
+void orc_system_collision_terms(const orc_system *s, double *out);
 /* last level-0 encounter lists */
 int64_t orc_system_plpl_list(const orc_system *s, int64_t cap, int32_t *i1, int32_t *i2);
 int64_t orc_system_pltp_list(const orc_system *s, int64_t cap, int32_t *i1, int32_t *i2);

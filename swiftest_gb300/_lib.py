@@ -67,6 +67,7 @@ SIGNATURES = {
     "swg_system_get_pl": (_INT, [_P, _P, _P, _P]),
     "swg_system_get_tp": (_INT, [_P, _P, _P, _P]),
     "swg_system_energy": (_INT, [_P, _P]),
+    "swg_system_collision_terms": (_INT, [_P, _P]),
     "swg_system_stats": (_INT, [_P, _P]),
     "swg_system_plpl_list": (_INT, [_P, _I64, C.POINTER(_I64), _P, _P]),
     "swg_system_pltp_list": (_INT, [_P, _I64, C.POINTER(_I64), _P, _P]),
@@ -85,6 +86,7 @@ SIGNATURES = {
     "swg_ensemble_get_pl": (_INT, [_P, _P, _P, _P]),
     "swg_ensemble_get_tp": (_INT, [_P, _P, _P, _P]),
     "swg_ensemble_energy": (_INT, [_P, _P]),
+    "swg_ensemble_collision_terms": (_INT, [_P, _P]),
     "swg_ensemble_stats": (_INT, [_P, _P]),
     "swg_ensemble_plpl_list": (_INT, [_P, _I32, _I64, C.POINTER(_I64), _P, _P]),
     "swg_ensemble_set_state": (_INT, [_P, _P, _P, _P, _P]),

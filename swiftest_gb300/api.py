@@ -293,8 +293,10 @@ class NBodySystem:
     def energy(self):
         out = np.zeros(9)
         self.ctx.check("swg_system_energy", self.ctx.lib.swg_system_energy(self.h, _ptr(out)))
+        ct = np.zeros(4)
+        self.ctx.check("swg_system_collision_terms", self.ctx.lib.swg_system_collision_terms(self.h, _ptr(ct)))
         return {"te": out[0], "ke": out[1], "pe": out[2], "be": out[3], "L": out[4:7].copy(), "GMtot": out[7],
-                "te_helio": out[8]}
+                "te_helio": out[8], "E_collisions": ct[0], "L_escape": ct[1:4].copy()}
 
     def stats(self):
         out = np.zeros(6, np.int64)
@@ -404,8 +406,12 @@ class Ensemble:
         """Per-system energy / momentum: dict of arrays (length nsys)."""
         out = np.zeros((self.nsys, 9))
         self.ctx.check("swg_ensemble_energy", self.ctx.lib.swg_ensemble_energy(self.h, _ptr(out)))
+        ct = np.zeros((self.nsys, 4))
+        self.ctx.check("swg_ensemble_collision_terms",
+                       self.ctx.lib.swg_ensemble_collision_terms(self.h, _ptr(ct)))
         return {"te": out[:, 0].copy(), "ke": out[:, 1].copy(), "pe": out[:, 2].copy(), "be": out[:, 3].copy(),
-                "L": out[:, 4:7].copy(), "GMtot": out[:, 7].copy(), "te_helio": out[:, 8].copy()}
+                "L": out[:, 4:7].copy(), "GMtot": out[:, 7].copy(), "te_helio": out[:, 8].copy(),
+                "E_collisions": ct[:, 0].copy(), "L_escape": ct[:, 1:4].copy()}
 
     def stats(self):
         out = np.zeros(6, np.int64)

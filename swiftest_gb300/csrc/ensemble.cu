@@ -139,6 +139,9 @@ struct swg_ensemble {
     std::vector<int32_t> h_pend;  // per-system pause flags read after a recursion launch
     EnsRecArgs rec_args;          // arguments of the step's recursion launch (reused to resume)
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
+    // per system: E_collisions, L_escape (x, y, z) booked by the collision resolution (G*m units)
+    std::vector<double> coll_terms;
+    double rec_dt = 0.0;  // step of the running recursion
     StepProfile prof;
     // side stream for the closing kick of systems without encounters (overlaps the recursion)
     cudaStream_t side = nullptr;
@@ -1168,8 +1171,9 @@ int resolve_collisions(swg_ensemble *e, int s) {
     const int64_t npp = seg[1], npt = seg[3];
     const size_t n = std::max(npl, 1), m = std::max(ntp, 1);
     std::vector<double> rh(3 * n), vb(3 * n), Gm(n), R(n), rhill(n), trh(3 * m), tvb(3 * m);
-    std::vector<int32_t> st(n), lm(n), tst(m), tlm(m);
-    std::vector<int32_t> pp(3 * std::max<int64_t>(npp, 1)), pt(3 * std::max<int64_t>(npt, 1));
+    std::vector<int32_t> st(n), lm(n), lev(n), tst(m), tlm(m);
+    std::vector<int32_t> pp(4 * std::max<int64_t>(npp, 1)), pt(3 * std::max<int64_t>(npt, 1));
+    int32_t irec = 0;
     struct Copy {
         void *h;
         void *d;
@@ -1187,9 +1191,15 @@ int resolve_collisions(swg_ensemble *e, int s) {
         if (npp) xs.push_back({pp.data() + f * npp, e->pp_l + field * e->pp_cap + seg[0], 4 * (size_t)npp});
         if (npt) xs.push_back({pt.data() + f * npt, e->pt_l + field * e->pt_cap + seg[2], 4 * (size_t)npt});
     }
-    for (const Copy &x : xs)
-        if (x.bytes)
-            SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.h, x.d, x.bytes, cudaMemcpyDeviceToHost, c->stream), "collision"));
+    // read only: the pl-pl lvdotr field and the levels (for the cascade check), the paused level
+    std::vector<Copy> inputs = {{lev.data(), e->levelg + P, 4 * (size_t)npl},
+                                {&irec, e->rec_resume + (size_t)REC_STATE * s + 1, 4}};
+    if (npp) inputs.push_back({pp.data() + 3 * npp, e->pp_l + 2 * e->pp_cap + seg[0], 4 * (size_t)npp});
+    for (auto *v : {&xs, &inputs})
+        for (const Copy &x : *v)
+            if (x.bytes)
+                SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.h, x.d, x.bytes, cudaMemcpyDeviceToHost, c->stream),
+                                    "collision"));
     SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "collision"));
     // global 1-based indices -> local
     for (int64_t k = 0; k < npp; k++) {
@@ -1223,7 +1233,21 @@ int resolve_collisions(swg_ensemble *e, int s) {
     cs.pt_i1 = pt.data();
     cs.pt_i2 = pt.data() + npt;
     cs.pt_st = pt.data() + 2 * npt;
-    e->stats[4] += resolve_collisions_host(cs);
+    cs.pp_lv = pp.data() + 3 * npp;
+    cs.levelg = lev.data();
+    cs.irec = irec;
+    cs.dt = level_dt(e->rec_dt, irec);
+    double *ct = &e->coll_terms[4 * (size_t)s];
+    cs.E_collisions = ct[0];
+    for (int d = 0; d < 3; d++) cs.L_escape[d] = ct[1 + d];
+    const int64_t nres = resolve_collisions_host(cs);
+    if (nres < 0) {
+        c->err = "runaway collisional cascade (more than 1000 rounds of merges in one resolution)";
+        return SWG_ERR_STATE;
+    }
+    e->stats[4] += nres;
+    ct[0] = cs.E_collisions;
+    for (int d = 0; d < 3; d++) ct[1 + d] = cs.L_escape[d];
     for (int64_t k = 0; k < npp; k++) {
         pp[k] += p0;
         pp[npp + k] += p0;
@@ -1242,6 +1266,7 @@ int resolve_collisions(swg_ensemble *e, int s) {
 // systems are resumed by recursion_finish.
 int recursion_launch(swg_ensemble *e, double dt) {
     swg_ctx *c = e->c;
+    e->rec_dt = dt;
     const int64_t n = e->pp_n + e->pt_n;
     SWG_TRY(ensure(c, e->rec_scratch, sizeof(double) * (size_t)(12 * n + 8) + (size_t)(3 * n + 96) +
                                           sizeof(int32_t) * (size_t)(7 * n + 128)));
@@ -1806,6 +1831,7 @@ int swg_ensemble_create(swg_ctx *c, int integrator, int32_t nsys, const int32_t 
     if (rc == SWG_OK) rc = dalloc(c, &e->tflag, m);
     if (rc == SWG_OK) rc = dalloc(c, &e->ndiscard, 1);
     e->h_pend.assign(S, 0);
+    e->coll_terms.assign(4 * (size_t)S, 0.0);
     if (rc == SWG_OK && integrator == SWG_HELIO && m > 0 && S > 1) {
         // two groups of systems with about equal pl-tp kick work (N_tp N_pl), split at a system
         double total = 0.0, cum = 0.0;
@@ -1954,6 +1980,7 @@ int swg_ensemble_set_param(swg_ensemble *e, double dt, double rhscale, int lclos
 int swg_ensemble_initialize(swg_ensemble *e) {
     if (!e || !e->cb_set || !(e->dt > 0.0)) return SWG_ERR_STATE;
     swg_ctx *c = e->c;
+    e->coll_terms.assign(4 * (size_t)e->nsys, 0.0);
     std::vector<int32_t> ones(std::max(e->NPL, e->NTP), 1), first(e->nsys, 1);
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->status, 0, 4 * std::max<int64_t>(e->NPL, 1), c->stream), "init"));
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->tstatus, 0, 4 * std::max<int64_t>(e->NTP, 1), c->stream), "init"));
@@ -2112,6 +2139,12 @@ int swg_ensemble_energy(swg_ensemble *e, double *out) {
                                            c->stream),
                         "energy"));
     return cuda_status(c, cudaStreamSynchronize(c->stream), "energy");
+}
+
+int swg_ensemble_collision_terms(swg_ensemble *e, double *out) {
+    if (!e || !out) return SWG_ERR_ARG;
+    for (size_t k = 0; k < e->coll_terms.size(); k++) out[k] = e->coll_terms[k];
+    return SWG_OK;
 }
 
 int swg_ensemble_stats(swg_ensemble *e, int64_t *out) {

@@ -326,9 +326,22 @@ struct CollisionSystem {
     double *trh = nullptr, *tvb = nullptr;
     int32_t *tstatus = nullptr, *tlmask = nullptr;
     int64_t npp = 0, npt = 0;
-    int32_t *pp_i1 = nullptr, *pp_i2 = nullptr, *pp_st = nullptr;
+    int32_t *pp_i1 = nullptr, *pp_i2 = nullptr, *pp_st = nullptr, *pp_lv = nullptr;
     int32_t *pt_i1 = nullptr, *pt_i2 = nullptr, *pt_st = nullptr;
+    int32_t *levelg = nullptr;  // recursion levels of the massive bodies (for the cascade check)
+    int irec = 0;               // recursion level at which the collisions were found
+    double dt = 0.0;            // that level's step
+    double E_collisions = 0.0;  // inout: collision_resolve.f90:638 (G*m units)
+    double L_escape[3] = {0.0, 0.0, 0.0};  // inout: collision_generate.f90:219
 };
+// Step of recursion level irec, formed as the device recursion forms it: dt / 3^irec.
+inline double level_dt(double dt, int irec) {
+    double p3 = 1.0;
+    for (int k = 0; k < irec; k++) p3 *= 3.0;
+    return dt / p3;
+}
+// Resolves the COLLIDED pairs in place; returns the number of merges plus discarded test
+// particles, or -1 for a runaway collisional cascade.
 int64_t resolve_collisions_host(CollisionSystem &c);
 
 // Scalar-broadcast helpers

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "collision_one.cuh"
 #include "drift_impl.cuh"
 #include "swg_internal.cuh"
 
@@ -661,66 +662,6 @@ static __device__ void blk_set_recur_levels(const RecArgs &a, int nbpl, int nbtp
         if (*lev == irecp) *lev = ireci;
     }
     __syncthreads();
-}
-
-// swiftest_orbel_xv2aeq (src/swiftest/swiftest_orbel.f90:700-764): semimajor axis,
-// eccentricity and pericentre distance of the relative two-body orbit.
-__device__ __forceinline__ void d_xv2aeq(double mu, double rx, double ry, double rz, double vx, double vy, double vz,
-                                         double &a, double &e, double &q) {
-    const double TINYV = 4.0e-15;  // swiftest_orbel.f90:11
-    a = 0.0;
-    e = 0.0;
-    q = 0.0;
-    const double r = sqrt(rx * rx + ry * ry + rz * rz);
-    const double v2 = vx * vx + vy * vy + vz * vz;
-    const double hx = ry * vz - rz * vy, hy = rz * vx - rx * vz, hz = rx * vy - ry * vx;
-    const double h2 = hx * hx + hy * hy + hz * hz;
-    if (h2 < 2.2250738585072014e-308) return;  // tiny(1.0_DP)
-    const double energy = 0.5 * v2 - mu / r;
-    int type;  // -1 ellipse, 0 parabola, 1 hyperbola
-    double fac = 0.0;
-    if (fabs(energy * r / mu) < sqrt(TINYV)) {
-        type = 0;
-    } else {
-        a = -0.5 * mu / energy;
-        if (a < 0.0) {
-            fac = -h2 / (mu * a);
-            type = fac > TINYV ? 1 : 0;
-        } else {
-            type = -1;
-        }
-    }
-    if (type == -1) {
-        fac = 1.0 - h2 / (mu * a);
-        if (fac > TINYV) e = sqrt(fac);
-        q = a * (1.0 - e);
-    } else if (type == 0) {
-        a = 0.5 * h2 / mu;
-        e = 1.0;
-        q = a;
-    } else {
-        e = sqrt(1.0 + fac);
-        q = a * (1.0 - e);
-    }
-}
-
-// collision_check_one (src/collision/collision_check.f90:16-57)
-__device__ __forceinline__ bool d_collision_one(double xr, double yr, double zr, double vxr, double vyr, double vzr,
-                                                double Gmtot, double rlim, double dt, bool lvdotr) {
-    const double r2 = xr * xr + yr * yr + zr * zr;
-    const double rlim2 = rlim * rlim;
-    if (r2 <= rlim2) return true;
-    const double vdotr = xr * vxr + yr * vyr + zr * vzr;
-    if (lvdotr && vdotr > 0.0) {
-        const double tcr2 = r2 / (vxr * vxr + vyr * vyr + vzr * vzr);
-        const double dt2 = dt * dt;
-        if (tcr2 <= dt2) {
-            double a, e, q;
-            d_xv2aeq(Gmtot, xr, yr, zr, vxr, vyr, vzr, a, e, q);
-            return q < rlim;
-        }
-    }
-    return false;
 }
 
 // collision_check_plpl / _pltp (src/collision/collision_check.f90:60-271) for the pairs of

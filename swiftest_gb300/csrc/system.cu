@@ -60,6 +60,8 @@ struct swg_system {
     int32_t *tflag = nullptr;               // tp flagged by the scan
     unsigned long long *ndiscard = nullptr; // tp removed by the scan
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
+    double E_collisions = 0.0, L_escape[3] = {0.0, 0.0, 0.0};  // collision bookkeeping (G*m units)
+    double rec_dt = 0.0;                                        // step of the running recursion
     StepProfile prof;  // optional CUDA-event profile per kernel class (PROF_*)
 };
 
@@ -634,9 +636,10 @@ int resolve_collisions(swg_system *s) {
     swg_ctx *c = s->c;
     const size_t n = std::max(s->npl, 1), m = std::max(s->ntp, 1);
     std::vector<double> rh(3 * n), vb(3 * n), Gm(n), R(n), rhill(n), trh(3 * m), tvb(3 * m);
-    std::vector<int32_t> st(n), lm(n), tst(m), tlm(m);
+    std::vector<int32_t> st(n), lm(n), lev(n), tst(m), tlm(m);
     const int64_t npp = s->plpl_n, npt = s->pltp_n;
-    std::vector<int32_t> pp(3 * std::max<int64_t>(npp, 1)), pt(3 * std::max<int64_t>(npt, 1));
+    std::vector<int32_t> pp(4 * std::max<int64_t>(npp, 1)), pt(3 * std::max<int64_t>(npt, 1));
+    int32_t irec = 0;
     struct Copy {
         void *h;
         void *d;
@@ -655,7 +658,10 @@ int resolve_collisions(swg_system *s) {
         if (npp) lists.push_back({pp.data() + f * npp, s->plpl_l + field * s->plpl_cap, 4 * (size_t)npp});
         if (npt) lists.push_back({pt.data() + f * npt, s->pltp_l + field * s->pltp_cap, 4 * (size_t)npt});
     }
-    for (auto *v : {&pl_arrays, &lists})
+    // read only: the pl-pl lvdotr field and the levels (for the cascade check), the paused level
+    std::vector<Copy> inputs = {{lev.data(), s->levelg, 4 * (size_t)s->npl}, {&irec, s->rec_resume + 1, 4}};
+    if (npp) inputs.push_back({pp.data() + 3 * npp, s->plpl_l + 2 * s->plpl_cap, 4 * (size_t)npp});
+    for (auto *v : {&pl_arrays, &lists, &inputs})
         for (const Copy &x : *v)
             if (x.bytes)
                 SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.h, x.d, x.bytes, cudaMemcpyDeviceToHost, c->stream), "collision"));
@@ -683,7 +689,20 @@ int resolve_collisions(swg_system *s) {
     cs.pt_i1 = pt.data();
     cs.pt_i2 = pt.data() + npt;
     cs.pt_st = pt.data() + 2 * npt;
-    s->stats[4] += resolve_collisions_host(cs);
+    cs.pp_lv = pp.data() + 3 * npp;
+    cs.levelg = lev.data();
+    cs.irec = irec;
+    cs.dt = level_dt(s->rec_dt, irec);
+    cs.E_collisions = s->E_collisions;
+    for (int d = 0; d < 3; d++) cs.L_escape[d] = s->L_escape[d];
+    const int64_t nres = resolve_collisions_host(cs);
+    if (nres < 0) {
+        c->err = "runaway collisional cascade (more than 1000 rounds of merges in one resolution)";
+        return SWG_ERR_STATE;
+    }
+    s->stats[4] += nres;
+    s->E_collisions = cs.E_collisions;
+    for (int d = 0; d < 3; d++) s->L_escape[d] = cs.L_escape[d];
     for (auto *v : {&pl_arrays, &lists})
         for (const Copy &x : *v)
             if (x.bytes)
@@ -695,6 +714,7 @@ int resolve_collisions(swg_system *s) {
 // as one single-block kernel; no host round trip until the next step's checks.
 int symba_recursion(swg_system *s, double dt) {
     swg_ctx *c = s->c;
+    s->rec_dt = dt;
     const int64_t n = s->plpl_n + s->pltp_n;
     SWG_TRY(ensure(c, s->rec_scratch, sizeof(double) * (size_t)(12 * n + 8) + (size_t)(3 * n + 96) +
                                           sizeof(int32_t) * (size_t)(7 * n + 128)));
@@ -962,6 +982,8 @@ int swg_system_set_param(swg_system *s, double dt, int loop_mode, int enc_plpl, 
 int swg_system_initialize(swg_system *s) {
     if (!s || !(s->GMcb > 0.0) || !(s->dt > 0.0)) return SWG_ERR_STATE;
     swg_ctx *c = s->c;
+    s->E_collisions = 0.0;
+    s->L_escape[0] = s->L_escape[1] = s->L_escape[2] = 0.0;
     const int n = s->npl;
     std::vector<int32_t> ones(std::max(n, s->ntp), 1), zeros(std::max(n, s->ntp), 0);
     if (n > 0) {
@@ -1080,6 +1102,13 @@ int swg_system_energy(swg_system *s, double *out) {
     SWG_TRY(L(c, "energy_final"));
     SWG_TRY(cuda_status(c, cudaMemcpyAsync(out, dout, 9 * 8, cudaMemcpyDeviceToHost, c->stream), "energy"));
     return cuda_status(c, cudaStreamSynchronize(c->stream), "energy");
+}
+
+int swg_system_collision_terms(swg_system *s, double *out) {
+    if (!s || !out) return SWG_ERR_ARG;
+    out[0] = s->E_collisions;
+    for (int d = 0; d < 3; d++) out[1 + d] = s->L_escape[d];
+    return SWG_OK;
 }
 
 int swg_system_stats(swg_system *s, int64_t *out) {

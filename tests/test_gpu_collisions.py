@@ -3,7 +3,8 @@ perfect merging on the host) against the oracle, single system and batched ensem
 
 Radii are inflated so that collisions happen within a short run; both pl-pl merges and
 pl-tp discards occur.  In FP64 the trajectories, statuses and statistics must match the
-oracle bit for bit.
+oracle bit for bit, and so must the collision bookkeeping (E_collisions, L_escape) that the
+host resolution keeps.
 """
 import numpy as np
 import pytest
@@ -45,6 +46,10 @@ def test_symba_collisions_bitexact(ctx):
     er = ref.energy()
     for k in ("te", "ke", "pe", "be"):
         assert np.isfinite(e1[k]) and abs(e1[k] - er[k]) <= 1e-12 * abs(er[k]), k
+    # the collision bookkeeping (E_collisions, L_escape) is computed on the host from the
+    # same state in the same order: the same bits
+    assert e1["E_collisions"] == er["E_collisions"] != 0.0
+    assert np.array_equal(e1["L_escape"], er["L_escape"]) and np.any(er["L_escape"] != 0.0)
 
 
 def test_ensemble_collisions_bitexact(ctx):
@@ -80,6 +85,8 @@ def test_ensemble_collisions_bitexact(ctx):
     for s, r in enumerate(refs):
         er = r.energy()
         assert np.isfinite(eg["te"][s]) and abs(eg["te"][s] - er["te"]) <= 1e-12 * abs(er["te"]), s
+        assert eg["E_collisions"][s] == er["E_collisions"], s
+        assert np.array_equal(eg["L_escape"][s], er["L_escape"]), s
 
 
 def _helio_crowded(seed, npl=60, ntp=600, inflate=1000.0):
