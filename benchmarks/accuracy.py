@@ -1,14 +1,22 @@
-"""Long-run accuracy of the mixed-precision batched path against the FP64 path.
+"""Long-run accuracy of the mixed-precision batched path against the FP64 path, C4 ensemble.
 
-    python benchmarks/accuracy.py [--nsys N] [--steps S] [--every K] [--full-mixed]
+    python benchmarks/accuracy.py [--steps S] [--every K] [--sample N] [--nsys M] [--out FILE]
 
-Steps the first N systems of the C4 ensemble (256 planetesimal disks, SyMBA, dt = 0.002 yr,
-1-Hill-radius encounter radius) for S steps in both precisions from the same initial
-conditions and prints one JSON line: per-system |dE/E| (central-body potential at the
-heliocentric distance, and the reference's formula) and |dL/L| at the end, their
-maxima and medians per path, the ratio of the mixed to the FP64 error, and the number of
-steps with encounters.  With --full-mixed the whole 256-system ensemble is also run in
-mixed precision (the FP64 path at that size takes ~0.27 s per step).
+1. The whole C4 ensemble (256 planetesimal disks, SyMBA, dt = 0.002 yr, 1-Hill-radius
+   encounter radius) runs S steps in mixed precision.  Recorded per system: |dE/E| with the
+   collision energy taken out as the reference's error terms do (central-body potential at
+   the heliocentric distance; the reference's own formula is recorded too), |dL/L| of the
+   system's angular momentum, the number of merges (bodies left INACTIVE), and the history of
+   |dE/E| every K steps.
+2. The FP64 path (the reference's operation order) then runs the same S steps on a subset of
+   the systems, batched together (each system's FP64 trajectory is independent of the others
+   in the batch): a random sample of N systems without merges (numpy default_rng(2024)), then
+   every system with a merge and every system whose mixed |dE/E| exceeds twice the largest
+   FP64 error of the sample.
+3. One JSON line: per-system tables, the mixed / FP64 ratio per compared system and its
+   maximum, and the wall times.
+
+--nsys M takes the first M systems instead of all 256 (quick runs).
 """
 from __future__ import annotations
 
@@ -33,7 +41,22 @@ def _errors(e0, e1):
     return dE, dEr, dL
 
 
-def _run(ctx, E, precision, steps, every):
+def subset(E, idx):
+    """The systems idx of a packed ensemble E, packed again."""
+    systems = [E["systems"][i] for i in idx]
+    out = {k: E[k] for k in ("integrator", "dt", "rhscale")}
+    out["npl"] = E["npl"][idx].copy()
+    out["ntp"] = E["ntp"][idx].copy()
+    out["GMcb"] = np.asarray(E["GMcb"])[idx].copy()
+    out["Rcb"] = np.asarray(E["Rcb"])[idx].copy()
+    out["pl"] = {k: np.concatenate([p[k] for p, _ in systems]) for k in ("rh", "vh", "Gmass", "radius", "rhill")}
+    ntp = sum(len(t["rh"]) for _, t in systems)
+    out["tp"] = {k: (np.concatenate([t[k] for _, t in systems]) if ntp else np.zeros((0, 3))) for k in ("rh", "vh")}
+    out["systems"] = systems
+    return out
+
+
+def run(ctx, E, precision, steps, every):
     from swiftest_gb300.api import Ensemble
     ens = Ensemble(ctx, E, precision=precision)
     e0 = ens.energy()
@@ -45,22 +68,26 @@ def _run(ctx, E, precision, steps, every):
         ens.step(k)
         done += k
         dE, _, _ = _errors(e0, ens.energy())
-        hist.append([done, float(dE.max()), float(np.median(dE))])
+        hist.append(dE.tolist())
     wall = time.perf_counter() - t0
-    dE, dEr, dL = _errors(e0, ens.energy())
-    st = ens.stats()
+    e1 = ens.energy()
+    dE, dEr, dL = _errors(e0, e1)
+    _, _, st = ens.get_pl()
+    merges = [int((st[ens.poff[s]:ens.poff[s + 1]] == 1).sum()) for s in range(len(E["npl"]))]
+    stats = ens.stats()
     ens.close()
-    return {"dE_E": dE.tolist(), "dE_E_ref_formula": dEr.tolist(), "dL_L": dL.tolist(),
-            "dE_E_max": float(dE.max()), "dE_E_median": float(np.median(dE)), "dL_L_max": float(dL.max()),
-            "history": hist, "stats": st, "wall_s": wall}
+    return {"dE_E": dE.tolist(), "dE_E_ref_formula": dEr.tolist(), "dL_L": dL.tolist(), "merges": merges,
+            "E_collisions_over_E0": (np.abs(e1["E_collisions"]) / np.abs(e0["te"])).tolist(),
+            "history_every": every, "history": hist, "stats": stats, "wall_s": wall}
 
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("--nsys", type=int, default=16)
     p.add_argument("--steps", type=int, default=10000)
     p.add_argument("--every", type=int, default=1000)
-    p.add_argument("--full-mixed", action="store_true")
+    p.add_argument("--sample", type=int, default=32)
+    p.add_argument("--nsys", type=int, default=None)
+    p.add_argument("--out", default=None)
     a = p.parse_args(argv)
     from swiftest_gb300 import build as B
     from swiftest_gb300 import initial_conditions as IC
@@ -68,19 +95,46 @@ def main(argv=None):
     B.build()
     ctx = Context(0)
     E = IC.make_ensemble("C4", nsys=a.nsys)
-    out = {"workload": f"first {a.nsys} systems of the C4 ensemble ({int(E['npl'].sum())} pl), SyMBA, dt=0.002 yr, "
-                       f"RHSCALE=1.0, {a.steps} steps", "steps": a.steps}
-    out["fp64"] = _run(ctx, E, "FP64", a.steps, a.every)
-    out["mixed"] = _run(ctx, E, "MIXED", a.steps, a.every)
-    f, m = np.array(out["fp64"]["dE_E"]), np.array(out["mixed"]["dE_E"])
-    out["ratio_mixed_over_fp64_max"] = float(m.max() / f.max())
-    out["ratio_mixed_over_fp64_per_system_max"] = float(np.max(m / np.maximum(f, 1e-300)))
-    if a.full_mixed:
-        Efull = IC.make_ensemble("C4")
-        r = _run(ctx, Efull, "MIXED", a.steps, a.every)
-        out["full_c4_mixed"] = {k: r[k] for k in ("dE_E_max", "dE_E_median", "dL_L_max", "history", "stats",
-                                                   "wall_s")}
-    print(json.dumps(out), flush=True)
+    nsys = len(E["npl"])
+    out = {"workload": f"C4 ensemble, {nsys} systems ({int(E['npl'].sum())} pl), SyMBA, dt=0.002 yr, RHSCALE=1.0, "
+                       f"{a.steps} steps", "steps": a.steps, "npl": E["npl"].tolist()}
+    mixed = run(ctx, E, "MIXED", a.steps, a.every)
+    out["mixed"] = mixed
+    dEm = np.array(mixed["dE_E"])
+    merged = [s for s in range(nsys) if mixed["merges"][s] > 0]
+    rng = np.random.default_rng(2024)
+    rest = [s for s in range(nsys) if s not in merged]
+    sample = sorted(int(x) for x in rng.choice(rest, size=min(a.sample, len(rest)), replace=False))
+    # the FP64 sample first: its largest error sets the outlier threshold for the mixed path
+    fp_sample = run(ctx, subset(E, np.array(sample)), "FP64", a.steps, a.every)
+    thresh = 2.0 * max(fp_sample["dE_E"])
+    outliers = [s for s in range(nsys) if dEm[s] > thresh and s not in merged and s not in sample]
+    extra = sorted(set(merged) | set(outliers))
+    fp_extra = run(ctx, subset(E, np.array(extra)), "FP64", a.steps, a.every) if extra else None
+    keys = ("dE_E", "dE_E_ref_formula", "dL_L", "merges")
+    fp = {s: {key: fp_sample[key][k] for key in keys} for k, s in enumerate(sample)}
+    if fp_extra:
+        fp.update({s: {key: fp_extra[key][k] for key in keys} for k, s in enumerate(extra)})
+    rows = []
+    for s in sorted(fp):
+        rows.append({"system": s, "npl": int(E["npl"][s]),
+                     "why": "merge" if s in merged else ("outlier" if s in outliers else "sample"),
+                     "merges_mixed": mixed["merges"][s], "merges_fp64": fp[s]["merges"],
+                     "dE_E_fp64": fp[s]["dE_E"], "dE_E_mixed": float(dEm[s]),
+                     "ratio": float(dEm[s] / max(fp[s]["dE_E"], 1e-300)),
+                     "dL_L_fp64": fp[s]["dL_L"], "dL_L_mixed": mixed["dL_L"][s]})
+    out["compared"] = rows
+    out["outlier_threshold"] = thresh
+    out["ratio_max"] = max(r["ratio"] for r in rows)
+    out["fp64_wall_s"] = fp_sample["wall_s"] + (fp_extra["wall_s"] if fp_extra else 0.0)
+    out["fp64_max_over_compared"] = max(r["dE_E_fp64"] for r in rows)
+    out["mixed_max_over_compared"] = max(r["dE_E_mixed"] for r in rows)
+    out["mixed_max_all"] = float(dEm.max())
+    line = json.dumps(out)
+    if a.out:
+        Path(a.out).write_text(line + "\n")
+    print(json.dumps({k: out[k] for k in ("workload", "ratio_max", "mixed_max_all", "fp64_max_over_compared",
+                                          "mixed_max_over_compared", "fp64_wall_s")}), flush=True)
     ctx.close()
 
 
