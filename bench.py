@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--workload", default="c4", choices=["c4", "c3", "c3w", "c1"])
     p.add_argument("--nsys", type=int, default=None, help="first NSYS systems of the C4 ensemble")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    p.add_argument("--encounter", default="triangular", choices=["triangular", "sortsweep"],
+                   help="mode of the SyMBA level-0 pl-pl and pl-tp checks (c4, c1)")
     return p.parse_args()
 
 
@@ -105,10 +107,12 @@ class C4:
         self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
         self.plpl_pairs = float(sum(int(n) * (int(n) - 1) for n in self.E["npl"]))  # per kick evaluation
         self.pairs_per_step = 2 * self.plpl_pairs
+        self.enc = getattr(args, "encounter", "triangular").upper()
 
     def make(self, ctx, precision):
         from swiftest_gb300.api import Ensemble
-        return Ensemble(ctx, self.E, precision=precision)
+        kw = {} if self.enc == "TRIANGULAR" else dict(encounter_check_plpl=self.enc, encounter_check_pltp=self.enc)
+        return Ensemble(ctx, self.E, precision=precision, **kw)
 
     def state_arrays(self):
         E = self.E
@@ -118,7 +122,7 @@ class C4:
         n = self.E["npl"]
         return {"workload": f"C4 batched SyMBA ensemble: {len(n)} planetesimal disks, N_pl log-uniform in "
                             f"[500, 5000] ({int(n.sum())} pl total, 0 tp), m in [1e-11, 1e-7] Msun, a in [0.5, 2] AU, "
-                            "e,i Rayleigh(0.02), dt=0.002 yr, RHSCALE=1.0 (1 Hill radius), TRIANGULAR level-0 checks",
+                            f"e,i Rayleigh(0.02), dt=0.002 yr, RHSCALE=1.0 (1 Hill radius), {self.enc} level-0 checks",
                 "nsys": len(n), "npl_total": int(n.sum()), "ntp_total": int(self.E["ntp"].sum()),
                 "npl_min": int(n.min()), "npl_max": int(n.max()), "dt": self.E["dt"], "rhscale": self.E["rhscale"],
                 "seed": 0, "precision": precision, "l2": "flushed before every timed step (512 MB memset, untimed)"}
@@ -130,7 +134,8 @@ class C4:
         cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
         bs, t_all, nsys = 0, 0.0, 0
         for pl, tp in self.E["systems"]:
-            s = O.OracleSystem("SYMBA", cb, pl, None, dt=self.E["dt"], rhscale=self.E["rhscale"], lclose=True)
+            s = O.OracleSystem("SYMBA", cb, pl, None, dt=self.E["dt"], rhscale=self.E["rhscale"], lclose=True,
+                               encounter_check_plpl=self.enc, encounter_check_pltp=self.enc)
             t0 = time.perf_counter()
             s.step(steps_per_system)
             t_all += time.perf_counter() - t0
@@ -146,6 +151,7 @@ class C3(C4):
 
     def __init__(self, args):
         from swiftest_gb300 import initial_conditions as IC
+        self.enc = "TRIANGULAR"  # HELIO checks no encounters
         self.E = IC.make_ensemble("C3", nsys=args.nsys)
         self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
         n = [int(x) for x in self.E["npl"]]
@@ -182,6 +188,7 @@ class C3W(C3):
 
     def __init__(self, args):
         from swiftest_gb300 import initial_conditions as IC
+        self.enc = "TRIANGULAR"  # WHM checks no encounters
         self.E = IC.make_ensemble("C3", nsys=args.nsys, integrator="WHM")
         self.nbodies = int(self.E["npl"].sum() + self.E["ntp"].sum())
         n = [int(x) for x in self.E["npl"]]
@@ -224,12 +231,13 @@ class C1:
         npl, ntp = cfg["npl"], cfg["ntp"]
         self.plpl_pairs = float(npl * (npl - 1))
         self.pairs_per_step = 2.0 * (npl * (npl - 1) + npl * ntp)
+        self.enc = getattr(args, "encounter", "triangular").upper()
 
     def make(self, ctx, precision):
         from swiftest_gb300.api import NBodySystem
         c = self.cfg
         return NBodySystem(ctx, "SYMBA", self.cb, self.pl, self.tp, dt=c["dt"], rhscale=c["rhscale"], lclose=True,
-                           precision=precision)
+                           precision=precision, encounter_check_plpl=self.enc, encounter_check_pltp=self.enc)
 
     def state_arrays(self):
         n, m = self.cfg["npl"], self.cfg["ntp"]
@@ -238,14 +246,15 @@ class C1:
     def config(self, precision):
         c = self.cfg
         return {"workload": f"C1 SyMBA disk: {c['npl']} pl + {c['ntp']} tp, a in [{c['amin']}, {c['amax']}] AU, "
-                            f"RHSCALE={c['rhscale']} (1 Hill radius), dt={c['dt']} yr, TRIANGULAR encounter checks",
+                            f"RHSCALE={c['rhscale']} (1 Hill radius), dt={c['dt']} yr, {self.enc} encounter checks",
                 "npl": c["npl"], "ntp": c["ntp"], "dt": c["dt"], "rhscale": c["rhscale"], "seed": c["seed"],
                 "precision": precision, "l2": "flushed before every timed step (512 MB memset, untimed)"}
 
     def oracle_sample(self, budget_s):
         from oracle import oracle as O
         c = self.cfg
-        s = O.OracleSystem("SYMBA", self.cb, self.pl, self.tp, dt=c["dt"], rhscale=c["rhscale"], lclose=True)
+        s = O.OracleSystem("SYMBA", self.cb, self.pl, self.tp, dt=c["dt"], rhscale=c["rhscale"], lclose=True,
+                           encounter_check_plpl=self.enc, encounter_check_pltp=self.enc)
         s.step(1)
         n, t0 = 0, time.perf_counter()
         while True:

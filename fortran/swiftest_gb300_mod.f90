@@ -143,6 +143,16 @@ module swiftest_gb300_mod
          integer(c_int), value :: mem
       end function
 
+      !! ---- util_sort(arr, ind) (base_module.f90:1361-1472): ind = 1-based ascending permutation
+      integer(c_int) function swg_util_sort_index(ctx, n, arr, ind, mem) bind(C, name="swg_util_sort_index")
+         import :: c_ptr, c_int, c_int32_t, c_int64_t, c_double
+         type(c_ptr), value :: ctx
+         integer(c_int64_t), value :: n
+         real(c_double), intent(in) :: arr(*)
+         integer(c_int32_t), intent(out) :: ind(*)
+         integer(c_int), value :: mem
+      end function
+
       !! ---- orbital elements (swiftest_orbel.f90:14-1072)
       integer(c_int) function swg_orbel_el2xv(ctx, n, mu, a, e, inc, capom, omega, capm, rh, vh, mem) &
                                               bind(C, name="swg_orbel_el2xv")
@@ -301,6 +311,12 @@ module swiftest_gb300_mod
          type(c_ptr), value :: ens
          real(c_double), value :: dt, rhscale
          integer(c_int), value :: lclose, precision
+      end function
+      integer(c_int) function swg_ensemble_set_encounter_modes(ens, enc_plpl, enc_pltp) &
+                                                               bind(C, name="swg_ensemble_set_encounter_modes")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: ens
+         integer(c_int), value :: enc_plpl, enc_pltp
       end function
       integer(c_int) function swg_ensemble_initialize(ens) bind(C, name="swg_ensemble_initialize")
          import :: c_ptr, c_int

@@ -119,6 +119,14 @@ int swg_encounter_check_all_pltp(swg_ctx *ctx, int mode, int32_t npl, int32_t nt
                                  double dt, int64_t cap, int64_t *nenc, int32_t *index1, int32_t *index2,
                                  int32_t *lvdotr, int mem);
 
+/* ---- sorting -------------------------------------------------------------------------
+ * Replaces util_sort(arr, ind) (src/base/base_module.f90:1361-1472), the index quicksort the
+ * sort-and-sweep check sorts its extents with: ind gets the 1-based permutation that orders
+ * arr ascending.  Stable LSD radix sort on the GPU; equal values (-0.0 and +0.0 included)
+ * keep their index order, where the reference's quicksort, seeded with the previous order,
+ * leaves ties in an order that depends on history. */
+int swg_util_sort_index(swg_ctx *ctx, int64_t n, const double *arr, int32_t *ind, int mem);
+
 /* ---- device-resident n-body system and step loops ---------------------------------
  * Mirrors swiftest_nbody_system with whm_step_system (src/whm/whm_step.f90:14-104),
  * helio_step_system (src/helio/helio_step.f90:14-119) and symba_step_system
@@ -192,7 +200,8 @@ int swg_orbel_xv2el(swg_ctx *ctx, int32_t n, const double *mu, const double *rh,
  * system's (3, npl[s]) block in system order (test particles likewise with ntp[s]), each
  * block ordered as the reference's initialize leaves it (HELIO/SyMBA: by mass, descending;
  * WHM: input order).  All systems share dt; GMTINY is not supported.  integrator: SWG_WHM,
- * SWG_HELIO or SWG_SYMBA (TRIANGULAR level-0 checks).  A WHM ensemble whose Danby drift
+ * SWG_HELIO or SWG_SYMBA (level-0 checks TRIANGULAR unless swg_ensemble_set_encounter_modes
+ * selects SORTSWEEP).  A WHM ensemble whose Danby drift
  * fails for a massive body returns SWG_ERR_DRIFT from the step call (the reference stops
  * the run). */
 typedef struct swg_ensemble swg_ensemble;
@@ -205,6 +214,11 @@ int swg_ensemble_set_pl(swg_ensemble *ens, const double *rh, const double *vh, c
                         const double *radius, const double *rhill);
 int swg_ensemble_set_tp(swg_ensemble *ens, const double *rh, const double *vh);
 int swg_ensemble_set_param(swg_ensemble *ens, double dt, double rhscale, int lclose, int precision);
+/* SyMBA: modes of the level-0 pl-pl and pl-tp checks (param%lencounter_sas_plpl / _pltp),
+ * SWG_ENC_TRIANGULAR (default) or SWG_ENC_SORTSWEEP: one radix sort of every system's
+ * bounding-box extents, each body sweeping its own system's run; each system's list is the
+ * one encounter_check_all_plpl / _pltp returns for it alone in that mode. */
+int swg_ensemble_set_encounter_modes(swg_ensemble *ens, int enc_plpl, int enc_pltp);
 int swg_ensemble_initialize(swg_ensemble *ens);
 int swg_ensemble_step(swg_ensemble *ens, int32_t nsteps);
 int swg_ensemble_get_pl(swg_ensemble *ens, double *rh, double *vh, int32_t *status);

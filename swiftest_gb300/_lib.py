@@ -56,6 +56,7 @@ SIGNATURES = {
                                              C.POINTER(_I64), _P, _P, _P, _INT]),
     "swg_encounter_check_all_pltp": (_INT, [_P, _INT, _I32, _I32, _P, _P, _P, _P, _P, _D, _I64, C.POINTER(_I64),
                                             _P, _P, _P, _INT]),
+    "swg_util_sort_index": (_INT, [_P, _I64, _P, _P, _INT]),
     "swg_system_create": (_INT, [_P, _INT, _I32, _I32, C.POINTER(_P)]),
     "swg_system_destroy": (_INT, [_P]),
     "swg_system_set_cb": (_INT, [_P, _D, _D]),
@@ -81,6 +82,7 @@ SIGNATURES = {
     "swg_ensemble_set_pl": (_INT, [_P, _P, _P, _P, _P, _P]),
     "swg_ensemble_set_tp": (_INT, [_P, _P, _P]),
     "swg_ensemble_set_param": (_INT, [_P, _D, _D, _INT, _INT]),
+    "swg_ensemble_set_encounter_modes": (_INT, [_P, _INT, _INT]),
     "swg_ensemble_initialize": (_INT, [_P]),
     "swg_ensemble_step": (_INT, [_P, _I32]),
     "swg_ensemble_get_pl": (_INT, [_P, _P, _P, _P]),

@@ -143,6 +143,14 @@ class Context:
         self.check("swg_drift_all", rc)
         return x, v, iflag
 
+    def util_sort_index(self, arr):
+        """util_sort(arr, ind): the 1-based permutation that sorts arr ascending (ties by index)."""
+        a = _f64(arr)
+        ind = np.zeros(a.shape[0], np.int32)
+        self.check("swg_util_sort_index", self.lib.swg_util_sort_index(self.h, a.shape[0], _ptr(a), _ptr(ind),
+                                                                       L.SWG_MEM_HOST))
+        return ind
+
     # ---- orbital elements ----------------------------------------------------
     ELEMENTS = ("a", "e", "inc", "capom", "omega", "capm", "varpi", "lam", "f", "cape", "capf")
 
@@ -347,7 +355,8 @@ class Ensemble:
 
     PROFILE_CLASSES = NBodySystem.PROFILE_CLASSES
 
-    def __init__(self, ctx: Context, ens: dict, dt=None, rhscale=None, lclose=True, precision="FP64"):
+    def __init__(self, ctx: Context, ens: dict, dt=None, rhscale=None, lclose=True, precision="FP64",
+                 encounter_check_plpl="TRIANGULAR", encounter_check_pltp="TRIANGULAR"):
         self.ctx = ctx
         lib = ctx.lib
         self.integrator = ens["integrator"].upper()
@@ -375,6 +384,10 @@ class Ensemble:
         ctx.check("swg_ensemble_set_param", lib.swg_ensemble_set_param(
             h, float(ens["dt"] if dt is None else dt), float(ens["rhscale"] if rhscale is None else rhscale),
             int(bool(lclose)), prec))
+        modes = {"TRIANGULAR": L.SWG_ENC_TRIANGULAR, "SORTSWEEP": L.SWG_ENC_SORTSWEEP}
+        m = (modes[encounter_check_plpl.upper()], modes[encounter_check_pltp.upper()])
+        if m != (L.SWG_ENC_TRIANGULAR, L.SWG_ENC_TRIANGULAR):
+            ctx.check("swg_ensemble_set_encounter_modes", lib.swg_ensemble_set_encounter_modes(h, *m))
         ctx.check("swg_ensemble_initialize", lib.swg_ensemble_initialize(h))
 
     def step(self, nsteps: int = 1):

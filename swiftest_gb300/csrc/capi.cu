@@ -281,6 +281,27 @@ int swg_drift_all(swg_ctx *c, const double *mu, double *x, double *v, int32_t n,
     return finish(c, mem);
 }
 
+int swg_util_sort_index(swg_ctx *c, int64_t n, const double *arr, int32_t *ind, int mem) {
+    if (!c || n < 0 || n > INT32_MAX || bad_mem(mem)) return SWG_ERR_ARG;
+    if (n == 0) return SWG_OK;
+    if (!arr || !ind) return SWG_ERR_ARG;
+    double *da;
+    int32_t *di;
+    void *scr;
+    SWG_TRY(stage_in(c, mem, 0, arr, (size_t)n, &da));
+    if (mem == SWG_MEM_DEVICE) {
+        di = ind;
+    } else {
+        void *p;
+        SWG_TRY(ensure_slot(c, 1, sizeof(int32_t) * (size_t)n, &p));
+        di = (int32_t *)p;
+    }
+    SWG_TRY(ensure_slot(c, 2, util_sort_index_scratch_bytes(n), &scr));
+    SWG_TRY(util_sort_index(c, n, da, di, scr));
+    SWG_TRY(stage_out(c, mem, ind, (const int32_t *)di, (size_t)n));
+    return finish(c, mem);
+}
+
 }  // extern "C"
 
 namespace {

@@ -4,8 +4,9 @@
 // in both of the reference's modes:
 //   * TRIANGULAR (:384-570): every pair is tested with encounter_check_one (:573-621).
 //   * SORTSWEEP  (:143-326, :763-988): 1-D radial bounding boxes |r| +- 1.1 renc,
-//     sorted; each body whose box holds >= 2 foreign extents strictly inside
-//     (the reference's loverlap test) tests the bodies whose extents lie inside.
+//     sorted by a stable radix sort on the extents (radix_sort.cu; ties by extent index);
+//     each body whose box holds >= 2 foreign extents strictly inside (the reference's
+//     loverlap test) tests the bodies whose extents lie inside.
 //
 // The encounter decision is made in FP64 with the reference's expression order
 // (this file is compiled with -fmad=false), so lists are bit-identical to the
@@ -17,7 +18,7 @@
 //
 // Output: pairs are appended with an atomic counter (up to cap), then sorted by
 // (index1, index2) with a bitonic sort (single CTA in shared memory when the
-// padded length fits, else global compare-exchange passes).
+// padded length fits, else global compare-exchange passes); the lists are short.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -341,6 +342,7 @@ int sort_pairs_unique(swg_ctx *c, int64_t n, int32_t *i1, int32_t *i2, int32_t *
 // ------------------------------------------------------------------ sort & sweep
 // orderable bit pattern of a double (ascending numeric order)
 __device__ __forceinline__ uint64_t d2key(double x) {
+    if (x == 0.0) x = 0.0;  // -0.0 compares equal to +0.0: one key for both
     uint64_t u = (uint64_t)__double_as_longlong(x);
     return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
 }
@@ -391,11 +393,15 @@ __global__ void k_sas_positions(int ntot, const uint32_t *vals, int32_t *ibeg, i
         iend[e - ntot] = k + 1;
 }
 
-// sweep: body b with loverlap tests the bodies whose extents are strictly inside its box
+// sweep: body b with loverlap tests the bodies whose extents are strictly inside its box.
+// FA/FB/FV: float copies of the ntot bodies (list 1 then list 2) for the conservative FP32
+// prefilter, which drops only pairs the FP64 test is certain to reject (see
+// prefilter_reject), so the list is the same.
 __global__ void k_sas_sweep(int n1, const double *r1, const double *v1, const double *renc1, int n2,
                             const double *r2, const double *v2, const double *renc2, int single, int shift2, double dt,
-                            const uint32_t *vals, const int32_t *ibeg, const int32_t *iend, long long cap,
-                            int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count) {
+                            const uint32_t *vals, const int32_t *ibeg, const int32_t *iend, const float4 *FA,
+                            const float4 *FB, const float4 *FV, long long cap, int32_t *o1, int32_t *o2, int32_t *olv,
+                            unsigned long long *count) {
     const int ntot = n1 + n2;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntot) return;
@@ -404,11 +410,15 @@ __global__ void k_sas_sweep(int n1, const double *r1, const double *v1, const do
     const double *ri = il1 ? &r1[3 * i] : &r2[3 * (i - n1)];
     const double *vi = il1 ? &v1[3 * i] : &v2[3 * (i - n1)];
     const double renci = il1 ? renc1[i] : (renc2 ? renc2[i - n1] : 0.0);
+    const BodyF q = {FA[i], FB[i], FV[i]};
+    const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);  // |dt| bounds either direction of time
     for (int p = ibeg[i] + 1; p <= iend[i] - 1; p++) {
         int b = (int)vals[p - 1];
         if (b >= ntot) b -= ntot;
         const bool bl1 = b < n1;
         if (!single && bl1 == il1) continue;
+        const BodyF f = {FA[b], FB[b], FV[b]};
+        if (prefilter_reject(f, q, dtf)) continue;
         const double *rb = bl1 ? &r1[3 * b] : &r2[3 * (b - n1)];
         const double *vb = bl1 ? &v1[3 * b] : &v2[3 * (b - n1)];
         const double rencb = bl1 ? renc1[b] : (renc2 ? renc2[b - n1] : 0.0);
@@ -436,8 +446,52 @@ __global__ void k_sas_sweep(int n1, const double *r1, const double *v1, const do
     }
 }
 
+// keys | vals | ibeg | iend | radix-sort scratch, each 256-byte aligned
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 size_t sas_scratch_bytes(int ntot) {
-    return (size_t)sort_padded_len(2 * (int64_t)ntot) * 12 + (size_t)ntot * 8 + 512;
+    const int64_t ne = 2 * (int64_t)ntot;
+    return align256((size_t)ne * 8) + align256((size_t)ne * 4) + align256((size_t)ntot * 8) +
+           align256((size_t)ntot * 3 * sizeof(float4)) + radix_sort_scratch_bytes(ne) + 256;
+}
+
+// Sort-and-sweep check of one list (single, pl-pl: list 1) or two lists (pl-tp), of one
+// system or, with seg_of (the system of every extent, 2 (n1 + n2) entries), of every system
+// of an ensemble at once: the extents sort into per-system runs and each body sweeps only its
+// own run.  Pairs land unsorted in (o1, o2, olv) with the total in *count.  host_skip: the
+// radix sort reads its digit counts back to skip constant digits (synchronizes the stream).
+int sas_launch(swg_ctx *c, int n1, const double *r1, const double *v1, const double *renc1, int n2, const double *r2,
+               const double *v2, const double *renc2, int single, int shift2, double dt, long long cap, int32_t *o1,
+               int32_t *o2, int32_t *olv, unsigned long long *count, void *scratch, const int32_t *seg_of,
+               int seg_bits, bool host_skip) {
+    const int nb1 = n1, nb2 = single ? 0 : n2;
+    const int ntot = nb1 + nb2;
+    if (ntot <= 0) return SWG_OK;
+    const int64_t ne = 2 * (int64_t)ntot;
+    char *p = (char *)scratch;
+    uint64_t *keys = (uint64_t *)p;
+    uint32_t *vals = (uint32_t *)(p += align256((size_t)ne * 8));
+    int32_t *ibeg = (int32_t *)(p += align256((size_t)ne * 4));
+    int32_t *iend = ibeg + ntot;
+    float4 *FA = (float4 *)(p += align256((size_t)ntot * 8)), *FB = FA + ntot, *FV = FB + ntot;
+    void *rs = p + align256((size_t)ntot * 3 * sizeof(float4));
+    k_sas_extents<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, renc1, nb2, r2, renc2, keys, vals);
+    c->launches++;
+    if (nb1 > 0) {
+        k_encounter_prep<<<(nb1 + 255) / 256, 256, 0, c->stream>>>(nb1, r1, v1, renc1, FA, FB, FV);
+        c->launches++;
+    }
+    if (nb2 > 0) {
+        k_encounter_prep<<<(nb2 + 255) / 256, 256, 0, c->stream>>>(nb2, r2, v2, renc2, FA + nb1, FB + nb1, FV + nb1);
+        c->launches++;
+    }
+    // stable radix sort by extent; the extents enter in index order, so ties keep it
+    SWG_TRY(radix_sort_kv(c, ne, keys, vals, rs, seg_of, seg_bits, host_skip));
+    k_sas_positions<<<(int)((ne + 255) / 256), 256, 0, c->stream>>>(ntot, vals, ibeg, iend);
+    c->launches++;
+    k_sas_sweep<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, v1, renc1, nb2, r2, v2, renc2, single, shift2, dt,
+                                                           vals, ibeg, iend, FA, FB, FV, cap, o1, o2, olv, count);
+    c->launches++;
+    return launch_status(c, "encounter_sas");
 }
 
 // Runs one encounter check; pairs land unsorted in (o1,o2,olv) (first cap of
@@ -446,28 +500,9 @@ int encounter_launch(swg_ctx *c, int mode, int n1, const double *r1, const doubl
                      const double *r2, const double *v2, const double *renc2, int upper, int shift2, double dt,
                      long long cap, int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
                      void *sas_scratch) {
-    if (mode == SWG_ENC_SORTSWEEP) {
-        // single list when upper (pl-pl), double list otherwise
-        const int single = upper ? 1 : 0;
-        const int nb1 = n1, nb2 = single ? 0 : n2;
-        const int ntot = nb1 + nb2;
-        if (ntot <= 0) return SWG_OK;
-        const int64_t n_pad = sort_padded_len(2 * (int64_t)ntot);
-        uint64_t *keys = (uint64_t *)sas_scratch;
-        uint32_t *vals = (uint32_t *)(keys + n_pad);
-        int32_t *ibeg = (int32_t *)(vals + n_pad);
-        int32_t *iend = ibeg + ntot;
-        k_sas_extents<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, renc1, nb2, r2, renc2, keys, vals);
-        c->launches++;
-        SWG_TRY(sort_kv(c, 2 * (int64_t)ntot, keys, vals));
-        k_sas_positions<<<(2 * ntot + 255) / 256, 256, 0, c->stream>>>(ntot, vals, ibeg, iend);
-        c->launches++;
-        k_sas_sweep<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, v1, renc1, nb2, r2, v2, renc2, single,
-                                                               shift2, dt, vals, ibeg, iend, cap, o1, o2, olv,
-                                                               count);
-        c->launches++;
-        return launch_status(c, "encounter_sas");
-    }
+    if (mode == SWG_ENC_SORTSWEEP)  // single list when upper (pl-pl), double list otherwise
+        return sas_launch(c, n1, r1, v1, renc1, n2, r2, v2, renc2, upper ? 1 : 0, shift2, dt, cap, o1, o2, olv, count,
+                          sas_scratch, nullptr, 0, true);
     if (n1 <= 0 || n2 <= 0) return SWG_OK;
     // float copies for the prefilter: list 1 then (unless it is the same list) list 2
     float4 *A1 = (float4 *)sas_scratch, *B1 = A1 + n1, *V1 = B1 + n1;

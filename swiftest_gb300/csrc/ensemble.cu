@@ -56,6 +56,11 @@ struct swg_ensemble {
     std::vector<double> h_GMcb, h_Rcb;
     double dt = 0, rhscale = 6.5, t = 0;
     int lclose = 0, precision = SWG_FP64, initialized = 0, cb_set = 0;
+    // level-0 encounter checks (encounter_check_all_plpl / _pltp modes)
+    int enc_plpl = SWG_ENC_TRIANGULAR, enc_pltp = SWG_ENC_TRIANGULAR;
+    // sort-and-sweep: the system of every extent (pl-pl: 2 NPL; pl-tp: 2 (NPL + NTP)), built on first use
+    int32_t *ext_pp = nullptr, *ext_pt = nullptr;
+    DevBuf sas;  // extents, positions and the radix-sort scratch
     // per system (device)
     int32_t *npl = nullptr, *ntp = nullptr, *poff = nullptr, *toff = nullptr;
     double *GMcb = nullptr, *dcb = nullptr;  // dcb: CB_N doubles per system
@@ -1044,8 +1049,27 @@ SortedSet tp_set(swg_ensemble *e, const double *r, const double *v) {
     return x;
 }
 
+// System of every sort-and-sweep extent: the bodies of list 1 (n1, systems psys) then list
+// 2 (n2, systems tsys), their lower extents first, then their upper ones (k_sas_extents).
+__global__ void k_ext_systems(int64_t n1, const int32_t *__restrict__ psys, int64_t n2,
+                              const int32_t *__restrict__ tsys, int32_t *ext) {
+    const int64_t ntot = n1 + n2;
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= 2 * ntot) return;
+    const int64_t b = k < ntot ? k : k - ntot;
+    ext[k] = b < n1 ? psys[b] : tsys[b - n1];
+}
+
+int bits_for(int32_t n) {
+    int b = 1;
+    while (b < 31 && (int64_t(1) << b) < n) b++;
+    return b;
+}
+
 // One level-0 check (kind 0 pl-pl, 1 pl-tp) of every system into the raw buffer, counted,
 // the count copied to the host.  resort: refresh the radial orders (pl-pl check).
+// SORTSWEEP: one sort of every system's extents (systems as the most significant digits),
+// then each body sweeps its own system's run; the raw list may hold a pair twice.
 int level0_check(swg_ensemble *e, int kind, double dt, bool resort) {
     swg_ctx *c = e->c;
     EncWork &x = kind == 0 ? e->enc_pp : e->enc_pt;
@@ -1053,7 +1077,23 @@ int level0_check(swg_ensemble *e, int kind, double dt, bool resort) {
     int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
     unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
-    if (kind == 0)
+    const int mode = kind == 0 ? e->enc_plpl : e->enc_pltp;
+    if (mode == SWG_ENC_SORTSWEEP) {
+        const int64_t n1 = e->NPL, n2 = kind == 0 ? 0 : e->NTP, ntot = n1 + n2;
+        if (ntot > INT32_MAX / 2) return SWG_ERR_ARG;
+        int32_t *&ext = kind == 0 ? e->ext_pp : e->ext_pt;
+        if (!ext) {
+            SWG_TRY(dalloc(c, &ext, 2 * (size_t)ntot));
+            k_ext_systems<<<grid_for(2 * ntot, 256), 256, 0, c->stream>>>(n1, e->psys, n2, e->tsys, ext);
+            SWG_TRY(L(c, "ext_systems"));
+        }
+        SWG_TRY(ensure(c, e->sas, sas_scratch_bytes((int)ntot)));
+        SWG_TRY(sas_launch(c, (int)n1, e->l0_r, e->l0_v, e->renc, (int)n2, e->l0_tr, e->l0_tv, nullptr, kind == 0, 0,
+                           dt, x.rawcap, i1, i2, lv, cnt, e->sas.ptr, ext, bits_for(e->nsys), false));
+    } else if (kind == 1 && e->enc_plpl == SWG_ENC_SORTSWEEP) {  // pl set prepared by level0_launch
+        SWG_TRY(pltp_sorted_batched(c, false, pl_set(e, e->l0_r, e->l0_v, e->renc), tp_set(e, e->l0_tr, e->l0_tv),
+                                    nullptr, e->n_tsp, e->it_tsp, dt, x.rawcap, i1, i2, lv, cnt, nullptr));
+    } else if (kind == 0)
         SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->l0_r, e->l0_v, e->renc, dt,
                                               resort, e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase,
                                               e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
@@ -1093,6 +1133,10 @@ int level0_launch(swg_ensemble *e, double dt, const double *r, const double *v, 
     const bool resort = e->nchecks++ % RESORT_EVERY == 0;
     h[0] = h[1] = 0;
     if (e->n_tsp > 0) SWG_TRY(sorted_set_prep(c, tp_set(e, tr, tv), e->nsys, resort, dt));
+    // the pl-tp check and the discard scan use the pl radial order and tiles, which a
+    // TRIANGULAR pl-pl check refreshes; after a sweep they are prepared here
+    if (e->n_tsp > 0 && e->enc_plpl == SWG_ENC_SORTSWEEP)
+        SWG_TRY(sorted_set_prep(c, pl_set(e, r, v, e->renc), e->nsys, resort, dt));
     SWG_TRY(level0_check(e, 0, dt, resort));
     if (e->n_tsp > 0) SWG_TRY(level0_check(e, 1, dt, resort));
     return SWG_OK;
@@ -1116,22 +1160,34 @@ int level0_finish(swg_ensemble *e, double dt) {
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->seg_pp, 0, sizeof(int32_t) * 2 * e->nsys, c->stream), "memset"));
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->seg_pt, 0, sizeof(int32_t) * 2 * e->nsys, c->stream), "memset"));
     for (int k = 0; k < 2; k++) {
-        const int64_t n = (int64_t)h[k];  // triangular lists hold no repeated pairs
+        int64_t n = (int64_t)h[k];  // triangular lists hold no repeated pairs; a sweep's may
         if (n == 0) continue;
+        const bool sweep = (k == 0 ? e->enc_plpl : e->enc_pltp) == SWG_ENC_SORTSWEEP;
         EncWork &x = *w[k];
         int32_t **list = k == 0 ? &e->pp_l : &e->pt_l;
         int64_t *cap = k == 0 ? &e->pp_cap : &e->pt_cap;
         SWG_TRY(ensure_pool(e, list, cap, n));
         int32_t *i1 = (int32_t *)x.raw.ptr, *i2 = i1 + x.rawcap, *lv = i2 + x.rawcap;
         unsigned long long *cnt = (unsigned long long *)x.counters.ptr;
+        // the number of distinct pairs of a sweep's list, known once the list is sorted
+        auto unique_count = [&]() -> int {
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(&h[2 + k], cnt + 1, sizeof(unsigned long long),
+                                                   cudaMemcpyDeviceToHost, c->stream),
+                                "count"));
+            SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "count"));
+            n = (int64_t)h[2 + k];
+            return SWG_OK;
+        };
         if (n <= 4096) {
             k_list_finalize<<<1, 1024, 0, c->stream>>>((int)n, i1, i2, lv, *list, *cap, k, e->levelg, e->levelm,
                                                        k == 0 ? e->nplenc : e->ntpenc, e->tlevelg, e->tlevelm,
                                                        e->tnplenc, cnt + 1);
             SWG_TRY(L(c, "list_finalize"));
+            if (sweep) SWG_TRY(unique_count());
         } else {
             SWG_TRY(ensure(c, x.sort, sort_pairs_scratch_bytes(n)));
             SWG_TRY(sort_pairs_unique(c, n, i1, i2, lv, x.sort.ptr, cnt + 1));
+            if (sweep) SWG_TRY(unique_count());
             for (int f = 0; f < 3; f++) {
                 const int32_t *src = f == 0 ? i1 : (f == 1 ? i2 : lv);
                 SWG_TRY(cuda_status(c, cudaMemcpyAsync(*list + f * *cap, src, sizeof(int32_t) * n,
@@ -1902,7 +1958,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
+                    e->enc_pt.counters.ptr, e->ext_pp, e->ext_pt, e->sas.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
@@ -1972,6 +2028,15 @@ int swg_ensemble_set_param(swg_ensemble *e, double dt, double rhscale, int lclos
     e->rhscale = rhscale;
     e->lclose = lclose != 0;
     e->precision = precision;
+    return SWG_OK;
+}
+
+int swg_ensemble_set_encounter_modes(swg_ensemble *e, int enc_plpl, int enc_pltp) {
+    auto ok = [](int m) { return m == SWG_ENC_TRIANGULAR || m == SWG_ENC_SORTSWEEP; };
+    if (!e || !ok(enc_plpl) || !ok(enc_pltp)) return SWG_ERR_ARG;
+    if (e->integrator != SWG_SYMBA) return SWG_ERR_STATE;  // only SyMBA checks encounters
+    e->enc_plpl = enc_plpl;
+    e->enc_pltp = enc_pltp;
     return SWG_OK;
 }
 

@@ -240,6 +240,20 @@ int drift_masked(swg_ctx *c, double mu, double *x, double *v, int32_t n, const i
 
 // encounter.cu -- encounter checks and sorting
 int64_t sort_padded_len(int64_t n);
+// Stable LSD radix sort of (key, val) by key (radix_sort.cu); with seg_of, the segment id
+// seg_of[val] (seg_bits wide) is the most significant part of the key.  host_skip: read a
+// digit histogram back to the host to skip constant digits (synchronizes the stream).
+size_t radix_sort_scratch_bytes(int64_t n);
+int radix_sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals, void *scratch, const int32_t *seg_of,
+                  int seg_bits, bool host_skip);
+size_t util_sort_index_scratch_bytes(int64_t n);
+int util_sort_index(swg_ctx *c, int64_t n, const double *arr, int32_t *ind, void *scratch);
+// sort-and-sweep check (encounter.cu); scratch of sas_scratch_bytes(n1 + n2) (single: n1)
+size_t sas_scratch_bytes(int ntot);
+int sas_launch(swg_ctx *c, int n1, const double *r1, const double *v1, const double *renc1, int n2, const double *r2,
+               const double *v2, const double *renc2, int single, int shift2, double dt, long long cap, int32_t *o1,
+               int32_t *o2, int32_t *olv, unsigned long long *count, void *scratch, const int32_t *seg_of,
+               int seg_bits, bool host_skip);
 size_t sort_pairs_scratch_bytes(int64_t n);
 int sort_pairs_unique(swg_ctx *c, int64_t n, int32_t *i1, int32_t *i2, int32_t *lv, void *scratch,
                       unsigned long long *d_nout);
