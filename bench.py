@@ -390,8 +390,13 @@ def run_path(ctx, wl, precision, steps, warmup, prof_steps=0, clocks=None):
         s.profile(False)
     e1 = s.energy()
     stats = s.stats()
+    plan = None
+    if hasattr(s, "kick_strip") and precision == "MIXED":  # ensembles: the autotuned mixed kicks
+        kv = s.kick_variant()
+        plan = {"plpl": "symmetric" if kv["pl"] == 5 else f"broadcast shape {kv['pl']}",
+                "plpl_strip": s.kick_strip(), "pltp_shape": kv["tp"]}
     s.close()
-    return total_ms, launches, (prof, prof_ms), rel_energy(e0, e1), stats
+    return total_ms, launches, (prof, prof_ms), rel_energy(e0, e1), stats, plan
 
 
 def run_e2e(ctx, wl, precision, steps):
@@ -458,14 +463,17 @@ def reference_arm(args, world, rank):
     return 0
 
 
-def load_traffic():
+def load_traffic(key):
+    """DRAM bytes per launch of a kernel class from the ncu capture recorded in
+    profiles/traffic.json (bytes, the capture's command and the commit it ran), or None."""
     p = ROOT / "profiles" / "traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except json.JSONDecodeError:
-            return {}
-    return {}
+    try:
+        rec = json.loads(p.read_text()).get(key)
+    except (OSError, json.JSONDecodeError):
+        return None, None
+    if not isinstance(rec, dict):
+        return None, None
+    return rec.get("bytes_per_launch"), {k: rec.get(k) for k in ("commit", "command", "note")}
 
 
 def main():
@@ -482,10 +490,10 @@ def main():
     if td:
         td.barrier()
     nprof = max(3, min(10, args.steps))
-    ms_mixed, launches, (prof, prof_ms), err_m, st_m = run_path(ctx, wl, "MIXED", args.steps, args.warmup, nprof,
-                                                                clocks=clocks)
+    ms_mixed, launches, (prof, prof_ms), err_m, st_m, plan = run_path(ctx, wl, "MIXED", args.steps, args.warmup,
+                                                                      nprof, clocks=clocks)
     steps64 = args.steps  # same steps as the mixed arm, so the two |dE/E| are over the same run
-    ms_fp64, _, (prof64, _), err_f, st_f = run_path(ctx, wl, "FP64", steps64, args.warmup, nprof)
+    ms_fp64, _, (prof64, _), err_f, st_f, _ = run_path(ctx, wl, "FP64", steps64, args.warmup, nprof)
     e2e_ms, e2e_bytes = run_e2e(ctx, wl, "MIXED", args.steps)
     ms_mixed, ms_fp64, e2e_ms = max_over_ranks(td, [ms_mixed, ms_fp64, e2e_ms])
     nb = wl.nbodies
@@ -495,7 +503,7 @@ def main():
     # roofline of the pair kick (mixed path), from the live CUDA-event profile on the library's stream
     peak32 = ctx.probe_peak_tflops("fp32")
     peak64 = ctx.probe_peak_tflops("fp64")
-    traffic = load_traffic()
+    traffic, traffic_src = load_traffic(f"kick_pl_{args.workload}")
     roof = None
     kick = prof["kick_pl"]
     if kick["launches"]:
@@ -507,7 +515,7 @@ def main():
                 "peak_source": "FP32 FFMA-chain probe measured by bench.py on this GPU (MEASURED_PEAKS.json has no "
                                "FP32 figure)",
                 "algorithmic_flops_per_launch": flops, "avg_launch_ms": avg_ms,
-                "traffic": traffic.get(f"kick_pl_{args.workload}")}
+                "traffic": traffic, "traffic_source": traffic_src}
     kernel_profile = {"steps": nprof, "ms_per_step": prof_ms / nprof,
                       **{k: {"launches": v["launches"], "ms_total": round(v["ms"], 4),
                              "share": round(v["ms"] / prof_ms, 4)} for k, v in prof.items()}}
@@ -522,7 +530,7 @@ def main():
                       "stats": st_f,
                       "kernel_profile": {k: {"launches": v["launches"], "ms_total": round(v["ms"], 4)}
                                          for k, v in prof64.items()}},
-        "mixed_path": {**err_summary(*err_m), "stats": st_m},
+        "mixed_path": {**err_summary(*err_m), "stats": st_m, "kick_plan": plan},
         "speedup_mixed_vs_fp64": value / fp64_value,
         "pair_interactions_per_s": whole_job_rate(world, wl.pairs_per_step, args.steps, ms_mixed),
         "kernel_profile": kernel_profile, "dominant_kernel_class": dom,

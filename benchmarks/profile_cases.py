@@ -3,7 +3,7 @@
     python benchmarks/profile_cases.py <case> [--npl N] [--ntp M] [--reps R]
 
 cases: kick_tp_mixed, kick_pl_mixed, kick_tp_fp64, kick_pl_fp64, drift, encounter_pltp,
-encounter_plpl, symba_mixed, symba_fp64 (inputs: the seeded C1 disk, AU, Msun, yr), and
+encounter_plpl (and _sas: sort-and-sweep), symba_mixed, symba_fp64 (inputs: the seeded C1 disk, AU, Msun, yr), and
 ens_mixed, ens_fp64 (steps of a batched ensemble, first --nsys systems: --ensemble C4, the
 SyMBA disks, or C3 / C3W, the HELIO / WHM systems with 5 tp per pl).
 Prints the average wall time per call (host buffers, so it includes the copies).
@@ -28,8 +28,10 @@ def main(argv=None):
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--nsys", type=int, default=None)
     p.add_argument("--ensemble", default="C4", choices=["C4", "C3", "C3W"])
+    p.add_argument("--encounter", default="TRIANGULAR", choices=["TRIANGULAR", "SORTSWEEP"],
+                   help="level-0 check mode of the SyMBA cases")
     a = p.parse_args(argv)
-    from swiftest_gb300 import SWG_FP64, SWG_MIXED
+    from swiftest_gb300 import SWG_ENC_SORTSWEEP, SWG_FP64, SWG_MIXED
     from swiftest_gb300 import build as B
     from swiftest_gb300 import initial_conditions as IC
     from swiftest_gb300.api import Context, NBodySystem
@@ -48,18 +50,25 @@ def main(argv=None):
         "drift": lambda: ctx.drift_all(IC.GMCB, tp["rh"], tp["vh"], 0.005),
         "encounter_pltp": lambda: ctx.encounter_check_all_pltp(pl["rh"], pl["vh"], tp["rh"], tp["vh"], renc, 0.005),
         "encounter_plpl": lambda: ctx.encounter_check_all_plpl(pl["rh"], pl["vh"], renc, 0.005),
+        "encounter_pltp_sas": lambda: ctx.encounter_check_all_pltp(pl["rh"], pl["vh"], tp["rh"], tp["vh"], renc, 0.005,
+                                                                   mode=SWG_ENC_SORTSWEEP),
+        "encounter_plpl_sas": lambda: ctx.encounter_check_all_plpl(pl["rh"], pl["vh"], renc, 0.005,
+                                                                   mode=SWG_ENC_SORTSWEEP),
     }
+    enc = {} if a.encounter == "TRIANGULAR" else dict(encounter_check_plpl=a.encounter,
+                                                      encounter_check_pltp=a.encounter)
     if a.case.startswith("ens"):
         from swiftest_gb300.api import Ensemble
         if a.ensemble == "C3W":
             E = IC.make_ensemble("C3", nsys=a.nsys, integrator="WHM")
         else:
             E = IC.make_ensemble(a.ensemble, nsys=a.nsys)
-        ens = Ensemble(ctx, E, precision="MIXED" if a.case.endswith("mixed") else "FP64")
+        ens = Ensemble(ctx, E, precision="MIXED" if a.case.endswith("mixed") else "FP64",
+                       **(enc if E["integrator"] == "SYMBA" else {}))
         run = lambda: ens.step(1)  # noqa: E731
     elif a.case.startswith("symba"):
         prec = "MIXED" if a.case.endswith("mixed") else "FP64"
-        s = NBodySystem(ctx, "SYMBA", cb, pl, tp, dt=0.005, rhscale=1.0, precision=prec)
+        s = NBodySystem(ctx, "SYMBA", cb, pl, tp, dt=0.005, rhscale=1.0, precision=prec, **enc)
         run = lambda: s.step(1)  # noqa: E731
     else:
         run = cases[a.case]

@@ -318,6 +318,11 @@ module swiftest_gb300_mod
          type(c_ptr), value :: ens
          integer(c_int), value :: enc_plpl, enc_pltp
       end function
+      integer(c_int) function swg_ensemble_set_kick_strip(ens, strip) bind(C, name="swg_ensemble_set_kick_strip")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: ens
+         integer(c_int), value :: strip
+      end function
       integer(c_int) function swg_ensemble_initialize(ens) bind(C, name="swg_ensemble_initialize")
          import :: c_ptr, c_int
          type(c_ptr), value :: ens

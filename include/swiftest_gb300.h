@@ -248,10 +248,18 @@ int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
  * accelerations; the symmetric kernel adds the same terms in another order.  Variants
  * 0 .. SWG_KICK_NVARIANT-1 force that broadcast shape on both kinds.  kick_variant reads
  * the kernel in use for kind 0 (pl-pl) or 1 (pl-tp), -1 before the first mixed kick of
- * that kind. */
+ * that kind, and with kind 2 the symmetric kick's strip length. */
 #define SWG_KICK_NVARIANT 5
 #define SWG_KICK_SYMMETRIC 5
 int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
+/* Strip length of the symmetric pl-pl kick: each work item evaluates one row tile against
+ * `strip` tile pairs, and a body's sums are split into one slot per item, so the strip sets
+ * how the terms are grouped (results within the mixed-kick tolerance of each other, each
+ * deterministic).  By default (0) the fastest of 1, 2, 4, 8, 16 is timed on the ensemble's
+ * own data at its first mixed kick and cached like the tile shapes; 1, 2, 4, 8 or 16 forces
+ * it.  swg_ensemble_kick_variant with kind 2 reads the strip in use (-1 before the first
+ * mixed kick). */
+int swg_ensemble_set_kick_strip(swg_ensemble *ens, int strip);
 /* swiftest_kick_getacch_int_all_tri_pl (swiftest_kick.f90:183-264) of every system from its
  * current positions, in the ensemble's precision and pair rule (radius guard for SyMBA or
  * with close-encounter checks): acc[3*NPL] on the host, zero-based sums over all pairs. */

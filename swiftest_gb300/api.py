@@ -454,6 +454,17 @@ class Ensemble:
         use the default (-1): symmetric pl-pl kernel, autotuned pl-tp shape."""
         self.ctx.check("swg_ensemble_set_kick_variant", self.ctx.lib.swg_ensemble_set_kick_variant(self.h, int(variant)))
 
+    def set_kick_strip(self, strip: int = 0):
+        """Force the symmetric pl-pl kick's strip length (1, 2, 4, 8 or 16 tile pairs per
+        item), or let the autotuner choose it (0)."""
+        self.ctx.check("swg_ensemble_set_kick_strip", self.ctx.lib.swg_ensemble_set_kick_strip(self.h, int(strip)))
+
+    def kick_strip(self) -> int:
+        """Strip length of the symmetric pl-pl kick in use (-1 before the first mixed kick)."""
+        v = C.c_int(-1)
+        self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, 2, C.byref(v)))
+        return int(v.value)
+
     def getacch_int_pl(self):
         """Pair accelerations of every system's massive bodies from the current positions."""
         out = np.zeros((int(self.poff[-1]), 3))

@@ -6,6 +6,7 @@
 // fastest.  Choices are kept for the process and appended to a small text file so later
 // runs skip the timing: $SWG_TUNE_CACHE if set, else $HOME/.cache/swiftest_gb300/kick_tune.txt
 // (no file is written when neither is available).  One line per choice: "<key> <variant>".
+// The symmetric pl-pl kick's strip length is kept the same way, as log2(strip).
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
@@ -45,7 +46,7 @@ void load_locked() {
     char key[512];
     int v = 0;
     while (std::fscanf(f, "%511s %d", key, &v) == 2)
-        if (v >= 0 && v < KICK_NVARIANT) g_tune[key] = v;
+        if (v >= 0 && v < 16) g_tune[key] = v;  // callers check the range of their own keys
     std::fclose(f);
 }
 

@@ -114,6 +114,7 @@ struct swg_ensemble {
     // symmetric pl-pl mixed kick (the default): tile-pair items, each system's first slot, slot sums
     int4 *it_sym = nullptr;
     int n_sym = 0, sym_strip = 1;
+    int force_strip = 0;  // > 0: strip length of the symmetric kick forced (0: tuned)
     int32_t *sym_base = nullptr;
     float *sym_part = nullptr, *sym_ppart = nullptr;  // receiver slots, then pair slots (one allocation)
     unsigned *head = nullptr;
@@ -817,6 +818,68 @@ int time_kick_variants(swg_ensemble *e, int k, bool rad, unsigned *head, const i
     return SWG_OK;
 }
 
+// The symmetric pl-pl kick's plan for row strips of `strip` tile pairs: items, per-system
+// slot bases and the receiver and pair slots (replacing any previous plan).
+int build_sym_plan(swg_ensemble *e, int strip) {
+    swg_ctx *c = e->c;
+    std::vector<int4> items;
+    std::vector<int32_t> base;
+    int64_t npair = 0;
+    const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), strip, items, base, &npair);
+    SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
+    if (e->sym_base) cudaFree(e->sym_base);
+    if (e->sym_part) cudaFree(e->sym_part);
+    e->sym_base = nullptr;
+    e->sym_part = nullptr;
+    SWG_TRY(dalloc(c, &e->sym_base, base.size()));
+    SWG_TRY(upload(c, e->sym_base, base));
+    SWG_TRY(dalloc(c, &e->sym_part, (size_t)(6 * nrecv + 3 * npair) * KICK_SYM_TILE));
+    e->sym_ppart = e->sym_part + (size_t)nrecv * 6 * KICK_SYM_TILE;
+    e->sym_strip = strip;
+    return SWG_OK;
+}
+
+// Strip lengths (tile pairs per work item) the autotuner tries for the symmetric kick.  The
+// strip decides how each body's receiver sums are split into slots, so unlike the
+// broadcast shapes the strips add the same terms in different groupings: results agree
+// within the mixed-kick tolerance, and each strip is deterministic.
+constexpr int SYM_STRIPS[] = {1, 2, 4, 8, 16};
+constexpr int SYM_NSTRIP = 5;
+
+// Times the symmetric kick (pair kernel and per-body sums, one warm-up and three timed
+// launches into scratch accelerations) for every candidate strip on this ensemble's
+// current data and returns the fastest; the partners must be split into kA/kB.
+int time_sym_strips(swg_ensemble *e, bool rad, unsigned *head, int *best) {
+    swg_ctx *c = e->c;
+    TuneScratch t;
+    SWG_TRY(dalloc(c, &t.acc, 3 * (size_t)e->NPL));
+    for (cudaEvent_t &x : t.ev) SWG_TRY(cuda_status(c, cudaEventCreate(&x), "event"));
+    const float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
+    float best_ms = 0.f;
+    *best = SYM_STRIPS[0];
+    for (int q = 0; q < SYM_NSTRIP; q++) {
+        SWG_TRY(build_sym_plan(e, SYM_STRIPS[q]));
+        auto once = [&]() -> int {
+            SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
+                                           e->sym_part, e->sym_ppart, head));
+            return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
+                                         e->sym_ppart, t.acc, 1, nullptr, 0);
+        };
+        SWG_TRY(once());
+        SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[0], c->stream), "event"));
+        for (int rep = 0; rep < 3; rep++) SWG_TRY(once());
+        SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[1], c->stream), "event"));
+        SWG_TRY(cuda_status(c, cudaEventSynchronize(t.ev[1]), "event"));
+        float ms = 0.f;
+        SWG_TRY(cuda_status(c, cudaEventElapsedTime(&ms, t.ev[0], t.ev[1]), "event"));
+        if (q == 0 || ms < best_ms) {
+            best_ms = ms;
+            *best = SYM_STRIPS[q];
+        }
+    }
+    return SWG_OK;
+}
+
 // Makes sure the mixed kick of kind k has a tile shape and items: the forced shape, else
 // the cached choice for (GPU, kind, size bucket), else the fastest one timed here (and
 // cached).  Runs eagerly at the first such kick; a CUDA graph capture never meets an
@@ -832,18 +895,22 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
         return SWG_ERR_STATE;
     }
     int v = e->force_variant;
-    if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel (built once)
+    if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel, its strip forced, cached or timed here
         if (!e->it_sym) {
-            std::vector<int4> items;
-            std::vector<int32_t> base;
-            int64_t npair = 0;
-            e->sym_strip = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms);
-            const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), e->sym_strip, items, base, &npair);
-            SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
-            SWG_TRY(dalloc(c, &e->sym_base, base.size()));
-            SWG_TRY(upload(c, e->sym_base, base));
-            SWG_TRY(dalloc(c, &e->sym_part, (size_t)(6 * nrecv + 3 * npair) * KICK_SYM_TILE));
-            e->sym_ppart = e->sym_part + (size_t)nrecv * 6 * KICK_SYM_TILE;
+            int strip = e->force_strip;
+            if (strip <= 0) {
+                const std::string key = tune_key(c->device, rad ? "kick_sym_rad" : "kick_sym", size_bucket(e, 0));
+                const int l = tune_lookup(key);  // cached as log2(strip)
+                if (l >= 0 && l < SYM_NSTRIP) {
+                    strip = 1 << l;
+                } else {
+                    SWG_TRY(time_sym_strips(e, rad, head, &strip));
+                    int lg = 0;
+                    while ((1 << lg) < strip) lg++;
+                    tune_store(key, lg);
+                }
+            }
+            SWG_TRY(build_sym_plan(e, strip));
         }
         e->kv[0] = KICK_SYMMETRIC;
         return SWG_OK;
@@ -2313,8 +2380,23 @@ int swg_ensemble_set_kick_variant(swg_ensemble *e, int variant) {
 }
 
 int swg_ensemble_kick_variant(swg_ensemble *e, int kind, int *variant) {
-    if (!e || !variant || kind < 0 || kind > 1) return SWG_ERR_ARG;
-    *variant = e->kv[kind];
+    if (!e || !variant || kind < 0 || kind > 2) return SWG_ERR_ARG;
+    if (kind == 2)
+        *variant = e->it_sym ? e->sym_strip : -1;
+    else
+        *variant = e->kv[kind];
+    return SWG_OK;
+}
+
+int swg_ensemble_set_kick_strip(swg_ensemble *e, int strip) {
+    if (!e || !(strip == 0 || strip == 1 || strip == 2 || strip == 4 || strip == 8 || strip == 16))
+        return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick strip"));
+    e->force_strip = strip;
+    if (e->it_sym) cudaFree(e->it_sym);
+    e->it_sym = nullptr;
+    e->n_sym = 0;
+    reset_kick_plans(e);
     return SWG_OK;
 }
 

@@ -260,6 +260,26 @@ def test_ensemble_getacch_mixed_tolerance(ctx, integrator, lclose):
         ens.close()
 
 
+@pytest.mark.parametrize("strip", [1, 2, 4, 8, 16, 0])
+def test_symmetric_kick_strips(ctx, strip):
+    # every strip length of the symmetric pl-pl kick (forced, and the autotuned default):
+    # within the mixed-kick tolerance of the oracle's FP64 triangular kick, and deterministic
+    E = IC.make_ensemble("C4", nsys=4, scale=0.5)
+    want = [O.kick_tri_pl(pl["rh"], pl["Gmass"], pl["radius"]) for pl, _ in E["systems"]]
+    ens = Ensemble(ctx, E, precision="MIXED")
+    ens.set_kick_strip(strip)
+    g = ens.getacch_int_pl()
+    used = ens.kick_strip()
+    assert used == strip if strip else used in (1, 2, 4, 8, 16)
+    for s, r in enumerate(want):
+        a, b = ens.poff[s], ens.poff[s + 1]
+        e = np.linalg.norm(g[a:b] - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
+        assert e.max() < 2e-5, (strip, s, e.max())
+        assert np.sqrt(np.mean(e ** 2)) < 1e-6, (strip, s)
+    assert np.array_equal(g, ens.getacch_int_pl())
+    ens.close()
+
+
 def test_mixed_drift_matches_fp64_drift(ctx):
     # massless bodies feel no pair forces and move the central body not at all, so the
     # mixed and FP64 ensembles differ only in the drift: the fast FP64 solver form of the
