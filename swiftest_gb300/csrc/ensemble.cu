@@ -846,17 +846,19 @@ int build_sym_plan(swg_ensemble *e, int strip) {
 constexpr int SYM_STRIPS[] = {1, 2, 4, 8, 16};
 constexpr int SYM_NSTRIP = 5;
 
-// Times the symmetric kick (pair kernel and per-body sums, one warm-up and three timed
-// launches into scratch accelerations) for every candidate strip on this ensemble's
-// current data and returns the fastest; the partners must be split into kA/kB.
+// Times the symmetric kick (pair kernel and per-body sums into scratch accelerations) for
+// every candidate strip on this ensemble's current data: one warm-up, then the shortest of
+// five launches timed one by one.  The strip of kick_sym_strip stays unless another is
+// faster by more than 3%, so that timing noise does not move the choice between
+// near-equal strips; the partners must be split into kA/kB.
 int time_sym_strips(swg_ensemble *e, bool rad, unsigned *head, int *best) {
     swg_ctx *c = e->c;
     TuneScratch t;
     SWG_TRY(dalloc(c, &t.acc, 3 * (size_t)e->NPL));
     for (cudaEvent_t &x : t.ev) SWG_TRY(cuda_status(c, cudaEventCreate(&x), "event"));
     const float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
-    float best_ms = 0.f;
-    *best = SYM_STRIPS[0];
+    const int deflt = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms);
+    float ms_strip[SYM_NSTRIP], best_ms = 0.f, deflt_ms = 0.f;
     for (int q = 0; q < SYM_NSTRIP; q++) {
         SWG_TRY(build_sym_plan(e, SYM_STRIPS[q]));
         auto once = [&]() -> int {
@@ -866,17 +868,25 @@ int time_sym_strips(swg_ensemble *e, bool rad, unsigned *head, int *best) {
                                          e->sym_ppart, t.acc, 1, nullptr, 0);
         };
         SWG_TRY(once());
-        SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[0], c->stream), "event"));
-        for (int rep = 0; rep < 3; rep++) SWG_TRY(once());
-        SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[1], c->stream), "event"));
-        SWG_TRY(cuda_status(c, cudaEventSynchronize(t.ev[1]), "event"));
-        float ms = 0.f;
-        SWG_TRY(cuda_status(c, cudaEventElapsedTime(&ms, t.ev[0], t.ev[1]), "event"));
-        if (q == 0 || ms < best_ms) {
-            best_ms = ms;
+        ms_strip[q] = 3.0e38f;
+        for (int rep = 0; rep < 5; rep++) {
+            SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[0], c->stream), "event"));
+            SWG_TRY(once());
+            SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[1], c->stream), "event"));
+            SWG_TRY(cuda_status(c, cudaEventSynchronize(t.ev[1]), "event"));
+            float ms = 0.f;
+            SWG_TRY(cuda_status(c, cudaEventElapsedTime(&ms, t.ev[0], t.ev[1]), "event"));
+            ms_strip[q] = std::min(ms_strip[q], ms);
+        }
+        if (SYM_STRIPS[q] == deflt) deflt_ms = ms_strip[q];
+    }
+    *best = deflt;
+    best_ms = deflt_ms;
+    for (int q = 0; q < SYM_NSTRIP; q++)
+        if (ms_strip[q] < 0.97f * deflt_ms && ms_strip[q] < best_ms) {
+            best_ms = ms_strip[q];
             *best = SYM_STRIPS[q];
         }
-    }
     return SWG_OK;
 }
 
