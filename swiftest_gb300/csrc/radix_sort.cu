@@ -8,8 +8,8 @@
 // extent in a batched ensemble) forms the most significant digits: one call sorts every
 // system's extents into contiguous per-system runs.
 //
-// Passes: 8-bit digits, least significant first, each a reduce-then-scan over tiles of
-// RS_TILE elements: per-tile digit counts (k_rs_upsweep), an exclusive scan of the counts in
+// Passes: 8-bit digits, least significant first, each a reduce-then-scan over tiles of 256
+// to 2048 elements (fewer per tile for small sorts): per-tile digit counts (k_rs_upsweep), an exclusive scan of the counts in
 // digit-major order (k_rs_scan), and a stable scatter (k_rs_scatter) that ranks the tile's
 // elements column by column with warp match_any and per-warp prefix counts in shared
 // memory.  One pass over the data first counts every digit of every pass
@@ -30,8 +30,7 @@ namespace {
 
 constexpr int RS_BINS = 256;
 constexpr int RS_THREADS = 256;
-constexpr int RS_COLS = 8;                       // elements per thread per tile
-constexpr int RS_TILE = RS_THREADS * RS_COLS;    // 2048
+constexpr int RS_COLS = 8;                       // most elements per thread per tile (tiles of up to 2048)
 constexpr int RS_KEY_PASSES = 8;                 // 64-bit keys
 constexpr int RS_MAX_SEG_PASSES = 4;             // 32-bit segment ids
 constexpr int RS_MAX_PASSES = RS_KEY_PASSES + RS_MAX_SEG_PASSES;
@@ -64,14 +63,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist_all(int64_t n, const uin
 // per-tile digit counts of pass p: cnt[d * ntiles + tile]
 __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(int64_t n, const uint64_t *__restrict__ keys,
                                                            const uint32_t *__restrict__ vals,
-                                                           const int32_t *__restrict__ seg_of, int p,
+                                                           const int32_t *__restrict__ seg_of, int p, int cols,
                                                            unsigned *__restrict__ cnt) {
     __shared__ unsigned sh[RS_BINS];
     sh[threadIdx.x] = 0u;
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
-#pragma unroll
-    for (int c = 0; c < RS_COLS; c++) {
+    const int64_t base = (int64_t)blockIdx.x * RS_THREADS * cols;
+    for (int c = 0; c < cols; c++) {
         const int64_t e = base + c * RS_THREADS + threadIdx.x;
         if (e < n) atomicAdd(&sh[rs_digit(p, keys[e], vals[e], seg_of)], 1u);
     }
@@ -118,7 +116,7 @@ __global__ void __launch_bounds__(1024) k_rs_scan(int64_t m, unsigned *__restric
 // columns (element c * 256 + t at column c), which is its element order.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(int64_t n, const uint64_t *__restrict__ kin,
                                                            const uint32_t *__restrict__ vin,
-                                                           const int32_t *__restrict__ seg_of, int p,
+                                                           const int32_t *__restrict__ seg_of, int p, int cols,
                                                            const unsigned *__restrict__ off,
                                                            uint64_t *__restrict__ kout, uint32_t *__restrict__ vout) {
     constexpr int NW = RS_THREADS / 32;
@@ -126,8 +124,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(int64_t n, const uint
     __shared__ unsigned s_wc[NW][RS_BINS];    // per-warp counts, then per-warp offsets, of one column
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     s_base[t] = off[(int64_t)t * gridDim.x + blockIdx.x];
-    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
-    for (int c = 0; c < RS_COLS; c++) {
+    const int64_t base = (int64_t)blockIdx.x * RS_THREADS * cols;
+    for (int c = 0; c < cols; c++) {
 #pragma unroll
         for (int q = 0; q < NW; q++) s_wc[q][t] = 0u;
         __syncthreads();
@@ -202,8 +200,16 @@ int util_sort_index(swg_ctx *c, int64_t n, const double *arr, int32_t *ind, void
     return launch_status(c, "sort_index_out");
 }
 
+// Elements per thread of a tile: fewer for small sorts, so that the tiles still spread
+// over the SMs (two per SM where n allows), at most RS_COLS.
+static int rs_cols(int64_t n, int num_sms) {
+    const int64_t per = (int64_t)RS_THREADS * 2 * (num_sms > 0 ? num_sms : 152);
+    const int64_t cols = n / per;
+    return (int)(cols < 1 ? 1 : (cols > RS_COLS ? RS_COLS : cols));
+}
+
 size_t radix_sort_scratch_bytes(int64_t n) {
-    const int64_t ntiles = (n + RS_TILE - 1) / RS_TILE;
+    const int64_t ntiles = (n + RS_THREADS - 1) / RS_THREADS;  // enough for any tile size
     return (size_t)n * 12 + (size_t)ntiles * RS_BINS * 4 + RS_MAX_PASSES * RS_BINS * 4 + 1024;
 }
 
@@ -212,7 +218,8 @@ int radix_sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals, void *s
     if (n <= 1) return SWG_OK;
     if (n > 0xffffffffll || seg_bits < 0 || seg_bits > 8 * RS_MAX_SEG_PASSES || (seg_bits > 0 && !seg_of))
         return SWG_ERR_ARG;
-    const int64_t ntiles = (n + RS_TILE - 1) / RS_TILE;
+    const int cols = rs_cols(n, c->num_sms);
+    const int64_t tile = (int64_t)RS_THREADS * cols, ntiles = (n + tile - 1) / tile;
     const int nseg = seg_of ? (seg_bits + 7) / 8 : 0;
     const int npass = RS_KEY_PASSES + nseg;
     uint64_t *k2 = (uint64_t *)scratch;
@@ -239,9 +246,9 @@ int radix_sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals, void *s
         bool trivial = false;
         for (int d = 0; d < RS_BINS && host_skip; d++) trivial |= h[p * RS_BINS + d] == (unsigned)n;
         if (trivial) continue;  // every element has the same digit: the pass keeps the order
-        k_rs_upsweep<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cnt);
+        k_rs_upsweep<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cols, cnt);
         k_rs_scan<<<1, 1024, 0, c->stream>>>(ntiles * RS_BINS, cnt);
-        k_rs_scatter<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cnt, kout, vout);
+        k_rs_scatter<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cols, cnt, kout, vout);
         c->launches += 3;
         SWG_TRY(launch_status(c, "radix_pass"));
         std::swap(kin, kout);
