@@ -18,7 +18,9 @@
 //      vh are not refreshed after this, the merged ones get theirs from b2h) and position
 //      (rh2rb, which also gives every body's rb);
 //   2. E_before, L_before: the system's energy and angular momentum
-//      (swiftest_util_get_energy_and_momentum_system, swiftest_util.f90:1172-1401);
+//      (swiftest_util_get_energy_and_momentum_system, swiftest_util.f90:1172-1401); its
+//      O(N^2) pairwise potential is formed on the device (k_pot_terms, k_pot_rowsum: each
+//      row added in ascending j), the rows and the O(N) terms are added here in index order;
 //   3. each COLLIDED pair whose two bodies were both flagged by the check, in list order:
 //      the impactors' centre of mass (rb = rh + cb rb), the angular momentum of each impactor
 //      about it, L_escape += both (no rotation: the reference books the pre-collision
@@ -51,7 +53,8 @@
 // ACTIVE again and merges in the cascade if it still collides).
 // pl-tp: the test particle of every collided pair is discarded (collision_resolve_pltp).
 // The OpenMP sums of the reference are taken in index order.  This file is compiled with
-// -ffp-contract=off, so the arithmetic is the C oracle's, bit for bit.
+// -ffp-contract=off on the host and -fmad=false on the device, so the arithmetic is the C
+// oracle's, bit for bit.
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -69,23 +72,68 @@ constexpr double PI = 3.141592653589793238462643383279502884197;
 constexpr double THIRD = 0.333333333333333333333333333333333333333;
 constexpr int MAXCASCADE = 1000;  // collision_resolve.f90:543
 
-// gfortran NORM2 (used by the operators .mag. and .unit.): scaled sum of squares
-double norm2_3(const double *x) {
-    double scale = 0.0, ssq = 1.0;
-    for (int k = 0; k < 3; k++) {
-        if (x[k] != 0.0) {
-            const double absx = std::fabs(x[k]);
-            if (scale < absx) {
-                const double q = scale / absx;
-                ssq = 1.0 + ssq * q * q;
-                scale = absx;
-            } else {
-                const double q = absx / scale;
-                ssq = ssq + q * q;
-            }
-        }
+// gfortran NORM2 (used by the operators .mag. and .unit.)
+double norm2_3(const double *x) { return hd_norm2_3(x[0], x[1], x[2]); }
+
+// ---- the O(N^2) part of the resolution's energies on the device
+// Term (i, j) of the pairwise potential for i < j < n, j in [j0, j1), at
+// terms[(j - j0) * n + i]; zero where either body is INACTIVE (adding +0.0 to a row that
+// starts at +0.0 and only gains negative terms leaves it unchanged, as skipping does).
+__global__ void __launch_bounds__(128) k_pot_terms(int n, int j0, int j1, const double *__restrict__ rb,
+                                                   const double *__restrict__ Gm, const int32_t *__restrict__ st,
+                                                   double *__restrict__ terms) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = j0 + (int)blockIdx.y;
+    if (i >= n || j >= j1 || i >= j) return;
+    const bool on = st[i] != ST_INACTIVE && st[j] != ST_INACTIVE;
+    terms[(size_t)(j - j0) * n + i] = on ? hd_pot_term(rb + 3 * (size_t)i, rb + 3 * (size_t)j, Gm[i], Gm[j]) : 0.0;
+}
+// Row i of the potential, one thread per row: the terms added in ascending j (the
+// reference's sum(pepl(i+1:npl)), swiftest_util.f90:1386), continued over j chunks.
+__global__ void __launch_bounds__(32) k_pot_rowsum(int n, int j0, int j1, const double *__restrict__ terms,
+                                                   double *__restrict__ rows) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double r = j0 == 0 ? 0.0 : rows[i];
+    int j = j0 > i + 1 ? j0 : i + 1;
+    const double *t = terms + (size_t)(j - j0) * n + i;
+    for (; j + 8 <= j1; j += 8, t += 8 * (size_t)n) {
+        double v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = t[(size_t)k * n];
+#pragma unroll
+        for (int k = 0; k < 8; k++) r = r + v[k];
     }
-    return scale * std::sqrt(ssq);
+    for (; j < j1; j++, t += n) r = r + *t;
+    rows[i] = r;
+}
+
+// rows[i] = sum over j > i of the potential terms, computed on c's device (scratch slot 23)
+int device_pot_rows(swg_ctx *c, int n, const double *rb, const double *Gm, const int32_t *st, double *rows) {
+    if (n <= 0) return SWG_OK;
+    const size_t un = (size_t)n;
+    const size_t J = std::max<size_t>(1, std::min<size_t>(std::min<size_t>(un, ((size_t)16 << 20) / un), 65535));
+    const size_t head = 5 * un * sizeof(double) + ((un * sizeof(int32_t) + 255) & ~(size_t)255);
+    void *p = nullptr;
+    SWG_TRY(ensure_slot(c, 23, head + J * un * sizeof(double), &p));
+    double *drb = (double *)p, *dGm = drb + 3 * un, *drows = dGm + un;
+    int32_t *dst = (int32_t *)(drows + un);
+    double *terms = (double *)((char *)p + head);
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(drb, rb, 3 * un * sizeof(double), cudaMemcpyHostToDevice, c->stream), "pot"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(dGm, Gm, un * sizeof(double), cudaMemcpyHostToDevice, c->stream), "pot"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(dst, st, un * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream), "pot"));
+    for (size_t j0 = 0; j0 < un; j0 += J) {
+        const size_t j1 = std::min(un, j0 + J);
+        k_pot_terms<<<dim3((unsigned)((un + 127) / 128), (unsigned)(j1 - j0)), 128, 0, c->stream>>>(
+            n, (int)j0, (int)j1, drb, dGm, dst, terms);
+        c->launches++;
+        SWG_TRY(launch_status(c, "pot_terms"));
+        k_pot_rowsum<<<(unsigned)((un + 31) / 32), 32, 0, c->stream>>>(n, (int)j0, (int)j1, terms, drows);
+        c->launches++;
+        SWG_TRY(launch_status(c, "pot_rowsum"));
+    }
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(rows, drows, un * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "pot"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "pot");
 }
 
 // operator .unit. (src/operator/operator_unit.f90)
@@ -145,9 +193,12 @@ struct Resolver {
     std::vector<unsigned char> coll;
     double cbrb[3] = {0.0, 0.0, 0.0}, cbvb[3] = {0.0, 0.0, 0.0};
 
+    std::vector<double> prow;  // rows of the pairwise potential
+    bool dev_failed = false;
+
     explicit Resolver(CollisionSystem &cs)
         : c(cs), rb(3 * (size_t)std::max(cs.npl, 1)), vh(3 * (size_t)std::max(cs.npl, 1)),
-          coll((size_t)std::max(cs.npl, 1), 0) {}
+          coll((size_t)std::max(cs.npl, 1), 0), prow((size_t)std::max(cs.npl, 1)) {}
 
     bool active(int32_t i) const { return c.status[i] != ST_INACTIVE; }
 
@@ -178,8 +229,10 @@ struct Resolver {
     }
 
     // swiftest_util_get_energy_and_momentum_system with the triangular potential, as the
-    // resolution calls it: no spin terms, cb rb/vb as the sync left them
-    void energy(double &te, double *L) const {
+    // resolution calls it: no spin terms, cb rb/vb as the sync left them.  The potential's
+    // rows (each added in ascending j) are formed on the device, the rows are added here in
+    // index order; with_te = false leaves te unset and forms only L.
+    void energy(double &te, double *L, bool with_te = true) {
         const double mcb = c.GMcb;
         const double kecb = mcb * (cbvb[0] * cbvb[0] + cbvb[1] * cbvb[1] + cbvb[2] * cbvb[2]);
         const double Lcb[3] = {mcb * (cbrb[1] * cbvb[2] - cbrb[2] * cbvb[1]),
@@ -195,18 +248,16 @@ struct Resolver {
             Lsum[2] = Lsum[2] + m * (r[0] * v[1] - r[1] * v[0]);
             kesum = kesum + m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         }
-        double pe = 0.0;
-        for (int32_t i = 0; i < c.npl; i++) {
-            if (!active(i)) continue;
-            double row = 0.0;
-            for (int32_t j = i + 1; j < c.npl; j++) {
-                if (!active(j)) continue;
-                const double d[3] = {rb[3 * i] - rb[3 * j], rb[3 * i + 1] - rb[3 * j + 1],
-                                     rb[3 * i + 2] - rb[3 * j + 2]};
-                row = row + (-(c.Gm[i] * c.Gm[j]) / norm2_3(d));
-            }
-            pe = pe + row;
+        for (int d = 0; d < 3; d++) L[d] = Lcb[d] + Lsum[d];
+        if (!with_te) return;
+        if (!c.dev || device_pot_rows(c.dev, c.npl, rb.data(), c.Gm, c.status, prow.data()) != SWG_OK) {
+            dev_failed = true;
+            te = 0.0;
+            return;
         }
+        double pe = 0.0;
+        for (int32_t i = 0; i < c.npl; i++)
+            if (active(i)) pe = pe + prow[i];
         double pecb = 0.0, be = 0.0;
         for (int32_t i = 0; i < c.npl; i++) {
             if (!active(i)) continue;
@@ -216,7 +267,6 @@ struct Resolver {
         pe = pe + pecb;
         const double ke = 0.5 * (kecb + kesum);
         te = ke + pe + be;
-        for (int d = 0; d < 3; d++) L[d] = Lcb[d] + Lsum[d];
     }
 
     // collision_check_plpl (collision_check.f90:60-160) over the list at the resolution's
@@ -326,6 +376,7 @@ struct Resolver {
         rh2rb();
         double E_before, L_before[3];
         energy(E_before, L_before);
+        if (dev_failed) return -2;
         std::vector<int32_t> newb;
         int64_t nres = 0;
         for (int loop = 1;; loop++) {
@@ -345,13 +396,14 @@ struct Resolver {
             for (int32_t b : newb) mnew = mnew + c.Gm[b];
             set_rhill();
             double E_after, L_after[3], dL[3];
-            energy(E_after, L_after);
+            energy(E_after, L_after, false);
             for (int d = 0; d < 3; d++) dL[d] = L_after[d] - L_before[d];
             for (int32_t b : newb) {
                 const double t[3] = {-dL[0] * c.Gm[b] / mnew, -dL[1] * c.Gm[b] / mnew, -dL[2] * c.Gm[b] / mnew};
                 velocity_torque(t, c.Gm[b], &rb[3 * b], &c.vb[3 * b]);
             }
             energy(E_after, L_after);
+            if (dev_failed) return -2;
             c.E_collisions = c.E_collisions + (E_after - E_before);
             if (!check_plpl()) break;
             if (loop == MAXCASCADE) return -1;
@@ -366,7 +418,7 @@ struct Resolver {
 int64_t resolve_collisions_host(CollisionSystem &c) {
     Resolver r(c);
     const int64_t npp = r.resolve_plpl();
-    if (npp < 0) return -1;
+    if (npp < 0) return npp;
     // pl-tp: the test particle of every collided pair is discarded
     int64_t nres = npp;
     for (int64_t k = 0; k < c.npt; k++) {

@@ -1,10 +1,37 @@
-// collision_one.cuh -- the pair test of the collision check, shared by the device
-// recursion (symba_dev.cuh) and the host collision resolution (collision.cu), so both
-// take the same operations (both are compiled without FMA contraction).
+// collision_one.cuh -- the pair test of the collision check and the potential term of the
+// energy, shared by device kernels (symba_dev.cuh, collision.cu) and the host collision
+// resolution (collision.cu), so both take the same operations (both are compiled without
+// FMA contraction).
 #pragma once
 #include <cmath>
 
 namespace swg {
+
+// gfortran NORM2 of a 3-vector (the operators .mag. and .unit., and the potential's
+// norm2(rb_i - rb_j)): scaled sum of squares
+__host__ __device__ inline double hd_norm2_3(double x0, double x1, double x2) {
+    double scale = 0.0, ssq = 1.0;
+    const double v[3] = {x0, x1, x2};
+    for (int k = 0; k < 3; k++) {
+        if (v[k] != 0.0) {
+            const double absx = fabs(v[k]);
+            if (scale < absx) {
+                const double q = scale / absx;
+                ssq = 1.0 + ssq * q * q;
+                scale = absx;
+            } else {
+                const double q = absx / scale;
+                ssq = ssq + q * q;
+            }
+        }
+    }
+    return scale * sqrt(ssq);
+}
+
+// One term of the pairwise potential (swiftest_util.f90:1385): -(Gm_i Gm_j) / |rb_i - rb_j|
+__host__ __device__ inline double hd_pot_term(const double *ri, const double *rj, double Gmi, double Gmj) {
+    return -(Gmi * Gmj) / hd_norm2_3(ri[0] - rj[0], ri[1] - rj[1], ri[2] - rj[2]);
+}
 
 // swiftest_orbel_xv2aeq (src/swiftest/swiftest_orbel.f90:700-764): semimajor axis,
 // eccentricity and pericentre distance of the relative two-body orbit.

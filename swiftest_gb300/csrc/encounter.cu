@@ -396,14 +396,17 @@ __global__ void k_sas_positions(int ntot, const uint32_t *vals, int32_t *ibeg, i
 // sweep: body b with loverlap tests the bodies whose extents are strictly inside its box.
 // FA/FB/FV: float copies of the ntot bodies (list 1 then list 2) for the conservative FP32
 // prefilter, which drops only pairs the FP64 test is certain to reject (see
-// prefilter_reject), so the list is the same.
+// prefilter_reject), so the list is the same.  One warp per body: its lanes take the
+// entries of the body's box 32 at a time (a box holds up to hundreds of entries in a
+// disk, and a thread per body left the scan latency-bound on its serial loads); the
+// pairs' order in the output does not matter (the lists are sorted afterwards).
 __global__ void k_sas_sweep(int n1, const double *r1, const double *v1, const double *renc1, int n2,
                             const double *r2, const double *v2, const double *renc2, int single, int shift2, double dt,
                             const uint32_t *vals, const int32_t *ibeg, const int32_t *iend, const float4 *FA,
                             const float4 *FB, const float4 *FV, long long cap, int32_t *o1, int32_t *o2, int32_t *olv,
                             unsigned long long *count) {
     const int ntot = n1 + n2;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);  // warp-uniform
     if (i >= ntot) return;
     if (!((ibeg[i] + 1) < (iend[i] - 1))) return;
     const bool il1 = i < n1;
@@ -412,7 +415,8 @@ __global__ void k_sas_sweep(int n1, const double *r1, const double *v1, const do
     const double renci = il1 ? renc1[i] : (renc2 ? renc2[i - n1] : 0.0);
     const BodyF q = {FA[i], FB[i], FV[i]};
     const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);  // |dt| bounds either direction of time
-    for (int p = ibeg[i] + 1; p <= iend[i] - 1; p++) {
+    const int pend = iend[i] - 1;
+    for (int p = ibeg[i] + 1 + (int)(threadIdx.x & 31); p <= pend; p += 32) {
         int b = (int)vals[p - 1];
         if (b >= ntot) b -= ntot;
         const bool bl1 = b < n1;
@@ -488,8 +492,9 @@ int sas_launch(swg_ctx *c, int n1, const double *r1, const double *v1, const dou
     SWG_TRY(radix_sort_kv(c, ne, keys, vals, rs, seg_of, seg_bits, host_skip));
     k_sas_positions<<<(int)((ne + 255) / 256), 256, 0, c->stream>>>(ntot, vals, ibeg, iend);
     c->launches++;
-    k_sas_sweep<<<(ntot + 127) / 128, 128, 0, c->stream>>>(nb1, r1, v1, renc1, nb2, r2, v2, renc2, single, shift2, dt,
-                                                           vals, ibeg, iend, FA, FB, FV, cap, o1, o2, olv, count);
+    k_sas_sweep<<<(unsigned)((32 * (int64_t)ntot + 127) / 128), 128, 0, c->stream>>>(
+        nb1, r1, v1, renc1, nb2, r2, v2, renc2, single, shift2, dt, vals, ibeg, iend, FA, FB, FV, cap, o1, o2, olv,
+        count);
     c->launches++;
     return launch_status(c, "encounter_sas");
 }

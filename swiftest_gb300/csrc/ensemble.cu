@@ -239,122 +239,6 @@ __global__ void __launch_bounds__(ENS_SUM_T) k_ens_vb2vh(const int32_t *__restri
     blk_vb2vh_pl(npl[s], Gm + o, vb + 3 * o, status + o, vh + 3 * o, GMcb[s], dcb + CB_N * s, exact, sh);
 }
 
-// ---- per-system sums of the mixed path over 256-body chunks of every system
-// The block-per-system kernels above leave the largest systems on one SM each, and these
-// sums are FP64 work on GB300's narrow FP64 pipe; the mixed path instead forms partial sums
-// over chunks of CHUNK bodies of every system (grid over all chunks), then each chunk adds
-// its system's partials in chunk order and applies the result to its own bodies.  The
-// order is fixed, so results are deterministic.
-constexpr int CHUNK = 256, CHUNK_T = 64;  // bodies per chunk, threads per chunk block
-enum { SUM_VH2VB = 0, SUM_LIN = 1, SUM_VB2VH = 2 };
-
-// chunk: (system, first body, bodies, unused); out: 4 doubles per chunk (sum of weights
-// for SUM_VH2VB, then the three momentum components)
-template <int MODE>
-__global__ void __launch_bounds__(CHUNK_T) k_chunk_sums(int nchunks, const int4 *__restrict__ chunks,
-                                                       const int32_t *__restrict__ lfirst,
-                                                       const double *__restrict__ Gm, const double *__restrict__ v,
-                                                       const int32_t *__restrict__ mask, double *__restrict__ out) {
-    const int c = blockIdx.x;
-    const int4 ch = chunks[c];
-    if (MODE == SUM_VH2VB && lfirst && !lfirst[ch.x]) return;
-    double w = 0.0, x = 0.0, y = 0.0, z = 0.0;
-    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
-        const int i = ch.y + k;
-        bool on = true;
-        if (MODE == SUM_LIN) on = mask[i] != 0;
-        if (MODE == SUM_VB2VH) on = mask[i] != ST_INACTIVE;
-        if (!on) continue;
-        const double g = Gm[i];
-        w += g;
-        x = fma(g, v[3 * i + 0], x);
-        y = fma(g, v[3 * i + 1], y);
-        z = fma(g, v[3 * i + 2], z);
-    }
-    __shared__ double sh[CHUNK_T / 32][4];
-    for (int off = 16; off > 0; off >>= 1) {
-        if (MODE == SUM_VH2VB) w += __shfl_down_sync(0xffffffffu, w, off);
-        x += __shfl_down_sync(0xffffffffu, x, off);
-        y += __shfl_down_sync(0xffffffffu, y, off);
-        z += __shfl_down_sync(0xffffffffu, z, off);
-    }
-    const int wp = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        sh[wp][0] = w;
-        sh[wp][1] = x;
-        sh[wp][2] = y;
-        sh[wp][3] = z;
-    }
-    __syncthreads();
-    if (threadIdx.x < 4) {
-        double t = 0.0;
-        for (int q = 0; q < CHUNK_T / 32; q++) t += sh[q][threadIdx.x];
-        out[4 * c + threadIdx.x] = t;
-    }
-}
-
-// The system's chunk partials added in chunk order, then applied to this chunk's bodies:
-// SUM_VH2VB: vb = vh + c, c = -sum(Gm vh) / (GMcb + sum Gm) (swiftest_util_coord_vh2vb_pl);
-// SUM_LIN: pt = sum(Gm vb) / GMcb, rh += pt dt (helio_drift_linear_pl);
-// SUM_VB2VH: c = -sum(Gm vb) / GMcb, vh = vb - c (swiftest_util_coord_vb2vh_pl).
-// The system's first chunk records the result in the central-body record.
-template <int MODE>
-__global__ void __launch_bounds__(CHUNK_T) k_chunk_apply(const int4 *__restrict__ chunks,
-                                                        const int2 *__restrict__ sys_chunks,
-                                                        const int32_t *__restrict__ lfirst,
-                                                        const double *__restrict__ part,
-                                                        const double *__restrict__ GMcb,
-                                                        const int32_t *__restrict__ lmask, const double *vin,
-                                                        double *vout, double *rh, double dt, double *dcb, int slot) {
-    const int c = blockIdx.x;
-    const int4 ch = chunks[c];
-    const int s = ch.x;
-    if (MODE == SUM_VH2VB && lfirst && !lfirst[s]) return;
-    __shared__ double tot[4];
-    if (threadIdx.x < 4) {
-        const int2 r = sys_chunks[s];
-        double t = 0.0;
-        for (int q = r.x; q < r.x + r.y; q++) t += part[4 * q + threadIdx.x];
-        tot[threadIdx.x] = t;
-    }
-    __syncthreads();
-    double cx, cy, cz;
-    if (MODE == SUM_VH2VB) {
-        const double f = -1.0 / (GMcb[s] + tot[0]);
-        cx = tot[1] * f;
-        cy = tot[2] * f;
-        cz = tot[3] * f;
-    } else {
-        const double f = (MODE == SUM_LIN ? 1.0 : -1.0) / GMcb[s];
-        cx = tot[1] * f;
-        cy = tot[2] * f;
-        cz = tot[3] * f;
-    }
-    if (ch.w == 0 && threadIdx.x == 0) {
-        double *d = dcb + CB_N * s + (MODE == SUM_LIN ? slot : CB_VB);
-        d[0] = cx;
-        d[1] = cy;
-        d[2] = cz;
-    }
-    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
-        const int i = ch.y + k;
-        if (MODE == SUM_VH2VB) {
-            vout[3 * i + 0] = vin[3 * i + 0] + cx;
-            vout[3 * i + 1] = vin[3 * i + 1] + cy;
-            vout[3 * i + 2] = vin[3 * i + 2] + cz;
-        } else if (MODE == SUM_LIN) {
-            if (!lmask[i]) continue;
-            rh[3 * i + 0] = fma(cx, dt, rh[3 * i + 0]);
-            rh[3 * i + 1] = fma(cy, dt, rh[3 * i + 1]);
-            rh[3 * i + 2] = fma(cz, dt, rh[3 * i + 2]);
-        } else {
-            vout[3 * i + 0] = vin[3 * i + 0] - cx;
-            vout[3 * i + 1] = vin[3 * i + 1] - cy;
-            vout[3 * i + 2] = vin[3 * i + 2] - cz;
-        }
-    }
-}
-
 // Test-particle coordinate updates with their own system's central-body record (modes
 // as k_tp_misc of system.cu: 2 linear drift, 3 linear drift then vb2vh, 4 vh2vb then
 // linear drift, 5 vb = vh + the central body's vb).  mode_first >= 0 replaces mode
@@ -1043,7 +927,8 @@ int chunk_sum(swg_ensemble *e, const int32_t *lfirst, const double *vsum, const 
                                                               e->chunk_part);
     SWG_TRY(L(c, "chunk_sums"));
     k_chunk_apply<MODE><<<e->nchunks, CHUNK_T, 0, c->stream>>>(e->chunks, e->sys_chunks, lfirst, e->chunk_part,
-                                                               e->GMcb, e->lmask, vin, vout, e->rh, dt, e->dcb, slot);
+                                                               e->GMcb, 0.0, e->lmask, vin, vout, e->rh, dt, e->dcb,
+                                                               slot);
     return L(c, "chunk_apply");
 }
 
@@ -1373,7 +1258,9 @@ int resolve_collisions(swg_ensemble *e, int s) {
     double *ct = &e->coll_terms[4 * (size_t)s];
     cs.E_collisions = ct[0];
     for (int d = 0; d < 3; d++) cs.L_escape[d] = ct[1 + d];
+    cs.dev = c;
     const int64_t nres = resolve_collisions_host(cs);
+    if (nres == -2) return SWG_ERR_CUDA;
     if (nres < 0) {
         c->err = "runaway collisional cascade (more than 1000 rounds of merges in one resolution)";
         return SWG_ERR_STATE;
@@ -1445,6 +1332,16 @@ int recursion_launch(swg_ensemble *e, double dt) {
     a.out = e->rec_out;
     a.lclose = e->lclose;
     a.fast = !exact(e);
+    // every block gets room for the stage of all lists together, up to REC_STAGE_ENS; a
+    // system whose own lists do not fit runs on the global arrays
+    a.stage_bytes = (int64_t)std::min(rec_stage_bytes(e->pp_n, e->pt_n), REC_STAGE_ENS);
+    static bool smem_set = false;  // the kernel's own shared arrays come on top of the stage
+    if (a.stage_bytes > 0 && !smem_set) {
+        SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_ens_symba_recursion, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)REC_STAGE_ENS),
+                            "recursion smem"));
+        smem_set = true;
+    }
     x.seg_pp = e->seg_pp;
     x.seg_pt = e->seg_pt;
     x.npl = e->npl;
@@ -1456,7 +1353,7 @@ int recursion_launch(swg_ensemble *e, double dt) {
     SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_out, 0, sizeof(int32_t), c->stream), "memset"));
     if (e->lclose)
         SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_pend, 0, sizeof(int32_t) * e->nsys, c->stream), "memset"));
-    k_ens_symba_recursion<<<e->nsys, RECT, 0, c->stream>>>(x, 0);
+    k_ens_symba_recursion<<<e->nsys, RECT, (size_t)a.stage_bytes, c->stream>>>(x, 0);
     return L(c, "ens_symba_recursion");
 }
 
@@ -1483,7 +1380,7 @@ int recursion_finish(swg_ensemble *e) {
             }
         if (!any) break;
         SWG_TRY(cuda_status(c, cudaMemsetAsync(e->rec_pend, 0, sizeof(int32_t) * e->nsys, c->stream), "memset"));
-        k_ens_symba_recursion<<<e->nsys, RECT, 0, c->stream>>>(e->rec_args, 1);
+        k_ens_symba_recursion<<<e->nsys, RECT, (size_t)e->rec_args.base.stage_bytes, c->stream>>>(e->rec_args, 1);
         SWG_TRY(L(c, "ens_symba_recursion"));
     }
     return cuda_status(c, cudaMemcpyAsync(e->h_flags + 2, e->rec_out, sizeof(int32_t), cudaMemcpyDeviceToHost,

@@ -198,13 +198,21 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
     if (!s_last) return;
     __threadfence();
     if (active) {
-        double sx = 0.0, sy = 0.0, sz = 0.0;
+        // the chunks' float-float partials are folded in float-float (FP32 instructions)
+        // and converted once: a fold in FP64 would put 12 FP64 instructions per chunk and
+        // receiver on the narrow FP64 pipe of the one SM that runs the last block
+        FF fx = {0.f, 0.f}, fy = {0.f, 0.f}, fz = {0.f, 0.f};
         for (int cidx = 0; cidx < nchunk; cidx++) {
             const volatile float *p = &partial[((size_t)cidx * nrecv + i) * 6];
-            sx += (double)p[0] + (double)p[1];
-            sy += (double)p[2] + (double)p[3];
-            sz += (double)p[4] + (double)p[5];
+            ff_add(fx, p[0]);
+            ff_add(fx, p[1]);
+            ff_add(fy, p[2]);
+            ff_add(fy, p[3]);
+            ff_add(fz, p[4]);
+            ff_add(fz, p[5]);
         }
+        const double sx = (double)fx.hi + (double)fx.lo, sy = (double)fy.hi + (double)fy.lo,
+                     sz = (double)fz.hi + (double)fz.lo;
         double *a = &acc[3 * i];
         a[0] = (acc_is_zero ? 0.0 : a[0]) + sx;
         a[1] = (acc_is_zero ? 0.0 : a[1]) + sy;

@@ -347,6 +347,7 @@ struct CollisionSystem {
     double dt = 0.0;            // that level's step
     double E_collisions = 0.0;  // inout: collision_resolve.f90:638 (G*m units)
     double L_escape[3] = {0.0, 0.0, 0.0};  // inout: collision_generate.f90:219
+    swg_ctx *dev = nullptr;     // context whose device forms the O(N^2) potential rows
 };
 // Step of recursion level irec, formed as the device recursion forms it: dt / 3^irec.
 inline double level_dt(double dt, int irec) {
@@ -355,7 +356,8 @@ inline double level_dt(double dt, int irec) {
     return dt / p3;
 }
 // Resolves the COLLIDED pairs in place; returns the number of merges plus discarded test
-// particles, or -1 for a runaway collisional cascade.
+// particles, -1 for a runaway collisional cascade, or -2 if the device work failed (the
+// error is in c.dev->err).
 int64_t resolve_collisions_host(CollisionSystem &c);
 
 // Scalar-broadcast helpers

@@ -399,6 +399,7 @@ struct RecArgs {
     int fast;                       // mixed path: fast FP64 forms of the drift and of r^-1.5
     int32_t *resume;                // REC_STATE ints: saved recursion stack of a paused step
     int32_t *pend;                  // set to 1 when the recursion pauses for a collision
+    int64_t stage_bytes;            // dynamic shared memory of the launch (0: none)
 };
 
 // Saved stack of a recursion paused for a collision: [0] 1 when paused, [1] level,
@@ -692,6 +693,125 @@ static __device__ void blk_collision_check(const RecArgs &a, int irec, double dt
     __syncthreads();
 }
 
+// ---- per-system sums of the mixed path over chunks of every system
+// A block-per-system sum leaves each system on one SM, and these sums are FP64 work on
+// GB300's narrow FP64 pipe (an SM issues about one FP64 warp instruction per 19 cycles);
+// the mixed path instead forms partial sums over chunks of bodies of every system (grid
+// over all chunks: CHUNK bodies per chunk in ensembles, CHUNK_ONE for a single system), then
+// each chunk adds its system's partials in chunk order and applies the result to its own
+// bodies.  The order is fixed, so results are deterministic.
+constexpr int CHUNK = 256, CHUNK_ONE = 128, CHUNK_T = 64;  // bodies per chunk, threads per chunk block
+enum { SUM_VH2VB = 0, SUM_LIN = 1, SUM_VB2VH = 2 };
+
+// chunk: (system, first body, bodies, unused); out: 4 doubles per chunk (sum of weights
+// for SUM_VH2VB, then the three momentum components)
+template <int MODE>
+__global__ void __launch_bounds__(CHUNK_T) k_chunk_sums(int nchunks, const int4 *__restrict__ chunks,
+                                                       const int32_t *__restrict__ lfirst,
+                                                       const double *__restrict__ Gm, const double *__restrict__ v,
+                                                       const int32_t *__restrict__ mask, double *__restrict__ out) {
+    const int c = blockIdx.x;
+    const int4 ch = chunks[c];
+    if (MODE == SUM_VH2VB && lfirst && !lfirst[ch.x]) return;
+    double w = 0.0, x = 0.0, y = 0.0, z = 0.0;
+    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
+        const int i = ch.y + k;
+        bool on = true;
+        if (MODE == SUM_LIN) on = mask[i] != 0;
+        if (MODE == SUM_VB2VH) on = mask[i] != ST_INACTIVE;
+        if (!on) continue;
+        const double g = Gm[i];
+        w += g;
+        x = fma(g, v[3 * i + 0], x);
+        y = fma(g, v[3 * i + 1], y);
+        z = fma(g, v[3 * i + 2], z);
+    }
+    __shared__ double sh[CHUNK_T / 32][4];
+    for (int off = 16; off > 0; off >>= 1) {
+        if (MODE == SUM_VH2VB) w += __shfl_down_sync(0xffffffffu, w, off);
+        x += __shfl_down_sync(0xffffffffu, x, off);
+        y += __shfl_down_sync(0xffffffffu, y, off);
+        z += __shfl_down_sync(0xffffffffu, z, off);
+    }
+    const int wp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        sh[wp][0] = w;
+        sh[wp][1] = x;
+        sh[wp][2] = y;
+        sh[wp][3] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int q = 0; q < CHUNK_T / 32; q++) t += sh[q][threadIdx.x];
+        out[4 * c + threadIdx.x] = t;
+    }
+}
+
+// The system's chunk partials added in chunk order, then applied to this chunk's bodies:
+// SUM_VH2VB: vb = vh + c, c = -sum(Gm vh) / (GMcb + sum Gm) (swiftest_util_coord_vh2vb_pl);
+// SUM_LIN: pt = sum(Gm vb) / GMcb, rh += pt dt (helio_drift_linear_pl);
+// SUM_VB2VH: c = -sum(Gm vb) / GMcb, vh = vb - c (swiftest_util_coord_vb2vh_pl).
+// GMcb: per-system central-body masses, or nullptr for the single value GMcb0.
+// The system's first chunk records the result in the central-body record.
+template <int MODE>
+__global__ void __launch_bounds__(CHUNK_T) k_chunk_apply(const int4 *__restrict__ chunks,
+                                                        const int2 *__restrict__ sys_chunks,
+                                                        const int32_t *__restrict__ lfirst,
+                                                        const double *__restrict__ part,
+                                                        const double *__restrict__ GMcb, double GMcb0,
+                                                        const int32_t *__restrict__ lmask, const double *vin,
+                                                        double *vout, double *rh, double dt, double *dcb, int slot) {
+    const int c = blockIdx.x;
+    const int4 ch = chunks[c];
+    const int s = ch.x;
+    if (MODE == SUM_VH2VB && lfirst && !lfirst[s]) return;
+    __shared__ double tot[4];
+    if (threadIdx.x < 4) {
+        const int2 r = sys_chunks[s];
+        double t = 0.0;
+        for (int q = r.x; q < r.x + r.y; q++) t += part[4 * q + threadIdx.x];
+        tot[threadIdx.x] = t;
+    }
+    __syncthreads();
+    double cx, cy, cz;
+    const double gmcb = GMcb ? GMcb[s] : GMcb0;
+    if (MODE == SUM_VH2VB) {
+        const double f = -1.0 / (gmcb + tot[0]);
+        cx = tot[1] * f;
+        cy = tot[2] * f;
+        cz = tot[3] * f;
+    } else {
+        const double f = (MODE == SUM_LIN ? 1.0 : -1.0) / gmcb;
+        cx = tot[1] * f;
+        cy = tot[2] * f;
+        cz = tot[3] * f;
+    }
+    if (ch.w == 0 && threadIdx.x == 0) {
+        double *d = dcb + CB_N * s + (MODE == SUM_LIN ? slot : CB_VB);
+        d[0] = cx;
+        d[1] = cy;
+        d[2] = cz;
+    }
+    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
+        const int i = ch.y + k;
+        if (MODE == SUM_VH2VB) {
+            vout[3 * i + 0] = vin[3 * i + 0] + cx;
+            vout[3 * i + 1] = vin[3 * i + 1] + cy;
+            vout[3 * i + 2] = vin[3 * i + 2] + cz;
+        } else if (MODE == SUM_LIN) {
+            if (!lmask[i]) continue;
+            rh[3 * i + 0] = fma(cx, dt, rh[3 * i + 0]);
+            rh[3 * i + 1] = fma(cy, dt, rh[3 * i + 1]);
+            rh[3 * i + 2] = fma(cz, dt, rh[3 * i + 2]);
+        } else {
+            vout[3 * i + 0] = vin[3 * i + 0] - cx;
+            vout[3 * i + 1] = vin[3 * i + 1] - cy;
+            vout[3 * i + 2] = vin[3 * i + 2] - cz;
+        }
+    }
+}
+
 constexpr int RECT = 256;  // threads of the recursion kernel
 
 // In-place exclusive prefix sum of v[0, n) by the whole block (blockDim a multiple of 32,
@@ -779,21 +899,354 @@ static __device__ void blk_build_adjacency(const RecArgs &a, int nbpl, int nbtp)
     __syncthreads();
 }
 
+// ---- the recursion's state staged in shared memory
+// Every phase of a sub-step is a short FP64 chain preceded by dependent global loads (list
+// entry -> body index -> position); on GB300 each L2 round trip costs hundreds of cycles on
+// that chain.  When the lists fit, the listed bodies (by slot) and the list entries are
+// copied into the block's dynamic shared memory once per launch, the phases below work
+// there with the same arithmetic as the global-memory phases above, and the state is
+// written back at the end (or at a pause for a collision).
+struct RecStage {
+    double *r, *v;                 // per slot: position, velocity (3 each)
+    double *gm, *rhill, *rad;      // per slot: G*m, Hill radius, radius (0 for test particles)
+    double *terms;                 // 12 per entry
+    int32_t *lev, *st, *gidx;      // per slot: levelg / tlevelg, status / tstatus, global index
+    int32_t *s1, *s2;              // per entry: slots of index1 and index2
+    int32_t *est, *elev, *elv;     // per entry: status, level, lvdotr
+    int32_t *adj_end, *adj;        // the adjacency of blk_build_adjacency
+    uint8_t *lenc, *good, *good2;  // per entry
+};
+// Largest stage of a single-system launch, and of each block of an ensemble launch (every
+// block gets the same size; systems whose lists do not fit use the global arrays).
+constexpr size_t REC_STAGE_MAX = 160 * 1024, REC_STAGE_ENS = 64 * 1024;
+// Bytes of the stage for npp pl-pl and npt pl-tp entries: at most two bodies per entry
+// (a pl-tp entry names one pl and one tp), and 2 npp + npt adjacency entries.
+__host__ __device__ inline size_t rec_stage_bytes(int64_t npp, int64_t npt) {
+    const int64_t n = npp + npt, nb = 2 * n;
+    return (size_t)(9 * nb + 12 * n) * 8 + (size_t)(4 * nb + 5 * n + 2 * npp + npt) * 4 + (size_t)(3 * n + 16);
+}
+static __device__ RecStage rec_stage_carve(void *base, int64_t npp, int64_t npt) {
+    const int64_t n = npp + npt, nb = 2 * n;
+    RecStage S;
+    double *d = (double *)base;
+    S.r = d;
+    S.v = d + 3 * nb;
+    S.gm = d + 6 * nb;
+    S.rhill = d + 7 * nb;
+    S.rad = d + 8 * nb;
+    S.terms = d + 9 * nb;
+    int32_t *i = (int32_t *)(S.terms + 12 * n);
+    S.lev = i;
+    S.st = i + nb;
+    S.gidx = i + 2 * nb;
+    S.adj_end = i + 3 * nb;
+    S.s1 = i + 4 * nb;
+    S.s2 = S.s1 + n;
+    S.est = S.s2 + n;
+    S.elev = S.est + n;
+    S.elv = S.elev + n;
+    S.adj = S.elv + n;
+    uint8_t *b = (uint8_t *)(S.adj + 2 * npp + npt);
+    S.lenc = b;
+    S.good = b + n;
+    S.good2 = b + 2 * n;
+    return S;
+}
+// Copy the listed bodies and the list entries in (after blk_build_adjacency: mark_pl /
+// mark_tp hold slot + 1), whole block.
+static __device__ void stg_load(const RecArgs &a, const RecStage &S, int nbpl, int nbtp) {
+    const int nb = nbpl + nbtp;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const bool isp = b < nbpl;
+        const int g = isp ? a.bpl[b] : a.btp[b - nbpl];
+        const double *x = isp ? &a.rh[3 * g] : &a.trh[3 * g];
+        const double *w = isp ? &a.vb[3 * g] : &a.tvb[3 * g];
+        for (int d = 0; d < 3; d++) {
+            S.r[3 * b + d] = x[d];
+            S.v[3 * b + d] = w[d];
+        }
+        S.gm[b] = isp ? a.Gm[g] : 0.0;
+        S.rhill[b] = isp ? a.rhill[g] : 0.0;
+        S.rad[b] = isp ? a.radius[g] : 0.0;
+        S.lev[b] = isp ? a.levelg[g] : a.tlevelg[g];
+        S.st[b] = isp ? a.status[g] : a.tstatus[g];
+        S.gidx[b] = g;
+        S.adj_end[b] = a.adj_end[b];
+    }
+    const int64_t n = a.npp + a.npt;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const bool isp = k < a.npp;
+        const int64_t q = isp ? k : k - a.npp;
+        const int32_t *l = isp ? a.pp : a.pt;
+        const int64_t cap = isp ? a.ppcap : a.ptcap;
+        const int i = l[q] - 1, j = l[cap + q] - 1;
+        S.s1[k] = a.mark_pl[i] - 1;
+        S.s2[k] = isp ? a.mark_pl[j] - 1 : a.mark_tp[j] - 1;
+        S.elv[k] = l[2 * cap + q];
+        S.est[k] = l[3 * cap + q];
+        S.elev[k] = l[4 * cap + q];
+    }
+    for (int64_t e = threadIdx.x; e < 2 * a.npp + a.npt; e += blockDim.x) S.adj[e] = a.adj[e];
+    __syncthreads();
+}
+// Write the staged state back to the global arrays, whole block.
+static __device__ void stg_store(const RecArgs &a, const RecStage &S, int nbpl, int nbtp) {
+    __syncthreads();
+    const int nb = nbpl + nbtp;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const bool isp = b < nbpl;
+        const int g = S.gidx[b];
+        double *x = isp ? &a.rh[3 * g] : &a.trh[3 * g];
+        double *w = isp ? &a.vb[3 * g] : &a.tvb[3 * g];
+        for (int d = 0; d < 3; d++) {
+            x[d] = S.r[3 * b + d];
+            w[d] = S.v[3 * b + d];
+        }
+        (isp ? a.levelg : a.tlevelg)[g] = S.lev[b];
+        (isp ? a.status : a.tstatus)[g] = S.st[b];
+    }
+    const int64_t n = a.npp + a.npt;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const bool isp = k < a.npp;
+        const int64_t q = isp ? k : k - a.npp;
+        int32_t *l = isp ? a.pp : a.pt;
+        const int64_t cap = isp ? a.ppcap : a.ptcap;
+        l[2 * cap + q] = S.elv[k];
+        l[3 * cap + q] = S.est[k];
+        l[4 * cap + q] = S.elev[k];
+    }
+    __syncthreads();
+}
+// blk_list_check on the stage
+static __device__ void stg_list_check(const RecArgs &a, const RecStage &S, int irec, double dt, int *s_any,
+                                      const double *rs_pow) {
+    const int64_t npp = a.npp, n = a.npp + a.npt;
+    for (int64_t k = spread_tid(); k < n; k += blockDim.x) {
+        const bool isp = k < npp;
+        uint8_t le_out = 0;
+        if (S.est[k] == ST_ACTIVE && S.elev[k] == irec - 1) {
+            const int b1 = S.s1[k], b2 = S.s2[k];
+            double xr[3], vr[3];
+            for (int d = 0; d < 3; d++) {
+                xr[d] = S.r[3 * b2 + d] - S.r[3 * b1 + d];
+                vr[d] = S.v[3 * b2 + d] - S.v[3 * b1 + d];
+            }
+            const double renci = S.rhill[b1] * a.rhscale * rs_pow[irec];  // d_renc(rhill_i, rhscale, irec)
+            const double rcrit = isp ? renci + S.rhill[b2] * a.rhscale * rs_pow[irec] : renci;
+            int le, lvd;
+            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            S.elv[k] = lvd;
+            if (le) {
+                const double rs = isp ? S.rad[b1] + S.rad[b2] : S.rad[b1];
+                const double rlim2 = isp ? rs * rs : S.rad[b1] * S.rad[b1];
+                const double rji2 = xr[0] * xr[0] + xr[1] * xr[1] + xr[2] * xr[2];
+                le = rji2 > rlim2;
+            }
+            le_out = (uint8_t)le;
+        }
+        S.lenc[k] = le_out;
+    }
+    __syncthreads();
+    for (int64_t k = spread_tid(); k < n; k += blockDim.x) {
+        if (!S.lenc[k]) continue;
+        *s_any = 1;
+        const bool isp = k < npp;
+        const int b1 = S.s1[k], b2 = S.s2[k];
+        S.lev[b1] = irec;
+        atomicMax(&a.levelm[S.gidx[b1]], irec);
+        S.lev[b2] = irec;
+        atomicMax(isp ? &a.levelm[S.gidx[b2]] : &a.tlevelm[S.gidx[b2]], irec);
+        S.elev[k] = irec;
+    }
+    __syncthreads();
+}
+// blk_kick_lists on the stage (same pair terms, same per-body order)
+static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int nbpl, int nbtp, double dt, int irec,
+                                      bool both, const double *pw) {
+    const int64_t npp = a.npp, n = a.npp + a.npt;
+    if (n == 0) return;
+    const int irm1 = irec - 1;
+    const double rs2 = a.rhscale * a.rhscale;
+    const double shell_p = pw[2 * irec], shell_m = pw[2 * (irec - 1)];
+    const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
+    for (int64_t k = spread_tid(); k < n; k += blockDim.x) {
+        const bool isp = k < npp;
+        const int b1 = S.s1[k], b2 = S.s2[k];
+        const bool g = (isp ? do_pp : do_pt) && (S.est[k] == ST_ACTIVE) && (S.lev[b1] >= irm1) && (S.lev[b2] >= irm1);
+        if (!g) {
+            S.good[k] = 0;
+            S.good2[k] = 0;
+            continue;
+        }
+        double base;
+        if (isp) {
+            const double rhs = S.rhill[b1] + S.rhill[b2];
+            base = (rhs * rhs) * rs2;
+        } else {
+            base = (S.rhill[b1] * S.rhill[b1]) * rs2;
+        }
+        const double ri_p = base * shell_p, ri_m = base * shell_m;
+        double dx[3];
+        for (int d = 0; d < 3; d++) dx[d] = S.r[3 * b2 + d] - S.r[3 * b1 + d];
+        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        const bool kp = !(r2 < ri_p * (RSHELL * RSHELL));
+        const bool km = both && !(r2 < ri_m * (RSHELL * RSHELL));
+        S.good[k] = kp ? 1 : 2;
+        S.good2[k] = both ? (km ? 1 : 2) : 0;
+        if (!kp && !km) continue;
+        const bool shp = kp && r2 < ri_p, shm = km && r2 < ri_m;
+        double r, ir3;
+        if (a.fast) {
+            const double y = rsqrt(r2);
+            r = r2 * y;
+            ir3 = (y * y) * y;
+        } else {
+            r = sqrt(r2);
+            ir3 = 1.0 / (r2 * r);
+        }
+        double p = ir3;
+        if (!a.fast && (shp || shm)) p = pow_m1p5(r2);
+        auto shell = [&](double ri) {
+            const double rr = a.fast ? (1.0 - r * rsqrt(ri)) * (1.0 / (1.0 - RSHELL))
+                                     : (sqrt(ri) - r) / (sqrt(ri) * (1.0 - RSHELL));
+            return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
+        };
+        double *t = &S.terms[12 * k];
+        for (int sg = 0; sg < 2; sg++) {
+            if (!(sg == 0 ? kp : km)) continue;
+            const bool sh = sg == 0 ? shp : shm;
+            const double fac = sh ? shell(sg == 0 ? ri_p : ri_m) : ir3;
+            double *ts = t + 6 * sg;
+            const double faci = fac * S.gm[b1];
+            if (isp) {
+                const double facj = fac * S.gm[b2];
+                for (int d = 0; d < 3; d++) {
+                    ts[d] = facj * dx[d];
+                    ts[3 + d] = faci * dx[d];
+                }
+            } else {
+                for (int d = 0; d < 3; d++) ts[d] = faci * dx[d];
+            }
+        }
+    }
+    __syncthreads();
+    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
+        const bool isp = b < nbpl;
+        bool zeroed[2] = {false, false}, kicked[2] = {false, false};
+        double ax[2] = {0.0, 0.0}, ay[2] = {0.0, 0.0}, az[2] = {0.0, 0.0};
+        const int e0 = b == 0 ? 0 : S.adj_end[b - 1], e1 = S.adj_end[b];
+        for (int e = e0; e < e1; e++) {
+            const int k = S.adj[e];
+            const int off = (isp && S.s1[k] != b) ? 3 : 0;
+            const bool sub = !isp || off == 3;
+            for (int sg = 0; sg < 2; sg++) {
+                const uint8_t g = sg == 0 ? S.good[k] : S.good2[k];
+                if (g == 0) continue;
+                zeroed[sg] = true;
+                if (g != 1) continue;
+                kicked[sg] = true;
+                const double *t = &S.terms[12 * k + 6 * sg + off];
+                if (sub) {
+                    ax[sg] = ax[sg] - t[0];
+                    ay[sg] = ay[sg] - t[1];
+                    az[sg] = az[sg] - t[2];
+                } else {
+                    ax[sg] = ax[sg] + t[0];
+                    ay[sg] = ay[sg] + t[1];
+                    az[sg] = az[sg] + t[2];
+                }
+            }
+        }
+        double *v = &S.v[3 * b];
+        double *acc = isp ? &a.ah[3 * S.gidx[b]] : &a.tah[3 * S.gidx[b]];
+        for (int sg = 0; sg < 2; sg++) {
+            if (!zeroed[sg]) continue;
+            const double sdt = sg == 0 ? dt : -dt;
+            if (kicked[sg]) {
+                v[0] = v[0] + sdt * ax[sg];
+                v[1] = v[1] + sdt * ay[sg];
+                v[2] = v[2] + sdt * az[sg];
+            }
+            acc[0] = acc[1] = acc[2] = 0.0;
+        }
+    }
+    __syncthreads();
+}
+// blk_drift on the stage
+static __device__ void stg_drift(const RecArgs &a, const RecStage &S, int nbpl, int nbtp, int irec, double dt) {
+    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
+        if (S.lev[b] != irec || S.st[b] == ST_INACTIVE) continue;
+        double *x = &S.r[3 * b], *v = &S.v[3 * b];
+        double rx = x[0], ry = x[1], rz = x[2], vx = v[0], vy = v[1], vz = v[2];
+        const int fl = a.fast ? d_drift_one_fast(a.GMcb, rx, ry, rz, vx, vy, vz, dt)
+                              : d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
+        x[0] = rx;
+        x[1] = ry;
+        x[2] = rz;
+        v[0] = vx;
+        v[1] = vy;
+        v[2] = vz;
+        if (fl != 0) S.st[b] = ST_DISCARDED_DRIFTERR;
+    }
+    __syncthreads();
+}
+// blk_set_recur_levels on the stage
+static __device__ void stg_set_recur_levels(const RecArgs &a, const RecStage &S, int nbpl, int nbtp, int ireci) {
+    const int irecp = ireci + 1;
+    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x)
+        if (S.lev[b] == irecp) S.lev[b] = ireci;
+    for (int64_t k = threadIdx.x; k < a.npp + a.npt; k += blockDim.x)
+        if (S.elev[k] == irecp) S.elev[k] = ireci;
+    __syncthreads();
+}
+// blk_collision_check on the stage
+static __device__ void stg_collision_check(const RecArgs &a, const RecStage &S, int irec, double dt, int *s_coll) {
+    for (int64_t k = spread_tid(); k < a.npp + a.npt; k += blockDim.x) {
+        if (S.est[k] != ST_ACTIVE) continue;
+        const bool isp = k < a.npp;
+        const int b1 = S.s1[k], b2 = S.s2[k];
+        if ((isp ? S.lev[b1] : S.lev[b2]) < irec) continue;
+        const double *ri = &S.r[3 * b1], *rj = &S.r[3 * b2], *vi = &S.v[3 * b1], *vj = &S.v[3 * b2];
+        const double xr = ri[0] - rj[0], yr = ri[1] - rj[1], zr = ri[2] - rj[2];
+        const double vxr = vi[0] - vj[0], vyr = vi[1] - vj[1], vzr = vi[2] - vj[2];
+        const double Gmtot = isp ? S.gm[b1] + S.gm[b2] : S.gm[b1];
+        const double rlim = isp ? S.rad[b1] + S.rad[b2] : S.rad[b1];
+        if (d_collision_one(xr, yr, zr, vxr, vyr, vzr, Gmtot, rlim, dt, S.elv[k] != 0)) {
+            S.est[k] = ST_COLLIDED;
+            *s_coll = 1;
+        }
+    }
+    __syncthreads();
+}
+
 // symba_step_recur_system (symba_step.f90:163-262) for the whole recursion tree of one
 // step, started at level 0, in a single block: the reference's recursive calls become
 // an explicit stack of (loop counter, phase) per level, and every per-level operation
 // is a block-wide device function separated by barriers.  a.out[0] receives
 // SWG_ERR_RECURSION if the step falls below machine precision (the caller zeroes it),
 // a.out[1] the deepest level (atomicMax) and a.out[2] the sub-steps run (atomicAdd), so
-// several blocks (systems of an ensemble) may share one out array.
-static __device__ void blk_symba_recursion(const RecArgs &a) {
+// several blocks (systems of an ensemble) may share one out array.  STAGED: the listed
+// bodies and the list entries live in `stage` (dynamic shared memory) during the launch.
+template <bool STAGED>
+static __device__ void blk_symba_recursion_t(const RecArgs &a, void *stage) {
     __shared__ int s_nbpl, s_nbtp, s_any;
     __shared__ int s_j[MAXLEV], s_phase[MAXLEV];
     // shell-radius powers, formed once per launch with the per-call algorithms (same bits):
     // s_pw[m] = d_powi(RSHELL, m) (the kick's shell radii), s_rs[k] = RSHELL^k by repeated
     // products (d_renc, the list check's encounter radii)
     __shared__ double s_pw[2 * MAXLEV + 2], s_rs[MAXLEV + 1];
+    // each level's step dt / 3^k and the underflow test of symba_step.f90:196-201, formed
+    // once per launch as the loop would form them (the FP64 divides are long on GB300)
+    __shared__ double s_dtl[MAXLEV];
+    __shared__ unsigned char s_under[MAXLEV];
     for (int m = threadIdx.x; m < 2 * MAXLEV + 2; m += blockDim.x) s_pw[m] = d_powi(RSHELL, m);
+    for (int k = threadIdx.x; k < MAXLEV; k += blockDim.x) {
+        double p3 = 1.0;
+        for (int q = 0; q < k; q++) p3 *= 3.0;
+        const double d = a.dt / p3;
+        s_dtl[k] = d;
+        s_under[k] = d / a.dt < 2.220446049250313e-16;
+    }
     if (threadIdx.x == 0) {
         double p = 1.0;
         s_rs[0] = p;
@@ -821,6 +1274,11 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
     __syncthreads();
     const int nbpl = s_nbpl, nbtp = s_nbtp;
     blk_build_adjacency(a, nbpl, nbtp);
+    RecStage S{};
+    if constexpr (STAGED) {
+        S = rec_stage_carve(stage, a.npp, a.npt);
+        stg_load(a, S, nbpl, nbtp);
+    }
     int ireci = 0;
     const bool resumed = a.resume && a.resume[0] == 1;
     if (resumed) {  // continue a step paused after a collision check
@@ -837,9 +1295,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
     int deepest = 0, substeps = 0;
     bool paused = false;
     for (;;) {
-        double p3 = 1.0;
-        for (int k = 0; k < ireci; k++) p3 *= 3.0;
-        const double dtl = a.dt / p3;
+        const double dtl = s_dtl[ireci];
         const double dth = 0.5 * dtl;
         const int irecp = ireci + 1;
         const int nloops = ireci == 0 ? 1 : NTENC;
@@ -853,7 +1309,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
                 __syncthreads();
                 continue;
             }
-            if (dtl / a.dt < 2.220446049250313e-16) {
+            if (s_under[ireci]) {
                 if (threadIdx.x == 0) a.out[0] = SWG_ERR_RECURSION;
                 break;
             }
@@ -861,9 +1317,15 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
             substeps++;
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
-            blk_list_check(a, irecp, dtl, &s_any, s_rs);
-            blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
-            blk_drift(a, nbpl, nbtp, ireci, dtl);
+            if constexpr (STAGED) {
+                stg_list_check(a, S, irecp, dtl, &s_any, s_rs);
+                stg_kick_lists(a, S, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
+                stg_drift(a, S, nbpl, nbtp, ireci, dtl);
+            } else {
+                blk_list_check(a, irecp, dtl, &s_any, s_rs);
+                blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
+                blk_drift(a, nbpl, nbtp, ireci, dtl);
+            }
             const int any = s_any;
             __syncthreads();
             if (any) {
@@ -881,11 +1343,17 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
             }
         }
         // after the deeper levels (or none) for loop j of level ireci
-        blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
+        if constexpr (STAGED)
+            stg_kick_lists(a, S, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
+        else
+            blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
         if (a.lclose) {
             if (threadIdx.x == 0) s_any = 0;
             __syncthreads();
-            blk_collision_check(a, ireci, dtl, &s_any);
+            if constexpr (STAGED)
+                stg_collision_check(a, S, ireci, dtl, &s_any);
+            else
+                blk_collision_check(a, ireci, dtl, &s_any);
             if (s_any) {  // pause: the host resolves the collisions, then resumes here
                 if (threadIdx.x == 0) {
                     s_phase[ireci] = 2;
@@ -902,7 +1370,10 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
             }
         }
     after_collision:
-        blk_set_recur_levels(a, nbpl, nbtp, ireci);
+        if constexpr (STAGED)
+            stg_set_recur_levels(a, S, nbpl, nbtp, ireci);
+        else
+            blk_set_recur_levels(a, nbpl, nbtp, ireci);
         if (threadIdx.x == 0) {
             s_j[ireci]++;
             s_phase[ireci] = 0;
@@ -910,6 +1381,7 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
         __syncthreads();
     }
     __syncthreads();
+    if constexpr (STAGED) stg_store(a, S, nbpl, nbtp);
     if (!paused && resumed && threadIdx.x == 0) a.resume[0] = 0;
     for (int b = threadIdx.x; b < nbpl; b += blockDim.x) a.mark_pl[a.bpl[b]] = 0;
     for (int b = threadIdx.x; b < nbtp; b += blockDim.x) a.mark_tp[a.btp[b]] = 0;
@@ -917,6 +1389,17 @@ static __device__ void blk_symba_recursion(const RecArgs &a) {
         atomicMax(&a.out[1], deepest);
         atomicAdd(&a.out[2], substeps);
     }
+}
+
+// The recursion of one system: staged in the launch's dynamic shared memory when its lists
+// fit there (a.stage_bytes: that memory's size, 0 for none), else on the global arrays.
+// Both forms take the same arithmetic in the same order, so they give the same bits.
+static __device__ void blk_symba_recursion(const RecArgs &a) {
+    extern __shared__ __align__(16) unsigned char rec_dyn[];
+    if (a.stage_bytes > 0 && rec_stage_bytes(a.npp, a.npt) <= (size_t)a.stage_bytes)
+        blk_symba_recursion_t<true>(a, rec_dyn);
+    else
+        blk_symba_recursion_t<false>(a, nullptr);
 }
 
 // ---- energy / momentum (swiftest_util.f90:1172-1401), masses as G*m

@@ -51,12 +51,19 @@ struct swg_system {
     int64_t plpl_n = 0, pltp_n = 0, plpl_cap = 0, pltp_cap = 0;
     EncWork enc, enc2;
     // scratch
-    DevBuf kick_scratch, pair_scratch, flags, red;
+    DevBuf kick_scratch, kick_scratch_tp, pair_scratch, flags, red;
+    // SyMBA with test particles: their half-steps run on a second stream beside the
+    // massive bodies' (events: 0 opening ready, 1 tp opening done, 2 closing ready,
+    // 3 central-body drift ready, 4 tp closing done)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail, [2] recursion status, [3] deepest level,
                                  // [4] collision pending
     int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr, *rec_resume = nullptr;
     DevBuf rec_scratch;
     DevBuf discard_scratch;                 // float copies of the close-approach scan
+    DevBuf chunk_buf;                       // mixed path: chunk table, system range, chunk partials
+    int nchunks = 0;
     int32_t *tflag = nullptr;               // tp flagged by the scan
     unsigned long long *ndiscard = nullptr; // tp removed by the scan
     int64_t stats[6] = {0, 0, 0, 0, 0, 0};
@@ -288,8 +295,10 @@ int accel_int_pl(swg_system *s, int acc_is_zero) {
     return kick_plpl_fp64(c, s->npl, nplm, s->rh, s->Gmass, rad, s->ah, mode, acc_is_zero);
 }
 
-// helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76)
-int kick_vb_pl(swg_system *s, double dt, int lbeg) {
+// helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76);
+// copy_r: record the positions as the step's start (lbeg) or end positions for the test
+// particles' kick (a caller that already copied them passes false)
+int kick_vb_pl(swg_system *s, double dt, int lbeg, bool copy_r = true) {
     swg_ctx *c = s->c;
     if (s->npl == 0) return SWG_OK;
     {
@@ -303,7 +312,7 @@ int kick_vb_pl(swg_system *s, double dt, int lbeg) {
                            s->radius, s->ah, -1.0, scr));
     }
     k_kick_update<<<grid_for(s->npl, 128), 128, 0, c->stream>>>(s->npl, s->vb, s->ah, s->lmask, dt, s->rh,
-                                                                 lbeg ? s->rbeg : s->rend);
+                                                                 copy_r ? (lbeg ? s->rbeg : s->rend) : nullptr);
     return L(c, "kick_update_pl");
 }
 
@@ -316,9 +325,9 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
         ProfScope ps(s->prof, s->c->stream, PROF_KICK_TP);
         if (s->precision == SWG_MIXED) {
             const int nch = kick_mixed_chunks(c, s->ntp, s->npl);
-            SWG_TRY(ensure_kick_scratch(c, s->kick_scratch, kick_mixed_scratch_bytes(s->ntp, s->npl, nch)));
+            SWG_TRY(ensure_kick_scratch(c, s->kick_scratch_tp, kick_mixed_scratch_bytes(s->ntp, s->npl, nch)));
             SWG_TRY(kick_mixed_launch(c, true, s->ntp, s->npl, 0, s->trh, rp, s->Gmass, nullptr, s->tlmask, s->tah,
-                                      1, nch, s->kick_scratch.ptr));
+                                      1, nch, s->kick_scratch_tp.ptr));
         } else {
             SWG_TRY(kick_tp_fp64(c, s->ntp, s->npl, s->trh, rp, s->Gmass, s->tlmask, s->tah, 1));
         }
@@ -340,8 +349,41 @@ int kick_vb_tp(swg_system *s, double dt, int lbeg) {
     return L(c, "kick_update_tp");
 }
 
+// Mixed path: the per-system sum MODE over chunks of CHUNK_ONE bodies on many SMs
+// (k_chunk_sums, then k_chunk_apply), instead of one block.
+template <int MODE>
+int chunk_sum(swg_system *s, const double *vsum, const int32_t *mask, const double *vin, double *vout, double dt,
+              int slot) {
+    swg_ctx *c = s->c;
+    if (s->nchunks == 0) {
+        std::vector<int4> tab;
+        for (int b0 = 0, k = 0; b0 < s->npl; b0 += CHUNK_ONE, k++)
+            tab.push_back(make_int4(0, b0, std::min(CHUNK_ONE, s->npl - b0), k));
+        const size_t nt = tab.size();
+        SWG_TRY(ensure(c, s->chunk_buf, sizeof(int4) * (nt + 1) + sizeof(double) * 4 * nt));
+        const int2 range = make_int2(0, (int)nt);
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->chunk_buf.ptr, tab.data(), sizeof(int4) * nt, cudaMemcpyHostToDevice,
+                                               c->stream),
+                            "chunks"));
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync((int4 *)s->chunk_buf.ptr + nt, &range, sizeof(int2),
+                                               cudaMemcpyHostToDevice, c->stream),
+                            "chunks"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "chunks"));  // the host vectors go out of scope
+        s->nchunks = (int)nt;
+    }
+    const int4 *tab = (const int4 *)s->chunk_buf.ptr;
+    const int2 *range = (const int2 *)(tab + s->nchunks);
+    double *part = (double *)(tab + s->nchunks + 1);
+    k_chunk_sums<MODE><<<s->nchunks, CHUNK_T, 0, c->stream>>>(s->nchunks, tab, nullptr, s->Gmass, vsum, mask, part);
+    SWG_TRY(L(c, "chunk_sums"));
+    k_chunk_apply<MODE><<<s->nchunks, CHUNK_T, 0, c->stream>>>(tab, range, nullptr, part, nullptr, s->GMcb, s->lmask,
+                                                               vin, vout, s->rh, dt, s->dcb, slot);
+    return L(c, "chunk_apply");
+}
+
 int lindrift_pl(swg_system *s, double dt, int lbeg) {
     if (s->npl == 0) return SWG_OK;
+    if (!exact(s)) return chunk_sum<SUM_LIN>(s, s->vb, s->lmask, nullptr, nullptr, dt, lbeg ? CB_PTBEG : CB_PTEND);
     k_lindrift_pl<<<1, RB, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->lmask, s->GMcb, s->rh, dt, s->dcb,
                                                lbeg ? CB_PTBEG : CB_PTEND, exact(s));
     return L(s->c, "lindrift_pl");
@@ -354,11 +396,13 @@ int tp_misc(swg_system *s, int slot, double dt, int mode) {
 }
 int vh2vb_pl(swg_system *s) {
     if (s->npl == 0) return SWG_OK;
+    if (!exact(s)) return chunk_sum<SUM_VH2VB>(s, s->vh, nullptr, s->vh, s->vb, 0.0, 0);
     k_vh2vb_pl<<<1, RB, 0, s->c->stream>>>(s->npl, s->Gmass, s->vh, s->vb, s->GMcb, s->dcb, exact(s));
     return L(s->c, "vh2vb_pl");
 }
 int vb2vh_pl(swg_system *s) {
     if (s->npl == 0) return SWG_OK;
+    if (!exact(s)) return chunk_sum<SUM_VB2VH>(s, s->vb, s->status, s->vb, s->vh, 0.0, 0);
     k_vb2vh_pl<<<1, RB, 0, s->c->stream>>>(s->npl, s->Gmass, s->vb, s->status, s->vh, s->GMcb, s->dcb, exact(s));
     return L(s->c, "vb2vh_pl");
 }
@@ -498,6 +542,28 @@ int whm_step(swg_system *s, double dt) {
 }
 
 // ---- SyMBA
+// Runs f with the context's stream temporarily replaced (single host thread).
+template <class F>
+int on_stream(swg_ctx *c, cudaStream_t st, F f) {
+    const cudaStream_t saved = c->stream;
+    c->stream = st;
+    const int rc = f();
+    c->stream = saved;
+    return rc;
+}
+
+int ensure_side(swg_system *s) {
+    if (s->side) return SWG_OK;
+    SWG_TRY(cuda_status(s->c, cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "side stream"));
+    for (cudaEvent_t &e : s->ev) SWG_TRY(cuda_status(s->c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event"));
+    return SWG_OK;
+}
+// stream b waits for the work queued so far on stream a (event e)
+int join(swg_ctx *c, cudaStream_t a, cudaStream_t b, cudaEvent_t e) {
+    SWG_TRY(cuda_status(c, cudaEventRecord(e, a), "event"));
+    return cuda_status(c, cudaStreamWaitEvent(b, e, 0), "event");
+}
+
 int ensure_list(swg_system *s, int32_t **l, int64_t *cap, int64_t need) {
     if (need <= *cap) return SWG_OK;
     const int64_t ncap = std::max<int64_t>(need + need / 2, 256);
@@ -559,8 +625,16 @@ int symba_level0(swg_system *s, double dt, int *lany) {
                            "count");
     };
     h[0] = h[1] = 0;
-    if (do_pp) SWG_TRY(launch(0));
-    if (do_pt) SWG_TRY(launch(1));
+    if (do_pp && do_pt) {  // the two checks are independent: pl-tp on the second stream
+        SWG_TRY(ensure_side(s));
+        SWG_TRY(join(c, c->stream, s->side, s->ev[0]));
+        SWG_TRY(on_stream(c, s->side, [&] { return launch(1); }));
+        SWG_TRY(launch(0));
+        SWG_TRY(join(c, s->side, c->stream, s->ev[1]));
+    } else {
+        if (do_pp) SWG_TRY(launch(0));
+        if (do_pt) SWG_TRY(launch(1));
+    }
     SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "level0"));
     for (int k = 0; k < 2; k++) {  // capacity overflow: grow the raw buffers and redo that check
         if ((int64_t)h[k] <= w[k]->rawcap) continue;
@@ -695,7 +769,9 @@ int resolve_collisions(swg_system *s) {
     cs.dt = level_dt(s->rec_dt, irec);
     cs.E_collisions = s->E_collisions;
     for (int d = 0; d < 3; d++) cs.L_escape[d] = s->L_escape[d];
+    cs.dev = c;
     const int64_t nres = resolve_collisions_host(cs);
+    if (nres == -2) return SWG_ERR_CUDA;
     if (nres < 0) {
         c->err = "runaway collisional cascade (more than 1000 rounds of merges in one resolution)";
         return SWG_ERR_STATE;
@@ -762,11 +838,23 @@ int symba_recursion(swg_system *s, double dt) {
     a.fast = !exact(s);
     a.resume = s->rec_resume;
     a.pend = s->rec_out + 3;
+    // lists that fit are staged in shared memory (a collision resolution can redirect list
+    // entries but never adds any, so the size holds for the resumed launches)
+    const size_t need = rec_stage_bytes(s->plpl_n, s->pltp_n);
+    const size_t smem = need <= REC_STAGE_MAX ? need : 0;
+    a.stage_bytes = (int64_t)smem;
+    static bool smem_set = false;  // the kernel's own shared arrays come on top of the stage
+    if (smem > 0 && !smem_set) {
+        SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_symba_recursion, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)REC_STAGE_MAX),
+                            "recursion smem"));
+        smem_set = true;
+    }
     ProfScope ps(s->prof, s->c->stream, PROF_RECUR);
     for (;;) {
         if (s->lclose)
             SWG_TRY(cuda_status(c, cudaMemsetAsync(a.pend, 0, sizeof(int32_t), c->stream), "memset"));
-        k_symba_recursion<<<1, RECT, 0, c->stream>>>(a);
+        k_symba_recursion<<<1, RECT, smem, c->stream>>>(a);
         SWG_TRY(L(c, "symba_recursion"));
         if (!s->lclose) break;
         // a collision pauses the recursion: resolve it on the host, then resume
@@ -783,25 +871,57 @@ int symba_recursion(swg_system *s, double dt) {
                        "recursion status");
 }
 
-// symba_step_interp_system (symba_step.f90:55-115)
+// symba_step_interp_system (symba_step.f90:55-115).  With test particles, their half-steps
+// run on a second stream beside the massive bodies': they read the massive bodies only
+// through the start and end positions (copied to rbeg / rend before the fork) and the
+// central-body record, and the recursion (which moves the listed test particles) waits
+// for their opening half.  Each kernel's arithmetic is unchanged, so the results are the
+// serial order's bits.
 int symba_interp(swg_system *s, double dt) {
+    swg_ctx *c = s->c;
     const double dth = 0.5 * dt;
     s->irec = -1;
+    const bool fork = s->ntp > 0 && s->npl > 0;
+    if (fork) SWG_TRY(ensure_side(s));
     if (s->lfirst_pl) SWG_TRY(vh2vb_pl(s));
     SWG_TRY(lindrift_pl(s, dth, 1));
-    SWG_TRY(kick_vb_pl(s, dth, 1));
+    if (fork) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->rbeg, s->rh, 24 * (size_t)s->npl, cudaMemcpyDeviceToDevice, c->stream),
+                            "rbeg"));
+        SWG_TRY(join(c, c->stream, s->side, s->ev[0]));
+        SWG_TRY(on_stream(c, s->side, [&] {
+            SWG_TRY(tp_misc(s, CB_PTBEG, dth, s->lfirst_tp ? 4 : 2));
+            SWG_TRY(kick_vb_tp(s, dth, 1));
+            return drift_tp(s, dt);
+        }));
+    }
+    SWG_TRY(kick_vb_pl(s, dth, 1, !fork));
     SWG_TRY(drift_pl(s, dt));
-    if (s->ntp > 0) {
+    if (fork) {
+        SWG_TRY(join(c, s->side, c->stream, s->ev[1]));
+    } else if (s->ntp > 0) {
         SWG_TRY(tp_misc(s, CB_PTBEG, dth, s->lfirst_tp ? 4 : 2));
         SWG_TRY(kick_vb_tp(s, dth, 1));
         SWG_TRY(drift_tp(s, dt));
     }
     SWG_TRY(symba_recursion(s, dt));
     s->irec = -1;
-    SWG_TRY(kick_vb_pl(s, dth, 0));
+    if (fork) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->rend, s->rh, 24 * (size_t)s->npl, cudaMemcpyDeviceToDevice, c->stream),
+                            "rend"));
+        SWG_TRY(join(c, c->stream, s->side, s->ev[2]));
+        SWG_TRY(on_stream(c, s->side, [&] { return kick_vb_tp(s, dth, 0); }));
+    }
+    SWG_TRY(kick_vb_pl(s, dth, 0, !fork));
     SWG_TRY(lindrift_pl(s, dth, 0));
+    if (fork) {  // the test particles' closing linear drift needs the central-body record
+        SWG_TRY(join(c, c->stream, s->side, s->ev[3]));
+        SWG_TRY(on_stream(c, s->side, [&] { return tp_misc(s, CB_PTEND, dth, 3); }));
+    }
     SWG_TRY(vb2vh_pl(s));
-    if (s->ntp > 0) {
+    if (fork) {
+        SWG_TRY(join(c, s->side, c->stream, s->ev[4]));
+    } else if (s->ntp > 0) {
         SWG_TRY(kick_vb_tp(s, dth, 0));
         SWG_TRY(tp_misc(s, CB_PTEND, dth, 3));
     }
@@ -915,10 +1035,13 @@ int swg_system_destroy(swg_system *s) {
                     s->tlevelm, s->tnplenc, s->tiflag, s->dcb, s->plpl_l, s->pltp_l, s->enc.raw.ptr,
                     s->enc.sort.ptr, s->enc.counters.ptr, s->enc2.raw.ptr, s->enc2.sort.ptr, s->enc2.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
                     s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_resume, s->rec_scratch.ptr,
-                    s->discard_scratch.ptr, s->tflag, s->ndiscard};
+                    s->discard_scratch.ptr, s->tflag, s->ndiscard, s->chunk_buf.ptr, s->kick_scratch_tp.ptr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);
+    for (cudaEvent_t e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->side) cudaStreamDestroy(s->side);
     s->prof.release();
     delete s;
     return SWG_OK;
