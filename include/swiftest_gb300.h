@@ -255,9 +255,10 @@ int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
 /* Strip length of the symmetric pl-pl kick: each work item evaluates one row tile against
  * `strip` tile pairs, and a body's sums are split into one slot per item, so the strip sets
  * how the terms are grouped (results within the mixed-kick tolerance of each other, each
- * deterministic).  By default (0) the fastest of 1, 2, 4, 8, 16 is timed on the ensemble's
- * own data at its first mixed kick and cached like the tile shapes; 1, 2, 4, 8 or 16 forces
- * it.  swg_ensemble_kick_variant with kind 2 reads the strip in use (-1 before the first
+ * deterministic).  By default (0) the strips 1, 2, 4, 8 and 16 are timed on the ensemble's
+ * own data at its first mixed kick (the minimum of five launches each) and the default 4 is
+ * kept unless another is more than 3% faster; the choice is cached like the tile shapes.
+ * 1, 2, 4, 8 or 16 forces it.  swg_ensemble_kick_variant with kind 2 reads the strip in use (-1 before the first
  * mixed kick). */
 int swg_ensemble_set_kick_strip(swg_ensemble *ens, int strip);
 /* swiftest_kick_getacch_int_all_tri_pl (swiftest_kick.f90:183-264) of every system from its
