@@ -9,8 +9,10 @@
 // system's extents into contiguous per-system runs.
 //
 // Passes: 8-bit digits, least significant first, each a reduce-then-scan over tiles of 256
-// to 2048 elements (fewer per tile for small sorts): per-tile digit counts (k_rs_upsweep), an exclusive scan of the counts in
-// digit-major order (k_rs_scan), and a stable scatter (k_rs_scatter) that ranks the tile's
+// to 2048 elements (fewer per tile for small sorts): per-tile digit counts (k_rs_upsweep),
+// an exclusive scan of each digit's row of tile counts with the row totals (k_rs_scan_rows,
+// one block per digit), and a stable scatter (k_rs_scatter) that adds the digit's base from
+// the totals and ranks the tile's
 // elements column by column with warp match_any and per-warp prefix counts in shared
 // memory.  One pass over the data first counts every digit of every pass
 // (k_rs_hist_all); the host reads those counts and skips the passes whose digit is the
@@ -77,38 +79,45 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(int64_t n, const uint
     cnt[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
 }
 
-// exclusive scan of m counts in place, one block of 1024 threads (each thread a run)
-__global__ void __launch_bounds__(1024) k_rs_scan(int64_t m, unsigned *__restrict__ cnt) {
-    __shared__ unsigned s_w[32];
+// Exclusive scan of each digit's row of tile counts in place (block d scans row d,
+// cnt[d * ntiles + tile], coalesced), and the row totals tot[d].  The scatter adds the
+// digits' exclusive prefix of tot (a 256-wide scan per block), so the offsets are the
+// digit-major exclusive scan of all counts without a single-block pass over all of them.
+__global__ void __launch_bounds__(1024) k_rs_scan_rows(int64_t ntiles, unsigned *__restrict__ cnt,
+                                                       unsigned *__restrict__ tot) {
+    __shared__ unsigned s_w[32], s_carry;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int64_t per = (m + 1023) / 1024, b0 = t * per, b1 = b0 + per < m ? b0 + per : m;
-    unsigned run = 0;
-    for (int64_t i = b0; i < b1; i++) run += cnt[i];
-    // block-wide exclusive scan of the run totals
-    unsigned x = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(FULL, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_w[w] = x;
+    unsigned *row = cnt + (int64_t)blockIdx.x * ntiles;
+    if (t == 0) s_carry = 0u;
     __syncthreads();
-    if (w == 0) {
-        unsigned z = s_w[lane];
+    for (int64_t b0 = 0; b0 < ntiles; b0 += 1024) {
+        const int64_t i = b0 + t;
+        const unsigned own = i < ntiles ? row[i] : 0u;
+        unsigned x = own;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(FULL, z, o);
-            if (lane >= o) z += y;
+            const unsigned y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
         }
-        s_w[lane] = z;
+        if (lane == 31) s_w[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            unsigned z = s_w[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(FULL, z, o);
+                if (lane >= o) z += y;
+            }
+            s_w[lane] = z;
+        }
+        __syncthreads();
+        const unsigned carry = s_carry;
+        if (i < ntiles) row[i] = carry + x - own + (w > 0 ? s_w[w - 1] : 0u);
+        __syncthreads();
+        if (t == 0) s_carry = carry + s_w[31];
+        __syncthreads();
     }
-    __syncthreads();
-    unsigned off = x - run + (w > 0 ? s_w[w - 1] : 0u);
-    for (int64_t i = b0; i < b1; i++) {
-        const unsigned c = cnt[i];
-        cnt[i] = off;
-        off += c;
-    }
+    if (t == 0) tot[blockIdx.x] = s_carry;
 }
 
 // stable scatter of pass p: element e of the tile goes to its digit's offset for this tile
@@ -118,12 +127,27 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(int64_t n, const uint
                                                            const uint32_t *__restrict__ vin,
                                                            const int32_t *__restrict__ seg_of, int p, int cols,
                                                            const unsigned *__restrict__ off,
+                                                           const unsigned *__restrict__ tot,
                                                            uint64_t *__restrict__ kout, uint32_t *__restrict__ vout) {
     constexpr int NW = RS_THREADS / 32;
     __shared__ unsigned s_base[RS_BINS];      // next free position of each digit for this tile
     __shared__ unsigned s_wc[NW][RS_BINS];    // per-warp counts, then per-warp offsets, of one column
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    s_base[t] = off[(int64_t)t * gridDim.x + blockIdx.x];
+    {  // digit t's first position: the totals of the smaller digits (256-wide exclusive scan)
+        const unsigned own = tot[t];
+        unsigned x = own;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_wc[0][w] = x;
+        __syncthreads();
+        unsigned before = 0u;
+        for (int q = 0; q < w; q++) before += s_wc[0][q];
+        s_base[t] = before + x - own + off[(int64_t)t * gridDim.x + blockIdx.x];
+        __syncthreads();  // s_wc is cleared next
+    }
     const int64_t base = (int64_t)blockIdx.x * RS_THREADS * cols;
     for (int c = 0; c < cols; c++) {
 #pragma unroll
@@ -210,7 +234,7 @@ static int rs_cols(int64_t n, int num_sms) {
 
 size_t radix_sort_scratch_bytes(int64_t n) {
     const int64_t ntiles = (n + RS_THREADS - 1) / RS_THREADS;  // enough for any tile size
-    return (size_t)n * 12 + (size_t)ntiles * RS_BINS * 4 + RS_MAX_PASSES * RS_BINS * 4 + 1024;
+    return (size_t)n * 12 + (size_t)ntiles * RS_BINS * 4 + (RS_MAX_PASSES + 1) * RS_BINS * 4 + 1024;
 }
 
 int radix_sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals, void *scratch, const int32_t *seg_of,
@@ -226,6 +250,7 @@ int radix_sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals, void *s
     uint32_t *v2 = (uint32_t *)(k2 + n);
     unsigned *cnt = (unsigned *)(v2 + n);
     unsigned *hist = cnt + ntiles * RS_BINS;
+    unsigned *tot = hist + RS_MAX_PASSES * RS_BINS;  // row totals of the current pass
     std::vector<unsigned> h;
     if (host_skip) {
         SWG_TRY(cuda_status(c, cudaMemsetAsync(hist, 0, sizeof(unsigned) * npass * RS_BINS, c->stream), "memset"));
@@ -247,8 +272,9 @@ int radix_sort_kv(swg_ctx *c, int64_t n, uint64_t *keys, uint32_t *vals, void *s
         for (int d = 0; d < RS_BINS && host_skip; d++) trivial |= h[p * RS_BINS + d] == (unsigned)n;
         if (trivial) continue;  // every element has the same digit: the pass keeps the order
         k_rs_upsweep<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cols, cnt);
-        k_rs_scan<<<1, 1024, 0, c->stream>>>(ntiles * RS_BINS, cnt);
-        k_rs_scatter<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cols, cnt, kout, vout);
+        k_rs_scan_rows<<<RS_BINS, 1024, 0, c->stream>>>(ntiles, cnt, tot);
+        k_rs_scatter<<<(int)ntiles, RS_THREADS, 0, c->stream>>>(n, kin, vin, seg_of, p, cols, cnt, tot, kout,
+                                                                 vout);
         c->launches += 3;
         SWG_TRY(launch_status(c, "radix_pass"));
         std::swap(kin, kout);
