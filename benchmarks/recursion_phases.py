@@ -44,10 +44,10 @@ def _patch(s: str) -> str:
     rep("        stg_load(a, S, nbpl, nbtp);\n    }", "        stg_load(a, S, nbpl, nbtp);\n    }\n    PH(11, t0)")
     for call, k in (("stg_list_check(a, S, irecp, dtl, &s_any, s_rs);", 1),
                     ("stg_kick_lists(a, S, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);\n                stg_drift", 2),
-                    ("stg_drift(a, S, nbpl, nbtp, ireci, dtl);", 3),
+                    ("stg_drift(a, S, nbpl, nbtp, ireci, dtl, inv_gm);", 3),
                     ("blk_list_check(a, irecp, dtl, &s_any, s_rs);", 1),
                     ("blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);\n                blk_drift", 2),
-                    ("blk_drift(a, nbpl, nbtp, ireci, dtl);", 3)):
+                    ("blk_drift(a, nbpl, nbtp, ireci, dtl, inv_gm);", 3)):
         if call.endswith("stg_drift") or call.endswith("blk_drift"):
             head, tail = call.split("\n")
             rep(call, f"{head}\n                PH({k}, t0)\n{tail}")

@@ -317,8 +317,9 @@ __device__ inline void d_kepmd_fast(double dm, double es, double ec, double &x, 
     c = cc;
 }
 
+// inv_mu: 1/mu when the caller has it (the same value, formed once), else 0
 __device__ inline void d_drift_dan_fast(double mu, double &rx0, double &ry0, double &rz0, double &vx0, double &vy0,
-                                        double &vz0, double dt0, int &iflag) {
+                                        double &vz0, double dt0, int &iflag, double inv_mu0 = 0.0) {
     iflag = 0;
     const double r2 = fma(rz0, rz0, fma(ry0, ry0, rx0 * rx0));
     const double inv_r0 = rsqrt(r2);
@@ -326,7 +327,7 @@ __device__ inline void d_drift_dan_fast(double mu, double &rx0, double &ry0, dou
     const double u = fma(rz0, vz0, fma(ry0, vy0, rx0 * vx0));
     const double alpha = fma(2.0 * mu, inv_r0, -v0s);
     if (alpha > 0.0) {
-        const double inv_mu = 1.0 / mu;
+        const double inv_mu = inv_mu0 != 0.0 ? inv_mu0 : 1.0 / mu;
         const double rsa = rsqrt(alpha);
         const double a = mu * rsa * rsa;                 // mu / alpha
         const double ia = alpha * inv_mu;                // 1 / a
@@ -369,13 +370,13 @@ __device__ inline void d_drift_dan_fast(double mu, double &rx0, double &ry0, dou
 }
 
 __device__ inline int d_drift_one_fast(double mu, double &rx, double &ry, double &rz, double &vx, double &vy,
-                                       double &vz, double dt) {
+                                       double &vz, double dt, double inv_mu = 0.0) {
     int iflag;
-    d_drift_dan_fast(mu, rx, ry, rz, vx, vy, vz, dt, iflag);
+    d_drift_dan_fast(mu, rx, ry, rz, vx, vy, vz, dt, iflag, inv_mu);
     if (iflag != 0) {
         const double dttmp = 0.1 * dt;
         for (int i = 1; i <= 10; i++) {
-            d_drift_dan_fast(mu, rx, ry, rz, vx, vy, vz, dttmp, iflag);
+            d_drift_dan_fast(mu, rx, ry, rz, vx, vy, vz, dttmp, iflag, inv_mu);
             if (iflag != 0) break;
         }
     }

@@ -351,6 +351,39 @@ __device__ __forceinline__ void d_enc_one(double xr, double yr, double zr, doubl
     lenc = lvdotr && (r2min <= r2crit);
 }
 
+// encounter_check_one for the recursion's list checks of the mixed path: the same test with
+// FMA-contracted dot products and one reciprocal of v^2 for its two quotients (each FP64
+// divide is a long sequence on GB300's narrow FP64 pipe, which sets the recursion's pace)
+__device__ __forceinline__ void d_enc_one_fast(double xr, double yr, double zr, double vxr, double vyr, double vzr,
+                                               double renc, double dt, int &lenc, int &lvdotr) {
+    const double r2 = fma(zr, zr, fma(yr, yr, xr * xr));
+    const double r2crit = renc * renc;
+    double vdotr, r2min;
+    if (r2 > r2crit) {
+        vdotr = fma(vzr, zr, fma(vyr, yr, vxr * xr));
+        if (vdotr > 0.0) {
+            r2min = r2;
+        } else {
+            const double v2 = fma(vzr, vzr, fma(vyr, vyr, vxr * vxr));
+            if (v2 <= VSMALL) {
+                r2min = r2;
+            } else {
+                const double iv2 = 1.0 / v2;
+                const double tmin = -vdotr * iv2;
+                if (tmin < dt)
+                    r2min = fma(-(vdotr * vdotr), iv2, r2);
+                else
+                    r2min = fma(v2, dt * dt, fma(2.0 * vdotr, dt, r2));
+            }
+        }
+    } else {
+        vdotr = -1.0;
+        r2min = r2;
+    }
+    lvdotr = (vdotr < 0.0);
+    lenc = lvdotr && (r2min <= r2crit);
+}
+
 // x**(-1.5) of the shell kick (symba_kick.f90:204,307): sqrt(x) and x*sqrt(x) as
 // double-double pairs (Dekker's error-free transformations with fma residuals),
 // then one Newton step on the reciprocal.  Within half an ulp except in rare
@@ -444,7 +477,10 @@ static __device__ void blk_list_check(const RecArgs &a, int irec, double dt, int
             const double renci = a.rhill[i] * a.rhscale * rs_pow[irec];  // d_renc(rhill_i, rhscale, irec)
             const double rcrit = isp ? renci + a.rhill[j] * a.rhscale * rs_pow[irec] : renci;
             int le, lvd;
-            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            if (a.fast)
+                d_enc_one_fast(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            else
+                d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
             lv[q] = lvd;
             if (le) {
                 const double rs = isp ? a.radius[i] + a.radius[j] : a.radius[i];
@@ -534,7 +570,8 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
         const double *rj = isp ? &a.rh[3 * j] : &a.trh[3 * j];
         double dx[3];
         for (int d = 0; d < 3; d++) dx[d] = rj[d] - a.rh[3 * i + d];
-        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        const double r2 = a.fast ? fma(dx[2], dx[2], fma(dx[1], dx[1], dx[0] * dx[0]))
+                                 : dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
         const bool kp = !(r2 < ri_p * (RSHELL * RSHELL));
         const bool km = both && !(r2 < ri_m * (RSHELL * RSHELL));
         a.good[k] = kp ? 1 : 2;
@@ -556,8 +593,11 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
         if (!a.fast && (shp || shm)) p = pow_m1p5(r2);
         auto shell = [&](double ri) {
             // rr = (sqrt(ri) - r) / (sqrt(ri) (1 - RSHELL)); mixed path as (1 - r / sqrt(ri)) / (1 - RSHELL)
-            const double rr = a.fast ? (1.0 - r * rsqrt(ri)) * (1.0 / (1.0 - RSHELL))
-                                     : (sqrt(ri) - r) / (sqrt(ri) * (1.0 - RSHELL));
+            if (a.fast) {  // 1 - 3 rr^2 + 2 rr^3 as 1 + rr^2 (2 rr - 3)
+                const double rr = fma(-r, rsqrt(ri), 1.0) * (1.0 / (1.0 - RSHELL));
+                return p * fma(rr * rr, fma(2.0, rr, -3.0), 1.0);
+            }
+            const double rr = (sqrt(ri) - r) / (sqrt(ri) * (1.0 - RSHELL));
             return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         };
         double *t = &a.terms[12 * k];
@@ -616,9 +656,15 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
             if (!zeroed[sg]) continue;
             const double sdt = sg == 0 ? dt : -dt;
             if (kicked[sg]) {
-                v[0] = v[0] + sdt * ax[sg];
-                v[1] = v[1] + sdt * ay[sg];
-                v[2] = v[2] + sdt * az[sg];
+                if (a.fast) {
+                    v[0] = fma(sdt, ax[sg], v[0]);
+                    v[1] = fma(sdt, ay[sg], v[1]);
+                    v[2] = fma(sdt, az[sg], v[2]);
+                } else {
+                    v[0] = v[0] + sdt * ax[sg];
+                    v[1] = v[1] + sdt * ay[sg];
+                    v[2] = v[2] + sdt * az[sg];
+                }
             }
             acc[0] = acc[1] = acc[2] = 0.0;
         }
@@ -628,7 +674,7 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
 
 // symba_drift_pl / _tp at level irec (symba_drift.f90:14-61) over the bodies that
 // appear in the lists (every other body has levelg == -1 inside the recursion).
-static __device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec, double dt) {
+static __device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec, double dt, double inv_gm) {
     for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
         const bool isp = b < nbpl;
         const int i = isp ? a.bpl[b] : a.btp[b - nbpl];
@@ -638,7 +684,7 @@ static __device__ void blk_drift(const RecArgs &a, int nbpl, int nbtp, int irec,
         double *x = isp ? &a.rh[3 * i] : &a.trh[3 * i];
         double *v = isp ? &a.vb[3 * i] : &a.tvb[3 * i];
         double rx = x[0], ry = x[1], rz = x[2], vx = v[0], vy = v[1], vz = v[2];
-        const int fl = a.fast ? d_drift_one_fast(a.GMcb, rx, ry, rz, vx, vy, vz, dt)
+        const int fl = a.fast ? d_drift_one_fast(a.GMcb, rx, ry, rz, vx, vy, vz, dt, inv_gm)
                               : d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
         x[0] = rx;
         x[1] = ry;
@@ -1034,7 +1080,10 @@ static __device__ void stg_list_check(const RecArgs &a, const RecStage &S, int i
             const double renci = S.rhill[b1] * a.rhscale * rs_pow[irec];  // d_renc(rhill_i, rhscale, irec)
             const double rcrit = isp ? renci + S.rhill[b2] * a.rhscale * rs_pow[irec] : renci;
             int le, lvd;
-            d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            if (a.fast)
+                d_enc_one_fast(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
+            else
+                d_enc_one(xr[0], xr[1], xr[2], vr[0], vr[1], vr[2], rcrit, dt, le, lvd);
             S.elv[k] = lvd;
             if (le) {
                 const double rs = isp ? S.rad[b1] + S.rad[b2] : S.rad[b1];
@@ -1088,7 +1137,8 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
         const double ri_p = base * shell_p, ri_m = base * shell_m;
         double dx[3];
         for (int d = 0; d < 3; d++) dx[d] = S.r[3 * b2 + d] - S.r[3 * b1 + d];
-        const double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        const double r2 = a.fast ? fma(dx[2], dx[2], fma(dx[1], dx[1], dx[0] * dx[0]))
+                                 : dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
         const bool kp = !(r2 < ri_p * (RSHELL * RSHELL));
         const bool km = both && !(r2 < ri_m * (RSHELL * RSHELL));
         S.good[k] = kp ? 1 : 2;
@@ -1107,8 +1157,11 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
         double p = ir3;
         if (!a.fast && (shp || shm)) p = pow_m1p5(r2);
         auto shell = [&](double ri) {
-            const double rr = a.fast ? (1.0 - r * rsqrt(ri)) * (1.0 / (1.0 - RSHELL))
-                                     : (sqrt(ri) - r) / (sqrt(ri) * (1.0 - RSHELL));
+            if (a.fast) {  // 1 - 3 rr^2 + 2 rr^3 as 1 + rr^2 (2 rr - 3)
+                const double rr = fma(-r, rsqrt(ri), 1.0) * (1.0 / (1.0 - RSHELL));
+                return p * fma(rr * rr, fma(2.0, rr, -3.0), 1.0);
+            }
+            const double rr = (sqrt(ri) - r) / (sqrt(ri) * (1.0 - RSHELL));
             return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         };
         double *t = &S.terms[12 * k];
@@ -1163,9 +1216,15 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
             if (!zeroed[sg]) continue;
             const double sdt = sg == 0 ? dt : -dt;
             if (kicked[sg]) {
-                v[0] = v[0] + sdt * ax[sg];
-                v[1] = v[1] + sdt * ay[sg];
-                v[2] = v[2] + sdt * az[sg];
+                if (a.fast) {
+                    v[0] = fma(sdt, ax[sg], v[0]);
+                    v[1] = fma(sdt, ay[sg], v[1]);
+                    v[2] = fma(sdt, az[sg], v[2]);
+                } else {
+                    v[0] = v[0] + sdt * ax[sg];
+                    v[1] = v[1] + sdt * ay[sg];
+                    v[2] = v[2] + sdt * az[sg];
+                }
             }
             acc[0] = acc[1] = acc[2] = 0.0;
         }
@@ -1173,12 +1232,13 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
     __syncthreads();
 }
 // blk_drift on the stage
-static __device__ void stg_drift(const RecArgs &a, const RecStage &S, int nbpl, int nbtp, int irec, double dt) {
+static __device__ void stg_drift(const RecArgs &a, const RecStage &S, int nbpl, int nbtp, int irec, double dt,
+                                 double inv_gm) {
     for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
         if (S.lev[b] != irec || S.st[b] == ST_INACTIVE) continue;
         double *x = &S.r[3 * b], *v = &S.v[3 * b];
         double rx = x[0], ry = x[1], rz = x[2], vx = v[0], vy = v[1], vz = v[2];
-        const int fl = a.fast ? d_drift_one_fast(a.GMcb, rx, ry, rz, vx, vy, vz, dt)
+        const int fl = a.fast ? d_drift_one_fast(a.GMcb, rx, ry, rz, vx, vy, vz, dt, inv_gm)
                               : d_drift_one(a.GMcb, rx, ry, rz, vx, vy, vz, dt);
         x[0] = rx;
         x[1] = ry;
@@ -1294,6 +1354,7 @@ static __device__ void blk_symba_recursion_t(const RecArgs &a, void *stage) {
     __syncthreads();
     int deepest = 0, substeps = 0;
     bool paused = false;
+    const double inv_gm = 1.0 / a.GMcb;  // the fast drift's 1/mu, formed once
     for (;;) {
         const double dtl = s_dtl[ireci];
         const double dth = 0.5 * dtl;
@@ -1320,11 +1381,11 @@ static __device__ void blk_symba_recursion_t(const RecArgs &a, void *stage) {
             if constexpr (STAGED) {
                 stg_list_check(a, S, irecp, dtl, &s_any, s_rs);
                 stg_kick_lists(a, S, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
-                stg_drift(a, S, nbpl, nbtp, ireci, dtl);
+                stg_drift(a, S, nbpl, nbtp, ireci, dtl, inv_gm);
             } else {
                 blk_list_check(a, irecp, dtl, &s_any, s_rs);
                 blk_kick_lists(a, nbpl, nbtp, dth, irecp, ireci != 0, s_pw);
-                blk_drift(a, nbpl, nbtp, ireci, dtl);
+                blk_drift(a, nbpl, nbtp, ireci, dtl, inv_gm);
             }
             const int any = s_any;
             __syncthreads();
