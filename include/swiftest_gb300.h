@@ -72,9 +72,9 @@ int swg_kick_getacch_int_all_flat_pl(swg_ctx *ctx, int32_t npl, int32_t nplm, in
 
 /* The mixed-precision pl-pl kick of swg_kick_getacch_int_all_tri_pl (SWG_MIXED) for callers
  * that cannot allocate device memory while they run: an application that owns every
- * device allocation in a fixed pool sized at start-up, or host code whose step is
- * recorded into a CUDA graph, where cudaMalloc/cudaFree are not allowed and can
- * synchronize the device.  It has no counterpart in the reference.  It calls no
+ * device allocation in a fixed pool sized at start-up (a cudaMalloc mid-run could fail
+ * or fragment that pool), or host code that keeps other streams busy and cannot let a
+ * cudaMalloc/cudaFree synchronize the device.  It has no counterpart in the reference.  It calls no
  * cudaMalloc or cudaFree, takes device pointers and a cudaStream_t, and accumulates into
  * acc like the regular entry point.  It runs the regular entry point's broadcast kernel
  * on the same grid, so its results are the same bits wherever that entry point takes the

@@ -1,14 +1,14 @@
 // kick_noalloc.cu -- the mixed-precision pl-pl kick for callers that cannot allocate
 // device memory.
 //
-// Who needs it: a host integrator that records its step into a CUDA graph, or that
-// runs inside an application which owns every device allocation (a memory pool, a
-// fixed arena sized at start-up), must not call cudaMalloc/cudaFree mid-run: both
-// can synchronize the whole device, and neither may appear inside stream capture.
-// The regular entry points grow scratch buffers on demand, so they cannot serve
-// such a caller.  This variant keeps its scratch (the per-block completion counters
-// and the float-float partial sums of the mixed kick) in a fixed, file-scope device
-// array instead.
+// Who needs it: a host integrator that runs inside an application which owns every
+// device allocation (a memory pool, a fixed arena sized at start-up) must not call
+// cudaMalloc/cudaFree mid-run: the pool has taken the memory, so a new allocation can
+// fail or fragment it, and both calls can synchronize the whole device, stalling the
+// work the application keeps in flight on its other streams.  The regular entry points
+// grow scratch buffers on demand, so they cannot serve such a caller.  This variant
+// keeps its scratch (the per-block completion counters and the float-float partial
+// sums of the mixed kick) in a fixed, file-scope device array instead.
 //
 // Limits and sharing:
 //  * the array is NOALLOC_SCRATCH_BYTES (16 MiB) and every GPU that loads the library
