@@ -2,9 +2,10 @@
 //
 // The reference's triangular check (src/encounter/encounter_check.f90:436-475) tests every
 // pair i < j with encounter_check_one (:573-621).  Here, per system, the bodies are ordered
-// by heliocentric distance (one shared-memory sort per system) and cut into tiles of 64;
-// a pair of tiles is skipped when no pair in it can pass the FP64 test, and every other
-// pair goes through the same FP32 prefilter and FP64 decision as the unsorted kernel, on
+// by heliocentric distance (one shared-memory sort per system) and cut into sub-tiles of
+// 32; a warp of 32 receivers skips every partner sub-tile in which no pair with its
+// receivers can pass the FP64 test, and every other pair goes through the same FP32
+// prefilter and FP64 decision as the unsorted kernel, on
 // the bodies' original indices and in the reference's orientation (i < j).  The list is
 // sorted by (index1, index2) afterwards, so it is the triangular check's list exactly; the
 // order only decides how much is skipped.
@@ -55,9 +56,10 @@ __global__ void __launch_bounds__(1024) k_radial_sort(const int32_t *__restrict_
     int32_t *idx = (int32_t *)(key + npad);
     for (int t = threadIdx.x; t < npad; t += blockDim.x) {
         float k = __int_as_float(0x7f800000);  // +inf pads the tail
-        if (t < n) {
+        if (t < n) {  // the order only has to be roughly radial: FP32 is enough
             const double *x = &r[3 * (size_t)(o + t)];
-            k = (float)sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+            const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
+            k = sqrtf(fmaf(x2, x2, fmaf(x1, x1, x0 * x0)));
         }
         key[t] = k;
         idx[t] = t;
@@ -89,14 +91,14 @@ __global__ void __launch_bounds__(1024) k_radial_sort(const int32_t *__restrict_
 }
 
 // One block of SB threads per bound tile (sys, first sorted position): the prefilter's
-// float copies in sorted order and the tile's bounds (min lo, max hi, max renc), rounded
-// outward.
+// float copies in sorted order and the bounds (min lo, max hi, max renc), rounded outward,
+// of each 32-body half u of the tile (bounds[2 t + u]; a half without bodies gets
+// (+inf, -inf, 0), which is apart from everything).
 __global__ void __launch_bounds__(SB) k_sorted_prep(const int2 *__restrict__ tiles, const int32_t *__restrict__ poff,
                                                     const int32_t *__restrict__ npl, const int32_t *__restrict__ perm,
                                                     const double *__restrict__ r, const double *__restrict__ v,
                                                     const double *__restrict__ renc, float adt, float4 *A, float4 *B,
                                                     float4 *V, float4 *bounds) {
-    __shared__ float s_lo[SB / 32], s_hi[SB / 32], s_R[SB / 32];
     const int2 tl = tiles[blockIdx.x];
     const int p = poff[tl.x] + tl.y + threadIdx.x;
     const bool in = tl.y + (int)threadIdx.x < npl[tl.x];
@@ -125,20 +127,7 @@ __global__ void __launch_bounds__(SB) k_sorted_prep(const int2 *__restrict__ til
         hi = fmaxf(hi, __shfl_down_sync(0xffffffffu, hi, off));
         Rm = fmaxf(Rm, __shfl_down_sync(0xffffffffu, Rm, off));
     }
-    if ((threadIdx.x & 31) == 0) {
-        s_lo[threadIdx.x >> 5] = lo;
-        s_hi[threadIdx.x >> 5] = hi;
-        s_R[threadIdx.x >> 5] = Rm;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < SB / 32; w++) {
-            lo = fminf(lo, s_lo[w]);
-            hi = fmaxf(hi, s_hi[w]);
-            Rm = fmaxf(Rm, s_R[w]);
-        }
-        bounds[blockIdx.x] = make_float4(lo, hi, Rm, 0.f);
-    }
+    if ((threadIdx.x & 31) == 0) bounds[(SB / 32) * blockIdx.x + (threadIdx.x >> 5)] = make_float4(lo, hi, Rm, 0.f);
 }
 
 // True when no pair across tiles P and Q can pass the FP64 test (see the file comment).
@@ -148,31 +137,40 @@ __device__ __forceinline__ bool tiles_apart(float4 P, float4 Q) {
     return gap > reach;
 }
 
+// One warp's partners: each lane stages one partner (float copies and global index) in the
+// warp's own shared slots.
+struct WarpStage {
+    float4 a[32], b[32], v[32];
+    int32_t g[32];
+};
+
 // Item (system, first receiver in sorted order q0, receivers nr): receivers are sorted
-// positions [q0, q0 + nr), partners sorted positions p < q; tbase[s] is the system's first
-// bound tile.
+// positions [q0, q0 + nr), partners sorted positions p < q.  Each warp works alone on its
+// 32 receivers (no block barriers): its lanes test the bounds of 32 partner sub-tiles (32
+// bodies each) at a time against the warp's own sub-tile bound, and for every sub-tile
+// that is not apart the lanes stage its partners in the warp's shared slots and each lane
+// runs its receiver against them.
 __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict__ items, const int32_t *__restrict__ poff,
                                                          const int32_t *__restrict__ tbase,
                                                          const int32_t *__restrict__ perm, const float4 *__restrict__ A,
                                                          const float4 *__restrict__ B, const float4 *__restrict__ V,
-                                                         const float4 *__restrict__ bounds, const double *__restrict__ r,
+                                                         const float4 *__restrict__ sub, const double *__restrict__ r,
                                                          const double *__restrict__ v, const double *__restrict__ renc,
                                                          double dt, long long cap, int32_t *__restrict__ o1,
                                                          int32_t *__restrict__ o2, int32_t *__restrict__ olv,
                                                          unsigned long long *__restrict__ count) {
-    __shared__ float4 sa[SB], sb[SB], sv[SB];
-    __shared__ int32_t sg[SB];
+    __shared__ WarpStage st_all[SQ / 32];
     const int4 w = items[blockIdx.x];
     const int s = w.x, q0 = w.y, nr = w.z;
+    const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (32 * wq >= nr) return;  // no receivers in this warp
+    WarpStage &st = st_all[wq];
     const int o = poff[s];
-    const int qt = tbase[s] + q0 / SB;  // first bound tile of the receivers
-    float4 Q = bounds[qt];
-    if (nr > SB) {
-        const float4 Q2 = bounds[qt + 1];
-        Q = make_float4(fminf(Q.x, Q2.x), fmaxf(Q.y, Q2.y), fmaxf(Q.z, Q2.z), 0.f);
-    }
+    const float4 *S = sub + (SB / 32) * (size_t)tbase[s];  // the system's sub-tile (half-tile) bounds
+    const float4 QW = S[q0 / 32 + wq];
     const int q = q0 + threadIdx.x;  // sorted position within the system
-    const bool active = (int)threadIdx.x < nr;
+    const int qb = min(q0 + nr, q0 + 32 * wq + 32);  // this warp's receivers end here
+    const bool active = q < qb;
     BodyF me;
     int gq = 0;
     if (active) {
@@ -182,26 +180,32 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
         gq = perm[o + q];
     }
     const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);
-    const int pend = q0 + nr;  // partners p < q <= q0 + nr - 1
-    for (int p0 = 0; p0 < pend; p0 += SB) {
-        if (tiles_apart(bounds[tbase[s] + p0 / SB], Q)) continue;  // block-uniform
-        if (threadIdx.x < SB && p0 + (int)threadIdx.x < pend) {
-            const int pp = o + p0 + threadIdx.x;
-            sa[threadIdx.x] = A[pp];
-            sb[threadIdx.x] = B[pp];
-            sv[threadIdx.x] = V[pp];
-            sg[threadIdx.x] = perm[pp];
-        }
-        __syncthreads();
-        if (active) {
-            const int nt = min(SB, q - p0);  // partners p < q of this tile
+    const int pend = qb - 1;  // partners p < q <= qb - 1
+    const int nsub = (pend + 31) / 32;
+    for (int u0 = 0; u0 < nsub; u0 += 32) {
+        const bool keep = u0 + lane < nsub && !tiles_apart(S[u0 + lane], QW);
+        unsigned m = __ballot_sync(0xffffffffu, keep);
+        while (m) {
+            const int p0 = 32 * (u0 + __ffs(m) - 1);
+            m &= m - 1;
+            __syncwarp();  // the previous sub-tile is consumed
+            if (p0 + lane < pend) {
+                const int pp = o + p0 + lane;
+                st.a[lane] = A[pp];
+                st.b[lane] = B[pp];
+                st.v[lane] = V[pp];
+                st.g[lane] = perm[pp];
+            }
+            __syncwarp();
+            if (!active) continue;
+            const int nt = min(32, q - p0);  // partners p < q of this sub-tile
             for (int ii = 0; ii < nt; ii++) {
                 BodyF other;
-                other.a = sa[ii];
-                other.b = sb[ii];
-                other.v = sv[ii];
+                other.a = st.a[ii];
+                other.b = st.b[ii];
+                other.v = st.v[ii];
                 if (prefilter_reject(other, me, dtf)) continue;
-                const int gp = sg[ii];
+                const int gp = st.g[ii];
                 const int i = min(gp, gq), j = max(gp, gq);  // the reference's orientation, i < j
                 const double xr = r[3 * (size_t)j + 0] - r[3 * (size_t)i + 0];
                 const double yr = r[3 * (size_t)j + 1] - r[3 * (size_t)i + 1];
@@ -212,16 +216,15 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
                 int lenc, lv;
                 d_encounter_one(xr, yr, zr, vxr, vyr, vzr, renc[i] + renc[j], dt, lenc, lv);
                 if (lenc) {
-                    const unsigned long long k = atomicAdd(count, 1ull);
-                    if ((long long)k < cap) {
-                        o1[k] = i + 1;
-                        o2[k] = j + 1;
-                        olv[k] = lv;
+                    const unsigned long long kk = atomicAdd(count, 1ull);
+                    if ((long long)kk < cap) {
+                        o1[kk] = i + 1;
+                        o2[kk] = j + 1;
+                        olv[kk] = lv;
                     }
                 }
             }
         }
-        __syncthreads();
     }
 }
 
@@ -231,35 +234,34 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
 // comes within a pl's radius, renc = radius).  Item (system, first tp in sorted order q0,
 // tp count nr): the tp receivers against every pl tile of the system that is not apart
 // from them (the bound argument of the file comment holds for both tests: same closest-
-// approach expression).  Pairs are written with global 1-based indices (pl, tp).
+// approach expression), each warp of 32 tp skipping the 32-body pl sub-tiles that are apart
+// from it, as in k_encounter_sorted.  Pairs are written with global 1-based indices (pl, tp).
 template <bool DISCARD>
 __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ items, const int32_t *__restrict__ poff,
                                                     const int32_t *__restrict__ npl, const int32_t *__restrict__ ptbase,
                                                     const int32_t *__restrict__ pperm, const float4 *__restrict__ PA,
                                                     const float4 *__restrict__ PB, const float4 *__restrict__ PV,
-                                                    const float4 *__restrict__ pbounds, const double *__restrict__ rp,
+                                                    const float4 *__restrict__ psub, const double *__restrict__ rp,
                                                     const double *__restrict__ vp, const double *__restrict__ rencp,
                                                     const int32_t *__restrict__ toff,
                                                     const int32_t *__restrict__ ttbase,
                                                     const int32_t *__restrict__ tperm, const float4 *__restrict__ TA,
                                                     const float4 *__restrict__ TB, const float4 *__restrict__ TV,
-                                                    const float4 *__restrict__ tbounds, const double *__restrict__ rt,
+                                                    const float4 *__restrict__ tsub, const double *__restrict__ rt,
                                                     const double *__restrict__ vt,
                                                     const int32_t *__restrict__ tstatus, double dt, long long cap,
                                                     int32_t *__restrict__ o1, int32_t *__restrict__ o2,
                                                     int32_t *__restrict__ olv, unsigned long long *__restrict__ count,
                                                     int32_t *__restrict__ flag) {
-    __shared__ float4 sa[SB], sb[SB], sv[SB];
-    __shared__ int32_t sg[SB];
+    __shared__ WarpStage st_all[SQ / 32];
     const int4 w = items[blockIdx.x];
     const int s = w.x, q0 = w.y, nr = w.z;
+    const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (32 * wq >= nr) return;  // no tp in this warp
+    WarpStage &st = st_all[wq];
     const int po = poff[s], n1 = npl[s], to = toff[s];
-    const int qt = ttbase[s] + q0 / SB;
-    float4 Q = tbounds[qt];
-    if (nr > SB) {
-        const float4 Q2 = tbounds[qt + 1];
-        Q = make_float4(fminf(Q.x, Q2.x), fmaxf(Q.y, Q2.y), fmaxf(Q.z, Q2.z), 0.f);
-    }
+    const float4 *SP = psub + (SB / 32) * (size_t)ptbase[s];
+    const float4 QW = tsub[(SB / 32) * (size_t)ttbase[s] + q0 / 32 + wq];
     bool active = (int)threadIdx.x < nr;
     BodyF me;
     int gq = 0;
@@ -271,25 +273,31 @@ __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ ite
         if (DISCARD) active = tstatus[gq] == ST_ACTIVE;
     }
     const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);
-    for (int p0 = 0; p0 < n1; p0 += SB) {
-        if (tiles_apart(pbounds[ptbase[s] + p0 / SB], Q)) continue;  // block-uniform
-        if (threadIdx.x < SB && p0 + (int)threadIdx.x < n1) {
-            const int pp = po + p0 + threadIdx.x;
-            sa[threadIdx.x] = PA[pp];
-            sb[threadIdx.x] = PB[pp];
-            sv[threadIdx.x] = PV[pp];
-            sg[threadIdx.x] = pperm[pp];
-        }
-        __syncthreads();
-        if (active) {
-            const int nt = min(SB, n1 - p0);
+    const int nsub = (n1 + 31) / 32;
+    for (int u0 = 0; u0 < nsub; u0 += 32) {
+        const bool keep = u0 + lane < nsub && !tiles_apart(SP[u0 + lane], QW);
+        unsigned m = __ballot_sync(0xffffffffu, keep);
+        while (m) {
+            const int p0 = 32 * (u0 + __ffs(m) - 1);
+            m &= m - 1;
+            __syncwarp();  // the previous sub-tile is consumed
+            if (p0 + lane < n1) {
+                const int pp = po + p0 + lane;
+                st.a[lane] = PA[pp];
+                st.b[lane] = PB[pp];
+                st.v[lane] = PV[pp];
+                st.g[lane] = pperm[pp];
+            }
+            __syncwarp();
+            if (!active) continue;
+            const int nt = min(32, n1 - p0);
             for (int ii = 0; ii < nt; ii++) {
                 BodyF other;
-                other.a = sa[ii];
-                other.b = sb[ii];
-                other.v = sv[ii];
+                other.a = st.a[ii];
+                other.b = st.b[ii];
+                other.v = st.v[ii];
                 if (prefilter_reject(other, me, dtf)) continue;
-                const int i = sg[ii];  // pl (global index)
+                const int i = st.g[ii];  // pl (global index)
                 const double xr = rt[3 * (size_t)gq + 0] - rp[3 * (size_t)i + 0];
                 const double yr = rt[3 * (size_t)gq + 1] - rp[3 * (size_t)i + 1];
                 const double zr = rt[3 * (size_t)gq + 2] - rp[3 * (size_t)i + 2];
@@ -303,16 +311,15 @@ __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ ite
                 int lenc, lv;
                 d_encounter_one(xr, yr, zr, vxr, vyr, vzr, rencp[i] + 0.0, dt, lenc, lv);
                 if (lenc) {
-                    const unsigned long long k = atomicAdd(count, 1ull);
-                    if ((long long)k < cap) {
-                        o1[k] = i + 1;
-                        o2[k] = gq + 1;
-                        olv[k] = lv;
+                    const unsigned long long kk = atomicAdd(count, 1ull);
+                    if ((long long)kk < cap) {
+                        o1[kk] = i + 1;
+                        o2[kk] = gq + 1;
+                        olv[kk] = lv;
                     }
                 }
             }
         }
-        __syncthreads();
     }
 }
 
@@ -350,9 +357,9 @@ int pltp_sorted_batched(swg_ctx *c, bool discard, const SortedSet &pl, const Sor
                         int32_t *olv, unsigned long long *count, int32_t *flag) {
     if (nitems <= 0 || pl.ntiles <= 0) return SWG_OK;
 #define SWG_PLTP_ARGS                                                                                                 \
-    items, pl.off, pl.n, pl.tbase, pl.perm, pl.F, pl.F + pl.N, pl.F + 2 * pl.N, pl.bounds, pl.r, pl.v, pl.renc,      \
-        tp.off, tp.tbase, tp.perm, tp.F, tp.F + tp.N, tp.F + 2 * tp.N, tp.bounds, tp.r, tp.v, tstatus, dt, cap, o1, o2, \
-        olv, count, flag
+    items, pl.off, pl.n, pl.tbase, pl.perm, pl.F, pl.F + pl.N, pl.F + 2 * pl.N, pl.bounds, pl.r, pl.v,    \
+        pl.renc, tp.off, tp.tbase, tp.perm, tp.F, tp.F + tp.N, tp.F + 2 * tp.N, tp.bounds, tp.r, tp.v,      \
+        tstatus, dt, cap, o1, o2, olv, count, flag
     if (discard)
         k_pltp_sorted<true><<<nitems, SQ, 0, c->stream>>>(SWG_PLTP_ARGS);
     else
@@ -386,8 +393,8 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
                                                 bounds);
     c->launches++;
     SWG_TRY(launch_status(c, "sorted_prep"));
-    k_encounter_sorted<<<nitems, SQ, 0, c->stream>>>(items, poff, tbase, perm, F, F + NPL, F + 2 * NPL, bounds, r, v,
-                                                     renc, dt, cap, o1, o2, olv, count);
+    k_encounter_sorted<<<nitems, SQ, 0, c->stream>>>(items, poff, tbase, perm, F, F + NPL, F + 2 * NPL, bounds, r,
+                                                     v, renc, dt, cap, o1, o2, olv, count);
     c->launches++;
     return launch_status(c, "encounter_sorted");
 }

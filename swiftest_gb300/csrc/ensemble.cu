@@ -584,7 +584,7 @@ int build_items(swg_ensemble *e) {
         SWG_TRY(upload(e->c, e->ttiles, tt));
         SWG_TRY(dalloc(e->c, &e->ttbase, tb.size()));
         SWG_TRY(upload(e->c, e->ttbase, tb));
-        SWG_TRY(dalloc(e->c, &e->tbounds, tt.size()));
+        SWG_TRY(dalloc(e->c, &e->tbounds, 2 * tt.size()));  // bounds of each tile's two 32-body halves
     }
     // radius-sorted pl-pl check: receiver tiles in system order (their cost depends on
     // the geometry), bound tiles of every system
@@ -602,7 +602,7 @@ int build_items(swg_ensemble *e) {
     SWG_TRY(upload(e->c, e->tiles, tiles));
     SWG_TRY(dalloc(e->c, &e->tbase, tbase.size()));
     SWG_TRY(upload(e->c, e->tbase, tbase));
-    SWG_TRY(dalloc(e->c, &e->bounds, tiles.size()));
+    SWG_TRY(dalloc(e->c, &e->bounds, 2 * tiles.size()));  // bounds of each tile's two 32-body halves
     std::vector<int4> chunks;
     std::vector<int2> sys_chunks(S);
     for (int s = 0; s < S; s++) {

@@ -300,7 +300,8 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
 // radius-sorted checks: offsets and counts, positions, velocities, encounter radii (nullptr:
 // zero), the order perm, float copies F (3 * N float4, sorted order), bound tiles
 // (ENC_BOUND_TILE bodies: tiles[k] = (system, first sorted position), tbase[s] = the
-// system's first tile) and their bounds; nmax = the largest system.
+// system's first tile) and the bounds of their 32-body halves (bounds[2 k + u], half u of
+// tile k); nmax = the largest system.
 struct SortedSet {
     const int32_t *off = nullptr, *n = nullptr;
     const double *r = nullptr, *v = nullptr, *renc = nullptr;
