@@ -74,7 +74,7 @@ MARKS = {
     10: ("recursion finished (pauses resolved)", "main"),
     11: ("listed closing items", "main"),
     12: ("closing sums joined", "main"),
-    13: ("closing kick applied", "main"),
+    13: ("closing kick, linear drift, vb2vh", "main"),
     14: ("step end", "main"),
     20: ("step start", "main"),
     21: ("level-0 checks + lists", "main"),
@@ -139,8 +139,8 @@ def _patch_ensemble(s: str) -> str:
         "            SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,\n"
         "                                          e->sym_ppart, e->ah, 1, e->lany, 1));\n"
         "            swg_tr(c->stream, 12);\n")
-    rep("        SWG_TRY(kick_vb_pl(e, dth, 0, true));\n    } else {",
-        "        SWG_TRY(kick_vb_pl(e, dth, 0, true));\n        swg_tr(c->stream, 13);\n    } else {")
+    rep("        SWG_TRY(close_pl(e, dth, true));\n    } else {",
+        "        SWG_TRY(close_pl(e, dth, true));\n        swg_tr(c->stream, 13);\n    } else {")
     rep("    k_ens_finish<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, symba ? e->lany : nullptr, e->lfirst,\n"
         "                                                                 e->enc_steps);\n"
         "    return L(c, \"ens_finish\");",

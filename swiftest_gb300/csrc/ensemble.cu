@@ -128,6 +128,7 @@ struct swg_ensemble {
     unsigned long long *ndiscard = nullptr;  // tp removed by the scan
     DevBuf rec_scratch, rows;
     DevBuf pair_terms;  // pl-pl pool: six pair terms and a kept flag per entry
+    DevBuf close_part;  // mixed path: six per-chunk sums of the closing half-step (close_pl)
     // WHM: per-body eta / muj (whm_util_set_mu_eta_pl), Jacobi coordinates, ir3 terms, drift
     // flags, the per-system ah0 of the tp kick, first-step flag (host: all systems start together)
     double *eta = nullptr, *muj = nullptr, *xj = nullptr, *vj = nullptr, *ir3h = nullptr, *ir3j = nullptr,
@@ -864,8 +865,9 @@ int on_stream(swg_ctx *c, cudaStream_t st, F f) {
 }
 
 // helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76).
-// have_acc: the accelerations are already in ah (see ens_step).
-int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false) {
+// have_acc: the accelerations are already in ah (see ens_step); update: apply vb += ah dt
+// here (close_pl applies the closing kick inside its sums instead).
+int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false, bool update = true) {
     swg_ctx *c = e->c;
     if (e->NPL == 0) return SWG_OK;
     if (!have_acc) {
@@ -883,6 +885,7 @@ int kick_vb_pl(swg_ensemble *e, double dt, int lbeg, bool have_acc = false) {
             e->nsys, e->seg_pp, e->pp_l, e->pp_cap, t, ok, e->ah);
         SWG_TRY(L(c, "ens_kick_pairs"));
     }
+    if (!update) return SWG_OK;
     k_kick_update<<<grid_for(e->NPL, 128), 128, 0, c->stream>>>((int)e->NPL, e->vb, e->ah, e->lmask, dt, e->rh,
                                                                  lbeg ? e->rbeg : e->rend);
     return L(c, "kick_update_pl");
@@ -960,6 +963,113 @@ int vb2vh_pl(swg_ensemble *e) {
                                                   exact(e));
     return L(e->c, "ens_vb2vh");
 }
+// The mixed path's closing pl half-step in two passes over the chunks (close_pl): the
+// closing velocity kick (k_kick_update's operation, with the copy of rh to rcopy for the
+// test particles' closing kick) and, on the kicked velocities, both per-chunk sums of the
+// step's end: sum(Gm vb) over lmask (helio_drift_linear_pl) and over status /= INACTIVE
+// (swiftest_util_coord_vb2vh_pl), each formed exactly as k_chunk_sums forms it (the same
+// thread per body, the same shuffles and warp order); then both results applied as
+// k_chunk_apply applies them.  vb is not changed by the linear drift, so the vb2vh sum can
+// be taken in the same pass: the same bits as the three separate steps.
+__global__ void __launch_bounds__(CHUNK_T) k_chunk_close_sums(const int4 *__restrict__ chunks,
+                                                             const double *__restrict__ Gm, double *v,
+                                                             const double *__restrict__ a,
+                                                             const int32_t *__restrict__ lmask,
+                                                             const int32_t *__restrict__ status, double dt,
+                                                             const double *__restrict__ r, double *rcopy,
+                                                             double *__restrict__ out) {
+    const int c = blockIdx.x;
+    const int4 ch = chunks[c];
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
+        const int i = ch.y + k;
+        if (rcopy)
+            for (int d = 0; d < 3; d++) rcopy[3 * i + d] = r[3 * i + d];
+        const bool lm = lmask[i] != 0;
+        if (lm)
+            for (int d = 0; d < 3; d++) v[3 * i + d] = v[3 * i + d] + a[3 * i + d] * dt;
+        const double g = Gm[i];
+        if (lm)
+            for (int d = 0; d < 3; d++) s[d] = fma(g, v[3 * i + d], s[d]);
+        if (status[i] != ST_INACTIVE)
+            for (int d = 0; d < 3; d++) s[3 + d] = fma(g, v[3 * i + d], s[3 + d]);
+    }
+    __shared__ double sh[CHUNK_T / 32][6];
+    for (int off = 16; off > 0; off >>= 1)
+        for (int q = 0; q < 6; q++) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 6; q++) sh[threadIdx.x >> 5][q] = s[q];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (int w = 0; w < CHUNK_T / 32; w++) t += sh[w][threadIdx.x];
+        out[6 * c + threadIdx.x] = t;
+    }
+}
+__global__ void __launch_bounds__(CHUNK_T) k_chunk_close_apply(const int4 *__restrict__ chunks,
+                                                              const int2 *__restrict__ sys_chunks,
+                                                              const double *__restrict__ part,
+                                                              const double *__restrict__ GMcb,
+                                                              const int32_t *__restrict__ lmask,
+                                                              const double *__restrict__ vb, double *vh, double *rh,
+                                                              double dt, double *dcb, int slot) {
+    const int c = blockIdx.x;
+    const int4 ch = chunks[c];
+    const int s = ch.x;
+    __shared__ double tot[6];
+    if (threadIdx.x < 6) {
+        const int2 rg = sys_chunks[s];
+        double t = 0.0;
+        for (int q = rg.x; q < rg.x + rg.y; q++) t += part[6 * q + threadIdx.x];
+        tot[threadIdx.x] = t;
+    }
+    __syncthreads();
+    const double fl = 1.0 / GMcb[s], fv = -1.0 / GMcb[s];
+    const double px = tot[0] * fl, py = tot[1] * fl, pz = tot[2] * fl;
+    const double cx = tot[3] * fv, cy = tot[4] * fv, cz = tot[5] * fv;
+    if (ch.w == 0 && threadIdx.x == 0) {
+        double *d = dcb + CB_N * s;
+        d[slot + 0] = px;
+        d[slot + 1] = py;
+        d[slot + 2] = pz;
+        d[CB_VB + 0] = cx;
+        d[CB_VB + 1] = cy;
+        d[CB_VB + 2] = cz;
+    }
+    for (int k = threadIdx.x; k < ch.z; k += CHUNK_T) {
+        const int i = ch.y + k;
+        if (lmask[i]) {
+            rh[3 * i + 0] = fma(px, dt, rh[3 * i + 0]);
+            rh[3 * i + 1] = fma(py, dt, rh[3 * i + 1]);
+            rh[3 * i + 2] = fma(pz, dt, rh[3 * i + 2]);
+        }
+        vh[3 * i + 0] = vb[3 * i + 0] - cx;
+        vh[3 * i + 1] = vb[3 * i + 1] - cy;
+        vh[3 * i + 2] = vb[3 * i + 2] - cz;
+    }
+}
+
+// The closing pl half of a step: kick_vb_pl (closing), lindrift_pl (CB_PTEND), vb2vh_pl.
+// The mixed path runs the velocity update and both sums as k_chunk_close_sums /
+// k_chunk_close_apply (same bits, two launches instead of five).
+int close_pl(swg_ensemble *e, double dth, bool have_acc = false) {
+    swg_ctx *c = e->c;
+    if (exact(e) || e->NPL == 0 || e->nchunks == 0) {
+        SWG_TRY(kick_vb_pl(e, dth, 0, have_acc));
+        SWG_TRY(lindrift_pl(e, dth, CB_PTEND));
+        return vb2vh_pl(e);
+    }
+    SWG_TRY(kick_vb_pl(e, dth, 0, have_acc, false));
+    SWG_TRY(ensure(c, e->close_part, sizeof(double) * 6 * (size_t)e->nchunks));
+    double *part = (double *)e->close_part.ptr;
+    k_chunk_close_sums<<<e->nchunks, CHUNK_T, 0, c->stream>>>(e->chunks, e->Gmass, e->vb, e->ah, e->lmask, e->status,
+                                                              dth, e->rh, e->NTP > 0 ? e->rend : nullptr, part);
+    SWG_TRY(L(c, "chunk_close_sums"));
+    k_chunk_close_apply<<<e->nchunks, CHUNK_T, 0, c->stream>>>(e->chunks, e->sys_chunks, part, e->GMcb, e->lmask,
+                                                               e->vb, e->vh, e->rh, dth, e->dcb, CB_PTEND);
+    return L(c, "chunk_close_apply");
+}
+
 // Danby drift of every body at level -1 (SyMBA: bodies outside encounters) with its
 // own system's GMcb; HELIO drifts every active body.
 int drift_bodies(swg_ensemble *e, double dt, bool pl = true, bool tp = true) {
@@ -1449,9 +1559,7 @@ int helio_step_groups(swg_ensemble *e, double dt) {
     }));
     SWG_TRY(drift_bodies(e, dt, true, false));
     e->kend = true;
-    int rc = kick_vb_pl(e, dth, 0);
-    if (rc == SWG_OK) rc = lindrift_pl(e, dth, CB_PTEND);
-    if (rc == SWG_OK) rc = vb2vh_pl(e);
+    int rc = close_pl(e, dth);
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventRecord(e->ev_drift, c->stream), "pl done");
     if (rc == SWG_OK) rc = cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_drift, 0), "pl done");
     if (rc == SWG_OK) rc = cuda_status(c, cudaStreamWaitEvent(e->side2, e->ev_drift, 0), "pl done");
@@ -1490,9 +1598,7 @@ int helio_step_split(swg_ensemble *e, double dt) {
     }));
     SWG_TRY(drift_bodies(e, dt, true, false));
     e->kend = true;
-    int rc = kick_vb_pl(e, dth, 0);
-    if (rc == SWG_OK) rc = lindrift_pl(e, dth, CB_PTEND);
-    if (rc == SWG_OK) rc = vb2vh_pl(e);
+    int rc = close_pl(e, dth);
     if (rc == SWG_OK) rc = cuda_status(c, cudaEventRecord(e->ev_drift, c->stream), "pl done");
     if (rc == SWG_OK) rc = cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_drift, 0), "pl done");
     if (rc == SWG_OK) rc = on_stream(c, e->side, [&] {
@@ -1627,7 +1733,7 @@ int ens_step(swg_ensemble *e, double dt) {
             SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
         }
-        SWG_TRY(kick_vb_pl(e, dth, 0, true));
+        SWG_TRY(close_pl(e, dth, true));
     } else {
         SWG_TRY(drift_bodies(e, dt));
         if (rec) {
@@ -1635,10 +1741,8 @@ int ens_step(swg_ensemble *e, double dt) {
             SWG_TRY(recursion_launch(e, dt));
             SWG_TRY(recursion_finish(e));
         }
-        SWG_TRY(kick_vb_pl(e, dth, 0));
+        SWG_TRY(close_pl(e, dth));
     }
-    SWG_TRY(lindrift_pl(e, dth, CB_PTEND));
-    SWG_TRY(vb2vh_pl(e));
     SWG_TRY(kick_vb_tp(e, dth, 0));
     SWG_TRY(tp_misc(e, CB_PTEND, dth, 3, -1));
     k_ens_finish<<<grid_for(e->nsys, 128), 128, 0, c->stream>>>(e->nsys, symba ? e->lany : nullptr, e->lfirst,
@@ -1932,7 +2036,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->ext_pp, e->ext_pt, e->sas.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
+                    e->enc_pt.counters.ptr, e->ext_pp, e->ext_pt, e->sas.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->close_part.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
