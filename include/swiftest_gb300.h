@@ -248,7 +248,8 @@ int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
  * accelerations; the symmetric kernel adds the same terms in another order.  Variants
  * 0 .. SWG_KICK_NVARIANT-1 force that broadcast shape on both kinds.  kick_variant reads
  * the kernel in use for kind 0 (pl-pl) or 1 (pl-tp), -1 before the first mixed kick of
- * that kind, and with kind 2 the symmetric kick's strip length. */
+ * that kind, with kind 2 the symmetric kick's strip length and with kind 3 its warps per
+ * block. */
 #define SWG_KICK_NVARIANT 5
 #define SWG_KICK_SYMMETRIC 5
 int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
@@ -261,6 +262,13 @@ int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
  * 1, 2, 4, 8 or 16 forces it.  swg_ensemble_kick_variant with kind 2 reads the strip in use (-1 before the first
  * mixed kick). */
 int swg_ensemble_set_kick_strip(swg_ensemble *ens, int strip);
+/* Warps per block of the symmetric pl-pl kick (no counterpart in the reference).  Every warp
+ * is an independent worker of the persistent grid, so 1, 2 and 4 give the same bits; by
+ * default (0) the autotuner times the three at the chosen strip and keeps one warp unless
+ * another count is more than 3% faster (cached with the strip).  1, 2 or 4 forces it;
+ * swg_ensemble_kick_variant with kind 3 reads the count in use (-1 before the first mixed
+ * kick). */
+int swg_ensemble_set_kick_warps(swg_ensemble *ens, int warps);
 /* swiftest_kick_getacch_int_all_tri_pl (swiftest_kick.f90:183-264) of every system from its
  * current positions, in the ensemble's precision and pair rule (radius guard for SyMBA or
  * with close-encounter checks): acc[3*NPL] on the host, zero-based sums over all pairs. */

@@ -465,6 +465,17 @@ class Ensemble:
         self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, 2, C.byref(v)))
         return int(v.value)
 
+    def set_kick_warps(self, warps: int = 0):
+        """Force the symmetric pl-pl kick's warps per block (1, 2 or 4; the same bits for
+        each), or let the autotuner choose it (0)."""
+        self.ctx.check("swg_ensemble_set_kick_warps", self.ctx.lib.swg_ensemble_set_kick_warps(self.h, int(warps)))
+
+    def kick_warps(self) -> int:
+        """Warps per block of the symmetric pl-pl kick in use (-1 before the first mixed kick)."""
+        v = C.c_int(-1)
+        self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, 3, C.byref(v)))
+        return int(v.value)
+
     def getacch_int_pl(self):
         """Pair accelerations of every system's massive bodies from the current positions."""
         out = np.zeros((int(self.poff[-1]), 3))

@@ -113,8 +113,9 @@ struct swg_ensemble {
     int force_variant = -1;
     // symmetric pl-pl mixed kick (the default): tile-pair items, each system's first slot, slot sums
     int4 *it_sym = nullptr;
-    int n_sym = 0, sym_strip = 1;
+    int n_sym = 0, sym_strip = 1, sym_warps = 1;
     int force_strip = 0;  // > 0: strip length of the symmetric kick forced (0: tuned)
+    int force_warps = 0;  // > 0: warps per block of the symmetric kick forced (0: tuned)
     int32_t *sym_base = nullptr;
     float *sym_part = nullptr, *sym_ppart = nullptr;  // receiver slots, then pair slots (one allocation)
     unsigned *head = nullptr;
@@ -731,29 +732,33 @@ int build_sym_plan(swg_ensemble *e, int strip) {
 constexpr int SYM_STRIPS[] = {1, 2, 4, 8, 16};
 constexpr int SYM_NSTRIP = 5;
 
-// Times the symmetric kick (pair kernel and per-body sums into scratch accelerations) for
-// every candidate strip on this ensemble's current data: one warm-up, then the shortest of
-// five launches timed one by one.  The strip of kick_sym_strip stays unless another is
-// faster by more than 3%, so that timing noise does not move the choice between
-// near-equal strips; the partners must be split into kA/kB.
-int time_sym_strips(swg_ensemble *e, bool rad, unsigned *head, int *best) {
+// Warps per block the autotuner tries for the symmetric kick (each warp is an independent
+// worker, so every count gives the same bits).
+constexpr int SYM_WARPS[] = {1, 2, 4};
+constexpr int SYM_NWARPS = 3;
+
+// Times the symmetric kick (pair kernel and per-body sums into scratch accelerations) on
+// this ensemble's current data: first every candidate strip with one warp per block, then,
+// at the chosen strip, every candidate block size; each candidate one warm-up, then the
+// shortest of five launches timed one by one.  The default (kick_sym_strip's strip, one
+// warp) stays unless another candidate is faster by more than 3%, so that timing noise
+// does not move the choice between near-equal candidates; the partners must be split into
+// kA/kB.
+int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_strip, int *best_warps) {
     swg_ctx *c = e->c;
     TuneScratch t;
     SWG_TRY(dalloc(c, &t.acc, 3 * (size_t)e->NPL));
     for (cudaEvent_t &x : t.ev) SWG_TRY(cuda_status(c, cudaEventCreate(&x), "event"));
     const float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
-    const int deflt = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms);
-    float ms_strip[SYM_NSTRIP], best_ms = 0.f, deflt_ms = 0.f;
-    for (int q = 0; q < SYM_NSTRIP; q++) {
-        SWG_TRY(build_sym_plan(e, SYM_STRIPS[q]));
+    auto timed = [&](int warps, float *out) -> int {
         auto once = [&]() -> int {
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
-                                           e->sym_part, e->sym_ppart, head));
+                                           e->sym_part, e->sym_ppart, head, nullptr, 0, nullptr, 0, warps));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
                                          e->sym_ppart, t.acc, 1, nullptr, 0);
         };
         SWG_TRY(once());
-        ms_strip[q] = 3.0e38f;
+        *out = 3.0e38f;
         for (int rep = 0; rep < 5; rep++) {
             SWG_TRY(cuda_status(c, cudaEventRecord(t.ev[0], c->stream), "event"));
             SWG_TRY(once());
@@ -761,17 +766,35 @@ int time_sym_strips(swg_ensemble *e, bool rad, unsigned *head, int *best) {
             SWG_TRY(cuda_status(c, cudaEventSynchronize(t.ev[1]), "event"));
             float ms = 0.f;
             SWG_TRY(cuda_status(c, cudaEventElapsedTime(&ms, t.ev[0], t.ev[1]), "event"));
-            ms_strip[q] = std::min(ms_strip[q], ms);
+            *out = std::min(*out, ms);
         }
+        return SWG_OK;
+    };
+    const int deflt = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms);
+    float ms_strip[SYM_NSTRIP], deflt_ms = 0.f;
+    for (int q = 0; q < SYM_NSTRIP; q++) {
+        SWG_TRY(build_sym_plan(e, SYM_STRIPS[q]));
+        SWG_TRY(timed(1, &ms_strip[q]));
         if (SYM_STRIPS[q] == deflt) deflt_ms = ms_strip[q];
     }
-    *best = deflt;
-    best_ms = deflt_ms;
+    *best_strip = deflt;
+    float best_ms = deflt_ms;
     for (int q = 0; q < SYM_NSTRIP; q++)
         if (ms_strip[q] < 0.97f * deflt_ms && ms_strip[q] < best_ms) {
             best_ms = ms_strip[q];
-            *best = SYM_STRIPS[q];
+            *best_strip = SYM_STRIPS[q];
         }
+    SWG_TRY(build_sym_plan(e, *best_strip));
+    *best_warps = 1;
+    const float one_ms = best_ms;
+    for (int q = 1; q < SYM_NWARPS; q++) {
+        float ms = 0.f;
+        SWG_TRY(timed(SYM_WARPS[q], &ms));
+        if (ms < 0.97f * one_ms && ms < best_ms) {
+            best_ms = ms;
+            *best_warps = SYM_WARPS[q];
+        }
+    }
     return SWG_OK;
 }
 
@@ -790,22 +813,28 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
         return SWG_ERR_STATE;
     }
     int v = e->force_variant;
-    if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel, its strip forced, cached or timed here
+    if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel, its strip and block size forced, cached or timed here
         if (!e->it_sym) {
-            int strip = e->force_strip;
-            if (strip <= 0) {
-                const std::string key = tune_key(c->device, rad ? "kick_sym_rad" : "kick_sym", size_bucket(e, 0));
-                const int l = tune_lookup(key);  // cached as log2(strip)
-                if (l >= 0 && l < SYM_NSTRIP) {
-                    strip = 1 << l;
+            int strip = e->force_strip, warps = e->force_warps;
+            if (strip <= 0 || warps <= 0) {
+                const std::string key = tune_key(c->device, rad ? "kick_sym2_rad" : "kick_sym2", size_bucket(e, 0));
+                const int l = tune_lookup(key);  // cached as log2(strip) + 8 log2(warps)
+                int ts = 0, tw = 0;
+                if (l >= 0 && (l & 7) < SYM_NSTRIP && (l >> 3) < SYM_NWARPS) {
+                    ts = 1 << (l & 7);
+                    tw = 1 << (l >> 3);
                 } else {
-                    SWG_TRY(time_sym_strips(e, rad, head, &strip));
-                    int lg = 0;
-                    while ((1 << lg) < strip) lg++;
-                    tune_store(key, lg);
+                    SWG_TRY(time_sym_plan(e, rad, head, &ts, &tw));
+                    int ls = 0, lw = 0;
+                    while ((1 << ls) < ts) ls++;
+                    while ((1 << lw) < tw) lw++;
+                    tune_store(key, ls + 8 * lw);
                 }
+                if (strip <= 0) strip = ts;
+                if (warps <= 0) warps = tw;
             }
             SWG_TRY(build_sym_plan(e, strip));
+            e->sym_warps = warps;
         }
         e->kv[0] = KICK_SYMMETRIC;
         return SWG_OK;
@@ -844,7 +873,7 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
         if (e->kv[0] == KICK_SYMMETRIC) {
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
-                                           e->sym_part, e->sym_ppart, head, flag, phase));
+                                           e->sym_part, e->sym_ppart, head, flag, phase, nullptr, 0, e->sym_warps));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
                                          e->sym_ppart, e->ah, acc_is_zero, flag, phase);
         }
@@ -1705,7 +1734,8 @@ int ens_step(swg_ensemble *e, double dt) {
                                           e->enc_body, 0));
                 SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_split, c->stream), "split"));
                 SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA,
-                                               e->kB, e->sym_part, e->sym_ppart, e->head2, nullptr, 0, iflag, 3u));
+                                               e->kB, e->sym_part, e->sym_ppart, e->head2, nullptr, 0, iflag, 3u,
+                                               e->sym_warps));
                 return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base,
                                              e->sym_part, e->sym_ppart, e->ah, 1, e->lany, 0);
             }));
@@ -1725,7 +1755,7 @@ int ens_step(swg_ensemble *e, double dt) {
             SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, e->radius, e->kA, e->kB, nullptr, nullptr, 0,
                                       e->enc_body, 1));
             SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
-                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u));
+                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u, e->sym_warps));
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
             SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
                                           e->sym_ppart, e->ah, 1, e->lany, 1));
@@ -2391,9 +2421,11 @@ int swg_ensemble_set_kick_variant(swg_ensemble *e, int variant) {
 }
 
 int swg_ensemble_kick_variant(swg_ensemble *e, int kind, int *variant) {
-    if (!e || !variant || kind < 0 || kind > 2) return SWG_ERR_ARG;
+    if (!e || !variant || kind < 0 || kind > 3) return SWG_ERR_ARG;
     if (kind == 2)
         *variant = e->it_sym ? e->sym_strip : -1;
+    else if (kind == 3)
+        *variant = e->it_sym ? e->sym_warps : -1;
     else
         *variant = e->kv[kind];
     return SWG_OK;
@@ -2404,6 +2436,17 @@ int swg_ensemble_set_kick_strip(swg_ensemble *e, int strip) {
         return SWG_ERR_ARG;
     SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick strip"));
     e->force_strip = strip;
+    if (e->it_sym) cudaFree(e->it_sym);
+    e->it_sym = nullptr;
+    e->n_sym = 0;
+    reset_kick_plans(e);
+    return SWG_OK;
+}
+
+int swg_ensemble_set_kick_warps(swg_ensemble *e, int warps) {
+    if (!e || !(warps == 0 || warps == 1 || warps == 2 || warps == 4)) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick warps"));
+    e->force_warps = warps;
     if (e->it_sym) cudaFree(e->it_sym);
     e->it_sym = nullptr;
     e->n_sym = 0;

@@ -277,8 +277,10 @@ __device__ __forceinline__ void diag_subtile(const SubTile (&sP)[SR], const Recv
 // Item: (system, tile I, first tile J0 | tiles nJ << 24, receiver slot).  pA/pB: every
 // body split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R).  A receiver slot is
 // [x_hi, x_lo, y_hi, y_lo, z_hi, z_lo] x TS floats, a pair slot [x, y, z] x TS floats.
-template <bool RAD>
-__global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *__restrict__ items,
+// W warps per block, each an independent worker with its own staged tile (the block size
+// only changes how the warps are packed on the SMs; every item's arithmetic is the same).
+template <bool RAD, int W>
+__global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int4 *__restrict__ items,
                                                       const int32_t *__restrict__ poff,
                                                       const int32_t *__restrict__ npl,
                                                       const int32_t *__restrict__ sbase,
@@ -287,8 +289,9 @@ __global__ void __launch_bounds__(32) k_kick_mixed_sym(int nitems, const int4 *_
                                                       unsigned *__restrict__ head,
                                                       const int32_t *__restrict__ sys_flag, int phase,
                                                       const uint8_t *__restrict__ iflag, unsigned accept) {
-    __shared__ SubTile sP[SR];
-    const int lane = threadIdx.x;
+    __shared__ SubTile sPw[W][SR];
+    SubTile(&sP)[SR] = sPw[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
     const float4 pad_a = make_float4(PAD_POS, PAD_POS, PAD_POS, 0.f), zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (;;) {
         unsigned it = 0;
@@ -483,28 +486,40 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<
     return nrs;
 }
 
-int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
-                           const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
-                           float *ppart, unsigned *head, const int32_t *sys_flag, int phase, const uint8_t *iflag,
-                           unsigned accept) {
-    if (nitems <= 0) return SWG_OK;
-    SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
-    static int occ[2] = {0, 0};  // resident blocks per SM, queried once per variant
-    int &o = occ[rad ? 1 : 0];
+template <bool RAD, int W>
+int sym_launch(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
+               const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart, float *ppart, unsigned *head,
+               const int32_t *sys_flag, int phase, const uint8_t *iflag, unsigned accept) {
+    static int o = 0;  // resident blocks per SM, queried once per variant
     if (o == 0) {
         int nb = 0;
-        SWG_TRY(cuda_status(c, rad ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<true>, 32, 0)
-                                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<false>, 32, 0),
+        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<RAD, W>, 32 * W, 0),
                             "occupancy"));
         o = nb > 0 ? nb : 1;
     }
-    const int grid = std::min(nitems, o * (c->num_sms > 0 ? c->num_sms : 152));
+    const int grid = std::min((nitems + W - 1) / W, o * (c->num_sms > 0 ? c->num_sms : 152));
+    k_kick_mixed_sym<RAD, W><<<grid, 32 * W, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
+                                                              head, sys_flag, phase, iflag, accept);
+    return SWG_OK;
+}
+
+int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
+                           const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
+                           float *ppart, unsigned *head, const int32_t *sys_flag, int phase, const uint8_t *iflag,
+                           unsigned accept, int warps) {
+    if (nitems <= 0) return SWG_OK;
+    if (warps != 1 && warps != 2 && warps != 4) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
+#define SWG_SYM_ARGS c, nitems, items, poff, npl, sbase, pA, pB, rpart, ppart, head, sys_flag, phase, iflag, accept
+    int rc;
     if (rad)
-        k_kick_mixed_sym<true><<<grid, 32, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
-                                                               head, sys_flag, phase, iflag, accept);
+        rc = warps == 1 ? sym_launch<true, 1>(SWG_SYM_ARGS)
+                        : (warps == 2 ? sym_launch<true, 2>(SWG_SYM_ARGS) : sym_launch<true, 4>(SWG_SYM_ARGS));
     else
-        k_kick_mixed_sym<false><<<grid, 32, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
-                                                                head, sys_flag, phase, iflag, accept);
+        rc = warps == 1 ? sym_launch<false, 1>(SWG_SYM_ARGS)
+                        : (warps == 2 ? sym_launch<false, 2>(SWG_SYM_ARGS) : sym_launch<false, 4>(SWG_SYM_ARGS));
+#undef SWG_SYM_ARGS
+    SWG_TRY(rc);
     c->launches++;
     return launch_status(c, "kick_mixed_sym");
 }

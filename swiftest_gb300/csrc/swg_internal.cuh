@@ -202,10 +202,11 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<
 // a single system has enough tile pairs to fill the GPU (else the broadcast kernel is faster)
 bool kick_sym_single_ok(int32_t npl, int num_sms);
 // iflag/accept (optional): only items it with bit iflag[it] of accept set are processed.
+// warps: warps per block (1, 2 or 4; the same bits for each).
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
                            float *ppart, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0,
-                           const uint8_t *iflag = nullptr, unsigned accept = 0);
+                           const uint8_t *iflag = nullptr, unsigned accept = 0, int warps = 1);
 // iflag[it] of every item: 0 when its system has no encounter (sys_enc[s] == 0), else 2 when
 // one of its tiles holds a body with enc[body] != 0, else 1.
 int kick_sym_item_flags(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,

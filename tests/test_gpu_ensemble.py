@@ -280,6 +280,28 @@ def test_symmetric_kick_strips(ctx, strip):
     ens.close()
 
 
+@pytest.mark.parametrize("warps", [2, 4, 0])
+def test_symmetric_kick_warps_same_bits(ctx, warps):
+    # warps per block of the symmetric pl-pl kick (forced, and the autotuned default): every
+    # warp is an independent worker of the persistent grid, so each count gives the bits of
+    # one warp per block at the same strip
+    E = IC.make_ensemble("C4", nsys=4, scale=0.5)
+
+    def accel(w):
+        ens = Ensemble(ctx, E, precision="MIXED")
+        ens.set_kick_strip(4)
+        ens.set_kick_warps(w)
+        g = ens.getacch_int_pl()
+        used = ens.kick_warps()
+        ens.close()
+        return g, used
+
+    g1, used1 = accel(1)
+    g, used = accel(warps)
+    assert used1 == 1 and (used == warps if warps else used in (1, 2, 4))
+    assert np.array_equal(g, g1)
+
+
 def test_mixed_drift_matches_fp64_drift(ctx):
     # massless bodies feel no pair forces and move the central body not at all, so the
     # mixed and FP64 ensembles differ only in the drift: the fast FP64 solver form of the
