@@ -394,7 +394,8 @@ def run_path(ctx, wl, precision, steps, warmup, prof_steps=0, clocks=None):
     if hasattr(s, "kick_strip") and precision == "MIXED":  # ensembles: the autotuned mixed kicks
         kv = s.kick_variant()
         plan = {"plpl": "symmetric" if kv["pl"] == 5 else f"broadcast shape {kv['pl']}",
-                "plpl_strip": s.kick_strip(), "plpl_warps_per_block": s.kick_warps(), "pltp_shape": kv["tp"]}
+                "plpl_tile": s.kick_tile(), "plpl_strip": s.kick_strip(), "plpl_warps_per_block": s.kick_warps(),
+                "pltp_shape": kv["tp"]}
     s.close()
     return total_ms, launches, (prof, prof_ms), rel_energy(e0, e1), stats, plan
 

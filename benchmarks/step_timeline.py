@@ -129,15 +129,13 @@ def _patch_ensemble(s: str) -> str:
         "        SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_join, e->side), \"join\"));\n"
         "        SWG_TRY(recursion_finish(e));\n"
         "        swg_tr(c->stream, 10);\n")
-    rep("                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u));\n"
-        "            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), \"join\"));\n"
-        "            SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,\n"
-        "                                          e->sym_ppart, e->ah, 1, e->lany, 1));\n",
-        "                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u));\n"
+    rep("            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), \"join\"));\n"
+        "            SWG_TRY(kick_mixed_sym_reduce(",
         "            swg_tr(c->stream, 11);\n"
         "            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), \"join\"));\n"
-        "            SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,\n"
-        "                                          e->sym_ppart, e->ah, 1, e->lany, 1));\n"
+        "            SWG_TRY(kick_mixed_sym_reduce(")
+    rep("                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile));\n",
+        "                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile));\n"
         "            swg_tr(c->stream, 12);\n")
     rep("        SWG_TRY(close_pl(e, dth, true));\n    } else {",
         "        SWG_TRY(close_pl(e, dth, true));\n        swg_tr(c->stream, 13);\n    } else {")

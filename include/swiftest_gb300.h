@@ -248,8 +248,8 @@ int swg_ensemble_use_graphs(swg_ensemble *ens, int enable);
  * accelerations; the symmetric kernel adds the same terms in another order.  Variants
  * 0 .. SWG_KICK_NVARIANT-1 force that broadcast shape on both kinds.  kick_variant reads
  * the kernel in use for kind 0 (pl-pl) or 1 (pl-tp), -1 before the first mixed kick of
- * that kind, with kind 2 the symmetric kick's strip length and with kind 3 its warps per
- * block. */
+ * that kind, with kind 2 the symmetric kick's strip length, with kind 3 its warps per
+ * block and with kind 4 its bodies per tile. */
 #define SWG_KICK_NVARIANT 5
 #define SWG_KICK_SYMMETRIC 5
 int swg_ensemble_set_kick_variant(swg_ensemble *ens, int variant);
@@ -269,6 +269,14 @@ int swg_ensemble_set_kick_strip(swg_ensemble *ens, int strip);
  * swg_ensemble_kick_variant with kind 3 reads the count in use (-1 before the first mixed
  * kick). */
 int swg_ensemble_set_kick_warps(swg_ensemble *ens, int warps);
+/* Bodies per tile of the symmetric pl-pl kick (no counterpart in the reference): 128 (four
+ * receivers per lane) or 64 (two; one warp per block).  The tile decides how a body's sums
+ * are split into slots, so the two agree within the mixed-kick tolerance, each
+ * deterministic.  By default (0) the autotuner times both (each at its default strip) before
+ * the strip and keeps 128 unless 64 is more than 3% faster (cached with the strip);
+ * swg_ensemble_kick_variant with kind 4 reads the tile in use (-1 before the first mixed
+ * kick). */
+int swg_ensemble_set_kick_tile(swg_ensemble *ens, int tile);
 /* swiftest_kick_getacch_int_all_tri_pl (swiftest_kick.f90:183-264) of every system from its
  * current positions, in the ensemble's precision and pair rule (radius guard for SyMBA or
  * with close-encounter checks): acc[3*NPL] on the host, zero-based sums over all pairs. */

@@ -470,6 +470,17 @@ class Ensemble:
         each), or let the autotuner choose it (0)."""
         self.ctx.check("swg_ensemble_set_kick_warps", self.ctx.lib.swg_ensemble_set_kick_warps(self.h, int(warps)))
 
+    def set_kick_tile(self, tile: int = 0):
+        """Force the symmetric pl-pl kick's bodies per tile (128 or 64), or let the autotuner
+        choose it (0)."""
+        self.ctx.check("swg_ensemble_set_kick_tile", self.ctx.lib.swg_ensemble_set_kick_tile(self.h, int(tile)))
+
+    def kick_tile(self) -> int:
+        """Bodies per tile of the symmetric pl-pl kick in use (-1 before the first mixed kick)."""
+        v = C.c_int(-1)
+        self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, 4, C.byref(v)))
+        return int(v.value)
+
     def kick_warps(self) -> int:
         """Warps per block of the symmetric pl-pl kick in use (-1 before the first mixed kick)."""
         v = C.c_int(-1)

@@ -113,9 +113,10 @@ struct swg_ensemble {
     int force_variant = -1;
     // symmetric pl-pl mixed kick (the default): tile-pair items, each system's first slot, slot sums
     int4 *it_sym = nullptr;
-    int n_sym = 0, sym_strip = 1, sym_warps = 1;
+    int n_sym = 0, sym_strip = 1, sym_warps = 1, sym_tile = KICK_SYM_TILE;
     int force_strip = 0;  // > 0: strip length of the symmetric kick forced (0: tuned)
     int force_warps = 0;  // > 0: warps per block of the symmetric kick forced (0: tuned)
+    int force_tile = 0;   // > 0: bodies per tile of the symmetric kick forced (0: tuned)
     int32_t *sym_base = nullptr;
     float *sym_part = nullptr, *sym_ppart = nullptr;  // receiver slots, then pair slots (one allocation)
     unsigned *head = nullptr;
@@ -711,7 +712,7 @@ int build_sym_plan(swg_ensemble *e, int strip) {
     std::vector<int4> items;
     std::vector<int32_t> base;
     int64_t npair = 0;
-    const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), strip, items, base, &npair);
+    const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), strip, items, base, &npair, e->sym_tile);
     SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
     if (e->sym_base) cudaFree(e->sym_base);
     if (e->sym_part) cudaFree(e->sym_part);
@@ -719,8 +720,8 @@ int build_sym_plan(swg_ensemble *e, int strip) {
     e->sym_part = nullptr;
     SWG_TRY(dalloc(c, &e->sym_base, base.size()));
     SWG_TRY(upload(c, e->sym_base, base));
-    SWG_TRY(dalloc(c, &e->sym_part, (size_t)(6 * nrecv + 3 * npair) * KICK_SYM_TILE));
-    e->sym_ppart = e->sym_part + (size_t)nrecv * 6 * KICK_SYM_TILE;
+    SWG_TRY(dalloc(c, &e->sym_part, (size_t)(6 * nrecv + 3 * npair) * e->sym_tile));
+    e->sym_ppart = e->sym_part + (size_t)nrecv * 6 * e->sym_tile;
     e->sym_strip = strip;
     return SWG_OK;
 }
@@ -738,13 +739,14 @@ constexpr int SYM_WARPS[] = {1, 2, 4};
 constexpr int SYM_NWARPS = 3;
 
 // Times the symmetric kick (pair kernel and per-body sums into scratch accelerations) on
-// this ensemble's current data: first every candidate strip with one warp per block, then,
-// at the chosen strip, every candidate block size; each candidate one warm-up, then the
-// shortest of five launches timed one by one.  The default (kick_sym_strip's strip, one
-// warp) stays unless another candidate is faster by more than 3%, so that timing noise
-// does not move the choice between near-equal candidates; the partners must be split into
-// kA/kB.
-int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_strip, int *best_warps) {
+// this ensemble's current data: first the two tile sizes (128 and 64 bodies, each at its
+// default strip), then every candidate strip at the chosen tile with one warp per block,
+// then (128-body tiles) every candidate block size at the chosen strip; each candidate one
+// warm-up, then the shortest of five launches timed one by one.  The defaults (128 bodies,
+// kick_sym_strip's strip, one warp) stay unless another candidate is faster by more than
+// 3%, so that timing noise does not move the choice between near-equal candidates; the
+// partners must be split into kA/kB.
+int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int *best_strip, int *best_warps) {
     swg_ctx *c = e->c;
     TuneScratch t;
     SWG_TRY(dalloc(c, &t.acc, 3 * (size_t)e->NPL));
@@ -753,9 +755,10 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_strip, in
     auto timed = [&](int warps, float *out) -> int {
         auto once = [&]() -> int {
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
-                                           e->sym_part, e->sym_ppart, head, nullptr, 0, nullptr, 0, warps));
+                                           e->sym_part, e->sym_ppart, head, nullptr, 0, nullptr, 0, warps,
+                                           e->sym_tile));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                         e->sym_ppart, t.acc, 1, nullptr, 0);
+                                         e->sym_ppart, t.acc, 1, nullptr, 0, e->sym_tile);
         };
         SWG_TRY(once());
         *out = 3.0e38f;
@@ -770,7 +773,16 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_strip, in
         }
         return SWG_OK;
     };
-    const int deflt = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms);
+    // tile size: 128 unless 64 is more than 3% faster, each at its default strip
+    float ms_tile[2];
+    for (int q = 0; q < 2; q++) {
+        e->sym_tile = q == 0 ? KICK_SYM_TILE : 64;
+        SWG_TRY(build_sym_plan(e, kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms, e->sym_tile)));
+        SWG_TRY(timed(1, &ms_tile[q]));
+    }
+    e->sym_tile = ms_tile[1] < 0.97f * ms_tile[0] ? 64 : KICK_SYM_TILE;
+    *best_tile = e->sym_tile;
+    const int deflt = kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms, e->sym_tile);
     float ms_strip[SYM_NSTRIP], deflt_ms = 0.f;
     for (int q = 0; q < SYM_NSTRIP; q++) {
         SWG_TRY(build_sym_plan(e, SYM_STRIPS[q]));
@@ -787,7 +799,7 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_strip, in
     SWG_TRY(build_sym_plan(e, *best_strip));
     *best_warps = 1;
     const float one_ms = best_ms;
-    for (int q = 1; q < SYM_NWARPS; q++) {
+    for (int q = 1; q < SYM_NWARPS && e->sym_tile == KICK_SYM_TILE; q++) {
         float ms = 0.f;
         SWG_TRY(timed(SYM_WARPS[q], &ms));
         if (ms < 0.97f * one_ms && ms < best_ms) {
@@ -815,26 +827,29 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
     int v = e->force_variant;
     if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel, its strip and block size forced, cached or timed here
         if (!e->it_sym) {
-            int strip = e->force_strip, warps = e->force_warps;
-            if (strip <= 0 || warps <= 0) {
-                const std::string key = tune_key(c->device, rad ? "kick_sym2_rad" : "kick_sym2", size_bucket(e, 0));
-                const int l = tune_lookup(key);  // cached as log2(strip) + 8 log2(warps)
-                int ts = 0, tw = 0;
-                if (l >= 0 && (l & 7) < SYM_NSTRIP && (l >> 3) < SYM_NWARPS) {
+            int tile = e->force_tile, strip = e->force_strip, warps = e->force_warps;
+            if (tile <= 0 || strip <= 0 || warps <= 0) {
+                const std::string key = tune_key(c->device, rad ? "kick_sym3_rad" : "kick_sym3", size_bucket(e, 0));
+                const int l = tune_lookup(key);  // cached as log2(strip) + 8 log2(warps) + 64 (tile == 64)
+                int tt = 0, ts = 0, tw = 0;
+                if (l >= 0 && (l & 7) < SYM_NSTRIP && ((l >> 3) & 7) < SYM_NWARPS && (l >> 6) < 2) {
+                    tt = (l >> 6) ? 64 : KICK_SYM_TILE;
                     ts = 1 << (l & 7);
-                    tw = 1 << (l >> 3);
+                    tw = 1 << ((l >> 3) & 7);
                 } else {
-                    SWG_TRY(time_sym_plan(e, rad, head, &ts, &tw));
+                    SWG_TRY(time_sym_plan(e, rad, head, &tt, &ts, &tw));
                     int ls = 0, lw = 0;
                     while ((1 << ls) < ts) ls++;
                     while ((1 << lw) < tw) lw++;
-                    tune_store(key, ls + 8 * lw);
+                    tune_store(key, ls + 8 * lw + (tt == 64 ? 64 : 0));
                 }
+                if (tile <= 0) tile = tt;
                 if (strip <= 0) strip = ts;
                 if (warps <= 0) warps = tw;
             }
+            e->sym_tile = tile;
             SWG_TRY(build_sym_plan(e, strip));
-            e->sym_warps = warps;
+            e->sym_warps = tile == KICK_SYM_TILE ? warps : 1;
         }
         e->kv[0] = KICK_SYMMETRIC;
         return SWG_OK;
@@ -873,9 +888,10 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
         if (e->kv[0] == KICK_SYMMETRIC) {
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
-                                           e->sym_part, e->sym_ppart, head, flag, phase, nullptr, 0, e->sym_warps));
+                                           e->sym_part, e->sym_ppart, head, flag, phase, nullptr, 0, e->sym_warps,
+                                           e->sym_tile));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                         e->sym_ppart, e->ah, acc_is_zero, flag, phase);
+                                         e->sym_ppart, e->ah, acc_is_zero, flag, phase, e->sym_tile);
         }
         return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase, acc_is_zero);
     }
@@ -1717,7 +1733,7 @@ int ens_step(swg_ensemble *e, double dt) {
             SWG_TRY(L(c, "mark_enc"));
             SWG_TRY(ensure(c, e->sym_iflag, (size_t)e->n_sym));
             SWG_TRY(kick_sym_item_flags(c, e->n_sym, e->it_sym, e->poff, e->npl, e->lany, e->enc_body,
-                                        (uint8_t *)e->sym_iflag.ptr));
+                                        (uint8_t *)e->sym_iflag.ptr, e->sym_tile));
         }
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
@@ -1735,9 +1751,9 @@ int ens_step(swg_ensemble *e, double dt) {
                 SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_split, c->stream), "split"));
                 SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA,
                                                e->kB, e->sym_part, e->sym_ppart, e->head2, nullptr, 0, iflag, 3u,
-                                               e->sym_warps));
+                                               e->sym_warps, e->sym_tile));
                 return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base,
-                                             e->sym_part, e->sym_ppart, e->ah, 1, e->lany, 0);
+                                             e->sym_part, e->sym_ppart, e->ah, 1, e->lany, 0, e->sym_tile);
             }));
         } else {
             SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
@@ -1755,10 +1771,11 @@ int ens_step(swg_ensemble *e, double dt) {
             SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, e->radius, e->kA, e->kB, nullptr, nullptr, 0,
                                       e->enc_body, 1));
             SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
-                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u, e->sym_warps));
+                                           e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u, e->sym_warps,
+                                           e->sym_tile));
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
             SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                          e->sym_ppart, e->ah, 1, e->lany, 1));
+                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile));
         } else {
             SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
@@ -2421,11 +2438,13 @@ int swg_ensemble_set_kick_variant(swg_ensemble *e, int variant) {
 }
 
 int swg_ensemble_kick_variant(swg_ensemble *e, int kind, int *variant) {
-    if (!e || !variant || kind < 0 || kind > 3) return SWG_ERR_ARG;
+    if (!e || !variant || kind < 0 || kind > 4) return SWG_ERR_ARG;
     if (kind == 2)
         *variant = e->it_sym ? e->sym_strip : -1;
     else if (kind == 3)
         *variant = e->it_sym ? e->sym_warps : -1;
+    else if (kind == 4)
+        *variant = e->it_sym ? e->sym_tile : -1;
     else
         *variant = e->kv[kind];
     return SWG_OK;
@@ -2447,6 +2466,17 @@ int swg_ensemble_set_kick_warps(swg_ensemble *e, int warps) {
     if (!e || !(warps == 0 || warps == 1 || warps == 2 || warps == 4)) return SWG_ERR_ARG;
     SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick warps"));
     e->force_warps = warps;
+    if (e->it_sym) cudaFree(e->it_sym);
+    e->it_sym = nullptr;
+    e->n_sym = 0;
+    reset_kick_plans(e);
+    return SWG_OK;
+}
+
+int swg_ensemble_set_kick_tile(swg_ensemble *e, int tile) {
+    if (!e || !(tile == 0 || tile == 64 || tile == 128)) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick tile"));
+    e->force_tile = tile;
     if (e->it_sym) cudaFree(e->it_sym);
     e->it_sym = nullptr;
     e->n_sym = 0;

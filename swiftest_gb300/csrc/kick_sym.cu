@@ -45,8 +45,7 @@ namespace swg {
 
 namespace {
 
-constexpr int TS = KICK_SYM_TILE;  // bodies per tile
-constexpr int SR = TS / 32;        // receivers per lane = 32-body sub-tiles per tile
+constexpr int TS = KICK_SYM_TILE;  // bodies per tile by default (the single-system plan's tile)
 constexpr int MAX_STRIP = 4;       // most tiles J per item (one row strip of the upper triangle)
 constexpr float PAD_POS = 3.0e6f;  // position of the padding beyond a system's last body
 constexpr unsigned FULL = 0xffffffffu;
@@ -130,10 +129,11 @@ __device__ __forceinline__ void rule2(f32x2 r2, f32x2 Rp, float Rk, int ja, int 
 // across lanes t and t ^ 16.  Outputs: receiver partials px.. and minus the partner sums
 // in qx.. (for this lane's partner t).  P points at the lane's first entry.
 // GUARD: the pair rule pair by pair (RAD only); else, with RAD, mn keeps the smallest r^2.
-template <bool RAD, bool GUARD, int NK>
-__device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Recv2 (&q)[SR], int src, float (&px)[SR],
-                                            float (&py)[SR], float (&pz)[SR], float &qx, float &qy, float &qz,
-                                            float (&mn)[SR]) {
+// NR: receivers per lane (the tile's 32-body sub-tiles).
+template <bool RAD, bool GUARD, int NK, int NR>
+__device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Recv2 (&q)[NR], int src, float (&px)[NR],
+                                            float (&py)[NR], float (&pz)[NR], float &qx, float &qy, float &qz,
+                                            float (&mn)[NR]) {
     f32x2 ax[NK], ay[NK], az[NK];
 #pragma unroll
     for (int k = 0; k < NK; k++) {
@@ -192,12 +192,12 @@ __device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Re
 
 // sym_subtile without the rule, then (RAD) recomputed with it when some receiver k < NK
 // may meet a partner within the radii.
-template <bool RAD, int NK>
-__device__ __forceinline__ void sym_subtile_ruled(const SubTile &S, int lane, const Recv2 (&q)[SR],
-                                                  const bool (&ok)[SR], int src, float (&px)[SR], float (&py)[SR],
-                                                  float (&pz)[SR], float &qx, float &qy, float &qz) {
-    float mn[SR];
-    sym_subtile<RAD, false, NK>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
+template <bool RAD, int NK, int NR>
+__device__ __forceinline__ void sym_subtile_ruled(const SubTile &S, int lane, const Recv2 (&q)[NR],
+                                                  const bool (&ok)[NR], int src, float (&px)[NR], float (&py)[NR],
+                                                  float (&pz)[NR], float &qx, float &qy, float &qz) {
+    float mn[NR];
+    sym_subtile<RAD, false, NK, NR>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
     if (RAD) {
         float Ra, Rb;
         f2_unpack(S.w[3][lane].y, Ra, Rb);  // the lane's entry: partners lane and lane ^ 16
@@ -209,7 +209,7 @@ __device__ __forceinline__ void sym_subtile_ruled(const SubTile &S, int lane, co
             need = need || (ok[k] && mn[k] <= rs * rs);
         }
         if (__any_sync(FULL, need))  // rare: a pair may lie within the radii
-            sym_subtile<RAD, true, NK>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
+            sym_subtile<RAD, true, NK, NR>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
     }
 }
 
@@ -258,13 +258,13 @@ __device__ __forceinline__ void own_subtile(const SubTile &S, int lane, const Re
 // Sub-tile U of a diagonal tile (I == J): receivers k < U against it with the rotation,
 // whose partner sums belong to receiver U of this lane, and receiver U against it
 // one-sided with the pair rule.
-template <bool RAD, int U>
-__device__ __forceinline__ void diag_subtile(const SubTile (&sP)[SR], const Recv2 (&q)[SR], const bool (&ok)[SR],
-                                             int lane, FF (&ax)[SR], FF (&ay)[SR], FF (&az)[SR]) {
+template <bool RAD, int U, int NR>
+__device__ __forceinline__ void diag_subtile(const SubTile (&sP)[NR], const Recv2 (&q)[NR], const bool (&ok)[NR],
+                                             int lane, FF (&ax)[NR], FF (&ay)[NR], FF (&az)[NR]) {
     float qx = 0.f, qy = 0.f, qz = 0.f;
     if constexpr (U > 0) {
-        float px[SR], py[SR], pz[SR];
-        sym_subtile_ruled<RAD, U>(sP[U], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
+        float px[NR], py[NR], pz[NR];
+        sym_subtile_ruled<RAD, U, NR>(sP[U], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
 #pragma unroll
         for (int k = 0; k < U; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
     }
@@ -276,10 +276,11 @@ __device__ __forceinline__ void diag_subtile(const SubTile (&sP)[SR], const Recv
 
 // Item: (system, tile I, first tile J0 | tiles nJ << 24, receiver slot).  pA/pB: every
 // body split into (x_hi, y_hi, z_hi, Gm), (x_lo, y_lo, z_lo, R).  A receiver slot is
-// [x_hi, x_lo, y_hi, y_lo, z_hi, z_lo] x TS floats, a pair slot [x, y, z] x TS floats.
+// [x_hi, x_lo, y_hi, y_lo, z_hi, z_lo] x T floats, a pair slot [x, y, z] x T floats.
 // W warps per block, each an independent worker with its own staged tile (the block size
 // only changes how the warps are packed on the SMs; every item's arithmetic is the same).
-template <bool RAD, int W>
+// T bodies per tile: 128 (four receivers per lane) or 64 (two).
+template <bool RAD, int W, int T>
 __global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int4 *__restrict__ items,
                                                       const int32_t *__restrict__ poff,
                                                       const int32_t *__restrict__ npl,
@@ -289,6 +290,8 @@ __global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int
                                                       unsigned *__restrict__ head,
                                                       const int32_t *__restrict__ sys_flag, int phase,
                                                       const uint8_t *__restrict__ iflag, unsigned accept) {
+    constexpr int SR = T / 32;  // receivers per lane = 32-body sub-tiles per tile
+    static_assert(SR == 2 || SR == 4, "tiles of 64 or 128 bodies");
     __shared__ SubTile sPw[W][SR];
     SubTile(&sP)[SR] = sPw[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -302,12 +305,12 @@ __global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int
         const int s = w.x, I = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
         if (sys_flag && sys_flag[s] != phase) continue;  // warp-uniform
         if (iflag && !((accept >> iflag[it]) & 1u)) continue;
-        const int p0 = poff[s], n = npl[s], nt = (n + TS - 1) / TS;
+        const int p0 = poff[s], n = npl[s], nt = (n + T - 1) / T;
         Recv2 q[SR];
         bool ok[SR];
 #pragma unroll
         for (int k = 0; k < SR; k++) {
-            const int i = I * TS + k * 32 + lane;
+            const int i = I * T + k * 32 + lane;
             ok[k] = i < n;
             const float4 a = ok[k] ? pA[p0 + i] : pad_a;
             const float4 b = ok[k] ? pB[p0 + i] : zero;
@@ -322,41 +325,42 @@ __global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int
             __syncwarp();  // the previous tile's shared data is consumed
 #pragma unroll
             for (int u = 0; u < SR; u++) {
-                const int j = J * TS + u * 32 + lane;
+                const int j = J * T + u * 32 + lane;
                 const float4 a = j < n ? pA[p0 + j] : pad_a;
                 const float4 b = j < n ? pB[p0 + j] : zero;
                 stage_subtile(sP[u], a, b, lane);
             }
             __syncwarp();
             if (I == J) {
-                static_assert(SR == 4, "diagonal sub-tiles");
-                diag_subtile<RAD, 0>(sP, q, ok, lane, ax, ay, az);
-                diag_subtile<RAD, 1>(sP, q, ok, lane, ax, ay, az);
-                diag_subtile<RAD, 2>(sP, q, ok, lane, ax, ay, az);
-                diag_subtile<RAD, 3>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 0, SR>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 1, SR>(sP, q, ok, lane, ax, ay, az);
+                if constexpr (SR > 2) {
+                    diag_subtile<RAD, 2, SR>(sP, q, ok, lane, ax, ay, az);
+                    diag_subtile<RAD, 3, SR>(sP, q, ok, lane, ax, ay, az);
+                }
                 continue;
             }
-            float *o1 = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, J, nt)) * 3 * TS;
+            float *o1 = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, J, nt)) * 3 * T;
             for (int u = 0; u < SR; u++) {
                 float px[SR], py[SR], pz[SR], qx, qy, qz;
-                sym_subtile_ruled<RAD, SR>(sP[u], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
+                sym_subtile_ruled<RAD, SR, SR>(sP[u], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
 #pragma unroll
                 for (int k = 0; k < SR; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
-                o1[0 * TS + u * 32 + lane] = qx;
-                o1[1 * TS + u * 32 + lane] = qy;
-                o1[2 * TS + u * 32 + lane] = qz;
+                o1[0 * T + u * 32 + lane] = qx;
+                o1[1 * T + u * 32 + lane] = qy;
+                o1[2 * T + u * 32 + lane] = qz;
             }
         }
-        float *o0 = rpart + (size_t)w.w * 6 * TS;
+        float *o0 = rpart + (size_t)w.w * 6 * T;
 #pragma unroll
         for (int k = 0; k < SR; k++) {
             const int il = k * 32 + lane;
-            o0[0 * TS + il] = ax[k].hi;
-            o0[1 * TS + il] = ax[k].lo;
-            o0[2 * TS + il] = ay[k].hi;
-            o0[3 * TS + il] = ay[k].lo;
-            o0[4 * TS + il] = az[k].hi;
-            o0[5 * TS + il] = az[k].lo;
+            o0[0 * T + il] = ax[k].hi;
+            o0[1 * T + il] = ax[k].lo;
+            o0[2 * T + il] = ay[k].hi;
+            o0[3 * T + il] = ay[k].lo;
+            o0[4 * T + il] = az[k].hi;
+            o0[5 * T + il] = az[k].lo;
         }
     }
 }
@@ -365,7 +369,7 @@ __global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int
 // strip's tiles J holds a body marked in enc, else 1 (see kick_sym_item_flags).
 __global__ void k_kick_sym_item_flags(int nitems, const int4 *__restrict__ items, const int32_t *__restrict__ poff,
                                       const int32_t *__restrict__ npl, const int32_t *__restrict__ sys_enc,
-                                      const uint8_t *__restrict__ enc, uint8_t *__restrict__ iflag) {
+                                      const uint8_t *__restrict__ enc, uint8_t *__restrict__ iflag, int ts) {
     const int it = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (it >= nitems) return;  // whole warps leave together
@@ -379,8 +383,8 @@ __global__ void k_kick_sym_item_flags(int nitems, const int4 *__restrict__ items
     bool dirty = false;
     for (int t = -1; t < nJ; t++) {
         const int T = t < 0 ? I : J0 + t;
-        for (int k = lane; k < TS; k += 32) {
-            const int i = T * TS + k;
+        for (int k = lane; k < ts; k += 32) {
+            const int i = T * ts + k;
             if (i < n && enc[p0 + i]) dirty = true;
         }
     }
@@ -396,27 +400,27 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
                                   const int32_t *__restrict__ npl, const int32_t *__restrict__ sbase,
                                   const float *__restrict__ rpart, const float *__restrict__ ppart,
                                   double *__restrict__ acc, int acc_is_zero, const int32_t *__restrict__ sys_flag,
-                                  int phase, int strip) {
+                                  int phase, int strip, int ts) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= n) return;
     const int s = psys ? psys[b] : 0;
     if (sys_flag && sys_flag[s] != phase) return;
     const int i = (int)(b - poff[s]);
-    const int nt = (npl[s] + TS - 1) / TS, K = i / TS, l = i % TS;
+    const int nt = (npl[s] + ts - 1) / ts, K = i / ts, l = i % ts;
     FF fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
     float lx = 0.f, ly = 0.f, lz = 0.f;
     int row = 0;  // first receiver slot of row K
     for (int I = 0; I < K; I++) {
-        const float *o = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, K, nt)) * 3 * TS;
-        ff_add3(fx, fy, fz, o[l], o[TS + l], o[2 * TS + l]);
+        const float *o = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, K, nt)) * 3 * ts;
+        ff_add3(fx, fy, fz, o[l], o[ts + l], o[2 * ts + l]);
         row += (nt - I + strip - 1) / strip;
     }
     for (int m = 0; m < (nt - K + strip - 1) / strip; m++) {
-        const float *o = rpart + (size_t)(sbase[2 * s] + row + m) * 6 * TS;
-        ff_add3(fx, fy, fz, o[l], o[2 * TS + l], o[4 * TS + l]);
-        lx += o[TS + l];
-        ly += o[3 * TS + l];
-        lz += o[5 * TS + l];
+        const float *o = rpart + (size_t)(sbase[2 * s] + row + m) * 6 * ts;
+        ff_add3(fx, fy, fz, o[l], o[2 * ts + l], o[4 * ts + l]);
+        lx += o[ts + l];
+        ly += o[3 * ts + l];
+        lz += o[5 * ts + l];
     }
     const double sx = (double)fx.hi + ((double)fx.lo + (double)lx);
     const double sy = (double)fy.hi + ((double)fy.lo + (double)ly);
@@ -430,19 +434,19 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
 }  // namespace
 
 int kick_sym_item_flags(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
-                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag) {
+                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag, int tile) {
     if (nitems <= 0) return SWG_OK;
     const int64_t threads = (int64_t)nitems * 32;
     k_kick_sym_item_flags<<<(int)((threads + 255) / 256), 256, 0, c->stream>>>(nitems, items, poff, npl, sys_enc,
-                                                                              enc, iflag);
+                                                                              enc, iflag, tile);
     c->launches++;
     return launch_status(c, "kick_sym_item_flags");
 }
 
-int kick_sym_strip(int32_t nsys, const int32_t *npl, int num_sms) {
+int kick_sym_strip(int32_t nsys, const int32_t *npl, int num_sms, int tile) {
     int64_t pairs = 0;
     for (int s = 0; s < nsys; s++) {
-        const int64_t nt = (npl[s] + TS - 1) / TS;
+        const int64_t nt = (npl[s] + tile - 1) / tile;
         pairs += nt * (nt + 1) / 2;
     }
     // strips of MAX_STRIP measured fastest whenever they leave a few items per SM; shorter
@@ -456,16 +460,16 @@ bool kick_sym_single_ok(int32_t npl, int num_sms) {
 }
 
 int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<int4> &items,
-                       std::vector<int32_t> &sbase, int64_t *npair_slots) {
+                       std::vector<int32_t> &sbase, int64_t *npair_slots, int tile) {
     items.clear();
     sbase.assign(2 * (size_t)nsys, 0);
     std::vector<int64_t> cost;
     int64_t nrs = 0, nps = 0;
     for (int s = 0; s < nsys; s++) {
-        const int nt = (npl[s] + TS - 1) / TS;
+        const int nt = (npl[s] + tile - 1) / tile;
         sbase[2 * s] = (int32_t)nrs;
         sbase[2 * s + 1] = (int32_t)nps;
-        auto rows = [&](int T) { return (int64_t)std::min(TS, npl[s] - T * TS); };
+        auto rows = [&](int T) { return (int64_t)std::min(tile, npl[s] - T * tile); };
         for (int I = 0; I < nt; I++)
             for (int J0 = I; J0 < nt; J0 += strip) {
                 const int nJ = std::min(strip, nt - J0);
@@ -486,19 +490,19 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<
     return nrs;
 }
 
-template <bool RAD, int W>
+template <bool RAD, int W, int T>
 int sym_launch(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
                const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart, float *ppart, unsigned *head,
                const int32_t *sys_flag, int phase, const uint8_t *iflag, unsigned accept) {
     static int o = 0;  // resident blocks per SM, queried once per variant
     if (o == 0) {
         int nb = 0;
-        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<RAD, W>, 32 * W, 0),
+        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym<RAD, W, T>, 32 * W, 0),
                             "occupancy"));
         o = nb > 0 ? nb : 1;
     }
     const int grid = std::min((nitems + W - 1) / W, o * (c->num_sms > 0 ? c->num_sms : 152));
-    k_kick_mixed_sym<RAD, W><<<grid, 32 * W, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
+    k_kick_mixed_sym<RAD, W, T><<<grid, 32 * W, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
                                                               head, sys_flag, phase, iflag, accept);
     return SWG_OK;
 }
@@ -506,18 +510,21 @@ int sym_launch(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, c
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
                            float *ppart, unsigned *head, const int32_t *sys_flag, int phase, const uint8_t *iflag,
-                           unsigned accept, int warps) {
+                           unsigned accept, int warps, int tile) {
     if (nitems <= 0) return SWG_OK;
-    if (warps != 1 && warps != 2 && warps != 4) return SWG_ERR_ARG;
+    if ((warps != 1 && warps != 2 && warps != 4) || (tile != 64 && tile != 128)) return SWG_ERR_ARG;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
 #define SWG_SYM_ARGS c, nitems, items, poff, npl, sbase, pA, pB, rpart, ppart, head, sys_flag, phase, iflag, accept
+    // 64-body tiles run with one warp per block (the block size is tuned on 128-body tiles)
     int rc;
-    if (rad)
-        rc = warps == 1 ? sym_launch<true, 1>(SWG_SYM_ARGS)
-                        : (warps == 2 ? sym_launch<true, 2>(SWG_SYM_ARGS) : sym_launch<true, 4>(SWG_SYM_ARGS));
+    if (tile == 64)
+        rc = rad ? sym_launch<true, 1, 64>(SWG_SYM_ARGS) : sym_launch<false, 1, 64>(SWG_SYM_ARGS);
+    else if (rad)
+        rc = warps == 1 ? sym_launch<true, 1, 128>(SWG_SYM_ARGS)
+                        : (warps == 2 ? sym_launch<true, 2, 128>(SWG_SYM_ARGS) : sym_launch<true, 4, 128>(SWG_SYM_ARGS));
     else
-        rc = warps == 1 ? sym_launch<false, 1>(SWG_SYM_ARGS)
-                        : (warps == 2 ? sym_launch<false, 2>(SWG_SYM_ARGS) : sym_launch<false, 4>(SWG_SYM_ARGS));
+        rc = warps == 1 ? sym_launch<false, 1, 128>(SWG_SYM_ARGS)
+                        : (warps == 2 ? sym_launch<false, 2, 128>(SWG_SYM_ARGS) : sym_launch<false, 4, 128>(SWG_SYM_ARGS));
 #undef SWG_SYM_ARGS
     SWG_TRY(rc);
     c->launches++;
@@ -526,10 +533,10 @@ int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, 
 
 int kick_mixed_sym_reduce(swg_ctx *c, int strip, int64_t n, const int32_t *psys, const int32_t *poff,
                           const int32_t *npl, const int32_t *sbase, const float *rpart, const float *ppart,
-                          double *acc, int acc_is_zero, const int32_t *sys_flag, int phase) {
+                          double *acc, int acc_is_zero, const int32_t *sys_flag, int phase, int tile) {
     if (n <= 0) return SWG_OK;
     k_kick_sym_reduce<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(n, psys, poff, npl, sbase, rpart, ppart, acc,
-                                                                      acc_is_zero, sys_flag, phase, strip);
+                                                                      acc_is_zero, sys_flag, phase, strip, tile);
     c->launches++;
     return launch_status(c, "kick_sym_reduce");
 }
@@ -582,8 +589,8 @@ int kick_mixed_sym_single(swg_ctx *c, int32_t npl, const double *r, const double
         std::vector<int4> items;
         std::vector<int32_t> base;
         int64_t npair = 0;
-        p.strip = kick_sym_strip(1, &npl, c->num_sms);
-        const int64_t nrecv = kick_sym_items(1, &npl, p.strip, items, base, &npair);
+        p.strip = kick_sym_strip(1, &npl, c->num_sms, TS);
+        const int64_t nrecv = kick_sym_items(1, &npl, p.strip, items, base, &npair, TS);
         const int32_t meta[4] = {0, npl, base[0], base[1]};
         SWG_TRY(sym_alloc(c, &p.items, items.size()));
         SWG_TRY(sym_alloc(c, &p.meta, 4));

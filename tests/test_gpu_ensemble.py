@@ -159,6 +159,26 @@ def test_symba_ensemble_mixed_conservation(ctx):
     assert f.stats()["plpl_encounters"] > 0
 
 
+@pytest.mark.parametrize("tile", [64, 128])
+def test_symba_ensemble_mixed_conservation_tiles(ctx, tile):
+    # both tile sizes of the symmetric pl-pl kick through whole SyMBA steps (the closing kick
+    # split by the items' encounter flags): energy within 2x of the FP64 path's error
+    E = _compact("C4", nsys=5, scale=0.06, tp_per_pl=0)
+    kw = dict(dt=0.005, rhscale=2.0)
+    f = Ensemble(ctx, E, precision="FP64", **kw)
+    m = Ensemble(ctx, E, precision="MIXED", **kw)
+    m.set_kick_tile(tile)
+    e0 = f.energy()
+    f.step(100)
+    m.step(100)
+    assert m.kick_tile() == tile
+    ef, em = f.energy(), m.energy()
+    dEf = np.abs(ef["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
+    dEm = np.abs(em["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
+    assert np.all(dEm < np.maximum(2 * dEf, 1e-9)), (dEm, dEf)
+    assert f.stats()["plpl_encounters"] > 0
+
+
 def test_symba_ensemble_lists_many_tiles(ctx):
     # systems of 150-1500 bodies (many 64-body tiles, radius-sorted culling active), lists
     # checked against the oracle's all-pairs check at every step across a re-sort boundary
@@ -280,15 +300,36 @@ def test_symmetric_kick_strips(ctx, strip):
     ens.close()
 
 
+@pytest.mark.parametrize("tile,strip", [(64, 1), (64, 4), (64, 16), (0, 0)])
+def test_symmetric_kick_tiles(ctx, tile, strip):
+    # 64-body tiles of the symmetric pl-pl kick (and the autotuned default): within the
+    # mixed-kick tolerance of the oracle's FP64 triangular kick, and deterministic
+    E = IC.make_ensemble("C4", nsys=4, scale=0.5)
+    want = [O.kick_tri_pl(pl["rh"], pl["Gmass"], pl["radius"]) for pl, _ in E["systems"]]
+    ens = Ensemble(ctx, E, precision="MIXED")
+    ens.set_kick_tile(tile)
+    ens.set_kick_strip(strip)
+    g = ens.getacch_int_pl()
+    assert ens.kick_tile() == tile if tile else ens.kick_tile() in (64, 128)
+    for s, r in enumerate(want):
+        a, b = ens.poff[s], ens.poff[s + 1]
+        e = np.linalg.norm(g[a:b] - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
+        assert e.max() < 2e-5, (tile, strip, s, e.max())
+        assert np.sqrt(np.mean(e ** 2)) < 1e-6, (tile, strip, s)
+    assert np.array_equal(g, ens.getacch_int_pl())
+    ens.close()
+
+
 @pytest.mark.parametrize("warps", [2, 4, 0])
 def test_symmetric_kick_warps_same_bits(ctx, warps):
     # warps per block of the symmetric pl-pl kick (forced, and the autotuned default): every
     # warp is an independent worker of the persistent grid, so each count gives the bits of
-    # one warp per block at the same strip
+    # one warp per block at the same tile and strip
     E = IC.make_ensemble("C4", nsys=4, scale=0.5)
 
     def accel(w):
         ens = Ensemble(ctx, E, precision="MIXED")
+        ens.set_kick_tile(128)
         ens.set_kick_strip(4)
         ens.set_kick_warps(w)
         g = ens.getacch_int_pl()
