@@ -236,6 +236,8 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
 // from them (the bound argument of the file comment holds for both tests: same closest-
 // approach expression), each warp of 32 tp skipping the 32-body pl sub-tiles that are apart
 // from it, as in k_encounter_sorted.  Pairs are written with global 1-based indices (pl, tp).
+// pchunk > 0: the item's fourth field c selects the pl sub-tiles [c pchunk, (c + 1) pchunk)
+// (a single system splits its pl range over several items to fill the GPU); 0: all of them.
 template <bool DISCARD>
 __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ items, const int32_t *__restrict__ poff,
                                                     const int32_t *__restrict__ npl, const int32_t *__restrict__ ptbase,
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ ite
                                                     const int32_t *__restrict__ tstatus, double dt, long long cap,
                                                     int32_t *__restrict__ o1, int32_t *__restrict__ o2,
                                                     int32_t *__restrict__ olv, unsigned long long *__restrict__ count,
-                                                    int32_t *__restrict__ flag) {
+                                                    int32_t *__restrict__ flag, int pchunk) {
     __shared__ WarpStage st_all[SQ / 32];
     const int4 w = items[blockIdx.x];
     const int s = w.x, q0 = w.y, nr = w.z;
@@ -273,9 +275,13 @@ __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ ite
         if (DISCARD) active = tstatus[gq] == ST_ACTIVE;
     }
     const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);
-    const int nsub = (n1 + 31) / 32;
-    for (int u0 = 0; u0 < nsub; u0 += 32) {
-        const bool keep = u0 + lane < nsub && !tiles_apart(SP[u0 + lane], QW);
+    int ubeg = 0, uend = (n1 + 31) / 32;
+    if (pchunk > 0) {
+        ubeg = w.w * pchunk;
+        uend = min(uend, ubeg + pchunk);
+    }
+    for (int u0 = ubeg; u0 < uend; u0 += 32) {
+        const bool keep = u0 + lane < uend && !tiles_apart(SP[u0 + lane], QW);
         unsigned m = __ballot_sync(0xffffffffu, keep);
         while (m) {
             const int p0 = 32 * (u0 + __ffs(m) - 1);
@@ -354,12 +360,12 @@ int sorted_set_prep(swg_ctx *c, const SortedSet &x, int nsys, bool resort, doubl
 
 int pltp_sorted_batched(swg_ctx *c, bool discard, const SortedSet &pl, const SortedSet &tp, const int32_t *tstatus,
                         int nitems, const int4 *items, double dt, long long cap, int32_t *o1, int32_t *o2,
-                        int32_t *olv, unsigned long long *count, int32_t *flag) {
+                        int32_t *olv, unsigned long long *count, int32_t *flag, int pchunk) {
     if (nitems <= 0 || pl.ntiles <= 0) return SWG_OK;
 #define SWG_PLTP_ARGS                                                                                                 \
     items, pl.off, pl.n, pl.tbase, pl.perm, pl.F, pl.F + pl.N, pl.F + 2 * pl.N, pl.bounds, pl.r, pl.v,    \
         pl.renc, tp.off, tp.tbase, tp.perm, tp.F, tp.F + tp.N, tp.F + 2 * tp.N, tp.bounds, tp.r, tp.v,      \
-        tstatus, dt, cap, o1, o2, olv, count, flag
+        tstatus, dt, cap, o1, o2, olv, count, flag, pchunk
     if (discard)
         k_pltp_sorted<true><<<nitems, SQ, 0, c->stream>>>(SWG_PLTP_ARGS);
     else

@@ -323,10 +323,11 @@ int sorted_set_prep(swg_ctx *c, const SortedSet &x, int nsys, bool resort, doubl
 // pl-tp over radius-sorted tiles (both sets prepared at the current state): the level-0
 // pl-tp check (pairs (pl, tp), global 1-based, into o1/o2/olv/count) or, discard, the
 // close-approach scan of swiftest_discard_pl_tp (flag[tp] = 1; tp renc = pl radius).
-// Items: (system, first tp in sorted order, tp count <= ENC_SORTED_TILE).
+// Items: (system, first tp in sorted order, tp count <= ENC_SORTED_TILE, pl chunk); pchunk > 0:
+// the item covers the pl sub-tiles (32 bodies) [chunk pchunk, (chunk + 1) pchunk), else all.
 int pltp_sorted_batched(swg_ctx *c, bool discard, const SortedSet &pl, const SortedSet &tp, const int32_t *tstatus,
                         int nitems, const int4 *items, double dt, long long cap, int32_t *o1, int32_t *o2,
-                        int32_t *olv, unsigned long long *count, int32_t *flag);
+                        int32_t *olv, unsigned long long *count, int32_t *flag, int pchunk = 0);
 
 // Full check of one kind (0 plpl, 1 plplm, 2 pltp): sorted unique pairs in the
 // workspace's raw buffers; *n_out gets the count (host).  Synchronizes.

@@ -26,6 +26,26 @@ using namespace swg;
 using namespace swg::sdev;
 
 
+// Radius-sorted pl and tp sets of one system, for its pl-tp level-0 check and close-approach
+// discard scan (the ensemble's radius-sorted kernels run with one system): the radial orders,
+// float copies and 32-body sub-tile bounds (encounter_sorted.cu), the 64-body bound tiles and
+// the tp receiver items.  Built at the first use (npl and ntp are fixed for the system's life).
+struct SortedOne {
+    int32_t *meta = nullptr;  // [0] 0 (first body and first tile of each set), [1] npl, [2] ntp
+    int32_t *pperm = nullptr, *tperm = nullptr;
+    float4 *pF = nullptr, *tF = nullptr, *pbounds = nullptr, *tbounds = nullptr;
+    int2 *ptiles = nullptr, *ttiles = nullptr;
+    int4 *items = nullptr;
+    int nitems = 0, nptiles = 0, nttiles = 0, pchunk = 0;  // pchunk: pl sub-tiles per item
+    int64_t npl_prep = 0, ntp_prep = 0;  // preparations so far: the pl order is refreshed at every
+                                         // 8th, the tp order at every 32nd (and at the first)
+    void release() {
+        void *ptrs[] = {meta, pperm, tperm, pF, tF, pbounds, tbounds, ptiles, ttiles, items};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+    }
+};
+
 struct swg_system {
     swg_ctx *c = nullptr;
     int integrator = SWG_HELIO;
@@ -70,6 +90,7 @@ struct swg_system {
     double E_collisions = 0.0, L_escape[3] = {0.0, 0.0, 0.0};  // collision bookkeeping (G*m units)
     double rec_dt = 0.0;                                        // step of the running recursion
     StepProfile prof;  // optional CUDA-event profile per kernel class (PROF_*)
+    SortedOne *srt = nullptr;  // radius-sorted sets of the pl-tp check and discard scan
 };
 
 namespace {
@@ -575,6 +596,83 @@ int ensure_list(swg_system *s, int32_t **l, int64_t *cap, int64_t need) {
     return SWG_OK;
 }
 
+// The radius-sorted sets of the system (SortedOne), built at the first call.
+template <typename T>
+int upload_vec(swg_ctx *c, T **dst, const std::vector<T> &v) {
+    SWG_TRY(dalloc(c, dst, v.size()));
+    if (v.empty()) return SWG_OK;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c->stream),
+                        "upload"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "upload");
+}
+int ensure_sorted(swg_system *s) {
+    if (s->srt) return SWG_OK;
+    swg_ctx *c = s->c;
+    SortedOne *x = new SortedOne();
+    s->srt = x;
+    const std::vector<int32_t> meta = {0, s->npl, s->ntp};
+    std::vector<int2> pt, tt;
+    for (int p0 = 0; p0 < s->npl; p0 += ENC_BOUND_TILE) pt.push_back(make_int2(0, p0));
+    for (int p0 = 0; p0 < s->ntp; p0 += ENC_BOUND_TILE) tt.push_back(make_int2(0, p0));
+    // tp receivers of ENC_SORTED_TILE by chunks of the pl's 32-body sub-tiles: about 1024
+    // blocks, so that one system fills the GPU
+    const int nq = (s->ntp + ENC_SORTED_TILE - 1) / ENC_SORTED_TILE, nsub = (s->npl + 31) / 32;
+    const int nch = std::max(1, std::min(nsub, 1024 / std::max(nq, 1)));
+    x->pchunk = (nsub + nch - 1) / nch;
+    std::vector<int4> items;
+    for (int q0 = 0; q0 < s->ntp; q0 += ENC_SORTED_TILE)
+        for (int u = 0, k = 0; u < nsub; u += x->pchunk, k++)
+            items.push_back(make_int4(0, q0, std::min(ENC_SORTED_TILE, s->ntp - q0), k));
+    x->nptiles = (int)pt.size();
+    x->nttiles = (int)tt.size();
+    x->nitems = (int)items.size();
+    SWG_TRY(upload_vec(c, &x->meta, meta));
+    SWG_TRY(upload_vec(c, &x->ptiles, pt));
+    SWG_TRY(upload_vec(c, &x->ttiles, tt));
+    SWG_TRY(upload_vec(c, &x->items, items));
+    SWG_TRY(dalloc(c, &x->pperm, (size_t)s->npl));
+    SWG_TRY(dalloc(c, &x->tperm, (size_t)s->ntp));
+    SWG_TRY(dalloc(c, &x->pF, 3 * (size_t)s->npl));
+    SWG_TRY(dalloc(c, &x->tF, 3 * (size_t)s->ntp));
+    SWG_TRY(dalloc(c, &x->pbounds, 2 * pt.size()));  // bounds of each tile's two 32-body halves
+    return dalloc(c, &x->tbounds, 2 * tt.size());
+}
+SortedSet sorted_pl(swg_system *s, const double *r, const double *v, const double *renc) {
+    SortedOne &x = *s->srt;
+    SortedSet p;
+    p.off = x.meta;
+    p.n = x.meta + 1;
+    p.r = r;
+    p.v = v;
+    p.renc = renc;
+    p.perm = x.pperm;
+    p.F = x.pF;
+    p.N = s->npl;
+    p.ntiles = x.nptiles;
+    p.tiles = x.ptiles;
+    p.tbase = x.meta;
+    p.bounds = x.pbounds;
+    p.nmax = s->npl;
+    return p;
+}
+SortedSet sorted_tp(swg_system *s, const double *r, const double *v) {
+    SortedOne &x = *s->srt;
+    SortedSet t;
+    t.off = x.meta;
+    t.n = x.meta + 2;
+    t.r = r;
+    t.v = v;
+    t.perm = x.tperm;
+    t.F = x.tF;
+    t.N = s->ntp;
+    t.ntiles = x.nttiles;
+    t.tiles = x.ttiles;
+    t.tbase = x.meta;
+    t.bounds = x.tbounds;
+    t.nmax = s->ntp;
+    return t;
+}
+
 // level-0 checks: symba_encounter_check_pl / _tp (symba_encounter_check.f90:14-87, 238-296)
 // Level-0 checks of symba_encounter_check_pl / _tp (symba_encounter_check.f90:14-87,
 // 238-296).  Both checks are launched before one host synchronization reads the two
@@ -599,6 +697,7 @@ int symba_level0(swg_system *s, double dt, int *lany) {
     }
     SWG_TRY(ensure(c, s->enc.sort, encounter_scratch_bytes(s->enc_plpl, s->npl, s->npl)));
     SWG_TRY(ensure(c, s->enc2.sort, encounter_scratch_bytes(s->enc_pltp, s->npl, s->ntp)));
+    if (do_pt && s->enc_pltp == SWG_ENC_TRIANGULAR) SWG_TRY(ensure_sorted(s));
     unsigned long long *h = (unsigned long long *)(s->h_flags + 8);
     auto launch = [&](int kind) -> int {
         EncWork &e = *w[kind];
@@ -616,6 +715,13 @@ int symba_level0(swg_system *s, double dt, int *lany) {
                                          s->vb + 3 * s->nplm, renc + s->nplm, 0, s->nplm, dt, e.rawcap, i1, i2, lv,
                                          cnt, e.sort.ptr));
             }
+        } else if (s->enc_pltp == SWG_ENC_TRIANGULAR) {
+            // the triangular pl-tp check over radius-sorted tiles (the same list once sorted)
+            const SortedSet pl = sorted_pl(s, s->rh, s->vb, renc), tp = sorted_tp(s, s->trh, s->tvb);
+            SWG_TRY(sorted_set_prep(c, pl, 1, s->srt->npl_prep++ % 8 == 0, dt));
+            SWG_TRY(sorted_set_prep(c, tp, 1, s->srt->ntp_prep++ % 32 == 0, dt));
+            SWG_TRY(pltp_sorted_batched(c, false, pl, tp, nullptr, s->srt->nitems, s->srt->items, dt, e.rawcap, i1, i2,
+                                        lv, cnt, nullptr, s->srt->pchunk));
         } else {
             SWG_TRY(encounter_launch(c, s->enc_pltp, s->npl, s->rh, s->vb, renc, s->ntp, s->trh, s->tvb, nullptr, 0, 0,
                                      dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
@@ -931,12 +1037,17 @@ int symba_interp(swg_system *s, double dt) {
 // swiftest_discard_pl_tp (src/swiftest/swiftest_discard.f90:244-290), run after each step
 // when close encounters are checked (param%lclose), as the reference's main loop
 // (swiftest_driver) does after every step.
+// The scan runs over the radius-sorted sets (the same flags as the all-pairs scan: a pl and a
+// tp whose radial intervals over the step are farther apart than the pl's radius are skipped).
 int discard_step(swg_system *s) {
     if (!s->lclose || s->npl == 0 || s->ntp == 0) return SWG_OK;
     swg_ctx *c = s->c;
-    SWG_TRY(ensure(c, s->discard_scratch, sizeof(float4) * 3 * ((size_t)s->npl + s->ntp) + 256));
-    SWG_TRY(discard_pl_tp_launch(c, s->npl, s->rh, s->vh, s->radius, s->ntp, s->trh, s->tvh, s->tstatus, s->dt,
-                                 (float4 *)s->discard_scratch.ptr, s->tflag));
+    SWG_TRY(ensure_sorted(s));
+    const SortedSet pl = sorted_pl(s, s->rh, s->vh, s->radius), tp = sorted_tp(s, s->trh, s->tvh);
+    SWG_TRY(sorted_set_prep(c, pl, 1, s->srt->npl_prep++ % 8 == 0, s->dt));
+    SWG_TRY(sorted_set_prep(c, tp, 1, s->srt->ntp_prep++ % 32 == 0, s->dt));
+    SWG_TRY(pltp_sorted_batched(c, true, pl, tp, s->tstatus, s->srt->nitems, s->srt->items, s->dt, 0, nullptr, nullptr,
+                                nullptr, nullptr, s->tflag, s->srt->pchunk));
     k_apply_discard<<<grid_for(s->ntp, 256), 256, 0, c->stream>>>(s->ntp, s->tflag, s->tstatus, s->tlmask, s->trh,
                                                                   s->tvh, s->tvb, s->npl, nullptr, nullptr, nullptr,
                                                                   s->ndiscard);
@@ -1043,6 +1154,10 @@ int swg_system_destroy(swg_system *s) {
         if (e) cudaEventDestroy(e);
     if (s->side) cudaStreamDestroy(s->side);
     s->prof.release();
+    if (s->srt) {
+        s->srt->release();
+        delete s->srt;
+    }
     delete s;
     return SWG_OK;
 }
