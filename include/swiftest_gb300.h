@@ -151,6 +151,10 @@ int swg_system_initialize(swg_system *sys);
 int swg_system_step(swg_system *sys, int32_t nsteps);
 int swg_system_get_pl(swg_system *sys, double *rh, double *vh, int32_t *status);
 int swg_system_get_tp(swg_system *sys, double *rh, double *vh, int32_t *status);
+/* Current Gmass, radius and rhill of the massive bodies (a collision merge changes them; any
+ * pointer may be NULL): what the reference's frame writer reads from pl%Gmass, pl%radius and
+ * pl%rhill (swiftest_io_netcdf_write_frame_body, swiftest_io.f90:1837-1996). */
+int swg_system_get_pl_masses(swg_system *sys, double *Gmass, double *radius, double *rhill);
 /* out[9]: te, ke, pe, be, Lx, Ly, Lz, GMtot (swiftest_util.f90:1172-1401, whose central-body
  * potential uses the body's barycentric distance), then te_helio: the same total with the
  * central-body potential at the heliocentric distance. */
@@ -223,6 +227,8 @@ int swg_ensemble_initialize(swg_ensemble *ens);
 int swg_ensemble_step(swg_ensemble *ens, int32_t nsteps);
 int swg_ensemble_get_pl(swg_ensemble *ens, double *rh, double *vh, int32_t *status);
 int swg_ensemble_get_tp(swg_ensemble *ens, double *rh, double *vh, int32_t *status);
+/* swg_system_get_pl_masses of every system (NPL values each, CSR order). */
+int swg_ensemble_get_pl_masses(swg_ensemble *ens, double *Gmass, double *radius, double *rhill);
 /* out[9*nsys]: per system the nine values of swg_system_energy */
 int swg_ensemble_energy(swg_ensemble *ens, double *out);
 /* out[4*nsys]: per system the four values of swg_system_collision_terms */

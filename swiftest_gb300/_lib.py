@@ -66,6 +66,7 @@ SIGNATURES = {
     "swg_system_initialize": (_INT, [_P]),
     "swg_system_step": (_INT, [_P, _I32]),
     "swg_system_get_pl": (_INT, [_P, _P, _P, _P]),
+    "swg_system_get_pl_masses": (_INT, [_P, _P, _P, _P]),
     "swg_system_get_tp": (_INT, [_P, _P, _P, _P]),
     "swg_system_energy": (_INT, [_P, _P]),
     "swg_system_collision_terms": (_INT, [_P, _P]),
@@ -86,6 +87,7 @@ SIGNATURES = {
     "swg_ensemble_initialize": (_INT, [_P]),
     "swg_ensemble_step": (_INT, [_P, _I32]),
     "swg_ensemble_get_pl": (_INT, [_P, _P, _P, _P]),
+    "swg_ensemble_get_pl_masses": (_INT, [_P, _P, _P, _P]),
     "swg_ensemble_get_tp": (_INT, [_P, _P, _P, _P]),
     "swg_ensemble_energy": (_INT, [_P, _P]),
     "swg_ensemble_collision_terms": (_INT, [_P, _P]),

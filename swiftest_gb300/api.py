@@ -291,6 +291,13 @@ class NBodySystem:
         self.ctx.check("swg_system_get_pl", self.ctx.lib.swg_system_get_pl(self.h, _ptr(rh), _ptr(vh), _ptr(st)))
         return rh, vh, st
 
+    def get_pl_masses(self):
+        """Current Gmass, radius and rhill of the massive bodies (merges change them)."""
+        g, r, h = np.zeros(self.npl), np.zeros(self.npl), np.zeros(self.npl)
+        self.ctx.check("swg_system_get_pl_masses",
+                       self.ctx.lib.swg_system_get_pl_masses(self.h, _ptr(g), _ptr(r), _ptr(h)))
+        return g, r, h
+
     def get_tp(self):
         rh = np.zeros((self.ntp, 3))
         vh = np.zeros((self.ntp, 3))
@@ -407,6 +414,13 @@ class Ensemble:
         st = np.zeros(self.NPL, np.int32)
         self.ctx.check("swg_ensemble_get_pl", self.ctx.lib.swg_ensemble_get_pl(self.h, _ptr(rh), _ptr(vh), _ptr(st)))
         return rh, vh, st
+
+    def get_pl_masses(self):
+        """Current Gmass, radius and rhill of every system's massive bodies (CSR order)."""
+        g, r, h = np.zeros(self.NPL), np.zeros(self.NPL), np.zeros(self.NPL)
+        self.ctx.check("swg_ensemble_get_pl_masses",
+                       self.ctx.lib.swg_ensemble_get_pl_masses(self.h, _ptr(g), _ptr(r), _ptr(h)))
+        return g, r, h
 
     def get_tp(self):
         rh = np.zeros((self.NTP, 3))

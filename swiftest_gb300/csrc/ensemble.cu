@@ -2282,6 +2282,19 @@ int swg_ensemble_step(swg_ensemble *e, int32_t nsteps) {
     return SWG_OK;
 }
 
+int swg_ensemble_get_pl_masses(swg_ensemble *e, double *Gmass, double *radius, double *rhill) {
+    if (!e) return SWG_ERR_ARG;
+    swg_ctx *c = e->c;
+    const size_t n = e->NPL;
+    if (n == 0) return SWG_OK;
+    const std::pair<double *, const double *> xs[] = {{Gmass, e->Gmass}, {radius, e->radius}, {rhill, e->rhill}};
+    for (const auto &x : xs)
+        if (x.first)
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.first, x.second, 8 * n, cudaMemcpyDeviceToHost, c->stream),
+                                "get_pl_masses"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "get_pl_masses");
+}
+
 int swg_ensemble_get_pl(swg_ensemble *e, double *rh, double *vh, int32_t *status) {
     if (!e) return SWG_ERR_ARG;
     swg_ctx *c = e->c;

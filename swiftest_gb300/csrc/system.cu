@@ -1297,6 +1297,19 @@ int swg_system_step(swg_system *s, int32_t nsteps) {
     return SWG_OK;
 }
 
+int swg_system_get_pl_masses(swg_system *s, double *Gmass, double *radius, double *rhill) {
+    if (!s) return SWG_ERR_ARG;
+    swg_ctx *c = s->c;
+    const size_t n = s->npl;
+    if (n == 0) return SWG_OK;
+    const std::pair<double *, const double *> xs[] = {{Gmass, s->Gmass}, {radius, s->radius}, {rhill, s->rhill}};
+    for (const auto &x : xs)
+        if (x.first)
+            SWG_TRY(cuda_status(c, cudaMemcpyAsync(x.first, x.second, 8 * n, cudaMemcpyDeviceToHost, c->stream),
+                                "get_pl_masses"));
+    return cuda_status(c, cudaStreamSynchronize(c->stream), "get_pl_masses");
+}
+
 int swg_system_get_pl(swg_system *s, double *rh, double *vh, int32_t *status) {
     if (!s) return SWG_ERR_ARG;
     swg_ctx *c = s->c;

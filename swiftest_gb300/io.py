@@ -16,8 +16,9 @@ of swiftest_io_param_reader (:2300-2500) that select them:
 Lines starting with ``!`` (the copyright headers of the reference's example files) are
 skipped.  Elements are converted to positions and velocities on the GPU
 (``Context.el2xv``, swiftest_orbel_el2xv) with mu = GMcb + Gmass for massive bodies and
-GMcb for test particles, as swiftest_orbel_el2xv_vec does after set_mu.  NetCDF input and
-output are not provided (no NetCDF library in this build).
+GMcb for test particles, as swiftest_orbel_el2xv_vec does after set_mu.  With IN_TYPE
+NETCDF_DOUBLE (or NETCDF_FLOAT) the run starts from the last frame of the NC_IN data file
+(``swiftest_gb300.netcdf``, the restart path of swiftest_io_netcdf_read_frame_system).
 """
 from __future__ import annotations
 
@@ -123,9 +124,15 @@ def load_run(param_path, ctx=None) -> dict:
     velocities heliocentric (elements converted with ``ctx``, a ``Context``, for IN_FORM EL).
     Returns {"param", "cb", "pl", "tp"}; massive bodies without RHILL_PRESENT get no rhill."""
     par = read_param(param_path)
-    if par.get("IN_TYPE", "ASCII").upper() != "ASCII":
-        raise ValueError("only IN_TYPE ASCII is read (no NetCDF library in this build)")
     base = Path(param_path).parent
+    in_type = par.get("IN_TYPE", "ASCII").upper()
+    if in_type in ("NETCDF_DOUBLE", "NETCDF_FLOAT"):
+        from . import netcdf
+        fr = netcdf.read_frame(base / par.get("NC_IN", "init_cond.nc"))
+        return {"param": par, "cb": fr["cb"], "pl": fr["pl"], "tp": fr["tp"] if len(fr["tp"]["rh"]) else None,
+                "time": fr["time"]}
+    if in_type != "ASCII":
+        raise ValueError(f"IN_TYPE {in_type}: ASCII, NETCDF_DOUBLE or NETCDF_FLOAT")
     form = par.get("IN_FORM", "XV").upper()
     rot = flag(par, "ROTATION")
     cb = read_cb(base / par["CB_IN"], rotation=rot)
