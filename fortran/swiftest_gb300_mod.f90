@@ -233,6 +233,12 @@ module swiftest_gb300_mod
          real(c_double), intent(out) :: rh(3,*), vh(3,*)
          integer(c_int32_t), intent(out) :: status(*)
       end function
+      integer(c_int) function swg_system_get_pl_masses(sys, Gmass, radius, rhill) &
+                                                       bind(C, name="swg_system_get_pl_masses")
+         import :: c_ptr, c_int, c_double
+         type(c_ptr), value :: sys
+         real(c_double), intent(out) :: Gmass(*), radius(*), rhill(*)
+      end function
       integer(c_int) function swg_system_energy(sys, out) bind(C, name="swg_system_energy")
          import :: c_ptr, c_int, c_double
          type(c_ptr), value :: sys
@@ -323,6 +329,16 @@ module swiftest_gb300_mod
          type(c_ptr), value :: ens
          integer(c_int), value :: strip
       end function
+      integer(c_int) function swg_ensemble_set_kick_warps(ens, warps) bind(C, name="swg_ensemble_set_kick_warps")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: ens
+         integer(c_int), value :: warps
+      end function
+      integer(c_int) function swg_ensemble_set_kick_tile(ens, tile) bind(C, name="swg_ensemble_set_kick_tile")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: ens
+         integer(c_int), value :: tile
+      end function
       integer(c_int) function swg_ensemble_initialize(ens) bind(C, name="swg_ensemble_initialize")
          import :: c_ptr, c_int
          type(c_ptr), value :: ens
@@ -343,6 +359,12 @@ module swiftest_gb300_mod
          type(c_ptr), value :: ens
          real(c_double), intent(out) :: rh(3,*), vh(3,*)
          integer(c_int32_t), intent(out) :: status(*)
+      end function
+      integer(c_int) function swg_ensemble_get_pl_masses(ens, Gmass, radius, rhill) &
+                                                         bind(C, name="swg_ensemble_get_pl_masses")
+         import :: c_ptr, c_int, c_double
+         type(c_ptr), value :: ens
+         real(c_double), intent(out) :: Gmass(*), radius(*), rhill(*)
       end function
       integer(c_int) function swg_ensemble_energy(ens, out) bind(C, name="swg_ensemble_energy")
          import :: c_ptr, c_int, c_double
