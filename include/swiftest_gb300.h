@@ -223,6 +223,13 @@ int swg_ensemble_set_param(swg_ensemble *ens, double dt, double rhscale, int lcl
  * bounding-box extents, each body sweeping its own system's run; each system's list is the
  * one encounter_check_all_plpl / _pltp returns for it alone in that mode. */
 int swg_ensemble_set_encounter_modes(swg_ensemble *ens, int enc_plpl, int enc_pltp);
+/* GMTINY of param%GMTINY (swiftest_io.f90 param reader, symba_util.f90:175-208): in a SyMBA
+ * ensemble, the bodies of a system with Gmass below gmtiny (which must follow the others in
+ * its block, as Gmass-descending order leaves them) are semi-interacting: pairs of two of them
+ * are left out of the pl-pl kick and the pl-pl level-0 check, each system's count of fully
+ * interacting bodies fixed at swg_ensemble_initialize (call this before it; 0 = none).  Such
+ * ensembles take the TRIANGULAR pl-pl check and the mixed path's broadcast pl-pl kernel. */
+int swg_ensemble_set_gmtiny(swg_ensemble *ens, double gmtiny);
 int swg_ensemble_initialize(swg_ensemble *ens);
 int swg_ensemble_step(swg_ensemble *ens, int32_t nsteps);
 int swg_ensemble_get_pl(swg_ensemble *ens, double *rh, double *vh, int32_t *status);

@@ -363,7 +363,7 @@ class Ensemble:
     PROFILE_CLASSES = NBodySystem.PROFILE_CLASSES
 
     def __init__(self, ctx: Context, ens: dict, dt=None, rhscale=None, lclose=True, precision="FP64",
-                 encounter_check_plpl="TRIANGULAR", encounter_check_pltp="TRIANGULAR"):
+                 encounter_check_plpl="TRIANGULAR", encounter_check_pltp="TRIANGULAR", gmtiny=0.0):
         self.ctx = ctx
         lib = ctx.lib
         self.integrator = ens["integrator"].upper()
@@ -395,6 +395,8 @@ class Ensemble:
         m = (modes[encounter_check_plpl.upper()], modes[encounter_check_pltp.upper()])
         if m != (L.SWG_ENC_TRIANGULAR, L.SWG_ENC_TRIANGULAR):
             ctx.check("swg_ensemble_set_encounter_modes", lib.swg_ensemble_set_encounter_modes(h, *m))
+        if gmtiny:
+            ctx.check("swg_ensemble_set_gmtiny", lib.swg_ensemble_set_gmtiny(h, float(gmtiny)))
         ctx.check("swg_ensemble_initialize", lib.swg_ensemble_initialize(h))
 
     def step(self, nsteps: int = 1):

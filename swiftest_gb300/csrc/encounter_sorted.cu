@@ -149,7 +149,9 @@ struct WarpStage {
 // 32 receivers (no block barriers): its lanes test the bounds of 32 partner sub-tiles (32
 // bodies each) at a time against the warp's own sub-tile bound, and for every sub-tile
 // that is not apart the lanes stage its partners in the warp's shared slots and each lane
-// runs its receiver against them.
+// runs its receiver against them.  nplm (optional, GMTINY): per system the count of fully
+// interacting bodies; a pair of two bodies both at local index >= nplm[s] is not tested
+// (the reference checks plm x pl only: encounter_check_all_plplm).
 __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict__ items, const int32_t *__restrict__ poff,
                                                          const int32_t *__restrict__ tbase,
                                                          const int32_t *__restrict__ perm, const float4 *__restrict__ A,
@@ -158,7 +160,8 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
                                                          const double *__restrict__ v, const double *__restrict__ renc,
                                                          double dt, long long cap, int32_t *__restrict__ o1,
                                                          int32_t *__restrict__ o2, int32_t *__restrict__ olv,
-                                                         unsigned long long *__restrict__ count) {
+                                                         unsigned long long *__restrict__ count,
+                                                         const int32_t *__restrict__ nplm) {
     __shared__ WarpStage st_all[SQ / 32];
     const int4 w = items[blockIdx.x];
     const int s = w.x, q0 = w.y, nr = w.z;
@@ -180,6 +183,7 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
         gq = perm[o + q];
     }
     const float dtf = __double2float_ru(fabs(dt)) * (1.0f + 1e-6f);
+    const int gm = nplm ? o + nplm[s] : INT32_MAX;  // first semi-interacting body (global index)
     const int pend = qb - 1;  // partners p < q <= qb - 1
     const int nsub = (pend + 31) / 32;
     for (int u0 = 0; u0 < nsub; u0 += 32) {
@@ -207,6 +211,7 @@ __global__ void __launch_bounds__(SQ) k_encounter_sorted(const int4 *__restrict_
                 if (prefilter_reject(other, me, dtf)) continue;
                 const int gp = st.g[ii];
                 const int i = min(gp, gq), j = max(gp, gq);  // the reference's orientation, i < j
+                if (i >= gm) continue;  // both semi-interacting
                 const double xr = r[3 * (size_t)j + 0] - r[3 * (size_t)i + 0];
                 const double yr = r[3 * (size_t)j + 1] - r[3 * (size_t)i + 1];
                 const double zr = r[3 * (size_t)j + 2] - r[3 * (size_t)i + 2];
@@ -379,7 +384,8 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
                                   const double *r, const double *v, const double *renc, double dt, bool resort,
                                   int32_t *perm, float4 *F, int64_t NPL, int ntiles, const int2 *tiles,
                                   const int32_t *tbase, float4 *bounds, int nitems, const int4 *items, long long cap,
-                                  int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count) {
+                                  int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
+                                  const int32_t *nplm) {
     if (nitems <= 0 || ntiles <= 0) return SWG_OK;
     if (resort) {
         const size_t smem = radial_sort_smem(nmax);
@@ -400,7 +406,7 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
     c->launches++;
     SWG_TRY(launch_status(c, "sorted_prep"));
     k_encounter_sorted<<<nitems, SQ, 0, c->stream>>>(items, poff, tbase, perm, F, F + NPL, F + 2 * NPL, bounds, r,
-                                                     v, renc, dt, cap, o1, o2, olv, count);
+                                                     v, renc, dt, cap, o1, o2, olv, count, nplm);
     c->launches++;
     return launch_status(c, "encounter_sorted");
 }

@@ -56,6 +56,11 @@ struct swg_ensemble {
     std::vector<double> h_GMcb, h_Rcb;
     double dt = 0, rhscale = 6.5, t = 0;
     int lclose = 0, precision = SWG_FP64, initialized = 0, cb_set = 0;
+    // GMTINY (SyMBA): per system the count of fully interacting bodies (Gmass >= gmtiny,
+    // bodies ordered by Gmass descending); tiny: some system has semi-interacting bodies
+    double gmtiny = 0.0;
+    int32_t *nplm = nullptr;
+    bool tiny = false;
     // level-0 encounter checks (encounter_check_all_plpl / _pltp modes)
     int enc_plpl = SWG_ENC_TRIANGULAR, enc_pltp = SWG_ENC_TRIANGULAR;
     // sort-and-sweep: the system of every extent (pl-pl: 2 NPL; pl-tp: 2 (NPL + NTP)), built on first use
@@ -655,7 +660,8 @@ int mixed_kick(swg_ensemble *e, int k, int variant, const int4 *items, int nitem
     const float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
     if (k == 0)
         return kick_mixed_batched(e->c, variant, false, rad, nitems, items, e->poff, e->poff, e->npl, e->rh,
-                                  rad ? e->radius : nullptr, pa, pb, nullptr, acc, acc_is_zero, head, flag, phase);
+                                  rad ? e->radius : nullptr, pa, pb, nullptr, acc, acc_is_zero, head, flag, phase,
+                                  e->tiny ? e->nplm : nullptr);
     return kick_mixed_batched(e->c, variant, true, false, nitems, items, e->toff, e->poff, e->npl, e->trh, nullptr,
                               pa, pb, e->tlmask, acc, acc_is_zero, head, flag, phase);
 }
@@ -825,7 +831,8 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
         return SWG_ERR_STATE;
     }
     int v = e->force_variant;
-    if (v < 0 && k == 0) {  // pl-pl: the symmetric kernel, its strip and block size forced, cached or timed here
+    if (v < 0 && k == 0 && !e->tiny) {  // pl-pl: the symmetric kernel (it has no GMTINY rule), its shape forced,
+                                        // cached or timed here
         if (!e->it_sym) {
             int tile = e->force_tile, strip = e->force_strip, warps = e->force_warps;
             if (tile <= 0 || strip <= 0 || warps <= 0) {
@@ -886,7 +893,7 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         float4 *pa = e->kend ? e->kA2 : e->kA, *pb = e->kend ? e->kB2 : e->kB;
         SWG_TRY(kick_split_launch(c, e->NPL, e->rh, e->Gmass, R, pa, pb, flag ? e->psys : nullptr, flag, phase));
         SWG_TRY(ensure_kick_plan(e, 0, rad, head, flag, phase));
-        if (e->kv[0] == KICK_SYMMETRIC) {
+        if (e->kv[0] == KICK_SYMMETRIC) {  // never with semi-interacting bodies (ensure_kick_plan)
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
                                            e->sym_part, e->sym_ppart, head, flag, phase, nullptr, 0, e->sym_warps,
                                            e->sym_tile));
@@ -896,7 +903,7 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase, acc_is_zero);
     }
     return kick_plpl_fp64_batched(c, rad, e->n_fpl, e->it_fpl, e->poff, e->npl, e->rh, e->Gmass, R, e->ah,
-                                  acc_is_zero, flag, phase);
+                                  acc_is_zero, flag, phase, e->tiny ? e->nplm : nullptr);
 }
 
 // Runs f with the context's stream temporarily replaced (single host thread).
@@ -1213,7 +1220,8 @@ int level0_check(swg_ensemble *e, int kind, double dt, bool resort) {
     } else if (kind == 0)
         SWG_TRY(encounter_plpl_sorted_batched(c, e->nsys, e->nmax, e->poff, e->npl, e->l0_r, e->l0_v, e->renc, dt,
                                               resort, e->perm, e->eS, e->NPL, e->ntiles, e->tiles, e->tbase,
-                                              e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt));
+                                              e->bounds, e->n_esp, e->it_esp, x.rawcap, i1, i2, lv, cnt,
+                                              e->tiny ? e->nplm : nullptr));
     else  // the pl set was prepared (renc, this state) by the pl-pl check just before
         SWG_TRY(pltp_sorted_batched(c, false, pl_set(e, e->l0_r, e->l0_v, e->renc), tp_set(e, e->l0_tr, e->l0_tv),
                                     nullptr, e->n_tsp, e->it_tsp, dt, x.rawcap, i1, i2, lv, cnt, nullptr));
@@ -2083,7 +2091,7 @@ int swg_ensemble_destroy(swg_ensemble *e) {
                     e->tiles, e->bounds, e->it_esp, e->head2, e->kit[0], e->kit[1], e->it_sym, e->sym_base, e->sym_part,
                     e->it_fpl, e->it_ftp, e->head, e->pp_l, e->pt_l, e->enc_pp.raw.ptr,
                     e->enc_pp.sort.ptr, e->enc_pp.counters.ptr, e->enc_pt.raw.ptr, e->enc_pt.sort.ptr,
-                    e->enc_pt.counters.ptr, e->ext_pp, e->ext_pt, e->sas.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->close_part.ptr, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
+                    e->enc_pt.counters.ptr, e->ext_pp, e->ext_pt, e->sas.ptr, e->rec_out, e->rec_resume, e->rec_pend, e->tflag, e->ndiscard, e->rec_scratch.ptr, e->rows.ptr, e->pair_terms.ptr, e->close_part.ptr, e->nplm, e->chunks, e->sys_chunks, e->chunk_part, e->eta, e->muj, e->xj, e->vj, e->ir3h, e->ir3j, e->whm_ah0, e->iflag, e->whm_fail, e->snap, e->eout};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (e->h_flags) cudaFreeHost(e->h_flags);
@@ -2143,6 +2151,13 @@ int swg_ensemble_set_tp(swg_ensemble *e, const double *rh, const double *vh) {
     SWG_TRY(cuda_status(c, cudaMemcpyAsync(e->tvh, vh, 24 * n, cudaMemcpyHostToDevice, c->stream), "set_tp"));
     e->initialized = 0;
     return cuda_status(c, cudaStreamSynchronize(c->stream), "set_tp");
+}
+
+int swg_ensemble_set_gmtiny(swg_ensemble *e, double gmtiny) {
+    if (!e || !(gmtiny >= 0.0)) return SWG_ERR_ARG;
+    e->gmtiny = gmtiny;
+    e->initialized = 0;
+    return SWG_OK;
 }
 
 int swg_ensemble_set_param(swg_ensemble *e, double dt, double rhscale, int lclose, int precision) {
@@ -2215,6 +2230,27 @@ int swg_ensemble_initialize(swg_ensemble *e) {
         e->initialized = 1;
         return SWG_OK;
     }
+    // GMTINY (symba_util_set_renc and the nplm loop bounds; fixed at initialisation as in the
+    // single-system path): the bodies of each system with Gmass >= gmtiny, which lead its block
+    e->tiny = false;
+    if (e->integrator == SWG_SYMBA && e->gmtiny > 0.0 && e->NPL > 0) {
+        std::vector<double> Gm(e->NPL);
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(Gm.data(), e->Gmass, 8 * e->NPL, cudaMemcpyDeviceToHost, c->stream),
+                            "init"));
+        SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "init"));
+        std::vector<int32_t> m(e->nsys, 0);
+        for (int s = 0; s < e->nsys; s++) {
+            for (int i = 0; i < e->h_npl[s]; i++) m[s] += !(Gm[e->h_poff[s] + i] < e->gmtiny);
+            e->tiny = e->tiny || m[s] < e->h_npl[s];
+        }
+        if (e->tiny && e->enc_plpl == SWG_ENC_SORTSWEEP) {
+            c->err = "GMTINY ensembles take TRIANGULAR pl-pl level-0 checks";
+            return SWG_ERR_ARG;
+        }
+        if (!e->nplm) SWG_TRY(dalloc(c, &e->nplm, (size_t)e->nsys));
+        SWG_TRY(upload(c, e->nplm, m));
+    }
+    reset_kick_plans(e);  // the pl-pl kernel depends on GMTINY
     SWG_TRY(vh2vb_pl(e, false));
     SWG_TRY(tp_misc(e, CB_VB, 0.0, 5, -1));  // tp vb = vh + the central body's vb
     e->t = 0.0;

@@ -234,7 +234,9 @@ __global__ void __launch_bounds__(MBLOCK) k_kick_mixed(int nrecv, int npart, int
 // receiver is skipped as its own partner through the radius rule (RAD) or the index test.
 // Every (T, RPT) variant adds each receiver's terms in the same order (64-partner tiles in
 // partner order), so the variants give identical bits; the autotuner picks among them.
-template <bool TP, bool RAD, int T, int RPT>
+// GMT (pl-pl with GMTINY): nplm[s] fully interacting bodies per system; a pair of two bodies
+// both at index >= nplm[s] is skipped (the reference's nplm loop bounds).
+template <bool TP, bool RAD, bool GMT, int T, int RPT>
 __global__ void __launch_bounds__(T) k_kick_mixed_batched(int nitems, const int4 *__restrict__ items,
                                                          const int32_t *__restrict__ roff,
                                                          const int32_t *__restrict__ poff,
@@ -244,7 +246,8 @@ __global__ void __launch_bounds__(T) k_kick_mixed_batched(int nitems, const int4
                                                          const float4 *__restrict__ pA, const float4 *__restrict__ pB,
                                                          const int32_t *__restrict__ lmask, double *__restrict__ acc,
                                                          int acc_is_zero, unsigned *__restrict__ head,
-                                                         const int32_t *__restrict__ sys_flag, int phase) {
+                                                         const int32_t *__restrict__ sys_flag, int phase,
+                                                         const int32_t *__restrict__ nplm) {
     __shared__ float4 sA[MT];
     __shared__ float4 sB[MT];
     __shared__ int s_item;
@@ -273,9 +276,13 @@ __global__ void __launch_bounds__(T) k_kick_mixed_batched(int nitems, const int4
         }
         const int p0 = poff[s];
         const int slo = roff[s] + w.y;  // receivers in partner indexing (pl-pl: roff == poff)
-        mixed_sweep<TP, RAD, false, RPT>(p0, p0 + npart[s], gi, slo, slo + w.z, 0, sm, q, nullptr, nullptr, nullptr, pA,
-                                         pB, sA, sB,
-                                         ax, ay, az);
+        const int nm = GMT ? p0 + nplm[s] : 0;  // first semi-interacting body, partner indexing
+        if (GMT) {
+#pragma unroll
+            for (int k = 0; k < RPT; k++) sm[k] = gi[k] < nm;
+        }
+        mixed_sweep<TP, RAD, GMT, RPT>(p0, p0 + npart[s], gi, slo, slo + w.z, nm, sm, q, nullptr, nullptr, nullptr, pA,
+                                       pB, sA, sB, ax, ay, az);
 #pragma unroll
         for (int k = 0; k < RPT; k++) {
             if (!inr[k]) continue;
@@ -584,35 +591,35 @@ static constexpr KickShape KICK_SHAPES[KICK_NVARIANT] = {{64, 2}, {128, 1}, {128
 
 int kick_variant_tile(int variant) { return KICK_SHAPES[variant].threads * KICK_SHAPES[variant].rpt; }
 
-template <bool TP, bool RAD, int T, int RPT>
+template <bool TP, bool RAD, bool GMT, int T, int RPT>
 static int launch_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *roff, const int32_t *poff,
                           const int32_t *npart, const double *rrecv, const double *R, const float4 *pA,
                           const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero, unsigned *head,
-                          const int32_t *sys_flag, int phase) {
+                          const int32_t *sys_flag, int phase, const int32_t *nplm) {
     static int occ = 0;  // resident blocks per SM of this variant, queried once
     if (occ == 0) {
         int nb = 0;
-        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_batched<TP, RAD, T, RPT>,
-                                                                             T, 0),
+        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                   &nb, k_kick_mixed_batched<TP, RAD, GMT, T, RPT>, T, 0),
                             "occupancy"));
         occ = nb > 0 ? nb : 1;
     }
     const int grid = std::min(nitems, occ * (c->num_sms > 0 ? c->num_sms : 152));
-    k_kick_mixed_batched<TP, RAD, T, RPT><<<grid, T, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R, pA,
-                                                                      pB, lmask, acc, acc_is_zero, head, sys_flag,
-                                                                      phase);
+    k_kick_mixed_batched<TP, RAD, GMT, T, RPT><<<grid, T, 0, c->stream>>>(nitems, items, roff, poff, npart, rrecv, R,
+                                                                           pA, pB, lmask, acc, acc_is_zero, head,
+                                                                           sys_flag, phase, nplm);
     c->launches++;
     return launch_status(c, "kick_mixed_batched");
 }
 
-template <bool TP, bool RAD>
+template <bool TP, bool RAD, bool GMT>
 static int launch_variant(swg_ctx *c, int variant, int nitems, const int4 *items, const int32_t *roff,
                           const int32_t *poff, const int32_t *npart, const double *rrecv, const double *R,
                           const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc, int acc_is_zero,
-                          unsigned *head, const int32_t *sys_flag, int phase) {
+                          unsigned *head, const int32_t *sys_flag, int phase, const int32_t *nplm) {
 #define SWG_KV(T, P)                                                                                                  \
-    return launch_batched<TP, RAD, T, P>(c, nitems, items, roff, poff, npart, rrecv, R, pA, pB, lmask, acc,           \
-                                         acc_is_zero, head, sys_flag, phase)
+    return launch_batched<TP, RAD, GMT, T, P>(c, nitems, items, roff, poff, npart, rrecv, R, pA, pB, lmask, acc,      \
+                                              acc_is_zero, head, sys_flag, phase, nplm)
     switch (variant) {
         case 0: SWG_KV(64, 2);
         case 1: SWG_KV(128, 1);
@@ -630,18 +637,22 @@ static int launch_variant(swg_ctx *c, int variant, int nitems, const int4 *items
 int kick_mixed_batched(swg_ctx *c, int variant, bool tp, bool rad, int nitems, const int4 *items,
                        const int32_t *roff, const int32_t *poff, const int32_t *npart, const double *rrecv,
                        const double *R, const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc,
-                       int acc_is_zero, unsigned *head, const int32_t *sys_flag, int phase) {
+                       int acc_is_zero, unsigned *head, const int32_t *sys_flag, int phase, const int32_t *nplm) {
     if (nitems <= 0) return SWG_OK;
     if (variant < 0 || variant >= KICK_NVARIANT) return SWG_ERR_ARG;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
     if (tp)
-        return launch_variant<true, false>(c, variant, nitems, items, roff, poff, npart, rrecv, nullptr, pA, pB, lmask,
-                                           acc, acc_is_zero, head, sys_flag, phase);
+        return launch_variant<true, false, false>(c, variant, nitems, items, roff, poff, npart, rrecv, nullptr, pA, pB,
+                                                  lmask, acc, acc_is_zero, head, sys_flag, phase, nullptr);
+    if (rad && nplm)  // GMTINY (SyMBA, always with radii)
+        return launch_variant<false, true, true>(c, variant, nitems, items, roff, poff, npart, rrecv, R, pA, pB,
+                                                 nullptr, acc, acc_is_zero, head, sys_flag, phase, nplm);
+    if (nplm) return SWG_ERR_ARG;
     if (rad)
-        return launch_variant<false, true>(c, variant, nitems, items, roff, poff, npart, rrecv, R, pA, pB, nullptr,
-                                           acc, acc_is_zero, head, sys_flag, phase);
-    return launch_variant<false, false>(c, variant, nitems, items, roff, poff, npart, rrecv, nullptr, pA, pB, nullptr,
-                                        acc, acc_is_zero, head, sys_flag, phase);
+        return launch_variant<false, true, false>(c, variant, nitems, items, roff, poff, npart, rrecv, R, pA, pB,
+                                                  nullptr, acc, acc_is_zero, head, sys_flag, phase, nullptr);
+    return launch_variant<false, false, false>(c, variant, nitems, items, roff, poff, npart, rrecv, nullptr, pA, pB,
+                                               nullptr, acc, acc_is_zero, head, sys_flag, phase, nullptr);
 }
 
 int kick_pairs(swg_ctx *c, int32_t npl, int64_t npairs, const int32_t *k, const int32_t *i1, const int32_t *i2,

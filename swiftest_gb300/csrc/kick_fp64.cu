@@ -219,8 +219,11 @@ __global__ void __launch_bounds__(FT) k_kick_tp_fp64(int ntp, int npl, const dou
 
 // Batched (ensemble) forms: block b takes item b = (system s, first receiver r0) of a
 // table sorted by cost; system s's pl occupy [poff[s], poff[s] + npl[s]) and its tp
-// [toff[s], toff[s] + ntp[s]).  Every system is fully interacting (KICK_DIRECT).  With
-// sys_flag, the pl-pl form kicks only systems whose flag equals `phase`.
+// [toff[s], toff[s] + ntp[s]).  nplm (optional): per system the count of fully
+// interacting bodies (GMTINY, SyMBA), which selects the reference's loop shape as the single
+// system does (KICK_SPLIT when the semi-interacting bodies outnumber the others); without
+// it every system is fully interacting (KICK_DIRECT).  With sys_flag, the pl-pl form kicks
+// only systems whose flag equals `phase`.
 template <bool RAD, int RT>
 __global__ void __launch_bounds__(FT) k_kick_plpl_fp64_batched(const int4 *__restrict__ items,
                                                               const int32_t *__restrict__ poff,
@@ -229,12 +232,16 @@ __global__ void __launch_bounds__(FT) k_kick_plpl_fp64_batched(const int4 *__res
                                                               const double *__restrict__ Gm,
                                                               const double *__restrict__ R, double *__restrict__ acc,
                                                               int acc_is_zero, const int32_t *__restrict__ sys_flag,
-                                                              int phase) {
+                                                              int phase, const int32_t *__restrict__ nplm) {
     const int4 w = items[blockIdx.x];
     if (sys_flag && sys_flag[w.x] != phase) return;  // another launch's system
-    const int o = poff[w.x], n = npl[w.x];
-    fp64_plpl_group<RAD, KICK_DIRECT, RT>(n, n, r + 3 * (size_t)o, Gm + o, RAD ? R + o : nullptr, acc + 3 * (size_t)o,
-                                          acc_is_zero, w.y);
+    const int o = poff[w.x], n = npl[w.x], m = nplm ? nplm[w.x] : n;
+    if (n - m > m)  // block-uniform
+        fp64_plpl_group<RAD, KICK_SPLIT, RT>(n, m, r + 3 * (size_t)o, Gm + o, RAD ? R + o : nullptr,
+                                             acc + 3 * (size_t)o, acc_is_zero, w.y);
+    else
+        fp64_plpl_group<RAD, KICK_DIRECT, RT>(n, m, r + 3 * (size_t)o, Gm + o, RAD ? R + o : nullptr,
+                                              acc + 3 * (size_t)o, acc_is_zero, w.y);
 }
 
 template <int RT>
@@ -287,14 +294,14 @@ int kick_tp_fp64(swg_ctx *c, int32_t ntp, int32_t npl, const double *rtp, const 
 
 int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const double *r, const double *Gm, const double *R, double *acc,
-                           int acc_is_zero, const int32_t *sys_flag, int phase) {
+                           int acc_is_zero, const int32_t *sys_flag, int phase, const int32_t *nplm) {
     if (nitems <= 0) return SWG_OK;
     if (rad)
         k_kick_plpl_fp64_batched<true, FP64_RT><<<nitems, FT, 0, c->stream>>>(items, poff, npl, r, Gm, R, acc,
-                                                                              acc_is_zero, sys_flag, phase);
+                                                                              acc_is_zero, sys_flag, phase, nplm);
     else
         k_kick_plpl_fp64_batched<false, FP64_RT><<<nitems, FT, 0, c->stream>>>(items, poff, npl, r, Gm, nullptr, acc,
-                                                                               acc_is_zero, sys_flag, phase);
+                                                                               acc_is_zero, sys_flag, phase, nplm);
     c->launches++;
     return launch_status(c, "kick_plpl_fp64_batched");
 }

@@ -172,10 +172,12 @@ int kick_variant_tile(int variant);
 int kick_mixed_batched(swg_ctx *c, int variant, bool tp, bool rad, int nitems, const int4 *items,
                        const int32_t *roff, const int32_t *poff, const int32_t *npart, const double *rrecv,
                        const double *R, const float4 *pA, const float4 *pB, const int32_t *lmask, double *acc,
-                       int acc_is_zero, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0);
+                       int acc_is_zero, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0,
+                       const int32_t *nplm = nullptr);
 int kick_plpl_fp64_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const double *r, const double *Gm, const double *R, double *acc,
-                           int acc_is_zero, const int32_t *sys_flag = nullptr, int phase = 0);
+                           int acc_is_zero, const int32_t *sys_flag = nullptr, int phase = 0,
+                           const int32_t *nplm = nullptr);
 int kick_tp_fp64_batched(swg_ctx *c, int nitems, const int4 *items, const int32_t *toff, const int32_t *ntp,
                          const int32_t *poff, const int32_t *npl, const double *rtp, const double *rpl,
                          const double *Gm, const int32_t *lmask, double *acc, int acc_is_zero);
@@ -298,7 +300,8 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
                                   const double *r, const double *v, const double *renc, double dt, bool resort,
                                   int32_t *perm, float4 *F, int64_t NPL, int ntiles, const int2 *tiles,
                                   const int32_t *tbase, float4 *bounds, int nitems, const int4 *items, long long cap,
-                                  int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count);
+                                  int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
+                                  const int32_t *nplm = nullptr);
 
 // One set of bodies (pl or tp) of CSR-packed systems ordered by |r| per system, for the
 // radius-sorted checks: offsets and counts, positions, velocities, encounter radii (nullptr:

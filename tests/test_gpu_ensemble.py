@@ -435,3 +435,69 @@ def test_stream_schedules_match_serial(ctx, integrator):
         assert stats["plpl_encounters"] > 0
     if integrator == "SYMBA_COLL":
         assert stats["collisions"] > 0
+
+
+def _gmtiny_ensemble():
+    # compact disks with a GMTINY threshold at each system's median G*m: the lighter half of
+    # every system (which the Gmass-descending order puts last) is semi-interacting
+    E = _compact("C4", nsys=4, scale=0.05, tp_per_pl=1)
+    gmtiny = float(np.median(E["pl"]["Gmass"]))
+    return E, gmtiny
+
+
+def test_symba_gmtiny_fp64_bitexact(ctx):
+    # GMTINY (symba_util.f90:175-208 and the nplm loop bounds): single systems and one ensemble,
+    # each system against the oracle stepping it alone (FP64, bit for bit, level-0 lists too)
+    from swiftest_gb300.api import NBodySystem
+    E, gmtiny = _gmtiny_ensemble()
+    kw = dict(dt=0.005, rhscale=3.0)
+    cb = {"Gmass": IC.GMCB, "radius": IC.RCB}
+    refs = [O.OracleSystem("SYMBA", cb, pl, tp, gmtiny=gmtiny, **kw) for pl, tp in E["systems"]]
+    ens = Ensemble(ctx, E, precision="FP64", gmtiny=gmtiny, **kw)
+    singles = [NBodySystem(ctx, "SYMBA", cb, pl, tp, gmtiny=gmtiny, precision="FP64", **kw) for pl, tp in E["systems"]]
+    for _ in range(4):
+        ens.step(25)
+        for s, ref in enumerate(refs):
+            ref.step(25)
+            singles[s].step(25)
+            ri = ref.plpl_list()
+            assert all(np.array_equal(a, b) for a, b in zip(ens.plpl_list(s), ri)), s
+            assert all(np.array_equal(a, b) for a, b in zip(singles[s].plpl_list(), ri)), s
+    assert _check_states(ens, refs)
+    for s, ref in enumerate(refs):
+        assert np.array_equal(singles[s].get_pl()[0], ref.get_pl()[0]), s
+        assert np.array_equal(singles[s].get_tp()[0], ref.get_tp()[0]), s
+        singles[s].close()
+    assert ens.stats()["plpl_encounters"] > 0
+
+
+def test_symba_gmtiny_mixed(ctx):
+    # the mixed path with GMTINY: the broadcast pl-pl kernel with the semi-interacting rule
+    # (within the mixed-kick tolerance of the oracle's nplm kick) and the energy error within
+    # 2x of the FP64 path's
+    E, gmtiny = _gmtiny_ensemble()
+    kw = dict(dt=0.005, rhscale=3.0)
+    m = Ensemble(ctx, E, precision="MIXED", gmtiny=gmtiny, **kw)
+    g = m.getacch_int_pl()
+    assert m.kick_variant()["pl"] != L.SWG_KICK_SYMMETRIC
+    for s, (pl, _) in enumerate(E["systems"]):
+        nplm = int(np.sum(pl["Gmass"] >= gmtiny))
+        assert nplm < len(pl["Gmass"])
+        r = O.kick_tri_pl(pl["rh"], pl["Gmass"], pl["radius"], nplm=nplm)
+        a, b = m.poff[s], m.poff[s + 1]
+        e = np.linalg.norm(g[a:b] - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
+        assert e.max() < 2e-5, (s, e.max())
+    f = Ensemble(ctx, E, precision="FP64", gmtiny=gmtiny, **kw)
+    e0 = f.energy()
+    f.step(200)
+    m.step(200)
+    ef, em = f.energy(), m.energy()
+    dEf = np.abs(ef["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
+    dEm = np.abs(em["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
+    assert np.all(dEm < np.maximum(2 * dEf, 1e-9)), (dEm, dEf)
+
+
+def test_gmtiny_ensemble_rejects_sortsweep(ctx):
+    E, gmtiny = _gmtiny_ensemble()
+    with pytest.raises(L.SwiftestGB300Error):
+        Ensemble(ctx, E, precision="FP64", gmtiny=gmtiny, encounter_check_plpl="SORTSWEEP")
