@@ -544,8 +544,11 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
     const int32_t *pi1 = a.pp, *pi2 = a.pp + a.ppcap, *pst = a.pp + 3 * a.ppcap;
     const int32_t *ti1 = a.pt, *ti2 = a.pt + a.ptcap, *tst = a.pt + 3 * a.ptcap;
     const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
-    // good flags and per-pair terms of both signs
-    for (int64_t k = spread_tid(); k < npp + npt; k += blockDim.x) {
+    // good flags and per-pair terms of both signs; three items per pair, one per vector
+    // component c (each forms the pair's factors and writes only its component's terms)
+    for (int64_t kc = spread_tid(); kc < 3 * (npp + npt); kc += blockDim.x) {
+        const int64_t k = kc / 3;
+        const int c = (int)(kc - 3 * k);
         const bool isp = k < npp;
         const int64_t q = isp ? k : k - npp;
         const int i = (isp ? pi1 : ti1)[q] - 1, j = (isp ? pi2 : ti2)[q] - 1;
@@ -555,8 +558,10 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
         else
             g = do_pt && (tst[q] == ST_ACTIVE) && (a.levelg[i] >= irm1) && (a.tlevelg[j] >= irm1);
         if (!g) {
-            a.good[k] = 0;
-            a.good2[k] = 0;
+            if (c == 0) {
+                a.good[k] = 0;
+                a.good2[k] = 0;
+            }
             continue;
         }
         double base;
@@ -574,8 +579,10 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
                                  : dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
         const bool kp = !(r2 < ri_p * (RSHELL * RSHELL));
         const bool km = both && !(r2 < ri_m * (RSHELL * RSHELL));
-        a.good[k] = kp ? 1 : 2;
-        a.good2[k] = both ? (km ? 1 : 2) : 0;
+        if (c == 0) {
+            a.good[k] = kp ? 1 : 2;
+            a.good2[k] = both ? (km ? 1 : 2) : 0;
+        }
         if (!kp && !km) continue;
         const bool shp = kp && r2 < ri_p, shm = km && r2 < ri_m;
         // FP64 path: IEEE square root and divide, and the correctly rounded r^-1.5 shared
@@ -601,6 +608,7 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
             return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         };
         double *t = &a.terms[12 * k];
+        const double dc = c == 0 ? dx[0] : (c == 1 ? dx[1] : dx[2]);
         for (int sg = 0; sg < 2; sg++) {
             if (!(sg == 0 ? kp : km)) continue;
             const bool sh = sg == 0 ? shp : shm;
@@ -609,22 +617,23 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
             const double faci = fac * a.Gm[i];
             if (isp) {
                 const double facj = fac * a.Gm[j];
-                for (int d = 0; d < 3; d++) {
-                    ts[d] = facj * dx[d];
-                    ts[3 + d] = faci * dx[d];
-                }
+                ts[c] = facj * dc;
+                ts[3 + c] = faci * dc;
             } else {
-                for (int d = 0; d < 3; d++) ts[d] = faci * dx[d];
+                ts[c] = faci * dc;
             }
         }
     }
     __syncthreads();
-    // ordered per-body accumulation and the velocity kicks, +1 then -1
-    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
+    // ordered per-body accumulation and the velocity kicks, +1 then -1; three items per body,
+    // one per vector component (each component's additions in list order, as one thread for
+    // all three would make them)
+    for (int bc = spread_tid(); bc < 3 * (nbpl + nbtp); bc += blockDim.x) {
+        const int b = bc / 3, c = bc - 3 * b;
         const bool isp = b < nbpl;
         const int body = isp ? a.bpl[b] : a.btp[b - nbpl];
         bool zeroed[2] = {false, false}, kicked[2] = {false, false};
-        double ax[2] = {0.0, 0.0}, ay[2] = {0.0, 0.0}, az[2] = {0.0, 0.0};
+        double ac[2] = {0.0, 0.0};
         const int e0 = b == 0 ? 0 : a.adj_end[b - 1], e1 = a.adj_end[b];
         for (int e = e0; e < e1; e++) {
             const int k = a.adj[e];
@@ -638,35 +647,17 @@ static __device__ void blk_kick_lists(const RecArgs &a, int nbpl, int nbtp, doub
                 zeroed[sg] = true;
                 if (g != 1) continue;
                 kicked[sg] = true;
-                const double *t = &a.terms[12 * k + 6 * sg + off];
-                if (sub) {
-                    ax[sg] = ax[sg] - t[0];
-                    ay[sg] = ay[sg] - t[1];
-                    az[sg] = az[sg] - t[2];
-                } else {
-                    ax[sg] = ax[sg] + t[0];
-                    ay[sg] = ay[sg] + t[1];
-                    az[sg] = az[sg] + t[2];
-                }
+                const double tc = a.terms[12 * k + 6 * sg + off + c];
+                ac[sg] = sub ? ac[sg] - tc : ac[sg] + tc;
             }
         }
-        double *v = isp ? &a.vb[3 * body] : &a.tvb[3 * body];
-        double *acc = isp ? &a.ah[3 * body] : &a.tah[3 * body];
+        double *v = isp ? &a.vb[3 * body + c] : &a.tvb[3 * body + c];
+        double *acc = isp ? &a.ah[3 * body + c] : &a.tah[3 * body + c];
         for (int sg = 0; sg < 2; sg++) {
             if (!zeroed[sg]) continue;
             const double sdt = sg == 0 ? dt : -dt;
-            if (kicked[sg]) {
-                if (a.fast) {
-                    v[0] = fma(sdt, ax[sg], v[0]);
-                    v[1] = fma(sdt, ay[sg], v[1]);
-                    v[2] = fma(sdt, az[sg], v[2]);
-                } else {
-                    v[0] = v[0] + sdt * ax[sg];
-                    v[1] = v[1] + sdt * ay[sg];
-                    v[2] = v[2] + sdt * az[sg];
-                }
-            }
-            acc[0] = acc[1] = acc[2] = 0.0;
+            if (kicked[sg]) *v = a.fast ? fma(sdt, ac[sg], *v) : *v + sdt * ac[sg];
+            *acc = 0.0;
         }
     }
     __syncthreads();
@@ -1118,13 +1109,20 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
     const double rs2 = a.rhscale * a.rhscale;
     const double shell_p = pw[2 * irec], shell_m = pw[2 * (irec - 1)];
     const bool do_pp = a.npl > 0, do_pt = a.npl > 0 && a.ntp > 0;
-    for (int64_t k = spread_tid(); k < n; k += blockDim.x) {
+    // three items per pair, one per vector component c: each forms the pair's factors (the
+    // same instructions in every lane, which costs a warp no more FP64 issue than one lane)
+    // and writes only its component's terms
+    for (int64_t kc = spread_tid(); kc < 3 * n; kc += blockDim.x) {
+        const int64_t k = kc / 3;
+        const int c = (int)(kc - 3 * k);
         const bool isp = k < npp;
         const int b1 = S.s1[k], b2 = S.s2[k];
         const bool g = (isp ? do_pp : do_pt) && (S.est[k] == ST_ACTIVE) && (S.lev[b1] >= irm1) && (S.lev[b2] >= irm1);
         if (!g) {
-            S.good[k] = 0;
-            S.good2[k] = 0;
+            if (c == 0) {
+                S.good[k] = 0;
+                S.good2[k] = 0;
+            }
             continue;
         }
         double base;
@@ -1141,8 +1139,10 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
                                  : dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
         const bool kp = !(r2 < ri_p * (RSHELL * RSHELL));
         const bool km = both && !(r2 < ri_m * (RSHELL * RSHELL));
-        S.good[k] = kp ? 1 : 2;
-        S.good2[k] = both ? (km ? 1 : 2) : 0;
+        if (c == 0) {
+            S.good[k] = kp ? 1 : 2;
+            S.good2[k] = both ? (km ? 1 : 2) : 0;
+        }
         if (!kp && !km) continue;
         const bool shp = kp && r2 < ri_p, shm = km && r2 < ri_m;
         double r, ir3;
@@ -1165,6 +1165,7 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
             return p * (1.0 - 3.0 * (rr * rr) + 2.0 * (rr * rr * rr));
         };
         double *t = &S.terms[12 * k];
+        const double dc = c == 0 ? dx[0] : (c == 1 ? dx[1] : dx[2]);
         for (int sg = 0; sg < 2; sg++) {
             if (!(sg == 0 ? kp : km)) continue;
             const bool sh = sg == 0 ? shp : shm;
@@ -1173,20 +1174,22 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
             const double faci = fac * S.gm[b1];
             if (isp) {
                 const double facj = fac * S.gm[b2];
-                for (int d = 0; d < 3; d++) {
-                    ts[d] = facj * dx[d];
-                    ts[3 + d] = faci * dx[d];
-                }
+                ts[c] = facj * dc;
+                ts[3 + c] = faci * dc;
             } else {
-                for (int d = 0; d < 3; d++) ts[d] = faci * dx[d];
+                ts[c] = faci * dc;
             }
         }
     }
     __syncthreads();
-    for (int b = spread_tid(); b < nbpl + nbtp; b += blockDim.x) {
+    // three items per body, one per vector component c: each adds its component of the
+    // body's terms in list order (the same additions as one thread for all three, so the
+    // same bits) and applies its component's velocity kicks
+    for (int bc = spread_tid(); bc < 3 * (nbpl + nbtp); bc += blockDim.x) {
+        const int b = bc / 3, c = bc - 3 * b;
         const bool isp = b < nbpl;
         bool zeroed[2] = {false, false}, kicked[2] = {false, false};
-        double ax[2] = {0.0, 0.0}, ay[2] = {0.0, 0.0}, az[2] = {0.0, 0.0};
+        double ac[2] = {0.0, 0.0};
         const int e0 = b == 0 ? 0 : S.adj_end[b - 1], e1 = S.adj_end[b];
         for (int e = e0; e < e1; e++) {
             const int k = S.adj[e];
@@ -1198,35 +1201,17 @@ static __device__ void stg_kick_lists(const RecArgs &a, const RecStage &S, int n
                 zeroed[sg] = true;
                 if (g != 1) continue;
                 kicked[sg] = true;
-                const double *t = &S.terms[12 * k + 6 * sg + off];
-                if (sub) {
-                    ax[sg] = ax[sg] - t[0];
-                    ay[sg] = ay[sg] - t[1];
-                    az[sg] = az[sg] - t[2];
-                } else {
-                    ax[sg] = ax[sg] + t[0];
-                    ay[sg] = ay[sg] + t[1];
-                    az[sg] = az[sg] + t[2];
-                }
+                const double tc = S.terms[12 * k + 6 * sg + off + c];
+                ac[sg] = sub ? ac[sg] - tc : ac[sg] + tc;
             }
         }
-        double *v = &S.v[3 * b];
-        double *acc = isp ? &a.ah[3 * S.gidx[b]] : &a.tah[3 * S.gidx[b]];
+        double *v = &S.v[3 * b + c];
+        double *acc = isp ? &a.ah[3 * S.gidx[b] + c] : &a.tah[3 * S.gidx[b] + c];
         for (int sg = 0; sg < 2; sg++) {
             if (!zeroed[sg]) continue;
             const double sdt = sg == 0 ? dt : -dt;
-            if (kicked[sg]) {
-                if (a.fast) {
-                    v[0] = fma(sdt, ax[sg], v[0]);
-                    v[1] = fma(sdt, ay[sg], v[1]);
-                    v[2] = fma(sdt, az[sg], v[2]);
-                } else {
-                    v[0] = v[0] + sdt * ax[sg];
-                    v[1] = v[1] + sdt * ay[sg];
-                    v[2] = v[2] + sdt * az[sg];
-                }
-            }
-            acc[0] = acc[1] = acc[2] = 0.0;
+            if (kicked[sg]) *v = a.fast ? fma(sdt, ac[sg], *v) : *v + sdt * ac[sg];
+            *acc = 0.0;
         }
     }
     __syncthreads();
