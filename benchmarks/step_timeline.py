@@ -77,8 +77,8 @@ MARKS = {
     13: ("closing kick, linear drift, vb2vh", "main"),
     14: ("step end", "main"),
     20: ("step start", "main"),
-    21: ("level-0 checks + lists", "main"),
-    22: ("opening sums + pl kick", "main"),
+    21: ("level-0 lists joined (opening sums + pl accelerations beside them)", "main"),
+    22: ("opening pl kick applied", "main"),
     23: ("pl drift", "main"),
     24: ("tp opening half-step", "side"),
     25: ("recursion", "main"),
@@ -155,8 +155,8 @@ def _patch_system(s: str) -> str:
         assert s.count(a) == 1, f"system source changed near: {a[:70]!r}"
         s = s.replace(a, b)
     rep("using namespace swg::sdev;\n", "using namespace swg::sdev;\nvoid swg_tr(cudaStream_t st, int id);\n")
-    rep("    SWG_TRY(kick_vb_pl(s, dth, 1, !fork));\n    SWG_TRY(drift_pl(s, dt));\n",
-        "    SWG_TRY(kick_vb_pl(s, dth, 1, !fork));\n    swg_tr(c->stream, 22);\n    SWG_TRY(drift_pl(s, dt));\n"
+    rep("    SWG_TRY(kick_vb_pl(s, dth, 1, !fork, opened));\n    SWG_TRY(drift_pl(s, dt));\n",
+        "    SWG_TRY(kick_vb_pl(s, dth, 1, !fork, opened));\n    swg_tr(c->stream, 22);\n    SWG_TRY(drift_pl(s, dt));\n"
         "    swg_tr(c->stream, 23);\n")
     rep("            return drift_tp(s, dt);\n        }));\n",
         "            SWG_TRY(drift_tp(s, dt));\n            swg_tr(c->stream, 24);\n            return SWG_OK;\n        }));\n")
@@ -170,8 +170,8 @@ def _patch_system(s: str) -> str:
     rep("    s->lfirst_tp = s->lfirstkick;\n    s->lfirst_pl = s->lfirstkick;\n    int lany = 0;\n",
         "    swg_tr(c->stream, 20);\n    s->lfirst_tp = s->lfirstkick;\n    s->lfirst_pl = s->lfirstkick;\n"
         "    int lany = 0;\n")
-    rep("        SWG_TRY(symba_level0(s, dt, &lany));\n    }\n",
-        "        SWG_TRY(symba_level0(s, dt, &lany));\n    }\n    swg_tr(c->stream, 21);\n")
+    rep("    SWG_TRY(join(c, s->side, c->stream, s->ev[5]));\n    if (lany) {",
+        "    SWG_TRY(join(c, s->side, c->stream, s->ev[5]));\n    swg_tr(c->stream, 21);\n    if (lany) {")
     rep("    s->lfirstkick = s->lfirst_pl;\n    return SWG_OK;\n}",
         "    s->lfirstkick = s->lfirst_pl;\n    swg_tr(c->stream, 28);\n    return SWG_OK;\n}")
     return s

@@ -72,11 +72,12 @@ struct swg_system {
     EncWork enc, enc2;
     // scratch
     DevBuf kick_scratch, kick_scratch_tp, pair_scratch, flags, red;
-    // SyMBA with test particles: their half-steps run on a second stream beside the
-    // massive bodies' (events: 0 opening ready, 1 tp opening done, 2 closing ready,
-    // 3 central-body drift ready, 4 tp closing done)
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // SyMBA: the level-0 checks and the test particles' half-steps run on a second stream
+    // beside the massive bodies' (events: 0 opening ready, 1 tp opening done, 2 closing
+    // ready, 3 central-body drift ready, 4 tp closing done, 5 level-0 lists ready)
+    cudaStream_t side = nullptr, side2 = nullptr;  // side2: the pl-tp check beside the pl-pl one on side
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    DevBuf snap;  // the start-of-step rh, vb, trh, tvb that the overlapped level-0 checks read
     int32_t *h_flags = nullptr;  // pinned: [0] lencounter, [1] nfail, [2] recursion status, [3] deepest level,
                                  // [4] collision pending
     int32_t *mark_pl = nullptr, *mark_tp = nullptr, *rec_out = nullptr, *rec_resume = nullptr;
@@ -319,10 +320,11 @@ int accel_int_pl(swg_system *s, int acc_is_zero) {
 // helio_kick_vb_pl (helio_kick.f90:91-132) with symba_kick_getacch_pl (symba_kick.f90:36-76);
 // copy_r: record the positions as the step's start (lbeg) or end positions for the test
 // particles' kick (a caller that already copied them passes false)
-int kick_vb_pl(swg_system *s, double dt, int lbeg, bool copy_r = true) {
+// (have_acc: the pair accelerations are already in ah)
+int kick_vb_pl(swg_system *s, double dt, int lbeg, bool copy_r = true, bool have_acc = false) {
     swg_ctx *c = s->c;
     if (s->npl == 0) return SWG_OK;
-    {
+    if (!have_acc) {
         ProfScope ps(s->prof, s->c->stream, PROF_KICK_PL);
         SWG_TRY(accel_int_pl(s, 1));
     }
@@ -445,16 +447,17 @@ int drift_tp(swg_system *s, double dt) {
 }
 
 // helio_step_pl / _tp (helio_step.f90:37-119) via whm_step_system (whm_step.f90:14-35)
-int helio_step(swg_system *s, double dt) {
+// opened: the opening sums and the pl-pl accelerations already ran (symba_step)
+int helio_step(swg_system *s, double dt, bool opened = false) {
     const double dth = 0.5 * dt;
     s->lfirst_tp = s->lfirst_pl;
     if (s->npl > 0) {
         if (s->lfirst_pl) {
-            SWG_TRY(vh2vb_pl(s));
+            if (!opened) SWG_TRY(vh2vb_pl(s));
             s->lfirst_pl = 0;
         }
-        SWG_TRY(lindrift_pl(s, dth, 1));
-        SWG_TRY(kick_vb_pl(s, dth, 1));
+        if (!opened) SWG_TRY(lindrift_pl(s, dth, 1));
+        SWG_TRY(kick_vb_pl(s, dth, 1, true, opened));
         SWG_TRY(drift_pl(s, dt));
         SWG_TRY(kick_vb_pl(s, dth, 0));
         SWG_TRY(lindrift_pl(s, dth, 0));
@@ -576,6 +579,7 @@ int on_stream(swg_ctx *c, cudaStream_t st, F f) {
 int ensure_side(swg_system *s) {
     if (s->side) return SWG_OK;
     SWG_TRY(cuda_status(s->c, cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "side stream"));
+    SWG_TRY(cuda_status(s->c, cudaStreamCreateWithFlags(&s->side2, cudaStreamNonBlocking), "side stream"));
     for (cudaEvent_t &e : s->ev) SWG_TRY(cuda_status(s->c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event"));
     return SWG_OK;
 }
@@ -678,7 +682,10 @@ SortedSet sorted_tp(swg_system *s, const double *r, const double *v) {
 // 238-296).  Both checks are launched before one host synchronization reads the two
 // counts; short lists are sorted, de-duplicated and turned into SyMBA encounter
 // lists (status, level, level-0 marks) by one single-block kernel each.
-int symba_level0(swg_system *s, double dt, int *lany) {
+// r, v, tr, tv: the positions and velocities the checks read (the state at the start of the
+// step, or a copy of it)
+int symba_level0(swg_system *s, double dt, int *lany, const double *r, const double *v, const double *tr,
+                 const double *tv) {
     swg_ctx *c = s->c;
     *lany = 0;
     s->plpl_n = s->pltp_n = 0;
@@ -706,24 +713,24 @@ int symba_level0(swg_system *s, double dt, int *lany) {
         SWG_TRY(cuda_status(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream), "memset"));
         if (kind == 0) {
             if (nplt == 0) {
-                SWG_TRY(encounter_launch(c, s->enc_plpl, s->npl, s->rh, s->vb, renc, s->npl, s->rh, s->vb, renc, 1, 0,
+                SWG_TRY(encounter_launch(c, s->enc_plpl, s->npl, r, v, renc, s->npl, r, v, renc, 1, 0,
                                          dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
             } else {
-                SWG_TRY(encounter_launch(c, s->enc_plpl, s->nplm, s->rh, s->vb, renc, s->nplm, s->rh, s->vb, renc, 1,
+                SWG_TRY(encounter_launch(c, s->enc_plpl, s->nplm, r, v, renc, s->nplm, r, v, renc, 1,
                                          0, dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
-                SWG_TRY(encounter_launch(c, s->enc_plpl, s->nplm, s->rh, s->vb, renc, nplt, s->rh + 3 * s->nplm,
-                                         s->vb + 3 * s->nplm, renc + s->nplm, 0, s->nplm, dt, e.rawcap, i1, i2, lv,
+                SWG_TRY(encounter_launch(c, s->enc_plpl, s->nplm, r, v, renc, nplt, r + 3 * s->nplm,
+                                         v + 3 * s->nplm, renc + s->nplm, 0, s->nplm, dt, e.rawcap, i1, i2, lv,
                                          cnt, e.sort.ptr));
             }
         } else if (s->enc_pltp == SWG_ENC_TRIANGULAR) {
             // the triangular pl-tp check over radius-sorted tiles (the same list once sorted)
-            const SortedSet pl = sorted_pl(s, s->rh, s->vb, renc), tp = sorted_tp(s, s->trh, s->tvb);
+            const SortedSet pl = sorted_pl(s, r, v, renc), tp = sorted_tp(s, tr, tv);
             SWG_TRY(sorted_set_prep(c, pl, 1, s->srt->npl_prep++ % 8 == 0, dt));
             SWG_TRY(sorted_set_prep(c, tp, 1, s->srt->ntp_prep++ % 32 == 0, dt));
             SWG_TRY(pltp_sorted_batched(c, false, pl, tp, nullptr, s->srt->nitems, s->srt->items, dt, e.rawcap, i1, i2,
                                         lv, cnt, nullptr, s->srt->pchunk));
         } else {
-            SWG_TRY(encounter_launch(c, s->enc_pltp, s->npl, s->rh, s->vb, renc, s->ntp, s->trh, s->tvb, nullptr, 0, 0,
+            SWG_TRY(encounter_launch(c, s->enc_pltp, s->npl, r, v, renc, s->ntp, tr, tv, nullptr, 0, 0,
                                      dt, e.rawcap, i1, i2, lv, cnt, e.sort.ptr));
         }
         return cuda_status(c, cudaMemcpyAsync(&h[kind], cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -731,12 +738,13 @@ int symba_level0(swg_system *s, double dt, int *lany) {
                            "count");
     };
     h[0] = h[1] = 0;
-    if (do_pp && do_pt) {  // the two checks are independent: pl-tp on the second stream
+    if (do_pp && do_pt) {  // the two checks are independent: pl-tp on another stream
         SWG_TRY(ensure_side(s));
-        SWG_TRY(join(c, c->stream, s->side, s->ev[0]));
-        SWG_TRY(on_stream(c, s->side, [&] { return launch(1); }));
+        const cudaStream_t other = c->stream == s->side ? s->side2 : s->side;
+        SWG_TRY(join(c, c->stream, other, s->ev[0]));
+        SWG_TRY(on_stream(c, other, [&] { return launch(1); }));
         SWG_TRY(launch(0));
-        SWG_TRY(join(c, s->side, c->stream, s->ev[1]));
+        SWG_TRY(join(c, other, c->stream, s->ev[1]));
     } else {
         if (do_pp) SWG_TRY(launch(0));
         if (do_pt) SWG_TRY(launch(1));
@@ -983,14 +991,17 @@ int symba_recursion(swg_system *s, double dt) {
 // central-body record, and the recursion (which moves the listed test particles) waits
 // for their opening half.  Each kernel's arithmetic is unchanged, so the results are the
 // serial order's bits.
-int symba_interp(swg_system *s, double dt) {
+// opened: the opening sums and the pl-pl accelerations already ran (symba_step).
+int symba_interp(swg_system *s, double dt, bool opened = false) {
     swg_ctx *c = s->c;
     const double dth = 0.5 * dt;
     s->irec = -1;
     const bool fork = s->ntp > 0 && s->npl > 0;
     if (fork) SWG_TRY(ensure_side(s));
-    if (s->lfirst_pl) SWG_TRY(vh2vb_pl(s));
-    SWG_TRY(lindrift_pl(s, dth, 1));
+    if (!opened) {
+        if (s->lfirst_pl) SWG_TRY(vh2vb_pl(s));
+        SWG_TRY(lindrift_pl(s, dth, 1));
+    }
     if (fork) {
         SWG_TRY(cuda_status(c, cudaMemcpyAsync(s->rbeg, s->rh, 24 * (size_t)s->npl, cudaMemcpyDeviceToDevice, c->stream),
                             "rbeg"));
@@ -1001,7 +1012,7 @@ int symba_interp(swg_system *s, double dt) {
             return drift_tp(s, dt);
         }));
     }
-    SWG_TRY(kick_vb_pl(s, dth, 1, !fork));
+    SWG_TRY(kick_vb_pl(s, dth, 1, !fork, opened));
     SWG_TRY(drift_pl(s, dt));
     if (fork) {
         SWG_TRY(join(c, s->side, c->stream, s->ev[1]));
@@ -1065,16 +1076,50 @@ int symba_step(swg_system *s, double dt) {
     s->lfirst_tp = s->lfirstkick;
     s->lfirst_pl = s->lfirstkick;
     int lany = 0;
-    {
-        ProfScope ps(s->prof, s->c->stream, PROF_ENC0);
-        SWG_TRY(symba_level0(s, dt, &lany));
+    if (s->prof.on || s->npl == 0) {
+        {
+            ProfScope ps(s->prof, s->c->stream, PROF_ENC0);
+            SWG_TRY(symba_level0(s, dt, &lany, s->rh, s->vb, s->trh, s->tvb));
+        }
+        if (lany) {
+            s->stats[0]++;
+            SWG_TRY(symba_interp(s, dt));
+        } else {
+            s->irec = -1;
+            SWG_TRY(helio_step(s, dt));
+        }
+        s->lfirstkick = s->lfirst_pl;
+        return SWG_OK;
     }
+    // The level-0 checks read a copy of the start-of-step state on the second stream while
+    // this stream runs the opening per-system sums (vh2vb on the first step, the linear
+    // drift) and the opening pair accelerations, which both the interpolated step and the
+    // HELIO step take first and which do not need the lists; the lists are joined before
+    // the encounter-pair subtraction.  Every kernel's arithmetic is unchanged.
+    SWG_TRY(ensure_side(s));
+    const size_t n = s->npl, m = s->ntp;
+    SWG_TRY(ensure(c, s->snap, sizeof(double) * 6 * (n + m)));
+    double *sr = (double *)s->snap.ptr, *sv = sr + 3 * n, *st = sv + 3 * n, *stv = st + 3 * m;
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(sr, s->rh, 24 * n, cudaMemcpyDeviceToDevice, c->stream), "snap"));
+    SWG_TRY(cuda_status(c, cudaMemcpyAsync(sv, s->vb, 24 * n, cudaMemcpyDeviceToDevice, c->stream), "snap"));
+    if (m) {
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(st, s->trh, 24 * m, cudaMemcpyDeviceToDevice, c->stream), "snap"));
+        SWG_TRY(cuda_status(c, cudaMemcpyAsync(stv, s->tvb, 24 * m, cudaMemcpyDeviceToDevice, c->stream), "snap"));
+    }
+    SWG_TRY(join(c, c->stream, s->side, s->ev[5]));
+    const double dth = 0.5 * dt;
+    if (s->lfirst_pl) SWG_TRY(vh2vb_pl(s));
+    SWG_TRY(lindrift_pl(s, dth, 1));
+    SWG_TRY(accel_int_pl(s, 1));
+    // the checks (their host synchronisation waits for the second stream only)
+    SWG_TRY(on_stream(c, s->side, [&] { return symba_level0(s, dt, &lany, sr, sv, st, stv); }));
+    SWG_TRY(join(c, s->side, c->stream, s->ev[5]));
     if (lany) {
         s->stats[0]++;
-        SWG_TRY(symba_interp(s, dt));
+        SWG_TRY(symba_interp(s, dt, true));
     } else {
         s->irec = -1;
-        SWG_TRY(helio_step(s, dt));
+        SWG_TRY(helio_step(s, dt, true));
     }
     s->lfirstkick = s->lfirst_pl;
     return SWG_OK;
@@ -1146,13 +1191,15 @@ int swg_system_destroy(swg_system *s) {
                     s->tlevelm, s->tnplenc, s->tiflag, s->dcb, s->plpl_l, s->pltp_l, s->enc.raw.ptr,
                     s->enc.sort.ptr, s->enc.counters.ptr, s->enc2.raw.ptr, s->enc2.sort.ptr, s->enc2.counters.ptr, s->kick_scratch.ptr, s->pair_scratch.ptr, s->flags.ptr,
                     s->red.ptr, s->mark_pl, s->mark_tp, s->rec_out, s->rec_resume, s->rec_scratch.ptr,
-                    s->discard_scratch.ptr, s->tflag, s->ndiscard, s->chunk_buf.ptr, s->kick_scratch_tp.ptr};
+                    s->discard_scratch.ptr, s->tflag, s->ndiscard, s->chunk_buf.ptr, s->kick_scratch_tp.ptr,
+                    s->snap.ptr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s->h_flags) cudaFreeHost(s->h_flags);
     for (cudaEvent_t e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->side) cudaStreamDestroy(s->side);
+    if (s->side2) cudaStreamDestroy(s->side2);
     s->prof.release();
     if (s->srt) {
         s->srt->release();
