@@ -609,11 +609,8 @@ int upload_vec(swg_ctx *c, T **dst, const std::vector<T> &v) {
                         "upload"));
     return cuda_status(c, cudaStreamSynchronize(c->stream), "upload");
 }
-int ensure_sorted(swg_system *s) {
-    if (s->srt) return SWG_OK;
+int build_sorted(swg_system *s, SortedOne *x) {
     swg_ctx *c = s->c;
-    SortedOne *x = new SortedOne();
-    s->srt = x;
     const std::vector<int32_t> meta = {0, s->npl, s->ntp};
     std::vector<int2> pt, tt;
     for (int p0 = 0; p0 < s->npl; p0 += ENC_BOUND_TILE) pt.push_back(make_int2(0, p0));
@@ -640,6 +637,18 @@ int ensure_sorted(swg_system *s) {
     SWG_TRY(dalloc(c, &x->tF, 3 * (size_t)s->ntp));
     SWG_TRY(dalloc(c, &x->pbounds, 2 * pt.size()));  // bounds of each tile's two 32-body halves
     return dalloc(c, &x->tbounds, 2 * tt.size());
+}
+int ensure_sorted(swg_system *s) {
+    if (s->srt) return SWG_OK;
+    SortedOne *x = new SortedOne();
+    const int rc = build_sorted(s, x);
+    if (rc != SWG_OK) {  // nothing half-built is kept
+        x->release();
+        delete x;
+        return rc;
+    }
+    s->srt = x;
+    return SWG_OK;
 }
 SortedSet sorted_pl(swg_system *s, const double *r, const double *v, const double *renc) {
     SortedOne &x = *s->srt;
