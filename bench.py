@@ -395,6 +395,7 @@ def run_path(ctx, wl, precision, steps, warmup, prof_steps=0, clocks=None):
         kv = s.kick_variant()
         plan = {"plpl": "symmetric" if kv["pl"] == 5 else f"broadcast shape {kv['pl']}",
                 "plpl_tile": s.kick_tile(), "plpl_strip": s.kick_strip(), "plpl_warps_per_block": s.kick_warps(),
+                "plpl_row_group": s.kick_group(),
                 "pltp_shape": kv["tp"]}
     s.close()
     return total_ms, launches, (prof, prof_ms), rel_energy(e0, e1), stats, plan
@@ -464,9 +465,11 @@ def reference_arm(args, world, rank):
     return 0
 
 
-def load_traffic(key):
+def load_traffic(key, plan=None):
     """DRAM bytes per launch of a kernel class from the ncu capture recorded in
-    profiles/traffic.json (bytes, the capture's command and the commit it ran), or None."""
+    profiles/traffic.json (bytes, the capture's command, the commit it ran and the kick shape
+    it captured), or None when there is none or it captured another shape than `plan` (the
+    kick shape this run used)."""
     p = ROOT / "profiles" / "traffic.json"
     try:
         rec = json.loads(p.read_text()).get(key)
@@ -474,7 +477,13 @@ def load_traffic(key):
         return None, None
     if not isinstance(rec, dict):
         return None, None
-    return rec.get("bytes_per_launch"), {k: rec.get(k) for k in ("commit", "command", "note")}
+    src = {k: rec.get(k) for k in ("commit", "command", "note", "plan")}
+    shape = rec.get("plan")
+    if plan and isinstance(shape, dict) and any(plan.get(k) != v for k, v in shape.items()):
+        src["note"] = "not used: the recorded capture is of another kick shape than this run's " + json.dumps(
+            {k: plan.get(k) for k in shape})
+        return None, src
+    return rec.get("bytes_per_launch"), src
 
 
 def main():
@@ -504,7 +513,7 @@ def main():
     # roofline of the pair kick (mixed path), from the live CUDA-event profile on the library's stream
     peak32 = ctx.probe_peak_tflops("fp32")
     peak64 = ctx.probe_peak_tflops("fp64")
-    traffic, traffic_src = load_traffic(f"kick_pl_{args.workload}")
+    traffic, traffic_src = load_traffic(f"kick_pl_{args.workload}", plan)
     roof = None
     kick = prof["kick_pl"]
     if kick["launches"]:

@@ -30,6 +30,11 @@ def main(argv=None):
     p.add_argument("--ensemble", default="C4", choices=["C4", "C3", "C3W"])
     p.add_argument("--encounter", default="TRIANGULAR", choices=["TRIANGULAR", "SORTSWEEP"],
                    help="level-0 check mode of the SyMBA cases")
+    for k, h in (("tile", "bodies per tile"), ("strip", "tiles J per item"), ("warps", "warps per block"),
+                 ("group", "tiles per row group")):
+        p.add_argument(f"--kick-{k}", type=int, default=0,
+                       help=f"ens_mixed: the symmetric pl-pl kick's {h} (0: autotuned; forcing all four skips "
+                            "the tuner's timing launches)")
     a = p.parse_args(argv)
     from swiftest_gb300 import SWG_ENC_SORTSWEEP, SWG_FP64, SWG_MIXED
     from swiftest_gb300 import build as B
@@ -65,6 +70,10 @@ def main(argv=None):
             E = IC.make_ensemble(a.ensemble, nsys=a.nsys)
         ens = Ensemble(ctx, E, precision="MIXED" if a.case.endswith("mixed") else "FP64",
                        **(enc if E["integrator"] == "SYMBA" else {}))
+        ens.set_kick_tile(a.kick_tile)
+        ens.set_kick_strip(a.kick_strip)
+        ens.set_kick_warps(a.kick_warps)
+        ens.set_kick_group(a.kick_group)
         run = lambda: ens.step(1)  # noqa: E731
     elif a.case.startswith("symba"):
         prec = "MIXED" if a.case.endswith("mixed") else "FP64"

@@ -339,6 +339,11 @@ module swiftest_gb300_mod
          type(c_ptr), value :: ens
          integer(c_int), value :: tile
       end function
+      integer(c_int) function swg_ensemble_set_kick_group(ens, group) bind(C, name="swg_ensemble_set_kick_group")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: ens
+         integer(c_int), value :: group
+      end function
       integer(c_int) function swg_ensemble_set_gmtiny(ens, gmtiny) bind(C, name="swg_ensemble_set_gmtiny")
          import :: c_ptr, c_int, c_double
          type(c_ptr), value :: ens

@@ -290,6 +290,19 @@ int swg_ensemble_set_kick_warps(swg_ensemble *ens, int warps);
  * swg_ensemble_kick_variant with kind 4 reads the tile in use (-1 before the first mixed
  * kick). */
 int swg_ensemble_set_kick_tile(swg_ensemble *ens, int tile);
+/* Tiles per row group of the symmetric pl-pl kick (no counterpart in the reference), 128-body
+ * tiles only: with 2 or 4, a block of that many warps takes each item, one receiver tile per
+ * warp against a strip of tiles J in step, and adds the warps' partner sums of each J in
+ * warp order into one pair slot per group instead of one per tile: fewer slot bytes written
+ * and read back.  The sums are grouped differently from one-row items (1), so results agree
+ * within the mixed-kick tolerance, each deterministic.  By default (0) the autotuner times
+ * groups 2 and 4 at strips 2 and 4 after the one-row shapes and takes the fastest group
+ * unless it is more than 1% slower than the best one-row shape (cached with the strip); a
+ * forced warps-per-block count or 64-body tile keeps one-row items, and a forced group of 2
+ * or 4 takes 128-body tiles unless the tile is forced.  1, 2 or 4 forces it;
+ * swg_ensemble_kick_variant with kind 5 reads the group in use (-1 before the first mixed
+ * kick; kind 3 then reads the group's block size). */
+int swg_ensemble_set_kick_group(swg_ensemble *ens, int group);
 /* swiftest_kick_getacch_int_all_tri_pl (swiftest_kick.f90:183-264) of every system from its
  * current positions, in the ensemble's precision and pair rule (radius guard for SyMBA or
  * with close-encounter checks): acc[3*NPL] on the host, zero-based sums over all pairs. */

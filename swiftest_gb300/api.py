@@ -497,6 +497,18 @@ class Ensemble:
         self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, 4, C.byref(v)))
         return int(v.value)
 
+    def set_kick_group(self, group: int = 0):
+        """Force the symmetric pl-pl kick's tiles per row group (1, 2 or 4; groups take
+        128-body tiles and a block of that many warps per item), or let the autotuner choose
+        it (0)."""
+        self.ctx.check("swg_ensemble_set_kick_group", self.ctx.lib.swg_ensemble_set_kick_group(self.h, int(group)))
+
+    def kick_group(self) -> int:
+        """Tiles per row group of the symmetric pl-pl kick in use (-1 before the first mixed kick)."""
+        v = C.c_int(-1)
+        self.ctx.check("swg_ensemble_kick_variant", self.ctx.lib.swg_ensemble_kick_variant(self.h, 5, C.byref(v)))
+        return int(v.value)
+
     def kick_warps(self) -> int:
         """Warps per block of the symmetric pl-pl kick in use (-1 before the first mixed kick)."""
         v = C.c_int(-1)

@@ -118,10 +118,11 @@ struct swg_ensemble {
     int force_variant = -1;
     // symmetric pl-pl mixed kick (the default): tile-pair items, each system's first slot, slot sums
     int4 *it_sym = nullptr;
-    int n_sym = 0, sym_strip = 1, sym_warps = 1, sym_tile = KICK_SYM_TILE;
+    int n_sym = 0, sym_strip = 1, sym_warps = 1, sym_tile = KICK_SYM_TILE, sym_group = 1;
     int force_strip = 0;  // > 0: strip length of the symmetric kick forced (0: tuned)
     int force_warps = 0;  // > 0: warps per block of the symmetric kick forced (0: tuned)
     int force_tile = 0;   // > 0: bodies per tile of the symmetric kick forced (0: tuned)
+    int force_group = 0;  // > 0: tiles per row group of the symmetric kick forced (0: tuned)
     int32_t *sym_base = nullptr;
     float *sym_part = nullptr, *sym_ppart = nullptr;  // receiver slots, then pair slots (one allocation)
     unsigned *head = nullptr;
@@ -711,14 +712,16 @@ int time_kick_variants(swg_ensemble *e, int k, bool rad, unsigned *head, const i
     return SWG_OK;
 }
 
-// The symmetric pl-pl kick's plan for row strips of `strip` tile pairs: items, per-system
-// slot bases and the receiver and pair slots (replacing any previous plan).
+// The symmetric pl-pl kick's plan for strips of `strip` tiles J against row groups of
+// e->sym_group tiles of e->sym_tile bodies: items, per-system slot bases and the receiver
+// and pair slots (replacing any previous plan).
 int build_sym_plan(swg_ensemble *e, int strip) {
     swg_ctx *c = e->c;
     std::vector<int4> items;
     std::vector<int32_t> base;
     int64_t npair = 0;
-    const int64_t nrecv = kick_sym_items(e->nsys, e->h_npl.data(), strip, items, base, &npair, e->sym_tile);
+    const int64_t nrecv =
+        kick_sym_items(e->nsys, e->h_npl.data(), strip, items, base, &npair, e->sym_tile, e->sym_group);
     SWG_TRY(put_items(e, &e->it_sym, &e->n_sym, items));
     if (e->sym_base) cudaFree(e->sym_base);
     if (e->sym_part) cudaFree(e->sym_part);
@@ -744,15 +747,33 @@ constexpr int SYM_NSTRIP = 5;
 constexpr int SYM_WARPS[] = {1, 2, 4};
 constexpr int SYM_NWARPS = 3;
 
+// Row groups (tiles per item row, one warp each) and their strips the autotuner tries for
+// the symmetric kick with 128-body tiles.  A row group writes 1/group of the pair slots of
+// one-row items, which the per-body sums read back: less DRAM traffic and L2 footprint,
+// which a kick timed alone does not show (on the C4 ensemble the slots fall from 124 MB to
+// 89 MB with groups of 2 at strip 4, and the pair kernel's DRAM bytes from 2.85x to 1.60x
+// the algorithmic bytes at the same kick time), so a group is taken unless it is more than
+// SYM_GROUP_MARGIN slower than the best one-row shape.  Strips stop at 4: a group's items
+// are coarser, and in a SyMBA step the closing kick's items that touch a body of the
+// encounter lists wait for the recursion (strip 8 kicks as fast alone, but the C4 step is
+// 1.5% slower).
+constexpr int SYM_GROUPS[] = {2, 4};
+constexpr int SYM_NGROUP = 2;
+constexpr int SYM_GROUP_STRIPS[] = {2, 4};
+constexpr int SYM_NGROUP_STRIP = 2;
+constexpr float SYM_GROUP_MARGIN = 1.01f;
+
 // Times the symmetric kick (pair kernel and per-body sums into scratch accelerations) on
 // this ensemble's current data: first the two tile sizes (128 and 64 bodies, each at its
 // default strip), then every candidate strip at the chosen tile with one warp per block,
 // then (128-body tiles) every candidate block size at the chosen strip; each candidate one
 // warm-up, then the shortest of five launches timed one by one.  The defaults (128 bodies,
 // kick_sym_strip's strip, one warp) stay unless another candidate is faster by more than
-// 3%, so that timing noise does not move the choice between near-equal candidates; the
+// 3%, so that timing noise does not move the choice between near-equal candidates.  Last
+// (128-body tiles) the row groups at their strips, taken as described at SYM_GROUPS.  The
 // partners must be split into kA/kB.
-int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int *best_strip, int *best_warps) {
+int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int *best_strip, int *best_warps,
+                  int *best_group) {
     swg_ctx *c = e->c;
     TuneScratch t;
     SWG_TRY(dalloc(c, &t.acc, 3 * (size_t)e->NPL));
@@ -762,9 +783,9 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int
         auto once = [&]() -> int {
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
                                            e->sym_part, e->sym_ppart, head, nullptr, 0, nullptr, 0, warps,
-                                           e->sym_tile));
+                                           e->sym_tile, e->sym_group));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                         e->sym_ppart, t.acc, 1, nullptr, 0, e->sym_tile);
+                                         e->sym_ppart, t.acc, 1, nullptr, 0, e->sym_tile, e->sym_group);
         };
         SWG_TRY(once());
         *out = 3.0e38f;
@@ -781,6 +802,7 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int
     };
     // tile size: 128 unless 64 is more than 3% faster, each at its default strip
     float ms_tile[2];
+    e->sym_group = 1;
     for (int q = 0; q < 2; q++) {
         e->sym_tile = q == 0 ? KICK_SYM_TILE : 64;
         SWG_TRY(build_sym_plan(e, kick_sym_strip(e->nsys, e->h_npl.data(), c->num_sms, e->sym_tile)));
@@ -813,6 +835,29 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int
             *best_warps = SYM_WARPS[q];
         }
     }
+    *best_group = 1;
+    if (e->sym_tile == KICK_SYM_TILE) {
+        float group_ms = 3.0e38f;
+        int group = 1, group_strip = 0;
+        for (int a = 0; a < SYM_NGROUP; a++)
+            for (int b = 0; b < SYM_NGROUP_STRIP; b++) {
+                e->sym_group = SYM_GROUPS[a];
+                SWG_TRY(build_sym_plan(e, SYM_GROUP_STRIPS[b]));
+                float ms = 0.f;
+                SWG_TRY(timed(1, &ms));
+                if (ms < group_ms) {
+                    group_ms = ms;
+                    group = SYM_GROUPS[a];
+                    group_strip = SYM_GROUP_STRIPS[b];
+                }
+            }
+        if (group_ms <= SYM_GROUP_MARGIN * best_ms) {
+            *best_group = group;
+            *best_strip = group_strip;
+            *best_warps = group;
+        }
+        e->sym_group = 1;
+    }
     return SWG_OK;
 }
 
@@ -834,29 +879,36 @@ int ensure_kick_plan(swg_ensemble *e, int k, bool rad, unsigned *head, const int
     if (v < 0 && k == 0 && !e->tiny) {  // pl-pl: the symmetric kernel (it has no GMTINY rule), its shape forced,
                                         // cached or timed here
         if (!e->it_sym) {
-            int tile = e->force_tile, strip = e->force_strip, warps = e->force_warps;
-            if (tile <= 0 || strip <= 0 || warps <= 0) {
-                const std::string key = tune_key(c->device, rad ? "kick_sym3_rad" : "kick_sym3", size_bucket(e, 0));
-                const int l = tune_lookup(key);  // cached as log2(strip) + 8 log2(warps) + 64 (tile == 64)
-                int tt = 0, ts = 0, tw = 0;
-                if (l >= 0 && (l & 7) < SYM_NSTRIP && ((l >> 3) & 7) < SYM_NWARPS && (l >> 6) < 2) {
-                    tt = (l >> 6) ? 64 : KICK_SYM_TILE;
+            int tile = e->force_tile, strip = e->force_strip, warps = e->force_warps, group = e->force_group;
+            if (tile <= 0 || strip <= 0 || warps <= 0 || group <= 0) {
+                const std::string key = tune_key(c->device, rad ? "kick_sym4_rad" : "kick_sym4", size_bucket(e, 0));
+                // cached as log2(strip) + 8 log2(warps) + 64 (tile == 64) + 128 log2(group)
+                const int l = tune_lookup(key);
+                int tt = 0, ts = 0, tw = 0, tg = 0;
+                if (l >= 0 && (l & 7) < SYM_NSTRIP && ((l >> 3) & 7) < SYM_NWARPS && (l >> 7) <= SYM_NGROUP) {
+                    tt = ((l >> 6) & 1) ? 64 : KICK_SYM_TILE;
                     ts = 1 << (l & 7);
                     tw = 1 << ((l >> 3) & 7);
+                    tg = 1 << (l >> 7);
                 } else {
-                    SWG_TRY(time_sym_plan(e, rad, head, &tt, &ts, &tw));
-                    int ls = 0, lw = 0;
+                    SWG_TRY(time_sym_plan(e, rad, head, &tt, &ts, &tw, &tg));
+                    int ls = 0, lw = 0, lg = 0;
                     while ((1 << ls) < ts) ls++;
                     while ((1 << lw) < tw) lw++;
-                    tune_store(key, ls + 8 * lw + (tt == 64 ? 64 : 0));
+                    while ((1 << lg) < tg) lg++;
+                    tune_store(key, ls + 8 * lw + (tt == 64 ? 64 : 0) + 128 * lg);
                 }
-                if (tile <= 0) tile = tt;
+                if (tile <= 0) tile = group > 1 ? KICK_SYM_TILE : tt;  // row groups take 128-body tiles
                 if (strip <= 0) strip = ts;
                 if (warps <= 0) warps = tw;
+                if (group <= 0) group = tg;
             }
+            // a forced one-row shape (warps per block or 64-body tiles) leaves row groups out
+            if (tile != KICK_SYM_TILE || (e->force_warps > 0 && e->force_group <= 0)) group = 1;
             e->sym_tile = tile;
+            e->sym_group = group;
             SWG_TRY(build_sym_plan(e, strip));
-            e->sym_warps = tile == KICK_SYM_TILE ? warps : 1;
+            e->sym_warps = group > 1 ? group : (tile == KICK_SYM_TILE ? warps : 1);
         }
         e->kv[0] = KICK_SYMMETRIC;
         return SWG_OK;
@@ -896,9 +948,9 @@ int accel_int_pl(swg_ensemble *e, unsigned *head, const int32_t *flag = nullptr,
         if (e->kv[0] == KICK_SYMMETRIC) {  // never with semi-interacting bodies (ensure_kick_plan)
             SWG_TRY(kick_mixed_sym_batched(c, rad, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, pa, pb,
                                            e->sym_part, e->sym_ppart, head, flag, phase, nullptr, 0, e->sym_warps,
-                                           e->sym_tile));
+                                           e->sym_tile, e->sym_group));
             return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                         e->sym_ppart, e->ah, acc_is_zero, flag, phase, e->sym_tile);
+                                         e->sym_ppart, e->ah, acc_is_zero, flag, phase, e->sym_tile, e->sym_group);
         }
         return mixed_kick(e, 0, e->kv[0], e->kit[0], e->n_kit[0], e->ah, rad, head, flag, phase, acc_is_zero);
     }
@@ -1741,7 +1793,7 @@ int ens_step(swg_ensemble *e, double dt) {
             SWG_TRY(L(c, "mark_enc"));
             SWG_TRY(ensure(c, e->sym_iflag, (size_t)e->n_sym));
             SWG_TRY(kick_sym_item_flags(c, e->n_sym, e->it_sym, e->poff, e->npl, e->lany, e->enc_body,
-                                        (uint8_t *)e->sym_iflag.ptr, e->sym_tile));
+                                        (uint8_t *)e->sym_iflag.ptr, e->sym_tile, e->sym_group));
         }
         SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_fork, c->stream), "fork"));
         SWG_TRY(cuda_status(c, cudaStreamWaitEvent(e->side, e->ev_fork, 0), "fork"));
@@ -1759,9 +1811,9 @@ int ens_step(swg_ensemble *e, double dt) {
                 SWG_TRY(cuda_status(c, cudaEventRecord(e->ev_split, c->stream), "split"));
                 SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA,
                                                e->kB, e->sym_part, e->sym_ppart, e->head2, nullptr, 0, iflag, 3u,
-                                               e->sym_warps, e->sym_tile));
+                                               e->sym_warps, e->sym_tile, e->sym_group));
                 return kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base,
-                                             e->sym_part, e->sym_ppart, e->ah, 1, e->lany, 0, e->sym_tile);
+                                             e->sym_part, e->sym_ppart, e->ah, 1, e->lany, 0, e->sym_tile, e->sym_group);
             }));
         } else {
             SWG_TRY(on_stream(c, e->side, [&] { return accel_int_pl(e, e->head2, e->lany, 0); }));
@@ -1780,10 +1832,10 @@ int ens_step(swg_ensemble *e, double dt) {
                                       e->enc_body, 1));
             SWG_TRY(kick_mixed_sym_batched(c, true, e->n_sym, e->it_sym, e->poff, e->npl, e->sym_base, e->kA, e->kB,
                                            e->sym_part, e->sym_ppart, e->head, nullptr, 0, iflag, 4u, e->sym_warps,
-                                           e->sym_tile));
+                                           e->sym_tile, e->sym_group));
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
             SWG_TRY(kick_mixed_sym_reduce(c, e->sym_strip, e->NPL, e->psys, e->poff, e->npl, e->sym_base, e->sym_part,
-                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile));
+                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile, e->sym_group));
         } else {
             SWG_TRY(accel_int_pl(e, e->head, e->lany, 1));
             SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), "join"));
@@ -2487,8 +2539,10 @@ int swg_ensemble_set_kick_variant(swg_ensemble *e, int variant) {
 }
 
 int swg_ensemble_kick_variant(swg_ensemble *e, int kind, int *variant) {
-    if (!e || !variant || kind < 0 || kind > 4) return SWG_ERR_ARG;
-    if (kind == 2)
+    if (!e || !variant || kind < 0 || kind > 5) return SWG_ERR_ARG;
+    if (kind == 5)
+        *variant = e->it_sym ? e->sym_group : -1;
+    else if (kind == 2)
         *variant = e->it_sym ? e->sym_strip : -1;
     else if (kind == 3)
         *variant = e->it_sym ? e->sym_warps : -1;
@@ -2526,6 +2580,17 @@ int swg_ensemble_set_kick_tile(swg_ensemble *e, int tile) {
     if (!e || !(tile == 0 || tile == 64 || tile == 128)) return SWG_ERR_ARG;
     SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick tile"));
     e->force_tile = tile;
+    if (e->it_sym) cudaFree(e->it_sym);
+    e->it_sym = nullptr;
+    e->n_sym = 0;
+    reset_kick_plans(e);
+    return SWG_OK;
+}
+
+int swg_ensemble_set_kick_group(swg_ensemble *e, int group) {
+    if (!e || !(group == 0 || group == 1 || group == 2 || group == 4)) return SWG_ERR_ARG;
+    SWG_TRY(cuda_status(e->c, cudaStreamSynchronize(e->c->stream), "kick group"));
+    e->force_group = group;
     if (e->it_sym) cudaFree(e->it_sym);
     e->it_sym = nullptr;
     e->n_sym = 0;

@@ -32,6 +32,10 @@
 // the system's pair slot of (I, J).  A second kernel adds, for every body, its pair slots
 // (tiles below its own) and then its receiver slots, in float-float, converted to FP64
 // once.  No atomics touch the sums, so results are deterministic.
+// Row groups (k_kick_mixed_sym_grp): a block of 2 or 4 warps takes as many consecutive
+// rows against one strip, tile J by tile J, and adds its warps' partner sums of J in
+// shared memory before writing them, so that one pair slot serves the whole group: fewer
+// slot bytes to write and read back.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -129,14 +133,15 @@ __device__ __forceinline__ void rule2(f32x2 r2, f32x2 Rp, float Rk, int ja, int 
 // across lanes t and t ^ 16.  Outputs: receiver partials px.. and minus the partner sums
 // in qx.. (for this lane's partner t).  P points at the lane's first entry.
 // GUARD: the pair rule pair by pair (RAD only); else, with RAD, mn keeps the smallest r^2.
-// NR: receivers per lane (the tile's 32-body sub-tiles).
-template <bool RAD, bool GUARD, int NK, int NR>
+// NR: receivers per lane (the tile's 32-body sub-tiles); K0: the first receiver taken
+// (receivers K0 <= k < NK).
+template <bool RAD, bool GUARD, int NK, int NR, int K0 = 0>
 __device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Recv2 (&q)[NR], int src, float (&px)[NR],
                                             float (&py)[NR], float (&pz)[NR], float &qx, float &qy, float &qz,
                                             float (&mn)[NR]) {
     f32x2 ax[NK], ay[NK], az[NK];
 #pragma unroll
-    for (int k = 0; k < NK; k++) {
+    for (int k = K0; k < NK; k++) {
         ax[k] = ay[k] = az[k] = 0ull;
         mn[k] = 3.0e38f;
     }
@@ -147,7 +152,7 @@ __device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Re
     for (int s = 0; s < 16; s++) {
         const ulonglong2 h = W0[s], hz = W1[s], l = W2[s], lz = W3[s];
 #pragma unroll
-        for (int k = 0; k < NK; k++) {
+        for (int k = K0; k < NK; k++) {
             const f32x2 dx = f2_add(f2_sub(h.x, q[k].xh), f2_sub(l.x, q[k].xl));
             const f32x2 dy = f2_add(f2_sub(h.y, q[k].yh), f2_sub(l.y, q[k].yl));
             const f32x2 dz = f2_add(f2_sub(hz.x, q[k].zh), f2_sub(lz.x, q[k].zl));
@@ -172,7 +177,7 @@ __device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Re
         bz = __shfl_sync(FULL, bz, src);
     }
 #pragma unroll
-    for (int k = 0; k < NK; k++) {
+    for (int k = K0; k < NK; k++) {
         float e, o;
         f2_unpack(ax[k], e, o);
         px[k] = e + o;
@@ -190,26 +195,26 @@ __device__ __forceinline__ void sym_subtile(const SubTile &S, int lane, const Re
     qz = -(hi + __shfl_xor_sync(FULL, lo, 16));
 }
 
-// sym_subtile without the rule, then (RAD) recomputed with it when some receiver k < NK
-// may meet a partner within the radii.
-template <bool RAD, int NK, int NR>
+// sym_subtile without the rule, then (RAD) recomputed with it when some receiver
+// K0 <= k < NK may meet a partner within the radii.
+template <bool RAD, int NK, int NR, int K0 = 0>
 __device__ __forceinline__ void sym_subtile_ruled(const SubTile &S, int lane, const Recv2 (&q)[NR],
                                                   const bool (&ok)[NR], int src, float (&px)[NR], float (&py)[NR],
                                                   float (&pz)[NR], float &qx, float &qy, float &qz) {
     float mn[NR];
-    sym_subtile<RAD, false, NK, NR>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
+    sym_subtile<RAD, false, NK, NR, K0>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
     if (RAD) {
         float Ra, Rb;
         f2_unpack(S.w[3][lane].y, Ra, Rb);  // the lane's entry: partners lane and lane ^ 16
         const float rt = __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(fmaxf(Ra, Rb))));  // radii >= 0
         bool need = false;
 #pragma unroll
-        for (int k = 0; k < NK; k++) {
+        for (int k = K0; k < NK; k++) {
             const float rs = q[k].R + rt;
             need = need || (ok[k] && mn[k] <= rs * rs);
         }
         if (__any_sync(FULL, need))  // rare: a pair may lie within the radii
-            sym_subtile<RAD, true, NK, NR>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
+            sym_subtile<RAD, true, NK, NR, K0>(S, lane, q, src, px, py, pz, qx, qy, qz, mn);
     }
 }
 
@@ -365,11 +370,181 @@ __global__ void __launch_bounds__(32 * W) k_kick_mixed_sym(int nitems, const int
     }
 }
 
-// One warp per item: 0 for a system without encounters, else 2 when tile I or one of the
-// strip's tiles J holds a body marked in enc, else 1 (see kick_sym_item_flags).
+// Row groups of G tiles (128 bodies): an item is G consecutive receiver tiles
+// I0 .. I0 + G - 1 (warp w of the block holds tile I0 + w) against a strip of tiles
+// J0 .. J0 + nJ - 1 (J0 >= I0), processed one tile J at a time by the whole block: J is
+// staged once in shared memory (each warp stages G-th of its sub-tiles), every warp
+// evaluates its tile against it (I < J with the rotation, I == J as a diagonal tile,
+// I > J not at all), and the warps' partner sums of J are added in warp order into the
+// pair slot (g, J) of the row group g = I0 / G, J > I0.  A row group thus writes one pair
+// slot per tile J where rows of one tile write G, so G times fewer pair slots go to memory
+// and come back in the per-body sums.  Each warp's receiver sums of the strip go to
+// receiver slot w.w + w.  Every body's terms are the same as with one-row items, grouped
+// into different partial sums (the results agree within the mixed-kick tolerance); each
+// launch gives the same bits.
+// With G = 2 the first two tiles of a group's first strip (the diagonal block: tiles I0 and
+// I0 + 1 on themselves and against each other) are one round in which both warps work:
+// warp 0 takes diagonal tile I0 and tile I0 against sub-tiles 0-1 of tile I0 + 1, warp 1
+// diagonal tile I0 + 1 and its sub-tiles 2-3 as receivers against tile I0 (staged apart),
+// whose partner sums warp 0 adds to its receiver sums; in step, one warp would wait for the
+// other on each of these two tiles.
+template <bool RAD, int G>
+__global__ void __launch_bounds__(32 * G) k_kick_mixed_sym_grp(int nitems, const int4 *__restrict__ items,
+                                                          const int32_t *__restrict__ poff,
+                                                          const int32_t *__restrict__ npl,
+                                                          const int32_t *__restrict__ sbase,
+                                                          const float4 *__restrict__ pA,
+                                                          const float4 *__restrict__ pB, float *__restrict__ rpart,
+                                                          float *__restrict__ ppart, unsigned *__restrict__ head,
+                                                          const int32_t *__restrict__ sys_flag, int phase,
+                                                          const uint8_t *__restrict__ iflag, unsigned accept) {
+    constexpr int T = KICK_SYM_TILE, SR = T / 32;
+    static_assert(G == 2 || G == 4, "row groups of 2 or 4 tiles");
+    __shared__ SubTile sP[SR];
+    __shared__ float sq[G][3 * T];  // partner sums of the staged tile J, one row per warp
+    __shared__ unsigned s_it[2];    // item of this round (two buffers: one barrier per round)
+    __shared__ SubTile sP0[G == 2 ? SR : 1];  // G = 2: tile I0 in the diagonal round
+    __shared__ float sq0[G == 2 ? 3 * T : 1];  // G = 2: partner sums for tile I0 from warp 1
+    const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float4 pad_a = make_float4(PAD_POS, PAD_POS, PAD_POS, 0.f), zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int round = 0;; round ^= 1) {
+        if (threadIdx.x == 0) s_it[round] = atomicAdd(head, 1u);
+        __syncthreads();
+        const unsigned it = s_it[round];
+        if (it >= (unsigned)nitems) break;  // block-uniform, as are the two skips below
+        const int4 w = items[it];
+        const int s = w.x, I0 = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
+        if (sys_flag && sys_flag[s] != phase) continue;
+        if (iflag && !((accept >> iflag[it]) & 1u)) continue;
+        const int p0 = poff[s], n = npl[s], nt = (n + T - 1) / T, I = I0 + wq, g = I0 / G;
+        // pair slot (g, J) = pbase + J: the groups before g hold nt - g'G - 1 slots each
+        const int pbase = sbase[2 * s + 1] + g * (nt - 1) - G * g * (g - 1) / 2 - I0 - 1;
+        Recv2 q[SR];
+        bool ok[SR];
+#pragma unroll
+        for (int k = 0; k < SR; k++) {
+            const int i = I * T + k * 32 + lane;
+            ok[k] = i < n;
+            const float4 a = ok[k] ? pA[p0 + i] : pad_a;
+            const float4 b = ok[k] ? pB[p0 + i] : zero;
+            q[k] = Recv2{f2_pack(a.x, a.x), f2_pack(a.y, a.y), f2_pack(a.z, a.z), f2_pack(b.x, b.x),
+                         f2_pack(b.y, b.y), f2_pack(b.z, b.z), f2_pack(a.w, a.w), b.w};
+        }
+        FF ax[SR], ay[SR], az[SR];
+#pragma unroll
+        for (int k = 0; k < SR; k++) ax[k] = ay[k] = az[k] = FF{0.f, 0.f};
+        int jj0 = 0;
+        if constexpr (G == 2) {
+            if (J0 == I0 && nJ >= 2 && I0 + 1 < nt) {  // the diagonal round (block-uniform)
+                SubTile(&own)[SR] = wq == 0 ? sP0 : sP;  // warp w stages its own tile I0 + w
+#pragma unroll
+                for (int u = 0; u < SR; u++) {
+                    const int j = I * T + u * 32 + lane;
+                    const float4 a = j < n ? pA[p0 + j] : pad_a;
+                    const float4 b = j < n ? pB[p0 + j] : zero;
+                    stage_subtile(own[u], a, b, lane);
+                }
+                __syncthreads();
+                diag_subtile<RAD, 0, SR>(own, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 1, SR>(own, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 2, SR>(own, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 3, SR>(own, q, ok, lane, ax, ay, az);
+                if (wq == 0) {
+                    for (int u = 0; u < SR; u++) {
+                        float qx = 0.f, qy = 0.f, qz = 0.f;
+                        if (u < 2) {
+                            float px[SR], py[SR], pz[SR];
+                            sym_subtile_ruled<RAD, SR, SR>(sP[u], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy,
+                                                           qz);
+#pragma unroll
+                            for (int k = 0; k < SR; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
+                        }
+                        sq[0][0 * T + u * 32 + lane] = qx;
+                        sq[0][1 * T + u * 32 + lane] = qy;
+                        sq[0][2 * T + u * 32 + lane] = qz;
+                    }
+                } else {
+                    for (int u = 0; u < SR; u++) {
+                        float px[SR], py[SR], pz[SR], qx, qy, qz;
+                        sym_subtile_ruled<RAD, SR, SR, 2>(sP0[u], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy,
+                                                          qz);
+#pragma unroll
+                        for (int k = 2; k < SR; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
+                        sq0[0 * T + u * 32 + lane] = qx;
+                        sq0[1 * T + u * 32 + lane] = qy;
+                        sq0[2 * T + u * 32 + lane] = qz;
+                    }
+                }
+                __syncthreads();
+                float *o = ppart + (size_t)(pbase + I0 + 1) * 3 * T;  // pair slot (g, I0 + 1): warp 0's sums
+                for (int e = threadIdx.x; e < 3 * T; e += 32 * G) o[e] = sq[0][e];
+                if (wq == 0) {
+#pragma unroll
+                    for (int u = 0; u < SR; u++)
+                        ff_add3(ax[u], ay[u], az[u], sq0[u * 32 + lane], sq0[T + u * 32 + lane],
+                                sq0[2 * T + u * 32 + lane]);
+                }
+                jj0 = 2;
+            }
+        }
+        for (int jj = jj0; jj < nJ; jj++) {
+            const int J = J0 + jj;
+            for (int u = wq; u < SR; u += G) {
+                const int j = J * T + u * 32 + lane;
+                const float4 a = j < n ? pA[p0 + j] : pad_a;
+                const float4 b = j < n ? pB[p0 + j] : zero;
+                stage_subtile(sP[u], a, b, lane);
+            }
+            __syncthreads();  // J staged; the previous tile's partner sums are consumed
+            if (I == J) {
+                diag_subtile<RAD, 0, SR>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 1, SR>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 2, SR>(sP, q, ok, lane, ax, ay, az);
+                diag_subtile<RAD, 3, SR>(sP, q, ok, lane, ax, ay, az);
+            } else if (I < J) {
+                for (int u = 0; u < SR; u++) {
+                    float px[SR], py[SR], pz[SR], qx, qy, qz;
+                    sym_subtile_ruled<RAD, SR, SR>(sP[u], lane, q, ok, (lane + 1) & 31, px, py, pz, qx, qy, qz);
+#pragma unroll
+                    for (int k = 0; k < SR; k++) ff_add3(ax[k], ay[k], az[k], px[k], py[k], pz[k]);
+                    sq[wq][0 * T + u * 32 + lane] = qx;
+                    sq[wq][1 * T + u * 32 + lane] = qy;
+                    sq[wq][2 * T + u * 32 + lane] = qz;
+                }
+            }
+            __syncthreads();  // partner sums of J complete; the staged tile is free
+            if (J > I0) {
+                const int nw = min(G, J - I0);  // warps whose tile lies below J
+                float *o = ppart + (size_t)(pbase + J) * 3 * T;
+                for (int e = threadIdx.x; e < 3 * T; e += 32 * G) {
+                    float v = sq[0][e];
+                    for (int m = 1; m < nw; m++) v += sq[m][e];
+                    o[e] = v;
+                }
+            }
+        }
+        if (I < nt) {
+            float *o0 = rpart + (size_t)(w.w + wq) * 6 * T;
+#pragma unroll
+            for (int k = 0; k < SR; k++) {
+                const int il = k * 32 + lane;
+                o0[0 * T + il] = ax[k].hi;
+                o0[1 * T + il] = ax[k].lo;
+                o0[2 * T + il] = ay[k].hi;
+                o0[3 * T + il] = ay[k].lo;
+                o0[4 * T + il] = az[k].hi;
+                o0[5 * T + il] = az[k].lo;
+            }
+        }
+    }
+}
+
+// One warp per item: 0 for a system without encounters, else 2 when one of the item's
+// receiver tiles (grp of them from tile I) or one of the strip's tiles J holds a body
+// marked in enc, else 1 (see kick_sym_item_flags).
 __global__ void k_kick_sym_item_flags(int nitems, const int4 *__restrict__ items, const int32_t *__restrict__ poff,
                                       const int32_t *__restrict__ npl, const int32_t *__restrict__ sys_enc,
-                                      const uint8_t *__restrict__ enc, uint8_t *__restrict__ iflag, int ts) {
+                                      const uint8_t *__restrict__ enc, uint8_t *__restrict__ iflag, int ts, int grp) {
     const int it = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (it >= nitems) return;  // whole warps leave together
@@ -381,8 +556,8 @@ __global__ void k_kick_sym_item_flags(int nitems, const int4 *__restrict__ items
     }
     const int p0 = poff[s], n = npl[s];
     bool dirty = false;
-    for (int t = -1; t < nJ; t++) {
-        const int T = t < 0 ? I : J0 + t;
+    for (int t = -grp; t < nJ; t++) {
+        const int T = t < 0 ? I + grp + t : J0 + t;
         for (int k = lane; k < ts; k += 32) {
             const int i = T * ts + k;
             if (i < n && enc[p0 + i]) dirty = true;
@@ -392,31 +567,41 @@ __global__ void k_kick_sym_item_flags(int nitems, const int4 *__restrict__ items
     if (lane == 0) iflag[it] = dirty ? 2 : 1;
 }
 
-// Per body: acc (+)= its slots in a fixed order (pair slots of the tiles below its own,
-// then the receiver slots of its own row).  The slots' values are added in float-float
-// (hi parts by TwoSum, lo parts plainly) and converted to FP64 once: FP64 arithmetic per
-// slot would run on the narrow FP64 pipe and bound this kernel.
+// Per body: acc (+)= its slots in a fixed order (pair slots of the row groups below its
+// tile, in group order, then the receiver slots of its own tile's items).  The slots'
+// values are added in float-float (hi parts by TwoSum, lo parts plainly) and converted to
+// FP64 once: FP64 arithmetic per slot would run on the narrow FP64 pipe and bound this
+// kernel.  grp: tiles per row group (1: one-row items, whose pair slot (g, K) is
+// pair_slot(g, K, nt)); a group g holds nt - g grp - 1 pair slots and one item per strip
+// of its tiles J >= g grp, each item grp receiver slots.
 __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, const int32_t *__restrict__ poff,
                                   const int32_t *__restrict__ npl, const int32_t *__restrict__ sbase,
                                   const float *__restrict__ rpart, const float *__restrict__ ppart,
                                   double *__restrict__ acc, int acc_is_zero, const int32_t *__restrict__ sys_flag,
-                                  int phase, int strip, int ts) {
+                                  int phase, int strip, int ts, int grp) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= n) return;
     const int s = psys ? psys[b] : 0;
     if (sys_flag && sys_flag[s] != phase) return;
     const int i = (int)(b - poff[s]);
-    const int nt = (npl[s] + ts - 1) / ts, K = i / ts, l = i % ts;
+    const int nt = (npl[s] + ts - 1) / ts, K = i / ts, l = i % ts, gK = K / grp;
     FF fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f};
     float lx = 0.f, ly = 0.f, lz = 0.f;
-    int row = 0;  // first receiver slot of row K
-    for (int I = 0; I < K; I++) {
-        const float *o = ppart + (size_t)(sbase[2 * s + 1] + pair_slot(I, K, nt)) * 3 * ts;
-        ff_add3(fx, fy, fz, o[l], o[ts + l], o[2 * ts + l]);
-        row += (nt - I + strip - 1) / strip;
+    int pslot = sbase[2 * s + 1];  // first pair slot of group g
+    int row = 0;                   // items of the groups before gK
+    for (int g = 0; g <= gK; g++) {
+        const int I0 = g * grp;
+        if (I0 < K) {
+            const float *o = ppart + (size_t)(pslot + K - I0 - 1) * 3 * ts;
+            ff_add3(fx, fy, fz, o[l], o[ts + l], o[2 * ts + l]);
+        }
+        if (g < gK) {
+            pslot += nt - I0 - 1;
+            row += (nt - I0 + strip - 1) / strip;
+        }
     }
-    for (int m = 0; m < (nt - K + strip - 1) / strip; m++) {
-        const float *o = rpart + (size_t)(sbase[2 * s] + row + m) * 6 * ts;
+    for (int m = 0; m < (nt - gK * grp + strip - 1) / strip; m++) {
+        const float *o = rpart + ((size_t)(sbase[2 * s] + (row + m) * grp + K - gK * grp)) * 6 * ts;
         ff_add3(fx, fy, fz, o[l], o[2 * ts + l], o[4 * ts + l]);
         lx += o[ts + l];
         ly += o[3 * ts + l];
@@ -434,11 +619,11 @@ __global__ void k_kick_sym_reduce(int64_t n, const int32_t *__restrict__ psys, c
 }  // namespace
 
 int kick_sym_item_flags(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
-                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag, int tile) {
+                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag, int tile, int group) {
     if (nitems <= 0) return SWG_OK;
     const int64_t threads = (int64_t)nitems * 32;
     k_kick_sym_item_flags<<<(int)((threads + 255) / 256), 256, 0, c->stream>>>(nitems, items, poff, npl, sys_enc,
-                                                                              enc, iflag, tile);
+                                                                              enc, iflag, tile, group);
     c->launches++;
     return launch_status(c, "kick_sym_item_flags");
 }
@@ -460,7 +645,7 @@ bool kick_sym_single_ok(int32_t npl, int num_sms) {
 }
 
 int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<int4> &items,
-                       std::vector<int32_t> &sbase, int64_t *npair_slots, int tile) {
+                       std::vector<int32_t> &sbase, int64_t *npair_slots, int tile, int group) {
     items.clear();
     sbase.assign(2 * (size_t)nsys, 0);
     std::vector<int64_t> cost;
@@ -470,15 +655,23 @@ int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<
         sbase[2 * s] = (int32_t)nrs;
         sbase[2 * s + 1] = (int32_t)nps;
         auto rows = [&](int T) { return (int64_t)std::min(tile, npl[s] - T * tile); };
-        for (int I = 0; I < nt; I++)
-            for (int J0 = I; J0 < nt; J0 += strip) {
+        for (int I0 = 0; I0 < nt; I0 += group) {
+            for (int J0 = I0; J0 < nt; J0 += strip) {
                 const int nJ = std::min(strip, nt - J0);
-                items.push_back(make_int4(s, I, J0 | (nJ << 24), (int)nrs++));
+                items.push_back(make_int4(s, I0, J0 | (nJ << 24), (int)nrs));
+                nrs += group;
+                // a row group's warps go through the strip's tiles J together: each J costs
+                // the largest of its rows' shares
                 int64_t c = 0;
-                for (int J = J0; J < J0 + nJ; J++) c += rows(I) * rows(J);
+                for (int J = J0; J < J0 + nJ; J++) {
+                    int64_t m = 0;
+                    for (int I = I0; I < std::min(I0 + group, nt) && I <= J; I++) m = std::max(m, rows(I));
+                    c += m * rows(J);
+                }
                 cost.push_back(c);
             }
-        nps += (int64_t)nt * (nt - 1) / 2;
+            nps += nt - I0 - 1;
+        }
     }
     std::vector<size_t> ord(items.size());
     for (size_t k = 0; k < ord.size(); k++) ord[k] = k;
@@ -507,17 +700,41 @@ int sym_launch(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, c
     return SWG_OK;
 }
 
+template <bool RAD, int G>
+int sym_grp_launch(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
+                   const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart, float *ppart, unsigned *head,
+                   const int32_t *sys_flag, int phase, const uint8_t *iflag, unsigned accept) {
+    static int o = 0;  // resident blocks per SM, queried once per variant
+    if (o == 0) {
+        int nb = 0;
+        SWG_TRY(cuda_status(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_kick_mixed_sym_grp<RAD, G>, 32 * G, 0),
+                            "occupancy"));
+        o = nb > 0 ? nb : 1;
+    }
+    const int grid = std::min(nitems, o * (c->num_sms > 0 ? c->num_sms : 152));
+    k_kick_mixed_sym_grp<RAD, G><<<grid, 32 * G, 0, c->stream>>>(nitems, items, poff, npl, sbase, pA, pB, rpart, ppart,
+                                                               head, sys_flag, phase, iflag, accept);
+    return SWG_OK;
+}
+
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
                            float *ppart, unsigned *head, const int32_t *sys_flag, int phase, const uint8_t *iflag,
-                           unsigned accept, int warps, int tile) {
+                           unsigned accept, int warps, int tile, int group) {
     if (nitems <= 0) return SWG_OK;
-    if ((warps != 1 && warps != 2 && warps != 4) || (tile != 64 && tile != 128)) return SWG_ERR_ARG;
+    if ((warps != 1 && warps != 2 && warps != 4) || (tile != 64 && tile != 128) ||
+        (group != 1 && group != 2 && group != 4) || (group > 1 && tile != KICK_SYM_TILE))
+        return SWG_ERR_ARG;
     SWG_TRY(cuda_status(c, cudaMemsetAsync(head, 0, sizeof(unsigned), c->stream), "memset"));
 #define SWG_SYM_ARGS c, nitems, items, poff, npl, sbase, pA, pB, rpart, ppart, head, sys_flag, phase, iflag, accept
-    // 64-body tiles run with one warp per block (the block size is tuned on 128-body tiles)
+    // 64-body tiles run with one warp per block (the block size is tuned on 128-body tiles);
+    // row groups take one warp per tile of the group
     int rc;
-    if (tile == 64)
+    if (group == 2)
+        rc = rad ? sym_grp_launch<true, 2>(SWG_SYM_ARGS) : sym_grp_launch<false, 2>(SWG_SYM_ARGS);
+    else if (group == 4)
+        rc = rad ? sym_grp_launch<true, 4>(SWG_SYM_ARGS) : sym_grp_launch<false, 4>(SWG_SYM_ARGS);
+    else if (tile == 64)
         rc = rad ? sym_launch<true, 1, 64>(SWG_SYM_ARGS) : sym_launch<false, 1, 64>(SWG_SYM_ARGS);
     else if (rad)
         rc = warps == 1 ? sym_launch<true, 1, 128>(SWG_SYM_ARGS)
@@ -533,10 +750,10 @@ int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, 
 
 int kick_mixed_sym_reduce(swg_ctx *c, int strip, int64_t n, const int32_t *psys, const int32_t *poff,
                           const int32_t *npl, const int32_t *sbase, const float *rpart, const float *ppart,
-                          double *acc, int acc_is_zero, const int32_t *sys_flag, int phase, int tile) {
+                          double *acc, int acc_is_zero, const int32_t *sys_flag, int phase, int tile, int group) {
     if (n <= 0) return SWG_OK;
     k_kick_sym_reduce<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(n, psys, poff, npl, sbase, rpart, ppart, acc,
-                                                                      acc_is_zero, sys_flag, phase, strip, tile);
+                                                                      acc_is_zero, sys_flag, phase, strip, tile, group);
     c->launches++;
     return launch_status(c, "kick_sym_reduce");
 }

@@ -192,29 +192,33 @@ int orbel_xv2el_launch(swg_ctx *c, int32_t n, const double *mu, const double *rh
 
 // kick_sym.cu -- symmetric mixed pl-pl kick (each pair once, applied to both bodies) over
 // tile pairs of `tile` bodies (KICK_SYM_TILE = 128 by default, or 64).  kick_sym_items builds
-// the items (row strips of tile pairs, sorted by cost) and per system its first receiver slot
-// and first pair slot (sbase[2s], sbase[2s+1]); returns the number of receiver slots,
-// *npair_slots the number of pair slots.  A receiver slot holds 6 * tile floats, a pair slot
-// 3 * tile; kick_mixed_sym_reduce writes acc (+)= the sums.  The same tile must be passed to
-// every call on one plan.
+// the items (strips of tile pairs of a row group of `group` tiles, sorted by cost) and per
+// system its first receiver slot and first pair slot (sbase[2s], sbase[2s+1]); returns the
+// number of receiver slots, *npair_slots the number of pair slots.  A receiver slot holds
+// 6 * tile floats, a pair slot 3 * tile; kick_mixed_sym_reduce writes acc (+)= the sums.  The
+// same tile, strip and group must be passed to every call on one plan; groups of 2 or 4
+// tiles take 128-body tiles.
 constexpr int KICK_SYM_TILE = 128;
 // strip: tiles J per item (4, or 1 when that would leave too few items to fill the GPU)
 int kick_sym_strip(int32_t nsys, const int32_t *npl, int num_sms, int tile = KICK_SYM_TILE);
 int64_t kick_sym_items(int32_t nsys, const int32_t *npl, int strip, std::vector<int4> &items,
-                       std::vector<int32_t> &sbase, int64_t *npair_slots, int tile = KICK_SYM_TILE);
+                       std::vector<int32_t> &sbase, int64_t *npair_slots, int tile = KICK_SYM_TILE,
+                       int group = 1);
 // a single system has enough tile pairs to fill the GPU (else the broadcast kernel is faster)
 bool kick_sym_single_ok(int32_t npl, int num_sms);
 // iflag/accept (optional): only items it with bit iflag[it] of accept set are processed.
-// warps: warps per block (1, 2 or 4; the same bits for each; tiles of 64 take one).
+// warps: warps per block of one-row items (1, 2 or 4; the same bits for each; tiles of 64
+// take one); with group 2 or 4 a block of `group` warps takes each row-group item.
 int kick_mixed_sym_batched(swg_ctx *c, bool rad, int nitems, const int4 *items, const int32_t *poff,
                            const int32_t *npl, const int32_t *sbase, const float4 *pA, const float4 *pB, float *rpart,
                            float *ppart, unsigned *head, const int32_t *sys_flag = nullptr, int phase = 0,
                            const uint8_t *iflag = nullptr, unsigned accept = 0, int warps = 1,
-                           int tile = KICK_SYM_TILE);
+                           int tile = KICK_SYM_TILE, int group = 1);
 // iflag[it] of every item: 0 when its system has no encounter (sys_enc[s] == 0), else 2 when
 // one of its tiles holds a body with enc[body] != 0, else 1.
 int kick_sym_item_flags(swg_ctx *c, int nitems, const int4 *items, const int32_t *poff, const int32_t *npl,
-                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag, int tile = KICK_SYM_TILE);
+                        const int32_t *sys_enc, const uint8_t *enc, uint8_t *iflag, int tile = KICK_SYM_TILE,
+                        int group = 1);
 // one system (psys == nullptr below): plan cached in the context for the last npl; acc (+)= the
 // pair accelerations (radius rule with R, else j != i); no GMTINY bodies
 int kick_mixed_sym_single(swg_ctx *c, int32_t npl, const double *r, const double *Gm, const double *R, double *acc,
@@ -223,7 +227,7 @@ void kick_sym_single_free(swg_ctx *c);
 int kick_mixed_sym_reduce(swg_ctx *c, int strip, int64_t n, const int32_t *psys, const int32_t *poff,
                           const int32_t *npl, const int32_t *sbase, const float *rpart, const float *ppart,
                           double *acc, int acc_is_zero, const int32_t *sys_flag = nullptr, int phase = 0,
-                          int tile = KICK_SYM_TILE);
+                          int tile = KICK_SYM_TILE, int group = 1);
 // autotune.cu -- cache of tuned kernel shapes: key of (device, kind, size bucket); the cached
 // variant or -1; store (kept for the process and appended to the cache file)
 std::string tune_key(int device, const char *kind, int bucket);

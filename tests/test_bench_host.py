@@ -95,3 +95,19 @@ def test_gpus_must_match_world_size(monkeypatch):
     with pytest.raises(SystemExit):
         bench.dist_setup(argparse.Namespace(gpus=2))
     assert bench.dist_setup(argparse.Namespace(gpus=1))[0] == 1
+
+
+def test_traffic_record_is_used_only_for_its_kick_shape(tmp_path, monkeypatch):
+    # the recorded DRAM bytes of a capture go into the roofline line only when the run used
+    # the kick shape that the capture ran
+    (tmp_path / "profiles").mkdir()
+    shape = {"plpl_tile": 128, "plpl_strip": 4, "plpl_warps_per_block": 2, "plpl_row_group": 2}
+    rec = {"kick_pl_c4": {"bytes_per_launch": 49.1e6, "commit": "abc", "command": "ncu ...", "note": "n",
+                          "plan": shape}}
+    (tmp_path / "profiles" / "traffic.json").write_text(json.dumps(rec))
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    b, src = bench.load_traffic("kick_pl_c4", dict(shape, plpl="symmetric", pltp_shape=-1))
+    assert b == 49.1e6 and src["commit"] == "abc"
+    b, src = bench.load_traffic("kick_pl_c4", dict(shape, plpl_row_group=1, plpl_warps_per_block=1))
+    assert b is None and "another kick shape" in src["note"]
+    assert bench.load_traffic("kick_pl_c1", shape) == (None, None)

@@ -159,19 +159,23 @@ def test_symba_ensemble_mixed_conservation(ctx):
     assert f.stats()["plpl_encounters"] > 0
 
 
-@pytest.mark.parametrize("tile", [64, 128])
-def test_symba_ensemble_mixed_conservation_tiles(ctx, tile):
-    # both tile sizes of the symmetric pl-pl kick through whole SyMBA steps (the closing kick
-    # split by the items' encounter flags): energy within 2x of the FP64 path's error
-    E = _compact("C4", nsys=5, scale=0.06, tp_per_pl=0)
+@pytest.mark.parametrize("tile,group,scale", [(64, 1, 0.06), (128, 1, 0.06), (128, 2, 0.06), (128, 4, 0.06),
+                                              (128, 2, 0.2), (128, 4, 0.2)])
+def test_symba_ensemble_mixed_conservation_tiles(ctx, tile, group, scale):
+    # both tile sizes and the row groups of the symmetric pl-pl kick through whole SyMBA
+    # steps (the closing kick split by the items' encounter flags; groups wider than a
+    # system's tiles, and systems of several groups): energy within 2x of the FP64 path's error
+    E = _compact("C4", nsys=5, scale=scale, tp_per_pl=0)
     kw = dict(dt=0.005, rhscale=2.0)
     f = Ensemble(ctx, E, precision="FP64", **kw)
     m = Ensemble(ctx, E, precision="MIXED", **kw)
     m.set_kick_tile(tile)
+    m.set_kick_group(group)
     e0 = f.energy()
-    f.step(100)
-    m.step(100)
-    assert m.kick_tile() == tile
+    nstep = 100 if scale < 0.1 else 40
+    f.step(nstep)
+    m.step(nstep)
+    assert m.kick_tile() == tile and m.kick_group() == group
     ef, em = f.energy(), m.energy()
     dEf = np.abs(ef["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
     dEm = np.abs(em["te_helio"] - e0["te_helio"]) / np.abs(e0["te_helio"])
@@ -316,6 +320,28 @@ def test_symmetric_kick_tiles(ctx, tile, strip):
         e = np.linalg.norm(g[a:b] - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
         assert e.max() < 2e-5, (tile, strip, s, e.max())
         assert np.sqrt(np.mean(e ** 2)) < 1e-6, (tile, strip, s)
+    assert np.array_equal(g, ens.getacch_int_pl())
+    ens.close()
+
+
+@pytest.mark.parametrize("group,strip", [(2, 2), (2, 4), (2, 8), (4, 1), (4, 4), (4, 8), (4, 16), (1, 4)])
+def test_symmetric_kick_groups(ctx, group, strip):
+    # row groups of the symmetric pl-pl kick (a block of `group` warps per item, one pair slot
+    # per group and tile J): within the mixed-kick tolerance of the oracle's FP64 triangular
+    # kick, deterministic, and reported as the plan in use
+    E = IC.make_ensemble("C4", nsys=4, scale=0.5)
+    want = [O.kick_tri_pl(pl["rh"], pl["Gmass"], pl["radius"]) for pl, _ in E["systems"]]
+    ens = Ensemble(ctx, E, precision="MIXED")
+    ens.set_kick_group(group)
+    ens.set_kick_strip(strip)
+    g = ens.getacch_int_pl()
+    assert ens.kick_group() == group and ens.kick_strip() == strip
+    assert group == 1 or (ens.kick_tile() == 128 and ens.kick_warps() == group)
+    for s, r in enumerate(want):
+        a, b = ens.poff[s], ens.poff[s + 1]
+        e = np.linalg.norm(g[a:b] - r, axis=1) / np.maximum(np.linalg.norm(r, axis=1), 1e-300)
+        assert e.max() < 2e-5, (group, strip, s, e.max())
+        assert np.sqrt(np.mean(e ** 2)) < 1e-6, (group, strip, s)
     assert np.array_equal(g, ens.getacch_int_pl())
     ens.close()
 
