@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="c4", choices=["c4", "c3", "c3w", "c1"])
     p.add_argument("--nsys", type=int, default=None, help="first NSYS systems of the C4 ensemble")
+    p.add_argument("--kick-shape", type=lambda v: tuple(int(x) for x in v.split(",")), default=None,
+                   metavar="TILE,STRIP,WARPS,GROUP",
+                   help="C4: force the symmetric pl-pl kick's shape (default: autotuned), e.g. 128,4,1,1")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     p.add_argument("--encounter", default="triangular", choices=["triangular", "sortsweep"],
                    help="mode of the SyMBA level-0 pl-pl and pl-tp checks (c4, c1)")
@@ -108,11 +111,19 @@ class C4:
         self.plpl_pairs = float(sum(int(n) * (int(n) - 1) for n in self.E["npl"]))  # per kick evaluation
         self.pairs_per_step = 2 * self.plpl_pairs
         self.enc = getattr(args, "encounter", "triangular").upper()
+        self.kick_shape = getattr(args, "kick_shape", None)
 
     def make(self, ctx, precision):
         from swiftest_gb300.api import Ensemble
         kw = {} if self.enc == "TRIANGULAR" else dict(encounter_check_plpl=self.enc, encounter_check_pltp=self.enc)
-        return Ensemble(ctx, self.E, precision=precision, **kw)
+        ens = Ensemble(ctx, self.E, precision=precision, **kw)
+        if self.kick_shape and precision == "MIXED":  # forced symmetric-kick shape (else autotuned)
+            tile, strip, warps, group = self.kick_shape
+            ens.set_kick_tile(tile)
+            ens.set_kick_strip(strip)
+            ens.set_kick_warps(warps)
+            ens.set_kick_group(group)
+        return ens
 
     def state_arrays(self):
         E = self.E

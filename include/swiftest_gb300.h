@@ -297,7 +297,7 @@ int swg_ensemble_set_kick_tile(swg_ensemble *ens, int tile);
  * and read back.  The sums are grouped differently from one-row items (1), so results agree
  * within the mixed-kick tolerance, each deterministic.  By default (0) the autotuner times
  * groups 2 and 4 at strips 2 and 4 after the one-row shapes and takes the fastest group
- * unless it is more than 1% slower than the best one-row shape (cached with the strip); a
+ * only when it is more than 3% faster than the best one-row shape (cached with the strip); a
  * forced warps-per-block count or 64-body tile keeps one-row items, and a forced group of 2
  * or 4 takes 128-body tiles unless the tile is forced.  1, 2 or 4 forces it;
  * swg_ensemble_kick_variant with kind 5 reads the group in use (-1 before the first mixed

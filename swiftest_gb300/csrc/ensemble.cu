@@ -749,19 +749,18 @@ constexpr int SYM_NWARPS = 3;
 
 // Row groups (tiles per item row, one warp each) and their strips the autotuner tries for
 // the symmetric kick with 128-body tiles.  A row group writes 1/group of the pair slots of
-// one-row items, which the per-body sums read back: less DRAM traffic and L2 footprint,
-// which a kick timed alone does not show (on the C4 ensemble the slots fall from 124 MB to
-// 89 MB with groups of 2 at strip 4, and the pair kernel's DRAM bytes from 2.85x to 1.60x
-// the algorithmic bytes at the same kick time), so a group is taken unless it is more than
-// SYM_GROUP_MARGIN slower than the best one-row shape.  Strips stop at 4: a group's items
-// are coarser, and in a SyMBA step the closing kick's items that touch a body of the
-// encounter lists wait for the recursion (strip 8 kicks as fast alone, but the C4 step is
-// 1.5% slower).
+// one-row items, which the per-body sums read back: on the C4 ensemble the slots fall from
+// 124 MB to 89 MB with groups of 2 at strip 4, and the pair kernel's DRAM bytes from 2.85x
+// to 1.61x the algorithmic bytes at the same kick time alone; in the SyMBA step, where the
+// closing kick shares the SMs with the FP64 drift and the recursion, the group's warps
+// wait for each other at every tile J and the step is 0.4-0.9% slower.  So a group is
+// taken, like every other candidate, only when it is more than 3% faster.  Strips stop at
+// 4: longer ones make the closing kick's items that touch a listed body (and so wait for
+// the recursion) coarser (strip 8: 1.5% slower steps).
 constexpr int SYM_GROUPS[] = {2, 4};
 constexpr int SYM_NGROUP = 2;
 constexpr int SYM_GROUP_STRIPS[] = {2, 4};
 constexpr int SYM_NGROUP_STRIP = 2;
-constexpr float SYM_GROUP_MARGIN = 1.01f;
 
 // Times the symmetric kick (pair kernel and per-body sums into scratch accelerations) on
 // this ensemble's current data: first the two tile sizes (128 and 64 bodies, each at its
@@ -770,8 +769,8 @@ constexpr float SYM_GROUP_MARGIN = 1.01f;
 // warm-up, then the shortest of five launches timed one by one.  The defaults (128 bodies,
 // kick_sym_strip's strip, one warp) stay unless another candidate is faster by more than
 // 3%, so that timing noise does not move the choice between near-equal candidates.  Last
-// (128-body tiles) the row groups at their strips, taken as described at SYM_GROUPS.  The
-// partners must be split into kA/kB.
+// (128-body tiles) the row groups at their strips, by the same rule.  The partners must be
+// split into kA/kB.
 int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int *best_strip, int *best_warps,
                   int *best_group) {
     swg_ctx *c = e->c;
@@ -851,7 +850,7 @@ int time_sym_plan(swg_ensemble *e, bool rad, unsigned *head, int *best_tile, int
                     group_strip = SYM_GROUP_STRIPS[b];
                 }
             }
-        if (group_ms <= SYM_GROUP_MARGIN * best_ms) {
+        if (group_ms < 0.97f * best_ms) {
             *best_group = group;
             *best_strip = group_strip;
             *best_warps = group;
