@@ -414,7 +414,8 @@ def run_path(ctx, wl, precision, steps, warmup, prof_steps=0, clocks=None):
 
 def run_e2e(ctx, wl, precision, steps):
     """The same metric through the public API with host buffers: every step uploads the
-    state (pinned host arrays -> device), steps once and reads the state back."""
+    state (pinned host arrays -> device), steps once and reads the state back.  Returns the
+    time and the bytes of the state arrays, which every step copies in each direction."""
     import torch
     s = wl.make(ctx, precision)
     s.step(2)
@@ -559,7 +560,7 @@ def main():
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "e2e": {"value": whole_job_rate(world, nb, args.steps, e2e_ms), "unit": UNIT,
-                "h2d_bytes_per_step": e2e_bytes // 2, "d2h_bytes_per_step": e2e_bytes // 2},
+                "h2d_bytes_per_step": e2e_bytes, "d2h_bytes_per_step": e2e_bytes},
         "gpu_launches": int(launches),
     }
     if rank == 0:

@@ -134,8 +134,8 @@ def _patch_ensemble(s: str) -> str:
         "            swg_tr(c->stream, 11);\n"
         "            SWG_TRY(cuda_status(c, cudaStreamWaitEvent(c->stream, e->ev_join, 0), \"join\"));\n"
         "            SWG_TRY(kick_mixed_sym_reduce(")
-    rep("                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile));\n",
-        "                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile));\n"
+    rep("                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile, e->sym_group));\n",
+        "                                          e->sym_ppart, e->ah, 1, e->lany, 1, e->sym_tile, e->sym_group));\n"
         "            swg_tr(c->stream, 12);\n")
     rep("        SWG_TRY(close_pl(e, dth, true));\n    } else {",
         "        SWG_TRY(close_pl(e, dth, true));\n        swg_tr(c->stream, 13);\n    } else {")

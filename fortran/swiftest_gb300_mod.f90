@@ -410,6 +410,14 @@ module swiftest_gb300_mod
          type(c_ptr), value :: ens
          real(c_double), intent(out), optional :: rh(3,*), vh(3,*), trh(3,*), tvh(3,*)
       end function
+      integer(c_int) function swg_ensemble_reset_first_step(ens) bind(C, name="swg_ensemble_reset_first_step")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: ens
+      end function
+      integer(c_int) function swg_system_reset_first_step(sys) bind(C, name="swg_system_reset_first_step")
+         import :: c_ptr, c_int
+         type(c_ptr), value :: sys
+      end function
       integer(c_int) function swg_ensemble_use_graphs(ens, enable) bind(C, name="swg_ensemble_use_graphs")
          import :: c_ptr, c_int
          type(c_ptr), value :: ens

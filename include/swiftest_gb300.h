@@ -179,9 +179,16 @@ int swg_system_pltp_list(swg_system *sys, int64_t cap, int64_t *n, int32_t *i1, 
  * massive bodies and test particles) of an initialized system without resetting its
  * step flags: the per-step exchange a host-side caller that owns the arrays performs.
  * NULL pointers are skipped.  get_state_async is ordered on the stream; call
- * swg_synchronize before reading the host arrays. */
+ * swg_synchronize before reading the host arrays.
+ * Like the reference's steps, a step after the first carries state of its own from the
+ * step before (HELIO/SyMBA: the barycentric velocities pl%vb, tp%vb; WHM: the closing
+ * accelerations), so an upload that changes the state reaches the next step only after
+ * swg_system_reset_first_step, which sets the reference's lfirst flags (helio_step_pl,
+ * whm_step_pl): the next step converts vh to vb and evaluates its opening accelerations
+ * afresh, as the first step after swg_system_initialize does. */
 int swg_system_set_state(swg_system *sys, const double *rh, const double *vh, const double *trh, const double *tvh);
 int swg_system_get_state_async(swg_system *sys, double *rh, double *vh, double *trh, double *tvh);
+int swg_system_reset_first_step(swg_system *sys);
 
 /* ---- orbital elements <-> Cartesian state (swiftest_orbel_el2xv_vec / _xv2el_vec,
  * swiftest_orbel.f90:14-42, 876-910, with swiftest_orbel_el2xv :45-144 and swiftest_orbel_xv2el
@@ -245,9 +252,12 @@ int swg_ensemble_collision_terms(swg_ensemble *ens, double *out);
 int swg_ensemble_stats(swg_ensemble *ens, int64_t *out);
 /* level-0 pl-pl list of system sys from the last step, indices local to the system */
 int swg_ensemble_plpl_list(swg_ensemble *ens, int32_t sys, int64_t cap, int64_t *n, int32_t *i1, int32_t *i2);
+/* The state exchange and the first-step flags of every system, as for single systems
+ * (swg_system_set_state, swg_system_reset_first_step). */
 int swg_ensemble_set_state(swg_ensemble *ens, const double *rh, const double *vh, const double *trh,
                            const double *tvh);
 int swg_ensemble_get_state_async(swg_ensemble *ens, double *rh, double *vh, double *trh, double *tvh);
+int swg_ensemble_reset_first_step(swg_ensemble *ens);
 /* WHM and HELIO ensembles replay each step as a CUDA graph captured after the first step
  * (default on; results are identical either way).  SyMBA steps always run eagerly: each
  * takes one host decision (the encounter-list sizes). */

@@ -100,6 +100,8 @@ SIGNATURES = {
     "swg_ensemble_set_kick_strip": (_INT, [_P, _INT]),
     "swg_ensemble_set_kick_warps": (_INT, [_P, _INT]),
     "swg_ensemble_set_kick_tile": (_INT, [_P, _INT]),
+    "swg_system_reset_first_step": (_INT, [_P]),
+    "swg_ensemble_reset_first_step": (_INT, [_P]),
     "swg_ensemble_set_kick_group": (_INT, [_P, _INT]),
     "swg_ensemble_set_gmtiny": (_INT, [_P, C.c_double]),
     "swg_ensemble_kick_variant": (_INT, [_P, _INT, C.POINTER(_INT)]),

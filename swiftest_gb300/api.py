@@ -265,13 +265,19 @@ class NBodySystem:
         self.ctx.check("swg_system_step", self.ctx.lib.swg_system_step(self.h, int(nsteps)))
 
     def set_state(self, rh=None, vh=None, trh=None, tvh=None):
-        """Upload positions / heliocentric velocities (host arrays) without resetting step flags."""
+        """Upload positions / heliocentric velocities (host arrays) without resetting step
+        flags; a changed state reaches the next step after reset_first_step."""
         self.ctx.check("swg_system_set_state", self.ctx.lib.swg_system_set_state(
             self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
 
     def get_state_async(self, rh=None, vh=None, trh=None, tvh=None):
         self.ctx.check("swg_system_get_state_async", self.ctx.lib.swg_system_get_state_async(
             self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
+
+    def reset_first_step(self):
+        """Set the first-step flags (the reference's lfirst): the next step takes the
+        uploaded vh and evaluates its opening accelerations afresh (see set_state)."""
+        self.ctx.check("swg_system_reset_first_step", self.ctx.lib.swg_system_reset_first_step(self.h))
 
     PROFILE_CLASSES = ("kick_pl", "kick_tp", "drift", "encounter_level0", "symba_recursion")
 
@@ -409,6 +415,11 @@ class Ensemble:
     def get_state_async(self, rh=None, vh=None, trh=None, tvh=None):
         self.ctx.check("swg_ensemble_get_state_async", self.ctx.lib.swg_ensemble_get_state_async(
             self.h, _ptr(rh), _ptr(vh), _ptr(trh), _ptr(tvh)))
+
+    def reset_first_step(self):
+        """Set every system's first-step flags (the reference's lfirst), as
+        NBodySystem.reset_first_step does for one system."""
+        self.ctx.check("swg_ensemble_reset_first_step", self.ctx.lib.swg_ensemble_reset_first_step(self.h))
 
     def get_pl(self):
         rh = np.zeros((self.NPL, 3))

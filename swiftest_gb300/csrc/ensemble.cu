@@ -2500,6 +2500,19 @@ int swg_ensemble_set_state(swg_ensemble *e, const double *rh, const double *vh, 
     return SWG_OK;
 }
 
+int swg_ensemble_reset_first_step(swg_ensemble *e) {
+    if (!e || !e->initialized) return SWG_ERR_STATE;
+    swg_ctx *c = e->c;
+    SWG_TRY(upload(c, e->lfirst, std::vector<int32_t>(e->nsys, 1)));
+    e->whm_first = 1;
+    // the captured step graph holds the steps after the first (WHM's first step differs on the host)
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "first step"));
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+    e->eager_steps = 0;
+    return SWG_OK;
+}
+
 int swg_ensemble_get_state_async(swg_ensemble *e, double *rh, double *vh, double *trh, double *tvh) {
     if (!e) return SWG_ERR_ARG;
     swg_ctx *c = e->c;

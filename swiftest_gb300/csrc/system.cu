@@ -1467,6 +1467,14 @@ int swg_system_set_state(swg_system *s, const double *rh, const double *vh, cons
     return SWG_OK;
 }
 
+int swg_system_reset_first_step(swg_system *s) {
+    if (!s || !s->initialized) return SWG_ERR_STATE;
+    swg_ctx *c = s->c;
+    SWG_TRY(cuda_status(c, cudaStreamSynchronize(c->stream), "first step"));
+    s->lfirst_pl = s->lfirst_tp = s->lfirstkick = 1;
+    return SWG_OK;
+}
+
 int swg_system_get_state_async(swg_system *s, double *rh, double *vh, double *trh, double *tvh) {
     if (!s) return SWG_ERR_ARG;
     swg_ctx *c = s->c;
