@@ -39,9 +39,20 @@ constexpr int SQ = 128;                  // receivers per block (two bound tiles
 constexpr int SORT_MAX = 16384;          // largest system ordered in shared memory
 static_assert(SQ == ENC_SORTED_TILE && SB == ENC_BOUND_TILE, "tile sizes of the sorted check");
 
-// Per system (one block): order the bodies by |r| (ties by index).  perm[poff + p] is the
-// global index of the body at sorted position p.  Systems above SORT_MAX keep their order.
-__global__ void __launch_bounds__(1024) k_radial_sort(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
+// Per system (one block of RS_T threads): order the bodies by |r| (ties by index).
+// perm[poff + p] is the global index of the body at sorted position p.  Systems above
+// SORT_MAX keep their order.  The order only steers the culling (every pair the cull keeps
+// is still decided in FP64), so a 24-bit key is enough: the FP32 |r| with its 7 lowest
+// mantissa bits dropped (its bit pattern orders like the value for r >= 0; a NaN sorts
+// last).  Stable LSD radix sort in shared memory, three passes of 8 bits: each warp takes
+// a contiguous segment of the bodies 32 at a time, ranks equal digits among its lanes with
+// __match_any_sync, and counts per (digit, warp); an exclusive scan over the counts in
+// (digit, warp) order gives every warp's first slot per digit, so each pass keeps the
+// previous order among equal digits and the result is ordered by (key, index).
+constexpr int RS_T = 512;                 // threads of k_radial_sort
+constexpr int RS_W = RS_T / 32;           // warps of k_radial_sort
+constexpr int RS_HIST = 256 * RS_W;       // (digit, warp) counts
+__global__ void __launch_bounds__(RS_T) k_radial_sort(const int32_t *__restrict__ poff, const int32_t *__restrict__ npl,
                                                       const double *__restrict__ r, int32_t *__restrict__ perm) {
     extern __shared__ unsigned char smem[];
     const int s = blockIdx.x;
@@ -50,44 +61,77 @@ __global__ void __launch_bounds__(1024) k_radial_sort(const int32_t *__restrict_
         for (int t = threadIdx.x; t < n; t += blockDim.x) perm[o + t] = o + t;
         return;
     }
-    int npad = 1;
-    while (npad < n) npad <<= 1;
-    float *key = (float *)smem;
-    int32_t *idx = (int32_t *)(key + npad);
-    for (int t = threadIdx.x; t < npad; t += blockDim.x) {
-        float k = __int_as_float(0x7f800000);  // +inf pads the tail
-        if (t < n) {  // the order only has to be roughly radial: FP32 is enough
-            const double *x = &r[3 * (size_t)(o + t)];
-            const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
-            k = sqrtf(fmaf(x2, x2, fmaf(x1, x1, x0 * x0)));
-        }
-        key[t] = k;
-        idx[t] = t;
+    uint32_t *hist = (uint32_t *)smem;  // [digit][warp]
+    uint32_t *key[2] = {hist + RS_HIST, hist + RS_HIST + n};
+    uint16_t *idx[2] = {(uint16_t *)(hist + RS_HIST + 2 * n), (uint16_t *)(hist + RS_HIST + 2 * n) + n};
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const double *x = &r[3 * (size_t)(o + t)];
+        const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
+        float k = sqrtf(fmaf(x2, x2, fmaf(x1, x1, x0 * x0)));
+        if (!(k >= 0.f)) k = __int_as_float(0x7f800000);
+        key[0][t] = (uint32_t)__float_as_int(k) >> 7;
+        idx[0][t] = (uint16_t)t;
     }
-    __syncthreads();
-    for (int k = 2; k <= npad; k <<= 1)
-        for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int t = threadIdx.x; t < npad; t += blockDim.x) {
-                const int p = t ^ jj;
-                if (p > t) {
-                    const bool up = (t & k) == 0;
-                    const float ka = key[t], kb = key[p];
-                    const int ia = idx[t], ib = idx[p];
-                    // (key, index) order; a NaN key compares as not-greater, which keeps
-                    // the network a permutation
-                    const bool gt = ka > kb || (ka == kb && ia > ib);
-                    const bool lt = kb > ka || (ka == kb && ib > ia);
-                    if (up ? gt : lt) {
-                        key[t] = kb;
-                        key[p] = ka;
-                        idx[t] = ib;
-                        idx[p] = ia;
-                    }
-                }
-            }
-            __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int seg = (n + RS_W - 1) / RS_W, b0 = min(n, w * seg), b1 = min(n, b0 + seg);
+    const unsigned lt = (1u << lane) - 1u;
+    int in = 0;
+    for (int shift = 0; shift < 24; shift += 8, in ^= 1) {
+        for (int t = threadIdx.x; t < RS_HIST; t += blockDim.x) hist[t] = 0;
+        __syncthreads();  // keys of this pass written, counts cleared
+        for (int b = b0; b < b1; b += 32) {  // counts of this warp's segment
+            const int i = b + lane;
+            const int d = i < b1 ? (int)((key[in][i] >> shift) & 255u) : 256;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            if (d < 256 && lane == __ffs(peers) - 1) hist[d * RS_W + w] += __popc(peers);
+            __syncwarp();
         }
-    for (int t = threadIdx.x; t < n; t += blockDim.x) perm[o + t] = o + idx[t];
+        __syncthreads();
+        // exclusive scan of the counts in (digit, warp) order: each thread its RS_HIST / RS_T
+        // consecutive entries, then the thread sums across the block
+        constexpr int PER = RS_HIST / RS_T;
+        uint32_t loc[PER], sum = 0;
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            loc[q] = hist[threadIdx.x * PER + q];
+            sum += loc[q];
+        }
+        uint32_t inc = sum;  // inclusive scan of the thread sums: in the warp, then across warps
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, dd);
+            if (lane >= dd) inc += y;
+        }
+        __shared__ uint32_t wsum[RS_W];
+        if (lane == 31) wsum[w] = inc;
+        __syncthreads();
+        uint32_t wbase = 0;
+        for (int q = 0; q < w; q++) wbase += wsum[q];
+        uint32_t run = wbase + inc - sum;
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            hist[threadIdx.x * PER + q] = run;
+            run += loc[q];
+        }
+        __syncthreads();  // first slots ready; wsum free for the next pass
+        for (int b = b0; b < b1; b += 32) {  // scatter, in segment order
+            const int i = b + lane;
+            const bool ok = i < b1;
+            const int d = ok ? (int)((key[in][i] >> shift) & 255u) : 256;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            uint32_t pos = 0;
+            if (ok) pos = hist[d * RS_W + w] + __popc(peers & lt);
+            __syncwarp();  // every lane has read its digit's slot before the leader moves it
+            if (ok) {
+                key[in ^ 1][pos] = key[in][i];
+                idx[in ^ 1][pos] = idx[in][i];
+                if (lane == __ffs(peers) - 1) hist[d * RS_W + w] += __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();  // the pass's output complete
+    }
+    for (int t = threadIdx.x; t < n; t += blockDim.x) perm[o + t] = o + (int32_t)idx[in][t];
 }
 
 // One block of SB threads per bound tile (sys, first sorted position): the prefilter's
@@ -334,28 +378,26 @@ __global__ void __launch_bounds__(SQ) k_pltp_sorted(const int4 *__restrict__ ite
     }
 }
 
-// Dynamic shared memory of k_radial_sort for systems of up to nmax bodies.
-static size_t radial_sort_smem(int nmax) {
-    int npad = 1;
-    while (npad < std::min(nmax, SORT_MAX)) npad <<= 1;
-    return (size_t)8 * npad;
+// k_radial_sort over nsys systems of up to nmax bodies; its dynamic shared memory holds the
+// counts, two key and two index buffers.
+static int radial_sort_launch(swg_ctx *c, int nsys, int nmax, const int32_t *poff, const int32_t *npl,
+                              const double *r, int32_t *perm) {
+    const size_t smem = 4 * (size_t)RS_HIST + 12 * (size_t)std::min(nmax, SORT_MAX);
+    static size_t smem_set = 0;  // the kernel's shared-memory limit raised so far
+    if (smem > 48 * 1024 && smem > smem_set) {
+        SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)smem),
+                            "radial sort smem"));
+        smem_set = smem;
+    }
+    k_radial_sort<<<nsys, RS_T, smem, c->stream>>>(poff, npl, r, perm);
+    c->launches++;
+    return launch_status(c, "radial_sort");
 }
 
 int sorted_set_prep(swg_ctx *c, const SortedSet &x, int nsys, bool resort, double dt) {
     if (x.ntiles <= 0) return SWG_OK;
-    if (resort) {
-        const size_t smem = radial_sort_smem(x.nmax);
-        static size_t smem_set = 0;
-        if (smem > 48 * 1024 && smem > smem_set) {
-            SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        (int)smem),
-                                "radial sort smem"));
-            smem_set = smem;
-        }
-        k_radial_sort<<<nsys, 1024, smem, c->stream>>>(x.off, x.n, x.r, x.perm);
-        c->launches++;
-        SWG_TRY(launch_status(c, "radial_sort"));
-    }
+    if (resort) SWG_TRY(radial_sort_launch(c, nsys, x.nmax, x.off, x.n, x.r, x.perm));
     const float adt = (float)fabs(dt) * (1.0f + 1e-6f);
     k_sorted_prep<<<x.ntiles, SB, 0, c->stream>>>(x.tiles, x.off, x.n, x.perm, x.r, x.v, x.renc, adt, x.F, x.F + x.N,
                                                   x.F + 2 * x.N, x.bounds);
@@ -387,19 +429,7 @@ int encounter_plpl_sorted_batched(swg_ctx *c, int nsys, int nmax, const int32_t 
                                   int32_t *o1, int32_t *o2, int32_t *olv, unsigned long long *count,
                                   const int32_t *nplm) {
     if (nitems <= 0 || ntiles <= 0) return SWG_OK;
-    if (resort) {
-        const size_t smem = radial_sort_smem(nmax);
-        static size_t smem_set = 0;
-        if (smem > 48 * 1024 && smem > smem_set) {
-            SWG_TRY(cuda_status(c, cudaFuncSetAttribute(k_radial_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        (int)smem),
-                                "radial sort smem"));
-            smem_set = smem;
-        }
-        k_radial_sort<<<nsys, 1024, smem, c->stream>>>(poff, npl, r, perm);
-        c->launches++;
-        SWG_TRY(launch_status(c, "radial_sort"));
-    }
+    if (resort) SWG_TRY(radial_sort_launch(c, nsys, nmax, poff, npl, r, perm));
     const float adt = (float)fabs(dt) * (1.0f + 1e-6f);  // |dt| rounded to float, then up
     k_sorted_prep<<<ntiles, SB, 0, c->stream>>>(tiles, poff, npl, perm, r, v, renc, adt, F, F + NPL, F + 2 * NPL,
                                                 bounds);
