@@ -332,7 +332,8 @@ int swg_flush_l2(swg_ctx *ctx, int64_t bytes);
 /* CUDA events on the context stream: 16 slots */
 int swg_event_record(swg_ctx *ctx, int slot);
 int swg_event_elapsed(swg_ctx *ctx, int a, int b, double *ms);
-/* FMA-chain throughput probe: kind 0 FP32 (FFMA), 1 FP64 (DFMA); TFLOP/s */
+/* FMA-chain throughput probe: kind 0 FP32 (FFMA), 1 FP64 (DFMA), 2 packed FP32 pairs
+ * (fma.rn.f32x2, two FMAs per lane and instruction); TFLOP/s */
 int swg_probe_peak(swg_ctx *ctx, int kind, double *tflops);
 
 #ifdef __cplusplus

@@ -83,7 +83,8 @@ class Context:
 
     def probe_peak_tflops(self, kind: str = "fp32") -> float:
         t = C.c_double()
-        self.check("swg_probe_peak", self.lib.swg_probe_peak(self.h, 0 if kind == "fp32" else 1, C.byref(t)))
+        k = {"fp32": 0, "fp64": 1, "fp32x2": 2}[kind]
+        self.check("swg_probe_peak", self.lib.swg_probe_peak(self.h, k, C.byref(t)))
         return float(t.value)
 
     # ---- kick -------------------------------------------------------------

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <vector>
 
+#include "kick_mixed.cuh"
 #include "swg_internal.cuh"
 
 namespace swg {
@@ -382,6 +383,25 @@ __global__ void k_probe_ffma(float *out, int iters, float seed) {
     const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
     if (s == 12345.678f) out[0] = s;  // keeps the chain live
 }
+// The same chains in packed FP32 pairs (fma.rn.f32x2: two FMAs per lane and instruction).
+__global__ void k_probe_ffma2(float *out, int iters, float seed) {
+    f32x2 a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = f2_pack(seed + threadIdx.x + k, seed + threadIdx.x + k + 0.5f);
+    const f32x2 m = f2_pack(0.9999999f, 0.9999999f), b = f2_pack(1e-7f, 1e-7f);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = f2_fma(a[k], m, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        float lo, hi;
+        f2_unpack(a[k], lo, hi);
+        s += lo + hi;
+    }
+    if (s == 12345.678f) out[0] = s;  // keeps the chains live
+}
 __global__ void k_probe_dfma(double *out, int iters, double seed) {
     double a0 = seed + threadIdx.x, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;
     const double m = 0.9999999, b = 1e-7;
@@ -421,11 +441,11 @@ int swg_event_elapsed(swg_ctx *c, int a, int b, double *ms) {
 }
 
 int swg_probe_peak(swg_ctx *c, int kind, double *tflops) {
-    if (!c || !tflops || (kind != 0 && kind != 1)) return SWG_ERR_ARG;
+    if (!c || !tflops || kind < 0 || kind > 2) return SWG_ERR_ARG;
     void *p;
     SWG_TRY(ensure_slot(c, 21, 64, &p));
     const int blocks = (c->num_sms > 0 ? c->num_sms : 152) * 8, threads = 256;
-    const int iters = kind == 0 ? 1 << 16 : 1 << 11;
+    const int iters = kind == 1 ? 1 << 11 : 1 << 16;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -434,13 +454,15 @@ int swg_probe_peak(swg_ctx *c, int kind, double *tflops) {
         cudaEventRecord(e0, c->stream);
         if (kind == 0)
             k_probe_ffma<<<blocks, threads, 0, c->stream>>>((float *)p, iters, 1.0f);
+        else if (kind == 2)
+            k_probe_ffma2<<<blocks, threads, 0, c->stream>>>((float *)p, iters, 1.0f);
         else
             k_probe_dfma<<<blocks, threads, 0, c->stream>>>((double *)p, iters, 1.0);
         cudaEventRecord(e1, c->stream);
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        const double flops = 2.0 * iters * (kind == 0 ? 8 : 4) * (double)blocks * threads;
+        const double flops = 2.0 * iters * (kind == 0 ? 8 : kind == 2 ? 16 : 4) * (double)blocks * threads;
         if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
     }
     cudaEventDestroy(e0);
