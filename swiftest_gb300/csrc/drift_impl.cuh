@@ -283,38 +283,63 @@ __device__ inline int d_drift_one(double mu, double &rx, double &ry, double &rz,
 }
 
 // ------------------------------------------------------------------ fast FP64 form
-// The same Danby drift, still entirely in FP64, for the mixed-precision path: where the
-// reference divides by the same quantity several times (r0, mu, alpha, en, fp) the fast
-// form takes one reciprocal (or reciprocal square root) and multiplies, contracts
-// products into FMAs, and folds the constant divisors.  On GB300 each FP64 divide or
-// square root is a multi-instruction sequence on the narrow FP64 pipe, so this roughly
-// halves the drift's FP64 work.  Results agree with the reference form to a few units
-// in the last place; the universal-variable branch (large steps or eccentric orbits) is
-// the reference form unchanged.
+// The same Danby drift for the mixed-precision path.  Where the reference divides by the
+// same quantity several times (r0, mu, alpha, en, fp) the fast form takes one reciprocal (or
+// reciprocal square root) and multiplies, contracts products into FMAs, and folds the
+// constant divisors; on GB300 each FP64 divide or square root is a multi-instruction
+// sequence on the narrow FP64 pipe.  The elliptic small-step branch solves Kepler's
+// difference equation (d_kepmd_fast) in FP32 and polishes the root with one FP64 Newton
+// step.  Results agree with the reference form to a few units in the last place; the
+// universal-variable branch (large steps or eccentric orbits) is the reference form
+// unchanged.
+//
+// Kepler's difference equation f(x) = x - ec sin x + es (1 - cos x) - dm = 0 (the
+// reference's _kepmd, swiftest_drift.f90:234-276): the reference's series guess and its
+// three corrections of increasing order run in FP32, which leaves x within a few FP32 ulps
+// of the root (|dx| below ~3e-7 over the branch: |dm| < 0.4, e < 0.6, f' >= 1 - e); one
+// Halley step in FP64, dx = -2 f f' / (2 f'^2 - f f''), then leaves an error of order dx^3,
+// below FP64 resolution.  sin and cos are formed once in FP64 at the FP32 root (the
+// reference's degree-11 sine polynomial, cos from sqrt(1 - sin^2)) and carried to the
+// polished root by their Taylor expansion to second order in dx.
 __device__ inline void d_kepmd_fast(double dm, double es, double ec, double &x, double &s, double &c) {
     const double a0 = 39916800.0, a1 = 6652800.0, a2 = 332640.0, a3 = 7920.0, a4 = 110.0;
     const double inv_a0 = 1.0 / 39916800.0;
-    const double fac1 = 1.0 / (1.0 - ec);
-    const double q = fac1 * dm;
-    const double fac2 = fma(es * es, fac1, -ec * THIRD);
-    double xx = q * (1.0 - 0.5 * fac1 * q * fma(-q, fac2, es));
-    double y = xx * xx;
-    double ss = xx * fma(-y, fma(-y, fma(-y, fma(-y, a4 - y, a3), a2), a1), a0) * inv_a0;
-    double cc = sqrt(fma(-ss, ss, 1.0));
+    // FP32 root: sin x as its Taylor series to x^11 in nested form
+    const float dmf = (float)dm, esf = (float)es, ecf = (float)ec;
+    const float fac1 = 1.0f / (1.0f - ecf);
+    const float q = fac1 * dmf;
+    const float fac2 = fmaf(esf * esf, fac1, -ecf * (1.0f / 3.0f));
+    float xf = q * (1.0f - 0.5f * fac1 * q * fmaf(-q, fac2, esf));
+    {
+        const float yf = xf * xf;
+        const float sf = xf * fmaf(-yf * (1.0f / 6.0f),
+                                   fmaf(-yf * (1.0f / 20.0f),
+                                        fmaf(-yf * (1.0f / 42.0f),
+                                             fmaf(-yf * (1.0f / 72.0f), fmaf(-yf, 1.0f / 110.0f, 1.0f), 1.0f), 1.0f),
+                                        1.0f),
+                                   1.0f);
+        const float cf = sqrtf(fmaf(-sf, sf, 1.0f));
+        const float f = fmaf(esf, 1.0f - cf, fmaf(-ecf, sf, xf)) - dmf;
+        const float fp = fmaf(esf, sf, fmaf(-ecf, cf, 1.0f));
+        const float fpp = fmaf(ecf, sf, esf * cf);
+        const float fppp = fmaf(ecf, cf, -esf * sf);
+        float dx = -(f / fp);
+        dx = -(f / fmaf(dx * fpp, 0.5f, fp));
+        dx = -(f / fmaf(dx * dx * fppp, 1.0f / 6.0f, fmaf(dx * fpp, 0.5f, fp)));
+        xf += dx;
+    }
+    // FP64 Halley step at the FP32 root
+    const double xx = (double)xf;
+    const double y = xx * xx;
+    const double ss = xx * fma(-y, fma(-y, fma(-y, fma(-y, a4 - y, a3), a2), a1), a0) * inv_a0;
+    const double cc = sqrt(fma(-ss, ss, 1.0));
     const double f = fma(es, 1.0 - cc, fma(-ec, ss, xx)) - dm;
     const double fp = fma(es, ss, fma(-ec, cc, 1.0));
     const double fpp = fma(ec, ss, es * cc);
-    const double fppp = fma(ec, cc, -es * ss);
-    double dx = -(f / fp);
-    dx = -(f / fma(dx * fpp, 0.5, fp));
-    dx = -(f / fma(dx * dx * fppp, SIXTH, fma(dx * fpp, 0.5, fp)));
-    xx = xx + dx;
-    y = xx * xx;
-    ss = xx * fma(-y, fma(-y, fma(-y, fma(-y, a4 - y, a3), a2), a1), a0) * inv_a0;
-    cc = sqrt(fma(-ss, ss, 1.0));
-    x = xx;
-    s = ss;
-    c = cc;
+    const double dx = -(2.0 * f * fp) / fma(2.0 * fp, fp, -f * fpp);
+    x = xx + dx;
+    s = fma(dx, fma(-0.5 * ss, dx, cc), ss);  // sin(x + dx) = s + c dx - s dx^2 / 2
+    c = fma(dx, fma(-0.5 * cc, dx, -ss), cc);  // cos(x + dx) = c - s dx - c dx^2 / 2
 }
 
 // inv_mu: 1/mu when the caller has it (the same value, formed once), else 0
