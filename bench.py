@@ -117,8 +117,9 @@ class C4:
         from swiftest_gb300.api import Ensemble
         kw = {} if self.enc == "TRIANGULAR" else dict(encounter_check_plpl=self.enc, encounter_check_pltp=self.enc)
         ens = Ensemble(ctx, self.E, precision=precision, **kw)
-        if self.kick_shape and precision == "MIXED":  # forced symmetric-kick shape (else autotuned)
-            tile, strip, warps, group = self.kick_shape
+        shape = getattr(self, "kick_shape", None)
+        if shape and precision == "MIXED":  # forced symmetric-kick shape (else autotuned)
+            tile, strip, warps, group = shape
             ens.set_kick_tile(tile)
             ens.set_kick_strip(strip)
             ens.set_kick_warps(warps)

@@ -5,6 +5,8 @@ import subprocess
 import sys
 from pathlib import Path
 
+import pytest
+
 import bench
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -111,3 +113,31 @@ def test_traffic_record_is_used_only_for_its_kick_shape(tmp_path, monkeypatch):
     b, src = bench.load_traffic("kick_pl_c4", dict(shape, plpl_row_group=1, plpl_warps_per_block=1))
     assert b is None and "another kick shape" in src["note"]
     assert bench.load_traffic("kick_pl_c1", shape) == (None, None)
+
+
+@pytest.mark.parametrize("workload", ["c4", "c3", "c3w", "c1"])
+def test_workloads_make_their_system(monkeypatch, workload):
+    # every workload builds its system through the public API classes, with or without a
+    # forced symmetric-kick shape (recorded here by a stand-in class instead of the GPU)
+    import swiftest_gb300.api as api
+    calls = []
+
+    class Fake:
+        def __init__(self, *a, **k):
+            calls.append(("new", k.get("precision")))
+
+        def __getattr__(self, name):
+            return lambda *a, **k: calls.append((name, a))
+
+    monkeypatch.setattr(api, "Ensemble", Fake)
+    monkeypatch.setattr(api, "NBodySystem", Fake)
+    for shape in (None, "128,4,1,2"):
+        argv = ["--workload", workload, "--nsys", "3"] + (["--kick-shape", shape] if shape else [])
+        monkeypatch.setattr(sys, "argv", ["bench.py"] + argv)
+        args = bench.parse()
+        wl = {"c4": bench.C4, "c3": bench.C3, "c3w": bench.C3W, "c1": bench.C1}[workload](args)
+        calls.clear()
+        wl.make(None, "MIXED")
+        assert calls[0] == ("new", "MIXED")
+        forced = [c for c in calls if c[0] == "set_kick_group"]
+        assert forced == ([("set_kick_group", (2,))] if shape and workload == "c4" else [])
