@@ -17,6 +17,12 @@
    maximum, and the wall times.
 
 --nsys M takes the first M systems instead of all 256 (quick runs).
+
+--fp64-from FILE reuses the FP64 errors of a recorded run (the per-system table of
+profiles/accuracy_c4_10k_steps.md) instead of rerunning the FP64 sample: the FP64 path is the
+reference's operation order, bit-identical to the oracle, so its trajectories do not change
+with the mixed path's kernels.  The FP64 path then runs only the systems outside that table
+that merge in this mixed run or exceed --outlier-threshold.
 """
 from __future__ import annotations
 
@@ -81,6 +87,19 @@ def run(ctx, E, precision, steps, every):
             "history_every": every, "history": hist, "stats": stats, "wall_s": wall}
 
 
+def recorded_fp64(path):
+    """{system: {dE_E, dL_L, merges}} of the FP64 path from a recorded table (rows
+    system | N_pl | why | merges mixed / FP64 | FP64 dE | mixed dE | ratio | FP64 dL | mixed dL)."""
+    out = {}
+    for line in Path(path).read_text().splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) != 9 or not cells[0].isdigit():
+            continue
+        out[int(cells[0])] = {"dE_E": float(cells[4]), "dL_L": float(cells[7]),
+                              "merges": int(cells[3].split("/")[1]), "why": cells[2]}
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--steps", type=int, default=10000)
@@ -88,6 +107,9 @@ def main(argv=None):
     p.add_argument("--sample", type=int, default=32)
     p.add_argument("--nsys", type=int, default=None)
     p.add_argument("--out", default=None)
+    p.add_argument("--fp64-from", default=None, help="recorded FP64 per-system table to reuse")
+    p.add_argument("--outlier-threshold", type=float, default=None,
+                   help="with --fp64-from: mixed |dE/E| above which a system outside the table runs in FP64")
     a = p.parse_args(argv)
     from swiftest_gb300 import build as B
     from swiftest_gb300 import initial_conditions as IC
@@ -102,6 +124,8 @@ def main(argv=None):
     out["mixed"] = mixed
     dEm = np.array(mixed["dE_E"])
     merged = [s for s in range(nsys) if mixed["merges"][s] > 0]
+    if a.fp64_from:
+        return compare_recorded(a, ctx, E, out, mixed, dEm, merged)
     rng = np.random.default_rng(2024)
     rest = [s for s in range(nsys) if s not in merged]
     sample = sorted(int(x) for x in rng.choice(rest, size=min(a.sample, len(rest)), replace=False))
@@ -136,6 +160,44 @@ def main(argv=None):
     print(json.dumps({k: out[k] for k in ("workload", "ratio_max", "mixed_max_all", "fp64_max_over_compared",
                                           "mixed_max_over_compared", "fp64_wall_s")}), flush=True)
     ctx.close()
+
+
+def compare_recorded(a, ctx, E, out, mixed, dEm, merged):
+    """The mixed run against recorded FP64 errors, plus FP64 runs of the systems the record
+    lacks (new merges, or mixed errors above the threshold)."""
+    rec = recorded_fp64(a.fp64_from)
+    nsys = len(E["npl"])
+    thresh = a.outlier_threshold if a.outlier_threshold is not None else 2.0 * max(
+        v["dE_E"] for v in rec.values() if v["why"] == "sample")
+    outliers = [s for s in range(nsys) if dEm[s] > thresh and s not in merged]
+    extra = sorted(s for s in set(merged) | set(outliers) if s not in rec)
+    fp_extra = run(ctx, subset(E, np.array(extra)), "FP64", a.steps, a.every) if extra else None
+    fp = {s: dict(v, source="recorded") for s, v in rec.items() if s < nsys}
+    if fp_extra:
+        fp.update({s: {"dE_E": fp_extra["dE_E"][k], "dL_L": fp_extra["dL_L"][k], "merges": fp_extra["merges"][k],
+                       "source": "run"} for k, s in enumerate(extra)})
+    rows = []
+    for s in sorted(fp):
+        rows.append({"system": s, "npl": int(E["npl"][s]),
+                     "why": "merge" if s in merged else ("outlier" if s in outliers else fp[s].get("why", "sample")),
+                     "fp64": fp[s]["source"], "merges_mixed": mixed["merges"][s], "merges_fp64": fp[s]["merges"],
+                     "dE_E_fp64": fp[s]["dE_E"], "dE_E_mixed": float(dEm[s]),
+                     "ratio": float(dEm[s] / max(fp[s]["dE_E"], 1e-300)),
+                     "dL_L_fp64": fp[s]["dL_L"], "dL_L_mixed": mixed["dL_L"][s]})
+    out["compared"] = rows
+    out["outlier_threshold"] = thresh
+    out["ratio_max"] = max(r["ratio"] for r in rows)
+    out["fp64_wall_s"] = fp_extra["wall_s"] if fp_extra else 0.0
+    out["fp64_run_systems"] = extra
+    out["mixed_max_all"] = float(dEm.max())
+    out["mixed_median_all"] = float(np.median(dEm))
+    line = json.dumps(out)
+    if a.out:
+        Path(a.out).write_text(line + "\n")
+    print(json.dumps({k: out[k] for k in ("workload", "ratio_max", "mixed_max_all", "mixed_median_all",
+                                          "fp64_run_systems", "fp64_wall_s")}), flush=True)
+    ctx.close()
+    return 0
 
 
 if __name__ == "__main__":
