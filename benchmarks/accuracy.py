@@ -18,6 +18,11 @@
 
 --nsys M takes the first M systems instead of all 256 (quick runs).
 
+--twin S runs system S in FP64 several times, batched: as generated and with its first
+body's x moved by each relative amount of --perturb (one unit in the last place when 0); the
+|dE/E| of the copies show how the FP64 error of that system depends on a perturbation of the
+size the mixed path's FP32 pair arithmetic makes (~1e-7 relative in each pair force).
+
 --fp64-from FILE reuses the FP64 errors of a recorded run (the per-system table of
 profiles/accuracy_c4_10k_steps.md) instead of rerunning the FP64 sample: the FP64 path is the
 reference's operation order, bit-identical to the oracle, so its trajectories do not change
@@ -108,6 +113,8 @@ def main(argv=None):
     p.add_argument("--nsys", type=int, default=None)
     p.add_argument("--out", default=None)
     p.add_argument("--fp64-from", default=None, help="recorded FP64 per-system table to reuse")
+    p.add_argument("--twin", type=int, default=None, help="FP64 runs of one system and perturbed copies")
+    p.add_argument("--perturb", default="0", help="--twin: relative moves of the first body's x (0: one ulp)")
     p.add_argument("--outlier-threshold", type=float, default=None,
                    help="with --fp64-from: mixed |dE/E| above which a system outside the table runs in FP64")
     a = p.parse_args(argv)
@@ -118,6 +125,8 @@ def main(argv=None):
     ctx = Context(0)
     E = IC.make_ensemble("C4", nsys=a.nsys)
     nsys = len(E["npl"])
+    if a.twin is not None:
+        return twin(a, ctx, E)
     out = {"workload": f"C4 ensemble, {nsys} systems ({int(E['npl'].sum())} pl), SyMBA, dt=0.002 yr, RHSCALE=1.0, "
                        f"{a.steps} steps", "steps": a.steps, "npl": E["npl"].tolist()}
     mixed = run(ctx, E, "MIXED", a.steps, a.every)
@@ -160,6 +169,27 @@ def main(argv=None):
     print(json.dumps({k: out[k] for k in ("workload", "ratio_max", "mixed_max_all", "fp64_max_over_compared",
                                           "mixed_max_over_compared", "fp64_wall_s")}), flush=True)
     ctx.close()
+
+
+def twin(a, ctx, E):
+    """FP64 runs of system a.twin and of copies whose first body's x is moved."""
+    moves = [float(x) for x in a.perturb.split(",")]
+    one = subset(E, np.array([a.twin] * (1 + len(moves))))
+    n = int(one["npl"][0])
+    pl = {k: v.copy() for k, v in one["pl"].items()}
+    for c, m in enumerate(moves, start=1):
+        x = pl["rh"][c * n, 0]
+        pl["rh"][c * n, 0] = np.nextafter(x, np.inf) if m == 0 else x * (1.0 + m)
+    one["pl"] = pl
+    res = run(ctx, one, "FP64", a.steps, a.every)
+    out = {"system": a.twin, "npl": n, "steps": a.steps, "perturb": [None] + moves, "dE_E": res["dE_E"],
+           "merges": res["merges"], "history": res["history"],
+           "ratios": [d / max(res["dE_E"][0], 1e-300) for d in res["dE_E"]], "wall_s": res["wall_s"]}
+    if a.out:
+        Path(a.out).write_text(json.dumps(out) + "\n")
+    print(json.dumps(out), flush=True)
+    ctx.close()
+    return 0
 
 
 def compare_recorded(a, ctx, E, out, mixed, dEm, merged):
