@@ -402,15 +402,15 @@ __global__ void __launch_bounds__(32 * G) k_kick_mixed_sym_grp(int nitems, const
     static_assert(G == 2 || G == 4, "row groups of 2 or 4 tiles");
     __shared__ SubTile sP[SR];
     __shared__ float sq[G][3 * T];  // partner sums of the staged tile J, one row per warp
-    __shared__ unsigned s_it[2];    // item of this round (two buffers: one barrier per round)
+    __shared__ unsigned s_it[2];    // the item of each pull (two buffers: one barrier per pull)
     __shared__ SubTile sP0[G == 2 ? SR : 1];  // G = 2: tile I0 in the diagonal round
     __shared__ float sq0[G == 2 ? 3 * T : 1];  // G = 2: partner sums for tile I0 from warp 1
     const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float4 pad_a = make_float4(PAD_POS, PAD_POS, PAD_POS, 0.f), zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int round = 0;; round ^= 1) {
-        if (threadIdx.x == 0) s_it[round] = atomicAdd(head, 1u);
+    for (int buf = 0;; buf ^= 1) {
+        if (threadIdx.x == 0) s_it[buf] = atomicAdd(head, 1u);
         __syncthreads();
-        const unsigned it = s_it[round];
+        const unsigned it = s_it[buf];
         if (it >= (unsigned)nitems) break;  // block-uniform, as are the two skips below
         const int4 w = items[it];
         const int s = w.x, I0 = w.y, J0 = w.z & 0xffffff, nJ = w.z >> 24;
